@@ -1,0 +1,566 @@
+/*
+ * CPU oracle (test infrastructure only): plain C restatement of the AdaM-DG
+ * reference algorithm for the linear constant-coefficient sparse-grid DG
+ * right-hand side and its SSP-RK3 time stepping.  Pinned against the
+ * reference library itself (oracle/ref_harness.cpp, fixtures in tests/golden/).
+ * Only tests/, __graft_entry__.smoke() and bench.py's cpu_baseline leg use it.
+ */
+#include "amdg_oracle.h"
+
+#include <math.h>
+#include <stdlib.h>
+#include <string.h>
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+#define ROUND_OFF 1e-13 /* Const::ROUND_OFF, libs.h:28 */
+
+/* ------------------------------------------------------------------------ */
+/* 1D Alpert multiwavelets (AlptBasis.cpp:57-81, 256-299).                    */
+/* Mother functions on [-1,1]: for x >= 0 a polynomial of degree k (monomial   */
+/* coefficients below, Alpert 1993); for x < 0, f(-x) = (-1)^(p+k+1) f(x).     */
+/* ------------------------------------------------------------------------ */
+static const double* alpert_right_poly(int k, int p, double* scale) {
+    /* returns monomial coefficients c[0..k] of the right-half polynomial */
+    static const double k1[2][4] = {{-1, 2, 0, 0}, {-2, 3, 0, 0}};
+    static const double k2[3][4] = {{1, -24, 30, 0}, {3, -16, 15, 0}, {4, -15, 12, 0}};
+    static const double k3[4][4] = {{1, 4, -30, 28}, {-4, 105, -300, 210}, {-5, 48, -105, 64}, {-16, 105, -192, 105}};
+    static const double k0[1][4] = {{1, 0, 0, 0}};
+    switch (k) {
+        case 0: *scale = sqrt(0.5); return k0[p];
+        case 1: *scale = (p == 0) ? sqrt(1.5) : sqrt(0.5); return k1[p];
+        case 2: *scale = (p == 0) ? sqrt(0.5) / 3.0 : (p == 1) ? sqrt(1.5) * 0.5 : sqrt(2.5) / 3.0; return k2[p];
+        case 3:
+            *scale = (p == 0) ? sqrt(15.0 / 34.0) : (p == 1) ? sqrt(1.0 / 42.0) : (p == 2) ? sqrt(35.0 / 34.0) * 0.5 : sqrt(5.0 / 42.0) * 0.5;
+            return k3[p];
+        default: *scale = 0; return NULL;
+    }
+}
+
+/* l-th derivative of the mother function at x in [-1,1] */
+static double alpert_mother(int k, int p, int l, double x) {
+    double sgn = 1.0;
+    if (x < 0) {
+        /* parity of the l-th derivative flips with l */
+        const int odd = (p + k + 1 + l) % 2;
+        sgn = odd ? -1.0 : 1.0;
+        x = -x;
+    }
+    double scale;
+    const double* c = alpert_right_poly(k, p, &scale);
+    if (!c) return 0.0;
+    double v = 0.0;
+    for (int m = k; m >= l; --m) {
+        double fac = 1.0;
+        for (int r = 0; r < l; ++r) fac *= (double)(m - r);
+        v = v * x + c[m] * fac; /* Horner on the derivative polynomial */
+    }
+    /* Horner above accumulates c[m]*fac with powers x^(m-l) */
+    return sgn * scale * v;
+}
+
+/* Legendre polynomial P_p and derivatives on [-1,1] by the three-term recurrence. */
+static double legendre_deriv(int p, int l, double x) {
+    if (fabs(x) > 1.0) return 0.0;
+    /* values and derivatives up to order l via recurrences on coefficients */
+    double c_prev[8] = {1, 0, 0, 0, 0, 0, 0, 0}; /* P_0 */
+    double c_cur[8] = {0, 1, 0, 0, 0, 0, 0, 0};  /* P_1 */
+    double c[8] = {0};
+    if (p == 0) memcpy(c, c_prev, sizeof c);
+    else if (p == 1) memcpy(c, c_cur, sizeof c);
+    else {
+        for (int n = 1; n < p; ++n) {
+            double nx[8] = {0};
+            /* (n+1) P_{n+1} = (2n+1) x P_n - n P_{n-1} */
+            for (int m = 0; m < 7; ++m) nx[m + 1] += (2.0 * n + 1.0) * c_cur[m];
+            for (int m = 0; m < 8; ++m) nx[m] -= n * c_prev[m];
+            for (int m = 0; m < 8; ++m) nx[m] /= (n + 1.0);
+            memcpy(c_prev, c_cur, sizeof c_prev);
+            memcpy(c_cur, nx, sizeof c_cur);
+        }
+        memcpy(c, c_cur, sizeof c);
+    }
+    double v = 0.0;
+    for (int m = 7; m >= l; --m) {
+        double fac = 1.0;
+        for (int r = 0; r < l; ++r) fac *= (double)(m - r);
+        v = v * x + c[m] * fac;
+    }
+    return v;
+}
+
+static double alpert_raw(int k, int n, int j, int p, int l, double x) {
+    if (n == 0) {
+        /* normalized Legendre polynomial on [0,1] */
+        return legendre_deriv(p, l, 2 * x - 1) * pow(2.0, l) * sqrt(2 * p + 1.0);
+    } else if (n == 1) {
+        if (x >= 0 && x <= 1) return pow(2.0, l + 0.5) * alpert_mother(k, p, l, 2 * x - 1);
+        return 0.0;
+    } else {
+        const int jodd = (j - 1) / 2;
+        const double sx = pow(2.0, n - 1) * x - jodd;
+        return pow(2.0, (n - 1) * (l + 0.5)) * alpert_raw(k, 1, 1, p, l, sx);
+    }
+}
+
+double amdg_oracle_alpert_val(int k, int level, int suppt, int p, int deriv, double x, int sgn) {
+    /* one-sided limits by a 1e-13 shift, zero outside [0,1] (AlptBasis.cpp:16-30) */
+    double xl = x;
+    if (sgn == -1) {
+        if (fabs(x) <= ROUND_OFF) return 0.0;
+        xl -= ROUND_OFF;
+    } else if (sgn == 1) {
+        if (fabs(x - 1) <= ROUND_OFF) return 0.0;
+        xl += ROUND_OFF;
+    }
+    return alpert_raw(k, level, suppt, p, deriv, xl);
+}
+
+/* ------------------------------------------------------------------------ */
+/* Gauss-Legendre nodes by Newton iteration on P_n.                           */
+/* ------------------------------------------------------------------------ */
+int amdg_oracle_gauss_legendre(int n, double* x, double* w) {
+    if (n < 1 || n > 16) return -1;
+    const double pi = 3.14159265358979323846;
+    for (int i = 0; i < n; ++i) {
+        double z = cos(pi * (i + 0.75) / (n + 0.5));
+        double dp = 1.0;
+        for (int it = 0; it < 100; ++it) {
+            double p0 = 1.0, p1 = z;
+            for (int m = 2; m <= n; ++m) {
+                double p2 = ((2.0 * m - 1.0) * z * p1 - (m - 1.0) * p0) / m;
+                p0 = p1;
+                p1 = p2;
+            }
+            if (n == 1) { p1 = z; p0 = 1.0; }
+            dp = n * (z * p1 - p0) / (z * z - 1.0);
+            double dz = p1 / dp;
+            z -= dz;
+            if (fabs(dz) < 1e-16) break;
+        }
+        {
+            double p0 = 1.0, p1 = z;
+            for (int m = 2; m <= n; ++m) {
+                double p2 = ((2.0 * m - 1.0) * z * p1 - (m - 1.0) * p0) / m;
+                p0 = p1;
+                p1 = p2;
+            }
+            if (n == 1) { p1 = z; p0 = 1.0; }
+            dp = n * (z * p1 - p0) / (z * z - 1.0);
+        }
+        /* ascending order */
+        x[n - 1 - i] = z;
+        w[n - 1 - i] = 2.0 / ((1.0 - z * z) * dp * dp);
+    }
+    if (n == 1) { x[0] = 0.0; w[0] = 2.0; }
+    return 0;
+}
+
+static double gl_integrate(double (*f)(double, const void*), const void* ctx, double a, double b, int npts) {
+    double gx[16], gw[16];
+    amdg_oracle_gauss_legendre(npts, gx, gw);
+    double s = 0.0;
+    for (int i = 0; i < npts; ++i) s += gw[i] * f(a + (gx[i] + 1.0) * 0.5 * (b - a), ctx);
+    return s * (b - a) / 2.0;
+}
+
+/* 1D element helpers ------------------------------------------------------ */
+typedef struct { int n, j; } elem1d;
+
+static elem1d elem_of_order(int o) {
+    elem1d e;
+    if (o == 0) { e.n = 0; e.j = 1; return e; }
+    int n = 1;
+    while ((1 << n) <= o) ++n;          /* 2^(n-1) <= o < 2^n */
+    e.n = n;
+    e.j = 2 * (o - (1 << (n - 1))) + 1;
+    return e;
+}
+
+static int order_of_elem(int n, int j) { return n == 0 ? 0 : (1 << (n - 1)) + (j - 1) / 2; }
+
+/* support in units of 2^-N */
+static void support_units(int n, int j, int N, long* a, long* b) {
+    if (n <= 1) { *a = 0; *b = 1L << N; return; }
+    const long w = 1L << (N - n + 1);
+    *a = (long)((j - 1) / 2) * w;
+    *b = *a + w;
+}
+
+static double support_lo(int n, int j) { return n <= 1 ? 0.0 : pow(2.0, -n + 1.0) * (j - 1.0) / 2.0; }
+static double support_hi(int n, int j) { return n <= 1 ? 1.0 : pow(2.0, -n + 1.0) * (j + 1.0) / 2.0; }
+
+/* ------------------------------------------------------------------------ */
+/* 1D operator matrices (OperatorMatrix1D.h:166-199, Basis.cpp:61-173)       */
+/* ------------------------------------------------------------------------ */
+typedef struct { int k; elem1d u, v; int pu, pv; int du, dv; } prod_ctx;
+
+static double prod_integrand(double x, const void* c) {
+    const prod_ctx* p = (const prod_ctx*)c;
+    return amdg_oracle_alpert_val(p->k, p->u.n, p->u.j, p->pu, p->du, x, 0) *
+           amdg_oracle_alpert_val(p->k, p->v.n, p->v.j, p->pv, p->dv, x, 0);
+}
+
+static double product_volume(int k, elem1d u, int pu, elem1d v, int pv, int du, int dv) {
+    const double ua = support_lo(u.n, u.j), ub = support_hi(u.n, u.j);
+    const double va = support_lo(v.n, v.j), vb = support_hi(v.n, v.j);
+    if (va >= ub || vb <= ua) return 0.0;
+    double xl = ua, xr = ub;
+    if (u.n <= v.n) { xl = va; xr = vb; }
+    const double xm = (xl + xr) / 2.0;
+    prod_ctx c = {k, u, v, pu, pv, du, dv};
+    return gl_integrate(prod_integrand, &c, xl, xm, 10) + gl_integrate(prod_integrand, &c, xm, xr, 10);
+}
+
+/* sum over the discontinuity points of v of u^(su) v^(sv), periodic boundary */
+static double product_edge_dis_v(int k, elem1d u, int pu, elem1d v, int pv, int su, int sv) {
+    const double pts[3] = {support_lo(v.n, v.j), 0.5 * (support_lo(v.n, v.j) + support_hi(v.n, v.j)), support_hi(v.n, v.j)};
+    double s = 0.0;
+    for (int i = 0; i < 3; ++i) {
+        if (v.n <= 1 && i == 2) continue; /* 0 and 1 are the same point */
+        const double x = pts[i];
+        double vu = amdg_oracle_alpert_val(k, u.n, u.j, pu, 0, x, su);
+        double vv = amdg_oracle_alpert_val(k, v.n, v.j, pv, 0, x, sv);
+        if (fabs(x) < ROUND_OFF) {
+            if (su == -1) vu = amdg_oracle_alpert_val(k, u.n, u.j, pu, 0, 1.0, su);
+            if (sv == -1) vv = amdg_oracle_alpert_val(k, v.n, v.j, pv, 0, 1.0, sv);
+        } else if (fabs(x - 1.0) < ROUND_OFF) {
+            if (su == 1) vu = amdg_oracle_alpert_val(k, u.n, u.j, pu, 0, 0.0, su);
+            if (sv == 1) vv = amdg_oracle_alpert_val(k, v.n, v.j, pv, 0, 0.0, sv);
+        }
+        s += vu * vv;
+    }
+    return s;
+}
+
+int amdg_oracle_oper1d(int N, int k, double* u_v, double* u_vx, double* ulft_vjp, double* urgt_vjp) {
+    const int nb = (1 << N) * (k + 1);
+#pragma omp parallel for schedule(dynamic)
+    for (int r = 0; r < nb; ++r) {
+        const elem1d u = elem_of_order(r / (k + 1));
+        const int pu = r % (k + 1);
+        for (int c = 0; c < nb; ++c) {
+            const elem1d v = elem_of_order(c / (k + 1));
+            const int pv = c % (k + 1);
+            const size_t idx = (size_t)r * nb + c;
+            if (u_v) u_v[idx] = product_volume(k, u, pu, v, pv, 0, 0);
+            if (u_vx) u_vx[idx] = product_volume(k, u, pu, v, pv, 0, 1);
+            if (ulft_vjp) ulft_vjp[idx] = product_edge_dis_v(k, u, pu, v, pv, -1, 1) - product_edge_dis_v(k, u, pu, v, pv, -1, -1);
+            if (urgt_vjp) urgt_vjp[idx] = product_edge_dis_v(k, u, pu, v, pv, 1, 1) - product_edge_dis_v(k, u, pu, v, pv, 1, -1);
+        }
+    }
+    return 0;
+}
+
+/* ------------------------------------------------------------------------ */
+/* Sparse / full grid (DGSolution.cpp:10-57)                                  */
+/* ------------------------------------------------------------------------ */
+static int64_t grid_walk(int dim, int N, int sparse, int32_t* level, int32_t* suppt) {
+    /* enumerate per-dim 1D orders o_d in [0, 2^N) lexicographically and keep
+     * those whose level sum obeys the sparse rule */
+    const int n1 = 1 << N;
+    int o[16] = {0};
+    int64_t count = 0;
+    for (;;) {
+        int lsum = 0;
+        for (int d = 0; d < dim; ++d) lsum += elem_of_order(o[d]).n;
+        if (!sparse || lsum <= N) {
+            if (level) {
+                for (int d = 0; d < dim; ++d) {
+                    elem1d e = elem_of_order(o[d]);
+                    level[count * dim + d] = e.n;
+                    suppt[count * dim + d] = e.j;
+                }
+            }
+            ++count;
+        }
+        int d = dim - 1;
+        while (d >= 0) {
+            if (++o[d] < n1) break;
+            o[d] = 0;
+            --d;
+        }
+        if (d < 0) break;
+    }
+    return count;
+}
+
+int64_t amdg_oracle_grid_count(int dim, int N, int sparse) {
+    if (dim < 1 || dim > 16 || N < 0 || N > 20) return -1;
+    return grid_walk(dim, N, sparse, NULL, NULL);
+}
+
+int64_t amdg_oracle_grid(int dim, int N, int sparse, int32_t* level, int32_t* suppt) {
+    if (dim < 1 || dim > 16 || N < 0 || N > 20) return -1;
+    return grid_walk(dim, N, sparse, level, suppt);
+}
+
+/* ------------------------------------------------------------------------ */
+/* Separable projection and initialisation (Basis.cpp:38-59, DGSolution.cpp:150-184) */
+/* ------------------------------------------------------------------------ */
+typedef struct { int k; elem1d e; int p; amdg_oracle_fn1d f; void* user; int d, term; } proj_ctx;
+
+static double proj_integrand(double x, const void* c) {
+    const proj_ctx* p = (const proj_ctx*)c;
+    return amdg_oracle_alpert_val(p->k, p->e.n, p->e.j, p->p, 0, x, 0) * p->f(x, p->d, p->term, p->user);
+}
+
+int amdg_oracle_project_separable(int N, int k, int dim, int nterms, amdg_oracle_fn1d f, void* user, double* out) {
+    const int nb = (1 << N) * (k + 1);
+    for (int t = 0; t < nterms; ++t)
+        for (int d = 0; d < dim; ++d)
+            for (int b = 0; b < nb; ++b) {
+                proj_ctx c = {k, elem_of_order(b / (k + 1)), b % (k + 1), f, user, d, t};
+                double s = 0.0;
+                if (c.e.n <= 4) {
+                    for (int i = 0; i < 16; ++i) s += gl_integrate(proj_integrand, &c, i / 16.0, (i + 1) / 16.0, 10);
+                } else {
+                    const double a = support_lo(c.e.n, c.e.j), bb = support_hi(c.e.n, c.e.j), m = (a + bb) / 2.0;
+                    s = gl_integrate(proj_integrand, &c, a, m, 10) + gl_integrate(proj_integrand, &c, m, bb, 10);
+                }
+                out[((size_t)t * dim + d) * nb + b] = s;
+            }
+    return 0;
+}
+
+static int ipow(int b, int e) { int r = 1; while (e-- > 0) r *= b; return r; }
+
+int amdg_oracle_init_separable(int dim, int N, int k, int64_t E, const int32_t* level, const int32_t* suppt,
+                               int nterms, const double* coef1d, double* u) {
+    const int nb1 = (1 << N) * (k + 1);
+    const int B = ipow(k + 1, dim);
+#pragma omp parallel for
+    for (int64_t e = 0; e < E; ++e) {
+        int o[16];
+        for (int d = 0; d < dim; ++d) o[d] = order_of_elem(level[e * dim + d], suppt[e * dim + d]);
+        for (int q = 0; q < B; ++q) u[e * B + q] = 0.0;
+        for (int t = 0; t < nterms; ++t)
+            for (int q = 0; q < B; ++q) {
+                int dig[16];
+                int rem = q;
+                for (int d = dim - 1; d >= 0; --d) { dig[d] = rem % (k + 1); rem /= (k + 1); }
+                double v = 1.0;
+                for (int d = 0; d < dim; ++d) v *= coef1d[((size_t)t * dim + d) * nb1 + o[d] * (k + 1) + dig[d]];
+                u[e * B + q] += v;
+            }
+    }
+    return 0;
+}
+
+/* ------------------------------------------------------------------------ */
+/* Element lookup: open-addressing hash over packed 1D orders.                */
+/* ------------------------------------------------------------------------ */
+typedef struct { uint64_t* keys; int64_t* vals; uint64_t mask; } ehash;
+
+static uint64_t pack_key(const int* o, int dim, int N) {
+    uint64_t key = 0;
+    for (int d = 0; d < dim; ++d) key = (key << N) | (uint64_t)o[d];
+    return key;
+}
+
+static uint64_t mix64(uint64_t x) {
+    x ^= x >> 33; x *= 0xff51afd7ed558ccdULL; x ^= x >> 33; x *= 0xc4ceb9fe1a85ec53ULL; x ^= x >> 33;
+    return x;
+}
+
+static int ehash_build(ehash* h, int dim, int N, int64_t E, const int32_t* level, const int32_t* suppt) {
+    uint64_t cap = 16;
+    while (cap < (uint64_t)E * 2) cap <<= 1;
+    h->keys = (uint64_t*)malloc(cap * sizeof(uint64_t));
+    h->vals = (int64_t*)malloc(cap * sizeof(int64_t));
+    if (!h->keys || !h->vals) return -1;
+    h->mask = cap - 1;
+    for (uint64_t i = 0; i < cap; ++i) h->vals[i] = -1;
+    for (int64_t e = 0; e < E; ++e) {
+        int o[16];
+        for (int d = 0; d < dim; ++d) o[d] = order_of_elem(level[e * dim + d], suppt[e * dim + d]);
+        const uint64_t key = pack_key(o, dim, N);
+        uint64_t s = mix64(key) & h->mask;
+        while (h->vals[s] >= 0 && h->keys[s] != key) s = (s + 1) & h->mask;
+        h->keys[s] = key;
+        h->vals[s] = e;
+    }
+    return 0;
+}
+
+static int64_t ehash_find(const ehash* h, uint64_t key) {
+    uint64_t s = mix64(key) & h->mask;
+    while (h->vals[s] >= 0) {
+        if (h->keys[s] == key) return h->vals[s];
+        s = (s + 1) & h->mask;
+    }
+    return -1;
+}
+
+static void ehash_free(ehash* h) { free(h->keys); free(h->vals); }
+
+/* flux-neighbour predicate in one dimension (Element.cpp:283-348): supports
+ * intersect, or are adjacent, or are adjacent across the periodic boundary */
+static int intersect_or_adjacent(long a, long b, long a2, long b2, long one) {
+    const int no_int = (a >= b2) || (b <= a2);
+    const int adj = (a == b2) || (b == a2);
+    const int per = (a == 0 && b2 == one) || (a2 == 0 && b == one);
+    return !no_int || adj || per;
+}
+
+/* ------------------------------------------------------------------------ */
+/* Linear operator (BilinearForm.cpp:25-87, 691-710)                          */
+/* ------------------------------------------------------------------------ */
+typedef struct {
+    int dim, N, k, nb1;
+    double* mvol; /* per dim: c_d * u_vx, dropped below ROUND_OFF */
+    double* mflx; /* per dim: c_d * (ulft_vjp | urgt_vjp) */
+} linop;
+
+static int linop_build(linop* L, int dim, int N, int k, const double* c) {
+    L->dim = dim; L->N = N; L->k = k;
+    L->nb1 = (1 << N) * (k + 1);
+    const size_t n2 = (size_t)L->nb1 * L->nb1;
+    double* uvx = (double*)malloc(n2 * sizeof(double));
+    double* ul = (double*)malloc(n2 * sizeof(double));
+    double* ur = (double*)malloc(n2 * sizeof(double));
+    L->mvol = (double*)malloc(n2 * dim * sizeof(double));
+    L->mflx = (double*)malloc(n2 * dim * sizeof(double));
+    if (!uvx || !ul || !ur || !L->mvol || !L->mflx) return -1;
+    amdg_oracle_oper1d(N, k, NULL, uvx, ul, ur);
+    for (int d = 0; d < dim; ++d) {
+        const double* f = (c[d] >= 0) ? ul : ur;
+        for (size_t i = 0; i < n2; ++i) {
+            double a = c[d] * uvx[i];
+            double b = c[d] * f[i];
+            L->mvol[d * n2 + i] = (fabs(a) >= ROUND_OFF) ? a : 0.0;
+            L->mflx[d * n2 + i] = (fabs(b) >= ROUND_OFF) ? b : 0.0;
+        }
+    }
+    free(uvx); free(ul); free(ur);
+    return 0;
+}
+
+static void linop_free(linop* L) { free(L->mvol); free(L->mflx); }
+
+static void linear_rhs_range(const linop* L, const ehash* h, int64_t E, const int32_t* level, const int32_t* suppt,
+                             const double* u, double* rhs, int64_t e0, int64_t e1, int nthreads) {
+    const int dim = L->dim, N = L->N, k = L->k, np = k + 1, nb1 = L->nb1;
+    const int B = ipow(np, dim);
+    const size_t n2 = (size_t)nb1 * nb1;
+    const long one = 1L << N;
+    (void)E;
+#ifdef _OPENMP
+    if (nthreads > 0) omp_set_num_threads(nthreads);
+#endif
+#pragma omp parallel for schedule(dynamic, 16)
+    for (int64_t e = e0; e < e1; ++e) {
+        int o[16], lv[16], sp[16];
+        for (int d = 0; d < dim; ++d) {
+            lv[d] = level[e * dim + d];
+            sp[d] = suppt[e * dim + d];
+            o[d] = order_of_elem(lv[d], sp[d]);
+        }
+        double* y = rhs + (e - e0) * B;
+        for (int q = 0; q < B; ++q) y[q] = 0.0;
+        int stride[16];
+        stride[dim - 1] = 1;
+        for (int d = dim - 2; d >= 0; --d) stride[d] = stride[d + 1] * np;
+        for (int t = 0; t < dim; ++t) {
+            long a, b;
+            support_units(lv[t], sp[t], N, &a, &b);
+            int o2[16];
+            memcpy(o2, o, sizeof(int) * dim);
+            for (int oc = 0; oc < (1 << N); ++oc) {
+                const elem1d ec = elem_of_order(oc);
+                long a2, b2;
+                support_units(ec.n, ec.j, N, &a2, &b2);
+                if (!intersect_or_adjacent(a, b, a2, b2, one)) continue;
+                o2[t] = oc;
+                const int64_t es = ehash_find(h, pack_key(o2, dim, N));
+                if (es < 0) continue;
+                const int is_vol = !((a >= b2) || (b <= a2));
+                const double* us = u + es * B;
+                const double* mv = L->mvol + t * n2;
+                const double* mf = L->mflx + t * n2;
+                for (int q = 0; q < B; ++q) {
+                    const int qt = (q / stride[t]) % np;
+                    const int base = q - qt * stride[t];
+                    const int col = o[t] * np + qt; /* test basis */
+                    double acc = 0.0;
+                    for (int p = 0; p < np; ++p) {
+                        const int row = oc * np + p; /* solution basis */
+                        const double m = (is_vol ? mv[(size_t)row * nb1 + col] : 0.0) + mf[(size_t)row * nb1 + col];
+                        acc += m * us[base + p * stride[t]];
+                    }
+                    y[q] += acc;
+                }
+            }
+        }
+    }
+}
+
+int amdg_oracle_linear_rhs_range(int dim, int N, int k, int64_t E, const int32_t* level, const int32_t* suppt,
+                                 const double* c, const double* u, double* rhs, int64_t e_begin, int64_t e_end,
+                                 int nthreads) {
+    if (dim < 1 || dim > 16 || dim * N > 64) return -1;
+    linop L;
+    ehash h;
+    if (linop_build(&L, dim, N, k, c)) return -2;
+    if (ehash_build(&h, dim, N, E, level, suppt)) return -2;
+    linear_rhs_range(&L, &h, E, level, suppt, u, rhs, e_begin, e_end, nthreads);
+    ehash_free(&h);
+    linop_free(&L);
+    return 0;
+}
+
+int amdg_oracle_linear_rhs(int dim, int N, int k, int64_t E, const int32_t* level, const int32_t* suppt,
+                           const double* c, const double* u, double* rhs, int nthreads) {
+    return amdg_oracle_linear_rhs_range(dim, N, k, E, level, suppt, c, u, rhs, 0, E, nthreads);
+}
+
+int amdg_oracle_linear_rk3(int dim, int N, int k, int64_t E, const int32_t* level, const int32_t* suppt,
+                           const double* c, double dt, int steps, double* u, int nthreads) {
+    if (dim < 1 || dim > 16 || dim * N > 64) return -1;
+    const int B = ipow(k + 1, dim);
+    const size_t n = (size_t)E * B;
+    linop L;
+    ehash h;
+    if (linop_build(&L, dim, N, k, c)) return -2;
+    if (ehash_build(&h, dim, N, E, level, suppt)) return -2;
+    double* rhs = (double*)malloc(n * sizeof(double));
+    double* u1 = (double*)malloc(n * sizeof(double));
+    double* u2 = (double*)malloc(n * sizeof(double));
+    if (!rhs || !u1 || !u2) return -2;
+    /* RK3SSP::step_rk (ODESolver.cpp:261-271), element-wise in the written order */
+    for (int s = 0; s < steps; ++s) {
+        linear_rhs_range(&L, &h, E, level, suppt, u, rhs, 0, E, nthreads);
+        for (size_t i = 0; i < n; ++i) u1[i] = u[i] + dt * rhs[i];
+        linear_rhs_range(&L, &h, E, level, suppt, u1, rhs, 0, E, nthreads);
+        for (size_t i = 0; i < n; ++i) u2[i] = 3. / 4. * u[i] + 1. / 4. * (u1[i] + dt * rhs[i]);
+        linear_rhs_range(&L, &h, E, level, suppt, u2, rhs, 0, E, nthreads);
+        for (size_t i = 0; i < n; ++i) u[i] = 1. / 3. * u[i] + 2. / 3. * (u2[i] + dt * rhs[i]);
+    }
+    free(rhs); free(u1); free(u2);
+    ehash_free(&h);
+    linop_free(&L);
+    return 0;
+}
+
+double amdg_oracle_l2_error_split(int dim, int N, int k, int64_t E, const int32_t* level, const int32_t* suppt,
+                                  const double* u, const double* coef1d_exact, double l2_norm_exact) {
+    const int nb1 = (1 << N) * (k + 1);
+    const int B = ipow(k + 1, dim);
+    double err2 = l2_norm_exact * l2_norm_exact;
+    for (int64_t e = 0; e < E; ++e) {
+        int o[16];
+        for (int d = 0; d < dim; ++d) o[d] = order_of_elem(level[e * dim + d], suppt[e * dim + d]);
+        for (int q = 0; q < B; ++q) {
+            const double v = u[e * B + q];
+            err2 += v * v;
+            int dig[16];
+            int rem = q;
+            for (int d = dim - 1; d >= 0; --d) { dig[d] = rem % (k + 1); rem /= (k + 1); }
+            double coe = 1.0;
+            for (int d = 0; d < dim; ++d) coe *= coef1d_exact[(size_t)d * nb1 + o[d] * (k + 1) + dig[d]];
+            err2 -= 2.0 * v * coe;
+        }
+    }
+    return sqrt(err2 > 0 ? err2 : 0.0);
+}

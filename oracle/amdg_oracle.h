@@ -1,0 +1,71 @@
+/*
+ * CPU oracle for the adaptive sparse-grid DG right-hand side: a plain C
+ * restatement of the reference algorithm (AdaM-DG), used ONLY as test
+ * infrastructure -- the checker in tests/, smoke() and the cpu_baseline leg of
+ * bench.py.  Nothing in the product library links or calls it.
+ *
+ * Conventions (shared with the reference):
+ *   - 1D element (level n, suppt j): n = 0..N, j odd; n<=1 -> support [0,1],
+ *     n>=2 -> [2^(1-n) (j-1)/2, 2^(1-n) (j+1)/2].  1D element order
+ *     o(n,j) = 0 for n=0, else 2^(n-1) + (j-1)/2  (Element.cpp:386-389).
+ *   - 1D basis order = o * (k+1) + p  (AllBasis.h:81-84).
+ *   - Per-element coefficient block: (k+1)^dim doubles, row-major over dims,
+ *     last dimension fastest (VecMultiD.h:114-116).
+ *   - 1D operator matrices are stored row = solution basis, col = test basis,
+ *     as OperatorMatrix1D::u_vx.at(row_idx, col_idx) (OperatorMatrix1D.h:166-199).
+ */
+#ifndef AMDG_ORACLE_H
+#define AMDG_ORACLE_H
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef double (*amdg_oracle_fn1d)(double x, int d, int term, void* user);
+
+/* Alpert basis value (or derivative) at x, limit sgn in {-1,0,1}. */
+double amdg_oracle_alpert_val(int k, int level, int suppt, int p, int deriv, double x, int sgn);
+
+/* Gauss-Legendre rule on [-1,1] (n <= 16 points). */
+int amdg_oracle_gauss_legendre(int n, double* x, double* w);
+
+/* 1D operator matrices, each (2^N (k+1))^2, row = solution basis, col = test basis.
+ * Any pointer may be NULL. */
+int amdg_oracle_oper1d(int N, int k, double* u_v, double* u_vx, double* ulft_vjp, double* urgt_vjp);
+
+/* Number of elements of the sparse (sum of levels <= N) or full grid. */
+int64_t amdg_oracle_grid_count(int dim, int N, int sparse);
+/* Elements in lexicographic order of (order_0,...,order_{dim-1}); level/suppt are E x dim. */
+int64_t amdg_oracle_grid(int dim, int N, int sparse, int32_t* level, int32_t* suppt);
+
+/* 1D projections onto all Alpert basis functions (Basis::product_function):
+ * out[term][d][basis] for nterms separable terms. */
+int amdg_oracle_project_separable(int N, int k, int dim, int nterms, amdg_oracle_fn1d f, void* user, double* out);
+
+/* Expand separable 1D projections into element coefficients: u[e][q] = sum_term prod_d coef. */
+int amdg_oracle_init_separable(int dim, int N, int k, int64_t E, const int32_t* level, const int32_t* suppt,
+                               int nterms, const double* coef1d, double* u);
+
+/* Linear constant-coefficient operator (HyperbolicAlpt::assemble_matrix_scalar, upwind flux),
+ * rhs = L u.  c has dim entries. nthreads <= 0 -> OpenMP default. */
+int amdg_oracle_linear_rhs(int dim, int N, int k, int64_t E, const int32_t* level, const int32_t* suppt,
+                           const double* c, const double* u, double* rhs, int nthreads);
+
+/* SSP-RK3 steps of the linear operator, in place on u (RK3SSP::step_rk). */
+int amdg_oracle_linear_rk3(int dim, int N, int k, int64_t E, const int32_t* level, const int32_t* suppt,
+                           const double* c, double dt, int steps, double* u, int nthreads);
+
+/* One linear RHS evaluation restricted to the test elements [e_begin, e_end) (timing samples). */
+int amdg_oracle_linear_rhs_range(int dim, int N, int k, int64_t E, const int32_t* level, const int32_t* suppt,
+                                 const double* c, const double* u, double* rhs, int64_t e_begin, int64_t e_end,
+                                 int nthreads);
+
+/* L2 error against a separable exact solution (DGSolution::get_L2_error_split_separable_scalar). */
+double amdg_oracle_l2_error_split(int dim, int N, int k, int64_t E, const int32_t* level, const int32_t* suppt,
+                                  const double* u, const double* coef1d_exact, double l2_norm_exact);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,238 @@
+// Harness that drives the AdaM-DG reference library (compiled from its own
+// sources, unmodified, against the Eigen stand-in in oracle/shim) and dumps
+// its results keyed by element multi-index.  Test infrastructure only: its
+// output pins the C restatement in oracle/amdg_oracle.c and becomes the
+// committed golden fixtures under tests/golden/.
+//
+// Usage:
+//   ref_harness linear <dim> <N> <k> <sparse 0|1> <ic> <engine> <steps> <dt> <c_0> ... <c_{dim-1}>
+//     ic     : sin_sum  -> u0 = sin(2 pi sum x_d)  (init_separable_scalar_sum, as in
+//                          example/02_hyperbolic_01_scalar_const_coefficient.cpp)
+//              sin_prod -> u0 = prod_d sin(2 pi x_d) (init_separable_scalar)
+//     engine : assembled -> HyperbolicAlpt::assemble_matrix_scalar + RK3SSP::step_rk
+//              matfree   -> FastRHS::transform_ucoe_alpt_to_rhs per dim with
+//                           c_d*(u_vx + ulft_vjp | urgt_vjp) on the "flx" sets,
+//                           RK3SSP::step_stage (the 4D/6D CPU baseline path)
+//   ref_harness matrices <N> <k>
+//     dumps the 1D operator matrices u_v, u_vx, ulft_vjp, urgt_vjp.
+//
+// Output (text, %.17g): blocks "BEGIN <name> <rows> <cols>" ... "END".
+// Element blocks have one row per element: level[dim] suppt[dim] coeff[(k+1)^dim]
+// where coeff is VecMultiD row-major order (last dimension fastest).
+#include "AllBasis.h"
+#include "AlptBasis.h"
+#include "BilinearForm.h"
+#include "DGAdapt.h"
+#include "DGSolution.h"
+#include "Element.h"
+#include "FastMultiplyLU.h"
+#include "Hash.h"
+#include "HermBasis.h"
+#include "Interpolation.h"
+#include "LagrBasis.h"
+#include "ODESolver.h"
+#include "OperatorMatrix1D.h"
+#include "Timer.h"
+
+#include <chrono>
+#include <cstdio>
+#include <cstdlib>
+#include <string>
+#include <vector>
+
+namespace {
+
+void set_statics(int dim, int k) {
+    AlptBasis::PMAX = k;
+    LagrBasis::PMAX = 3;
+    LagrBasis::msh_case = 1;
+    HermBasis::PMAX = 3;
+    HermBasis::msh_case = 1;
+    Element::PMAX_alpt = AlptBasis::PMAX;
+    Element::PMAX_intp = LagrBasis::PMAX;
+    Element::DIM = dim;
+    Element::VEC_NUM = 1;
+    DGSolution::DIM = dim;
+    DGSolution::VEC_NUM = 1;
+    Interpolation::DIM = dim;
+    Interpolation::VEC_NUM = 1;
+    DGSolution::ind_var_vec = {0};
+    DGAdapt::indicator_var_adapt = {0};
+    Element::is_intp.assign(1, std::vector<bool>(dim, true));
+}
+
+void dump_elements(const char* name, DGSolution& dg, int which) {
+    const int dim = DGSolution::DIM;
+    const int nb = (int)dg.dg.begin()->second.size_alpt();
+    std::printf("BEGIN %s %zu %d\n", name, dg.dg.size(), 2 * dim + nb);
+    for (auto& it : dg.dg) {
+        const Element& e = it.second;
+        for (int d = 0; d < dim; ++d) std::printf("%d ", e.level[d]);
+        for (int d = 0; d < dim; ++d) std::printf("%d ", e.suppt[d]);
+        const VecMultiD<double>& v = (which == 0) ? e.ucoe_alpt[0] : e.rhs[0];
+        for (int i = 0; i < nb; ++i) std::printf("%.17g ", v.at(i));
+        std::printf("\n");
+    }
+    std::printf("END\n");
+}
+
+void dump_matrix(const char* name, const VecMultiD<double>& m, int rows, int cols) {
+    std::printf("BEGIN %s %d %d\n", name, rows, cols);
+    for (int r = 0; r < rows; ++r) {
+        for (int c = 0; c < cols; ++c) std::printf("%.17g ", m.at(r, c));
+        std::printf("\n");
+    }
+    std::printf("END\n");
+}
+
+// The reference's FastRHS transforms are protected; this subclass exposes the
+// single-dimension Alpert->Alpert transform that a linear constant-coefficient
+// operator needs (FastMultiplyLU.cpp:46-59).
+class LinearMatFree : public FastRHS {
+public:
+    explicit LinearMatFree(DGSolution& dg) : FastRHS(dg), dg_(dg) {}
+    void apply_dim(const VecMultiD<double>* mat, int d, double c) {
+        transform_ucoe_alpt_to_rhs(mat, std::string("flx"), d, c, 0);
+    }
+    void zero_rhs() { dg_.set_rhs_zero(); }
+private:
+    DGSolution& dg_;
+};
+
+int run_linear(int argc, char** argv) {
+    if (argc < 10) { std::fprintf(stderr, "linear: bad args\n"); return 2; }
+    const int dim = std::atoi(argv[2]);
+    const int N = std::atoi(argv[3]);
+    const int k = std::atoi(argv[4]);
+    const bool sparse = std::atoi(argv[5]) != 0;
+    const std::string ic = argv[6];
+    const std::string engine = argv[7];
+    const int steps = std::atoi(argv[8]);
+    const double dt = std::atof(argv[9]);
+    if (argc < 10 + dim) { std::fprintf(stderr, "linear: need %d coefficients\n", dim); return 2; }
+    std::vector<double> c(dim);
+    for (int d = 0; d < dim; ++d) c[d] = std::atof(argv[10 + d]);
+
+    set_statics(dim, k);
+    Hash hash;
+    LagrBasis::set_interp_msh01();
+    HermBasis::set_interp_msh01();
+    AllBasis<AlptBasis> all_bas_alpt(N);
+    AllBasis<LagrBasis> all_bas_lagr(N);
+    AllBasis<HermBasis> all_bas_herm(N);
+    OperatorMatrix1D<AlptBasis, AlptBasis> oper(all_bas_alpt, all_bas_alpt, "period");
+
+    const double refine_eps = 1e10, coarsen_eta = -1;
+    DGAdapt dg(sparse, N, N, all_bas_alpt, all_bas_lagr, all_bas_herm, hash, refine_eps, coarsen_eta, true, false);
+
+    const double PI = Const::PI;
+    if (ic == "sin_sum") {
+        // sin(2 pi sum x) expanded into 2^(dim-1) separable products of sin/cos
+        std::vector<std::function<double(double, int)>> funcs;
+        const int nterm = 1 << dim;
+        for (int mask = 0; mask < nterm; ++mask) {
+            // a product with an odd number of sin factors contributes with sign
+            int nsin = __builtin_popcount(mask);
+            if (nsin % 2 == 0) continue;
+            const double sign = ((nsin - 1) / 2) % 2 == 0 ? 1.0 : -1.0;
+            funcs.push_back([=](double x, int d) {
+                double v = ((mask >> d) & 1) ? std::sin(2 * PI * x) : std::cos(2 * PI * x);
+                return d == 0 ? sign * v : v;
+            });
+        }
+        dg.init_separable_scalar_sum(funcs);
+    } else if (ic == "sin_prod") {
+        dg.init_separable_scalar([=](double x, int) { return std::sin(2 * PI * x); });
+    } else {
+        std::fprintf(stderr, "unknown ic\n");
+        return 2;
+    }
+    std::printf("META dim=%d N=%d k=%d sparse=%d elements=%zu dof=%d\n", dim, N, k, (int)sparse, dg.dg.size(), dg.get_dof());
+    dump_elements("u0", dg, 0);
+
+    double t_evolve = 0;
+    if (engine == "assembled") {
+        HyperbolicAlpt op(dg, oper);
+        op.assemble_matrix_scalar(c);
+        RK3SSP ode(op, dt);
+        ode.init();
+        // one operator application on u0, written back into Element::rhs
+        op.multi(ode.ucoe, ode.rhs);
+        ode.eigenvec_to_rhs();
+        dump_elements("rhs0", dg, 1);
+        ode.rhs.setZero();
+        auto t0 = std::chrono::steady_clock::now();
+        for (int s = 0; s < steps; ++s) ode.step_rk();
+        auto t1 = std::chrono::steady_clock::now();
+        t_evolve = std::chrono::duration<double>(t1 - t0).count();
+        ode.final();
+    } else if (engine == "matfree") {
+        std::vector<VecMultiD<double>> mats;
+        for (int d = 0; d < dim; ++d) {
+            VecMultiD<double> m = oper.u_vx;
+            const VecMultiD<double>& f = (c[d] >= 0) ? oper.ulft_vjp : oper.urgt_vjp;
+            for (int r = 0; r < oper.row; ++r)
+                for (int q = 0; q < oper.col; ++q) m.at(r, q) = oper.u_vx.at(r, q) + f.at(r, q);
+            mats.push_back(m);
+        }
+        LinearMatFree fast(dg);
+        auto rhs_eval = [&]() {
+            fast.zero_rhs();
+            for (int d = 0; d < dim; ++d) fast.apply_dim(&mats[d], d, c[d]);
+        };
+        rhs_eval();
+        dump_elements("rhs0", dg, 1);
+        auto t0 = std::chrono::steady_clock::now();
+        for (int s = 0; s < steps; ++s) {
+            RK3SSP ode(dg, dt);
+            ode.init();
+            for (int stage = 0; stage < 3; ++stage) {
+                rhs_eval();
+                ode.set_rhs_zero();
+                ode.add_rhs_to_eigenvec();
+                ode.step_stage(stage);
+                ode.final();
+            }
+        }
+        auto t1 = std::chrono::steady_clock::now();
+        t_evolve = std::chrono::duration<double>(t1 - t0).count();
+    } else {
+        std::fprintf(stderr, "unknown engine\n");
+        return 2;
+    }
+    dump_elements("uT", dg, 0);
+    if (ic == "sin_prod") {
+        // exact solution: translation by c*t
+        const double T = steps * dt;
+        auto f = [=](double x, int d) { return std::sin(2 * PI * (x - c[d] * T)); };
+        const double err = dg.get_L2_error_split_separable_scalar(f, std::pow(0.5, 0.5 * dim));
+        std::printf("L2ERR %.17g\n", err);
+    }
+    std::printf("TIME evolve_s=%.9g dof_stage=%.17g\n", t_evolve, 3.0 * steps * dg.get_dof());
+    return 0;
+}
+
+int run_matrices(int argc, char** argv) {
+    if (argc < 4) return 2;
+    const int N = std::atoi(argv[2]);
+    const int k = std::atoi(argv[3]);
+    set_statics(1, k);
+    AllBasis<AlptBasis> all_bas_alpt(N);
+    OperatorMatrix1D<AlptBasis, AlptBasis> oper(all_bas_alpt, all_bas_alpt, "period");
+    dump_matrix("u_v", oper.u_v, oper.row, oper.col);
+    dump_matrix("u_vx", oper.u_vx, oper.row, oper.col);
+    dump_matrix("ulft_vjp", oper.ulft_vjp, oper.row, oper.col);
+    dump_matrix("urgt_vjp", oper.urgt_vjp, oper.row, oper.col);
+    return 0;
+}
+
+}  // namespace
+
+int main(int argc, char** argv) {
+    if (argc < 2) { std::fprintf(stderr, "usage: ref_harness linear|matrices ...\n"); return 2; }
+    const std::string mode = argv[1];
+    if (mode == "linear") return run_linear(argc, argv);
+    if (mode == "matrices") return run_matrices(argc, argv);
+    std::fprintf(stderr, "unknown mode %s\n", mode.c_str());
+    return 2;
+}

@@ -1,0 +1,100 @@
+"""Generate the golden fixtures that pin the oracle to the AdaM-DG reference.
+
+Runs oracle/_ref/ref_harness (the reference library compiled from its own
+sources, see oracle/Makefile) and stores its outputs, keyed by element
+multi-index, as small .npz files in this directory.  Run in a tree that has
+the reference checkout:  python tests/golden/make_golden.py
+"""
+from __future__ import annotations
+
+import json
+import os
+import subprocess
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+HARNESS = os.path.join(ROOT, "oracle", "_ref", "ref_harness")
+
+
+def parse_harness(text: str) -> dict:
+    """Parse BEGIN/END blocks, META and scalar lines of ref_harness output."""
+    out: dict = {"meta": {}}
+    lines = text.splitlines()
+    i = 0
+    while i < len(lines):
+        ln = lines[i].strip()
+        if ln.startswith("BEGIN"):
+            _, name, rows, cols = ln.split()
+            rows, cols = int(rows), int(cols)
+            data = np.array([[float(v) for v in lines[i + 1 + r].split()] for r in range(rows)]).reshape(rows, cols)
+            out[name] = data
+            i += rows + 2
+            continue
+        if ln.startswith("META"):
+            for kv in ln.split()[1:]:
+                k, v = kv.split("=")
+                out["meta"][k] = int(v)
+        elif ln.startswith("L2ERR"):
+            out["l2err"] = float(ln.split()[1])
+        elif ln.startswith("TIME"):
+            for kv in ln.split()[1:]:
+                k, v = kv.split("=")
+                out["meta"][k] = float(v)
+        i += 1
+    return out
+
+
+def split_elements(block: np.ndarray, dim: int):
+    level = block[:, :dim].astype(np.int32)
+    suppt = block[:, dim:2 * dim].astype(np.int32)
+    coef = block[:, 2 * dim:]
+    return level, suppt, coef
+
+
+def run(args):
+    res = subprocess.run([HARNESS] + [str(a) for a in args], check=True, capture_output=True, text=True)
+    return parse_harness(res.stdout)
+
+
+# (name, dim, N, k, ic, engine, steps, dt, c)
+LINEAR_CASES = [
+    ("lin2d_n4_sinsum", 2, 4, 2, "sin_sum", "assembled", 5, 0.005, [1.0, 1.0]),
+    ("lin2d_n5_mixedc", 2, 5, 2, "sin_sum", "assembled", 3, 0.002, [1.0, -0.5]),
+    ("lin2d_n7_config1", 2, 7, 2, "sin_sum", "assembled", 4, 1.0 / 2561.0, [1.0, 1.0]),
+    ("lin3d_n4_sinprod", 3, 4, 2, "sin_prod", "assembled", 3, 0.004, [1.0, 1.0, 1.0]),
+    ("lin4d_n3_matfree", 4, 3, 2, "sin_prod", "matfree", 2, 0.005, [1.0, 1.0, 1.0, 1.0]),
+    ("lin2d_n4_k1", 2, 4, 1, "sin_sum", "assembled", 3, 0.005, [1.0, 1.0]),
+    ("lin2d_n3_k3", 2, 3, 3, "sin_sum", "assembled", 3, 0.005, [0.7, -1.3]),
+]
+
+
+def main():
+    if not os.path.exists(HARNESS):
+        sys.exit("build the reference first: make -C oracle ref")
+    manifest = {}
+    for name, dim, N, k, ic, engine, steps, dt, c in LINEAR_CASES:
+        r = run(["linear", dim, N, k, 1, ic, engine, steps, repr(dt)] + [repr(x) for x in c])
+        lv, sp, u0 = split_elements(r["u0"], dim)
+        lv2, sp2, rhs0 = split_elements(r["rhs0"], dim)
+        lv3, sp3, uT = split_elements(r["uT"], dim)
+        assert (lv == lv2).all() and (sp == sp2).all() and (lv == lv3).all() and (sp == sp3).all()
+        np.savez_compressed(os.path.join(HERE, name + ".npz"), level=lv, suppt=sp, u0=u0, rhs0=rhs0, uT=uT,
+                            l2err=np.float64(r.get("l2err", np.nan)))
+        manifest[name] = dict(kind="linear", dim=dim, N=N, k=k, ic=ic, engine=engine, steps=steps, dt=dt, c=c,
+                              elements=int(r["meta"]["elements"]))
+        print(name, r["meta"])
+    for N, k in [(4, 2), (3, 1), (3, 3)]:
+        r = run(["matrices", N, k])
+        name = f"oper1d_n{N}_k{k}"
+        np.savez_compressed(os.path.join(HERE, name + ".npz"),
+                            **{m: r[m] for m in ("u_v", "u_vx", "ulft_vjp", "urgt_vjp")})
+        manifest[name] = dict(kind="oper1d", N=N, k=k)
+    with open(os.path.join(HERE, "manifest.json"), "w") as f:
+        json.dump(manifest, f, indent=1)
+
+
+if __name__ == "__main__":
+    main()
