@@ -1,0 +1,520 @@
+// C-ABI of libamdg_gb300 (declared in include/amdg.h).  Host-side handle
+// management, set-up (1D matrices, element table, neighbour lists) and the
+// launch sequences of the device kernels.  No CPU fallback: every compute
+// entry point runs on the device or fails with a status.
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <cstring>
+#include <new>
+#include <string>
+#include <vector>
+
+#include "amdg.h"
+#include "amdg_internal.hpp"
+#include "kernels.cuh"
+
+namespace amdg {
+
+static thread_local std::string g_last_error;
+
+void set_error(const std::string& msg) { g_last_error = msg; }
+
+amdg_status fail(amdg_status s, const std::string& msg) {
+    set_error(msg);
+    return s;
+}
+
+}  // namespace amdg
+
+using namespace amdg;
+
+#define AMDG_CK(call)                                                                                   \
+    do {                                                                                                \
+        cudaError_t amdg_err_ = (call);                                                                 \
+        if (amdg_err_ != cudaSuccess)                                                                   \
+            return fail(AMDG_ERR_CUDA, std::string(#call) + ": " + cudaGetErrorString(amdg_err_));      \
+    } while (0)
+
+#define AMDG_REQUIRE(cond, code, msg) \
+    do {                              \
+        if (!(cond)) return fail(code, msg); \
+    } while (0)
+
+namespace {
+
+cudaStream_t stream_of(const amdg_context* ctx) { return static_cast<cudaStream_t>(ctx->stream); }
+
+template <class T>
+amdg_status dev_alloc(T** p, size_t count) {
+    *p = nullptr;
+    if (count == 0) return AMDG_OK;
+    cudaError_t e = cudaMalloc(reinterpret_cast<void**>(p), count * sizeof(T));
+    if (e != cudaSuccess) return fail(AMDG_ERR_NOMEM, std::string("cudaMalloc: ") + cudaGetErrorString(e));
+    return AMDG_OK;
+}
+
+template <class T>
+amdg_status upload(T** p, const std::vector<T>& host, cudaStream_t st) {
+    amdg_status s = dev_alloc(p, host.size());
+    if (s != AMDG_OK) return s;
+    if (!host.empty()) AMDG_CK(cudaMemcpyAsync(*p, host.data(), host.size() * sizeof(T), cudaMemcpyHostToDevice, st));
+    return AMDG_OK;
+}
+
+int ipow(int b, int e) {
+    int r = 1;
+    while (e-- > 0) r *= b;
+    return r;
+}
+
+amdg_status set_device(const amdg_context* ctx) {
+    AMDG_CK(cudaSetDevice(ctx->device));
+    return AMDG_OK;
+}
+
+// 1D separable projections of nterms terms: [term][d][nb1]
+amdg_status project_terms(const amdg_grid* g, int nterms, amdg_fn1d f, void* user, std::vector<double>* out) {
+    Basis1D b{g->host.k, g->host.nmax};
+    const int nb1 = b.num_basis(), dim = g->host.dim;
+    out->assign(size_t(nterms) * dim * nb1, 0.0);
+    for (int t = 0; t < nterms; ++t)
+        for (int d = 0; d < dim; ++d) project_1d(b, f, user, d, t, out->data() + (size_t(t) * dim + d) * nb1);
+    for (double v : *out)
+        if (!std::isfinite(v)) return fail(AMDG_ERR_NONFINITE, "separable projection produced a non-finite value");
+    return AMDG_OK;
+}
+
+StageCoef rk3_stage_coef(int stage, double dt) {
+    switch (stage) {
+        case 0: return StageCoef{1, 0.0, 1.0, dt};
+        case 1: return StageCoef{1, 3. / 4., 1. / 4., dt};
+        default: return StageCoef{1, 1. / 3., 2. / 3., dt};
+    }
+}
+
+LinearLaunch linear_launch(const amdg_linear_op* op) {
+    const amdg_grid* g = op->grid;
+    LinearLaunch L{};
+    L.dim = g->host.dim;
+    L.np = g->host.k + 1;
+    L.num_elements = g->host.num_elements;
+    L.num_blocks = op->num_blocks;
+    L.row_ptr = op->d_row_ptr;
+    L.src = op->d_src;
+    L.blk = op->d_blk;
+    L.blocks64 = op->d_blocks64;
+    L.blocks32 = op->d_blocks32;
+    return L;
+}
+
+amdg_status rk3_steps_device(amdg_linear_op* op, double dt, int nsteps, amdg_precision prec) {
+    amdg_grid* g = op->grid;
+    cudaStream_t st = stream_of(g->ctx);
+    LinearLaunch L = linear_launch(op);
+    const bool mixed = prec == AMDG_PREC_MIXED;
+    for (int s = 0; s < nsteps; ++s) {
+        // u1 = u + dt L(u); u2 = 3/4 u + 1/4 (u1 + dt L(u1)); u = 1/3 u + 2/3 (u2 + dt L(u2))
+        double* in[3] = {g->d_u, op->d_u1, op->d_u2};
+        double* outp[3] = {op->d_u1, op->d_u2, g->d_u};
+        for (int stage = 0; stage < 3; ++stage) {
+            L.us = in[stage];
+            L.un = g->d_u;
+            L.out = outp[stage];
+            AMDG_CK(launch_linear(L, mixed, rk3_stage_coef(stage, dt), st));
+            g->ctx->launches++;
+        }
+    }
+    return AMDG_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int amdg_abi_version(void) { return AMDG_ABI_VERSION; }
+
+const char* amdg_status_string(amdg_status s) {
+    switch (s) {
+        case AMDG_OK: return "ok";
+        case AMDG_ERR_ARG: return "invalid argument";
+        case AMDG_ERR_CAPACITY: return "capacity exceeded";
+        case AMDG_ERR_NONFINITE: return "non-finite value";
+        case AMDG_ERR_TIMEOUT: return "device wait timed out";
+        case AMDG_ERR_CUDA: return "CUDA error";
+        case AMDG_ERR_STATE: return "invalid state";
+        case AMDG_ERR_NOMEM: return "out of memory";
+    }
+    return "unknown status";
+}
+
+const char* amdg_last_error(void) { return g_last_error.c_str(); }
+
+amdg_status amdg_context_create(int device, amdg_context** out) {
+    AMDG_REQUIRE(out, AMDG_ERR_ARG, "out is null");
+    *out = nullptr;
+    int n = 0;
+    AMDG_CK(cudaGetDeviceCount(&n));
+    AMDG_REQUIRE(device >= 0 && device < n, AMDG_ERR_ARG, "device index out of range");
+    AMDG_CK(cudaSetDevice(device));
+    cudaStream_t st = nullptr;
+    AMDG_CK(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
+    amdg_context* ctx = new (std::nothrow) amdg_context;
+    if (!ctx) {
+        cudaStreamDestroy(st);
+        return fail(AMDG_ERR_NOMEM, "host allocation failed");
+    }
+    ctx->device = device;
+    ctx->stream = st;
+    ctx->own_stream = st;
+    *out = ctx;
+    return AMDG_OK;
+}
+
+amdg_status amdg_context_destroy(amdg_context* ctx) {
+    if (!ctx) return AMDG_OK;
+    cudaSetDevice(ctx->device);
+    if (ctx->own_stream) {
+        cudaStreamSynchronize(static_cast<cudaStream_t>(ctx->own_stream));
+        cudaStreamDestroy(static_cast<cudaStream_t>(ctx->own_stream));
+    }
+    delete ctx;
+    return AMDG_OK;
+}
+
+amdg_status amdg_context_set_stream(amdg_context* ctx, void* cuda_stream) {
+    AMDG_REQUIRE(ctx, AMDG_ERR_ARG, "ctx is null");
+    ctx->stream = cuda_stream ? cuda_stream : ctx->own_stream;
+    return AMDG_OK;
+}
+
+amdg_status amdg_context_get_stream(amdg_context* ctx, void** cuda_stream) {
+    AMDG_REQUIRE(ctx && cuda_stream, AMDG_ERR_ARG, "null argument");
+    *cuda_stream = ctx->stream;
+    return AMDG_OK;
+}
+
+amdg_status amdg_context_synchronize(amdg_context* ctx) {
+    AMDG_REQUIRE(ctx, AMDG_ERR_ARG, "ctx is null");
+    AMDG_CK(cudaStreamSynchronize(stream_of(ctx)));
+    return AMDG_OK;
+}
+
+amdg_status amdg_context_launch_count(amdg_context* ctx, int64_t* count) {
+    AMDG_REQUIRE(ctx && count, AMDG_ERR_ARG, "null argument");
+    *count = ctx->launches;
+    return AMDG_OK;
+}
+
+// ---- host-side set-up --------------------------------------------------------
+
+amdg_status amdg_oper1d_build(int nmax, int k, double* u_v, double* u_vx, double* ulft_vjp, double* urgt_vjp) {
+    AMDG_REQUIRE(k >= 1 && k <= 3, AMDG_ERR_ARG, "Alpert degree k must be 1..3");
+    AMDG_REQUIRE(nmax >= 0 && nmax <= 12, AMDG_ERR_ARG, "nmax must be 0..12");
+    Basis1D b{k, nmax};
+    Oper1D op;
+    build_oper1d(b, &op, u_v != nullptr);
+    const size_t n = size_t(op.nb) * op.nb;
+    if (u_v) std::memcpy(u_v, op.u_v.data(), n * sizeof(double));
+    if (u_vx) std::memcpy(u_vx, op.u_vx.data(), n * sizeof(double));
+    if (ulft_vjp) std::memcpy(ulft_vjp, op.ulft_vjp.data(), n * sizeof(double));
+    if (urgt_vjp) std::memcpy(urgt_vjp, op.urgt_vjp.data(), n * sizeof(double));
+    return AMDG_OK;
+}
+
+amdg_status amdg_grid_enumerate(int dim, int nmax, int sparse, int64_t* num_elements, int32_t* level, int32_t* suppt) {
+    AMDG_REQUIRE(num_elements, AMDG_ERR_ARG, "num_elements is null");
+    AMDG_REQUIRE(dim >= 1 && dim <= kMaxDim, AMDG_ERR_ARG, "dim must be 1..6");
+    AMDG_REQUIRE(nmax >= 0 && nmax <= 16 && dim * nmax <= 60, AMDG_ERR_ARG, "nmax out of range");
+    HostGrid g;
+    build_grid(dim, nmax, sparse, &g);
+    *num_elements = g.num_elements;
+    if (level) {
+        AMDG_REQUIRE(suppt, AMDG_ERR_ARG, "suppt is null");
+        for (size_t i = 0; i < g.order.size(); ++i) {
+            int lv, j;
+            elem_of_order(g.order[i], &lv, &j);
+            level[i] = lv;
+            suppt[i] = j;
+        }
+    }
+    return AMDG_OK;
+}
+
+// ---- grid ------------------------------------------------------------------
+
+amdg_status amdg_grid_create(amdg_context* ctx, int dim, int nmax, int k, int sparse, amdg_grid** out) {
+    AMDG_REQUIRE(ctx && out, AMDG_ERR_ARG, "null argument");
+    *out = nullptr;
+    AMDG_REQUIRE(dim >= 1 && dim <= kMaxDim, AMDG_ERR_ARG, "dim must be 1..6");
+    AMDG_REQUIRE(k >= 1 && k <= 3, AMDG_ERR_ARG, "Alpert degree k must be 1..3");
+    AMDG_REQUIRE(nmax >= 0 && nmax <= 16 && dim * nmax <= 60, AMDG_ERR_ARG, "nmax out of range");
+    amdg_status s = set_device(ctx);
+    if (s != AMDG_OK) return s;
+    amdg_grid* g = new (std::nothrow) amdg_grid;
+    AMDG_REQUIRE(g, AMDG_ERR_NOMEM, "host allocation failed");
+    g->ctx = ctx;
+    g->host.k = k;
+    build_grid(dim, nmax, sparse, &g->host);
+    g->block = ipow(k + 1, dim);
+    g->dof = g->host.num_elements * g->block;
+    if (g->host.num_elements > (int64_t(1) << 31) - 1) {
+        delete g;
+        return fail(AMDG_ERR_CAPACITY, "more than 2^31-1 elements");
+    }
+    cudaStream_t st = stream_of(ctx);
+    if ((s = upload(&g->d_order, g->host.order, st)) != AMDG_OK ||
+        (s = dev_alloc(&g->d_u, size_t(g->dof))) != AMDG_OK ||
+        (s = dev_alloc(&g->d_scratch, size_t(reduce_partials_needed()))) != AMDG_OK) {
+        amdg_grid_destroy(g);
+        return s;
+    }
+    g->scratch_bytes = size_t(reduce_partials_needed()) * sizeof(double);
+    cudaError_t e = cudaMemsetAsync(g->d_u, 0, size_t(g->dof) * sizeof(double), st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    if (e != cudaSuccess) {
+        amdg_grid_destroy(g);
+        return fail(AMDG_ERR_CUDA, std::string("grid init: ") + cudaGetErrorString(e));
+    }
+    *out = g;
+    return AMDG_OK;
+}
+
+amdg_status amdg_grid_destroy(amdg_grid* g) {
+    if (!g) return AMDG_OK;
+    cudaSetDevice(g->ctx->device);
+    cudaStreamSynchronize(stream_of(g->ctx));
+    cudaFree(g->d_order);
+    cudaFree(g->d_u);
+    cudaFree(g->d_scratch);
+    delete g;
+    return AMDG_OK;
+}
+
+amdg_status amdg_grid_size(const amdg_grid* g, int64_t* num_elements, int64_t* dof) {
+    AMDG_REQUIRE(g, AMDG_ERR_ARG, "grid is null");
+    if (num_elements) *num_elements = g->host.num_elements;
+    if (dof) *dof = g->dof;
+    return AMDG_OK;
+}
+
+amdg_status amdg_grid_elements(const amdg_grid* g, int32_t* level, int32_t* suppt) {
+    AMDG_REQUIRE(g && level && suppt, AMDG_ERR_ARG, "null argument");
+    const size_t n = g->host.order.size();
+    for (size_t i = 0; i < n; ++i) {
+        int lv, j;
+        elem_of_order(g->host.order[i], &lv, &j);
+        level[i] = lv;
+        suppt[i] = j;
+    }
+    return AMDG_OK;
+}
+
+amdg_status amdg_grid_max_mesh_level(const amdg_grid* g, int32_t* levels) {
+    AMDG_REQUIRE(g && levels, AMDG_ERR_ARG, "null argument");
+    const int dim = g->host.dim;
+    for (int d = 0; d < dim; ++d) levels[d] = 0;
+    for (int64_t e = 0; e < g->host.num_elements; ++e)
+        for (int d = 0; d < dim; ++d) {
+            const int lv = level_of_order(g->host.order[size_t(e) * dim + d]);
+            if (lv > levels[d]) levels[d] = lv;
+        }
+    return AMDG_OK;
+}
+
+amdg_status amdg_grid_set_coefficients(amdg_grid* g, const double* host, int64_t n) {
+    AMDG_REQUIRE(g && host, AMDG_ERR_ARG, "null argument");
+    AMDG_REQUIRE(n == g->dof, AMDG_ERR_ARG, "size must equal the grid's dof");
+    amdg_status s = set_device(g->ctx);
+    if (s != AMDG_OK) return s;
+    cudaStream_t st = stream_of(g->ctx);
+    AMDG_CK(cudaMemcpyAsync(g->d_u, host, size_t(n) * sizeof(double), cudaMemcpyHostToDevice, st));
+    AMDG_CK(cudaStreamSynchronize(st));
+    return AMDG_OK;
+}
+
+amdg_status amdg_grid_get_coefficients(const amdg_grid* g, double* host, int64_t n) {
+    AMDG_REQUIRE(g && host, AMDG_ERR_ARG, "null argument");
+    AMDG_REQUIRE(n == g->dof, AMDG_ERR_ARG, "size must equal the grid's dof");
+    amdg_status s = set_device(g->ctx);
+    if (s != AMDG_OK) return s;
+    cudaStream_t st = stream_of(g->ctx);
+    AMDG_CK(cudaMemcpyAsync(host, g->d_u, size_t(n) * sizeof(double), cudaMemcpyDeviceToHost, st));
+    AMDG_CK(cudaStreamSynchronize(st));
+    return AMDG_OK;
+}
+
+amdg_status amdg_grid_coefficients_device(amdg_grid* g, double** device_ptr) {
+    AMDG_REQUIRE(g && device_ptr, AMDG_ERR_ARG, "null argument");
+    *device_ptr = g->d_u;
+    return AMDG_OK;
+}
+
+amdg_status amdg_grid_init_separable(amdg_grid* g, int nterms, amdg_fn1d f, void* user) {
+    AMDG_REQUIRE(g && f && nterms > 0, AMDG_ERR_ARG, "bad arguments");
+    amdg_status s = set_device(g->ctx);
+    if (s != AMDG_OK) return s;
+    std::vector<double> coef;
+    if ((s = project_terms(g, nterms, f, user, &coef)) != AMDG_OK) return s;
+    cudaStream_t st = stream_of(g->ctx);
+    double* d_coef = nullptr;
+    if ((s = upload(&d_coef, coef, st)) != AMDG_OK) return s;
+    const int np = g->host.k + 1;
+    cudaError_t e = launch_init_separable(g->d_order, d_coef, g->host.dim, np, (1 << g->host.nmax) * np, nterms,
+                                          g->host.num_elements, g->d_u, st);
+    g->ctx->launches++;
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    cudaFree(d_coef);
+    if (e != cudaSuccess) return fail(AMDG_ERR_CUDA, std::string("init_separable: ") + cudaGetErrorString(e));
+    return AMDG_OK;
+}
+
+static amdg_status reduce_grid(const amdg_grid* g, const double* d_coef, int mode, double* out) {
+    amdg_status s = set_device(g->ctx);
+    if (s != AMDG_OK) return s;
+    cudaStream_t st = stream_of(g->ctx);
+    const int np = g->host.k + 1;
+    AMDG_CK(launch_reduce(g->d_u, g->d_order, d_coef, g->host.dim, np, (1 << g->host.nmax) * np, g->host.num_elements,
+                          mode, g->d_scratch, st));
+    g->ctx->launches += 2;
+    double r = 0.0;
+    AMDG_CK(cudaMemcpyAsync(&r, g->d_scratch + kReduceBlocks, sizeof(double), cudaMemcpyDeviceToHost, st));
+    AMDG_CK(cudaStreamSynchronize(st));
+    if (!std::isfinite(r)) return fail(AMDG_ERR_NONFINITE, "reduction met a non-finite value");
+    *out = r;
+    return AMDG_OK;
+}
+
+amdg_status amdg_grid_l2_norm(const amdg_grid* g, double* out) {
+    AMDG_REQUIRE(g && out, AMDG_ERR_ARG, "null argument");
+    return reduce_grid(g, nullptr, 0, out);
+}
+
+amdg_status amdg_grid_l2_error_separable(const amdg_grid* g, amdg_fn1d f, void* user, double l2_norm_exact, double* out) {
+    AMDG_REQUIRE(g && f && out, AMDG_ERR_ARG, "null argument");
+    std::vector<double> coef;
+    amdg_status s = project_terms(g, 1, f, user, &coef);
+    if (s != AMDG_OK) return s;
+    cudaStream_t st = stream_of(g->ctx);
+    double* d_coef = nullptr;
+    if ((s = upload(&d_coef, coef, st)) != AMDG_OK) return s;
+    double r = 0.0;
+    s = reduce_grid(g, d_coef, 1, &r);
+    cudaFree(d_coef);
+    if (s != AMDG_OK) return s;
+    const double err2 = l2_norm_exact * l2_norm_exact + r;
+    *out = std::sqrt(err2 > 0.0 ? err2 : 0.0);
+    return AMDG_OK;
+}
+
+// ---- linear operator ---------------------------------------------------------
+
+amdg_status amdg_linear_create(amdg_grid* g, const double* coef, amdg_linear_op** out) {
+    AMDG_REQUIRE(g && coef && out, AMDG_ERR_ARG, "null argument");
+    *out = nullptr;
+    amdg_status s = set_device(g->ctx);
+    if (s != AMDG_OK) return s;
+    const int dim = g->host.dim;
+    for (int d = 0; d < dim; ++d) AMDG_REQUIRE(std::isfinite(coef[d]), AMDG_ERR_ARG, "non-finite coefficient");
+    Basis1D b{g->host.k, g->host.nmax};
+    Oper1D op1d;
+    build_oper1d(b, &op1d, false);
+    LinearTopology topo;
+    build_linear_topology(g->host, op1d, coef, &topo);
+    amdg_linear_op* op = new (std::nothrow) amdg_linear_op;
+    AMDG_REQUIRE(op, AMDG_ERR_NOMEM, "host allocation failed");
+    op->grid = g;
+    op->coef.assign(coef, coef + dim);
+    op->pairs = int64_t(topo.src.size());
+    op->num_blocks = topo.num_blocks;
+    std::vector<float> b32(topo.blocks.begin(), topo.blocks.end());
+    cudaStream_t st = stream_of(g->ctx);
+    if ((s = upload(&op->d_row_ptr, topo.row_ptr, st)) != AMDG_OK || (s = upload(&op->d_src, topo.src, st)) != AMDG_OK ||
+        (s = upload(&op->d_blk, topo.blk, st)) != AMDG_OK || (s = upload(&op->d_blocks64, topo.blocks, st)) != AMDG_OK ||
+        (s = upload(&op->d_blocks32, b32, st)) != AMDG_OK || (s = dev_alloc(&op->d_u1, size_t(g->dof))) != AMDG_OK ||
+        (s = dev_alloc(&op->d_u2, size_t(g->dof))) != AMDG_OK) {
+        amdg_linear_destroy(op);
+        return s;
+    }
+    cudaError_t e = cudaStreamSynchronize(st);
+    if (e != cudaSuccess) {
+        amdg_linear_destroy(op);
+        return fail(AMDG_ERR_CUDA, std::string("linear_create: ") + cudaGetErrorString(e));
+    }
+    *out = op;
+    return AMDG_OK;
+}
+
+amdg_status amdg_linear_destroy(amdg_linear_op* op) {
+    if (!op) return AMDG_OK;
+    cudaSetDevice(op->grid->ctx->device);
+    cudaStreamSynchronize(stream_of(op->grid->ctx));
+    cudaFree(op->d_row_ptr);
+    cudaFree(op->d_src);
+    cudaFree(op->d_blk);
+    cudaFree(op->d_blocks64);
+    cudaFree(op->d_blocks32);
+    cudaFree(op->d_u1);
+    cudaFree(op->d_u2);
+    delete op;
+    return AMDG_OK;
+}
+
+amdg_status amdg_linear_stats(const amdg_linear_op* op, int64_t* pairs, double* flops_per_apply) {
+    AMDG_REQUIRE(op, AMDG_ERR_ARG, "op is null");
+    const int np = op->grid->host.k + 1;
+    if (pairs) *pairs = op->pairs;
+    if (flops_per_apply) *flops_per_apply = 2.0 * double(op->pairs) * double(ipow(np, op->grid->host.dim + 1));
+    return AMDG_OK;
+}
+
+amdg_status amdg_linear_apply(amdg_linear_op* op, const double* d_u, double* d_rhs, amdg_precision prec) {
+    AMDG_REQUIRE(op && d_u && d_rhs, AMDG_ERR_ARG, "null argument");
+    AMDG_REQUIRE(d_u != d_rhs, AMDG_ERR_ARG, "input and output must differ");
+    AMDG_REQUIRE(prec == AMDG_PREC_FP64 || prec == AMDG_PREC_MIXED, AMDG_ERR_ARG, "bad precision");
+    amdg_status s = set_device(op->grid->ctx);
+    if (s != AMDG_OK) return s;
+    LinearLaunch L = linear_launch(op);
+    L.us = d_u;
+    L.un = nullptr;
+    L.out = d_rhs;
+    AMDG_CK(launch_linear(L, prec == AMDG_PREC_MIXED, StageCoef{0, 0.0, 0.0, 0.0}, stream_of(op->grid->ctx)));
+    op->grid->ctx->launches++;
+    return AMDG_OK;
+}
+
+amdg_status amdg_rk3ssp_steps(amdg_linear_op* op, double dt, int nsteps, amdg_precision prec) {
+    AMDG_REQUIRE(op && nsteps >= 0 && std::isfinite(dt), AMDG_ERR_ARG, "bad arguments");
+    AMDG_REQUIRE(prec == AMDG_PREC_FP64 || prec == AMDG_PREC_MIXED, AMDG_ERR_ARG, "bad precision");
+    amdg_status s = set_device(op->grid->ctx);
+    if (s != AMDG_OK) return s;
+    return rk3_steps_device(op, dt, nsteps, prec);
+}
+
+amdg_status amdg_rk3ssp_steps_host(amdg_linear_op* op, double dt, int nsteps, double* host_u, amdg_precision prec) {
+    AMDG_REQUIRE(op && host_u && nsteps >= 0 && std::isfinite(dt), AMDG_ERR_ARG, "bad arguments");
+    AMDG_REQUIRE(prec == AMDG_PREC_FP64 || prec == AMDG_PREC_MIXED, AMDG_ERR_ARG, "bad precision");
+    amdg_grid* g = op->grid;
+    amdg_status s = set_device(g->ctx);
+    if (s != AMDG_OK) return s;
+    cudaStream_t st = stream_of(g->ctx);
+    const size_t bytes = size_t(g->dof) * sizeof(double);
+    AMDG_CK(cudaMemcpyAsync(g->d_u, host_u, bytes, cudaMemcpyHostToDevice, st));
+    if ((s = rk3_steps_device(op, dt, nsteps, prec)) != AMDG_OK) return s;
+    AMDG_CK(cudaMemcpyAsync(host_u, g->d_u, bytes, cudaMemcpyDeviceToHost, st));
+    AMDG_CK(cudaStreamSynchronize(st));
+    return AMDG_OK;
+}
+
+amdg_status amdg_rk3_stage_update(amdg_context* ctx, int stage, double dt, const double* d_un, double* d_u,
+                                  const double* d_rhs, int64_t n) {
+    AMDG_REQUIRE(ctx && d_un && d_u && d_rhs && n >= 0, AMDG_ERR_ARG, "bad arguments");
+    AMDG_REQUIRE(stage >= 0 && stage <= 2, AMDG_ERR_ARG, "stage must be 0..2");
+    amdg_status s = set_device(ctx);
+    if (s != AMDG_OK) return s;
+    AMDG_CK(launch_stage_update(d_un, d_u, d_rhs, n, rk3_stage_coef(stage, dt), stream_of(ctx)));
+    ctx->launches++;
+    return AMDG_OK;
+}
+
+}  // extern "C"

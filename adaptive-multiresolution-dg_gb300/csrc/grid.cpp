@@ -1,0 +1,159 @@
+// Flattened sparse-grid element table and the neighbour lists of the linear
+// operator.  Replaces the reference's std::unordered_map<int,Element> with an
+// int32 hash key (DGSolution.h:219, Hash.cpp:55-114) and its O(E^2) pointer
+// discovery (DGSolution.cpp:675-728): elements are sorted packed 64-bit keys
+// and neighbours are found by binary search.
+#include <algorithm>
+#include <cmath>
+#include <unordered_map>
+
+#include "amdg_internal.hpp"
+
+namespace amdg {
+
+static uint64_t pack(const int32_t* o, int dim, int nmax) {
+    uint64_t key = 0;
+    for (int d = 0; d < dim; ++d) key = (key << nmax) | uint64_t(o[d]);
+    return key;
+}
+
+void build_grid(int dim, int nmax, int sparse, HostGrid* g) {
+    g->dim = dim;
+    g->nmax = nmax;
+    g->sparse = sparse;
+    g->order.clear();
+    g->key.clear();
+    // Level vectors with sum <= nmax (sparse) or all of them (full),
+    // DGSolution.cpp:17-27; within a level vector every support combination.
+    // Keys are then sorted, which orders elements lexicographically by their
+    // 1D orders.
+    std::vector<int> lv(dim, 0);
+    std::vector<int32_t> o(dim);
+    for (;;) {
+        int lsum = 0;
+        for (int d = 0; d < dim; ++d) lsum += lv[d];
+        if (!sparse || lsum <= nmax) {
+            int64_t ne = 1;
+            for (int d = 0; d < dim; ++d) ne *= lv[d] == 0 ? 1 : (int64_t(1) << (lv[d] - 1));
+            for (int64_t i = 0; i < ne; ++i) {
+                int64_t rem = i;
+                for (int d = dim - 1; d >= 0; --d) {
+                    const int64_t nd = lv[d] == 0 ? 1 : (int64_t(1) << (lv[d] - 1));
+                    o[d] = lv[d] == 0 ? 0 : int32_t((int64_t(1) << (lv[d] - 1)) + rem % nd);
+                    rem /= nd;
+                }
+                g->key.push_back(pack(o.data(), dim, nmax));
+            }
+        }
+        int d = dim - 1;
+        while (d >= 0) {
+            if (++lv[d] <= nmax) break;
+            lv[d] = 0;
+            --d;
+        }
+        if (d < 0) break;
+    }
+    std::sort(g->key.begin(), g->key.end());
+    g->num_elements = int64_t(g->key.size());
+    g->order.resize(size_t(g->num_elements) * dim);
+    const uint64_t mask = nmax == 0 ? 0 : ((uint64_t(1) << nmax) - 1);
+    for (int64_t e = 0; e < g->num_elements; ++e)
+        for (int d = 0; d < dim; ++d)
+            g->order[size_t(e) * dim + d] = int32_t((g->key[e] >> (uint64_t(nmax) * (dim - 1 - d))) & mask);
+}
+
+int64_t find_element(const HostGrid& g, const int32_t* orders) {
+    const uint64_t key = pack(orders, g.dim, g.nmax);
+    auto it = std::lower_bound(g.key.begin(), g.key.end(), key);
+    if (it == g.key.end() || *it != key) return -1;
+    return int64_t(it - g.key.begin());
+}
+
+// 1D flux-neighbour predicate (Element.cpp:283-348): supports intersect, are
+// adjacent, or are adjacent across the periodic boundary.
+static bool flux_related(int64_t a, int64_t b, int64_t a2, int64_t b2, int64_t one) {
+    const bool no_int = (a >= b2) || (b <= a2);
+    const bool adj = (a == b2) || (b == a2);
+    const bool per = (a == 0 && b2 == one) || (a2 == 0 && b == one);
+    return !no_int || adj || per;
+}
+
+void build_linear_topology(const HostGrid& g, const Oper1D& op, const double* coef, LinearTopology* out) {
+    const int dim = g.dim, nmax = g.nmax, np = g.k + 1, n1 = 1 << nmax;
+    const int64_t one = int64_t(1) << nmax;
+    const int nb = op.nb;
+    // 1D block of (solution element oc -> test element o) in dimension t:
+    // c_t*u_vx on intersecting supports plus c_t*flux, each entry dropped below
+    // 1e-13 as in BilinearFormAlpt::assemble_matrix_alpt (BilinearForm.cpp:64-75).
+    std::vector<std::vector<int>> rel1d(n1);  // solution orders related to test order o
+    out->blocks.clear();
+    // count blocks per dimension first: identical pair list for every dimension
+    std::vector<std::vector<std::vector<double>>> tmp(dim);
+    int nblocks = 0;
+    for (int o = 0; o < n1; ++o) {
+        int64_t a, b;
+        support_units(o, nmax, &a, &b);
+        for (int oc = 0; oc < n1; ++oc) {
+            int64_t a2, b2;
+            support_units(oc, nmax, &a2, &b2);
+            if (!flux_related(a, b, a2, b2, one)) continue;
+            const bool vol = !((a >= b2) || (b <= a2));
+            bool any = false;
+            std::vector<std::vector<double>> blk(dim, std::vector<double>(np * np, 0.0));
+            for (int t = 0; t < dim; ++t) {
+                const std::vector<double>& flux = coef[t] >= 0 ? op.ulft_vjp : op.urgt_vjp;
+                for (int p = 0; p < np; ++p)
+                    for (int q = 0; q < np; ++q) {
+                        const size_t idx = size_t(oc * np + p) * nb + (o * np + q);
+                        double v = 0.0;
+                        const double mv = coef[t] * op.u_vx[idx];
+                        const double mf = coef[t] * flux[idx];
+                        if (vol && std::fabs(mv) >= kRoundOff) v += mv;
+                        if (std::fabs(mf) >= kRoundOff) v += mf;
+                        blk[t][p * np + q] = v;
+                        any = any || (v != 0.0);
+                    }
+            }
+            if (!any) continue;
+            rel1d[o].push_back(oc);
+            for (int t = 0; t < dim; ++t) tmp[t].push_back(blk[t]);
+            ++nblocks;
+        }
+    }
+    out->num_blocks = nblocks;
+    out->blocks.assign(size_t(dim) * nblocks * np * np, 0.0);
+    for (int t = 0; t < dim; ++t)
+        for (int i = 0; i < nblocks; ++i)
+            std::copy(tmp[t][i].begin(), tmp[t][i].end(), out->blocks.begin() + (size_t(t) * nblocks + i) * np * np);
+    // block id of (o, idx-th related)
+    std::vector<int> blk_base(n1 + 1, 0);
+    for (int o = 0; o < n1; ++o) blk_base[o + 1] = blk_base[o] + int(rel1d[o].size());
+
+    const int64_t E = g.num_elements;
+    out->row_ptr.assign(size_t(E) * dim + 1, 0);
+    out->src.clear();
+    out->blk.clear();
+    std::vector<int32_t> o2(dim);
+    for (int64_t e = 0; e < E; ++e) {
+        const int32_t* oe = &g.order[size_t(e) * dim];
+        for (int t = 0; t < dim; ++t) {
+            std::copy(oe, oe + dim, o2.begin());
+            const int o = oe[t];
+            for (size_t i = 0; i < rel1d[o].size(); ++i) {
+                const int id = blk_base[o] + int(i);
+                const double* bp = &out->blocks[(size_t(t) * nblocks + id) * np * np];
+                bool nz = false;
+                for (int m = 0; m < np * np; ++m) nz = nz || (bp[m] != 0.0);
+                if (!nz) continue;  // zero in this dimension (e.g. c_t == 0)
+                o2[t] = rel1d[o][i];
+                const int64_t s = find_element(g, o2.data());
+                if (s < 0) continue;
+                out->src.push_back(int32_t(s));
+                out->blk.push_back(int32_t(id));
+            }
+            out->row_ptr[size_t(e) * dim + t + 1] = int32_t(out->src.size());
+        }
+    }
+}
+
+}  // namespace amdg

@@ -1,0 +1,204 @@
+// Device kernels of the sparse-grid DG right-hand side (sm_103a).
+//
+// linear_apply: matrix-free apply of the linear constant-coefficient operator
+//   rhs[e][q] = sum_t sum_{(s,b) in N_t(e)} sum_p M_t[b][p][q_t] * u[s][q with q_t <- p]
+// i.e. the per-dimension 1D transform of FastMultiplyLU::transform_1D
+// (FastMultiplyLU.cpp:436-512) with the "full" schedule, summed over
+// dimensions as HyperbolicAlpt assembles it (BilinearForm.cpp:691-710).  One
+// thread per output coefficient; every thread of an element walks the same
+// neighbour list, so the list and the 1D block are warp-uniform loads and the
+// neighbour block reads coalesce through L1.  The SSP-RK3 stage update
+// (ODESolver.cpp:285-301) is fused into the epilogue, in FP64 with the
+// reference's operation order and no contraction.
+#include <cuda_runtime.h>
+
+#include <cstdint>
+
+#include "kernels.cuh"
+
+namespace amdg {
+
+template <int B, int E>
+struct IPow { static constexpr int v = B * IPow<B, E - 1>::v; };
+template <int B>
+struct IPow<B, 0> { static constexpr int v = 1; };
+
+__device__ __forceinline__ double rk_combine(double a, double un, double b, double us, double dt, double rhs) {
+    // a*un + b*(us + dt*rhs), each operation rounded (no FMA), as Eigen evaluates it
+    return __dadd_rn(__dmul_rn(a, un), __dmul_rn(b, __dadd_rn(us, __dmul_rn(dt, rhs))));
+}
+
+template <int D, int NP, typename T>
+__global__ void __launch_bounds__(256) linear_apply_kernel(const double* __restrict__ us, const double* un,
+                                                           double* out, const int32_t* __restrict__ row_ptr,
+                                                           const int32_t* __restrict__ src, const int32_t* __restrict__ blk,
+                                                           const T* __restrict__ blocks, int nblocks, int64_t total,
+                                                           StageCoef rk) {
+    constexpr int B = IPow<NP, D>::v;
+    const int64_t gid = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (gid >= total) return;
+    const int64_t e = gid / B;
+    const int q = int(gid - e * B);
+    T acc = T(0);
+#pragma unroll
+    for (int t = 0; t < D; ++t) {
+        int stride = 1;
+#pragma unroll
+        for (int s = t + 1; s < D; ++s) stride *= NP;
+        const int qt = (q / stride) % NP;
+        const int base = q - qt * stride;
+        const int beg = __ldg(row_ptr + e * D + t);
+        const int end = __ldg(row_ptr + e * D + t + 1);
+        const T* bt = blocks + size_t(t) * nblocks * NP * NP + qt;
+        for (int i = beg; i < end; ++i) {
+            const int s = __ldg(src + i);
+            const T* m = bt + __ldg(blk + i) * NP * NP;
+            const double* x = us + int64_t(s) * B + base;
+#pragma unroll
+            for (int p = 0; p < NP; ++p) acc = fma(__ldg(m + p * NP), T(__ldg(x + p * stride)), acc);
+        }
+    }
+    const double rhs = double(acc);
+    if (rk.mode == 0) {
+        out[gid] = rhs;
+    } else {
+        out[gid] = rk_combine(rk.a, un[gid], rk.b, us[gid], rk.dt, rhs);
+    }
+}
+
+template <int D, int NP, typename T>
+static cudaError_t launch_linear_t(const LinearLaunch& L, const T* blocks, StageCoef rk, cudaStream_t st) {
+    constexpr int B = IPow<NP, D>::v;
+    const int64_t total = L.num_elements * B;
+    if (total == 0) return cudaSuccess;
+    const int threads = 256;
+    const int64_t grid = (total + threads - 1) / threads;
+    linear_apply_kernel<D, NP, T><<<unsigned(grid), threads, 0, st>>>(L.us, L.un, L.out, L.row_ptr, L.src, L.blk, blocks,
+                                                                     L.num_blocks, total, rk);
+    return cudaGetLastError();
+}
+
+template <typename T>
+static cudaError_t dispatch_linear(const LinearLaunch& L, const T* blocks, StageCoef rk, cudaStream_t st) {
+#define AMDG_CASE(D, NP) \
+    if (L.dim == D && L.np == NP) return launch_linear_t<D, NP, T>(L, blocks, rk, st);
+    AMDG_CASE(1, 2) AMDG_CASE(1, 3) AMDG_CASE(1, 4)
+    AMDG_CASE(2, 2) AMDG_CASE(2, 3) AMDG_CASE(2, 4)
+    AMDG_CASE(3, 2) AMDG_CASE(3, 3) AMDG_CASE(3, 4)
+    AMDG_CASE(4, 2) AMDG_CASE(4, 3) AMDG_CASE(4, 4)
+    AMDG_CASE(5, 2) AMDG_CASE(5, 3) AMDG_CASE(5, 4)
+    AMDG_CASE(6, 2) AMDG_CASE(6, 3) AMDG_CASE(6, 4)
+#undef AMDG_CASE
+    return cudaErrorInvalidValue;
+}
+
+cudaError_t launch_linear(const LinearLaunch& L, bool mixed, StageCoef rk, cudaStream_t st) {
+    return mixed ? dispatch_linear<float>(L, L.blocks32, rk, st) : dispatch_linear<double>(L, L.blocks64, rk, st);
+}
+
+// ---- stage update for an externally computed rhs --------------------------
+__global__ void stage_update_kernel(const double* un, double* u, const double* __restrict__ rhs,
+                                    int64_t n, StageCoef rk) {
+    const int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (i < n) u[i] = rk_combine(rk.a, un[i], rk.b, u[i], rk.dt, rhs[i]);
+}
+
+cudaError_t launch_stage_update(const double* un, double* u, const double* rhs, int64_t n, StageCoef rk, cudaStream_t st) {
+    if (n == 0) return cudaSuccess;
+    const int threads = 256;
+    stage_update_kernel<<<unsigned((n + threads - 1) / threads), threads, 0, st>>>(un, u, rhs, n, rk);
+    return cudaGetLastError();
+}
+
+// ---- separable initialisation ----------------------------------------------
+// u[e][q] = sum_term prod_d coef1d[term][d][o_d*(k+1) + q_d]
+// (DGSolution::init_elem_separable, DGSolution.cpp:170-184; same product order)
+__global__ void init_separable_kernel(const int32_t* __restrict__ order, const double* __restrict__ coef1d, int dim, int np,
+                                      int nb1, int nterms, int B, int64_t total, double* __restrict__ u) {
+    const int64_t gid = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (gid >= total) return;
+    const int64_t e = gid / B;
+    const int q = int(gid - e * B);
+    int dig[8];
+    int rem = q;
+    for (int d = dim - 1; d >= 0; --d) { dig[d] = rem % np; rem /= np; }
+    double sum = 0.0;
+    for (int t = 0; t < nterms; ++t) {
+        double v = 1.0;
+        for (int d = 0; d < dim; ++d) v = __dmul_rn(v, coef1d[(size_t(t) * dim + d) * nb1 + order[e * dim + d] * np + dig[d]]);
+        sum = __dadd_rn(sum, v);
+    }
+    u[gid] = sum;
+}
+
+cudaError_t launch_init_separable(const int32_t* order, const double* coef1d, int dim, int np, int nb1, int nterms,
+                                  int64_t num_elements, double* u, cudaStream_t st) {
+    int B = 1;
+    for (int d = 0; d < dim; ++d) B *= np;
+    const int64_t total = num_elements * B;
+    if (total == 0) return cudaSuccess;
+    init_separable_kernel<<<unsigned((total + 255) / 256), 256, 0, st>>>(order, coef1d, dim, np, nb1, nterms, B, total, u);
+    return cudaGetLastError();
+}
+
+// ---- FP64 reductions (deterministic two-pass) -------------------------------
+// mode 0: sum u^2;  mode 1: sum (u^2 - 2 u prod_d c_exact) (split L2 error,
+// DGSolution.cpp:217-256)
+constexpr int kReduceThreads = 256;
+
+__global__ void reduce_pass1(const double* __restrict__ u, const int32_t* __restrict__ order,
+                             const double* __restrict__ coef1d, int dim, int np, int nb1, int B, int64_t total, int mode,
+                             double* __restrict__ partial) {
+    __shared__ double sh[kReduceThreads];
+    double s = 0.0;
+    for (int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; i < total; i += int64_t(gridDim.x) * blockDim.x) {
+        const double v = u[i];
+        double term = v * v;
+        if (mode == 1) {
+            const int64_t e = i / B;
+            int rem = int(i - e * B);
+            int dig[8];
+            for (int d = dim - 1; d >= 0; --d) { dig[d] = rem % np; rem /= np; }
+            double c = 1.0;
+            for (int d = 0; d < dim; ++d) c *= coef1d[size_t(d) * nb1 + order[e * dim + d] * np + dig[d]];
+            term -= 2.0 * v * c;
+        }
+        s += term;
+    }
+    sh[threadIdx.x] = s;
+    __syncthreads();
+    for (int w = blockDim.x / 2; w > 0; w >>= 1) {
+        if (threadIdx.x < w) sh[threadIdx.x] += sh[threadIdx.x + w];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) partial[blockIdx.x] = sh[0];
+}
+
+__global__ void reduce_pass2(const double* __restrict__ partial, int n, double* __restrict__ result) {
+    __shared__ double sh[kReduceThreads];
+    double s = 0.0;
+    for (int i = threadIdx.x; i < n; i += blockDim.x) s += partial[i];
+    sh[threadIdx.x] = s;
+    __syncthreads();
+    for (int w = blockDim.x / 2; w > 0; w >>= 1) {
+        if (threadIdx.x < w) sh[threadIdx.x] += sh[threadIdx.x + w];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) result[0] = sh[0];
+}
+
+int reduce_partials_needed() { return kReduceBlocks + 1; }
+
+cudaError_t launch_reduce(const double* u, const int32_t* order, const double* coef1d, int dim, int np, int nb1,
+                          int64_t num_elements, int mode, double* scratch, cudaStream_t st) {
+    int B = 1;
+    for (int d = 0; d < dim; ++d) B *= np;
+    const int64_t total = num_elements * B;
+    reduce_pass1<<<kReduceBlocks, kReduceThreads, 0, st>>>(u, order, coef1d, dim, np, nb1, B, total, mode, scratch);
+    cudaError_t err = cudaGetLastError();
+    if (err != cudaSuccess) return err;
+    reduce_pass2<<<1, kReduceThreads, 0, st>>>(scratch, kReduceBlocks, scratch + kReduceBlocks);
+    return cudaGetLastError();
+}
+
+}  // namespace amdg

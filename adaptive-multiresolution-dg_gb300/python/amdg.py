@@ -1,0 +1,261 @@
+"""ctypes binding of libamdg_gb300 (include/amdg.h).
+
+Thin Python mirror of the reference's C++ interface for the sparse-grid DG
+right-hand side: Grid ~ DGSolution/DGAdapt, LinearOperator ~ HyperbolicAlpt +
+RK3SSP.  Every compute call goes to the CUDA library; if the shared library
+is missing this module raises instead of computing anything on the CPU.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+PKG = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+LIB_PATH = os.path.join(PKG, "lib", "libamdg_gb300.so")
+HEADER = os.path.join(os.path.dirname(PKG), "include", "amdg.h")
+
+FP64 = 0
+MIXED = 1
+
+STATUS = {0: "ok", 1: "invalid argument", 2: "capacity exceeded", 3: "non-finite value", 4: "device wait timed out",
+          5: "CUDA error", 6: "invalid state", 7: "out of memory"}
+
+FN1D = C.CFUNCTYPE(C.c_double, C.c_double, C.c_int, C.c_int, C.c_void_p)
+
+
+class AmdgError(RuntimeError):
+    def __init__(self, status: int, where: str, msg: str):
+        super().__init__(f"{where}: {STATUS.get(status, status)}: {msg}")
+        self.status = status
+
+
+_lib = None
+
+
+def load():
+    """Load libamdg_gb300.so (build it first with __graft_entry__.build())."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(LIB_PATH):
+        raise ImportError(f"{LIB_PATH} not found: the CUDA library must be built (no CPU fallback exists)")
+    L = C.CDLL(LIB_PATH)
+    vp, i32, i64, dbl = C.c_void_p, C.c_int, C.c_int64, C.c_double
+    pp = C.POINTER(C.c_void_p)
+    sig = {
+        "amdg_abi_version": ([], i32),
+        "amdg_status_string": ([i32], C.c_char_p),
+        "amdg_last_error": ([], C.c_char_p),
+        "amdg_context_create": ([i32, pp], i32),
+        "amdg_context_destroy": ([vp], i32),
+        "amdg_context_set_stream": ([vp, vp], i32),
+        "amdg_context_get_stream": ([vp, pp], i32),
+        "amdg_context_synchronize": ([vp], i32),
+        "amdg_context_launch_count": ([vp, C.POINTER(i64)], i32),
+        "amdg_oper1d_build": ([i32, i32, vp, vp, vp, vp], i32),
+        "amdg_grid_enumerate": ([i32, i32, i32, C.POINTER(i64), vp, vp], i32),
+        "amdg_grid_create": ([vp, i32, i32, i32, i32, pp], i32),
+        "amdg_grid_destroy": ([vp], i32),
+        "amdg_grid_size": ([vp, C.POINTER(i64), C.POINTER(i64)], i32),
+        "amdg_grid_elements": ([vp, vp, vp], i32),
+        "amdg_grid_max_mesh_level": ([vp, vp], i32),
+        "amdg_grid_set_coefficients": ([vp, vp, i64], i32),
+        "amdg_grid_get_coefficients": ([vp, vp, i64], i32),
+        "amdg_grid_coefficients_device": ([vp, pp], i32),
+        "amdg_grid_init_separable": ([vp, i32, FN1D, vp], i32),
+        "amdg_grid_l2_norm": ([vp, C.POINTER(dbl)], i32),
+        "amdg_grid_l2_error_separable": ([vp, FN1D, vp, dbl, C.POINTER(dbl)], i32),
+        "amdg_linear_create": ([vp, vp, pp], i32),
+        "amdg_linear_destroy": ([vp], i32),
+        "amdg_linear_stats": ([vp, C.POINTER(i64), C.POINTER(dbl)], i32),
+        "amdg_linear_apply": ([vp, vp, vp, i32], i32),
+        "amdg_rk3ssp_steps": ([vp, dbl, i32, i32], i32),
+        "amdg_rk3ssp_steps_host": ([vp, dbl, i32, vp, i32], i32),
+        "amdg_rk3_stage_update": ([vp, i32, dbl, vp, vp, vp, i64], i32),
+    }
+    for name, (args, res) in sig.items():
+        fn = getattr(L, name)
+        fn.argtypes = args
+        fn.restype = res
+    _lib = L
+    return L
+
+
+def _ck(status: int, where: str):
+    if status != 0:
+        raise AmdgError(status, where, load().amdg_last_error().decode())
+
+
+def _ptr(a: np.ndarray):
+    return a.ctypes.data_as(C.c_void_p)
+
+
+def declared_functions() -> list[str]:
+    """Names of every entry point declared in include/amdg.h."""
+    import re
+    text = open(HEADER).read()
+    return sorted(set(re.findall(r"^\s*(?:amdg_status|int|const char\*)\s+(amdg_\w+)\s*\(", text, re.M)))
+
+
+def oper1d(nmax: int, k: int) -> dict:
+    """OperatorMatrix1D equivalent (host): u_v, u_vx, ulft_vjp, urgt_vjp."""
+    nb = (1 << nmax) * (k + 1)
+    mats = {n: np.zeros((nb, nb)) for n in ("u_v", "u_vx", "ulft_vjp", "urgt_vjp")}
+    _ck(load().amdg_oper1d_build(nmax, k, *(_ptr(m) for m in mats.values())), "oper1d_build")
+    return mats
+
+
+def enumerate_grid(dim: int, nmax: int, sparse: bool = True):
+    n = C.c_int64()
+    _ck(load().amdg_grid_enumerate(dim, nmax, int(sparse), C.byref(n), None, None), "grid_enumerate")
+    level = np.zeros((n.value, dim), np.int32)
+    suppt = np.zeros((n.value, dim), np.int32)
+    _ck(load().amdg_grid_enumerate(dim, nmax, int(sparse), C.byref(n), _ptr(level), _ptr(suppt)), "grid_enumerate")
+    return level, suppt
+
+
+def _fn1d(funcs):
+    def cb(x, d, term, _user):
+        return float(funcs[term](x, d))
+    return FN1D(cb)
+
+
+class Context:
+    def __init__(self, device: int = 0):
+        self._h = C.c_void_p()
+        _ck(load().amdg_context_create(device, C.byref(self._h)), "context_create")
+
+    @property
+    def handle(self):
+        return self._h
+
+    def set_stream(self, stream_handle: int | None):
+        _ck(load().amdg_context_set_stream(self._h, C.c_void_p(stream_handle or 0)), "context_set_stream")
+
+    def synchronize(self):
+        _ck(load().amdg_context_synchronize(self._h), "context_synchronize")
+
+    def launch_count(self) -> int:
+        n = C.c_int64()
+        _ck(load().amdg_context_launch_count(self._h, C.byref(n)), "context_launch_count")
+        return n.value
+
+    def stage_update(self, stage: int, dt: float, d_un: int, d_u: int, d_rhs: int, n: int):
+        _ck(load().amdg_rk3_stage_update(self._h, stage, dt, C.c_void_p(d_un), C.c_void_p(d_u), C.c_void_p(d_rhs), n),
+            "rk3_stage_update")
+
+    def close(self):
+        if self._h:
+            load().amdg_context_destroy(self._h)
+            self._h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class Grid:
+    """DGSolution/DGAdapt on the device (sparse or full grid, Alpert degree k)."""
+
+    def __init__(self, ctx: Context, dim: int, nmax: int, k: int = 2, sparse: bool = True):
+        self.ctx, self.dim, self.nmax, self.k = ctx, dim, nmax, k
+        self._h = C.c_void_p()
+        _ck(load().amdg_grid_create(ctx.handle, dim, nmax, k, int(sparse), C.byref(self._h)), "grid_create")
+        ne, dof = C.c_int64(), C.c_int64()
+        _ck(load().amdg_grid_size(self._h, C.byref(ne), C.byref(dof)), "grid_size")
+        self.num_elements, self.dof = ne.value, dof.value
+        self.block = (k + 1) ** dim
+
+    @property
+    def handle(self):
+        return self._h
+
+    def elements(self):
+        level = np.zeros((self.num_elements, self.dim), np.int32)
+        suppt = np.zeros((self.num_elements, self.dim), np.int32)
+        _ck(load().amdg_grid_elements(self._h, _ptr(level), _ptr(suppt)), "grid_elements")
+        return level, suppt
+
+    def max_mesh_level(self):
+        out = np.zeros(self.dim, np.int32)
+        _ck(load().amdg_grid_max_mesh_level(self._h, _ptr(out)), "grid_max_mesh_level")
+        return out
+
+    def set_coefficients(self, u: np.ndarray):
+        u = np.ascontiguousarray(u, np.float64).reshape(-1)
+        _ck(load().amdg_grid_set_coefficients(self._h, _ptr(u), u.size), "grid_set_coefficients")
+
+    def coefficients(self) -> np.ndarray:
+        u = np.zeros(self.dof)
+        _ck(load().amdg_grid_get_coefficients(self._h, _ptr(u), u.size), "grid_get_coefficients")
+        return u.reshape(self.num_elements, self.block)
+
+    def device_ptr(self) -> int:
+        p = C.c_void_p()
+        _ck(load().amdg_grid_coefficients_device(self._h, C.byref(p)), "grid_coefficients_device")
+        return p.value
+
+    def init_separable(self, funcs):
+        cb = _fn1d(funcs)
+        _ck(load().amdg_grid_init_separable(self._h, len(funcs), cb, None), "grid_init_separable")
+
+    def l2_norm_sq(self) -> float:
+        r = C.c_double()
+        _ck(load().amdg_grid_l2_norm(self._h, C.byref(r)), "grid_l2_norm")
+        return r.value
+
+    def l2_error_separable(self, func, l2_norm_exact: float) -> float:
+        cb = _fn1d([func])
+        r = C.c_double()
+        _ck(load().amdg_grid_l2_error_separable(self._h, cb, None, l2_norm_exact, C.byref(r)), "grid_l2_error_separable")
+        return r.value
+
+    def close(self):
+        if self._h:
+            load().amdg_grid_destroy(self._h)
+            self._h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class LinearOperator:
+    """HyperbolicAlpt (upwind, constant coefficients) + RK3SSP on the device."""
+
+    def __init__(self, grid: Grid, coef):
+        self.grid = grid
+        c = np.ascontiguousarray(coef, np.float64)
+        assert c.size == grid.dim
+        self._h = C.c_void_p()
+        _ck(load().amdg_linear_create(grid.handle, _ptr(c), C.byref(self._h)), "linear_create")
+        pairs, flops = C.c_int64(), C.c_double()
+        _ck(load().amdg_linear_stats(self._h, C.byref(pairs), C.byref(flops)), "linear_stats")
+        self.pairs, self.flops_per_apply = pairs.value, flops.value
+
+    def apply_device(self, d_u: int, d_rhs: int, prec: int = FP64):
+        _ck(load().amdg_linear_apply(self._h, C.c_void_p(d_u), C.c_void_p(d_rhs), prec), "linear_apply")
+
+    def rk3_steps(self, dt: float, nsteps: int, prec: int = FP64):
+        _ck(load().amdg_rk3ssp_steps(self._h, dt, nsteps, prec), "rk3ssp_steps")
+
+    def rk3_steps_host(self, u: np.ndarray, dt: float, nsteps: int, prec: int = FP64):
+        assert u.dtype == np.float64 and u.flags.c_contiguous and u.size == self.grid.dof
+        _ck(load().amdg_rk3ssp_steps_host(self._h, dt, nsteps, _ptr(u), prec), "rk3ssp_steps_host")
+
+    def close(self):
+        if self._h:
+            load().amdg_linear_destroy(self._h)
+            self._h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

@@ -1,0 +1,329 @@
+"""Benchmark: DOF-stage updates/s of the sparse-grid DG right-hand side with
+fused SSP-RK3 stage updates, on the 6D constant-coefficient linear advection
+workload (u_t + sum_d u_{x_d} = 0 on the periodic unit cube, sparse grid
+N=8, Alpert k=2: 47,264 elements, 34,455,456 DOF, IC prod_d sin(2 pi x_d)).
+
+One step = one SSP-RK3 time step (3 stages) over the whole grid.  Both
+arithmetic modes are timed: plain FP64 and mixed (FP32 operator apply, FP64
+state and stage accumulation); the headline `value` is the mixed mode, with
+the FP64 mode and both L2 errors against the exact solution beside it.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+--impl reference times the oracle's CPU implementation of the same path
+(port of the reference algorithm) on the host cores.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.join(ROOT, "adaptive-multiresolution-dg_gb300", "python"))
+sys.path.insert(0, os.path.join(ROOT, "oracle"))
+
+DIM, NMAX, K = 6, 8, 2
+COEF = [1.0] * DIM
+CFL = 0.1
+METRIC = "DOF-stage updates/s at matched L2 error: plain FP64 vs mixed+learned-adapt"
+WORKLOAD = "6D linear advection, sparse grid N=8, Alpert k=2, SSP-RK3 (34,455,456 DOF)"
+
+
+def peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            return json.load(f), "measured"
+    except OSError:
+        return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0}, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+              "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+              "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index=0):
+        self.index = index
+        self.samples = []
+        self._stop = threading.Event()
+        self._t = None
+
+    def _run(self):
+        while not self._stop.is_set():
+            try:
+                out = subprocess.run(["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.FIELDS}",
+                                      "--format=csv,noheader,nounits"], capture_output=True, text=True, timeout=5)
+                self.samples.append([v.strip() for v in out.stdout.strip().split(",")])
+            except Exception:
+                pass
+            self._stop.wait(0.2)
+
+    def __enter__(self):
+        self._t = threading.Thread(target=self._run, daemon=True)
+        self._t.start()
+        return self
+
+    def __exit__(self, *exc):
+        self._stop.set()
+        self._t.join(timeout=10)
+
+    def summary(self):
+        sm = [float(s[0]) for s in self.samples if len(s) >= 7 and s[0].replace(".", "").isdigit()]
+        mx = [float(s[1]) for s in self.samples if len(s) >= 7 and s[1].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for s in self.samples if len(s) >= 7 for i in range(4) if s[3 + i] == "Active"})
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(self.samples)}
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+def dt_for():
+    dx = 1.0 / (1 << NMAX)
+    return CFL * dx / sum(abs(c) for c in COEF)
+
+
+def exact_l2(g, t):
+    return g.l2_error_separable(lambda x, d: math.sin(2 * math.pi * (x - COEF[d] * t)), 0.5 ** (0.5 * DIM))
+
+
+def fp64_peak_tflops(torch):
+    """Measured FP64 FMA throughput of this GPU (torch float64 GEMM, best of 5)."""
+    n = 4096
+    a = torch.randn(n, n, dtype=torch.float64, device="cuda")
+    b = torch.randn(n, n, dtype=torch.float64, device="cuda")
+    for _ in range(2):
+        torch.mm(a, b)
+    torch.cuda.synchronize()
+    best = float("inf")
+    for _ in range(5):
+        s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        s.record()
+        torch.mm(a, b)
+        e.record()
+        e.synchronize()
+        best = min(best, s.elapsed_time(e) / 1e3)
+    del a, b
+    return 2.0 * n ** 3 / best / 1e12
+
+
+def run_ours(args):
+    import torch
+
+    import amdg
+
+    rank, world, local = dist_env()
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    ctx = amdg.Context(local)
+    stream = torch.cuda.current_stream()
+    ctx.set_stream(stream.cuda_stream)
+    g = amdg.Grid(ctx, DIM, NMAX, K)
+    g.init_separable([lambda x, d: math.sin(2 * math.pi * x)])
+    u0 = g.coefficients().reshape(-1).copy()
+    op = amdg.LinearOperator(g, COEF)
+    dt = dt_for()
+    dof = g.dof
+
+    def barrier():
+        if world > 1:
+            torch.distributed.barrier()
+        torch.cuda.synchronize()
+
+    def timed_device(prec):
+        g.set_coefficients(u0)
+        op.rk3_steps(dt, args.warmup, prec)
+        g.set_coefficients(u0)
+        barrier()
+        l0 = ctx.launch_count()
+        s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        s.record(stream)
+        op.rk3_steps(dt, args.steps, prec)
+        e.record(stream)
+        barrier()
+        launches = ctx.launch_count() - l0
+        sec = s.elapsed_time(e) / 1e3
+        if world > 1:
+            t = torch.tensor([sec], device="cuda")
+            torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+            sec = float(t.item())
+        err = exact_l2(g, args.steps * dt)
+        return sec, launches, err
+
+    def timed_kernel(prec, reps=6):
+        """Average duration of one fused stage launch (dominant kernel), CUDA events on its stream."""
+        g.set_coefficients(u0)
+        op.rk3_steps(dt, 1, prec)
+        torch.cuda.synchronize()
+        s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        s.record(stream)
+        op.rk3_steps(dt, reps, prec)
+        e.record(stream)
+        e.synchronize()
+        return s.elapsed_time(e) / 1e3 / (3 * reps)
+
+    with ClockSampler(local) as clk:
+        sec64, launches64, err64 = timed_device(amdg.FP64)
+        sec32, launches32, err32 = timed_device(amdg.MIXED)
+    clocks = clk.summary()
+    k64 = timed_kernel(amdg.FP64)
+    k32 = timed_kernel(amdg.MIXED)
+
+    # end-to-end through the C-ABI host-buffer call: H2D of the state, 3 stages, D2H, every step
+    pinned = torch.empty(dof, dtype=torch.float64, pin_memory=True)
+    host = pinned.numpy()
+    host[:] = u0
+    op.rk3_steps_host(host, dt, 1, amdg.MIXED)  # warm-up
+    host[:] = u0
+    barrier()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        op.rk3_steps_host(host, dt, 1, amdg.MIXED)
+    barrier()
+    e2e_sec = time.perf_counter() - t0
+
+    pairs, flops = op.pairs, op.flops_per_apply
+    E = g.num_elements
+    bytes_per_launch = 24.0 * dof + 8.0 * pairs + 4.0 * (E * DIM + 1)
+    pk, pk_kind = peaks()
+    fp64_peak = fp64_peak_tflops(torch)
+    units = 3.0 * dof * args.steps * world
+    value32 = units / sec32
+    value64 = units / sec64
+    ach32 = bytes_per_launch / k32 / 1e9
+    ach64 = bytes_per_launch / k64 / 1e9
+    line = {
+        "metric": METRIC,
+        "value": value32,
+        "unit": "DOF-stage updates/s",
+        "n_gpus": world,
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "ms_per_step": sec32 / args.steps * 1e3,
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "f32 operator apply, f64 state and RK3 stage accumulation",
+        "data": "synthetic: IC prod_d sin(2 pi x_d) projected onto the sparse grid",
+        "config": {"workload": WORKLOAD, "dim": DIM, "nmax": NMAX, "k": K, "elements": E, "dof": dof,
+                   "dt": dt, "l2_flush": "inputs larger than L2 (state 276 MB > 129 MB L2)",
+                   "parallelism": "replicas" if world > 1 else "single GPU"},
+        "l2_error_vs_exact": {"mixed": err32, "fp64": err64, "rel_diff": abs(err32 - err64) / err64},
+        "plain_fp64": {"value": value64, "ms_per_step": sec64 / args.steps * 1e3, "kernel_ms": k64 * 1e3,
+                       "fp64_tflops": flops / k64 / 1e12, "fp64_peak_tflops_measured": fp64_peak,
+                       "fp64_frac": flops / k64 / 1e12 / fp64_peak,
+                       "hbm_frac": ach64 / pk["hbm_gbs"]},
+        "roofline": {"bound": "hbm", "achieved": ach32, "peak": pk["hbm_gbs"], "unit": "GB/s",
+                     "frac": ach32 / pk["hbm_gbs"], "traffic": None, "peak_kind": pk_kind,
+                     "kernel": "linear_apply_kernel<6,3,float> (fused RK3 stage)", "kernel_ms": k32 * 1e3,
+                     "algorithmic_bytes_per_launch": bytes_per_launch,
+                     "fp32_tflops": flops / k32 / 1e12},
+        "e2e": {"value": units / e2e_sec if world == 1 else None, "unit": "DOF-stage updates/s",
+                "h2d_bytes_per_step": 8 * dof, "d2h_bytes_per_step": 8 * dof,
+                "call": "amdg_rk3ssp_steps_host (mixed), pinned host buffer"},
+        "gpu_launches": launches32,
+        "clocks": clocks,
+    }
+    if rank == 0 and world == 1:
+        line["cpu_baseline"] = cpu_baseline(g, u0, budget_s=args.cpu_seconds)
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        torch.distributed.destroy_process_group()
+
+
+def cpu_baseline(g, u0, budget_s=15.0):
+    """Oracle (port of the reference algorithm) on the host cores: one RHS
+    evaluation over a bounded, contiguous sample of elements of the same grid,
+    repeated until ~budget_s of CPU time; DOF-stage updates/s."""
+    import amdg_oracle as O
+    lv, sp = g.elements()
+    op = O.LinearOp(DIM, NMAX, K, lv, sp, COEF)
+    cores = os.cpu_count() or 1
+    u = u0.reshape(g.num_elements, -1)
+    n_el = 4096
+    e0 = g.num_elements // 2 - n_el // 2
+    op.apply_range(u, e0, e0 + 64, cores)  # warm caches
+    done, t0 = 0, time.perf_counter()
+    while time.perf_counter() - t0 < budget_s:
+        op.apply_range(u, e0, e0 + n_el, cores)
+        done += n_el
+    sec = time.perf_counter() - t0
+    op.close()
+    return {"value": done * g.block / sec, "unit": "DOF-stage updates/s", "cores": cores, "kind": "port",
+            "sample": f"{done} element-RHS evaluations (blocks of {n_el} contiguous elements of the 6D N=8 grid), "
+                      f"{sec:.1f} s"}
+
+
+def run_reference(args):
+    """CPU implementation of the same path (oracle port of the reference
+    algorithm), all host threads, bounded sample per step."""
+    rank, world, _ = dist_env()
+    if rank != 0:
+        return
+    import amdg_oracle as O
+    lv, sp = O.grid(DIM, NMAX)
+    E = lv.shape[0]
+    B = (K + 1) ** DIM
+    coef = O.project_separable(NMAX, K, DIM, [lambda x, d: math.sin(2 * math.pi * x)])
+    u = O.init_separable(DIM, NMAX, K, lv, sp, coef)
+    op = O.LinearOp(DIM, NMAX, K, lv, sp, COEF)
+    cores = os.cpu_count() or 1
+    n_el = 2048  # per step: 3 stage evaluations over a 2048-element sample
+    e0 = E // 2 - n_el // 2
+    for _ in range(args.warmup):
+        op.apply_range(u, e0, e0 + n_el, cores)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        for _stage in range(3):
+            op.apply_range(u, e0, e0 + n_el, cores)
+    sec = time.perf_counter() - t0
+    value = 3.0 * n_el * B * args.steps / sec
+    line = {
+        "metric": METRIC, "value": value, "unit": "DOF-stage updates/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": sec / args.steps * 1e3, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic: IC prod_d sin(2 pi x_d)",
+        "config": {"workload": WORKLOAD, "dim": DIM, "nmax": NMAX, "k": K, "elements": E, "dof": E * B},
+        "impl": "reference",
+        "cpu_baseline": {"value": value, "unit": "DOF-stage updates/s", "cores": cores, "kind": "port",
+                         "sample": f"3 RHS evaluations per step over {n_el} contiguous elements ({n_el * B} DOF)"},
+        "e2e": {"value": value, "unit": "DOF-stage updates/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    op.close()
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--cpu-seconds", type=float, default=15.0)
+    args = ap.parse_args()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,156 @@
+/*
+ * amdg.h -- C-ABI of the GB300-native adaptive sparse-grid DG right-hand-side
+ * library (libamdg_gb300.so).
+ *
+ * Plain C types only: opaque handles, pointers and sizes.  Every call returns
+ * an amdg_status; no C++ exception crosses this boundary.  The caller owns
+ * host buffers; the library owns device memory.  A context and the handles
+ * created from it are not thread-safe: use one host thread per context.
+ *
+ * Each entry point names the AdaM-DG reference interface it replaces
+ * (file:line in the reference tree).
+ *
+ * Data layout shared by every call:
+ *   - element e of a grid has a level and a support index per dimension
+ *     (Element::level / Element::suppt, Element.h:24-25); elements are kept
+ *     sorted by their per-dimension 1D element orders o_d = 0 for level 0,
+ *     2^(n-1) + (j-1)/2 otherwise (Element.cpp:386-389), first dimension most
+ *     significant;
+ *   - the coefficient block of an element holds (k+1)^dim doubles, row-major
+ *     over dimensions, last dimension fastest (VecMultiD.h:114-116), i.e. the
+ *     layout of Element::ucoe_alpt[0];
+ *   - a grid's coefficient vector is the concatenation of its element blocks
+ *     in element order (num_elements * (k+1)^dim doubles).
+ */
+#ifndef AMDG_H
+#define AMDG_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define AMDG_ABI_VERSION 1
+
+typedef enum amdg_status {
+    AMDG_OK = 0,
+    AMDG_ERR_ARG = 1,       /* invalid argument (bad size, null pointer, unsupported degree/dimension) */
+    AMDG_ERR_CAPACITY = 2,  /* a size exceeds what the handle was built for */
+    AMDG_ERR_NONFINITE = 3, /* a reduction met NaN or Inf */
+    AMDG_ERR_TIMEOUT = 4,   /* a bounded device-side wait gave up */
+    AMDG_ERR_CUDA = 5,      /* a CUDA runtime call failed (see amdg_last_error) */
+    AMDG_ERR_STATE = 6,     /* call out of order (e.g. state not initialised) */
+    AMDG_ERR_NOMEM = 7      /* device or host allocation failed */
+} amdg_status;
+
+/* Arithmetic of the operator applies.  The state and the RK stage
+ * accumulation stay FP64 in both modes. */
+typedef enum amdg_precision {
+    AMDG_PREC_FP64 = 0,  /* plain FP64 everywhere */
+    AMDG_PREC_MIXED = 1  /* operator blocks and products in FP32, FP32 accumulation */
+} amdg_precision;
+
+typedef struct amdg_context amdg_context;
+typedef struct amdg_grid amdg_grid;
+typedef struct amdg_linear_op amdg_linear_op;
+
+/* Separable 1D factor g_d(x) of term `term` (the std::function<double(double,int)>
+ * the reference takes, DGAdapt.h:17-38). */
+typedef double (*amdg_fn1d)(double x, int d, int term, void* user);
+
+/* ---- library / context ------------------------------------------------- */
+int amdg_abi_version(void);
+const char* amdg_status_string(amdg_status s);
+/* Message of the last failing call on this host thread ("" if none). */
+const char* amdg_last_error(void);
+
+/* Binds a CUDA device and creates the library's stream.  No reference
+ * counterpart: the reference is single-process CPU code. */
+amdg_status amdg_context_create(int device, amdg_context** out);
+amdg_status amdg_context_destroy(amdg_context* ctx);
+/* Run all later work of this context on an existing cudaStream_t (NULL = the
+ * context's own stream). */
+amdg_status amdg_context_set_stream(amdg_context* ctx, void* cuda_stream);
+amdg_status amdg_context_get_stream(amdg_context* ctx, void** cuda_stream);
+amdg_status amdg_context_synchronize(amdg_context* ctx);
+/* Number of kernels this context has launched so far. */
+amdg_status amdg_context_launch_count(amdg_context* ctx, int64_t* count);
+
+/* ---- host-side set-up (no device needed) -------------------------------- */
+/* OperatorMatrix1D<AlptBasis,AlptBasis>(all_bas, all_bas, "period")
+ * (OperatorMatrix1D.h:125-199): dense 1D matrices of the (2^nmax)(k+1) Alpert
+ * basis functions, row = solution basis, column = test basis, row-major.  Any
+ * output pointer may be NULL. */
+amdg_status amdg_oper1d_build(int nmax, int k, double* u_v, double* u_vx, double* ulft_vjp, double* urgt_vjp);
+/* Element multi-indices of the sparse or full grid in the library's element
+ * order (DGSolution.cpp:17-54).  Call with level == NULL to get the count. */
+amdg_status amdg_grid_enumerate(int dim, int nmax, int sparse, int64_t* num_elements, int32_t* level, int32_t* suppt);
+
+/* ---- grid (DGSolution / DGAdapt) --------------------------------------- */
+/* Sparse (sum of levels <= nmax) or full grid of Alpert degree k.
+ * Replaces DGSolution::DGSolution (DGSolution.cpp:10-57) and the
+ * DGAdapt constructor with find_ptr_alpt (DGAdapt.cpp:5-37,
+ * DGSolution.cpp:675-728).  dim 1..6, nmax*dim <= 60, k 1..3. */
+amdg_status amdg_grid_create(amdg_context* ctx, int dim, int nmax, int k, int sparse, amdg_grid** out);
+amdg_status amdg_grid_destroy(amdg_grid* g);
+/* DGSolution::size_elem / get_dof (DGSolution.cpp:836-849). */
+amdg_status amdg_grid_size(const amdg_grid* g, int64_t* num_elements, int64_t* dof);
+/* level and suppt of every element, num_elements x dim each (host buffers). */
+amdg_status amdg_grid_elements(const amdg_grid* g, int32_t* level, int32_t* suppt);
+/* DGSolution::max_mesh_level_vec (DGSolution.cpp:948-959): dim entries. */
+amdg_status amdg_grid_max_mesh_level(const amdg_grid* g, int32_t* levels);
+/* Element::ucoe_alpt of every element, host <-> device (n = dof doubles). */
+amdg_status amdg_grid_set_coefficients(amdg_grid* g, const double* host, int64_t n);
+amdg_status amdg_grid_get_coefficients(const amdg_grid* g, double* host, int64_t n);
+/* Device pointer of the grid's FP64 coefficient vector (valid until destroy). */
+amdg_status amdg_grid_coefficients_device(amdg_grid* g, double** device_ptr);
+/* DGAdapt::init_separable_scalar_sum / init_separable_scalar
+ * (DGAdapt.cpp:63-147; DGSolution.cpp:150-184): coefficients of
+ * sum_term prod_d f(x_d, d, term).  The 1D projections run on the host, the
+ * expansion into element blocks on the device.  Without adaptivity
+ * (refine threshold not reached), as in the reference drivers that pass
+ * refine_eps = 1e10. */
+amdg_status amdg_grid_init_separable(amdg_grid* g, int nterms, amdg_fn1d f, void* user);
+/* DGSolution::get_L2_norm (DGSolution.cpp:933-946): sum of squares of all
+ * coefficients (the reference returns the squared norm). */
+amdg_status amdg_grid_l2_norm(const amdg_grid* g, double* out);
+/* DGSolution::get_L2_error_split_separable_scalar (DGSolution.cpp:217-256). */
+amdg_status amdg_grid_l2_error_separable(const amdg_grid* g, amdg_fn1d f, void* user, double l2_norm_exact,
+                                         double* out);
+
+/* ---- linear constant-coefficient operator (HyperbolicAlpt) -------------- */
+/* HyperbolicAlpt::assemble_matrix_scalar (BilinearForm.cpp:691-710): volume
+ * term c_d * u_vx plus upwind flux c_d * ulft_vjp (c_d >= 0) or c_d * urgt_vjp
+ * (c_d < 0) in each dimension, entries below 1e-13 dropped as in
+ * BilinearFormAlpt::assemble_matrix_alpt (BilinearForm.cpp:25-87).  Matrix
+ * free: the 1D blocks and the per-(element, dimension) neighbour lists live on
+ * the device.  coef has dim entries. */
+amdg_status amdg_linear_create(amdg_grid* g, const double* coef, amdg_linear_op** out);
+amdg_status amdg_linear_destroy(amdg_linear_op* op);
+/* Number of nonzero (element, neighbour, dimension) block pairs and the
+ * algorithmic flops of one apply (2 * (k+1)^(dim+1) per pair). */
+amdg_status amdg_linear_stats(const amdg_linear_op* op, int64_t* pairs, double* flops_per_apply);
+/* BilinearForm::multi (BilinearForm.h:23): d_rhs = L d_u, device pointers of
+ * dof doubles each. */
+amdg_status amdg_linear_apply(amdg_linear_op* op, const double* d_u, double* d_rhs, amdg_precision prec);
+/* RK3SSP::step_rk (ODESolver.cpp:261-271), nsteps steps of size dt on the
+ * grid's device state; stage updates fused into the operator kernel. */
+amdg_status amdg_rk3ssp_steps(amdg_linear_op* op, double dt, int nsteps, amdg_precision prec);
+/* Same, through host memory: uploads host_u (dof doubles), steps, and writes
+ * the result back into host_u.  The call a host-side driver makes per step
+ * when it keeps Element::ucoe_alpt on the host (ODESolver::init/final,
+ * ODESolver.cpp:25-60). */
+amdg_status amdg_rk3ssp_steps_host(amdg_linear_op* op, double dt, int nsteps, double* host_u, amdg_precision prec);
+
+/* ---- stage updates for an externally computed right-hand side ----------- */
+/* RK3SSP::step_stage / ForwardEuler::step_stage (ODESolver.cpp:209-213,
+ * 285-301) on device vectors of n doubles: stage 0 u = un + dt*rhs,
+ * stage 1 u = 3/4 un + 1/4 (u + dt*rhs), stage 2 u = 1/3 un + 2/3 (u + dt*rhs). */
+amdg_status amdg_rk3_stage_update(amdg_context* ctx, int stage, double dt, const double* d_un, double* d_u,
+                                  const double* d_rhs, int64_t n);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* AMDG_H */

@@ -61,6 +61,12 @@ int amdg_oracle_linear_rhs_range(int dim, int N, int k, int64_t E, const int32_t
                                  const double* c, const double* u, double* rhs, int64_t e_begin, int64_t e_end,
                                  int nthreads);
 
+/* Operator handle for repeated evaluations (level/suppt must outlive it). */
+void* amdg_oracle_linop_create(int dim, int N, int k, int64_t E, const int32_t* level, const int32_t* suppt,
+                               const double* c);
+int amdg_oracle_linop_apply_range(void* handle, const double* u, double* rhs, int64_t e_begin, int64_t e_end, int nthreads);
+void amdg_oracle_linop_destroy(void* handle);
+
 /* L2 error against a separable exact solution (DGSolution::get_L2_error_split_separable_scalar). */
 double amdg_oracle_l2_error_split(int dim, int N, int k, int64_t E, const int32_t* level, const int32_t* suppt,
                                   const double* u, const double* coef1d_exact, double l2_norm_exact);

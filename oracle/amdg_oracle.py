@@ -49,6 +49,10 @@ def lib():
                                                    C.c_int64, C.c_int64, C.c_int]
         L.amdg_oracle_linear_rk3.argtypes = [C.c_int, C.c_int, C.c_int, C.c_int64, i32p, i32p, f64p, C.c_double, C.c_int,
                                              f64p, C.c_int]
+        L.amdg_oracle_linop_create.restype = C.c_void_p
+        L.amdg_oracle_linop_create.argtypes = [C.c_int, C.c_int, C.c_int, C.c_int64, i32p, i32p, f64p]
+        L.amdg_oracle_linop_apply_range.argtypes = [C.c_void_p, f64p, f64p, C.c_int64, C.c_int64, C.c_int]
+        L.amdg_oracle_linop_destroy.argtypes = [C.c_void_p]
         L.amdg_oracle_l2_error_split.restype = C.c_double
         L.amdg_oracle_l2_error_split.argtypes = [C.c_int, C.c_int, C.c_int, C.c_int64, i32p, i32p, f64p, f64p, C.c_double]
         _lib = L
@@ -120,6 +124,32 @@ def linear_rhs_range(dim, N, k, level, suppt, c, u, e0, e1, nthreads=0):
     _check(lib().amdg_oracle_linear_rhs_range(dim, N, k, level.shape[0], level, suppt, np.asarray(c, np.float64),
                                               np.ascontiguousarray(u), rhs, e0, e1, nthreads))
     return rhs
+
+
+class LinearOp:
+    """Prebuilt oracle operator: apply_range() times only the RHS evaluation."""
+
+    def __init__(self, dim, N, k, level, suppt, c):
+        self.level = np.ascontiguousarray(level, np.int32)
+        self.suppt = np.ascontiguousarray(suppt, np.int32)
+        self.B = (k + 1) ** dim
+        self.h = lib().amdg_oracle_linop_create(dim, N, k, self.level.shape[0], self.level, self.suppt,
+                                                np.asarray(c, np.float64))
+        if not self.h:
+            raise RuntimeError("oracle operator build failed")
+
+    def apply_range(self, u, e0, e1, nthreads=0, out=None):
+        rhs = out if out is not None else np.zeros((e1 - e0, self.B))
+        _check(lib().amdg_oracle_linop_apply_range(self.h, np.ascontiguousarray(u), rhs, e0, e1, nthreads))
+        return rhs
+
+    def close(self):
+        if self.h:
+            lib().amdg_oracle_linop_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        self.close()
 
 
 def linear_rk3(dim, N, k, level, suppt, c, u, dt, steps, nthreads=0):

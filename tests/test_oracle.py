@@ -1,0 +1,100 @@
+"""The CPU oracle against the reference library's own outputs (golden
+fixtures from oracle/ref_harness, see tests/golden/make_golden.py) and the
+reference's known-answer unit tests for the path's ingredients."""
+import math
+
+import numpy as np
+import pytest
+
+import amdg_oracle as O
+from helpers import align, golden, ic_terms, manifest, rel_err
+
+LINEAR = [n for n, m in manifest().items() if m["kind"] == "linear"]
+OPER = [n for n, m in manifest().items() if m["kind"] == "oper1d"]
+
+
+@pytest.mark.parametrize("name", OPER)
+def test_oper1d_matches_reference(name):
+    m = manifest()[name]
+    z = golden(name)
+    mats = O.oper1d(m["N"], m["k"])
+    for key in ("u_v", "u_vx", "ulft_vjp", "urgt_vjp"):
+        scale = max(1.0, np.abs(z[key]).max())
+        assert np.abs(mats[key] - z[key]).max() <= 1e-13 * scale * 10, key
+
+
+@pytest.mark.parametrize("name", LINEAR)
+def test_linear_matches_reference(name):
+    m = manifest()[name]
+    z = golden(name)
+    dim, N, k = m["dim"], m["N"], m["k"]
+    lv, sp = O.grid(dim, N)
+    assert lv.shape[0] == m["elements"] == z["level"].shape[0]
+    perm = align(z["level"], z["suppt"], lv, sp)
+    coef = O.project_separable(N, k, dim, ic_terms(m["ic"], dim))
+    u0 = O.init_separable(dim, N, k, lv, sp, coef)
+    assert rel_err(u0, z["u0"][perm]) < 1e-13
+    rhs = O.linear_rhs(dim, N, k, lv, sp, m["c"], z["u0"][perm])
+    assert rel_err(rhs, z["rhs0"][perm]) < 1e-12
+    uT = O.linear_rk3(dim, N, k, lv, sp, m["c"], z["u0"][perm], m["dt"], m["steps"])
+    assert rel_err(uT, z["uT"][perm]) < 1e-12
+
+
+def test_l2_error_matches_reference():
+    name = "lin3d_n4_sinprod"
+    m = manifest()[name]
+    z = golden(name)
+    dim, N, k = m["dim"], m["N"], m["k"]
+    T = m["steps"] * m["dt"]
+    lv, sp = z["level"], z["suppt"]
+    exact = O.project_separable(N, k, dim, [lambda x, d: math.sin(2 * math.pi * (x - m["c"][d] * T))])[0]
+    err = O.l2_error_split(dim, N, k, lv, sp, z["uT"], exact, 0.5 ** (0.5 * dim))
+    assert abs(err - float(z["l2err"])) <= 1e-10 * max(err, 1e-30) + 1e-15
+
+
+def test_alpert_orthonormal():
+    # test/test_AlptBasis.cpp:8-36: Alpert basis orthonormal on [0,1] (PMAX=2, tol 1e-14)
+    mats = O.oper1d(4, 2)
+    assert np.abs(mats["u_v"] - np.eye(mats["u_v"].shape[0])).max() < 1e-13
+
+
+@pytest.mark.parametrize("n", [1, 2, 3, 5, 10])
+def test_gauss_legendre_exactness(n):
+    # test/test_Quad.cpp:13-38: n-point rule integrates x^m exactly for m <= 2n-1
+    x, w = O.gauss_legendre(n)
+    for m in range(2 * n):
+        exact = (1 - (-1) ** (m + 1)) / (m + 1)
+        assert abs(np.dot(w, x ** m) - exact) < 5e-15 * 10
+
+
+@pytest.mark.parametrize("dim,N,E", [(2, 7, 576), (3, 8, 4096), (4, 8, 10496), (6, 8, 47264), (2, 3, 20)])
+def test_sparse_grid_counts(dim, N, E):
+    assert O.lib().amdg_oracle_grid_count(dim, N, 1) == E
+
+
+def test_full_grid_count():
+    assert O.lib().amdg_oracle_grid_count(2, 3, 0) == 64
+
+
+def test_linear_operator_is_linear():
+    dim, N, k = 3, 3, 2
+    lv, sp = O.grid(dim, N)
+    rng = np.random.default_rng(0)
+    a = rng.standard_normal((lv.shape[0], 27))
+    b = rng.standard_normal((lv.shape[0], 27))
+    c = [1.0, -0.5, 0.25]
+    la = O.linear_rhs(dim, N, k, lv, sp, c, a)
+    lb = O.linear_rhs(dim, N, k, lv, sp, c, b)
+    lab = O.linear_rhs(dim, N, k, lv, sp, c, 2.0 * a - 3.0 * b)
+    assert np.abs(lab - (2.0 * la - 3.0 * lb)).max() < 1e-10 * np.abs(lab).max()
+
+
+def test_constant_mode_is_conserved():
+    # the level-0 constant mode carries the mean, which the periodic advection operator conserves
+    dim, N, k = 2, 4, 2
+    lv, sp = O.grid(dim, N)
+    rng = np.random.default_rng(1)
+    u = rng.standard_normal((lv.shape[0], 9))
+    rhs = O.linear_rhs(dim, N, k, lv, sp, [1.0, 1.0], u)
+    root = np.where((lv == 0).all(axis=1))[0][0]
+    assert abs(rhs[root, 0]) < 1e-10
