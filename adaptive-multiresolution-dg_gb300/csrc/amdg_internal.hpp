@@ -57,6 +57,25 @@ void build_oper1d(const Basis1D& b, Oper1D* out, bool want_u_v);
 // 1D projection of f(., d, term) onto every basis function (Basis::product_function).
 void project_1d(const Basis1D& b, amdg_fn1d f, void* user, int d, int term, double* out);
 
+// ---- Lagrange interpolation path (degree-3 hierarchical Lagrange) ---------
+struct LagrTables {
+    int n_lagr = 0, n_alpt = 0;
+    std::vector<double> a2p;    // [n_alpt][n_lagr]: Alpert basis at Lagrange points
+    std::vector<double> lv;     // [n_lagr][n_alpt]: u_v   (Lagrange x Alpert)
+    std::vector<double> lvx;    // [n_lagr][n_alpt]: u_vx
+    std::vector<double> lflx;   // [n_lagr][n_alpt]: ulft_vjp + urgt_vjp
+    std::vector<double> ajump;  // [n_alpt][n_alpt]: ujp_vjp (Alpert x Alpert)
+    std::vector<int32_t> anc_order;  // [n_elem1d][4]: 1D order of the ancestor owning surplus point ic
+    std::vector<int32_t> anc_point;  // [n_elem1d][4]: its point index
+    std::vector<int32_t> anc_rank;   // [n_elem1d][4]: rank of its position among the four
+    double weight[16] = {0};         // [p0][rank]
+};
+double lagr_eval(int order, double x, int sgn);
+double lagr_point(int o, int p);
+void build_lagr_tables(const Basis1D& alpt, LagrTables* t);
+// dimension orders and L(0)/full(1)/U(2) tags of the 2^(dim-1) partial sums
+void transform_schedule(int dim, std::vector<std::vector<int>>* dim_order, std::vector<std::vector<int>>* lu);
+
 // ---- grid topology (host build, device copy) -------------------------------
 struct HostGrid {
     int dim = 0, nmax = 0, k = 0, sparse = 1;
@@ -78,6 +97,18 @@ struct LinearTopology {
 };
 void build_linear_topology(const HostGrid& g, const Oper1D& op, const double* coef, LinearTopology* out);
 
+// Per-(element, dimension) neighbour lists of the fast transforms:
+// vol = supports intersect in the dimension, flx = intersect or adjacent
+// (periodic), identical indices elsewhere (Element.cpp:265-299).  Each entry
+// carries the neighbour's level in that dimension for the L/U filters.
+struct TransformTopology {
+    std::vector<int32_t> vol_ptr, vol_src, vol_lev;  // ptr: num_elements*dim + 1
+    std::vector<int32_t> flx_ptr, flx_src, flx_lev;
+};
+void build_transform_topology(const HostGrid& g, TransformTopology* out);
+// surplus ancestors: [e][d][ic] element index (-1 for level 0 in d); false if a hole is found
+bool build_surplus_ancestors(const HostGrid& g, const LagrTables& t, std::vector<int32_t>* anc);
+
 }  // namespace amdg
 
 // ---- opaque handle layouts (plain structs, owned by the C-ABI layer) ------
@@ -90,6 +121,7 @@ struct amdg_context {
 
 struct amdg_grid {
     amdg_context* ctx = nullptr;
+    int device = 0;                  // kept so destroy never dereferences ctx
     amdg::HostGrid host;
     int block = 0;                   // (k+1)^dim
     int64_t dof = 0;
@@ -101,6 +133,7 @@ struct amdg_grid {
 
 struct amdg_linear_op {
     amdg_grid* grid = nullptr;
+    int device = 0;                  // kept so destroy never dereferences grid
     std::vector<double> coef;
     int64_t pairs = 0;
     int num_blocks = 0;              // 1D blocks per dimension in the table
@@ -112,4 +145,24 @@ struct amdg_linear_op {
     float* d_blocks32 = nullptr;
     double* d_u1 = nullptr;          // RK stage vectors
     double* d_u2 = nullptr;
+};
+
+struct amdg_burgers_op {
+    amdg_grid* grid = nullptr;
+    int device = 0;
+    std::vector<double> alpha;
+    int points = 0;                  // 4^dim interpolation points per element
+    int n1 = 0;                      // 1D elements
+    // 1D matrices, FP64 and FP32 copies
+    double *d_a2p = nullptr, *d_lv = nullptr, *d_lvx = nullptr, *d_lflx = nullptr, *d_ajump = nullptr;
+    float *f_a2p = nullptr, *f_lv = nullptr, *f_lvx = nullptr, *f_lflx = nullptr, *f_ajump = nullptr;
+    // neighbour lists of the fast transforms and the surplus ancestors
+    int32_t *d_vol_ptr = nullptr, *d_vol_src = nullptr, *d_vol_lev = nullptr;
+    int32_t *d_flx_ptr = nullptr, *d_flx_src = nullptr, *d_flx_lev = nullptr;
+    int32_t *d_anc = nullptr, *d_anc_point = nullptr, *d_anc_rank = nullptr;
+    double weight[16] = {0};
+    std::vector<std::vector<int>> sched_dims, sched_lu;
+    // work buffers sized for FP64 (E x 4^dim doubles each)
+    void *w_up = nullptr, *w_fu = nullptr, *w_a = nullptr, *w_b = nullptr, *w_rhs = nullptr, *w_u = nullptr;
+    double *d_u1 = nullptr, *d_u2 = nullptr, *d_rhs64 = nullptr;
 };

@@ -29,11 +29,11 @@ amdg_status fail(amdg_status s, const std::string& msg) {
 
 using namespace amdg;
 
-#define AMDG_CK(call)                                                                                   \
+#define AMDG_CK(...)                                                                                   \
     do {                                                                                                \
-        cudaError_t amdg_err_ = (call);                                                                 \
+        cudaError_t amdg_err_ = (__VA_ARGS__);                                                                 \
         if (amdg_err_ != cudaSuccess)                                                                   \
-            return fail(AMDG_ERR_CUDA, std::string(#call) + ": " + cudaGetErrorString(amdg_err_));      \
+            return fail(AMDG_ERR_CUDA, std::string(#__VA_ARGS__) + ": " + cudaGetErrorString(amdg_err_));      \
     } while (0)
 
 #define AMDG_REQUIRE(cond, code, msg) \
@@ -254,6 +254,7 @@ amdg_status amdg_grid_create(amdg_context* ctx, int dim, int nmax, int k, int sp
     amdg_grid* g = new (std::nothrow) amdg_grid;
     AMDG_REQUIRE(g, AMDG_ERR_NOMEM, "host allocation failed");
     g->ctx = ctx;
+    g->device = ctx->device;
     g->host.k = k;
     build_grid(dim, nmax, sparse, &g->host);
     g->block = ipow(k + 1, dim);
@@ -282,8 +283,8 @@ amdg_status amdg_grid_create(amdg_context* ctx, int dim, int nmax, int k, int sp
 
 amdg_status amdg_grid_destroy(amdg_grid* g) {
     if (!g) return AMDG_OK;
-    cudaSetDevice(g->ctx->device);
-    cudaStreamSynchronize(stream_of(g->ctx));
+    // cudaFree synchronises with the device; the context may already be gone
+    cudaSetDevice(g->device);
     cudaFree(g->d_order);
     cudaFree(g->d_u);
     cudaFree(g->d_scratch);
@@ -424,6 +425,7 @@ amdg_status amdg_linear_create(amdg_grid* g, const double* coef, amdg_linear_op*
     amdg_linear_op* op = new (std::nothrow) amdg_linear_op;
     AMDG_REQUIRE(op, AMDG_ERR_NOMEM, "host allocation failed");
     op->grid = g;
+    op->device = g->device;
     op->coef.assign(coef, coef + dim);
     op->pairs = int64_t(topo.src.size());
     op->num_blocks = topo.num_blocks;
@@ -447,8 +449,7 @@ amdg_status amdg_linear_create(amdg_grid* g, const double* coef, amdg_linear_op*
 
 amdg_status amdg_linear_destroy(amdg_linear_op* op) {
     if (!op) return AMDG_OK;
-    cudaSetDevice(op->grid->ctx->device);
-    cudaStreamSynchronize(stream_of(op->grid->ctx));
+    cudaSetDevice(op->device);
     cudaFree(op->d_row_ptr);
     cudaFree(op->d_src);
     cudaFree(op->d_blk);

@@ -1,0 +1,386 @@
+// C-ABI of the Lagrange-interpolation path (Burgers flux): set-up of the 1D
+// tables and neighbour lists, and the launch sequence of one right-hand-side
+// evaluation -- point values by 2^(dim-1) partial sums of dim 1D transforms,
+// flux at the points, dim hierarchical-surplus passes, volume and interface
+// terms by the same partial sums back to Alpert coefficients, LxF penalty,
+// and the SSP-RK3 stage update.
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <cstring>
+#include <new>
+#include <string>
+#include <vector>
+
+#include "amdg.h"
+#include "amdg_internal.hpp"
+#include "kernels.cuh"
+#include "kernels_lagr.cuh"
+
+using namespace amdg;
+
+#define AMDG_CK(...)                                                                              \
+    do {                                                                                           \
+        cudaError_t amdg_err_ = (__VA_ARGS__);                                                            \
+        if (amdg_err_ != cudaSuccess)                                                              \
+            return fail(AMDG_ERR_CUDA, std::string(#__VA_ARGS__) + ": " + cudaGetErrorString(amdg_err_)); \
+    } while (0)
+
+#define AMDG_REQUIRE(cond, code, msg)        \
+    do {                                     \
+        if (!(cond)) return fail(code, msg); \
+    } while (0)
+
+namespace {
+
+template <class T>
+amdg_status upload_vec(T** p, const std::vector<T>& host) {
+    *p = nullptr;
+    if (host.empty()) return AMDG_OK;
+    cudaError_t e = cudaMalloc(reinterpret_cast<void**>(p), host.size() * sizeof(T));
+    if (e != cudaSuccess) return fail(AMDG_ERR_NOMEM, std::string("cudaMalloc: ") + cudaGetErrorString(e));
+    AMDG_CK(cudaMemcpy(*p, host.data(), host.size() * sizeof(T), cudaMemcpyHostToDevice));
+    return AMDG_OK;
+}
+
+amdg_status upload_both(double** d, float** f, const std::vector<double>& host) {
+    amdg_status s = upload_vec(d, host);
+    if (s != AMDG_OK) return s;
+    std::vector<float> h32(host.begin(), host.end());
+    return upload_vec(f, h32);
+}
+
+amdg_status alloc_bytes(void** p, size_t bytes) {
+    *p = nullptr;
+    if (bytes == 0) return AMDG_OK;
+    cudaError_t e = cudaMalloc(p, bytes);
+    if (e != cudaSuccess) return fail(AMDG_ERR_NOMEM, std::string("cudaMalloc: ") + cudaGetErrorString(e));
+    return AMDG_OK;
+}
+
+cudaStream_t stream_of(const amdg_burgers_op* op) { return static_cast<cudaStream_t>(op->grid->ctx->stream); }
+
+template <typename T>
+struct Mats {
+    const T *a2p, *lv, *lvx, *lflx, *ajump;
+};
+
+Mats<double> mats64(const amdg_burgers_op* op) { return {op->d_a2p, op->d_lv, op->d_lvx, op->d_lflx, op->d_ajump}; }
+Mats<float> mats32(const amdg_burgers_op* op) { return {op->f_a2p, op->f_lv, op->f_lvx, op->f_lflx, op->f_ajump}; }
+
+int prod(const int* s, int n) {
+    int p = 1;
+    for (int i = 0; i < n; ++i) p *= s[i];
+    return p;
+}
+
+template <typename T>
+TransformArgs<T> base_args(const amdg_burgers_op* op, int t, const int* from, const int* to, bool flx) {
+    const amdg_grid* g = op->grid;
+    const int dim = g->host.dim;
+    TransformArgs<T> a{};
+    a.dim = dim;
+    a.t = t;
+    a.n_from = from[t];
+    a.n_to = to[t];
+    a.stride = prod(from + t + 1, dim - t - 1);
+    a.in_block = prod(from, dim);
+    a.out_block = prod(to, dim);
+    a.num_elements = g->host.num_elements;
+    a.order = g->d_order;
+    a.ptr = flx ? op->d_flx_ptr : op->d_vol_ptr;
+    a.src = flx ? op->d_flx_src : op->d_vol_src;
+    a.lev = flx ? op->d_flx_lev : op->d_vol_lev;
+    return a;
+}
+
+// One partial sum: dim successive 1D transforms, the first scaled by coef, the
+// last accumulated into out (FastRHS::transform_multiD_partial_sum,
+// FastInterpolation::transform_multiD_partial_sum).
+template <typename T>
+amdg_status partial_sum(amdg_burgers_op* op, const std::vector<int>& dims, const std::vector<int>& lu, int n_in, int n_out,
+                        const T* const* mat, const bool* flx, T coef, const T* in, T* out, T* tmp_a, T* tmp_b,
+                        cudaStream_t st) {
+    const int dim = op->grid->host.dim;
+    int from[kMaxDim], to[kMaxDim];
+    for (int d = 0; d < dim; ++d) from[d] = n_in;
+    const T* cur = in;
+    for (int i = 0; i < dim; ++i) {
+        const int t = dims[i];
+        std::memcpy(to, from, sizeof(int) * dim);
+        to[t] = n_out;
+        TransformArgs<T> a = base_args<T>(op, t, from, to, flx[t]);
+        a.M = mat[t];
+        a.ncols = op->n1 * n_out;
+        a.lu = lu[i];
+        a.coef = (i == 0) ? coef : T(1);
+        a.in = cur;
+        const bool last = (i == dim - 1);
+        T* dst = last ? out : ((cur == tmp_a) ? tmp_b : tmp_a);
+        a.out = dst;
+        a.accumulate = last ? 1 : 0;
+        AMDG_CK(launch_fibre_transform<T>(a, st));
+        op->grid->ctx->launches++;
+        cur = dst;
+        std::memcpy(from, to, sizeof(int) * dim);
+    }
+    return AMDG_OK;
+}
+
+template <typename T>
+amdg_status eval_point_values(amdg_burgers_op* op, const Mats<T>& m, const T* u, T* up, cudaStream_t st) {
+    const amdg_grid* g = op->grid;
+    const int dim = g->host.dim, np = g->host.k + 1;
+    AMDG_CK(cudaMemsetAsync(up, 0, size_t(g->host.num_elements) * op->points * sizeof(T), st));
+    const T* mats[kMaxDim];
+    bool flx[kMaxDim];
+    for (int d = 0; d < dim; ++d) { mats[d] = m.a2p; flx[d] = false; }
+    T* ta = static_cast<T*>(op->w_a);
+    T* tb = static_cast<T*>(op->w_b);
+    for (size_t s = 0; s < op->sched_dims.size(); ++s) {
+        amdg_status r = partial_sum<T>(op, op->sched_dims[s], op->sched_lu[s], np, 4, mats, flx, T(1), u, up, ta, tb, st);
+        if (r != AMDG_OK) return r;
+    }
+    return AMDG_OK;
+}
+
+// flux interpolation coefficients: f(u) at the points, then dim surplus passes (result in op->w_fu)
+template <typename T>
+amdg_status eval_flux_coefficients(amdg_burgers_op* op, const T* up, cudaStream_t st) {
+    const amdg_grid* g = op->grid;
+    const int dim = g->host.dim;
+    const int64_t n = g->host.num_elements * op->points;
+    T* ta = static_cast<T*>(op->w_a);
+    T* tb = static_cast<T*>(op->w_b);
+    T* fu = static_cast<T*>(op->w_fu);
+    AMDG_CK(launch_burgers_flux<T>(up, ta, n, st));
+    op->grid->ctx->launches++;
+    const T* cur = ta;
+    for (int d = 0; d < dim; ++d) {
+        SurplusArgs<T> a{};
+        a.dim = dim;
+        a.d = d;
+        a.points = op->points;
+        a.stride = 1;
+        for (int s = d + 1; s < dim; ++s) a.stride *= 4;
+        a.num_elements = g->host.num_elements;
+        a.order = g->d_order;
+        a.anc = op->d_anc;
+        a.anc_point = op->d_anc_point;
+        a.anc_rank = op->d_anc_rank;
+        for (int i = 0; i < 16; ++i) a.weight[i] = T(op->weight[i]);
+        T* dst = (d == dim - 1) ? fu : ((cur == tb) ? ta : tb);
+        a.in = cur;
+        a.out = dst;
+        AMDG_CK(launch_surplus_pass<T>(a, st));
+        op->grid->ctx->launches++;
+        cur = dst;
+    }
+    return AMDG_OK;
+}
+
+template <typename T>
+amdg_status eval_rhs_t(amdg_burgers_op* op, const Mats<T>& m, const T* u, T* rhs, cudaStream_t st) {
+    const amdg_grid* g = op->grid;
+    const int dim = g->host.dim, np = g->host.k + 1;
+    T* up = static_cast<T*>(op->w_up);
+    amdg_status r = eval_point_values<T>(op, m, u, up, st);
+    if (r != AMDG_OK) return r;
+    if ((r = eval_flux_coefficients<T>(op, up, st)) != AMDG_OK) return r;
+    const T* fu = static_cast<const T*>(op->w_fu);
+    T* ta = static_cast<T*>(op->w_a);
+    T* tb = static_cast<T*>(op->w_b);
+    AMDG_CK(cudaMemsetAsync(rhs, 0, size_t(g->dof) * sizeof(T), st));
+    for (int d = 0; d < dim; ++d) {
+        for (int term = 0; term < 2; ++term) {
+            // term 0: volume (u_vx in d, u_v elsewhere, vol sets);
+            // term 1: interface (ulft+urgt)_vjp in d on flx sets, coefficient 0.5
+            const T* mats[kMaxDim];
+            bool flx[kMaxDim];
+            for (int t = 0; t < dim; ++t) {
+                mats[t] = (t == d) ? (term == 0 ? m.lvx : m.lflx) : m.lv;
+                flx[t] = (term == 1 && t == d);
+            }
+            const T coef = term == 0 ? T(1) : T(0.5);
+            for (size_t s = 0; s < op->sched_dims.size(); ++s) {
+                r = partial_sum<T>(op, op->sched_dims[s], op->sched_lu[s], 4, np, mats, flx, coef, fu, rhs, ta, tb, st);
+                if (r != AMDG_OK) return r;
+            }
+        }
+        // LxF penalty -alpha_d/2 ujp_vjp in dimension d (FastRHS::transform_ucoe_alpt_to_rhs, FastMultiplyLU.cpp:46-59)
+        int from[kMaxDim];
+        for (int t = 0; t < dim; ++t) from[t] = np;
+        TransformArgs<T> a = base_args<T>(op, d, from, from, true);
+        a.M = m.ajump;
+        a.ncols = op->n1 * np;
+        a.lu = 1;
+        a.coef = T(-op->alpha[d] / 2.0);
+        a.in = u;
+        a.out = rhs;
+        a.accumulate = 1;
+        AMDG_CK(launch_fibre_transform<T>(a, st));
+        op->grid->ctx->launches++;
+    }
+    return AMDG_OK;
+}
+
+// rhs (FP64, dof entries) of the FP64 state u
+amdg_status eval_rhs(amdg_burgers_op* op, const double* u, double* rhs, amdg_precision prec) {
+    cudaStream_t st = stream_of(op);
+    const int64_t n = op->grid->dof;
+    if (prec == AMDG_PREC_FP64) return eval_rhs_t<double>(op, mats64(op), u, rhs, st);
+    float* u32 = static_cast<float*>(op->w_u);
+    float* r32 = static_cast<float*>(op->w_rhs);
+    AMDG_CK(launch_convert<double, float>(u, u32, n, st));
+    op->grid->ctx->launches++;
+    amdg_status r = eval_rhs_t<float>(op, mats32(op), u32, r32, st);
+    if (r != AMDG_OK) return r;
+    AMDG_CK(launch_convert<float, double>(r32, rhs, n, st));
+    op->grid->ctx->launches++;
+    return AMDG_OK;
+}
+
+StageCoef stage_coef(int stage, double dt) {
+    switch (stage) {
+        case 0: return StageCoef{1, 0.0, 1.0, dt};
+        case 1: return StageCoef{1, 3. / 4., 1. / 4., dt};
+        default: return StageCoef{1, 1. / 3., 2. / 3., dt};
+    }
+}
+
+}  // namespace
+
+extern "C" {
+
+amdg_status amdg_burgers_create(amdg_grid* g, const double* alpha, amdg_burgers_op** out) {
+    AMDG_REQUIRE(g && alpha && out, AMDG_ERR_ARG, "null argument");
+    *out = nullptr;
+    AMDG_REQUIRE(g->host.k == 2, AMDG_ERR_ARG, "the Lagrange path is built for Alpert degree k = 2");
+    AMDG_CK(cudaSetDevice(g->device));
+    const int dim = g->host.dim;
+    for (int d = 0; d < dim; ++d) AMDG_REQUIRE(std::isfinite(alpha[d]), AMDG_ERR_ARG, "non-finite alpha");
+    amdg_burgers_op* op = new (std::nothrow) amdg_burgers_op;
+    AMDG_REQUIRE(op, AMDG_ERR_NOMEM, "host allocation failed");
+    op->grid = g;
+    op->device = g->device;
+    op->alpha.assign(alpha, alpha + dim);
+    op->points = 1;
+    for (int d = 0; d < dim; ++d) op->points *= 4;
+    op->n1 = 1 << g->host.nmax;
+    Basis1D b{g->host.k, g->host.nmax};
+    LagrTables t;
+    build_lagr_tables(b, &t);
+    std::memcpy(op->weight, t.weight, sizeof(op->weight));
+    TransformTopology topo;
+    build_transform_topology(g->host, &topo);
+    std::vector<int32_t> anc;
+    if (!build_surplus_ancestors(g->host, t, &anc)) {
+        delete op;
+        return fail(AMDG_ERR_STATE, "element set has a hole: a surplus ancestor is missing");
+    }
+    transform_schedule(dim, &op->sched_dims, &op->sched_lu);
+    const size_t work = size_t(g->host.num_elements) * op->points * sizeof(double);
+    amdg_status s;
+    if ((s = upload_both(&op->d_a2p, &op->f_a2p, t.a2p)) != AMDG_OK || (s = upload_both(&op->d_lv, &op->f_lv, t.lv)) != AMDG_OK ||
+        (s = upload_both(&op->d_lvx, &op->f_lvx, t.lvx)) != AMDG_OK ||
+        (s = upload_both(&op->d_lflx, &op->f_lflx, t.lflx)) != AMDG_OK ||
+        (s = upload_both(&op->d_ajump, &op->f_ajump, t.ajump)) != AMDG_OK ||
+        (s = upload_vec(&op->d_vol_ptr, topo.vol_ptr)) != AMDG_OK || (s = upload_vec(&op->d_vol_src, topo.vol_src)) != AMDG_OK ||
+        (s = upload_vec(&op->d_vol_lev, topo.vol_lev)) != AMDG_OK || (s = upload_vec(&op->d_flx_ptr, topo.flx_ptr)) != AMDG_OK ||
+        (s = upload_vec(&op->d_flx_src, topo.flx_src)) != AMDG_OK || (s = upload_vec(&op->d_flx_lev, topo.flx_lev)) != AMDG_OK ||
+        (s = upload_vec(&op->d_anc, anc)) != AMDG_OK || (s = upload_vec(&op->d_anc_point, t.anc_point)) != AMDG_OK ||
+        (s = upload_vec(&op->d_anc_rank, t.anc_rank)) != AMDG_OK || (s = alloc_bytes(&op->w_up, work)) != AMDG_OK ||
+        (s = alloc_bytes(&op->w_fu, work)) != AMDG_OK || (s = alloc_bytes(&op->w_a, work)) != AMDG_OK ||
+        (s = alloc_bytes(&op->w_b, work)) != AMDG_OK ||
+        (s = alloc_bytes(&op->w_rhs, size_t(g->dof) * sizeof(double))) != AMDG_OK ||
+        (s = alloc_bytes(&op->w_u, size_t(g->dof) * sizeof(double))) != AMDG_OK ||
+        (s = alloc_bytes(reinterpret_cast<void**>(&op->d_u1), size_t(g->dof) * sizeof(double))) != AMDG_OK ||
+        (s = alloc_bytes(reinterpret_cast<void**>(&op->d_rhs64), size_t(g->dof) * sizeof(double))) != AMDG_OK) {
+        amdg_burgers_destroy(op);
+        return s;
+    }
+    *out = op;
+    return AMDG_OK;
+}
+
+amdg_status amdg_burgers_destroy(amdg_burgers_op* op) {
+    if (!op) return AMDG_OK;
+    cudaSetDevice(op->device);
+    void* ptrs[] = {op->d_a2p, op->d_lv, op->d_lvx, op->d_lflx, op->d_ajump, op->f_a2p, op->f_lv, op->f_lvx, op->f_lflx,
+                    op->f_ajump, op->d_vol_ptr, op->d_vol_src, op->d_vol_lev, op->d_flx_ptr, op->d_flx_src, op->d_flx_lev,
+                    op->d_anc, op->d_anc_point, op->d_anc_rank, op->w_up, op->w_fu, op->w_a, op->w_b, op->w_rhs, op->w_u,
+                    op->d_u1, op->d_u2, op->d_rhs64};
+    for (void* p : ptrs) cudaFree(p);
+    delete op;
+    return AMDG_OK;
+}
+
+amdg_status amdg_burgers_rhs(amdg_burgers_op* op, const double* d_u, double* d_rhs, amdg_precision prec) {
+    AMDG_REQUIRE(op && d_u && d_rhs && d_u != d_rhs, AMDG_ERR_ARG, "bad arguments");
+    AMDG_REQUIRE(prec == AMDG_PREC_FP64 || prec == AMDG_PREC_MIXED, AMDG_ERR_ARG, "bad precision");
+    AMDG_CK(cudaSetDevice(op->device));
+    return eval_rhs(op, d_u, d_rhs, prec);
+}
+
+amdg_status amdg_burgers_point_values(amdg_burgers_op* op, const double* d_u, double* d_up, amdg_precision prec) {
+    AMDG_REQUIRE(op && d_u && d_up, AMDG_ERR_ARG, "bad arguments");
+    AMDG_REQUIRE(prec == AMDG_PREC_FP64 || prec == AMDG_PREC_MIXED, AMDG_ERR_ARG, "bad precision");
+    AMDG_CK(cudaSetDevice(op->device));
+    cudaStream_t st = stream_of(op);
+    if (prec == AMDG_PREC_FP64) return eval_point_values<double>(op, mats64(op), d_u, d_up, st);
+    const int64_t n = op->grid->dof, np = op->grid->host.num_elements * op->points;
+    float* u32 = static_cast<float*>(op->w_u);
+    float* up32 = static_cast<float*>(op->w_up);
+    AMDG_CK(launch_convert<double, float>(d_u, u32, n, st));
+    amdg_status r = eval_point_values<float>(op, mats32(op), u32, up32, st);
+    if (r != AMDG_OK) return r;
+    AMDG_CK(launch_convert<float, double>(up32, d_up, np, st));
+    op->grid->ctx->launches += 2;
+    return AMDG_OK;
+}
+
+amdg_status amdg_burgers_flux_coefficients(amdg_burgers_op* op, const double* d_u, double* d_fu, amdg_precision prec) {
+    AMDG_REQUIRE(op && d_u && d_fu, AMDG_ERR_ARG, "bad arguments");
+    AMDG_REQUIRE(prec == AMDG_PREC_FP64 || prec == AMDG_PREC_MIXED, AMDG_ERR_ARG, "bad precision");
+    AMDG_CK(cudaSetDevice(op->device));
+    cudaStream_t st = stream_of(op);
+    const int64_t np = op->grid->host.num_elements * op->points;
+    if (prec == AMDG_PREC_FP64) {
+        amdg_status r = eval_point_values<double>(op, mats64(op), d_u, static_cast<double*>(op->w_up), st);
+        if (r != AMDG_OK) return r;
+        if ((r = eval_flux_coefficients<double>(op, static_cast<double*>(op->w_up), st)) != AMDG_OK) return r;
+        AMDG_CK(cudaMemcpyAsync(d_fu, op->w_fu, np * sizeof(double), cudaMemcpyDeviceToDevice, st));
+        return AMDG_OK;
+    }
+    float* u32 = static_cast<float*>(op->w_u);
+    AMDG_CK(launch_convert<double, float>(d_u, u32, op->grid->dof, st));
+    amdg_status r = eval_point_values<float>(op, mats32(op), u32, static_cast<float*>(op->w_up), st);
+    if (r != AMDG_OK) return r;
+    if ((r = eval_flux_coefficients<float>(op, static_cast<float*>(op->w_up), st)) != AMDG_OK) return r;
+    AMDG_CK(launch_convert<float, double>(static_cast<float*>(op->w_fu), d_fu, np, st));
+    op->grid->ctx->launches += 2;
+    return AMDG_OK;
+}
+
+amdg_status amdg_burgers_rk3_steps(amdg_burgers_op* op, double dt, int nsteps, amdg_precision prec) {
+    AMDG_REQUIRE(op && nsteps >= 0 && std::isfinite(dt), AMDG_ERR_ARG, "bad arguments");
+    AMDG_REQUIRE(prec == AMDG_PREC_FP64 || prec == AMDG_PREC_MIXED, AMDG_ERR_ARG, "bad precision");
+    AMDG_CK(cudaSetDevice(op->device));
+    amdg_grid* g = op->grid;
+    cudaStream_t st = stream_of(op);
+    const size_t bytes = size_t(g->dof) * sizeof(double);
+    for (int s = 0; s < nsteps; ++s) {
+        // ucoe is updated in place per stage, ucoe_tn holds u^n (RK3SSP::step_stage)
+        AMDG_CK(cudaMemcpyAsync(op->d_u1, g->d_u, bytes, cudaMemcpyDeviceToDevice, st));
+        for (int stage = 0; stage < 3; ++stage) {
+            amdg_status r = eval_rhs(op, op->d_u1, op->d_rhs64, prec);
+            if (r != AMDG_OK) return r;
+            AMDG_CK(launch_stage_update(g->d_u, op->d_u1, op->d_rhs64, g->dof, stage_coef(stage, dt), st));
+            g->ctx->launches++;
+        }
+        AMDG_CK(cudaMemcpyAsync(g->d_u, op->d_u1, bytes, cudaMemcpyDeviceToDevice, st));
+    }
+    return AMDG_OK;
+}
+
+}  // extern "C"

@@ -157,3 +157,71 @@ void build_linear_topology(const HostGrid& g, const Oper1D& op, const double* co
 }
 
 }  // namespace amdg
+
+namespace amdg {
+
+void build_transform_topology(const HostGrid& g, TransformTopology* out) {
+    const int dim = g.dim, nmax = g.nmax, n1 = 1 << nmax;
+    const int64_t one = int64_t(1) << nmax;
+    std::vector<std::vector<int>> vol1(n1), flx1(n1);
+    for (int o = 0; o < n1; ++o) {
+        int64_t a, b;
+        support_units(o, nmax, &a, &b);
+        for (int oc = 0; oc < n1; ++oc) {
+            int64_t a2, b2;
+            support_units(oc, nmax, &a2, &b2);
+            if (!((a >= b2) || (b <= a2))) vol1[o].push_back(oc);
+            if (flux_related(a, b, a2, b2, one)) flx1[o].push_back(oc);
+        }
+    }
+    const int64_t E = g.num_elements;
+    out->vol_ptr.assign(size_t(E) * dim + 1, 0);
+    out->flx_ptr.assign(size_t(E) * dim + 1, 0);
+    out->vol_src.clear(); out->vol_lev.clear(); out->flx_src.clear(); out->flx_lev.clear();
+    std::vector<int32_t> o2(dim);
+    for (int64_t e = 0; e < E; ++e) {
+        const int32_t* oe = &g.order[size_t(e) * dim];
+        for (int t = 0; t < dim; ++t) {
+            std::copy(oe, oe + dim, o2.begin());
+            for (int oc : vol1[oe[t]]) {
+                o2[t] = oc;
+                const int64_t s = find_element(g, o2.data());
+                if (s < 0) continue;
+                out->vol_src.push_back(int32_t(s));
+                out->vol_lev.push_back(level_of_order(oc));
+            }
+            for (int oc : flx1[oe[t]]) {
+                o2[t] = oc;
+                const int64_t s = find_element(g, o2.data());
+                if (s < 0) continue;
+                out->flx_src.push_back(int32_t(s));
+                out->flx_lev.push_back(level_of_order(oc));
+            }
+            out->vol_ptr[size_t(e) * dim + t + 1] = int32_t(out->vol_src.size());
+            out->flx_ptr[size_t(e) * dim + t + 1] = int32_t(out->flx_src.size());
+        }
+    }
+}
+
+bool build_surplus_ancestors(const HostGrid& g, const LagrTables& t, std::vector<int32_t>* anc) {
+    const int dim = g.dim;
+    const int64_t E = g.num_elements;
+    anc->assign(size_t(E) * dim * 4, -1);
+    std::vector<int32_t> o2(dim);
+    for (int64_t e = 0; e < E; ++e) {
+        const int32_t* oe = &g.order[size_t(e) * dim];
+        for (int d = 0; d < dim; ++d) {
+            if (oe[d] == 0) continue;
+            std::copy(oe, oe + dim, o2.begin());
+            for (int ic = 0; ic < 4; ++ic) {
+                o2[d] = t.anc_order[size_t(oe[d]) * 4 + ic];
+                const int64_t s = find_element(g, o2.data());
+                if (s < 0) return false;  // the element set has a hole
+                (*anc)[(size_t(e) * dim + d) * 4 + ic] = int32_t(s);
+            }
+        }
+    }
+    return true;
+}
+
+}  // namespace amdg

@@ -1,0 +1,137 @@
+// Device kernels of the Lagrange-interpolation path for nonlinear fluxes.
+//
+// fibre_transform: one 1D transform of the fast multi-dimensional algorithm
+// (FastMultiplyLU::transform_1D, FastMultiplyLU.cpp:436-512): for every
+// element e and every entry of its output block,
+//   out[e][idx] (+)= coef * sum_{s in N_t(e), L/U filter} sum_k in[s][idx, dim t <- k] * M[o_t(s)*n_from + k][o_t(e)*n_to + idx_t]
+// where N_t(e) is the vol or flx neighbour list of e in dimension t.  The
+// per-element block shapes follow the partial-sum schedule
+// (series_vec_transform_size, FastMultiplyLU.cpp:596-612).  One thread per
+// output entry; the neighbour list is warp-uniform within an element.
+//
+// surplus_pass: pass d of the hierarchical surplus
+// (LagrInterpolation::eval_fp_to_coe_D_Lag, Interplation.cpp:1222-1434).
+#include <cuda_runtime.h>
+
+#include <cstdint>
+
+#include "kernels_lagr.cuh"
+
+namespace amdg {
+
+__device__ __forceinline__ int level_of(int o) { return o == 0 ? 0 : 32 - __clz(o); }
+
+template <typename T>
+__global__ void __launch_bounds__(256) fibre_transform_kernel(TransformArgs<T> a) {
+    const int64_t gid = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+    const int64_t total = a.num_elements * a.out_block;
+    if (gid >= total) return;
+    const int64_t e = gid / a.out_block;
+    const int idx = int(gid - e * a.out_block);
+    const int inner = idx % a.stride;
+    const int qt = (idx / a.stride) % a.n_to;
+    const int outer = idx / (a.stride * a.n_to);
+    const int oe = __ldg(a.order + e * a.dim + a.t);
+    const int le = level_of(oe);
+    const int beg = __ldg(a.ptr + e * a.dim + a.t), end = __ldg(a.ptr + e * a.dim + a.t + 1);
+    const T* mcol = a.M + size_t(oe) * a.n_to + qt;
+    const int in_off = outer * a.n_from * a.stride + inner;
+    T acc = T(0);
+    for (int i = beg; i < end; ++i) {
+        const int ls = __ldg(a.lev + i);
+        if (a.lu == 0 && le >= ls) continue;  // "L": finer neighbours only
+        if (a.lu == 2 && le < ls) continue;   // "U": coarser or equal
+        const int s = __ldg(a.src + i);
+        const int os = __ldg(a.order + int64_t(s) * a.dim + a.t);
+        const T* x = a.in + int64_t(s) * a.in_block + in_off;
+        const T* m = mcol + size_t(os) * a.n_from * a.ncols;
+        for (int k = 0; k < a.n_from; ++k) acc = fma(__ldg(x + k * a.stride), __ldg(m + size_t(k) * a.ncols), acc);
+    }
+    acc *= a.coef;
+    if (a.accumulate) a.out[gid] += acc;
+    else a.out[gid] = acc;
+}
+
+template <typename T>
+cudaError_t launch_fibre_transform(const TransformArgs<T>& a, cudaStream_t st) {
+    const int64_t total = a.num_elements * a.out_block;
+    if (total == 0) return cudaSuccess;
+    fibre_transform_kernel<T><<<unsigned((total + 255) / 256), 256, 0, st>>>(a);
+    return cudaGetLastError();
+}
+
+template cudaError_t launch_fibre_transform<double>(const TransformArgs<double>&, cudaStream_t);
+template cudaError_t launch_fibre_transform<float>(const TransformArgs<float>&, cudaStream_t);
+
+// f(u) = u^2/2 at every interpolation point (FluxFunction::burgers_flux_scalar, Interplation.cpp:5070-5073)
+template <typename T>
+__global__ void burgers_flux_kernel(const T* __restrict__ up, T* __restrict__ fp, int64_t n) {
+    const int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (i < n) {
+        const T u = up[i];
+        fp[i] = u * u * T(0.5);
+    }
+}
+
+template <typename T>
+cudaError_t launch_burgers_flux(const T* up, T* fp, int64_t n, cudaStream_t st) {
+    if (n == 0) return cudaSuccess;
+    burgers_flux_kernel<T><<<unsigned((n + 255) / 256), 256, 0, st>>>(up, fp, n);
+    return cudaGetLastError();
+}
+
+template cudaError_t launch_burgers_flux<double>(const double*, double*, int64_t, cudaStream_t);
+template cudaError_t launch_burgers_flux<float>(const float*, float*, int64_t, cudaStream_t);
+
+template <typename T>
+__global__ void __launch_bounds__(256) surplus_pass_kernel(SurplusArgs<T> a) {
+    const int64_t gid = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+    const int64_t total = a.num_elements * a.points;
+    if (gid >= total) return;
+    const int64_t e = gid / a.points;
+    const int p = int(gid - e * a.points);
+    T c = a.in[gid];
+    const int od = __ldg(a.order + e * a.dim + a.d);
+    if (od != 0) {
+        const int pd = (p / a.stride) % 4;
+        const int base = p - pd * a.stride;
+        const int32_t* anc = a.anc + (e * a.dim + a.d) * 4;
+#pragma unroll
+        for (int ic = 0; ic < 4; ++ic) {
+            const int s = __ldg(anc + ic);
+            const int q = __ldg(a.anc_point + od * 4 + ic);
+            const int r = __ldg(a.anc_rank + od * 4 + ic);
+            c = fma(a.weight[pd * 4 + r], a.in[int64_t(s) * a.points + base + q * a.stride], c);
+        }
+    }
+    a.out[gid] = c;
+}
+
+template <typename T>
+cudaError_t launch_surplus_pass(const SurplusArgs<T>& a, cudaStream_t st) {
+    const int64_t total = a.num_elements * a.points;
+    if (total == 0) return cudaSuccess;
+    surplus_pass_kernel<T><<<unsigned((total + 255) / 256), 256, 0, st>>>(a);
+    return cudaGetLastError();
+}
+
+template cudaError_t launch_surplus_pass<double>(const SurplusArgs<double>&, cudaStream_t);
+template cudaError_t launch_surplus_pass<float>(const SurplusArgs<float>&, cudaStream_t);
+
+template <typename Ti, typename To>
+__global__ void convert_kernel(const Ti* __restrict__ in, To* __restrict__ out, int64_t n) {
+    const int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (i < n) out[i] = To(in[i]);
+}
+
+template <typename Ti, typename To>
+cudaError_t launch_convert(const Ti* in, To* out, int64_t n, cudaStream_t st) {
+    if (n == 0) return cudaSuccess;
+    convert_kernel<Ti, To><<<unsigned((n + 255) / 256), 256, 0, st>>>(in, out, n);
+    return cudaGetLastError();
+}
+
+template cudaError_t launch_convert<double, float>(const double*, float*, int64_t, cudaStream_t);
+template cudaError_t launch_convert<float, double>(const float*, double*, int64_t, cudaStream_t);
+
+}  // namespace amdg

@@ -1,0 +1,230 @@
+// Host set-up of the Lagrange-interpolation path for nonlinear fluxes:
+// hierarchical degree-3 Lagrange basis (node layout msh_case 1,
+// LagrBasis.cpp:65-70), the Alpert-at-Lagrange-point table
+// (Interplation.cpp:16-101), the Lagrange x Alpert 1D matrices
+// (OperatorMatrix1D<LagrBasis,AlptBasis>, OperatorMatrix1D.h:166-199), the
+// dimension-order / L-U schedule of the fast transforms
+// (FastMultiplyLU.cpp:596-664) and the ancestor table of the hierarchical
+// surplus (Interplation.cpp:775-888).
+#include <algorithm>
+#include <cmath>
+
+#include "amdg_internal.hpp"
+
+namespace amdg {
+namespace {
+
+// nodes on [-1,1]: level 0, and level >= 1 (two on each half of the support)
+const double kMsh0[4] = {-0.6, -0.2, 0.2, 0.6};
+const double kMsh1[4] = {-0.8, -0.4, 0.4, 0.8};
+
+double lagrange_poly(const double* nodes, int i, double x) {
+    double v = 1.0;
+    for (int m = 0; m < 4; ++m)
+        if (m != i) v *= (x - nodes[m]) / (nodes[i] - nodes[m]);
+    return v;
+}
+
+// level-0 / level-1 mother functions on [0,1]
+double lagr_mother(double xt, int msh, int p) {
+    const double x = 2.0 * xt - 1.0;
+    if (x < -1.0 || x > 1.0) return 0.0;
+    if (msh == 0) return lagrange_poly(kMsh0, p, x);
+    if (p <= 1) {
+        if (x > 0.0) return 0.0;
+        static const double left[4] = {-0.8, -0.6, -0.4, -0.2};
+        return lagrange_poly(left, p == 0 ? 0 : 2, x);
+    }
+    if (x < 0.0) return 0.0;
+    static const double right[4] = {0.2, 0.4, 0.6, 0.8};
+    return lagrange_poly(right, p == 2 ? 1 : 3, x);
+}
+
+double supp_lo(int o) { int n, j; elem_of_order(o, &n, &j); return n <= 1 ? 0.0 : std::pow(2.0, 1.0 - n) * (j - 1.0) / 2.0; }
+double supp_hi(int o) { int n, j; elem_of_order(o, &n, &j); return n <= 1 ? 1.0 : std::pow(2.0, 1.0 - n) * (j + 1.0) / 2.0; }
+
+struct GL10 {
+    double x[10], w[10];
+    GL10() {
+        for (int i = 0; i < 10; ++i) {
+            double z = std::cos(M_PI * (i + 0.75) / 10.5), dp = 1.0;
+            for (int it = 0; it < 100; ++it) {
+                double p0 = 1.0, p1 = z;
+                for (int m = 2; m <= 10; ++m) {
+                    const double p2 = ((2.0 * m - 1.0) * z * p1 - (m - 1.0) * p0) / m;
+                    p0 = p1;
+                    p1 = p2;
+                }
+                dp = 10 * (z * p1 - p0) / (z * z - 1.0);
+                const double dz = p1 / dp;
+                z -= dz;
+                if (std::fabs(dz) < 1e-16) break;
+            }
+            double p0 = 1.0, p1 = z;
+            for (int m = 2; m <= 10; ++m) {
+                const double p2 = ((2.0 * m - 1.0) * z * p1 - (m - 1.0) * p0) / m;
+                p0 = p1;
+                p1 = p2;
+            }
+            dp = 10 * (z * p1 - p0) / (z * z - 1.0);
+            x[9 - i] = z;
+            w[9 - i] = 2.0 / ((1.0 - z * z) * dp * dp);
+        }
+    }
+    template <class F>
+    double integrate(F&& f, double a, double b) const {
+        double s = 0.0;
+        for (int i = 0; i < 10; ++i) s += w[i] * f(a + (x[i] + 1.0) * 0.5 * (b - a));
+        return s * (b - a) / 2.0;
+    }
+};
+
+}  // namespace
+
+double lagr_eval(int order, double x, int sgn) {
+    const int o = order / 4, p = order % 4;
+    int n, j;
+    elem_of_order(o, &n, &j);
+    double xl = x;
+    if (sgn == -1) {
+        if (std::fabs(x) <= kRoundOff) return 0.0;
+        xl -= kRoundOff;
+    } else if (sgn == 1) {
+        if (std::fabs(x - 1.0) <= kRoundOff) return 0.0;
+        xl += kRoundOff;
+    }
+    if (n <= 1) return lagr_mother(xl, n, p);
+    return lagr_mother(std::pow(2.0, n - 1) * xl - double((j - 1) / 2), 1, p);
+}
+
+double lagr_point(int o, int p) {
+    int n, j;
+    elem_of_order(o, &n, &j);
+    if (n == 0) return (kMsh0[p] + 1.0) / 2.0;
+    const double a = supp_lo(o), b = supp_hi(o);
+    return a + (b - a) * (kMsh1[p] + 1.0) / 2.0;
+}
+
+void build_lagr_tables(const Basis1D& alpt, LagrTables* t) {
+    static const GL10 g;
+    const int n1 = alpt.num_elem(), na = alpt.num_basis(), np = alpt.k + 1, nl = n1 * 4;
+    t->n_lagr = nl;
+    t->n_alpt = na;
+    // Alpert basis at Lagrange points, row = Alpert basis, col = Lagrange point
+    t->a2p.assign(size_t(na) * nl, 0.0);
+    for (int c = 0; c < nl; ++c) {
+        const double x = lagr_point(c / 4, c % 4);
+        for (int r = 0; r < na; ++r) {
+            const int o = r / np;
+            if (x < supp_lo(o) || x > supp_hi(o)) continue;
+            t->a2p[size_t(r) * nl + c] = alpt.eval(r, 0, x, 0);
+        }
+    }
+    // Lagrange (row) x Alpert (col) products
+    t->lv.assign(size_t(nl) * na, 0.0);
+    t->lvx.assign(size_t(nl) * na, 0.0);
+    t->lflx.assign(size_t(nl) * na, 0.0);
+#pragma omp parallel for schedule(dynamic)
+    for (int r = 0; r < nl; ++r) {
+        const int ou = r / 4;
+        const int lu = level_of_order(ou);
+        const double ua = supp_lo(ou), ub = supp_hi(ou);
+        for (int c = 0; c < na; ++c) {
+            const int ov = c / np;
+            const double va = supp_lo(ov), vb = supp_hi(ov);
+            const size_t idx = size_t(r) * na + c;
+            if (!(va >= ub || vb <= ua)) {
+                double xl = ua, xr = ub;
+                if (lu <= level_of_order(ov)) { xl = va; xr = vb; }
+                const double xm = 0.5 * (xl + xr);
+                auto fv = [&](double x) { return lagr_eval(r, x, 0) * alpt.eval(c, 0, x, 0); };
+                auto fvx = [&](double x) { return lagr_eval(r, x, 0) * alpt.eval(c, 1, x, 0); };
+                t->lv[idx] = g.integrate(fv, xl, xm) + g.integrate(fv, xm, xr);
+                t->lvx[idx] = g.integrate(fvx, xl, xm) + g.integrate(fvx, xm, xr);
+            }
+            const double pts[3] = {va, 0.5 * (va + vb), vb};
+            const int npts = level_of_order(ov) <= 1 ? 2 : 3;
+            auto edge = [&](int su, int sv) {
+                double s = 0.0;
+                for (int i = 0; i < npts; ++i) {
+                    const double x = pts[i];
+                    double fu = lagr_eval(r, x, su), fw = alpt.eval(c, 0, x, sv);
+                    if (std::fabs(x) < kRoundOff) {
+                        if (su == -1) fu = lagr_eval(r, 1.0, su);
+                        if (sv == -1) fw = alpt.eval(c, 0, 1.0, sv);
+                    } else if (std::fabs(x - 1.0) < kRoundOff) {
+                        if (su == 1) fu = lagr_eval(r, 0.0, su);
+                        if (sv == 1) fw = alpt.eval(c, 0, 0.0, sv);
+                    }
+                    s += fu * fw;
+                }
+                return s;
+            };
+            // (ulft_vjp + urgt_vjp), HyperbolicLagrRHS::rhs_flx_intp_scalar (FastMultiplyLU.cpp:1166)
+            t->lflx[idx] = (edge(-1, 1) - edge(-1, -1)) + (edge(1, 1) - edge(1, -1));
+        }
+    }
+    // Alpert x Alpert jump-jump (ujp_vjp = urgt_vjp - ulft_vjp), LxF penalty
+    Oper1D op;
+    build_oper1d(alpt, &op, false);
+    t->ajump.assign(size_t(na) * na, 0.0);
+    for (size_t i = 0; i < t->ajump.size(); ++i) t->ajump[i] = op.urgt_vjp[i] - op.ulft_vjp[i];
+    // surplus: ancestors (coarser-level points inside each element's support) and weights
+    t->anc_order.assign(size_t(n1) * 4, -1);
+    t->anc_point.assign(size_t(n1) * 4, 0);
+    t->anc_rank.assign(size_t(n1) * 4, 0);
+    for (int o = 1; o < n1; ++o) {
+        const int l = level_of_order(o);
+        const double xl = supp_lo(o), xr = supp_hi(o);
+        int ic = 0;
+        double pos[4] = {0, 0, 0, 0};
+        for (int oa = 0; oa < n1 && ic < 4; ++oa) {
+            if (level_of_order(oa) >= l) break;
+            for (int q = 0; q < 4 && ic < 4; ++q) {
+                const double x = lagr_point(oa, q);
+                if (x > xl && x < xr) {
+                    t->anc_order[size_t(o) * 4 + ic] = oa;
+                    t->anc_point[size_t(o) * 4 + ic] = q;
+                    pos[ic] = x;
+                    ++ic;
+                }
+            }
+        }
+        for (int a = 0; a < 4; ++a) {
+            int rk = 0;
+            for (int b = 0; b < 4; ++b) rk += pos[b] < pos[a];
+            t->anc_rank[size_t(o) * 4 + a] = rk;
+        }
+    }
+    // weight[p0][rank] = -L0_rank(node p0 of the element, in its reference coordinates)
+    for (int p0 = 0; p0 < 4; ++p0)
+        for (int r = 0; r < 4; ++r) t->weight[p0 * 4 + r] = -lagr_mother((kMsh1[p0] + 1.0) / 2.0, 0, r);
+}
+
+void transform_schedule(int dim, std::vector<std::vector<int>>* dim_order, std::vector<std::vector<int>>* lu) {
+    // 2^(dim-1) partial sums; sum s: dimension d gets tag 2*bit_d(s) for d < dim-1
+    // and tag 1 for the last, then dimensions are ordered by tag
+    // (0 = L, 1 = full, 2 = U); FastMultiplyLU.cpp:614-664
+    dim_order->clear();
+    lu->clear();
+    if (dim == 1) {
+        dim_order->push_back({0});
+        lu->push_back({1});
+        return;
+    }
+    const int nsum = 1 << (dim - 1);
+    for (int s = 0; s < nsum; ++s) {
+        std::vector<int> tag(dim);
+        for (int d = 0; d < dim - 1; ++d) tag[d] = 2 * ((s >> (dim - 2 - d)) & 1);
+        tag[dim - 1] = 1;
+        std::vector<int> order(dim);
+        for (int d = 0; d < dim; ++d) order[d] = d;
+        std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return tag[a] < tag[b]; });
+        std::vector<int> tags_sorted(dim);
+        for (int d = 0; d < dim; ++d) tags_sorted[d] = tag[order[d]];
+        dim_order->push_back(order);
+        lu->push_back(tags_sorted);
+    }
+}
+
+}  // namespace amdg

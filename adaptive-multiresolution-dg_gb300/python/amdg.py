@@ -74,6 +74,12 @@ def load():
         "amdg_rk3ssp_steps": ([vp, dbl, i32, i32], i32),
         "amdg_rk3ssp_steps_host": ([vp, dbl, i32, vp, i32], i32),
         "amdg_rk3_stage_update": ([vp, i32, dbl, vp, vp, vp, i64], i32),
+        "amdg_burgers_create": ([vp, vp, pp], i32),
+        "amdg_burgers_destroy": ([vp], i32),
+        "amdg_burgers_rhs": ([vp, vp, vp, i32], i32),
+        "amdg_burgers_point_values": ([vp, vp, vp, i32], i32),
+        "amdg_burgers_flux_coefficients": ([vp, vp, vp, i32], i32),
+        "amdg_burgers_rk3_steps": ([vp, dbl, i32, i32], i32),
     }
     for name, (args, res) in sig.items():
         fn = getattr(L, name)
@@ -162,7 +168,7 @@ class Grid:
     """DGSolution/DGAdapt on the device (sparse or full grid, Alpert degree k)."""
 
     def __init__(self, ctx: Context, dim: int, nmax: int, k: int = 2, sparse: bool = True):
-        self.ctx, self.dim, self.nmax, self.k = ctx, dim, nmax, k
+        self.ctx, self.dim, self.nmax, self.k, self.sparse = ctx, dim, nmax, k, sparse
         self._h = C.c_void_p()
         _ck(load().amdg_grid_create(ctx.handle, dim, nmax, k, int(sparse), C.byref(self._h)), "grid_create")
         ne, dof = C.c_int64(), C.c_int64()
@@ -252,6 +258,42 @@ class LinearOperator:
     def close(self):
         if self._h:
             load().amdg_linear_destroy(self._h)
+            self._h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class BurgersOperator:
+    """LagrInterpolation + HyperbolicLagrRHS + HyperbolicAlptRHS for the Burgers
+    flux u^2/2 with global Lax-Friedrichs penalty alpha, on the device."""
+
+    def __init__(self, grid: Grid, alpha):
+        self.grid = grid
+        a = np.ascontiguousarray(np.broadcast_to(np.asarray(alpha, np.float64), (grid.dim,)))
+        self._h = C.c_void_p()
+        _ck(load().amdg_burgers_create(grid.handle, _ptr(a), C.byref(self._h)), "burgers_create")
+        self.points = 4 ** grid.dim
+
+    def rhs_device(self, d_u: int, d_rhs: int, prec: int = FP64):
+        _ck(load().amdg_burgers_rhs(self._h, C.c_void_p(d_u), C.c_void_p(d_rhs), prec), "burgers_rhs")
+
+    def point_values_device(self, d_u: int, d_up: int, prec: int = FP64):
+        _ck(load().amdg_burgers_point_values(self._h, C.c_void_p(d_u), C.c_void_p(d_up), prec), "burgers_point_values")
+
+    def flux_coefficients_device(self, d_u: int, d_fu: int, prec: int = FP64):
+        _ck(load().amdg_burgers_flux_coefficients(self._h, C.c_void_p(d_u), C.c_void_p(d_fu), prec),
+            "burgers_flux_coefficients")
+
+    def rk3_steps(self, dt: float, nsteps: int, prec: int = FP64):
+        _ck(load().amdg_burgers_rk3_steps(self._h, dt, nsteps, prec), "burgers_rk3_steps")
+
+    def close(self):
+        if self._h:
+            load().amdg_burgers_destroy(self._h)
             self._h = C.c_void_p()
 
     def __del__(self):

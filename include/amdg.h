@@ -54,6 +54,7 @@ typedef enum amdg_precision {
 typedef struct amdg_context amdg_context;
 typedef struct amdg_grid amdg_grid;
 typedef struct amdg_linear_op amdg_linear_op;
+typedef struct amdg_burgers_op amdg_burgers_op;
 
 /* Separable 1D factor g_d(x) of term `term` (the std::function<double(double,int)>
  * the reference takes, DGAdapt.h:17-38). */
@@ -149,6 +150,36 @@ amdg_status amdg_rk3ssp_steps_host(amdg_linear_op* op, double dt, int nsteps, do
  * stage 1 u = 3/4 un + 1/4 (u + dt*rhs), stage 2 u = 1/3 un + 2/3 (u + dt*rhs). */
 amdg_status amdg_rk3_stage_update(amdg_context* ctx, int stage, double dt, const double* d_un, double* d_u,
                                   const double* d_rhs, int64_t n);
+
+/* ---- nonlinear flux through Lagrange interpolation (Burgers) ------------- */
+/* Scalar inviscid Burgers u_t + sum_d (u^2/2)_{x_d} = 0 with global
+ * Lax-Friedrichs flux, the flux interpolated by degree-3 hierarchical
+ * Lagrange interpolation (msh_case 1).  Replaces the set-up of
+ * LagrInterpolation(dg) + FastLagrIntp + HyperbolicLagrRHS +
+ * HyperbolicAlptRHS (Interpolation.h:36-47, FastMultiplyLU.h:194-205,
+ * 575-629) for the registered flux u^2/2 (FluxFunction::burgers_flux_scalar,
+ * Interplation.cpp:5070-5073).  alpha has dim entries (lxf_alpha).  The grid
+ * must be free of holes (every element's parents present, DGAdapt::check_hole);
+ * otherwise AMDG_ERR_STATE. */
+amdg_status amdg_burgers_create(amdg_grid* g, const double* alpha, amdg_burgers_op** out);
+amdg_status amdg_burgers_destroy(amdg_burgers_op* op);
+/* One right-hand-side evaluation, d_rhs = R(d_u) (device vectors of dof doubles):
+ * LagrInterpolation::nonlinear_Lagr_fast (Interplation.cpp:4033-4047),
+ * DGSolution::set_rhs_zero, HyperbolicLagrRHS::rhs_vol_scalar and
+ * rhs_flx_intp_scalar (FastMultiplyLU.cpp:1125-1189),
+ * HyperbolicAlptRHS::rhs_flx_penalty_scalar (FastMultiplyLU.cpp:1269-1276). */
+amdg_status amdg_burgers_rhs(amdg_burgers_op* op, const double* d_u, double* d_rhs, amdg_precision prec);
+/* Values of u_h at every Lagrange interpolation point, num_elements x 4^dim
+ * (FastLagrIntp::eval_up_Lagr, FastMultiplyLU.cpp:1362; Element::up_intp). */
+amdg_status amdg_burgers_point_values(amdg_burgers_op* op, const double* d_u, double* d_up, amdg_precision prec);
+/* Interpolation coefficients of the flux, num_elements x 4^dim, identical in
+ * every dimension for this flux (Element::fucoe_intp after
+ * LagrInterpolation::eval_fp_to_coe_D_Lag, Interplation.cpp:1222-1434). */
+amdg_status amdg_burgers_flux_coefficients(amdg_burgers_op* op, const double* d_u, double* d_fu, amdg_precision prec);
+/* nsteps SSP-RK3 steps of size dt on the grid's device state, the RHS
+ * re-evaluated per stage (RK3SSP::step_stage, ODESolver.cpp:285-301, in the
+ * stage loop of example/07_vlasov_maxwell_adapt.cpp:278-320). */
+amdg_status amdg_burgers_rk3_steps(amdg_burgers_op* op, double dt, int nsteps, amdg_precision prec);
 
 #ifdef __cplusplus
 }

@@ -635,3 +635,390 @@ double amdg_oracle_l2_error_split(int dim, int N, int k, int64_t E, const int32_
     }
     return sqrt(err2 > 0 ? err2 : 0.0);
 }
+
+/* ======================================================================== */
+/* Lagrange interpolation path for nonlinear fluxes (config: 3D Burgers)     */
+/* ======================================================================== */
+/* Hierarchical Lagrange basis of degree 3, node layout msh_case 1
+ * (LagrBasis.cpp:65-70): level-0 nodes {-3/5,-1/5,1/5,3/5} on [-1,1]; level-1
+ * nodes {-4/5,-2/5} on the left half and {2/5,4/5} on the right half, each
+ * interpolating on its half together with the two level-0 nodes of that half
+ * (LagrBasis.cpp:300-330). */
+static const double LAGR_MSH0[4] = {-0.6, -0.2, 0.2, 0.6};
+static const double LAGR_MSH1[4] = {-0.8, -0.4, 0.4, 0.8};
+
+static double lagr_poly(const double* nodes, int i, double x) {
+    double v = 1.0;
+    for (int m = 0; m < 4; ++m)
+        if (m != i) v *= (x - nodes[m]) / (nodes[i] - nodes[m]);
+    return v;
+}
+
+static double lagr_phi(double xt, int msh, int p) {
+    const double x = 2.0 * xt - 1.0;
+    if (x < -1.0 || x > 1.0) return 0.0;
+    if (msh == 0) return lagr_poly(LAGR_MSH0, p, x);
+    if (p <= 1) {
+        if (x > 0) return 0.0;
+        const double nodes[4] = {-0.8, -0.6, -0.4, -0.2};
+        return lagr_poly(nodes, p == 0 ? 0 : 2, x);
+    }
+    if (x < 0) return 0.0;
+    const double nodes[4] = {0.2, 0.4, 0.6, 0.8};
+    return lagr_poly(nodes, p == 2 ? 1 : 3, x);
+}
+
+double amdg_oracle_lagr_val(int level, int suppt, int p, double x, int sgn) {
+    double xl = x;
+    if (sgn == -1) {
+        if (fabs(x) <= ROUND_OFF) return 0.0;
+        xl -= ROUND_OFF;
+    } else if (sgn == 1) {
+        if (fabs(x - 1) <= ROUND_OFF) return 0.0;
+        xl += ROUND_OFF;
+    }
+    if (level <= 1) return lagr_phi(xl, level, p);
+    const double xt = pow(2.0, level - 1) * xl - (suppt - 1) / 2;
+    return lagr_phi(xt, 1, p);
+}
+
+/* interpolation point p of 1D element (n, j) (LagrBasis.cpp:18-27) */
+double amdg_oracle_lagr_point(int level, int suppt, int p) {
+    if (level == 0) return (LAGR_MSH0[p] + 1.0) / 2.0;
+    const double a = support_lo(level, suppt), b = support_hi(level, suppt);
+    return a + (b - a) * (LAGR_MSH1[p] + 1.0) / 2.0;
+}
+
+/* generic 1D basis evaluation: type 0 = Alpert (degree k), 1 = Lagrange degree 3 */
+static double basis_val(int type, int k, int n, int j, int p, int deriv, double x, int sgn) {
+    if (type == 0) return amdg_oracle_alpert_val(k, n, j, p, deriv, x, sgn);
+    return amdg_oracle_lagr_val(n, j, p, x, sgn);
+}
+
+typedef struct { int tu, tv, k; elem1d u, v; int pu, pv, du, dv; } gprod_ctx;
+
+static double gprod_integrand(double x, const void* c) {
+    const gprod_ctx* p = (const gprod_ctx*)c;
+    return basis_val(p->tu, p->k, p->u.n, p->u.j, p->pu, p->du, x, 0) * basis_val(p->tv, p->k, p->v.n, p->v.j, p->pv, p->dv, x, 0);
+}
+
+static double gproduct_volume(int tu, int tv, int k, elem1d u, int pu, elem1d v, int pv, int du, int dv) {
+    const double ua = support_lo(u.n, u.j), ub = support_hi(u.n, u.j);
+    const double va = support_lo(v.n, v.j), vb = support_hi(v.n, v.j);
+    if (va >= ub || vb <= ua) return 0.0;
+    double xl = ua, xr = ub;
+    if (u.n <= v.n) { xl = va; xr = vb; }
+    const double xm = (xl + xr) / 2.0;
+    gprod_ctx c = {tu, tv, k, u, v, pu, pv, du, dv};
+    return gl_integrate(gprod_integrand, &c, xl, xm, 10) + gl_integrate(gprod_integrand, &c, xm, xr, 10);
+}
+
+static double gproduct_edge(int tu, int tv, int k, elem1d u, int pu, elem1d v, int pv, int su, int sv) {
+    const double pts[3] = {support_lo(v.n, v.j), 0.5 * (support_lo(v.n, v.j) + support_hi(v.n, v.j)), support_hi(v.n, v.j)};
+    double s = 0.0;
+    for (int i = 0; i < 3; ++i) {
+        if (v.n <= 1 && i == 2) continue;
+        const double x = pts[i];
+        double fu = basis_val(tu, k, u.n, u.j, pu, 0, x, su), fv = basis_val(tv, k, v.n, v.j, pv, 0, x, sv);
+        if (fabs(x) < ROUND_OFF) {
+            if (su == -1) fu = basis_val(tu, k, u.n, u.j, pu, 0, 1.0, su);
+            if (sv == -1) fv = basis_val(tv, k, v.n, v.j, pv, 0, 1.0, sv);
+        } else if (fabs(x - 1.0) < ROUND_OFF) {
+            if (su == 1) fu = basis_val(tu, k, u.n, u.j, pu, 0, 0.0, su);
+            if (sv == 1) fv = basis_val(tv, k, v.n, v.j, pv, 0, 0.0, sv);
+        }
+        s += fu * fv;
+    }
+    return s;
+}
+
+/* Lagrange (rows, degree 3) x Alpert (cols, degree k) 1D matrices, each
+ * (2^N*4) x (2^N*(k+1)): u_v, u_vx and (ulft_vjp + urgt_vjp). */
+int amdg_oracle_oper1d_lagr(int N, int k, double* u_v, double* u_vx, double* uave2_vjp) {
+    const int nr = (1 << N) * 4, nc = (1 << N) * (k + 1);
+#pragma omp parallel for schedule(dynamic)
+    for (int r = 0; r < nr; ++r) {
+        const elem1d u = elem_of_order(r / 4);
+        const int pu = r % 4;
+        for (int c = 0; c < nc; ++c) {
+            const elem1d v = elem_of_order(c / (k + 1));
+            const int pv = c % (k + 1);
+            const size_t idx = (size_t)r * nc + c;
+            if (u_v) u_v[idx] = gproduct_volume(1, 0, k, u, pu, v, pv, 0, 0);
+            if (u_vx) u_vx[idx] = gproduct_volume(1, 0, k, u, pu, v, pv, 0, 1);
+            if (uave2_vjp) {
+                const double l = gproduct_edge(1, 0, k, u, pu, v, pv, -1, 1) - gproduct_edge(1, 0, k, u, pu, v, pv, -1, -1);
+                const double rr = gproduct_edge(1, 0, k, u, pu, v, pv, 1, 1) - gproduct_edge(1, 0, k, u, pu, v, pv, 1, -1);
+                uave2_vjp[idx] = l + rr;
+            }
+        }
+    }
+    return 0;
+}
+
+/* 1D element order containing x at level n (x never on a cell boundary) */
+static int order_containing(int n, double x) {
+    if (n == 0) return 0;
+    if (n == 1) return 1;
+    int s = (int)floor(x * (double)(1 << (n - 1)));
+    if (s >= (1 << (n - 1))) s = (1 << (n - 1)) - 1;
+    return (1 << (n - 1)) + s;
+}
+
+/* u_h at every interpolation point of every element, summed directly over
+ * all elements whose support contains the point:  up[e][p], (m+1)^dim per
+ * element.  Same quantity as FastLagrIntp::eval_up_Lagr (FastMultiplyLU.cpp:1362). */
+int amdg_oracle_lagr_point_values(int dim, int N, int k, int64_t E, const int32_t* level, const int32_t* suppt,
+                                  const double* u, double* up) {
+    ehash h;
+    if (ehash_build(&h, dim, N, E, level, suppt)) return -2;
+    const int np = k + 1, B = ipow(np, dim), P = ipow(4, dim);
+#pragma omp parallel for schedule(dynamic, 8)
+    for (int64_t e = 0; e < E; ++e) {
+        for (int p = 0; p < P; ++p) {
+            double x[16];
+            int rem = p;
+            int pd[16];
+            for (int d = dim - 1; d >= 0; --d) { pd[d] = rem % 4; rem /= 4; }
+            for (int d = 0; d < dim; ++d) x[d] = amdg_oracle_lagr_point(level[e * dim + d], suppt[e * dim + d], pd[d]);
+            double val = 0.0;
+            int lv[16] = {0};
+            for (;;) {
+                int o[16];
+                for (int d = 0; d < dim; ++d) o[d] = order_containing(lv[d], x[d]);
+                const int64_t s = ehash_find(&h, pack_key(o, dim, N));
+                if (s >= 0) {
+                    double phi[16][4];
+                    for (int d = 0; d < dim; ++d) {
+                        const elem1d ed = elem_of_order(o[d]);
+                        for (int q = 0; q < np; ++q) phi[d][q] = amdg_oracle_alpert_val(k, ed.n, ed.j, q, 0, x[d], 0);
+                    }
+                    for (int q = 0; q < B; ++q) {
+                        int r2 = q;
+                        double w = 1.0;
+                        int qd[16];
+                        for (int d = dim - 1; d >= 0; --d) { qd[d] = r2 % np; r2 /= np; }
+                        for (int d = 0; d < dim; ++d) w *= phi[d][qd[d]];
+                        val += w * u[s * B + q];
+                    }
+                }
+                int d = dim - 1;
+                while (d >= 0) {
+                    if (++lv[d] <= N) break;
+                    lv[d] = 0;
+                    --d;
+                }
+                if (d < 0) break;
+            }
+            up[e * P + p] = val;
+        }
+    }
+    ehash_free(&h);
+    return 0;
+}
+
+/* Hierarchical surplus of point values, dimension by dimension
+ * (LagrInterpolation::eval_fp_to_coe_D_Lag, Interplation.cpp:1222-1434, with
+ * the weights of set_pts_wts_1d_ada_Lag, :775-888): in pass d every element
+ * with level_d > 0 subtracts the degree-3 interpolant, through the four
+ * coarser-level points inside its dimension-d support, of the values left by
+ * pass d-1.  fp and out are E x 4^dim; fp may equal out. */
+int amdg_oracle_lagr_surplus(int dim, int N, int64_t E, const int32_t* level, const int32_t* suppt, const double* fp,
+                             double* out) {
+    ehash h;
+    if (ehash_build(&h, dim, N, E, level, suppt)) return -2;
+    const int P = ipow(4, dim);
+    double* cur = (double*)malloc((size_t)E * P * sizeof(double));
+    double* nxt = (double*)malloc((size_t)E * P * sizeof(double));
+    if (!cur || !nxt) return -2;
+    memcpy(cur, fp, (size_t)E * P * sizeof(double));
+    for (int d = 0; d < dim; ++d) {
+        int stride = 1;
+        for (int s = d + 1; s < dim; ++s) stride *= 4;
+#pragma omp parallel for schedule(dynamic, 8)
+        for (int64_t e = 0; e < E; ++e) {
+            const int l = level[e * dim + d], j = suppt[e * dim + d];
+            if (l == 0) {
+                memcpy(nxt + e * P, cur + e * P, P * sizeof(double));
+                continue;
+            }
+            /* the four coarser points inside this element's dimension-d support */
+            const double xl = support_lo(l, j), xr = support_hi(l, j);
+            int anc_o[4], anc_q[4];
+            double anc_x[4];
+            int ic = 0;
+            for (int o = 0; o < (1 << l) && ic < 4; ++o) {
+                const elem1d ea = elem_of_order(o);
+                if (ea.n >= l) break;
+                for (int q = 0; q < 4; ++q) {
+                    const double pos = amdg_oracle_lagr_point(ea.n, ea.j, q);
+                    if (pos > xl && pos < xr && ic < 4) {
+                        anc_o[ic] = o;
+                        anc_q[ic] = q;
+                        anc_x[ic] = pos;
+                        ++ic;
+                    }
+                }
+            }
+            /* weight: minus the level-0 Lagrange basis of the ancestor's rank among the
+             * sorted ancestor positions, at this element's own node */
+            int rank[4];
+            for (int a = 0; a < 4; ++a) {
+                rank[a] = 0;
+                for (int b = 0; b < 4; ++b) if (anc_x[b] < anc_x[a]) ++rank[a];
+            }
+            int64_t anc_e[4];
+            for (int a = 0; a < 4; ++a) {
+                int o[16];
+                for (int s = 0; s < dim; ++s) o[s] = order_of_elem(level[e * dim + s], suppt[e * dim + s]);
+                o[d] = anc_o[a];
+                anc_e[a] = ehash_find(&h, pack_key(o, dim, N));
+            }
+            if (ic != 4 || anc_e[0] < 0 || anc_e[1] < 0 || anc_e[2] < 0 || anc_e[3] < 0) continue; /* hole: checked below */
+            for (int p = 0; p < P; ++p) {
+                const int pd = (p / stride) % 4;
+                const int base = p - pd * stride;
+                double c = cur[e * P + p];
+                const double xt = (LAGR_MSH1[pd] + 1.0) / 2.0;
+                for (int a = 0; a < 4; ++a) {
+                    const double wt = -lagr_phi(xt, 0, rank[a]);
+                    c += wt * cur[anc_e[a] * P + base + anc_q[a] * stride];
+                }
+                nxt[e * P + p] = c;
+            }
+        }
+        double* t = cur; cur = nxt; nxt = t;
+    }
+    memcpy(out, cur, (size_t)E * P * sizeof(double));
+    free(cur); free(nxt);
+    ehash_free(&h);
+    return 0;
+}
+
+/* contract a 4^dim block with per-dimension 1D matrices M_s (rows: 4 source
+ * Lagrange indices of the source element, cols: np target Alpert indices)
+ * into a np^dim block, accumulating scale * result into y */
+static void contract_block(int dim, int np, const double* x, const double* const* M, int nc, const int* row0,
+                           const int* col0, double scale, double* y) {
+    double bufA[4096], bufB[4096];
+    const double* src = x;
+    int shape[16];
+    for (int s = 0; s < dim; ++s) shape[s] = 4;
+    double* dst = bufA;
+    for (int s = 0; s < dim; ++s) {
+        /* contract dimension s: size 4 -> np */
+        int outer = 1, inner = 1;
+        for (int r = 0; r < s; ++r) outer *= shape[r];
+        for (int r = s + 1; r < dim; ++r) inner *= shape[r];
+        for (int a = 0; a < outer; ++a)
+            for (int q = 0; q < np; ++q)
+                for (int b = 0; b < inner; ++b) {
+                    double acc = 0.0;
+                    for (int p = 0; p < 4; ++p)
+                        acc += src[(a * 4 + p) * inner + b] * M[s][(size_t)(row0[s] + p) * nc + col0[s] + q];
+                    dst[(a * np + q) * inner + b] = acc;
+                }
+        shape[s] = np;
+        src = dst;
+        dst = (dst == bufA) ? bufB : bufA;
+    }
+    const int B = ipow(np, dim);
+    for (int i = 0; i < B; ++i) y[i] += scale * src[i];
+}
+
+/* Right-hand side of the Lagrange-interpolated Burgers operator with global
+ * Lax-Friedrichs flux, summed directly over element pairs:
+ *   volume   sum_d  <F_d, (u_vx in d, u_v elsewhere)>            (HyperbolicLagrRHS::rhs_vol_scalar)
+ *   interface 0.5 sum_d <F_d, ((ulft+urgt)_vjp in d, u_v elsewhere)> (rhs_flx_intp_scalar)
+ *   penalty  -alpha/2 sum_d ujp_vjp(Alpert) in d                   (HyperbolicAlptRHS::rhs_flx_penalty_scalar)
+ * fucoe: dim x E x 4^dim interpolation coefficients of the flux per dimension. */
+int amdg_oracle_burgers_rhs(int dim, int N, int k, int64_t E, const int32_t* level, const int32_t* suppt,
+                            const double* fucoe, const double* u, double alpha, double* rhs) {
+    const int np = k + 1, B = ipow(np, dim), P = ipow(4, dim), n1 = 1 << N;
+    const int nr = n1 * 4, nc = n1 * np;
+    const long one = 1L << N;
+    double* Lv = (double*)malloc((size_t)nr * nc * sizeof(double));
+    double* Lvx = (double*)malloc((size_t)nr * nc * sizeof(double));
+    double* Lf = (double*)malloc((size_t)nr * nc * sizeof(double));
+    double* ul = (double*)malloc((size_t)nc * nc * sizeof(double));
+    double* ur = (double*)malloc((size_t)nc * nc * sizeof(double));
+    ehash h;
+    if (!Lv || !Lvx || !Lf || !ul || !ur || ehash_build(&h, dim, N, E, level, suppt)) return -2;
+    amdg_oracle_oper1d_lagr(N, k, Lv, Lvx, Lf);
+    amdg_oracle_oper1d(N, k, NULL, NULL, ul, ur);
+    /* 1D relations: vol (supports intersect), flx (intersect, adjacent or periodic-adjacent) */
+    int* volc = (int*)calloc(n1, sizeof(int));
+    int* flxc = (int*)calloc(n1, sizeof(int));
+    int* vol = (int*)malloc((size_t)n1 * n1 * sizeof(int));
+    int* flx = (int*)malloc((size_t)n1 * n1 * sizeof(int));
+    for (int o = 0; o < n1; ++o) {
+        const elem1d eo = elem_of_order(o);
+        long a, b;
+        support_units(eo.n, eo.j, N, &a, &b);
+        for (int oc = 0; oc < n1; ++oc) {
+            const elem1d ec = elem_of_order(oc);
+            long a2, b2;
+            support_units(ec.n, ec.j, N, &a2, &b2);
+            if (!((a >= b2) || (b <= a2))) vol[o * n1 + volc[o]++] = oc;
+            if (intersect_or_adjacent(a, b, a2, b2, one)) flx[o * n1 + flxc[o]++] = oc;
+        }
+    }
+#pragma omp parallel for schedule(dynamic, 4)
+    for (int64_t e = 0; e < E; ++e) {
+        int o[16];
+        for (int s = 0; s < dim; ++s) o[s] = order_of_elem(level[e * dim + s], suppt[e * dim + s]);
+        double* y = rhs + e * B;
+        for (int q = 0; q < B; ++q) y[q] = 0.0;
+        for (int d = 0; d < dim; ++d) {
+            for (int term = 0; term < 2; ++term) {
+                /* term 0: volume, vol sets everywhere; term 1: interface, flx set in d */
+                const double* M[16];
+                for (int s = 0; s < dim; ++s) M[s] = (s == d) ? (term == 0 ? Lvx : Lf) : Lv;
+                const double scale = term == 0 ? 1.0 : 0.5;
+                int idx[16] = {0};
+                for (;;) {
+                    int oc[16], row0[16], col0[16];
+                    for (int s = 0; s < dim; ++s) {
+                        const int use_flx = (term == 1 && s == d);
+                        oc[s] = use_flx ? flx[o[s] * n1 + idx[s]] : vol[o[s] * n1 + idx[s]];
+                        row0[s] = oc[s] * 4;
+                        col0[s] = o[s] * np;
+                    }
+                    const int64_t es = ehash_find(&h, pack_key(oc, dim, N));
+                    if (es >= 0) contract_block(dim, np, fucoe + ((size_t)d * E + es) * P, M, nc, row0, col0, scale, y);
+                    int s = dim - 1;
+                    while (s >= 0) {
+                        const int cnt = (term == 1 && s == d) ? flxc[o[s]] : volc[o[s]];
+                        if (++idx[s] < cnt) break;
+                        idx[s] = 0;
+                        --s;
+                    }
+                    if (s < 0) break;
+                }
+            }
+            /* penalty on Alpert coefficients, same indices in the other dimensions */
+            int stride = 1;
+            for (int s = d + 1; s < dim; ++s) stride *= np;
+            int o2[16];
+            memcpy(o2, o, sizeof(int) * dim);
+            for (int i = 0; i < flxc[o[d]]; ++i) {
+                o2[d] = flx[o[d] * n1 + i];
+                const int64_t es = ehash_find(&h, pack_key(o2, dim, N));
+                if (es < 0) continue;
+                for (int q = 0; q < B; ++q) {
+                    const int qd = (q / stride) % np, base = q - qd * stride;
+                    double acc = 0.0;
+                    for (int p = 0; p < np; ++p) {
+                        const size_t mi = (size_t)(o2[d] * np + p) * nc + o[d] * np + qd;
+                        acc += (ur[mi] - ul[mi]) * u[es * B + base + p * stride];
+                    }
+                    y[q] += -alpha / 2.0 * acc;
+                }
+            }
+        }
+    }
+    free(Lv); free(Lvx); free(Lf); free(ul); free(ur);
+    free(volc); free(flxc); free(vol); free(flx);
+    ehash_free(&h);
+    return 0;
+}

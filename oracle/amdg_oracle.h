@@ -71,6 +71,21 @@ void amdg_oracle_linop_destroy(void* handle);
 double amdg_oracle_l2_error_split(int dim, int N, int k, int64_t E, const int32_t* level, const int32_t* suppt,
                                   const double* u, const double* coef1d_exact, double l2_norm_exact);
 
+/* ---- Lagrange interpolation path (degree-3 hierarchical Lagrange, msh_case 1) ---- */
+double amdg_oracle_lagr_val(int level, int suppt, int p, double x, int sgn);
+double amdg_oracle_lagr_point(int level, int suppt, int p);
+/* Lagrange (rows) x Alpert (cols) 1D matrices: u_v, u_vx, ulft_vjp + urgt_vjp. */
+int amdg_oracle_oper1d_lagr(int N, int k, double* u_v, double* u_vx, double* uave2_vjp);
+/* u_h at every interpolation point (E x 4^dim). */
+int amdg_oracle_lagr_point_values(int dim, int N, int k, int64_t E, const int32_t* level, const int32_t* suppt,
+                                  const double* u, double* up);
+/* Hierarchical surplus of point values (E x 4^dim). */
+int amdg_oracle_lagr_surplus(int dim, int N, int64_t E, const int32_t* level, const int32_t* suppt, const double* fp,
+                             double* out);
+/* Burgers right-hand side from flux interpolation coefficients (dim x E x 4^dim) and u. */
+int amdg_oracle_burgers_rhs(int dim, int N, int k, int64_t E, const int32_t* level, const int32_t* suppt,
+                            const double* fucoe, const double* u, double alpha, double* rhs);
+
 #ifdef __cplusplus
 }
 #endif

@@ -55,6 +55,15 @@ def lib():
         L.amdg_oracle_linop_destroy.argtypes = [C.c_void_p]
         L.amdg_oracle_l2_error_split.restype = C.c_double
         L.amdg_oracle_l2_error_split.argtypes = [C.c_int, C.c_int, C.c_int, C.c_int64, i32p, i32p, f64p, f64p, C.c_double]
+        L.amdg_oracle_lagr_val.restype = C.c_double
+        L.amdg_oracle_lagr_val.argtypes = [C.c_int, C.c_int, C.c_int, C.c_double, C.c_int]
+        L.amdg_oracle_lagr_point.restype = C.c_double
+        L.amdg_oracle_lagr_point.argtypes = [C.c_int, C.c_int, C.c_int]
+        L.amdg_oracle_oper1d_lagr.argtypes = [C.c_int, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p]
+        L.amdg_oracle_lagr_point_values.argtypes = [C.c_int, C.c_int, C.c_int, C.c_int64, i32p, i32p, f64p, f64p]
+        L.amdg_oracle_lagr_surplus.argtypes = [C.c_int, C.c_int, C.c_int64, i32p, i32p, f64p, f64p]
+        L.amdg_oracle_burgers_rhs.argtypes = [C.c_int, C.c_int, C.c_int, C.c_int64, i32p, i32p, f64p, f64p, C.c_double,
+                                              f64p]
         _lib = L
     return _lib
 
@@ -179,4 +188,53 @@ def sin_sum_terms(dim, shift=0.0):
             return sign * v if d == 0 else v
 
         terms.append(f)
+    return terms
+
+
+def lagr_point_values(dim, N, k, level, suppt, u):
+    up = np.zeros((level.shape[0], 4 ** dim))
+    _check(lib().amdg_oracle_lagr_point_values(dim, N, k, level.shape[0], level, suppt, np.ascontiguousarray(u), up))
+    return up
+
+
+def lagr_surplus(dim, N, level, suppt, fp):
+    out = np.zeros_like(fp)
+    _check(lib().amdg_oracle_lagr_surplus(dim, N, level.shape[0], level, suppt, np.ascontiguousarray(fp), out))
+    return out
+
+
+def burgers_rhs(dim, N, k, level, suppt, u, alpha):
+    """Full Burgers RHS: point values -> flux u^2/2 -> surplus -> volume/interface/penalty terms."""
+    up = lagr_point_values(dim, N, k, level, suppt, u)
+    fp = 0.5 * up * up
+    fu = lagr_surplus(dim, N, level, suppt, fp)
+    fucoe = np.ascontiguousarray(np.broadcast_to(fu, (dim,) + fu.shape))
+    rhs = np.zeros_like(u)
+    _check(lib().amdg_oracle_burgers_rhs(dim, N, k, level.shape[0], level, suppt, fucoe, np.ascontiguousarray(u),
+                                         float(alpha), rhs))
+    return rhs, up, fu
+
+
+def burgers_rk3(dim, N, k, level, suppt, u, alpha, dt, steps):
+    """SSP-RK3 stages with step_stage semantics (ODESolver.cpp:285-301)."""
+    un = np.array(u, np.float64, copy=True)
+    for _ in range(steps):
+        cur = un.copy()
+        for stage in range(3):
+            rhs = burgers_rhs(dim, N, k, level, suppt, cur, alpha)[0]
+            if stage == 0:
+                cur = un + dt * rhs
+            elif stage == 1:
+                cur = 3. / 4. * un + 1. / 4. * (cur + dt * rhs)
+            else:
+                cur = 1. / 3. * un + 2. / 3. * (cur + dt * rhs)
+        un = cur
+    return un
+
+
+def burgers_ic_terms(dim):
+    """0.5 + 0.25 sin(2 pi sum x) as separable terms."""
+    terms = [lambda x, d: 0.5 if d == 0 else 1.0]
+    for f in sin_sum_terms(dim):
+        terms.append(lambda x, d, f=f: (0.25 if d == 0 else 1.0) * f(x, d))
     return terms

@@ -13,6 +13,14 @@
 //              matfree   -> FastRHS::transform_ucoe_alpt_to_rhs per dim with
 //                           c_d*(u_vx + ulft_vjp | urgt_vjp) on the "flx" sets,
 //                           RK3SSP::step_stage (the 4D/6D CPU baseline path)
+//   ref_harness burgers <dim> <N> <alpha> <steps> <dt>
+//     u_t + sum_d (u^2/2)_{x_d} = 0, u0 = 0.5 + 0.25 sin(2 pi sum x_d), Alpert k=2,
+//     Lagrange degree 3 (msh_case 1) interpolation of the flux
+//     (LagrInterpolation::nonlinear_Lagr_fast), HyperbolicLagrRHS volume and
+//     interface terms, HyperbolicAlptRHS::rhs_flx_penalty_scalar(alpha), RK3SSP
+//     step_stage, sparse grid without adaptivity (07_vlasov_maxwell_adapt.cpp
+//     stage loop).  Dumps u0, up0 (point values), fu0_d (interpolation
+//     coefficients of the flux in dimension d), rhs0 and uT.
 //   ref_harness matrices <N> <k>
 //     dumps the 1D operator matrices u_v, u_vx, ulft_vjp, urgt_vjp.
 //
@@ -70,6 +78,21 @@ void dump_elements(const char* name, DGSolution& dg, int which) {
         for (int d = 0; d < dim; ++d) std::printf("%d ", e.level[d]);
         for (int d = 0; d < dim; ++d) std::printf("%d ", e.suppt[d]);
         const VecMultiD<double>& v = (which == 0) ? e.ucoe_alpt[0] : e.rhs[0];
+        for (int i = 0; i < nb; ++i) std::printf("%.17g ", v.at(i));
+        std::printf("\n");
+    }
+    std::printf("END\n");
+}
+
+void dump_elements_vec(const char* name, DGSolution& dg, const std::function<const VecMultiD<double>&(const Element&)>& get) {
+    const int dim = DGSolution::DIM;
+    const int nb = (int)get(dg.dg.begin()->second).get_index_iterator().size();
+    std::printf("BEGIN %s %zu %d\n", name, dg.dg.size(), 2 * dim + nb);
+    for (auto& it : dg.dg) {
+        const Element& e = it.second;
+        for (int d = 0; d < dim; ++d) std::printf("%d ", e.level[d]);
+        for (int d = 0; d < dim; ++d) std::printf("%d ", e.suppt[d]);
+        const VecMultiD<double>& v = get(e);
         for (int i = 0; i < nb; ++i) std::printf("%.17g ", v.at(i));
         std::printf("\n");
     }
@@ -212,6 +235,82 @@ int run_linear(int argc, char** argv) {
     return 0;
 }
 
+int run_burgers(int argc, char** argv) {
+    if (argc < 7) { std::fprintf(stderr, "burgers: bad args\n"); return 2; }
+    const int dim = std::atoi(argv[2]);
+    const int N = std::atoi(argv[3]);
+    const double alpha = std::atof(argv[4]);
+    const int steps = std::atoi(argv[5]);
+    const double dt = std::atof(argv[6]);
+    const int k = 2;
+    set_statics(dim, k);
+    Hash hash;
+    LagrBasis::set_interp_msh01();
+    HermBasis::set_interp_msh01();
+    AllBasis<AlptBasis> all_bas_alpt(N);
+    AllBasis<LagrBasis> all_bas_lagr(N);
+    AllBasis<HermBasis> all_bas_herm(N);
+    OperatorMatrix1D<AlptBasis, AlptBasis> oper_alpt(all_bas_alpt, all_bas_alpt, "period");
+    OperatorMatrix1D<LagrBasis, AlptBasis> oper_lagr(all_bas_lagr, all_bas_alpt, "period");
+    DGAdapt dg(true, N, N, all_bas_alpt, all_bas_lagr, all_bas_herm, hash, 1e10, -1, true, false);
+
+    const double PI = Const::PI;
+    std::vector<std::function<double(double, int)>> funcs;
+    funcs.push_back([](double, int d) { return d == 0 ? 0.5 : 1.0; });
+    for (int mask = 0; mask < (1 << dim); ++mask) {
+        int nsin = __builtin_popcount(mask);
+        if (nsin % 2 == 0) continue;
+        const double sign = ((nsin - 1) / 2) % 2 == 0 ? 0.25 : -0.25;
+        funcs.push_back([=](double x, int d) {
+            double v = ((mask >> d) & 1) ? std::sin(2 * PI * x) : std::cos(2 * PI * x);
+            return d == 0 ? sign * v : v;
+        });
+    }
+    dg.init_separable_scalar_sum(funcs);
+    std::printf("META dim=%d N=%d k=%d sparse=1 elements=%zu dof=%d\n", dim, N, k, dg.dg.size(), dg.get_dof());
+    dump_elements("u0", dg, 0);
+
+    auto flux = [](std::vector<double> u, int, int) -> double { return FluxFunction::burgers_flux_scalar(u[0]); };
+    std::vector<std::vector<bool>> is_intp(1, std::vector<bool>(dim, true));
+    LagrInterpolation interp(dg);
+    FastLagrIntp fast_lagr(dg, interp.Lag_pt_Alpt_1D, interp.Lag_pt_Alpt_1D_d1);
+    HyperbolicLagrRHS rhs_lagr(dg, oper_lagr);
+    HyperbolicAlptRHS rhs_alpt(dg, oper_alpt);
+    const std::vector<double> lxf(dim, alpha);
+    auto rhs_eval = [&]() {
+        interp.nonlinear_Lagr_fast(flux, is_intp, fast_lagr);
+        dg.set_rhs_zero();
+        rhs_lagr.rhs_vol_scalar();
+        rhs_lagr.rhs_flx_intp_scalar();
+        rhs_alpt.rhs_flx_penalty_scalar(lxf);
+    };
+    rhs_eval();
+    dump_elements_vec("up0", dg, [](const Element& e) -> const VecMultiD<double>& { return e.up_intp[0]; });
+    for (int d = 0; d < dim; ++d) {
+        char nm[32];
+        std::snprintf(nm, sizeof nm, "fu0_%d", d);
+        dump_elements_vec(nm, dg, [d](const Element& e) -> const VecMultiD<double>& { return e.fucoe_intp[0][d]; });
+    }
+    dump_elements("rhs0", dg, 1);
+    auto t0 = std::chrono::steady_clock::now();
+    for (int s = 0; s < steps; ++s) {
+        RK3SSP ode(dg, dt);
+        ode.init();
+        for (int stage = 0; stage < 3; ++stage) {
+            rhs_eval();
+            ode.set_rhs_zero();
+            ode.add_rhs_to_eigenvec();
+            ode.step_stage(stage);
+            ode.final();
+        }
+    }
+    auto t1 = std::chrono::steady_clock::now();
+    dump_elements("uT", dg, 0);
+    std::printf("TIME evolve_s=%.9g dof_stage=%.17g\n", std::chrono::duration<double>(t1 - t0).count(),
+                3.0 * steps * dg.get_dof());
+    return 0;
+}
+
 int run_matrices(int argc, char** argv) {
     if (argc < 4) return 2;
     const int N = std::atoi(argv[2]);
@@ -233,6 +332,7 @@ int main(int argc, char** argv) {
     const std::string mode = argv[1];
     if (mode == "linear") return run_linear(argc, argv);
     if (mode == "matrices") return run_matrices(argc, argv);
+    if (mode == "burgers") return run_burgers(argc, argv);
     std::fprintf(stderr, "unknown mode %s\n", mode.c_str());
     return 2;
 }

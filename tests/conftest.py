@@ -18,4 +18,3 @@ def ctx():
     import amdg
     c = amdg.Context(0)
     yield c
-    c.close()

@@ -71,6 +71,14 @@ LINEAR_CASES = [
 ]
 
 
+# (name, dim, N, alpha, steps, dt): Lagrange-interpolated Burgers, LxF, SSP-RK3
+BURGERS_CASES = [
+    ("burgers2d_n4", 2, 4, 1.1, 2, 0.002),
+    ("burgers3d_n4", 3, 4, 0.825, 2, 0.001),
+    ("burgers3d_n5", 3, 5, 0.825, 1, 0.0005),
+]
+
+
 def main():
     if not os.path.exists(HARNESS):
         sys.exit("build the reference first: make -C oracle ref")
@@ -84,6 +92,18 @@ def main():
         np.savez_compressed(os.path.join(HERE, name + ".npz"), level=lv, suppt=sp, u0=u0, rhs0=rhs0, uT=uT,
                             l2err=np.float64(r.get("l2err", np.nan)))
         manifest[name] = dict(kind="linear", dim=dim, N=N, k=k, ic=ic, engine=engine, steps=steps, dt=dt, c=c,
+                              elements=int(r["meta"]["elements"]))
+        print(name, r["meta"])
+    for name, dim, N, alpha, steps, dt in BURGERS_CASES:
+        r = run(["burgers", dim, N, repr(alpha), steps, repr(dt)])
+        lv, sp, u0 = split_elements(r["u0"], dim)
+        arrs = {"level": lv, "suppt": sp, "u0": u0}
+        for key in ["up0", "rhs0", "uT"] + [f"fu0_{d}" for d in range(dim)]:
+            lv2, sp2, v = split_elements(r[key], dim)
+            assert (lv == lv2).all() and (sp == sp2).all()
+            arrs[key] = v
+        np.savez_compressed(os.path.join(HERE, name + ".npz"), **arrs)
+        manifest[name] = dict(kind="burgers", dim=dim, N=N, k=2, alpha=alpha, steps=steps, dt=dt,
                               elements=int(r["meta"]["elements"]))
         print(name, r["meta"])
     for N, k in [(4, 2), (3, 1), (3, 3)]:

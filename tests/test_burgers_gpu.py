@@ -1,0 +1,90 @@
+"""Parity of the CUDA Lagrange-interpolation path (Burgers flux, LxF) with the
+reference fixtures and the oracle.  Tolerances: FP64 1e-12 relative to the
+field's max norm for point values, flux coefficients and RK3 steps, 5e-12 for
+one RHS (a difference of larger volume and interface terms); mixed mode
+(FP32 transforms, FP64 state) 1e-5 for one RHS and 1e-6 for RK3 steps."""
+import numpy as np
+import pytest
+
+import amdg
+import amdg_oracle as O
+from helpers import align, golden, manifest, rel_err
+
+pytestmark = pytest.mark.gpu
+torch = pytest.importorskip("torch")
+
+BURGERS = [n for n, m in manifest().items() if m["kind"] == "burgers"]
+
+
+def dev(n):
+    return torch.zeros(n, dtype=torch.float64, device="cuda")
+
+
+def run_on(ctx, fn, u, nout):
+    """Copy u to the device, call fn(d_u, d_out), return the output on the host."""
+    torch.cuda.synchronize()
+    du = torch.from_numpy(np.ascontiguousarray(u).reshape(-1)).cuda()
+    out = dev(nout)
+    torch.cuda.synchronize()
+    fn(du.data_ptr(), out.data_ptr())
+    ctx.synchronize()
+    return out.cpu().numpy()
+
+
+@pytest.mark.parametrize("name", BURGERS)
+def test_burgers_matches_reference(ctx, name):
+    m = manifest()[name]
+    z = golden(name)
+    dim, N, k = m["dim"], m["N"], m["k"]
+    g = amdg.Grid(ctx, dim, N, k)
+    lv, sp = g.elements()
+    perm = align(z["level"], z["suppt"], lv, sp)
+    g.init_separable(O.burgers_ic_terms(dim))
+    assert rel_err(g.coefficients(), z["u0"][perm]) < 1e-13
+    u0 = np.ascontiguousarray(z["u0"][perm])
+    op = amdg.BurgersOperator(g, m["alpha"])
+    P = 4 ** dim
+    up = run_on(ctx, op.point_values_device, u0, g.num_elements * P).reshape(-1, P)
+    assert rel_err(up, z["up0"][perm]) < 1e-12
+    fu = run_on(ctx, op.flux_coefficients_device, u0, g.num_elements * P).reshape(-1, P)
+    assert rel_err(fu, z["fu0_0"][perm]) < 1e-12
+    rhs = run_on(ctx, op.rhs_device, u0, g.dof).reshape(-1, g.block)
+    assert rel_err(rhs, z["rhs0"][perm]) < 5e-12
+    rhs32 = run_on(ctx, lambda a, b: op.rhs_device(a, b, amdg.MIXED), u0, g.dof).reshape(-1, g.block)
+    assert rel_err(rhs32, z["rhs0"][perm]) < 1e-5
+    g.set_coefficients(u0)
+    op.rk3_steps(m["dt"], m["steps"], amdg.FP64)
+    ctx.synchronize()
+    assert rel_err(g.coefficients(), z["uT"][perm]) < 1e-12
+    g.set_coefficients(u0)
+    op.rk3_steps(m["dt"], m["steps"], amdg.MIXED)
+    ctx.synchronize()
+    assert rel_err(g.coefficients(), z["uT"][perm]) < 1e-6
+    op.close()
+    g.close()
+
+
+def test_burgers_3d_n6_matches_oracle(ctx):
+    dim, N, k, alpha = 3, 6, 2, 0.825
+    g = amdg.Grid(ctx, dim, N, k)
+    lv, sp = g.elements()
+    g.init_separable(O.burgers_ic_terms(dim))
+    u0 = g.coefficients().copy()
+    op = amdg.BurgersOperator(g, alpha)
+    rhs = run_on(ctx, op.rhs_device, u0, g.dof).reshape(-1, g.block)
+    ref, _, _ = O.burgers_rhs(dim, N, k, lv, sp, u0, alpha)
+    assert rel_err(rhs, ref) < 5e-12
+    op.close()
+    g.close()
+
+
+def test_burgers_rhs_deterministic_and_hole_detection(ctx):
+    g = amdg.Grid(ctx, 2, 5, 2)
+    g.init_separable(O.burgers_ic_terms(2))
+    u0 = g.coefficients().copy()
+    op = amdg.BurgersOperator(g, 1.0)
+    a = run_on(ctx, op.rhs_device, u0, g.dof)
+    b = run_on(ctx, op.rhs_device, u0, g.dof)
+    assert np.array_equal(a, b)
+    op.close()
+    g.close()

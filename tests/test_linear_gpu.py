@@ -21,12 +21,10 @@ TOL_MIXED_STEP = 1e-6
 
 def _device_apply(ctx, op, grid, u, prec):
     """rhs = L u through the C-ABI, using the grid's state buffer as input."""
-    import ctypes as C
     grid.set_coefficients(u)
     keep = grid.coefficients().copy()
-    lib = amdg.load()
     # second device buffer: a scratch grid of the same shape holds the rhs
-    out = amdg.Grid(ctx, grid.dim, grid.nmax, grid.k)
+    out = amdg.Grid(ctx, grid.dim, grid.nmax, grid.k, grid.sparse)
     op.apply_device(grid.device_ptr(), out.device_ptr(), prec)
     ctx.synchronize()
     rhs = out.coefficients().copy()
@@ -121,10 +119,11 @@ def test_6d_n8_sampled_parity_and_properties(ctx):
     ctx.synchronize()
     rhs = out.coefficients().copy()
     oop = O.LinearOp(dim, N, k, lv, sp, c)
+    scale = np.abs(rhs).max()  # relative to the field's max norm, as for the smaller cases
     for e0 in (0, 1000, 23000, 47000):
         e1 = min(e0 + 264, g.num_elements)
         ref = oop.apply_range(u0, e0, e1)
-        assert rel_err(rhs[e0:e1], ref) < TOL64
+        assert np.abs(rhs[e0:e1] - ref).max() < TOL64 * scale
     # determinism: a second apply is bitwise identical
     op.apply_device(g.device_ptr(), out.device_ptr(), amdg.FP64)
     ctx.synchronize()
@@ -148,7 +147,9 @@ def test_6d_n8_sampled_parity_and_properties(ctx):
     err = g.l2_error_separable(lambda x, d: math.sin(2 * math.pi * (x - T)), 0.5 ** 3)
     err0_ex = O.project_separable(N, k, dim, [lambda x, d: math.sin(2 * math.pi * (x - T))])[0]
     ref_err = O.l2_error_split(dim, N, k, lv, sp, dev, err0_ex, 0.5 ** 3)
-    assert abs(err - ref_err) <= 1e-9 * ref_err
+    # the split formula sqrt(|u|^2 + sum(u_h^2 - 2 u_h c)) cancels ~0.125 down to err^2 ~ 4e-9,
+    # so summation order alone moves err by ~1e-7 relative
+    assert abs(err - ref_err) <= 1e-6 * ref_err
     oop.close()
     out.close()
     op.close()

@@ -98,3 +98,38 @@ def test_constant_mode_is_conserved():
     rhs = O.linear_rhs(dim, N, k, lv, sp, [1.0, 1.0], u)
     root = np.where((lv == 0).all(axis=1))[0][0]
     assert abs(rhs[root, 0]) < 1e-10
+
+
+BURGERS = [n for n, m in manifest().items() if m["kind"] == "burgers"]
+
+
+@pytest.mark.parametrize("name", BURGERS)
+def test_burgers_lagrange_path_matches_reference(name):
+    """Point values, flux interpolation coefficients, RHS and RK3 steps of the
+    Lagrange-interpolated Burgers operator against the reference's fast LU path."""
+    m = manifest()[name]
+    z = golden(name)
+    dim, N, k = m["dim"], m["N"], m["k"]
+    lv, sp = O.grid(dim, N)
+    perm = align(z["level"], z["suppt"], lv, sp)
+    coef = O.project_separable(N, k, dim, O.burgers_ic_terms(dim))
+    u0 = O.init_separable(dim, N, k, lv, sp, coef)
+    assert rel_err(u0, z["u0"][perm]) < 1e-13
+    u0 = np.ascontiguousarray(z["u0"][perm])
+    rhs, up, fu = O.burgers_rhs(dim, N, k, lv, sp, u0, m["alpha"])
+    assert rel_err(up, z["up0"][perm]) < 1e-13
+    for d in range(dim):
+        assert rel_err(fu, z[f"fu0_{d}"][perm]) < 1e-12
+    assert rel_err(rhs, z["rhs0"][perm]) < 5e-12
+    uT = O.burgers_rk3(dim, N, k, lv, sp, u0, m["alpha"], m["dt"], m["steps"])
+    assert rel_err(uT, z["uT"][perm]) < 1e-12
+
+
+def test_lagrange_basis_interpolates_its_nodes():
+    # hierarchical Lagrange basis: 1 at its own node, 0 at the other nodes of its element
+    for n, j in [(0, 1), (1, 1), (2, 1), (2, 3), (3, 5)]:
+        for p in range(4):
+            for q in range(4):
+                x = O.lib().amdg_oracle_lagr_point(n, j, q)
+                v = O.lib().amdg_oracle_lagr_val(n, j, p, x, 0)
+                assert abs(v - (1.0 if p == q else 0.0)) < 1e-13
