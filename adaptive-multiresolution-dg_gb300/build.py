@@ -54,6 +54,21 @@ def compile_one(src: str) -> str:
     return obj
 
 
+def build_examples() -> list[str]:
+    """C++ drivers written against host/amdg_dg.hpp, linked to the library."""
+    ex_dir = os.path.join(PKG, "examples")
+    outs = []
+    for src in sorted(f for f in os.listdir(ex_dir) if f.endswith(".cpp")):
+        exe = os.path.join(LIB_DIR, src[:-4])
+        cmd = ["g++", "-std=c++17", "-O2", "-I", os.path.join(ROOT, "include"), "-I", os.path.join(PKG, "host"),
+               os.path.join(ex_dir, src), "-o", exe, "-L", LIB_DIR, "-lamdg_gb300", f"-Wl,-rpath,{LIB_DIR}"]
+        res = subprocess.run(cmd, capture_output=True, text=True)
+        if res.returncode != 0:
+            raise RuntimeError(f"example build failed: {' '.join(cmd)}\n{res.stderr}")
+        outs.append(exe)
+    return outs
+
+
 def build(verbose: bool = False) -> str:
     os.makedirs(OBJ, exist_ok=True)
     os.makedirs(LIB_DIR, exist_ok=True)
@@ -64,6 +79,7 @@ def build(verbose: bool = False) -> str:
     res = subprocess.run(cmd, capture_output=True, text=True)
     if res.returncode != 0:
         raise RuntimeError(f"link failed: {' '.join(cmd)}\n{res.stdout}\n{res.stderr}")
+    build_examples()
     if verbose:
         print("built", LIB)
     return LIB

@@ -1,0 +1,166 @@
+// Adaptivity on the flattened element table: refine, coarsen and hole
+// filling on packed keys (DGAdapt::refine DGAdapt.cpp:371-404, coarsen
+// :675-688,982-1016, check_hole :1351-1385, child/parent index rules
+// :1250-1312), and the adaptive separable initialisation
+// (DGAdapt::init_separable_scalar_sum, :120-147, 850-894).
+//
+// Keys pack the 1D orders of an element, nmax bits per dimension, first
+// dimension most significant.  In 1D order space the children of o are
+// {1} for o = 0, {2o, 2o+1} for 1 <= level < nmax and none at level nmax; the
+// parent of o >= 1 is 0 for o = 1 and o/2 otherwise.
+#include <algorithm>
+#include <cmath>
+#include <unordered_set>
+
+#include "amdg_internal.hpp"
+
+namespace amdg {
+namespace {
+
+inline int field(uint64_t key, int d, int dim, int nmax) {
+    const uint64_t mask = nmax == 0 ? 0 : ((uint64_t(1) << nmax) - 1);
+    return int((key >> (uint64_t(nmax) * (dim - 1 - d))) & mask);
+}
+
+inline uint64_t with_field(uint64_t key, int d, int dim, int nmax, int o) {
+    const uint64_t shift = uint64_t(nmax) * (dim - 1 - d);
+    const uint64_t mask = (nmax == 0 ? 0 : ((uint64_t(1) << nmax) - 1)) << shift;
+    return (key & ~mask) | (uint64_t(o) << shift);
+}
+
+int children_1d(int o, int nmax, int* out) {
+    const int n = level_of_order(o);
+    if (n == 0) { out[0] = 1; return nmax >= 1 ? 1 : 0; }
+    if (n == nmax) return 0;
+    out[0] = 2 * o;
+    out[1] = 2 * o + 1;
+    return 2;
+}
+
+void fill_holes(std::unordered_set<uint64_t>* set, std::vector<uint64_t> work, int dim, int nmax) {
+    while (!work.empty()) {
+        std::vector<uint64_t> next;
+        for (uint64_t key : work)
+            for (int d = 0; d < dim; ++d) {
+                const int o = field(key, d, dim, nmax);
+                if (o == 0) continue;
+                const uint64_t p = with_field(key, d, dim, nmax, o == 1 ? 0 : o / 2);
+                if (set->insert(p).second) next.push_back(p);
+            }
+        work.swap(next);
+    }
+}
+
+}  // namespace
+
+std::vector<uint64_t> refine_keys(const HostGrid& g, const double* norms, double eps) {
+    const int dim = g.dim, nmax = g.nmax;
+    std::unordered_set<uint64_t> present(g.key.begin(), g.key.end());
+    std::unordered_set<uint64_t> out(present);
+    std::vector<uint64_t> added;
+    int ch[2];
+    for (int64_t e = 0; e < g.num_elements; ++e) {
+        const uint64_t key = g.key[e];
+        int total = 0, existing = 0;
+        for (int d = 0; d < dim; ++d) {
+            const int nc = children_1d(field(key, d, dim, nmax), nmax, ch);
+            total += nc;
+            for (int c = 0; c < nc; ++c) existing += present.count(with_field(key, d, dim, nmax, ch[c])) ? 1 : 0;
+        }
+        // a leaf has fewer existing children than possible (DGAdapt::update_leaf)
+        if (existing >= total || !(norms[e] > eps)) continue;
+        for (int d = 0; d < dim; ++d) {
+            const int nc = children_1d(field(key, d, dim, nmax), nmax, ch);
+            for (int c = 0; c < nc; ++c) {
+                const uint64_t ck = with_field(key, d, dim, nmax, ch[c]);
+                if (out.insert(ck).second) added.push_back(ck);
+            }
+        }
+    }
+    fill_holes(&out, added, dim, nmax);
+    std::vector<uint64_t> keys(out.begin(), out.end());
+    std::sort(keys.begin(), keys.end());
+    return keys;
+}
+
+std::vector<uint64_t> coarsen_keys(const HostGrid& g, const double* norms, double eta) {
+    const int dim = g.dim, nmax = g.nmax;
+    const int64_t E = g.num_elements;
+    std::vector<char> alive(E, 1);
+    // existing-children counts, kept up to date as elements are removed
+    std::vector<int> kids(E, 0);
+    auto index_of = [&](uint64_t k) -> int64_t {
+        auto it = std::lower_bound(g.key.begin(), g.key.end(), k);
+        return (it != g.key.end() && *it == k) ? int64_t(it - g.key.begin()) : -1;
+    };
+    std::vector<std::vector<int64_t>> parents(E);
+    for (int64_t e = 0; e < E; ++e)
+        for (int d = 0; d < dim; ++d) {
+            const int o = field(g.key[e], d, dim, nmax);
+            if (o == 0) continue;
+            const int64_t p = index_of(with_field(g.key[e], d, dim, nmax, o == 1 ? 0 : o / 2));
+            if (p >= 0) { parents[e].push_back(p); ++kids[p]; }
+        }
+    auto removable = [&](int64_t e) {
+        if (!alive[e] || kids[e] != 0 || !(norms[e] < eta)) return false;
+        int maxlev = 0;
+        for (int d = 0; d < dim; ++d) maxlev = std::max(maxlev, level_of_order(field(g.key[e], d, dim, nmax)));
+        return maxlev > 0;
+    };
+    // repeated sweeps over childless elements until nothing changes (DGAdapt::coarsen_no_leaf)
+    std::vector<int64_t> work;
+    for (int64_t e = 0; e < E; ++e) if (removable(e)) work.push_back(e);
+    while (!work.empty()) {
+        std::vector<int64_t> next;
+        for (int64_t e : work) {
+            if (!removable(e)) continue;
+            alive[e] = 0;
+            for (int64_t p : parents[e]) {
+                if (--kids[p] == 0 && removable(p)) next.push_back(p);
+            }
+        }
+        work.swap(next);
+    }
+    std::vector<uint64_t> keys;
+    for (int64_t e = 0; e < E; ++e) if (alive[e]) keys.push_back(g.key[e]);
+    return keys;
+}
+
+void grid_from_keys(int dim, int nmax, int k, std::vector<uint64_t> keys, HostGrid* g) {
+    std::sort(keys.begin(), keys.end());
+    keys.erase(std::unique(keys.begin(), keys.end()), keys.end());
+    g->dim = dim;
+    g->nmax = nmax;
+    g->k = k;
+    g->key = std::move(keys);
+    g->num_elements = int64_t(g->key.size());
+    g->order.resize(size_t(g->num_elements) * dim);
+    for (int64_t e = 0; e < g->num_elements; ++e)
+        for (int d = 0; d < dim; ++d) g->order[size_t(e) * dim + d] = field(g->key[e], d, dim, nmax);
+}
+
+void element_separable_norms(const HostGrid& g, const std::vector<double>& coef1d, int nterms, std::vector<double>* norms) {
+    const int dim = g.dim, np = g.k + 1, nb1 = (1 << g.nmax) * np;
+    int B = 1;
+    for (int d = 0; d < dim; ++d) B *= np;
+    norms->assign(g.num_elements, 0.0);
+    for (int64_t e = 0; e < g.num_elements; ++e) {
+        double s = 0.0;
+        for (int q = 0; q < B; ++q) {
+            int dig[kMaxDim];
+            int rem = q;
+            for (int d = dim - 1; d >= 0; --d) { dig[d] = rem % np; rem /= np; }
+            double v = 0.0;
+            for (int t = 0; t < nterms; ++t) {
+                double p = 1.0;
+                for (int d = 0; d < dim; ++d)
+                    p *= coef1d[(size_t(t) * dim + d) * nb1 + g.order[size_t(e) * dim + d] * np + dig[d]];
+                v += p;
+            }
+            s += v * v;
+        }
+        (*norms)[e] = std::sqrt(s);
+    }
+}
+
+}  // namespace amdg

@@ -73,6 +73,7 @@ struct LagrTables {
 double lagr_eval(int order, double x, int sgn);
 double lagr_point(int o, int p);
 void build_lagr_tables(const Basis1D& alpt, LagrTables* t);
+void build_lagr_ancestors(const Basis1D& alpt, LagrTables* t);  // anc_order/anc_point/anc_rank only
 // dimension orders and L(0)/full(1)/U(2) tags of the 2^(dim-1) partial sums
 void transform_schedule(int dim, std::vector<std::vector<int>>* dim_order, std::vector<std::vector<int>>* lu);
 
@@ -83,8 +84,15 @@ struct HostGrid {
     std::vector<int32_t> order;  // num_elements x dim, 1D element orders, sorted lexicographically
     std::vector<uint64_t> key;   // packed orders (nmax bits per dimension), ascending
 };
-void build_grid(int dim, int nmax, int sparse, HostGrid* g);
+void build_grid(int dim, int nmax, int sparse, HostGrid* g, int level_init = -1);
 int64_t find_element(const HostGrid& g, const int32_t* orders);  // binary search, -1 if absent
+
+// Adaptivity on packed keys (one refine pass with hole filling; repeated coarsening).
+std::vector<uint64_t> refine_keys(const HostGrid& g, const double* norms, double eps);
+std::vector<uint64_t> coarsen_keys(const HostGrid& g, const double* norms, double eta);
+void grid_from_keys(int dim, int nmax, int k, std::vector<uint64_t> keys, HostGrid* g);
+// element norms of the separable expansion sum_t prod_d coef1d[t][d] (host, same arithmetic order as the device init)
+void element_separable_norms(const HostGrid& g, const std::vector<double>& coef1d, int nterms, std::vector<double>* norms);
 
 // Matrix-free linear operator topology: for every (element, dimension) the
 // neighbours whose 1D block is nonzero, and the deduplicated 1D blocks.
@@ -120,6 +128,8 @@ struct amdg_context {
 };
 
 struct amdg_grid {
+    int64_t version = 0;             // bumped whenever the element set changes
+    int64_t capacity = 0;            // elements the device arrays can hold
     amdg_context* ctx = nullptr;
     int device = 0;                  // kept so destroy never dereferences ctx
     amdg::HostGrid host;
@@ -132,6 +142,8 @@ struct amdg_grid {
 };
 
 struct amdg_linear_op {
+    int64_t built_version = -1;      // grid version the topology was built for
+    int64_t capacity = 0;            // dof the stage vectors can hold
     amdg_grid* grid = nullptr;
     int device = 0;                  // kept so destroy never dereferences grid
     std::vector<double> coef;
@@ -148,6 +160,8 @@ struct amdg_linear_op {
 };
 
 struct amdg_burgers_op {
+    int64_t built_version = -1;
+    int64_t capacity = 0;            // elements the work buffers can hold
     amdg_grid* grid = nullptr;
     int device = 0;
     std::vector<double> alpha;
@@ -164,5 +178,6 @@ struct amdg_burgers_op {
     std::vector<std::vector<int>> sched_dims, sched_lu;
     // work buffers sized for FP64 (E x 4^dim doubles each)
     void *w_up = nullptr, *w_fu = nullptr, *w_a = nullptr, *w_b = nullptr, *w_rhs = nullptr, *w_u = nullptr;
-    double *d_u1 = nullptr, *d_u2 = nullptr, *d_rhs64 = nullptr;
+    double *d_u1 = nullptr, *d_u2 = nullptr, *d_rhs64 = nullptr, *d_pred = nullptr;
+    std::vector<double> host_norms;
 };

@@ -4,6 +4,7 @@
 // entry point runs on the device or fails with a status.
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cmath>
 #include <cstring>
 #include <new>
@@ -85,6 +86,67 @@ amdg_status project_terms(const amdg_grid* g, int nterms, amdg_fn1d f, void* use
     return AMDG_OK;
 }
 
+
+// Replace the grid's element set by `keys` (sorted, unique), carrying the
+// coefficients of surviving elements over and zeroing new ones.
+amdg_status grid_set_keys(amdg_grid* g, std::vector<uint64_t> keys) {
+    HostGrid ng;
+    ng.sparse = g->host.sparse;
+    grid_from_keys(g->host.dim, g->host.nmax, g->host.k, std::move(keys), &ng);
+    if (ng.num_elements > (int64_t(1) << 31) - 1) return fail(AMDG_ERR_CAPACITY, "more than 2^31-1 elements");
+    std::vector<int32_t> map(ng.num_elements);
+    for (int64_t e = 0; e < ng.num_elements; ++e) {
+        auto it = std::lower_bound(g->host.key.begin(), g->host.key.end(), ng.key[e]);
+        map[e] = (it != g->host.key.end() && *it == ng.key[e]) ? int32_t(it - g->host.key.begin()) : -1;
+    }
+    cudaStream_t st = stream_of(g->ctx);
+    const int64_t E = ng.num_elements;
+    const int64_t cap = std::max<int64_t>(E, g->capacity);
+    double* nu = nullptr;
+    int32_t* dmap = nullptr;
+    amdg_status s;
+    if ((s = dev_alloc(&nu, size_t(cap) * g->block)) != AMDG_OK) return s;
+    if ((s = upload(&dmap, map, st)) != AMDG_OK) { cudaFree(nu); return s; }
+    cudaError_t e = launch_remap(g->d_u, dmap, g->block, E, nu, st);
+    g->ctx->launches++;
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    cudaFree(dmap);
+    if (e != cudaSuccess) { cudaFree(nu); return fail(AMDG_ERR_CUDA, std::string("remap: ") + cudaGetErrorString(e)); }
+    cudaFree(g->d_u);
+    g->d_u = nu;
+    if (E > g->capacity || !g->d_order) {
+        cudaFree(g->d_order);
+        g->d_order = nullptr;
+        if ((s = dev_alloc(&g->d_order, size_t(cap) * g->host.dim)) != AMDG_OK) return s;
+    }
+    g->capacity = cap;
+    AMDG_CK(cudaMemcpyAsync(g->d_order, ng.order.data(), ng.order.size() * sizeof(int32_t), cudaMemcpyHostToDevice, st));
+    AMDG_CK(cudaStreamSynchronize(st));
+    g->host = std::move(ng);
+    g->dof = g->host.num_elements * g->block;
+    g->version++;
+    return AMDG_OK;
+}
+
+// indicator norms of a device coefficient vector on the grid's current element set
+amdg_status grid_norms(amdg_grid* g, const double* d_u, std::vector<double>* norms) {
+    cudaStream_t st = stream_of(g->ctx);
+    double* d_n = nullptr;
+    amdg_status s = dev_alloc(&d_n, size_t(std::max<int64_t>(g->host.num_elements, 1)));
+    if (s != AMDG_OK) return s;
+    cudaError_t e = launch_element_norms(d_u, g->block, g->host.num_elements, d_n, st);
+    g->ctx->launches++;
+    norms->assign(g->host.num_elements, 0.0);
+    if (e == cudaSuccess && g->host.num_elements > 0)
+        e = cudaMemcpyAsync(norms->data(), d_n, norms->size() * sizeof(double), cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    cudaFree(d_n);
+    if (e != cudaSuccess) return fail(AMDG_ERR_CUDA, std::string("element norms: ") + cudaGetErrorString(e));
+    for (double v : *norms)
+        if (!std::isfinite(v)) return fail(AMDG_ERR_NONFINITE, "element indicator is not finite");
+    return AMDG_OK;
+}
+
 StageCoef rk3_stage_coef(int stage, double dt) {
     switch (stage) {
         case 0: return StageCoef{1, 0.0, 1.0, dt};
@@ -125,6 +187,42 @@ amdg_status rk3_steps_device(amdg_linear_op* op, double dt, int nsteps, amdg_pre
             g->ctx->launches++;
         }
     }
+    return AMDG_OK;
+}
+
+// (Re)build the operator's neighbour lists and 1D blocks for the grid's
+// current element set; stage vectors grow with the grid.
+amdg_status linear_sync(amdg_linear_op* op) {
+    amdg_grid* g = op->grid;
+    if (op->built_version == g->version) return AMDG_OK;
+    Basis1D b{g->host.k, g->host.nmax};
+    Oper1D op1d;
+    build_oper1d(b, &op1d, false);
+    LinearTopology topo;
+    build_linear_topology(g->host, op1d, op->coef.data(), &topo);
+    cudaFree(op->d_row_ptr); cudaFree(op->d_src); cudaFree(op->d_blk); cudaFree(op->d_blocks64); cudaFree(op->d_blocks32);
+    op->d_row_ptr = op->d_src = op->d_blk = nullptr;
+    op->d_blocks64 = nullptr;
+    op->d_blocks32 = nullptr;
+    op->pairs = int64_t(topo.src.size());
+    op->num_blocks = topo.num_blocks;
+    std::vector<float> b32(topo.blocks.begin(), topo.blocks.end());
+    cudaStream_t st = stream_of(g->ctx);
+    amdg_status s;
+    if ((s = upload(&op->d_row_ptr, topo.row_ptr, st)) != AMDG_OK || (s = upload(&op->d_src, topo.src, st)) != AMDG_OK ||
+        (s = upload(&op->d_blk, topo.blk, st)) != AMDG_OK || (s = upload(&op->d_blocks64, topo.blocks, st)) != AMDG_OK ||
+        (s = upload(&op->d_blocks32, b32, st)) != AMDG_OK)
+        return s;
+    if (g->dof > op->capacity) {
+        cudaFree(op->d_u1);
+        cudaFree(op->d_u2);
+        op->d_u1 = op->d_u2 = nullptr;
+        if ((s = dev_alloc(&op->d_u1, size_t(g->dof))) != AMDG_OK || (s = dev_alloc(&op->d_u2, size_t(g->dof))) != AMDG_OK)
+            return s;
+        op->capacity = g->dof;
+    }
+    AMDG_CK(cudaStreamSynchronize(st));
+    op->built_version = g->version;
     return AMDG_OK;
 }
 
@@ -243,12 +341,13 @@ amdg_status amdg_grid_enumerate(int dim, int nmax, int sparse, int64_t* num_elem
 
 // ---- grid ------------------------------------------------------------------
 
-amdg_status amdg_grid_create(amdg_context* ctx, int dim, int nmax, int k, int sparse, amdg_grid** out) {
+amdg_status amdg_grid_create_ex(amdg_context* ctx, int dim, int level_init, int nmax, int k, int sparse, amdg_grid** out) {
     AMDG_REQUIRE(ctx && out, AMDG_ERR_ARG, "null argument");
     *out = nullptr;
     AMDG_REQUIRE(dim >= 1 && dim <= kMaxDim, AMDG_ERR_ARG, "dim must be 1..6");
     AMDG_REQUIRE(k >= 1 && k <= 3, AMDG_ERR_ARG, "Alpert degree k must be 1..3");
     AMDG_REQUIRE(nmax >= 0 && nmax <= 16 && dim * nmax <= 60, AMDG_ERR_ARG, "nmax out of range");
+    AMDG_REQUIRE(level_init >= 0 && level_init <= nmax, AMDG_ERR_ARG, "level_init must be 0..nmax");
     amdg_status s = set_device(ctx);
     if (s != AMDG_OK) return s;
     amdg_grid* g = new (std::nothrow) amdg_grid;
@@ -256,9 +355,10 @@ amdg_status amdg_grid_create(amdg_context* ctx, int dim, int nmax, int k, int sp
     g->ctx = ctx;
     g->device = ctx->device;
     g->host.k = k;
-    build_grid(dim, nmax, sparse, &g->host);
+    build_grid(dim, nmax, sparse, &g->host, level_init);
     g->block = ipow(k + 1, dim);
     g->dof = g->host.num_elements * g->block;
+    g->capacity = g->host.num_elements;
     if (g->host.num_elements > (int64_t(1) << 31) - 1) {
         delete g;
         return fail(AMDG_ERR_CAPACITY, "more than 2^31-1 elements");
@@ -279,6 +379,10 @@ amdg_status amdg_grid_create(amdg_context* ctx, int dim, int nmax, int k, int sp
     }
     *out = g;
     return AMDG_OK;
+}
+
+amdg_status amdg_grid_create(amdg_context* ctx, int dim, int nmax, int k, int sparse, amdg_grid** out) {
+    return amdg_grid_create_ex(ctx, dim, nmax, nmax, k, sparse, out);
 }
 
 amdg_status amdg_grid_destroy(amdg_grid* g) {
@@ -370,6 +474,64 @@ amdg_status amdg_grid_init_separable(amdg_grid* g, int nterms, amdg_fn1d f, void
     return AMDG_OK;
 }
 
+amdg_status amdg_grid_init_separable_adaptive(amdg_grid* g, int nterms, amdg_fn1d f, void* user, double eps) {
+    AMDG_REQUIRE(g && f && nterms > 0, AMDG_ERR_ARG, "bad arguments");
+    amdg_status s = set_device(g->ctx);
+    if (s != AMDG_OK) return s;
+    std::vector<double> coef;
+    if ((s = project_terms(g, nterms, f, user, &coef)) != AMDG_OK) return s;
+    // refine every leaf whose projected block exceeds eps, fill holes, repeat
+    // until nothing changes (DGAdapt::refine_init_separable_scalar_sum)
+    for (;;) {
+        std::vector<double> norms;
+        element_separable_norms(g->host, coef, nterms, &norms);
+        std::vector<uint64_t> keys = refine_keys(g->host, norms.data(), eps);
+        if (int64_t(keys.size()) == g->host.num_elements) break;
+        if ((s = grid_set_keys(g, std::move(keys))) != AMDG_OK) return s;
+    }
+    cudaStream_t st = stream_of(g->ctx);
+    double* d_coef = nullptr;
+    if ((s = upload(&d_coef, coef, st)) != AMDG_OK) return s;
+    const int np = g->host.k + 1;
+    cudaError_t e = launch_init_separable(g->d_order, d_coef, g->host.dim, np, (1 << g->host.nmax) * np, nterms,
+                                          g->host.num_elements, g->d_u, st);
+    g->ctx->launches++;
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    cudaFree(d_coef);
+    if (e != cudaSuccess) return fail(AMDG_ERR_CUDA, std::string("init_separable: ") + cudaGetErrorString(e));
+    return AMDG_OK;
+}
+
+amdg_status amdg_grid_refine(amdg_grid* g, const double* d_indicator, double eps, int64_t* num_elements) {
+    AMDG_REQUIRE(g, AMDG_ERR_ARG, "grid is null");
+    amdg_status s = set_device(g->ctx);
+    if (s != AMDG_OK) return s;
+    std::vector<double> norms;
+    if ((s = grid_norms(g, d_indicator ? d_indicator : g->d_u, &norms)) != AMDG_OK) return s;
+    std::vector<uint64_t> keys = refine_keys(g->host, norms.data(), eps);
+    if (int64_t(keys.size()) != g->host.num_elements && (s = grid_set_keys(g, std::move(keys))) != AMDG_OK) return s;
+    if (num_elements) *num_elements = g->host.num_elements;
+    return AMDG_OK;
+}
+
+amdg_status amdg_grid_coarsen(amdg_grid* g, double eta, int64_t* num_elements) {
+    AMDG_REQUIRE(g, AMDG_ERR_ARG, "grid is null");
+    amdg_status s = set_device(g->ctx);
+    if (s != AMDG_OK) return s;
+    std::vector<double> norms;
+    if ((s = grid_norms(g, g->d_u, &norms)) != AMDG_OK) return s;
+    std::vector<uint64_t> keys = coarsen_keys(g->host, norms.data(), eta);
+    if (int64_t(keys.size()) != g->host.num_elements && (s = grid_set_keys(g, std::move(keys))) != AMDG_OK) return s;
+    if (num_elements) *num_elements = g->host.num_elements;
+    return AMDG_OK;
+}
+
+amdg_status amdg_grid_version(const amdg_grid* g, int64_t* version) {
+    AMDG_REQUIRE(g && version, AMDG_ERR_ARG, "null argument");
+    *version = g->version;
+    return AMDG_OK;
+}
+
 static amdg_status reduce_grid(const amdg_grid* g, const double* d_coef, int mode, double* out) {
     amdg_status s = set_device(g->ctx);
     if (s != AMDG_OK) return s;
@@ -417,31 +579,14 @@ amdg_status amdg_linear_create(amdg_grid* g, const double* coef, amdg_linear_op*
     if (s != AMDG_OK) return s;
     const int dim = g->host.dim;
     for (int d = 0; d < dim; ++d) AMDG_REQUIRE(std::isfinite(coef[d]), AMDG_ERR_ARG, "non-finite coefficient");
-    Basis1D b{g->host.k, g->host.nmax};
-    Oper1D op1d;
-    build_oper1d(b, &op1d, false);
-    LinearTopology topo;
-    build_linear_topology(g->host, op1d, coef, &topo);
     amdg_linear_op* op = new (std::nothrow) amdg_linear_op;
     AMDG_REQUIRE(op, AMDG_ERR_NOMEM, "host allocation failed");
     op->grid = g;
     op->device = g->device;
     op->coef.assign(coef, coef + dim);
-    op->pairs = int64_t(topo.src.size());
-    op->num_blocks = topo.num_blocks;
-    std::vector<float> b32(topo.blocks.begin(), topo.blocks.end());
-    cudaStream_t st = stream_of(g->ctx);
-    if ((s = upload(&op->d_row_ptr, topo.row_ptr, st)) != AMDG_OK || (s = upload(&op->d_src, topo.src, st)) != AMDG_OK ||
-        (s = upload(&op->d_blk, topo.blk, st)) != AMDG_OK || (s = upload(&op->d_blocks64, topo.blocks, st)) != AMDG_OK ||
-        (s = upload(&op->d_blocks32, b32, st)) != AMDG_OK || (s = dev_alloc(&op->d_u1, size_t(g->dof))) != AMDG_OK ||
-        (s = dev_alloc(&op->d_u2, size_t(g->dof))) != AMDG_OK) {
+    if ((s = linear_sync(op)) != AMDG_OK) {
         amdg_linear_destroy(op);
         return s;
-    }
-    cudaError_t e = cudaStreamSynchronize(st);
-    if (e != cudaSuccess) {
-        amdg_linear_destroy(op);
-        return fail(AMDG_ERR_CUDA, std::string("linear_create: ") + cudaGetErrorString(e));
     }
     *out = op;
     return AMDG_OK;
@@ -475,6 +620,7 @@ amdg_status amdg_linear_apply(amdg_linear_op* op, const double* d_u, double* d_r
     AMDG_REQUIRE(prec == AMDG_PREC_FP64 || prec == AMDG_PREC_MIXED, AMDG_ERR_ARG, "bad precision");
     amdg_status s = set_device(op->grid->ctx);
     if (s != AMDG_OK) return s;
+    if ((s = linear_sync(op)) != AMDG_OK) return s;
     LinearLaunch L = linear_launch(op);
     L.us = d_u;
     L.un = nullptr;
@@ -489,6 +635,7 @@ amdg_status amdg_rk3ssp_steps(amdg_linear_op* op, double dt, int nsteps, amdg_pr
     AMDG_REQUIRE(prec == AMDG_PREC_FP64 || prec == AMDG_PREC_MIXED, AMDG_ERR_ARG, "bad precision");
     amdg_status s = set_device(op->grid->ctx);
     if (s != AMDG_OK) return s;
+    if ((s = linear_sync(op)) != AMDG_OK) return s;
     return rk3_steps_device(op, dt, nsteps, prec);
 }
 
@@ -498,6 +645,7 @@ amdg_status amdg_rk3ssp_steps_host(amdg_linear_op* op, double dt, int nsteps, do
     amdg_grid* g = op->grid;
     amdg_status s = set_device(g->ctx);
     if (s != AMDG_OK) return s;
+    if ((s = linear_sync(op)) != AMDG_OK) return s;
     cudaStream_t st = stream_of(g->ctx);
     const size_t bytes = size_t(g->dof) * sizeof(double);
     AMDG_CK(cudaMemcpyAsync(g->d_u, host_u, bytes, cudaMemcpyHostToDevice, st));

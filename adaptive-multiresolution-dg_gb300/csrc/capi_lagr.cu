@@ -179,15 +179,12 @@ amdg_status eval_flux_coefficients(amdg_burgers_op* op, const T* up, cudaStream_
     return AMDG_OK;
 }
 
+// volume and interface terms from the flux coefficients fu, and the LxF
+// penalty from the Alpert coefficients u, into rhs (set, not added)
 template <typename T>
-amdg_status eval_rhs_t(amdg_burgers_op* op, const Mats<T>& m, const T* u, T* rhs, cudaStream_t st) {
+amdg_status eval_back_transforms(amdg_burgers_op* op, const Mats<T>& m, const T* fu, const T* u, T* rhs, cudaStream_t st) {
     const amdg_grid* g = op->grid;
     const int dim = g->host.dim, np = g->host.k + 1;
-    T* up = static_cast<T*>(op->w_up);
-    amdg_status r = eval_point_values<T>(op, m, u, up, st);
-    if (r != AMDG_OK) return r;
-    if ((r = eval_flux_coefficients<T>(op, up, st)) != AMDG_OK) return r;
-    const T* fu = static_cast<const T*>(op->w_fu);
     T* ta = static_cast<T*>(op->w_a);
     T* tb = static_cast<T*>(op->w_b);
     AMDG_CK(cudaMemsetAsync(rhs, 0, size_t(g->dof) * sizeof(T), st));
@@ -203,7 +200,7 @@ amdg_status eval_rhs_t(amdg_burgers_op* op, const Mats<T>& m, const T* u, T* rhs
             }
             const T coef = term == 0 ? T(1) : T(0.5);
             for (size_t s = 0; s < op->sched_dims.size(); ++s) {
-                r = partial_sum<T>(op, op->sched_dims[s], op->sched_lu[s], 4, np, mats, flx, coef, fu, rhs, ta, tb, st);
+                amdg_status r = partial_sum<T>(op, op->sched_dims[s], op->sched_lu[s], 4, np, mats, flx, coef, fu, rhs, ta, tb, st);
                 if (r != AMDG_OK) return r;
             }
         }
@@ -224,19 +221,73 @@ amdg_status eval_rhs_t(amdg_burgers_op* op, const Mats<T>& m, const T* u, T* rhs
     return AMDG_OK;
 }
 
-// rhs (FP64, dof entries) of the FP64 state u
+// rhs (FP64, dof entries) of the FP64 state u.  The point values and the
+// hierarchical surplus always run in FP64: fine-level surpluses are small
+// differences of O(1) point values, which FP32 rounding would swamp.  In mixed
+// mode the back transforms (the bulk of the work) and the penalty run in FP32.
 amdg_status eval_rhs(amdg_burgers_op* op, const double* u, double* rhs, amdg_precision prec) {
     cudaStream_t st = stream_of(op);
     const int64_t n = op->grid->dof;
-    if (prec == AMDG_PREC_FP64) return eval_rhs_t<double>(op, mats64(op), u, rhs, st);
+    const int64_t npts = op->grid->host.num_elements * op->points;
+    double* up = static_cast<double*>(op->w_up);
+    amdg_status r = eval_point_values<double>(op, mats64(op), u, up, st);
+    if (r != AMDG_OK) return r;
+    if ((r = eval_flux_coefficients<double>(op, up, st)) != AMDG_OK) return r;
+    const double* fu = static_cast<const double*>(op->w_fu);
+    if (prec == AMDG_PREC_FP64) return eval_back_transforms<double>(op, mats64(op), fu, u, rhs, st);
+    float* fu32 = static_cast<float*>(op->w_up);  // point values are no longer needed
     float* u32 = static_cast<float*>(op->w_u);
     float* r32 = static_cast<float*>(op->w_rhs);
+    AMDG_CK(launch_convert<double, float>(fu, fu32, npts, st));
     AMDG_CK(launch_convert<double, float>(u, u32, n, st));
-    op->grid->ctx->launches++;
-    amdg_status r = eval_rhs_t<float>(op, mats32(op), u32, r32, st);
-    if (r != AMDG_OK) return r;
+    op->grid->ctx->launches += 2;
+    if ((r = eval_back_transforms<float>(op, mats32(op), fu32, u32, r32, st)) != AMDG_OK) return r;
     AMDG_CK(launch_convert<float, double>(r32, rhs, n, st));
     op->grid->ctx->launches++;
+    return AMDG_OK;
+}
+
+
+// (Re)build the neighbour lists and surplus ancestors for the grid's current
+// element set; work buffers grow with the grid.
+amdg_status burgers_sync(amdg_burgers_op* op) {
+    amdg_grid* g = op->grid;
+    if (op->built_version == g->version) return AMDG_OK;
+    Basis1D b{g->host.k, g->host.nmax};
+    LagrTables t;
+    t.anc_order.assign(size_t(op->n1) * 4, -1);
+    // ancestor orders only depend on nmax: recompute them cheaply on the host
+    build_lagr_ancestors(b, &t);
+    TransformTopology topo;
+    build_transform_topology(g->host, &topo);
+    std::vector<int32_t> anc;
+    if (!build_surplus_ancestors(g->host, t, &anc)) return fail(AMDG_ERR_STATE, "element set has a hole: a surplus ancestor is missing");
+    int32_t* old[] = {op->d_vol_ptr, op->d_vol_src, op->d_vol_lev, op->d_flx_ptr, op->d_flx_src, op->d_flx_lev, op->d_anc};
+    for (int32_t* p : old) cudaFree(p);
+    op->d_vol_ptr = op->d_vol_src = op->d_vol_lev = op->d_flx_ptr = op->d_flx_src = op->d_flx_lev = op->d_anc = nullptr;
+    amdg_status s;
+    if ((s = upload_vec(&op->d_vol_ptr, topo.vol_ptr)) != AMDG_OK || (s = upload_vec(&op->d_vol_src, topo.vol_src)) != AMDG_OK ||
+        (s = upload_vec(&op->d_vol_lev, topo.vol_lev)) != AMDG_OK || (s = upload_vec(&op->d_flx_ptr, topo.flx_ptr)) != AMDG_OK ||
+        (s = upload_vec(&op->d_flx_src, topo.flx_src)) != AMDG_OK || (s = upload_vec(&op->d_flx_lev, topo.flx_lev)) != AMDG_OK ||
+        (s = upload_vec(&op->d_anc, anc)) != AMDG_OK)
+        return s;
+    const int64_t E = g->host.num_elements;
+    if (E > op->capacity) {
+        const int64_t cap = E + E / 2 + 16;
+        void* bufs[] = {op->w_up, op->w_fu, op->w_a, op->w_b, op->w_rhs, op->w_u, op->d_u1, op->d_rhs64, op->d_pred};
+        for (void* p : bufs) cudaFree(p);
+        const size_t work = size_t(cap) * op->points * sizeof(double);
+        const size_t vec = size_t(cap) * g->block * sizeof(double);
+        if ((s = alloc_bytes(&op->w_up, work)) != AMDG_OK || (s = alloc_bytes(&op->w_fu, work)) != AMDG_OK ||
+            (s = alloc_bytes(&op->w_a, work)) != AMDG_OK || (s = alloc_bytes(&op->w_b, work)) != AMDG_OK ||
+            (s = alloc_bytes(&op->w_rhs, vec)) != AMDG_OK || (s = alloc_bytes(&op->w_u, vec)) != AMDG_OK ||
+            (s = alloc_bytes(reinterpret_cast<void**>(&op->d_u1), vec)) != AMDG_OK ||
+            (s = alloc_bytes(reinterpret_cast<void**>(&op->d_rhs64), vec)) != AMDG_OK ||
+            (s = alloc_bytes(reinterpret_cast<void**>(&op->d_pred), vec)) != AMDG_OK)
+            return s;
+        op->capacity = cap;
+    }
+    op->built_version = g->version;
     return AMDG_OK;
 }
 
@@ -271,31 +322,14 @@ amdg_status amdg_burgers_create(amdg_grid* g, const double* alpha, amdg_burgers_
     LagrTables t;
     build_lagr_tables(b, &t);
     std::memcpy(op->weight, t.weight, sizeof(op->weight));
-    TransformTopology topo;
-    build_transform_topology(g->host, &topo);
-    std::vector<int32_t> anc;
-    if (!build_surplus_ancestors(g->host, t, &anc)) {
-        delete op;
-        return fail(AMDG_ERR_STATE, "element set has a hole: a surplus ancestor is missing");
-    }
     transform_schedule(dim, &op->sched_dims, &op->sched_lu);
-    const size_t work = size_t(g->host.num_elements) * op->points * sizeof(double);
     amdg_status s;
     if ((s = upload_both(&op->d_a2p, &op->f_a2p, t.a2p)) != AMDG_OK || (s = upload_both(&op->d_lv, &op->f_lv, t.lv)) != AMDG_OK ||
         (s = upload_both(&op->d_lvx, &op->f_lvx, t.lvx)) != AMDG_OK ||
         (s = upload_both(&op->d_lflx, &op->f_lflx, t.lflx)) != AMDG_OK ||
         (s = upload_both(&op->d_ajump, &op->f_ajump, t.ajump)) != AMDG_OK ||
-        (s = upload_vec(&op->d_vol_ptr, topo.vol_ptr)) != AMDG_OK || (s = upload_vec(&op->d_vol_src, topo.vol_src)) != AMDG_OK ||
-        (s = upload_vec(&op->d_vol_lev, topo.vol_lev)) != AMDG_OK || (s = upload_vec(&op->d_flx_ptr, topo.flx_ptr)) != AMDG_OK ||
-        (s = upload_vec(&op->d_flx_src, topo.flx_src)) != AMDG_OK || (s = upload_vec(&op->d_flx_lev, topo.flx_lev)) != AMDG_OK ||
-        (s = upload_vec(&op->d_anc, anc)) != AMDG_OK || (s = upload_vec(&op->d_anc_point, t.anc_point)) != AMDG_OK ||
-        (s = upload_vec(&op->d_anc_rank, t.anc_rank)) != AMDG_OK || (s = alloc_bytes(&op->w_up, work)) != AMDG_OK ||
-        (s = alloc_bytes(&op->w_fu, work)) != AMDG_OK || (s = alloc_bytes(&op->w_a, work)) != AMDG_OK ||
-        (s = alloc_bytes(&op->w_b, work)) != AMDG_OK ||
-        (s = alloc_bytes(&op->w_rhs, size_t(g->dof) * sizeof(double))) != AMDG_OK ||
-        (s = alloc_bytes(&op->w_u, size_t(g->dof) * sizeof(double))) != AMDG_OK ||
-        (s = alloc_bytes(reinterpret_cast<void**>(&op->d_u1), size_t(g->dof) * sizeof(double))) != AMDG_OK ||
-        (s = alloc_bytes(reinterpret_cast<void**>(&op->d_rhs64), size_t(g->dof) * sizeof(double))) != AMDG_OK) {
+        (s = upload_vec(&op->d_anc_point, t.anc_point)) != AMDG_OK || (s = upload_vec(&op->d_anc_rank, t.anc_rank)) != AMDG_OK ||
+        (s = burgers_sync(op)) != AMDG_OK) {
         amdg_burgers_destroy(op);
         return s;
     }
@@ -309,7 +343,7 @@ amdg_status amdg_burgers_destroy(amdg_burgers_op* op) {
     void* ptrs[] = {op->d_a2p, op->d_lv, op->d_lvx, op->d_lflx, op->d_ajump, op->f_a2p, op->f_lv, op->f_lvx, op->f_lflx,
                     op->f_ajump, op->d_vol_ptr, op->d_vol_src, op->d_vol_lev, op->d_flx_ptr, op->d_flx_src, op->d_flx_lev,
                     op->d_anc, op->d_anc_point, op->d_anc_rank, op->w_up, op->w_fu, op->w_a, op->w_b, op->w_rhs, op->w_u,
-                    op->d_u1, op->d_u2, op->d_rhs64};
+                    op->d_u1, op->d_u2, op->d_rhs64, op->d_pred};
     for (void* p : ptrs) cudaFree(p);
     delete op;
     return AMDG_OK;
@@ -319,6 +353,7 @@ amdg_status amdg_burgers_rhs(amdg_burgers_op* op, const double* d_u, double* d_r
     AMDG_REQUIRE(op && d_u && d_rhs && d_u != d_rhs, AMDG_ERR_ARG, "bad arguments");
     AMDG_REQUIRE(prec == AMDG_PREC_FP64 || prec == AMDG_PREC_MIXED, AMDG_ERR_ARG, "bad precision");
     AMDG_CK(cudaSetDevice(op->device));
+    if (amdg_status rs = burgers_sync(op); rs != AMDG_OK) return rs;
     return eval_rhs(op, d_u, d_rhs, prec);
 }
 
@@ -326,6 +361,7 @@ amdg_status amdg_burgers_point_values(amdg_burgers_op* op, const double* d_u, do
     AMDG_REQUIRE(op && d_u && d_up, AMDG_ERR_ARG, "bad arguments");
     AMDG_REQUIRE(prec == AMDG_PREC_FP64 || prec == AMDG_PREC_MIXED, AMDG_ERR_ARG, "bad precision");
     AMDG_CK(cudaSetDevice(op->device));
+    if (amdg_status rs = burgers_sync(op); rs != AMDG_OK) return rs;
     cudaStream_t st = stream_of(op);
     if (prec == AMDG_PREC_FP64) return eval_point_values<double>(op, mats64(op), d_u, d_up, st);
     const int64_t n = op->grid->dof, np = op->grid->host.num_elements * op->points;
@@ -343,6 +379,7 @@ amdg_status amdg_burgers_flux_coefficients(amdg_burgers_op* op, const double* d_
     AMDG_REQUIRE(op && d_u && d_fu, AMDG_ERR_ARG, "bad arguments");
     AMDG_REQUIRE(prec == AMDG_PREC_FP64 || prec == AMDG_PREC_MIXED, AMDG_ERR_ARG, "bad precision");
     AMDG_CK(cudaSetDevice(op->device));
+    if (amdg_status rs = burgers_sync(op); rs != AMDG_OK) return rs;
     cudaStream_t st = stream_of(op);
     const int64_t np = op->grid->host.num_elements * op->points;
     if (prec == AMDG_PREC_FP64) {
@@ -366,6 +403,7 @@ amdg_status amdg_burgers_rk3_steps(amdg_burgers_op* op, double dt, int nsteps, a
     AMDG_REQUIRE(op && nsteps >= 0 && std::isfinite(dt), AMDG_ERR_ARG, "bad arguments");
     AMDG_REQUIRE(prec == AMDG_PREC_FP64 || prec == AMDG_PREC_MIXED, AMDG_ERR_ARG, "bad precision");
     AMDG_CK(cudaSetDevice(op->device));
+    if (amdg_status rs = burgers_sync(op); rs != AMDG_OK) return rs;
     amdg_grid* g = op->grid;
     cudaStream_t st = stream_of(op);
     const size_t bytes = size_t(g->dof) * sizeof(double);
@@ -380,6 +418,35 @@ amdg_status amdg_burgers_rk3_steps(amdg_burgers_op* op, double dt, int nsteps, a
         }
         AMDG_CK(cudaMemcpyAsync(g->d_u, op->d_u1, bytes, cudaMemcpyDeviceToDevice, st));
     }
+    return AMDG_OK;
+}
+
+amdg_status amdg_burgers_adaptive_step(amdg_burgers_op* op, double cfl, double wave_speed, double eps, double eta,
+                                       amdg_precision prec, double* dt_out) {
+    AMDG_REQUIRE(op && std::isfinite(cfl) && cfl > 0 && std::isfinite(wave_speed) && wave_speed > 0, AMDG_ERR_ARG,
+                 "bad arguments");
+    AMDG_REQUIRE(prec == AMDG_PREC_FP64 || prec == AMDG_PREC_MIXED, AMDG_ERR_ARG, "bad precision");
+    AMDG_CK(cudaSetDevice(op->device));
+    if (amdg_status rs = burgers_sync(op); rs != AMDG_OK) return rs;
+    amdg_grid* g = op->grid;
+    cudaStream_t st = stream_of(op);
+    // dt = cfl / sum_d c_d 2^maxlevel_d  (02_hyperbolic_05_burgers_adapt.cpp:239-247)
+    std::vector<int32_t> lv(g->host.dim);
+    amdg_status s = amdg_grid_max_mesh_level(g, lv.data());
+    if (s != AMDG_OK) return s;
+    double sum_c_dx = 0.0;
+    for (int d = 0; d < g->host.dim; ++d) sum_c_dx += wave_speed * std::pow(2.0, lv[d]);
+    const double dt = cfl / sum_c_dx;
+    // predictor: forward Euler into the prediction buffer (ForwardEuler::step_stage)
+    if ((s = eval_rhs(op, g->d_u, op->d_rhs64, prec)) != AMDG_OK) return s;
+    AMDG_CK(cudaMemcpyAsync(op->d_pred, g->d_u, size_t(g->dof) * sizeof(double), cudaMemcpyDeviceToDevice, st));
+    AMDG_CK(launch_stage_update(g->d_u, op->d_pred, op->d_rhs64, g->dof, stage_coef(0, dt), st));
+    g->ctx->launches++;
+    // refine on the predicted coefficients; new elements start from zero (DGAdapt::refine, copy_predict_to_ucoe)
+    if ((s = amdg_grid_refine(g, op->d_pred, eps, nullptr)) != AMDG_OK) return s;
+    if ((s = amdg_burgers_rk3_steps(op, dt, 1, prec)) != AMDG_OK) return s;
+    if ((s = amdg_grid_coarsen(g, eta, nullptr)) != AMDG_OK) return s;
+    if (dt_out) *dt_out = dt;
     return AMDG_OK;
 }
 

@@ -17,7 +17,8 @@ static uint64_t pack(const int32_t* o, int dim, int nmax) {
     return key;
 }
 
-void build_grid(int dim, int nmax, int sparse, HostGrid* g) {
+void build_grid(int dim, int nmax, int sparse, HostGrid* g, int level_init) {
+    if (level_init < 0 || level_init > nmax) level_init = nmax;
     g->dim = dim;
     g->nmax = nmax;
     g->sparse = sparse;
@@ -32,7 +33,7 @@ void build_grid(int dim, int nmax, int sparse, HostGrid* g) {
     for (;;) {
         int lsum = 0;
         for (int d = 0; d < dim; ++d) lsum += lv[d];
-        if (!sparse || lsum <= nmax) {
+        if (!sparse || lsum <= level_init) {
             int64_t ne = 1;
             for (int d = 0; d < dim; ++d) ne *= lv[d] == 0 ? 1 : (int64_t(1) << (lv[d] - 1));
             for (int64_t i = 0; i < ne; ++i) {
@@ -47,7 +48,7 @@ void build_grid(int dim, int nmax, int sparse, HostGrid* g) {
         }
         int d = dim - 1;
         while (d >= 0) {
-            if (++lv[d] <= nmax) break;
+            if (++lv[d] <= level_init) break;
             lv[d] = 0;
             --d;
         }

@@ -202,3 +202,43 @@ cudaError_t launch_reduce(const double* u, const int32_t* order, const double* c
 }
 
 }  // namespace amdg
+
+namespace amdg {
+
+// ---- adaptivity -----------------------------------------------------------------
+// Indicator of every element: sqrt of the sum of squares of its block, summed in
+// block order (DGAdapt::indicator_norm, DGAdapt.cpp:1018-1030; VecMultiD::norm).
+__global__ void element_norm_kernel(const double* __restrict__ u, int B, int64_t E, double* __restrict__ out) {
+    const int64_t e = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (e >= E) return;
+    const double* x = u + e * B;
+    double s = 0.0;
+    for (int q = 0; q < B; ++q) s = __dadd_rn(s, __dmul_rn(x[q], x[q]));
+    out[e] = sqrt(s);
+}
+
+cudaError_t launch_element_norms(const double* u, int B, int64_t E, double* out, cudaStream_t st) {
+    if (E == 0) return cudaSuccess;
+    element_norm_kernel<<<unsigned((E + 127) / 128), 128, 0, st>>>(u, B, E, out);
+    return cudaGetLastError();
+}
+
+// new[e] = old[map[e]] block-wise, zero where map[e] < 0 (elements created by refinement)
+__global__ void remap_kernel(const double* __restrict__ old_u, const int32_t* __restrict__ map, int B, int64_t total,
+                             double* __restrict__ new_u) {
+    const int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (i >= total) return;
+    const int64_t e = i / B;
+    const int q = int(i - e * B);
+    const int32_t src = map[e];
+    new_u[i] = src >= 0 ? old_u[int64_t(src) * B + q] : 0.0;
+}
+
+cudaError_t launch_remap(const double* old_u, const int32_t* map, int B, int64_t E_new, double* new_u, cudaStream_t st) {
+    const int64_t total = E_new * B;
+    if (total == 0) return cudaSuccess;
+    remap_kernel<<<unsigned((total + 255) / 256), 256, 0, st>>>(old_u, map, B, total, new_u);
+    return cudaGetLastError();
+}
+
+}  // namespace amdg

@@ -37,5 +37,7 @@ cudaError_t launch_init_separable(const int32_t* order, const double* coef1d, in
 cudaError_t launch_reduce(const double* u, const int32_t* order, const double* coef1d, int dim, int np, int nb1,
                           int64_t num_elements, int mode, double* scratch, cudaStream_t st);
 int reduce_partials_needed();
+cudaError_t launch_element_norms(const double* u, int B, int64_t E, double* out, cudaStream_t st);
+cudaError_t launch_remap(const double* old_u, const int32_t* map, int B, int64_t E_new, double* new_u, cudaStream_t st);
 
 }  // namespace amdg

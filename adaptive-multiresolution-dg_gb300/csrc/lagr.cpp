@@ -105,6 +105,37 @@ double lagr_point(int o, int p) {
     return a + (b - a) * (kMsh1[p] + 1.0) / 2.0;
 }
 
+void build_lagr_ancestors(const Basis1D& alpt, LagrTables* t) {
+    const int n1 = alpt.num_elem();
+    // surplus: ancestors (coarser-level points inside each element's support) and weights
+    t->anc_order.assign(size_t(n1) * 4, -1);
+    t->anc_point.assign(size_t(n1) * 4, 0);
+    t->anc_rank.assign(size_t(n1) * 4, 0);
+    for (int o = 1; o < n1; ++o) {
+        const int l = level_of_order(o);
+        const double xl = supp_lo(o), xr = supp_hi(o);
+        int ic = 0;
+        double pos[4] = {0, 0, 0, 0};
+        for (int oa = 0; oa < n1 && ic < 4; ++oa) {
+            if (level_of_order(oa) >= l) break;
+            for (int q = 0; q < 4 && ic < 4; ++q) {
+                const double x = lagr_point(oa, q);
+                if (x > xl && x < xr) {
+                    t->anc_order[size_t(o) * 4 + ic] = oa;
+                    t->anc_point[size_t(o) * 4 + ic] = q;
+                    pos[ic] = x;
+                    ++ic;
+                }
+            }
+        }
+        for (int a = 0; a < 4; ++a) {
+            int rk = 0;
+            for (int b = 0; b < 4; ++b) rk += pos[b] < pos[a];
+            t->anc_rank[size_t(o) * 4 + a] = rk;
+        }
+    }
+}
+
 void build_lagr_tables(const Basis1D& alpt, LagrTables* t) {
     static const GL10 g;
     const int n1 = alpt.num_elem(), na = alpt.num_basis(), np = alpt.k + 1, nl = n1 * 4;
@@ -169,33 +200,7 @@ void build_lagr_tables(const Basis1D& alpt, LagrTables* t) {
     build_oper1d(alpt, &op, false);
     t->ajump.assign(size_t(na) * na, 0.0);
     for (size_t i = 0; i < t->ajump.size(); ++i) t->ajump[i] = op.urgt_vjp[i] - op.ulft_vjp[i];
-    // surplus: ancestors (coarser-level points inside each element's support) and weights
-    t->anc_order.assign(size_t(n1) * 4, -1);
-    t->anc_point.assign(size_t(n1) * 4, 0);
-    t->anc_rank.assign(size_t(n1) * 4, 0);
-    for (int o = 1; o < n1; ++o) {
-        const int l = level_of_order(o);
-        const double xl = supp_lo(o), xr = supp_hi(o);
-        int ic = 0;
-        double pos[4] = {0, 0, 0, 0};
-        for (int oa = 0; oa < n1 && ic < 4; ++oa) {
-            if (level_of_order(oa) >= l) break;
-            for (int q = 0; q < 4 && ic < 4; ++q) {
-                const double x = lagr_point(oa, q);
-                if (x > xl && x < xr) {
-                    t->anc_order[size_t(o) * 4 + ic] = oa;
-                    t->anc_point[size_t(o) * 4 + ic] = q;
-                    pos[ic] = x;
-                    ++ic;
-                }
-            }
-        }
-        for (int a = 0; a < 4; ++a) {
-            int rk = 0;
-            for (int b = 0; b < 4; ++b) rk += pos[b] < pos[a];
-            t->anc_rank[size_t(o) * 4 + a] = rk;
-        }
-    }
+    build_lagr_ancestors(alpt, t);
     // weight[p0][rank] = -L0_rank(node p0 of the element, in its reference coordinates)
     for (int p0 = 0; p0 < 4; ++p0)
         for (int r = 0; r < 4; ++r) t->weight[p0 * 4 + r] = -lagr_mother((kMsh1[p0] + 1.0) / 2.0, 0, r);

@@ -1,0 +1,228 @@
+// C++ mirror of the AdaM-DG driver-facing API for the sparse-grid DG
+// right-hand side, implemented over the C-ABI in include/amdg.h.
+//
+// A driver written against the reference (example/*.cpp) keeps its structure:
+// the same class names, constructor arguments and method names, with the
+// element table, coefficients and operators living on the GPU.  Classes whose
+// reference role is host-side bookkeeping (AllBasis, OperatorMatrix1D, Hash)
+// keep their constructors but hold only what the device needs; the 1D tables
+// are built inside the library.  Errors throw amdg_gpu::Error (the reference
+// prints and calls exit(1)).
+//
+// Mirrors: DGSolution/DGAdapt (DGAdapt.h:10-91, DGSolution.h:21-214),
+// HyperbolicAlpt (BilinearForm.h:137-152), RK3SSP/ForwardEuler (ODESolver.h:93-205),
+// LagrInterpolation + FastLagrIntp + HyperbolicLagrRHS + HyperbolicAlptRHS
+// (Interpolation.h:36-97, FastMultiplyLU.h:194-205, 575-629).
+#pragma once
+
+#include <cmath>
+#include <functional>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include "amdg.h"
+
+namespace amdg_gpu {
+
+struct Error : std::runtime_error {
+    amdg_status status;
+    Error(amdg_status s, const std::string& where)
+        : std::runtime_error(where + ": " + amdg_status_string(s) + ": " + amdg_last_error()), status(s) {}
+};
+
+inline void check(amdg_status s, const char* where) {
+    if (s != AMDG_OK) throw Error(s, where);
+}
+
+// ---- static configuration, as set by the reference drivers ----------------
+struct AlptBasis { static inline int PMAX = 2; };
+struct LagrBasis {
+    static inline int PMAX = 3;
+    static inline int msh_case = 1;
+    static void set_interp_msh01() {}
+};
+struct HermBasis {
+    static inline int PMAX = 3;
+    static inline int msh_case = 1;
+    static void set_interp_msh01() {}
+};
+struct Element {
+    static inline int DIM = 1, VEC_NUM = 1, PMAX_alpt = 2, PMAX_intp = 3;
+    static inline std::vector<std::vector<bool>> is_intp;
+};
+struct Interpolation { static inline int DIM = 1, VEC_NUM = 1; };
+struct Hash {};
+
+template <class T>
+struct AllBasis {
+    explicit AllBasis(int max_level) : NMAX(max_level), PMAX(T::PMAX) {}
+    const int NMAX;
+    const int PMAX;
+};
+
+template <class U, class V>
+struct OperatorMatrix1D {
+    OperatorMatrix1D(const AllBasis<U>& u, const AllBasis<V>&, const std::string& boundary_type) : nmax(u.NMAX) {
+        if (boundary_type != "period") throw Error(AMDG_ERR_ARG, "OperatorMatrix1D: only periodic boundaries are supported");
+    }
+    const int nmax;
+};
+
+// ---- library context (one per process and device) ---------------------------
+class Runtime {
+public:
+    static amdg_context* context(int device = 0) {
+        static Runtime rt(device);
+        return rt.ctx_;
+    }
+private:
+    explicit Runtime(int device) { check(amdg_context_create(device, &ctx_), "amdg_context_create"); }
+    ~Runtime() { amdg_context_destroy(ctx_); }
+    amdg_context* ctx_ = nullptr;
+};
+
+namespace detail {
+struct SepFns {
+    const std::vector<std::function<double(double, int)>>* fns;
+};
+inline double sep_trampoline(double x, int d, int term, void* user) {
+    return (*static_cast<SepFns*>(user)->fns)[term](x, d);
+}
+}  // namespace detail
+
+// ---- DGSolution / DGAdapt ------------------------------------------------------
+class DGSolution {
+public:
+    static inline int DIM = 1;
+    static inline int VEC_NUM = 1;
+    static inline std::vector<int> ind_var_vec{0};
+
+    DGSolution(bool sparse, int level_init, int NMAX, AllBasis<AlptBasis>& all_bas, AllBasis<LagrBasis>&,
+               AllBasis<HermBasis>&, Hash&)
+        : nmax_(NMAX) {
+        if (level_init != NMAX) throw Error(AMDG_ERR_ARG, "DGSolution: level_init must equal NMAX");
+        check(amdg_grid_create(Runtime::context(), DIM, NMAX, all_bas.PMAX, sparse ? 1 : 0, &grid_), "amdg_grid_create");
+    }
+    DGSolution(const DGSolution&) = delete;
+    DGSolution& operator=(const DGSolution&) = delete;
+    virtual ~DGSolution() { amdg_grid_destroy(grid_); }
+
+    int size_elem() const { int64_t e = 0; check(amdg_grid_size(grid_, &e, nullptr), "amdg_grid_size"); return int(e); }
+    int size_basis_alpt() const { int64_t d = 0; check(amdg_grid_size(grid_, nullptr, &d), "amdg_grid_size"); return int(d); }
+    int get_dof() const { return size_basis_alpt() * int(ind_var_vec.size()); }
+    int nmax_level() const { return nmax_; }
+    std::vector<int> max_mesh_level_vec() const {
+        std::vector<int32_t> lv(DIM);
+        check(amdg_grid_max_mesh_level(grid_, lv.data()), "amdg_grid_max_mesh_level");
+        return std::vector<int>(lv.begin(), lv.end());
+    }
+    int max_mesh_level() const {
+        int m = 0;
+        for (int v : max_mesh_level_vec()) m = std::max(m, v);
+        return m;
+    }
+    // sum of squares of all coefficients (DGSolution::get_L2_norm)
+    std::vector<double> get_L2_norm() const {
+        double s = 0;
+        check(amdg_grid_l2_norm(grid_, &s), "amdg_grid_l2_norm");
+        return {s};
+    }
+    double get_L2_error_split_separable_scalar(std::function<double(double, int)> func, double l2_norm_exact_soln) const {
+        std::vector<std::function<double(double, int)>> fns{func};
+        detail::SepFns sf{&fns};
+        double err = 0;
+        check(amdg_grid_l2_error_separable(grid_, detail::sep_trampoline, &sf, l2_norm_exact_soln, &err),
+              "amdg_grid_l2_error_separable");
+        return err;
+    }
+    // coefficients of all elements, element blocks in the library's element order
+    std::vector<double> coefficients() const {
+        std::vector<double> u(size_basis_alpt());
+        check(amdg_grid_get_coefficients(grid_, u.data(), int64_t(u.size())), "amdg_grid_get_coefficients");
+        return u;
+    }
+    amdg_grid* handle() const { return grid_; }
+
+protected:
+    amdg_grid* grid_ = nullptr;
+    int nmax_;
+};
+
+class DGAdapt : public DGSolution {
+public:
+    static inline std::vector<int> indicator_var_adapt{0};
+    DGAdapt(bool sparse, int level_init, int NMAX, AllBasis<AlptBasis>& a, AllBasis<LagrBasis>& l, AllBasis<HermBasis>& h,
+            Hash& hash, double eps, double eta, bool /*is_find_ptr_alpt*/, bool /*is_find_ptr_intp*/,
+            bool /*is_find_ptr_general*/ = false)
+        : DGSolution(sparse, level_init, NMAX, a, l, h, hash), eps_(eps), eta_(eta) {}
+    void init_separable_scalar(std::function<double(double, int)> f) { init_separable_scalar_sum({f}); }
+    void init_separable_scalar_sum(std::vector<std::function<double(double, int)>> fns) {
+        detail::SepFns sf{&fns};
+        check(amdg_grid_init_separable(grid_, int(fns.size()), detail::sep_trampoline, &sf), "amdg_grid_init_separable");
+    }
+    double refine_eps() const { return eps_; }
+    double coarsen_eta() const { return eta_; }
+
+private:
+    double eps_, eta_;
+};
+
+// ---- linear constant-coefficient operator + explicit RK ----------------------
+class HyperbolicAlpt {
+public:
+    HyperbolicAlpt(DGSolution& dg, OperatorMatrix1D<AlptBasis, AlptBasis>&) : dg_(dg) {}
+    HyperbolicAlpt(const HyperbolicAlpt&) = delete;
+    ~HyperbolicAlpt() { amdg_linear_destroy(op_); }
+    void assemble_matrix_scalar(const std::vector<double>& coef) {
+        amdg_linear_destroy(op_);
+        op_ = nullptr;
+        check(amdg_linear_create(dg_.handle(), coef.data(), &op_), "amdg_linear_create");
+    }
+    amdg_linear_op* handle() const { return op_; }
+    DGSolution& solution() const { return dg_; }
+
+private:
+    DGSolution& dg_;
+    amdg_linear_op* op_ = nullptr;
+};
+
+class RK3SSP {
+public:
+    RK3SSP(HyperbolicAlpt& op, double dt, amdg_precision prec = AMDG_PREC_FP64) : op_(op), dt_(dt), prec_(prec) {}
+    const int num_stage = 3;
+    // the state stays on the device between init() and final()
+    void init() {}
+    void step_rk() { check(amdg_rk3ssp_steps(op_.handle(), dt_, 1, prec_), "amdg_rk3ssp_steps"); }
+    void final() {}
+
+private:
+    HyperbolicAlpt& op_;
+    double dt_;
+    amdg_precision prec_;
+};
+
+// ---- nonlinear flux (Burgers) through Lagrange interpolation ------------------
+// The reference composes LagrInterpolation::nonlinear_Lagr_fast,
+// HyperbolicLagrRHS::rhs_vol_scalar / rhs_flx_intp_scalar and
+// HyperbolicAlptRHS::rhs_flx_penalty_scalar per stage; on the device the
+// whole right-hand side is one call for the registered flux u^2/2.
+class BurgersLagrRHS {
+public:
+    BurgersLagrRHS(DGSolution& dg, const std::vector<double>& lxf_alpha) {
+        check(amdg_burgers_create(dg.handle(), lxf_alpha.data(), &op_), "amdg_burgers_create");
+    }
+    BurgersLagrRHS(const BurgersLagrRHS&) = delete;
+    ~BurgersLagrRHS() { amdg_burgers_destroy(op_); }
+    void rk3_step(double dt, amdg_precision prec = AMDG_PREC_FP64) {
+        check(amdg_burgers_rk3_steps(op_, dt, 1, prec), "amdg_burgers_rk3_steps");
+    }
+    amdg_burgers_op* handle() const { return op_; }
+
+private:
+    amdg_burgers_op* op_ = nullptr;
+};
+
+inline void synchronize() { check(amdg_context_synchronize(Runtime::context()), "amdg_context_synchronize"); }
+
+}  // namespace amdg_gpu

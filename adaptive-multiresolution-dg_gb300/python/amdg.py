@@ -75,6 +75,12 @@ def load():
         "amdg_rk3ssp_steps_host": ([vp, dbl, i32, vp, i32], i32),
         "amdg_rk3_stage_update": ([vp, i32, dbl, vp, vp, vp, i64], i32),
         "amdg_burgers_create": ([vp, vp, pp], i32),
+        "amdg_burgers_adaptive_step": ([vp, dbl, dbl, dbl, dbl, i32, C.POINTER(dbl)], i32),
+        "amdg_grid_create_ex": ([vp, i32, i32, i32, i32, i32, pp], i32),
+        "amdg_grid_init_separable_adaptive": ([vp, i32, FN1D, vp, dbl], i32),
+        "amdg_grid_refine": ([vp, vp, dbl, C.POINTER(i64)], i32),
+        "amdg_grid_coarsen": ([vp, dbl, C.POINTER(i64)], i32),
+        "amdg_grid_version": ([vp, C.POINTER(i64)], i32),
         "amdg_burgers_destroy": ([vp], i32),
         "amdg_burgers_rhs": ([vp, vp, vp, i32], i32),
         "amdg_burgers_point_values": ([vp, vp, vp, i32], i32),
@@ -167,14 +173,40 @@ class Context:
 class Grid:
     """DGSolution/DGAdapt on the device (sparse or full grid, Alpert degree k)."""
 
-    def __init__(self, ctx: Context, dim: int, nmax: int, k: int = 2, sparse: bool = True):
+    def __init__(self, ctx: Context, dim: int, nmax: int, k: int = 2, sparse: bool = True, level_init: int | None = None):
         self.ctx, self.dim, self.nmax, self.k, self.sparse = ctx, dim, nmax, k, sparse
         self._h = C.c_void_p()
-        _ck(load().amdg_grid_create(ctx.handle, dim, nmax, k, int(sparse), C.byref(self._h)), "grid_create")
+        li = nmax if level_init is None else level_init
+        _ck(load().amdg_grid_create_ex(ctx.handle, dim, li, nmax, k, int(sparse), C.byref(self._h)), "grid_create")
+        self.block = (k + 1) ** dim
+        self._refresh()
+
+    def _refresh(self):
         ne, dof = C.c_int64(), C.c_int64()
         _ck(load().amdg_grid_size(self._h, C.byref(ne), C.byref(dof)), "grid_size")
         self.num_elements, self.dof = ne.value, dof.value
-        self.block = (k + 1) ** dim
+
+    def init_separable_adaptive(self, funcs, eps: float):
+        cb = _fn1d(funcs)
+        _ck(load().amdg_grid_init_separable_adaptive(self._h, len(funcs), cb, None, eps), "grid_init_separable_adaptive")
+        self._refresh()
+
+    def refine(self, eps: float, d_indicator: int | None = None):
+        n = C.c_int64()
+        _ck(load().amdg_grid_refine(self._h, C.c_void_p(d_indicator or 0), eps, C.byref(n)), "grid_refine")
+        self._refresh()
+        return n.value
+
+    def coarsen(self, eta: float):
+        n = C.c_int64()
+        _ck(load().amdg_grid_coarsen(self._h, eta, C.byref(n)), "grid_coarsen")
+        self._refresh()
+        return n.value
+
+    def version(self) -> int:
+        v = C.c_int64()
+        _ck(load().amdg_grid_version(self._h, C.byref(v)), "grid_version")
+        return v.value
 
     @property
     def handle(self):
@@ -290,6 +322,13 @@ class BurgersOperator:
 
     def rk3_steps(self, dt: float, nsteps: int, prec: int = FP64):
         _ck(load().amdg_burgers_rk3_steps(self._h, dt, nsteps, prec), "burgers_rk3_steps")
+
+    def adaptive_step(self, cfl: float, wave_speed: float, eps: float, eta: float, prec: int = FP64) -> float:
+        dt = C.c_double()
+        _ck(load().amdg_burgers_adaptive_step(self._h, cfl, wave_speed, eps, eta, prec, C.byref(dt)),
+            "burgers_adaptive_step")
+        self.grid._refresh()
+        return dt.value
 
     def close(self):
         if self._h:

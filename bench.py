@@ -134,7 +134,9 @@ def run_ours(args):
         import torch.distributed as dist
         dist.init_process_group("nccl")
     ctx = amdg.Context(local)
-    stream = torch.cuda.current_stream()
+    # a non-default stream shared by torch (events) and the library (kernels)
+    stream = torch.cuda.Stream()
+    torch.cuda.set_stream(stream)
     ctx.set_stream(stream.cuda_stream)
     g = amdg.Grid(ctx, DIM, NMAX, K)
     g.init_separable([lambda x, d: math.sin(2 * math.pi * x)])
@@ -242,12 +244,60 @@ def run_ours(args):
         "gpu_launches": launches32,
         "clocks": clocks,
     }
+    line["burgers3d"] = bench_burgers(ctx, stream, args)
     if rank == 0 and world == 1:
         line["cpu_baseline"] = cpu_baseline(g, u0, budget_s=args.cpu_seconds)
     if rank == 0:
         print(json.dumps(line), flush=True)
     if world > 1:
         torch.distributed.destroy_process_group()
+
+
+def bench_burgers(ctx, stream, args):
+    """3D inviscid Burgers, 0.5 + 0.25 sin(2 pi (x+y+z)), sparse grid N=8 (no
+    adaptivity), Lagrange degree-3 flux interpolation, LxF alpha = 1.1 max|u|,
+    SSP-RK3, dt = CFL 0.1 / (max|u| sum_d 2^N): DOF-stage updates/s in both modes."""
+    import torch
+
+    import amdg
+    import amdg_oracle as O
+    dim, N = 3, 8
+    g = amdg.Grid(ctx, dim, N, 2)
+    g.init_separable(O.burgers_ic_terms(dim))
+    u0 = g.coefficients().reshape(-1).copy()
+    umax = 0.75
+    op = amdg.BurgersOperator(g, 1.1 * umax)
+    dt = CFL / (umax * dim * (1 << N))
+    out = {"workload": "3D Burgers, sparse grid N=8 (4096 elements, 110,592 DOF), Lagrange m=3, LxF, SSP-RK3",
+           "dof": g.dof}
+    for name, prec in (("fp64", amdg.FP64), ("mixed", amdg.MIXED)):
+        g.set_coefficients(u0)
+        op.rk3_steps(dt, args.warmup, prec)
+        g.set_coefficients(u0)
+        torch.cuda.synchronize()
+        l0 = ctx.launch_count()
+        s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        s.record(stream)
+        op.rk3_steps(dt, args.steps, prec)
+        e.record(stream)
+        torch.cuda.synchronize()
+        sec = s.elapsed_time(e) / 1e3
+        out[name] = {"value": 3.0 * g.dof * args.steps / sec, "ms_per_step": sec / args.steps * 1e3,
+                     "launches_per_step": (ctx.launch_count() - l0) / args.steps}
+    ref = g.coefficients().reshape(-1).copy()
+    g.set_coefficients(u0)
+    op.rk3_steps(dt, args.steps, amdg.FP64)
+    ctx.synchronize()
+    u64 = g.coefficients().reshape(-1)
+    g.set_coefficients(u0)
+    op.rk3_steps(dt, args.steps, amdg.MIXED)
+    ctx.synchronize()
+    u32 = g.coefficients().reshape(-1)
+    out["mixed_vs_fp64_rel_l2"] = float(np.linalg.norm(u32 - u64) / np.linalg.norm(u64))
+    del ref
+    op.close()
+    g.close()
+    return out
 
 
 def cpu_baseline(g, u0, budget_s=15.0):

@@ -95,6 +95,10 @@ amdg_status amdg_grid_enumerate(int dim, int nmax, int sparse, int64_t* num_elem
  * DGSolution.cpp:675-728).  dim 1..6, nmax*dim <= 60, k 1..3. */
 amdg_status amdg_grid_create(amdg_context* ctx, int dim, int nmax, int k, int sparse, amdg_grid** out);
 amdg_status amdg_grid_destroy(amdg_grid* g);
+/* DGAdapt(sparse, level_init, NMAX, ...) with level_init < NMAX: the sparse
+ * (or full) grid of level level_init whose elements may later refine up to
+ * level nmax (DGAdapt.cpp:5-37). */
+amdg_status amdg_grid_create_ex(amdg_context* ctx, int dim, int level_init, int nmax, int k, int sparse, amdg_grid** out);
 /* DGSolution::size_elem / get_dof (DGSolution.cpp:836-849). */
 amdg_status amdg_grid_size(const amdg_grid* g, int64_t* num_elements, int64_t* dof);
 /* level and suppt of every element, num_elements x dim each (host buffers). */
@@ -113,6 +117,23 @@ amdg_status amdg_grid_coefficients_device(amdg_grid* g, double** device_ptr);
  * (refine threshold not reached), as in the reference drivers that pass
  * refine_eps = 1e10. */
 amdg_status amdg_grid_init_separable(amdg_grid* g, int nterms, amdg_fn1d f, void* user);
+/* DGAdapt::init_separable_scalar_sum with adaptivity (DGAdapt.cpp:120-147,
+ * 850-894): every leaf whose projected block has norm > eps gets its children,
+ * holes are filled, until nothing changes; then the coefficients are set. */
+amdg_status amdg_grid_init_separable_adaptive(amdg_grid* g, int nterms, amdg_fn1d f, void* user, double eps);
+/* DGAdapt::refine (DGAdapt.cpp:371-404): one pass -- leaves whose indicator
+ * (the 2-norm of the element block of d_indicator, or of the grid's own
+ * coefficients when NULL; DGAdapt::indicator_norm :1018-1030) exceeds eps get
+ * all their children up to level nmax, then holes are filled (check_hole).
+ * The grid's coefficients are carried over, new elements start at zero
+ * (copy_predict_to_ucoe).  Operators built on the grid rebuild themselves on
+ * their next call.  num_elements may be NULL. */
+amdg_status amdg_grid_refine(amdg_grid* g, const double* d_indicator, double eps, int64_t* num_elements);
+/* DGAdapt::coarsen (DGAdapt.cpp:675-688, 982-1016): childless elements with
+ * indicator < eta and a level > 0 in some dimension are removed, repeatedly. */
+amdg_status amdg_grid_coarsen(amdg_grid* g, double eta, int64_t* num_elements);
+/* Counter bumped on every change of the element set. */
+amdg_status amdg_grid_version(const amdg_grid* g, int64_t* version);
 /* DGSolution::get_L2_norm (DGSolution.cpp:933-946): sum of squares of all
  * coefficients (the reference returns the squared norm). */
 amdg_status amdg_grid_l2_norm(const amdg_grid* g, double* out);
@@ -163,7 +184,10 @@ amdg_status amdg_rk3_stage_update(amdg_context* ctx, int stage, double dt, const
  * otherwise AMDG_ERR_STATE. */
 amdg_status amdg_burgers_create(amdg_grid* g, const double* alpha, amdg_burgers_op** out);
 amdg_status amdg_burgers_destroy(amdg_burgers_op* op);
-/* One right-hand-side evaluation, d_rhs = R(d_u) (device vectors of dof doubles):
+/* One right-hand-side evaluation, d_rhs = R(d_u) (device vectors of dof doubles).
+ * Point values and the hierarchical surplus run in FP64 in both modes; with
+ * AMDG_PREC_MIXED the transforms back to Alpert coefficients and the penalty
+ * run in FP32.  Composition:
  * LagrInterpolation::nonlinear_Lagr_fast (Interplation.cpp:4033-4047),
  * DGSolution::set_rhs_zero, HyperbolicLagrRHS::rhs_vol_scalar and
  * rhs_flx_intp_scalar (FastMultiplyLU.cpp:1125-1189),
@@ -180,6 +204,14 @@ amdg_status amdg_burgers_flux_coefficients(amdg_burgers_op* op, const double* d_
  * re-evaluated per stage (RK3SSP::step_stage, ODESolver.cpp:285-301, in the
  * stage loop of example/07_vlasov_maxwell_adapt.cpp:278-320). */
 amdg_status amdg_burgers_rk3_steps(amdg_burgers_op* op, double dt, int nsteps, amdg_precision prec);
+
+/* One adaptive time step of the Burgers solver, the loop body of
+ * example/02_hyperbolic_05_burgers_adapt.cpp:223-476 with the Lagrange
+ * right-hand side: dt = cfl / sum_d wave_speed 2^maxlevel_d, forward-Euler
+ * prediction, amdg_grid_refine on the prediction (eps), one SSP-RK3 step,
+ * amdg_grid_coarsen (eta).  dt_out may be NULL. */
+amdg_status amdg_burgers_adaptive_step(amdg_burgers_op* op, double cfl, double wave_speed, double eps, double eta,
+                                       amdg_precision prec, double* dt_out);
 
 #ifdef __cplusplus
 }

@@ -1022,3 +1022,201 @@ int amdg_oracle_burgers_rhs(int dim, int N, int k, int64_t E, const int32_t* lev
     ehash_free(&h);
     return 0;
 }
+
+/* ------------------------------------------------------------------------ */
+/* The reference's fast transforms, restated (FastMultiplyLU.cpp:436-512,   */
+/* 596-664): on adaptive grids the L/U partial sums only see intermediate   */
+/* elements that exist, so they are the reference's operator there; on      */
+/* sparse grids they equal the direct pair sums above.                      */
+/* ------------------------------------------------------------------------ */
+typedef struct {
+    int dim, N, n1;
+    int64_t E;
+    const int32_t* level;
+    const int32_t* suppt;
+    int* order;    /* E x dim */
+    ehash h;
+    int* volc; int* vol;  /* 1D relations */
+    int* flxc; int* flx;
+} fast_ctx;
+
+static int fast_ctx_init(fast_ctx* c, int dim, int N, int64_t E, const int32_t* level, const int32_t* suppt) {
+    c->dim = dim; c->N = N; c->n1 = 1 << N; c->E = E; c->level = level; c->suppt = suppt;
+    c->order = (int*)malloc((size_t)E * dim * sizeof(int));
+    if (!c->order || ehash_build(&c->h, dim, N, E, level, suppt)) return -2;
+    for (int64_t e = 0; e < E * dim; ++e) c->order[e] = order_of_elem(level[e], suppt[e]);
+    const int n1 = c->n1;
+    const long one = 1L << N;
+    c->volc = (int*)calloc(n1, sizeof(int)); c->flxc = (int*)calloc(n1, sizeof(int));
+    c->vol = (int*)malloc((size_t)n1 * n1 * sizeof(int)); c->flx = (int*)malloc((size_t)n1 * n1 * sizeof(int));
+    for (int o = 0; o < n1; ++o) {
+        const elem1d eo = elem_of_order(o);
+        long a, b;
+        support_units(eo.n, eo.j, N, &a, &b);
+        for (int oc = 0; oc < n1; ++oc) {
+            const elem1d ec = elem_of_order(oc);
+            long a2, b2;
+            support_units(ec.n, ec.j, N, &a2, &b2);
+            if (!((a >= b2) || (b <= a2))) c->vol[o * n1 + c->volc[o]++] = oc;
+            if (intersect_or_adjacent(a, b, a2, b2, one)) c->flx[o * n1 + c->flxc[o]++] = oc;
+        }
+    }
+    return 0;
+}
+
+static void fast_ctx_free(fast_ctx* c) {
+    free(c->order); free(c->volc); free(c->flxc); free(c->vol); free(c->flx);
+    ehash_free(&c->h);
+}
+
+/* one 1D transform in dimension t (lu: 0 = "L", 1 = full, 2 = "U"; flx: neighbour set) */
+static void fast_transform_1d(const fast_ctx* c, const double* in, const int* from, double* out, const int* to, int t,
+                              const double* M, int ncols, int lu, int flx, double coef, int accumulate) {
+    const int dim = c->dim, n1 = c->n1;
+    int in_block = 1, out_block = 1, stride = 1;
+    for (int s = 0; s < dim; ++s) { in_block *= from[s]; out_block *= to[s]; }
+    for (int s = t + 1; s < dim; ++s) stride *= from[s];
+    const int nf = from[t], nt = to[t];
+#pragma omp parallel for schedule(dynamic, 16)
+    for (int64_t e = 0; e < c->E; ++e) {
+        const int* oe = c->order + e * dim;
+        const int le = c->level[e * dim + t];
+        int o2[16];
+        memcpy(o2, oe, sizeof(int) * dim);
+        const int cnt = flx ? c->flxc[oe[t]] : c->volc[oe[t]];
+        const int* lst = (flx ? c->flx : c->vol) + (size_t)oe[t] * n1;
+        double* y = out + e * out_block;
+        for (int idx = 0; idx < out_block; ++idx) {
+            const int inner = idx % stride, qt = (idx / stride) % nt, outer = idx / (stride * nt);
+            double acc = 0.0;
+            for (int i = 0; i < cnt; ++i) {
+                const int oc = lst[i];
+                const int ls = elem_of_order(oc).n;
+                if (lu == 0 && le >= ls) continue;
+                if (lu == 2 && le < ls) continue;
+                o2[t] = oc;
+                const int64_t s = ehash_find(&c->h, pack_key(o2, dim, c->N));
+                if (s < 0) continue;
+                const double* x = in + s * in_block + outer * nf * stride + inner;
+                for (int k = 0; k < nf; ++k) acc += x[k * stride] * M[(size_t)(oc * nf + k) * ncols + oe[t] * nt + qt];
+            }
+            acc *= coef;
+            if (accumulate) y[idx] += acc; else y[idx] = acc;
+        }
+    }
+}
+
+/* partial-sum schedule (generate_transform_order): nsum x dim dims and L/full/U tags */
+static int fast_schedule(int dim, int dims[][16], int tags[][16]) {
+    if (dim == 1) { dims[0][0] = 0; tags[0][0] = 1; return 1; }
+    const int nsum = 1 << (dim - 1);
+    for (int s = 0; s < nsum; ++s) {
+        int tag[16];
+        for (int d = 0; d < dim - 1; ++d) tag[d] = 2 * ((s >> (dim - 2 - d)) & 1);
+        tag[dim - 1] = 1;
+        int n = 0;
+        for (int v = 0; v <= 2; ++v)
+            for (int d = 0; d < dim; ++d)
+                if (tag[d] == v) { dims[s][n] = d; tags[s][n] = v; ++n; }
+    }
+    return nsum;
+}
+
+/* sum over the partial sums of dim successive transforms n_in -> n_out, added into out */
+static int fast_partial_sums(const fast_ctx* c, const double* in, int n_in, int n_out, const double* const* M, const int* flx,
+                             double coef, double* out) {
+    const int dim = c->dim;
+    int dims[64][16], tags[64][16];
+    const int nsum = fast_schedule(dim, dims, tags);
+    int maxb = 1;
+    for (int s = 0; s < dim; ++s) maxb *= (n_in > n_out ? n_in : n_out);
+    double* ta = (double*)malloc((size_t)c->E * maxb * sizeof(double));
+    double* tb = (double*)malloc((size_t)c->E * maxb * sizeof(double));
+    if (!ta || !tb) return -2;
+    for (int s = 0; s < nsum; ++s) {
+        int from[16], to[16];
+        for (int d = 0; d < dim; ++d) from[d] = n_in;
+        const double* cur = in;
+        for (int i = 0; i < dim; ++i) {
+            const int t = dims[s][i];
+            memcpy(to, from, sizeof(int) * dim);
+            to[t] = n_out;
+            const int last = (i == dim - 1);
+            double* dst = last ? out : (cur == ta ? tb : ta);
+            fast_transform_1d(c, cur, from, dst, to, t, M[t], c->n1 * n_out, tags[s][i], flx[t], i == 0 ? coef : 1.0, last);
+            cur = dst;
+            memcpy(from, to, sizeof(int) * dim);
+        }
+    }
+    free(ta); free(tb);
+    return 0;
+}
+
+/* Alpert basis at Lagrange points, rows = Alpert basis, cols = Lagrange point (Interplation.cpp:16-101) */
+static double* alpt_at_lagr_points(int N, int k) {
+    const int np = k + 1, n1 = 1 << N, na = n1 * np, nl = n1 * 4;
+    double* m = (double*)calloc((size_t)na * nl, sizeof(double));
+    for (int c = 0; c < nl; ++c) {
+        const elem1d el = elem_of_order(c / 4);
+        const double x = amdg_oracle_lagr_point(el.n, el.j, c % 4);
+        for (int r = 0; r < na; ++r) {
+            const elem1d ea = elem_of_order(r / np);
+            if (x < support_lo(ea.n, ea.j) || x > support_hi(ea.n, ea.j)) continue;
+            m[(size_t)r * nl + c] = amdg_oracle_alpert_val(k, ea.n, ea.j, r % np, 0, x, 0);
+        }
+    }
+    return m;
+}
+
+int amdg_oracle_lagr_point_values_fast(int dim, int N, int k, int64_t E, const int32_t* level, const int32_t* suppt,
+                                       const double* u, double* up) {
+    fast_ctx c;
+    if (fast_ctx_init(&c, dim, N, E, level, suppt)) return -2;
+    double* a2p = alpt_at_lagr_points(N, k);
+    const double* M[16];
+    int flx[16];
+    for (int d = 0; d < dim; ++d) { M[d] = a2p; flx[d] = 0; }
+    memset(up, 0, (size_t)E * ipow(4, dim) * sizeof(double));
+    int rc = fast_partial_sums(&c, u, k + 1, 4, M, flx, 1.0, up);
+    free(a2p);
+    fast_ctx_free(&c);
+    return rc;
+}
+
+/* Burgers RHS by the reference's fast transforms (HyperbolicLagrRHS::rhs_vol_scalar,
+ * rhs_flx_intp_scalar, HyperbolicAlptRHS::rhs_flx_penalty_scalar) */
+int amdg_oracle_burgers_rhs_fast(int dim, int N, int k, int64_t E, const int32_t* level, const int32_t* suppt,
+                                 const double* fucoe, const double* u, double alpha, double* rhs) {
+    const int np = k + 1, n1 = 1 << N, nr = n1 * 4, nc = n1 * np;
+    const int B = ipow(np, dim), P = ipow(4, dim);
+    fast_ctx c;
+    if (fast_ctx_init(&c, dim, N, E, level, suppt)) return -2;
+    double* Lv = (double*)malloc((size_t)nr * nc * sizeof(double));
+    double* Lvx = (double*)malloc((size_t)nr * nc * sizeof(double));
+    double* Lf = (double*)malloc((size_t)nr * nc * sizeof(double));
+    double* ul = (double*)malloc((size_t)nc * nc * sizeof(double));
+    double* ur = (double*)malloc((size_t)nc * nc * sizeof(double));
+    if (!Lv || !Lvx || !Lf || !ul || !ur) return -2;
+    amdg_oracle_oper1d_lagr(N, k, Lv, Lvx, Lf);
+    amdg_oracle_oper1d(N, k, NULL, NULL, ul, ur);
+    for (size_t i = 0; i < (size_t)nc * nc; ++i) ur[i] = ur[i] - ul[i]; /* ujp_vjp */
+    memset(rhs, 0, (size_t)E * B * sizeof(double));
+    int rc = 0;
+    for (int d = 0; d < dim && !rc; ++d) {
+        for (int term = 0; term < 2 && !rc; ++term) {
+            const double* M[16];
+            int flx[16];
+            for (int s = 0; s < dim; ++s) {
+                M[s] = (s == d) ? (term == 0 ? Lvx : Lf) : Lv;
+                flx[s] = (term == 1 && s == d);
+            }
+            rc = fast_partial_sums(&c, fucoe + (size_t)d * E * P, 4, np, M, flx, term == 0 ? 1.0 : 0.5, rhs);
+        }
+        int from[16];
+        for (int s = 0; s < dim; ++s) from[s] = np;
+        fast_transform_1d(&c, u, from, rhs, from, d, ur, nc, 1, 1, -alpha / 2.0, 1);
+    }
+    free(Lv); free(Lvx); free(Lf); free(ul); free(ur);
+    fast_ctx_free(&c);
+    return rc;
+}

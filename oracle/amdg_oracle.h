@@ -86,6 +86,14 @@ int amdg_oracle_lagr_surplus(int dim, int N, int64_t E, const int32_t* level, co
 int amdg_oracle_burgers_rhs(int dim, int N, int k, int64_t E, const int32_t* level, const int32_t* suppt,
                             const double* fucoe, const double* u, double alpha, double* rhs);
 
+/* The same two quantities by the reference's fast L/U partial-sum transforms
+ * (the reference's operator on adaptive grids; equal to the direct sums on
+ * sparse grids). */
+int amdg_oracle_lagr_point_values_fast(int dim, int N, int k, int64_t E, const int32_t* level, const int32_t* suppt,
+                                       const double* u, double* up);
+int amdg_oracle_burgers_rhs_fast(int dim, int N, int k, int64_t E, const int32_t* level, const int32_t* suppt,
+                                 const double* fucoe, const double* u, double alpha, double* rhs);
+
 #ifdef __cplusplus
 }
 #endif

@@ -64,6 +64,9 @@ def lib():
         L.amdg_oracle_lagr_surplus.argtypes = [C.c_int, C.c_int, C.c_int64, i32p, i32p, f64p, f64p]
         L.amdg_oracle_burgers_rhs.argtypes = [C.c_int, C.c_int, C.c_int, C.c_int64, i32p, i32p, f64p, f64p, C.c_double,
                                               f64p]
+        L.amdg_oracle_lagr_point_values_fast.argtypes = [C.c_int, C.c_int, C.c_int, C.c_int64, i32p, i32p, f64p, f64p]
+        L.amdg_oracle_burgers_rhs_fast.argtypes = [C.c_int, C.c_int, C.c_int, C.c_int64, i32p, i32p, f64p, f64p,
+                                                   C.c_double, f64p]
         _lib = L
     return _lib
 
@@ -203,15 +206,29 @@ def lagr_surplus(dim, N, level, suppt, fp):
     return out
 
 
-def burgers_rhs(dim, N, k, level, suppt, u, alpha):
-    """Full Burgers RHS: point values -> flux u^2/2 -> surplus -> volume/interface/penalty terms."""
-    up = lagr_point_values(dim, N, k, level, suppt, u)
+def lagr_point_values_fast(dim, N, k, level, suppt, u):
+    up = np.zeros((level.shape[0], 4 ** dim))
+    _check(lib().amdg_oracle_lagr_point_values_fast(dim, N, k, level.shape[0], level, suppt, np.ascontiguousarray(u),
+                                                    up))
+    return up
+
+
+def burgers_rhs(dim, N, k, level, suppt, u, alpha, direct=False):
+    """Full Burgers RHS: point values -> flux u^2/2 -> surplus -> volume/interface/penalty terms.
+    direct=False follows the reference's fast L/U transforms (its operator on any
+    hole-free grid); direct=True sums element pairs directly (equal on sparse grids)."""
+    level = np.ascontiguousarray(level, np.int32)
+    suppt = np.ascontiguousarray(suppt, np.int32)
+    if direct:
+        up = lagr_point_values(dim, N, k, level, suppt, u)
+    else:
+        up = lagr_point_values_fast(dim, N, k, level, suppt, u)
     fp = 0.5 * up * up
     fu = lagr_surplus(dim, N, level, suppt, fp)
     fucoe = np.ascontiguousarray(np.broadcast_to(fu, (dim,) + fu.shape))
     rhs = np.zeros_like(u)
-    _check(lib().amdg_oracle_burgers_rhs(dim, N, k, level.shape[0], level, suppt, fucoe, np.ascontiguousarray(u),
-                                         float(alpha), rhs))
+    fn = lib().amdg_oracle_burgers_rhs if direct else lib().amdg_oracle_burgers_rhs_fast
+    _check(fn(dim, N, k, level.shape[0], level, suppt, fucoe, np.ascontiguousarray(u), float(alpha), rhs))
     return rhs, up, fu
 
 
@@ -238,3 +255,161 @@ def burgers_ic_terms(dim):
     for f in sin_sum_terms(dim):
         terms.append(lambda x, d, f=f: (0.25 if d == 0 else 1.0) * f(x, d))
     return terms
+
+
+# ---------------------------------------------------------------------------
+# Adaptivity (DGAdapt::refine / coarsen / check_hole, DGAdapt.cpp:371-404,
+# 675-688, 982-1063, 1250-1385; adaptive separable initialisation,
+# DGAdapt.cpp:120-147, 850-894).  Elements are tuples of 1D orders.
+# ---------------------------------------------------------------------------
+
+def _level(o):
+    return int(o).bit_length()
+
+
+def _elem_of_order(o):
+    o = int(o)
+    if o == 0:
+        return 0, 1
+    n = o.bit_length()
+    return n, 2 * (o - (1 << (n - 1))) + 1
+
+
+def keys_to_arrays(keys, dim):
+    level = np.zeros((len(keys), dim), np.int32)
+    suppt = np.zeros((len(keys), dim), np.int32)
+    for i, key in enumerate(keys):
+        for d, o in enumerate(key):
+            level[i, d], suppt[i, d] = _elem_of_order(o)
+    return level, suppt
+
+
+def arrays_to_keys(level, suppt):
+    keys = []
+    for lv, sp in zip(level, suppt):
+        keys.append(tuple(0 if n == 0 else (1 << (int(n) - 1)) + (int(j) - 1) // 2 for n, j in zip(lv, sp)))
+    return keys
+
+
+def children_of(key, nmax):
+    out = []
+    for d, o in enumerate(key):
+        n = _level(o)
+        if n == 0:
+            cs = [1]
+        elif n == nmax:
+            cs = []
+        else:
+            cs = [2 * o, 2 * o + 1]
+        for c in cs:
+            out.append(key[:d] + (c,) + key[d + 1:])
+    return out
+
+
+def parents_of(key):
+    out = []
+    for d, o in enumerate(key):
+        if o == 0:
+            continue
+        p = 0 if o == 1 else o // 2
+        out.append(key[:d] + (p,) + key[d + 1:])
+    return out
+
+
+def fill_holes(keyset):
+    work = list(keyset)
+    while work:
+        nxt = []
+        for key in work:
+            for p in parents_of(key):
+                if p not in keyset:
+                    keyset.add(p)
+                    nxt.append(p)
+        work = nxt
+    return keyset
+
+
+def refine_keys(keys, norms, eps, nmax):
+    """One refine pass: leaves (fewer existing children than possible) whose
+    indicator exceeds eps get all their children, then holes are filled."""
+    keyset = set(keys)
+    new = set(keyset)
+    for key, nrm in zip(keys, norms):
+        ch = children_of(key, nmax)
+        if sum(c in keyset for c in ch) < len(ch) and nrm > eps:
+            new.update(ch)
+    return sorted(fill_holes(new))
+
+
+def coarsen_keys(keys, norms, eta):
+    """Repeatedly delete childless elements with indicator < eta and max level > 0."""
+    keyset = set(keys)
+    norm = dict(zip(keys, norms))
+    nmax = 64
+    changed = True
+    while changed:
+        changed = False
+        kids = {k: 0 for k in keyset}
+        for k in keyset:
+            for p in parents_of(k):
+                if p in kids:
+                    kids[p] += 1
+        for k in list(keyset):
+            if kids[k] == 0 and norm[k] < eta and max(_level(o) for o in k) > 0:
+                keyset.discard(k)
+                changed = True
+    del nmax
+    return sorted(keyset)
+
+
+def element_norms(u):
+    return np.sqrt(np.sum(np.asarray(u) ** 2, axis=1))
+
+
+def init_adaptive_separable(dim, n_init, nmax, k, terms, eps):
+    """Adaptive initialisation: start from the sparse grid of level n_init,
+    refine every leaf whose projected coefficients exceed eps, fill holes,
+    repeat until nothing changes."""
+    coef = project_separable(nmax, k, dim, terms)
+    lv, sp = grid(dim, n_init)
+    keys = arrays_to_keys(lv, sp)
+    while True:
+        lv, sp = keys_to_arrays(keys, dim)
+        u = init_separable(dim, nmax, k, lv, sp, coef)
+        nrm = element_norms(u)
+        new = refine_keys(keys, nrm, eps, nmax)
+        if len(new) == len(keys):
+            return keys, u
+        keys = new
+
+
+def remap(old_keys, u_old, new_keys):
+    pos = {k: i for i, k in enumerate(old_keys)}
+    out = np.zeros((len(new_keys), u_old.shape[1]))
+    for i, k in enumerate(new_keys):
+        j = pos.get(k)
+        if j is not None:
+            out[i] = u_old[j]
+    return out
+
+
+def burgers_adaptive_run(dim, n_init, nmax, eps, eta, alpha, cfl, umax, steps, k=2):
+    """The adaptive Burgers time loop: predictor, refine, RK3, coarsen."""
+    keys, u = init_adaptive_separable(dim, n_init, nmax, k, burgers_ic_terms(dim), eps)
+    history = [(list(keys), u.copy(), None)]
+    for _ in range(steps):
+        lv, sp = keys_to_arrays(keys, dim)
+        maxlev = lv.max(axis=0)
+        dt = cfl / sum(umax * 2.0 ** int(m) for m in maxlev)
+        rhs = burgers_rhs(dim, nmax, k, lv, sp, u, alpha)[0]
+        pred = u + dt * rhs
+        new_keys = refine_keys(keys, element_norms(pred), eps, nmax)
+        u = remap(keys, u, new_keys)
+        keys = new_keys
+        lv, sp = keys_to_arrays(keys, dim)
+        u = burgers_rk3(dim, nmax, k, lv, sp, u, alpha, dt, 1)
+        new_keys = coarsen_keys(keys, element_norms(u), eta)
+        u = remap(keys, u, new_keys)
+        keys = new_keys
+        history.append((list(keys), u.copy(), dt))
+    return history

@@ -21,6 +21,14 @@
 //     step_stage, sparse grid without adaptivity (07_vlasov_maxwell_adapt.cpp
 //     stage loop).  Dumps u0, up0 (point values), fu0_d (interpolation
 //     coefficients of the flux in dimension d), rhs0 and uT.
+//   ref_harness burgers_adapt <dim> <N_init> <NMAX> <eps> <eta> <alpha> <cfl> <umax> <steps>
+//     adaptive version of the above, following the time loop of
+//     example/02_hyperbolic_05_burgers_adapt.cpp:223-476 with the Lagrange
+//     right-hand side: adaptive separable initialisation, then per step
+//     dt = cfl / sum_d umax 2^maxlevel_d, copy_ucoe_to_predict, ForwardEuler
+//     predictor, refine, copy_predict_to_ucoe, three RK3SSP stages, coarsen.
+//     Dumps the element set and coefficients after init (u_init) and after
+//     every step (u_step<i>), with the step sizes.
 //   ref_harness matrices <N> <k>
 //     dumps the 1D operator matrices u_v, u_vx, ulft_vjp, urgt_vjp.
 //
@@ -311,6 +319,99 @@ int run_burgers(int argc, char** argv) {
     return 0;
 }
 
+int run_burgers_adapt(int argc, char** argv) {
+    if (argc < 11) { std::fprintf(stderr, "burgers_adapt: bad args\n"); return 2; }
+    const int dim = std::atoi(argv[2]);
+    const int N_init = std::atoi(argv[3]);
+    const int NMAX = std::atoi(argv[4]);
+    const double eps = std::atof(argv[5]);
+    const double eta = std::atof(argv[6]);
+    const double alpha = std::atof(argv[7]);
+    const double cfl = std::atof(argv[8]);
+    const double umax = std::atof(argv[9]);
+    const int steps = std::atoi(argv[10]);
+    const int k = 2;
+    set_statics(dim, k);
+    Hash hash;
+    LagrBasis::set_interp_msh01();
+    HermBasis::set_interp_msh01();
+    AllBasis<AlptBasis> all_bas_alpt(NMAX);
+    AllBasis<LagrBasis> all_bas_lagr(NMAX);
+    AllBasis<HermBasis> all_bas_herm(NMAX);
+    OperatorMatrix1D<AlptBasis, AlptBasis> oper_alpt(all_bas_alpt, all_bas_alpt, "period");
+    OperatorMatrix1D<LagrBasis, AlptBasis> oper_lagr(all_bas_lagr, all_bas_alpt, "period");
+    DGAdapt dg(true, N_init, NMAX, all_bas_alpt, all_bas_lagr, all_bas_herm, hash, eps, eta, true, false);
+
+    const double PI = Const::PI;
+    std::vector<std::function<double(double, int)>> funcs;
+    funcs.push_back([](double, int d) { return d == 0 ? 0.5 : 1.0; });
+    for (int mask = 0; mask < (1 << dim); ++mask) {
+        int nsin = __builtin_popcount(mask);
+        if (nsin % 2 == 0) continue;
+        const double sign = ((nsin - 1) / 2) % 2 == 0 ? 0.25 : -0.25;
+        funcs.push_back([=](double x, int d) {
+            double v = ((mask >> d) & 1) ? std::sin(2 * PI * x) : std::cos(2 * PI * x);
+            return d == 0 ? sign * v : v;
+        });
+    }
+    dg.init_separable_scalar_sum(funcs);
+    std::printf("META dim=%d N=%d k=%d sparse=1 elements=%zu dof=%d\n", dim, NMAX, k, dg.dg.size(), dg.get_dof());
+    dump_elements("u_init", dg, 0);
+
+    auto flux = [](std::vector<double> u, int, int) -> double { return FluxFunction::burgers_flux_scalar(u[0]); };
+    std::vector<std::vector<bool>> is_intp(1, std::vector<bool>(dim, true));
+    HyperbolicLagrRHS rhs_lagr(dg, oper_lagr);
+    HyperbolicAlptRHS rhs_alpt(dg, oper_alpt);
+    const std::vector<double> lxf(dim, alpha);
+    double t = 0.0;
+    for (int step = 0; step < steps; ++step) {
+        const std::vector<int> max_mesh = dg.max_mesh_level_vec();
+        double sum_c_dx = 0.;
+        for (int d = 0; d < dim; ++d) sum_c_dx += umax * std::pow(2., max_mesh[d]);
+        const double dt = cfl / sum_c_dx;
+        // LagrInterpolation and FastLagrIntp hold per-grid data: rebuild after adaptation
+        auto rhs_eval = [&]() {
+            LagrInterpolation interp(dg);
+            FastLagrIntp fast_lagr(dg, interp.Lag_pt_Alpt_1D, interp.Lag_pt_Alpt_1D_d1);
+            interp.nonlinear_Lagr_fast(flux, is_intp, fast_lagr);
+            dg.set_rhs_zero();
+            rhs_lagr.rhs_vol_scalar();
+            rhs_lagr.rhs_flx_intp_scalar();
+            rhs_alpt.rhs_flx_penalty_scalar(lxf);
+        };
+        dg.copy_ucoe_to_predict();
+        {
+            ForwardEuler ode(dg, dt);
+            ode.init();
+            rhs_eval();
+            ode.set_rhs_zero();
+            ode.add_rhs_to_eigenvec();
+            ode.step_stage(0);
+            ode.final();
+        }
+        dg.refine();
+        dg.copy_predict_to_ucoe();
+        {
+            RK3SSP ode(dg, dt);
+            ode.init();
+            for (int stage = 0; stage < 3; ++stage) {
+                rhs_eval();
+                ode.set_rhs_zero();
+                ode.add_rhs_to_eigenvec();
+                ode.step_stage(stage);
+                ode.final();
+            }
+        }
+        dg.coarsen();
+        t += dt;
+        std::printf("STEP %d dt=%.17g elements=%zu\n", step, dt, dg.dg.size());
+        char nm[32];
+        std::snprintf(nm, sizeof nm, "u_step%d", step);
+        dump_elements(nm, dg, 0);
+    }
+    return 0;
+}
+
 int run_matrices(int argc, char** argv) {
     if (argc < 4) return 2;
     const int N = std::atoi(argv[2]);
@@ -333,6 +434,7 @@ int main(int argc, char** argv) {
     if (mode == "linear") return run_linear(argc, argv);
     if (mode == "matrices") return run_matrices(argc, argv);
     if (mode == "burgers") return run_burgers(argc, argv);
+    if (mode == "burgers_adapt") return run_burgers_adapt(argc, argv);
     std::fprintf(stderr, "unknown mode %s\n", mode.c_str());
     return 2;
 }

@@ -79,6 +79,13 @@ BURGERS_CASES = [
 ]
 
 
+# (name, dim, n_init, nmax, eps, eta, alpha, cfl, umax, steps): adaptive Burgers time loop
+BURGERS_ADAPT_CASES = [
+    ("burgers_adapt2d", 2, 3, 7, 1e-4, 1e-5, 0.825, 0.1, 0.75, 4),
+    ("burgers_adapt3d", 3, 3, 6, 3e-5, 3e-6, 0.825, 0.1, 0.75, 2),
+]
+
+
 def main():
     if not os.path.exists(HARNESS):
         sys.exit("build the reference first: make -C oracle ref")
@@ -105,6 +112,16 @@ def main():
         np.savez_compressed(os.path.join(HERE, name + ".npz"), **arrs)
         manifest[name] = dict(kind="burgers", dim=dim, N=N, k=2, alpha=alpha, steps=steps, dt=dt,
                               elements=int(r["meta"]["elements"]))
+        print(name, r["meta"])
+    for name, dim, n0, nmax, eps, eta, alpha, cfl, umax, steps in BURGERS_ADAPT_CASES:
+        r = run(["burgers_adapt", dim, n0, nmax, repr(eps), repr(eta), repr(alpha), repr(cfl), repr(umax), steps])
+        arrs = {}
+        for i, key in enumerate(["u_init"] + [f"u_step{s}" for s in range(steps)]):
+            lv, sp, u = split_elements(r[key], dim)
+            arrs[f"level_{i}"], arrs[f"suppt_{i}"], arrs[f"u_{i}"] = lv, sp, u
+        np.savez_compressed(os.path.join(HERE, name + ".npz"), **arrs)
+        manifest[name] = dict(kind="burgers_adapt", dim=dim, n_init=n0, nmax=nmax, eps=eps, eta=eta, alpha=alpha,
+                              cfl=cfl, umax=umax, steps=steps)
         print(name, r["meta"])
     for N, k in [(4, 2), (3, 1), (3, 3)]:
         r = run(["matrices", N, k])

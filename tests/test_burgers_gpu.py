@@ -2,7 +2,9 @@
 reference fixtures and the oracle.  Tolerances: FP64 1e-12 relative to the
 field's max norm for point values, flux coefficients and RK3 steps, 5e-12 for
 one RHS (a difference of larger volume and interface terms); mixed mode
-(FP32 transforms, FP64 state) 1e-5 for one RHS and 1e-6 for RK3 steps."""
+(FP64 point values and surplus, FP32 back transforms and penalty, FP64
+state) 1e-4 relative in the L2 norm for one RHS (FP32 rounding of back
+transforms whose 1D matrices grow like 2^level) and 1e-6 for RK3 steps."""
 import numpy as np
 import pytest
 
@@ -51,7 +53,8 @@ def test_burgers_matches_reference(ctx, name):
     rhs = run_on(ctx, op.rhs_device, u0, g.dof).reshape(-1, g.block)
     assert rel_err(rhs, z["rhs0"][perm]) < 5e-12
     rhs32 = run_on(ctx, lambda a, b: op.rhs_device(a, b, amdg.MIXED), u0, g.dof).reshape(-1, g.block)
-    assert rel_err(rhs32, z["rhs0"][perm]) < 1e-5
+    ref = z["rhs0"][perm]
+    assert np.linalg.norm(rhs32 - ref) / np.linalg.norm(ref) < 1e-4
     g.set_coefficients(u0)
     op.rk3_steps(m["dt"], m["steps"], amdg.FP64)
     ctx.synchronize()

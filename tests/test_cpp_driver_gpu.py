@@ -1,0 +1,37 @@
+"""The C++ mirror of the reference driver API (host/amdg_dg.hpp): the
+example driver built like example/02_hyperbolic_01_scalar_const_coefficient.cpp
+runs on the GPU and reproduces the oracle's L2 error."""
+import math
+import os
+import subprocess
+
+import numpy as np
+import pytest
+
+import amdg
+import amdg_oracle as O
+
+pytestmark = pytest.mark.gpu
+
+EXE = os.path.join(os.path.dirname(amdg.LIB_PATH), "hyperbolic_const_coefficient")
+
+
+def test_cpp_driver_matches_oracle():
+    assert os.path.exists(EXE), "example driver not built"
+    N, T = 5, 0.05
+    out = subprocess.run([EXE, str(N), str(T)], capture_output=True, text=True, timeout=300, check=True).stdout
+    fields = dict(line.split(":", 1) for line in out.splitlines() if ":" in line)
+    err = float(fields["L2 error at final time"])
+    head = out.splitlines()[0].split()
+    steps, dt = int(head[5]), float(head[7])
+    dim, k = 2, 2
+    lv, sp = O.grid(dim, N)
+    u0 = O.init_separable(dim, N, k, lv, sp, O.project_separable(N, k, dim, O.sin_sum_terms(dim)))
+    uT = O.linear_rk3(dim, N, k, lv, sp, [1.0, 1.0], u0, dt, steps)
+    exact = O.project_separable(N, k, dim, O.sin_sum_terms(dim, shift=2 * T))
+    # |u - u_h|^2 = 1/2 + |u_h|^2 - 2 sum_terms <u_h, term>
+    n2 = float(np.sum(uT * uT))
+    cross = sum(0.5 * (1.0 + n2 - O.l2_error_split(dim, N, k, lv, sp, uT, exact[t], 1.0) ** 2) for t in range(2))
+    ref = math.sqrt(max(0.0, 0.5 + n2 - 2.0 * cross))
+    assert abs(err - ref) <= 1e-6 * ref
+    assert ref < 1e-3

@@ -133,3 +133,34 @@ def test_lagrange_basis_interpolates_its_nodes():
                 x = O.lib().amdg_oracle_lagr_point(n, j, q)
                 v = O.lib().amdg_oracle_lagr_val(n, j, p, x, 0)
                 assert abs(v - (1.0 if p == q else 0.0)) < 1e-13
+
+
+ADAPT = [n for n, m in manifest().items() if m["kind"] == "burgers_adapt"]
+
+
+@pytest.mark.parametrize("name", ADAPT)
+def test_adaptive_burgers_matches_reference(name):
+    """Element sets bit-exact and coefficients to 1e-12 after adaptive init and
+    every predictor/refine/RK3/coarsen step of the reference time loop."""
+    m = manifest()[name]
+    z = golden(name)
+    dim = m["dim"]
+    hist = O.burgers_adaptive_run(dim, m["n_init"], m["nmax"], m["eps"], m["eta"], m["alpha"], m["cfl"], m["umax"],
+                                  m["steps"])
+    for i, (keys, u, _dt) in enumerate(hist):
+        ref_keys = O.arrays_to_keys(z[f"level_{i}"], z[f"suppt_{i}"])
+        assert set(ref_keys) == set(keys), f"element set differs after step {i}"
+        pos = {k: j for j, k in enumerate(ref_keys)}
+        perm = np.array([pos[k] for k in keys])
+        assert rel_err(u, z[f"u_{i}"][perm]) < 1e-12
+
+
+def test_fast_transforms_equal_direct_sums_on_sparse_grids():
+    """On a sparse grid the reference's L/U partial sums equal the direct sums
+    over element pairs (an independent check of both formulations)."""
+    dim, N, k = 3, 4, 2
+    lv, sp = O.grid(dim, N)
+    u = O.init_separable(dim, N, k, lv, sp, O.project_separable(N, k, dim, O.burgers_ic_terms(dim)))
+    a = O.burgers_rhs(dim, N, k, lv, sp, u, 0.8)[0]
+    b = O.burgers_rhs(dim, N, k, lv, sp, u, 0.8, direct=True)[0]
+    assert rel_err(a, b) < 1e-12
