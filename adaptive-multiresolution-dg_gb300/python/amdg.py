@@ -74,6 +74,7 @@ def load():
         "amdg_rk3ssp_steps": ([vp, dbl, i32, i32], i32),
         "amdg_rk3ssp_steps_host": ([vp, dbl, i32, vp, i32], i32),
         "amdg_rk3_stage_update": ([vp, i32, dbl, vp, vp, vp, i64], i32),
+        "amdg_rk3ssp_steps_noalloc": ([vp, vp, dbl, i32, i32], i32),
         "amdg_burgers_create": ([vp, vp, pp], i32),
         "amdg_burgers_adaptive_step": ([vp, dbl, dbl, dbl, dbl, i32, C.POINTER(dbl)], i32),
         "amdg_grid_create_ex": ([vp, i32, i32, i32, i32, i32, pp], i32),
@@ -282,6 +283,10 @@ class LinearOperator:
 
     def rk3_steps(self, dt: float, nsteps: int, prec: int = FP64):
         _ck(load().amdg_rk3ssp_steps(self._h, dt, nsteps, prec), "rk3ssp_steps")
+
+    def rk3_steps_noalloc(self, d_u: int, dt: float, nsteps: int, prec: int = FP64):
+        """RK3 steps on the caller's device vector without any device allocation."""
+        _ck(load().amdg_rk3ssp_steps_noalloc(self._h, C.c_void_p(d_u), dt, nsteps, prec), "rk3ssp_steps_noalloc")
 
     def rk3_steps_host(self, u: np.ndarray, dt: float, nsteps: int, prec: int = FP64):
         assert u.dtype == np.float64 and u.flags.c_contiguous and u.size == self.grid.dof

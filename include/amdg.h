@@ -165,6 +165,17 @@ amdg_status amdg_rk3ssp_steps(amdg_linear_op* op, double dt, int nsteps, amdg_pr
  * ODESolver.cpp:25-60). */
 amdg_status amdg_rk3ssp_steps_host(amdg_linear_op* op, double dt, int nsteps, double* host_u, amdg_precision prec);
 
+/* Allocation-free variant of amdg_rk3ssp_steps, with no counterpart in the
+ * reference: for callers that cannot call cudaMalloc (code running during CUDA
+ * stream capture, host callbacks, processes whose device memory belongs to
+ * another allocator).  d_u is the caller's device state (dof doubles, input
+ * and output).  The stage vectors live in a fixed 4 MiB device array shared by
+ * every call, so the grid may hold at most 262,144 coefficients (larger grids
+ * get AMDG_ERR_CAPACITY) and calls that overlap on the GPU race.  The first
+ * call on a device looks up the array's address; make it before any stream
+ * capture. */
+amdg_status amdg_rk3ssp_steps_noalloc(amdg_linear_op* op, double* d_u, double dt, int nsteps, amdg_precision prec);
+
 /* ---- stage updates for an externally computed right-hand side ----------- */
 /* RK3SSP::step_stage / ForwardEuler::step_stage (ODESolver.cpp:209-213,
  * 285-301) on device vectors of n doubles: stage 0 u = un + dt*rhs,
