@@ -112,6 +112,7 @@ void build_linear_topology(const HostGrid& g, const Oper1D& op, const double* co
 struct TransformTopology {
     std::vector<int32_t> vol_ptr, vol_src, vol_lev;  // ptr: num_elements*dim + 1
     std::vector<int32_t> flx_ptr, flx_src, flx_lev;
+    std::vector<int32_t> vol_split, flx_split;       // [e*dim+t]: first neighbour finer than e in t
 };
 void build_transform_topology(const HostGrid& g, TransformTopology* out);
 // surplus ancestors: [e][d][ic] element index (-1 for level 0 in d); false if a hole is found
@@ -157,6 +158,7 @@ struct amdg_linear_op {
     float* d_blocks32 = nullptr;
     double* d_u1 = nullptr;          // RK stage vectors
     double* d_u2 = nullptr;
+    float* d_shadow = nullptr;       // mixed mode: float copies of u, u1, u2 (3 x capacity)
 };
 
 struct amdg_burgers_op {
@@ -173,6 +175,7 @@ struct amdg_burgers_op {
     // neighbour lists of the fast transforms and the surplus ancestors
     int32_t *d_vol_ptr = nullptr, *d_vol_src = nullptr, *d_vol_lev = nullptr;
     int32_t *d_flx_ptr = nullptr, *d_flx_src = nullptr, *d_flx_lev = nullptr;
+    int32_t *d_vol_split = nullptr, *d_flx_split = nullptr;
     int32_t *d_anc = nullptr, *d_anc_point = nullptr, *d_anc_rank = nullptr;
     double weight[16] = {0};
     std::vector<std::vector<int>> sched_dims, sched_lu;

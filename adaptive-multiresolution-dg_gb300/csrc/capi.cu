@@ -175,14 +175,27 @@ amdg_status rk3_steps_device(amdg_linear_op* op, double dt, int nsteps, amdg_pre
     cudaStream_t st = stream_of(g->ctx);
     LinearLaunch L = linear_launch(op);
     const bool mixed = prec == AMDG_PREC_MIXED;
+    // mixed mode reads neighbours from float shadows of the stage inputs; the
+    // shadow of u is refreshed once per call, later ones come from the epilogues
+    float* s_u = op->d_shadow;
+    float* s_1 = mixed ? op->d_shadow + op->capacity : nullptr;
+    float* s_2 = mixed ? op->d_shadow + 2 * op->capacity : nullptr;
+    if (mixed && nsteps > 0) {
+        AMDG_CK(launch_to_float(g->d_u, s_u, g->dof, st));
+        g->ctx->launches++;
+    }
     for (int s = 0; s < nsteps; ++s) {
         // u1 = u + dt L(u); u2 = 3/4 u + 1/4 (u1 + dt L(u1)); u = 1/3 u + 2/3 (u2 + dt L(u2))
         double* in[3] = {g->d_u, op->d_u1, op->d_u2};
         double* outp[3] = {op->d_u1, op->d_u2, g->d_u};
+        float* sin_[3] = {s_u, s_1, s_2};
+        float* sout[3] = {s_1, s_2, s_u};
         for (int stage = 0; stage < 3; ++stage) {
             L.us = in[stage];
             L.un = g->d_u;
             L.out = outp[stage];
+            L.us_shadow = mixed ? sin_[stage] : nullptr;
+            L.shadow_out = mixed ? sout[stage] : nullptr;
             AMDG_CK(launch_linear(L, mixed, rk3_stage_coef(stage, dt), st));
             g->ctx->launches++;
         }
@@ -216,8 +229,11 @@ amdg_status linear_sync(amdg_linear_op* op) {
     if (g->dof > op->capacity) {
         cudaFree(op->d_u1);
         cudaFree(op->d_u2);
+        cudaFree(op->d_shadow);
         op->d_u1 = op->d_u2 = nullptr;
-        if ((s = dev_alloc(&op->d_u1, size_t(g->dof))) != AMDG_OK || (s = dev_alloc(&op->d_u2, size_t(g->dof))) != AMDG_OK)
+        op->d_shadow = nullptr;
+        if ((s = dev_alloc(&op->d_u1, size_t(g->dof))) != AMDG_OK || (s = dev_alloc(&op->d_u2, size_t(g->dof))) != AMDG_OK ||
+            (s = dev_alloc(&op->d_shadow, size_t(g->dof) * 3)) != AMDG_OK)
             return s;
         op->capacity = g->dof;
     }
@@ -602,6 +618,7 @@ amdg_status amdg_linear_destroy(amdg_linear_op* op) {
     cudaFree(op->d_blocks32);
     cudaFree(op->d_u1);
     cudaFree(op->d_u2);
+    cudaFree(op->d_shadow);
     delete op;
     return AMDG_OK;
 }
@@ -625,7 +642,13 @@ amdg_status amdg_linear_apply(amdg_linear_op* op, const double* d_u, double* d_r
     L.us = d_u;
     L.un = nullptr;
     L.out = d_rhs;
-    AMDG_CK(launch_linear(L, prec == AMDG_PREC_MIXED, StageCoef{0, 0.0, 0.0, 0.0}, stream_of(op->grid->ctx)));
+    cudaStream_t st = stream_of(op->grid->ctx);
+    if (prec == AMDG_PREC_MIXED) {
+        AMDG_CK(launch_to_float(d_u, op->d_shadow, op->grid->dof, st));
+        op->grid->ctx->launches++;
+        L.us_shadow = op->d_shadow;
+    }
+    AMDG_CK(launch_linear(L, prec == AMDG_PREC_MIXED, StageCoef{0, 0.0, 0.0, 0.0}, st));
     op->grid->ctx->launches++;
     return AMDG_OK;
 }

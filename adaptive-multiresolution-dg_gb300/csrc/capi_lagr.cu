@@ -90,7 +90,7 @@ TransformArgs<T> base_args(const amdg_burgers_op* op, int t, const int* from, co
     a.order = g->d_order;
     a.ptr = flx ? op->d_flx_ptr : op->d_vol_ptr;
     a.src = flx ? op->d_flx_src : op->d_vol_src;
-    a.lev = flx ? op->d_flx_lev : op->d_vol_lev;
+    a.split = flx ? op->d_flx_split : op->d_vol_split;
     return a;
 }
 
@@ -262,14 +262,17 @@ amdg_status burgers_sync(amdg_burgers_op* op) {
     build_transform_topology(g->host, &topo);
     std::vector<int32_t> anc;
     if (!build_surplus_ancestors(g->host, t, &anc)) return fail(AMDG_ERR_STATE, "element set has a hole: a surplus ancestor is missing");
-    int32_t* old[] = {op->d_vol_ptr, op->d_vol_src, op->d_vol_lev, op->d_flx_ptr, op->d_flx_src, op->d_flx_lev, op->d_anc};
+    int32_t* old[] = {op->d_vol_ptr, op->d_vol_src, op->d_vol_lev, op->d_flx_ptr, op->d_flx_src, op->d_flx_lev, op->d_anc,
+                      op->d_vol_split, op->d_flx_split};
     for (int32_t* p : old) cudaFree(p);
     op->d_vol_ptr = op->d_vol_src = op->d_vol_lev = op->d_flx_ptr = op->d_flx_src = op->d_flx_lev = op->d_anc = nullptr;
+    op->d_vol_split = op->d_flx_split = nullptr;
     amdg_status s;
     if ((s = upload_vec(&op->d_vol_ptr, topo.vol_ptr)) != AMDG_OK || (s = upload_vec(&op->d_vol_src, topo.vol_src)) != AMDG_OK ||
         (s = upload_vec(&op->d_vol_lev, topo.vol_lev)) != AMDG_OK || (s = upload_vec(&op->d_flx_ptr, topo.flx_ptr)) != AMDG_OK ||
         (s = upload_vec(&op->d_flx_src, topo.flx_src)) != AMDG_OK || (s = upload_vec(&op->d_flx_lev, topo.flx_lev)) != AMDG_OK ||
-        (s = upload_vec(&op->d_anc, anc)) != AMDG_OK)
+        (s = upload_vec(&op->d_anc, anc)) != AMDG_OK || (s = upload_vec(&op->d_vol_split, topo.vol_split)) != AMDG_OK ||
+        (s = upload_vec(&op->d_flx_split, topo.flx_split)) != AMDG_OK)
         return s;
     const int64_t E = g->host.num_elements;
     if (E > op->capacity) {
@@ -343,7 +346,7 @@ amdg_status amdg_burgers_destroy(amdg_burgers_op* op) {
     void* ptrs[] = {op->d_a2p, op->d_lv, op->d_lvx, op->d_lflx, op->d_ajump, op->f_a2p, op->f_lv, op->f_lvx, op->f_lflx,
                     op->f_ajump, op->d_vol_ptr, op->d_vol_src, op->d_vol_lev, op->d_flx_ptr, op->d_flx_src, op->d_flx_lev,
                     op->d_anc, op->d_anc_point, op->d_anc_rank, op->w_up, op->w_fu, op->w_a, op->w_b, op->w_rhs, op->w_u,
-                    op->d_u1, op->d_u2, op->d_rhs64, op->d_pred};
+                    op->d_u1, op->d_u2, op->d_rhs64, op->d_pred, op->d_vol_split, op->d_flx_split};
     for (void* p : ptrs) cudaFree(p);
     delete op;
     return AMDG_OK;

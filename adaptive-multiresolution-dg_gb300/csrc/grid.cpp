@@ -178,6 +178,8 @@ void build_transform_topology(const HostGrid& g, TransformTopology* out) {
     const int64_t E = g.num_elements;
     out->vol_ptr.assign(size_t(E) * dim + 1, 0);
     out->flx_ptr.assign(size_t(E) * dim + 1, 0);
+    out->vol_split.assign(size_t(E) * dim, 0);
+    out->flx_split.assign(size_t(E) * dim, 0);
     out->vol_src.clear(); out->vol_lev.clear(); out->flx_src.clear(); out->flx_lev.clear();
     std::vector<int32_t> o2(dim);
     for (int64_t e = 0; e < E; ++e) {
@@ -200,6 +202,14 @@ void build_transform_topology(const HostGrid& g, TransformTopology* out) {
             }
             out->vol_ptr[size_t(e) * dim + t + 1] = int32_t(out->vol_src.size());
             out->flx_ptr[size_t(e) * dim + t + 1] = int32_t(out->flx_src.size());
+            // neighbours are listed in increasing 1D order, hence increasing level:
+            // the "U" part (level <= own) is a prefix, the "L" part (finer) the rest
+            const int own = level_of_order(oe[t]);
+            int32_t sv = out->vol_ptr[size_t(e) * dim + t], sf = out->flx_ptr[size_t(e) * dim + t];
+            while (sv < int32_t(out->vol_src.size()) && out->vol_lev[sv] <= own) ++sv;
+            while (sf < int32_t(out->flx_src.size()) && out->flx_lev[sf] <= own) ++sf;
+            out->vol_split[size_t(e) * dim + t] = sv;
+            out->flx_split[size_t(e) * dim + t] = sf;
         }
     }
 }

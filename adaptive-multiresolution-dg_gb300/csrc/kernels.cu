@@ -28,9 +28,14 @@ __device__ __forceinline__ double rk_combine(double a, double un, double b, doub
     return __dadd_rn(__dmul_rn(a, un), __dmul_rn(b, __dadd_rn(us, __dmul_rn(dt, rhs))));
 }
 
-template <int D, int NP, typename T>
-__global__ void __launch_bounds__(256) linear_apply_kernel(const double* __restrict__ us, const double* un,
-                                                           double* out, const int32_t* __restrict__ row_ptr,
+// X: type of the neighbour values read by the contraction (double, or the
+// float shadow of the stage input in mixed mode, so no per-FMA conversion is
+// needed: double->float conversion issues on the FP64 pipe, which on this part
+// is as slow as an FP64 FMA).  shadow_out, when set, receives float(out).
+template <int D, int NP, typename T, typename X>
+__global__ void __launch_bounds__(256) linear_apply_kernel(const double* __restrict__ us, const X* __restrict__ xs,
+                                                           const double* un, double* out, float* shadow_out,
+                                                           const int32_t* __restrict__ row_ptr,
                                                            const int32_t* __restrict__ src, const int32_t* __restrict__ blk,
                                                            const T* __restrict__ blocks, int nblocks, int64_t total,
                                                            StageCoef rk) {
@@ -53,35 +58,38 @@ __global__ void __launch_bounds__(256) linear_apply_kernel(const double* __restr
         for (int i = beg; i < end; ++i) {
             const int s = __ldg(src + i);
             const T* m = bt + __ldg(blk + i) * NP * NP;
-            const double* x = us + int64_t(s) * B + base;
+            const X* x = xs + int64_t(s) * B + base;
 #pragma unroll
             for (int p = 0; p < NP; ++p) acc = fma(__ldg(m + p * NP), T(__ldg(x + p * stride)), acc);
         }
     }
     const double rhs = double(acc);
+    double v;
     if (rk.mode == 0) {
-        out[gid] = rhs;
+        v = rhs;
     } else {
-        out[gid] = rk_combine(rk.a, un[gid], rk.b, us[gid], rk.dt, rhs);
+        v = rk_combine(rk.a, un[gid], rk.b, us[gid], rk.dt, rhs);
     }
+    out[gid] = v;
+    if (shadow_out) shadow_out[gid] = float(v);
 }
 
-template <int D, int NP, typename T>
-static cudaError_t launch_linear_t(const LinearLaunch& L, const T* blocks, StageCoef rk, cudaStream_t st) {
+template <int D, int NP, typename T, typename X>
+static cudaError_t launch_linear_t(const LinearLaunch& L, const T* blocks, const X* xs, StageCoef rk, cudaStream_t st) {
     constexpr int B = IPow<NP, D>::v;
     const int64_t total = L.num_elements * B;
     if (total == 0) return cudaSuccess;
     const int threads = 256;
     const int64_t grid = (total + threads - 1) / threads;
-    linear_apply_kernel<D, NP, T><<<unsigned(grid), threads, 0, st>>>(L.us, L.un, L.out, L.row_ptr, L.src, L.blk, blocks,
-                                                                     L.num_blocks, total, rk);
+    linear_apply_kernel<D, NP, T, X><<<unsigned(grid), threads, 0, st>>>(L.us, xs, L.un, L.out, L.shadow_out, L.row_ptr,
+                                                                        L.src, L.blk, blocks, L.num_blocks, total, rk);
     return cudaGetLastError();
 }
 
-template <typename T>
-static cudaError_t dispatch_linear(const LinearLaunch& L, const T* blocks, StageCoef rk, cudaStream_t st) {
+template <typename T, typename X>
+static cudaError_t dispatch_linear(const LinearLaunch& L, const T* blocks, const X* xs, StageCoef rk, cudaStream_t st) {
 #define AMDG_CASE(D, NP) \
-    if (L.dim == D && L.np == NP) return launch_linear_t<D, NP, T>(L, blocks, rk, st);
+    if (L.dim == D && L.np == NP) return launch_linear_t<D, NP, T, X>(L, blocks, xs, rk, st);
     AMDG_CASE(1, 2) AMDG_CASE(1, 3) AMDG_CASE(1, 4)
     AMDG_CASE(2, 2) AMDG_CASE(2, 3) AMDG_CASE(2, 4)
     AMDG_CASE(3, 2) AMDG_CASE(3, 3) AMDG_CASE(3, 4)
@@ -93,7 +101,20 @@ static cudaError_t dispatch_linear(const LinearLaunch& L, const T* blocks, Stage
 }
 
 cudaError_t launch_linear(const LinearLaunch& L, bool mixed, StageCoef rk, cudaStream_t st) {
-    return mixed ? dispatch_linear<float>(L, L.blocks32, rk, st) : dispatch_linear<double>(L, L.blocks64, rk, st);
+    if (!mixed) return dispatch_linear<double, double>(L, L.blocks64, L.us, rk, st);
+    if (L.us_shadow) return dispatch_linear<float, float>(L, L.blocks32, L.us_shadow, rk, st);
+    return dispatch_linear<float, double>(L, L.blocks32, L.us, rk, st);
+}
+
+__global__ void to_float_kernel(const double* __restrict__ in, float* __restrict__ out, int64_t n) {
+    const int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (i < n) out[i] = float(in[i]);
+}
+
+cudaError_t launch_to_float(const double* in, float* out, int64_t n, cudaStream_t st) {
+    if (n == 0) return cudaSuccess;
+    to_float_kernel<<<unsigned((n + 255) / 256), 256, 0, st>>>(in, out, n);
+    return cudaGetLastError();
 }
 
 // ---- stage update for an externally computed rhs --------------------------

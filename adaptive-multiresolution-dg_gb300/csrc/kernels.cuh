@@ -18,6 +18,8 @@ struct LinearLaunch {
     int64_t num_elements;
     int num_blocks;
     const double* us;        // input coefficients of the stage
+    const float* us_shadow;  // float copy of us (mixed mode), or null to convert on the fly
+    float* shadow_out;       // receives float(out) when not null
     const double* un;        // coefficients at t_n (mode 1)
     double* out;             // rhs (mode 0) or updated coefficients (mode 1)
     const int32_t* row_ptr;  // CSR over (element, dimension)
@@ -30,6 +32,7 @@ struct LinearLaunch {
 constexpr int kReduceBlocks = 1216;  // 8 CTAs per SM on 152 SMs
 
 cudaError_t launch_linear(const LinearLaunch& L, bool mixed, StageCoef rk, cudaStream_t st);
+cudaError_t launch_to_float(const double* in, float* out, int64_t n, cudaStream_t st);
 cudaError_t launch_stage_update(const double* un, double* u, const double* rhs, int64_t n, StageCoef rk, cudaStream_t st);
 cudaError_t launch_init_separable(const int32_t* order, const double* coef1d, int dim, int np, int nb1, int nterms,
                                   int64_t num_elements, double* u, cudaStream_t st);

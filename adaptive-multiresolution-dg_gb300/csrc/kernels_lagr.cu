@@ -19,8 +19,6 @@
 
 namespace amdg {
 
-__device__ __forceinline__ int level_of(int o) { return o == 0 ? 0 : 32 - __clz(o); }
-
 template <typename T>
 __global__ void __launch_bounds__(256) fibre_transform_kernel(TransformArgs<T> a) {
     const int64_t gid = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
@@ -32,15 +30,14 @@ __global__ void __launch_bounds__(256) fibre_transform_kernel(TransformArgs<T> a
     const int qt = (idx / a.stride) % a.n_to;
     const int outer = idx / (a.stride * a.n_to);
     const int oe = __ldg(a.order + e * a.dim + a.t);
-    const int le = level_of(oe);
-    const int beg = __ldg(a.ptr + e * a.dim + a.t), end = __ldg(a.ptr + e * a.dim + a.t + 1);
+    // "L": neighbours finer than e in dimension t; "U": coarser or equal; neighbours are level-sorted
+    const int64_t et = e * a.dim + a.t;
+    const int beg = a.lu == 0 ? __ldg(a.split + et) : __ldg(a.ptr + et);
+    const int end = a.lu == 2 ? __ldg(a.split + et) : __ldg(a.ptr + et + 1);
     const T* mcol = a.M + size_t(oe) * a.n_to + qt;
     const int in_off = outer * a.n_from * a.stride + inner;
     T acc = T(0);
     for (int i = beg; i < end; ++i) {
-        const int ls = __ldg(a.lev + i);
-        if (a.lu == 0 && le >= ls) continue;  // "L": finer neighbours only
-        if (a.lu == 2 && le < ls) continue;   // "U": coarser or equal
         const int s = __ldg(a.src + i);
         const int os = __ldg(a.order + int64_t(s) * a.dim + a.t);
         const T* x = a.in + int64_t(s) * a.in_block + in_off;

@@ -21,7 +21,7 @@ struct TransformArgs {
     const T* M;              // [1D elements * n_from][ncols]
     const int32_t* ptr;      // CSR over (element, dimension)
     const int32_t* src;
-    const int32_t* lev;      // neighbour level in dimension t
+    const int32_t* split;    // [e*dim+t]: first neighbour finer than e in dimension t
     const int32_t* order;    // [element][dim] 1D orders
     const T* in;
     T* out;

@@ -1,0 +1,67 @@
+"""Adaptivity on the device against the reference's adaptive Burgers runs
+(fixtures from oracle/ref_harness burgers_adapt): adaptive separable
+initialisation, then per step the forward-Euler prediction, refine, one
+SSP-RK3 step and coarsen.  Element sets must match exactly; coefficients to
+1e-12 relative (max norm over the field), FP64."""
+import numpy as np
+import pytest
+
+import amdg
+import amdg_oracle as O
+from helpers import golden, manifest, rel_err
+
+pytestmark = pytest.mark.gpu
+
+ADAPT = [n for n, m in manifest().items() if m["kind"] == "burgers_adapt"]
+
+
+def _check(g, z, i):
+    lv, sp = g.elements()
+    keys = O.arrays_to_keys(lv, sp)
+    ref_keys = O.arrays_to_keys(z[f"level_{i}"], z[f"suppt_{i}"])
+    assert set(keys) == set(ref_keys), f"element set differs at step {i}"
+    pos = {k: j for j, k in enumerate(ref_keys)}
+    perm = np.array([pos[k] for k in keys])
+    assert rel_err(g.coefficients(), z[f"u_{i}"][perm]) < 1e-12, f"coefficients differ at step {i}"
+
+
+@pytest.mark.parametrize("name", ADAPT)
+def test_adaptive_burgers_matches_reference(ctx, name):
+    m = manifest()[name]
+    z = golden(name)
+    g = amdg.Grid(ctx, m["dim"], m["nmax"], 2, level_init=m["n_init"])
+    g.init_separable_adaptive(O.burgers_ic_terms(m["dim"]), m["eps"])
+    _check(g, z, 0)
+    op = amdg.BurgersOperator(g, m["alpha"])
+    for i in range(m["steps"]):
+        op.adaptive_step(m["cfl"], m["umax"], m["eps"], m["eta"], amdg.FP64)
+        ctx.synchronize()
+        _check(g, z, i + 1)
+    op.close()
+    g.close()
+
+
+def test_refine_coarsen_round_trip_and_version(ctx):
+    g = amdg.Grid(ctx, 2, 6, 2, level_init=3)
+    g.init_separable(O.burgers_ic_terms(2))
+    v0, e0 = g.version(), g.num_elements
+    u0 = g.coefficients().copy()
+    n = g.refine(-1.0)          # every leaf refines by one level
+    assert n > e0 and g.version() == v0 + 1
+    # old coefficients carried over, new elements zero
+    lv0, sp0 = O.grid(2, 3)
+    keys0 = O.arrays_to_keys(lv0, sp0)
+    lv, sp = g.elements()
+    keys = O.arrays_to_keys(lv, sp)
+    u = g.coefficients()
+    pos0 = {k: i for i, k in enumerate(keys0)}
+    for i, k in enumerate(keys):
+        if k in pos0:
+            assert np.array_equal(u[i], u0[pos0[k]])
+        else:
+            assert not u[i].any()
+    # zero-coefficient children are coarsened away again
+    g.coarsen(1e-300)
+    assert g.num_elements == e0
+    assert np.array_equal(g.coefficients(), u0)
+    g.close()
