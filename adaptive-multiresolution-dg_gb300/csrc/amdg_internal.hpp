@@ -87,6 +87,17 @@ struct HostGrid {
 void build_grid(int dim, int nmax, int sparse, HostGrid* g, int level_init = -1);
 int64_t find_element(const HostGrid& g, const int32_t* orders);  // binary search, -1 if absent
 
+// Batched independent grids sharing nmax, k and dim.
+struct BatchTopology {
+    std::vector<int64_t> row_ptr, src;   // CSR over (global element, dimension)
+    std::vector<int32_t> blk;
+    std::vector<double> blocks;          // [2][num_blocks][k+1][k+1]
+    std::vector<int32_t> solve_of;       // global element -> solve
+    std::vector<int64_t> elem_offset;    // solves + 1
+    int num_blocks = 0;
+};
+void build_batch_topology(const std::vector<const HostGrid*>& grids, const Oper1D& op, BatchTopology* out);
+
 // Adaptivity on packed keys (one refine pass with hole filling; repeated coarsening).
 std::vector<uint64_t> refine_keys(const HostGrid& g, const double* norms, double eps);
 std::vector<uint64_t> coarsen_keys(const HostGrid& g, const double* norms, double eta);
@@ -159,6 +170,8 @@ struct amdg_linear_op {
     double* d_u1 = nullptr;          // RK stage vectors
     double* d_u2 = nullptr;
     float* d_shadow = nullptr;       // mixed mode: float copies of u, u1, u2 (3 x capacity)
+    int variant[2] = {0, 0};         // kernel variant per precision, picked by the autotuner
+    float variant_ms[2][2] = {{0, 0}, {0, 0}};  // measured stage time [precision][variant]
 };
 
 struct amdg_burgers_op {
@@ -183,4 +196,22 @@ struct amdg_burgers_op {
     void *w_up = nullptr, *w_fu = nullptr, *w_a = nullptr, *w_b = nullptr, *w_rhs = nullptr, *w_u = nullptr;
     double *d_u1 = nullptr, *d_u2 = nullptr, *d_rhs64 = nullptr, *d_pred = nullptr;
     std::vector<double> host_norms;
+};
+
+struct amdg_batch {
+    amdg_context* ctx = nullptr;
+    int device = 0;
+    int dim = 0, nmax = 0, k = 0, block = 0, nsolves = 0;
+    std::vector<amdg_grid*> grids;
+    std::vector<int64_t> elem_offset;
+    int64_t num_elements = 0, dof = 0, pairs = 0;
+    int num_blocks = 0;
+    int64_t *d_row_ptr = nullptr, *d_src = nullptr;
+    int32_t *d_blk = nullptr, *d_solve = nullptr;
+    double *d_blocks64 = nullptr, *d_coef64 = nullptr, *d_dt = nullptr;
+    float *d_blocks32 = nullptr, *d_coef32 = nullptr;
+    double *d_u = nullptr, *d_u1 = nullptr, *d_u2 = nullptr;
+    float* d_shadow = nullptr;           // 3 x dof
+    void* graph_exec[2] = {nullptr, nullptr};  // cudaGraphExec_t per precision
+    int64_t launches_per_graph = 0;
 };

@@ -155,9 +155,10 @@ StageCoef rk3_stage_coef(int stage, double dt) {
     }
 }
 
-LinearLaunch linear_launch(const amdg_linear_op* op) {
+LinearLaunch linear_launch(const amdg_linear_op* op, amdg_precision prec = AMDG_PREC_FP64) {
     const amdg_grid* g = op->grid;
     LinearLaunch L{};
+    L.variant = op->variant[prec == AMDG_PREC_MIXED ? 1 : 0];
     L.dim = g->host.dim;
     L.np = g->host.k + 1;
     L.num_elements = g->host.num_elements;
@@ -173,7 +174,7 @@ LinearLaunch linear_launch(const amdg_linear_op* op) {
 amdg_status rk3_steps_device(amdg_linear_op* op, double dt, int nsteps, amdg_precision prec) {
     amdg_grid* g = op->grid;
     cudaStream_t st = stream_of(g->ctx);
-    LinearLaunch L = linear_launch(op);
+    LinearLaunch L = linear_launch(op, prec);
     const bool mixed = prec == AMDG_PREC_MIXED;
     // mixed mode reads neighbours from float shadows of the stage inputs; the
     // shadow of u is refreshed once per call, later ones come from the epilogues
@@ -200,6 +201,46 @@ amdg_status rk3_steps_device(amdg_linear_op* op, double dt, int nsteps, amdg_pre
             g->ctx->launches++;
         }
     }
+    return AMDG_OK;
+}
+
+// Pick the kernel variant per precision by timing one fused stage of each on
+// the operator's own grid (the grid's state as input, u1 as output).  Small
+// grids skip the timing and take the column variant when it applies.
+amdg_status autotune_linear(amdg_linear_op* op) {
+    amdg_grid* g = op->grid;
+    const int dim = g->host.dim, np = g->host.k + 1;
+    const bool col = linear_col_supported(dim, np);
+    for (int p = 0; p < 2; ++p) op->variant[p] = col ? 1 : 0;
+    if (!col || g->dof < 200000) return AMDG_OK;
+    cudaStream_t st = stream_of(g->ctx);
+    cudaEvent_t a, b;
+    AMDG_CK(cudaEventCreate(&a));
+    AMDG_CK(cudaEventCreate(&b));
+    AMDG_CK(launch_to_float(g->d_u, op->d_shadow, g->dof, st));
+    for (int p = 0; p < 2; ++p) {
+        float best = 1e30f;
+        for (int v = 0; v < 2; ++v) {
+            LinearLaunch L = linear_launch(op);
+            L.variant = v;
+            L.us = g->d_u;
+            L.un = g->d_u;
+            L.out = op->d_u1;
+            L.us_shadow = p == 1 ? op->d_shadow : nullptr;
+            const StageCoef rk{1, 0.0, 1.0, 0.0};
+            AMDG_CK(launch_linear(L, p == 1, rk, st));  // warm-up
+            AMDG_CK(cudaEventRecord(a, st));
+            for (int r = 0; r < 3; ++r) AMDG_CK(launch_linear(L, p == 1, rk, st));
+            AMDG_CK(cudaEventRecord(b, st));
+            AMDG_CK(cudaEventSynchronize(b));
+            float ms = 0;
+            AMDG_CK(cudaEventElapsedTime(&ms, a, b));
+            op->variant_ms[p][v] = ms / 3;
+            if (ms < best) { best = ms; op->variant[p] = v; }
+        }
+    }
+    cudaEventDestroy(a);
+    cudaEventDestroy(b);
     return AMDG_OK;
 }
 
@@ -239,7 +280,7 @@ amdg_status linear_sync(amdg_linear_op* op) {
     }
     AMDG_CK(cudaStreamSynchronize(st));
     op->built_version = g->version;
-    return AMDG_OK;
+    return autotune_linear(op);
 }
 
 }  // namespace
@@ -623,6 +664,24 @@ amdg_status amdg_linear_destroy(amdg_linear_op* op) {
     return AMDG_OK;
 }
 
+amdg_status amdg_linear_tuning(const amdg_linear_op* op, int* variants, float* stage_ms) {
+    AMDG_REQUIRE(op, AMDG_ERR_ARG, "op is null");
+    for (int p = 0; p < 2; ++p) {
+        if (variants) variants[p] = op->variant[p];
+        for (int v = 0; v < 2; ++v)
+            if (stage_ms) stage_ms[p * 2 + v] = op->variant_ms[p][v];
+    }
+    return AMDG_OK;
+}
+
+amdg_status amdg_linear_set_variant(amdg_linear_op* op, amdg_precision prec, int variant) {
+    AMDG_REQUIRE(op && (prec == AMDG_PREC_FP64 || prec == AMDG_PREC_MIXED), AMDG_ERR_ARG, "bad arguments");
+    AMDG_REQUIRE(variant == 0 || (variant == 1 && linear_col_supported(op->grid->host.dim, op->grid->host.k + 1)),
+                 AMDG_ERR_ARG, "unsupported kernel variant");
+    op->variant[prec == AMDG_PREC_MIXED ? 1 : 0] = variant;
+    return AMDG_OK;
+}
+
 amdg_status amdg_linear_stats(const amdg_linear_op* op, int64_t* pairs, double* flops_per_apply) {
     AMDG_REQUIRE(op, AMDG_ERR_ARG, "op is null");
     const int np = op->grid->host.k + 1;
@@ -638,7 +697,7 @@ amdg_status amdg_linear_apply(amdg_linear_op* op, const double* d_u, double* d_r
     amdg_status s = set_device(op->grid->ctx);
     if (s != AMDG_OK) return s;
     if ((s = linear_sync(op)) != AMDG_OK) return s;
-    LinearLaunch L = linear_launch(op);
+    LinearLaunch L = linear_launch(op, prec);
     L.us = d_u;
     L.un = nullptr;
     L.out = d_rhs;

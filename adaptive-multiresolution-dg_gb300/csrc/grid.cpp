@@ -236,3 +236,82 @@ bool build_surplus_ancestors(const HostGrid& g, const LagrTables& t, std::vector
 }
 
 }  // namespace amdg
+
+namespace amdg {
+
+void build_batch_topology(const std::vector<const HostGrid*>& grids, const Oper1D& op, BatchTopology* out) {
+    const int dim = grids[0]->dim, nmax = grids[0]->nmax, np = grids[0]->k + 1, n1 = 1 << nmax;
+    const int64_t one = int64_t(1) << nmax;
+    const int nb = op.nb;
+    // shared 1D blocks, one table per upwind side: u_vx on intersecting supports
+    // plus ulft_vjp (c >= 0) or urgt_vjp (c < 0), entries below 1e-13 dropped;
+    // a pair is listed when either side is nonzero
+    std::vector<std::vector<int>> rel1d(n1);
+    std::vector<double> t0, t1;
+    for (int o = 0; o < n1; ++o) {
+        int64_t a, b;
+        support_units(o, nmax, &a, &b);
+        for (int oc = 0; oc < n1; ++oc) {
+            int64_t a2, b2;
+            support_units(oc, nmax, &a2, &b2);
+            if (!flux_related(a, b, a2, b2, one)) continue;
+            const bool vol = !((a >= b2) || (b <= a2));
+            double blk[2][16];
+            bool any = false;
+            for (int side = 0; side < 2; ++side) {
+                const std::vector<double>& flux = side == 0 ? op.ulft_vjp : op.urgt_vjp;
+                for (int p = 0; p < np; ++p)
+                    for (int q = 0; q < np; ++q) {
+                        const size_t idx = size_t(oc * np + p) * nb + (o * np + q);
+                        double v = 0.0;
+                        if (vol && std::fabs(op.u_vx[idx]) >= kRoundOff) v += op.u_vx[idx];
+                        if (std::fabs(flux[idx]) >= kRoundOff) v += flux[idx];
+                        blk[side][p * np + q] = v;
+                        any = any || v != 0.0;
+                    }
+            }
+            if (!any) continue;
+            rel1d[o].push_back(oc);
+            t0.insert(t0.end(), blk[0], blk[0] + np * np);
+            t1.insert(t1.end(), blk[1], blk[1] + np * np);
+        }
+    }
+    out->num_blocks = int(t0.size() / (np * np));
+    out->blocks = t0;
+    out->blocks.insert(out->blocks.end(), t1.begin(), t1.end());
+    std::vector<int> blk_base(n1 + 1, 0);
+    for (int o = 0; o < n1; ++o) blk_base[o + 1] = blk_base[o] + int(rel1d[o].size());
+    int64_t total = 0;
+    for (const HostGrid* g : grids) total += g->num_elements;
+    out->row_ptr.assign(size_t(total) * dim + 1, 0);
+    out->src.clear();
+    out->blk.clear();
+    out->solve_of.assign(total, 0);
+    out->elem_offset.assign(grids.size() + 1, 0);
+    std::vector<int32_t> o2(dim);
+    int64_t base = 0;
+    for (size_t sv = 0; sv < grids.size(); ++sv) {
+        const HostGrid& g = *grids[sv];
+        out->elem_offset[sv] = base;
+        for (int64_t e = 0; e < g.num_elements; ++e) {
+            out->solve_of[base + e] = int32_t(sv);
+            const int32_t* oe = &g.order[size_t(e) * dim];
+            for (int t = 0; t < dim; ++t) {
+                std::copy(oe, oe + dim, o2.begin());
+                const int o = oe[t];
+                for (size_t i = 0; i < rel1d[o].size(); ++i) {
+                    o2[t] = rel1d[o][i];
+                    const int64_t s = find_element(g, o2.data());
+                    if (s < 0) continue;
+                    out->src.push_back(base + s);
+                    out->blk.push_back(blk_base[o] + int32_t(i));
+                }
+                out->row_ptr[size_t(base + e) * dim + t + 1] = int64_t(out->src.size());
+            }
+        }
+        base += g.num_elements;
+    }
+    out->elem_offset[grids.size()] = base;
+}
+
+}  // namespace amdg

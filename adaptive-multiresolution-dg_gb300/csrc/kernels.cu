@@ -74,6 +74,96 @@ __global__ void __launch_bounds__(256) linear_apply_kernel(const double* __restr
     if (shadow_out) shadow_out[gid] = float(v);
 }
 
+// Column variant: a CTA owns G whole elements (G = 256 / C, C = B / NP columns
+// of a block along one dimension).  In dimension t thread (g, c) reads the NP
+// neighbour values of column c once and produces all NP outputs of that
+// column (NP^2 FMAs per NP loads instead of NP FMAs per NP loads), adding
+// them into the element's block in shared memory; the dimensions are
+// separated by barriers so every output has one writer per dimension.  The
+// fused RK epilogue then streams the G blocks out coalesced.
+template <int D, int NP, typename T, typename X>
+__global__ void __launch_bounds__(256) linear_col_kernel(const double* __restrict__ us, const X* __restrict__ xs,
+                                                         const double* un, double* out, float* shadow_out,
+                                                         const int32_t* __restrict__ row_ptr,
+                                                         const int32_t* __restrict__ src, const int32_t* __restrict__ blk,
+                                                         const T* __restrict__ blocks, int nblocks, int64_t num_elements,
+                                                         StageCoef rk) {
+    constexpr int B = IPow<NP, D>::v;
+    constexpr int C = B / NP;
+    constexpr int G = 256 / C;
+    __shared__ T y[G * B];
+    const int tid = threadIdx.x;
+    const int g = tid / C, c = tid - (tid / C) * C;
+    const int64_t e = int64_t(blockIdx.x) * G + g;
+    const bool active = (g < G) && (e < num_elements);
+    for (int i = tid; i < G * B; i += blockDim.x) y[i] = T(0);
+    __syncthreads();
+#pragma unroll
+    for (int t = 0; t < D; ++t) {
+        int stride = 1;
+#pragma unroll
+        for (int s = t + 1; s < D; ++s) stride *= NP;
+        const int lo = c % stride, hi = c / stride;
+        const int base = hi * stride * NP + lo;
+        if (active) {
+            T acc[NP];
+#pragma unroll
+            for (int q = 0; q < NP; ++q) acc[q] = T(0);
+            const int beg = __ldg(row_ptr + e * D + t);
+            const int end = __ldg(row_ptr + e * D + t + 1);
+            const T* bt = blocks + size_t(t) * nblocks * NP * NP;
+            for (int i = beg; i < end; ++i) {
+                const int sidx = __ldg(src + i);
+                const T* m = bt + __ldg(blk + i) * NP * NP;
+                const X* x = xs + int64_t(sidx) * B + base;
+                T xv[NP];
+#pragma unroll
+                for (int p = 0; p < NP; ++p) xv[p] = T(__ldg(x + p * stride));
+#pragma unroll
+                for (int p = 0; p < NP; ++p)
+#pragma unroll
+                    for (int q = 0; q < NP; ++q) acc[q] = fma(__ldg(m + p * NP + q), xv[p], acc[q]);
+            }
+            T* yb = y + g * B + base;
+#pragma unroll
+            for (int q = 0; q < NP; ++q) yb[q * stride] += acc[q];
+        }
+        __syncthreads();
+    }
+    const int64_t first = int64_t(blockIdx.x) * G * B;
+    const int64_t total = num_elements * B;
+    for (int i = tid; i < G * B; i += blockDim.x) {
+        const int64_t gid = first + i;
+        if (gid >= total) break;
+        const double rhs = double(y[i]);
+        const double v = rk.mode == 0 ? rhs : rk_combine(rk.a, un[gid], rk.b, us[gid], rk.dt, rhs);
+        out[gid] = v;
+        if (shadow_out) shadow_out[gid] = float(v);
+    }
+}
+
+template <int D, int NP, typename T, typename X>
+static cudaError_t launch_col_t(const LinearLaunch& L, const T* blocks, const X* xs, StageCoef rk, cudaStream_t st) {
+    constexpr int B = IPow<NP, D>::v;
+    constexpr int C = B / NP;
+    if constexpr (C > 256) {
+        return cudaErrorInvalidValue;
+    } else {
+        constexpr int G = 256 / C;
+        if (L.num_elements == 0) return cudaSuccess;
+        const int64_t grid = (L.num_elements + G - 1) / G;
+        linear_col_kernel<D, NP, T, X><<<unsigned(grid), 256, 0, st>>>(L.us, xs, L.un, L.out, L.shadow_out, L.row_ptr,
+                                                                      L.src, L.blk, blocks, L.num_blocks, L.num_elements, rk);
+        return cudaGetLastError();
+    }
+}
+
+bool linear_col_supported(int dim, int np) {
+    int B = 1;
+    for (int d = 0; d < dim; ++d) B *= np;
+    return B / np <= 256;
+}
+
 template <int D, int NP, typename T, typename X>
 static cudaError_t launch_linear_t(const LinearLaunch& L, const T* blocks, const X* xs, StageCoef rk, cudaStream_t st) {
     constexpr int B = IPow<NP, D>::v;
@@ -88,8 +178,10 @@ static cudaError_t launch_linear_t(const LinearLaunch& L, const T* blocks, const
 
 template <typename T, typename X>
 static cudaError_t dispatch_linear(const LinearLaunch& L, const T* blocks, const X* xs, StageCoef rk, cudaStream_t st) {
-#define AMDG_CASE(D, NP) \
-    if (L.dim == D && L.np == NP) return launch_linear_t<D, NP, T, X>(L, blocks, xs, rk, st);
+#define AMDG_CASE(D, NP)                                                                \
+    if (L.dim == D && L.np == NP)                                                         \
+        return L.variant == 1 ? launch_col_t<D, NP, T, X>(L, blocks, xs, rk, st)          \
+                              : launch_linear_t<D, NP, T, X>(L, blocks, xs, rk, st);
     AMDG_CASE(1, 2) AMDG_CASE(1, 3) AMDG_CASE(1, 4)
     AMDG_CASE(2, 2) AMDG_CASE(2, 3) AMDG_CASE(2, 4)
     AMDG_CASE(3, 2) AMDG_CASE(3, 3) AMDG_CASE(3, 4)

@@ -15,6 +15,7 @@ struct StageCoef {
 
 struct LinearLaunch {
     int dim, np;
+    int variant;             // 0: thread per output coefficient; 1: column variant (linear_col_supported)
     int64_t num_elements;
     int num_blocks;
     const double* us;        // input coefficients of the stage
@@ -29,9 +30,33 @@ struct LinearLaunch {
     const float* blocks32;
 };
 
+// Batched solves: concatenated element tables, per-element solve index.
+template <typename T, typename X>
+struct BatchLaunch {
+    int dim, np, mode;       // mode 0: rhs; 1: RK stage a*un + b*(us + dt[solve]*rhs)
+    double a, b;
+    int64_t num_elements;
+    int num_blocks;
+    const double* us;
+    const X* xs;             // neighbour values (us, or its float shadow)
+    const double* un;
+    double* out;
+    float* shadow_out;
+    const int64_t* row_ptr;  // CSR over (element, dimension)
+    const int64_t* src;
+    const int32_t* blk;
+    const T* blocks;         // [2][num_blocks][np][np]: u_vx + ulft_vjp, u_vx + urgt_vjp
+    const T* coef;           // [solve][dim] velocities
+    const double* dt;        // [solve] step sizes
+    const int32_t* solve_of; // [element]
+};
+template <typename T, typename X>
+cudaError_t launch_batch(const BatchLaunch<T, X>& L, cudaStream_t st);
+
 constexpr int kReduceBlocks = 1216;  // 8 CTAs per SM on 152 SMs
 
 cudaError_t launch_linear(const LinearLaunch& L, bool mixed, StageCoef rk, cudaStream_t st);
+bool linear_col_supported(int dim, int np);
 cudaError_t launch_to_float(const double* in, float* out, int64_t n, cudaStream_t st);
 cudaError_t launch_stage_update(const double* un, double* u, const double* rhs, int64_t n, StageCoef rk, cudaStream_t st);
 cudaError_t launch_init_separable(const int32_t* order, const double* coef1d, int dim, int np, int nb1, int nterms,

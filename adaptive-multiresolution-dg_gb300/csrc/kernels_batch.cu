@@ -1,0 +1,106 @@
+// Batched independent solves of the linear constant-coefficient operator:
+// the element tables of many grids are concatenated and one launch per RK
+// stage advances all of them.  Each element carries its solve index; the
+// solve's velocity c scales the per-dimension sum of the shared 1D blocks
+// (u_vx + upwind flux, one table per flux side), and the solve's dt enters
+// the fused SSP-RK3 epilogue.  Column layout as linear_col_kernel.
+#include <cuda_runtime.h>
+
+#include <cstdint>
+
+#include "kernels.cuh"
+
+namespace amdg {
+
+template <int B, int E>
+struct BPow { static constexpr int v = B * BPow<B, E - 1>::v; };
+template <int B>
+struct BPow<B, 0> { static constexpr int v = 1; };
+
+__device__ __forceinline__ double batch_combine(double a, double un, double b, double us, double dt, double rhs) {
+    return __dadd_rn(__dmul_rn(a, un), __dmul_rn(b, __dadd_rn(us, __dmul_rn(dt, rhs))));
+}
+
+template <int D, int NP, typename T, typename X>
+__global__ void __launch_bounds__(256) batch_col_kernel(BatchLaunch<T, X> L) {
+    constexpr int B = BPow<NP, D>::v;
+    constexpr int C = B / NP;
+    constexpr int G = 256 / C;
+    __shared__ T y[G * B];
+    const int tid = threadIdx.x;
+    const int g = tid / C, c = tid - (tid / C) * C;
+    const int64_t e = int64_t(blockIdx.x) * G + g;
+    const bool active = (g < G) && (e < L.num_elements);
+    const int solve = active ? __ldg(L.solve_of + e) : 0;
+    for (int i = tid; i < G * B; i += blockDim.x) y[i] = T(0);
+    __syncthreads();
+#pragma unroll
+    for (int t = 0; t < D; ++t) {
+        int stride = 1;
+#pragma unroll
+        for (int s = t + 1; s < D; ++s) stride *= NP;
+        const int lo = c % stride, hi = c / stride;
+        const int base = hi * stride * NP + lo;
+        if (active) {
+            const T ct = L.coef[solve * D + t];
+            const T* table = L.blocks + (ct >= T(0) ? 0 : size_t(L.num_blocks) * NP * NP);
+            T acc[NP];
+#pragma unroll
+            for (int q = 0; q < NP; ++q) acc[q] = T(0);
+            const int64_t beg = __ldg(L.row_ptr + e * D + t);
+            const int64_t end = __ldg(L.row_ptr + e * D + t + 1);
+            for (int64_t i = beg; i < end; ++i) {
+                const int64_t sidx = __ldg(L.src + i);
+                const T* m = table + __ldg(L.blk + i) * NP * NP;
+                const X* x = L.xs + sidx * B + base;
+                T xv[NP];
+#pragma unroll
+                for (int p = 0; p < NP; ++p) xv[p] = T(__ldg(x + p * stride));
+#pragma unroll
+                for (int p = 0; p < NP; ++p)
+#pragma unroll
+                    for (int q = 0; q < NP; ++q) acc[q] = fma(__ldg(m + p * NP + q), xv[p], acc[q]);
+            }
+            T* yb = y + g * B + base;
+#pragma unroll
+            for (int q = 0; q < NP; ++q) yb[q * stride] += ct * acc[q];
+        }
+        __syncthreads();
+    }
+    const int64_t first = int64_t(blockIdx.x) * G * B;
+    const int64_t total = L.num_elements * B;
+    for (int i = tid; i < G * B; i += blockDim.x) {
+        const int64_t gid = first + i;
+        if (gid >= total) break;
+        const int sv = __ldg(L.solve_of + gid / B);
+        const double rhs = double(y[i]);
+        const double v = L.mode == 0 ? rhs : batch_combine(L.a, L.un[gid], L.b, L.us[gid], L.dt[sv], rhs);
+        L.out[gid] = v;
+        if (L.shadow_out) L.shadow_out[gid] = float(v);
+    }
+}
+
+template <typename T, typename X>
+cudaError_t launch_batch(const BatchLaunch<T, X>& L, cudaStream_t st) {
+    if (L.num_elements == 0) return cudaSuccess;
+#define AMDG_BCASE(D, NP)                                                                        \
+    if (L.dim == D && L.np == NP) {                                                               \
+        constexpr int G = 256 / (BPow<NP, D>::v / NP);                                            \
+        const int64_t grid = (L.num_elements + G - 1) / G;                                        \
+        batch_col_kernel<D, NP, T, X><<<unsigned(grid), 256, 0, st>>>(L);                         \
+        return cudaGetLastError();                                                                \
+    }
+    AMDG_BCASE(1, 2) AMDG_BCASE(1, 3) AMDG_BCASE(1, 4)
+    AMDG_BCASE(2, 2) AMDG_BCASE(2, 3) AMDG_BCASE(2, 4)
+    AMDG_BCASE(3, 2) AMDG_BCASE(3, 3) AMDG_BCASE(3, 4)
+    AMDG_BCASE(4, 2) AMDG_BCASE(4, 3) AMDG_BCASE(4, 4)
+    AMDG_BCASE(5, 2) AMDG_BCASE(5, 3) AMDG_BCASE(5, 4)
+    AMDG_BCASE(6, 2) AMDG_BCASE(6, 3)
+#undef AMDG_BCASE
+    return cudaErrorInvalidValue;
+}
+
+template cudaError_t launch_batch<double, double>(const BatchLaunch<double, double>&, cudaStream_t);
+template cudaError_t launch_batch<float, float>(const BatchLaunch<float, float>&, cudaStream_t);
+
+}  // namespace amdg

@@ -80,6 +80,7 @@ extern "C" amdg_status amdg_rk3ssp_steps_noalloc(amdg_linear_op* op, double* d_u
     double* u2 = scratch + kNoAllocMaxDof;
     cudaStream_t st = static_cast<cudaStream_t>(g->ctx->stream);
     LinearLaunch L{};
+    L.variant = op->variant[prec == AMDG_PREC_MIXED ? 1 : 0];  // same kernel as amdg_rk3ssp_steps
     L.dim = g->host.dim;
     L.np = g->host.k + 1;
     L.num_elements = g->host.num_elements;

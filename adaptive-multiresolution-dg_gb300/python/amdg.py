@@ -71,6 +71,8 @@ def load():
         "amdg_linear_destroy": ([vp], i32),
         "amdg_linear_stats": ([vp, C.POINTER(i64), C.POINTER(dbl)], i32),
         "amdg_linear_apply": ([vp, vp, vp, i32], i32),
+        "amdg_linear_tuning": ([vp, vp, vp], i32),
+        "amdg_linear_set_variant": ([vp, i32, i32], i32),
         "amdg_rk3ssp_steps": ([vp, dbl, i32, i32], i32),
         "amdg_rk3ssp_steps_host": ([vp, dbl, i32, vp, i32], i32),
         "amdg_rk3_stage_update": ([vp, i32, dbl, vp, vp, vp, i64], i32),
@@ -277,6 +279,16 @@ class LinearOperator:
         pairs, flops = C.c_int64(), C.c_double()
         _ck(load().amdg_linear_stats(self._h, C.byref(pairs), C.byref(flops)), "linear_stats")
         self.pairs, self.flops_per_apply = pairs.value, flops.value
+
+    def tuning(self):
+        """(variants[fp64, mixed], stage_ms[[fp64 v0, v1], [mixed v0, v1]]) chosen by the autotuner."""
+        v = np.zeros(2, np.int32)
+        ms = np.zeros(4, np.float32)
+        _ck(load().amdg_linear_tuning(self._h, _ptr(v), _ptr(ms)), "linear_tuning")
+        return v.tolist(), ms.reshape(2, 2).tolist()
+
+    def set_variant(self, prec: int, variant: int):
+        _ck(load().amdg_linear_set_variant(self._h, prec, variant), "linear_set_variant")
 
     def apply_device(self, d_u: int, d_rhs: int, prec: int = FP64):
         _ck(load().amdg_linear_apply(self._h, C.c_void_p(d_u), C.c_void_p(d_rhs), prec), "linear_apply")
