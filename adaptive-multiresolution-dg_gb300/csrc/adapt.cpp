@@ -53,11 +53,13 @@ void fill_holes(std::unordered_set<uint64_t>* set, std::vector<uint64_t> work, i
 
 }  // namespace
 
-std::vector<uint64_t> refine_keys(const HostGrid& g, const double* norms, double eps) {
+std::vector<uint64_t> refine_keys(const HostGrid& g, const double* norms, double eps, std::vector<uint8_t>* refined,
+                                  const uint8_t* force) {
     const int dim = g.dim, nmax = g.nmax;
     std::unordered_set<uint64_t> present(g.key.begin(), g.key.end());
     std::unordered_set<uint64_t> out(present);
     std::vector<uint64_t> added;
+    if (refined) refined->assign(g.num_elements, 0);
     int ch[2];
     for (int64_t e = 0; e < g.num_elements; ++e) {
         const uint64_t key = g.key[e];
@@ -68,7 +70,9 @@ std::vector<uint64_t> refine_keys(const HostGrid& g, const double* norms, double
             for (int c = 0; c < nc; ++c) existing += present.count(with_field(key, d, dim, nmax, ch[c])) ? 1 : 0;
         }
         // a leaf has fewer existing children than possible (DGAdapt::update_leaf)
-        if (existing >= total || !(norms[e] > eps)) continue;
+        const bool want = force ? force[e] != 0 : (norms[e] > eps);
+        if (existing >= total || !want) continue;
+        if (refined) (*refined)[e] = 1;
         for (int d = 0; d < dim; ++d) {
             const int nc = children_1d(field(key, d, dim, nmax), nmax, ch);
             for (int c = 0; c < nc; ++c) {
@@ -124,6 +128,41 @@ std::vector<uint64_t> coarsen_keys(const HostGrid& g, const double* norms, doubl
     std::vector<uint64_t> keys;
     for (int64_t e = 0; e < E; ++e) if (alive[e]) keys.push_back(g.key[e]);
     return keys;
+}
+
+void leaf_flags(const HostGrid& g, std::vector<uint8_t>* leaf) {
+    const int dim = g.dim, nmax = g.nmax;
+    std::unordered_set<uint64_t> present(g.key.begin(), g.key.end());
+    leaf->assign(g.num_elements, 0);
+    int ch[2];
+    for (int64_t e = 0; e < g.num_elements; ++e) {
+        int total = 0, existing = 0;
+        for (int d = 0; d < dim; ++d) {
+            const int nc = children_1d(field(g.key[e], d, dim, nmax), nmax, ch);
+            total += nc;
+            for (int c = 0; c < nc; ++c) existing += present.count(with_field(g.key[e], d, dim, nmax, ch[c])) ? 1 : 0;
+        }
+        (*leaf)[e] = existing < total ? 1 : 0;
+    }
+}
+
+void parent_table(const HostGrid& g, std::vector<int32_t>* pg) {
+    const int dim = g.dim, nmax = g.nmax;
+    pg->assign(size_t(g.num_elements) * dim * 2, -1);
+    auto index_of = [&](uint64_t k) -> int64_t {
+        auto it = std::lower_bound(g.key.begin(), g.key.end(), k);
+        return (it != g.key.end() && *it == k) ? int64_t(it - g.key.begin()) : -1;
+    };
+    for (int64_t e = 0; e < g.num_elements; ++e)
+        for (int d = 0; d < dim; ++d) {
+            uint64_t k = g.key[e];
+            for (int gen = 0; gen < 2; ++gen) {
+                const int o = field(k, d, dim, nmax);
+                if (o == 0) break;
+                k = with_field(k, d, dim, nmax, o == 1 ? 0 : o / 2);
+                (*pg)[(size_t(e) * dim + d) * 2 + gen] = int32_t(index_of(k));
+            }
+        }
 }
 
 void grid_from_keys(int dim, int nmax, int k, std::vector<uint64_t> keys, HostGrid* g) {

@@ -12,6 +12,7 @@ namespace amdg {
 
 constexpr double kRoundOff = 1e-13;  // Const::ROUND_OFF (libs.h:28)
 constexpr int kMaxDim = 6;
+constexpr int kLongRowHost = 24;  // neighbour rows longer than this are split across a warp (kLongRow)
 
 // ---- error plumbing ------------------------------------------------------
 void set_error(const std::string& msg);
@@ -99,7 +100,13 @@ struct BatchTopology {
 void build_batch_topology(const std::vector<const HostGrid*>& grids, const Oper1D& op, BatchTopology* out);
 
 // Adaptivity on packed keys (one refine pass with hole filling; repeated coarsening).
-std::vector<uint64_t> refine_keys(const HostGrid& g, const double* norms, double eps);
+// refined (optional): per element, 1 where the element was refined; force (optional): refine
+// the leaves flagged instead of those with norm > eps
+std::vector<uint64_t> refine_keys(const HostGrid& g, const double* norms, double eps, std::vector<uint8_t>* refined = nullptr,
+                                  const uint8_t* force = nullptr);
+void leaf_flags(const HostGrid& g, std::vector<uint8_t>* leaf);
+// [e][d][2]: parent and grandparent in dimension d, -1 when absent
+void parent_table(const HostGrid& g, std::vector<int32_t>* pg);
 std::vector<uint64_t> coarsen_keys(const HostGrid& g, const double* norms, double eta);
 void grid_from_keys(int dim, int nmax, int k, std::vector<uint64_t> keys, HostGrid* g);
 // element norms of the separable expansion sum_t prod_d coef1d[t][d] (host, same arithmetic order as the device init)
@@ -124,6 +131,8 @@ struct TransformTopology {
     std::vector<int32_t> vol_ptr, vol_src, vol_lev;  // ptr: num_elements*dim + 1
     std::vector<int32_t> flx_ptr, flx_src, flx_lev;
     std::vector<int32_t> vol_split, flx_split;       // [e*dim+t]: first neighbour finer than e in t
+    std::vector<uint8_t> vol_long, flx_long;         // [e*dim+t]: row longer than kLongRowHost
+    std::vector<std::vector<int32_t>> vol_long_elems, flx_long_elems;  // [t]: elements with a long row
 };
 void build_transform_topology(const HostGrid& g, TransformTopology* out);
 // surplus ancestors: [e][d][ic] element index (-1 for level 0 in d); false if a hole is found
@@ -167,9 +176,13 @@ struct amdg_linear_op {
     int32_t* d_blk = nullptr;        // block index within the dimension's table
     double* d_blocks64 = nullptr;    // [dim][num_blocks][k+1][k+1], row = solution p, col = test q
     float* d_blocks32 = nullptr;
+    int32_t* d_pairs = nullptr;      // column variant: (src, blk) interleaved
+    double* d_blocks64p = nullptr;   // column variant: blocks padded to a multiple of 4 entries
+    float* d_blocks32p = nullptr;
     double* d_u1 = nullptr;          // RK stage vectors
     double* d_u2 = nullptr;
-    float* d_shadow = nullptr;       // mixed mode: float copies of u, u1, u2 (3 x capacity)
+    float* d_shadow = nullptr;       // mixed mode: hi parts of u, u1, u2 (3 x capacity)
+    float* d_lo = nullptr;           // mixed mode: lo parts of u, u1, u2 (3 x capacity)
     int variant[2] = {0, 0};         // kernel variant per precision, picked by the autotuner
     float variant_ms[2][2] = {{0, 0}, {0, 0}};  // measured stage time [precision][variant]
 };
@@ -189,6 +202,9 @@ struct amdg_burgers_op {
     int32_t *d_vol_ptr = nullptr, *d_vol_src = nullptr, *d_vol_lev = nullptr;
     int32_t *d_flx_ptr = nullptr, *d_flx_src = nullptr, *d_flx_lev = nullptr;
     int32_t *d_vol_split = nullptr, *d_flx_split = nullptr;
+    uint8_t *d_vol_long = nullptr, *d_flx_long = nullptr;
+    int32_t *d_vol_long_elems = nullptr, *d_flx_long_elems = nullptr;  // concatenated over t
+    std::vector<int32_t> vol_long_off, flx_long_off;                   // dim + 1 offsets
     int32_t *d_anc = nullptr, *d_anc_point = nullptr, *d_anc_rank = nullptr;
     double weight[16] = {0};
     std::vector<std::vector<int>> sched_dims, sched_lu;
@@ -196,7 +212,21 @@ struct amdg_burgers_op {
     void *w_up = nullptr, *w_fu = nullptr, *w_a = nullptr, *w_b = nullptr, *w_rhs = nullptr, *w_u = nullptr;
     double *d_u1 = nullptr, *d_u2 = nullptr, *d_rhs64 = nullptr, *d_pred = nullptr;
     std::vector<double> host_norms;
+    // one SSP-RK3 step captured as a CUDA graph, valid for (grid version, precision, dt)
+    int32_t* d_pg = nullptr;         // [e][d][2] parent / grandparent (learned adaptivity features)
+    void* graph_exec = nullptr;
+    int64_t graph_version = -1;
+    int graph_prec = -1;
+    double graph_dt = 0.0;
+    int64_t graph_launches = 0;
 };
+
+namespace amdg {
+// replace a grid's element set (coefficients carried over, new elements zero; bumps the version)
+amdg_status grid_set_keys(amdg_grid* g, std::vector<uint64_t> keys);
+// indicator norms of a device coefficient vector on the grid's element set (synchronises)
+amdg_status grid_norms(amdg_grid* g, const double* d_u, std::vector<double>* norms);
+}  // namespace amdg
 
 struct amdg_batch {
     amdg_context* ctx = nullptr;

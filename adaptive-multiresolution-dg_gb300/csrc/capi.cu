@@ -6,6 +6,7 @@
 
 #include <algorithm>
 #include <cmath>
+#include <unordered_map>
 #include <cstring>
 #include <new>
 #include <string>
@@ -87,6 +88,10 @@ amdg_status project_terms(const amdg_grid* g, int nterms, amdg_fn1d f, void* use
 }
 
 
+}  // namespace
+
+namespace amdg {
+
 // Replace the grid's element set by `keys` (sorted, unique), carrying the
 // coefficients of surviving elements over and zeroing new ones.
 amdg_status grid_set_keys(amdg_grid* g, std::vector<uint64_t> keys) {
@@ -147,6 +152,10 @@ amdg_status grid_norms(amdg_grid* g, const double* d_u, std::vector<double>* nor
     return AMDG_OK;
 }
 
+}  // namespace amdg
+
+namespace {
+
 StageCoef rk3_stage_coef(int stage, double dt) {
     switch (stage) {
         case 0: return StageCoef{1, 0.0, 1.0, dt};
@@ -168,6 +177,9 @@ LinearLaunch linear_launch(const amdg_linear_op* op, amdg_precision prec = AMDG_
     L.blk = op->d_blk;
     L.blocks64 = op->d_blocks64;
     L.blocks32 = op->d_blocks32;
+    L.pairs = reinterpret_cast<const int2*>(op->d_pairs);
+    L.blocks64p = op->d_blocks64p;
+    L.blocks32p = op->d_blocks32p;
     return L;
 }
 
@@ -175,29 +187,46 @@ amdg_status rk3_steps_device(amdg_linear_op* op, double dt, int nsteps, amdg_pre
     amdg_grid* g = op->grid;
     cudaStream_t st = stream_of(g->ctx);
     LinearLaunch L = linear_launch(op, prec);
-    const bool mixed = prec == AMDG_PREC_MIXED;
-    // mixed mode reads neighbours from float shadows of the stage inputs; the
-    // shadow of u is refreshed once per call, later ones come from the epilogues
-    float* s_u = op->d_shadow;
-    float* s_1 = mixed ? op->d_shadow + op->capacity : nullptr;
-    float* s_2 = mixed ? op->d_shadow + 2 * op->capacity : nullptr;
-    if (mixed && nsteps > 0) {
-        AMDG_CK(launch_to_float(g->d_u, s_u, g->dof, st));
+    if (prec == AMDG_PREC_MIXED) {
+        // the stage vectors live as FP32 (hi, lo) pairs for the whole call:
+        // split u once, step without touching the FP64 pipe, merge back once
+        float* hi[3] = {op->d_shadow, op->d_shadow + op->capacity, op->d_shadow + 2 * op->capacity};
+        float* lo[3] = {op->d_lo, op->d_lo + op->capacity, op->d_lo + 2 * op->capacity};
+        if (nsteps == 0) return AMDG_OK;
+        AMDG_CK(launch_split(g->d_u, hi[0], lo[0], g->dof, st));
         g->ctx->launches++;
+        const int in_i[3] = {0, 1, 2}, out_i[3] = {1, 2, 0};
+        for (int s = 0; s < nsteps; ++s) {
+            for (int stage = 0; stage < 3; ++stage) {
+                L.us = nullptr;
+                L.un = nullptr;
+                L.out = nullptr;
+                L.us_shadow = hi[in_i[stage]];
+                L.shadow_out = nullptr;
+                L.df = df_stage(rk3_stage_coef(stage, dt));
+                L.df.us_hi = hi[in_i[stage]];
+                L.df.us_lo = lo[in_i[stage]];
+                L.df.un_hi = hi[0];
+                L.df.un_lo = lo[0];
+                L.df.out_hi = hi[out_i[stage]];
+                L.df.out_lo = lo[out_i[stage]];
+                AMDG_CK(launch_linear(L, true, rk3_stage_coef(stage, dt), st));
+                g->ctx->launches++;
+            }
+        }
+        AMDG_CK(launch_merge(hi[0], lo[0], g->d_u, g->dof, st));
+        g->ctx->launches++;
+        return AMDG_OK;
     }
     for (int s = 0; s < nsteps; ++s) {
         // u1 = u + dt L(u); u2 = 3/4 u + 1/4 (u1 + dt L(u1)); u = 1/3 u + 2/3 (u2 + dt L(u2))
         double* in[3] = {g->d_u, op->d_u1, op->d_u2};
         double* outp[3] = {op->d_u1, op->d_u2, g->d_u};
-        float* sin_[3] = {s_u, s_1, s_2};
-        float* sout[3] = {s_1, s_2, s_u};
         for (int stage = 0; stage < 3; ++stage) {
             L.us = in[stage];
             L.un = g->d_u;
             L.out = outp[stage];
-            L.us_shadow = mixed ? sin_[stage] : nullptr;
-            L.shadow_out = mixed ? sout[stage] : nullptr;
-            AMDG_CK(launch_linear(L, mixed, rk3_stage_coef(stage, dt), st));
+            AMDG_CK(launch_linear(L, false, rk3_stage_coef(stage, dt), st));
             g->ctx->launches++;
         }
     }
@@ -217,17 +246,24 @@ amdg_status autotune_linear(amdg_linear_op* op) {
     cudaEvent_t a, b;
     AMDG_CK(cudaEventCreate(&a));
     AMDG_CK(cudaEventCreate(&b));
-    AMDG_CK(launch_to_float(g->d_u, op->d_shadow, g->dof, st));
+    AMDG_CK(launch_split(g->d_u, op->d_shadow, op->d_lo, g->dof, st));
     for (int p = 0; p < 2; ++p) {
         float best = 1e30f;
         for (int v = 0; v < 2; ++v) {
             LinearLaunch L = linear_launch(op);
             L.variant = v;
+            const StageCoef rk{1, 0.0, 1.0, 0.0};
             L.us = g->d_u;
             L.un = g->d_u;
             L.out = op->d_u1;
-            L.us_shadow = p == 1 ? op->d_shadow : nullptr;
-            const StageCoef rk{1, 0.0, 1.0, 0.0};
+            if (p == 1) {  // the mixed stage as rk3_steps_device runs it
+                L.us_shadow = op->d_shadow;
+                L.df = df_stage(rk);
+                L.df.us_hi = L.df.un_hi = op->d_shadow;
+                L.df.us_lo = L.df.un_lo = op->d_lo;
+                L.df.out_hi = op->d_shadow + op->capacity;
+                L.df.out_lo = op->d_lo + op->capacity;
+            }
             AMDG_CK(launch_linear(L, p == 1, rk, st));  // warm-up
             AMDG_CK(cudaEventRecord(a, st));
             for (int r = 0; r < 3; ++r) AMDG_CK(launch_linear(L, p == 1, rk, st));
@@ -255,26 +291,42 @@ amdg_status linear_sync(amdg_linear_op* op) {
     LinearTopology topo;
     build_linear_topology(g->host, op1d, op->coef.data(), &topo);
     cudaFree(op->d_row_ptr); cudaFree(op->d_src); cudaFree(op->d_blk); cudaFree(op->d_blocks64); cudaFree(op->d_blocks32);
+    cudaFree(op->d_pairs); cudaFree(op->d_blocks64p); cudaFree(op->d_blocks32p);
+    op->d_pairs = nullptr;
+    op->d_blocks64p = nullptr;
+    op->d_blocks32p = nullptr;
     op->d_row_ptr = op->d_src = op->d_blk = nullptr;
     op->d_blocks64 = nullptr;
     op->d_blocks32 = nullptr;
     op->pairs = int64_t(topo.src.size());
     op->num_blocks = topo.num_blocks;
     std::vector<float> b32(topo.blocks.begin(), topo.blocks.end());
+    // column variant: interleaved (src, blk) pairs and blocks padded to 16-byte multiples
+    const int np = g->host.k + 1, bs = (np * np + 3) / 4 * 4;
+    std::vector<int32_t> pairs(topo.src.size() * 2);
+    for (size_t i = 0; i < topo.src.size(); ++i) { pairs[2 * i] = topo.src[i]; pairs[2 * i + 1] = topo.blk[i]; }
+    const size_t nblk = topo.blocks.size() / size_t(np * np);
+    std::vector<double> p64(nblk * bs, 0.0);
+    for (size_t b = 0; b < nblk; ++b)
+        for (int j = 0; j < np * np; ++j) p64[b * bs + j] = topo.blocks[b * np * np + j];
+    std::vector<float> p32(p64.begin(), p64.end());
     cudaStream_t st = stream_of(g->ctx);
     amdg_status s;
     if ((s = upload(&op->d_row_ptr, topo.row_ptr, st)) != AMDG_OK || (s = upload(&op->d_src, topo.src, st)) != AMDG_OK ||
         (s = upload(&op->d_blk, topo.blk, st)) != AMDG_OK || (s = upload(&op->d_blocks64, topo.blocks, st)) != AMDG_OK ||
-        (s = upload(&op->d_blocks32, b32, st)) != AMDG_OK)
+        (s = upload(&op->d_blocks32, b32, st)) != AMDG_OK || (s = upload(&op->d_pairs, pairs, st)) != AMDG_OK ||
+        (s = upload(&op->d_blocks64p, p64, st)) != AMDG_OK || (s = upload(&op->d_blocks32p, p32, st)) != AMDG_OK)
         return s;
     if (g->dof > op->capacity) {
         cudaFree(op->d_u1);
         cudaFree(op->d_u2);
         cudaFree(op->d_shadow);
+        cudaFree(op->d_lo);
         op->d_u1 = op->d_u2 = nullptr;
-        op->d_shadow = nullptr;
+        op->d_shadow = op->d_lo = nullptr;
         if ((s = dev_alloc(&op->d_u1, size_t(g->dof))) != AMDG_OK || (s = dev_alloc(&op->d_u2, size_t(g->dof))) != AMDG_OK ||
-            (s = dev_alloc(&op->d_shadow, size_t(g->dof) * 3)) != AMDG_OK)
+            (s = dev_alloc(&op->d_shadow, size_t(g->dof) * 3)) != AMDG_OK ||
+            (s = dev_alloc(&op->d_lo, size_t(g->dof) * 3)) != AMDG_OK)
             return s;
         op->capacity = g->dof;
     }
@@ -539,13 +591,27 @@ amdg_status amdg_grid_init_separable_adaptive(amdg_grid* g, int nterms, amdg_fn1
     if ((s = project_terms(g, nterms, f, user, &coef)) != AMDG_OK) return s;
     // refine every leaf whose projected block exceeds eps, fill holes, repeat
     // until nothing changes (DGAdapt::refine_init_separable_scalar_sum)
+    // norms depend only on the element, so each is computed once; the element
+    // set is refined on the host and the device arrays are rebuilt once at the end
+    HostGrid work = g->host;
+    std::unordered_map<uint64_t, double> cache;
     for (;;) {
-        std::vector<double> norms;
-        element_separable_norms(g->host, coef, nterms, &norms);
-        std::vector<uint64_t> keys = refine_keys(g->host, norms.data(), eps);
-        if (int64_t(keys.size()) == g->host.num_elements) break;
-        if ((s = grid_set_keys(g, std::move(keys))) != AMDG_OK) return s;
+        HostGrid fresh;
+        fresh.dim = work.dim; fresh.nmax = work.nmax; fresh.k = work.k;
+        std::vector<uint64_t> todo;
+        for (int64_t e = 0; e < work.num_elements; ++e)
+            if (!cache.count(work.key[e])) todo.push_back(work.key[e]);
+        grid_from_keys(work.dim, work.nmax, work.k, todo, &fresh);
+        std::vector<double> fn;
+        element_separable_norms(fresh, coef, nterms, &fn);
+        for (int64_t e = 0; e < fresh.num_elements; ++e) cache[fresh.key[e]] = fn[e];
+        std::vector<double> norms(work.num_elements);
+        for (int64_t e = 0; e < work.num_elements; ++e) norms[e] = cache[work.key[e]];
+        std::vector<uint64_t> keys = refine_keys(work, norms.data(), eps);
+        if (int64_t(keys.size()) == work.num_elements) break;
+        grid_from_keys(work.dim, work.nmax, work.k, std::move(keys), &work);
     }
+    if (work.num_elements != g->host.num_elements && (s = grid_set_keys(g, work.key)) != AMDG_OK) return s;
     cudaStream_t st = stream_of(g->ctx);
     double* d_coef = nullptr;
     if ((s = upload(&d_coef, coef, st)) != AMDG_OK) return s;
@@ -589,13 +655,13 @@ amdg_status amdg_grid_version(const amdg_grid* g, int64_t* version) {
     return AMDG_OK;
 }
 
-static amdg_status reduce_grid(const amdg_grid* g, const double* d_coef, int mode, double* out) {
+static amdg_status reduce_grid(const amdg_grid* g, const double* d_coef, int mode, double* out, int nterms = 1) {
     amdg_status s = set_device(g->ctx);
     if (s != AMDG_OK) return s;
     cudaStream_t st = stream_of(g->ctx);
     const int np = g->host.k + 1;
     AMDG_CK(launch_reduce(g->d_u, g->d_order, d_coef, g->host.dim, np, (1 << g->host.nmax) * np, g->host.num_elements,
-                          mode, g->d_scratch, st));
+                          mode, g->d_scratch, st, nterms));
     g->ctx->launches += 2;
     double r = 0.0;
     AMDG_CK(cudaMemcpyAsync(&r, g->d_scratch + kReduceBlocks, sizeof(double), cudaMemcpyDeviceToHost, st));
@@ -611,15 +677,20 @@ amdg_status amdg_grid_l2_norm(const amdg_grid* g, double* out) {
 }
 
 amdg_status amdg_grid_l2_error_separable(const amdg_grid* g, amdg_fn1d f, void* user, double l2_norm_exact, double* out) {
-    AMDG_REQUIRE(g && f && out, AMDG_ERR_ARG, "null argument");
+    return amdg_grid_l2_error_separable_sum(g, 1, f, user, l2_norm_exact, out);
+}
+
+amdg_status amdg_grid_l2_error_separable_sum(const amdg_grid* g, int nterms, amdg_fn1d f, void* user,
+                                             double l2_norm_exact, double* out) {
+    AMDG_REQUIRE(g && f && out && nterms > 0, AMDG_ERR_ARG, "bad arguments");
     std::vector<double> coef;
-    amdg_status s = project_terms(g, 1, f, user, &coef);
+    amdg_status s = project_terms(g, nterms, f, user, &coef);
     if (s != AMDG_OK) return s;
     cudaStream_t st = stream_of(g->ctx);
     double* d_coef = nullptr;
     if ((s = upload(&d_coef, coef, st)) != AMDG_OK) return s;
     double r = 0.0;
-    s = reduce_grid(g, d_coef, 1, &r);
+    s = reduce_grid(g, d_coef, 1, &r, nterms);
     cudaFree(d_coef);
     if (s != AMDG_OK) return s;
     const double err2 = l2_norm_exact * l2_norm_exact + r;
@@ -655,11 +726,15 @@ amdg_status amdg_linear_destroy(amdg_linear_op* op) {
     cudaFree(op->d_row_ptr);
     cudaFree(op->d_src);
     cudaFree(op->d_blk);
+    cudaFree(op->d_pairs);
+    cudaFree(op->d_blocks64p);
+    cudaFree(op->d_blocks32p);
     cudaFree(op->d_blocks64);
     cudaFree(op->d_blocks32);
     cudaFree(op->d_u1);
     cudaFree(op->d_u2);
     cudaFree(op->d_shadow);
+    cudaFree(op->d_lo);
     delete op;
     return AMDG_OK;
 }

@@ -1,0 +1,247 @@
+// C-ABI of batched independent solves (many grids, one launch per RK stage).
+//
+// The grids keep their own element tables and coefficients; the batch copies
+// them into one concatenated device state, builds one neighbour list over all
+// elements, and advances every solve with one fused launch per SSP-RK3 stage.
+// A step's launches can be captured once into a CUDA graph and replayed.
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <cstring>
+#include <new>
+#include <string>
+#include <vector>
+
+#include "amdg.h"
+#include "amdg_internal.hpp"
+#include "kernels.cuh"
+
+using namespace amdg;
+
+#define AMDG_CK(...)                                                                                    \
+    do {                                                                                                \
+        cudaError_t amdg_err_ = (__VA_ARGS__);                                                          \
+        if (amdg_err_ != cudaSuccess)                                                                   \
+            return fail(AMDG_ERR_CUDA, std::string(#__VA_ARGS__) + ": " + cudaGetErrorString(amdg_err_)); \
+    } while (0)
+
+#define AMDG_REQUIRE(cond, code, msg)        \
+    do {                                     \
+        if (!(cond)) return fail(code, msg); \
+    } while (0)
+
+namespace {
+
+template <class T>
+amdg_status alloc(T** p, size_t n) {
+    *p = nullptr;
+    if (n == 0) return AMDG_OK;
+    cudaError_t e = cudaMalloc(reinterpret_cast<void**>(p), n * sizeof(T));
+    if (e != cudaSuccess) return fail(AMDG_ERR_NOMEM, std::string("cudaMalloc: ") + cudaGetErrorString(e));
+    return AMDG_OK;
+}
+
+template <class T>
+amdg_status put(T** p, const std::vector<T>& h) {
+    amdg_status s = alloc(p, h.size());
+    if (s != AMDG_OK || h.empty()) return s;
+    AMDG_CK(cudaMemcpy(*p, h.data(), h.size() * sizeof(T), cudaMemcpyHostToDevice));
+    return AMDG_OK;
+}
+
+cudaStream_t stream_of(const amdg_batch* b) { return static_cast<cudaStream_t>(b->ctx->stream); }
+
+StageCoef coef_of(int stage) {
+    switch (stage) {
+        case 0: return StageCoef{1, 0.0, 1.0, 0.0};
+        case 1: return StageCoef{1, 3. / 4., 1. / 4., 0.0};
+        default: return StageCoef{1, 1. / 3., 2. / 3., 0.0};
+    }
+}
+
+// one SSP-RK3 step of every solve: three fused launches
+amdg_status batch_step(amdg_batch* b, amdg_precision prec, cudaStream_t st) {
+    double* in[3] = {b->d_u, b->d_u1, b->d_u2};
+    double* out[3] = {b->d_u1, b->d_u2, b->d_u};
+    float* sh[3] = {b->d_shadow, b->d_shadow + b->dof, b->d_shadow + 2 * b->dof};
+    const int sout[3] = {1, 2, 0};
+    for (int stage = 0; stage < 3; ++stage) {
+        const StageCoef c = coef_of(stage);
+        if (prec == AMDG_PREC_MIXED) {
+            BatchLaunch<float, float> L{};
+            L.dim = b->dim; L.np = b->k + 1; L.mode = 1; L.a = c.a; L.b = c.b;
+            L.num_elements = b->num_elements; L.num_blocks = b->num_blocks;
+            L.us = in[stage]; L.xs = sh[stage]; L.un = b->d_u; L.out = out[stage]; L.shadow_out = sh[sout[stage]];
+            L.row_ptr = b->d_row_ptr; L.src = b->d_src; L.blk = b->d_blk; L.blocks = b->d_blocks32;
+            L.coef = b->d_coef32; L.dt = b->d_dt; L.solve_of = b->d_solve;
+            AMDG_CK(launch_batch<float, float>(L, st));
+        } else {
+            BatchLaunch<double, double> L{};
+            L.dim = b->dim; L.np = b->k + 1; L.mode = 1; L.a = c.a; L.b = c.b;
+            L.num_elements = b->num_elements; L.num_blocks = b->num_blocks;
+            L.us = in[stage]; L.xs = in[stage]; L.un = b->d_u; L.out = out[stage]; L.shadow_out = nullptr;
+            L.row_ptr = b->d_row_ptr; L.src = b->d_src; L.blk = b->d_blk; L.blocks = b->d_blocks64;
+            L.coef = b->d_coef64; L.dt = b->d_dt; L.solve_of = b->d_solve;
+            AMDG_CK(launch_batch<double, double>(L, st));
+        }
+    }
+    return AMDG_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+amdg_status amdg_batch_create(amdg_context* ctx, int n, amdg_grid* const* grids, const double* coef, amdg_batch** out) {
+    AMDG_REQUIRE(ctx && grids && coef && out && n > 0, AMDG_ERR_ARG, "bad arguments");
+    *out = nullptr;
+    const int dim = grids[0]->host.dim, nmax = grids[0]->host.nmax, k = grids[0]->host.k;
+    std::vector<const HostGrid*> hg(n);
+    for (int i = 0; i < n; ++i) {
+        AMDG_REQUIRE(grids[i] && grids[i]->ctx == ctx, AMDG_ERR_ARG, "every grid must belong to the context");
+        AMDG_REQUIRE(grids[i]->host.dim == dim && grids[i]->host.nmax == nmax && grids[i]->host.k == k, AMDG_ERR_ARG,
+                     "grids must share dim, nmax and k");
+        hg[i] = &grids[i]->host;
+    }
+    for (int i = 0; i < n * dim; ++i) AMDG_REQUIRE(std::isfinite(coef[i]), AMDG_ERR_ARG, "non-finite velocity");
+    AMDG_CK(cudaSetDevice(ctx->device));
+    amdg_batch* b = new (std::nothrow) amdg_batch;
+    AMDG_REQUIRE(b, AMDG_ERR_NOMEM, "host allocation failed");
+    b->ctx = ctx;
+    b->device = ctx->device;
+    b->dim = dim; b->nmax = nmax; b->k = k; b->nsolves = n;
+    b->block = grids[0]->block;
+    b->grids.assign(grids, grids + n);
+    Basis1D basis{k, nmax};
+    Oper1D op;
+    build_oper1d(basis, &op, false);
+    BatchTopology topo;
+    build_batch_topology(hg, op, &topo);
+    b->elem_offset = topo.elem_offset;
+    b->num_elements = topo.elem_offset[n];
+    b->dof = b->num_elements * b->block;
+    b->pairs = int64_t(topo.src.size());
+    b->num_blocks = topo.num_blocks;
+    std::vector<double> c64(coef, coef + size_t(n) * dim);
+    std::vector<float> c32(c64.begin(), c64.end());
+    std::vector<float> b32(topo.blocks.begin(), topo.blocks.end());
+    std::vector<double> dt(n, 0.0);
+    amdg_status s;
+    if ((s = put(&b->d_row_ptr, topo.row_ptr)) != AMDG_OK || (s = put(&b->d_src, topo.src)) != AMDG_OK ||
+        (s = put(&b->d_blk, topo.blk)) != AMDG_OK || (s = put(&b->d_solve, topo.solve_of)) != AMDG_OK ||
+        (s = put(&b->d_blocks64, topo.blocks)) != AMDG_OK || (s = put(&b->d_blocks32, b32)) != AMDG_OK ||
+        (s = put(&b->d_coef64, c64)) != AMDG_OK || (s = put(&b->d_coef32, c32)) != AMDG_OK ||
+        (s = put(&b->d_dt, dt)) != AMDG_OK || (s = alloc(&b->d_u, size_t(b->dof))) != AMDG_OK ||
+        (s = alloc(&b->d_u1, size_t(b->dof))) != AMDG_OK || (s = alloc(&b->d_u2, size_t(b->dof))) != AMDG_OK ||
+        (s = alloc(&b->d_shadow, size_t(b->dof) * 3)) != AMDG_OK) {
+        amdg_batch_destroy(b);
+        return s;
+    }
+    cudaStream_t st = stream_of(b);
+    for (int i = 0; i < n; ++i) {
+        cudaError_t e = cudaMemcpyAsync(b->d_u + b->elem_offset[i] * b->block, grids[i]->d_u,
+                                        size_t(grids[i]->dof) * sizeof(double), cudaMemcpyDeviceToDevice, st);
+        if (e != cudaSuccess) {
+            amdg_batch_destroy(b);
+            return fail(AMDG_ERR_CUDA, std::string("batch gather: ") + cudaGetErrorString(e));
+        }
+    }
+    cudaError_t e = cudaStreamSynchronize(st);
+    if (e != cudaSuccess) {
+        amdg_batch_destroy(b);
+        return fail(AMDG_ERR_CUDA, std::string("batch create: ") + cudaGetErrorString(e));
+    }
+    *out = b;
+    return AMDG_OK;
+}
+
+amdg_status amdg_batch_destroy(amdg_batch* b) {
+    if (!b) return AMDG_OK;
+    cudaSetDevice(b->device);
+    for (int p = 0; p < 2; ++p)
+        if (b->graph_exec[p]) cudaGraphExecDestroy(static_cast<cudaGraphExec_t>(b->graph_exec[p]));
+    void* ptrs[] = {b->d_row_ptr, b->d_src, b->d_blk, b->d_solve, b->d_blocks64, b->d_blocks32, b->d_coef64,
+                    b->d_coef32, b->d_dt, b->d_u, b->d_u1, b->d_u2, b->d_shadow};
+    for (void* p : ptrs) cudaFree(p);
+    delete b;
+    return AMDG_OK;
+}
+
+amdg_status amdg_batch_size(const amdg_batch* b, int64_t* num_elements, int64_t* dof, int64_t* pairs) {
+    AMDG_REQUIRE(b, AMDG_ERR_ARG, "batch is null");
+    if (num_elements) *num_elements = b->num_elements;
+    if (dof) *dof = b->dof;
+    if (pairs) *pairs = b->pairs;
+    return AMDG_OK;
+}
+
+amdg_status amdg_batch_set_dt(amdg_batch* b, const double* dt) {
+    AMDG_REQUIRE(b && dt, AMDG_ERR_ARG, "null argument");
+    for (int i = 0; i < b->nsolves; ++i) AMDG_REQUIRE(std::isfinite(dt[i]), AMDG_ERR_ARG, "non-finite dt");
+    AMDG_CK(cudaSetDevice(b->device));
+    AMDG_CK(cudaMemcpyAsync(b->d_dt, dt, size_t(b->nsolves) * sizeof(double), cudaMemcpyHostToDevice, stream_of(b)));
+    AMDG_CK(cudaStreamSynchronize(stream_of(b)));
+    return AMDG_OK;
+}
+
+amdg_status amdg_batch_rk3_steps(amdg_batch* b, int nsteps, amdg_precision prec, int use_graph) {
+    AMDG_REQUIRE(b && nsteps >= 0, AMDG_ERR_ARG, "bad arguments");
+    AMDG_REQUIRE(prec == AMDG_PREC_FP64 || prec == AMDG_PREC_MIXED, AMDG_ERR_ARG, "bad precision");
+    AMDG_CK(cudaSetDevice(b->device));
+    cudaStream_t st = stream_of(b);
+    const int pi = prec == AMDG_PREC_MIXED ? 1 : 0;
+    if (nsteps == 0) return AMDG_OK;
+    if (prec == AMDG_PREC_MIXED) {
+        AMDG_CK(launch_to_float(b->d_u, b->d_shadow, b->dof, st));
+        b->ctx->launches++;
+    }
+    if (!use_graph) {
+        for (int s = 0; s < nsteps; ++s) {
+            amdg_status r = batch_step(b, prec, st);
+            if (r != AMDG_OK) return r;
+            b->ctx->launches += 3;
+        }
+        return AMDG_OK;
+    }
+    if (!b->graph_exec[pi]) {
+        // capture one step (three launches) once; pointers and the dt array are fixed
+        cudaGraph_t graph = nullptr;
+        AMDG_CK(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+        amdg_status r = batch_step(b, prec, st);
+        cudaError_t e = cudaStreamEndCapture(st, &graph);
+        if (r != AMDG_OK) return r;
+        if (e != cudaSuccess) return fail(AMDG_ERR_CUDA, std::string("graph capture: ") + cudaGetErrorString(e));
+        cudaGraphExec_t exec = nullptr;
+        e = cudaGraphInstantiate(&exec, graph, 0);
+        cudaGraphDestroy(graph);
+        if (e != cudaSuccess) return fail(AMDG_ERR_CUDA, std::string("graph instantiate: ") + cudaGetErrorString(e));
+        b->graph_exec[pi] = exec;
+    }
+    for (int s = 0; s < nsteps; ++s) {
+        AMDG_CK(cudaGraphLaunch(static_cast<cudaGraphExec_t>(b->graph_exec[pi]), st));
+        b->ctx->launches += 3;
+    }
+    return AMDG_OK;
+}
+
+amdg_status amdg_batch_store(amdg_batch* b, int solve) {
+    AMDG_REQUIRE(b && solve >= 0 && solve < b->nsolves, AMDG_ERR_ARG, "bad arguments");
+    amdg_grid* g = b->grids[solve];
+    AMDG_REQUIRE(g->host.num_elements == b->elem_offset[solve + 1] - b->elem_offset[solve], AMDG_ERR_STATE,
+                 "the grid changed since the batch was built");
+    AMDG_CK(cudaSetDevice(b->device));
+    AMDG_CK(cudaMemcpyAsync(g->d_u, b->d_u + b->elem_offset[solve] * b->block, size_t(g->dof) * sizeof(double),
+                            cudaMemcpyDeviceToDevice, stream_of(b)));
+    AMDG_CK(cudaStreamSynchronize(stream_of(b)));
+    return AMDG_OK;
+}
+
+amdg_status amdg_batch_coefficients_device(amdg_batch* b, double** device_ptr, int64_t* elem_offsets) {
+    AMDG_REQUIRE(b && device_ptr, AMDG_ERR_ARG, "null argument");
+    *device_ptr = b->d_u;
+    if (elem_offsets)
+        for (int i = 0; i <= b->nsolves; ++i) elem_offsets[i] = b->elem_offset[i];
+    return AMDG_OK;
+}
+
+}  // extern "C"

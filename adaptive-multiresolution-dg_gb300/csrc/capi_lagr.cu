@@ -6,6 +6,7 @@
 // and the SSP-RK3 stage update.
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cmath>
 #include <cstring>
 #include <new>
@@ -16,6 +17,7 @@
 #include "amdg_internal.hpp"
 #include "kernels.cuh"
 #include "kernels_lagr.cuh"
+#include "kernels_mlp.cuh"
 
 using namespace amdg;
 
@@ -91,6 +93,10 @@ TransformArgs<T> base_args(const amdg_burgers_op* op, int t, const int* from, co
     a.ptr = flx ? op->d_flx_ptr : op->d_vol_ptr;
     a.src = flx ? op->d_flx_src : op->d_vol_src;
     a.split = flx ? op->d_flx_split : op->d_vol_split;
+    a.long_flag = flx ? op->d_flx_long : op->d_vol_long;
+    const std::vector<int32_t>& off = flx ? op->flx_long_off : op->vol_long_off;
+    a.long_elems = (flx ? op->d_flx_long_elems : op->d_vol_long_elems) + off[t];
+    a.num_long = off[t + 1] - off[t];
     return a;
 }
 
@@ -267,13 +273,34 @@ amdg_status burgers_sync(amdg_burgers_op* op) {
     for (int32_t* p : old) cudaFree(p);
     op->d_vol_ptr = op->d_vol_src = op->d_vol_lev = op->d_flx_ptr = op->d_flx_src = op->d_flx_lev = op->d_anc = nullptr;
     op->d_vol_split = op->d_flx_split = nullptr;
+    cudaFree(op->d_vol_long); cudaFree(op->d_flx_long); cudaFree(op->d_vol_long_elems); cudaFree(op->d_flx_long_elems);
+    op->d_vol_long = op->d_flx_long = nullptr;
+    op->d_vol_long_elems = op->d_flx_long_elems = nullptr;
+    std::vector<int32_t> vle, fle;
+    op->vol_long_off.assign(1, 0);
+    op->flx_long_off.assign(1, 0);
+    for (int t = 0; t < g->host.dim; ++t) {
+        vle.insert(vle.end(), topo.vol_long_elems[t].begin(), topo.vol_long_elems[t].end());
+        fle.insert(fle.end(), topo.flx_long_elems[t].begin(), topo.flx_long_elems[t].end());
+        op->vol_long_off.push_back(int32_t(vle.size()));
+        op->flx_long_off.push_back(int32_t(fle.size()));
+    }
     amdg_status s;
     if ((s = upload_vec(&op->d_vol_ptr, topo.vol_ptr)) != AMDG_OK || (s = upload_vec(&op->d_vol_src, topo.vol_src)) != AMDG_OK ||
         (s = upload_vec(&op->d_vol_lev, topo.vol_lev)) != AMDG_OK || (s = upload_vec(&op->d_flx_ptr, topo.flx_ptr)) != AMDG_OK ||
         (s = upload_vec(&op->d_flx_src, topo.flx_src)) != AMDG_OK || (s = upload_vec(&op->d_flx_lev, topo.flx_lev)) != AMDG_OK ||
         (s = upload_vec(&op->d_anc, anc)) != AMDG_OK || (s = upload_vec(&op->d_vol_split, topo.vol_split)) != AMDG_OK ||
-        (s = upload_vec(&op->d_flx_split, topo.flx_split)) != AMDG_OK)
+        (s = upload_vec(&op->d_flx_split, topo.flx_split)) != AMDG_OK ||
+        (s = upload_vec(&op->d_vol_long, topo.vol_long)) != AMDG_OK || (s = upload_vec(&op->d_flx_long, topo.flx_long)) != AMDG_OK ||
+        (s = upload_vec(&op->d_vol_long_elems, vle)) != AMDG_OK || (s = upload_vec(&op->d_flx_long_elems, fle)) != AMDG_OK)
         return s;
+    {
+        std::vector<int32_t> pg;
+        parent_table(g->host, &pg);
+        cudaFree(op->d_pg);
+        op->d_pg = nullptr;
+        if ((s = upload_vec(&op->d_pg, pg)) != AMDG_OK) return s;
+    }
     const int64_t E = g->host.num_elements;
     if (E > op->capacity) {
         const int64_t cap = E + E / 2 + 16;
@@ -343,10 +370,12 @@ amdg_status amdg_burgers_create(amdg_grid* g, const double* alpha, amdg_burgers_
 amdg_status amdg_burgers_destroy(amdg_burgers_op* op) {
     if (!op) return AMDG_OK;
     cudaSetDevice(op->device);
+    if (op->graph_exec) cudaGraphExecDestroy(static_cast<cudaGraphExec_t>(op->graph_exec));
     void* ptrs[] = {op->d_a2p, op->d_lv, op->d_lvx, op->d_lflx, op->d_ajump, op->f_a2p, op->f_lv, op->f_lvx, op->f_lflx,
                     op->f_ajump, op->d_vol_ptr, op->d_vol_src, op->d_vol_lev, op->d_flx_ptr, op->d_flx_src, op->d_flx_lev,
                     op->d_anc, op->d_anc_point, op->d_anc_rank, op->w_up, op->w_fu, op->w_a, op->w_b, op->w_rhs, op->w_u,
-                    op->d_u1, op->d_u2, op->d_rhs64, op->d_pred, op->d_vol_split, op->d_flx_split};
+                    op->d_u1, op->d_u2, op->d_rhs64, op->d_pred, op->d_vol_split, op->d_flx_split,
+                    op->d_vol_long, op->d_flx_long, op->d_vol_long_elems, op->d_flx_long_elems, op->d_pg};
     for (void* p : ptrs) cudaFree(p);
     delete op;
     return AMDG_OK;
@@ -409,23 +438,68 @@ amdg_status amdg_burgers_rk3_steps(amdg_burgers_op* op, double dt, int nsteps, a
     if (amdg_status rs = burgers_sync(op); rs != AMDG_OK) return rs;
     amdg_grid* g = op->grid;
     cudaStream_t st = stream_of(op);
-    const size_t bytes = size_t(g->dof) * sizeof(double);
-    for (int s = 0; s < nsteps; ++s) {
+    if (nsteps == 0) return AMDG_OK;
+    // the launch sequence of a step is fixed for a grid, precision and dt:
+    // capture it once as a CUDA graph and replay it
+    if (!op->graph_exec || op->graph_version != g->version || op->graph_prec != int(prec) || op->graph_dt != dt) {
+        if (op->graph_exec) cudaGraphExecDestroy(static_cast<cudaGraphExec_t>(op->graph_exec));
+        op->graph_exec = nullptr;
+        const size_t bytes = size_t(g->dof) * sizeof(double);
+        const int64_t l0 = g->ctx->launches;
+        cudaGraph_t graph = nullptr;
+        AMDG_CK(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
         // ucoe is updated in place per stage, ucoe_tn holds u^n (RK3SSP::step_stage)
-        AMDG_CK(cudaMemcpyAsync(op->d_u1, g->d_u, bytes, cudaMemcpyDeviceToDevice, st));
-        for (int stage = 0; stage < 3; ++stage) {
-            amdg_status r = eval_rhs(op, op->d_u1, op->d_rhs64, prec);
-            if (r != AMDG_OK) return r;
-            AMDG_CK(launch_stage_update(g->d_u, op->d_u1, op->d_rhs64, g->dof, stage_coef(stage, dt), st));
+        amdg_status r = AMDG_OK;
+        cudaError_t e = cudaMemcpyAsync(op->d_u1, g->d_u, bytes, cudaMemcpyDeviceToDevice, st);
+        for (int stage = 0; stage < 3 && r == AMDG_OK && e == cudaSuccess; ++stage) {
+            r = eval_rhs(op, op->d_u1, op->d_rhs64, prec);
+            if (r == AMDG_OK) e = launch_stage_update(g->d_u, op->d_u1, op->d_rhs64, g->dof, stage_coef(stage, dt), st);
             g->ctx->launches++;
         }
-        AMDG_CK(cudaMemcpyAsync(g->d_u, op->d_u1, bytes, cudaMemcpyDeviceToDevice, st));
+        if (r == AMDG_OK && e == cudaSuccess) e = cudaMemcpyAsync(g->d_u, op->d_u1, bytes, cudaMemcpyDeviceToDevice, st);
+        cudaError_t ec = cudaStreamEndCapture(st, &graph);
+        op->graph_launches = g->ctx->launches - l0;
+        g->ctx->launches = l0;
+        if (r != AMDG_OK) { if (graph) cudaGraphDestroy(graph); return r; }
+        if (e != cudaSuccess || ec != cudaSuccess) {
+            if (graph) cudaGraphDestroy(graph);
+            return fail(AMDG_ERR_CUDA, std::string("graph capture: ") + cudaGetErrorString(e != cudaSuccess ? e : ec));
+        }
+        cudaGraphExec_t exec = nullptr;
+        e = cudaGraphInstantiate(&exec, graph, 0);
+        cudaGraphDestroy(graph);
+        if (e != cudaSuccess) return fail(AMDG_ERR_CUDA, std::string("graph instantiate: ") + cudaGetErrorString(e));
+        op->graph_exec = exec;
+        op->graph_version = g->version;
+        op->graph_prec = int(prec);
+        op->graph_dt = dt;
+    }
+    for (int s = 0; s < nsteps; ++s) {
+        AMDG_CK(cudaGraphLaunch(static_cast<cudaGraphExec_t>(op->graph_exec), st));
+        g->ctx->launches += op->graph_launches;
     }
     return AMDG_OK;
 }
 
-amdg_status amdg_burgers_adaptive_step(amdg_burgers_op* op, double cfl, double wave_speed, double eps, double eta,
-                                       amdg_precision prec, double* dt_out) {
+static double adaptive_dt(const amdg_grid* g, double cfl, double wave_speed) {
+    // dt = cfl / sum_d c_d 2^maxlevel_d  (02_hyperbolic_05_burgers_adapt.cpp:239-247)
+    std::vector<int> lv(g->host.dim, 0);
+    for (int64_t e = 0; e < g->host.num_elements; ++e)
+        for (int d = 0; d < g->host.dim; ++d)
+            lv[d] = std::max(lv[d], level_of_order(g->host.order[size_t(e) * g->host.dim + d]));
+    double sum_c_dx = 0.0;
+    for (int d = 0; d < g->host.dim; ++d) sum_c_dx += wave_speed * std::pow(2.0, lv[d]);
+    return cfl / sum_c_dx;
+}
+
+// keys of the elements present after a step, to mark coarsened ones
+static void mark_removed(const std::vector<uint64_t>& old_keys, const HostGrid& now, int8_t* decisions) {
+    for (size_t e = 0; e < old_keys.size(); ++e)
+        if (!std::binary_search(now.key.begin(), now.key.end(), old_keys[e])) decisions[e] = 2;
+}
+
+amdg_status amdg_burgers_adaptive_step_ex(amdg_burgers_op* op, double cfl, double wave_speed, double eps, double eta,
+                                          amdg_precision prec, double* dt_out, int8_t* decisions) {
     AMDG_REQUIRE(op && std::isfinite(cfl) && cfl > 0 && std::isfinite(wave_speed) && wave_speed > 0, AMDG_ERR_ARG,
                  "bad arguments");
     AMDG_REQUIRE(prec == AMDG_PREC_FP64 || prec == AMDG_PREC_MIXED, AMDG_ERR_ARG, "bad precision");
@@ -433,23 +507,107 @@ amdg_status amdg_burgers_adaptive_step(amdg_burgers_op* op, double cfl, double w
     if (amdg_status rs = burgers_sync(op); rs != AMDG_OK) return rs;
     amdg_grid* g = op->grid;
     cudaStream_t st = stream_of(op);
-    // dt = cfl / sum_d c_d 2^maxlevel_d  (02_hyperbolic_05_burgers_adapt.cpp:239-247)
-    std::vector<int32_t> lv(g->host.dim);
-    amdg_status s = amdg_grid_max_mesh_level(g, lv.data());
-    if (s != AMDG_OK) return s;
-    double sum_c_dx = 0.0;
-    for (int d = 0; d < g->host.dim; ++d) sum_c_dx += wave_speed * std::pow(2.0, lv[d]);
-    const double dt = cfl / sum_c_dx;
+    const double dt = adaptive_dt(g, cfl, wave_speed);
+    const std::vector<uint64_t> old_keys = g->host.key;
     // predictor: forward Euler into the prediction buffer (ForwardEuler::step_stage)
-    if ((s = eval_rhs(op, g->d_u, op->d_rhs64, prec)) != AMDG_OK) return s;
+    amdg_status s = eval_rhs(op, g->d_u, op->d_rhs64, prec);
+    if (s != AMDG_OK) return s;
     AMDG_CK(cudaMemcpyAsync(op->d_pred, g->d_u, size_t(g->dof) * sizeof(double), cudaMemcpyDeviceToDevice, st));
     AMDG_CK(launch_stage_update(g->d_u, op->d_pred, op->d_rhs64, g->dof, stage_coef(0, dt), st));
     g->ctx->launches++;
     // refine on the predicted coefficients; new elements start from zero (DGAdapt::refine, copy_predict_to_ucoe)
-    if ((s = amdg_grid_refine(g, op->d_pred, eps, nullptr)) != AMDG_OK) return s;
+    std::vector<double> norms;
+    if ((s = grid_norms(g, op->d_pred, &norms)) != AMDG_OK) return s;
+    std::vector<uint8_t> refined;
+    std::vector<uint64_t> keys = refine_keys(g->host, norms.data(), eps, &refined);
+    if (decisions)
+        for (size_t e = 0; e < refined.size(); ++e) decisions[e] = refined[e] ? 1 : 0;
+    if (int64_t(keys.size()) != g->host.num_elements && (s = grid_set_keys(g, std::move(keys))) != AMDG_OK) return s;
     if ((s = amdg_burgers_rk3_steps(op, dt, 1, prec)) != AMDG_OK) return s;
     if ((s = amdg_grid_coarsen(g, eta, nullptr)) != AMDG_OK) return s;
+    if (decisions) mark_removed(old_keys, g->host, decisions);
     if (dt_out) *dt_out = dt;
+    return AMDG_OK;
+}
+
+amdg_status amdg_burgers_adaptive_step(amdg_burgers_op* op, double cfl, double wave_speed, double eps, double eta,
+                                       amdg_precision prec, double* dt_out) {
+    return amdg_burgers_adaptive_step_ex(op, cfl, wave_speed, eps, eta, prec, dt_out, nullptr);
+}
+
+amdg_status amdg_burgers_features(amdg_burgers_op* op, const double* d_u, float* d_features) {
+    AMDG_REQUIRE(op && d_u && d_features, AMDG_ERR_ARG, "null argument");
+    AMDG_CK(cudaSetDevice(op->device));
+    if (amdg_status rs = burgers_sync(op); rs != AMDG_OK) return rs;
+    const amdg_grid* g = op->grid;
+    AMDG_CK(launch_element_features(d_u, op->d_pg, g->host.num_elements, g->host.dim, g->block, d_features, stream_of(op)));
+    g->ctx->launches++;
+    return AMDG_OK;
+}
+
+amdg_status amdg_burgers_adaptive_step_learned(amdg_burgers_op* op, amdg_mlp* mlp, double cfl, double wave_speed,
+                                               double eps, double eta, double tau, amdg_precision prec, double* dt_out,
+                                               int64_t* stats) {
+    AMDG_REQUIRE(op && mlp && std::isfinite(cfl) && cfl > 0 && std::isfinite(wave_speed) && wave_speed > 0, AMDG_ERR_ARG,
+                 "bad arguments");
+    AMDG_REQUIRE(prec == AMDG_PREC_FP64 || prec == AMDG_PREC_MIXED, AMDG_ERR_ARG, "bad precision");
+    AMDG_CK(cudaSetDevice(op->device));
+    if (amdg_status rs = burgers_sync(op); rs != AMDG_OK) return rs;
+    amdg_grid* g = op->grid;
+    cudaStream_t st = stream_of(op);
+    const double dt = adaptive_dt(g, cfl, wave_speed);
+    const int64_t E = g->host.num_elements;
+    const int F = g->block * (1 + 2 * g->host.dim);
+    // 1. the network's refine/keep/coarsen probabilities from the current coefficients
+    float* d_feat = reinterpret_cast<float*>(op->w_a);  // E x F floats fit in the E x 4^dim double work buffer
+    float* d_prob = reinterpret_cast<float*>(op->w_b);
+    if (size_t(F) * sizeof(float) > size_t(op->points) * sizeof(double))
+        return fail(AMDG_ERR_CAPACITY, "feature vector larger than the work buffer");
+    AMDG_CK(launch_element_features(g->d_u, op->d_pg, E, g->host.dim, g->block, d_feat, st));
+    g->ctx->launches++;
+    amdg_status s = amdg_mlp_predict(mlp, d_feat, E, d_prob);
+    if (s != AMDG_OK) return s;
+    std::vector<float> prob(size_t(E) * 3);
+    AMDG_CK(cudaMemcpyAsync(prob.data(), d_prob, prob.size() * sizeof(float), cudaMemcpyDeviceToHost, st));
+    std::vector<double> norms;
+    if ((s = grid_norms(g, g->d_u, &norms)) != AMDG_OK) return s;  // synchronises the stream
+    // 2. pre-adapt: leaves the network marks "refine" get children; where it is
+    //    unsure (max probability < tau) the surplus criterion on the current
+    //    coefficients decides instead
+    std::vector<uint8_t> force(E, 0);
+    int64_t n_net = 0, n_unsure = 0;
+    for (int64_t e = 0; e < E; ++e) {
+        const float* p = &prob[size_t(e) * 3];
+        const int arg = (p[1] > p[0] && p[1] >= p[2]) ? 1 : (p[2] > p[0] ? 2 : 0);
+        const float pmax = std::max(p[0], std::max(p[1], p[2]));
+        if (pmax < float(tau)) {
+            ++n_unsure;
+            force[e] = norms[e] > eps ? 1 : 0;
+        } else if (arg == 1) {
+            force[e] = 1;
+            ++n_net;
+        }
+    }
+    std::vector<uint64_t> keys = refine_keys(g->host, norms.data(), eps, nullptr, force.data());
+    if (int64_t(keys.size()) != g->host.num_elements && (s = grid_set_keys(g, std::move(keys))) != AMDG_OK) return s;
+    // 3. one SSP-RK3 step, no predictor step
+    if ((s = amdg_burgers_rk3_steps(op, dt, 1, prec)) != AMDG_OK) return s;
+    // 4. the surplus criterion judges the result: leaves still above eps are missed
+    //    refinements and get their children now; then the usual coarsening
+    if ((s = grid_norms(g, g->d_u, &norms)) != AMDG_OK) return s;
+    std::vector<uint8_t> missed;
+    keys = refine_keys(g->host, norms.data(), eps, &missed);
+    int64_t n_missed = 0;
+    for (uint8_t v : missed) n_missed += v;
+    if (int64_t(keys.size()) != g->host.num_elements && (s = grid_set_keys(g, std::move(keys))) != AMDG_OK) return s;
+    if ((s = amdg_grid_coarsen(g, eta, nullptr)) != AMDG_OK) return s;
+    if (dt_out) *dt_out = dt;
+    if (stats) {
+        stats[0] = n_net;
+        stats[1] = n_unsure;
+        stats[2] = n_missed;
+        stats[3] = g->host.num_elements;
+    }
     return AMDG_OK;
 }
 

@@ -180,6 +180,10 @@ void build_transform_topology(const HostGrid& g, TransformTopology* out) {
     out->flx_ptr.assign(size_t(E) * dim + 1, 0);
     out->vol_split.assign(size_t(E) * dim, 0);
     out->flx_split.assign(size_t(E) * dim, 0);
+    out->vol_long.assign(size_t(E) * dim, 0);
+    out->flx_long.assign(size_t(E) * dim, 0);
+    out->vol_long_elems.assign(dim, {});
+    out->flx_long_elems.assign(dim, {});
     out->vol_src.clear(); out->vol_lev.clear(); out->flx_src.clear(); out->flx_lev.clear();
     std::vector<int32_t> o2(dim);
     for (int64_t e = 0; e < E; ++e) {
@@ -210,6 +214,10 @@ void build_transform_topology(const HostGrid& g, TransformTopology* out) {
             while (sf < int32_t(out->flx_src.size()) && out->flx_lev[sf] <= own) ++sf;
             out->vol_split[size_t(e) * dim + t] = sv;
             out->flx_split[size_t(e) * dim + t] = sf;
+            const int vlen = out->vol_ptr[size_t(e) * dim + t + 1] - out->vol_ptr[size_t(e) * dim + t];
+            const int flen = out->flx_ptr[size_t(e) * dim + t + 1] - out->flx_ptr[size_t(e) * dim + t];
+            if (vlen > kLongRowHost) { out->vol_long[size_t(e) * dim + t] = 1; out->vol_long_elems[t].push_back(int32_t(e)); }
+            if (flen > kLongRowHost) { out->flx_long[size_t(e) * dim + t] = 1; out->flx_long_elems[t].push_back(int32_t(e)); }
         }
     }
 }

@@ -28,6 +28,44 @@ __device__ __forceinline__ double rk_combine(double a, double un, double b, doub
     return __dadd_rn(__dmul_rn(a, un), __dmul_rn(b, __dadd_rn(us, __dmul_rn(dt, rhs))));
 }
 
+// ---- FP32-pair (double-float) arithmetic for the mixed-mode stage update ----
+__device__ __forceinline__ void two_sum(float a, float b, float& s, float& e) {
+    s = __fadd_rn(a, b);
+    const float bb = __fsub_rn(s, a);
+    e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb));
+}
+__device__ __forceinline__ void fast_two_sum(float a, float b, float& s, float& e) {
+    s = __fadd_rn(a, b);
+    e = __fsub_rn(b, __fsub_rn(s, a));
+}
+__device__ __forceinline__ void df_mul(float ah, float al, float bh, float bl, float& ph, float& pl) {
+    const float p = __fmul_rn(ah, bh);
+    float e = fmaf(ah, bh, -p);
+    e = fmaf(ah, bl, e);
+    e = fmaf(al, bh, e);
+    fast_two_sum(p, e, ph, pl);
+}
+__device__ __forceinline__ void df_add(float ah, float al, float bh, float bl, float& sh, float& sl) {
+    float s, e;
+    two_sum(ah, bh, s, e);
+    e = __fadd_rn(e, __fadd_rn(al, bl));
+    fast_two_sum(s, e, sh, sl);
+}
+// out = a*un + b*(us + dt*rhs) on (hi, lo) pairs; rhs is only FP32-accurate, so dt*rhs is one FP32 product
+__device__ __forceinline__ void df_stage_update(const DFState& df, int64_t i, float rhs) {
+    const float p = __fmul_rn(df.dt, rhs);
+    float th, tl;
+    two_sum(df.us_hi[i], p, th, tl);
+    tl = __fadd_rn(tl, df.us_lo[i]);
+    fast_two_sum(th, tl, th, tl);
+    float x1h, x1l, x2h, x2l, vh, vl;
+    df_mul(df.ah, df.al, df.un_hi[i], df.un_lo[i], x1h, x1l);
+    df_mul(df.bh, df.bl, th, tl, x2h, x2l);
+    df_add(x1h, x1l, x2h, x2l, vh, vl);
+    df.out_hi[i] = vh;
+    df.out_lo[i] = vl;
+}
+
 // X: type of the neighbour values read by the contraction (double, or the
 // float shadow of the stage input in mixed mode, so no per-FMA conversion is
 // needed: double->float conversion issues on the FP64 pipe, which on this part
@@ -38,7 +76,7 @@ __global__ void __launch_bounds__(256) linear_apply_kernel(const double* __restr
                                                            const int32_t* __restrict__ row_ptr,
                                                            const int32_t* __restrict__ src, const int32_t* __restrict__ blk,
                                                            const T* __restrict__ blocks, int nblocks, int64_t total,
-                                                           StageCoef rk) {
+                                                           StageCoef rk, DFState df) {
     constexpr int B = IPow<NP, D>::v;
     const int64_t gid = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
     if (gid >= total) return;
@@ -63,6 +101,10 @@ __global__ void __launch_bounds__(256) linear_apply_kernel(const double* __restr
             for (int p = 0; p < NP; ++p) acc = fma(__ldg(m + p * NP), T(__ldg(x + p * stride)), acc);
         }
     }
+    if (df.out_hi) {
+        df_stage_update(df, gid, float(acc));
+        return;
+    }
     const double rhs = double(acc);
     double v;
     if (rk.mode == 0) {
@@ -81,16 +123,44 @@ __global__ void __launch_bounds__(256) linear_apply_kernel(const double* __restr
 // them into the element's block in shared memory; the dimensions are
 // separated by barriers so every output has one writer per dimension.  The
 // fused RK epilogue then streams the G blocks out coalesced.
+template <typename T, int N>
+struct BlockRegs {
+    T v[N];
+};
+
+// load a padded 1D block (N entries, N a multiple of 4 floats / 2 doubles) with vector loads
+template <int N>
+__device__ __forceinline__ BlockRegs<float, N> load_block(const float* m) {
+    BlockRegs<float, N> r;
+#pragma unroll
+    for (int j = 0; j < N / 4; ++j) {
+        const float4 v = __ldg(reinterpret_cast<const float4*>(m) + j);
+        r.v[4 * j] = v.x; r.v[4 * j + 1] = v.y; r.v[4 * j + 2] = v.z; r.v[4 * j + 3] = v.w;
+    }
+    return r;
+}
+template <int N>
+__device__ __forceinline__ BlockRegs<double, N> load_block(const double* m) {
+    BlockRegs<double, N> r;
+#pragma unroll
+    for (int j = 0; j < N / 2; ++j) {
+        const double2 v = __ldg(reinterpret_cast<const double2*>(m) + j);
+        r.v[2 * j] = v.x; r.v[2 * j + 1] = v.y;
+    }
+    return r;
+}
+
 template <int D, int NP, typename T, typename X>
 __global__ void __launch_bounds__(256) linear_col_kernel(const double* __restrict__ us, const X* __restrict__ xs,
                                                          const double* un, double* out, float* shadow_out,
                                                          const int32_t* __restrict__ row_ptr,
-                                                         const int32_t* __restrict__ src, const int32_t* __restrict__ blk,
+                                                         const int2* __restrict__ pairs,
                                                          const T* __restrict__ blocks, int nblocks, int64_t num_elements,
-                                                         StageCoef rk) {
+                                                         StageCoef rk, DFState df) {
     constexpr int B = IPow<NP, D>::v;
     constexpr int C = B / NP;
     constexpr int G = 256 / C;
+    constexpr int BS = (NP * NP + 3) / 4 * 4;  // padded block stride (16-byte vector loads)
     __shared__ T y[G * B];
     const int tid = threadIdx.x;
     const int g = tid / C, c = tid - (tid / C) * C;
@@ -111,18 +181,18 @@ __global__ void __launch_bounds__(256) linear_col_kernel(const double* __restric
             for (int q = 0; q < NP; ++q) acc[q] = T(0);
             const int beg = __ldg(row_ptr + e * D + t);
             const int end = __ldg(row_ptr + e * D + t + 1);
-            const T* bt = blocks + size_t(t) * nblocks * NP * NP;
+            const T* bt = blocks + size_t(t) * nblocks * BS;
             for (int i = beg; i < end; ++i) {
-                const int sidx = __ldg(src + i);
-                const T* m = bt + __ldg(blk + i) * NP * NP;
-                const X* x = xs + int64_t(sidx) * B + base;
+                const int2 pr = __ldg(pairs + i);  // (neighbour element, block id)
+                const BlockRegs<T, BS> m = load_block<BS>(bt + size_t(pr.y) * BS);
+                const X* x = xs + int64_t(pr.x) * B + base;
                 T xv[NP];
 #pragma unroll
                 for (int p = 0; p < NP; ++p) xv[p] = T(__ldg(x + p * stride));
 #pragma unroll
                 for (int p = 0; p < NP; ++p)
 #pragma unroll
-                    for (int q = 0; q < NP; ++q) acc[q] = fma(__ldg(m + p * NP + q), xv[p], acc[q]);
+                    for (int q = 0; q < NP; ++q) acc[q] = fma(m.v[p * NP + q], xv[p], acc[q]);
             }
             T* yb = y + g * B + base;
 #pragma unroll
@@ -135,6 +205,10 @@ __global__ void __launch_bounds__(256) linear_col_kernel(const double* __restric
     for (int i = tid; i < G * B; i += blockDim.x) {
         const int64_t gid = first + i;
         if (gid >= total) break;
+        if (df.out_hi) {
+            df_stage_update(df, gid, float(y[i]));
+            continue;
+        }
         const double rhs = double(y[i]);
         const double v = rk.mode == 0 ? rhs : rk_combine(rk.a, un[gid], rk.b, us[gid], rk.dt, rhs);
         out[gid] = v;
@@ -152,8 +226,11 @@ static cudaError_t launch_col_t(const LinearLaunch& L, const T* blocks, const X*
         constexpr int G = 256 / C;
         if (L.num_elements == 0) return cudaSuccess;
         const int64_t grid = (L.num_elements + G - 1) / G;
+        const T* padded = nullptr;
+        if constexpr (sizeof(T) == 4) padded = L.blocks32p; else padded = L.blocks64p;
         linear_col_kernel<D, NP, T, X><<<unsigned(grid), 256, 0, st>>>(L.us, xs, L.un, L.out, L.shadow_out, L.row_ptr,
-                                                                      L.src, L.blk, blocks, L.num_blocks, L.num_elements, rk);
+                                                                      L.pairs, padded, L.num_blocks, L.num_elements, rk,
+                                                                      L.df);
         return cudaGetLastError();
     }
 }
@@ -172,7 +249,7 @@ static cudaError_t launch_linear_t(const LinearLaunch& L, const T* blocks, const
     const int threads = 256;
     const int64_t grid = (total + threads - 1) / threads;
     linear_apply_kernel<D, NP, T, X><<<unsigned(grid), threads, 0, st>>>(L.us, xs, L.un, L.out, L.shadow_out, L.row_ptr,
-                                                                        L.src, L.blk, blocks, L.num_blocks, total, rk);
+                                                                        L.src, L.blk, blocks, L.num_blocks, total, rk, L.df);
     return cudaGetLastError();
 }
 
@@ -196,6 +273,42 @@ cudaError_t launch_linear(const LinearLaunch& L, bool mixed, StageCoef rk, cudaS
     if (!mixed) return dispatch_linear<double, double>(L, L.blocks64, L.us, rk, st);
     if (L.us_shadow) return dispatch_linear<float, float>(L, L.blocks32, L.us_shadow, rk, st);
     return dispatch_linear<float, double>(L, L.blocks32, L.us, rk, st);
+}
+
+__global__ void split_kernel(const double* __restrict__ in, float* __restrict__ hi, float* __restrict__ lo, int64_t n) {
+    const int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const double d = in[i];
+    const float h = __double2float_rn(d);
+    hi[i] = h;
+    lo[i] = __double2float_rn(d - double(h));
+}
+
+cudaError_t launch_split(const double* in, float* hi, float* lo, int64_t n, cudaStream_t st) {
+    if (n == 0) return cudaSuccess;
+    split_kernel<<<unsigned((n + 255) / 256), 256, 0, st>>>(in, hi, lo, n);
+    return cudaGetLastError();
+}
+
+__global__ void merge_kernel(const float* __restrict__ hi, const float* __restrict__ lo, double* __restrict__ out, int64_t n) {
+    const int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (i < n) out[i] = double(hi[i]) + double(lo[i]);
+}
+
+cudaError_t launch_merge(const float* hi, const float* lo, double* out, int64_t n, cudaStream_t st) {
+    if (n == 0) return cudaSuccess;
+    merge_kernel<<<unsigned((n + 255) / 256), 256, 0, st>>>(hi, lo, out, n);
+    return cudaGetLastError();
+}
+
+DFState df_stage(StageCoef rk) {
+    DFState d{};
+    d.ah = float(rk.a);
+    d.al = float(rk.a - double(d.ah));
+    d.bh = float(rk.b);
+    d.bl = float(rk.b - double(d.bh));
+    d.dt = float(rk.dt);
+    return d;
 }
 
 __global__ void to_float_kernel(const double* __restrict__ in, float* __restrict__ out, int64_t n) {
@@ -261,7 +374,7 @@ constexpr int kReduceThreads = 256;
 
 __global__ void reduce_pass1(const double* __restrict__ u, const int32_t* __restrict__ order,
                              const double* __restrict__ coef1d, int dim, int np, int nb1, int B, int64_t total, int mode,
-                             double* __restrict__ partial) {
+                             int nterms, double* __restrict__ partial) {
     __shared__ double sh[kReduceThreads];
     double s = 0.0;
     for (int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; i < total; i += int64_t(gridDim.x) * blockDim.x) {
@@ -272,8 +385,12 @@ __global__ void reduce_pass1(const double* __restrict__ u, const int32_t* __rest
             int rem = int(i - e * B);
             int dig[8];
             for (int d = dim - 1; d >= 0; --d) { dig[d] = rem % np; rem /= np; }
-            double c = 1.0;
-            for (int d = 0; d < dim; ++d) c *= coef1d[size_t(d) * nb1 + order[e * dim + d] * np + dig[d]];
+            double c = 0.0;
+            for (int t = 0; t < nterms; ++t) {
+                double p = 1.0;
+                for (int d = 0; d < dim; ++d) p *= coef1d[(size_t(t) * dim + d) * nb1 + order[e * dim + d] * np + dig[d]];
+                c += p;
+            }
             term -= 2.0 * v * c;
         }
         s += term;
@@ -303,11 +420,11 @@ __global__ void reduce_pass2(const double* __restrict__ partial, int n, double* 
 int reduce_partials_needed() { return kReduceBlocks + 1; }
 
 cudaError_t launch_reduce(const double* u, const int32_t* order, const double* coef1d, int dim, int np, int nb1,
-                          int64_t num_elements, int mode, double* scratch, cudaStream_t st) {
+                          int64_t num_elements, int mode, double* scratch, cudaStream_t st, int nterms) {
     int B = 1;
     for (int d = 0; d < dim; ++d) B *= np;
     const int64_t total = num_elements * B;
-    reduce_pass1<<<kReduceBlocks, kReduceThreads, 0, st>>>(u, order, coef1d, dim, np, nb1, B, total, mode, scratch);
+    reduce_pass1<<<kReduceBlocks, kReduceThreads, 0, st>>>(u, order, coef1d, dim, np, nb1, B, total, mode, nterms, scratch);
     cudaError_t err = cudaGetLastError();
     if (err != cudaSuccess) return err;
     reduce_pass2<<<1, kReduceThreads, 0, st>>>(scratch, kReduceBlocks, scratch + kReduceBlocks);

@@ -13,6 +13,17 @@ struct StageCoef {
     double a, b, dt;
 };
 
+// Mixed-mode stage state as FP32 (hi, lo) pairs: the stage vectors stay at
+// ~48-bit precision without touching the FP64 pipe (a double->float
+// conversion or an FP64 add costs an FP64-pipe slot, 1/64 of the FP32 rate on
+// this part).  hi doubles as the FP32 value read by the operator apply.
+struct DFState {
+    const float *us_hi, *us_lo, *un_hi, *un_lo;
+    float *out_hi, *out_lo;  // out_hi == nullptr: FP64 epilogue
+    float ah, al, bh, bl;    // stage coefficients a, b as (hi, lo)
+    float dt;
+};
+
 struct LinearLaunch {
     int dim, np;
     int variant;             // 0: thread per output coefficient; 1: column variant (linear_col_supported)
@@ -28,6 +39,10 @@ struct LinearLaunch {
     const int32_t* blk;
     const double* blocks64;
     const float* blocks32;
+    const int2* pairs;        // column variant: (src, blk) interleaved
+    const double* blocks64p;  // column variant: blocks padded to a multiple of 4 entries
+    const float* blocks32p;
+    DFState df;              // zero-initialised: FP64 epilogue
 };
 
 // Batched solves: concatenated element tables, per-element solve index.
@@ -57,13 +72,17 @@ constexpr int kReduceBlocks = 1216;  // 8 CTAs per SM on 152 SMs
 
 cudaError_t launch_linear(const LinearLaunch& L, bool mixed, StageCoef rk, cudaStream_t st);
 bool linear_col_supported(int dim, int np);
+// FP64 vector <-> FP32 (hi, lo) pairs
+cudaError_t launch_split(const double* in, float* hi, float* lo, int64_t n, cudaStream_t st);
+cudaError_t launch_merge(const float* hi, const float* lo, double* out, int64_t n, cudaStream_t st);
+DFState df_stage(StageCoef rk);
 cudaError_t launch_to_float(const double* in, float* out, int64_t n, cudaStream_t st);
 cudaError_t launch_stage_update(const double* un, double* u, const double* rhs, int64_t n, StageCoef rk, cudaStream_t st);
 cudaError_t launch_init_separable(const int32_t* order, const double* coef1d, int dim, int np, int nb1, int nterms,
                                   int64_t num_elements, double* u, cudaStream_t st);
 // scratch: kReduceBlocks + 1 doubles; result in scratch[kReduceBlocks]
 cudaError_t launch_reduce(const double* u, const int32_t* order, const double* coef1d, int dim, int np, int nb1,
-                          int64_t num_elements, int mode, double* scratch, cudaStream_t st);
+                          int64_t num_elements, int mode, double* scratch, cudaStream_t st, int nterms = 1);
 int reduce_partials_needed();
 cudaError_t launch_element_norms(const double* u, int B, int64_t E, double* out, cudaStream_t st);
 cudaError_t launch_remap(const double* old_u, const int32_t* map, int B, int64_t E_new, double* new_u, cudaStream_t st);

@@ -29,9 +29,10 @@ __global__ void __launch_bounds__(256) fibre_transform_kernel(TransformArgs<T> a
     const int inner = idx % a.stride;
     const int qt = (idx / a.stride) % a.n_to;
     const int outer = idx / (a.stride * a.n_to);
+    const int64_t et = e * a.dim + a.t;
+    if (a.long_flag && __ldg(a.long_flag + et)) return;  // done by fibre_transform_long_kernel
     const int oe = __ldg(a.order + e * a.dim + a.t);
     // "L": neighbours finer than e in dimension t; "U": coarser or equal; neighbours are level-sorted
-    const int64_t et = e * a.dim + a.t;
     const int beg = a.lu == 0 ? __ldg(a.split + et) : __ldg(a.ptr + et);
     const int end = a.lu == 2 ? __ldg(a.split + et) : __ldg(a.ptr + et + 1);
     const T* mcol = a.M + size_t(oe) * a.n_to + qt;
@@ -49,11 +50,53 @@ __global__ void __launch_bounds__(256) fibre_transform_kernel(TransformArgs<T> a
     else a.out[gid] = acc;
 }
 
+// Long rows (an element at a coarse level of its fibre sees every finer
+// element of the fibre): one warp per output entry, lanes stride over the
+// neighbours, fixed-order shuffle reduction.  Without the split such rows
+// serialise hundreds of dependent neighbour loads in one thread.
+template <typename T>
+__global__ void __launch_bounds__(256) fibre_transform_long_kernel(TransformArgs<T> a) {
+    const int64_t w = (int64_t(blockIdx.x) * blockDim.x + threadIdx.x) / 32;
+    const int lane = threadIdx.x & 31;
+    if (w >= int64_t(a.num_long) * a.out_block) return;
+    const int64_t e = __ldg(a.long_elems + w / a.out_block);
+    const int idx = int(w % a.out_block);
+    const int inner = idx % a.stride;
+    const int qt = (idx / a.stride) % a.n_to;
+    const int outer = idx / (a.stride * a.n_to);
+    const int64_t et = e * a.dim + a.t;
+    const int oe = __ldg(a.order + et);
+    const int beg = a.lu == 0 ? __ldg(a.split + et) : __ldg(a.ptr + et);
+    const int end = a.lu == 2 ? __ldg(a.split + et) : __ldg(a.ptr + et + 1);
+    const T* mcol = a.M + size_t(oe) * a.n_to + qt;
+    const int in_off = outer * a.n_from * a.stride + inner;
+    T acc = T(0);
+    for (int i = beg + lane; i < end; i += 32) {
+        const int s = __ldg(a.src + i);
+        const int os = __ldg(a.order + int64_t(s) * a.dim + a.t);
+        const T* x = a.in + int64_t(s) * a.in_block + in_off;
+        const T* m = mcol + size_t(os) * a.n_from * a.ncols;
+        for (int k = 0; k < a.n_from; ++k) acc = fma(__ldg(x + k * a.stride), __ldg(m + size_t(k) * a.ncols), acc);
+    }
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, off);
+    if (lane == 0) {
+        acc *= a.coef;
+        const int64_t gid = e * a.out_block + idx;
+        if (a.accumulate) a.out[gid] += acc;
+        else a.out[gid] = acc;
+    }
+}
+
 template <typename T>
 cudaError_t launch_fibre_transform(const TransformArgs<T>& a, cudaStream_t st) {
     const int64_t total = a.num_elements * a.out_block;
     if (total == 0) return cudaSuccess;
     fibre_transform_kernel<T><<<unsigned((total + 255) / 256), 256, 0, st>>>(a);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess || !a.long_flag || a.num_long == 0) return e;
+    const int64_t warps = int64_t(a.num_long) * a.out_block;
+    fibre_transform_long_kernel<T><<<unsigned((warps * 32 + 255) / 256), 256, 0, st>>>(a);
     return cudaGetLastError();
 }
 

@@ -25,7 +25,13 @@ struct TransformArgs {
     const int32_t* order;    // [element][dim] 1D orders
     const T* in;
     T* out;
+    const uint8_t* long_flag;   // [e*dim+t]: row handled by the warp-per-output kernel (null: none)
+    const int32_t* long_elems;  // elements with a long row in dimension t
+    int num_long;
 };
+
+// rows longer than this many neighbours are split across a warp
+constexpr int kLongRow = 24;
 
 template <typename T>
 struct SurplusArgs {

@@ -90,6 +90,9 @@ extern "C" amdg_status amdg_rk3ssp_steps_noalloc(amdg_linear_op* op, double* d_u
     L.blk = op->d_blk;
     L.blocks64 = op->d_blocks64;
     L.blocks32 = op->d_blocks32;
+    L.pairs = reinterpret_cast<const int2*>(op->d_pairs);
+    L.blocks64p = op->d_blocks64p;
+    L.blocks32p = op->d_blocks32p;
     const StageCoef coef[3] = {{1, 0.0, 1.0, dt}, {1, 3. / 4., 1. / 4., dt}, {1, 1. / 3., 2. / 3., dt}};
     for (int step = 0; step < nsteps; ++step) {
         const double* in[3] = {d_u, u1, u2};

@@ -79,11 +79,30 @@ def load():
         "amdg_rk3ssp_steps_noalloc": ([vp, vp, dbl, i32, i32], i32),
         "amdg_burgers_create": ([vp, vp, pp], i32),
         "amdg_burgers_adaptive_step": ([vp, dbl, dbl, dbl, dbl, i32, C.POINTER(dbl)], i32),
+        "amdg_burgers_adaptive_step_ex": ([vp, dbl, dbl, dbl, dbl, i32, C.POINTER(dbl), vp], i32),
+        "amdg_burgers_features": ([vp, vp, vp], i32),
+        "amdg_burgers_adaptive_step_learned": ([vp, vp, dbl, dbl, dbl, dbl, dbl, i32, C.POINTER(dbl), vp], i32),
+        "amdg_mlp_create": ([vp, i32, i32, i32, i32, C.c_uint64, pp], i32),
+        "amdg_mlp_destroy": ([vp], i32),
+        "amdg_mlp_num_params": ([vp, C.POINTER(i64)], i32),
+        "amdg_mlp_get_params": ([vp, vp, i64], i32),
+        "amdg_mlp_set_params": ([vp, vp, i64], i32),
+        "amdg_mlp_predict": ([vp, vp, i64, vp], i32),
+        "amdg_mlp_loss_grad": ([vp, vp, vp, i64, C.POINTER(dbl), vp], i32),
+        "amdg_mlp_train": ([vp, vp, vp, i64, i32, i32, C.c_float, C.c_uint64, C.POINTER(dbl)], i32),
         "amdg_grid_create_ex": ([vp, i32, i32, i32, i32, i32, pp], i32),
         "amdg_grid_init_separable_adaptive": ([vp, i32, FN1D, vp, dbl], i32),
         "amdg_grid_refine": ([vp, vp, dbl, C.POINTER(i64)], i32),
         "amdg_grid_coarsen": ([vp, dbl, C.POINTER(i64)], i32),
         "amdg_grid_version": ([vp, C.POINTER(i64)], i32),
+        "amdg_grid_l2_error_separable_sum": ([vp, i32, FN1D, vp, dbl, C.POINTER(dbl)], i32),
+        "amdg_batch_create": ([vp, i32, vp, vp, pp], i32),
+        "amdg_batch_destroy": ([vp], i32),
+        "amdg_batch_size": ([vp, C.POINTER(i64), C.POINTER(i64), C.POINTER(i64)], i32),
+        "amdg_batch_set_dt": ([vp, vp], i32),
+        "amdg_batch_rk3_steps": ([vp, i32, i32, i32], i32),
+        "amdg_batch_store": ([vp, i32], i32),
+        "amdg_batch_coefficients_device": ([vp, pp, vp], i32),
         "amdg_burgers_destroy": ([vp], i32),
         "amdg_burgers_rhs": ([vp, vp, vp, i32], i32),
         "amdg_burgers_point_values": ([vp, vp, vp, i32], i32),
@@ -249,6 +268,13 @@ class Grid:
         _ck(load().amdg_grid_l2_norm(self._h, C.byref(r)), "grid_l2_norm")
         return r.value
 
+    def l2_error_separable_sum(self, funcs, l2_norm_exact: float) -> float:
+        cb = _fn1d(funcs)
+        r = C.c_double()
+        _ck(load().amdg_grid_l2_error_separable_sum(self._h, len(funcs), cb, None, l2_norm_exact, C.byref(r)),
+            "grid_l2_error_separable_sum")
+        return r.value
+
     def l2_error_separable(self, func, l2_norm_exact: float) -> float:
         cb = _fn1d([func])
         r = C.c_double()
@@ -340,6 +366,27 @@ class BurgersOperator:
     def rk3_steps(self, dt: float, nsteps: int, prec: int = FP64):
         _ck(load().amdg_burgers_rk3_steps(self._h, dt, nsteps, prec), "burgers_rk3_steps")
 
+    def adaptive_step_ex(self, cfl: float, wave_speed: float, eps: float, eta: float, prec: int = FP64):
+        """Adaptive step that also returns the surplus criterion's decision per old element (0 keep, 1 refine, 2 coarsen)."""
+        dec = np.zeros(self.grid.num_elements, np.int8)
+        dt = C.c_double()
+        _ck(load().amdg_burgers_adaptive_step_ex(self._h, cfl, wave_speed, eps, eta, prec, C.byref(dt), _ptr(dec)),
+            "burgers_adaptive_step_ex")
+        self.grid._refresh()
+        return dt.value, dec
+
+    def features_device(self, d_u: int, d_feat: int):
+        _ck(load().amdg_burgers_features(self._h, C.c_void_p(d_u), C.c_void_p(d_feat)), "burgers_features")
+
+    def adaptive_step_learned(self, mlp, cfl: float, wave_speed: float, eps: float, eta: float, tau: float,
+                              prec: int = FP64):
+        stats = np.zeros(4, np.int64)
+        dt = C.c_double()
+        _ck(load().amdg_burgers_adaptive_step_learned(self._h, mlp.handle, cfl, wave_speed, eps, eta, tau, prec,
+                                                      C.byref(dt), _ptr(stats)), "burgers_adaptive_step_learned")
+        self.grid._refresh()
+        return dt.value, stats
+
     def adaptive_step(self, cfl: float, wave_speed: float, eps: float, eta: float, prec: int = FP64) -> float:
         dt = C.c_double()
         _ck(load().amdg_burgers_adaptive_step(self._h, cfl, wave_speed, eps, eta, prec, C.byref(dt)),
@@ -350,6 +397,94 @@ class BurgersOperator:
     def close(self):
         if self._h:
             load().amdg_burgers_destroy(self._h)
+            self._h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class Batch:
+    """Independent constant-coefficient solves advanced together (one launch per RK stage)."""
+
+    def __init__(self, ctx: Context, grids, coef):
+        self.ctx, self.grids = ctx, list(grids)
+        arr = (C.c_void_p * len(self.grids))(*[g.handle.value for g in self.grids])
+        c = np.ascontiguousarray(coef, np.float64).reshape(len(self.grids), -1)
+        self._h = C.c_void_p()
+        _ck(load().amdg_batch_create(ctx.handle, len(self.grids), arr, _ptr(c), C.byref(self._h)), "batch_create")
+        ne, dof, pairs = C.c_int64(), C.c_int64(), C.c_int64()
+        _ck(load().amdg_batch_size(self._h, C.byref(ne), C.byref(dof), C.byref(pairs)), "batch_size")
+        self.num_elements, self.dof, self.pairs = ne.value, dof.value, pairs.value
+
+    def set_dt(self, dt):
+        a = np.ascontiguousarray(dt, np.float64)
+        _ck(load().amdg_batch_set_dt(self._h, _ptr(a)), "batch_set_dt")
+
+    def rk3_steps(self, nsteps: int, prec: int = FP64, use_graph: bool = True):
+        _ck(load().amdg_batch_rk3_steps(self._h, nsteps, prec, int(use_graph)), "batch_rk3_steps")
+
+    def store(self, solve: int):
+        _ck(load().amdg_batch_store(self._h, solve), "batch_store")
+
+    def close(self):
+        if self._h:
+            load().amdg_batch_destroy(self._h)
+            self._h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class MLP:
+    """Per-element refine/keep/coarsen classifier trained and run by the library's own kernels."""
+
+    def __init__(self, ctx: Context, n_in: int, hidden: int = 64, n_hidden_layers: int = 3, n_out: int = 3, seed: int = 0):
+        self.ctx = ctx
+        self.dims = [n_in] + [hidden] * n_hidden_layers + [n_out]
+        self._h = C.c_void_p()
+        _ck(load().amdg_mlp_create(ctx.handle, n_in, hidden, n_hidden_layers, n_out, seed, C.byref(self._h)), "mlp_create")
+        n = C.c_int64()
+        _ck(load().amdg_mlp_num_params(self._h, C.byref(n)), "mlp_num_params")
+        self.num_params = n.value
+
+    @property
+    def handle(self):
+        return self._h
+
+    def params(self) -> np.ndarray:
+        p = np.zeros(self.num_params, np.float32)
+        _ck(load().amdg_mlp_get_params(self._h, _ptr(p), p.size), "mlp_get_params")
+        return p
+
+    def set_params(self, p):
+        p = np.ascontiguousarray(p, np.float32)
+        _ck(load().amdg_mlp_set_params(self._h, _ptr(p), p.size), "mlp_set_params")
+
+    def predict_device(self, d_x: int, n: int, d_probs: int):
+        _ck(load().amdg_mlp_predict(self._h, C.c_void_p(d_x), n, C.c_void_p(d_probs)), "mlp_predict")
+
+    def loss_grad_device(self, d_x: int, d_labels: int, n: int):
+        g = np.zeros(self.num_params, np.float32)
+        loss = C.c_double()
+        _ck(load().amdg_mlp_loss_grad(self._h, C.c_void_p(d_x), C.c_void_p(d_labels), n, C.byref(loss), _ptr(g)),
+            "mlp_loss_grad")
+        return loss.value, g
+
+    def train_device(self, d_x: int, d_labels: int, n: int, epochs: int, batch: int, lr: float, seed: int = 0) -> float:
+        loss = C.c_double()
+        _ck(load().amdg_mlp_train(self._h, C.c_void_p(d_x), C.c_void_p(d_labels), n, epochs, batch, lr, seed,
+                                  C.byref(loss)), "mlp_train")
+        return loss.value
+
+    def close(self):
+        if self._h:
+            load().amdg_mlp_destroy(self._h)
             self._h = C.c_void_p()
 
     def __del__(self):

@@ -223,7 +223,7 @@ def run_ours(args):
         "higher_is_better": True,
         "scaling": "weak",
         "vs_baseline": None,
-        "dtype": "f32 operator apply, f64 state and RK3 stage accumulation",
+        "dtype": "f32 operator apply; f64 state, stage vectors as f32 (hi, lo) pairs",
         "data": "synthetic: IC prod_d sin(2 pi x_d) projected onto the sparse grid",
         "config": {"workload": WORKLOAD, "dim": DIM, "nmax": NMAX, "k": K, "elements": E, "dof": dof,
                    "dt": dt, "l2_flush": "inputs larger than L2 (state 276 MB > 129 MB L2)",
@@ -235,16 +235,23 @@ def run_ours(args):
                        "hbm_frac": ach64 / pk["hbm_gbs"]},
         "roofline": {"bound": "hbm", "achieved": ach32, "peak": pk["hbm_gbs"], "unit": "GB/s",
                      "frac": ach32 / pk["hbm_gbs"], "traffic": None, "peak_kind": pk_kind,
-                     "kernel": "linear_apply_kernel<6,3,float> (fused RK3 stage)", "kernel_ms": k32 * 1e3,
+                     "kernel": ("linear_col_kernel" if op.tuning()[0][1] == 1 else "linear_apply_kernel")
+                               + "<6,3,float,float> (fused RK3 stage, FP32-pair stage state)",
+                     "kernel_ms": k32 * 1e3,
                      "algorithmic_bytes_per_launch": bytes_per_launch,
                      "fp32_tflops": flops / k32 / 1e12},
         "e2e": {"value": units / e2e_sec if world == 1 else None, "unit": "DOF-stage updates/s",
                 "h2d_bytes_per_step": 8 * dof, "d2h_bytes_per_step": 8 * dof,
                 "call": "amdg_rk3ssp_steps_host (mixed), pinned host buffer"},
         "gpu_launches": launches32,
+        "autotune": {"variants": {"fp64": op.tuning()[0][0], "mixed": op.tuning()[0][1]},
+                     "stage_ms": {"fp64": op.tuning()[1][0], "mixed": op.tuning()[1][1]},
+                     "legend": "variant 0 = thread per output, 1 = column variant"},
         "clocks": clocks,
     }
     line["burgers3d"] = bench_burgers(ctx, stream, args)
+    if args.batch_solves > 0:
+        line["batched"] = bench_batched(ctx, stream, args)
     if rank == 0 and world == 1:
         line["cpu_baseline"] = cpu_baseline(g, u0, budget_s=args.cpu_seconds)
     if rank == 0:
@@ -297,6 +304,65 @@ def bench_burgers(ctx, stream, args):
     del ref
     op.close()
     g.close()
+    return out
+
+
+def bench_batched(ctx, stream, args):
+    """Batched serving: independent 3D linear advection solves, random velocity
+    in [-1,1]^3, 1-4 periodic Gaussian bumps (centres U[0.2,0.8]^3, widths
+    U[0.03,0.15]), adaptive grids up to level 8 (uneven sizes), all advanced by
+    one graph-captured launch per RK stage; per-solve L2 error against the
+    exact translated solution."""
+    import torch
+
+    import amdg
+    import amdg_oracle as O
+    work = O.batched_workload(args.batch_solves, seed=0)
+    t0 = time.perf_counter()
+    grids = []
+    for w in work:
+        g = amdg.Grid(ctx, 3, 8, 2, level_init=2)
+        g.init_separable_adaptive(O.gaussian_bump_terms(w["centers"], w["widths"], w["amplitudes"]), args.batch_eps)
+        grids.append(g)
+    init_s = time.perf_counter() - t0
+    sizes = [g.num_elements for g in grids]
+    dts = []
+    for g, w in zip(grids, work):
+        lv = g.max_mesh_level()
+        dts.append(CFL / sum(abs(v) * 2.0 ** int(m) for v, m in zip(w["velocity"], lv)))
+    out = {"workload": f"{len(work)} independent 3D linear advection solves, adaptive N<=8, k=2, seed 0",
+           "solves": len(work), "elements_min": min(sizes), "elements_max": max(sizes),
+           "elements_total": sum(sizes), "init_s": init_s, "eps": args.batch_eps}
+    for name, prec in (("fp64", amdg.FP64), ("mixed", amdg.MIXED)):
+        batch = amdg.Batch(ctx, grids, [w["velocity"] for w in work])
+        batch.set_dt(dts)
+        batch.rk3_steps(args.warmup, prec, use_graph=True)
+        torch.cuda.synchronize()
+        s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        s.record(stream)
+        batch.rk3_steps(args.steps, prec, use_graph=True)
+        e.record(stream)
+        torch.cuda.synchronize()
+        sec = s.elapsed_time(e) / 1e3
+        out[name] = {"value": 3.0 * batch.dof * args.steps / sec, "ms_per_step": sec / args.steps * 1e3,
+                     "dof": batch.dof, "launches_per_step": 3}
+        errs = []
+        nsteps = args.warmup + args.steps
+        for i in range(0, len(work), max(1, len(work) // 16)):
+            w = work[i]
+            batch.store(i)
+            shift = [v * dts[i] * nsteps for v in w["velocity"]]
+            exact = O.gaussian_bump_terms(w["centers"], w["widths"], w["amplitudes"], shift=shift)
+            norm = O.gaussian_bump_norm(w["centers"], w["widths"], w["amplitudes"])
+            errs.append(grids[i].l2_error_separable_sum(exact, norm) / norm)
+        out[name]["rel_l2_error_sampled"] = {"median": float(np.median(errs)), "max": float(np.max(errs)),
+                                             "solves_sampled": len(errs)}
+        batch.close()
+        # restore the initial coefficients for the next precision
+        for g, w in zip(grids, work):
+            g.init_separable(O.gaussian_bump_terms(w["centers"], w["widths"], w["amplitudes"]))
+    for g in grids:
+        g.close()
     return out
 
 
@@ -368,6 +434,8 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
+    ap.add_argument("--batch-solves", type=int, default=256)
+    ap.add_argument("--batch-eps", type=float, default=1e-5)
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)

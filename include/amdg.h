@@ -55,6 +55,8 @@ typedef struct amdg_context amdg_context;
 typedef struct amdg_grid amdg_grid;
 typedef struct amdg_linear_op amdg_linear_op;
 typedef struct amdg_burgers_op amdg_burgers_op;
+typedef struct amdg_batch amdg_batch;
+typedef struct amdg_mlp amdg_mlp;
 
 /* Separable 1D factor g_d(x) of term `term` (the std::function<double(double,int)>
  * the reference takes, DGAdapt.h:17-38). */
@@ -141,6 +143,11 @@ amdg_status amdg_grid_l2_norm(const amdg_grid* g, double* out);
 amdg_status amdg_grid_l2_error_separable(const amdg_grid* g, amdg_fn1d f, void* user, double l2_norm_exact,
                                          double* out);
 
+/* Same for an exact solution given as a sum of nterms separable terms
+ * (|u - u_h|^2 = |u|^2 + sum u_h^2 - 2 sum_terms <u_h, term>). */
+amdg_status amdg_grid_l2_error_separable_sum(const amdg_grid* g, int nterms, amdg_fn1d f, void* user,
+                                             double l2_norm_exact, double* out);
+
 /* ---- linear constant-coefficient operator (HyperbolicAlpt) -------------- */
 /* HyperbolicAlpt::assemble_matrix_scalar (BilinearForm.cpp:691-710): volume
  * term c_d * u_vx plus upwind flux c_d * ulft_vjp (c_d >= 0) or c_d * urgt_vjp
@@ -224,6 +231,27 @@ amdg_status amdg_burgers_flux_coefficients(amdg_burgers_op* op, const double* d_
  * stage loop of example/07_vlasov_maxwell_adapt.cpp:278-320). */
 amdg_status amdg_burgers_rk3_steps(amdg_burgers_op* op, double dt, int nsteps, amdg_precision prec);
 
+/* ---- batched independent linear solves ------------------------------------ */
+/* Many independent constant-coefficient solves (one HyperbolicAlpt + RK3SSP
+ * per grid in the reference, run one after the other) advanced together: the
+ * grids' element tables are concatenated and every SSP-RK3 stage of all
+ * solves is one fused launch.  No reference counterpart for the batching
+ * itself.  grids: n grids sharing dim, nmax and k (their current
+ * coefficients are copied in); coef: n x dim velocities.  The batch does not
+ * follow later changes of the grids' element sets. */
+amdg_status amdg_batch_create(amdg_context* ctx, int n, amdg_grid* const* grids, const double* coef, amdg_batch** out);
+amdg_status amdg_batch_destroy(amdg_batch* b);
+amdg_status amdg_batch_size(const amdg_batch* b, int64_t* num_elements, int64_t* dof, int64_t* pairs);
+/* Per-solve time step sizes (n doubles). */
+amdg_status amdg_batch_set_dt(amdg_batch* b, const double* dt);
+/* nsteps SSP-RK3 steps of every solve; use_graph != 0 captures one step's
+ * launches into a CUDA graph on first use and replays it. */
+amdg_status amdg_batch_rk3_steps(amdg_batch* b, int nsteps, amdg_precision prec, int use_graph);
+/* Copy solve `solve`'s coefficients back into its grid (for norms, errors, IO). */
+amdg_status amdg_batch_store(amdg_batch* b, int solve);
+/* Device pointer of the concatenated state and the element offsets (n+1 entries, may be NULL). */
+amdg_status amdg_batch_coefficients_device(amdg_batch* b, double** device_ptr, int64_t* elem_offsets);
+
 /* One adaptive time step of the Burgers solver, the loop body of
  * example/02_hyperbolic_05_burgers_adapt.cpp:223-476 with the Lagrange
  * right-hand side: dt = cfl / sum_d wave_speed 2^maxlevel_d, forward-Euler
@@ -231,6 +259,46 @@ amdg_status amdg_burgers_rk3_steps(amdg_burgers_op* op, double dt, int nsteps, a
  * amdg_grid_coarsen (eta).  dt_out may be NULL. */
 amdg_status amdg_burgers_adaptive_step(amdg_burgers_op* op, double cfl, double wave_speed, double eps, double eta,
                                        amdg_precision prec, double* dt_out);
+/* Same, and records what the surplus criterion decided for every element of
+ * the grid at the start of the step: decisions[e] = 1 refined, 2 coarsened
+ * away, 0 kept (host buffer of num_elements entries, may be NULL).  These are
+ * the labels the learned classifier is trained on. */
+amdg_status amdg_burgers_adaptive_step_ex(amdg_burgers_op* op, double cfl, double wave_speed, double eps, double eta,
+                                          amdg_precision prec, double* dt_out, int8_t* decisions);
+
+/* ---- learned refine/coarsen (no reference counterpart) -------------------- */
+/* Per-element classifier refine / keep / coarsen: n_in -> n_hidden_layers x
+ * hidden (ReLU) -> n_out (softmax), FP32, He-initialised from seed.  Judged
+ * against DGAdapt::refine / coarsen (DGAdapt.cpp:371-404, 675-688). */
+amdg_status amdg_mlp_create(amdg_context* ctx, int n_in, int hidden, int n_hidden_layers, int n_out, uint64_t seed,
+                            amdg_mlp** out);
+amdg_status amdg_mlp_destroy(amdg_mlp* m);
+/* Flat parameters: per layer W[out][in] row-major, then b[out]. */
+amdg_status amdg_mlp_num_params(const amdg_mlp* m, int64_t* n);
+amdg_status amdg_mlp_get_params(const amdg_mlp* m, float* host, int64_t n);
+amdg_status amdg_mlp_set_params(amdg_mlp* m, const float* host, int64_t n);
+/* Class probabilities of n samples (device arrays n x n_in -> n x n_out). */
+amdg_status amdg_mlp_predict(amdg_mlp* m, const float* d_x, int64_t n, float* d_probs);
+/* Mean cross entropy of n labelled samples and its gradient (host, num_params floats; may be NULL). */
+amdg_status amdg_mlp_loss_grad(amdg_mlp* m, const float* d_x, const int32_t* d_labels, int64_t n, double* loss,
+                               float* host_grad);
+/* Adam (0.9, 0.999, 1e-8) on minibatches of a seeded shuffle; mean loss of the last epoch in final_loss. */
+amdg_status amdg_mlp_train(amdg_mlp* m, const float* d_x, const int32_t* d_labels, int64_t n, int epochs, int batch,
+                           float lr, uint64_t seed, double* final_loss);
+/* Classifier inputs of every element: |coefficients| of the element and of its
+ * parent and grandparent in each dimension, log-scaled (log10(|c| + 1e-20)/20 + 1),
+ * (k+1)^dim * (1 + 2 dim) floats per element (device). */
+amdg_status amdg_burgers_features(amdg_burgers_op* op, const double* d_u, float* d_features);
+/* Adaptive step with learned pre-adaptation: the classifier decides which
+ * leaves to refine before the step (no forward-Euler predictor); on elements
+ * whose largest class probability is below tau the surplus criterion on the
+ * current coefficients decides; after the SSP-RK3 step the surplus criterion
+ * refines the leaves it still finds above eps (missed refinements), then
+ * coarsens as amdg_grid_coarsen.  stats (may be NULL): [refined by the
+ * network, uncertain, missed refinements, elements after the step]. */
+amdg_status amdg_burgers_adaptive_step_learned(amdg_burgers_op* op, amdg_mlp* mlp, double cfl, double wave_speed,
+                                               double eps, double eta, double tau, amdg_precision prec, double* dt_out,
+                                               int64_t* stats);
 
 #ifdef __cplusplus
 }

@@ -413,3 +413,102 @@ def burgers_adaptive_run(dim, n_init, nmax, eps, eta, alpha, cfl, umax, steps, k
         keys = new_keys
         history.append((list(keys), u.copy(), dt))
     return history
+
+
+# ---------------------------------------------------------------------------
+# Batched-serving workload: sums of periodic Gaussian bumps (separable terms)
+# ---------------------------------------------------------------------------
+
+def gaussian_bump_terms(centers, widths, amplitudes, shift=None):
+    """Separable terms of sum_g a_g prod_d G(x_d; c_gd, w_g), G(x) = sum_{m=-1,0,1} exp(-((x - c + m)/w)^2);
+    shift (dim,) translates every centre (periodic)."""
+    terms = []
+    dim = len(centers[0])
+    for c, w, a in zip(centers, widths, amplitudes):
+        cc = [(c[d] + (shift[d] if shift is not None else 0.0)) % 1.0 for d in range(dim)]
+
+        def f(x, d, cc=cc, w=w, a=a):
+            v = sum(math.exp(-((x - cc[d] + m) / w) ** 2) for m in (-1.0, 0.0, 1.0))
+            return a * v if d == 0 else v
+
+        terms.append(f)
+    return terms
+
+
+def gaussian_bump_norm(centers, widths, amplitudes, n=4000):
+    """Exact L2 norm over [0,1]^dim of the bump sum (1D integrals by the midpoint rule on n cells)."""
+    x = (np.arange(n) + 0.5) / n
+    dim = len(centers[0])
+
+    def g1(c, w):
+        return sum(np.exp(-((x - c + m) / w) ** 2) for m in (-1.0, 0.0, 1.0))
+
+    tot = 0.0
+    for i in range(len(centers)):
+        for j in range(len(centers)):
+            p = amplitudes[i] * amplitudes[j]
+            for d in range(dim):
+                p *= float(np.mean(g1(centers[i][d], widths[i]) * g1(centers[j][d], widths[j])))
+            tot += p
+    return math.sqrt(tot)
+
+
+def batched_workload(nsolves, seed=0, dim=3):
+    """Seeded config: velocity U[-1,1]^dim, 1..4 bumps, centres U[0.2,0.8]^dim, widths U[0.03,0.15]."""
+    rng = np.random.default_rng(seed)
+    out = []
+    for _ in range(nsolves):
+        vel = rng.uniform(-1.0, 1.0, dim)
+        nb = int(rng.integers(1, 5))
+        centers = rng.uniform(0.2, 0.8, (nb, dim)).tolist()
+        widths = rng.uniform(0.03, 0.15, nb).tolist()
+        out.append(dict(velocity=vel.tolist(), centers=centers, widths=widths, amplitudes=[1.0] * nb))
+    return out
+
+
+# ---------------------------------------------------------------------------
+# CPU reference of the refine/keep/coarsen classifier (float64): forward pass,
+# analytic backward pass, and finite differences, for checking the device
+# kernels' gradients.  Parameter layout: per layer W[out][in] then b[out].
+# ---------------------------------------------------------------------------
+
+def mlp_unpack(params, dims):
+    out, off = [], 0
+    for i in range(len(dims) - 1):
+        n_in, n_out = dims[i], dims[i + 1]
+        W = np.asarray(params[off:off + n_in * n_out], np.float64).reshape(n_out, n_in)
+        off += n_in * n_out
+        b = np.asarray(params[off:off + n_out], np.float64)
+        off += n_out
+        out.append((W, b))
+    return out
+
+
+def mlp_loss_grad(params, dims, x, labels):
+    layers = mlp_unpack(params, dims)
+    acts = [np.asarray(x, np.float64)]
+    for i, (W, b) in enumerate(layers):
+        z = acts[-1] @ W.T + b
+        acts.append(np.maximum(z, 0.0) if i + 1 < len(layers) else z)
+    z = acts[-1]
+    z = z - z.max(axis=1, keepdims=True)
+    p = np.exp(z) / np.exp(z).sum(axis=1, keepdims=True)
+    n = x.shape[0]
+    loss = float(-np.mean(np.log(p[np.arange(n), labels])))
+    delta = p.copy()
+    delta[np.arange(n), labels] -= 1.0
+    delta /= n
+    grads = []
+    for i in range(len(layers) - 1, -1, -1):
+        W, _b = layers[i]
+        xin = acts[i]
+        grads.append((delta.T @ xin, delta.sum(axis=0)))
+        if i > 0:
+            delta = (delta @ W) * (xin > 0)
+    grads.reverse()
+    flat = np.concatenate([np.concatenate([gW.ravel(), gb]) for gW, gb in grads])
+    return loss, flat
+
+
+def mlp_loss(params, dims, x, labels):
+    return mlp_loss_grad(params, dims, x, labels)[0]

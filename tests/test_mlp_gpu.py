@@ -1,0 +1,133 @@
+"""The learned refine/coarsen classifier: device forward/backward kernels
+against the float64 CPU reference (tolerance 2e-4 relative to the gradient's
+max, FP32 kernels), Adam training on the device, and what the trained network
+gains inside the adaptive Burgers loop over the surplus criterion alone."""
+import time
+
+import numpy as np
+import pytest
+
+import amdg
+import amdg_oracle as O
+
+pytestmark = pytest.mark.gpu
+torch = pytest.importorskip("torch")
+
+
+def test_mlp_gradients_match_cpu_reference(ctx):
+    dims = [45, 64, 64, 64, 3]  # 2D features: 9 coefficients x (1 + 2 x 2) blocks
+    mlp = amdg.MLP(ctx, 45, 64, 3, 3, seed=5)
+    rng = np.random.default_rng(1)
+    n = 257
+    x = rng.uniform(0.0, 1.0, (n, 45)).astype(np.float32)
+    labels = rng.integers(0, 3, n).astype(np.int32)
+    dx = torch.from_numpy(x).cuda()
+    dl = torch.from_numpy(labels).cuda()
+    torch.cuda.synchronize()
+    loss, g = mlp.loss_grad_device(dx.data_ptr(), dl.data_ptr(), n)
+    ref_loss, ref_g = O.mlp_loss_grad(mlp.params().astype(np.float64), dims, x.astype(np.float64), labels)
+    assert abs(loss - ref_loss) <= 1e-5 * abs(ref_loss)
+    assert np.abs(g - ref_g).max() <= 2e-4 * np.abs(ref_g).max()
+    # probabilities of the forward pass
+    probs = torch.zeros(n * 3, dtype=torch.float32, device="cuda")
+    mlp.predict_device(dx.data_ptr(), n, probs.data_ptr())
+    ctx.synchronize()
+    p = probs.cpu().numpy().reshape(n, 3)
+    assert np.allclose(p.sum(axis=1), 1.0, atol=1e-5)
+    mlp.close()
+
+
+def test_mlp_training_learns_a_separable_rule(ctx):
+    rng = np.random.default_rng(2)
+    n = 4096
+    x = rng.uniform(0.0, 1.0, (n, 45)).astype(np.float32)
+    labels = np.where(x[:, 0] > 0.66, 0, np.where(x[:, 0] < 0.33, 2, 1)).astype(np.int32)
+    dx = torch.from_numpy(x).cuda()
+    dl = torch.from_numpy(labels).cuda()
+    torch.cuda.synchronize()
+    mlp = amdg.MLP(ctx, 45, 64, 3, 3, seed=3)
+    loss0, _ = mlp.loss_grad_device(dx.data_ptr(), dl.data_ptr(), n)
+    loss = mlp.train_device(dx.data_ptr(), dl.data_ptr(), n, epochs=30, batch=256, lr=3e-3, seed=4)
+    assert loss < 0.25 * loss0
+    probs = torch.zeros(n * 3, dtype=torch.float32, device="cuda")
+    mlp.predict_device(dx.data_ptr(), n, probs.data_ptr())
+    ctx.synchronize()
+    acc = float((probs.cpu().numpy().reshape(n, 3).argmax(axis=1) == labels).mean())
+    assert acc > 0.95
+    mlp.close()
+
+
+def _collect(ctx, dim, nmax, eps, eta, steps, seeds):
+    """Features and surplus-criterion labels from plain adaptive Burgers runs."""
+    feats, labs = [], []
+    for seed in seeds:
+        rng = np.random.default_rng(seed)
+        amp = rng.uniform(0.15, 0.3)
+        terms = [lambda x, d: 0.5 if d == 0 else 1.0]
+        for f in O.sin_sum_terms(dim, shift=rng.uniform(0.0, 1.0)):
+            terms.append(lambda x, d, f=f, a=amp: (a if d == 0 else 1.0) * f(x, d))
+        g = amdg.Grid(ctx, dim, nmax, 2, level_init=3)
+        g.init_separable_adaptive(terms, eps)
+        op = amdg.BurgersOperator(g, 1.1 * 0.8)
+        F = g.block * (1 + 2 * dim)
+        for _ in range(steps):
+            buf = torch.zeros(g.num_elements * F, dtype=torch.float32, device="cuda")
+            torch.cuda.synchronize()
+            op.features_device(g.device_ptr(), buf.data_ptr())
+            ctx.synchronize()
+            f_np = buf.cpu().numpy().reshape(g.num_elements, F)
+            _dt, dec = op.adaptive_step_ex(0.1, 0.8, eps, eta)
+            feats.append(f_np)
+            labs.append(np.where(dec == 1, 0, np.where(dec == 2, 2, 1)).astype(np.int32))
+        op.close()
+        g.close()
+    return np.concatenate(feats), np.concatenate(labs)
+
+
+def test_learned_adaptivity_gains_over_the_plain_criterion(ctx):
+    dim, nmax, eps, eta = 2, 7, 1e-4, 1e-5
+    x, y = _collect(ctx, dim, nmax, eps, eta, steps=6, seeds=range(6))
+    assert (y == 0).sum() > 0, "training data must contain refinements"
+    dx = torch.from_numpy(x).cuda()
+    dy = torch.from_numpy(y).cuda()
+    torch.cuda.synchronize()
+    mlp = amdg.MLP(ctx, x.shape[1], 64, 3, 3, seed=11)
+    mlp.train_device(dx.data_ptr(), dy.data_ptr(), x.shape[0], epochs=40, batch=256, lr=2e-3, seed=12)
+
+    def run(learned):
+        terms = O.burgers_ic_terms(dim)
+        g = amdg.Grid(ctx, dim, nmax, 2, level_init=3)
+        g.init_separable_adaptive(terms, eps)
+        op = amdg.BurgersOperator(g, 1.1 * 0.75)
+        missed = 0
+        ctx.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(10):
+            if learned:
+                _dt, st = op.adaptive_step_learned(mlp, 0.1, 0.75, eps, eta, 0.8)
+                missed += int(st[2])
+            else:
+                op.adaptive_step(0.1, 0.75, eps, eta)
+        ctx.synchronize()
+        sec = time.perf_counter() - t0
+        lv, sp = g.elements()
+        keys = O.arrays_to_keys(lv, sp)
+        u = g.coefficients().copy()
+        op.close()
+        g.close()
+        return sec, keys, u, missed
+
+    t_plain, k_plain, u_plain, _ = run(False)
+    t_learn, k_learn, u_learn, missed = run(True)
+    # the learned path skips the predictor's right-hand side (one of four per step)
+    assert t_learn < t_plain
+    # both runs end on grids whose solutions agree on the common elements
+    common = sorted(set(k_plain) & set(k_learn))
+    pp = {k: i for i, k in enumerate(k_plain)}
+    pl = {k: i for i, k in enumerate(k_learn)}
+    a = np.array([u_plain[pp[k]] for k in common])
+    b = np.array([u_learn[pl[k]] for k in common])
+    assert np.linalg.norm(a - b) <= 1e-3 * np.linalg.norm(a)
+    print(f"plain {t_plain:.3f}s, learned {t_learn:.3f}s, missed refinements {missed}, "
+          f"elements {len(k_plain)} vs {len(k_learn)}")
+    mlp.close()

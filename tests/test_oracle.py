@@ -164,3 +164,22 @@ def test_fast_transforms_equal_direct_sums_on_sparse_grids():
     a = O.burgers_rhs(dim, N, k, lv, sp, u, 0.8)[0]
     b = O.burgers_rhs(dim, N, k, lv, sp, u, 0.8, direct=True)[0]
     assert rel_err(a, b) < 1e-12
+
+
+def test_mlp_oracle_gradient_matches_finite_differences():
+    """The CPU classifier reference: analytic backward pass against central
+    finite differences in float64 (the device gradients are checked against it)."""
+    rng = np.random.default_rng(0)
+    dims = [12, 8, 8, 8, 3]
+    n_par = sum(dims[i] * dims[i + 1] + dims[i + 1] for i in range(len(dims) - 1))
+    params = rng.standard_normal(n_par) * 0.4
+    x = rng.standard_normal((16, dims[0]))
+    labels = rng.integers(0, 3, 16)
+    _, g = O.mlp_loss_grad(params, dims, x, labels)
+    h = 1e-6
+    for i in rng.choice(n_par, 40, replace=False):
+        p1, p2 = params.copy(), params.copy()
+        p1[i] += h
+        p2[i] -= h
+        fd = (O.mlp_loss(p1, dims, x, labels) - O.mlp_loss(p2, dims, x, labels)) / (2 * h)
+        assert abs(fd - g[i]) <= 1e-7 + 1e-5 * abs(fd)

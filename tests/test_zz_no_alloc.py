@@ -19,6 +19,7 @@ import amdg
 pytestmark = pytest.mark.gpu
 
 TOL64 = 1e-12
+TOL_MIXED = 1e-6  # mixed mode: the allocating path keeps its stage vectors as FP32 pairs
 
 
 def _max_rel(a, b):
@@ -42,7 +43,7 @@ def test_noalloc_matches_allocating_steps(prec):
         ctx.synchronize()
         want = g.coefficients()
         got = caller.coefficients()
-        assert _max_rel(got, want) < TOL64, f"call {call}"
+        assert _max_rel(got, want) < (TOL64 if prec == amdg.FP64 else TOL_MIXED), f"call {call}"
     caller.close()
     op.close()
     g.close()
