@@ -4,6 +4,7 @@
 
 #include <cstdint>
 #include <string>
+#include <unordered_map>
 #include <vector>
 
 #include "amdg.h"
@@ -107,6 +108,8 @@ std::vector<uint64_t> refine_keys(const HostGrid& g, const double* norms, double
 void leaf_flags(const HostGrid& g, std::vector<uint8_t>* leaf);
 // [e][d][2]: parent and grandparent in dimension d, -1 when absent
 void parent_table(const HostGrid& g, std::vector<int32_t>* pg);
+// input and output widths of a classifier (capi_mlp.cu)
+void mlp_shape(const amdg_mlp* m, int* n_in, int* n_out);
 std::vector<uint64_t> coarsen_keys(const HostGrid& g, const double* norms, double eta);
 void grid_from_keys(int dim, int nmax, int k, std::vector<uint64_t> keys, HostGrid* g);
 // element norms of the separable expansion sum_t prod_d coef1d[t][d] (host, same arithmetic order as the device init)
@@ -130,6 +133,7 @@ void build_linear_topology(const HostGrid& g, const Oper1D& op, const double* co
 struct TransformTopology {
     std::vector<int32_t> vol_ptr, vol_src, vol_lev;  // ptr: num_elements*dim + 1
     std::vector<int32_t> flx_ptr, flx_src, flx_lev;
+    std::vector<int32_t> vol_nbr, flx_nbr;           // (element, 1D order along t) pairs of the src lists
     std::vector<int32_t> vol_split, flx_split;       // [e*dim+t]: first neighbour finer than e in t
     std::vector<uint8_t> vol_long, flx_long;         // [e*dim+t]: row longer than kLongRowHost
     std::vector<std::vector<int32_t>> vol_long_elems, flx_long_elems;  // [t]: elements with a long row
@@ -199,8 +203,8 @@ struct amdg_burgers_op {
     double *d_a2p = nullptr, *d_lv = nullptr, *d_lvx = nullptr, *d_lflx = nullptr, *d_ajump = nullptr;
     float *f_a2p = nullptr, *f_lv = nullptr, *f_lvx = nullptr, *f_lflx = nullptr, *f_ajump = nullptr;
     // neighbour lists of the fast transforms and the surplus ancestors
-    int32_t *d_vol_ptr = nullptr, *d_vol_src = nullptr, *d_vol_lev = nullptr;
-    int32_t *d_flx_ptr = nullptr, *d_flx_src = nullptr, *d_flx_lev = nullptr;
+    int32_t *d_vol_ptr = nullptr, *d_vol_nbr = nullptr;  // nbr: (element, 1D order along t) pairs
+    int32_t *d_flx_ptr = nullptr, *d_flx_nbr = nullptr;
     int32_t *d_vol_split = nullptr, *d_flx_split = nullptr;
     uint8_t *d_vol_long = nullptr, *d_flx_long = nullptr;
     int32_t *d_vol_long_elems = nullptr, *d_flx_long_elems = nullptr;  // concatenated over t
@@ -214,11 +218,18 @@ struct amdg_burgers_op {
     std::vector<double> host_norms;
     // one SSP-RK3 step captured as a CUDA graph, valid for (grid version, precision, dt)
     int32_t* d_pg = nullptr;         // [e][d][2] parent / grandparent (learned adaptivity features)
+    float *d_feat = nullptr, *d_prob = nullptr;  // classifier features / probabilities
+    int64_t feat_cap = 0;                        // elements the two hold
     void* graph_exec = nullptr;
     int64_t graph_version = -1;
     int graph_prec = -1;
     double graph_dt = 0.0;
     int64_t graph_launches = 0;
+    int64_t last_version = -1;  // configuration of the previous rk3 call
+    int last_prec = -1;
+    double last_dt = 0.0;
+    std::vector<int32_t> anc_order;                   // surplus ancestor 1D orders (depend on nmax only)
+    std::unordered_map<const void*, size_t> dev_cap;  // bytes held by each grow-only device array
 };
 
 namespace amdg {

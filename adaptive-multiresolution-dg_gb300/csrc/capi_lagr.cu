@@ -91,7 +91,7 @@ TransformArgs<T> base_args(const amdg_burgers_op* op, int t, const int* from, co
     a.num_elements = g->host.num_elements;
     a.order = g->d_order;
     a.ptr = flx ? op->d_flx_ptr : op->d_vol_ptr;
-    a.src = flx ? op->d_flx_src : op->d_vol_src;
+    a.nbr = reinterpret_cast<const int2*>(flx ? op->d_flx_nbr : op->d_vol_nbr);
     a.split = flx ? op->d_flx_split : op->d_vol_split;
     a.long_flag = flx ? op->d_flx_long : op->d_vol_long;
     const std::vector<int32_t>& off = flx ? op->flx_long_off : op->vol_long_off;
@@ -254,53 +254,70 @@ amdg_status eval_rhs(amdg_burgers_op* op, const double* u, double* rhs, amdg_pre
 }
 
 
+// Copy a host vector into a grow-only device array of the operator (stream
+// ordered: kernels queued before still see the old contents).
+template <class T>
+amdg_status upload_grow(amdg_burgers_op* op, T** p, const std::vector<T>& host, cudaStream_t st) {
+    size_t& cap = op->dev_cap[static_cast<const void*>(p)];
+    const size_t bytes = host.size() * sizeof(T);
+    if (bytes > cap) {
+        cudaFree(*p);
+        *p = nullptr;
+        cap = 0;
+        const size_t want = bytes + bytes / 4 + 256;
+        cudaError_t e = cudaMalloc(reinterpret_cast<void**>(p), want);
+        if (e != cudaSuccess) return fail(AMDG_ERR_NOMEM, std::string("cudaMalloc: ") + cudaGetErrorString(e));
+        cap = want;
+    }
+    if (bytes) AMDG_CK(cudaMemcpyAsync(*p, host.data(), bytes, cudaMemcpyHostToDevice, st));
+    return AMDG_OK;
+}
+
 // (Re)build the neighbour lists and surplus ancestors for the grid's current
-// element set; work buffers grow with the grid.
+// element set; device arrays and work buffers only grow.
 amdg_status burgers_sync(amdg_burgers_op* op) {
     amdg_grid* g = op->grid;
     if (op->built_version == g->version) return AMDG_OK;
-    Basis1D b{g->host.k, g->host.nmax};
+    cudaStream_t st = stream_of(op);
     LagrTables t;
-    t.anc_order.assign(size_t(op->n1) * 4, -1);
-    // ancestor orders only depend on nmax: recompute them cheaply on the host
-    build_lagr_ancestors(b, &t);
+    if (op->anc_order.empty()) {
+        // ancestor orders only depend on nmax
+        Basis1D b{g->host.k, g->host.nmax};
+        t.anc_order.assign(size_t(op->n1) * 4, -1);
+        build_lagr_ancestors(b, &t);
+        op->anc_order = t.anc_order;
+    } else {
+        t.anc_order = op->anc_order;
+    }
     TransformTopology topo;
     build_transform_topology(g->host, &topo);
     std::vector<int32_t> anc;
     if (!build_surplus_ancestors(g->host, t, &anc)) return fail(AMDG_ERR_STATE, "element set has a hole: a surplus ancestor is missing");
-    int32_t* old[] = {op->d_vol_ptr, op->d_vol_src, op->d_vol_lev, op->d_flx_ptr, op->d_flx_src, op->d_flx_lev, op->d_anc,
-                      op->d_vol_split, op->d_flx_split};
-    for (int32_t* p : old) cudaFree(p);
-    op->d_vol_ptr = op->d_vol_src = op->d_vol_lev = op->d_flx_ptr = op->d_flx_src = op->d_flx_lev = op->d_anc = nullptr;
-    op->d_vol_split = op->d_flx_split = nullptr;
-    cudaFree(op->d_vol_long); cudaFree(op->d_flx_long); cudaFree(op->d_vol_long_elems); cudaFree(op->d_flx_long_elems);
-    op->d_vol_long = op->d_flx_long = nullptr;
-    op->d_vol_long_elems = op->d_flx_long_elems = nullptr;
     std::vector<int32_t> vle, fle;
     op->vol_long_off.assign(1, 0);
     op->flx_long_off.assign(1, 0);
-    for (int t = 0; t < g->host.dim; ++t) {
-        vle.insert(vle.end(), topo.vol_long_elems[t].begin(), topo.vol_long_elems[t].end());
-        fle.insert(fle.end(), topo.flx_long_elems[t].begin(), topo.flx_long_elems[t].end());
+    for (int d = 0; d < g->host.dim; ++d) {
+        vle.insert(vle.end(), topo.vol_long_elems[d].begin(), topo.vol_long_elems[d].end());
+        fle.insert(fle.end(), topo.flx_long_elems[d].begin(), topo.flx_long_elems[d].end());
         op->vol_long_off.push_back(int32_t(vle.size()));
         op->flx_long_off.push_back(int32_t(fle.size()));
     }
+    std::vector<int32_t> pg;
+    parent_table(g->host, &pg);
     amdg_status s;
-    if ((s = upload_vec(&op->d_vol_ptr, topo.vol_ptr)) != AMDG_OK || (s = upload_vec(&op->d_vol_src, topo.vol_src)) != AMDG_OK ||
-        (s = upload_vec(&op->d_vol_lev, topo.vol_lev)) != AMDG_OK || (s = upload_vec(&op->d_flx_ptr, topo.flx_ptr)) != AMDG_OK ||
-        (s = upload_vec(&op->d_flx_src, topo.flx_src)) != AMDG_OK || (s = upload_vec(&op->d_flx_lev, topo.flx_lev)) != AMDG_OK ||
-        (s = upload_vec(&op->d_anc, anc)) != AMDG_OK || (s = upload_vec(&op->d_vol_split, topo.vol_split)) != AMDG_OK ||
-        (s = upload_vec(&op->d_flx_split, topo.flx_split)) != AMDG_OK ||
-        (s = upload_vec(&op->d_vol_long, topo.vol_long)) != AMDG_OK || (s = upload_vec(&op->d_flx_long, topo.flx_long)) != AMDG_OK ||
-        (s = upload_vec(&op->d_vol_long_elems, vle)) != AMDG_OK || (s = upload_vec(&op->d_flx_long_elems, fle)) != AMDG_OK)
+    if ((s = upload_grow(op, &op->d_vol_ptr, topo.vol_ptr, st)) != AMDG_OK ||
+        (s = upload_grow(op, &op->d_vol_nbr, topo.vol_nbr, st)) != AMDG_OK ||
+        (s = upload_grow(op, &op->d_flx_ptr, topo.flx_ptr, st)) != AMDG_OK ||
+        (s = upload_grow(op, &op->d_flx_nbr, topo.flx_nbr, st)) != AMDG_OK ||
+        (s = upload_grow(op, &op->d_anc, anc, st)) != AMDG_OK ||
+        (s = upload_grow(op, &op->d_vol_split, topo.vol_split, st)) != AMDG_OK ||
+        (s = upload_grow(op, &op->d_flx_split, topo.flx_split, st)) != AMDG_OK ||
+        (s = upload_grow(op, &op->d_vol_long, topo.vol_long, st)) != AMDG_OK ||
+        (s = upload_grow(op, &op->d_flx_long, topo.flx_long, st)) != AMDG_OK ||
+        (s = upload_grow(op, &op->d_vol_long_elems, vle, st)) != AMDG_OK ||
+        (s = upload_grow(op, &op->d_flx_long_elems, fle, st)) != AMDG_OK ||
+        (s = upload_grow(op, &op->d_pg, pg, st)) != AMDG_OK)
         return s;
-    {
-        std::vector<int32_t> pg;
-        parent_table(g->host, &pg);
-        cudaFree(op->d_pg);
-        op->d_pg = nullptr;
-        if ((s = upload_vec(&op->d_pg, pg)) != AMDG_OK) return s;
-    }
     const int64_t E = g->host.num_elements;
     if (E > op->capacity) {
         const int64_t cap = E + E / 2 + 16;
@@ -317,6 +334,8 @@ amdg_status burgers_sync(amdg_burgers_op* op) {
             return s;
         op->capacity = cap;
     }
+    // the host vectors above are released on return: wait for their copies
+    AMDG_CK(cudaStreamSynchronize(st));
     op->built_version = g->version;
     return AMDG_OK;
 }
@@ -372,10 +391,11 @@ amdg_status amdg_burgers_destroy(amdg_burgers_op* op) {
     cudaSetDevice(op->device);
     if (op->graph_exec) cudaGraphExecDestroy(static_cast<cudaGraphExec_t>(op->graph_exec));
     void* ptrs[] = {op->d_a2p, op->d_lv, op->d_lvx, op->d_lflx, op->d_ajump, op->f_a2p, op->f_lv, op->f_lvx, op->f_lflx,
-                    op->f_ajump, op->d_vol_ptr, op->d_vol_src, op->d_vol_lev, op->d_flx_ptr, op->d_flx_src, op->d_flx_lev,
+                    op->f_ajump, op->d_vol_ptr, op->d_vol_nbr, op->d_flx_ptr, op->d_flx_nbr,
                     op->d_anc, op->d_anc_point, op->d_anc_rank, op->w_up, op->w_fu, op->w_a, op->w_b, op->w_rhs, op->w_u,
                     op->d_u1, op->d_u2, op->d_rhs64, op->d_pred, op->d_vol_split, op->d_flx_split,
-                    op->d_vol_long, op->d_flx_long, op->d_vol_long_elems, op->d_flx_long_elems, op->d_pg};
+                    op->d_vol_long, op->d_flx_long, op->d_vol_long_elems, op->d_flx_long_elems, op->d_pg,
+                    op->d_feat, op->d_prob};
     for (void* p : ptrs) cudaFree(p);
     delete op;
     return AMDG_OK;
@@ -439,34 +459,46 @@ amdg_status amdg_burgers_rk3_steps(amdg_burgers_op* op, double dt, int nsteps, a
     amdg_grid* g = op->grid;
     cudaStream_t st = stream_of(op);
     if (nsteps == 0) return AMDG_OK;
-    // the launch sequence of a step is fixed for a grid, precision and dt:
-    // capture it once as a CUDA graph and replay it
-    if (!op->graph_exec || op->graph_version != g->version || op->graph_prec != int(prec) || op->graph_dt != dt) {
+    const size_t bytes = size_t(g->dof) * sizeof(double);
+    // one step: ucoe is updated in place per stage, ucoe_tn holds u^n (RK3SSP::step_stage)
+    auto step = [&]() -> amdg_status {
+        AMDG_CK(cudaMemcpyAsync(op->d_u1, g->d_u, bytes, cudaMemcpyDeviceToDevice, st));
+        for (int stage = 0; stage < 3; ++stage) {
+            if (amdg_status r = eval_rhs(op, op->d_u1, op->d_rhs64, prec); r != AMDG_OK) return r;
+            AMDG_CK(launch_stage_update(g->d_u, op->d_u1, op->d_rhs64, g->dof, stage_coef(stage, dt), st));
+            g->ctx->launches++;
+        }
+        AMDG_CK(cudaMemcpyAsync(g->d_u, op->d_u1, bytes, cudaMemcpyDeviceToDevice, st));
+        return AMDG_OK;
+    };
+    const bool graph_valid = op->graph_exec && op->graph_version == g->version && op->graph_prec == int(prec) &&
+                             op->graph_dt == dt;
+    // the launch sequence of a step is fixed for a grid, precision and dt: it is
+    // captured as a CUDA graph once it will be replayed (several steps in this
+    // call, or the same configuration as the previous call); a single step on a
+    // grid that keeps changing (the adaptive loop) is launched directly
+    const bool repeat = op->last_version == g->version && op->last_prec == int(prec) && op->last_dt == dt;
+    op->last_version = g->version;
+    op->last_prec = int(prec);
+    op->last_dt = dt;
+    if (!graph_valid && nsteps == 1 && !repeat) return step();
+    if (!graph_valid) {
         if (op->graph_exec) cudaGraphExecDestroy(static_cast<cudaGraphExec_t>(op->graph_exec));
         op->graph_exec = nullptr;
-        const size_t bytes = size_t(g->dof) * sizeof(double);
         const int64_t l0 = g->ctx->launches;
         cudaGraph_t graph = nullptr;
         AMDG_CK(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
-        // ucoe is updated in place per stage, ucoe_tn holds u^n (RK3SSP::step_stage)
-        amdg_status r = AMDG_OK;
-        cudaError_t e = cudaMemcpyAsync(op->d_u1, g->d_u, bytes, cudaMemcpyDeviceToDevice, st);
-        for (int stage = 0; stage < 3 && r == AMDG_OK && e == cudaSuccess; ++stage) {
-            r = eval_rhs(op, op->d_u1, op->d_rhs64, prec);
-            if (r == AMDG_OK) e = launch_stage_update(g->d_u, op->d_u1, op->d_rhs64, g->dof, stage_coef(stage, dt), st);
-            g->ctx->launches++;
-        }
-        if (r == AMDG_OK && e == cudaSuccess) e = cudaMemcpyAsync(g->d_u, op->d_u1, bytes, cudaMemcpyDeviceToDevice, st);
+        const amdg_status r = step();
         cudaError_t ec = cudaStreamEndCapture(st, &graph);
         op->graph_launches = g->ctx->launches - l0;
         g->ctx->launches = l0;
         if (r != AMDG_OK) { if (graph) cudaGraphDestroy(graph); return r; }
-        if (e != cudaSuccess || ec != cudaSuccess) {
+        if (ec != cudaSuccess) {
             if (graph) cudaGraphDestroy(graph);
-            return fail(AMDG_ERR_CUDA, std::string("graph capture: ") + cudaGetErrorString(e != cudaSuccess ? e : ec));
+            return fail(AMDG_ERR_CUDA, std::string("graph capture: ") + cudaGetErrorString(ec));
         }
         cudaGraphExec_t exec = nullptr;
-        e = cudaGraphInstantiate(&exec, graph, 0);
+        cudaError_t e = cudaGraphInstantiate(&exec, graph, 0);
         cudaGraphDestroy(graph);
         if (e != cudaSuccess) return fail(AMDG_ERR_CUDA, std::string("graph instantiate: ") + cudaGetErrorString(e));
         op->graph_exec = exec;
@@ -558,14 +590,30 @@ amdg_status amdg_burgers_adaptive_step_learned(amdg_burgers_op* op, amdg_mlp* ml
     const double dt = adaptive_dt(g, cfl, wave_speed);
     const int64_t E = g->host.num_elements;
     const int F = g->block * (1 + 2 * g->host.dim);
+    int n_in = 0, n_out = 0;
+    mlp_shape(mlp, &n_in, &n_out);
+    AMDG_REQUIRE(n_in == F && n_out == 3, AMDG_ERR_ARG,
+                 "classifier must take " + std::to_string(F) + " features and give 3 classes");
     // 1. the network's refine/keep/coarsen probabilities from the current coefficients
-    float* d_feat = reinterpret_cast<float*>(op->w_a);  // E x F floats fit in the E x 4^dim double work buffer
-    float* d_prob = reinterpret_cast<float*>(op->w_b);
-    if (size_t(F) * sizeof(float) > size_t(op->points) * sizeof(double))
-        return fail(AMDG_ERR_CAPACITY, "feature vector larger than the work buffer");
+    amdg_status s = AMDG_OK;
+    if (E > op->feat_cap) {
+        cudaFree(op->d_feat);
+        cudaFree(op->d_prob);
+        op->d_feat = op->d_prob = nullptr;
+        op->feat_cap = 0;
+        const int64_t cap = E + E / 4;
+        void *pf = nullptr, *pp = nullptr;
+        if ((s = alloc_bytes(&pf, size_t(cap) * F * sizeof(float))) != AMDG_OK) return s;
+        op->d_feat = static_cast<float*>(pf);
+        if ((s = alloc_bytes(&pp, size_t(cap) * 3 * sizeof(float))) != AMDG_OK) return s;
+        op->d_prob = static_cast<float*>(pp);
+        op->feat_cap = cap;
+    }
+    float* d_feat = op->d_feat;
+    float* d_prob = op->d_prob;
     AMDG_CK(launch_element_features(g->d_u, op->d_pg, E, g->host.dim, g->block, d_feat, st));
     g->ctx->launches++;
-    amdg_status s = amdg_mlp_predict(mlp, d_feat, E, d_prob);
+    s = amdg_mlp_predict(mlp, d_feat, E, d_prob);
     if (s != AMDG_OK) return s;
     std::vector<float> prob(size_t(E) * 3);
     AMDG_CK(cudaMemcpyAsync(prob.data(), d_prob, prob.size() * sizeof(float), cudaMemcpyDeviceToHost, st));

@@ -117,6 +117,11 @@ __global__ void gather_rows(const float* __restrict__ x, const int32_t* __restri
 
 }  // namespace
 
+void amdg::mlp_shape(const amdg_mlp* m, int* n_in, int* n_out) {
+    *n_in = m->dims.front();
+    *n_out = m->dims.back();
+}
+
 extern "C" {
 
 amdg_status amdg_mlp_create(amdg_context* ctx, int n_in, int hidden, int n_hidden_layers, int n_out, uint64_t seed,

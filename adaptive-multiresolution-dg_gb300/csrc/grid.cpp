@@ -161,63 +161,112 @@ void build_linear_topology(const HostGrid& g, const Oper1D& op, const double* co
 
 namespace amdg {
 
+// Element indices grouped into fibres along dimension t (equal orders in every
+// other dimension), each fibre in increasing order along t; start holds the
+// fibre boundaries.
+static void fibres_along(const HostGrid& g, int t, std::vector<int32_t>* perm, std::vector<int64_t>* start) {
+    const uint64_t shift = uint64_t(g.nmax) * (g.dim - 1 - t);
+    const uint64_t mask = (g.nmax == 0 ? 0 : ((uint64_t(1) << g.nmax) - 1)) << shift;
+    const int64_t E = g.num_elements;
+    perm->resize(E);
+    for (int64_t e = 0; e < E; ++e) (*perm)[e] = int32_t(e);
+    if (t != g.dim - 1) {  // sorted keys are already grouped along the last dimension
+        std::sort(perm->begin(), perm->end(), [&](int32_t a, int32_t b) {
+            const uint64_t fa = g.key[a] & ~mask, fb = g.key[b] & ~mask;
+            return fa != fb ? fa < fb : (g.key[a] & mask) < (g.key[b] & mask);
+        });
+    }
+    start->clear();
+    for (int64_t i = 0; i < E; ++i)
+        if (i == 0 || (g.key[(*perm)[i]] & ~mask) != (g.key[(*perm)[i - 1]] & ~mask)) start->push_back(i);
+    start->push_back(E);
+}
+
 void build_transform_topology(const HostGrid& g, TransformTopology* out) {
     const int dim = g.dim, nmax = g.nmax, n1 = 1 << nmax;
     const int64_t one = int64_t(1) << nmax;
-    std::vector<std::vector<int>> vol1(n1), flx1(n1);
-    for (int o = 0; o < n1; ++o) {
-        int64_t a, b;
-        support_units(o, nmax, &a, &b);
-        for (int oc = 0; oc < n1; ++oc) {
-            int64_t a2, b2;
-            support_units(oc, nmax, &a2, &b2);
-            if (!((a >= b2) || (b <= a2))) vol1[o].push_back(oc);
-            if (flux_related(a, b, a2, b2, one)) flx1[o].push_back(oc);
-        }
-    }
+    std::vector<int64_t> lo(n1), hi(n1);
+    for (int o = 0; o < n1; ++o) support_units(o, nmax, &lo[o], &hi[o]);
+    auto vol_rel = [&](int o, int oc) { return !((lo[o] >= hi[oc]) || (hi[o] <= lo[oc])); };
+    auto flx_rel = [&](int o, int oc) { return flux_related(lo[o], hi[o], lo[oc], hi[oc], one); };
     const int64_t E = g.num_elements;
+    // neighbours of e in dimension t are the members of e's fibre along t whose
+    // 1D supports intersect (vol) or intersect / touch, periodically (flx)
+    std::vector<std::vector<int32_t>> perm(dim);
+    std::vector<std::vector<int64_t>> start(dim);
+    std::vector<int32_t> vcnt(size_t(E) * dim, 0), fcnt(size_t(E) * dim, 0);
+    for (int t = 0; t < dim; ++t) {
+        fibres_along(g, t, &perm[t], &start[t]);
+        for (size_t f = 0; f + 1 < start[t].size(); ++f)
+            for (int64_t i = start[t][f]; i < start[t][f + 1]; ++i) {
+                const int32_t e = perm[t][i];
+                const int oe = g.order[size_t(e) * dim + t];
+                int32_t nv = 0, nf = 0;
+                for (int64_t j = start[t][f]; j < start[t][f + 1]; ++j) {
+                    const int os = g.order[size_t(perm[t][j]) * dim + t];
+                    nv += vol_rel(oe, os) ? 1 : 0;
+                    nf += flx_rel(oe, os) ? 1 : 0;
+                }
+                vcnt[size_t(e) * dim + t] = nv;
+                fcnt[size_t(e) * dim + t] = nf;
+            }
+    }
     out->vol_ptr.assign(size_t(E) * dim + 1, 0);
     out->flx_ptr.assign(size_t(E) * dim + 1, 0);
+    for (size_t r = 0; r < size_t(E) * dim; ++r) {
+        out->vol_ptr[r + 1] = out->vol_ptr[r] + vcnt[r];
+        out->flx_ptr[r + 1] = out->flx_ptr[r] + fcnt[r];
+    }
+    out->vol_src.assign(out->vol_ptr.back(), 0);
+    out->vol_lev.assign(out->vol_ptr.back(), 0);
+    out->flx_src.assign(out->flx_ptr.back(), 0);
+    out->flx_lev.assign(out->flx_ptr.back(), 0);
+    out->vol_nbr.assign(size_t(2) * out->vol_ptr.back(), 0);
+    out->flx_nbr.assign(size_t(2) * out->flx_ptr.back(), 0);
+    // neighbours are written in increasing 1D order along t, hence increasing level
+    for (int t = 0; t < dim; ++t)
+        for (size_t f = 0; f + 1 < start[t].size(); ++f)
+            for (int64_t i = start[t][f]; i < start[t][f + 1]; ++i) {
+                const int32_t e = perm[t][i];
+                const int oe = g.order[size_t(e) * dim + t];
+                int32_t pv = out->vol_ptr[size_t(e) * dim + t], pf = out->flx_ptr[size_t(e) * dim + t];
+                for (int64_t j = start[t][f]; j < start[t][f + 1]; ++j) {
+                    const int32_t s = perm[t][j];
+                    const int os = g.order[size_t(s) * dim + t];
+                    if (vol_rel(oe, os)) {
+                        out->vol_src[pv] = s;
+                        out->vol_lev[pv] = level_of_order(os);
+                        out->vol_nbr[2 * size_t(pv)] = s;
+                        out->vol_nbr[2 * size_t(pv) + 1] = os;
+                        ++pv;
+                    }
+                    if (flx_rel(oe, os)) {
+                        out->flx_src[pf] = s;
+                        out->flx_lev[pf] = level_of_order(os);
+                        out->flx_nbr[2 * size_t(pf)] = s;
+                        out->flx_nbr[2 * size_t(pf) + 1] = os;
+                        ++pf;
+                    }
+                }
+            }
     out->vol_split.assign(size_t(E) * dim, 0);
     out->flx_split.assign(size_t(E) * dim, 0);
     out->vol_long.assign(size_t(E) * dim, 0);
     out->flx_long.assign(size_t(E) * dim, 0);
     out->vol_long_elems.assign(dim, {});
     out->flx_long_elems.assign(dim, {});
-    out->vol_src.clear(); out->vol_lev.clear(); out->flx_src.clear(); out->flx_lev.clear();
-    std::vector<int32_t> o2(dim);
     for (int64_t e = 0; e < E; ++e) {
-        const int32_t* oe = &g.order[size_t(e) * dim];
         for (int t = 0; t < dim; ++t) {
-            std::copy(oe, oe + dim, o2.begin());
-            for (int oc : vol1[oe[t]]) {
-                o2[t] = oc;
-                const int64_t s = find_element(g, o2.data());
-                if (s < 0) continue;
-                out->vol_src.push_back(int32_t(s));
-                out->vol_lev.push_back(level_of_order(oc));
-            }
-            for (int oc : flx1[oe[t]]) {
-                o2[t] = oc;
-                const int64_t s = find_element(g, o2.data());
-                if (s < 0) continue;
-                out->flx_src.push_back(int32_t(s));
-                out->flx_lev.push_back(level_of_order(oc));
-            }
-            out->vol_ptr[size_t(e) * dim + t + 1] = int32_t(out->vol_src.size());
-            out->flx_ptr[size_t(e) * dim + t + 1] = int32_t(out->flx_src.size());
-            // neighbours are listed in increasing 1D order, hence increasing level:
+            const size_t r = size_t(e) * dim + t;
             // the "U" part (level <= own) is a prefix, the "L" part (finer) the rest
-            const int own = level_of_order(oe[t]);
-            int32_t sv = out->vol_ptr[size_t(e) * dim + t], sf = out->flx_ptr[size_t(e) * dim + t];
-            while (sv < int32_t(out->vol_src.size()) && out->vol_lev[sv] <= own) ++sv;
-            while (sf < int32_t(out->flx_src.size()) && out->flx_lev[sf] <= own) ++sf;
-            out->vol_split[size_t(e) * dim + t] = sv;
-            out->flx_split[size_t(e) * dim + t] = sf;
-            const int vlen = out->vol_ptr[size_t(e) * dim + t + 1] - out->vol_ptr[size_t(e) * dim + t];
-            const int flen = out->flx_ptr[size_t(e) * dim + t + 1] - out->flx_ptr[size_t(e) * dim + t];
-            if (vlen > kLongRowHost) { out->vol_long[size_t(e) * dim + t] = 1; out->vol_long_elems[t].push_back(int32_t(e)); }
-            if (flen > kLongRowHost) { out->flx_long[size_t(e) * dim + t] = 1; out->flx_long_elems[t].push_back(int32_t(e)); }
+            const int own = level_of_order(g.order[r]);
+            int32_t sv = out->vol_ptr[r], sf = out->flx_ptr[r];
+            while (sv < out->vol_ptr[r + 1] && out->vol_lev[sv] <= own) ++sv;
+            while (sf < out->flx_ptr[r + 1] && out->flx_lev[sf] <= own) ++sf;
+            out->vol_split[r] = sv;
+            out->flx_split[r] = sf;
+            if (vcnt[r] > kLongRowHost) { out->vol_long[r] = 1; out->vol_long_elems[t].push_back(int32_t(e)); }
+            if (fcnt[r] > kLongRowHost) { out->flx_long[r] = 1; out->flx_long_elems[t].push_back(int32_t(e)); }
         }
     }
 }

@@ -19,6 +19,25 @@
 
 namespace amdg {
 
+// acc + sum over four neighbours j (in order) and k < NF of x[j][k*stride] * m[j][k*ncols],
+// all operands loaded before the first multiply-add
+template <int NF, typename T>
+__device__ __forceinline__ T fibre_quad(const T* const* x, const T* const* m, int stride, int ncols, T acc) {
+    T xv[4][NF], mv[4][NF];
+#pragma unroll
+    for (int j = 0; j < 4; ++j)
+#pragma unroll
+        for (int k = 0; k < NF; ++k) {
+            xv[j][k] = __ldg(x[j] + k * stride);
+            mv[j][k] = __ldg(m[j] + size_t(k) * ncols);
+        }
+#pragma unroll
+    for (int j = 0; j < 4; ++j)
+#pragma unroll
+        for (int k = 0; k < NF; ++k) acc = fma(xv[j][k], mv[j][k], acc);
+    return acc;
+}
+
 template <typename T>
 __global__ void __launch_bounds__(256) fibre_transform_kernel(TransformArgs<T> a) {
     const int64_t gid = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
@@ -37,12 +56,34 @@ __global__ void __launch_bounds__(256) fibre_transform_kernel(TransformArgs<T> a
     const int end = a.lu == 2 ? __ldg(a.split + et) : __ldg(a.ptr + et + 1);
     const T* mcol = a.M + size_t(oe) * a.n_to + qt;
     const int in_off = outer * a.n_from * a.stride + inner;
+    const size_t mstep = size_t(a.n_from) * a.ncols;
     T acc = T(0);
-    for (int i = beg; i < end; ++i) {
-        const int s = __ldg(a.src + i);
-        const int os = __ldg(a.order + int64_t(s) * a.dim + a.t);
-        const T* x = a.in + int64_t(s) * a.in_block + in_off;
-        const T* m = mcol + size_t(os) * a.n_from * a.ncols;
+    // four neighbours per pass: their (element, order) pairs and operands are
+    // independent loads issued together; the sum keeps the neighbour order
+    int i = beg;
+    for (; i + 4 <= end; i += 4) {
+        int2 nb[4];
+#pragma unroll
+        for (int j = 0; j < 4; ++j) nb[j] = __ldg(a.nbr + i + j);
+        const T* x[4];
+        const T* m[4];
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+            x[j] = a.in + int64_t(nb[j].x) * a.in_block + in_off;
+            m[j] = mcol + size_t(nb[j].y) * mstep;
+        }
+        if (a.n_from == 4) acc = fibre_quad<4>(x, m, a.stride, a.ncols, acc);
+        else if (a.n_from == 3) acc = fibre_quad<3>(x, m, a.stride, a.ncols, acc);
+        else {
+#pragma unroll
+            for (int j = 0; j < 4; ++j)
+                for (int k = 0; k < a.n_from; ++k) acc = fma(__ldg(x[j] + k * a.stride), __ldg(m[j] + size_t(k) * a.ncols), acc);
+        }
+    }
+    for (; i < end; ++i) {
+        const int2 nb = __ldg(a.nbr + i);
+        const T* x = a.in + int64_t(nb.x) * a.in_block + in_off;
+        const T* m = mcol + size_t(nb.y) * mstep;
         for (int k = 0; k < a.n_from; ++k) acc = fma(__ldg(x + k * a.stride), __ldg(m + size_t(k) * a.ncols), acc);
     }
     acc *= a.coef;
@@ -72,10 +113,9 @@ __global__ void __launch_bounds__(256) fibre_transform_long_kernel(TransformArgs
     const int in_off = outer * a.n_from * a.stride + inner;
     T acc = T(0);
     for (int i = beg + lane; i < end; i += 32) {
-        const int s = __ldg(a.src + i);
-        const int os = __ldg(a.order + int64_t(s) * a.dim + a.t);
-        const T* x = a.in + int64_t(s) * a.in_block + in_off;
-        const T* m = mcol + size_t(os) * a.n_from * a.ncols;
+        const int2 nb = __ldg(a.nbr + i);
+        const T* x = a.in + int64_t(nb.x) * a.in_block + in_off;
+        const T* m = mcol + size_t(nb.y) * a.n_from * a.ncols;
         for (int k = 0; k < a.n_from; ++k) acc = fma(__ldg(x + k * a.stride), __ldg(m + size_t(k) * a.ncols), acc);
     }
 #pragma unroll

@@ -20,7 +20,7 @@ struct TransformArgs {
     int64_t num_elements;
     const T* M;              // [1D elements * n_from][ncols]
     const int32_t* ptr;      // CSR over (element, dimension)
-    const int32_t* src;
+    const int2* nbr;         // (element, 1D order along t) per neighbour
     const int32_t* split;    // [e*dim+t]: first neighbour finer than e in dimension t
     const int32_t* order;    // [element][dim] 1D orders
     const T* in;

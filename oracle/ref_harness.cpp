@@ -20,7 +20,9 @@
 //     interface terms, HyperbolicAlptRHS::rhs_flx_penalty_scalar(alpha), RK3SSP
 //     step_stage, sparse grid without adaptivity (07_vlasov_maxwell_adapt.cpp
 //     stage loop).  Dumps u0, up0 (point values), fu0_d (interpolation
-//     coefficients of the flux in dimension d), rhs0 and uT.
+//     coefficients of the flux in dimension d), rhs0 and uT; then DGSolution::val
+//     and the exact solution at 48 fixed points ("vals") and the L1/L2/Linf errors
+//     of get_error_no_separable_scalar with 1 and 2 Gauss points ("NORMERR").
 //   ref_harness burgers_adapt <dim> <N_init> <NMAX> <eps> <eta> <alpha> <cfl> <umax> <steps>
 //     adaptive version of the above, following the time loop of
 //     example/02_hyperbolic_05_burgers_adapt.cpp:223-476 with the Lagrange
@@ -41,6 +43,7 @@
 #include "DGAdapt.h"
 #include "DGSolution.h"
 #include "Element.h"
+#include "ExactSolution.h"
 #include "FastMultiplyLU.h"
 #include "Hash.h"
 #include "HermBasis.h"
@@ -316,6 +319,33 @@ int run_burgers(int argc, char** argv) {
     dump_elements("uT", dg, 0);
     std::printf("TIME evolve_s=%.9g dof_stage=%.17g\n", std::chrono::duration<double>(t1 - t0).count(),
                 3.0 * steps * dg.get_dof());
+    // exact solution u(x, T) = exact_1d(sum_d x_d, dim T) of BurgersExact(0.5, 0.25, 0)
+    // (ExactSolution.h:13-19: a + b v(X - a T' + c, b T') with X = sum x_d, T' = dim T)
+    BurgersExact burgers(0.5, 0.25, 0.0);
+    const double T = steps * dt;
+    auto exact = [&](std::vector<double> x) -> double {
+        double s = 0.0;
+        for (int d = 0; d < dim; ++d) s += x[d];
+        return burgers.exact_1d(s, dim * T);
+    };
+    // DGSolution::val and the exact solution at fixed quasi-random points
+    const int npts = 48;
+    std::printf("BEGIN vals %d %d\n", npts, dim + 2);
+    for (int i = 0; i < npts; ++i) {
+        std::vector<double> x(dim);
+        for (int d = 0; d < dim; ++d) {
+            const double a = 0.7548776662466927 * (d + 1) + 0.5698402909980532 * d * d;
+            x[d] = std::fmod(0.5 + a * (i + 1), 1.0);
+        }
+        for (int d = 0; d < dim; ++d) std::printf("%.17g ", x[d]);
+        std::printf("%.17g %.17g\n", dg.val(x, std::vector<int>(dim, 0))[0], exact(x));
+    }
+    std::printf("END\n");
+    // DGSolution::get_error_no_separable_scalar (DGSolution.cpp:326-335) with 1 and 2 Gauss points
+    for (int gp = 1; gp <= 2; ++gp) {
+        std::vector<double> err = dg.get_error_no_separable_scalar(exact, gp);
+        std::printf("NORMERR %d %.17g %.17g %.17g\n", gp, err[0], err[1], err[2]);
+    }
     return 0;
 }
 

@@ -37,6 +37,9 @@ def parse_harness(text: str) -> dict:
             for kv in ln.split()[1:]:
                 k, v = kv.split("=")
                 out["meta"][k] = int(v)
+        elif ln.startswith("NORMERR"):
+            f = ln.split()
+            out.setdefault("normerr", {})[int(f[1])] = [float(v) for v in f[2:5]]
         elif ln.startswith("L2ERR"):
             out["l2err"] = float(ln.split()[1])
         elif ln.startswith("TIME"):
@@ -109,6 +112,9 @@ def main():
             lv2, sp2, v = split_elements(r[key], dim)
             assert (lv == lv2).all() and (sp == sp2).all()
             arrs[key] = v
+        arrs["vals"] = r["vals"]
+        for gp, err in r["normerr"].items():
+            arrs[f"normerr_g{gp}"] = np.array(err)
         np.savez_compressed(os.path.join(HERE, name + ".npz"), **arrs)
         manifest[name] = dict(kind="burgers", dim=dim, N=N, k=2, alpha=alpha, steps=steps, dt=dt,
                               elements=int(r["meta"]["elements"]))
