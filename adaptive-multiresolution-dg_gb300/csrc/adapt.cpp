@@ -37,17 +37,46 @@ int children_1d(int o, int nmax, int* out) {
     return 2;
 }
 
-void fill_holes(std::unordered_set<uint64_t>* set, std::vector<uint64_t> work, int dim, int nmax) {
-    while (!work.empty()) {
-        std::vector<uint64_t> next;
-        for (uint64_t key : work)
-            for (int d = 0; d < dim; ++d) {
-                const int o = field(key, d, dim, nmax);
-                if (o == 0) continue;
-                const uint64_t p = with_field(key, d, dim, nmax, o == 1 ? 0 : o / 2);
-                if (set->insert(p).second) next.push_back(p);
+// Growable open-addressing set of keys (keys never have all bits set: they
+// use at most 60 bits).
+class KeySet {
+public:
+    bool insert(uint64_t k) {
+        if (2 * (n_ + 1) > slot_.size()) grow();
+        const uint64_t mask = slot_.size() - 1;
+        for (uint64_t h = hash(k, mask); ; h = (h + 1) & mask) {
+            if (slot_[h] == kEmpty) {
+                slot_[h] = k;
+                ++n_;
+                return true;
             }
-        work.swap(next);
+            if (slot_[h] == k) return false;
+        }
+    }
+private:
+    static constexpr uint64_t kEmpty = ~uint64_t(0);
+    static uint64_t hash(uint64_t k, uint64_t mask) { return (k * 0x9E3779B97F4A7C15ull >> 17) & mask; }
+    void grow() {
+        std::vector<uint64_t> old;
+        old.swap(slot_);
+        slot_.assign(std::max<size_t>(64, old.size() * 2), kEmpty);
+        n_ = 0;
+        for (uint64_t k : old)
+            if (k != kEmpty) insert(k);
+    }
+    std::vector<uint64_t> slot_;
+    size_t n_ = 0;
+};
+
+// existing children of element e and the number it can have
+void child_counts(const HostGrid& g, int64_t e, int* existing, int* total) {
+    const int dim = g.dim, nmax = g.nmax;
+    int ch[2];
+    *existing = *total = 0;
+    for (int d = 0; d < dim; ++d) {
+        const int nc = children_1d(field(g.key[e], d, dim, nmax), nmax, ch);
+        *total += nc;
+        for (int c = 0; c < nc; ++c) *existing += g.index_of(with_field(g.key[e], d, dim, nmax, ch[c])) >= 0 ? 1 : 0;
     }
 }
 
@@ -56,33 +85,47 @@ void fill_holes(std::unordered_set<uint64_t>* set, std::vector<uint64_t> work, i
 std::vector<uint64_t> refine_keys(const HostGrid& g, const double* norms, double eps, std::vector<uint8_t>* refined,
                                   const uint8_t* force) {
     const int dim = g.dim, nmax = g.nmax;
-    std::unordered_set<uint64_t> present(g.key.begin(), g.key.end());
-    std::unordered_set<uint64_t> out(present);
-    std::vector<uint64_t> added;
+    KeySet added;  // keys not in g
+    std::vector<uint64_t> work, fresh;
     if (refined) refined->assign(g.num_elements, 0);
     int ch[2];
     for (int64_t e = 0; e < g.num_elements; ++e) {
-        const uint64_t key = g.key[e];
-        int total = 0, existing = 0;
-        for (int d = 0; d < dim; ++d) {
-            const int nc = children_1d(field(key, d, dim, nmax), nmax, ch);
-            total += nc;
-            for (int c = 0; c < nc; ++c) existing += present.count(with_field(key, d, dim, nmax, ch[c])) ? 1 : 0;
-        }
         // a leaf has fewer existing children than possible (DGAdapt::update_leaf)
         const bool want = force ? force[e] != 0 : (norms[e] > eps);
-        if (existing >= total || !want) continue;
+        if (!want) continue;
+        int existing, total;
+        child_counts(g, e, &existing, &total);
+        if (existing >= total) continue;
         if (refined) (*refined)[e] = 1;
+        const uint64_t key = g.key[e];
         for (int d = 0; d < dim; ++d) {
             const int nc = children_1d(field(key, d, dim, nmax), nmax, ch);
             for (int c = 0; c < nc; ++c) {
                 const uint64_t ck = with_field(key, d, dim, nmax, ch[c]);
-                if (out.insert(ck).second) added.push_back(ck);
+                if (g.index_of(ck) < 0 && added.insert(ck)) work.push_back(ck);
             }
         }
     }
-    fill_holes(&out, added, dim, nmax);
-    std::vector<uint64_t> keys(out.begin(), out.end());
+    // hole filling: every parent of a new element must exist (DGAdapt::check_hole)
+    fresh = work;
+    while (!work.empty()) {
+        std::vector<uint64_t> next;
+        for (uint64_t key : work)
+            for (int d = 0; d < dim; ++d) {
+                const int o = field(key, d, dim, nmax);
+                if (o == 0) continue;
+                const uint64_t p = with_field(key, d, dim, nmax, o == 1 ? 0 : o / 2);
+                if (g.index_of(p) < 0 && added.insert(p)) {
+                    next.push_back(p);
+                    fresh.push_back(p);
+                }
+            }
+        work.swap(next);
+    }
+    std::vector<uint64_t> keys;
+    keys.reserve(g.key.size() + fresh.size());
+    keys.insert(keys.end(), g.key.begin(), g.key.end());
+    keys.insert(keys.end(), fresh.begin(), fresh.end());
     std::sort(keys.begin(), keys.end());
     return keys;
 }
@@ -93,17 +136,14 @@ std::vector<uint64_t> coarsen_keys(const HostGrid& g, const double* norms, doubl
     std::vector<char> alive(E, 1);
     // existing-children counts, kept up to date as elements are removed
     std::vector<int> kids(E, 0);
-    auto index_of = [&](uint64_t k) -> int64_t {
-        auto it = std::lower_bound(g.key.begin(), g.key.end(), k);
-        return (it != g.key.end() && *it == k) ? int64_t(it - g.key.begin()) : -1;
-    };
-    std::vector<std::vector<int64_t>> parents(E);
+    std::vector<int64_t> parent(size_t(E) * dim, -1);
     for (int64_t e = 0; e < E; ++e)
         for (int d = 0; d < dim; ++d) {
             const int o = field(g.key[e], d, dim, nmax);
             if (o == 0) continue;
-            const int64_t p = index_of(with_field(g.key[e], d, dim, nmax, o == 1 ? 0 : o / 2));
-            if (p >= 0) { parents[e].push_back(p); ++kids[p]; }
+            const int64_t p = g.index_of(with_field(g.key[e], d, dim, nmax, o == 1 ? 0 : o / 2));
+            parent[size_t(e) * dim + d] = p;
+            if (p >= 0) ++kids[p];
         }
     auto removable = [&](int64_t e) {
         if (!alive[e] || kids[e] != 0 || !(norms[e] < eta)) return false;
@@ -119,8 +159,9 @@ std::vector<uint64_t> coarsen_keys(const HostGrid& g, const double* norms, doubl
         for (int64_t e : work) {
             if (!removable(e)) continue;
             alive[e] = 0;
-            for (int64_t p : parents[e]) {
-                if (--kids[p] == 0 && removable(p)) next.push_back(p);
+            for (int d = 0; d < dim; ++d) {
+                const int64_t p = parent[size_t(e) * dim + d];
+                if (p >= 0 && --kids[p] == 0 && removable(p)) next.push_back(p);
             }
         }
         work.swap(next);
@@ -131,17 +172,10 @@ std::vector<uint64_t> coarsen_keys(const HostGrid& g, const double* norms, doubl
 }
 
 void leaf_flags(const HostGrid& g, std::vector<uint8_t>* leaf) {
-    const int dim = g.dim, nmax = g.nmax;
-    std::unordered_set<uint64_t> present(g.key.begin(), g.key.end());
     leaf->assign(g.num_elements, 0);
-    int ch[2];
     for (int64_t e = 0; e < g.num_elements; ++e) {
-        int total = 0, existing = 0;
-        for (int d = 0; d < dim; ++d) {
-            const int nc = children_1d(field(g.key[e], d, dim, nmax), nmax, ch);
-            total += nc;
-            for (int c = 0; c < nc; ++c) existing += present.count(with_field(g.key[e], d, dim, nmax, ch[c])) ? 1 : 0;
-        }
+        int existing, total;
+        child_counts(g, e, &existing, &total);
         (*leaf)[e] = existing < total ? 1 : 0;
     }
 }
@@ -149,10 +183,6 @@ void leaf_flags(const HostGrid& g, std::vector<uint8_t>* leaf) {
 void parent_table(const HostGrid& g, std::vector<int32_t>* pg) {
     const int dim = g.dim, nmax = g.nmax;
     pg->assign(size_t(g.num_elements) * dim * 2, -1);
-    auto index_of = [&](uint64_t k) -> int64_t {
-        auto it = std::lower_bound(g.key.begin(), g.key.end(), k);
-        return (it != g.key.end() && *it == k) ? int64_t(it - g.key.begin()) : -1;
-    };
     for (int64_t e = 0; e < g.num_elements; ++e)
         for (int d = 0; d < dim; ++d) {
             uint64_t k = g.key[e];
@@ -160,7 +190,7 @@ void parent_table(const HostGrid& g, std::vector<int32_t>* pg) {
                 const int o = field(k, d, dim, nmax);
                 if (o == 0) break;
                 k = with_field(k, d, dim, nmax, o == 1 ? 0 : o / 2);
-                (*pg)[(size_t(e) * dim + d) * 2 + gen] = int32_t(index_of(k));
+                (*pg)[(size_t(e) * dim + d) * 2 + gen] = int32_t(g.index_of(k));
             }
         }
 }
@@ -176,6 +206,7 @@ void grid_from_keys(int dim, int nmax, int k, std::vector<uint64_t> keys, HostGr
     g->order.resize(size_t(g->num_elements) * dim);
     for (int64_t e = 0; e < g->num_elements; ++e)
         for (int d = 0; d < dim; ++d) g->order[size_t(e) * dim + d] = field(g->key[e], d, dim, nmax);
+    build_key_index(g);
 }
 
 void element_separable_norms(const HostGrid& g, const std::vector<double>& coef1d, int nterms, std::vector<double>* norms) {

@@ -13,7 +13,6 @@ namespace amdg {
 
 constexpr double kRoundOff = 1e-13;  // Const::ROUND_OFF (libs.h:28)
 constexpr int kMaxDim = 6;
-constexpr int kLongRowHost = 24;  // neighbour rows longer than this are split across a warp (kLongRow)
 
 // ---- error plumbing ------------------------------------------------------
 void set_error(const std::string& msg);
@@ -56,6 +55,9 @@ struct Oper1D {
 };
 void build_oper1d(const Basis1D& b, Oper1D* out, bool want_u_v);
 
+// n-point Gauss-Legendre nodes and weights on [-1, 1] (n <= 16)
+void gauss_legendre(int n, double* x, double* w);
+
 // 1D projection of f(., d, term) onto every basis function (Basis::product_function).
 void project_1d(const Basis1D& b, amdg_fn1d f, void* user, int d, int term, double* out);
 
@@ -85,7 +87,22 @@ struct HostGrid {
     int64_t num_elements = 0;
     std::vector<int32_t> order;  // num_elements x dim, 1D element orders, sorted lexicographically
     std::vector<uint64_t> key;   // packed orders (nmax bits per dimension), ascending
+    // open-addressing index key -> element (load <= 1/2; built with the element set)
+    std::vector<uint64_t> hkey;
+    std::vector<int32_t> hval;   // -1: empty slot
+    int hbits = 0;
+    int64_t index_of(uint64_t k) const {
+        if (hval.empty()) return -1;
+        const uint64_t mask = (uint64_t(1) << hbits) - 1;
+        for (uint64_t h = (k * 0x9E3779B97F4A7C15ull) >> (64 - hbits);; h = (h + 1) & mask) {
+            const int32_t v = hval[h];
+            if (v < 0) return -1;
+            if (hkey[h] == k) return v;
+        }
+    }
 };
+// (re)build g->hkey / hval / hbits from g->key
+void build_key_index(HostGrid* g);
 void build_grid(int dim, int nmax, int sparse, HostGrid* g, int level_init = -1);
 int64_t find_element(const HostGrid& g, const int32_t* orders);  // binary search, -1 if absent
 
@@ -131,14 +148,28 @@ void build_linear_topology(const HostGrid& g, const Oper1D& op, const double* co
 // (periodic), identical indices elsewhere (Element.cpp:265-299).  Each entry
 // carries the neighbour's level in that dimension for the L/U filters.
 struct TransformTopology {
-    std::vector<int32_t> vol_ptr, vol_src, vol_lev;  // ptr: num_elements*dim + 1
-    std::vector<int32_t> flx_ptr, flx_src, flx_lev;
-    std::vector<int32_t> vol_nbr, flx_nbr;           // (element, 1D order along t) pairs of the src lists
-    std::vector<int32_t> vol_split, flx_split;       // [e*dim+t]: first neighbour finer than e in t
-    std::vector<uint8_t> vol_long, flx_long;         // [e*dim+t]: row longer than kLongRowHost
-    std::vector<std::vector<int32_t>> vol_long_elems, flx_long_elems;  // [t]: elements with a long row
+    std::vector<int32_t> vol_ptr, flx_ptr;       // CSR over (element, dimension): num_elements*dim + 1
+    std::vector<int32_t> vol_nbr, flx_nbr;       // (element, 1D order along t) pairs, increasing order
+    std::vector<int32_t> vol_split, flx_split;   // [e*dim+t]: first neighbour finer than e in t
 };
 void build_transform_topology(const HostGrid& g, TransformTopology* out);
+
+// Matrices of the Lagrange path, indexed by PartialSum::mat.
+enum LagrMat { kMatA2P = 0, kMatLV = 1, kMatLVX = 2, kMatLFLX = 3, kMatAJump = 4, kNumLagrMats = 5 };
+
+// One term of a right-hand side or of the point values: either a partial sum
+// of dim successive 1D transforms (FastRHS::transform_multiD_partial_sum,
+// FastMultiplyLU.cpp:121-213; FastInterpolation, :904-968) -- in sweep j the
+// transform runs along dims[j] with matrix mat[j] over the "vol" or "flx"
+// (flx[j]) neighbour sets restricted by lu[j] (0 "L": finer neighbours, 1
+// all, 2 "U": coarser or equal), the first sweep scaled by coef -- or (kind 1)
+// the single full transform of the LxF penalty along dims[0] with the jump
+// matrix on the flx sets (FastRHS::transform_ucoe_alpt_to_rhs, :46-59).
+struct PartialSum {
+    int8_t dims[kMaxDim], lu[kMaxDim], mat[kMaxDim], flx[kMaxDim];
+    int32_t kind;
+    double coef;
+};
 // surplus ancestors: [e][d][ic] element index (-1 for level 0 in d); false if a hole is found
 bool build_surplus_ancestors(const HostGrid& g, const LagrTables& t, std::vector<int32_t>* anc);
 
@@ -150,7 +181,26 @@ struct amdg_context {
     void* stream = nullptr;        // cudaStream_t in use
     void* own_stream = nullptr;    // stream created by the context
     int64_t launches = 0;
+    // host phase profile (amdg_context_profile): wall seconds and calls per phase
+    bool profile = false;
+    double phase_sec[AMDG_PHASE_COUNT] = {0};
+    int64_t phase_calls[AMDG_PHASE_COUNT] = {0};
 };
+
+namespace amdg {
+// Adds the wall time of its scope to a phase of the context's profile (when enabled).
+class PhaseTimer {
+public:
+    PhaseTimer(amdg_context* ctx, int phase);
+    ~PhaseTimer();
+    PhaseTimer(const PhaseTimer&) = delete;
+    PhaseTimer& operator=(const PhaseTimer&) = delete;
+private:
+    amdg_context* ctx_;
+    int phase_;
+    double t0_;
+};
+}  // namespace amdg
 
 struct amdg_grid {
     int64_t version = 0;             // bumped whenever the element set changes
@@ -161,9 +211,19 @@ struct amdg_grid {
     int block = 0;                   // (k+1)^dim
     int64_t dof = 0;
     int32_t* d_order = nullptr;      // device copy of host.order
-    double* d_u = nullptr;           // FP64 coefficients
+    double* d_u = nullptr;           // FP64 coefficients (capacity elements)
     double* d_scratch = nullptr;     // reduction scratch
     size_t scratch_bytes = 0;
+    // grow-only buffers of element-set changes: the spare coefficient array the
+    // remap writes into (then swapped with d_u), the old-to-new index map, the
+    // indicator norms
+    int64_t order_capacity = 0;
+    double* d_u_spare = nullptr;
+    int64_t spare_capacity = 0;
+    int32_t* d_map = nullptr;
+    int64_t map_capacity = 0;
+    double* d_norms = nullptr;
+    int64_t norms_capacity = 0;
 };
 
 struct amdg_linear_op {
@@ -206,25 +266,33 @@ struct amdg_burgers_op {
     int32_t *d_vol_ptr = nullptr, *d_vol_nbr = nullptr;  // nbr: (element, 1D order along t) pairs
     int32_t *d_flx_ptr = nullptr, *d_flx_nbr = nullptr;
     int32_t *d_vol_split = nullptr, *d_flx_split = nullptr;
-    uint8_t *d_vol_long = nullptr, *d_flx_long = nullptr;
-    int32_t *d_vol_long_elems = nullptr, *d_flx_long_elems = nullptr;  // concatenated over t
-    std::vector<int32_t> vol_long_off, flx_long_off;                   // dim + 1 offsets
     int32_t *d_anc = nullptr, *d_anc_point = nullptr, *d_anc_rank = nullptr;
     double weight[16] = {0};
     std::vector<std::vector<int>> sched_dims, sched_lu;
-    // work buffers sized for FP64 (E x 4^dim doubles each)
-    void *w_up = nullptr, *w_fu = nullptr, *w_a = nullptr, *w_b = nullptr, *w_rhs = nullptr, *w_u = nullptr;
+    // terms of the point values (first n_pv_terms) and of the right-hand side, in summation order
+    std::vector<amdg::PartialSum> terms;
+    amdg::PartialSum* d_terms = nullptr;
+    int n_pv_terms = 0;
+    int chunk = 1;  // terms per launch
+    // work buffers sized for FP64: E x 4^dim doubles each, the sweep buffers and
+    // term slices chunk times that
+    void *w_up = nullptr, *w_fu = nullptr, *w_a = nullptr, *w_b = nullptr, *w_u = nullptr;
+    void *w_s0 = nullptr, *w_s1 = nullptr, *w_slots = nullptr;
     double *d_u1 = nullptr, *d_u2 = nullptr, *d_rhs64 = nullptr, *d_pred = nullptr;
     std::vector<double> host_norms;
     // one SSP-RK3 step captured as a CUDA graph, valid for (grid version, precision, dt)
     int32_t* d_pg = nullptr;         // [e][d][2] parent / grandparent (learned adaptivity features)
     float *d_feat = nullptr, *d_prob = nullptr;  // classifier features / probabilities
     int64_t feat_cap = 0;                        // elements the two hold
+    int64_t pg_version = -1;                     // element set d_pg was built for
+    std::vector<uint64_t> missed_keys;           // leaves the criterion found above eps after the last learned step
     void* graph_exec = nullptr;
     int64_t graph_version = -1;
     int graph_prec = -1;
     double graph_dt = 0.0;
     int64_t graph_launches = 0;
+    int64_t stage_dof_updates = 0;  // RK stages x DOF advanced since creation
+    int64_t rhs_evaluations = 0;    // right-hand sides evaluated since creation
     int64_t last_version = -1;  // configuration of the previous rk3 call
     int last_prec = -1;
     double last_dt = 0.0;

@@ -250,4 +250,12 @@ void project_1d(const Basis1D& b, amdg_fn1d f, void* user, int d, int term, doub
     }
 }
 
+void gauss_legendre(int n, double* x, double* w) {
+    const GaussRule g(n);
+    for (int i = 0; i < n; ++i) {
+        x[i] = g.x[i];
+        w[i] = g.w[i];
+    }
+}
+
 }  // namespace amdg

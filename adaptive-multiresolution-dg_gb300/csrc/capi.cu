@@ -5,6 +5,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <chrono>
 #include <cmath>
 #include <unordered_map>
 #include <cstring>
@@ -92,9 +93,28 @@ amdg_status project_terms(const amdg_grid* g, int nterms, amdg_fn1d f, void* use
 
 namespace amdg {
 
+static double wall_seconds() {
+    return std::chrono::duration<double>(std::chrono::steady_clock::now().time_since_epoch()).count();
+}
+
+PhaseTimer::PhaseTimer(amdg_context* ctx, int phase)
+    : ctx_(ctx), phase_(phase), t0_(ctx && ctx->profile ? wall_seconds() : 0.0) {}
+
+PhaseTimer::~PhaseTimer() {
+    if (ctx_ && ctx_->profile) {
+        ctx_->phase_sec[phase_] += wall_seconds() - t0_;
+        ctx_->phase_calls[phase_]++;
+    }
+}
+
+}  // namespace amdg
+
+namespace amdg {
+
 // Replace the grid's element set by `keys` (sorted, unique), carrying the
 // coefficients of surviving elements over and zeroing new ones.
 amdg_status grid_set_keys(amdg_grid* g, std::vector<uint64_t> keys) {
+    PhaseTimer timer(g->ctx, AMDG_PHASE_SET_KEYS);
     HostGrid ng;
     ng.sparse = g->host.sparse;
     grid_from_keys(g->host.dim, g->host.nmax, g->host.k, std::move(keys), &ng);
@@ -106,27 +126,37 @@ amdg_status grid_set_keys(amdg_grid* g, std::vector<uint64_t> keys) {
     }
     cudaStream_t st = stream_of(g->ctx);
     const int64_t E = ng.num_elements;
-    const int64_t cap = std::max<int64_t>(E, g->capacity);
-    double* nu = nullptr;
-    int32_t* dmap = nullptr;
+    const int64_t grown = E + E / 4 + 16;
     amdg_status s;
-    if ((s = dev_alloc(&nu, size_t(cap) * g->block)) != AMDG_OK) return s;
-    if ((s = upload(&dmap, map, st)) != AMDG_OK) { cudaFree(nu); return s; }
-    cudaError_t e = launch_remap(g->d_u, dmap, g->block, E, nu, st);
-    g->ctx->launches++;
-    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
-    cudaFree(dmap);
-    if (e != cudaSuccess) { cudaFree(nu); return fail(AMDG_ERR_CUDA, std::string("remap: ") + cudaGetErrorString(e)); }
-    cudaFree(g->d_u);
-    g->d_u = nu;
-    if (E > g->capacity || !g->d_order) {
+    // remap into the spare coefficient array, then swap it in; buffers grow by a quarter
+    if (E > g->spare_capacity) {
+        cudaFree(g->d_u_spare);
+        g->d_u_spare = nullptr;
+        g->spare_capacity = 0;
+        if ((s = dev_alloc(&g->d_u_spare, size_t(grown) * g->block)) != AMDG_OK) return s;
+        g->spare_capacity = grown;
+    }
+    if (E > g->map_capacity) {
+        cudaFree(g->d_map);
+        g->d_map = nullptr;
+        g->map_capacity = 0;
+        if ((s = dev_alloc(&g->d_map, size_t(grown))) != AMDG_OK) return s;
+        g->map_capacity = grown;
+    }
+    if (E > g->order_capacity) {
         cudaFree(g->d_order);
         g->d_order = nullptr;
-        if ((s = dev_alloc(&g->d_order, size_t(cap) * g->host.dim)) != AMDG_OK) return s;
+        g->order_capacity = 0;
+        if ((s = dev_alloc(&g->d_order, size_t(grown) * g->host.dim)) != AMDG_OK) return s;
+        g->order_capacity = grown;
     }
-    g->capacity = cap;
+    if (E > 0) AMDG_CK(cudaMemcpyAsync(g->d_map, map.data(), size_t(E) * sizeof(int32_t), cudaMemcpyHostToDevice, st));
+    AMDG_CK(launch_remap(g->d_u, g->d_map, g->block, E, g->d_u_spare, st));
+    g->ctx->launches++;
+    std::swap(g->d_u, g->d_u_spare);
+    std::swap(g->capacity, g->spare_capacity);
     AMDG_CK(cudaMemcpyAsync(g->d_order, ng.order.data(), ng.order.size() * sizeof(int32_t), cudaMemcpyHostToDevice, st));
-    AMDG_CK(cudaStreamSynchronize(st));
+    AMDG_CK(cudaStreamSynchronize(st));  // the host map and orders are released on return
     g->host = std::move(ng);
     g->dof = g->host.num_elements * g->block;
     g->version++;
@@ -135,17 +165,22 @@ amdg_status grid_set_keys(amdg_grid* g, std::vector<uint64_t> keys) {
 
 // indicator norms of a device coefficient vector on the grid's current element set
 amdg_status grid_norms(amdg_grid* g, const double* d_u, std::vector<double>* norms) {
+    PhaseTimer timer(g->ctx, AMDG_PHASE_NORMS);
     cudaStream_t st = stream_of(g->ctx);
-    double* d_n = nullptr;
-    amdg_status s = dev_alloc(&d_n, size_t(std::max<int64_t>(g->host.num_elements, 1)));
-    if (s != AMDG_OK) return s;
-    cudaError_t e = launch_element_norms(d_u, g->block, g->host.num_elements, d_n, st);
+    const int64_t E = g->host.num_elements;
+    if (E > g->norms_capacity) {
+        cudaFree(g->d_norms);
+        g->d_norms = nullptr;
+        g->norms_capacity = 0;
+        const int64_t cap = E + E / 4 + 16;
+        if (amdg_status s = dev_alloc(&g->d_norms, size_t(cap)); s != AMDG_OK) return s;
+        g->norms_capacity = cap;
+    }
+    cudaError_t e = launch_element_norms(d_u, g->block, E, g->d_norms, st);
     g->ctx->launches++;
-    norms->assign(g->host.num_elements, 0.0);
-    if (e == cudaSuccess && g->host.num_elements > 0)
-        e = cudaMemcpyAsync(norms->data(), d_n, norms->size() * sizeof(double), cudaMemcpyDeviceToHost, st);
+    norms->assign(E, 0.0);
+    if (e == cudaSuccess && E > 0) e = cudaMemcpyAsync(norms->data(), g->d_norms, size_t(E) * sizeof(double), cudaMemcpyDeviceToHost, st);
     if (e == cudaSuccess) e = cudaStreamSynchronize(st);
-    cudaFree(d_n);
     if (e != cudaSuccess) return fail(AMDG_ERR_CUDA, std::string("element norms: ") + cudaGetErrorString(e));
     for (double v : *norms)
         if (!std::isfinite(v)) return fail(AMDG_ERR_NONFINITE, "element indicator is not finite");
@@ -413,6 +448,25 @@ amdg_status amdg_context_launch_count(amdg_context* ctx, int64_t* count) {
     return AMDG_OK;
 }
 
+amdg_status amdg_context_profile(amdg_context* ctx, int enable) {
+    AMDG_REQUIRE(ctx, AMDG_ERR_ARG, "null context");
+    ctx->profile = enable != 0;
+    for (int i = 0; i < AMDG_PHASE_COUNT; ++i) {
+        ctx->phase_sec[i] = 0.0;
+        ctx->phase_calls[i] = 0;
+    }
+    return AMDG_OK;
+}
+
+amdg_status amdg_context_profile_read(const amdg_context* ctx, double* seconds, int64_t* calls) {
+    AMDG_REQUIRE(ctx, AMDG_ERR_ARG, "null context");
+    for (int i = 0; i < AMDG_PHASE_COUNT; ++i) {
+        if (seconds) seconds[i] = ctx->phase_sec[i];
+        if (calls) calls[i] = ctx->phase_calls[i];
+    }
+    return AMDG_OK;
+}
+
 // ---- host-side set-up --------------------------------------------------------
 
 amdg_status amdg_oper1d_build(int nmax, int k, double* u_v, double* u_vx, double* ulft_vjp, double* urgt_vjp) {
@@ -468,6 +522,7 @@ amdg_status amdg_grid_create_ex(amdg_context* ctx, int dim, int level_init, int 
     g->block = ipow(k + 1, dim);
     g->dof = g->host.num_elements * g->block;
     g->capacity = g->host.num_elements;
+    g->order_capacity = g->host.num_elements;
     if (g->host.num_elements > (int64_t(1) << 31) - 1) {
         delete g;
         return fail(AMDG_ERR_CAPACITY, "more than 2^31-1 elements");
@@ -501,6 +556,9 @@ amdg_status amdg_grid_destroy(amdg_grid* g) {
     cudaFree(g->d_order);
     cudaFree(g->d_u);
     cudaFree(g->d_scratch);
+    cudaFree(g->d_u_spare);
+    cudaFree(g->d_map);
+    cudaFree(g->d_norms);
     delete g;
     return AMDG_OK;
 }
@@ -631,7 +689,11 @@ amdg_status amdg_grid_refine(amdg_grid* g, const double* d_indicator, double eps
     if (s != AMDG_OK) return s;
     std::vector<double> norms;
     if ((s = grid_norms(g, d_indicator ? d_indicator : g->d_u, &norms)) != AMDG_OK) return s;
-    std::vector<uint64_t> keys = refine_keys(g->host, norms.data(), eps);
+    std::vector<uint64_t> keys;
+    {
+        PhaseTimer timer(g->ctx, AMDG_PHASE_ADAPT_HOST);
+        keys = refine_keys(g->host, norms.data(), eps);
+    }
     if (int64_t(keys.size()) != g->host.num_elements && (s = grid_set_keys(g, std::move(keys))) != AMDG_OK) return s;
     if (num_elements) *num_elements = g->host.num_elements;
     return AMDG_OK;
@@ -643,7 +705,11 @@ amdg_status amdg_grid_coarsen(amdg_grid* g, double eta, int64_t* num_elements) {
     if (s != AMDG_OK) return s;
     std::vector<double> norms;
     if ((s = grid_norms(g, g->d_u, &norms)) != AMDG_OK) return s;
-    std::vector<uint64_t> keys = coarsen_keys(g->host, norms.data(), eta);
+    std::vector<uint64_t> keys;
+    {
+        PhaseTimer timer(g->ctx, AMDG_PHASE_ADAPT_HOST);
+        keys = coarsen_keys(g->host, norms.data(), eta);
+    }
     if (int64_t(keys.size()) != g->host.num_elements && (s = grid_set_keys(g, std::move(keys))) != AMDG_OK) return s;
     if (num_elements) *num_elements = g->host.num_elements;
     return AMDG_OK;

@@ -35,6 +35,9 @@ using namespace amdg;
 
 namespace {
 
+// device bytes the term slices of one launch may take (sweep buffers and outputs)
+constexpr size_t kTermBudget = size_t(3) << 29;
+
 template <class T>
 amdg_status upload_vec(T** p, const std::vector<T>& host) {
     *p = nullptr;
@@ -64,195 +67,204 @@ cudaStream_t stream_of(const amdg_burgers_op* op) { return static_cast<cudaStrea
 
 template <typename T>
 struct Mats {
-    const T *a2p, *lv, *lvx, *lflx, *ajump;
+    const T* m[kNumLagrMats];
 };
 
-Mats<double> mats64(const amdg_burgers_op* op) { return {op->d_a2p, op->d_lv, op->d_lvx, op->d_lflx, op->d_ajump}; }
-Mats<float> mats32(const amdg_burgers_op* op) { return {op->f_a2p, op->f_lv, op->f_lvx, op->f_lflx, op->f_ajump}; }
+Mats<double> mats64(const amdg_burgers_op* op) { return {{op->d_a2p, op->d_lv, op->d_lvx, op->d_lflx, op->d_ajump}}; }
+Mats<float> mats32(const amdg_burgers_op* op) { return {{op->f_a2p, op->f_lv, op->f_lvx, op->f_lflx, op->f_ajump}}; }
 
-int prod(const int* s, int n) {
+int ipow(int b, int e) {
     int p = 1;
-    for (int i = 0; i < n; ++i) p *= s[i];
+    for (int i = 0; i < e; ++i) p *= b;
     return p;
 }
 
+// The terms of the path (host side, built once per operator):
+//  - point values: the 2^(dim-1) partial sums of the schedule with the
+//    Alpert-at-Lagrange-point matrix in every dimension (FastLagrIntp::eval_up_Lagr);
+//  - right-hand side, in the order the reference adds them: for each dimension
+//    d the volume partial sums (u_vx in d, u_v elsewhere, vol sets), the
+//    interface partial sums (0.5 (ulft+urgt)_vjp in d on the flx sets, u_v
+//    elsewhere) (HyperbolicLagrRHS::rhs_vol_scalar / rhs_flx_intp_scalar,
+//    FastMultiplyLU.cpp:1125-1189), then the LxF penalty -alpha_d/2 ujp_vjp
+//    along d (HyperbolicAlptRHS::rhs_flx_penalty_scalar, :1269-1276).
+void build_terms(amdg_burgers_op* op) {
+    const int dim = op->grid->host.dim;
+    op->terms.clear();
+    auto psum = [&](const std::vector<int>& dims, const std::vector<int>& lu, const int* mat, const int* flx, double coef) {
+        PartialSum p{};
+        for (int j = 0; j < dim; ++j) {
+            p.dims[j] = int8_t(dims[j]);
+            p.lu[j] = int8_t(lu[j]);
+            p.mat[j] = int8_t(mat[dims[j]]);
+            p.flx[j] = int8_t(flx[dims[j]]);
+        }
+        p.kind = 0;
+        p.coef = coef;
+        op->terms.push_back(p);
+    };
+    int mat[kMaxDim], flx[kMaxDim];
+    for (int t = 0; t < dim; ++t) { mat[t] = kMatA2P; flx[t] = 0; }
+    for (size_t s = 0; s < op->sched_dims.size(); ++s) psum(op->sched_dims[s], op->sched_lu[s], mat, flx, 1.0);
+    op->n_pv_terms = int(op->terms.size());
+    for (int d = 0; d < dim; ++d) {
+        for (int term = 0; term < 2; ++term) {
+            for (int t = 0; t < dim; ++t) {
+                mat[t] = (t == d) ? (term == 0 ? kMatLVX : kMatLFLX) : kMatLV;
+                flx[t] = (term == 1 && t == d) ? 1 : 0;
+            }
+            for (size_t s = 0; s < op->sched_dims.size(); ++s)
+                psum(op->sched_dims[s], op->sched_lu[s], mat, flx, term == 0 ? 1.0 : 0.5);
+        }
+        PartialSum p{};
+        p.dims[0] = int8_t(d);
+        p.kind = 1;
+        p.coef = -op->alpha[d] / 2.0;
+        op->terms.push_back(p);
+    }
+}
+
 template <typename T>
-TransformArgs<T> base_args(const amdg_burgers_op* op, int t, const int* from, const int* to, bool flx) {
+SweepArgs<T> sweep_args(const amdg_burgers_op* op, const Mats<T>& m) {
     const amdg_grid* g = op->grid;
-    const int dim = g->host.dim;
-    TransformArgs<T> a{};
-    a.dim = dim;
-    a.t = t;
-    a.n_from = from[t];
-    a.n_to = to[t];
-    a.stride = prod(from + t + 1, dim - t - 1);
-    a.in_block = prod(from, dim);
-    a.out_block = prod(to, dim);
+    SweepArgs<T> a{};
+    a.dim = g->host.dim;
+    a.np = g->host.k + 1;
+    a.n1 = op->n1;
     a.num_elements = g->host.num_elements;
+    a.desc = op->d_terms;
+    for (int i = 0; i < kNumLagrMats; ++i) a.mats[i] = m.m[i];
+    a.vol_ptr = op->d_vol_ptr;
+    a.vol_split = op->d_vol_split;
+    a.vol_nbr = reinterpret_cast<const int2*>(op->d_vol_nbr);
+    a.flx_ptr = op->d_flx_ptr;
+    a.flx_split = op->d_flx_split;
+    a.flx_nbr = reinterpret_cast<const int2*>(op->d_flx_nbr);
     a.order = g->d_order;
-    a.ptr = flx ? op->d_flx_ptr : op->d_vol_ptr;
-    a.nbr = reinterpret_cast<const int2*>(flx ? op->d_flx_nbr : op->d_vol_nbr);
-    a.split = flx ? op->d_flx_split : op->d_vol_split;
-    a.long_flag = flx ? op->d_flx_long : op->d_vol_long;
-    const std::vector<int32_t>& off = flx ? op->flx_long_off : op->vol_long_off;
-    a.long_elems = (flx ? op->d_flx_long_elems : op->d_vol_long_elems) + off[t];
-    a.num_long = off[t + 1] - off[t];
     return a;
 }
 
-// One partial sum: dim successive 1D transforms, the first scaled by coef, the
-// last accumulated into out (FastRHS::transform_multiD_partial_sum,
-// FastInterpolation::transform_multiD_partial_sum).
+// Terms [first, first + count): dim sweeps, the last one into `slots`
+// (count slices of E x n_out^dim, or E x np^dim for a right-hand side).
 template <typename T>
-amdg_status partial_sum(amdg_burgers_op* op, const std::vector<int>& dims, const std::vector<int>& lu, int n_in, int n_out,
-                        const T* const* mat, const bool* flx, T coef, const T* in, T* out, T* tmp_a, T* tmp_b,
-                        cudaStream_t st) {
+amdg_status run_terms(amdg_burgers_op* op, const Mats<T>& m, int first, int count, int n_in, int n_out, const T* in,
+                      const T* pen_in, T* slots, cudaStream_t st) {
     const int dim = op->grid->host.dim;
-    int from[kMaxDim], to[kMaxDim];
-    for (int d = 0; d < dim; ++d) from[d] = n_in;
+    const int64_t E = op->grid->host.num_elements;
+    T* ping = static_cast<T*>(op->w_s0);
+    T* pong = static_cast<T*>(op->w_s1);
+    SweepArgs<T> a = sweep_args<T>(op, m);
+    a.first = first;
+    a.count = count;
+    a.n_in = n_in;
+    a.n_out = n_out;
+    a.pen_in = pen_in;
     const T* cur = in;
-    for (int i = 0; i < dim; ++i) {
-        const int t = dims[i];
-        std::memcpy(to, from, sizeof(int) * dim);
-        to[t] = n_out;
-        TransformArgs<T> a = base_args<T>(op, t, from, to, flx[t]);
-        a.M = mat[t];
-        a.ncols = op->n1 * n_out;
-        a.lu = lu[i];
-        a.coef = (i == 0) ? coef : T(1);
+    for (int j = 0; j < dim; ++j) {
+        const bool last = j == dim - 1;
+        a.sweep = j;
         a.in = cur;
-        const bool last = (i == dim - 1);
-        T* dst = last ? out : ((cur == tmp_a) ? tmp_b : tmp_a);
-        a.out = dst;
-        a.accumulate = last ? 1 : 0;
-        AMDG_CK(launch_fibre_transform<T>(a, st));
+        a.in_slice = j == 0 ? 0 : E * ipow(n_out, j) * ipow(n_in, dim - j);
+        a.out_block = ipow(n_out, j + 1) * ipow(n_in, dim - j - 1);
+        a.out = last ? slots : (j % 2 == 0 ? ping : pong);
+        AMDG_CK(launch_sweep<T>(a, st));
         op->grid->ctx->launches++;
-        cur = dst;
-        std::memcpy(from, to, sizeof(int) * dim);
+        cur = a.out;
     }
     return AMDG_OK;
 }
 
+// u_h at the interpolation points (FP64 or FP32 arithmetic): into up, or, when
+// fp is given, f(u) = u^2/2 at the points into fp
 template <typename T>
-amdg_status eval_point_values(amdg_burgers_op* op, const Mats<T>& m, const T* u, T* up, cudaStream_t st) {
-    const amdg_grid* g = op->grid;
-    const int dim = g->host.dim, np = g->host.k + 1;
-    AMDG_CK(cudaMemsetAsync(up, 0, size_t(g->host.num_elements) * op->points * sizeof(T), st));
-    const T* mats[kMaxDim];
-    bool flx[kMaxDim];
-    for (int d = 0; d < dim; ++d) { mats[d] = m.a2p; flx[d] = false; }
-    T* ta = static_cast<T*>(op->w_a);
-    T* tb = static_cast<T*>(op->w_b);
-    for (size_t s = 0; s < op->sched_dims.size(); ++s) {
-        amdg_status r = partial_sum<T>(op, op->sched_dims[s], op->sched_lu[s], np, 4, mats, flx, T(1), u, up, ta, tb, st);
-        if (r != AMDG_OK) return r;
+amdg_status eval_point_values(amdg_burgers_op* op, const Mats<T>& m, const T* u, T* up, T* fp, cudaStream_t st) {
+    const int np = op->grid->host.k + 1;
+    const int64_t n = op->grid->host.num_elements * op->points;
+    T* slots = static_cast<T*>(op->w_slots);
+    for (int c0 = 0; c0 < op->n_pv_terms; c0 += op->chunk) {
+        const int cnt = std::min(op->chunk, op->n_pv_terms - c0);
+        if (amdg_status r = run_terms<T>(op, m, c0, cnt, np, 4, u, nullptr, slots, st); r != AMDG_OK) return r;
+        const bool last = c0 + cnt == op->n_pv_terms;
+        AMDG_CK(launch_reduce_points<T>(slots, cnt, n, c0 == 0 ? 1 : 0, up, last ? fp : nullptr, st));
+        op->grid->ctx->launches++;
     }
     return AMDG_OK;
 }
 
-// flux interpolation coefficients: f(u) at the points, then dim surplus passes (result in op->w_fu)
-template <typename T>
-amdg_status eval_flux_coefficients(amdg_burgers_op* op, const T* up, cudaStream_t st) {
+// flux interpolation coefficients from f(u) at the points (in w_a): dim surplus
+// passes, the last one into `out` (type To)
+template <typename T, typename To>
+amdg_status eval_surplus(amdg_burgers_op* op, To* out, cudaStream_t st) {
     const amdg_grid* g = op->grid;
     const int dim = g->host.dim;
-    const int64_t n = g->host.num_elements * op->points;
     T* ta = static_cast<T*>(op->w_a);
     T* tb = static_cast<T*>(op->w_b);
-    T* fu = static_cast<T*>(op->w_fu);
-    AMDG_CK(launch_burgers_flux<T>(up, ta, n, st));
-    op->grid->ctx->launches++;
+    SurplusArgs<T> a{};
+    a.dim = dim;
+    a.points = op->points;
+    a.num_elements = g->host.num_elements;
+    a.order = g->d_order;
+    a.anc = op->d_anc;
+    a.anc_point = op->d_anc_point;
+    a.anc_rank = op->d_anc_rank;
+    for (int i = 0; i < 16; ++i) a.weight[i] = op->weight[i];
     const T* cur = ta;
     for (int d = 0; d < dim; ++d) {
-        SurplusArgs<T> a{};
-        a.dim = dim;
         a.d = d;
-        a.points = op->points;
-        a.stride = 1;
-        for (int s = d + 1; s < dim; ++s) a.stride *= 4;
-        a.num_elements = g->host.num_elements;
-        a.order = g->d_order;
-        a.anc = op->d_anc;
-        a.anc_point = op->d_anc_point;
-        a.anc_rank = op->d_anc_rank;
-        for (int i = 0; i < 16; ++i) a.weight[i] = T(op->weight[i]);
-        T* dst = (d == dim - 1) ? fu : ((cur == tb) ? ta : tb);
-        a.in = cur;
-        a.out = dst;
-        AMDG_CK(launch_surplus_pass<T>(a, st));
-        op->grid->ctx->launches++;
-        cur = dst;
-    }
-    return AMDG_OK;
-}
-
-// volume and interface terms from the flux coefficients fu, and the LxF
-// penalty from the Alpert coefficients u, into rhs (set, not added)
-template <typename T>
-amdg_status eval_back_transforms(amdg_burgers_op* op, const Mats<T>& m, const T* fu, const T* u, T* rhs, cudaStream_t st) {
-    const amdg_grid* g = op->grid;
-    const int dim = g->host.dim, np = g->host.k + 1;
-    T* ta = static_cast<T*>(op->w_a);
-    T* tb = static_cast<T*>(op->w_b);
-    AMDG_CK(cudaMemsetAsync(rhs, 0, size_t(g->dof) * sizeof(T), st));
-    for (int d = 0; d < dim; ++d) {
-        for (int term = 0; term < 2; ++term) {
-            // term 0: volume (u_vx in d, u_v elsewhere, vol sets);
-            // term 1: interface (ulft+urgt)_vjp in d on flx sets, coefficient 0.5
-            const T* mats[kMaxDim];
-            bool flx[kMaxDim];
-            for (int t = 0; t < dim; ++t) {
-                mats[t] = (t == d) ? (term == 0 ? m.lvx : m.lflx) : m.lv;
-                flx[t] = (term == 1 && t == d);
-            }
-            const T coef = term == 0 ? T(1) : T(0.5);
-            for (size_t s = 0; s < op->sched_dims.size(); ++s) {
-                amdg_status r = partial_sum<T>(op, op->sched_dims[s], op->sched_lu[s], 4, np, mats, flx, coef, fu, rhs, ta, tb, st);
-                if (r != AMDG_OK) return r;
-            }
+        a.stride = ipow(4, dim - d - 1);
+        if (d == dim - 1) {
+            AMDG_CK(launch_surplus_pass<T, To>(a, cur, out, st));
+        } else {
+            T* dst = (cur == ta) ? tb : ta;
+            AMDG_CK(launch_surplus_pass<T, T>(a, cur, dst, st));
+            cur = dst;
         }
-        // LxF penalty -alpha_d/2 ujp_vjp in dimension d (FastRHS::transform_ucoe_alpt_to_rhs, FastMultiplyLU.cpp:46-59)
-        int from[kMaxDim];
-        for (int t = 0; t < dim; ++t) from[t] = np;
-        TransformArgs<T> a = base_args<T>(op, d, from, from, true);
-        a.M = m.ajump;
-        a.ncols = op->n1 * np;
-        a.lu = 1;
-        a.coef = T(-op->alpha[d] / 2.0);
-        a.in = u;
-        a.out = rhs;
-        a.accumulate = 1;
-        AMDG_CK(launch_fibre_transform<T>(a, st));
         op->grid->ctx->launches++;
     }
     return AMDG_OK;
 }
 
-// rhs (FP64, dof entries) of the FP64 state u.  The point values and the
-// hierarchical surplus always run in FP64: fine-level surpluses are small
-// differences of O(1) point values, which FP32 rounding would swamp.  In mixed
-// mode the back transforms (the bulk of the work) and the penalty run in FP32.
-amdg_status eval_rhs(amdg_burgers_op* op, const double* u, double* rhs, amdg_precision prec) {
-    cudaStream_t st = stream_of(op);
-    const int64_t n = op->grid->dof;
-    const int64_t npts = op->grid->host.num_elements * op->points;
-    double* up = static_cast<double*>(op->w_up);
-    amdg_status r = eval_point_values<double>(op, mats64(op), u, up, st);
-    if (r != AMDG_OK) return r;
-    if ((r = eval_flux_coefficients<double>(op, up, st)) != AMDG_OK) return r;
-    const double* fu = static_cast<const double*>(op->w_fu);
-    if (prec == AMDG_PREC_FP64) return eval_back_transforms<double>(op, mats64(op), fu, u, rhs, st);
-    float* fu32 = static_cast<float*>(op->w_up);  // point values are no longer needed
-    float* u32 = static_cast<float*>(op->w_u);
-    float* r32 = static_cast<float*>(op->w_rhs);
-    AMDG_CK(launch_convert<double, float>(fu, fu32, npts, st));
-    AMDG_CK(launch_convert<double, float>(u, u32, n, st));
-    op->grid->ctx->launches += 2;
-    if ((r = eval_back_transforms<float>(op, mats32(op), fu32, u32, r32, st)) != AMDG_OK) return r;
-    AMDG_CK(launch_convert<float, double>(r32, rhs, n, st));
-    op->grid->ctx->launches++;
+// volume, interface and penalty terms from the flux coefficients fu and the
+// Alpert coefficients u: into rhs, or, when so.fused, straight into the RK
+// stage update
+template <typename T>
+amdg_status eval_back_transforms(amdg_burgers_op* op, const Mats<T>& m, const T* fu, const T* u, double* rhs, StageOut so,
+                                 cudaStream_t st) {
+    const int np = op->grid->host.k + 1;
+    T* slots = static_cast<T*>(op->w_slots);
+    const int first = op->n_pv_terms, total = int(op->terms.size()) - op->n_pv_terms;
+    for (int c0 = 0; c0 < total; c0 += op->chunk) {
+        const int cnt = std::min(op->chunk, total - c0);
+        if (amdg_status r = run_terms<T>(op, m, first + c0, cnt, 4, np, fu, u, slots, st); r != AMDG_OK) return r;
+        AMDG_CK(launch_reduce_rhs<T>(slots, cnt, op->grid->dof, c0 == 0 ? 1 : 0, c0 + cnt == total ? 1 : 0, rhs, so, st));
+        op->grid->ctx->launches++;
+    }
     return AMDG_OK;
 }
 
+// rhs (FP64, dof entries) of the FP64 state u, or the stage update `so` with it.
+// The point values and the hierarchical surplus always run in FP64:
+// fine-level surpluses are small differences of O(1) point values, which FP32
+// rounding would swamp.  In mixed mode the back transforms (the bulk of the
+// work) and the penalty run in FP32, their terms summed in FP64.
+amdg_status eval_rhs(amdg_burgers_op* op, const double* u, double* rhs, amdg_precision prec, StageOut so = StageOut{}) {
+    PhaseTimer timer(op->grid->ctx, AMDG_PHASE_RHS);
+    cudaStream_t st = stream_of(op);
+    double* fp = static_cast<double*>(op->w_a);
+    amdg_status r = eval_point_values<double>(op, mats64(op), u, static_cast<double*>(op->w_up), fp, st);
+    if (r != AMDG_OK) return r;
+    if (prec == AMDG_PREC_FP64) {
+        double* fu = static_cast<double*>(op->w_fu);
+        if ((r = eval_surplus<double, double>(op, fu, st)) != AMDG_OK) return r;
+        return eval_back_transforms<double>(op, mats64(op), fu, u, rhs, so, st);
+    }
+    float* fu32 = static_cast<float*>(op->w_fu);
+    float* u32 = static_cast<float*>(op->w_u);
+    if ((r = eval_surplus<double, float>(op, fu32, st)) != AMDG_OK) return r;
+    AMDG_CK(launch_convert<double, float>(u, u32, op->grid->dof, st));
+    op->grid->ctx->launches++;
+    return eval_back_transforms<float>(op, mats32(op), fu32, u32, rhs, so, st);
+}
 
 // Copy a host vector into a grow-only device array of the operator (stream
 // ordered: kernels queued before still see the old contents).
@@ -278,6 +290,7 @@ amdg_status upload_grow(amdg_burgers_op* op, T** p, const std::vector<T>& host, 
 amdg_status burgers_sync(amdg_burgers_op* op) {
     amdg_grid* g = op->grid;
     if (op->built_version == g->version) return AMDG_OK;
+    PhaseTimer timer(g->ctx, AMDG_PHASE_TOPOLOGY);
     cudaStream_t st = stream_of(op);
     LagrTables t;
     if (op->anc_order.empty()) {
@@ -293,17 +306,6 @@ amdg_status burgers_sync(amdg_burgers_op* op) {
     build_transform_topology(g->host, &topo);
     std::vector<int32_t> anc;
     if (!build_surplus_ancestors(g->host, t, &anc)) return fail(AMDG_ERR_STATE, "element set has a hole: a surplus ancestor is missing");
-    std::vector<int32_t> vle, fle;
-    op->vol_long_off.assign(1, 0);
-    op->flx_long_off.assign(1, 0);
-    for (int d = 0; d < g->host.dim; ++d) {
-        vle.insert(vle.end(), topo.vol_long_elems[d].begin(), topo.vol_long_elems[d].end());
-        fle.insert(fle.end(), topo.flx_long_elems[d].begin(), topo.flx_long_elems[d].end());
-        op->vol_long_off.push_back(int32_t(vle.size()));
-        op->flx_long_off.push_back(int32_t(fle.size()));
-    }
-    std::vector<int32_t> pg;
-    parent_table(g->host, &pg);
     amdg_status s;
     if ((s = upload_grow(op, &op->d_vol_ptr, topo.vol_ptr, st)) != AMDG_OK ||
         (s = upload_grow(op, &op->d_vol_nbr, topo.vol_nbr, st)) != AMDG_OK ||
@@ -311,23 +313,28 @@ amdg_status burgers_sync(amdg_burgers_op* op) {
         (s = upload_grow(op, &op->d_flx_nbr, topo.flx_nbr, st)) != AMDG_OK ||
         (s = upload_grow(op, &op->d_anc, anc, st)) != AMDG_OK ||
         (s = upload_grow(op, &op->d_vol_split, topo.vol_split, st)) != AMDG_OK ||
-        (s = upload_grow(op, &op->d_flx_split, topo.flx_split, st)) != AMDG_OK ||
-        (s = upload_grow(op, &op->d_vol_long, topo.vol_long, st)) != AMDG_OK ||
-        (s = upload_grow(op, &op->d_flx_long, topo.flx_long, st)) != AMDG_OK ||
-        (s = upload_grow(op, &op->d_vol_long_elems, vle, st)) != AMDG_OK ||
-        (s = upload_grow(op, &op->d_flx_long_elems, fle, st)) != AMDG_OK ||
-        (s = upload_grow(op, &op->d_pg, pg, st)) != AMDG_OK)
+        (s = upload_grow(op, &op->d_flx_split, topo.flx_split, st)) != AMDG_OK)
         return s;
     const int64_t E = g->host.num_elements;
     if (E > op->capacity) {
         const int64_t cap = E + E / 2 + 16;
-        void* bufs[] = {op->w_up, op->w_fu, op->w_a, op->w_b, op->w_rhs, op->w_u, op->d_u1, op->d_rhs64, op->d_pred};
+        void* bufs[] = {op->w_up, op->w_fu, op->w_a, op->w_b, op->w_u, op->w_s0, op->w_s1, op->w_slots,
+                        op->d_u1, op->d_rhs64, op->d_pred};
         for (void* p : bufs) cudaFree(p);
+        op->w_up = op->w_fu = op->w_a = op->w_b = op->w_u = op->w_s0 = op->w_s1 = op->w_slots = nullptr;
+        op->d_u1 = op->d_rhs64 = op->d_pred = nullptr;
+        op->capacity = 0;
         const size_t work = size_t(cap) * op->points * sizeof(double);
         const size_t vec = size_t(cap) * g->block * sizeof(double);
+        // terms per launch: all of them unless their three slices per term
+        // (two sweep buffers and the output) would pass kTermBudget bytes
+        const int nterms = int(op->terms.size());
+        op->chunk = int(std::max<int64_t>(1, std::min<int64_t>(nterms, int64_t(kTermBudget / (3 * work)))));
+        const size_t slices = size_t(op->chunk) * work;
         if ((s = alloc_bytes(&op->w_up, work)) != AMDG_OK || (s = alloc_bytes(&op->w_fu, work)) != AMDG_OK ||
             (s = alloc_bytes(&op->w_a, work)) != AMDG_OK || (s = alloc_bytes(&op->w_b, work)) != AMDG_OK ||
-            (s = alloc_bytes(&op->w_rhs, vec)) != AMDG_OK || (s = alloc_bytes(&op->w_u, vec)) != AMDG_OK ||
+            (s = alloc_bytes(&op->w_u, vec)) != AMDG_OK || (s = alloc_bytes(&op->w_s0, slices)) != AMDG_OK ||
+            (s = alloc_bytes(&op->w_s1, slices)) != AMDG_OK || (s = alloc_bytes(&op->w_slots, slices)) != AMDG_OK ||
             (s = alloc_bytes(reinterpret_cast<void**>(&op->d_u1), vec)) != AMDG_OK ||
             (s = alloc_bytes(reinterpret_cast<void**>(&op->d_rhs64), vec)) != AMDG_OK ||
             (s = alloc_bytes(reinterpret_cast<void**>(&op->d_pred), vec)) != AMDG_OK)
@@ -337,6 +344,35 @@ amdg_status burgers_sync(amdg_burgers_op* op) {
     // the host vectors above are released on return: wait for their copies
     AMDG_CK(cudaStreamSynchronize(st));
     op->built_version = g->version;
+    return AMDG_OK;
+}
+
+// Parent / grandparent table of the current element set (uploaded once per
+// element set) and classifier buffers for E elements of F features (E = 0:
+// the table only).
+amdg_status ensure_features(amdg_burgers_op* op, int64_t E, int F) {
+    amdg_grid* g = op->grid;
+    amdg_status s;
+    if (op->pg_version != g->version) {
+        std::vector<int32_t> pg;
+        parent_table(g->host, &pg);
+        if ((s = upload_grow(op, &op->d_pg, pg, stream_of(op))) != AMDG_OK) return s;
+        AMDG_CK(cudaStreamSynchronize(stream_of(op)));  // pg is released on return
+        op->pg_version = g->version;
+    }
+    if (E > op->feat_cap) {
+        cudaFree(op->d_feat);
+        cudaFree(op->d_prob);
+        op->d_feat = op->d_prob = nullptr;
+        op->feat_cap = 0;
+        const int64_t cap = E + E / 4;
+        void *pf = nullptr, *pp = nullptr;
+        if ((s = alloc_bytes(&pf, size_t(cap) * F * sizeof(float))) != AMDG_OK) return s;
+        op->d_feat = static_cast<float*>(pf);
+        if ((s = alloc_bytes(&pp, size_t(cap) * 3 * sizeof(float))) != AMDG_OK) return s;
+        op->d_prob = static_cast<float*>(pp);
+        op->feat_cap = cap;
+    }
     return AMDG_OK;
 }
 
@@ -372,13 +408,14 @@ amdg_status amdg_burgers_create(amdg_grid* g, const double* alpha, amdg_burgers_
     build_lagr_tables(b, &t);
     std::memcpy(op->weight, t.weight, sizeof(op->weight));
     transform_schedule(dim, &op->sched_dims, &op->sched_lu);
+    build_terms(op);
     amdg_status s;
     if ((s = upload_both(&op->d_a2p, &op->f_a2p, t.a2p)) != AMDG_OK || (s = upload_both(&op->d_lv, &op->f_lv, t.lv)) != AMDG_OK ||
         (s = upload_both(&op->d_lvx, &op->f_lvx, t.lvx)) != AMDG_OK ||
         (s = upload_both(&op->d_lflx, &op->f_lflx, t.lflx)) != AMDG_OK ||
         (s = upload_both(&op->d_ajump, &op->f_ajump, t.ajump)) != AMDG_OK ||
         (s = upload_vec(&op->d_anc_point, t.anc_point)) != AMDG_OK || (s = upload_vec(&op->d_anc_rank, t.anc_rank)) != AMDG_OK ||
-        (s = burgers_sync(op)) != AMDG_OK) {
+        (s = upload_vec(&op->d_terms, op->terms)) != AMDG_OK || (s = burgers_sync(op)) != AMDG_OK) {
         amdg_burgers_destroy(op);
         return s;
     }
@@ -392,9 +429,10 @@ amdg_status amdg_burgers_destroy(amdg_burgers_op* op) {
     if (op->graph_exec) cudaGraphExecDestroy(static_cast<cudaGraphExec_t>(op->graph_exec));
     void* ptrs[] = {op->d_a2p, op->d_lv, op->d_lvx, op->d_lflx, op->d_ajump, op->f_a2p, op->f_lv, op->f_lvx, op->f_lflx,
                     op->f_ajump, op->d_vol_ptr, op->d_vol_nbr, op->d_flx_ptr, op->d_flx_nbr,
-                    op->d_anc, op->d_anc_point, op->d_anc_rank, op->w_up, op->w_fu, op->w_a, op->w_b, op->w_rhs, op->w_u,
+                    op->d_anc, op->d_anc_point, op->d_anc_rank, op->w_up, op->w_fu, op->w_a, op->w_b, op->w_u,
+                    op->w_s0, op->w_s1, op->w_slots, op->d_terms,
                     op->d_u1, op->d_u2, op->d_rhs64, op->d_pred, op->d_vol_split, op->d_flx_split,
-                    op->d_vol_long, op->d_flx_long, op->d_vol_long_elems, op->d_flx_long_elems, op->d_pg,
+                    op->d_pg,
                     op->d_feat, op->d_prob};
     for (void* p : ptrs) cudaFree(p);
     delete op;
@@ -406,6 +444,7 @@ amdg_status amdg_burgers_rhs(amdg_burgers_op* op, const double* d_u, double* d_r
     AMDG_REQUIRE(prec == AMDG_PREC_FP64 || prec == AMDG_PREC_MIXED, AMDG_ERR_ARG, "bad precision");
     AMDG_CK(cudaSetDevice(op->device));
     if (amdg_status rs = burgers_sync(op); rs != AMDG_OK) return rs;
+    op->rhs_evaluations++;
     return eval_rhs(op, d_u, d_rhs, prec);
 }
 
@@ -415,12 +454,12 @@ amdg_status amdg_burgers_point_values(amdg_burgers_op* op, const double* d_u, do
     AMDG_CK(cudaSetDevice(op->device));
     if (amdg_status rs = burgers_sync(op); rs != AMDG_OK) return rs;
     cudaStream_t st = stream_of(op);
-    if (prec == AMDG_PREC_FP64) return eval_point_values<double>(op, mats64(op), d_u, d_up, st);
+    if (prec == AMDG_PREC_FP64) return eval_point_values<double>(op, mats64(op), d_u, d_up, nullptr, st);
     const int64_t n = op->grid->dof, np = op->grid->host.num_elements * op->points;
     float* u32 = static_cast<float*>(op->w_u);
     float* up32 = static_cast<float*>(op->w_up);
     AMDG_CK(launch_convert<double, float>(d_u, u32, n, st));
-    amdg_status r = eval_point_values<float>(op, mats32(op), u32, up32, st);
+    amdg_status r = eval_point_values<float>(op, mats32(op), u32, up32, nullptr, st);
     if (r != AMDG_OK) return r;
     AMDG_CK(launch_convert<float, double>(up32, d_up, np, st));
     op->grid->ctx->launches += 2;
@@ -435,17 +474,17 @@ amdg_status amdg_burgers_flux_coefficients(amdg_burgers_op* op, const double* d_
     cudaStream_t st = stream_of(op);
     const int64_t np = op->grid->host.num_elements * op->points;
     if (prec == AMDG_PREC_FP64) {
-        amdg_status r = eval_point_values<double>(op, mats64(op), d_u, static_cast<double*>(op->w_up), st);
+        amdg_status r = eval_point_values<double>(op, mats64(op), d_u, static_cast<double*>(op->w_up),
+                                                  static_cast<double*>(op->w_a), st);
         if (r != AMDG_OK) return r;
-        if ((r = eval_flux_coefficients<double>(op, static_cast<double*>(op->w_up), st)) != AMDG_OK) return r;
-        AMDG_CK(cudaMemcpyAsync(d_fu, op->w_fu, np * sizeof(double), cudaMemcpyDeviceToDevice, st));
-        return AMDG_OK;
+        return eval_surplus<double, double>(op, d_fu, st);
     }
     float* u32 = static_cast<float*>(op->w_u);
     AMDG_CK(launch_convert<double, float>(d_u, u32, op->grid->dof, st));
-    amdg_status r = eval_point_values<float>(op, mats32(op), u32, static_cast<float*>(op->w_up), st);
+    amdg_status r = eval_point_values<float>(op, mats32(op), u32, static_cast<float*>(op->w_up),
+                                             static_cast<float*>(op->w_a), st);
     if (r != AMDG_OK) return r;
-    if ((r = eval_flux_coefficients<float>(op, static_cast<float*>(op->w_up), st)) != AMDG_OK) return r;
+    if ((r = eval_surplus<float, float>(op, static_cast<float*>(op->w_fu), st)) != AMDG_OK) return r;
     AMDG_CK(launch_convert<float, double>(static_cast<float*>(op->w_fu), d_fu, np, st));
     op->grid->ctx->launches += 2;
     return AMDG_OK;
@@ -457,6 +496,7 @@ amdg_status amdg_burgers_rk3_steps(amdg_burgers_op* op, double dt, int nsteps, a
     AMDG_CK(cudaSetDevice(op->device));
     if (amdg_status rs = burgers_sync(op); rs != AMDG_OK) return rs;
     amdg_grid* g = op->grid;
+    PhaseTimer timer(g->ctx, AMDG_PHASE_RK3);
     cudaStream_t st = stream_of(op);
     if (nsteps == 0) return AMDG_OK;
     const size_t bytes = size_t(g->dof) * sizeof(double);
@@ -464,13 +504,15 @@ amdg_status amdg_burgers_rk3_steps(amdg_burgers_op* op, double dt, int nsteps, a
     auto step = [&]() -> amdg_status {
         AMDG_CK(cudaMemcpyAsync(op->d_u1, g->d_u, bytes, cudaMemcpyDeviceToDevice, st));
         for (int stage = 0; stage < 3; ++stage) {
-            if (amdg_status r = eval_rhs(op, op->d_u1, op->d_rhs64, prec); r != AMDG_OK) return r;
-            AMDG_CK(launch_stage_update(g->d_u, op->d_u1, op->d_rhs64, g->dof, stage_coef(stage, dt), st));
-            g->ctx->launches++;
+            // the last reduction applies the stage update in place (u1 is the stage input)
+            const StageOut so{1, stage_coef(stage, dt), g->d_u, op->d_u1, op->d_u1};
+            if (amdg_status r = eval_rhs(op, op->d_u1, op->d_rhs64, prec, so); r != AMDG_OK) return r;
         }
         AMDG_CK(cudaMemcpyAsync(g->d_u, op->d_u1, bytes, cudaMemcpyDeviceToDevice, st));
         return AMDG_OK;
     };
+    op->rhs_evaluations += 3 * int64_t(nsteps);
+    op->stage_dof_updates += 3 * int64_t(nsteps) * g->dof;
     const bool graph_valid = op->graph_exec && op->graph_version == g->version && op->graph_prec == int(prec) &&
                              op->graph_dt == dt;
     // the launch sequence of a step is fixed for a grid, precision and dt: it is
@@ -538,20 +580,23 @@ amdg_status amdg_burgers_adaptive_step_ex(amdg_burgers_op* op, double cfl, doubl
     AMDG_CK(cudaSetDevice(op->device));
     if (amdg_status rs = burgers_sync(op); rs != AMDG_OK) return rs;
     amdg_grid* g = op->grid;
-    cudaStream_t st = stream_of(op);
+    PhaseTimer timer(g->ctx, AMDG_PHASE_ADAPT_STEP);
     const double dt = adaptive_dt(g, cfl, wave_speed);
     const std::vector<uint64_t> old_keys = g->host.key;
     // predictor: forward Euler into the prediction buffer (ForwardEuler::step_stage)
-    amdg_status s = eval_rhs(op, g->d_u, op->d_rhs64, prec);
+    op->rhs_evaluations++;
+    const StageOut so{1, stage_coef(0, dt), g->d_u, g->d_u, op->d_pred};
+    amdg_status s = eval_rhs(op, g->d_u, op->d_rhs64, prec, so);
     if (s != AMDG_OK) return s;
-    AMDG_CK(cudaMemcpyAsync(op->d_pred, g->d_u, size_t(g->dof) * sizeof(double), cudaMemcpyDeviceToDevice, st));
-    AMDG_CK(launch_stage_update(g->d_u, op->d_pred, op->d_rhs64, g->dof, stage_coef(0, dt), st));
-    g->ctx->launches++;
     // refine on the predicted coefficients; new elements start from zero (DGAdapt::refine, copy_predict_to_ucoe)
     std::vector<double> norms;
     if ((s = grid_norms(g, op->d_pred, &norms)) != AMDG_OK) return s;
     std::vector<uint8_t> refined;
-    std::vector<uint64_t> keys = refine_keys(g->host, norms.data(), eps, &refined);
+    std::vector<uint64_t> keys;
+    {
+        PhaseTimer th(g->ctx, AMDG_PHASE_ADAPT_HOST);
+        keys = refine_keys(g->host, norms.data(), eps, &refined);
+    }
     if (decisions)
         for (size_t e = 0; e < refined.size(); ++e) decisions[e] = refined[e] ? 1 : 0;
     if (int64_t(keys.size()) != g->host.num_elements && (s = grid_set_keys(g, std::move(keys))) != AMDG_OK) return s;
@@ -572,6 +617,7 @@ amdg_status amdg_burgers_features(amdg_burgers_op* op, const double* d_u, float*
     AMDG_CK(cudaSetDevice(op->device));
     if (amdg_status rs = burgers_sync(op); rs != AMDG_OK) return rs;
     const amdg_grid* g = op->grid;
+    if (amdg_status s = ensure_features(op, 0, 0); s != AMDG_OK) return s;
     AMDG_CK(launch_element_features(d_u, op->d_pg, g->host.num_elements, g->host.dim, g->block, d_features, stream_of(op)));
     g->ctx->launches++;
     return AMDG_OK;
@@ -586,6 +632,7 @@ amdg_status amdg_burgers_adaptive_step_learned(amdg_burgers_op* op, amdg_mlp* ml
     AMDG_CK(cudaSetDevice(op->device));
     if (amdg_status rs = burgers_sync(op); rs != AMDG_OK) return rs;
     amdg_grid* g = op->grid;
+    PhaseTimer timer(g->ctx, AMDG_PHASE_ADAPT_STEP);
     cudaStream_t st = stream_of(op);
     const double dt = adaptive_dt(g, cfl, wave_speed);
     const int64_t E = g->host.num_elements;
@@ -596,66 +643,80 @@ amdg_status amdg_burgers_adaptive_step_learned(amdg_burgers_op* op, amdg_mlp* ml
                  "classifier must take " + std::to_string(F) + " features and give 3 classes");
     // 1. the network's refine/keep/coarsen probabilities from the current coefficients
     amdg_status s = AMDG_OK;
-    if (E > op->feat_cap) {
-        cudaFree(op->d_feat);
-        cudaFree(op->d_prob);
-        op->d_feat = op->d_prob = nullptr;
-        op->feat_cap = 0;
-        const int64_t cap = E + E / 4;
-        void *pf = nullptr, *pp = nullptr;
-        if ((s = alloc_bytes(&pf, size_t(cap) * F * sizeof(float))) != AMDG_OK) return s;
-        op->d_feat = static_cast<float*>(pf);
-        if ((s = alloc_bytes(&pp, size_t(cap) * 3 * sizeof(float))) != AMDG_OK) return s;
-        op->d_prob = static_cast<float*>(pp);
-        op->feat_cap = cap;
-    }
-    float* d_feat = op->d_feat;
-    float* d_prob = op->d_prob;
-    AMDG_CK(launch_element_features(g->d_u, op->d_pg, E, g->host.dim, g->block, d_feat, st));
-    g->ctx->launches++;
-    s = amdg_mlp_predict(mlp, d_feat, E, d_prob);
-    if (s != AMDG_OK) return s;
     std::vector<float> prob(size_t(E) * 3);
-    AMDG_CK(cudaMemcpyAsync(prob.data(), d_prob, prob.size() * sizeof(float), cudaMemcpyDeviceToHost, st));
+    {
+        PhaseTimer tc(g->ctx, AMDG_PHASE_CLASSIFIER);
+        if ((s = ensure_features(op, E, F)) != AMDG_OK) return s;
+        AMDG_CK(launch_element_features(g->d_u, op->d_pg, E, g->host.dim, g->block, op->d_feat, st));
+        g->ctx->launches++;
+        if ((s = amdg_mlp_predict(mlp, op->d_feat, E, op->d_prob)) != AMDG_OK) return s;
+        AMDG_CK(cudaMemcpyAsync(prob.data(), op->d_prob, prob.size() * sizeof(float), cudaMemcpyDeviceToHost, st));
+    }
     std::vector<double> norms;
     if ((s = grid_norms(g, g->d_u, &norms)) != AMDG_OK) return s;  // synchronises the stream
-    // 2. pre-adapt: leaves the network marks "refine" get children; where it is
-    //    unsure (max probability < tau) the surplus criterion on the current
-    //    coefficients decides instead
+    // 2. pre-adapt: leaves the network marks "refine" (class 0) get children;
+    //    where it is unsure (max probability < tau) the surplus criterion on
+    //    the current coefficients decides instead; leaves the criterion found
+    //    above eps after the previous step (missed refinements) are refined too
     std::vector<uint8_t> force(E, 0);
     int64_t n_net = 0, n_unsure = 0;
-    for (int64_t e = 0; e < E; ++e) {
-        const float* p = &prob[size_t(e) * 3];
-        const int arg = (p[1] > p[0] && p[1] >= p[2]) ? 1 : (p[2] > p[0] ? 2 : 0);
-        const float pmax = std::max(p[0], std::max(p[1], p[2]));
-        if (pmax < float(tau)) {
-            ++n_unsure;
-            force[e] = norms[e] > eps ? 1 : 0;
-        } else if (arg == 1) {
-            force[e] = 1;
-            ++n_net;
+    {
+        PhaseTimer th(g->ctx, AMDG_PHASE_ADAPT_HOST);
+        for (int64_t e = 0; e < E; ++e) {
+            const float* p = &prob[size_t(e) * 3];
+            int arg = 0;  // classes: 0 refine, 1 keep, 2 coarsen
+            for (int q = 1; q < 3; ++q)
+                if (p[q] > p[arg]) arg = q;
+            if (p[arg] < float(tau)) {
+                ++n_unsure;
+                force[e] = norms[e] > eps ? 1 : 0;
+            } else if (arg == 0) {
+                force[e] = 1;
+                ++n_net;
+            }
         }
+        for (uint64_t k : op->missed_keys) {
+            auto it = std::lower_bound(g->host.key.begin(), g->host.key.end(), k);
+            if (it != g->host.key.end() && *it == k) force[it - g->host.key.begin()] = 1;
+        }
+        std::vector<uint64_t> keys = refine_keys(g->host, norms.data(), eps, nullptr, force.data());
+        if (int64_t(keys.size()) != g->host.num_elements && (s = grid_set_keys(g, std::move(keys))) != AMDG_OK) return s;
     }
-    std::vector<uint64_t> keys = refine_keys(g->host, norms.data(), eps, nullptr, force.data());
-    if (int64_t(keys.size()) != g->host.num_elements && (s = grid_set_keys(g, std::move(keys))) != AMDG_OK) return s;
     // 3. one SSP-RK3 step, no predictor step
     if ((s = amdg_burgers_rk3_steps(op, dt, 1, prec)) != AMDG_OK) return s;
-    // 4. the surplus criterion judges the result: leaves still above eps are missed
-    //    refinements and get their children now; then the usual coarsening
+    // 4. coarsening (amdg_grid_coarsen), then the surplus criterion judges the
+    //    result: leaves still above eps are missed refinements, refined at the
+    //    start of the next step
     if ((s = grid_norms(g, g->d_u, &norms)) != AMDG_OK) return s;
-    std::vector<uint8_t> missed;
-    keys = refine_keys(g->host, norms.data(), eps, &missed);
-    int64_t n_missed = 0;
-    for (uint8_t v : missed) n_missed += v;
-    if (int64_t(keys.size()) != g->host.num_elements && (s = grid_set_keys(g, std::move(keys))) != AMDG_OK) return s;
-    if ((s = amdg_grid_coarsen(g, eta, nullptr)) != AMDG_OK) return s;
+    std::vector<std::pair<uint64_t, double>> above;
+    {
+        PhaseTimer th(g->ctx, AMDG_PHASE_ADAPT_HOST);
+        for (int64_t e = 0; e < g->host.num_elements; ++e)
+            if (norms[e] > eps) above.emplace_back(g->host.key[e], norms[e]);
+        std::vector<uint64_t> keys = coarsen_keys(g->host, norms.data(), eta);
+        if (int64_t(keys.size()) != g->host.num_elements && (s = grid_set_keys(g, std::move(keys))) != AMDG_OK) return s;
+        std::vector<uint8_t> leaf;
+        leaf_flags(g->host, &leaf);
+        op->missed_keys.clear();
+        for (const auto& kv : above) {
+            auto it = std::lower_bound(g->host.key.begin(), g->host.key.end(), kv.first);
+            if (it != g->host.key.end() && *it == kv.first && leaf[it - g->host.key.begin()]) op->missed_keys.push_back(kv.first);
+        }
+    }
     if (dt_out) *dt_out = dt;
     if (stats) {
         stats[0] = n_net;
         stats[1] = n_unsure;
-        stats[2] = n_missed;
+        stats[2] = int64_t(op->missed_keys.size());
         stats[3] = g->host.num_elements;
     }
+    return AMDG_OK;
+}
+
+amdg_status amdg_burgers_counters(const amdg_burgers_op* op, int64_t* stage_dof_updates, int64_t* rhs_evaluations) {
+    AMDG_REQUIRE(op, AMDG_ERR_ARG, "null operator");
+    if (stage_dof_updates) *stage_dof_updates = op->stage_dof_updates;
+    if (rhs_evaluations) *rhs_evaluations = op->rhs_evaluations;
     return AMDG_OK;
 }
 

@@ -61,14 +61,26 @@ void build_grid(int dim, int nmax, int sparse, HostGrid* g, int level_init) {
     for (int64_t e = 0; e < g->num_elements; ++e)
         for (int d = 0; d < dim; ++d)
             g->order[size_t(e) * dim + d] = int32_t((g->key[e] >> (uint64_t(nmax) * (dim - 1 - d))) & mask);
+    build_key_index(g);
 }
 
-int64_t find_element(const HostGrid& g, const int32_t* orders) {
-    const uint64_t key = pack(orders, g.dim, g.nmax);
-    auto it = std::lower_bound(g.key.begin(), g.key.end(), key);
-    if (it == g.key.end() || *it != key) return -1;
-    return int64_t(it - g.key.begin());
+void build_key_index(HostGrid* g) {
+    const int64_t E = g->num_elements;
+    int bits = 4;
+    while ((int64_t(1) << bits) < 2 * E) ++bits;
+    const uint64_t cap = uint64_t(1) << bits, mask = cap - 1;
+    g->hbits = bits;
+    g->hkey.assign(cap, 0);
+    g->hval.assign(cap, -1);
+    for (int64_t e = 0; e < E; ++e) {
+        uint64_t h = (g->key[e] * 0x9E3779B97F4A7C15ull) >> (64 - bits);
+        while (g->hval[h] >= 0) h = (h + 1) & mask;
+        g->hkey[h] = g->key[e];
+        g->hval[h] = int32_t(e);
+    }
 }
+
+int64_t find_element(const HostGrid& g, const int32_t* orders) { return g.index_of(pack(orders, g.dim, g.nmax)); }
 
 // 1D flux-neighbour predicate (Element.cpp:283-348): supports intersect, are
 // adjacent, or are adjacent across the periodic boundary.
@@ -166,19 +178,23 @@ namespace amdg {
 // fibre boundaries.
 static void fibres_along(const HostGrid& g, int t, std::vector<int32_t>* perm, std::vector<int64_t>* start) {
     const uint64_t shift = uint64_t(g.nmax) * (g.dim - 1 - t);
-    const uint64_t mask = (g.nmax == 0 ? 0 : ((uint64_t(1) << g.nmax) - 1)) << shift;
+    const uint64_t field = (g.nmax == 0 ? 0 : ((uint64_t(1) << g.nmax) - 1));
     const int64_t E = g.num_elements;
     perm->resize(E);
-    for (int64_t e = 0; e < E; ++e) (*perm)[e] = int32_t(e);
-    if (t != g.dim - 1) {  // sorted keys are already grouped along the last dimension
-        std::sort(perm->begin(), perm->end(), [&](int32_t a, int32_t b) {
-            const uint64_t fa = g.key[a] & ~mask, fb = g.key[b] & ~mask;
-            return fa != fb ? fa < fb : (g.key[a] & mask) < (g.key[b] & mask);
-        });
+    // sort key: the other dimensions' fields (fibre), then the field of t
+    std::vector<std::pair<uint64_t, int32_t>> ck(E);
+    for (int64_t e = 0; e < E; ++e) {
+        const uint64_t k = g.key[e];
+        const uint64_t high = shift + g.nmax >= 64 ? 0 : k >> (shift + g.nmax);
+        const uint64_t low = k & ((uint64_t(1) << shift) - 1);
+        ck[e] = {(((high << shift) | low) << g.nmax) | ((k >> shift) & field), int32_t(e)};
     }
+    if (t != g.dim - 1) std::sort(ck.begin(), ck.end());  // sorted keys are already grouped along the last dimension
     start->clear();
-    for (int64_t i = 0; i < E; ++i)
-        if (i == 0 || (g.key[(*perm)[i]] & ~mask) != (g.key[(*perm)[i - 1]] & ~mask)) start->push_back(i);
+    for (int64_t i = 0; i < E; ++i) {
+        (*perm)[i] = ck[i].second;
+        if (i == 0 || (ck[i].first >> g.nmax) != (ck[i - 1].first >> g.nmax)) start->push_back(i);
+    }
     start->push_back(E);
 }
 
@@ -186,110 +202,99 @@ void build_transform_topology(const HostGrid& g, TransformTopology* out) {
     const int dim = g.dim, nmax = g.nmax, n1 = 1 << nmax;
     const int64_t one = int64_t(1) << nmax;
     std::vector<int64_t> lo(n1), hi(n1);
-    for (int o = 0; o < n1; ++o) support_units(o, nmax, &lo[o], &hi[o]);
-    auto vol_rel = [&](int o, int oc) { return !((lo[o] >= hi[oc]) || (hi[o] <= lo[oc])); };
-    auto flx_rel = [&](int o, int oc) { return flux_related(lo[o], hi[o], lo[oc], hi[oc], one); };
+    std::vector<int32_t> lev(n1);
+    for (int o = 0; o < n1; ++o) {
+        support_units(o, nmax, &lo[o], &hi[o]);
+        lev[o] = level_of_order(o);
+    }
     const int64_t E = g.num_elements;
     // neighbours of e in dimension t are the members of e's fibre along t whose
-    // 1D supports intersect (vol) or intersect / touch, periodically (flx)
-    std::vector<std::vector<int32_t>> perm(dim);
-    std::vector<std::vector<int64_t>> start(dim);
-    std::vector<int32_t> vcnt(size_t(E) * dim, 0), fcnt(size_t(E) * dim, 0);
+    // 1D supports intersect (vol) or intersect / touch, periodically (flx); one
+    // pass per dimension collects them fibre by fibre, in increasing 1D order
+    // (hence increasing level), then they are laid out element-major
+    struct Rows {
+        std::vector<int32_t> vnbr, fnbr;       // (element, order) pairs
+        std::vector<int32_t> voff, vlen, foff, flen;
+    };
+    std::vector<Rows> rows(dim);
+#pragma omp parallel for schedule(static) if (E >= 256)
     for (int t = 0; t < dim; ++t) {
-        fibres_along(g, t, &perm[t], &start[t]);
-        for (size_t f = 0; f + 1 < start[t].size(); ++f)
-            for (int64_t i = start[t][f]; i < start[t][f + 1]; ++i) {
-                const int32_t e = perm[t][i];
+        std::vector<int32_t> perm;
+        std::vector<int64_t> start;
+        fibres_along(g, t, &perm, &start);
+        Rows& R = rows[t];
+        R.voff.assign(E, 0); R.vlen.assign(E, 0); R.foff.assign(E, 0); R.flen.assign(E, 0);
+        for (size_t f = 0; f + 1 < start.size(); ++f)
+            for (int64_t i = start[f]; i < start[f + 1]; ++i) {
+                const int32_t e = perm[i];
                 const int oe = g.order[size_t(e) * dim + t];
-                int32_t nv = 0, nf = 0;
-                for (int64_t j = start[t][f]; j < start[t][f + 1]; ++j) {
-                    const int os = g.order[size_t(perm[t][j]) * dim + t];
-                    nv += vol_rel(oe, os) ? 1 : 0;
-                    nf += flx_rel(oe, os) ? 1 : 0;
+                const int64_t a0 = lo[oe], b0 = hi[oe];
+                R.voff[e] = int32_t(R.vnbr.size() / 2);
+                R.foff[e] = int32_t(R.fnbr.size() / 2);
+                for (int64_t j = start[f]; j < start[f + 1]; ++j) {
+                    const int32_t s = perm[j];
+                    const int os = g.order[size_t(s) * dim + t];
+                    const int64_t a2 = lo[os], b2 = hi[os];
+                    const bool vol = !((a0 >= b2) || (b0 <= a2));
+                    if (vol) { R.vnbr.push_back(s); R.vnbr.push_back(os); }
+                    if (vol || flux_related(a0, b0, a2, b2, one)) { R.fnbr.push_back(s); R.fnbr.push_back(os); }
                 }
-                vcnt[size_t(e) * dim + t] = nv;
-                fcnt[size_t(e) * dim + t] = nf;
+                R.vlen[e] = int32_t(R.vnbr.size() / 2) - R.voff[e];
+                R.flen[e] = int32_t(R.fnbr.size() / 2) - R.foff[e];
             }
     }
     out->vol_ptr.assign(size_t(E) * dim + 1, 0);
     out->flx_ptr.assign(size_t(E) * dim + 1, 0);
-    for (size_t r = 0; r < size_t(E) * dim; ++r) {
-        out->vol_ptr[r + 1] = out->vol_ptr[r] + vcnt[r];
-        out->flx_ptr[r + 1] = out->flx_ptr[r] + fcnt[r];
-    }
-    out->vol_src.assign(out->vol_ptr.back(), 0);
-    out->vol_lev.assign(out->vol_ptr.back(), 0);
-    out->flx_src.assign(out->flx_ptr.back(), 0);
-    out->flx_lev.assign(out->flx_ptr.back(), 0);
-    out->vol_nbr.assign(size_t(2) * out->vol_ptr.back(), 0);
-    out->flx_nbr.assign(size_t(2) * out->flx_ptr.back(), 0);
-    // neighbours are written in increasing 1D order along t, hence increasing level
-    for (int t = 0; t < dim; ++t)
-        for (size_t f = 0; f + 1 < start[t].size(); ++f)
-            for (int64_t i = start[t][f]; i < start[t][f + 1]; ++i) {
-                const int32_t e = perm[t][i];
-                const int oe = g.order[size_t(e) * dim + t];
-                int32_t pv = out->vol_ptr[size_t(e) * dim + t], pf = out->flx_ptr[size_t(e) * dim + t];
-                for (int64_t j = start[t][f]; j < start[t][f + 1]; ++j) {
-                    const int32_t s = perm[t][j];
-                    const int os = g.order[size_t(s) * dim + t];
-                    if (vol_rel(oe, os)) {
-                        out->vol_src[pv] = s;
-                        out->vol_lev[pv] = level_of_order(os);
-                        out->vol_nbr[2 * size_t(pv)] = s;
-                        out->vol_nbr[2 * size_t(pv) + 1] = os;
-                        ++pv;
-                    }
-                    if (flx_rel(oe, os)) {
-                        out->flx_src[pf] = s;
-                        out->flx_lev[pf] = level_of_order(os);
-                        out->flx_nbr[2 * size_t(pf)] = s;
-                        out->flx_nbr[2 * size_t(pf) + 1] = os;
-                        ++pf;
-                    }
-                }
-            }
-    out->vol_split.assign(size_t(E) * dim, 0);
-    out->flx_split.assign(size_t(E) * dim, 0);
-    out->vol_long.assign(size_t(E) * dim, 0);
-    out->flx_long.assign(size_t(E) * dim, 0);
-    out->vol_long_elems.assign(dim, {});
-    out->flx_long_elems.assign(dim, {});
-    for (int64_t e = 0; e < E; ++e) {
+    for (int64_t e = 0; e < E; ++e)
         for (int t = 0; t < dim; ++t) {
             const size_t r = size_t(e) * dim + t;
+            out->vol_ptr[r + 1] = out->vol_ptr[r] + rows[t].vlen[e];
+            out->flx_ptr[r + 1] = out->flx_ptr[r] + rows[t].flen[e];
+        }
+    out->vol_nbr.resize(size_t(2) * out->vol_ptr.back());
+    out->flx_nbr.resize(size_t(2) * out->flx_ptr.back());
+    out->vol_split.assign(size_t(E) * dim, 0);
+    out->flx_split.assign(size_t(E) * dim, 0);
+#pragma omp parallel for schedule(static) if (E >= 4096)
+    for (int64_t e = 0; e < E; ++e)
+        for (int t = 0; t < dim; ++t) {
+            const size_t r = size_t(e) * dim + t;
+            const Rows& R = rows[t];
+            std::copy(R.vnbr.begin() + 2 * size_t(R.voff[e]), R.vnbr.begin() + 2 * size_t(R.voff[e] + R.vlen[e]),
+                      out->vol_nbr.begin() + 2 * size_t(out->vol_ptr[r]));
+            std::copy(R.fnbr.begin() + 2 * size_t(R.foff[e]), R.fnbr.begin() + 2 * size_t(R.foff[e] + R.flen[e]),
+                      out->flx_nbr.begin() + 2 * size_t(out->flx_ptr[r]));
             // the "U" part (level <= own) is a prefix, the "L" part (finer) the rest
-            const int own = level_of_order(g.order[r]);
+            const int own = lev[g.order[r]];
             int32_t sv = out->vol_ptr[r], sf = out->flx_ptr[r];
-            while (sv < out->vol_ptr[r + 1] && out->vol_lev[sv] <= own) ++sv;
-            while (sf < out->flx_ptr[r + 1] && out->flx_lev[sf] <= own) ++sf;
+            while (sv < out->vol_ptr[r + 1] && lev[out->vol_nbr[2 * size_t(sv) + 1]] <= own) ++sv;
+            while (sf < out->flx_ptr[r + 1] && lev[out->flx_nbr[2 * size_t(sf) + 1]] <= own) ++sf;
             out->vol_split[r] = sv;
             out->flx_split[r] = sf;
-            if (vcnt[r] > kLongRowHost) { out->vol_long[r] = 1; out->vol_long_elems[t].push_back(int32_t(e)); }
-            if (fcnt[r] > kLongRowHost) { out->flx_long[r] = 1; out->flx_long_elems[t].push_back(int32_t(e)); }
         }
-    }
 }
 
 bool build_surplus_ancestors(const HostGrid& g, const LagrTables& t, std::vector<int32_t>* anc) {
     const int dim = g.dim;
     const int64_t E = g.num_elements;
     anc->assign(size_t(E) * dim * 4, -1);
-    std::vector<int32_t> o2(dim);
+    int holes = 0;
+#pragma omp parallel for schedule(static) reduction(+ : holes) if (E >= 4096)
     for (int64_t e = 0; e < E; ++e) {
+        int32_t o2[kMaxDim];
         const int32_t* oe = &g.order[size_t(e) * dim];
         for (int d = 0; d < dim; ++d) {
             if (oe[d] == 0) continue;
-            std::copy(oe, oe + dim, o2.begin());
             for (int ic = 0; ic < 4; ++ic) {
+                std::copy(oe, oe + dim, o2);
                 o2[d] = t.anc_order[size_t(oe[d]) * 4 + ic];
-                const int64_t s = find_element(g, o2.data());
-                if (s < 0) return false;  // the element set has a hole
+                const int64_t s = find_element(g, o2);
+                if (s < 0) ++holes;  // the element set has a hole
                 (*anc)[(size_t(e) * dim + d) * 4 + ic] = int32_t(s);
             }
         }
     }
-    return true;
+    return holes == 0;
 }
 
 }  // namespace amdg

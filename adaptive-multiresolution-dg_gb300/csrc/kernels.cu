@@ -23,10 +23,6 @@ struct IPow { static constexpr int v = B * IPow<B, E - 1>::v; };
 template <int B>
 struct IPow<B, 0> { static constexpr int v = 1; };
 
-__device__ __forceinline__ double rk_combine(double a, double un, double b, double us, double dt, double rhs) {
-    // a*un + b*(us + dt*rhs), each operation rounded (no FMA), as Eigen evaluates it
-    return __dadd_rn(__dmul_rn(a, un), __dmul_rn(b, __dadd_rn(us, __dmul_rn(dt, rhs))));
-}
 
 // ---- FP32-pair (double-float) arithmetic for the mixed-mode stage update ----
 __device__ __forceinline__ void two_sum(float a, float b, float& s, float& e) {

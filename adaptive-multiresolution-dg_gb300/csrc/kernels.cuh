@@ -13,6 +13,13 @@ struct StageCoef {
     double a, b, dt;
 };
 
+#ifdef __CUDACC__
+// a*un + b*(us + dt*rhs), each operation rounded (no FMA), as Eigen evaluates it
+__device__ __forceinline__ double rk_combine(double a, double un, double b, double us, double dt, double rhs) {
+    return __dadd_rn(__dmul_rn(a, un), __dmul_rn(b, __dadd_rn(us, __dmul_rn(dt, rhs))));
+}
+#endif
+
 // Mixed-mode stage state as FP32 (hi, lo) pairs: the stage vectors stay at
 // ~48-bit precision without touching the FP64 pipe (a double->float
 // conversion or an FP64 add costs an FP64-pipe slot, 1/64 of the FP32 rate on

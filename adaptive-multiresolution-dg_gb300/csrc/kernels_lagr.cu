@@ -1,13 +1,16 @@
 // Device kernels of the Lagrange-interpolation path for nonlinear fluxes.
 //
-// fibre_transform: one 1D transform of the fast multi-dimensional algorithm
-// (FastMultiplyLU::transform_1D, FastMultiplyLU.cpp:436-512): for every
-// element e and every entry of its output block,
-//   out[e][idx] (+)= coef * sum_{s in N_t(e), L/U filter} sum_k in[s][idx, dim t <- k] * M[o_t(s)*n_from + k][o_t(e)*n_to + idx_t]
-// where N_t(e) is the vol or flx neighbour list of e in dimension t.  The
-// per-element block shapes follow the partial-sum schedule
-// (series_vec_transform_size, FastMultiplyLU.cpp:596-612).  One thread per
-// output entry; the neighbour list is warp-uniform within an element.
+// A right-hand side is a sum of many independent terms, each a partial sum of
+// dim 1D transforms (FastMultiplyLU::transform_1D, FastMultiplyLU.cpp:436-512):
+// for every element e and every entry of its output block,
+//   out[e][idx] = coef * sum_{s in N_t(e), L/U filter} sum_k in[s][idx, dim t <- k] * M[o_t(s)*n_from + k][o_t(e)*n_to + idx_t]
+// where N_t(e) is the vol or flx neighbour list of e in dimension t.  Instead
+// of one launch per transform, sweep j of every term of a range runs in one
+// launch (thread per term, element and output entry) with each term in its own
+// slice of the work buffer; the last sweep writes one slice per term and a
+// reduction adds the slices in the reference's order (and, for an RK stage,
+// applies the stage update), so a whole right-hand side is about a dozen
+// launches.
 //
 // surplus_pass: pass d of the hierarchical surplus
 // (LagrInterpolation::eval_fp_to_coe_D_Lag, Interplation.cpp:1222-1434).
@@ -39,24 +42,60 @@ __device__ __forceinline__ T fibre_quad(const T* const* x, const T* const* m, in
 }
 
 template <typename T>
-__global__ void __launch_bounds__(256) fibre_transform_kernel(TransformArgs<T> a) {
+__global__ void __launch_bounds__(256) sweep_kernel(SweepArgs<T> a) {
+    const int64_t per = a.num_elements * a.out_block;
     const int64_t gid = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
-    const int64_t total = a.num_elements * a.out_block;
-    if (gid >= total) return;
-    const int64_t e = gid / a.out_block;
-    const int idx = int(gid - e * a.out_block);
-    const int inner = idx % a.stride;
-    const int qt = (idx / a.stride) % a.n_to;
-    const int outer = idx / (a.stride * a.n_to);
-    const int64_t et = e * a.dim + a.t;
-    if (a.long_flag && __ldg(a.long_flag + et)) return;  // done by fibre_transform_long_kernel
-    const int oe = __ldg(a.order + e * a.dim + a.t);
+    if (gid >= per * a.count) return;
+    const int slot = int(gid / per);
+    const int64_t r = gid - int64_t(slot) * per;
+    const int64_t e = r / a.out_block;
+    const int idx = int(r - e * a.out_block);
+    const PartialSum& D = a.desc[a.first + slot];
+    if (D.kind == 1 && a.sweep + 1 < a.dim) return;  // a penalty term is a single (last) sweep
+    int t, lu, flx, n_from, n_to, stride = 1, in_block = 1;
+    const T* M;
+    const T* in;
+    T coef;
+    if (D.kind == 0) {
+        t = D.dims[a.sweep];
+        lu = D.lu[a.sweep];
+        flx = D.flx[a.sweep];
+        M = a.mats[D.mat[a.sweep]];
+        n_from = a.n_in;
+        n_to = a.n_out;
+        coef = a.sweep == 0 ? T(D.coef) : T(1);
+        in = a.in + int64_t(slot) * a.in_slice;
+        // block shape: n_out along the dimensions already transformed, n_in elsewhere
+        int done_after = 0;
+        for (int j = 0; j < a.sweep; ++j) done_after += D.dims[j] > t ? 1 : 0;
+        for (int d = 0; d < a.dim - 1 - t; ++d) stride *= d < done_after ? a.n_out : a.n_in;
+        for (int d = 0; d < a.dim; ++d) in_block *= d < a.sweep ? a.n_out : a.n_in;
+    } else {
+        t = D.dims[0];
+        lu = 1;
+        flx = 1;
+        M = a.mats[kMatAJump];
+        n_from = n_to = a.np;
+        coef = T(D.coef);
+        in = a.pen_in;
+        for (int d = 0; d < a.dim - 1 - t; ++d) stride *= a.np;
+        for (int d = 0; d < a.dim; ++d) in_block *= a.np;
+    }
+    const int inner = idx % stride;
+    const int qt = (idx / stride) % n_to;
+    const int outer = idx / (stride * n_to);
+    const int64_t et = e * a.dim + t;
+    const int32_t* ptr = flx ? a.flx_ptr : a.vol_ptr;
+    const int32_t* split = flx ? a.flx_split : a.vol_split;
+    const int2* nbr = flx ? a.flx_nbr : a.vol_nbr;
+    const int oe = __ldg(a.order + et);
     // "L": neighbours finer than e in dimension t; "U": coarser or equal; neighbours are level-sorted
-    const int beg = a.lu == 0 ? __ldg(a.split + et) : __ldg(a.ptr + et);
-    const int end = a.lu == 2 ? __ldg(a.split + et) : __ldg(a.ptr + et + 1);
-    const T* mcol = a.M + size_t(oe) * a.n_to + qt;
-    const int in_off = outer * a.n_from * a.stride + inner;
-    const size_t mstep = size_t(a.n_from) * a.ncols;
+    const int beg = lu == 0 ? __ldg(split + et) : __ldg(ptr + et);
+    const int end = lu == 2 ? __ldg(split + et) : __ldg(ptr + et + 1);
+    const int ncols = a.n1 * n_to;
+    const T* mcol = M + size_t(oe) * n_to + qt;
+    const int in_off = outer * n_from * stride + inner;
+    const size_t mstep = size_t(n_from) * ncols;
     T acc = T(0);
     // four neighbours per pass: their (element, order) pairs and operands are
     // independent loads issued together; the sum keeps the neighbour order
@@ -64,113 +103,92 @@ __global__ void __launch_bounds__(256) fibre_transform_kernel(TransformArgs<T> a
     for (; i + 4 <= end; i += 4) {
         int2 nb[4];
 #pragma unroll
-        for (int j = 0; j < 4; ++j) nb[j] = __ldg(a.nbr + i + j);
+        for (int j = 0; j < 4; ++j) nb[j] = __ldg(nbr + i + j);
         const T* x[4];
         const T* m[4];
 #pragma unroll
         for (int j = 0; j < 4; ++j) {
-            x[j] = a.in + int64_t(nb[j].x) * a.in_block + in_off;
+            x[j] = in + int64_t(nb[j].x) * in_block + in_off;
             m[j] = mcol + size_t(nb[j].y) * mstep;
         }
-        if (a.n_from == 4) acc = fibre_quad<4>(x, m, a.stride, a.ncols, acc);
-        else if (a.n_from == 3) acc = fibre_quad<3>(x, m, a.stride, a.ncols, acc);
+        if (n_from == 4) acc = fibre_quad<4>(x, m, stride, ncols, acc);
+        else if (n_from == 3) acc = fibre_quad<3>(x, m, stride, ncols, acc);
         else {
 #pragma unroll
             for (int j = 0; j < 4; ++j)
-                for (int k = 0; k < a.n_from; ++k) acc = fma(__ldg(x[j] + k * a.stride), __ldg(m[j] + size_t(k) * a.ncols), acc);
+                for (int k = 0; k < n_from; ++k) acc = fma(__ldg(x[j] + k * stride), __ldg(m[j] + size_t(k) * ncols), acc);
         }
     }
     for (; i < end; ++i) {
-        const int2 nb = __ldg(a.nbr + i);
-        const T* x = a.in + int64_t(nb.x) * a.in_block + in_off;
+        const int2 nb = __ldg(nbr + i);
+        const T* x = in + int64_t(nb.x) * in_block + in_off;
         const T* m = mcol + size_t(nb.y) * mstep;
-        for (int k = 0; k < a.n_from; ++k) acc = fma(__ldg(x + k * a.stride), __ldg(m + size_t(k) * a.ncols), acc);
+        for (int k = 0; k < n_from; ++k) acc = fma(__ldg(x + k * stride), __ldg(m + size_t(k) * ncols), acc);
     }
-    acc *= a.coef;
-    if (a.accumulate) a.out[gid] += acc;
-    else a.out[gid] = acc;
-}
-
-// Long rows (an element at a coarse level of its fibre sees every finer
-// element of the fibre): one warp per output entry, lanes stride over the
-// neighbours, fixed-order shuffle reduction.  Without the split such rows
-// serialise hundreds of dependent neighbour loads in one thread.
-template <typename T>
-__global__ void __launch_bounds__(256) fibre_transform_long_kernel(TransformArgs<T> a) {
-    const int64_t w = (int64_t(blockIdx.x) * blockDim.x + threadIdx.x) / 32;
-    const int lane = threadIdx.x & 31;
-    if (w >= int64_t(a.num_long) * a.out_block) return;
-    const int64_t e = __ldg(a.long_elems + w / a.out_block);
-    const int idx = int(w % a.out_block);
-    const int inner = idx % a.stride;
-    const int qt = (idx / a.stride) % a.n_to;
-    const int outer = idx / (a.stride * a.n_to);
-    const int64_t et = e * a.dim + a.t;
-    const int oe = __ldg(a.order + et);
-    const int beg = a.lu == 0 ? __ldg(a.split + et) : __ldg(a.ptr + et);
-    const int end = a.lu == 2 ? __ldg(a.split + et) : __ldg(a.ptr + et + 1);
-    const T* mcol = a.M + size_t(oe) * a.n_to + qt;
-    const int in_off = outer * a.n_from * a.stride + inner;
-    T acc = T(0);
-    for (int i = beg + lane; i < end; i += 32) {
-        const int2 nb = __ldg(a.nbr + i);
-        const T* x = a.in + int64_t(nb.x) * a.in_block + in_off;
-        const T* m = mcol + size_t(nb.y) * a.n_from * a.ncols;
-        for (int k = 0; k < a.n_from; ++k) acc = fma(__ldg(x + k * a.stride), __ldg(m + size_t(k) * a.ncols), acc);
-    }
-#pragma unroll
-    for (int off = 16; off > 0; off >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, off);
-    if (lane == 0) {
-        acc *= a.coef;
-        const int64_t gid = e * a.out_block + idx;
-        if (a.accumulate) a.out[gid] += acc;
-        else a.out[gid] = acc;
-    }
+    a.out[int64_t(slot) * per + r] = acc * coef;
 }
 
 template <typename T>
-cudaError_t launch_fibre_transform(const TransformArgs<T>& a, cudaStream_t st) {
-    const int64_t total = a.num_elements * a.out_block;
+cudaError_t launch_sweep(const SweepArgs<T>& a, cudaStream_t st) {
+    const int64_t total = a.num_elements * a.out_block * a.count;
     if (total == 0) return cudaSuccess;
-    fibre_transform_kernel<T><<<unsigned((total + 255) / 256), 256, 0, st>>>(a);
-    cudaError_t e = cudaGetLastError();
-    if (e != cudaSuccess || !a.long_flag || a.num_long == 0) return e;
-    const int64_t warps = int64_t(a.num_long) * a.out_block;
-    fibre_transform_long_kernel<T><<<unsigned((warps * 32 + 255) / 256), 256, 0, st>>>(a);
+    sweep_kernel<T><<<unsigned((total + 255) / 256), 256, 0, st>>>(a);
     return cudaGetLastError();
 }
 
-template cudaError_t launch_fibre_transform<double>(const TransformArgs<double>&, cudaStream_t);
-template cudaError_t launch_fibre_transform<float>(const TransformArgs<float>&, cudaStream_t);
+template cudaError_t launch_sweep<double>(const SweepArgs<double>&, cudaStream_t);
+template cudaError_t launch_sweep<float>(const SweepArgs<float>&, cudaStream_t);
 
-// f(u) = u^2/2 at every interpolation point (FluxFunction::burgers_flux_scalar, Interplation.cpp:5070-5073)
 template <typename T>
-__global__ void burgers_flux_kernel(const T* __restrict__ up, T* __restrict__ fp, int64_t n) {
+__global__ void reduce_points_kernel(const T* __restrict__ buf, int count, int64_t n, int first, T* acc, T* fp) {
     const int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
-    if (i < n) {
-        const T u = up[i];
-        fp[i] = u * u * T(0.5);
-    }
+    if (i >= n) return;
+    T v = first ? T(0) : acc[i];
+    for (int s = 0; s < count; ++s) v += buf[int64_t(s) * n + i];
+    if (fp) fp[i] = v * v * T(0.5);  // u^2/2
+    else acc[i] = v;
 }
 
 template <typename T>
-cudaError_t launch_burgers_flux(const T* up, T* fp, int64_t n, cudaStream_t st) {
+cudaError_t launch_reduce_points(const T* buf, int count, int64_t n, int first, T* acc, T* fp, cudaStream_t st) {
     if (n == 0) return cudaSuccess;
-    burgers_flux_kernel<T><<<unsigned((n + 255) / 256), 256, 0, st>>>(up, fp, n);
+    reduce_points_kernel<T><<<unsigned((n + 255) / 256), 256, 0, st>>>(buf, count, n, first, acc, fp);
     return cudaGetLastError();
 }
 
-template cudaError_t launch_burgers_flux<double>(const double*, double*, int64_t, cudaStream_t);
-template cudaError_t launch_burgers_flux<float>(const float*, float*, int64_t, cudaStream_t);
+template cudaError_t launch_reduce_points<double>(const double*, int, int64_t, int, double*, double*, cudaStream_t);
+template cudaError_t launch_reduce_points<float>(const float*, int, int64_t, int, float*, float*, cudaStream_t);
 
 template <typename T>
-__global__ void __launch_bounds__(256) surplus_pass_kernel(SurplusArgs<T> a) {
+__global__ void reduce_rhs_kernel(const T* __restrict__ buf, int count, int64_t n, int first, int last, double* acc,
+                                  StageOut so) {
+    const int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    double v = first ? 0.0 : acc[i];
+    for (int s = 0; s < count; ++s) v += double(buf[int64_t(s) * n + i]);
+    if (last && so.fused) so.out[i] = rk_combine(so.rk.a, so.un[i], so.rk.b, so.us[i], so.rk.dt, v);
+    else acc[i] = v;
+}
+
+template <typename T>
+cudaError_t launch_reduce_rhs(const T* buf, int count, int64_t n, int first, int last, double* acc, StageOut so,
+                              cudaStream_t st) {
+    if (n == 0) return cudaSuccess;
+    reduce_rhs_kernel<T><<<unsigned((n + 255) / 256), 256, 0, st>>>(buf, count, n, first, last, acc, so);
+    return cudaGetLastError();
+}
+
+template cudaError_t launch_reduce_rhs<double>(const double*, int, int64_t, int, int, double*, StageOut, cudaStream_t);
+template cudaError_t launch_reduce_rhs<float>(const float*, int, int64_t, int, int, double*, StageOut, cudaStream_t);
+
+template <typename Ti, typename To>
+__global__ void __launch_bounds__(256) surplus_pass_kernel(SurplusArgs<Ti> a, const Ti* __restrict__ in, To* __restrict__ out) {
     const int64_t gid = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
     const int64_t total = a.num_elements * a.points;
     if (gid >= total) return;
     const int64_t e = gid / a.points;
     const int p = int(gid - e * a.points);
-    T c = a.in[gid];
+    Ti c = in[gid];
     const int od = __ldg(a.order + e * a.dim + a.d);
     if (od != 0) {
         const int pd = (p / a.stride) % 4;
@@ -181,22 +199,23 @@ __global__ void __launch_bounds__(256) surplus_pass_kernel(SurplusArgs<T> a) {
             const int s = __ldg(anc + ic);
             const int q = __ldg(a.anc_point + od * 4 + ic);
             const int r = __ldg(a.anc_rank + od * 4 + ic);
-            c = fma(a.weight[pd * 4 + r], a.in[int64_t(s) * a.points + base + q * a.stride], c);
+            c = fma(Ti(a.weight[pd * 4 + r]), in[int64_t(s) * a.points + base + q * a.stride], c);
         }
     }
-    a.out[gid] = c;
+    out[gid] = To(c);
 }
 
-template <typename T>
-cudaError_t launch_surplus_pass(const SurplusArgs<T>& a, cudaStream_t st) {
+template <typename Ti, typename To>
+cudaError_t launch_surplus_pass(const SurplusArgs<Ti>& a, const Ti* in, To* out, cudaStream_t st) {
     const int64_t total = a.num_elements * a.points;
     if (total == 0) return cudaSuccess;
-    surplus_pass_kernel<T><<<unsigned((total + 255) / 256), 256, 0, st>>>(a);
+    surplus_pass_kernel<Ti, To><<<unsigned((total + 255) / 256), 256, 0, st>>>(a, in, out);
     return cudaGetLastError();
 }
 
-template cudaError_t launch_surplus_pass<double>(const SurplusArgs<double>&, cudaStream_t);
-template cudaError_t launch_surplus_pass<float>(const SurplusArgs<float>&, cudaStream_t);
+template cudaError_t launch_surplus_pass<double, double>(const SurplusArgs<double>&, const double*, double*, cudaStream_t);
+template cudaError_t launch_surplus_pass<double, float>(const SurplusArgs<double>&, const double*, float*, cudaStream_t);
+template cudaError_t launch_surplus_pass<float, float>(const SurplusArgs<float>&, const float*, float*, cudaStream_t);
 
 template <typename Ti, typename To>
 __global__ void convert_kernel(const Ti* __restrict__ in, To* __restrict__ out, int64_t n) {

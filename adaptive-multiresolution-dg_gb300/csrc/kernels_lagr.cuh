@@ -5,33 +5,56 @@
 
 #include <cstdint>
 
+#include "amdg_internal.hpp"
+#include "kernels.cuh"
+
 namespace amdg {
 
+// One sweep over a range of terms: thread per (term, element, output entry).
+// Sweep j of a kind-0 term reads its block shape from the dimensions already
+// transformed (n_out there, n_in elsewhere); sweep 0 reads the shared input,
+// later sweeps the term's own slice of `in`.  Kind-1 terms (only in the last
+// sweep) read pen_in with np entries per dimension.  Output: the term's slice
+// of `out`, overwritten (out[slot][e][idx]).
 template <typename T>
-struct TransformArgs {
-    int dim, t;              // dimensions, transform dimension
-    int n_from, n_to;        // block size in dimension t before / after
-    int stride;              // product of block sizes of the dimensions after t (same in and out)
-    int in_block, out_block; // block sizes (entries per element) of in / out
-    int ncols;               // columns of M (= 1D elements * n_to)
-    int lu;                  // 0 "L" (neighbour level > own), 1 full, 2 "U" (neighbour level <= own)
-    int accumulate;          // 0: out = ..., 1: out += ...
-    T coef;
+struct SweepArgs {
+    int dim, sweep, n_in, n_out, np, n1;
     int64_t num_elements;
-    const T* M;              // [1D elements * n_from][ncols]
-    const int32_t* ptr;      // CSR over (element, dimension)
-    const int2* nbr;         // (element, 1D order along t) per neighbour
-    const int32_t* split;    // [e*dim+t]: first neighbour finer than e in dimension t
-    const int32_t* order;    // [element][dim] 1D orders
+    int first, count;              // terms [first, first + count) of desc
+    const PartialSum* desc;
+    const T* mats[kNumLagrMats];   // [n1 * rows per element][n1 * cols per element]
+    const int32_t *vol_ptr, *vol_split, *flx_ptr, *flx_split;
+    const int2 *vol_nbr, *flx_nbr; // (element, 1D order along t)
+    const int32_t* order;          // [element][dim]
     const T* in;
+    int64_t in_slice;              // entries per term slice of in (0: every term reads the same input)
+    const T* pen_in;               // Alpert coefficients for kind-1 terms
     T* out;
-    const uint8_t* long_flag;   // [e*dim+t]: row handled by the warp-per-output kernel (null: none)
-    const int32_t* long_elems;  // elements with a long row in dimension t
-    int num_long;
+    int out_block;                 // output entries per element (uniform over the range)
 };
 
-// rows longer than this many neighbours are split across a warp
-constexpr int kLongRow = 24;
+template <typename T>
+cudaError_t launch_sweep(const SweepArgs<T>& a, cudaStream_t st);
+
+// Point values: acc = (first ? 0 : acc) + sum_s buf[s] over count slices of n
+// entries (in order); on the last chunk fp = acc^2/2 (Burgers flux
+// FluxFunction::burgers_flux_scalar, Interplation.cpp:5070-5073) instead.
+template <typename T>
+cudaError_t launch_reduce_points(const T* buf, int count, int64_t n, int first, T* acc, T* fp, cudaStream_t st);
+
+// Right-hand side: v = (first ? 0 : acc) + sum_s buf[s] (in order, in FP64);
+// not last: acc = v; last: out = rk_combine(rk, un, us, v) when stage is set,
+// else acc = v.
+struct StageOut {
+    int fused;
+    StageCoef rk;
+    const double* un;
+    const double* us;
+    double* out;
+};
+template <typename T>
+cudaError_t launch_reduce_rhs(const T* buf, int count, int64_t n, int first, int last, double* acc, StageOut so,
+                              cudaStream_t st);
 
 template <typename T>
 struct SurplusArgs {
@@ -41,17 +64,12 @@ struct SurplusArgs {
     const int32_t* anc;          // [element][dim][4]
     const int32_t* anc_point;    // [1D order][4]
     const int32_t* anc_rank;     // [1D order][4]
-    T weight[16];                // [p0][rank]
-    const T* in;
-    T* out;
+    double weight[16];           // [p0][rank]
 };
-
-template <typename T>
-cudaError_t launch_fibre_transform(const TransformArgs<T>& a, cudaStream_t st);
-template <typename T>
-cudaError_t launch_burgers_flux(const T* up, T* fp, int64_t n, cudaStream_t st);
-template <typename T>
-cudaError_t launch_surplus_pass(const SurplusArgs<T>& a, cudaStream_t st);
+// one surplus pass, input and output types may differ (the last pass of the
+// mixed mode writes the FP32 coefficients of the back transforms)
+template <typename Ti, typename To>
+cudaError_t launch_surplus_pass(const SurplusArgs<Ti>& a, const Ti* in, To* out, cudaStream_t st);
 template <typename Ti, typename To>
 cudaError_t launch_convert(const Ti* in, To* out, int64_t n, cudaStream_t st);
 

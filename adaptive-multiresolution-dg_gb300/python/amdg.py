@@ -96,6 +96,11 @@ def load():
         "amdg_grid_coarsen": ([vp, dbl, C.POINTER(i64)], i32),
         "amdg_grid_version": ([vp, C.POINTER(i64)], i32),
         "amdg_grid_l2_error_separable_sum": ([vp, i32, FN1D, vp, dbl, C.POINTER(dbl)], i32),
+        "amdg_grid_eval_tensor": ([vp, i32, vp, vp], i32),
+        "amdg_context_profile": ([vp, i32], i32),
+        "amdg_context_profile_read": ([vp, vp, vp], i32),
+        "amdg_burgers_counters": ([vp, C.POINTER(i64), C.POINTER(i64)], i32),
+        "amdg_grid_error_burgers": ([vp, dbl, dbl, dbl, dbl, i32, vp], i32),
         "amdg_batch_create": ([vp, i32, vp, vp, pp], i32),
         "amdg_batch_destroy": ([vp], i32),
         "amdg_batch_size": ([vp, C.POINTER(i64), C.POINTER(i64), C.POINTER(i64)], i32),
@@ -175,6 +180,19 @@ class Context:
         n = C.c_int64()
         _ck(load().amdg_context_launch_count(self._h, C.byref(n)), "context_launch_count")
         return n.value
+
+    PHASES = ("topology", "set_keys", "norms", "adapt_host", "rhs", "rk3", "classifier", "adapt_step")
+
+    def profile(self, enable: bool = True):
+        """Start (and reset) or stop the host phase profile."""
+        _ck(load().amdg_context_profile(self._h, 1 if enable else 0), "context_profile")
+
+    def profile_read(self) -> dict:
+        """{phase: (wall seconds, calls)} of the host phase profile."""
+        sec = np.zeros(len(self.PHASES))
+        calls = np.zeros(len(self.PHASES), np.int64)
+        _ck(load().amdg_context_profile_read(self._h, _ptr(sec), _ptr(calls)), "context_profile_read")
+        return {p: (float(s), int(c)) for p, s, c in zip(self.PHASES, sec, calls)}
 
     def stage_update(self, stage: int, dt: float, d_un: int, d_u: int, d_rhs: int, n: int):
         _ck(load().amdg_rk3_stage_update(self._h, stage, dt, C.c_void_p(d_un), C.c_void_p(d_u), C.c_void_p(d_rhs), n),
@@ -274,6 +292,17 @@ class Grid:
         _ck(load().amdg_grid_l2_error_separable_sum(self._h, len(funcs), cb, None, l2_norm_exact, C.byref(r)),
             "grid_l2_error_separable_sum")
         return r.value
+
+    def eval_tensor_device(self, x1d, d_out: int):
+        """u_h on the tensor mesh x1d^dim into d_out (device, len(x1d)^dim doubles, last index fastest)."""
+        x = np.ascontiguousarray(x1d, np.float64).reshape(-1)
+        _ck(load().amdg_grid_eval_tensor(self._h, x.size, _ptr(x), C.c_void_p(d_out)), "grid_eval_tensor")
+
+    def error_burgers(self, t: float, a: float = 0.5, b: float = 0.25, c: float = 0.0, gauss_points: int = 1):
+        """(L1, L2, Linf) of u_h - u against the exact Burgers solution from a + b sin(2 pi (sum x + c))."""
+        out = np.zeros(3)
+        _ck(load().amdg_grid_error_burgers(self._h, a, b, c, t, gauss_points, _ptr(out)), "grid_error_burgers")
+        return out
 
     def l2_error_separable(self, func, l2_norm_exact: float) -> float:
         cb = _fn1d([func])
@@ -386,6 +415,12 @@ class BurgersOperator:
                                                       C.byref(dt), _ptr(stats)), "burgers_adaptive_step_learned")
         self.grid._refresh()
         return dt.value, stats
+
+    def counters(self):
+        """(RK-stage DOF updates, right-hand-side evaluations) since creation."""
+        a, b = C.c_int64(), C.c_int64()
+        _ck(load().amdg_burgers_counters(self._h, C.byref(a), C.byref(b)), "burgers_counters")
+        return a.value, b.value
 
     def adaptive_step(self, cfl: float, wave_speed: float, eps: float, eta: float, prec: int = FP64) -> float:
         dt = C.c_double()

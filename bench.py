@@ -252,6 +252,8 @@ def run_ours(args):
     line["burgers3d"] = bench_burgers(ctx, stream, args)
     if args.batch_solves > 0:
         line["batched"] = bench_batched(ctx, stream, args)
+    if args.learn_runs > 0:
+        line["burgers3d_adaptive"] = bench_burgers_adaptive(ctx, stream, args)
     if rank == 0 and world == 1:
         line["cpu_baseline"] = cpu_baseline(g, u0, budget_s=args.cpu_seconds)
     if rank == 0:
@@ -304,6 +306,125 @@ def bench_burgers(ctx, stream, args):
     del ref
     op.close()
     g.close()
+    return out
+
+
+def wave_ic_terms(dim, a, b, c):
+    """a + b sin(2 pi (sum_d x_d + c)) as separable terms."""
+    import amdg_oracle as O
+    terms = [lambda x, d, a=a: a if d == 0 else 1.0]
+    for f in O.sin_sum_terms(dim, shift=-c):
+        terms.append(lambda x, d, f=f, b=b: (b if d == 0 else 1.0) * f(x, d))
+    return terms
+
+
+def bench_burgers_adaptive(ctx, stream, args):
+    """3D adaptive Burgers to T = 0.05 (before the shock): the plain FP64 path
+    (forward-Euler predictor, refine, SSP-RK3, coarsen; the reference's adaptive
+    loop) against mixed precision with the learned refine/coarsen classifier
+    (no predictor: the network pre-adapts the grid, the surplus criterion
+    decides where the network is unsure and judges its missed refinements).
+    DOF-stage updates/s over the whole run (host adaptivity included, wall
+    clock), and each run's L1/L2/Linf error against the exact solution.  The
+    classifier is trained first on the decisions of plain FP64 runs of other
+    seeded waves a + b sin(2 pi (x+y+z+c))."""
+    import torch
+
+    import amdg
+    import amdg_oracle as O
+    dim, nmax, level_init, eps, eta, T, tau = 3, 8, 3, 1e-5, 1e-6, 0.05, 0.8
+    umax = 0.75
+    F = 27 * (1 + 2 * dim)
+    out = {"workload": "3D Burgers, u0 = 0.5 + 0.25 sin(2 pi (x+y+z)), adaptive (refine 1e-5, coarsen 1e-6, "
+                       "max level 8, start level 3), Alpert k=2, Lagrange m=3, LxF alpha 0.825, SSP-RK3, CFL 0.1, "
+                       "to T = 0.05"}
+    # training data from plain FP64 runs of other waves
+    t0 = time.perf_counter()
+    rng = np.random.default_rng(1)
+    feats, labs = [], []
+    for _ in range(args.learn_runs):
+        a, b, c = rng.uniform(0.4, 0.6), rng.uniform(0.15, 0.3), rng.uniform(0.0, 1.0)
+        g = amdg.Grid(ctx, dim, nmax, 2, level_init=level_init)
+        g.init_separable_adaptive(wave_ic_terms(dim, a, b, c), eps)
+        op = amdg.BurgersOperator(g, 1.1 * (a + b))
+        for _s in range(args.learn_steps):
+            buf = torch.empty(g.num_elements * F, dtype=torch.float32, device="cuda")
+            torch.cuda.synchronize()
+            op.features_device(g.device_ptr(), buf.data_ptr())
+            ctx.synchronize()
+            feats.append(buf.cpu().numpy().reshape(-1, F))
+            _dt, dec = op.adaptive_step_ex(CFL, a + b, eps, eta)
+            labs.append(np.where(dec == 1, 0, np.where(dec == 2, 2, 1)).astype(np.int32))
+        op.close()
+        g.close()
+    x, y = np.concatenate(feats), np.concatenate(labs)
+    collect_s = time.perf_counter() - t0
+    dx, dy = torch.from_numpy(x).cuda(), torch.from_numpy(y).cuda()
+    torch.cuda.synchronize()
+    mlp = amdg.MLP(ctx, F, 64, 3, 3, seed=11)
+    t0 = time.perf_counter()
+    loss = mlp.train_device(dx.data_ptr(), dy.data_ptr(), len(y), epochs=args.learn_epochs, batch=256, lr=2e-3,
+                            seed=12)
+    train_s = time.perf_counter() - t0
+    out["training"] = {"runs": args.learn_runs, "steps_per_run": args.learn_steps, "samples": int(len(y)),
+                       "class_counts": [int((y == i).sum()) for i in range(3)], "epochs": args.learn_epochs,
+                       "final_loss": loss, "collect_s": collect_s, "train_s": train_s}
+
+    mesh = (np.arange(48) + 0.5) / 48
+
+    def run(learned, prec, t_end):
+        g = amdg.Grid(ctx, dim, nmax, 2, level_init=level_init)
+        g.init_separable_adaptive(O.burgers_ic_terms(dim), eps)
+        op = amdg.BurgersOperator(g, 1.1 * umax)
+        t, steps, cls = 0.0, 0, np.zeros(3, np.int64)
+        ctx.synchronize()
+        ctx.profile(True)
+        t0 = time.perf_counter()
+        while t < t_end - 1e-12:
+            lv = g.max_mesh_level()
+            dt_full = CFL / sum(umax * 2.0 ** int(m) for m in lv)
+            cfl = CFL if t + dt_full <= t_end else CFL * (t_end - t) / dt_full
+            if learned:
+                dt, st = op.adaptive_step_learned(mlp, cfl, umax, eps, eta, tau, prec)
+                cls += st[:3]
+            else:
+                dt = op.adaptive_step(cfl, umax, eps, eta, prec)
+            t += dt
+            steps += 1
+        ctx.synchronize()
+        wall = time.perf_counter() - t0
+        prof = ctx.profile_read()
+        ctx.profile(False)
+        stage_dof, rhs = op.counters()
+        res = {"value": stage_dof / wall, "wall_s": wall, "steps": steps, "t_end": t,
+               "stage_dof_updates": stage_dof, "rhs_evaluations": rhs, "elements_final": g.num_elements,
+               "dof_final": g.dof,
+               "host_phase_ms": {k: round(v[0] * 1e3, 3) for k, v in prof.items() if v[1]}}
+        if t_end >= T:
+            res["error_vs_exact_l1_l2_linf"] = [float(v) for v in g.error_burgers(t, gauss_points=2)]
+            vals = torch.zeros(len(mesh) ** dim, dtype=torch.float64, device="cuda")
+            torch.cuda.synchronize()
+            g.eval_tensor_device(mesh, vals.data_ptr())
+            ctx.synchronize()
+            res["_mesh_values"] = vals.cpu().numpy()
+        if learned:
+            res["classifier"] = {"net_refine": int(cls[0]), "unsure": int(cls[1]), "missed_refinements": int(cls[2])}
+        op.close()
+        g.close()
+        return res
+
+    for name, learned, prec in (("plain_fp64", False, amdg.FP64), ("mixed_learned", True, amdg.MIXED),
+                                ("mixed_plain", False, amdg.MIXED)):
+        run(learned, prec, 4 * CFL / (umax * dim * 32))  # warm-up: a few steps
+        out[name] = run(learned, prec, T)
+    ref = out["plain_fp64"].pop("_mesh_values")
+    for name in ("mixed_learned", "mixed_plain"):
+        v = out[name].pop("_mesh_values")
+        out[name]["rel_l2_diff_vs_plain_fp64"] = float(np.linalg.norm(v - ref) / np.linalg.norm(ref))
+        out[name]["l2_error_ratio_vs_plain_fp64"] = (out[name]["error_vs_exact_l1_l2_linf"][1] /
+                                                    out["plain_fp64"]["error_vs_exact_l1_l2_linf"][1])
+        out[name]["speedup_vs_plain_fp64"] = out[name]["value"] / out["plain_fp64"]["value"]
+    mlp.close()
     return out
 
 
@@ -436,6 +557,9 @@ def main():
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--batch-solves", type=int, default=256)
     ap.add_argument("--batch-eps", type=float, default=1e-5)
+    ap.add_argument("--learn-runs", type=int, default=4, help="plain runs whose decisions train the classifier (0: skip)")
+    ap.add_argument("--learn-steps", type=int, default=12)
+    ap.add_argument("--learn-epochs", type=int, default=30)
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)

@@ -80,6 +80,24 @@ amdg_status amdg_context_synchronize(amdg_context* ctx);
 /* Number of kernels this context has launched so far. */
 amdg_status amdg_context_launch_count(amdg_context* ctx, int64_t* count);
 
+/* Host phase profile (no counterpart in the reference): wall time spent in the
+ * library's host phases, including the waits on the stream they contain. */
+enum {
+    AMDG_PHASE_TOPOLOGY = 0,   /* neighbour lists / ancestors rebuilt for a new element set, uploads */
+    AMDG_PHASE_SET_KEYS = 1,   /* element set replaced, coefficients carried over */
+    AMDG_PHASE_NORMS = 2,      /* element indicator norms computed and read back */
+    AMDG_PHASE_ADAPT_HOST = 3, /* refine / coarsen / hole filling on the host key set */
+    AMDG_PHASE_RHS = 4,        /* Burgers right-hand sides enqueued */
+    AMDG_PHASE_RK3 = 5,        /* Burgers SSP-RK3 steps enqueued (graph capture included) */
+    AMDG_PHASE_CLASSIFIER = 6, /* learned refine/coarsen: features, network, probabilities read back */
+    AMDG_PHASE_ADAPT_STEP = 7, /* whole adaptive steps (plain or learned) */
+    AMDG_PHASE_COUNT = 8
+};
+/* enable != 0 starts (and resets) the profile, 0 stops it. */
+amdg_status amdg_context_profile(amdg_context* ctx, int enable);
+/* seconds[AMDG_PHASE_COUNT] and calls[AMDG_PHASE_COUNT] (either may be NULL). */
+amdg_status amdg_context_profile_read(const amdg_context* ctx, double* seconds, int64_t* calls);
+
 /* ---- host-side set-up (no device needed) -------------------------------- */
 /* OperatorMatrix1D<AlptBasis,AlptBasis>(all_bas, all_bas, "period")
  * (OperatorMatrix1D.h:125-199): dense 1D matrices of the (2^nmax)(k+1) Alpert
@@ -147,6 +165,26 @@ amdg_status amdg_grid_l2_error_separable(const amdg_grid* g, amdg_fn1d f, void* 
  * (|u - u_h|^2 = |u|^2 + sum u_h^2 - 2 sum_terms <u_h, term>). */
 amdg_status amdg_grid_l2_error_separable_sum(const amdg_grid* g, int nterms, amdg_fn1d f, void* user,
                                              double l2_norm_exact, double* out);
+
+/* Values of the solution on the tensor mesh x1d^dim (x1d: n1 host coordinates,
+ * the same in every dimension): d_out[i_0]...[i_{dim-1}] (device, n1^dim
+ * doubles, last index fastest) = u_h(x1d[i_0], ..., x1d[i_{dim-1}]), summed over
+ * every element whose closed support holds the point (DGSolution::val,
+ * DGSolution.cpp:613-625; Element::val, Element.cpp:123-147).  At most 2^31
+ * points per call. */
+amdg_status amdg_grid_eval_tensor(const amdg_grid* g, int n1, const double* x1d, double* d_out);
+
+/* err[3] = L1, L2, Linf of u_h - u at time t, u the exact solution of
+ * u_t + sum_d (u^2/2)_{x_d} = 0 with u(x,0) = a + b sin(2 pi (sum_d x_d + c)),
+ * by gauss_points (1..10) Gauss-Legendre points per dimension in every cell of
+ * the uniform mesh of the finest element level
+ * (DGSolution::get_error_no_separable_scalar, DGSolution.cpp:326-335;
+ * Quad::norm_multiD, Quad.cpp:261-318; BurgersExact::exact_1d / norm_1d,
+ * ExactSolution.cpp:8-71, with x -> sum_d x_d and t -> dim t).
+ * AMDG_ERR_NONFINITE when the exact solution's Newton iteration fails (past
+ * the shock time). */
+amdg_status amdg_grid_error_burgers(const amdg_grid* g, double a, double b, double c, double t, int gauss_points,
+                                    double* err);
 
 /* ---- linear constant-coefficient operator (HyperbolicAlpt) -------------- */
 /* HyperbolicAlpt::assemble_matrix_scalar (BilinearForm.cpp:691-710): volume
@@ -252,6 +290,11 @@ amdg_status amdg_batch_store(amdg_batch* b, int solve);
 /* Device pointer of the concatenated state and the element offsets (n+1 entries, may be NULL). */
 amdg_status amdg_batch_coefficients_device(amdg_batch* b, double** device_ptr, int64_t* elem_offsets);
 
+/* Work counters since creation: RK-stage DOF updates (3 x DOF per SSP-RK3
+ * step) and right-hand-side evaluations (including adaptive predictors).  No
+ * counterpart in the reference. */
+amdg_status amdg_burgers_counters(const amdg_burgers_op* op, int64_t* stage_dof_updates, int64_t* rhs_evaluations);
+
 /* One adaptive time step of the Burgers solver, the loop body of
  * example/02_hyperbolic_05_burgers_adapt.cpp:223-476 with the Lagrange
  * right-hand side: dt = cfl / sum_d wave_speed 2^maxlevel_d, forward-Euler
@@ -289,13 +332,16 @@ amdg_status amdg_mlp_train(amdg_mlp* m, const float* d_x, const int32_t* d_label
  * parent and grandparent in each dimension, log-scaled (log10(|c| + 1e-20)/20 + 1),
  * (k+1)^dim * (1 + 2 dim) floats per element (device). */
 amdg_status amdg_burgers_features(amdg_burgers_op* op, const double* d_u, float* d_features);
-/* Adaptive step with learned pre-adaptation: the classifier decides which
- * leaves to refine before the step (no forward-Euler predictor); on elements
- * whose largest class probability is below tau the surplus criterion on the
- * current coefficients decides; after the SSP-RK3 step the surplus criterion
- * refines the leaves it still finds above eps (missed refinements), then
- * coarsens as amdg_grid_coarsen.  stats (may be NULL): [refined by the
- * network, uncertain, missed refinements, elements after the step]. */
+/* Adaptive step with learned pre-adaptation: the classifier (3 classes: 0
+ * refine, 1 keep, 2 coarsen, i.e. the decisions 1, 0, 2 of
+ * amdg_burgers_adaptive_step_ex) decides which leaves to refine before the
+ * step (no forward-Euler predictor); on elements whose largest class
+ * probability is below tau the surplus criterion on the current coefficients
+ * decides.  After the SSP-RK3 step the grid is coarsened as amdg_grid_coarsen
+ * and the surplus criterion judges the result: leaves still above eps are
+ * missed refinements, refined at the start of the next learned step.  stats
+ * (may be NULL): [refined by the network, uncertain, missed refinements,
+ * elements after the step]. */
 amdg_status amdg_burgers_adaptive_step_learned(amdg_burgers_op* op, amdg_mlp* mlp, double cfl, double wave_speed,
                                                double eps, double eta, double tau, amdg_precision prec, double* dt_out,
                                                int64_t* stats);

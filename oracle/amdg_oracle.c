@@ -1220,3 +1220,131 @@ int amdg_oracle_burgers_rhs_fast(int dim, int N, int k, int64_t E, const int32_t
     fast_ctx_free(&c);
     return rc;
 }
+
+/* ------------------------------------------------------------------------ */
+/* Point values and quadrature errors against the Burgers exact solution.    */
+/* ------------------------------------------------------------------------ */
+static void elem_support(int level, int suppt, double* lo, double* hi) {
+    if (level <= 1) { *lo = 0.0; *hi = 1.0; return; }
+    const double h = ldexp(1.0, 1 - level);
+    *lo = h * (suppt - 1) / 2.0;
+    *hi = h * (suppt + 1) / 2.0;
+}
+
+static double eval_one(int dim, int k, int64_t E, const int32_t* level, const int32_t* suppt, const double* u,
+                       const double* x) {
+    const int np = k + 1;
+    int B = 1;
+    for (int d = 0; d < dim; ++d) B *= np;
+    double v = 0.0;
+    for (int64_t e = 0; e < E; ++e) {
+        int inside = 1;
+        for (int d = 0; d < dim && inside; ++d) {
+            double lo, hi;
+            elem_support(level[e * dim + d], suppt[e * dim + d], &lo, &hi);
+            if (x[d] < lo || x[d] > hi) inside = 0;
+        }
+        if (!inside) continue;
+        double phi[8][4];
+        for (int d = 0; d < dim; ++d)
+            for (int p = 0; p < np; ++p) phi[d][p] = amdg_oracle_alpert_val(k, level[e * dim + d], suppt[e * dim + d], p, 0, x[d], 0);
+        double ve = 0.0;
+        for (int idx = 0; idx < B; ++idx) {
+            int pd[8], r = idx;
+            for (int d = dim - 1; d >= 0; --d) { pd[d] = r % np; r /= np; }
+            double t = u[e * B + idx];
+            for (int d = 0; d < dim; ++d) t *= phi[d][pd[d]];
+            ve += t;
+        }
+        v += ve;
+    }
+    return v;
+}
+
+int amdg_oracle_eval_points(int dim, int N, int k, int64_t E, const int32_t* level, const int32_t* suppt,
+                            const double* u, int64_t npts, const double* x, double* out) {
+    (void)N;
+    if (dim < 1 || dim > 8 || k < 0 || k > 3) return -1;
+#pragma omp parallel for schedule(static)
+    for (int64_t i = 0; i < npts; ++i) out[i] = eval_one(dim, k, E, level, suppt, u, x + i * dim);
+    return 0;
+}
+
+double amdg_oracle_burgers_wave(double x, double t) {
+    const double pi = 3.14159265358979323846;
+    double xp = fmod(x, 1.0);
+    if (xp < 0) xp = fmod(xp + 1.0, 1.0);
+    if (fabs(xp) < ROUND_OFF || fabs(1 - xp) < ROUND_OFF || fabs(xp - 0.5) < ROUND_OFF) return 0.0;
+    /* odd symmetry v(x) = -v(1 - x) */
+    if (xp < 0.5) return -amdg_oracle_burgers_wave(1 - xp, t);
+    /* initial guess: the first characteristic x0 + sin(2 pi x0) t (x0 from 1 down to 0.5) left of xp */
+    const int n = 100;
+    const double xl = 0.5, xr = 1.0, h = (xr - xl) / n;
+    double u = 0.0;
+    for (int i = 0; i < n; ++i) {
+        const double x0 = xr - i * h;
+        const double xT = x0 + sin(2 * pi * x0) * t;
+        if (xp > xT) { u = sin(2 * pi * x0); break; }
+    }
+    /* Newton on f(u) = u - sin(2 pi (xp - u t)) */
+    double err = 1.0;
+    int iter = 0;
+    while (err > ROUND_OFF) {
+        const double un = u - (u + sin(2 * pi * (u * t - xp))) / (1 + 2 * pi * t * cos(2 * pi * (u * t - xp)));
+        err = fabs(un - u);
+        u = un;
+        if (++iter > 10) return NAN;
+    }
+    return u;
+}
+
+double amdg_oracle_burgers_exact(int dim, const double* x, double a, double b, double c, double t) {
+    double s = 0.0;
+    for (int d = 0; d < dim; ++d) s += x[d];
+    const double T = dim * t;
+    return a + b * amdg_oracle_burgers_wave(s - a * T + c, b * T);
+}
+
+int amdg_oracle_error_burgers(int dim, int N, int k, int64_t E, const int32_t* level, const int32_t* suppt,
+                              const double* u, int gauss, double a, double b, double c, double t, double* err3) {
+    (void)N;
+    if (dim < 1 || dim > 8 || gauss < 1 || gauss > 10) return -1;
+    int qlev = 0;
+    for (int64_t i = 0; i < E * dim; ++i) qlev = level[i] > qlev ? level[i] : qlev;
+    const int64_t n = (int64_t)1 << qlev;
+    const double h = 1.0 / n;
+    double gx[16], gw[16];
+    amdg_oracle_gauss_legendre(gauss, gx, gw);
+    int64_t cells = 1, qn = 1;
+    for (int d = 0; d < dim; ++d) { cells *= n; qn *= gauss; }
+    double l1 = 0.0, l2 = 0.0, linf = 0.0;
+    int bad = 0;
+#pragma omp parallel for schedule(static) reduction(+ : l1, l2, bad) reduction(max : linf)
+    for (int64_t cell = 0; cell < cells; ++cell) {
+        int64_t ci[8], r = cell;
+        for (int d = dim - 1; d >= 0; --d) { ci[d] = r % n; r /= n; }
+        for (int64_t q = 0; q < qn; ++q) {
+            double x[8], w = 1.0;
+            int64_t rq = q;
+            for (int d = dim - 1; d >= 0; --d) {
+                const int qd = (int)(rq % gauss);
+                rq /= gauss;
+                const double tl = ci[d] * h, tr = (ci[d] + 1) * h;
+                x[d] = tl + (gx[qd] + 1.0) * 0.5 * (tr - tl);
+                w *= gw[qd];
+            }
+            const double ex = amdg_oracle_burgers_exact(dim, x, a, b, c, t);
+            if (isnan(ex)) bad += 1;
+            const double f = fabs(eval_one(dim, k, E, level, suppt, u, x) - ex);
+            l1 += w * f;
+            l2 += w * f * f;
+            if (f > linf) linf = f;
+        }
+    }
+    if (bad) return -2;
+    const double s = pow(h / 2.0, dim);
+    err3[0] = l1 * s;
+    err3[1] = sqrt(l2 * s);
+    err3[2] = linf;
+    return 0;
+}

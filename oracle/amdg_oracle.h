@@ -94,6 +94,22 @@ int amdg_oracle_lagr_point_values_fast(int dim, int N, int k, int64_t E, const i
 int amdg_oracle_burgers_rhs_fast(int dim, int N, int k, int64_t E, const int32_t* level, const int32_t* suppt,
                                  const double* fucoe, const double* u, double alpha, double* rhs);
 
+/* ---- point values and quadrature errors ---- */
+/* DGSolution::val (DGSolution.cpp:613-625, Element::val Element.cpp:123-147): the sum over
+ * the elements whose closed support contains x.  x is npts x dim. */
+int amdg_oracle_eval_points(int dim, int N, int k, int64_t E, const int32_t* level, const int32_t* suppt,
+                            const double* u, int64_t npts, const double* x, double* out);
+/* BurgersExact::norm_1d (ExactSolution.cpp:8-66): v(x, t) with v = sin(2 pi (x - v t)); NaN when
+ * Newton's iteration does not converge within 10 steps (the reference exits there). */
+double amdg_oracle_burgers_wave(double x, double t);
+/* a + b v(X - a T + c, b T) with X = sum_d x_d, T = dim t (BurgersExact::exact_1d, ExactSolution.cpp:68-71) */
+double amdg_oracle_burgers_exact(int dim, const double* x, double a, double b, double c, double t);
+/* L1, L2, Linf of u_h - u_exact by `gauss` Gauss-Legendre points per dimension on the uniform
+ * mesh of the finest element level (DGSolution::get_error_no_separable_scalar, DGSolution.cpp:326-335;
+ * Quad::norm_multiD, Quad.cpp:261-318). */
+int amdg_oracle_error_burgers(int dim, int N, int k, int64_t E, const int32_t* level, const int32_t* suppt,
+                              const double* u, int gauss, double a, double b, double c, double t, double* err3);
+
 #ifdef __cplusplus
 }
 #endif

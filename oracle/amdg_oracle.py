@@ -67,6 +67,14 @@ def lib():
         L.amdg_oracle_lagr_point_values_fast.argtypes = [C.c_int, C.c_int, C.c_int, C.c_int64, i32p, i32p, f64p, f64p]
         L.amdg_oracle_burgers_rhs_fast.argtypes = [C.c_int, C.c_int, C.c_int, C.c_int64, i32p, i32p, f64p, f64p,
                                                    C.c_double, f64p]
+        L.amdg_oracle_eval_points.argtypes = [C.c_int, C.c_int, C.c_int, C.c_int64, i32p, i32p, f64p, C.c_int64, f64p,
+                                              f64p]
+        L.amdg_oracle_burgers_wave.restype = C.c_double
+        L.amdg_oracle_burgers_wave.argtypes = [C.c_double, C.c_double]
+        L.amdg_oracle_burgers_exact.restype = C.c_double
+        L.amdg_oracle_burgers_exact.argtypes = [C.c_int, f64p, C.c_double, C.c_double, C.c_double, C.c_double]
+        L.amdg_oracle_error_burgers.argtypes = [C.c_int, C.c_int, C.c_int, C.c_int64, i32p, i32p, f64p, C.c_int,
+                                                C.c_double, C.c_double, C.c_double, C.c_double, f64p]
         _lib = L
     return _lib
 
@@ -174,6 +182,32 @@ def linear_rk3(dim, N, k, level, suppt, c, u, dt, steps, nthreads=0):
 def l2_error_split(dim, N, k, level, suppt, u, coef1d_exact, l2_norm_exact):
     return lib().amdg_oracle_l2_error_split(dim, N, k, level.shape[0], level, suppt, np.ascontiguousarray(u),
                                             np.ascontiguousarray(coef1d_exact), float(l2_norm_exact))
+
+
+def eval_points(dim, N, k, level, suppt, u, x):
+    """DGSolution::val at the rows of x (npts x dim)."""
+    x = np.ascontiguousarray(x, np.float64).reshape(-1, dim)
+    out = np.zeros(len(x))
+    _check(lib().amdg_oracle_eval_points(dim, N, k, len(level), np.ascontiguousarray(level, np.int32),
+                                         np.ascontiguousarray(suppt, np.int32), np.ascontiguousarray(u, np.float64),
+                                         len(x), x, out))
+    return out
+
+
+def burgers_exact(dim, x, a=0.5, b=0.25, c=0.0, t=0.0):
+    """Exact Burgers solution a + b v(sum x - dim a t + c, dim b t) at the rows of x."""
+    x = np.ascontiguousarray(x, np.float64).reshape(-1, dim)
+    f = lib().amdg_oracle_burgers_exact
+    return np.array([f(dim, np.ascontiguousarray(xi), a, b, c, t) for xi in x])
+
+
+def error_burgers(dim, N, k, level, suppt, u, gauss, a=0.5, b=0.25, c=0.0, t=0.0):
+    """(L1, L2, Linf) error against the exact Burgers solution by uniform-mesh Gauss quadrature."""
+    out = np.zeros(3)
+    _check(lib().amdg_oracle_error_burgers(dim, N, k, len(level), np.ascontiguousarray(level, np.int32),
+                                           np.ascontiguousarray(suppt, np.int32), np.ascontiguousarray(u, np.float64),
+                                           gauss, a, b, c, t, out))
+    return out
 
 
 def sin_sum_terms(dim, shift=0.0):

@@ -65,3 +65,30 @@ def test_refine_coarsen_round_trip_and_version(ctx):
     assert g.num_elements == e0
     assert np.array_equal(g.coefficients(), u0)
     g.close()
+
+
+def test_host_phase_profile_counts_adaptive_work(ctx):
+    """Two plain adaptive steps: every step evaluates four right-hand sides
+    (predictor and three stages), reads norms twice, and rebuilds the neighbour
+    lists whenever the element set changed; the profile stops when disabled."""
+    g = amdg.Grid(ctx, 2, 6, 2, level_init=3)
+    g.init_separable_adaptive(O.burgers_ic_terms(2), 1e-4)
+    op = amdg.BurgersOperator(g, 0.825)
+    ctx.synchronize()
+    ctx.profile(True)
+    for _ in range(2):
+        op.adaptive_step(0.1, 0.75, 1e-4, 1e-5)
+    ctx.synchronize()
+    prof = ctx.profile_read()
+    assert prof["adapt_step"][1] == 2
+    assert prof["rhs"][1] == 8
+    assert prof["rk3"][1] == 2
+    assert prof["norms"][1] == 4
+    assert prof["topology"][1] >= 1
+    assert all(v[0] >= 0.0 for v in prof.values())
+    assert prof["adapt_step"][0] >= prof["rk3"][0]
+    ctx.profile(False)
+    op.adaptive_step(0.1, 0.75, 1e-4, 1e-5)
+    assert ctx.profile_read() == {k: (0.0, 0) for k in amdg.Context.PHASES}
+    op.close()
+    g.close()

@@ -113,12 +113,17 @@ def test_learned_adaptivity_gains_over_the_plain_criterion(ctx):
         lv, sp = g.elements()
         keys = O.arrays_to_keys(lv, sp)
         u = g.coefficients().copy()
+        work = op.counters()
         op.close()
         g.close()
-        return sec, keys, u, missed
+        return sec, keys, u, missed, work
 
-    t_plain, k_plain, u_plain, _ = run(False)
-    t_learn, k_learn, u_learn, missed = run(True)
+    t_plain, k_plain, u_plain, _, w_plain = run(False)
+    t_learn, k_learn, u_learn, missed, w_learn = run(True)
+    # one right-hand side fewer per step (no predictor), and the pre-adapted
+    # grids stay close in size to the surplus criterion's
+    assert w_learn[1] == 30 and w_plain[1] == 40
+    assert abs(w_learn[0] - w_plain[0]) <= 0.25 * w_plain[0], (w_learn, w_plain)
     # the learned path skips the predictor's right-hand side (one of four per
     # step); at this size both are bound by host work, so the times are only
     # reported (the bench measures the gain on a 3D grid)

@@ -183,3 +183,40 @@ def test_mlp_oracle_gradient_matches_finite_differences():
         p2[i] -= h
         fd = (O.mlp_loss(p1, dims, x, labels) - O.mlp_loss(p2, dims, x, labels)) / (2 * h)
         assert abs(fd - g[i]) <= 1e-7 + 1e-5 * abs(fd)
+
+
+BURGERS = [n for n, m in manifest().items() if m["kind"] == "burgers"]
+
+
+@pytest.mark.parametrize("name", BURGERS)
+def test_point_values_and_exact_solution_match_reference(name):
+    """DGSolution::val and BurgersExact at the reference's 48 fixed points."""
+    m = manifest()[name]
+    z = golden(name)
+    dim = m["dim"]
+    vals = z["vals"]
+    x = vals[:, :dim]
+    v = O.eval_points(dim, m["N"], 2, z["level"], z["suppt"], z["uT"], x)
+    assert np.abs(v - vals[:, dim]).max() <= 1e-14 * max(1.0, np.abs(vals[:, dim]).max())
+    ex = O.burgers_exact(dim, x, t=m["steps"] * m["dt"])
+    assert np.abs(ex - vals[:, dim + 1]).max() <= 1e-15
+
+
+@pytest.mark.parametrize("name", [n for n in BURGERS if manifest()[n]["N"] <= 4])
+@pytest.mark.parametrize("gauss", [1, 2])
+def test_quadrature_error_matches_reference(name, gauss):
+    """get_error_no_separable_scalar (L1, L2, Linf) against the exact Burgers solution."""
+    m = manifest()[name]
+    z = golden(name)
+    err = O.error_burgers(m["dim"], m["N"], 2, z["level"], z["suppt"], z["uT"], gauss, t=m["steps"] * m["dt"])
+    ref = z[f"normerr_g{gauss}"]
+    assert np.all(np.abs(err - ref) <= 1e-12 * ref)
+
+
+def test_burgers_wave_solves_its_characteristic_equation():
+    """v = sin(2 pi (x - v t)) and the odd symmetry v(x) = -v(1 - x) before the shock time."""
+    rng = np.random.default_rng(3)
+    for x, t in zip(rng.uniform(-2, 3, 64), rng.uniform(0.0, 0.15, 64)):
+        v = O.lib().amdg_oracle_burgers_wave(x, t)
+        assert abs(v - math.sin(2 * math.pi * (x - v * t))) <= 1e-12
+        assert abs(v + O.lib().amdg_oracle_burgers_wave(1 - x, t)) <= 1e-12
