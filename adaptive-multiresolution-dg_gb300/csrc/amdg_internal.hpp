@@ -228,7 +228,7 @@ struct amdg_grid {
 
 struct amdg_linear_op {
     int64_t built_version = -1;      // grid version the topology was built for
-    int64_t capacity = 0;            // dof the stage vectors can hold
+    int64_t capacity = 0;            // dof the stage vectors can hold (a multiple of 4, with 4 spare)
     amdg_grid* grid = nullptr;
     int device = 0;                  // kept so destroy never dereferences grid
     std::vector<double> coef;
@@ -247,8 +247,9 @@ struct amdg_linear_op {
     double* d_u2 = nullptr;
     float* d_shadow = nullptr;       // mixed mode: hi parts of u, u1, u2 (3 x capacity)
     float* d_lo = nullptr;           // mixed mode: lo parts of u, u1, u2 (3 x capacity)
+    int* d_err = nullptr;            // set by a bounded copy wait that gave up (variant 2)
     int variant[2] = {0, 0};         // kernel variant per precision, picked by the autotuner
-    float variant_ms[2][2] = {{0, 0}, {0, 0}};  // measured stage time [precision][variant]
+    float variant_ms[2][3] = {{0, 0, 0}, {0, 0, 0}};  // measured stage time [precision][variant]
 };
 
 struct amdg_burgers_op {

@@ -215,7 +215,19 @@ LinearLaunch linear_launch(const amdg_linear_op* op, amdg_precision prec = AMDG_
     L.pairs = reinterpret_cast<const int2*>(op->d_pairs);
     L.blocks64p = op->d_blocks64p;
     L.blocks32p = op->d_blocks32p;
+    L.err = op->d_err;
     return L;
+}
+
+// A bounded copy wait of the bulk-copy variant gave up: report it and clear the flag.
+amdg_status check_copy_waits(amdg_linear_op* op) {
+    cudaStream_t st = stream_of(op->grid->ctx);
+    int h = 0;
+    AMDG_CK(cudaMemcpyAsync(&h, op->d_err, sizeof(int), cudaMemcpyDeviceToHost, st));
+    AMDG_CK(cudaStreamSynchronize(st));
+    if (h == 0) return AMDG_OK;
+    AMDG_CK(cudaMemsetAsync(op->d_err, 0, sizeof(int), st));
+    return fail(AMDG_ERR_TIMEOUT, "linear stage: a bulk copy did not complete within its wait limit; results are invalid");
 }
 
 amdg_status rk3_steps_device(amdg_linear_op* op, double dt, int nsteps, amdg_precision prec) {
@@ -251,7 +263,7 @@ amdg_status rk3_steps_device(amdg_linear_op* op, double dt, int nsteps, amdg_pre
         }
         AMDG_CK(launch_merge(hi[0], lo[0], g->d_u, g->dof, st));
         g->ctx->launches++;
-        return AMDG_OK;
+        return L.variant == 2 ? check_copy_waits(op) : AMDG_OK;
     }
     for (int s = 0; s < nsteps; ++s) {
         // u1 = u + dt L(u); u2 = 3/4 u + 1/4 (u1 + dt L(u1)); u = 1/3 u + 2/3 (u2 + dt L(u2))
@@ -275,6 +287,7 @@ amdg_status autotune_linear(amdg_linear_op* op) {
     amdg_grid* g = op->grid;
     const int dim = g->host.dim, np = g->host.k + 1;
     const bool col = linear_col_supported(dim, np);
+    const bool tma = linear_tma_supported(dim, np);
     for (int p = 0; p < 2; ++p) op->variant[p] = col ? 1 : 0;
     if (!col || g->dof < 200000) return AMDG_OK;
     cudaStream_t st = stream_of(g->ctx);
@@ -284,7 +297,7 @@ amdg_status autotune_linear(amdg_linear_op* op) {
     AMDG_CK(launch_split(g->d_u, op->d_shadow, op->d_lo, g->dof, st));
     for (int p = 0; p < 2; ++p) {
         float best = 1e30f;
-        for (int v = 0; v < 2; ++v) {
+        for (int v = 0; v < (p == 1 && tma ? 3 : 2); ++v) {
             LinearLaunch L = linear_launch(op);
             L.variant = v;
             const StageCoef rk{1, 0.0, 1.0, 0.0};
@@ -312,7 +325,7 @@ amdg_status autotune_linear(amdg_linear_op* op) {
     }
     cudaEventDestroy(a);
     cudaEventDestroy(b);
-    return AMDG_OK;
+    return tma ? check_copy_waits(op) : AMDG_OK;
 }
 
 // (Re)build the operator's neighbour lists and 1D blocks for the grid's
@@ -359,11 +372,19 @@ amdg_status linear_sync(amdg_linear_op* op) {
         cudaFree(op->d_lo);
         op->d_u1 = op->d_u2 = nullptr;
         op->d_shadow = op->d_lo = nullptr;
-        if ((s = dev_alloc(&op->d_u1, size_t(g->dof))) != AMDG_OK || (s = dev_alloc(&op->d_u2, size_t(g->dof))) != AMDG_OK ||
-            (s = dev_alloc(&op->d_shadow, size_t(g->dof) * 3)) != AMDG_OK ||
-            (s = dev_alloc(&op->d_lo, size_t(g->dof) * 3)) != AMDG_OK)
+        op->capacity = 0;
+        // a multiple of 4 plus 4 spare: the three FP32 arrays start 16-byte
+        // aligned and the bulk copies of their last block stay inside
+        const int64_t cap = (g->dof + 3) / 4 * 4 + 4;
+        if ((s = dev_alloc(&op->d_u1, size_t(cap))) != AMDG_OK || (s = dev_alloc(&op->d_u2, size_t(cap))) != AMDG_OK ||
+            (s = dev_alloc(&op->d_shadow, size_t(cap) * 3)) != AMDG_OK ||
+            (s = dev_alloc(&op->d_lo, size_t(cap) * 3)) != AMDG_OK)
             return s;
-        op->capacity = g->dof;
+        op->capacity = cap;
+    }
+    if (!op->d_err) {
+        if ((s = dev_alloc(&op->d_err, 1)) != AMDG_OK) return s;
+        AMDG_CK(cudaMemsetAsync(op->d_err, 0, sizeof(int), st));
     }
     AMDG_CK(cudaStreamSynchronize(st));
     op->built_version = g->version;
@@ -799,6 +820,7 @@ amdg_status amdg_linear_destroy(amdg_linear_op* op) {
     cudaFree(op->d_blocks32);
     cudaFree(op->d_u1);
     cudaFree(op->d_u2);
+    cudaFree(op->d_err);
     cudaFree(op->d_shadow);
     cudaFree(op->d_lo);
     delete op;
@@ -809,15 +831,17 @@ amdg_status amdg_linear_tuning(const amdg_linear_op* op, int* variants, float* s
     AMDG_REQUIRE(op, AMDG_ERR_ARG, "op is null");
     for (int p = 0; p < 2; ++p) {
         if (variants) variants[p] = op->variant[p];
-        for (int v = 0; v < 2; ++v)
-            if (stage_ms) stage_ms[p * 2 + v] = op->variant_ms[p][v];
+        for (int v = 0; v < 3; ++v)
+            if (stage_ms) stage_ms[p * 3 + v] = op->variant_ms[p][v];
     }
     return AMDG_OK;
 }
 
 amdg_status amdg_linear_set_variant(amdg_linear_op* op, amdg_precision prec, int variant) {
     AMDG_REQUIRE(op && (prec == AMDG_PREC_FP64 || prec == AMDG_PREC_MIXED), AMDG_ERR_ARG, "bad arguments");
-    AMDG_REQUIRE(variant == 0 || (variant == 1 && linear_col_supported(op->grid->host.dim, op->grid->host.k + 1)),
+    const int dim = op->grid->host.dim, np = op->grid->host.k + 1;
+    AMDG_REQUIRE(variant == 0 || (variant == 1 && linear_col_supported(dim, np)) ||
+                     (variant == 2 && prec == AMDG_PREC_MIXED && linear_tma_supported(dim, np)),
                  AMDG_ERR_ARG, "unsupported kernel variant");
     op->variant[prec == AMDG_PREC_MIXED ? 1 : 0] = variant;
     return AMDG_OK;

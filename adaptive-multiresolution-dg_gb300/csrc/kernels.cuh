@@ -33,7 +33,9 @@ struct DFState {
 
 struct LinearLaunch {
     int dim, np;
-    int variant;             // 0: thread per output coefficient; 1: column variant (linear_col_supported)
+    int variant;             // 0: thread per output coefficient; 1: column variant (linear_col_supported);
+                             // 2: column variant fed by bulk asynchronous copies (linear_tma_supported;
+                             //    FP32-pair stage state only, else as 1)
     int64_t num_elements;
     int num_blocks;
     const double* us;        // input coefficients of the stage
@@ -50,6 +52,7 @@ struct LinearLaunch {
     const double* blocks64p;  // column variant: blocks padded to a multiple of 4 entries
     const float* blocks32p;
     DFState df;              // zero-initialised: FP64 epilogue
+    int* err;                // variant 2: set to 1 when a copy wait gives up (device flag)
 };
 
 // Batched solves: concatenated element tables, per-element solve index.
@@ -78,6 +81,9 @@ cudaError_t launch_batch(const BatchLaunch<T, X>& L, cudaStream_t st);
 constexpr int kReduceBlocks = 1216;  // 8 CTAs per SM on 152 SMs
 
 cudaError_t launch_linear(const LinearLaunch& L, bool mixed, StageCoef rk, cudaStream_t st);
+// Variant 2 needs the FP32 stage state with 16-byte aligned array bases and
+// at least 16 bytes readable past the last coefficient.
+bool linear_tma_supported(int dim, int np);
 bool linear_col_supported(int dim, int np);
 // FP64 vector <-> FP32 (hi, lo) pairs
 cudaError_t launch_split(const double* in, float* hi, float* lo, int64_t n, cudaStream_t st);

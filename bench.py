@@ -235,8 +235,9 @@ def run_ours(args):
                        "hbm_frac": ach64 / pk["hbm_gbs"]},
         "roofline": {"bound": "hbm", "achieved": ach32, "peak": pk["hbm_gbs"], "unit": "GB/s",
                      "frac": ach32 / pk["hbm_gbs"], "traffic": None, "peak_kind": pk_kind,
-                     "kernel": ("linear_col_kernel" if op.tuning()[0][1] == 1 else "linear_apply_kernel")
-                               + "<6,3,float,float> (fused RK3 stage, FP32-pair stage state)",
+                     "kernel": {0: "linear_apply_kernel<6,3,float,float>", 1: "linear_col_kernel<6,3,float,float>",
+                                2: "linear_tma_kernel<6,3>"}[op.tuning()[0][1]]
+                               + " (fused RK3 stage, FP32-pair stage state)",
                      "kernel_ms": k32 * 1e3,
                      "algorithmic_bytes_per_launch": bytes_per_launch,
                      "fp32_tflops": flops / k32 / 1e12},
@@ -246,7 +247,8 @@ def run_ours(args):
         "gpu_launches": launches32,
         "autotune": {"variants": {"fp64": op.tuning()[0][0], "mixed": op.tuning()[0][1]},
                      "stage_ms": {"fp64": op.tuning()[1][0], "mixed": op.tuning()[1][1]},
-                     "legend": "variant 0 = thread per output, 1 = column variant"},
+                     "legend": "variant 0 = thread per output, 1 = column variant, "
+                               "2 = column variant fed by bulk asynchronous copies (mixed only)"},
         "clocks": clocks,
     }
     line["burgers3d"] = bench_burgers(ctx, stream, args)

@@ -31,7 +31,7 @@
 extern "C" {
 #endif
 
-#define AMDG_ABI_VERSION 1
+#define AMDG_ABI_VERSION 2
 
 typedef enum amdg_status {
     AMDG_OK = 0,
@@ -198,11 +198,12 @@ amdg_status amdg_linear_destroy(amdg_linear_op* op);
 /* Number of nonzero (element, neighbour, dimension) block pairs and the
  * algorithmic flops of one apply (2 * (k+1)^(dim+1) per pair). */
 amdg_status amdg_linear_stats(const amdg_linear_op* op, int64_t* pairs, double* flops_per_apply);
-/* Kernel variant of the fused linear stage per precision (variants[0] FP64,
- * variants[1] mixed; 0 = one thread per output coefficient, 1 = column
- * variant), chosen when the operator is built by timing both on its grid, and
- * the measured stage times stage_ms[precision*2 + variant] (0 where not
- * timed).  No reference counterpart.  Either pointer may be NULL. */
+/* Kernel variant per precision (variants[0] FP64, variants[1] mixed; 0 = one
+ * thread per output coefficient, 1 = column variant, 2 = column variant whose
+ * neighbour blocks arrive in shared memory by bulk asynchronous copies, mixed
+ * only), chosen when the operator is built by timing the candidates on its
+ * grid, and the measured stage times stage_ms[precision*3 + variant] (0 where
+ * not timed).  No reference counterpart.  Either pointer may be NULL. */
 amdg_status amdg_linear_tuning(const amdg_linear_op* op, int* variants, float* stage_ms);
 /* Override the autotuner's choice (kept until the grid changes). */
 amdg_status amdg_linear_set_variant(amdg_linear_op* op, amdg_precision prec, int variant);

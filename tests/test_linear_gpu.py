@@ -190,3 +190,30 @@ def test_nonfinite_norm_reports_status(ctx):
     with pytest.raises(amdg.AmdgError) as ei:
         g.l2_norm_sq()
     assert ei.value.status == 3
+
+
+def test_kernel_variants_agree_on_mixed_steps(ctx):
+    """The three mixed-precision kernels (thread per output, column, column fed
+    by bulk asynchronous copies) sum in the same order per output, so two SSP-RK3
+    steps agree to rounding of the stage update (1e-14 relative)."""
+    dim, N, k = 4, 6, 2
+    g = amdg.Grid(ctx, dim, N, k)
+    g.init_separable([lambda x, d: math.sin(2 * math.pi * x) + 0.3 * math.cos(6 * math.pi * x)])
+    u0 = g.coefficients().copy()
+    op = amdg.LinearOperator(g, [1.0, -0.5, 0.25, 0.75])
+    out = {}
+    for v in (0, 1, 2):
+        g.set_coefficients(u0)
+        op.rk3_steps(1e-3, 1, amdg.MIXED)  # builds the operator (the autotuner may pick any variant)
+        g.set_coefficients(u0)
+        op.set_variant(amdg.MIXED, v)
+        op.rk3_steps(1e-3, 2, amdg.MIXED)
+        ctx.synchronize()
+        out[v] = g.coefficients().copy()
+    ref = np.abs(out[1]).max()
+    assert np.abs(out[2] - out[1]).max() <= 1e-14 * ref
+    assert np.abs(out[0] - out[1]).max() <= 1e-6 * ref
+    with pytest.raises(amdg.AmdgError):
+        op.set_variant(amdg.FP64, 2)
+    op.close()
+    g.close()
