@@ -234,25 +234,23 @@ static cudaError_t launch_col_t(const LinearLaunch& L, const T* blocks, const X*
 }
 
 // ---- column variant fed by bulk asynchronous copies (mixed precision) --------
-// One CTA of kTmaThreads threads per element, each thread owning up to
-// ceil(C / kTmaThreads) columns of the block along the current dimension.
-// The element's neighbour blocks (all dimensions, in CSR order) stream into a
-// ring of kRing shared-memory slots by cp.async.bulk: slot b has a "full"
-// mbarrier (the producer's expect_tx plus the copy's completion) and an
-// "empty" mbarrier (one arrival per warp once the warp has read the slot);
-// thread 0 refills a slot once all warps released it.  The column reads come
-// from shared memory, so the load/store pipe carries no global traffic for the
-// neighbour values (the copy engine moves them), and each 1D block is loaded
-// once per thread for all of its columns.  A block of B floats starts
-// 16-byte aligned only when its index allows, so the copy takes the aligned
-// superset (at most 12 bytes either side, inside the allocation: the FP32
-// state arrays have 16-byte aligned bases and slack) and the reads skip the
-// (e*B mod 4) leading floats.  Dimensions end with a CTA barrier (the column
-// partition changes), where a failed wait anywhere in the CTA is agreed on.
-// Every wait is bounded (kSpinLimit polls); on a timeout the kernel sets *err,
-// waits (bounded) for its copies still in flight and returns without writing.
-constexpr int kRing = 4;
-constexpr int kTmaThreads = 96;
+// One warp (one CTA) per element; lane l owns the columns c = l + 32 j of the
+// block along the current dimension.  The element's neighbour blocks (all
+// dimensions, in CSR order) stream into a ring of kRing shared-memory slots
+// by cp.async.bulk together with their 1D operator blocks, completion
+// signalled on one mbarrier per slot; lane 0 refills a slot as soon as the
+// warp has read it, so no global load sits on a neighbour's critical path.  The column reads come from
+// shared memory and each 1D block is loaded once per lane for all of its
+// columns, so a neighbour costs the warp a few dozen instructions besides its
+// multiply-adds (the one-thread-per-column variants spend most of their issue
+// slots on per-neighbour overhead).  A block of B floats starts 16-byte
+// aligned only when its index allows, so the copy takes the aligned superset
+// (at most 12 bytes either side, inside the allocation: the FP32 state arrays
+// have 16-byte aligned bases and slack) and the reads skip the (e*B mod 4)
+// leading floats.  Every wait is bounded (kSpinLimit polls) and agreed on by
+// the whole warp; on a timeout the kernel sets *err, waits (bounded) for its
+// copies still in flight and returns without writing.
+constexpr int kRing = 3;
 constexpr uint32_t kSpinLimit = 1u << 22;
 
 __device__ __forceinline__ uint32_t smem_u32(const void* p) { return uint32_t(__cvta_generic_to_shared(p)); }
@@ -263,10 +261,6 @@ __device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
 
 __device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, uint32_t bytes) {
     asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes) : "memory");
-}
-
-__device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
-    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
 }
 
 __device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
@@ -296,56 +290,59 @@ __device__ __forceinline__ void bulk_copy_g2s(void* dst, const void* src, uint32
 }
 
 template <int D, int NP>
-__global__ void __launch_bounds__(kTmaThreads) linear_tma_kernel(const float* __restrict__ xs,
-                                                                 const int32_t* __restrict__ row_ptr,
-                                                                 const int2* __restrict__ pairs,
-                                                                 const float* __restrict__ blocks, int nblocks,
-                                                                 int64_t num_elements, DFState df, int* err) {
+__global__ void __launch_bounds__(32) linear_tma_kernel(const float* __restrict__ xs, const int32_t* __restrict__ row_ptr,
+                                                        const int2* __restrict__ pairs, const float* __restrict__ blocks,
+                                                        int nblocks, int64_t num_elements, DFState df, int* err) {
     constexpr int B = IPow<NP, D>::v;
     constexpr int C = B / NP;
-    constexpr int CPT = (C + kTmaThreads - 1) / kTmaThreads;  // columns per thread
-    constexpr int NW = kTmaThreads / 32;
+    constexpr int CPT = (C + 31) / 32;  // columns per lane
     constexpr int BS = (NP * NP + 3) / 4 * 4;
-    constexpr int SLOT = (B + 3) / 4 * 4 + 4;  // floats: an aligned superset of any block
+    constexpr int DATA = (B + 3) / 4 * 4 + 4;  // floats: an aligned superset of any block
+    constexpr int SLOT = DATA + BS;            // then the 1D operator block
     __shared__ __align__(128) float ring[kRing * SLOT];
     __shared__ float y[B];
     __shared__ __align__(8) uint64_t full[kRing];
-    __shared__ __align__(8) uint64_t empty[kRing];
-    const int tid = threadIdx.x, lane = tid & 31;
+    __shared__ int lead[kRing];                // floats before the block in its slot
+    const int lane = threadIdx.x;
     const int64_t e = blockIdx.x;
     if (e >= num_elements) return;
-    for (int i = tid; i < B; i += kTmaThreads) y[i] = 0.f;
+    for (int i = lane; i < B; i += 32) y[i] = 0.f;
     const int beg = __ldg(row_ptr + e * D), n = __ldg(row_ptr + e * D + D) - beg;
-    if (tid == 0) {
-        for (int b = 0; b < kRing; ++b) {
-            mbar_init(&full[b], 1);
-            mbar_init(&empty[b], NW);
-        }
+    if (lane == 0) {
+        for (int b = 0; b < kRing; ++b) mbar_init(&full[b], 1);
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
-    __syncthreads();
-    auto issue = [&](int k) {  // neighbour k of the element into slot k % kRing (thread 0)
-        const int2 pr = __ldg(pairs + beg + k);
+    __syncwarp();
+    int issued = 0, idim = 0;  // lane 0: neighbours issued, dimension of the next one
+    auto issue = [&]() {       // next neighbour of the element into slot issued % kRing (lane 0)
+        const int kk = issued;
+        while (kk >= __ldg(row_ptr + e * D + idim + 1) - beg) ++idim;
+        const int2 pr = __ldg(pairs + beg + kk);
         const uintptr_t a = reinterpret_cast<uintptr_t>(xs + int64_t(pr.x) * B);
         const uintptr_t a0 = a & ~uintptr_t(15);
         const uint32_t bytes = uint32_t(((a + uintptr_t(B) * 4 + 15) & ~uintptr_t(15)) - a0);
-        uint64_t* fb = &full[k % kRing];
-        mbar_expect_tx(fb, bytes);
-        bulk_copy_g2s(ring + (k % kRing) * SLOT, reinterpret_cast<const void*>(a0), bytes, fb);
+        float* dst = ring + (kk % kRing) * SLOT;
+        lead[kk % kRing] = int((a - a0) / 4);
+        uint64_t* fb = &full[kk % kRing];
+        mbar_expect_tx(fb, bytes + uint32_t(BS * sizeof(float)));
+        bulk_copy_g2s(dst, reinterpret_cast<const void*>(a0), bytes, fb);
+        bulk_copy_g2s(dst + DATA, blocks + (size_t(idim) * nblocks + pr.y) * BS, uint32_t(BS * sizeof(float)), fb);
+        ++issued;
     };
-    int issued = 0, done = 0;  // thread 0: copies issued, neighbours whose copy it saw complete
-    if (tid == 0)
-        for (; issued < n && issued < kRing; ++issued) issue(issued);
+    if (lane == 0)
+        while (issued < n && issued < kRing) issue();
+    __syncwarp();
     bool failed = false;
-    int k = 0;
-    for (int t = 0; t < D; ++t) {
+    int k = 0, slot = 0;
+    uint32_t parity = 0;  // bit b: phase parity of slot b's next completion
+    for (int t = 0; t < D && !failed; ++t) {
         int stride = 1;
 #pragma unroll
         for (int s2 = t + 1; s2 < D; ++s2) stride *= NP;
         int base[CPT];
 #pragma unroll
         for (int j = 0; j < CPT; ++j) {
-            const int c = tid + j * kTmaThreads;
+            const int c = lane + 32 * j;
             base[j] = (c / stride) * stride * NP + c % stride;
         }
         float acc[CPT][NP];
@@ -355,64 +352,61 @@ __global__ void __launch_bounds__(kTmaThreads) linear_tma_kernel(const float* __
             for (int q = 0; q < NP; ++q) acc[j][q] = 0.f;
         const int kend = __ldg(row_ptr + e * D + t + 1) - beg;
         for (; k < kend; ++k) {
-            const int b = k % kRing;
-            const uint32_t use = uint32_t(k / kRing) & 1u;
-            if (!failed && !mbar_wait_bounded(&full[b], use, kSpinLimit)) failed = true;
-            if (tid == 0 && !failed) done = k + 1;
-            if (!failed) {
-                const int2 pr = __ldg(pairs + beg + k);
-                const float* x = ring + b * SLOT + int((int64_t(pr.x) * B) & 3);
-                const float4* m4 = reinterpret_cast<const float4*>(blocks + (size_t(t) * nblocks + pr.y) * BS);
-                float m[BS];
+            const bool ok = mbar_wait_bounded(&full[slot], (parity >> slot) & 1u, kSpinLimit);
+            if (__any_sync(0xffffffffu, !ok)) {
+                failed = true;
+                break;
+            }
+            parity ^= 1u << slot;
+            const float* x = ring + slot * SLOT + lead[slot];
+            const float4* m4 = reinterpret_cast<const float4*>(ring + slot * SLOT + DATA);
+            float m[BS];
 #pragma unroll
-                for (int jj = 0; jj < BS / 4; ++jj) {
-                    const float4 v = __ldg(m4 + jj);
-                    m[4 * jj] = v.x; m[4 * jj + 1] = v.y; m[4 * jj + 2] = v.z; m[4 * jj + 3] = v.w;
-                }
+            for (int jj = 0; jj < BS / 4; ++jj) {
+                const float4 v = m4[jj];
+                m[4 * jj] = v.x; m[4 * jj + 1] = v.y; m[4 * jj + 2] = v.z; m[4 * jj + 3] = v.w;
+            }
 #pragma unroll
-                for (int j = 0; j < CPT; ++j) {
-                    if (tid + j * kTmaThreads < C) {
-                        float xv[NP];
+            for (int j = 0; j < CPT; ++j) {
+                if (C % 32 == 0 || lane + 32 * j < C) {
+                    float xv[NP];
 #pragma unroll
-                        for (int p = 0; p < NP; ++p) xv[p] = x[base[j] + p * stride];
+                    for (int p = 0; p < NP; ++p) xv[p] = x[base[j] + p * stride];
 #pragma unroll
-                        for (int p = 0; p < NP; ++p)
+                    for (int p = 0; p < NP; ++p)
 #pragma unroll
-                            for (int q = 0; q < NP; ++q) acc[j][q] = fmaf(m[p * NP + q], xv[p], acc[j][q]);
-                    }
+                        for (int q = 0; q < NP; ++q) acc[j][q] = fmaf(m[p * NP + q], xv[p], acc[j][q]);
                 }
             }
-            __syncwarp();
-            if (lane == 0 && !failed) mbar_arrive(&empty[b]);  // this warp is done with slot b
-            if (tid == 0 && !failed && k + kRing < n) {
-                // refill slot b once every warp released it
-                if (!mbar_wait_bounded(&empty[b], use, kSpinLimit)) {
-                    failed = true;
-                } else {
-                    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-                    issue(k + kRing);
-                    ++issued;
-                }
+            __syncwarp();  // the warp has read slot `slot`
+            if (lane == 0 && issued < n) {
+                asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+                issue();
             }
+            __syncwarp();  // lead[] of the refilled slot is written before any lane reads it
+            slot = slot + 1 == kRing ? 0 : slot + 1;
         }
+        if (failed) break;
 #pragma unroll
         for (int j = 0; j < CPT; ++j)
-            if (!failed && tid + j * kTmaThreads < C)
+            if (C % 32 == 0 || lane + 32 * j < C)
 #pragma unroll
                 for (int q = 0; q < NP; ++q) y[base[j] + q * stride] += acc[j][q];
-        failed = __syncthreads_or(failed ? 1 : 0) != 0;  // next dimension: another column partition
-        if (failed) break;
+        __syncwarp();  // next dimension: another column partition
     }
     if (failed) {
-        if (tid == 0) {
+        if (lane == 0) {
             atomicExch(err, 1);
             // let the copies still in flight land before the CTA's shared memory is released
-            for (int k2 = done; k2 < issued; ++k2)
-                mbar_wait_bounded(&full[k2 % kRing], uint32_t(k2 / kRing) & 1u, 1u << 16);
+            for (int k2 = k; k2 < issued; ++k2) {
+                const int s2 = k2 % kRing;
+                mbar_wait_bounded(&full[s2], (parity >> s2) & 1u, 1u << 16);
+                parity ^= 1u << s2;
+            }
         }
         return;
     }
-    for (int i = tid; i < B; i += kTmaThreads) df_stage_update(df, e * B + i, y[i]);
+    for (int i = lane; i < B; i += 32) df_stage_update(df, e * B + i, y[i]);
 }
 
 template <int D, int NP>
@@ -422,8 +416,8 @@ static cudaError_t launch_tma_t(const LinearLaunch& L, cudaStream_t st) {
         return cudaErrorInvalidValue;
     } else {
         if (L.num_elements == 0) return cudaSuccess;
-        linear_tma_kernel<D, NP><<<unsigned(L.num_elements), kTmaThreads, 0, st>>>(
-            L.us_shadow, L.row_ptr, L.pairs, L.blocks32p, L.num_blocks, L.num_elements, L.df, L.err);
+        linear_tma_kernel<D, NP><<<unsigned(L.num_elements), 32, 0, st>>>(L.us_shadow, L.row_ptr, L.pairs, L.blocks32p,
+                                                                          L.num_blocks, L.num_elements, L.df, L.err);
         return cudaGetLastError();
     }
 }
@@ -432,7 +426,7 @@ bool linear_tma_supported(int dim, int np) {
     int B = 1;
     for (int d = 0; d < dim; ++d) B *= np;
     // the ring, the accumulator and the mbarriers must fit the static shared-memory limit (48 KB)
-    return B / np <= 256 && size_t(kRing * ((B + 3) / 4 * 4 + 4) + B) * sizeof(float) + 256 <= 48 * 1024;
+    return B / np <= 256 && size_t(kRing * ((B + 3) / 4 * 4 + 4 + 16) + B) * sizeof(float) + 256 <= 48 * 1024;
 }
 
 bool linear_col_supported(int dim, int np) {
