@@ -34,6 +34,9 @@ sys.path.insert(0, os.path.join(ROOT, "oracle"))
 DIM, NMAX, K = 6, 8, 2
 COEF = [1.0] * DIM
 CFL = 0.1
+# DRAM bytes of one mixed stage launch of the 6D N=8 workload, per kernel variant, from ncu
+# (dram__bytes_read.sum + dram__bytes_write.sum; variant 0 was not captured)
+NCU_TRAFFIC_BYTES = {1: (720.902 + 241.610) * 1e6, 2: (441.883 + 238.190) * 1e6}
 METRIC = "DOF-stage updates/s at matched L2 error: plain FP64 vs mixed+learned-adapt"
 WORKLOAD = "6D linear advection, sparse grid N=8, Alpert k=2, SSP-RK3 (34,455,456 DOF)"
 
@@ -234,7 +237,9 @@ def run_ours(args):
                        "fp64_frac": flops / k64 / 1e12 / fp64_peak,
                        "hbm_frac": ach64 / pk["hbm_gbs"]},
         "roofline": {"bound": "hbm", "achieved": ach32, "peak": pk["hbm_gbs"], "unit": "GB/s",
-                     "frac": ach32 / pk["hbm_gbs"], "traffic": None, "peak_kind": pk_kind,
+                     "frac": ach32 / pk["hbm_gbs"], "traffic": NCU_TRAFFIC_BYTES.get(op.tuning()[0][1]),
+                     "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum of one launch of this "
+                                       "workload's stage kernel (bytes)", "peak_kind": pk_kind,
                      "kernel": {0: "linear_apply_kernel<6,3,float,float>", 1: "linear_col_kernel<6,3,float,float>",
                                 2: "linear_tma_kernel<6,3>"}[op.tuning()[0][1]]
                                + " (fused RK3 stage, FP32-pair stage state)",
