@@ -1152,8 +1152,11 @@ static int fast_partial_sums(const fast_ctx* c, const double* in, int n_in, int 
     return 0;
 }
 
-/* Alpert basis at Lagrange points, rows = Alpert basis, cols = Lagrange point (Interplation.cpp:16-101) */
-static double* alpt_at_lagr_points(int N, int k) {
+/* Alpert basis (deriv = 0) or its derivative (deriv = 1) at Lagrange points, rows = Alpert basis,
+ * cols = Lagrange point (Lag_pt_Alpt_1D / Lag_pt_Alpt_1D_d1, Interplation.cpp:16-101) */
+static double* alpt_at_lagr_points_d(int N, int k, int deriv);
+static double* alpt_at_lagr_points(int N, int k) { return alpt_at_lagr_points_d(N, k, 0); }
+static double* alpt_at_lagr_points_d(int N, int k, int deriv) {
     const int np = k + 1, n1 = 1 << N, na = n1 * np, nl = n1 * 4;
     double* m = (double*)calloc((size_t)na * nl, sizeof(double));
     for (int c = 0; c < nl; ++c) {
@@ -1162,7 +1165,7 @@ static double* alpt_at_lagr_points(int N, int k) {
         for (int r = 0; r < na; ++r) {
             const elem1d ea = elem_of_order(r / np);
             if (x < support_lo(ea.n, ea.j) || x > support_hi(ea.n, ea.j)) continue;
-            m[(size_t)r * nl + c] = amdg_oracle_alpert_val(k, ea.n, ea.j, r % np, 0, x, 0);
+            m[(size_t)r * nl + c] = amdg_oracle_alpert_val(k, ea.n, ea.j, r % np, deriv, x, 0);
         }
     }
     return m;
@@ -1347,4 +1350,149 @@ int amdg_oracle_error_burgers(int dim, int N, int k, int64_t E, const int32_t* l
     err3[1] = sqrt(l2 * s);
     err3[2] = linf;
     return 0;
+}
+
+/* ------------------------------------------------------------------------ */
+/* Wave equation u_tt = div(K(x) grad u), K = (1 + 0.5 prod_d sin(2 pi x_d))^2,  */
+/* periodic: DiffusionRHS with Lagrange-interpolated K u_x and K u            */
+/* (03_wave_06_var_coeff_adapt.cpp:154-245; Interplation.cpp:527-577,         */
+/* 648-698, 4159-4212; FastMultiplyLU.cpp:1691-1765) plus the IPDG jump        */
+/* penalty -sigma/dx [u][v] (BilinearForm.cpp:920-929).                       */
+/* ------------------------------------------------------------------------ */
+
+/* sum over the discontinuity points of u (lo, mid, hi of u's support; 0 and 1/2 at levels
+ * 0 and 1, periodic) of u(x^su) v'(x^sv) (Basis::product_edge_dis_u, Basis.cpp:175-230) */
+static double gproduct_edge_dis_u(int tu, int tv, int k, elem1d u, int pu, elem1d v, int pv, int su, int sv, int dv) {
+    const double pts[3] = {support_lo(u.n, u.j), 0.5 * (support_lo(u.n, u.j) + support_hi(u.n, u.j)), support_hi(u.n, u.j)};
+    double s = 0.0;
+    for (int i = 0; i < 3; ++i) {
+        if (u.n <= 1 && i == 2) continue;
+        const double x = pts[i];
+        double fu = basis_val(tu, k, u.n, u.j, pu, 0, x, su), fv = basis_val(tv, k, v.n, v.j, pv, dv, x, sv);
+        if (fabs(x) < ROUND_OFF) {
+            if (su == -1) fu = basis_val(tu, k, u.n, u.j, pu, 0, 1.0, su);
+            if (sv == -1) fv = basis_val(tv, k, v.n, v.j, pv, dv, 1.0, sv);
+        } else if (fabs(x - 1.0) < ROUND_OFF) {
+            if (su == 1) fu = basis_val(tu, k, u.n, u.j, pu, 0, 0.0, su);
+            if (sv == 1) fv = basis_val(tv, k, v.n, v.j, pv, dv, 0.0, sv);
+        }
+        s += fu * fv;
+    }
+    return s;
+}
+
+/* Lagrange (rows) x Alpert (cols): ujp_vxlft + ujp_vxrgt, [u] times the one-sided v_x
+ * (OperatorMatrix1D.h:206-211) */
+int amdg_oracle_oper1d_lagr_ujp_vx(int N, int k, double* ujp_vxave) {
+    const int nr = (1 << N) * 4, nc = (1 << N) * (k + 1);
+#pragma omp parallel for schedule(dynamic)
+    for (int r = 0; r < nr; ++r) {
+        const elem1d u = elem_of_order(r / 4);
+        const int pu = r % 4;
+        for (int c = 0; c < nc; ++c) {
+            const elem1d v = elem_of_order(c / (k + 1));
+            const int pv = c % (k + 1);
+            const double ur_vxr = gproduct_edge_dis_u(1, 0, k, u, pu, v, pv, 1, 1, 1);
+            const double ul_vxr = gproduct_edge_dis_u(1, 0, k, u, pu, v, pv, -1, 1, 1);
+            const double ur_vxl = gproduct_edge_dis_u(1, 0, k, u, pu, v, pv, 1, -1, 1);
+            const double ul_vxl = gproduct_edge_dis_u(1, 0, k, u, pu, v, pv, -1, -1, 1);
+            const double lft = ur_vxl - ul_vxl, rgt = ur_vxr - ul_vxr;
+            ujp_vxave[(size_t)r * nc + c] = lft + rgt;
+        }
+    }
+    return 0;
+}
+
+double amdg_oracle_wave_coef(int dim, const double* x) {
+    const double pi = 3.14159265358979323846;
+    double s = 1.0;
+    for (int d = 0; d < dim; ++d) s *= sin(2 * pi * x[d]);
+    const double c = 1.0 + 0.5 * s;
+    return c * c;
+}
+
+/* K at every interpolation point times the given point values, then the surplus */
+static int wave_coef_surplus(int dim, int N, int64_t E, const int32_t* level, const int32_t* suppt, double* up, double* fucoe) {
+    const int P = ipow(4, dim);
+#pragma omp parallel for schedule(static)
+    for (int64_t e = 0; e < E; ++e)
+        for (int p = 0; p < P; ++p) {
+            double x[16];
+            int r = p;
+            for (int d = dim - 1; d >= 0; --d) {
+                x[d] = amdg_oracle_lagr_point(level[e * dim + d], suppt[e * dim + d], r % 4);
+                r /= 4;
+            }
+            up[e * P + p] = amdg_oracle_wave_coef(dim, x) * up[e * P + p];
+        }
+    return amdg_oracle_lagr_surplus(dim, N, E, level, suppt, up, fucoe);
+}
+
+int amdg_oracle_wave_rhs_fast(int dim, int N, int k, int64_t E, const int32_t* level, const int32_t* suppt,
+                              const double* u, double sigma, double* rhs) {
+    const int np = k + 1, n1 = 1 << N, nr = n1 * 4, nc = n1 * np;
+    const int B = ipow(np, dim), P = ipow(4, dim);
+    fast_ctx c;
+    if (fast_ctx_init(&c, dim, N, E, level, suppt)) return -2;
+    double* a2p = alpt_at_lagr_points_d(N, k, 0);
+    double* a2pd = alpt_at_lagr_points_d(N, k, 1);
+    double* Lv = (double*)malloc((size_t)nr * nc * sizeof(double));
+    double* Lvx = (double*)malloc((size_t)nr * nc * sizeof(double));
+    double* Lf = (double*)malloc((size_t)nr * nc * sizeof(double));
+    double* Lj = (double*)malloc((size_t)nr * nc * sizeof(double));
+    double* ul = (double*)malloc((size_t)nc * nc * sizeof(double));
+    double* ur = (double*)malloc((size_t)nc * nc * sizeof(double));
+    double* up = (double*)malloc((size_t)E * P * sizeof(double));
+    double* fg = (double*)malloc((size_t)dim * E * P * sizeof(double));
+    double* fu = (double*)malloc((size_t)E * P * sizeof(double));
+    if (!a2p || !a2pd || !Lv || !Lvx || !Lf || !Lj || !ul || !ur || !up || !fg || !fu) return -2;
+    amdg_oracle_oper1d_lagr(N, k, Lv, Lvx, Lf);
+    amdg_oracle_oper1d_lagr_ujp_vx(N, k, Lj);
+    amdg_oracle_oper1d(N, k, NULL, NULL, ul, ur);
+    for (size_t i = 0; i < (size_t)nc * nc; ++i) ur[i] = ur[i] - ul[i]; /* ujp_vjp */
+    int rc = 0;
+    const double* M[16] = {0};
+    int flx[16] = {0};
+    /* K u_{x_d} at the points and its interpolation coefficients, per d */
+    for (int d = 0; d < dim && !rc; ++d) {
+        for (int s = 0; s < dim; ++s) { M[s] = (s == d) ? a2pd : a2p; flx[s] = 0; }
+        memset(up, 0, (size_t)E * P * sizeof(double));
+        rc = fast_partial_sums(&c, u, np, 4, M, flx, 1.0, up);
+        if (!rc) rc = wave_coef_surplus(dim, N, E, level, suppt, up, fg + (size_t)d * E * P);
+    }
+    /* K u at the points */
+    if (!rc) {
+        for (int s = 0; s < dim; ++s) { M[s] = a2p; flx[s] = 0; }
+        memset(up, 0, (size_t)E * P * sizeof(double));
+        rc = fast_partial_sums(&c, u, np, 4, M, flx, 1.0, up);
+        if (!rc) rc = wave_coef_surplus(dim, N, E, level, suppt, up, fu);
+    }
+    memset(rhs, 0, (size_t)E * B * sizeof(double));
+    /* rhs_flx_gradu: -{K u_x}[v] (uave_vjp = (ulft + urgt)_vjp / 2) */
+    for (int d = 0; d < dim && !rc; ++d) {
+        for (int s = 0; s < dim; ++s) { M[s] = (s == d) ? Lf : Lv; flx[s] = (s == d); }
+        rc = fast_partial_sums(&c, fg + (size_t)d * E * P, 4, np, M, flx, -0.5, rhs);
+    }
+    /* rhs_vol: -K u_x v_x */
+    for (int d = 0; d < dim && !rc; ++d) {
+        for (int s = 0; s < dim; ++s) { M[s] = (s == d) ? Lvx : Lv; flx[s] = 0; }
+        rc = fast_partial_sums(&c, fg + (size_t)d * E * P, 4, np, M, flx, -1.0, rhs);
+    }
+    /* rhs_flx_u: -1/2 [K u] (v_x^- + v_x^+) */
+    for (int d = 0; d < dim && !rc; ++d) {
+        for (int s = 0; s < dim; ++s) { M[s] = (s == d) ? Lj : Lv; flx[s] = (s == d); }
+        rc = fast_partial_sums(&c, fu, 4, np, M, flx, -0.5, rhs);
+    }
+    /* IPDG: -sigma/dx [u][v], dx the finest element size */
+    int maxl = 0;
+    for (int64_t i = 0; i < E * dim; ++i) maxl = level[i] > maxl ? level[i] : maxl;
+    const double dx = 1.0 / pow(2.0, maxl);
+    for (int d = 0; d < dim && !rc; ++d) {
+        int from[16];
+        for (int s = 0; s < dim; ++s) from[s] = np;
+        fast_transform_1d(&c, u, from, rhs, from, d, ur, nc, 1, 1, -sigma / dx, 1);
+    }
+    free(a2p); free(a2pd); free(Lv); free(Lvx); free(Lf); free(Lj); free(ul); free(ur); free(up); free(fg); free(fu);
+    fast_ctx_free(&c);
+    return rc;
 }

@@ -75,6 +75,9 @@ def lib():
         L.amdg_oracle_burgers_exact.argtypes = [C.c_int, f64p, C.c_double, C.c_double, C.c_double, C.c_double]
         L.amdg_oracle_error_burgers.argtypes = [C.c_int, C.c_int, C.c_int, C.c_int64, i32p, i32p, f64p, C.c_int,
                                                 C.c_double, C.c_double, C.c_double, C.c_double, f64p]
+        L.amdg_oracle_wave_rhs_fast.argtypes = [C.c_int, C.c_int, C.c_int, C.c_int64, i32p, i32p, f64p, C.c_double, f64p]
+        L.amdg_oracle_wave_coef.restype = C.c_double
+        L.amdg_oracle_wave_coef.argtypes = [C.c_int, f64p]
         _lib = L
     return _lib
 
@@ -208,6 +211,43 @@ def error_burgers(dim, N, k, level, suppt, u, gauss, a=0.5, b=0.25, c=0.0, t=0.0
                                            np.ascontiguousarray(suppt, np.int32), np.ascontiguousarray(u, np.float64),
                                            gauss, a, b, c, t, out))
     return out
+
+
+def wave_rhs(dim, N, k, level, suppt, u, sigma):
+    """Right-hand side of u_tt = div(K grad u), K = (1 + 0.5 prod sin(2 pi x_d))^2, with the IPDG
+    penalty -sigma/dx [u][v] (fast transforms, the reference's operator on adaptive grids)."""
+    B = (k + 1) ** dim
+    rhs = np.zeros((len(level), B))
+    _check(lib().amdg_oracle_wave_rhs_fast(dim, N, k, len(level), np.ascontiguousarray(level, np.int32),
+                                           np.ascontiguousarray(suppt, np.int32),
+                                           np.ascontiguousarray(u, np.float64).reshape(-1), sigma, rhs))
+    return rhs
+
+
+def wave_rk4(dim, N, k, level, suppt, u, v, sigma, dt, steps):
+    """RK4ODE2nd steps of u' = v, v' = L u (ODESolver.cpp:579-615, same combination order)."""
+    u = np.array(u, np.float64)
+    v = np.array(v, np.float64)
+    for _ in range(steps):
+        un, vn = u.copy(), v.copy()
+        ku, kv = [], []
+        for stage in range(4):
+            rhs = wave_rhs(dim, N, k, level, suppt, u, sigma)
+            ku.append(dt * v)
+            kv.append(dt * rhs)
+            if stage < 2:
+                u, v = un + ku[-1] / 2.0, vn + kv[-1] / 2.0
+            elif stage == 2:
+                u, v = un + ku[-1], vn + kv[-1]
+            else:
+                u = un + 1.0 / 6.0 * (ku[0] + 2 * ku[1] + 2 * ku[2] + ku[3])
+                v = vn + 1.0 / 6.0 * (kv[0] + 2 * kv[1] + 2 * kv[2] + kv[3])
+    return u, v
+
+
+def wave_ic_terms(dim, centre=(0.3, 0.4, 0.5), width=200.0):
+    """Gaussian bump exp(-width |x - centre|^2) as one separable term."""
+    return [lambda x, d: math.exp(-width * (x - centre[d]) ** 2)]
 
 
 def sin_sum_terms(dim, shift=0.0):

@@ -31,6 +31,10 @@
 //     predictor, refine, copy_predict_to_ucoe, three RK3SSP stages, coarsen.
 //     Dumps the element set and coefficients after init (u_init) and after
 //     every step (u_step<i>), with the step sizes.
+//   ref_harness wave <dim> <N> <sigma> <steps> <dt>
+//     u_tt = div(K grad u), K = (1 + 0.5 prod_d sin(2 pi x_d))^2, u0 = Gaussian bump, u_t(0) = 0:
+//     DiffusionRHS with Lagrange-interpolated K grad u and K u, IPDG penalty, RK4ODE2nd
+//     (03_wave_06_var_coeff_adapt.cpp:154-279). Dumps u0, rhs0, uT, vT.
 //   ref_harness matrices <N> <k>
 //     dumps the 1D operator matrices u_v, u_vx, ulft_vjp, urgt_vjp.
 //
@@ -54,6 +58,7 @@
 #include "Timer.h"
 
 #include <chrono>
+#include <cmath>
 #include <cstdio>
 #include <cstdlib>
 #include <string>
@@ -88,7 +93,7 @@ void dump_elements(const char* name, DGSolution& dg, int which) {
         const Element& e = it.second;
         for (int d = 0; d < dim; ++d) std::printf("%d ", e.level[d]);
         for (int d = 0; d < dim; ++d) std::printf("%d ", e.suppt[d]);
-        const VecMultiD<double>& v = (which == 0) ? e.ucoe_alpt[0] : e.rhs[0];
+        const VecMultiD<double>& v = (which == 0) ? e.ucoe_alpt[0] : (which == 1 ? e.rhs[0] : e.ucoe_ut[0]);
         for (int i = 0; i < nb; ++i) std::printf("%.17g ", v.at(i));
         std::printf("\n");
     }
@@ -442,6 +447,104 @@ int run_burgers_adapt(int argc, char** argv) {
     return 0;
 }
 
+// Wave equation u_tt = div(K grad u), K = (1 + 0.5 prod_d sin(2 pi x_d))^2, periodic, Alpert k = 2,
+// Lagrange degree 3 (msh_case 1) interpolation of K u_x and K u, DiffusionRHS terms and the IPDG
+// penalty as 03_wave_06_var_coeff_adapt.cpp:154-279 (no source, no adaptivity): u0 a Gaussian bump,
+// u_t = 0. Dumps u0, rhs0 (the right-hand side at u0, read through EulerODE2nd with dt = 1 on a
+// second solution) and uT, vT after `steps` RK4ODE2nd steps.
+int run_wave(int argc, char** argv) {
+    if (argc < 7) { std::fprintf(stderr, "wave: bad args\n"); return 2; }
+    const int dim = std::atoi(argv[2]);
+    const int N = std::atoi(argv[3]);
+    const double sigma = std::atof(argv[4]);
+    const int steps = std::atoi(argv[5]);
+    const double dt = std::atof(argv[6]);
+    const int k = 2;
+    set_statics(dim, k);
+    DGSolution::prob = "wave";
+    Hash hash;
+    LagrBasis::set_interp_msh01();
+    HermBasis::set_interp_msh01();
+    AllBasis<AlptBasis> all_bas_alpt(N);
+    AllBasis<LagrBasis> all_bas_lagr(N);
+    AllBasis<HermBasis> all_bas_herm(N);
+    OperatorMatrix1D<AlptBasis, AlptBasis> oper_alpt(all_bas_alpt, all_bas_alpt, "period");
+    OperatorMatrix1D<LagrBasis, AlptBasis> oper_lagr(all_bas_lagr, all_bas_alpt, "period");
+    const double centre[3] = {0.3, 0.4, 0.5};
+    auto zero = [](double, int) { return 0.0; };
+    auto bump = [&](double x, int d) { return std::exp(-200.0 * (x - centre[d]) * (x - centre[d])); };
+    const double PI = Const::PI;
+    auto coe = [=](std::vector<double> x, int) -> double {
+        double s = 1.0;
+        for (int d = 0; d < dim; ++d) s *= std::sin(2 * PI * x[d]);
+        const double c = 1.0 + 0.5 * s;
+        return c * c;
+    };
+    std::vector<std::vector<bool>> is_intp(1, std::vector<bool>(dim, true));
+    std::vector<std::vector<bool>> is_intp_d0(1, std::vector<bool>(dim, false));
+    is_intp_d0[0][0] = true;
+    auto init = [&](DGAdapt& dg) {
+        dg.init_separable_scalar(zero);
+        dg.copy_ucoe_to_ucoe_ut();
+        dg.init_separable_scalar(bump);
+    };
+    // right-hand side at u0: v1 = v0 + 1 * rhs with v0 = 0
+    {
+        DGAdapt dg(true, N, N, all_bas_alpt, all_bas_lagr, all_bas_herm, hash, 1e10, -1, true, false);
+        init(dg);
+        LagrInterpolation interp(dg);
+        FastLagrIntp fast(dg, interp.Lag_pt_Alpt_1D, interp.Lag_pt_Alpt_1D_d1);
+        DiffusionRHS diffuse(dg, oper_lagr);
+        DiffusionAlpt ipdg(dg, oper_alpt, sigma);
+        ipdg.assemble_matrix_flx_ujp_vjp();
+        EulerODE2nd ode(ipdg, 1.0);
+        ode.init();
+        dg.set_rhs_zero();
+        interp.var_coeff_gradu_Lagr_fast(coe, is_intp, fast);
+        diffuse.rhs_flx_gradu();
+        diffuse.rhs_vol();
+        interp.var_coeff_u_Lagr_fast(coe, is_intp_d0, fast);
+        diffuse.rhs_flx_u();
+        ode.rhs_to_eigenvec();
+        ode.add_rhs_matrix(ipdg);
+        ode.step_stage(0);
+        ode.final();
+        dump_elements("rhs0", dg, 2);
+    }
+    DGAdapt dg(true, N, N, all_bas_alpt, all_bas_lagr, all_bas_herm, hash, 1e10, -1, true, false);
+    init(dg);
+    std::printf("META dim=%d N=%d k=%d sparse=1 elements=%zu dof=%d\n", dim, N, k, dg.dg.size(), dg.get_dof());
+    dump_elements("u0", dg, 0);
+    LagrInterpolation interp(dg);
+    FastLagrIntp fast(dg, interp.Lag_pt_Alpt_1D, interp.Lag_pt_Alpt_1D_d1);
+    DiffusionRHS diffuse(dg, oper_lagr);
+    auto t0 = std::chrono::steady_clock::now();
+    for (int s = 0; s < steps; ++s) {
+        DiffusionAlpt ipdg(dg, oper_alpt, sigma);
+        ipdg.assemble_matrix_flx_ujp_vjp();
+        RK4ODE2nd ode(ipdg, dt);
+        ode.init();
+        for (int stage = 0; stage < 4; ++stage) {
+            dg.set_rhs_zero();
+            interp.var_coeff_gradu_Lagr_fast(coe, is_intp, fast);
+            diffuse.rhs_flx_gradu();
+            diffuse.rhs_vol();
+            interp.var_coeff_u_Lagr_fast(coe, is_intp_d0, fast);
+            diffuse.rhs_flx_u();
+            ode.rhs_to_eigenvec();
+            ode.add_rhs_matrix(ipdg);
+            ode.step_stage(stage);
+            ode.final();
+        }
+    }
+    auto t1 = std::chrono::steady_clock::now();
+    dump_elements("uT", dg, 0);
+    dump_elements("vT", dg, 2);
+    std::printf("TIME evolve_s=%.9g dof_stage=%.17g\n", std::chrono::duration<double>(t1 - t0).count(),
+                4.0 * steps * dg.get_dof());
+    return 0;
+}
+
 int run_matrices(int argc, char** argv) {
     if (argc < 4) return 2;
     const int N = std::atoi(argv[2]);
@@ -465,6 +568,7 @@ int main(int argc, char** argv) {
     if (mode == "matrices") return run_matrices(argc, argv);
     if (mode == "burgers") return run_burgers(argc, argv);
     if (mode == "burgers_adapt") return run_burgers_adapt(argc, argv);
+    if (mode == "wave") return run_wave(argc, argv);
     std::fprintf(stderr, "unknown mode %s\n", mode.c_str());
     return 2;
 }

@@ -89,6 +89,14 @@ BURGERS_ADAPT_CASES = [
 ]
 
 
+# (name, dim, N, sigma, steps, dt): wave equation with interpolated K grad u, IPDG, RK4ODE2nd
+WAVE_CASES = [
+    ("wave2d_n4", 2, 4, 10.0, 2, 0.001),
+    ("wave2d_n5", 2, 5, 10.0, 2, 0.0005),
+    ("wave3d_n4", 3, 4, 20.0, 1, 0.0005),
+]
+
+
 def main():
     if not os.path.exists(HARNESS):
         sys.exit("build the reference first: make -C oracle ref")
@@ -128,6 +136,18 @@ def main():
         np.savez_compressed(os.path.join(HERE, name + ".npz"), **arrs)
         manifest[name] = dict(kind="burgers_adapt", dim=dim, n_init=n0, nmax=nmax, eps=eps, eta=eta, alpha=alpha,
                               cfl=cfl, umax=umax, steps=steps)
+        print(name, r["meta"])
+    for name, dim, N, sigma, steps, dt in WAVE_CASES:
+        r = run(["wave", dim, N, repr(sigma), steps, repr(dt)])
+        lv, sp, u0 = split_elements(r["u0"], dim)
+        arrs = {"level": lv, "suppt": sp, "u0": u0}
+        for key in ("rhs0", "uT", "vT"):
+            lv2, sp2, v = split_elements(r[key], dim)
+            idx = {tuple(a) + tuple(b): i for i, (a, b) in enumerate(zip(lv2, sp2))}
+            arrs[key] = v[[idx[tuple(a) + tuple(b)] for a, b in zip(lv, sp)]]
+        np.savez_compressed(os.path.join(HERE, name + ".npz"), **arrs)
+        manifest[name] = dict(kind="wave", dim=dim, N=N, k=2, sigma=sigma, steps=steps, dt=dt,
+                              elements=int(r["meta"]["elements"]))
         print(name, r["meta"])
     for N, k in [(4, 2), (3, 1), (3, 3)]:
         r = run(["matrices", N, k])

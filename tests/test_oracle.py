@@ -220,3 +220,21 @@ def test_burgers_wave_solves_its_characteristic_equation():
         v = O.lib().amdg_oracle_burgers_wave(x, t)
         assert abs(v - math.sin(2 * math.pi * (x - v * t))) <= 1e-12
         assert abs(v + O.lib().amdg_oracle_burgers_wave(1 - x, t)) <= 1e-12
+
+
+WAVE = [n for n, m in manifest().items() if m["kind"] == "wave"]
+
+
+@pytest.mark.parametrize("name", WAVE)
+def test_wave_operator_matches_reference(name):
+    """u_tt = div(K grad u): Lagrange-interpolated K grad u and K u, DiffusionRHS terms, IPDG
+    penalty, RK4ODE2nd (03_wave_06_var_coeff_adapt.cpp) against the reference run."""
+    m = manifest()[name]
+    z = golden(name)
+    dim, N = m["dim"], m["N"]
+    rhs = O.wave_rhs(dim, N, 2, z["level"], z["suppt"], z["u0"], m["sigma"])
+    assert rel_err(rhs, z["rhs0"]) < 1e-12
+    u, v = O.wave_rk4(dim, N, 2, z["level"], z["suppt"], z["u0"], np.zeros_like(z["u0"]), m["sigma"], m["dt"],
+                      m["steps"])
+    assert rel_err(u, z["uT"]) < 1e-13
+    assert rel_err(v, z["vT"]) < 1e-12
