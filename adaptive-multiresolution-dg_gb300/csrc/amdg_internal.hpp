@@ -69,6 +69,10 @@ struct LagrTables {
     std::vector<double> lvx;    // [n_lagr][n_alpt]: u_vx
     std::vector<double> lflx;   // [n_lagr][n_alpt]: ulft_vjp + urgt_vjp
     std::vector<double> ajump;  // [n_alpt][n_alpt]: ujp_vjp (Alpert x Alpert)
+    // diffusion terms (built when asked for)
+    std::vector<double> a2pd;   // [n_alpt][n_lagr]: Alpert basis derivative at Lagrange points
+    std::vector<double> ljv;    // [n_lagr][n_alpt]: ujp_vxlft + ujp_vxrgt
+    std::vector<double> pts;    // [n_lagr]: coordinate of each Lagrange point
     std::vector<int32_t> anc_order;  // [n_elem1d][4]: 1D order of the ancestor owning surplus point ic
     std::vector<int32_t> anc_point;  // [n_elem1d][4]: its point index
     std::vector<int32_t> anc_rank;   // [n_elem1d][4]: rank of its position among the four
@@ -76,7 +80,7 @@ struct LagrTables {
 };
 double lagr_eval(int order, double x, int sgn);
 double lagr_point(int o, int p);
-void build_lagr_tables(const Basis1D& alpt, LagrTables* t);
+void build_lagr_tables(const Basis1D& alpt, LagrTables* t, bool diffusion = false);
 void build_lagr_ancestors(const Basis1D& alpt, LagrTables* t);  // anc_order/anc_point/anc_rank only
 // dimension orders and L(0)/full(1)/U(2) tags of the 2^(dim-1) partial sums
 void transform_schedule(int dim, std::vector<std::vector<int>>* dim_order, std::vector<std::vector<int>>* lu);
@@ -155,7 +159,9 @@ struct TransformTopology {
 void build_transform_topology(const HostGrid& g, TransformTopology* out);
 
 // Matrices of the Lagrange path, indexed by PartialSum::mat.
-enum LagrMat { kMatA2P = 0, kMatLV = 1, kMatLVX = 2, kMatLFLX = 3, kMatAJump = 4, kNumLagrMats = 5 };
+enum LagrMat { kMatA2P = 0, kMatLV = 1, kMatLVX = 2, kMatLFLX = 3, kMatAJump = 4, kMatA2PD = 5, kMatLJV = 6,
+               kNumLagrMats = 7 };
+constexpr int kMaxTermSources = kMaxDim + 1;  // inputs a term's first sweep can read
 
 // One term of a right-hand side or of the point values: either a partial sum
 // of dim successive 1D transforms (FastRHS::transform_multiD_partial_sum,
@@ -167,6 +173,7 @@ enum LagrMat { kMatA2P = 0, kMatLV = 1, kMatLVX = 2, kMatLFLX = 3, kMatAJump = 4
 // matrix on the flx sets (FastRHS::transform_ucoe_alpt_to_rhs, :46-59).
 struct PartialSum {
     int8_t dims[kMaxDim], lu[kMaxDim], mat[kMaxDim], flx[kMaxDim];
+    int8_t src;    // input of the first sweep (index into the launch's sources)
     int32_t kind;
     double coef;
 };
@@ -224,6 +231,10 @@ struct amdg_grid {
     int64_t map_capacity = 0;
     double* d_norms = nullptr;
     int64_t norms_capacity = 0;
+    // second field v = u_t of second-order-in-time problems (Element::ucoe_ut), remapped with u
+    double* d_v = nullptr;           // v_capacity elements, null until set
+    double* d_v_spare = nullptr;
+    int64_t v_capacity = 0, v_spare_capacity = 0;
 };
 
 struct amdg_linear_op {
@@ -253,6 +264,8 @@ struct amdg_linear_op {
 };
 
 struct amdg_burgers_op {
+    int kind = 0;                    // 0: Burgers flux u^2/2; 1: wave u_tt = div(K grad u) (amdg_wave_op)
+    double sigma = 0.0;              // wave: IPDG penalty parameter
     int64_t built_version = -1;
     int64_t capacity = 0;            // elements the work buffers can hold
     amdg_grid* grid = nullptr;
@@ -263,6 +276,10 @@ struct amdg_burgers_op {
     // 1D matrices, FP64 and FP32 copies
     double *d_a2p = nullptr, *d_lv = nullptr, *d_lvx = nullptr, *d_lflx = nullptr, *d_ajump = nullptr;
     float *f_a2p = nullptr, *f_lv = nullptr, *f_lvx = nullptr, *f_lflx = nullptr, *f_ajump = nullptr;
+    double *d_a2pd = nullptr, *d_ljv = nullptr, *d_pts = nullptr;  // wave: derivative and jump tables, point coordinates
+    float *f_a2pd = nullptr, *f_ljv = nullptr;
+    void* w_fields = nullptr;        // wave: (dim+1) coefficient-weighted point fields and their surpluses, 2 (dim+1) x E x 4^dim doubles
+    double *d_v1 = nullptr, *d_su = nullptr, *d_sv = nullptr;  // wave: RK4ODE2nd stage v and running sums
     // neighbour lists of the fast transforms and the surplus ancestors
     int32_t *d_vol_ptr = nullptr, *d_vol_nbr = nullptr;  // nbr: (element, 1D order along t) pairs
     int32_t *d_flx_ptr = nullptr, *d_flx_nbr = nullptr;
@@ -299,6 +316,11 @@ struct amdg_burgers_op {
     double last_dt = 0.0;
     std::vector<int32_t> anc_order;                   // surplus ancestor 1D orders (depend on nmax only)
     std::unordered_map<const void*, size_t> dev_cap;  // bytes held by each grow-only device array
+};
+
+// wave-equation operator: the Lagrange-path operator of kind 1
+struct amdg_wave_op {
+    amdg_burgers_op* lagr = nullptr;
 };
 
 namespace amdg {

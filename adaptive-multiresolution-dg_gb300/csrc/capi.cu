@@ -153,6 +153,19 @@ amdg_status grid_set_keys(amdg_grid* g, std::vector<uint64_t> keys) {
     if (E > 0) AMDG_CK(cudaMemcpyAsync(g->d_map, map.data(), size_t(E) * sizeof(int32_t), cudaMemcpyHostToDevice, st));
     AMDG_CK(launch_remap(g->d_u, g->d_map, g->block, E, g->d_u_spare, st));
     g->ctx->launches++;
+    if (g->d_v) {  // the velocity field follows the element set (into its own spare, then swapped)
+        if (E > g->v_spare_capacity) {
+            cudaFree(g->d_v_spare);
+            g->d_v_spare = nullptr;
+            g->v_spare_capacity = 0;
+            if ((s = dev_alloc(&g->d_v_spare, size_t(grown) * g->block)) != AMDG_OK) return s;
+            g->v_spare_capacity = grown;
+        }
+        AMDG_CK(launch_remap(g->d_v, g->d_map, g->block, E, g->d_v_spare, st));
+        g->ctx->launches++;
+        std::swap(g->d_v, g->d_v_spare);
+        std::swap(g->v_capacity, g->v_spare_capacity);
+    }
     std::swap(g->d_u, g->d_u_spare);
     std::swap(g->capacity, g->spare_capacity);
     AMDG_CK(cudaMemcpyAsync(g->d_order, ng.order.data(), ng.order.size() * sizeof(int32_t), cudaMemcpyHostToDevice, st));
@@ -580,6 +593,8 @@ amdg_status amdg_grid_destroy(amdg_grid* g) {
     cudaFree(g->d_u_spare);
     cudaFree(g->d_map);
     cudaFree(g->d_norms);
+    cudaFree(g->d_v);
+    cudaFree(g->d_v_spare);
     delete g;
     return AMDG_OK;
 }
@@ -733,6 +748,35 @@ amdg_status amdg_grid_coarsen(amdg_grid* g, double eta, int64_t* num_elements) {
     }
     if (int64_t(keys.size()) != g->host.num_elements && (s = grid_set_keys(g, std::move(keys))) != AMDG_OK) return s;
     if (num_elements) *num_elements = g->host.num_elements;
+    return AMDG_OK;
+}
+
+amdg_status amdg_grid_set_velocity(amdg_grid* g, const double* host, int64_t n) {
+    AMDG_REQUIRE(g && host && n == g->dof, AMDG_ERR_ARG, "velocity must have dof entries");
+    amdg_status s = set_device(g->ctx);
+    if (s != AMDG_OK) return s;
+    if (!g->d_v || g->v_capacity < g->host.num_elements) {
+        cudaFree(g->d_v);
+        g->d_v = nullptr;
+        g->v_capacity = 0;
+        const int64_t cap = std::max<int64_t>(g->capacity, g->host.num_elements);
+        if ((s = dev_alloc(&g->d_v, size_t(std::max<int64_t>(cap, 1)) * g->block)) != AMDG_OK) return s;
+        g->v_capacity = cap;
+    }
+    cudaStream_t st = stream_of(g->ctx);
+    if (n) AMDG_CK(cudaMemcpyAsync(g->d_v, host, size_t(n) * sizeof(double), cudaMemcpyHostToDevice, st));
+    AMDG_CK(cudaStreamSynchronize(st));
+    return AMDG_OK;
+}
+
+amdg_status amdg_grid_get_velocity(const amdg_grid* g, double* host, int64_t n) {
+    AMDG_REQUIRE(g && host && n == g->dof, AMDG_ERR_ARG, "velocity must have dof entries");
+    AMDG_REQUIRE(g->d_v, AMDG_ERR_STATE, "the grid has no velocity field");
+    amdg_status s = set_device(g->ctx);
+    if (s != AMDG_OK) return s;
+    cudaStream_t st = stream_of(g->ctx);
+    if (n) AMDG_CK(cudaMemcpyAsync(host, g->d_v, size_t(n) * sizeof(double), cudaMemcpyDeviceToHost, st));
+    AMDG_CK(cudaStreamSynchronize(st));
     return AMDG_OK;
 }
 

@@ -70,8 +70,12 @@ struct Mats {
     const T* m[kNumLagrMats];
 };
 
-Mats<double> mats64(const amdg_burgers_op* op) { return {{op->d_a2p, op->d_lv, op->d_lvx, op->d_lflx, op->d_ajump}}; }
-Mats<float> mats32(const amdg_burgers_op* op) { return {{op->f_a2p, op->f_lv, op->f_lvx, op->f_lflx, op->f_ajump}}; }
+Mats<double> mats64(const amdg_burgers_op* op) {
+    return {{op->d_a2p, op->d_lv, op->d_lvx, op->d_lflx, op->d_ajump, op->d_a2pd, op->d_ljv}};
+}
+Mats<float> mats32(const amdg_burgers_op* op) {
+    return {{op->f_a2p, op->f_lv, op->f_lvx, op->f_lflx, op->f_ajump, op->f_a2pd, op->f_ljv}};
+}
 
 int ipow(int b, int e) {
     int p = 1;
@@ -79,7 +83,38 @@ int ipow(int b, int e) {
     return p;
 }
 
-// The terms of the path (host side, built once per operator):
+// partial sums of the schedule with the given matrix and vol/flx choice per
+// dimension, reading input `src`, appended to op->terms
+void push_psums(amdg_burgers_op* op, const int* mat, const int* flx, double coef, int src) {
+    const int dim = op->grid->host.dim;
+    for (size_t s = 0; s < op->sched_dims.size(); ++s) {
+        PartialSum p{};
+        for (int j = 0; j < dim; ++j) {
+            const int t = op->sched_dims[s][j];
+            p.dims[j] = int8_t(t);
+            p.lu[j] = int8_t(op->sched_lu[s][j]);
+            p.mat[j] = int8_t(mat[t]);
+            p.flx[j] = int8_t(flx[t]);
+        }
+        p.src = int8_t(src);
+        p.kind = 0;
+        p.coef = coef;
+        op->terms.push_back(p);
+    }
+}
+
+// a single full transform of the Alpert coefficients along d with the jump matrix (penalty)
+void push_penalty(amdg_burgers_op* op, int d, double coef) {
+    PartialSum p{};
+    p.dims[0] = int8_t(d);
+    p.kind = 1;
+    p.coef = coef;
+    op->terms.push_back(p);
+}
+
+// The terms of the path (host side, built once per operator; the wave penalty's
+// coefficient follows the finest level, see wave_penalty_coef).
+// Burgers:
 //  - point values: the 2^(dim-1) partial sums of the schedule with the
 //    Alpert-at-Lagrange-point matrix in every dimension (FastLagrIntp::eval_up_Lagr);
 //  - right-hand side, in the order the reference adds them: for each dimension
@@ -88,40 +123,60 @@ int ipow(int b, int e) {
 //    elsewhere) (HyperbolicLagrRHS::rhs_vol_scalar / rhs_flx_intp_scalar,
 //    FastMultiplyLU.cpp:1125-1189), then the LxF penalty -alpha_d/2 ujp_vjp
 //    along d (HyperbolicAlptRHS::rhs_flx_penalty_scalar, :1269-1276).
+// Wave (03_wave_06_var_coeff_adapt.cpp:154-245):
+//  - point values: group d < dim is u_{x_d} (the Alpert derivative at the
+//    points along d, FastLagrIntp::eval_der_up_Lagr), group dim is u;
+//  - right-hand side (sources 0..dim-1: the interpolated K u_{x_d}, source
+//    dim: K u): DiffusionRHS::rhs_flx_gradu -{K u_x}[v] with uave_vjp =
+//    (ulft+urgt)_vjp/2 along d, rhs_vol -K u_x v_x, rhs_flx_u -1/2 [K u] (v_x^- +
+//    v_x^+) (FastMultiplyLU.cpp:1691-1765), each over d; then the IPDG penalty
+//    -sigma/dx [u][v] along each d (DiffusionAlpt::assemble_matrix_flx_ujp_vjp,
+//    BilinearForm.cpp:920-929).
 void build_terms(amdg_burgers_op* op) {
     const int dim = op->grid->host.dim;
     op->terms.clear();
-    auto psum = [&](const std::vector<int>& dims, const std::vector<int>& lu, const int* mat, const int* flx, double coef) {
-        PartialSum p{};
-        for (int j = 0; j < dim; ++j) {
-            p.dims[j] = int8_t(dims[j]);
-            p.lu[j] = int8_t(lu[j]);
-            p.mat[j] = int8_t(mat[dims[j]]);
-            p.flx[j] = int8_t(flx[dims[j]]);
-        }
-        p.kind = 0;
-        p.coef = coef;
-        op->terms.push_back(p);
-    };
     int mat[kMaxDim], flx[kMaxDim];
-    for (int t = 0; t < dim; ++t) { mat[t] = kMatA2P; flx[t] = 0; }
-    for (size_t s = 0; s < op->sched_dims.size(); ++s) psum(op->sched_dims[s], op->sched_lu[s], mat, flx, 1.0);
-    op->n_pv_terms = int(op->terms.size());
-    for (int d = 0; d < dim; ++d) {
-        for (int term = 0; term < 2; ++term) {
-            for (int t = 0; t < dim; ++t) {
-                mat[t] = (t == d) ? (term == 0 ? kMatLVX : kMatLFLX) : kMatLV;
-                flx[t] = (term == 1 && t == d) ? 1 : 0;
+    if (op->kind == 0) {
+        for (int t = 0; t < dim; ++t) { mat[t] = kMatA2P; flx[t] = 0; }
+        push_psums(op, mat, flx, 1.0, 0);
+        op->n_pv_terms = int(op->terms.size());
+        for (int d = 0; d < dim; ++d) {
+            for (int term = 0; term < 2; ++term) {
+                for (int t = 0; t < dim; ++t) {
+                    mat[t] = (t == d) ? (term == 0 ? kMatLVX : kMatLFLX) : kMatLV;
+                    flx[t] = (term == 1 && t == d) ? 1 : 0;
+                }
+                push_psums(op, mat, flx, term == 0 ? 1.0 : 0.5, 0);
             }
-            for (size_t s = 0; s < op->sched_dims.size(); ++s)
-                psum(op->sched_dims[s], op->sched_lu[s], mat, flx, term == 0 ? 1.0 : 0.5);
+            push_penalty(op, d, -op->alpha[d] / 2.0);
         }
-        PartialSum p{};
-        p.dims[0] = int8_t(d);
-        p.kind = 1;
-        p.coef = -op->alpha[d] / 2.0;
-        op->terms.push_back(p);
+        return;
     }
+    for (int g = 0; g <= dim; ++g) {
+        for (int t = 0; t < dim; ++t) { mat[t] = (t == g) ? kMatA2PD : kMatA2P; flx[t] = 0; }
+        push_psums(op, mat, flx, 1.0, 0);
+    }
+    op->n_pv_terms = int(op->terms.size());
+    for (int d = 0; d < dim; ++d) {  // -{K u_x}[v]: uave_vjp = lflx / 2 exactly
+        for (int t = 0; t < dim; ++t) { mat[t] = (t == d) ? kMatLFLX : kMatLV; flx[t] = (t == d) ? 1 : 0; }
+        push_psums(op, mat, flx, -0.5, d);
+    }
+    for (int d = 0; d < dim; ++d) {  // -K u_x v_x
+        for (int t = 0; t < dim; ++t) { mat[t] = (t == d) ? kMatLVX : kMatLV; flx[t] = 0; }
+        push_psums(op, mat, flx, -1.0, d);
+    }
+    for (int d = 0; d < dim; ++d) {  // -1/2 [K u](v_x^- + v_x^+)
+        for (int t = 0; t < dim; ++t) { mat[t] = (t == d) ? kMatLJV : kMatLV; flx[t] = (t == d) ? 1 : 0; }
+        push_psums(op, mat, flx, -0.5, dim);
+    }
+    for (int d = 0; d < dim; ++d) push_penalty(op, d, 0.0);  // coefficient set per element set
+}
+
+// IPDG coefficient -sigma/dx, dx = 2^-(finest level of the grid) (BilinearForm.cpp:922-923)
+double wave_penalty_coef(const amdg_burgers_op* op) {
+    int maxl = 0;
+    for (int32_t o : op->grid->host.order) maxl = std::max(maxl, level_of_order(o));
+    return -op->sigma / (1.0 / std::pow(2.0, maxl));
 }
 
 template <typename T>
@@ -144,11 +199,12 @@ SweepArgs<T> sweep_args(const amdg_burgers_op* op, const Mats<T>& m) {
     return a;
 }
 
-// Terms [first, first + count): dim sweeps, the last one into `slots`
-// (count slices of E x n_out^dim, or E x np^dim for a right-hand side).
+// Terms [first, first + count): dim sweeps, the first reading src[term.src],
+// the last one into `slots` (count slices of E x n_out^dim, or E x np^dim for
+// a right-hand side).
 template <typename T>
-amdg_status run_terms(amdg_burgers_op* op, const Mats<T>& m, int first, int count, int n_in, int n_out, const T* in,
-                      const T* pen_in, T* slots, cudaStream_t st) {
+amdg_status run_terms(amdg_burgers_op* op, const Mats<T>& m, int first, int count, int n_in, int n_out,
+                      const T* const* src, int nsrc, const T* pen_in, T* slots, cudaStream_t st) {
     const int dim = op->grid->host.dim;
     const int64_t E = op->grid->host.num_elements;
     T* ping = static_cast<T*>(op->w_s0);
@@ -159,7 +215,8 @@ amdg_status run_terms(amdg_burgers_op* op, const Mats<T>& m, int first, int coun
     a.n_in = n_in;
     a.n_out = n_out;
     a.pen_in = pen_in;
-    const T* cur = in;
+    for (int i = 0; i < nsrc && i < kMaxTermSources; ++i) a.src[i] = src[i];
+    const T* cur = nullptr;
     for (int j = 0; j < dim; ++j) {
         const bool last = j == dim - 1;
         a.sweep = j;
@@ -181,9 +238,10 @@ amdg_status eval_point_values(amdg_burgers_op* op, const Mats<T>& m, const T* u,
     const int np = op->grid->host.k + 1;
     const int64_t n = op->grid->host.num_elements * op->points;
     T* slots = static_cast<T*>(op->w_slots);
+    const T* src[1] = {u};
     for (int c0 = 0; c0 < op->n_pv_terms; c0 += op->chunk) {
         const int cnt = std::min(op->chunk, op->n_pv_terms - c0);
-        if (amdg_status r = run_terms<T>(op, m, c0, cnt, np, 4, u, nullptr, slots, st); r != AMDG_OK) return r;
+        if (amdg_status r = run_terms<T>(op, m, c0, cnt, np, 4, src, 1, nullptr, slots, st); r != AMDG_OK) return r;
         const bool last = c0 + cnt == op->n_pv_terms;
         AMDG_CK(launch_reduce_points<T>(slots, cnt, n, c0 == 0 ? 1 : 0, up, last ? fp : nullptr, st));
         op->grid->ctx->launches++;
@@ -191,10 +249,10 @@ amdg_status eval_point_values(amdg_burgers_op* op, const Mats<T>& m, const T* u,
     return AMDG_OK;
 }
 
-// flux interpolation coefficients from f(u) at the points (in w_a): dim surplus
-// passes, the last one into `out` (type To)
+// interpolation coefficients from values at the points: dim surplus passes
+// (w_a / w_b as ping-pong buffers), the last one into `out` (type To)
 template <typename T, typename To>
-amdg_status eval_surplus(amdg_burgers_op* op, To* out, cudaStream_t st) {
+amdg_status eval_surplus(amdg_burgers_op* op, const T* in, To* out, cudaStream_t st) {
     const amdg_grid* g = op->grid;
     const int dim = g->host.dim;
     T* ta = static_cast<T*>(op->w_a);
@@ -208,7 +266,7 @@ amdg_status eval_surplus(amdg_burgers_op* op, To* out, cudaStream_t st) {
     a.anc_point = op->d_anc_point;
     a.anc_rank = op->d_anc_rank;
     for (int i = 0; i < 16; ++i) a.weight[i] = op->weight[i];
-    const T* cur = ta;
+    const T* cur = in;
     for (int d = 0; d < dim; ++d) {
         a.d = d;
         a.stride = ipow(4, dim - d - 1);
@@ -224,20 +282,57 @@ amdg_status eval_surplus(amdg_burgers_op* op, To* out, cudaStream_t st) {
     return AMDG_OK;
 }
 
-// volume, interface and penalty terms from the flux coefficients fu and the
-// Alpert coefficients u: into rhs, or, when so.fused, straight into the RK
-// stage update
+// right-hand-side terms from their sources and the Alpert coefficients u
+// (penalty): into rhs, or, when so.fused, straight into the RK stage update
 template <typename T>
-amdg_status eval_back_transforms(amdg_burgers_op* op, const Mats<T>& m, const T* fu, const T* u, double* rhs, StageOut so,
-                                 cudaStream_t st) {
+amdg_status eval_back_transforms(amdg_burgers_op* op, const Mats<T>& m, const T* const* src, int nsrc, const T* u,
+                                 double* rhs, StageOut so, cudaStream_t st) {
     const int np = op->grid->host.k + 1;
     T* slots = static_cast<T*>(op->w_slots);
     const int first = op->n_pv_terms, total = int(op->terms.size()) - op->n_pv_terms;
     for (int c0 = 0; c0 < total; c0 += op->chunk) {
         const int cnt = std::min(op->chunk, total - c0);
-        if (amdg_status r = run_terms<T>(op, m, first + c0, cnt, 4, np, fu, u, slots, st); r != AMDG_OK) return r;
+        if (amdg_status r = run_terms<T>(op, m, first + c0, cnt, 4, np, src, nsrc, u, slots, st); r != AMDG_OK) return r;
         AMDG_CK(launch_reduce_rhs<T>(slots, cnt, op->grid->dof, c0 == 0 ? 1 : 0, c0 + cnt == total ? 1 : 0, rhs, so, st));
         op->grid->ctx->launches++;
+    }
+    return AMDG_OK;
+}
+
+// wave: K u_{x_d} (d < dim) and K u at the points, then their interpolation
+// coefficients (type To) into fields dim+1 .. 2 dim+1 of w_fields
+template <typename To>
+amdg_status eval_wave_fields(amdg_burgers_op* op, const double* u, To** fucoe, cudaStream_t st) {
+    amdg_grid* g = op->grid;
+    const int dim = g->host.dim, np = g->host.k + 1;
+    const int64_t E = g->host.num_elements, n = E * op->points;
+    const int G = int(op->sched_dims.size());  // terms per point field
+    double* slots = static_cast<double*>(op->w_slots);
+    double* fields = static_cast<double*>(op->w_fields);
+    const size_t stride = size_t(op->capacity) * op->points;
+    const double* src[1] = {u};
+    for (int f = 0; f <= dim; ++f) {
+        double* kp = fields + size_t(f) * stride;  // K times the point values of field f
+        double* acc = static_cast<double*>(op->w_up);
+        for (int c0 = 0; c0 < G; c0 += op->chunk) {
+            const int cnt = std::min(op->chunk, G - c0);
+            if (amdg_status r = run_terms<double>(op, mats64(op), f * G + c0, cnt, np, 4, src, 1, nullptr, slots, st);
+                r != AMDG_OK)
+                return r;
+            if (c0 + cnt == G) {
+                if (c0 > 0) {  // earlier chunks were summed into acc: fold them in as one more slice
+                    AMDG_CK(launch_reduce_points<double>(slots, cnt, n, 0, acc, nullptr, st));
+                    AMDG_CK(launch_reduce_points_coef(acc, 1, E, dim, g->d_order, op->d_pts, kp, st));
+                    op->grid->ctx->launches++;
+                } else {
+                    AMDG_CK(launch_reduce_points_coef(slots, cnt, E, dim, g->d_order, op->d_pts, kp, st));
+                }
+            } else {
+                AMDG_CK(launch_reduce_points<double>(slots, cnt, n, c0 == 0 ? 1 : 0, acc, nullptr, st));
+            }
+            op->grid->ctx->launches++;
+        }
+        if (amdg_status r = eval_surplus<double, To>(op, kp, fucoe[f], st); r != AMDG_OK) return r;
     }
     return AMDG_OK;
 }
@@ -250,20 +345,40 @@ amdg_status eval_back_transforms(amdg_burgers_op* op, const Mats<T>& m, const T*
 amdg_status eval_rhs(amdg_burgers_op* op, const double* u, double* rhs, amdg_precision prec, StageOut so = StageOut{}) {
     PhaseTimer timer(op->grid->ctx, AMDG_PHASE_RHS);
     cudaStream_t st = stream_of(op);
+    const int dim = op->grid->host.dim;
+    if (op->kind == 1) {
+        const size_t stride = size_t(op->capacity) * op->points;
+        double* fields = static_cast<double*>(op->w_fields);
+        if (prec == AMDG_PREC_FP64) {
+            double* fc[kMaxTermSources];
+            for (int f = 0; f <= dim; ++f) fc[f] = fields + size_t(dim + 1 + f) * stride;
+            if (amdg_status r = eval_wave_fields<double>(op, u, fc, st); r != AMDG_OK) return r;
+            return eval_back_transforms<double>(op, mats64(op), fc, dim + 1, u, rhs, so, st);
+        }
+        float* fc[kMaxTermSources];
+        for (int f = 0; f <= dim; ++f) fc[f] = reinterpret_cast<float*>(fields + size_t(dim + 1 + f) * stride);
+        if (amdg_status r = eval_wave_fields<float>(op, u, fc, st); r != AMDG_OK) return r;
+        float* u32 = static_cast<float*>(op->w_u);
+        AMDG_CK(launch_convert<double, float>(u, u32, op->grid->dof, st));
+        op->grid->ctx->launches++;
+        return eval_back_transforms<float>(op, mats32(op), fc, dim + 1, u32, rhs, so, st);
+    }
     double* fp = static_cast<double*>(op->w_a);
     amdg_status r = eval_point_values<double>(op, mats64(op), u, static_cast<double*>(op->w_up), fp, st);
     if (r != AMDG_OK) return r;
     if (prec == AMDG_PREC_FP64) {
         double* fu = static_cast<double*>(op->w_fu);
-        if ((r = eval_surplus<double, double>(op, fu, st)) != AMDG_OK) return r;
-        return eval_back_transforms<double>(op, mats64(op), fu, u, rhs, so, st);
+        if ((r = eval_surplus<double, double>(op, fp, fu, st)) != AMDG_OK) return r;
+        const double* src[1] = {fu};
+        return eval_back_transforms<double>(op, mats64(op), src, 1, u, rhs, so, st);
     }
     float* fu32 = static_cast<float*>(op->w_fu);
     float* u32 = static_cast<float*>(op->w_u);
-    if ((r = eval_surplus<double, float>(op, fu32, st)) != AMDG_OK) return r;
+    if ((r = eval_surplus<double, float>(op, fp, fu32, st)) != AMDG_OK) return r;
     AMDG_CK(launch_convert<double, float>(u, u32, op->grid->dof, st));
     op->grid->ctx->launches++;
-    return eval_back_transforms<float>(op, mats32(op), fu32, u32, rhs, so, st);
+    const float* src[1] = {fu32};
+    return eval_back_transforms<float>(op, mats32(op), src, 1, u32, rhs, so, st);
 }
 
 // Copy a host vector into a grow-only device array of the operator (stream
@@ -319,10 +434,10 @@ amdg_status burgers_sync(amdg_burgers_op* op) {
     if (E > op->capacity) {
         const int64_t cap = E + E / 2 + 16;
         void* bufs[] = {op->w_up, op->w_fu, op->w_a, op->w_b, op->w_u, op->w_s0, op->w_s1, op->w_slots,
-                        op->d_u1, op->d_rhs64, op->d_pred};
+                        op->d_u1, op->d_rhs64, op->d_pred, op->w_fields, op->d_v1, op->d_su, op->d_sv};
         for (void* p : bufs) cudaFree(p);
-        op->w_up = op->w_fu = op->w_a = op->w_b = op->w_u = op->w_s0 = op->w_s1 = op->w_slots = nullptr;
-        op->d_u1 = op->d_rhs64 = op->d_pred = nullptr;
+        op->w_up = op->w_fu = op->w_a = op->w_b = op->w_u = op->w_s0 = op->w_s1 = op->w_slots = op->w_fields = nullptr;
+        op->d_u1 = op->d_rhs64 = op->d_pred = op->d_v1 = op->d_su = op->d_sv = nullptr;
         op->capacity = 0;
         const size_t work = size_t(cap) * op->points * sizeof(double);
         const size_t vec = size_t(cap) * g->block * sizeof(double);
@@ -339,7 +454,22 @@ amdg_status burgers_sync(amdg_burgers_op* op) {
             (s = alloc_bytes(reinterpret_cast<void**>(&op->d_rhs64), vec)) != AMDG_OK ||
             (s = alloc_bytes(reinterpret_cast<void**>(&op->d_pred), vec)) != AMDG_OK)
             return s;
+        if (op->kind == 1 &&
+            ((s = alloc_bytes(&op->w_fields, 2 * size_t(g->host.dim + 1) * work)) != AMDG_OK ||
+             (s = alloc_bytes(reinterpret_cast<void**>(&op->d_v1), vec)) != AMDG_OK ||
+             (s = alloc_bytes(reinterpret_cast<void**>(&op->d_su), vec)) != AMDG_OK ||
+             (s = alloc_bytes(reinterpret_cast<void**>(&op->d_sv), vec)) != AMDG_OK))
+            return s;
         op->capacity = cap;
+    }
+    if (op->kind == 1) {  // the IPDG coefficient follows the finest level
+        const double c = wave_penalty_coef(op);
+        bool changed = false;
+        for (PartialSum& p : op->terms)
+            if (p.kind == 1 && p.coef != c) { p.coef = c; changed = true; }
+        if (changed)
+            AMDG_CK(cudaMemcpyAsync(op->d_terms, op->terms.data(), op->terms.size() * sizeof(PartialSum),
+                                    cudaMemcpyHostToDevice, st));
     }
     // the host vectors above are released on return: wait for their copies
     AMDG_CK(cudaStreamSynchronize(st));
@@ -388,24 +518,26 @@ StageCoef stage_coef(int stage, double dt) {
 
 extern "C" {
 
-amdg_status amdg_burgers_create(amdg_grid* g, const double* alpha, amdg_burgers_op** out) {
-    AMDG_REQUIRE(g && alpha && out, AMDG_ERR_ARG, "null argument");
+// a Lagrange-path operator of the given kind on g (tables, terms, neighbour lists)
+static amdg_status lagr_create(amdg_grid* g, int kind, const double* alpha, double sigma, amdg_burgers_op** out) {
     *out = nullptr;
     AMDG_REQUIRE(g->host.k == 2, AMDG_ERR_ARG, "the Lagrange path is built for Alpert degree k = 2");
     AMDG_CK(cudaSetDevice(g->device));
     const int dim = g->host.dim;
-    for (int d = 0; d < dim; ++d) AMDG_REQUIRE(std::isfinite(alpha[d]), AMDG_ERR_ARG, "non-finite alpha");
     amdg_burgers_op* op = new (std::nothrow) amdg_burgers_op;
     AMDG_REQUIRE(op, AMDG_ERR_NOMEM, "host allocation failed");
+    op->kind = kind;
+    op->sigma = sigma;
     op->grid = g;
     op->device = g->device;
-    op->alpha.assign(alpha, alpha + dim);
+    if (alpha) op->alpha.assign(alpha, alpha + dim);
+    else op->alpha.assign(dim, 0.0);
     op->points = 1;
     for (int d = 0; d < dim; ++d) op->points *= 4;
     op->n1 = 1 << g->host.nmax;
     Basis1D b{g->host.k, g->host.nmax};
     LagrTables t;
-    build_lagr_tables(b, &t);
+    build_lagr_tables(b, &t, kind == 1);
     std::memcpy(op->weight, t.weight, sizeof(op->weight));
     transform_schedule(dim, &op->sched_dims, &op->sched_lu);
     build_terms(op);
@@ -414,6 +546,9 @@ amdg_status amdg_burgers_create(amdg_grid* g, const double* alpha, amdg_burgers_
         (s = upload_both(&op->d_lvx, &op->f_lvx, t.lvx)) != AMDG_OK ||
         (s = upload_both(&op->d_lflx, &op->f_lflx, t.lflx)) != AMDG_OK ||
         (s = upload_both(&op->d_ajump, &op->f_ajump, t.ajump)) != AMDG_OK ||
+        (kind == 1 && ((s = upload_both(&op->d_a2pd, &op->f_a2pd, t.a2pd)) != AMDG_OK ||
+                       (s = upload_both(&op->d_ljv, &op->f_ljv, t.ljv)) != AMDG_OK ||
+                       (s = upload_vec(&op->d_pts, t.pts)) != AMDG_OK)) ||
         (s = upload_vec(&op->d_anc_point, t.anc_point)) != AMDG_OK || (s = upload_vec(&op->d_anc_rank, t.anc_rank)) != AMDG_OK ||
         (s = upload_vec(&op->d_terms, op->terms)) != AMDG_OK || (s = burgers_sync(op)) != AMDG_OK) {
         amdg_burgers_destroy(op);
@@ -421,6 +556,12 @@ amdg_status amdg_burgers_create(amdg_grid* g, const double* alpha, amdg_burgers_
     }
     *out = op;
     return AMDG_OK;
+}
+
+amdg_status amdg_burgers_create(amdg_grid* g, const double* alpha, amdg_burgers_op** out) {
+    AMDG_REQUIRE(g && alpha && out, AMDG_ERR_ARG, "null argument");
+    for (int d = 0; d < g->host.dim; ++d) AMDG_REQUIRE(std::isfinite(alpha[d]), AMDG_ERR_ARG, "non-finite alpha");
+    return lagr_create(g, 0, alpha, 0.0, out);
 }
 
 amdg_status amdg_burgers_destroy(amdg_burgers_op* op) {
@@ -433,7 +574,8 @@ amdg_status amdg_burgers_destroy(amdg_burgers_op* op) {
                     op->w_s0, op->w_s1, op->w_slots, op->d_terms,
                     op->d_u1, op->d_u2, op->d_rhs64, op->d_pred, op->d_vol_split, op->d_flx_split,
                     op->d_pg,
-                    op->d_feat, op->d_prob};
+                    op->d_feat, op->d_prob, op->d_a2pd, op->d_ljv, op->d_pts, op->f_a2pd, op->f_ljv,
+                    op->w_fields, op->d_v1, op->d_su, op->d_sv};
     for (void* p : ptrs) cudaFree(p);
     delete op;
     return AMDG_OK;
@@ -477,14 +619,16 @@ amdg_status amdg_burgers_flux_coefficients(amdg_burgers_op* op, const double* d_
         amdg_status r = eval_point_values<double>(op, mats64(op), d_u, static_cast<double*>(op->w_up),
                                                   static_cast<double*>(op->w_a), st);
         if (r != AMDG_OK) return r;
-        return eval_surplus<double, double>(op, d_fu, st);
+        return eval_surplus<double, double>(op, static_cast<const double*>(op->w_a), d_fu, st);
     }
     float* u32 = static_cast<float*>(op->w_u);
     AMDG_CK(launch_convert<double, float>(d_u, u32, op->grid->dof, st));
     amdg_status r = eval_point_values<float>(op, mats32(op), u32, static_cast<float*>(op->w_up),
                                              static_cast<float*>(op->w_a), st);
     if (r != AMDG_OK) return r;
-    if ((r = eval_surplus<float, float>(op, static_cast<float*>(op->w_fu), st)) != AMDG_OK) return r;
+    if ((r = eval_surplus<float, float>(op, static_cast<const float*>(op->w_a), static_cast<float*>(op->w_fu), st)) !=
+        AMDG_OK)
+        return r;
     AMDG_CK(launch_convert<float, double>(static_cast<float*>(op->w_fu), d_fu, np, st));
     op->grid->ctx->launches += 2;
     return AMDG_OK;
@@ -718,6 +862,121 @@ amdg_status amdg_burgers_counters(const amdg_burgers_op* op, int64_t* stage_dof_
     if (stage_dof_updates) *stage_dof_updates = op->stage_dof_updates;
     if (rhs_evaluations) *rhs_evaluations = op->rhs_evaluations;
     return AMDG_OK;
+}
+
+// ---- wave equation u_tt = div(K grad u) (03_wave_06_var_coeff_adapt.cpp) -----------------
+
+amdg_status amdg_wave_create(amdg_grid* g, double sigma, amdg_wave_op** out) {
+    AMDG_REQUIRE(g && out && std::isfinite(sigma) && sigma >= 0, AMDG_ERR_ARG, "bad arguments");
+    *out = nullptr;
+    amdg_wave_op* w = new (std::nothrow) amdg_wave_op;
+    AMDG_REQUIRE(w, AMDG_ERR_NOMEM, "host allocation failed");
+    amdg_status s = lagr_create(g, 1, nullptr, sigma, &w->lagr);
+    if (s != AMDG_OK) {
+        delete w;
+        return s;
+    }
+    *out = w;
+    return AMDG_OK;
+}
+
+amdg_status amdg_wave_destroy(amdg_wave_op* w) {
+    if (!w) return AMDG_OK;
+    amdg_burgers_destroy(w->lagr);
+    delete w;
+    return AMDG_OK;
+}
+
+amdg_status amdg_wave_rhs(amdg_wave_op* w, const double* d_u, double* d_rhs, amdg_precision prec) {
+    AMDG_REQUIRE(w && d_u && d_rhs && d_u != d_rhs, AMDG_ERR_ARG, "bad arguments");
+    AMDG_REQUIRE(prec == AMDG_PREC_FP64 || prec == AMDG_PREC_MIXED, AMDG_ERR_ARG, "bad precision");
+    amdg_burgers_op* op = w->lagr;
+    AMDG_CK(cudaSetDevice(op->device));
+    if (amdg_status rs = burgers_sync(op); rs != AMDG_OK) return rs;
+    op->rhs_evaluations++;
+    return eval_rhs(op, d_u, d_rhs, prec);
+}
+
+// the grid's velocity field, created as zero when absent
+static amdg_status ensure_velocity(amdg_grid* g) {
+    if (g->d_v) return AMDG_OK;
+    const int64_t cap = std::max<int64_t>(g->capacity, 1);
+    AMDG_CK(cudaMalloc(reinterpret_cast<void**>(&g->d_v), size_t(cap) * g->block * sizeof(double)));
+    AMDG_CK(cudaMemsetAsync(g->d_v, 0, size_t(cap) * g->block * sizeof(double), static_cast<cudaStream_t>(g->ctx->stream)));
+    g->v_capacity = cap;
+    return AMDG_OK;
+}
+
+// nsteps RK4ODE2nd steps of (u, v) (RK4ODE2nd::step_stage, ODESolver.cpp:579-615), the
+// right-hand side re-evaluated at every stage
+static amdg_status wave_rk4(amdg_burgers_op* op, double dt, int nsteps, amdg_precision prec) {
+    amdg_grid* g = op->grid;
+    cudaStream_t st = stream_of(op);
+    PhaseTimer timer(g->ctx, AMDG_PHASE_RK3);
+    if (amdg_status s = ensure_velocity(g); s != AMDG_OK) return s;
+    const size_t bytes = size_t(g->dof) * sizeof(double);
+    for (int step = 0; step < nsteps; ++step) {
+        AMDG_CK(cudaMemcpyAsync(op->d_u1, g->d_u, bytes, cudaMemcpyDeviceToDevice, st));
+        AMDG_CK(cudaMemcpyAsync(op->d_v1, g->d_v, bytes, cudaMemcpyDeviceToDevice, st));
+        for (int stage = 0; stage < 4; ++stage) {
+            if (amdg_status r = eval_rhs(op, op->d_u1, op->d_rhs64, prec); r != AMDG_OK) return r;
+            AMDG_CK(launch_rk4_2nd_stage(stage, dt, op->d_rhs64, g->d_u, g->d_v, op->d_u1, op->d_v1, op->d_su, op->d_sv,
+                                         g->dof, st));
+            g->ctx->launches++;
+        }
+        op->rhs_evaluations += 4;
+        op->stage_dof_updates += 4 * g->dof;
+    }
+    return AMDG_OK;
+}
+
+amdg_status amdg_wave_rk4_steps(amdg_wave_op* w, double dt, int nsteps, amdg_precision prec) {
+    AMDG_REQUIRE(w && nsteps >= 0 && std::isfinite(dt), AMDG_ERR_ARG, "bad arguments");
+    AMDG_REQUIRE(prec == AMDG_PREC_FP64 || prec == AMDG_PREC_MIXED, AMDG_ERR_ARG, "bad precision");
+    amdg_burgers_op* op = w->lagr;
+    AMDG_CK(cudaSetDevice(op->device));
+    if (amdg_status rs = burgers_sync(op); rs != AMDG_OK) return rs;
+    return wave_rk4(op, dt, nsteps, prec);
+}
+
+amdg_status amdg_wave_adaptive_step(amdg_wave_op* w, double cfl, double wave_speed, double eps, double eta,
+                                    amdg_precision prec, double* dt_out) {
+    AMDG_REQUIRE(w && std::isfinite(cfl) && cfl > 0 && std::isfinite(wave_speed) && wave_speed > 0, AMDG_ERR_ARG,
+                 "bad arguments");
+    AMDG_REQUIRE(prec == AMDG_PREC_FP64 || prec == AMDG_PREC_MIXED, AMDG_ERR_ARG, "bad precision");
+    amdg_burgers_op* op = w->lagr;
+    AMDG_CK(cudaSetDevice(op->device));
+    if (amdg_status rs = burgers_sync(op); rs != AMDG_OK) return rs;
+    amdg_grid* g = op->grid;
+    PhaseTimer timer(g->ctx, AMDG_PHASE_ADAPT_STEP);
+    cudaStream_t st = stream_of(op);
+    if (amdg_status s = ensure_velocity(g); s != AMDG_OK) return s;
+    const double dt = adaptive_dt(g, cfl, wave_speed);
+    // predictor: EulerODE2nd on copies of (u, v); only the predicted u is kept (the refine indicator)
+    op->rhs_evaluations++;
+    amdg_status s = eval_rhs(op, g->d_u, op->d_rhs64, prec);
+    if (s != AMDG_OK) return s;
+    AMDG_CK(launch_rk4_2nd_stage(-1, dt, op->d_rhs64, g->d_u, g->d_v, op->d_pred, op->d_su, nullptr, nullptr, g->dof, st));
+    g->ctx->launches++;
+    // refine on the predicted u; new elements start from zero in u and v (copy_predict_to_ucoe(_ut))
+    std::vector<double> norms;
+    if ((s = grid_norms(g, op->d_pred, &norms)) != AMDG_OK) return s;
+    std::vector<uint64_t> keys;
+    {
+        PhaseTimer th(g->ctx, AMDG_PHASE_ADAPT_HOST);
+        keys = refine_keys(g->host, norms.data(), eps);
+    }
+    if (int64_t(keys.size()) != g->host.num_elements && (s = grid_set_keys(g, std::move(keys))) != AMDG_OK) return s;
+    if ((s = burgers_sync(op)) != AMDG_OK) return s;
+    if ((s = wave_rk4(op, dt, 1, prec)) != AMDG_OK) return s;
+    if ((s = amdg_grid_coarsen(g, eta, nullptr)) != AMDG_OK) return s;
+    if (dt_out) *dt_out = dt;
+    return AMDG_OK;
+}
+
+amdg_status amdg_wave_counters(const amdg_wave_op* w, int64_t* stage_dof_updates, int64_t* rhs_evaluations) {
+    AMDG_REQUIRE(w, AMDG_ERR_ARG, "null operator");
+    return amdg_burgers_counters(w->lagr, stage_dof_updates, rhs_evaluations);
 }
 
 }  // extern "C"

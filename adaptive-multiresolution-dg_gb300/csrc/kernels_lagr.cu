@@ -64,7 +64,7 @@ __global__ void __launch_bounds__(256) sweep_kernel(SweepArgs<T> a) {
         n_from = a.n_in;
         n_to = a.n_out;
         coef = a.sweep == 0 ? T(D.coef) : T(1);
-        in = a.in + int64_t(slot) * a.in_slice;
+        in = a.sweep == 0 ? a.src[D.src] : a.in + int64_t(slot) * a.in_slice;
         // block shape: n_out along the dimensions already transformed, n_in elsewhere
         int done_after = 0;
         for (int j = 0; j < a.sweep; ++j) done_after += D.dims[j] > t ? 1 : 0;
@@ -232,5 +232,78 @@ cudaError_t launch_convert(const Ti* in, To* out, int64_t n, cudaStream_t st) {
 
 template cudaError_t launch_convert<double, float>(const double*, float*, int64_t, cudaStream_t);
 template cudaError_t launch_convert<float, double>(const float*, double*, int64_t, cudaStream_t);
+
+__global__ void reduce_points_coef_kernel(const double* __restrict__ buf, int count, int64_t E, int dim,
+                                          const int32_t* __restrict__ order, const double* __restrict__ pts,
+                                          double* __restrict__ out) {
+    int P = 1;
+    for (int d = 0; d < dim; ++d) P *= 4;
+    const int64_t n = E * P;
+    const int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    double v = 0.0;
+    for (int s = 0; s < count; ++s) v += buf[int64_t(s) * n + i];
+    const int64_t e = i / P;
+    int r = int(i - e * P);
+    // the coefficient function of the registered wave problem, at this point
+    const double pi = 3.14159265358979323846;
+    double x[kMaxDim];
+    for (int d = dim - 1; d >= 0; --d) {
+        x[d] = __ldg(pts + __ldg(order + e * dim + d) * 4 + r % 4);
+        r /= 4;
+    }
+    double prod = 1.0;
+    for (int d = 0; d < dim; ++d) prod *= sin(2 * pi * x[d]);
+    const double c = 1.0 + 0.5 * prod;
+    out[i] = (c * c) * v;
+}
+
+cudaError_t launch_reduce_points_coef(const double* buf, int count, int64_t E, int dim, const int32_t* order,
+                                      const double* pts, double* out, cudaStream_t st) {
+    int64_t n = E;
+    for (int d = 0; d < dim; ++d) n *= 4;
+    if (n == 0) return cudaSuccess;
+    reduce_points_coef_kernel<<<unsigned((n + 255) / 256), 256, 0, st>>>(buf, count, E, dim, order, pts, out);
+    return cudaGetLastError();
+}
+
+// Eigen evaluates each vector expression elementwise with one rounding per operation (no contraction)
+__global__ void rk4_2nd_stage_kernel(int stage, double dt, const double* __restrict__ rhs, double* un, double* vn,
+                                     double* us, double* vs, double* su, double* sv, int64_t n) {
+    const int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    if (stage < 0) {  // EulerODE2nd: u = u + dt v, v = v + dt rhs (ODESolver.cpp:409-414)
+        const double u0 = un[i], v0 = vn[i];
+        us[i] = __dadd_rn(u0, __dmul_rn(dt, v0));
+        vs[i] = __dadd_rn(v0, __dmul_rn(dt, rhs[i]));
+        return;
+    }
+    const double ku = __dmul_rn(dt, vs[i]), kv = __dmul_rn(dt, rhs[i]);
+    if (stage == 0) {
+        su[i] = ku;
+        sv[i] = kv;
+    } else if (stage < 3) {
+        su[i] = __dadd_rn(su[i], __dmul_rn(2.0, ku));
+        sv[i] = __dadd_rn(sv[i], __dmul_rn(2.0, kv));
+    }
+    if (stage < 2) {
+        us[i] = __dadd_rn(un[i], ku / 2.);
+        vs[i] = __dadd_rn(vn[i], kv / 2.);
+    } else if (stage == 2) {
+        us[i] = __dadd_rn(un[i], ku);
+        vs[i] = __dadd_rn(vn[i], kv);
+    } else {
+        const double tu = __dadd_rn(su[i], ku), tv = __dadd_rn(sv[i], kv);
+        un[i] = __dadd_rn(un[i], __dmul_rn(1. / 6., tu));
+        vn[i] = __dadd_rn(vn[i], __dmul_rn(1. / 6., tv));
+    }
+}
+
+cudaError_t launch_rk4_2nd_stage(int stage, double dt, const double* rhs, double* un, double* vn, double* us, double* vs,
+                                 double* su, double* sv, int64_t n, cudaStream_t st) {
+    if (n == 0) return cudaSuccess;
+    rk4_2nd_stage_kernel<<<unsigned((n + 255) / 256), 256, 0, st>>>(stage, dt, rhs, un, vn, us, vs, su, sv, n);
+    return cudaGetLastError();
+}
 
 }  // namespace amdg

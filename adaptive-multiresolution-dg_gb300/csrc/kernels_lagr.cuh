@@ -26,8 +26,9 @@ struct SweepArgs {
     const int32_t *vol_ptr, *vol_split, *flx_ptr, *flx_split;
     const int2 *vol_nbr, *flx_nbr; // (element, 1D order along t)
     const int32_t* order;          // [element][dim]
-    const T* in;
-    int64_t in_slice;              // entries per term slice of in (0: every term reads the same input)
+    const T* src[kMaxTermSources]; // sweep 0: term t reads src[t.src]
+    const T* in;                   // later sweeps: term slot s reads in + s * in_slice
+    int64_t in_slice;
     const T* pen_in;               // Alpert coefficients for kind-1 terms
     T* out;
     int out_block;                 // output entries per element (uniform over the range)
@@ -41,6 +42,18 @@ cudaError_t launch_sweep(const SweepArgs<T>& a, cudaStream_t st);
 // FluxFunction::burgers_flux_scalar, Interplation.cpp:5070-5073) instead.
 template <typename T>
 cudaError_t launch_reduce_points(const T* buf, int count, int64_t n, int first, T* acc, T* fp, cudaStream_t st);
+
+// Diffusion coefficient at the points: out = K(x) * sum_s buf[s] (in order), K = (1 + 0.5
+// prod_d sin(2 pi x_d))^2 at the point's coordinates (pts[order * 4 + p_d] per dimension).
+cudaError_t launch_reduce_points_coef(const double* buf, int count, int64_t E, int dim, const int32_t* order,
+                                      const double* pts, double* out, cudaStream_t st);
+
+// One RK4ODE2nd stage (ODESolver.cpp:579-615) given the right-hand side at (us, vs):
+// ku = dt vs, kv = dt rhs; stages 0-2 update (us, vs) from (un, vn) and the running sums
+// (su, sv); stage 3 writes un + su/6, vn + sv/6 into (un, vn).  EulerODE2nd (stage -1):
+// out_u = un + dt vn, out_v = vn + dt rhs into (us, vs).
+cudaError_t launch_rk4_2nd_stage(int stage, double dt, const double* rhs, double* un, double* vn, double* us, double* vs,
+                                 double* su, double* sv, int64_t n, cudaStream_t st);
 
 // Right-hand side: v = (first ? 0 : acc) + sum_s buf[s] (in order, in FP64);
 // not last: acc = v; last: out = rk_combine(rk, un, us, v) when stage is set,

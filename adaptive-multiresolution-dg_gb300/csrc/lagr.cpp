@@ -136,7 +136,7 @@ void build_lagr_ancestors(const Basis1D& alpt, LagrTables* t) {
     }
 }
 
-void build_lagr_tables(const Basis1D& alpt, LagrTables* t) {
+void build_lagr_tables(const Basis1D& alpt, LagrTables* t, bool diffusion) {
     static const GL10 g;
     const int n1 = alpt.num_elem(), na = alpt.num_basis(), np = alpt.k + 1, nl = n1 * 4;
     t->n_lagr = nl;
@@ -193,6 +193,51 @@ void build_lagr_tables(const Basis1D& alpt, LagrTables* t) {
             };
             // (ulft_vjp + urgt_vjp), HyperbolicLagrRHS::rhs_flx_intp_scalar (FastMultiplyLU.cpp:1166)
             t->lflx[idx] = (edge(-1, 1) - edge(-1, -1)) + (edge(1, 1) - edge(1, -1));
+        }
+    }
+    if (diffusion) {
+        // Alpert derivative at the Lagrange points (Lag_pt_Alpt_1D_d1, Interplation.cpp:16-101)
+        // and the point coordinates
+        t->a2pd.assign(size_t(na) * nl, 0.0);
+        t->pts.assign(nl, 0.0);
+        for (int c = 0; c < nl; ++c) {
+            const double x = lagr_point(c / 4, c % 4);
+            t->pts[c] = x;
+            for (int r = 0; r < na; ++r) {
+                const int o = r / np;
+                if (x < supp_lo(o) || x > supp_hi(o)) continue;
+                t->a2pd[size_t(r) * nl + c] = alpt.eval(r, 1, x, 0);
+            }
+        }
+        // [u] times the one-sided v_x at u's discontinuities: ujp_vxlft + ujp_vxrgt
+        // (OperatorMatrix1D.h:206-211, Basis::product_edge_dis_u, Basis.cpp:175-230)
+        t->ljv.assign(size_t(nl) * na, 0.0);
+#pragma omp parallel for schedule(dynamic)
+        for (int r = 0; r < nl; ++r) {
+            const int ou = r / 4;
+            const double ua = supp_lo(ou), ub = supp_hi(ou);
+            const double pts[3] = {ua, 0.5 * (ua + ub), ub};
+            const int npts = level_of_order(ou) <= 1 ? 2 : 3;
+            for (int c = 0; c < na; ++c) {
+                auto edge = [&](int su, int sv) {
+                    double s = 0.0;
+                    for (int i = 0; i < npts; ++i) {
+                        const double x = pts[i];
+                        double fu = lagr_eval(r, x, su), fw = alpt.eval(c, 1, x, sv);
+                        if (std::fabs(x) < kRoundOff) {
+                            if (su == -1) fu = lagr_eval(r, 1.0, su);
+                            if (sv == -1) fw = alpt.eval(c, 1, 1.0, sv);
+                        } else if (std::fabs(x - 1.0) < kRoundOff) {
+                            if (su == 1) fu = lagr_eval(r, 0.0, su);
+                            if (sv == 1) fw = alpt.eval(c, 1, 0.0, sv);
+                        }
+                        s += fu * fw;
+                    }
+                    return s;
+                };
+                const double lft = edge(1, -1) - edge(-1, -1), rgt = edge(1, 1) - edge(-1, 1);
+                t->ljv[size_t(r) * na + c] = lft + rgt;
+            }
         }
     }
     // Alpert x Alpert jump-jump (ujp_vjp = urgt_vjp - ulft_vjp), LxF penalty

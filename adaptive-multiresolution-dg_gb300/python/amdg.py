@@ -97,6 +97,14 @@ def load():
         "amdg_grid_version": ([vp, C.POINTER(i64)], i32),
         "amdg_grid_l2_error_separable_sum": ([vp, i32, FN1D, vp, dbl, C.POINTER(dbl)], i32),
         "amdg_grid_eval_tensor": ([vp, i32, vp, vp], i32),
+        "amdg_grid_set_velocity": ([vp, vp, i64], i32),
+        "amdg_grid_get_velocity": ([vp, vp, i64], i32),
+        "amdg_wave_create": ([vp, dbl, pp], i32),
+        "amdg_wave_destroy": ([vp], i32),
+        "amdg_wave_rhs": ([vp, vp, vp, i32], i32),
+        "amdg_wave_rk4_steps": ([vp, dbl, i32, i32], i32),
+        "amdg_wave_adaptive_step": ([vp, dbl, dbl, dbl, dbl, i32, C.POINTER(dbl)], i32),
+        "amdg_wave_counters": ([vp, C.POINTER(i64), C.POINTER(i64)], i32),
         "amdg_context_profile": ([vp, i32], i32),
         "amdg_context_profile_read": ([vp, vp, vp], i32),
         "amdg_burgers_counters": ([vp, C.POINTER(i64), C.POINTER(i64)], i32),
@@ -293,6 +301,15 @@ class Grid:
             "grid_l2_error_separable_sum")
         return r.value
 
+    def set_velocity(self, v: np.ndarray):
+        v = np.ascontiguousarray(v, np.float64).reshape(-1)
+        _ck(load().amdg_grid_set_velocity(self._h, _ptr(v), v.size), "grid_set_velocity")
+
+    def velocity(self) -> np.ndarray:
+        out = np.zeros((self.num_elements, self.block))
+        _ck(load().amdg_grid_get_velocity(self._h, _ptr(out), out.size), "grid_get_velocity")
+        return out
+
     def eval_tensor_device(self, x1d, d_out: int):
         """u_h on the tensor mesh x1d^dim into d_out (device, len(x1d)^dim doubles, last index fastest)."""
         x = np.ascontiguousarray(x1d, np.float64).reshape(-1)
@@ -432,6 +449,45 @@ class BurgersOperator:
     def close(self):
         if self._h:
             load().amdg_burgers_destroy(self._h)
+            self._h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class WaveOperator:
+    """u_tt = div(K grad u), K = (1 + 0.5 prod sin(2 pi x_d))^2, interpolated K grad u and K u,
+    DiffusionRHS terms and the IPDG penalty (sigma), on the device."""
+
+    def __init__(self, grid: Grid, sigma: float):
+        self.grid = grid
+        self._h = C.c_void_p()
+        _ck(load().amdg_wave_create(grid.handle, sigma, C.byref(self._h)), "wave_create")
+
+    def rhs_device(self, d_u: int, d_rhs: int, prec: int = FP64):
+        _ck(load().amdg_wave_rhs(self._h, C.c_void_p(d_u), C.c_void_p(d_rhs), prec), "wave_rhs")
+
+    def rk4_steps(self, dt: float, nsteps: int, prec: int = FP64):
+        _ck(load().amdg_wave_rk4_steps(self._h, dt, nsteps, prec), "wave_rk4_steps")
+
+    def adaptive_step(self, cfl: float, wave_speed: float, eps: float, eta: float, prec: int = FP64) -> float:
+        dt = C.c_double()
+        _ck(load().amdg_wave_adaptive_step(self._h, cfl, wave_speed, eps, eta, prec, C.byref(dt)),
+            "wave_adaptive_step")
+        self.grid._refresh()
+        return dt.value
+
+    def counters(self):
+        a, b = C.c_int64(), C.c_int64()
+        _ck(load().amdg_wave_counters(self._h, C.byref(a), C.byref(b)), "wave_counters")
+        return a.value, b.value
+
+    def close(self):
+        if self._h:
+            load().amdg_wave_destroy(self._h)
             self._h = C.c_void_p()
 
     def __del__(self):

@@ -57,6 +57,7 @@ typedef struct amdg_linear_op amdg_linear_op;
 typedef struct amdg_burgers_op amdg_burgers_op;
 typedef struct amdg_batch amdg_batch;
 typedef struct amdg_mlp amdg_mlp;
+typedef struct amdg_wave_op amdg_wave_op;
 
 /* Separable 1D factor g_d(x) of term `term` (the std::function<double(double,int)>
  * the reference takes, DGAdapt.h:17-38). */
@@ -309,6 +310,34 @@ amdg_status amdg_burgers_adaptive_step(amdg_burgers_op* op, double cfl, double w
  * the labels the learned classifier is trained on. */
 amdg_status amdg_burgers_adaptive_step_ex(amdg_burgers_op* op, double cfl, double wave_speed, double eps, double eta,
                                           amdg_precision prec, double* dt_out, int8_t* decisions);
+
+/* ---- second-order wave equation (config of 03_wave_06_var_coeff_adapt.cpp) ---- */
+/* Second field v = u_t of the grid (Element::ucoe_ut), dof entries, remapped with u when the
+ * element set changes (new elements zero).  A grid without one reads as v = 0 in the wave
+ * calls below, which create it. */
+amdg_status amdg_grid_set_velocity(amdg_grid* g, const double* host, int64_t n);
+amdg_status amdg_grid_get_velocity(const amdg_grid* g, double* host, int64_t n);
+
+/* u_tt = div(K grad u) on the periodic unit cube, K = (1 + 0.5 prod_d sin(2 pi x_d))^2, Alpert
+ * k = 2: K u_{x_d} and K u interpolated by degree-3 Lagrange (LagrInterpolation::
+ * var_coeff_gradu_Lagr_fast / var_coeff_u_Lagr_fast, Interplation.cpp:4159-4212), the
+ * DiffusionRHS terms rhs_flx_gradu, rhs_vol, rhs_flx_u (FastMultiplyLU.cpp:1691-1765) and the
+ * IPDG penalty -sigma/dx [u][v], dx the finest element size
+ * (DiffusionAlpt::assemble_matrix_flx_ujp_vjp, BilinearForm.cpp:920-929), evaluated matrix free. */
+amdg_status amdg_wave_create(amdg_grid* g, double sigma, amdg_wave_op** out);
+amdg_status amdg_wave_destroy(amdg_wave_op* op);
+/* d_rhs = L(d_u) (device arrays, dof entries). */
+amdg_status amdg_wave_rhs(amdg_wave_op* op, const double* d_u, double* d_rhs, amdg_precision prec);
+/* nsteps RK4ODE2nd steps of u' = v, v' = L u on the grid's (u, v)
+ * (RK4ODE2nd::step_stage, ODESolver.cpp:579-615). */
+amdg_status amdg_wave_rk4_steps(amdg_wave_op* op, double dt, int nsteps, amdg_precision prec);
+/* One adaptive step, the loop body of 03_wave_06_var_coeff_adapt.cpp:195-265 without source:
+ * dt = cfl / sum_d wave_speed 2^maxlevel_d, EulerODE2nd predictor, refine on the predicted u,
+ * one RK4ODE2nd step, coarsen on u. */
+amdg_status amdg_wave_adaptive_step(amdg_wave_op* op, double cfl, double wave_speed, double eps, double eta,
+                                    amdg_precision prec, double* dt_out);
+/* As amdg_burgers_counters (4 x DOF per RK4ODE2nd step). */
+amdg_status amdg_wave_counters(const amdg_wave_op* op, int64_t* stage_dof_updates, int64_t* rhs_evaluations);
 
 /* ---- learned refine/coarsen (no reference counterpart) -------------------- */
 /* Per-element classifier refine / keep / coarsen: n_in -> n_hidden_layers x

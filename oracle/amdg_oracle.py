@@ -489,6 +489,30 @@ def burgers_adaptive_run(dim, n_init, nmax, eps, eta, alpha, cfl, umax, steps, k
     return history
 
 
+def wave_adaptive_run(dim, n_init, nmax, eps, eta, sigma, cfl, speed, steps, k=2):
+    """The adaptive wave loop of 03_wave_06_var_coeff_adapt.cpp without source: EulerODE2nd
+    predictor, refine on the predicted u, RK4ODE2nd step, coarsen on u; u0 the Gaussian bump,
+    v0 = 0."""
+    keys, u = init_adaptive_separable(dim, n_init, nmax, k, wave_ic_terms(dim), eps)
+    v = np.zeros_like(u)
+    history = [(list(keys), u.copy(), v.copy(), None)]
+    for _ in range(steps):
+        lv, sp = keys_to_arrays(keys, dim)
+        maxlev = lv.max(axis=0)
+        dt = cfl / sum(speed * 2.0 ** int(m) for m in maxlev)
+        pred = u + dt * v
+        new_keys = refine_keys(keys, element_norms(pred), eps, nmax)
+        u, v = remap(keys, u, new_keys), remap(keys, v, new_keys)
+        keys = new_keys
+        lv, sp = keys_to_arrays(keys, dim)
+        u, v = wave_rk4(dim, nmax, k, lv, sp, u, v, sigma, dt, 1)
+        new_keys = coarsen_keys(keys, element_norms(u), eta)
+        u, v = remap(keys, u, new_keys), remap(keys, v, new_keys)
+        keys = new_keys
+        history.append((list(keys), u.copy(), v.copy(), dt))
+    return history
+
+
 # ---------------------------------------------------------------------------
 # Batched-serving workload: sums of periodic Gaussian bumps (separable terms)
 # ---------------------------------------------------------------------------

@@ -1,0 +1,101 @@
+"""The second-order wave path (u_tt = div(K grad u): interpolated K grad u and K u,
+DiffusionRHS terms, IPDG penalty, RK4ODE2nd) on the GPU against the reference fixtures and
+the oracle.  FP64: 1e-12 relative (max norm) for the right-hand side and RK4 steps;
+mixed (FP64 point values and surplus, FP32 back transforms): 1e-4 relative in L2 for one
+right-hand side (the IPDG penalty makes it a difference of large terms) and 1e-6 for steps."""
+import numpy as np
+import pytest
+
+import amdg
+import amdg_oracle as O
+from helpers import align, golden, manifest, rel_err
+
+pytestmark = pytest.mark.gpu
+torch = pytest.importorskip("torch")
+
+WAVE = [n for n, m in manifest().items() if m["kind"] == "wave"]
+
+
+def _on_device(u):
+    torch.cuda.synchronize()
+    return torch.from_numpy(np.ascontiguousarray(u).reshape(-1)).cuda()
+
+
+@pytest.mark.parametrize("name", WAVE)
+def test_wave_matches_reference(ctx, name):
+    m = manifest()[name]
+    z = golden(name)
+    dim, N = m["dim"], m["N"]
+    g = amdg.Grid(ctx, dim, N, 2)
+    lv, sp = g.elements()
+    perm = align(z["level"], z["suppt"], lv, sp)
+    u0 = np.ascontiguousarray(z["u0"][perm])
+    op = amdg.WaveOperator(g, m["sigma"])
+    du = _on_device(u0)
+    out = torch.zeros_like(du)
+    torch.cuda.synchronize()
+    op.rhs_device(du.data_ptr(), out.data_ptr())
+    ctx.synchronize()
+    ref = z["rhs0"][perm]
+    assert rel_err(out.cpu().numpy().reshape(ref.shape), ref) < 1e-12
+    op.rhs_device(du.data_ptr(), out.data_ptr(), amdg.MIXED)
+    ctx.synchronize()
+    r32 = out.cpu().numpy().reshape(ref.shape)
+    assert np.linalg.norm(r32 - ref) / np.linalg.norm(ref) < 1e-4
+    for prec, tol in ((amdg.FP64, 1e-12), (amdg.MIXED, 1e-6)):
+        g.set_coefficients(u0)
+        g.set_velocity(np.zeros_like(u0))
+        op.rk4_steps(m["dt"], m["steps"], prec)
+        ctx.synchronize()
+        assert rel_err(g.coefficients(), z["uT"][perm]) < tol
+        assert rel_err(g.velocity(), z["vT"][perm]) < tol * 10
+    op.close()
+    g.close()
+
+
+def test_wave_rhs_matches_oracle_on_random_state(ctx):
+    dim, N = 2, 6
+    g = amdg.Grid(ctx, dim, N, 2)
+    rng = np.random.default_rng(4)
+    u = rng.standard_normal((g.num_elements, g.block))
+    op = amdg.WaveOperator(g, 10.0)
+    du = _on_device(u)
+    out = torch.zeros_like(du)
+    torch.cuda.synchronize()
+    op.rhs_device(du.data_ptr(), out.data_ptr())
+    ctx.synchronize()
+    lv, sp = g.elements()
+    ref = O.wave_rhs(dim, N, 2, lv, sp, u, 10.0)
+    assert rel_err(out.cpu().numpy().reshape(ref.shape), ref) < 1e-12
+    op.close()
+    g.close()
+
+
+def test_adaptive_wave_matches_oracle(ctx):
+    """Element sets identical to the oracle's adaptive loop after every step, (u, v) to 1e-12."""
+    dim, nmax, eps, eta, sigma, cfl = 2, 6, 1e-4, 1e-5, 10.0, 0.1
+    steps = 3
+    hist = O.wave_adaptive_run(dim, 3, nmax, eps, eta, sigma, cfl, 1.0, steps)
+    g = amdg.Grid(ctx, dim, nmax, 2, level_init=3)
+    g.init_separable_adaptive(O.wave_ic_terms(dim), eps)
+    op = amdg.WaveOperator(g, sigma)
+    def check(keys, u, v):
+        lv, sp = g.elements()
+        mine = O.arrays_to_keys(lv, sp)
+        assert set(mine) == set(keys)
+        pos = {k: j for j, k in enumerate(keys)}
+        perm = np.array([pos[k] for k in mine])
+        assert rel_err(g.coefficients(), u[perm]) < 1e-12
+        if np.abs(v).max() > 0:
+            assert rel_err(g.velocity(), v[perm]) < 1e-11
+
+    check(hist[0][0], hist[0][1], hist[0][2])
+    for s in range(steps):
+        dt = op.adaptive_step(cfl, 1.0, eps, eta)
+        keys, u, v, dt_ref = hist[s + 1]
+        assert dt == dt_ref
+        check(keys, u, v)
+    stage_dof, rhs = op.counters()
+    assert rhs == 5 * steps
+    op.close()
+    g.close()
