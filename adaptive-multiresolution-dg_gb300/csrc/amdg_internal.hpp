@@ -266,6 +266,7 @@ struct amdg_linear_op {
 struct amdg_burgers_op {
     int kind = 0;                    // 0: Burgers flux u^2/2; 1: wave u_tt = div(K grad u) (amdg_wave_op)
     double sigma = 0.0;              // wave: IPDG penalty parameter
+    double amp = 0.5;                // wave: K = (1 + amp prod_d sin(2 pi x_d))^2
     int64_t built_version = -1;
     int64_t capacity = 0;            // elements the work buffers can hold
     amdg_grid* grid = nullptr;

@@ -322,10 +322,10 @@ amdg_status eval_wave_fields(amdg_burgers_op* op, const double* u, To** fucoe, c
             if (c0 + cnt == G) {
                 if (c0 > 0) {  // earlier chunks were summed into acc: fold them in as one more slice
                     AMDG_CK(launch_reduce_points<double>(slots, cnt, n, 0, acc, nullptr, st));
-                    AMDG_CK(launch_reduce_points_coef(acc, 1, E, dim, g->d_order, op->d_pts, kp, st));
+                    AMDG_CK(launch_reduce_points_coef(acc, 1, E, dim, g->d_order, op->d_pts, op->amp, kp, st));
                     op->grid->ctx->launches++;
                 } else {
-                    AMDG_CK(launch_reduce_points_coef(slots, cnt, E, dim, g->d_order, op->d_pts, kp, st));
+                    AMDG_CK(launch_reduce_points_coef(slots, cnt, E, dim, g->d_order, op->d_pts, op->amp, kp, st));
                 }
             } else {
                 AMDG_CK(launch_reduce_points<double>(slots, cnt, n, c0 == 0 ? 1 : 0, acc, nullptr, st));
@@ -716,8 +716,20 @@ static void mark_removed(const std::vector<uint64_t>& old_keys, const HostGrid& 
         if (!std::binary_search(now.key.begin(), now.key.end(), old_keys[e])) decisions[e] = 2;
 }
 
-amdg_status amdg_burgers_adaptive_step_ex(amdg_burgers_op* op, double cfl, double wave_speed, double eps, double eta,
-                                          amdg_precision prec, double* dt_out, int8_t* decisions) {
+static amdg_status wave_rk4(amdg_burgers_op* op, double dt, int nsteps, amdg_precision prec);
+static amdg_status ensure_velocity(amdg_grid* g);
+
+// one time step of the operator's scheme: SSP-RK3 (Burgers) or RK4ODE2nd (wave)
+static amdg_status one_step(amdg_burgers_op* op, double dt, amdg_precision prec) {
+    if (op->kind == 0) return amdg_burgers_rk3_steps(op, dt, 1, prec);
+    if (amdg_status s = burgers_sync(op); s != AMDG_OK) return s;
+    return wave_rk4(op, dt, 1, prec);
+}
+
+// the adaptive time step of either operator: predictor (ForwardEuler / EulerODE2nd on u),
+// refine on the predicted u, one step, coarsen
+static amdg_status adaptive_step_any(amdg_burgers_op* op, double cfl, double wave_speed, double eps, double eta,
+                                     amdg_precision prec, double* dt_out, int8_t* decisions) {
     AMDG_REQUIRE(op && std::isfinite(cfl) && cfl > 0 && std::isfinite(wave_speed) && wave_speed > 0, AMDG_ERR_ARG,
                  "bad arguments");
     AMDG_REQUIRE(prec == AMDG_PREC_FP64 || prec == AMDG_PREC_MIXED, AMDG_ERR_ARG, "bad precision");
@@ -725,13 +737,23 @@ amdg_status amdg_burgers_adaptive_step_ex(amdg_burgers_op* op, double cfl, doubl
     if (amdg_status rs = burgers_sync(op); rs != AMDG_OK) return rs;
     amdg_grid* g = op->grid;
     PhaseTimer timer(g->ctx, AMDG_PHASE_ADAPT_STEP);
+    cudaStream_t st = stream_of(op);
     const double dt = adaptive_dt(g, cfl, wave_speed);
     const std::vector<uint64_t> old_keys = g->host.key;
-    // predictor: forward Euler into the prediction buffer (ForwardEuler::step_stage)
     op->rhs_evaluations++;
-    const StageOut so{1, stage_coef(0, dt), g->d_u, g->d_u, op->d_pred};
-    amdg_status s = eval_rhs(op, g->d_u, op->d_rhs64, prec, so);
-    if (s != AMDG_OK) return s;
+    amdg_status s;
+    if (op->kind == 0) {
+        // forward Euler into the prediction buffer (ForwardEuler::step_stage)
+        const StageOut so{1, stage_coef(0, dt), g->d_u, g->d_u, op->d_pred};
+        if ((s = eval_rhs(op, g->d_u, op->d_rhs64, prec, so)) != AMDG_OK) return s;
+    } else {
+        // EulerODE2nd on copies of (u, v) (ODESolver.cpp:409-414); only the predicted u is kept
+        if ((s = ensure_velocity(g)) != AMDG_OK) return s;
+        if ((s = eval_rhs(op, g->d_u, op->d_rhs64, prec)) != AMDG_OK) return s;
+        AMDG_CK(launch_rk4_2nd_stage(-1, dt, op->d_rhs64, g->d_u, g->d_v, op->d_pred, op->d_su, nullptr, nullptr, g->dof,
+                                     st));
+        g->ctx->launches++;
+    }
     // refine on the predicted coefficients; new elements start from zero (DGAdapt::refine, copy_predict_to_ucoe)
     std::vector<double> norms;
     if ((s = grid_norms(g, op->d_pred, &norms)) != AMDG_OK) return s;
@@ -744,16 +766,21 @@ amdg_status amdg_burgers_adaptive_step_ex(amdg_burgers_op* op, double cfl, doubl
     if (decisions)
         for (size_t e = 0; e < refined.size(); ++e) decisions[e] = refined[e] ? 1 : 0;
     if (int64_t(keys.size()) != g->host.num_elements && (s = grid_set_keys(g, std::move(keys))) != AMDG_OK) return s;
-    if ((s = amdg_burgers_rk3_steps(op, dt, 1, prec)) != AMDG_OK) return s;
+    if ((s = one_step(op, dt, prec)) != AMDG_OK) return s;
     if ((s = amdg_grid_coarsen(g, eta, nullptr)) != AMDG_OK) return s;
     if (decisions) mark_removed(old_keys, g->host, decisions);
     if (dt_out) *dt_out = dt;
     return AMDG_OK;
 }
 
+amdg_status amdg_burgers_adaptive_step_ex(amdg_burgers_op* op, double cfl, double wave_speed, double eps, double eta,
+                                          amdg_precision prec, double* dt_out, int8_t* decisions) {
+    return adaptive_step_any(op, cfl, wave_speed, eps, eta, prec, dt_out, decisions);
+}
+
 amdg_status amdg_burgers_adaptive_step(amdg_burgers_op* op, double cfl, double wave_speed, double eps, double eta,
                                        amdg_precision prec, double* dt_out) {
-    return amdg_burgers_adaptive_step_ex(op, cfl, wave_speed, eps, eta, prec, dt_out, nullptr);
+    return adaptive_step_any(op, cfl, wave_speed, eps, eta, prec, dt_out, nullptr);
 }
 
 amdg_status amdg_burgers_features(amdg_burgers_op* op, const double* d_u, float* d_features) {
@@ -767,9 +794,8 @@ amdg_status amdg_burgers_features(amdg_burgers_op* op, const double* d_u, float*
     return AMDG_OK;
 }
 
-amdg_status amdg_burgers_adaptive_step_learned(amdg_burgers_op* op, amdg_mlp* mlp, double cfl, double wave_speed,
-                                               double eps, double eta, double tau, amdg_precision prec, double* dt_out,
-                                               int64_t* stats) {
+static amdg_status learned_step_any(amdg_burgers_op* op, amdg_mlp* mlp, double cfl, double wave_speed, double eps,
+                                    double eta, double tau, amdg_precision prec, double* dt_out, int64_t* stats) {
     AMDG_REQUIRE(op && mlp && std::isfinite(cfl) && cfl > 0 && std::isfinite(wave_speed) && wave_speed > 0, AMDG_ERR_ARG,
                  "bad arguments");
     AMDG_REQUIRE(prec == AMDG_PREC_FP64 || prec == AMDG_PREC_MIXED, AMDG_ERR_ARG, "bad precision");
@@ -826,8 +852,8 @@ amdg_status amdg_burgers_adaptive_step_learned(amdg_burgers_op* op, amdg_mlp* ml
         std::vector<uint64_t> keys = refine_keys(g->host, norms.data(), eps, nullptr, force.data());
         if (int64_t(keys.size()) != g->host.num_elements && (s = grid_set_keys(g, std::move(keys))) != AMDG_OK) return s;
     }
-    // 3. one SSP-RK3 step, no predictor step
-    if ((s = amdg_burgers_rk3_steps(op, dt, 1, prec)) != AMDG_OK) return s;
+    // 3. one time step, no predictor step
+    if ((s = one_step(op, dt, prec)) != AMDG_OK) return s;
     // 4. coarsening (amdg_grid_coarsen), then the surplus criterion judges the
     //    result: leaves still above eps are missed refinements, refined at the
     //    start of the next step
@@ -857,6 +883,12 @@ amdg_status amdg_burgers_adaptive_step_learned(amdg_burgers_op* op, amdg_mlp* ml
     return AMDG_OK;
 }
 
+amdg_status amdg_burgers_adaptive_step_learned(amdg_burgers_op* op, amdg_mlp* mlp, double cfl, double wave_speed,
+                                               double eps, double eta, double tau, amdg_precision prec, double* dt_out,
+                                               int64_t* stats) {
+    return learned_step_any(op, mlp, cfl, wave_speed, eps, eta, tau, prec, dt_out, stats);
+}
+
 amdg_status amdg_burgers_counters(const amdg_burgers_op* op, int64_t* stage_dof_updates, int64_t* rhs_evaluations) {
     AMDG_REQUIRE(op, AMDG_ERR_ARG, "null operator");
     if (stage_dof_updates) *stage_dof_updates = op->stage_dof_updates;
@@ -866,12 +898,14 @@ amdg_status amdg_burgers_counters(const amdg_burgers_op* op, int64_t* stage_dof_
 
 // ---- wave equation u_tt = div(K grad u) (03_wave_06_var_coeff_adapt.cpp) -----------------
 
-amdg_status amdg_wave_create(amdg_grid* g, double sigma, amdg_wave_op** out) {
-    AMDG_REQUIRE(g && out && std::isfinite(sigma) && sigma >= 0, AMDG_ERR_ARG, "bad arguments");
+amdg_status amdg_wave_create(amdg_grid* g, double sigma, double amplitude, amdg_wave_op** out) {
+    AMDG_REQUIRE(g && out && std::isfinite(sigma) && sigma >= 0 && std::isfinite(amplitude), AMDG_ERR_ARG,
+                 "bad arguments");
     *out = nullptr;
     amdg_wave_op* w = new (std::nothrow) amdg_wave_op;
     AMDG_REQUIRE(w, AMDG_ERR_NOMEM, "host allocation failed");
     amdg_status s = lagr_create(g, 1, nullptr, sigma, &w->lagr);
+    if (s == AMDG_OK) w->lagr->amp = amplitude;
     if (s != AMDG_OK) {
         delete w;
         return s;
@@ -941,37 +975,25 @@ amdg_status amdg_wave_rk4_steps(amdg_wave_op* w, double dt, int nsteps, amdg_pre
 
 amdg_status amdg_wave_adaptive_step(amdg_wave_op* w, double cfl, double wave_speed, double eps, double eta,
                                     amdg_precision prec, double* dt_out) {
-    AMDG_REQUIRE(w && std::isfinite(cfl) && cfl > 0 && std::isfinite(wave_speed) && wave_speed > 0, AMDG_ERR_ARG,
-                 "bad arguments");
-    AMDG_REQUIRE(prec == AMDG_PREC_FP64 || prec == AMDG_PREC_MIXED, AMDG_ERR_ARG, "bad precision");
-    amdg_burgers_op* op = w->lagr;
-    AMDG_CK(cudaSetDevice(op->device));
-    if (amdg_status rs = burgers_sync(op); rs != AMDG_OK) return rs;
-    amdg_grid* g = op->grid;
-    PhaseTimer timer(g->ctx, AMDG_PHASE_ADAPT_STEP);
-    cudaStream_t st = stream_of(op);
-    if (amdg_status s = ensure_velocity(g); s != AMDG_OK) return s;
-    const double dt = adaptive_dt(g, cfl, wave_speed);
-    // predictor: EulerODE2nd on copies of (u, v); only the predicted u is kept (the refine indicator)
-    op->rhs_evaluations++;
-    amdg_status s = eval_rhs(op, g->d_u, op->d_rhs64, prec);
-    if (s != AMDG_OK) return s;
-    AMDG_CK(launch_rk4_2nd_stage(-1, dt, op->d_rhs64, g->d_u, g->d_v, op->d_pred, op->d_su, nullptr, nullptr, g->dof, st));
-    g->ctx->launches++;
-    // refine on the predicted u; new elements start from zero in u and v (copy_predict_to_ucoe(_ut))
-    std::vector<double> norms;
-    if ((s = grid_norms(g, op->d_pred, &norms)) != AMDG_OK) return s;
-    std::vector<uint64_t> keys;
-    {
-        PhaseTimer th(g->ctx, AMDG_PHASE_ADAPT_HOST);
-        keys = refine_keys(g->host, norms.data(), eps);
-    }
-    if (int64_t(keys.size()) != g->host.num_elements && (s = grid_set_keys(g, std::move(keys))) != AMDG_OK) return s;
-    if ((s = burgers_sync(op)) != AMDG_OK) return s;
-    if ((s = wave_rk4(op, dt, 1, prec)) != AMDG_OK) return s;
-    if ((s = amdg_grid_coarsen(g, eta, nullptr)) != AMDG_OK) return s;
-    if (dt_out) *dt_out = dt;
-    return AMDG_OK;
+    AMDG_REQUIRE(w, AMDG_ERR_ARG, "null operator");
+    return adaptive_step_any(w->lagr, cfl, wave_speed, eps, eta, prec, dt_out, nullptr);
+}
+
+amdg_status amdg_wave_adaptive_step_ex(amdg_wave_op* w, double cfl, double wave_speed, double eps, double eta,
+                                       amdg_precision prec, double* dt_out, int8_t* decisions) {
+    AMDG_REQUIRE(w, AMDG_ERR_ARG, "null operator");
+    return adaptive_step_any(w->lagr, cfl, wave_speed, eps, eta, prec, dt_out, decisions);
+}
+
+amdg_status amdg_wave_features(amdg_wave_op* w, const double* d_u, float* d_features) {
+    AMDG_REQUIRE(w, AMDG_ERR_ARG, "null operator");
+    return amdg_burgers_features(w->lagr, d_u, d_features);
+}
+
+amdg_status amdg_wave_adaptive_step_learned(amdg_wave_op* w, amdg_mlp* mlp, double cfl, double wave_speed, double eps,
+                                            double eta, double tau, amdg_precision prec, double* dt_out, int64_t* stats) {
+    AMDG_REQUIRE(w, AMDG_ERR_ARG, "null operator");
+    return learned_step_any(w->lagr, mlp, cfl, wave_speed, eps, eta, tau, prec, dt_out, stats);
 }
 
 amdg_status amdg_wave_counters(const amdg_wave_op* w, int64_t* stage_dof_updates, int64_t* rhs_evaluations) {

@@ -234,7 +234,7 @@ template cudaError_t launch_convert<double, float>(const double*, float*, int64_
 template cudaError_t launch_convert<float, double>(const float*, double*, int64_t, cudaStream_t);
 
 __global__ void reduce_points_coef_kernel(const double* __restrict__ buf, int count, int64_t E, int dim,
-                                          const int32_t* __restrict__ order, const double* __restrict__ pts,
+                                          const int32_t* __restrict__ order, const double* __restrict__ pts, double amp,
                                           double* __restrict__ out) {
     int P = 1;
     for (int d = 0; d < dim; ++d) P *= 4;
@@ -254,16 +254,16 @@ __global__ void reduce_points_coef_kernel(const double* __restrict__ buf, int co
     }
     double prod = 1.0;
     for (int d = 0; d < dim; ++d) prod *= sin(2 * pi * x[d]);
-    const double c = 1.0 + 0.5 * prod;
+    const double c = 1.0 + amp * prod;
     out[i] = (c * c) * v;
 }
 
 cudaError_t launch_reduce_points_coef(const double* buf, int count, int64_t E, int dim, const int32_t* order,
-                                      const double* pts, double* out, cudaStream_t st) {
+                                      const double* pts, double amp, double* out, cudaStream_t st) {
     int64_t n = E;
     for (int d = 0; d < dim; ++d) n *= 4;
     if (n == 0) return cudaSuccess;
-    reduce_points_coef_kernel<<<unsigned((n + 255) / 256), 256, 0, st>>>(buf, count, E, dim, order, pts, out);
+    reduce_points_coef_kernel<<<unsigned((n + 255) / 256), 256, 0, st>>>(buf, count, E, dim, order, pts, amp, out);
     return cudaGetLastError();
 }
 

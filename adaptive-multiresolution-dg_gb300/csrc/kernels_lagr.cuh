@@ -43,10 +43,10 @@ cudaError_t launch_sweep(const SweepArgs<T>& a, cudaStream_t st);
 template <typename T>
 cudaError_t launch_reduce_points(const T* buf, int count, int64_t n, int first, T* acc, T* fp, cudaStream_t st);
 
-// Diffusion coefficient at the points: out = K(x) * sum_s buf[s] (in order), K = (1 + 0.5
+// Diffusion coefficient at the points: out = K(x) * sum_s buf[s] (in order), K = (1 + amp
 // prod_d sin(2 pi x_d))^2 at the point's coordinates (pts[order * 4 + p_d] per dimension).
 cudaError_t launch_reduce_points_coef(const double* buf, int count, int64_t E, int dim, const int32_t* order,
-                                      const double* pts, double* out, cudaStream_t st);
+                                      const double* pts, double amp, double* out, cudaStream_t st);
 
 // One RK4ODE2nd stage (ODESolver.cpp:579-615) given the right-hand side at (us, vs):
 // ku = dt vs, kv = dt rhs; stages 0-2 update (us, vs) from (un, vn) and the running sums

@@ -99,12 +99,15 @@ def load():
         "amdg_grid_eval_tensor": ([vp, i32, vp, vp], i32),
         "amdg_grid_set_velocity": ([vp, vp, i64], i32),
         "amdg_grid_get_velocity": ([vp, vp, i64], i32),
-        "amdg_wave_create": ([vp, dbl, pp], i32),
+        "amdg_wave_create": ([vp, dbl, dbl, pp], i32),
         "amdg_wave_destroy": ([vp], i32),
         "amdg_wave_rhs": ([vp, vp, vp, i32], i32),
         "amdg_wave_rk4_steps": ([vp, dbl, i32, i32], i32),
         "amdg_wave_adaptive_step": ([vp, dbl, dbl, dbl, dbl, i32, C.POINTER(dbl)], i32),
         "amdg_wave_counters": ([vp, C.POINTER(i64), C.POINTER(i64)], i32),
+        "amdg_wave_adaptive_step_ex": ([vp, dbl, dbl, dbl, dbl, i32, C.POINTER(dbl), vp], i32),
+        "amdg_wave_features": ([vp, vp, vp], i32),
+        "amdg_wave_adaptive_step_learned": ([vp, vp, dbl, dbl, dbl, dbl, dbl, i32, C.POINTER(dbl), vp], i32),
         "amdg_context_profile": ([vp, i32], i32),
         "amdg_context_profile_read": ([vp, vp, vp], i32),
         "amdg_burgers_counters": ([vp, C.POINTER(i64), C.POINTER(i64)], i32),
@@ -459,13 +462,13 @@ class BurgersOperator:
 
 
 class WaveOperator:
-    """u_tt = div(K grad u), K = (1 + 0.5 prod sin(2 pi x_d))^2, interpolated K grad u and K u,
+    """u_tt = div(K grad u), K = (1 + amplitude prod sin(2 pi x_d))^2, interpolated K grad u and K u,
     DiffusionRHS terms and the IPDG penalty (sigma), on the device."""
 
-    def __init__(self, grid: Grid, sigma: float):
+    def __init__(self, grid: Grid, sigma: float, amplitude: float = 0.5):
         self.grid = grid
         self._h = C.c_void_p()
-        _ck(load().amdg_wave_create(grid.handle, sigma, C.byref(self._h)), "wave_create")
+        _ck(load().amdg_wave_create(grid.handle, sigma, amplitude, C.byref(self._h)), "wave_create")
 
     def rhs_device(self, d_u: int, d_rhs: int, prec: int = FP64):
         _ck(load().amdg_wave_rhs(self._h, C.c_void_p(d_u), C.c_void_p(d_rhs), prec), "wave_rhs")
@@ -484,6 +487,27 @@ class WaveOperator:
         a, b = C.c_int64(), C.c_int64()
         _ck(load().amdg_wave_counters(self._h, C.byref(a), C.byref(b)), "wave_counters")
         return a.value, b.value
+
+    def adaptive_step_ex(self, cfl: float, wave_speed: float, eps: float, eta: float, prec: int = FP64):
+        """Adaptive step that also returns the criterion's decision per old element (0 keep, 1 refine, 2 coarsen)."""
+        dec = np.zeros(self.grid.num_elements, np.int8)
+        dt = C.c_double()
+        _ck(load().amdg_wave_adaptive_step_ex(self._h, cfl, wave_speed, eps, eta, prec, C.byref(dt), _ptr(dec)),
+            "wave_adaptive_step_ex")
+        self.grid._refresh()
+        return dt.value, dec
+
+    def features_device(self, d_u: int, d_feat: int):
+        _ck(load().amdg_wave_features(self._h, C.c_void_p(d_u), C.c_void_p(d_feat)), "wave_features")
+
+    def adaptive_step_learned(self, mlp, cfl: float, wave_speed: float, eps: float, eta: float, tau: float,
+                              prec: int = FP64):
+        stats = np.zeros(4, np.int64)
+        dt = C.c_double()
+        _ck(load().amdg_wave_adaptive_step_learned(self._h, mlp.handle, cfl, wave_speed, eps, eta, tau, prec,
+                                                   C.byref(dt), _ptr(stats)), "wave_adaptive_step_learned")
+        self.grid._refresh()
+        return dt.value, stats
 
     def close(self):
         if self._h:

@@ -261,6 +261,8 @@ def run_ours(args):
         line["batched"] = bench_batched(ctx, stream, args)
     if args.learn_runs > 0:
         line["burgers3d_adaptive"] = bench_burgers_adaptive(ctx, stream, args)
+    if args.wave_learn_runs > 0:
+        line["wave2d_adaptive"] = bench_wave_adaptive(ctx, stream, args)
     if rank == 0 and world == 1:
         line["cpu_baseline"] = cpu_baseline(g, u0, budget_s=args.cpu_seconds)
     if rank == 0:
@@ -435,6 +437,115 @@ def bench_burgers_adaptive(ctx, stream, args):
     return out
 
 
+def bench_wave_adaptive(ctx, stream, args):
+    """2D wave equation u_tt = div(c^2 grad u), c = 1 + 0.5 sin(2 pi x) sin(2 pi y), Gaussian bump
+    exp(-200 |x - (0.3, 0.4)|^2) at rest, adaptive (refine 1e-5, coarsen 1e-6, max level 9, start
+    level 3), IPDG sigma = 10, RK4ODE2nd, CFL 0.1, to T = 0.5: the plain FP64 path (EulerODE2nd
+    predictor, refine, RK4, coarsen) against mixed precision with the learned refine/coarsen
+    classifier, trained on the plain criterion's decisions in 20 seeded runs (bump centre in
+    [0.25, 0.75]^2, width parameter in [100, 300]).  No exact solution: each final solution is
+    compared, on a 128^2 cell-centre mesh, with a plain FP64 run at refine 1e-6 / coarsen 1e-7 and
+    max level 10."""
+    import torch
+
+    import amdg
+    import amdg_oracle as O
+    dim, nmax, level_init, eps, eta, sigma, T, tau, speed = 2, 9, 3, 1e-5, 1e-6, 10.0, args.wave_time, 0.8, 1.0
+    F = 9 * (1 + 2 * dim)
+    out = {"workload": f"2D wave u_tt = div(c^2 grad u), c = 1 + 0.5 sin(2 pi x) sin(2 pi y), Gaussian bump at "
+                       f"rest, adaptive (refine 1e-5, coarsen 1e-6, max level 9, start level 3), Alpert k=2, "
+                       f"Lagrange m=3, IPDG sigma 10, RK4ODE2nd, CFL 0.1, to T = {T}"}
+    t0 = time.perf_counter()
+    rng = np.random.default_rng(2)
+    feats, labs = [], []
+    for _ in range(args.wave_learn_runs):
+        centre = tuple(rng.uniform(0.25, 0.75, 2))
+        width = rng.uniform(100.0, 300.0)
+        g = amdg.Grid(ctx, dim, nmax, 2, level_init=level_init)
+        g.init_separable_adaptive(O.wave_ic_terms(dim, centre, width), eps)
+        op = amdg.WaveOperator(g, sigma)
+        for _s in range(args.wave_learn_steps):
+            buf = torch.empty(g.num_elements * F, dtype=torch.float32, device="cuda")
+            torch.cuda.synchronize()
+            op.features_device(g.device_ptr(), buf.data_ptr())
+            ctx.synchronize()
+            feats.append(buf.cpu().numpy().reshape(-1, F))
+            _dt, dec = op.adaptive_step_ex(CFL, speed, eps, eta)
+            labs.append(np.where(dec == 1, 0, np.where(dec == 2, 2, 1)).astype(np.int32))
+        op.close()
+        g.close()
+    x, y = np.concatenate(feats), np.concatenate(labs)
+    collect_s = time.perf_counter() - t0
+    dx, dy = torch.from_numpy(x).cuda(), torch.from_numpy(y).cuda()
+    torch.cuda.synchronize()
+    mlp = amdg.MLP(ctx, F, 64, 3, 3, seed=21)
+    t0 = time.perf_counter()
+    loss = mlp.train_device(dx.data_ptr(), dy.data_ptr(), len(y), epochs=args.learn_epochs, batch=256, lr=2e-3,
+                            seed=22)
+    out["training"] = {"runs": args.wave_learn_runs, "steps_per_run": args.wave_learn_steps, "samples": int(len(y)),
+                       "class_counts": [int((y == i).sum()) for i in range(3)], "epochs": args.learn_epochs,
+                       "final_loss": loss, "collect_s": collect_s, "train_s": time.perf_counter() - t0}
+    mesh = (np.arange(128) + 0.5) / 128
+
+    def run(learned, prec, t_end, e=eps, et=eta, nm=nmax):
+        g = amdg.Grid(ctx, dim, nm, 2, level_init=level_init)
+        g.init_separable_adaptive(O.wave_ic_terms(dim), e)
+        op = amdg.WaveOperator(g, sigma)
+        t, steps, cls = 0.0, 0, np.zeros(3, np.int64)
+        ctx.synchronize()
+        ctx.profile(True)
+        t0 = time.perf_counter()
+        while t < t_end - 1e-12:
+            lv = g.max_mesh_level()
+            dt_full = CFL / sum(speed * 2.0 ** int(m) for m in lv)
+            cfl = CFL if t + dt_full <= t_end else CFL * (t_end - t) / dt_full
+            if learned:
+                dt, st = op.adaptive_step_learned(mlp, cfl, speed, e, et, tau, prec)
+                cls += st[:3]
+            else:
+                dt = op.adaptive_step(cfl, speed, e, et, prec)
+            t += dt
+            steps += 1
+        ctx.synchronize()
+        wall = time.perf_counter() - t0
+        prof = ctx.profile_read()
+        ctx.profile(False)
+        stage_dof, rhs = op.counters()
+        res = {"value": stage_dof / wall, "wall_s": wall, "steps": steps, "t_end": t, "stage_dof_updates": stage_dof,
+               "rhs_evaluations": rhs, "elements_final": g.num_elements, "dof_final": g.dof,
+               "host_phase_ms": {k: round(v[0] * 1e3, 3) for k, v in prof.items() if v[1]}}
+        if t_end >= T:
+            vals = torch.zeros(len(mesh) ** dim, dtype=torch.float64, device="cuda")
+            torch.cuda.synchronize()
+            g.eval_tensor_device(mesh, vals.data_ptr())
+            ctx.synchronize()
+            res["_mesh_values"] = vals.cpu().numpy()
+        if learned:
+            res["classifier"] = {"net_refine": int(cls[0]), "unsure": int(cls[1]), "missed_refinements": int(cls[2])}
+        op.close()
+        g.close()
+        return res
+
+    ref = run(False, amdg.FP64, T, eps / 10, eta / 10, 10)["_mesh_values"]
+    out["reference_run"] = "plain FP64, refine 1e-6, coarsen 1e-7, max level 10"
+    for name, learned, prec in (("plain_fp64", False, amdg.FP64), ("mixed_learned", True, amdg.MIXED),
+                                ("mixed_plain", False, amdg.MIXED)):
+        run(learned, prec, 4 * CFL / (speed * dim * 128))  # warm-up: a few steps
+        out[name] = run(learned, prec, T)
+        v = out[name].pop("_mesh_values")
+        out[name]["rel_l2_diff_vs_reference_run"] = float(np.linalg.norm(v - ref) / np.linalg.norm(ref))
+        out[name]["_v"] = v
+    base = out["plain_fp64"].pop("_v")
+    for name in ("mixed_learned", "mixed_plain"):
+        v = out[name].pop("_v")
+        out[name]["rel_l2_diff_vs_plain_fp64"] = float(np.linalg.norm(v - base) / np.linalg.norm(base))
+        out[name]["error_ratio_vs_plain_fp64"] = (out[name]["rel_l2_diff_vs_reference_run"] /
+                                                 out["plain_fp64"]["rel_l2_diff_vs_reference_run"])
+        out[name]["speedup_vs_plain_fp64"] = out["plain_fp64"]["wall_s"] / out[name]["wall_s"]
+    mlp.close()
+    return out
+
+
 def bench_batched(ctx, stream, args):
     """Batched serving: independent 3D linear advection solves, random velocity
     in [-1,1]^3, 1-4 periodic Gaussian bumps (centres U[0.2,0.8]^3, widths
@@ -567,6 +678,9 @@ def main():
     ap.add_argument("--learn-runs", type=int, default=4, help="plain runs whose decisions train the classifier (0: skip)")
     ap.add_argument("--learn-steps", type=int, default=12)
     ap.add_argument("--learn-epochs", type=int, default=30)
+    ap.add_argument("--wave-learn-runs", type=int, default=20, help="plain wave runs that train its classifier (0: skip)")
+    ap.add_argument("--wave-learn-steps", type=int, default=30)
+    ap.add_argument("--wave-time", type=float, default=0.5)
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)

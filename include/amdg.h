@@ -318,13 +318,13 @@ amdg_status amdg_burgers_adaptive_step_ex(amdg_burgers_op* op, double cfl, doubl
 amdg_status amdg_grid_set_velocity(amdg_grid* g, const double* host, int64_t n);
 amdg_status amdg_grid_get_velocity(const amdg_grid* g, double* host, int64_t n);
 
-/* u_tt = div(K grad u) on the periodic unit cube, K = (1 + 0.5 prod_d sin(2 pi x_d))^2, Alpert
+/* u_tt = div(K grad u) on the periodic unit cube, K = (1 + a prod_d sin(2 pi x_d))^2 (a = amplitude), Alpert
  * k = 2: K u_{x_d} and K u interpolated by degree-3 Lagrange (LagrInterpolation::
  * var_coeff_gradu_Lagr_fast / var_coeff_u_Lagr_fast, Interplation.cpp:4159-4212), the
  * DiffusionRHS terms rhs_flx_gradu, rhs_vol, rhs_flx_u (FastMultiplyLU.cpp:1691-1765) and the
  * IPDG penalty -sigma/dx [u][v], dx the finest element size
  * (DiffusionAlpt::assemble_matrix_flx_ujp_vjp, BilinearForm.cpp:920-929), evaluated matrix free. */
-amdg_status amdg_wave_create(amdg_grid* g, double sigma, amdg_wave_op** out);
+amdg_status amdg_wave_create(amdg_grid* g, double sigma, double amplitude, amdg_wave_op** out);
 amdg_status amdg_wave_destroy(amdg_wave_op* op);
 /* d_rhs = L(d_u) (device arrays, dof entries). */
 amdg_status amdg_wave_rhs(amdg_wave_op* op, const double* d_u, double* d_rhs, amdg_precision prec);
@@ -336,6 +336,13 @@ amdg_status amdg_wave_rk4_steps(amdg_wave_op* op, double dt, int nsteps, amdg_pr
  * one RK4ODE2nd step, coarsen on u. */
 amdg_status amdg_wave_adaptive_step(amdg_wave_op* op, double cfl, double wave_speed, double eps, double eta,
                                     amdg_precision prec, double* dt_out);
+/* As amdg_burgers_adaptive_step_ex / amdg_burgers_features / amdg_burgers_adaptive_step_learned for
+ * the wave operator (the classifier reads |coefficients| of u; the step is RK4ODE2nd). */
+amdg_status amdg_wave_adaptive_step_ex(amdg_wave_op* op, double cfl, double wave_speed, double eps, double eta,
+                                       amdg_precision prec, double* dt_out, int8_t* decisions);
+amdg_status amdg_wave_features(amdg_wave_op* op, const double* d_u, float* d_features);
+amdg_status amdg_wave_adaptive_step_learned(amdg_wave_op* op, amdg_mlp* mlp, double cfl, double wave_speed, double eps,
+                                            double eta, double tau, amdg_precision prec, double* dt_out, int64_t* stats);
 /* As amdg_burgers_counters (4 x DOF per RK4ODE2nd step). */
 amdg_status amdg_wave_counters(const amdg_wave_op* op, int64_t* stage_dof_updates, int64_t* rhs_evaluations);
 

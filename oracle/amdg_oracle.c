@@ -1353,7 +1353,7 @@ int amdg_oracle_error_burgers(int dim, int N, int k, int64_t E, const int32_t* l
 }
 
 /* ------------------------------------------------------------------------ */
-/* Wave equation u_tt = div(K(x) grad u), K = (1 + 0.5 prod_d sin(2 pi x_d))^2,  */
+/* Wave equation u_tt = div(K(x) grad u), K = (1 + a prod_d sin(2 pi x_d))^2,    */
 /* periodic: DiffusionRHS with Lagrange-interpolated K u_x and K u            */
 /* (03_wave_06_var_coeff_adapt.cpp:154-245; Interplation.cpp:527-577,         */
 /* 648-698, 4159-4212; FastMultiplyLU.cpp:1691-1765) plus the IPDG jump        */
@@ -1403,16 +1403,17 @@ int amdg_oracle_oper1d_lagr_ujp_vx(int N, int k, double* ujp_vxave) {
     return 0;
 }
 
-double amdg_oracle_wave_coef(int dim, const double* x) {
+double amdg_oracle_wave_coef(int dim, const double* x, double amp) {
     const double pi = 3.14159265358979323846;
     double s = 1.0;
     for (int d = 0; d < dim; ++d) s *= sin(2 * pi * x[d]);
-    const double c = 1.0 + 0.5 * s;
+    const double c = 1.0 + amp * s;
     return c * c;
 }
 
 /* K at every interpolation point times the given point values, then the surplus */
-static int wave_coef_surplus(int dim, int N, int64_t E, const int32_t* level, const int32_t* suppt, double* up, double* fucoe) {
+static int wave_coef_surplus(int dim, int N, int64_t E, const int32_t* level, const int32_t* suppt, double amp, double* up,
+                             double* fucoe) {
     const int P = ipow(4, dim);
 #pragma omp parallel for schedule(static)
     for (int64_t e = 0; e < E; ++e)
@@ -1423,13 +1424,13 @@ static int wave_coef_surplus(int dim, int N, int64_t E, const int32_t* level, co
                 x[d] = amdg_oracle_lagr_point(level[e * dim + d], suppt[e * dim + d], r % 4);
                 r /= 4;
             }
-            up[e * P + p] = amdg_oracle_wave_coef(dim, x) * up[e * P + p];
+            up[e * P + p] = amdg_oracle_wave_coef(dim, x, amp) * up[e * P + p];
         }
     return amdg_oracle_lagr_surplus(dim, N, E, level, suppt, up, fucoe);
 }
 
 int amdg_oracle_wave_rhs_fast(int dim, int N, int k, int64_t E, const int32_t* level, const int32_t* suppt,
-                              const double* u, double sigma, double* rhs) {
+                              const double* u, double sigma, double amp, double* rhs) {
     const int np = k + 1, n1 = 1 << N, nr = n1 * 4, nc = n1 * np;
     const int B = ipow(np, dim), P = ipow(4, dim);
     fast_ctx c;
@@ -1458,14 +1459,14 @@ int amdg_oracle_wave_rhs_fast(int dim, int N, int k, int64_t E, const int32_t* l
         for (int s = 0; s < dim; ++s) { M[s] = (s == d) ? a2pd : a2p; flx[s] = 0; }
         memset(up, 0, (size_t)E * P * sizeof(double));
         rc = fast_partial_sums(&c, u, np, 4, M, flx, 1.0, up);
-        if (!rc) rc = wave_coef_surplus(dim, N, E, level, suppt, up, fg + (size_t)d * E * P);
+        if (!rc) rc = wave_coef_surplus(dim, N, E, level, suppt, amp, up, fg + (size_t)d * E * P);
     }
     /* K u at the points */
     if (!rc) {
         for (int s = 0; s < dim; ++s) { M[s] = a2p; flx[s] = 0; }
         memset(up, 0, (size_t)E * P * sizeof(double));
         rc = fast_partial_sums(&c, u, np, 4, M, flx, 1.0, up);
-        if (!rc) rc = wave_coef_surplus(dim, N, E, level, suppt, up, fu);
+        if (!rc) rc = wave_coef_surplus(dim, N, E, level, suppt, amp, up, fu);
     }
     memset(rhs, 0, (size_t)E * B * sizeof(double));
     /* rhs_flx_gradu: -{K u_x}[v] (uave_vjp = (ulft + urgt)_vjp / 2) */

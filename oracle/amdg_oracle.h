@@ -110,13 +110,13 @@ double amdg_oracle_burgers_exact(int dim, const double* x, double a, double b, d
 int amdg_oracle_error_burgers(int dim, int N, int k, int64_t E, const int32_t* level, const int32_t* suppt,
                               const double* u, int gauss, double a, double b, double c, double t, double* err3);
 
-/* ---- wave equation u_tt = div(K grad u), K = (1 + 0.5 prod_d sin(2 pi x_d))^2 ---- */
+/* ---- wave equation u_tt = div(K grad u), K = (1 + a prod_d sin(2 pi x_d))^2 ---- */
 /* Lagrange x Alpert ujp_vxlft + ujp_vxrgt, (2^N*4) x (2^N*(k+1)). */
 int amdg_oracle_oper1d_lagr_ujp_vx(int N, int k, double* ujp_vxave);
-double amdg_oracle_wave_coef(int dim, const double* x);
+double amdg_oracle_wave_coef(int dim, const double* x, double amp);
 /* right-hand side of the semi-discrete wave equation (fast transforms), rhs = E x (k+1)^dim */
 int amdg_oracle_wave_rhs_fast(int dim, int N, int k, int64_t E, const int32_t* level, const int32_t* suppt,
-                              const double* u, double sigma, double* rhs);
+                              const double* u, double sigma, double amp, double* rhs);
 
 #ifdef __cplusplus
 }

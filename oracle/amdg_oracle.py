@@ -75,9 +75,10 @@ def lib():
         L.amdg_oracle_burgers_exact.argtypes = [C.c_int, f64p, C.c_double, C.c_double, C.c_double, C.c_double]
         L.amdg_oracle_error_burgers.argtypes = [C.c_int, C.c_int, C.c_int, C.c_int64, i32p, i32p, f64p, C.c_int,
                                                 C.c_double, C.c_double, C.c_double, C.c_double, f64p]
-        L.amdg_oracle_wave_rhs_fast.argtypes = [C.c_int, C.c_int, C.c_int, C.c_int64, i32p, i32p, f64p, C.c_double, f64p]
+        L.amdg_oracle_wave_rhs_fast.argtypes = [C.c_int, C.c_int, C.c_int, C.c_int64, i32p, i32p, f64p, C.c_double,
+                                                C.c_double, f64p]
         L.amdg_oracle_wave_coef.restype = C.c_double
-        L.amdg_oracle_wave_coef.argtypes = [C.c_int, f64p]
+        L.amdg_oracle_wave_coef.argtypes = [C.c_int, f64p, C.c_double]
         _lib = L
     return _lib
 
@@ -213,18 +214,18 @@ def error_burgers(dim, N, k, level, suppt, u, gauss, a=0.5, b=0.25, c=0.0, t=0.0
     return out
 
 
-def wave_rhs(dim, N, k, level, suppt, u, sigma):
-    """Right-hand side of u_tt = div(K grad u), K = (1 + 0.5 prod sin(2 pi x_d))^2, with the IPDG
+def wave_rhs(dim, N, k, level, suppt, u, sigma, amp=0.5):
+    """Right-hand side of u_tt = div(K grad u), K = (1 + amp prod sin(2 pi x_d))^2, with the IPDG
     penalty -sigma/dx [u][v] (fast transforms, the reference's operator on adaptive grids)."""
     B = (k + 1) ** dim
     rhs = np.zeros((len(level), B))
     _check(lib().amdg_oracle_wave_rhs_fast(dim, N, k, len(level), np.ascontiguousarray(level, np.int32),
                                            np.ascontiguousarray(suppt, np.int32),
-                                           np.ascontiguousarray(u, np.float64).reshape(-1), sigma, rhs))
+                                           np.ascontiguousarray(u, np.float64).reshape(-1), sigma, amp, rhs))
     return rhs
 
 
-def wave_rk4(dim, N, k, level, suppt, u, v, sigma, dt, steps):
+def wave_rk4(dim, N, k, level, suppt, u, v, sigma, dt, steps, amp=0.5):
     """RK4ODE2nd steps of u' = v, v' = L u (ODESolver.cpp:579-615, same combination order)."""
     u = np.array(u, np.float64)
     v = np.array(v, np.float64)
@@ -232,7 +233,7 @@ def wave_rk4(dim, N, k, level, suppt, u, v, sigma, dt, steps):
         un, vn = u.copy(), v.copy()
         ku, kv = [], []
         for stage in range(4):
-            rhs = wave_rhs(dim, N, k, level, suppt, u, sigma)
+            rhs = wave_rhs(dim, N, k, level, suppt, u, sigma, amp)
             ku.append(dt * v)
             kv.append(dt * rhs)
             if stage < 2:
@@ -489,7 +490,7 @@ def burgers_adaptive_run(dim, n_init, nmax, eps, eta, alpha, cfl, umax, steps, k
     return history
 
 
-def wave_adaptive_run(dim, n_init, nmax, eps, eta, sigma, cfl, speed, steps, k=2):
+def wave_adaptive_run(dim, n_init, nmax, eps, eta, sigma, cfl, speed, steps, k=2, amp=0.5):
     """The adaptive wave loop of 03_wave_06_var_coeff_adapt.cpp without source: EulerODE2nd
     predictor, refine on the predicted u, RK4ODE2nd step, coarsen on u; u0 the Gaussian bump,
     v0 = 0."""
@@ -505,7 +506,7 @@ def wave_adaptive_run(dim, n_init, nmax, eps, eta, sigma, cfl, speed, steps, k=2
         u, v = remap(keys, u, new_keys), remap(keys, v, new_keys)
         keys = new_keys
         lv, sp = keys_to_arrays(keys, dim)
-        u, v = wave_rk4(dim, nmax, k, lv, sp, u, v, sigma, dt, 1)
+        u, v = wave_rk4(dim, nmax, k, lv, sp, u, v, sigma, dt, 1, amp)
         new_keys = coarsen_keys(keys, element_norms(u), eta)
         u, v = remap(keys, u, new_keys), remap(keys, v, new_keys)
         keys = new_keys

@@ -31,8 +31,9 @@
 //     predictor, refine, copy_predict_to_ucoe, three RK3SSP stages, coarsen.
 //     Dumps the element set and coefficients after init (u_init) and after
 //     every step (u_step<i>), with the step sizes.
-//   ref_harness wave <dim> <N> <sigma> <steps> <dt>
-//     u_tt = div(K grad u), K = (1 + 0.5 prod_d sin(2 pi x_d))^2, u0 = Gaussian bump, u_t(0) = 0:
+//   ref_harness wave <dim> <N> <sigma> <steps> <dt> [a]
+//     u_tt = div(K grad u), K = (1 + a prod_d sin(2 pi x_d))^2 (a = 0.5 by default), u0 = Gaussian
+//     bump, u_t(0) = 0:
 //     DiffusionRHS with Lagrange-interpolated K grad u and K u, IPDG penalty, RK4ODE2nd
 //     (03_wave_06_var_coeff_adapt.cpp:154-279). Dumps u0, rhs0, uT, vT.
 //   ref_harness matrices <N> <k>
@@ -447,7 +448,7 @@ int run_burgers_adapt(int argc, char** argv) {
     return 0;
 }
 
-// Wave equation u_tt = div(K grad u), K = (1 + 0.5 prod_d sin(2 pi x_d))^2, periodic, Alpert k = 2,
+// Wave equation u_tt = div(K grad u), K = (1 + a prod_d sin(2 pi x_d))^2, periodic, Alpert k = 2,
 // Lagrange degree 3 (msh_case 1) interpolation of K u_x and K u, DiffusionRHS terms and the IPDG
 // penalty as 03_wave_06_var_coeff_adapt.cpp:154-279 (no source, no adaptivity): u0 a Gaussian bump,
 // u_t = 0. Dumps u0, rhs0 (the right-hand side at u0, read through EulerODE2nd with dt = 1 on a
@@ -459,6 +460,7 @@ int run_wave(int argc, char** argv) {
     const double sigma = std::atof(argv[4]);
     const int steps = std::atoi(argv[5]);
     const double dt = std::atof(argv[6]);
+    const double amp = argc > 7 ? std::atof(argv[7]) : 0.5;
     const int k = 2;
     set_statics(dim, k);
     DGSolution::prob = "wave";
@@ -477,7 +479,7 @@ int run_wave(int argc, char** argv) {
     auto coe = [=](std::vector<double> x, int) -> double {
         double s = 1.0;
         for (int d = 0; d < dim; ++d) s *= std::sin(2 * PI * x[d]);
-        const double c = 1.0 + 0.5 * s;
+        const double c = 1.0 + amp * s;
         return c * c;
     };
     std::vector<std::vector<bool>> is_intp(1, std::vector<bool>(dim, true));

@@ -139,3 +139,62 @@ def test_learned_adaptivity_gains_over_the_plain_criterion(ctx):
     print(f"plain {t_plain:.3f}s, learned {t_learn:.3f}s, missed refinements {missed}, "
           f"elements {len(k_plain)} vs {len(k_learn)}")
     mlp.close()
+
+
+def test_learned_wave_steps_follow_the_plain_criterion(ctx):
+    """The classifier on the wave operator: trained on the plain criterion's decisions of a few
+    seeded runs, the learned steps (one right-hand side fewer per step) end on a grid whose
+    solution agrees with the plain run's on the common elements."""
+    dim, nmax, eps, eta, sigma = 2, 7, 1e-4, 1e-5, 10.0
+    F = 9 * (1 + 2 * dim)
+    rng = np.random.default_rng(5)
+    feats, labs = [], []
+    for _ in range(4):
+        centre = tuple(rng.uniform(0.3, 0.7, 2))
+        g = amdg.Grid(ctx, dim, nmax, 2, level_init=3)
+        g.init_separable_adaptive(O.wave_ic_terms(dim, centre, rng.uniform(100, 300)), eps)
+        op = amdg.WaveOperator(g, sigma)
+        for _ in range(8):
+            buf = torch.zeros(g.num_elements * F, dtype=torch.float32, device="cuda")
+            torch.cuda.synchronize()
+            op.features_device(g.device_ptr(), buf.data_ptr())
+            ctx.synchronize()
+            feats.append(buf.cpu().numpy().reshape(-1, F))
+            _dt, dec = op.adaptive_step_ex(0.1, 1.0, eps, eta)
+            labs.append(np.where(dec == 1, 0, np.where(dec == 2, 2, 1)).astype(np.int32))
+        op.close()
+        g.close()
+    x, y = np.concatenate(feats), np.concatenate(labs)
+    dx, dy = torch.from_numpy(x).cuda(), torch.from_numpy(y).cuda()
+    torch.cuda.synchronize()
+    mlp = amdg.MLP(ctx, F, 64, 3, 3, seed=3)
+    mlp.train_device(dx.data_ptr(), dy.data_ptr(), len(y), epochs=20, batch=256, lr=2e-3, seed=4)
+
+    def run(learned):
+        g = amdg.Grid(ctx, dim, nmax, 2, level_init=3)
+        g.init_separable_adaptive(O.wave_ic_terms(dim), eps)
+        op = amdg.WaveOperator(g, sigma)
+        for _ in range(10):
+            if learned:
+                op.adaptive_step_learned(mlp, 0.1, 1.0, eps, eta, 0.8)
+            else:
+                op.adaptive_step(0.1, 1.0, eps, eta)
+        ctx.synchronize()
+        lv, sp = g.elements()
+        keys = O.arrays_to_keys(lv, sp)
+        u = g.coefficients().copy()
+        work = op.counters()
+        op.close()
+        g.close()
+        return keys, u, work
+
+    k_plain, u_plain, w_plain = run(False)
+    k_learn, u_learn, w_learn = run(True)
+    assert w_plain[1] == 50 and w_learn[1] == 40
+    common = sorted(set(k_plain) & set(k_learn))
+    pp = {k: i for i, k in enumerate(k_plain)}
+    pl = {k: i for i, k in enumerate(k_learn)}
+    a = np.array([u_plain[pp[k]] for k in common])
+    b = np.array([u_learn[pl[k]] for k in common])
+    assert np.linalg.norm(a - b) <= 1e-3 * np.linalg.norm(a)
+    mlp.close()
