@@ -61,8 +61,27 @@ void gauss_legendre(int n, double* x, double* w);
 // 1D projection of f(., d, term) onto every basis function (Basis::product_function).
 void project_1d(const Basis1D& b, amdg_fn1d f, void* user, int d, int term, double* out);
 
-// ---- Lagrange interpolation path (degree-3 hierarchical Lagrange) ---------
+// ---- Lagrange interpolation path (hierarchical Lagrange of degree 3 or 4) ----
+constexpr int kMaxLagrPoints = 5;  // points per element and dimension (degree 4)
+
+// Node layout of a hierarchical Lagrange basis (LagrBasis.cpp:33-155): degree 3
+// with msh_case 1 (the Burgers examples) or degree 4 with msh_case 2 (the wave
+// example, 03_wave_06_var_coeff_adapt.cpp:53-54).
+struct LagrSpec {
+    int p1 = 4;                               // points per element and dimension
+    double pt0[kMaxLagrPoints];               // level-0 interpolation points on [-1, 1]
+    double pt1[kMaxLagrPoints];               // level >= 1 points, in the element's own [-1, 1]
+    double node0[kMaxLagrPoints];             // level-0 polynomial nodes
+    double half[2][kMaxLagrPoints];           // level-1 polynomial nodes of the left / right half
+    int side[kMaxLagrPoints];                 // level-1 function p lives on the left (0) / right (1) half
+    int node[kMaxLagrPoints];                 // ... and interpolates at half[side][node]
+};
+// the layout of the given degree (3 or 4); nullptr for any other
+const LagrSpec* lagr_spec(int degree);
+
 struct LagrTables {
+    const LagrSpec* spec = nullptr;
+    int p1 = 4;
     int n_lagr = 0, n_alpt = 0;
     std::vector<double> a2p;    // [n_alpt][n_lagr]: Alpert basis at Lagrange points
     std::vector<double> lv;     // [n_lagr][n_alpt]: u_v   (Lagrange x Alpert)
@@ -73,15 +92,18 @@ struct LagrTables {
     std::vector<double> a2pd;   // [n_alpt][n_lagr]: Alpert basis derivative at Lagrange points
     std::vector<double> ljv;    // [n_lagr][n_alpt]: ujp_vxlft + ujp_vxrgt
     std::vector<double> pts;    // [n_lagr]: coordinate of each Lagrange point
-    std::vector<int32_t> anc_order;  // [n_elem1d][4]: 1D order of the ancestor owning surplus point ic
-    std::vector<int32_t> anc_point;  // [n_elem1d][4]: its point index
-    std::vector<int32_t> anc_rank;   // [n_elem1d][4]: rank of its position among the four
-    double weight[16] = {0};         // [p0][rank]
+    std::vector<int32_t> anc_order;  // [n_elem1d][p1]: 1D order of the ancestor owning surplus point ic
+    std::vector<int32_t> anc_point;  // [n_elem1d][p1]: its point index
+    std::vector<int32_t> anc_rank;   // [n_elem1d][p1]: rank of its position among the p1
+    double weight[kMaxLagrPoints * kMaxLagrPoints] = {0};  // [p0][rank]
 };
-double lagr_eval(int order, double x, int sgn);
-double lagr_point(int o, int p);
-void build_lagr_tables(const Basis1D& alpt, LagrTables* t, bool diffusion = false);
-void build_lagr_ancestors(const Basis1D& alpt, LagrTables* t);  // anc_order/anc_point/anc_rank only
+// basis function `order` (1D element order * p1 + p) at x, one-sided for sgn = -1 / 1
+double lagr_eval(const LagrSpec& s, int order, double x, int sgn);
+double lagr_point(const LagrSpec& s, int o, int p);
+// all tables for Lagrange degree `degree` (3 or 4)
+void build_lagr_tables(const Basis1D& alpt, int degree, LagrTables* t, bool diffusion = false);
+// anc_order/anc_point/anc_rank only (t->spec and t->p1 set from `degree`)
+void build_lagr_ancestors(const Basis1D& alpt, int degree, LagrTables* t);
 // dimension orders and L(0)/full(1)/U(2) tags of the 2^(dim-1) partial sums
 void transform_schedule(int dim, std::vector<std::vector<int>>* dim_order, std::vector<std::vector<int>>* lu);
 
@@ -177,7 +199,7 @@ struct PartialSum {
     int32_t kind;
     double coef;
 };
-// surplus ancestors: [e][d][ic] element index (-1 for level 0 in d); false if a hole is found
+// surplus ancestors: [e][d][ic] element index, ic < t.p1 (-1 for level 0 in d); false if a hole is found
 bool build_surplus_ancestors(const HostGrid& g, const LagrTables& t, std::vector<int32_t>* anc);
 
 }  // namespace amdg
@@ -272,28 +294,29 @@ struct amdg_burgers_op {
     amdg_grid* grid = nullptr;
     int device = 0;
     std::vector<double> alpha;
-    int points = 0;                  // 4^dim interpolation points per element
+    int p1 = 4;                      // Lagrange points per element and dimension (degree + 1)
+    int points = 0;                  // p1^dim interpolation points per element
     int n1 = 0;                      // 1D elements
     // 1D matrices, FP64 and FP32 copies
     double *d_a2p = nullptr, *d_lv = nullptr, *d_lvx = nullptr, *d_lflx = nullptr, *d_ajump = nullptr;
     float *f_a2p = nullptr, *f_lv = nullptr, *f_lvx = nullptr, *f_lflx = nullptr, *f_ajump = nullptr;
     double *d_a2pd = nullptr, *d_ljv = nullptr, *d_pts = nullptr;  // wave: derivative and jump tables, point coordinates
     float *f_a2pd = nullptr, *f_ljv = nullptr;
-    void* w_fields = nullptr;        // wave: (dim+1) coefficient-weighted point fields and their surpluses, 2 (dim+1) x E x 4^dim doubles
+    void* w_fields = nullptr;        // wave: (dim+1) coefficient-weighted point fields and their surpluses, 2 (dim+1) x E x p1^dim doubles
     double *d_v1 = nullptr, *d_su = nullptr, *d_sv = nullptr;  // wave: RK4ODE2nd stage v and running sums
     // neighbour lists of the fast transforms and the surplus ancestors
     int32_t *d_vol_ptr = nullptr, *d_vol_nbr = nullptr;  // nbr: (element, 1D order along t) pairs
     int32_t *d_flx_ptr = nullptr, *d_flx_nbr = nullptr;
     int32_t *d_vol_split = nullptr, *d_flx_split = nullptr;
     int32_t *d_anc = nullptr, *d_anc_point = nullptr, *d_anc_rank = nullptr;
-    double weight[16] = {0};
+    double weight[amdg::kMaxLagrPoints * amdg::kMaxLagrPoints] = {0};
     std::vector<std::vector<int>> sched_dims, sched_lu;
     // terms of the point values (first n_pv_terms) and of the right-hand side, in summation order
     std::vector<amdg::PartialSum> terms;
     amdg::PartialSum* d_terms = nullptr;
     int n_pv_terms = 0;
     int chunk = 1;  // terms per launch
-    // work buffers sized for FP64: E x 4^dim doubles each, the sweep buffers and
+    // work buffers sized for FP64: E x p1^dim doubles each, the sweep buffers and
     // term slices chunk times that
     void *w_up = nullptr, *w_fu = nullptr, *w_a = nullptr, *w_b = nullptr, *w_u = nullptr;
     void *w_s0 = nullptr, *w_s1 = nullptr, *w_slots = nullptr;
@@ -327,8 +350,11 @@ struct amdg_wave_op {
 namespace amdg {
 // replace a grid's element set (coefficients carried over, new elements zero; bumps the version)
 amdg_status grid_set_keys(amdg_grid* g, std::vector<uint64_t> keys);
-// indicator norms of a device coefficient vector on the grid's element set (synchronises)
-amdg_status grid_norms(amdg_grid* g, const double* d_u, std::vector<double>* norms);
+// indicator norms of a device coefficient vector on the grid's element set, plus those of a
+// second vector when d_u2 is given (the wave problem's u_t) (synchronises)
+amdg_status grid_norms(amdg_grid* g, const double* d_u, std::vector<double>* norms, const double* d_u2 = nullptr);
+// coarsen the grid on the indicator ||u|| (+ ||u2|| when d_u2 is given)
+amdg_status grid_coarsen(amdg_grid* g, double eta, const double* d_u2, int64_t* num_elements);
 }  // namespace amdg
 
 struct amdg_batch {

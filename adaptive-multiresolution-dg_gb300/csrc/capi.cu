@@ -177,7 +177,14 @@ amdg_status grid_set_keys(amdg_grid* g, std::vector<uint64_t> keys) {
 }
 
 // indicator norms of a device coefficient vector on the grid's current element set
-amdg_status grid_norms(amdg_grid* g, const double* d_u, std::vector<double>* norms) {
+amdg_status grid_norms(amdg_grid* g, const double* d_u, std::vector<double>* norms, const double* d_u2) {
+    if (d_u2) {  // ||u_e|| + ||u2_e||, added in that order (DGAdapt::indicator_norm, DGAdapt.cpp:1018-1030)
+        std::vector<double> second;
+        if (amdg_status s = grid_norms(g, d_u2, &second); s != AMDG_OK) return s;
+        if (amdg_status s = grid_norms(g, d_u, norms); s != AMDG_OK) return s;
+        for (size_t e = 0; e < norms->size(); ++e) (*norms)[e] += second[e];
+        return AMDG_OK;
+    }
     PhaseTimer timer(g->ctx, AMDG_PHASE_NORMS);
     cudaStream_t st = stream_of(g->ctx);
     const int64_t E = g->host.num_elements;
@@ -197,6 +204,21 @@ amdg_status grid_norms(amdg_grid* g, const double* d_u, std::vector<double>* nor
     if (e != cudaSuccess) return fail(AMDG_ERR_CUDA, std::string("element norms: ") + cudaGetErrorString(e));
     for (double v : *norms)
         if (!std::isfinite(v)) return fail(AMDG_ERR_NONFINITE, "element indicator is not finite");
+    return AMDG_OK;
+}
+
+amdg_status grid_coarsen(amdg_grid* g, double eta, const double* d_u2, int64_t* num_elements) {
+    amdg_status s = set_device(g->ctx);
+    if (s != AMDG_OK) return s;
+    std::vector<double> norms;
+    if ((s = grid_norms(g, g->d_u, &norms, d_u2)) != AMDG_OK) return s;
+    std::vector<uint64_t> keys;
+    {
+        PhaseTimer timer(g->ctx, AMDG_PHASE_ADAPT_HOST);
+        keys = coarsen_keys(g->host, norms.data(), eta);
+    }
+    if (int64_t(keys.size()) != g->host.num_elements && (s = grid_set_keys(g, std::move(keys))) != AMDG_OK) return s;
+    if (num_elements) *num_elements = g->host.num_elements;
     return AMDG_OK;
 }
 
@@ -737,18 +759,7 @@ amdg_status amdg_grid_refine(amdg_grid* g, const double* d_indicator, double eps
 
 amdg_status amdg_grid_coarsen(amdg_grid* g, double eta, int64_t* num_elements) {
     AMDG_REQUIRE(g, AMDG_ERR_ARG, "grid is null");
-    amdg_status s = set_device(g->ctx);
-    if (s != AMDG_OK) return s;
-    std::vector<double> norms;
-    if ((s = grid_norms(g, g->d_u, &norms)) != AMDG_OK) return s;
-    std::vector<uint64_t> keys;
-    {
-        PhaseTimer timer(g->ctx, AMDG_PHASE_ADAPT_HOST);
-        keys = coarsen_keys(g->host, norms.data(), eta);
-    }
-    if (int64_t(keys.size()) != g->host.num_elements && (s = grid_set_keys(g, std::move(keys))) != AMDG_OK) return s;
-    if (num_elements) *num_elements = g->host.num_elements;
-    return AMDG_OK;
+    return amdg::grid_coarsen(g, eta, nullptr, num_elements);
 }
 
 amdg_status amdg_grid_set_velocity(amdg_grid* g, const double* host, int64_t n) {

@@ -241,7 +241,7 @@ amdg_status eval_point_values(amdg_burgers_op* op, const Mats<T>& m, const T* u,
     const T* src[1] = {u};
     for (int c0 = 0; c0 < op->n_pv_terms; c0 += op->chunk) {
         const int cnt = std::min(op->chunk, op->n_pv_terms - c0);
-        if (amdg_status r = run_terms<T>(op, m, c0, cnt, np, 4, src, 1, nullptr, slots, st); r != AMDG_OK) return r;
+        if (amdg_status r = run_terms<T>(op, m, c0, cnt, np, op->p1, src, 1, nullptr, slots, st); r != AMDG_OK) return r;
         const bool last = c0 + cnt == op->n_pv_terms;
         AMDG_CK(launch_reduce_points<T>(slots, cnt, n, c0 == 0 ? 1 : 0, up, last ? fp : nullptr, st));
         op->grid->ctx->launches++;
@@ -259,17 +259,18 @@ amdg_status eval_surplus(amdg_burgers_op* op, const T* in, To* out, cudaStream_t
     T* tb = static_cast<T*>(op->w_b);
     SurplusArgs<T> a{};
     a.dim = dim;
+    a.p1 = op->p1;
     a.points = op->points;
     a.num_elements = g->host.num_elements;
     a.order = g->d_order;
     a.anc = op->d_anc;
     a.anc_point = op->d_anc_point;
     a.anc_rank = op->d_anc_rank;
-    for (int i = 0; i < 16; ++i) a.weight[i] = op->weight[i];
+    for (int i = 0; i < kMaxLagrPoints * kMaxLagrPoints; ++i) a.weight[i] = op->weight[i];
     const T* cur = in;
     for (int d = 0; d < dim; ++d) {
         a.d = d;
-        a.stride = ipow(4, dim - d - 1);
+        a.stride = ipow(op->p1, dim - d - 1);
         if (d == dim - 1) {
             AMDG_CK(launch_surplus_pass<T, To>(a, cur, out, st));
         } else {
@@ -282,21 +283,40 @@ amdg_status eval_surplus(amdg_burgers_op* op, const T* in, To* out, cudaStream_t
     return AMDG_OK;
 }
 
-// right-hand-side terms from their sources and the Alpert coefficients u
-// (penalty): into rhs, or, when so.fused, straight into the RK stage update
+// right-hand-side terms [first, first + total) from their sources and the Alpert
+// coefficients u (penalty): into rhs, or, when so.fused, straight into the RK
+// stage update
 template <typename T>
-amdg_status eval_back_transforms(amdg_burgers_op* op, const Mats<T>& m, const T* const* src, int nsrc, const T* u,
-                                 double* rhs, StageOut so, cudaStream_t st) {
+amdg_status eval_term_range(amdg_burgers_op* op, const Mats<T>& m, int first, int total, const T* const* src, int nsrc,
+                            const T* u, double* rhs, StageOut so, cudaStream_t st) {
     const int np = op->grid->host.k + 1;
     T* slots = static_cast<T*>(op->w_slots);
-    const int first = op->n_pv_terms, total = int(op->terms.size()) - op->n_pv_terms;
     for (int c0 = 0; c0 < total; c0 += op->chunk) {
         const int cnt = std::min(op->chunk, total - c0);
-        if (amdg_status r = run_terms<T>(op, m, first + c0, cnt, 4, np, src, nsrc, u, slots, st); r != AMDG_OK) return r;
+        if (amdg_status r = run_terms<T>(op, m, first + c0, cnt, op->p1, np, src, nsrc, u, slots, st); r != AMDG_OK)
+            return r;
         AMDG_CK(launch_reduce_rhs<T>(slots, cnt, op->grid->dof, c0 == 0 ? 1 : 0, c0 + cnt == total ? 1 : 0, rhs, so, st));
         op->grid->ctx->launches++;
     }
     return AMDG_OK;
+}
+
+// all right-hand-side terms (those after the point-value terms)
+template <typename T>
+amdg_status eval_back_transforms(amdg_burgers_op* op, const Mats<T>& m, const T* const* src, int nsrc, const T* u,
+                                 double* rhs, StageOut so, cudaStream_t st) {
+    return eval_term_range<T>(op, m, op->n_pv_terms, int(op->terms.size()) - op->n_pv_terms, src, nsrc, u, rhs, so, st);
+}
+
+// wave: the IPDG term alone, -sigma/dx [u][v] summed over the dimensions, in FP64.  The
+// predictor of the adaptive step uses it as its whole right-hand side: EulerODE2nd::
+// step_rk_source recomputes rhs as the operator matrix (the IPDG penalty) times u,
+// replacing the interpolated terms assembled before it (ODESolver.cpp:402-407,
+// BilinearForm.h:23; 03_wave_06_var_coeff_adapt.cpp:215-241).
+amdg_status eval_wave_penalty(amdg_burgers_op* op, const double* u, double* rhs, cudaStream_t st) {
+    const int dim = op->grid->host.dim;
+    const double* src[1] = {u};
+    return eval_term_range<double>(op, mats64(op), int(op->terms.size()) - dim, dim, src, 1, u, rhs, StageOut{}, st);
 }
 
 // wave: K u_{x_d} (d < dim) and K u at the points, then their interpolation
@@ -316,16 +336,16 @@ amdg_status eval_wave_fields(amdg_burgers_op* op, const double* u, To** fucoe, c
         double* acc = static_cast<double*>(op->w_up);
         for (int c0 = 0; c0 < G; c0 += op->chunk) {
             const int cnt = std::min(op->chunk, G - c0);
-            if (amdg_status r = run_terms<double>(op, mats64(op), f * G + c0, cnt, np, 4, src, 1, nullptr, slots, st);
+            if (amdg_status r = run_terms<double>(op, mats64(op), f * G + c0, cnt, np, op->p1, src, 1, nullptr, slots, st);
                 r != AMDG_OK)
                 return r;
             if (c0 + cnt == G) {
                 if (c0 > 0) {  // earlier chunks were summed into acc: fold them in as one more slice
                     AMDG_CK(launch_reduce_points<double>(slots, cnt, n, 0, acc, nullptr, st));
-                    AMDG_CK(launch_reduce_points_coef(acc, 1, E, dim, g->d_order, op->d_pts, op->amp, kp, st));
+                    AMDG_CK(launch_reduce_points_coef(acc, 1, E, dim, op->p1, g->d_order, op->d_pts, op->amp, kp, st));
                     op->grid->ctx->launches++;
                 } else {
-                    AMDG_CK(launch_reduce_points_coef(slots, cnt, E, dim, g->d_order, op->d_pts, op->amp, kp, st));
+                    AMDG_CK(launch_reduce_points_coef(slots, cnt, E, dim, op->p1, g->d_order, op->d_pts, op->amp, kp, st));
                 }
             } else {
                 AMDG_CK(launch_reduce_points<double>(slots, cnt, n, c0 == 0 ? 1 : 0, acc, nullptr, st));
@@ -411,11 +431,11 @@ amdg_status burgers_sync(amdg_burgers_op* op) {
     if (op->anc_order.empty()) {
         // ancestor orders only depend on nmax
         Basis1D b{g->host.k, g->host.nmax};
-        t.anc_order.assign(size_t(op->n1) * 4, -1);
-        build_lagr_ancestors(b, &t);
+        build_lagr_ancestors(b, op->p1 - 1, &t);
         op->anc_order = t.anc_order;
     } else {
         t.anc_order = op->anc_order;
+        t.p1 = op->p1;
     }
     TransformTopology topo;
     build_transform_topology(g->host, &topo);
@@ -532,12 +552,15 @@ static amdg_status lagr_create(amdg_grid* g, int kind, const double* alpha, doub
     op->device = g->device;
     if (alpha) op->alpha.assign(alpha, alpha + dim);
     else op->alpha.assign(dim, 0.0);
+    // Lagrange degree as the examples set it: 3 for Burgers, 4 for the wave equation
+    const int degree = kind == 1 ? 4 : 3;
+    op->p1 = degree + 1;
     op->points = 1;
-    for (int d = 0; d < dim; ++d) op->points *= 4;
+    for (int d = 0; d < dim; ++d) op->points *= op->p1;
     op->n1 = 1 << g->host.nmax;
     Basis1D b{g->host.k, g->host.nmax};
     LagrTables t;
-    build_lagr_tables(b, &t, kind == 1);
+    build_lagr_tables(b, degree, &t, kind == 1);
     std::memcpy(op->weight, t.weight, sizeof(op->weight));
     transform_schedule(dim, &op->sched_dims, &op->sched_lu);
     build_terms(op);
@@ -726,8 +749,8 @@ static amdg_status one_step(amdg_burgers_op* op, double dt, amdg_precision prec)
     return wave_rk4(op, dt, 1, prec);
 }
 
-// the adaptive time step of either operator: predictor (ForwardEuler / EulerODE2nd on u),
-// refine on the predicted u, one step, coarsen
+// the adaptive time step of either operator: predictor (ForwardEuler on u / EulerODE2nd on
+// (u, u_t)), refine on the predicted indicator, one step, coarsen
 static amdg_status adaptive_step_any(amdg_burgers_op* op, double cfl, double wave_speed, double eps, double eta,
                                      amdg_precision prec, double* dt_out, int8_t* decisions) {
     AMDG_REQUIRE(op && std::isfinite(cfl) && cfl > 0 && std::isfinite(wave_speed) && wave_speed > 0, AMDG_ERR_ARG,
@@ -740,23 +763,25 @@ static amdg_status adaptive_step_any(amdg_burgers_op* op, double cfl, double wav
     cudaStream_t st = stream_of(op);
     const double dt = adaptive_dt(g, cfl, wave_speed);
     const std::vector<uint64_t> old_keys = g->host.key;
-    op->rhs_evaluations++;
     amdg_status s;
     if (op->kind == 0) {
+        op->rhs_evaluations++;
         // forward Euler into the prediction buffer (ForwardEuler::step_stage)
         const StageOut so{1, stage_coef(0, dt), g->d_u, g->d_u, op->d_pred};
         if ((s = eval_rhs(op, g->d_u, op->d_rhs64, prec, so)) != AMDG_OK) return s;
     } else {
-        // EulerODE2nd on copies of (u, v) (ODESolver.cpp:409-414); only the predicted u is kept
+        // EulerODE2nd::step_rk_source on copies of (u, v): u + dt v, v + dt (IPDG u)
         if ((s = ensure_velocity(g)) != AMDG_OK) return s;
-        if ((s = eval_rhs(op, g->d_u, op->d_rhs64, prec)) != AMDG_OK) return s;
+        if ((s = eval_wave_penalty(op, g->d_u, op->d_rhs64, st)) != AMDG_OK) return s;
         AMDG_CK(launch_rk4_2nd_stage(-1, dt, op->d_rhs64, g->d_u, g->d_v, op->d_pred, op->d_su, nullptr, nullptr, g->dof,
                                      st));
         g->ctx->launches++;
     }
-    // refine on the predicted coefficients; new elements start from zero (DGAdapt::refine, copy_predict_to_ucoe)
+    // refine on the predicted coefficients (and, for the wave, the predicted u_t: the
+    // indicator of prob "wave" is ||u|| + ||u_t||); new elements start from zero
+    // (DGAdapt::refine, copy_predict_to_ucoe)
     std::vector<double> norms;
-    if ((s = grid_norms(g, op->d_pred, &norms)) != AMDG_OK) return s;
+    if ((s = grid_norms(g, op->d_pred, &norms, op->kind == 1 ? op->d_su : nullptr)) != AMDG_OK) return s;
     std::vector<uint8_t> refined;
     std::vector<uint64_t> keys;
     {
@@ -767,7 +792,7 @@ static amdg_status adaptive_step_any(amdg_burgers_op* op, double cfl, double wav
         for (size_t e = 0; e < refined.size(); ++e) decisions[e] = refined[e] ? 1 : 0;
     if (int64_t(keys.size()) != g->host.num_elements && (s = grid_set_keys(g, std::move(keys))) != AMDG_OK) return s;
     if ((s = one_step(op, dt, prec)) != AMDG_OK) return s;
-    if ((s = amdg_grid_coarsen(g, eta, nullptr)) != AMDG_OK) return s;
+    if ((s = grid_coarsen(g, eta, op->kind == 1 ? g->d_v : nullptr, nullptr)) != AMDG_OK) return s;
     if (decisions) mark_removed(old_keys, g->host, decisions);
     if (dt_out) *dt_out = dt;
     return AMDG_OK;
@@ -787,9 +812,12 @@ amdg_status amdg_burgers_features(amdg_burgers_op* op, const double* d_u, float*
     AMDG_REQUIRE(op && d_u && d_features, AMDG_ERR_ARG, "null argument");
     AMDG_CK(cudaSetDevice(op->device));
     if (amdg_status rs = burgers_sync(op); rs != AMDG_OK) return rs;
-    const amdg_grid* g = op->grid;
+    amdg_grid* g = op->grid;
     if (amdg_status s = ensure_features(op, 0, 0); s != AMDG_OK) return s;
-    AMDG_CK(launch_element_features(d_u, op->d_pg, g->host.num_elements, g->host.dim, g->block, d_features, stream_of(op)));
+    if (op->kind == 1)
+        if (amdg_status s = ensure_velocity(g); s != AMDG_OK) return s;
+    AMDG_CK(launch_element_features(d_u, op->kind == 1 ? g->d_v : nullptr, op->d_pg, g->host.num_elements, g->host.dim,
+                                    g->block, d_features, stream_of(op)));
     g->ctx->launches++;
     return AMDG_OK;
 }
@@ -806,7 +834,8 @@ static amdg_status learned_step_any(amdg_burgers_op* op, amdg_mlp* mlp, double c
     cudaStream_t st = stream_of(op);
     const double dt = adaptive_dt(g, cfl, wave_speed);
     const int64_t E = g->host.num_elements;
-    const int F = g->block * (1 + 2 * g->host.dim);
+    // the wave classifier also reads u_t (the indicator of prob "wave" adds ||u_t||)
+    const int F = g->block * (1 + 2 * g->host.dim) * (op->kind == 1 ? 2 : 1);
     int n_in = 0, n_out = 0;
     mlp_shape(mlp, &n_in, &n_out);
     AMDG_REQUIRE(n_in == F && n_out == 3, AMDG_ERR_ARG,
@@ -817,13 +846,17 @@ static amdg_status learned_step_any(amdg_burgers_op* op, amdg_mlp* mlp, double c
     {
         PhaseTimer tc(g->ctx, AMDG_PHASE_CLASSIFIER);
         if ((s = ensure_features(op, E, F)) != AMDG_OK) return s;
-        AMDG_CK(launch_element_features(g->d_u, op->d_pg, E, g->host.dim, g->block, op->d_feat, st));
+        if (op->kind == 1 && (s = ensure_velocity(g)) != AMDG_OK) return s;
+        AMDG_CK(launch_element_features(g->d_u, op->kind == 1 ? g->d_v : nullptr, op->d_pg, E, g->host.dim, g->block,
+                                        op->d_feat, st));
         g->ctx->launches++;
         if ((s = amdg_mlp_predict(mlp, op->d_feat, E, op->d_prob)) != AMDG_OK) return s;
         AMDG_CK(cudaMemcpyAsync(prob.data(), op->d_prob, prob.size() * sizeof(float), cudaMemcpyDeviceToHost, st));
     }
+    if (op->kind == 1 && (s = ensure_velocity(g)) != AMDG_OK) return s;
+    const double* d_ut = op->kind == 1 ? g->d_v : nullptr;  // the wave indicator adds ||u_t||
     std::vector<double> norms;
-    if ((s = grid_norms(g, g->d_u, &norms)) != AMDG_OK) return s;  // synchronises the stream
+    if ((s = grid_norms(g, g->d_u, &norms, d_ut)) != AMDG_OK) return s;  // synchronises the stream
     // 2. pre-adapt: leaves the network marks "refine" (class 0) get children;
     //    where it is unsure (max probability < tau) the surplus criterion on
     //    the current coefficients decides instead; leaves the criterion found
@@ -857,7 +890,7 @@ static amdg_status learned_step_any(amdg_burgers_op* op, amdg_mlp* mlp, double c
     // 4. coarsening (amdg_grid_coarsen), then the surplus criterion judges the
     //    result: leaves still above eps are missed refinements, refined at the
     //    start of the next step
-    if ((s = grid_norms(g, g->d_u, &norms)) != AMDG_OK) return s;
+    if ((s = grid_norms(g, g->d_u, &norms, op->kind == 1 ? g->d_v : nullptr)) != AMDG_OK) return s;
     std::vector<std::pair<uint64_t, double>> above;
     {
         PhaseTimer th(g->ctx, AMDG_PHASE_ADAPT_HOST);

@@ -277,7 +277,8 @@ void build_transform_topology(const HostGrid& g, TransformTopology* out) {
 bool build_surplus_ancestors(const HostGrid& g, const LagrTables& t, std::vector<int32_t>* anc) {
     const int dim = g.dim;
     const int64_t E = g.num_elements;
-    anc->assign(size_t(E) * dim * 4, -1);
+    const int P1 = t.p1;
+    anc->assign(size_t(E) * dim * P1, -1);
     int holes = 0;
 #pragma omp parallel for schedule(static) reduction(+ : holes) if (E >= 4096)
     for (int64_t e = 0; e < E; ++e) {
@@ -285,12 +286,12 @@ bool build_surplus_ancestors(const HostGrid& g, const LagrTables& t, std::vector
         const int32_t* oe = &g.order[size_t(e) * dim];
         for (int d = 0; d < dim; ++d) {
             if (oe[d] == 0) continue;
-            for (int ic = 0; ic < 4; ++ic) {
+            for (int ic = 0; ic < P1; ++ic) {
                 std::copy(oe, oe + dim, o2);
-                o2[d] = t.anc_order[size_t(oe[d]) * 4 + ic];
+                o2[d] = t.anc_order[size_t(oe[d]) * P1 + ic];
                 const int64_t s = find_element(g, o2);
                 if (s < 0) ++holes;  // the element set has a hole
-                (*anc)[(size_t(e) * dim + d) * 4 + ic] = int32_t(s);
+                (*anc)[(size_t(e) * dim + d) * P1 + ic] = int32_t(s);
             }
         }
     }

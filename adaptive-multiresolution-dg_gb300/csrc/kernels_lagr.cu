@@ -113,6 +113,7 @@ __global__ void __launch_bounds__(256) sweep_kernel(SweepArgs<T> a) {
         }
         if (n_from == 4) acc = fibre_quad<4>(x, m, stride, ncols, acc);
         else if (n_from == 3) acc = fibre_quad<3>(x, m, stride, ncols, acc);
+        else if (n_from == 5) acc = fibre_quad<5>(x, m, stride, ncols, acc);
         else {
 #pragma unroll
             for (int j = 0; j < 4; ++j)
@@ -191,15 +192,15 @@ __global__ void __launch_bounds__(256) surplus_pass_kernel(SurplusArgs<Ti> a, co
     Ti c = in[gid];
     const int od = __ldg(a.order + e * a.dim + a.d);
     if (od != 0) {
-        const int pd = (p / a.stride) % 4;
+        const int P1 = a.p1;
+        const int pd = (p / a.stride) % P1;
         const int base = p - pd * a.stride;
-        const int32_t* anc = a.anc + (e * a.dim + a.d) * 4;
-#pragma unroll
-        for (int ic = 0; ic < 4; ++ic) {
+        const int32_t* anc = a.anc + (e * a.dim + a.d) * P1;
+        for (int ic = 0; ic < P1; ++ic) {
             const int s = __ldg(anc + ic);
-            const int q = __ldg(a.anc_point + od * 4 + ic);
-            const int r = __ldg(a.anc_rank + od * 4 + ic);
-            c = fma(Ti(a.weight[pd * 4 + r]), in[int64_t(s) * a.points + base + q * a.stride], c);
+            const int q = __ldg(a.anc_point + od * P1 + ic);
+            const int r = __ldg(a.anc_rank + od * P1 + ic);
+            c = fma(Ti(a.weight[pd * P1 + r]), in[int64_t(s) * a.points + base + q * a.stride], c);
         }
     }
     out[gid] = To(c);
@@ -233,11 +234,11 @@ cudaError_t launch_convert(const Ti* in, To* out, int64_t n, cudaStream_t st) {
 template cudaError_t launch_convert<double, float>(const double*, float*, int64_t, cudaStream_t);
 template cudaError_t launch_convert<float, double>(const float*, double*, int64_t, cudaStream_t);
 
-__global__ void reduce_points_coef_kernel(const double* __restrict__ buf, int count, int64_t E, int dim,
+__global__ void reduce_points_coef_kernel(const double* __restrict__ buf, int count, int64_t E, int dim, int p1,
                                           const int32_t* __restrict__ order, const double* __restrict__ pts, double amp,
                                           double* __restrict__ out) {
     int P = 1;
-    for (int d = 0; d < dim; ++d) P *= 4;
+    for (int d = 0; d < dim; ++d) P *= p1;
     const int64_t n = E * P;
     const int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
     if (i >= n) return;
@@ -249,8 +250,8 @@ __global__ void reduce_points_coef_kernel(const double* __restrict__ buf, int co
     const double pi = 3.14159265358979323846;
     double x[kMaxDim];
     for (int d = dim - 1; d >= 0; --d) {
-        x[d] = __ldg(pts + __ldg(order + e * dim + d) * 4 + r % 4);
-        r /= 4;
+        x[d] = __ldg(pts + __ldg(order + e * dim + d) * p1 + r % p1);
+        r /= p1;
     }
     double prod = 1.0;
     for (int d = 0; d < dim; ++d) prod *= sin(2 * pi * x[d]);
@@ -258,12 +259,12 @@ __global__ void reduce_points_coef_kernel(const double* __restrict__ buf, int co
     out[i] = (c * c) * v;
 }
 
-cudaError_t launch_reduce_points_coef(const double* buf, int count, int64_t E, int dim, const int32_t* order,
+cudaError_t launch_reduce_points_coef(const double* buf, int count, int64_t E, int dim, int p1, const int32_t* order,
                                       const double* pts, double amp, double* out, cudaStream_t st) {
     int64_t n = E;
-    for (int d = 0; d < dim; ++d) n *= 4;
+    for (int d = 0; d < dim; ++d) n *= p1;
     if (n == 0) return cudaSuccess;
-    reduce_points_coef_kernel<<<unsigned((n + 255) / 256), 256, 0, st>>>(buf, count, E, dim, order, pts, amp, out);
+    reduce_points_coef_kernel<<<unsigned((n + 255) / 256), 256, 0, st>>>(buf, count, E, dim, p1, order, pts, amp, out);
     return cudaGetLastError();
 }
 

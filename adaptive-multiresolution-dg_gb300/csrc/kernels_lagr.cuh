@@ -44,8 +44,9 @@ template <typename T>
 cudaError_t launch_reduce_points(const T* buf, int count, int64_t n, int first, T* acc, T* fp, cudaStream_t st);
 
 // Diffusion coefficient at the points: out = K(x) * sum_s buf[s] (in order), K = (1 + amp
-// prod_d sin(2 pi x_d))^2 at the point's coordinates (pts[order * 4 + p_d] per dimension).
-cudaError_t launch_reduce_points_coef(const double* buf, int count, int64_t E, int dim, const int32_t* order,
+// prod_d sin(2 pi x_d))^2 at the point's coordinates (pts[order * p1 + p_d] per dimension,
+// p1 points per dimension).
+cudaError_t launch_reduce_points_coef(const double* buf, int count, int64_t E, int dim, int p1, const int32_t* order,
                                       const double* pts, double amp, double* out, cudaStream_t st);
 
 // One RK4ODE2nd stage (ODESolver.cpp:579-615) given the right-hand side at (us, vs):
@@ -71,13 +72,13 @@ cudaError_t launch_reduce_rhs(const T* buf, int count, int64_t n, int first, int
 
 template <typename T>
 struct SurplusArgs {
-    int dim, d, points, stride;  // points = 4^dim, stride of dimension d
+    int dim, d, p1, points, stride;  // p1 points per dimension, points = p1^dim, stride of dimension d
     int64_t num_elements;
     const int32_t* order;
-    const int32_t* anc;          // [element][dim][4]
-    const int32_t* anc_point;    // [1D order][4]
-    const int32_t* anc_rank;     // [1D order][4]
-    double weight[16];           // [p0][rank]
+    const int32_t* anc;          // [element][dim][p1]
+    const int32_t* anc_point;    // [1D order][p1]
+    const int32_t* anc_rank;     // [1D order][p1]
+    double weight[kMaxLagrPoints * kMaxLagrPoints];  // [p0][rank]
 };
 // one surplus pass, input and output types may differ (the last pass of the
 // mixed mode writes the FP32 coefficients of the back transforms)

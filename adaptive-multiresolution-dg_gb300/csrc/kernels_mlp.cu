@@ -89,13 +89,19 @@ __global__ void adam_kernel(float* __restrict__ p, const float* __restrict__ g, 
 
 // features of element e: magnitudes of its block, then for every dimension
 // the blocks of its parent and grandparent in that dimension (zero when absent)
-__global__ void element_features_kernel(const double* __restrict__ u, const int32_t* __restrict__ anc, int64_t E, int dim,
-                                        int B, float* __restrict__ feat) {
+__global__ void element_features_kernel(const double* __restrict__ u, const double* __restrict__ u2,
+                                        const int32_t* __restrict__ anc, int64_t E, int dim, int B,
+                                        float* __restrict__ feat) {
     const int64_t gid = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
-    const int F = B * (1 + 2 * dim);
+    const int F1 = B * (1 + 2 * dim), F = u2 ? 2 * F1 : F1;
     if (gid >= E * F) return;
     const int64_t e = gid / F;
-    const int f = int(gid - e * F);
+    int f = int(gid - e * F);
+    const double* field = u;
+    if (f >= F1) {  // second field's block of the row
+        f -= F1;
+        field = u2;
+    }
     const int slot = f / B, q = f - slot * B;
     int64_t src = e;
     if (slot > 0) {
@@ -104,7 +110,7 @@ __global__ void element_features_kernel(const double* __restrict__ u, const int3
     }
     float v = 0.f;
     if (src >= 0) {
-        const double c = fabs(u[src * B + q]);
+        const double c = fabs(field[src * B + q]);
         v = float(log10(c + 1e-20) / 20.0 + 1.0);
     }
     feat[gid] = v;
@@ -145,11 +151,11 @@ cudaError_t launch_adam(float* p, const float* g, float* m, float* v, int64_t n,
     return cudaGetLastError();
 }
 
-cudaError_t launch_element_features(const double* u, const int32_t* anc, int64_t E, int dim, int B, float* feat,
-                                    cudaStream_t st) {
-    const int64_t total = E * int64_t(B) * (1 + 2 * dim);
+cudaError_t launch_element_features(const double* u, const double* u2, const int32_t* anc, int64_t E, int dim, int B,
+                                    float* feat, cudaStream_t st) {
+    const int64_t total = E * int64_t(B) * (1 + 2 * dim) * (u2 ? 2 : 1);
     if (total == 0) return cudaSuccess;
-    element_features_kernel<<<blocks_for(total), 256, 0, st>>>(u, anc, E, dim, B, feat);
+    element_features_kernel<<<blocks_for(total), 256, 0, st>>>(u, u2, anc, E, dim, B, feat);
     return cudaGetLastError();
 }
 

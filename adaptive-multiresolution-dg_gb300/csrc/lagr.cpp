@@ -1,6 +1,7 @@
 // Host set-up of the Lagrange-interpolation path for nonlinear fluxes:
-// hierarchical degree-3 Lagrange basis (node layout msh_case 1,
-// LagrBasis.cpp:65-70), the Alpert-at-Lagrange-point table
+// hierarchical Lagrange bases of degree 3 (node layout msh_case 1,
+// LagrBasis.cpp:65-70, the Burgers examples) and degree 4 (msh_case 2,
+// LagrBasis.cpp:92-97, the wave example), the Alpert-at-Lagrange-point table
 // (Interplation.cpp:16-101), the Lagrange x Alpert 1D matrices
 // (OperatorMatrix1D<LagrBasis,AlptBasis>, OperatorMatrix1D.h:166-199), the
 // dimension-order / L-U schedule of the fast transforms
@@ -14,30 +15,47 @@
 namespace amdg {
 namespace {
 
-// nodes on [-1,1]: level 0, and level >= 1 (two on each half of the support)
-const double kMsh0[4] = {-0.6, -0.2, 0.2, 0.6};
-const double kMsh1[4] = {-0.8, -0.4, 0.4, 0.8};
+// Degree 3, msh_case 1: level-0 nodes {-3/5,-1/5,1/5,3/5}; level-1 nodes
+// {-4/5,-2/5} on the left half and {2/5,4/5} on the right half, each the cubic
+// through the four nodes of its half (with the two level-0 nodes there).
+const LagrSpec kDeg3 = {4,
+                        {-0.6, -0.2, 0.2, 0.6},
+                        {-0.8, -0.4, 0.4, 0.8},
+                        {-0.6, -0.2, 0.2, 0.6},
+                        {{-0.8, -0.6, -0.4, -0.2}, {0.2, 0.4, 0.6, 0.8}},
+                        {0, 0, 1, 1},
+                        {0, 2, 1, 3}};
+// Degree 4, msh_case 2: level-0 nodes {-1,-1/2,0,1/2,1}, whose points sit
+// 1e-13 inside the element (left of the node except at -1); level-1 nodes
+// {-3/4,-1/4} on the left half and {0,1/4,3/4} on the right half (the point
+// at 0 just right of it), each the quartic through the nodes of its half at
+// spacing 1/4.
+const LagrSpec kDeg4 = {5,
+                        {-1 + kRoundOff, -0.5 - kRoundOff, 0 - kRoundOff, 0.5 - kRoundOff, 1 - kRoundOff},
+                        {-0.75 - kRoundOff, -0.25 - kRoundOff, 0 + kRoundOff, 0.25 - kRoundOff, 0.75 - kRoundOff},
+                        {-1, -0.5, 0, 0.5, 1},
+                        {{-1, -0.75, -0.5, -0.25, 0}, {0, 0.25, 0.5, 0.75, 1}},
+                        {0, 0, 1, 1, 1},
+                        {1, 3, 0, 1, 3}};
 
-double lagrange_poly(const double* nodes, int i, double x) {
+double lagrange_poly(const double* nodes, int n, int i, double x) {
     double v = 1.0;
-    for (int m = 0; m < 4; ++m)
+    for (int m = 0; m < n; ++m)
         if (m != i) v *= (x - nodes[m]) / (nodes[i] - nodes[m]);
     return v;
 }
 
 // level-0 / level-1 mother functions on [0,1]
-double lagr_mother(double xt, int msh, int p) {
+double lagr_mother(const LagrSpec& s, double xt, int msh, int p) {
     const double x = 2.0 * xt - 1.0;
     if (x < -1.0 || x > 1.0) return 0.0;
-    if (msh == 0) return lagrange_poly(kMsh0, p, x);
-    if (p <= 1) {
+    if (msh == 0) return lagrange_poly(s.node0, s.p1, p, x);
+    if (s.side[p] == 0) {
         if (x > 0.0) return 0.0;
-        static const double left[4] = {-0.8, -0.6, -0.4, -0.2};
-        return lagrange_poly(left, p == 0 ? 0 : 2, x);
+        return lagrange_poly(s.half[0], s.p1, s.node[p], x);
     }
     if (x < 0.0) return 0.0;
-    static const double right[4] = {0.2, 0.4, 0.6, 0.8};
-    return lagrange_poly(right, p == 2 ? 1 : 3, x);
+    return lagrange_poly(s.half[1], s.p1, s.node[p], x);
 }
 
 double supp_lo(int o) { int n, j; elem_of_order(o, &n, &j); return n <= 1 ? 0.0 : std::pow(2.0, 1.0 - n) * (j - 1.0) / 2.0; }
@@ -81,8 +99,14 @@ struct GL10 {
 
 }  // namespace
 
-double lagr_eval(int order, double x, int sgn) {
-    const int o = order / 4, p = order % 4;
+const LagrSpec* lagr_spec(int degree) {
+    if (degree == 3) return &kDeg3;
+    if (degree == 4) return &kDeg4;
+    return nullptr;
+}
+
+double lagr_eval(const LagrSpec& s, int order, double x, int sgn) {
+    const int o = order / s.p1, p = order % s.p1;
     int n, j;
     elem_of_order(o, &n, &j);
     double xl = x;
@@ -93,58 +117,65 @@ double lagr_eval(int order, double x, int sgn) {
         if (std::fabs(x - 1.0) <= kRoundOff) return 0.0;
         xl += kRoundOff;
     }
-    if (n <= 1) return lagr_mother(xl, n, p);
-    return lagr_mother(std::pow(2.0, n - 1) * xl - double((j - 1) / 2), 1, p);
+    if (n <= 1) return lagr_mother(s, xl, n, p);
+    return lagr_mother(s, std::pow(2.0, n - 1) * xl - double((j - 1) / 2), 1, p);
 }
 
-double lagr_point(int o, int p) {
+double lagr_point(const LagrSpec& s, int o, int p) {
     int n, j;
     elem_of_order(o, &n, &j);
-    if (n == 0) return (kMsh0[p] + 1.0) / 2.0;
+    if (n == 0) return (s.pt0[p] + 1.0) / 2.0;
     const double a = supp_lo(o), b = supp_hi(o);
-    return a + (b - a) * (kMsh1[p] + 1.0) / 2.0;
+    return a + (b - a) * (s.pt1[p] + 1.0) / 2.0;
 }
 
-void build_lagr_ancestors(const Basis1D& alpt, LagrTables* t) {
-    const int n1 = alpt.num_elem();
+void build_lagr_ancestors(const Basis1D& alpt, int degree, LagrTables* t) {
+    const LagrSpec& S = *lagr_spec(degree);
+    const int n1 = alpt.num_elem(), P1 = S.p1;
+    t->spec = &S;
+    t->p1 = P1;
     // surplus: ancestors (coarser-level points inside each element's support) and weights
-    t->anc_order.assign(size_t(n1) * 4, -1);
-    t->anc_point.assign(size_t(n1) * 4, 0);
-    t->anc_rank.assign(size_t(n1) * 4, 0);
+    t->anc_order.assign(size_t(n1) * P1, -1);
+    t->anc_point.assign(size_t(n1) * P1, 0);
+    t->anc_rank.assign(size_t(n1) * P1, 0);
     for (int o = 1; o < n1; ++o) {
         const int l = level_of_order(o);
         const double xl = supp_lo(o), xr = supp_hi(o);
         int ic = 0;
-        double pos[4] = {0, 0, 0, 0};
-        for (int oa = 0; oa < n1 && ic < 4; ++oa) {
+        double pos[kMaxLagrPoints] = {0};
+        for (int oa = 0; oa < n1 && ic < P1; ++oa) {
             if (level_of_order(oa) >= l) break;
-            for (int q = 0; q < 4 && ic < 4; ++q) {
-                const double x = lagr_point(oa, q);
+            for (int q = 0; q < P1 && ic < P1; ++q) {
+                const double x = lagr_point(S, oa, q);
                 if (x > xl && x < xr) {
-                    t->anc_order[size_t(o) * 4 + ic] = oa;
-                    t->anc_point[size_t(o) * 4 + ic] = q;
+                    t->anc_order[size_t(o) * P1 + ic] = oa;
+                    t->anc_point[size_t(o) * P1 + ic] = q;
                     pos[ic] = x;
                     ++ic;
                 }
             }
         }
-        for (int a = 0; a < 4; ++a) {
+        for (int a = 0; a < P1; ++a) {
             int rk = 0;
-            for (int b = 0; b < 4; ++b) rk += pos[b] < pos[a];
-            t->anc_rank[size_t(o) * 4 + a] = rk;
+            for (int b = 0; b < P1; ++b) rk += pos[b] < pos[a];
+            t->anc_rank[size_t(o) * P1 + a] = rk;
         }
     }
 }
 
-void build_lagr_tables(const Basis1D& alpt, LagrTables* t, bool diffusion) {
+void build_lagr_tables(const Basis1D& alpt, int degree, LagrTables* t, bool diffusion) {
     static const GL10 g;
-    const int n1 = alpt.num_elem(), na = alpt.num_basis(), np = alpt.k + 1, nl = n1 * 4;
+    const LagrSpec& S = *lagr_spec(degree);
+    const int P1 = S.p1;
+    const int n1 = alpt.num_elem(), na = alpt.num_basis(), np = alpt.k + 1, nl = n1 * P1;
+    t->spec = &S;
+    t->p1 = P1;
     t->n_lagr = nl;
     t->n_alpt = na;
     // Alpert basis at Lagrange points, row = Alpert basis, col = Lagrange point
     t->a2p.assign(size_t(na) * nl, 0.0);
     for (int c = 0; c < nl; ++c) {
-        const double x = lagr_point(c / 4, c % 4);
+        const double x = lagr_point(S, c / P1, c % P1);
         for (int r = 0; r < na; ++r) {
             const int o = r / np;
             if (x < supp_lo(o) || x > supp_hi(o)) continue;
@@ -157,7 +188,7 @@ void build_lagr_tables(const Basis1D& alpt, LagrTables* t, bool diffusion) {
     t->lflx.assign(size_t(nl) * na, 0.0);
 #pragma omp parallel for schedule(dynamic)
     for (int r = 0; r < nl; ++r) {
-        const int ou = r / 4;
+        const int ou = r / P1;
         const int lu = level_of_order(ou);
         const double ua = supp_lo(ou), ub = supp_hi(ou);
         for (int c = 0; c < na; ++c) {
@@ -168,8 +199,8 @@ void build_lagr_tables(const Basis1D& alpt, LagrTables* t, bool diffusion) {
                 double xl = ua, xr = ub;
                 if (lu <= level_of_order(ov)) { xl = va; xr = vb; }
                 const double xm = 0.5 * (xl + xr);
-                auto fv = [&](double x) { return lagr_eval(r, x, 0) * alpt.eval(c, 0, x, 0); };
-                auto fvx = [&](double x) { return lagr_eval(r, x, 0) * alpt.eval(c, 1, x, 0); };
+                auto fv = [&](double x) { return lagr_eval(S, r, x, 0) * alpt.eval(c, 0, x, 0); };
+                auto fvx = [&](double x) { return lagr_eval(S, r, x, 0) * alpt.eval(c, 1, x, 0); };
                 t->lv[idx] = g.integrate(fv, xl, xm) + g.integrate(fv, xm, xr);
                 t->lvx[idx] = g.integrate(fvx, xl, xm) + g.integrate(fvx, xm, xr);
             }
@@ -179,12 +210,12 @@ void build_lagr_tables(const Basis1D& alpt, LagrTables* t, bool diffusion) {
                 double s = 0.0;
                 for (int i = 0; i < npts; ++i) {
                     const double x = pts[i];
-                    double fu = lagr_eval(r, x, su), fw = alpt.eval(c, 0, x, sv);
+                    double fu = lagr_eval(S, r, x, su), fw = alpt.eval(c, 0, x, sv);
                     if (std::fabs(x) < kRoundOff) {
-                        if (su == -1) fu = lagr_eval(r, 1.0, su);
+                        if (su == -1) fu = lagr_eval(S, r, 1.0, su);
                         if (sv == -1) fw = alpt.eval(c, 0, 1.0, sv);
                     } else if (std::fabs(x - 1.0) < kRoundOff) {
-                        if (su == 1) fu = lagr_eval(r, 0.0, su);
+                        if (su == 1) fu = lagr_eval(S, r, 0.0, su);
                         if (sv == 1) fw = alpt.eval(c, 0, 0.0, sv);
                     }
                     s += fu * fw;
@@ -201,7 +232,7 @@ void build_lagr_tables(const Basis1D& alpt, LagrTables* t, bool diffusion) {
         t->a2pd.assign(size_t(na) * nl, 0.0);
         t->pts.assign(nl, 0.0);
         for (int c = 0; c < nl; ++c) {
-            const double x = lagr_point(c / 4, c % 4);
+            const double x = lagr_point(S, c / P1, c % P1);
             t->pts[c] = x;
             for (int r = 0; r < na; ++r) {
                 const int o = r / np;
@@ -214,7 +245,7 @@ void build_lagr_tables(const Basis1D& alpt, LagrTables* t, bool diffusion) {
         t->ljv.assign(size_t(nl) * na, 0.0);
 #pragma omp parallel for schedule(dynamic)
         for (int r = 0; r < nl; ++r) {
-            const int ou = r / 4;
+            const int ou = r / P1;
             const double ua = supp_lo(ou), ub = supp_hi(ou);
             const double pts[3] = {ua, 0.5 * (ua + ub), ub};
             const int npts = level_of_order(ou) <= 1 ? 2 : 3;
@@ -223,12 +254,12 @@ void build_lagr_tables(const Basis1D& alpt, LagrTables* t, bool diffusion) {
                     double s = 0.0;
                     for (int i = 0; i < npts; ++i) {
                         const double x = pts[i];
-                        double fu = lagr_eval(r, x, su), fw = alpt.eval(c, 1, x, sv);
+                        double fu = lagr_eval(S, r, x, su), fw = alpt.eval(c, 1, x, sv);
                         if (std::fabs(x) < kRoundOff) {
-                            if (su == -1) fu = lagr_eval(r, 1.0, su);
+                            if (su == -1) fu = lagr_eval(S, r, 1.0, su);
                             if (sv == -1) fw = alpt.eval(c, 1, 1.0, sv);
                         } else if (std::fabs(x - 1.0) < kRoundOff) {
-                            if (su == 1) fu = lagr_eval(r, 0.0, su);
+                            if (su == 1) fu = lagr_eval(S, r, 0.0, su);
                             if (sv == 1) fw = alpt.eval(c, 1, 0.0, sv);
                         }
                         s += fu * fw;
@@ -245,10 +276,10 @@ void build_lagr_tables(const Basis1D& alpt, LagrTables* t, bool diffusion) {
     build_oper1d(alpt, &op, false);
     t->ajump.assign(size_t(na) * na, 0.0);
     for (size_t i = 0; i < t->ajump.size(); ++i) t->ajump[i] = op.urgt_vjp[i] - op.ulft_vjp[i];
-    build_lagr_ancestors(alpt, t);
-    // weight[p0][rank] = -L0_rank(node p0 of the element, in its reference coordinates)
-    for (int p0 = 0; p0 < 4; ++p0)
-        for (int r = 0; r < 4; ++r) t->weight[p0 * 4 + r] = -lagr_mother((kMsh1[p0] + 1.0) / 2.0, 0, r);
+    build_lagr_ancestors(alpt, degree, t);
+    // weight[p0][rank] = -L0_rank(point p0 of the element, in its reference coordinates)
+    for (int p0 = 0; p0 < P1; ++p0)
+        for (int r = 0; r < P1; ++r) t->weight[p0 * P1 + r] = -lagr_mother(S, (S.pt1[p0] + 1.0) / 2.0, 0, r);
 }
 
 void transform_schedule(int dim, std::vector<std::vector<int>>* dim_order, std::vector<std::vector<int>>* lu) {

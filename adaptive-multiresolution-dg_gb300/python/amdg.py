@@ -20,7 +20,7 @@ FP64 = 0
 MIXED = 1
 
 STATUS = {0: "ok", 1: "invalid argument", 2: "capacity exceeded", 3: "non-finite value", 4: "device wait timed out",
-          5: "CUDA error", 6: "invalid state", 7: "out of memory"}
+          5: "CUDA error", 6: "invalid state", 7: "out of memory", 8: "I/O error", 9: "bad checkpoint"}
 
 FN1D = C.CFUNCTYPE(C.c_double, C.c_double, C.c_int, C.c_int, C.c_void_p)
 
@@ -99,6 +99,10 @@ def load():
         "amdg_grid_eval_tensor": ([vp, i32, vp, vp], i32),
         "amdg_grid_set_velocity": ([vp, vp, i64], i32),
         "amdg_grid_get_velocity": ([vp, vp, i64], i32),
+        "amdg_grid_save": ([vp, C.c_char_p, dbl], i32),
+        "amdg_grid_load": ([vp, C.c_char_p, pp, vp], i32),
+        "amdg_grid_write_level_support": ([vp, C.c_char_p], i32),
+        "amdg_grid_config": ([vp, vp, vp, vp, vp], i32),
         "amdg_wave_create": ([vp, dbl, dbl, pp], i32),
         "amdg_wave_destroy": ([vp], i32),
         "amdg_wave_rhs": ([vp, vp, vp, i32], i32),
@@ -236,6 +240,28 @@ class Grid:
         ne, dof = C.c_int64(), C.c_int64()
         _ck(load().amdg_grid_size(self._h, C.byref(ne), C.byref(dof)), "grid_size")
         self.num_elements, self.dof = ne.value, dof.value
+
+    def save(self, path: str, time: float = 0.0):
+        """Binary checkpoint: element keys, coefficients, u_t when present, and time."""
+        _ck(load().amdg_grid_save(self._h, os.fsencode(path), time), "grid_save")
+
+    @classmethod
+    def load(cls, ctx: Context, path: str):
+        """(grid, time) restored from a checkpoint written by save."""
+        h, t = C.c_void_p(), C.c_double()
+        _ck(load().amdg_grid_load(ctx.handle, os.fsencode(path), C.byref(h), C.byref(t)), "grid_load")
+        dim, nmax, k, sparse = C.c_int(), C.c_int(), C.c_int(), C.c_int()
+        _ck(load().amdg_grid_config(h, C.byref(dim), C.byref(nmax), C.byref(k), C.byref(sparse)), "grid_config")
+        g = cls.__new__(cls)
+        g.ctx, g.dim, g.nmax, g.k, g.sparse = ctx, dim.value, nmax.value, k.value, bool(sparse.value)
+        g._h = h
+        g.block = (g.k + 1) ** g.dim
+        g._refresh()
+        return g, t.value
+
+    def write_level_support(self, path: str):
+        """IO::output_element_level_support: "level xl xr " per dimension, one element per line."""
+        _ck(load().amdg_grid_write_level_support(self._h, os.fsencode(path)), "grid_write_level_support")
 
     def init_separable_adaptive(self, funcs, eps: float):
         cb = _fn1d(funcs)
@@ -496,6 +522,11 @@ class WaveOperator:
             "wave_adaptive_step_ex")
         self.grid._refresh()
         return dt.value, dec
+
+    @property
+    def num_features(self) -> int:
+        """Classifier inputs per element: the features of u followed by those of u_t."""
+        return 2 * self.grid.block * (1 + 2 * self.grid.dim)
 
     def features_device(self, d_u: int, d_feat: int):
         _ck(load().amdg_wave_features(self._h, C.c_void_p(d_u), C.c_void_p(d_feat)), "wave_features")

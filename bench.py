@@ -451,10 +451,10 @@ def bench_wave_adaptive(ctx, stream, args):
     import amdg
     import amdg_oracle as O
     dim, nmax, level_init, eps, eta, sigma, T, tau, speed = 2, 9, 3, 1e-5, 1e-6, 10.0, args.wave_time, 0.8, 1.0
-    F = 9 * (1 + 2 * dim)
+    F = 2 * 9 * (1 + 2 * dim)  # features of u and of u_t
     out = {"workload": f"2D wave u_tt = div(c^2 grad u), c = 1 + 0.5 sin(2 pi x) sin(2 pi y), Gaussian bump at "
                        f"rest, adaptive (refine 1e-5, coarsen 1e-6, max level 9, start level 3), Alpert k=2, "
-                       f"Lagrange m=3, IPDG sigma 10, RK4ODE2nd, CFL 0.1, to T = {T}"}
+                       f"Lagrange degree 4 (msh_case 2 nodes), IPDG sigma 10, RK4ODE2nd, CFL 0.1, to T = {T}"}
     t0 = time.perf_counter()
     rng = np.random.default_rng(2)
     feats, labs = [], []

@@ -41,7 +41,9 @@ typedef enum amdg_status {
     AMDG_ERR_TIMEOUT = 4,   /* a bounded device-side wait gave up */
     AMDG_ERR_CUDA = 5,      /* a CUDA runtime call failed (see amdg_last_error) */
     AMDG_ERR_STATE = 6,     /* call out of order (e.g. state not initialised) */
-    AMDG_ERR_NOMEM = 7      /* device or host allocation failed */
+    AMDG_ERR_NOMEM = 7,     /* device or host allocation failed */
+    AMDG_ERR_IO = 8,        /* a file could not be opened, read or written */
+    AMDG_ERR_FORMAT = 9     /* a file is not a valid checkpoint (magic, version, range, checksum) */
 } amdg_status;
 
 /* Arithmetic of the operator applies.  The state and the RK stage
@@ -318,8 +320,22 @@ amdg_status amdg_burgers_adaptive_step_ex(amdg_burgers_op* op, double cfl, doubl
 amdg_status amdg_grid_set_velocity(amdg_grid* g, const double* host, int64_t n);
 amdg_status amdg_grid_get_velocity(const amdg_grid* g, double* host, int64_t n);
 
+/* ---- checkpoint / restart (no reference counterpart: the reference's IO writes text only) ---- */
+/* Binary checkpoint of the grid: sorted element keys, FP64 coefficients, u_t when the grid has
+ * one, and `time` as given, with an FNV-1a checksum; written to path.tmp and renamed. */
+amdg_status amdg_grid_save(const amdg_grid* g, const char* path, double time);
+/* A new grid with the checkpoint's element set, coefficients and u_t; *time gets the stored time
+ * (may be null).  AMDG_ERR_FORMAT for a bad magic, version, header, size, key order or checksum. */
+amdg_status amdg_grid_load(amdg_context* ctx, const char* path, amdg_grid** out, double* time);
+/* Text dump of IO::output_element_level_support (IO.cpp:502-517): one line per element, in key
+ * order, "level xl xr " per dimension (xl, xr its support, printed as %g). */
+amdg_status amdg_grid_write_level_support(const amdg_grid* g, const char* path);
+/* The grid's dimension, finest level, Alpert degree and sparse flag (any pointer may be null). */
+amdg_status amdg_grid_config(const amdg_grid* g, int* dim, int* nmax, int* k, int* sparse);
+
 /* u_tt = div(K grad u) on the periodic unit cube, K = (1 + a prod_d sin(2 pi x_d))^2 (a = amplitude), Alpert
- * k = 2: K u_{x_d} and K u interpolated by degree-3 Lagrange (LagrInterpolation::
+ * k = 2: K u_{x_d} and K u interpolated by degree-4 Lagrange with the msh_case 2 nodes, as
+ * 03_wave_06_var_coeff_adapt.cpp:53-54 sets it (LagrInterpolation::
  * var_coeff_gradu_Lagr_fast / var_coeff_u_Lagr_fast, Interplation.cpp:4159-4212), the
  * DiffusionRHS terms rhs_flx_gradu, rhs_vol, rhs_flx_u (FastMultiplyLU.cpp:1691-1765) and the
  * IPDG penalty -sigma/dx [u][v], dx the finest element size
@@ -332,12 +348,16 @@ amdg_status amdg_wave_rhs(amdg_wave_op* op, const double* d_u, double* d_rhs, am
  * (RK4ODE2nd::step_stage, ODESolver.cpp:579-615). */
 amdg_status amdg_wave_rk4_steps(amdg_wave_op* op, double dt, int nsteps, amdg_precision prec);
 /* One adaptive step, the loop body of 03_wave_06_var_coeff_adapt.cpp:195-265 without source:
- * dt = cfl / sum_d wave_speed 2^maxlevel_d, EulerODE2nd predictor, refine on the predicted u,
- * one RK4ODE2nd step, coarsen on u. */
+ * dt = cfl / sum_d wave_speed 2^maxlevel_d; EulerODE2nd predictor as step_rk_source runs it (the
+ * predicted u_t takes the IPDG term of u alone, ODESolver.cpp:402-407); refine on the predicted
+ * ||u|| + ||u_t|| (DGAdapt::indicator_norm for prob "wave", DGAdapt.cpp:1018-1030); one RK4ODE2nd
+ * step; coarsen on ||u|| + ||u_t||. */
 amdg_status amdg_wave_adaptive_step(amdg_wave_op* op, double cfl, double wave_speed, double eps, double eta,
                                     amdg_precision prec, double* dt_out);
 /* As amdg_burgers_adaptive_step_ex / amdg_burgers_features / amdg_burgers_adaptive_step_learned for
- * the wave operator (the classifier reads |coefficients| of u; the step is RK4ODE2nd). */
+ * the wave operator: the step is RK4ODE2nd, the criterion ||u|| + ||u_t||, and the classifier reads
+ * the features of u followed by those of the grid's u_t, 2 (k+1)^dim (1 + 2 dim) floats per
+ * element. */
 amdg_status amdg_wave_adaptive_step_ex(amdg_wave_op* op, double cfl, double wave_speed, double eps, double eta,
                                        amdg_precision prec, double* dt_out, int8_t* decisions);
 amdg_status amdg_wave_features(amdg_wave_op* op, const double* d_u, float* d_features);

@@ -639,17 +639,53 @@ double amdg_oracle_l2_error_split(int dim, int N, int k, int64_t E, const int32_
 /* ======================================================================== */
 /* Lagrange interpolation path for nonlinear fluxes (config: 3D Burgers)     */
 /* ======================================================================== */
-/* Hierarchical Lagrange basis of degree 3, node layout msh_case 1
- * (LagrBasis.cpp:65-70): level-0 nodes {-3/5,-1/5,1/5,3/5} on [-1,1]; level-1
- * nodes {-4/5,-2/5} on the left half and {2/5,4/5} on the right half, each
- * interpolating on its half together with the two level-0 nodes of that half
- * (LagrBasis.cpp:300-330). */
-static const double LAGR_MSH0[4] = {-0.6, -0.2, 0.2, 0.6};
-static const double LAGR_MSH1[4] = {-0.8, -0.4, 0.4, 0.8};
+/* Hierarchical Lagrange bases (node layouts LagrBasis.cpp:33-155, mother
+ * functions LagrBasis.cpp:190-615), chosen by amdg_oracle_set_lagr_degree:
+ *  - degree 3, msh_case 1 (the Burgers examples): level-0 nodes {-3/5,-1/5,1/5,3/5}
+ *    on [-1,1]; level-1 nodes {-4/5,-2/5} on the left half and {2/5,4/5} on the
+ *    right half, each interpolating on its half together with the two level-0
+ *    nodes of that half;
+ *  - degree 4, msh_case 2 (03_wave_06_var_coeff_adapt.cpp:53-54): level-0 nodes
+ *    {-1,-1/2,0,1/2,1} whose points sit 1e-13 inside the element (left of the
+ *    node, except at -1); level-1 nodes {-3/4,-1/4} on the left half and
+ *    {0,1/4,3/4} on the right half (the one at 0 just right of it), each the
+ *    degree-4 polynomial on the nodes of its half at spacing 1/4. */
+typedef struct {
+    int p1;                /* points per element and dimension: degree + 1 */
+    double pt0[5], pt1[5]; /* interpolation points of level 0 / levels >= 1 on [-1, 1] */
+    double node0[5];       /* level-0 polynomial nodes */
+    double half[2][5];     /* level-1 polynomial nodes of the left / right half */
+    int side[5], node[5];  /* level-1 function p: its half and its node there */
+} lagr_spec;
+
+static const lagr_spec LAGR_DEG3 = {4,
+                                    {-0.6, -0.2, 0.2, 0.6},
+                                    {-0.8, -0.4, 0.4, 0.8},
+                                    {-0.6, -0.2, 0.2, 0.6},
+                                    {{-0.8, -0.6, -0.4, -0.2}, {0.2, 0.4, 0.6, 0.8}},
+                                    {0, 0, 1, 1},
+                                    {0, 2, 1, 3}};
+static const lagr_spec LAGR_DEG4 = {5,
+                                    {-1 + ROUND_OFF, -0.5 - ROUND_OFF, 0 - ROUND_OFF, 0.5 - ROUND_OFF, 1 - ROUND_OFF},
+                                    {-0.75 - ROUND_OFF, -0.25 - ROUND_OFF, 0 + ROUND_OFF, 0.25 - ROUND_OFF, 0.75 - ROUND_OFF},
+                                    {-1, -0.5, 0, 0.5, 1},
+                                    {{-1, -0.75, -0.5, -0.25, 0}, {0, 0.25, 0.5, 0.75, 1}},
+                                    {0, 0, 1, 1, 1},
+                                    {1, 3, 0, 1, 3}};
+static const lagr_spec* LS = &LAGR_DEG3;
+
+int amdg_oracle_set_lagr_degree(int degree) {
+    if (degree == 3) LS = &LAGR_DEG3;
+    else if (degree == 4) LS = &LAGR_DEG4;
+    else return -1;
+    return 0;
+}
+
+int amdg_oracle_lagr_points_per_dim(void) { return LS->p1; }
 
 static double lagr_poly(const double* nodes, int i, double x) {
     double v = 1.0;
-    for (int m = 0; m < 4; ++m)
+    for (int m = 0; m < LS->p1; ++m)
         if (m != i) v *= (x - nodes[m]) / (nodes[i] - nodes[m]);
     return v;
 }
@@ -657,15 +693,13 @@ static double lagr_poly(const double* nodes, int i, double x) {
 static double lagr_phi(double xt, int msh, int p) {
     const double x = 2.0 * xt - 1.0;
     if (x < -1.0 || x > 1.0) return 0.0;
-    if (msh == 0) return lagr_poly(LAGR_MSH0, p, x);
-    if (p <= 1) {
+    if (msh == 0) return lagr_poly(LS->node0, p, x);
+    if (LS->side[p] == 0) {
         if (x > 0) return 0.0;
-        const double nodes[4] = {-0.8, -0.6, -0.4, -0.2};
-        return lagr_poly(nodes, p == 0 ? 0 : 2, x);
+        return lagr_poly(LS->half[0], LS->node[p], x);
     }
     if (x < 0) return 0.0;
-    const double nodes[4] = {0.2, 0.4, 0.6, 0.8};
-    return lagr_poly(nodes, p == 2 ? 1 : 3, x);
+    return lagr_poly(LS->half[1], LS->node[p], x);
 }
 
 double amdg_oracle_lagr_val(int level, int suppt, int p, double x, int sgn) {
@@ -684,12 +718,12 @@ double amdg_oracle_lagr_val(int level, int suppt, int p, double x, int sgn) {
 
 /* interpolation point p of 1D element (n, j) (LagrBasis.cpp:18-27) */
 double amdg_oracle_lagr_point(int level, int suppt, int p) {
-    if (level == 0) return (LAGR_MSH0[p] + 1.0) / 2.0;
+    if (level == 0) return (LS->pt0[p] + 1.0) / 2.0;
     const double a = support_lo(level, suppt), b = support_hi(level, suppt);
-    return a + (b - a) * (LAGR_MSH1[p] + 1.0) / 2.0;
+    return a + (b - a) * (LS->pt1[p] + 1.0) / 2.0;
 }
 
-/* generic 1D basis evaluation: type 0 = Alpert (degree k), 1 = Lagrange degree 3 */
+/* generic 1D basis evaluation: type 0 = Alpert (degree k), 1 = Lagrange (the chosen degree) */
 static double basis_val(int type, int k, int n, int j, int p, int deriv, double x, int sgn) {
     if (type == 0) return amdg_oracle_alpert_val(k, n, j, p, deriv, x, sgn);
     return amdg_oracle_lagr_val(n, j, p, x, sgn);
@@ -732,14 +766,14 @@ static double gproduct_edge(int tu, int tv, int k, elem1d u, int pu, elem1d v, i
     return s;
 }
 
-/* Lagrange (rows, degree 3) x Alpert (cols, degree k) 1D matrices, each
- * (2^N*4) x (2^N*(k+1)): u_v, u_vx and (ulft_vjp + urgt_vjp). */
+/* Lagrange (rows) x Alpert (cols, degree k) 1D matrices, each
+ * (2^N*p1) x (2^N*(k+1)): u_v, u_vx and (ulft_vjp + urgt_vjp). */
 int amdg_oracle_oper1d_lagr(int N, int k, double* u_v, double* u_vx, double* uave2_vjp) {
-    const int nr = (1 << N) * 4, nc = (1 << N) * (k + 1);
+    const int nr = (1 << N) * LS->p1, nc = (1 << N) * (k + 1);
 #pragma omp parallel for schedule(dynamic)
     for (int r = 0; r < nr; ++r) {
-        const elem1d u = elem_of_order(r / 4);
-        const int pu = r % 4;
+        const elem1d u = elem_of_order(r / LS->p1);
+        const int pu = r % LS->p1;
         for (int c = 0; c < nc; ++c) {
             const elem1d v = elem_of_order(c / (k + 1));
             const int pv = c % (k + 1);
@@ -772,14 +806,14 @@ int amdg_oracle_lagr_point_values(int dim, int N, int k, int64_t E, const int32_
                                   const double* u, double* up) {
     ehash h;
     if (ehash_build(&h, dim, N, E, level, suppt)) return -2;
-    const int np = k + 1, B = ipow(np, dim), P = ipow(4, dim);
+    const int np = k + 1, B = ipow(np, dim), P = ipow(LS->p1, dim);
 #pragma omp parallel for schedule(dynamic, 8)
     for (int64_t e = 0; e < E; ++e) {
         for (int p = 0; p < P; ++p) {
             double x[16];
             int rem = p;
             int pd[16];
-            for (int d = dim - 1; d >= 0; --d) { pd[d] = rem % 4; rem /= 4; }
+            for (int d = dim - 1; d >= 0; --d) { pd[d] = rem % LS->p1; rem /= LS->p1; }
             for (int d = 0; d < dim; ++d) x[d] = amdg_oracle_lagr_point(level[e * dim + d], suppt[e * dim + d], pd[d]);
             double val = 0.0;
             int lv[16] = {0};
@@ -820,21 +854,21 @@ int amdg_oracle_lagr_point_values(int dim, int N, int k, int64_t E, const int32_
 /* Hierarchical surplus of point values, dimension by dimension
  * (LagrInterpolation::eval_fp_to_coe_D_Lag, Interplation.cpp:1222-1434, with
  * the weights of set_pts_wts_1d_ada_Lag, :775-888): in pass d every element
- * with level_d > 0 subtracts the degree-3 interpolant, through the four
- * coarser-level points inside its dimension-d support, of the values left by
- * pass d-1.  fp and out are E x 4^dim; fp may equal out. */
+ * with level_d > 0 subtracts the interpolant, through the p1 coarser-level
+ * points inside its dimension-d support, of the values left by pass d-1.  fp
+ * and out are E x p1^dim; fp may equal out. */
 int amdg_oracle_lagr_surplus(int dim, int N, int64_t E, const int32_t* level, const int32_t* suppt, const double* fp,
                              double* out) {
     ehash h;
     if (ehash_build(&h, dim, N, E, level, suppt)) return -2;
-    const int P = ipow(4, dim);
+    const int P = ipow(LS->p1, dim);
     double* cur = (double*)malloc((size_t)E * P * sizeof(double));
     double* nxt = (double*)malloc((size_t)E * P * sizeof(double));
     if (!cur || !nxt) return -2;
     memcpy(cur, fp, (size_t)E * P * sizeof(double));
     for (int d = 0; d < dim; ++d) {
         int stride = 1;
-        for (int s = d + 1; s < dim; ++s) stride *= 4;
+        for (int s = d + 1; s < dim; ++s) stride *= LS->p1;
 #pragma omp parallel for schedule(dynamic, 8)
         for (int64_t e = 0; e < E; ++e) {
             const int l = level[e * dim + d], j = suppt[e * dim + d];
@@ -842,17 +876,18 @@ int amdg_oracle_lagr_surplus(int dim, int N, int64_t E, const int32_t* level, co
                 memcpy(nxt + e * P, cur + e * P, P * sizeof(double));
                 continue;
             }
-            /* the four coarser points inside this element's dimension-d support */
+            /* the p1 coarser points inside this element's dimension-d support */
+            const int P1 = LS->p1;
             const double xl = support_lo(l, j), xr = support_hi(l, j);
-            int anc_o[4], anc_q[4];
-            double anc_x[4];
+            int anc_o[5], anc_q[5];
+            double anc_x[5];
             int ic = 0;
-            for (int o = 0; o < (1 << l) && ic < 4; ++o) {
+            for (int o = 0; o < (1 << l) && ic < P1; ++o) {
                 const elem1d ea = elem_of_order(o);
                 if (ea.n >= l) break;
-                for (int q = 0; q < 4; ++q) {
+                for (int q = 0; q < P1; ++q) {
                     const double pos = amdg_oracle_lagr_point(ea.n, ea.j, q);
-                    if (pos > xl && pos < xr && ic < 4) {
+                    if (pos > xl && pos < xr && ic < P1) {
                         anc_o[ic] = o;
                         anc_q[ic] = q;
                         anc_x[ic] = pos;
@@ -862,25 +897,27 @@ int amdg_oracle_lagr_surplus(int dim, int N, int64_t E, const int32_t* level, co
             }
             /* weight: minus the level-0 Lagrange basis of the ancestor's rank among the
              * sorted ancestor positions, at this element's own node */
-            int rank[4];
-            for (int a = 0; a < 4; ++a) {
+            int rank[5];
+            for (int a = 0; a < P1; ++a) {
                 rank[a] = 0;
-                for (int b = 0; b < 4; ++b) if (anc_x[b] < anc_x[a]) ++rank[a];
+                for (int b = 0; b < P1; ++b) if (anc_x[b] < anc_x[a]) ++rank[a];
             }
-            int64_t anc_e[4];
-            for (int a = 0; a < 4; ++a) {
+            int64_t anc_e[5];
+            int missing = ic != P1;
+            for (int a = 0; a < P1 && !missing; ++a) {
                 int o[16];
                 for (int s = 0; s < dim; ++s) o[s] = order_of_elem(level[e * dim + s], suppt[e * dim + s]);
                 o[d] = anc_o[a];
                 anc_e[a] = ehash_find(&h, pack_key(o, dim, N));
+                missing |= anc_e[a] < 0;
             }
-            if (ic != 4 || anc_e[0] < 0 || anc_e[1] < 0 || anc_e[2] < 0 || anc_e[3] < 0) continue; /* hole: checked below */
+            if (missing) continue; /* hole: checked below */
             for (int p = 0; p < P; ++p) {
-                const int pd = (p / stride) % 4;
+                const int pd = (p / stride) % P1;
                 const int base = p - pd * stride;
                 double c = cur[e * P + p];
-                const double xt = (LAGR_MSH1[pd] + 1.0) / 2.0;
-                for (int a = 0; a < 4; ++a) {
+                const double xt = (LS->pt1[pd] + 1.0) / 2.0;
+                for (int a = 0; a < P1; ++a) {
                     const double wt = -lagr_phi(xt, 0, rank[a]);
                     c += wt * cur[anc_e[a] * P + base + anc_q[a] * stride];
                 }
@@ -895,7 +932,7 @@ int amdg_oracle_lagr_surplus(int dim, int N, int64_t E, const int32_t* level, co
     return 0;
 }
 
-/* contract a 4^dim block with per-dimension 1D matrices M_s (rows: 4 source
+/* contract a p1^dim block with per-dimension 1D matrices M_s (rows: p1 source
  * Lagrange indices of the source element, cols: np target Alpert indices)
  * into a np^dim block, accumulating scale * result into y */
 static void contract_block(int dim, int np, const double* x, const double* const* M, int nc, const int* row0,
@@ -903,10 +940,11 @@ static void contract_block(int dim, int np, const double* x, const double* const
     double bufA[4096], bufB[4096];
     const double* src = x;
     int shape[16];
-    for (int s = 0; s < dim; ++s) shape[s] = 4;
+    const int P1 = LS->p1;
+    for (int s = 0; s < dim; ++s) shape[s] = P1;
     double* dst = bufA;
     for (int s = 0; s < dim; ++s) {
-        /* contract dimension s: size 4 -> np */
+        /* contract dimension s: size p1 -> np */
         int outer = 1, inner = 1;
         for (int r = 0; r < s; ++r) outer *= shape[r];
         for (int r = s + 1; r < dim; ++r) inner *= shape[r];
@@ -914,8 +952,8 @@ static void contract_block(int dim, int np, const double* x, const double* const
             for (int q = 0; q < np; ++q)
                 for (int b = 0; b < inner; ++b) {
                     double acc = 0.0;
-                    for (int p = 0; p < 4; ++p)
-                        acc += src[(a * 4 + p) * inner + b] * M[s][(size_t)(row0[s] + p) * nc + col0[s] + q];
+                    for (int p = 0; p < P1; ++p)
+                        acc += src[(a * P1 + p) * inner + b] * M[s][(size_t)(row0[s] + p) * nc + col0[s] + q];
                     dst[(a * np + q) * inner + b] = acc;
                 }
         shape[s] = np;
@@ -931,11 +969,11 @@ static void contract_block(int dim, int np, const double* x, const double* const
  *   volume   sum_d  <F_d, (u_vx in d, u_v elsewhere)>            (HyperbolicLagrRHS::rhs_vol_scalar)
  *   interface 0.5 sum_d <F_d, ((ulft+urgt)_vjp in d, u_v elsewhere)> (rhs_flx_intp_scalar)
  *   penalty  -alpha/2 sum_d ujp_vjp(Alpert) in d                   (HyperbolicAlptRHS::rhs_flx_penalty_scalar)
- * fucoe: dim x E x 4^dim interpolation coefficients of the flux per dimension. */
+ * fucoe: dim x E x p1^dim interpolation coefficients of the flux per dimension. */
 int amdg_oracle_burgers_rhs(int dim, int N, int k, int64_t E, const int32_t* level, const int32_t* suppt,
                             const double* fucoe, const double* u, double alpha, double* rhs) {
-    const int np = k + 1, B = ipow(np, dim), P = ipow(4, dim), n1 = 1 << N;
-    const int nr = n1 * 4, nc = n1 * np;
+    const int np = k + 1, B = ipow(np, dim), P = ipow(LS->p1, dim), n1 = 1 << N;
+    const int nr = n1 * LS->p1, nc = n1 * np;
     const long one = 1L << N;
     double* Lv = (double*)malloc((size_t)nr * nc * sizeof(double));
     double* Lvx = (double*)malloc((size_t)nr * nc * sizeof(double));
@@ -981,7 +1019,7 @@ int amdg_oracle_burgers_rhs(int dim, int N, int k, int64_t E, const int32_t* lev
                     for (int s = 0; s < dim; ++s) {
                         const int use_flx = (term == 1 && s == d);
                         oc[s] = use_flx ? flx[o[s] * n1 + idx[s]] : vol[o[s] * n1 + idx[s]];
-                        row0[s] = oc[s] * 4;
+                        row0[s] = oc[s] * LS->p1;
                         col0[s] = o[s] * np;
                     }
                     const int64_t es = ehash_find(&h, pack_key(oc, dim, N));
@@ -1157,11 +1195,11 @@ static int fast_partial_sums(const fast_ctx* c, const double* in, int n_in, int 
 static double* alpt_at_lagr_points_d(int N, int k, int deriv);
 static double* alpt_at_lagr_points(int N, int k) { return alpt_at_lagr_points_d(N, k, 0); }
 static double* alpt_at_lagr_points_d(int N, int k, int deriv) {
-    const int np = k + 1, n1 = 1 << N, na = n1 * np, nl = n1 * 4;
+    const int np = k + 1, n1 = 1 << N, na = n1 * np, nl = n1 * LS->p1;
     double* m = (double*)calloc((size_t)na * nl, sizeof(double));
     for (int c = 0; c < nl; ++c) {
-        const elem1d el = elem_of_order(c / 4);
-        const double x = amdg_oracle_lagr_point(el.n, el.j, c % 4);
+        const elem1d el = elem_of_order(c / LS->p1);
+        const double x = amdg_oracle_lagr_point(el.n, el.j, c % LS->p1);
         for (int r = 0; r < na; ++r) {
             const elem1d ea = elem_of_order(r / np);
             if (x < support_lo(ea.n, ea.j) || x > support_hi(ea.n, ea.j)) continue;
@@ -1179,8 +1217,8 @@ int amdg_oracle_lagr_point_values_fast(int dim, int N, int k, int64_t E, const i
     const double* M[16];
     int flx[16];
     for (int d = 0; d < dim; ++d) { M[d] = a2p; flx[d] = 0; }
-    memset(up, 0, (size_t)E * ipow(4, dim) * sizeof(double));
-    int rc = fast_partial_sums(&c, u, k + 1, 4, M, flx, 1.0, up);
+    memset(up, 0, (size_t)E * ipow(LS->p1, dim) * sizeof(double));
+    int rc = fast_partial_sums(&c, u, k + 1, LS->p1, M, flx, 1.0, up);
     free(a2p);
     fast_ctx_free(&c);
     return rc;
@@ -1190,8 +1228,8 @@ int amdg_oracle_lagr_point_values_fast(int dim, int N, int k, int64_t E, const i
  * rhs_flx_intp_scalar, HyperbolicAlptRHS::rhs_flx_penalty_scalar) */
 int amdg_oracle_burgers_rhs_fast(int dim, int N, int k, int64_t E, const int32_t* level, const int32_t* suppt,
                                  const double* fucoe, const double* u, double alpha, double* rhs) {
-    const int np = k + 1, n1 = 1 << N, nr = n1 * 4, nc = n1 * np;
-    const int B = ipow(np, dim), P = ipow(4, dim);
+    const int np = k + 1, n1 = 1 << N, nr = n1 * LS->p1, nc = n1 * np;
+    const int B = ipow(np, dim), P = ipow(LS->p1, dim);
     fast_ctx c;
     if (fast_ctx_init(&c, dim, N, E, level, suppt)) return -2;
     double* Lv = (double*)malloc((size_t)nr * nc * sizeof(double));
@@ -1213,7 +1251,7 @@ int amdg_oracle_burgers_rhs_fast(int dim, int N, int k, int64_t E, const int32_t
                 M[s] = (s == d) ? (term == 0 ? Lvx : Lf) : Lv;
                 flx[s] = (term == 1 && s == d);
             }
-            rc = fast_partial_sums(&c, fucoe + (size_t)d * E * P, 4, np, M, flx, term == 0 ? 1.0 : 0.5, rhs);
+            rc = fast_partial_sums(&c, fucoe + (size_t)d * E * P, LS->p1, np, M, flx, term == 0 ? 1.0 : 0.5, rhs);
         }
         int from[16];
         for (int s = 0; s < dim; ++s) from[s] = np;
@@ -1384,11 +1422,11 @@ static double gproduct_edge_dis_u(int tu, int tv, int k, elem1d u, int pu, elem1
 /* Lagrange (rows) x Alpert (cols): ujp_vxlft + ujp_vxrgt, [u] times the one-sided v_x
  * (OperatorMatrix1D.h:206-211) */
 int amdg_oracle_oper1d_lagr_ujp_vx(int N, int k, double* ujp_vxave) {
-    const int nr = (1 << N) * 4, nc = (1 << N) * (k + 1);
+    const int nr = (1 << N) * LS->p1, nc = (1 << N) * (k + 1);
 #pragma omp parallel for schedule(dynamic)
     for (int r = 0; r < nr; ++r) {
-        const elem1d u = elem_of_order(r / 4);
-        const int pu = r % 4;
+        const elem1d u = elem_of_order(r / LS->p1);
+        const int pu = r % LS->p1;
         for (int c = 0; c < nc; ++c) {
             const elem1d v = elem_of_order(c / (k + 1));
             const int pv = c % (k + 1);
@@ -1414,15 +1452,15 @@ double amdg_oracle_wave_coef(int dim, const double* x, double amp) {
 /* K at every interpolation point times the given point values, then the surplus */
 static int wave_coef_surplus(int dim, int N, int64_t E, const int32_t* level, const int32_t* suppt, double amp, double* up,
                              double* fucoe) {
-    const int P = ipow(4, dim);
+    const int P = ipow(LS->p1, dim);
 #pragma omp parallel for schedule(static)
     for (int64_t e = 0; e < E; ++e)
         for (int p = 0; p < P; ++p) {
             double x[16];
             int r = p;
             for (int d = dim - 1; d >= 0; --d) {
-                x[d] = amdg_oracle_lagr_point(level[e * dim + d], suppt[e * dim + d], r % 4);
-                r /= 4;
+                x[d] = amdg_oracle_lagr_point(level[e * dim + d], suppt[e * dim + d], r % LS->p1);
+                r /= LS->p1;
             }
             up[e * P + p] = amdg_oracle_wave_coef(dim, x, amp) * up[e * P + p];
         }
@@ -1431,8 +1469,8 @@ static int wave_coef_surplus(int dim, int N, int64_t E, const int32_t* level, co
 
 int amdg_oracle_wave_rhs_fast(int dim, int N, int k, int64_t E, const int32_t* level, const int32_t* suppt,
                               const double* u, double sigma, double amp, double* rhs) {
-    const int np = k + 1, n1 = 1 << N, nr = n1 * 4, nc = n1 * np;
-    const int B = ipow(np, dim), P = ipow(4, dim);
+    const int np = k + 1, n1 = 1 << N, nr = n1 * LS->p1, nc = n1 * np;
+    const int B = ipow(np, dim), P = ipow(LS->p1, dim);
     fast_ctx c;
     if (fast_ctx_init(&c, dim, N, E, level, suppt)) return -2;
     double* a2p = alpt_at_lagr_points_d(N, k, 0);
@@ -1458,31 +1496,31 @@ int amdg_oracle_wave_rhs_fast(int dim, int N, int k, int64_t E, const int32_t* l
     for (int d = 0; d < dim && !rc; ++d) {
         for (int s = 0; s < dim; ++s) { M[s] = (s == d) ? a2pd : a2p; flx[s] = 0; }
         memset(up, 0, (size_t)E * P * sizeof(double));
-        rc = fast_partial_sums(&c, u, np, 4, M, flx, 1.0, up);
+        rc = fast_partial_sums(&c, u, np, LS->p1, M, flx, 1.0, up);
         if (!rc) rc = wave_coef_surplus(dim, N, E, level, suppt, amp, up, fg + (size_t)d * E * P);
     }
     /* K u at the points */
     if (!rc) {
         for (int s = 0; s < dim; ++s) { M[s] = a2p; flx[s] = 0; }
         memset(up, 0, (size_t)E * P * sizeof(double));
-        rc = fast_partial_sums(&c, u, np, 4, M, flx, 1.0, up);
+        rc = fast_partial_sums(&c, u, np, LS->p1, M, flx, 1.0, up);
         if (!rc) rc = wave_coef_surplus(dim, N, E, level, suppt, amp, up, fu);
     }
     memset(rhs, 0, (size_t)E * B * sizeof(double));
     /* rhs_flx_gradu: -{K u_x}[v] (uave_vjp = (ulft + urgt)_vjp / 2) */
     for (int d = 0; d < dim && !rc; ++d) {
         for (int s = 0; s < dim; ++s) { M[s] = (s == d) ? Lf : Lv; flx[s] = (s == d); }
-        rc = fast_partial_sums(&c, fg + (size_t)d * E * P, 4, np, M, flx, -0.5, rhs);
+        rc = fast_partial_sums(&c, fg + (size_t)d * E * P, LS->p1, np, M, flx, -0.5, rhs);
     }
     /* rhs_vol: -K u_x v_x */
     for (int d = 0; d < dim && !rc; ++d) {
         for (int s = 0; s < dim; ++s) { M[s] = (s == d) ? Lvx : Lv; flx[s] = 0; }
-        rc = fast_partial_sums(&c, fg + (size_t)d * E * P, 4, np, M, flx, -1.0, rhs);
+        rc = fast_partial_sums(&c, fg + (size_t)d * E * P, LS->p1, np, M, flx, -1.0, rhs);
     }
     /* rhs_flx_u: -1/2 [K u] (v_x^- + v_x^+) */
     for (int d = 0; d < dim && !rc; ++d) {
         for (int s = 0; s < dim; ++s) { M[s] = (s == d) ? Lj : Lv; flx[s] = (s == d); }
-        rc = fast_partial_sums(&c, fu, 4, np, M, flx, -0.5, rhs);
+        rc = fast_partial_sums(&c, fu, LS->p1, np, M, flx, -0.5, rhs);
     }
     /* IPDG: -sigma/dx [u][v], dx the finest element size */
     int maxl = 0;
@@ -1496,4 +1534,31 @@ int amdg_oracle_wave_rhs_fast(int dim, int N, int k, int64_t E, const int32_t* l
     free(a2p); free(a2pd); free(Lv); free(Lvx); free(Lf); free(Lj); free(ul); free(ur); free(up); free(fg); free(fu);
     fast_ctx_free(&c);
     return rc;
+}
+
+/* The IPDG term alone, rhs = -sigma/dx sum_d [u][v]: what EulerODE2nd::step_rk_source uses as
+ * the predictor's right-hand side (it recomputes rhs as the operator matrix times u,
+ * ODESolver.cpp:402-407, BilinearForm.h:23). */
+int amdg_oracle_wave_penalty(int dim, int N, int k, int64_t E, const int32_t* level, const int32_t* suppt,
+                             const double* u, double sigma, double* rhs) {
+    const int np = k + 1, nc = (1 << N) * np, B = ipow(np, dim);
+    fast_ctx c;
+    if (fast_ctx_init(&c, dim, N, E, level, suppt)) return -2;
+    double* ul = (double*)malloc((size_t)nc * nc * sizeof(double));
+    double* ur = (double*)malloc((size_t)nc * nc * sizeof(double));
+    if (!ul || !ur) return -2;
+    amdg_oracle_oper1d(N, k, NULL, NULL, ul, ur);
+    for (size_t i = 0; i < (size_t)nc * nc; ++i) ur[i] = ur[i] - ul[i]; /* ujp_vjp */
+    int maxl = 0;
+    for (int64_t i = 0; i < E * dim; ++i) maxl = level[i] > maxl ? level[i] : maxl;
+    const double dx = 1.0 / pow(2.0, maxl);
+    memset(rhs, 0, (size_t)E * B * sizeof(double));
+    for (int d = 0; d < dim; ++d) {
+        int from[16];
+        for (int s = 0; s < dim; ++s) from[s] = np;
+        fast_transform_1d(&c, u, from, rhs, from, d, ur, nc, 1, 1, -sigma / dx, 1);
+    }
+    free(ul); free(ur);
+    fast_ctx_free(&c);
+    return 0;
 }

@@ -72,6 +72,10 @@ double amdg_oracle_l2_error_split(int dim, int N, int k, int64_t E, const int32_
                                   const double* u, const double* coef1d_exact, double l2_norm_exact);
 
 /* ---- Lagrange interpolation path (degree-3 hierarchical Lagrange, msh_case 1) ---- */
+/* Lagrange interpolation degree of the calls that follow: 3 (node layout msh_case 1,
+ * the default) or 4 (msh_case 2); -1 for anything else */
+int amdg_oracle_set_lagr_degree(int degree);
+int amdg_oracle_lagr_points_per_dim(void);
 double amdg_oracle_lagr_val(int level, int suppt, int p, double x, int sgn);
 double amdg_oracle_lagr_point(int level, int suppt, int p);
 /* Lagrange (rows) x Alpert (cols) 1D matrices: u_v, u_vx, ulft_vjp + urgt_vjp. */
@@ -117,6 +121,9 @@ double amdg_oracle_wave_coef(int dim, const double* x, double amp);
 /* right-hand side of the semi-discrete wave equation (fast transforms), rhs = E x (k+1)^dim */
 int amdg_oracle_wave_rhs_fast(int dim, int N, int k, int64_t E, const int32_t* level, const int32_t* suppt,
                               const double* u, double sigma, double amp, double* rhs);
+/* the IPDG term alone (the adaptive wave loop's predictor right-hand side) */
+int amdg_oracle_wave_penalty(int dim, int N, int k, int64_t E, const int32_t* level, const int32_t* suppt,
+                             const double* u, double sigma, double* rhs);
 
 #ifdef __cplusplus
 }

@@ -55,6 +55,7 @@ def lib():
         L.amdg_oracle_linop_destroy.argtypes = [C.c_void_p]
         L.amdg_oracle_l2_error_split.restype = C.c_double
         L.amdg_oracle_l2_error_split.argtypes = [C.c_int, C.c_int, C.c_int, C.c_int64, i32p, i32p, f64p, f64p, C.c_double]
+        L.amdg_oracle_set_lagr_degree.argtypes = [C.c_int]
         L.amdg_oracle_lagr_val.restype = C.c_double
         L.amdg_oracle_lagr_val.argtypes = [C.c_int, C.c_int, C.c_int, C.c_double, C.c_int]
         L.amdg_oracle_lagr_point.restype = C.c_double
@@ -77,6 +78,7 @@ def lib():
                                                 C.c_double, C.c_double, C.c_double, C.c_double, f64p]
         L.amdg_oracle_wave_rhs_fast.argtypes = [C.c_int, C.c_int, C.c_int, C.c_int64, i32p, i32p, f64p, C.c_double,
                                                 C.c_double, f64p]
+        L.amdg_oracle_wave_penalty.argtypes = [C.c_int, C.c_int, C.c_int, C.c_int64, i32p, i32p, f64p, C.c_double, f64p]
         L.amdg_oracle_wave_coef.restype = C.c_double
         L.amdg_oracle_wave_coef.argtypes = [C.c_int, f64p, C.c_double]
         _lib = L
@@ -214,14 +216,37 @@ def error_burgers(dim, N, k, level, suppt, u, gauss, a=0.5, b=0.25, c=0.0, t=0.0
     return out
 
 
+def lagr_degree(degree):
+    """Select the Lagrange interpolation degree of the oracle calls that follow: 3 (node
+    layout msh_case 1, the Burgers examples) or 4 (msh_case 2, the wave example)."""
+    _check(lib().amdg_oracle_set_lagr_degree(degree))
+
+
+# Lagrange degree of each problem, as its example program sets it
+BURGERS_LAGR_DEGREE = 3
+WAVE_LAGR_DEGREE = 4
+
+
 def wave_rhs(dim, N, k, level, suppt, u, sigma, amp=0.5):
     """Right-hand side of u_tt = div(K grad u), K = (1 + amp prod sin(2 pi x_d))^2, with the IPDG
-    penalty -sigma/dx [u][v] (fast transforms, the reference's operator on adaptive grids)."""
+    penalty -sigma/dx [u][v] (fast transforms, the reference's operator on adaptive grids;
+    degree-4 Lagrange interpolation, node layout msh_case 2)."""
+    lagr_degree(WAVE_LAGR_DEGREE)
     B = (k + 1) ** dim
     rhs = np.zeros((len(level), B))
     _check(lib().amdg_oracle_wave_rhs_fast(dim, N, k, len(level), np.ascontiguousarray(level, np.int32),
                                            np.ascontiguousarray(suppt, np.int32),
                                            np.ascontiguousarray(u, np.float64).reshape(-1), sigma, amp, rhs))
+    return rhs
+
+
+def wave_penalty(dim, N, k, level, suppt, u, sigma):
+    """The IPDG term alone, -sigma/dx [u][v]: the adaptive loop's predictor right-hand side
+    (EulerODE2nd::step_rk_source recomputes rhs as the operator matrix times u)."""
+    rhs = np.zeros((len(level), (k + 1) ** dim))
+    _check(lib().amdg_oracle_wave_penalty(dim, N, k, len(level), np.ascontiguousarray(level, np.int32),
+                                          np.ascontiguousarray(suppt, np.int32),
+                                          np.ascontiguousarray(u, np.float64).reshape(-1), sigma, rhs))
     return rhs
 
 
@@ -269,20 +294,23 @@ def sin_sum_terms(dim, shift=0.0):
     return terms
 
 
-def lagr_point_values(dim, N, k, level, suppt, u):
-    up = np.zeros((level.shape[0], 4 ** dim))
+def lagr_point_values(dim, N, k, level, suppt, u, degree=BURGERS_LAGR_DEGREE):
+    lagr_degree(degree)
+    up = np.zeros((level.shape[0], (degree + 1) ** dim))
     _check(lib().amdg_oracle_lagr_point_values(dim, N, k, level.shape[0], level, suppt, np.ascontiguousarray(u), up))
     return up
 
 
-def lagr_surplus(dim, N, level, suppt, fp):
+def lagr_surplus(dim, N, level, suppt, fp, degree=BURGERS_LAGR_DEGREE):
+    lagr_degree(degree)
     out = np.zeros_like(fp)
     _check(lib().amdg_oracle_lagr_surplus(dim, N, level.shape[0], level, suppt, np.ascontiguousarray(fp), out))
     return out
 
 
-def lagr_point_values_fast(dim, N, k, level, suppt, u):
-    up = np.zeros((level.shape[0], 4 ** dim))
+def lagr_point_values_fast(dim, N, k, level, suppt, u, degree=BURGERS_LAGR_DEGREE):
+    lagr_degree(degree)
+    up = np.zeros((level.shape[0], (degree + 1) ** dim))
     _check(lib().amdg_oracle_lagr_point_values_fast(dim, N, k, level.shape[0], level, suppt, np.ascontiguousarray(u),
                                                     up))
     return up
@@ -490,24 +518,28 @@ def burgers_adaptive_run(dim, n_init, nmax, eps, eta, alpha, cfl, umax, steps, k
     return history
 
 
-def wave_adaptive_run(dim, n_init, nmax, eps, eta, sigma, cfl, speed, steps, k=2, amp=0.5):
+def wave_adaptive_run(dim, n_init, nmax, eps, eta, sigma, cfl, speed, steps, k=2, amp=0.5, centre=(0.3, 0.4, 0.5),
+                      width=200.0):
     """The adaptive wave loop of 03_wave_06_var_coeff_adapt.cpp without source: EulerODE2nd
-    predictor, refine on the predicted u, RK4ODE2nd step, coarsen on u; u0 the Gaussian bump,
-    v0 = 0."""
-    keys, u = init_adaptive_separable(dim, n_init, nmax, k, wave_ic_terms(dim), eps)
+    predictor (u + dt v, v + dt (IPDG u): step_rk_source replaces the assembled right-hand side
+    by the operator matrix times u), refine on the predicted ||u|| + ||u_t|| (the indicator of
+    prob "wave", DGAdapt.cpp:1018-1030), RK4ODE2nd step, coarsen on ||u|| + ||u_t||; u0 the
+    Gaussian bump, v0 = 0."""
+    keys, u = init_adaptive_separable(dim, n_init, nmax, k, wave_ic_terms(dim, centre, width), eps)
     v = np.zeros_like(u)
     history = [(list(keys), u.copy(), v.copy(), None)]
     for _ in range(steps):
         lv, sp = keys_to_arrays(keys, dim)
         maxlev = lv.max(axis=0)
         dt = cfl / sum(speed * 2.0 ** int(m) for m in maxlev)
-        pred = u + dt * v
-        new_keys = refine_keys(keys, element_norms(pred), eps, nmax)
+        pred_u = u + dt * v
+        pred_v = v + dt * wave_penalty(dim, nmax, k, lv, sp, u, sigma)
+        new_keys = refine_keys(keys, element_norms(pred_u) + element_norms(pred_v), eps, nmax)
         u, v = remap(keys, u, new_keys), remap(keys, v, new_keys)
         keys = new_keys
         lv, sp = keys_to_arrays(keys, dim)
         u, v = wave_rk4(dim, nmax, k, lv, sp, u, v, sigma, dt, 1, amp)
-        new_keys = coarsen_keys(keys, element_norms(u), eta)
+        new_keys = coarsen_keys(keys, element_norms(u) + element_norms(v), eta)
         u, v = remap(keys, u, new_keys), remap(keys, v, new_keys)
         keys = new_keys
         history.append((list(keys), u.copy(), v.copy(), dt))

@@ -34,8 +34,11 @@
 //   ref_harness wave <dim> <N> <sigma> <steps> <dt> [a]
 //     u_tt = div(K grad u), K = (1 + a prod_d sin(2 pi x_d))^2 (a = 0.5 by default), u0 = Gaussian
 //     bump, u_t(0) = 0:
-//     DiffusionRHS with Lagrange-interpolated K grad u and K u, IPDG penalty, RK4ODE2nd
-//     (03_wave_06_var_coeff_adapt.cpp:154-279). Dumps u0, rhs0, uT, vT.
+//     DiffusionRHS with Lagrange-interpolated (degree 4, msh_case 2) K grad u and K u, IPDG
+//     penalty, RK4ODE2nd (03_wave_06_var_coeff_adapt.cpp:154-279). Dumps u0, rhs0, uT, vT.
+//   ref_harness wave_adapt <dim> <N_init> <NMAX> <eps> <eta> <sigma> <cfl> <steps> [a]
+//     the adaptive loop of 03_wave_06_var_coeff_adapt.cpp:181-297 for the same problem (no
+//     source); dumps u and u_t after the adaptive initialisation and after every step.
 //   ref_harness matrices <N> <k>
 //     dumps the 1D operator matrices u_v, u_vx, ulft_vjp, urgt_vjp.
 //
@@ -67,10 +70,10 @@
 
 namespace {
 
-void set_statics(int dim, int k) {
+void set_statics(int dim, int k, int lagr_degree = 3) {
     AlptBasis::PMAX = k;
-    LagrBasis::PMAX = 3;
-    LagrBasis::msh_case = 1;
+    LagrBasis::PMAX = lagr_degree;
+    LagrBasis::msh_case = lagr_degree == 4 ? 2 : 1;
     HermBasis::PMAX = 3;
     HermBasis::msh_case = 1;
     Element::PMAX_alpt = AlptBasis::PMAX;
@@ -449,7 +452,7 @@ int run_burgers_adapt(int argc, char** argv) {
 }
 
 // Wave equation u_tt = div(K grad u), K = (1 + a prod_d sin(2 pi x_d))^2, periodic, Alpert k = 2,
-// Lagrange degree 3 (msh_case 1) interpolation of K u_x and K u, DiffusionRHS terms and the IPDG
+// Lagrange degree 4 (msh_case 2, as the example sets it) interpolation of K u_x and K u, DiffusionRHS terms and the IPDG
 // penalty as 03_wave_06_var_coeff_adapt.cpp:154-279 (no source, no adaptivity): u0 a Gaussian bump,
 // u_t = 0. Dumps u0, rhs0 (the right-hand side at u0, read through EulerODE2nd with dt = 1 on a
 // second solution) and uT, vT after `steps` RK4ODE2nd steps.
@@ -462,7 +465,7 @@ int run_wave(int argc, char** argv) {
     const double dt = std::atof(argv[6]);
     const double amp = argc > 7 ? std::atof(argv[7]) : 0.5;
     const int k = 2;
-    set_statics(dim, k);
+    set_statics(dim, k, 4);
     DGSolution::prob = "wave";
     Hash hash;
     LagrBasis::set_interp_msh01();
@@ -547,6 +550,106 @@ int run_wave(int argc, char** argv) {
     return 0;
 }
 
+// The adaptive wave loop of 03_wave_06_var_coeff_adapt.cpp:181-297 (no source): dt from the
+// finest level, EulerODE2nd predictor on copies of (u, u_t) through step_rk (the source-free
+// step_rk_source: rhs recomputed as the IPDG matrix times u), refine, copy the predictions
+// back, four RK4ODE2nd stages with the interpolated DiffusionRHS terms plus the IPDG matrix,
+// coarsen. u0 the Gaussian bump, u_t(0) = 0, adaptive initialisation. Dumps u and u_t after
+// the initialisation and after every step.
+int run_wave_adapt(int argc, char** argv) {
+    if (argc < 10) { std::fprintf(stderr, "wave_adapt: bad args\n"); return 2; }
+    const int dim = std::atoi(argv[2]);
+    const int N_init = std::atoi(argv[3]);
+    const int NMAX = std::atoi(argv[4]);
+    const double eps = std::atof(argv[5]);
+    const double eta = std::atof(argv[6]);
+    const double sigma = std::atof(argv[7]);
+    const double cfl = std::atof(argv[8]);
+    const int steps = std::atoi(argv[9]);
+    const double amp = argc > 10 ? std::atof(argv[10]) : 0.5;
+    const int k = 2;
+    set_statics(dim, k, 4);
+    DGSolution::prob = "wave";
+    Hash hash;
+    LagrBasis::set_interp_msh01();
+    HermBasis::set_interp_msh01();
+    AllBasis<AlptBasis> all_bas_alpt(NMAX);
+    AllBasis<LagrBasis> all_bas_lagr(NMAX);
+    AllBasis<HermBasis> all_bas_herm(NMAX);
+    OperatorMatrix1D<AlptBasis, AlptBasis> oper_alpt(all_bas_alpt, all_bas_alpt, "period");
+    OperatorMatrix1D<LagrBasis, AlptBasis> oper_lagr(all_bas_lagr, all_bas_alpt, "period");
+    DGAdapt dg(true, N_init, NMAX, all_bas_alpt, all_bas_lagr, all_bas_herm, hash, eps, eta, true, false);
+    const double centre[3] = {0.3, 0.4, 0.5};
+    auto zero = [](double, int) { return 0.0; };
+    auto bump = [&](double x, int d) { return std::exp(-200.0 * (x - centre[d]) * (x - centre[d])); };
+    const double PI = Const::PI;
+    auto coe = [=](std::vector<double> x, int) -> double {
+        double s = 1.0;
+        for (int d = 0; d < dim; ++d) s *= std::sin(2 * PI * x[d]);
+        const double c = 1.0 + amp * s;
+        return c * c;
+    };
+    std::vector<std::vector<bool>> is_intp(1, std::vector<bool>(dim, true));
+    std::vector<std::vector<bool>> is_intp_d0(1, std::vector<bool>(dim, false));
+    is_intp_d0[0][0] = true;
+    dg.init_separable_scalar(zero);
+    dg.copy_ucoe_to_ucoe_ut();
+    dg.init_separable_scalar(bump);
+    std::printf("META dim=%d N=%d k=%d sparse=1 elements=%zu dof=%d\n", dim, NMAX, k, dg.dg.size(), dg.get_dof());
+    dump_elements("u_init", dg, 0);
+    dump_elements("ut_init", dg, 2);
+    DiffusionRHS diffuse(dg, oper_lagr);
+    double t = 0.0;
+    for (int step = 0; step < steps; ++step) {
+        const std::vector<int> max_mesh = dg.max_mesh_level_vec();
+        double sum_c_dx = 0.;
+        for (int d = 0; d < dim; ++d) sum_c_dx += 1.0 * std::pow(2., max_mesh[d]);
+        const double dt = cfl / sum_c_dx;
+        dg.copy_ucoe_to_predict();
+        dg.copy_ucoe_ut_to_predict();
+        {
+            DiffusionAlpt ipdg(dg, oper_alpt, sigma);
+            ipdg.assemble_matrix_flx_ujp_vjp();
+            EulerODE2nd ode(ipdg, dt);
+            ode.init();
+            ode.step_rk();
+            ode.final();
+        }
+        dg.refine();
+        dg.copy_predict_to_ucoe();
+        dg.copy_predict_to_ucoe_ut();
+        {
+            DiffusionAlpt ipdg(dg, oper_alpt, sigma);
+            ipdg.assemble_matrix_flx_ujp_vjp();
+            RK4ODE2nd ode(ipdg, dt);
+            ode.init();
+            LagrInterpolation interp(dg);
+            FastLagrIntp fast(dg, interp.Lag_pt_Alpt_1D, interp.Lag_pt_Alpt_1D_d1);
+            for (int stage = 0; stage < 4; ++stage) {
+                dg.set_rhs_zero();
+                interp.var_coeff_gradu_Lagr_fast(coe, is_intp, fast);
+                diffuse.rhs_flx_gradu();
+                diffuse.rhs_vol();
+                interp.var_coeff_u_Lagr_fast(coe, is_intp_d0, fast);
+                diffuse.rhs_flx_u();
+                ode.rhs_to_eigenvec();
+                ode.add_rhs_matrix(ipdg);
+                ode.step_stage(stage);
+                ode.final();
+            }
+        }
+        dg.coarsen();
+        t += dt;
+        std::printf("STEP %d dt=%.17g elements=%zu\n", step, dt, dg.dg.size());
+        char nm[32];
+        std::snprintf(nm, sizeof nm, "u_step%d", step);
+        dump_elements(nm, dg, 0);
+        std::snprintf(nm, sizeof nm, "ut_step%d", step);
+        dump_elements(nm, dg, 2);
+    }
+    return 0;
+}
+
 int run_matrices(int argc, char** argv) {
     if (argc < 4) return 2;
     const int N = std::atoi(argv[2]);
@@ -571,6 +674,7 @@ int main(int argc, char** argv) {
     if (mode == "burgers") return run_burgers(argc, argv);
     if (mode == "burgers_adapt") return run_burgers_adapt(argc, argv);
     if (mode == "wave") return run_wave(argc, argv);
+    if (mode == "wave_adapt") return run_wave_adapt(argc, argv);
     std::fprintf(stderr, "unknown mode %s\n", mode.c_str());
     return 2;
 }

@@ -97,6 +97,12 @@ WAVE_CASES = [
 ]
 
 
+# (name, dim, N_init, NMAX, eps, eta, sigma, cfl, steps): the adaptive wave loop
+WAVE_ADAPT_CASES = [
+    ("wave_adapt2d", 2, 3, 5, 1e-5, 1e-6, 10.0, 0.1, 4),
+]
+
+
 def main():
     if not os.path.exists(HARNESS):
         sys.exit("build the reference first: make -C oracle ref")
@@ -146,8 +152,20 @@ def main():
             idx = {tuple(a) + tuple(b): i for i, (a, b) in enumerate(zip(lv2, sp2))}
             arrs[key] = v[[idx[tuple(a) + tuple(b)] for a, b in zip(lv, sp)]]
         np.savez_compressed(os.path.join(HERE, name + ".npz"), **arrs)
-        manifest[name] = dict(kind="wave", dim=dim, N=N, k=2, sigma=sigma, steps=steps, dt=dt,
+        manifest[name] = dict(kind="wave", dim=dim, N=N, k=2, lagr_degree=4, sigma=sigma, steps=steps, dt=dt,
                               elements=int(r["meta"]["elements"]))
+        print(name, r["meta"])
+    for name, dim, n0, nmax, eps, eta, sigma, cfl, steps in WAVE_ADAPT_CASES:
+        r = run(["wave_adapt", dim, n0, nmax, repr(eps), repr(eta), repr(sigma), repr(cfl), steps])
+        arrs = {}
+        for i, tag in enumerate(["init"] + [f"step{s}" for s in range(steps)]):
+            lv, sp, u = split_elements(r["u_" + tag], dim)
+            lv2, sp2, ut = split_elements(r["ut_" + tag], dim)
+            assert (lv == lv2).all() and (sp == sp2).all()
+            arrs[f"level_{i}"], arrs[f"suppt_{i}"], arrs[f"u_{i}"], arrs[f"ut_{i}"] = lv, sp, u, ut
+        np.savez_compressed(os.path.join(HERE, name + ".npz"), **arrs)
+        manifest[name] = dict(kind="wave_adapt", dim=dim, n_init=n0, nmax=nmax, eps=eps, eta=eta, sigma=sigma,
+                              cfl=cfl, steps=steps, lagr_degree=4)
         print(name, r["meta"])
     for N, k in [(4, 2), (3, 1), (3, 3)]:
         r = run(["matrices", N, k])

@@ -143,10 +143,10 @@ def test_learned_adaptivity_gains_over_the_plain_criterion(ctx):
 
 def test_learned_wave_steps_follow_the_plain_criterion(ctx):
     """The classifier on the wave operator: trained on the plain criterion's decisions of a few
-    seeded runs, the learned steps (one right-hand side fewer per step) end on a grid whose
-    solution agrees with the plain run's on the common elements."""
+    seeded runs, the learned steps (no predictor) end on a grid whose solution agrees with the
+    plain run's on the common elements."""
     dim, nmax, eps, eta, sigma = 2, 7, 1e-4, 1e-5, 10.0
-    F = 9 * (1 + 2 * dim)
+    F = 2 * 9 * (1 + 2 * dim)  # features of u and of u_t
     rng = np.random.default_rng(5)
     feats, labs = [], []
     for _ in range(4):
@@ -190,7 +190,7 @@ def test_learned_wave_steps_follow_the_plain_criterion(ctx):
 
     k_plain, u_plain, w_plain = run(False)
     k_learn, u_learn, w_learn = run(True)
-    assert w_plain[1] == 50 and w_learn[1] == 40
+    assert w_plain[1] == 40 and w_learn[1] == 40
     common = sorted(set(k_plain) & set(k_learn))
     pp = {k: i for i, k in enumerate(k_plain)}
     pl = {k: i for i, k in enumerate(k_learn)}

@@ -125,14 +125,18 @@ def test_burgers_lagrange_path_matches_reference(name):
     assert rel_err(uT, z["uT"][perm]) < 1e-12
 
 
-def test_lagrange_basis_interpolates_its_nodes():
+@pytest.mark.parametrize("degree", [3, 4])
+def test_lagrange_basis_interpolates_its_nodes(degree):
     # hierarchical Lagrange basis: 1 at its own node, 0 at the other nodes of its element
+    # (degree 4 points sit 1e-13 off the nodes, relative to the element size)
+    O.lagr_degree(degree)
     for n, j in [(0, 1), (1, 1), (2, 1), (2, 3), (3, 5)]:
-        for p in range(4):
-            for q in range(4):
+        for p in range(degree + 1):
+            for q in range(degree + 1):
                 x = O.lib().amdg_oracle_lagr_point(n, j, q)
                 v = O.lib().amdg_oracle_lagr_val(n, j, p, x, 0)
-                assert abs(v - (1.0 if p == q else 0.0)) < 1e-13
+                assert abs(v - (1.0 if p == q else 0.0)) < 1e-11
+    O.lagr_degree(O.BURGERS_LAGR_DEGREE)
 
 
 ADAPT = [n for n, m in manifest().items() if m["kind"] == "burgers_adapt"]
@@ -223,6 +227,26 @@ def test_burgers_wave_solves_its_characteristic_equation():
 
 
 WAVE = [n for n, m in manifest().items() if m["kind"] == "wave"]
+WAVE_ADAPT = [n for n, m in manifest().items() if m["kind"] == "wave_adapt"]
+
+
+@pytest.mark.parametrize("name", WAVE_ADAPT)
+def test_adaptive_wave_matches_reference(name):
+    """The adaptive wave loop (EulerODE2nd predictor with the IPDG-only right-hand side, refine
+    on ||u|| + ||u_t||, RK4ODE2nd, coarsen): element sets bit-exact and u, u_t to 1e-12 of
+    their largest entry after the adaptive initialisation and every step."""
+    m = manifest()[name]
+    z = golden(name)
+    dim = m["dim"]
+    hist = O.wave_adaptive_run(dim, m["n_init"], m["nmax"], m["eps"], m["eta"], m["sigma"], m["cfl"], 1.0, m["steps"])
+    assert len(hist) == m["steps"] + 1
+    for i, (keys, u, v, _dt) in enumerate(hist):
+        ref_keys = O.arrays_to_keys(z[f"level_{i}"], z[f"suppt_{i}"])
+        assert sorted(ref_keys) == sorted(keys), f"element set differs after step {i}"
+        pos = {kk: j for j, kk in enumerate(ref_keys)}
+        perm = [pos[kk] for kk in keys]
+        assert np.abs(u - z[f"u_{i}"][perm]).max() <= 1e-12 * np.abs(z[f"u_{i}"]).max()
+        assert np.abs(v - z[f"ut_{i}"][perm]).max() <= 1e-12 * max(np.abs(z[f"ut_{i}"]).max(), 1e-30)
 
 
 @pytest.mark.parametrize("name", WAVE)
