@@ -373,4 +373,6 @@ struct amdg_batch {
     float* d_shadow = nullptr;           // 3 x dof
     void* graph_exec[2] = {nullptr, nullptr};  // cudaGraphExec_t per precision
     int64_t launches_per_graph = 0;
+    int tile[2] = {256, 256};             // CTA size of the stage kernel per precision (FP64, mixed)
+    float tile_ms[2][3] = {{0}};          // autotuner: one stage per candidate of kBatchTiles (0: not timed)
 };

@@ -69,7 +69,7 @@ amdg_status batch_step(amdg_batch* b, amdg_precision prec, cudaStream_t st) {
         const StageCoef c = coef_of(stage);
         if (prec == AMDG_PREC_MIXED) {
             BatchLaunch<float, float> L{};
-            L.dim = b->dim; L.np = b->k + 1; L.mode = 1; L.a = c.a; L.b = c.b;
+            L.dim = b->dim; L.np = b->k + 1; L.mode = 1; L.a = c.a; L.b = c.b; L.threads = b->tile[1];
             L.num_elements = b->num_elements; L.num_blocks = b->num_blocks;
             L.us = in[stage]; L.xs = sh[stage]; L.un = b->d_u; L.out = out[stage]; L.shadow_out = sh[sout[stage]];
             L.row_ptr = b->d_row_ptr; L.src = b->d_src; L.blk = b->d_blk; L.blocks = b->d_blocks32;
@@ -77,7 +77,7 @@ amdg_status batch_step(amdg_batch* b, amdg_precision prec, cudaStream_t st) {
             AMDG_CK(launch_batch<float, float>(L, st));
         } else {
             BatchLaunch<double, double> L{};
-            L.dim = b->dim; L.np = b->k + 1; L.mode = 1; L.a = c.a; L.b = c.b;
+            L.dim = b->dim; L.np = b->k + 1; L.mode = 1; L.a = c.a; L.b = c.b; L.threads = b->tile[0];
             L.num_elements = b->num_elements; L.num_blocks = b->num_blocks;
             L.us = in[stage]; L.xs = in[stage]; L.un = b->d_u; L.out = out[stage]; L.shadow_out = nullptr;
             L.row_ptr = b->d_row_ptr; L.src = b->d_src; L.blk = b->d_blk; L.blocks = b->d_blocks64;
@@ -86,6 +86,65 @@ amdg_status batch_step(amdg_batch* b, amdg_precision prec, cudaStream_t st) {
         }
     }
     return AMDG_OK;
+}
+
+// Autotuner of the stage kernel's tile: for each precision, time one stage
+// (the first RK stage from the current state into the scratch vectors, best of
+// three after a warm-up) with every CTA size the dimension supports and keep
+// the fastest.  Batches under 100,000 DOF keep 256 threads.
+amdg_status autotune_batch(amdg_batch* b, cudaStream_t st) {
+    if (b->dof < 100000) return AMDG_OK;
+    cudaEvent_t e0, e1;
+    AMDG_CK(cudaEventCreate(&e0));
+    AMDG_CK(cudaEventCreate(&e1));
+    amdg_status status = AMDG_OK;
+    AMDG_CK(launch_to_float(b->d_u, b->d_shadow, b->dof, st));
+    const StageCoef c = coef_of(0);
+    for (int pi = 0; pi < 2 && status == AMDG_OK; ++pi) {
+        float best = 0.f;
+        for (int ci = 0; ci < 3; ++ci) {
+            const int th = kBatchTiles[ci];
+            if (!batch_tile_supported(b->dim, b->k + 1, th)) continue;
+            float t_min = 0.f;
+            for (int rep = 0; rep < 4 && status == AMDG_OK; ++rep) {
+                cudaError_t e = cudaEventRecord(e0, st);
+                if (pi == 1) {
+                    BatchLaunch<float, float> L{};
+                    L.dim = b->dim; L.np = b->k + 1; L.mode = 1; L.a = c.a; L.b = c.b; L.threads = th;
+                    L.num_elements = b->num_elements; L.num_blocks = b->num_blocks;
+                    L.us = b->d_u; L.xs = b->d_shadow; L.un = b->d_u; L.out = b->d_u1; L.shadow_out = b->d_shadow + b->dof;
+                    L.row_ptr = b->d_row_ptr; L.src = b->d_src; L.blk = b->d_blk; L.blocks = b->d_blocks32;
+                    L.coef = b->d_coef32; L.dt = b->d_dt; L.solve_of = b->d_solve;
+                    if (e == cudaSuccess) e = launch_batch<float, float>(L, st);
+                } else {
+                    BatchLaunch<double, double> L{};
+                    L.dim = b->dim; L.np = b->k + 1; L.mode = 1; L.a = c.a; L.b = c.b; L.threads = th;
+                    L.num_elements = b->num_elements; L.num_blocks = b->num_blocks;
+                    L.us = b->d_u; L.xs = b->d_u; L.un = b->d_u; L.out = b->d_u1; L.shadow_out = nullptr;
+                    L.row_ptr = b->d_row_ptr; L.src = b->d_src; L.blk = b->d_blk; L.blocks = b->d_blocks64;
+                    L.coef = b->d_coef64; L.dt = b->d_dt; L.solve_of = b->d_solve;
+                    if (e == cudaSuccess) e = launch_batch<double, double>(L, st);
+                }
+                if (e == cudaSuccess) e = cudaEventRecord(e1, st);
+                if (e == cudaSuccess) e = cudaEventSynchronize(e1);
+                float ms = 0.f;
+                if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, e0, e1);
+                if (e != cudaSuccess) {
+                    status = fail(AMDG_ERR_CUDA, std::string("batch autotune: ") + cudaGetErrorString(e));
+                    break;
+                }
+                if (rep > 0 && (t_min == 0.f || ms < t_min)) t_min = ms;  // rep 0 warms up
+            }
+            b->tile_ms[pi][ci] = t_min;
+            if (status == AMDG_OK && (best == 0.f || t_min < best)) {
+                best = t_min;
+                b->tile[pi] = th;
+            }
+        }
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    return status;
 }
 
 }  // namespace
@@ -151,7 +210,37 @@ amdg_status amdg_batch_create(amdg_context* ctx, int n, amdg_grid* const* grids,
         amdg_batch_destroy(b);
         return fail(AMDG_ERR_CUDA, std::string("batch create: ") + cudaGetErrorString(e));
     }
+    if ((s = autotune_batch(b, st)) != AMDG_OK) {
+        amdg_batch_destroy(b);
+        return s;
+    }
     *out = b;
+    return AMDG_OK;
+}
+
+amdg_status amdg_batch_tuning(const amdg_batch* b, int* tile, float* stage_ms) {
+    AMDG_REQUIRE(b, AMDG_ERR_ARG, "batch is null");
+    if (tile) {
+        tile[0] = b->tile[0];
+        tile[1] = b->tile[1];
+    }
+    if (stage_ms)
+        for (int p = 0; p < 2; ++p)
+            for (int c = 0; c < 3; ++c) stage_ms[p * 3 + c] = b->tile_ms[p][c];
+    return AMDG_OK;
+}
+
+amdg_status amdg_batch_set_tile(amdg_batch* b, amdg_precision prec, int threads) {
+    AMDG_REQUIRE(b, AMDG_ERR_ARG, "batch is null");
+    AMDG_REQUIRE(prec == AMDG_PREC_FP64 || prec == AMDG_PREC_MIXED, AMDG_ERR_ARG, "bad precision");
+    AMDG_REQUIRE(batch_tile_supported(b->dim, b->k + 1, threads), AMDG_ERR_ARG, "unsupported CTA size for this dimension");
+    const int pi = prec == AMDG_PREC_MIXED ? 1 : 0;
+    if (b->tile[pi] != threads && b->graph_exec[pi]) {
+        AMDG_CK(cudaSetDevice(b->device));
+        cudaGraphExecDestroy(static_cast<cudaGraphExec_t>(b->graph_exec[pi]));
+        b->graph_exec[pi] = nullptr;
+    }
+    b->tile[pi] = threads;
     return AMDG_OK;
 }
 

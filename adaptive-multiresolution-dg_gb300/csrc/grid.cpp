@@ -198,80 +198,135 @@ static void fibres_along(const HostGrid& g, int t, std::vector<int32_t>* perm, s
     start->push_back(E);
 }
 
+namespace {
+
+// One fibre along t: members perm[s0 .. s0 + n) sorted by 1D order, and cum[o] = the number of
+// members whose 1D order is below o (o = 0 .. 2^nmax), so the members with orders in [lo, hi]
+// are perm[s0 + cum[lo] .. s0 + cum[hi + 1]).
+struct Fibre {
+    const HostGrid& g;
+    const int32_t* perm;
+    int t;
+    int64_t s0;
+    std::vector<int32_t>& cum;
+    Fibre(const HostGrid& g_, const int32_t* perm_, int t_, int64_t s0_, int64_t s1, std::vector<int32_t>& cum_)
+        : g(g_), perm(perm_), t(t_), s0(s0_), cum(cum_) {
+        const int n1 = 1 << g.nmax;
+        cum.assign(size_t(n1) + 1, 0);
+        for (int64_t j = s0; j < s1; ++j) ++cum[size_t(ord(j)) + 1];
+        for (int o = 0; o < n1; ++o) cum[size_t(o) + 1] += cum[o];
+    }
+    int ord(int64_t j) const { return g.order[size_t(perm[j]) * g.dim + t]; }
+    template <class Fn>
+    void range(int64_t lo, int64_t hi, Fn&& fn) const {
+        for (int64_t j = s0 + cum[size_t(lo)]; j < s0 + cum[size_t(hi) + 1]; ++j) fn(perm[j], ord(j));
+    }
+};
+
+// The neighbours of fibre member i along t, in increasing 1D order: vol(s, o) for the members
+// whose 1D supports intersect i's, flx(s, o) for those that intersect or touch it, also across
+// the periodic boundary (Element.cpp:283-348).  Levels 0 and 1 cover the whole domain; at level
+// l >= 2 the intervals meeting [a, b) are an index range, widened by one on a side where an
+// interval ends (or starts) exactly at the boundary, plus the wrap-around neighbour.
+template <class V, class F>
+void fibre_neighbours(const Fibre& fb, int64_t i, V&& vol, F&& flx) {
+    const int nmax = fb.g.nmax;
+    const int64_t one = int64_t(1) << nmax;
+    int64_t a0, b0;
+    support_units(fb.ord(i), nmax, &a0, &b0);
+    for (int l = 0; l <= nmax && l <= 1; ++l) {
+        fb.range(l, l, vol);
+        fb.range(l, l, flx);
+    }
+    for (int l = 2; l <= nmax; ++l) {
+        const int64_t cnt = int64_t(1) << (l - 1), w = one >> (l - 1);
+        const int64_t first = a0 / w, last = (b0 - 1) / w;
+        fb.range(cnt + first, cnt + last, vol);
+        int64_t lo = first, hi = last;
+        if (a0 % w == 0 && first >= 1) --lo;
+        if (b0 % w == 0 && last + 1 < cnt) ++hi;
+        if (b0 == one && lo > 0) fb.range(cnt, cnt, flx);  // the first interval, across x = 1
+        fb.range(cnt + lo, cnt + hi, flx);
+        if (a0 == 0 && hi < cnt - 1) fb.range(2 * cnt - 1, 2 * cnt - 1, flx);  // the last, across x = 0
+    }
+}
+
+}  // namespace
+
 void build_transform_topology(const HostGrid& g, TransformTopology* out) {
     const int dim = g.dim, nmax = g.nmax, n1 = 1 << nmax;
-    const int64_t one = int64_t(1) << nmax;
-    std::vector<int64_t> lo(n1), hi(n1);
     std::vector<int32_t> lev(n1);
-    for (int o = 0; o < n1; ++o) {
-        support_units(o, nmax, &lo[o], &hi[o]);
-        lev[o] = level_of_order(o);
-    }
+    for (int o = 0; o < n1; ++o) lev[o] = level_of_order(o);
     const int64_t E = g.num_elements;
-    // neighbours of e in dimension t are the members of e's fibre along t whose
-    // 1D supports intersect (vol) or intersect / touch, periodically (flx); one
-    // pass per dimension collects them fibre by fibre, in increasing 1D order
-    // (hence increasing level), then they are laid out element-major
-    struct Rows {
-        std::vector<int32_t> vnbr, fnbr;       // (element, order) pairs
-        std::vector<int32_t> voff, vlen, foff, flen;
-    };
-    std::vector<Rows> rows(dim);
-#pragma omp parallel for schedule(static) if (E >= 256)
+    std::vector<std::vector<int32_t>> perm(dim);
+    std::vector<std::vector<int64_t>> start(dim);
+#pragma omp parallel for schedule(static) if (E >= 4096)
+    for (int t = 0; t < dim; ++t) fibres_along(g, t, &perm[t], &start[t]);
+    // pass 1: neighbour counts per (element, dimension); pass 2: the lists at their final place
+    std::vector<int32_t> vcnt(size_t(E) * dim), fcnt(size_t(E) * dim);
     for (int t = 0; t < dim; ++t) {
-        std::vector<int32_t> perm;
-        std::vector<int64_t> start;
-        fibres_along(g, t, &perm, &start);
-        Rows& R = rows[t];
-        R.voff.assign(E, 0); R.vlen.assign(E, 0); R.foff.assign(E, 0); R.flen.assign(E, 0);
-        for (size_t f = 0; f + 1 < start.size(); ++f)
-            for (int64_t i = start[f]; i < start[f + 1]; ++i) {
-                const int32_t e = perm[i];
-                const int oe = g.order[size_t(e) * dim + t];
-                const int64_t a0 = lo[oe], b0 = hi[oe];
-                R.voff[e] = int32_t(R.vnbr.size() / 2);
-                R.foff[e] = int32_t(R.fnbr.size() / 2);
-                for (int64_t j = start[f]; j < start[f + 1]; ++j) {
-                    const int32_t s = perm[j];
-                    const int os = g.order[size_t(s) * dim + t];
-                    const int64_t a2 = lo[os], b2 = hi[os];
-                    const bool vol = !((a0 >= b2) || (b0 <= a2));
-                    if (vol) { R.vnbr.push_back(s); R.vnbr.push_back(os); }
-                    if (vol || flux_related(a0, b0, a2, b2, one)) { R.fnbr.push_back(s); R.fnbr.push_back(os); }
+        const int64_t nf = int64_t(start[t].size()) - 1;
+#pragma omp parallel if (E >= 4096)
+        {
+            std::vector<int32_t> cum;
+#pragma omp for schedule(dynamic, 8)
+            for (int64_t f = 0; f < nf; ++f) {
+                const Fibre fb(g, perm[t].data(), t, start[t][f], start[t][f + 1], cum);
+                for (int64_t i = start[t][f]; i < start[t][f + 1]; ++i) {
+                    int32_t nv = 0, nfx = 0;
+                    fibre_neighbours(fb, i, [&](int32_t, int) { ++nv; }, [&](int32_t, int) { ++nfx; });
+                    const size_t r = size_t(perm[t][i]) * dim + t;
+                    vcnt[r] = nv;
+                    fcnt[r] = nfx;
                 }
-                R.vlen[e] = int32_t(R.vnbr.size() / 2) - R.voff[e];
-                R.flen[e] = int32_t(R.fnbr.size() / 2) - R.foff[e];
             }
+        }
     }
     out->vol_ptr.assign(size_t(E) * dim + 1, 0);
     out->flx_ptr.assign(size_t(E) * dim + 1, 0);
-    for (int64_t e = 0; e < E; ++e)
-        for (int t = 0; t < dim; ++t) {
-            const size_t r = size_t(e) * dim + t;
-            out->vol_ptr[r + 1] = out->vol_ptr[r] + rows[t].vlen[e];
-            out->flx_ptr[r + 1] = out->flx_ptr[r] + rows[t].flen[e];
-        }
+    for (size_t r = 0; r < size_t(E) * dim; ++r) {
+        out->vol_ptr[r + 1] = out->vol_ptr[r] + vcnt[r];
+        out->flx_ptr[r + 1] = out->flx_ptr[r] + fcnt[r];
+    }
     out->vol_nbr.resize(size_t(2) * out->vol_ptr.back());
     out->flx_nbr.resize(size_t(2) * out->flx_ptr.back());
     out->vol_split.assign(size_t(E) * dim, 0);
     out->flx_split.assign(size_t(E) * dim, 0);
-#pragma omp parallel for schedule(static) if (E >= 4096)
-    for (int64_t e = 0; e < E; ++e)
-        for (int t = 0; t < dim; ++t) {
-            const size_t r = size_t(e) * dim + t;
-            const Rows& R = rows[t];
-            std::copy(R.vnbr.begin() + 2 * size_t(R.voff[e]), R.vnbr.begin() + 2 * size_t(R.voff[e] + R.vlen[e]),
-                      out->vol_nbr.begin() + 2 * size_t(out->vol_ptr[r]));
-            std::copy(R.fnbr.begin() + 2 * size_t(R.foff[e]), R.fnbr.begin() + 2 * size_t(R.foff[e] + R.flen[e]),
-                      out->flx_nbr.begin() + 2 * size_t(out->flx_ptr[r]));
-            // the "U" part (level <= own) is a prefix, the "L" part (finer) the rest
-            const int own = lev[g.order[r]];
-            int32_t sv = out->vol_ptr[r], sf = out->flx_ptr[r];
-            while (sv < out->vol_ptr[r + 1] && lev[out->vol_nbr[2 * size_t(sv) + 1]] <= own) ++sv;
-            while (sf < out->flx_ptr[r + 1] && lev[out->flx_nbr[2 * size_t(sf) + 1]] <= own) ++sf;
-            out->vol_split[r] = sv;
-            out->flx_split[r] = sf;
+    for (int t = 0; t < dim; ++t) {
+        const int64_t nf = int64_t(start[t].size()) - 1;
+#pragma omp parallel if (E >= 4096)
+        {
+            std::vector<int32_t> cum;
+#pragma omp for schedule(dynamic, 8)
+            for (int64_t f = 0; f < nf; ++f) {
+                const Fibre fb(g, perm[t].data(), t, start[t][f], start[t][f + 1], cum);
+                for (int64_t i = start[t][f]; i < start[t][f + 1]; ++i) {
+                    const size_t r = size_t(perm[t][i]) * dim + t;
+                    const int own = lev[fb.ord(i)];
+                    int32_t* vp = &out->vol_nbr[2 * size_t(out->vol_ptr[r])];
+                    int32_t* fp = &out->flx_nbr[2 * size_t(out->flx_ptr[r])];
+                    // the "U" part (level <= own) is a prefix, the "L" part (finer) the rest
+                    int32_t nv = 0, nfx = 0, sv = 0, sf = 0;
+                    fibre_neighbours(
+                        fb, i,
+                        [&](int32_t s, int o) {
+                            vp[2 * nv] = s;
+                            vp[2 * nv + 1] = o;
+                            ++nv;
+                            if (lev[o] <= own) sv = nv;
+                        },
+                        [&](int32_t s, int o) {
+                            fp[2 * nfx] = s;
+                            fp[2 * nfx + 1] = o;
+                            ++nfx;
+                            if (lev[o] <= own) sf = nfx;
+                        });
+                    out->vol_split[r] = out->vol_ptr[r] + sv;
+                    out->flx_split[r] = out->flx_ptr[r] + sf;
+                }
+            }
         }
+    }
 }
 
 bool build_surplus_ancestors(const HostGrid& g, const LagrTables& t, std::vector<int32_t>* anc) {

@@ -59,6 +59,7 @@ struct LinearLaunch {
 template <typename T, typename X>
 struct BatchLaunch {
     int dim, np, mode;       // mode 0: rhs; 1: RK stage a*un + b*(us + dt[solve]*rhs)
+    int threads;             // CTA size (the tile: threads / (np^(dim-1)) elements per CTA); 0 = 256
     double a, b;
     int64_t num_elements;
     int num_blocks;
@@ -77,6 +78,9 @@ struct BatchLaunch {
 };
 template <typename T, typename X>
 cudaError_t launch_batch(const BatchLaunch<T, X>& L, cudaStream_t st);
+// CTA sizes launch_batch offers for a dimension (all of them fit at least one element)
+constexpr int kBatchTiles[3] = {128, 256, 512};
+bool batch_tile_supported(int dim, int np, int threads);
 
 constexpr int kReduceBlocks = 1216;  // 8 CTAs per SM on 152 SMs
 

@@ -3,7 +3,10 @@
 // stage advances all of them.  Each element carries its solve index; the
 // solve's velocity c scales the per-dimension sum of the shared 1D blocks
 // (u_vx + upwind flux, one table per flux side), and the solve's dt enters
-// the fused SSP-RK3 epilogue.  Column layout as linear_col_kernel.
+// the fused SSP-RK3 epilogue.  Column layout as linear_col_kernel; the CTA
+// size TH (the tile: TH / np^(dim-1) elements per CTA) is a template
+// parameter the batch's autotuner picks (128, 256 or 512 threads for
+// dim <= 3, 256 above).
 #include <cuda_runtime.h>
 
 #include <cstdint>
@@ -21,11 +24,11 @@ __device__ __forceinline__ double batch_combine(double a, double un, double b, d
     return __dadd_rn(__dmul_rn(a, un), __dmul_rn(b, __dadd_rn(us, __dmul_rn(dt, rhs))));
 }
 
-template <int D, int NP, typename T, typename X>
-__global__ void __launch_bounds__(256) batch_col_kernel(BatchLaunch<T, X> L) {
+template <int D, int NP, int TH, typename T, typename X>
+__global__ void __launch_bounds__(TH) batch_col_kernel(BatchLaunch<T, X> L) {
     constexpr int B = BPow<NP, D>::v;
     constexpr int C = B / NP;
-    constexpr int G = 256 / C;
+    constexpr int G = TH / C > 0 ? TH / C : 1;  // launch_batch only launches TH >= C
     __shared__ T y[G * B];
     const int tid = threadIdx.x;
     const int g = tid / C, c = tid - (tid / C) * C;
@@ -80,23 +83,45 @@ __global__ void __launch_bounds__(256) batch_col_kernel(BatchLaunch<T, X> L) {
     }
 }
 
+bool batch_tile_supported(int dim, int np, int threads) {
+    int c = 1;
+    for (int d = 1; d < dim; ++d) c *= np;
+    if (threads < c) return false;
+    if (dim <= 3) return threads == 128 || threads == 256 || threads == 512;
+    return threads == 256;
+}
+
+template <int D, int NP, int TH, typename T, typename X>
+cudaError_t launch_batch_tile(const BatchLaunch<T, X>& L, cudaStream_t st) {
+    constexpr int C = BPow<NP, D>::v / NP;
+    if (TH < C) return cudaErrorInvalidValue;
+    constexpr int G = TH / C > 0 ? TH / C : 1;
+    const int64_t grid = (L.num_elements + G - 1) / G;
+    batch_col_kernel<D, NP, TH, T, X><<<unsigned(grid), TH, 0, st>>>(L);
+    return cudaGetLastError();
+}
+
 template <typename T, typename X>
 cudaError_t launch_batch(const BatchLaunch<T, X>& L, cudaStream_t st) {
     if (L.num_elements == 0) return cudaSuccess;
-#define AMDG_BCASE(D, NP)                                                                        \
-    if (L.dim == D && L.np == NP) {                                                               \
-        constexpr int G = 256 / (BPow<NP, D>::v / NP);                                            \
-        const int64_t grid = (L.num_elements + G - 1) / G;                                        \
-        batch_col_kernel<D, NP, T, X><<<unsigned(grid), 256, 0, st>>>(L);                         \
-        return cudaGetLastError();                                                                \
+    const int th = L.threads ? L.threads : 256;
+    if (!batch_tile_supported(L.dim, L.np, th)) return cudaErrorInvalidValue;
+#define AMDG_BCASE3(D, NP)                                                            \
+    if (L.dim == D && L.np == NP) {                                                    \
+        if (th == 128) return launch_batch_tile<D, NP, 128, T, X>(L, st);              \
+        if (th == 512) return launch_batch_tile<D, NP, 512, T, X>(L, st);              \
+        return launch_batch_tile<D, NP, 256, T, X>(L, st);                             \
     }
-    AMDG_BCASE(1, 2) AMDG_BCASE(1, 3) AMDG_BCASE(1, 4)
-    AMDG_BCASE(2, 2) AMDG_BCASE(2, 3) AMDG_BCASE(2, 4)
-    AMDG_BCASE(3, 2) AMDG_BCASE(3, 3) AMDG_BCASE(3, 4)
-    AMDG_BCASE(4, 2) AMDG_BCASE(4, 3) AMDG_BCASE(4, 4)
-    AMDG_BCASE(5, 2) AMDG_BCASE(5, 3) AMDG_BCASE(5, 4)
-    AMDG_BCASE(6, 2) AMDG_BCASE(6, 3)
-#undef AMDG_BCASE
+#define AMDG_BCASE1(D, NP) \
+    if (L.dim == D && L.np == NP) return launch_batch_tile<D, NP, 256, T, X>(L, st);
+    AMDG_BCASE3(1, 2) AMDG_BCASE3(1, 3) AMDG_BCASE3(1, 4)
+    AMDG_BCASE3(2, 2) AMDG_BCASE3(2, 3) AMDG_BCASE3(2, 4)
+    AMDG_BCASE3(3, 2) AMDG_BCASE3(3, 3) AMDG_BCASE3(3, 4)
+    AMDG_BCASE1(4, 2) AMDG_BCASE1(4, 3) AMDG_BCASE1(4, 4)
+    AMDG_BCASE1(5, 2) AMDG_BCASE1(5, 3) AMDG_BCASE1(5, 4)
+    AMDG_BCASE1(6, 2) AMDG_BCASE1(6, 3)
+#undef AMDG_BCASE3
+#undef AMDG_BCASE1
     return cudaErrorInvalidValue;
 }
 

@@ -123,6 +123,8 @@ def load():
         "amdg_batch_rk3_steps": ([vp, i32, i32, i32], i32),
         "amdg_batch_store": ([vp, i32], i32),
         "amdg_batch_coefficients_device": ([vp, pp, vp], i32),
+        "amdg_batch_tuning": ([vp, vp, vp], i32),
+        "amdg_batch_set_tile": ([vp, i32, i32], i32),
         "amdg_burgers_destroy": ([vp], i32),
         "amdg_burgers_rhs": ([vp, vp, vp, i32], i32),
         "amdg_burgers_point_values": ([vp, vp, vp, i32], i32),
@@ -574,6 +576,16 @@ class Batch:
 
     def store(self, solve: int):
         _ck(load().amdg_batch_store(self._h, solve), "batch_store")
+
+    def tuning(self):
+        """(CTA size per precision [FP64, mixed], stage ms per candidate [2][128, 256, 512 threads])."""
+        tile = np.zeros(2, np.int32)
+        ms = np.zeros(6, np.float32)
+        _ck(load().amdg_batch_tuning(self._h, _ptr(tile), _ptr(ms)), "batch_tuning")
+        return tile.tolist(), ms.reshape(2, 3).tolist()
+
+    def set_tile(self, prec: int, threads: int):
+        _ck(load().amdg_batch_set_tile(self._h, prec, threads), "batch_set_tile")
 
     def close(self):
         if self._h:

@@ -293,6 +293,13 @@ amdg_status amdg_batch_rk3_steps(amdg_batch* b, int nsteps, amdg_precision prec,
 amdg_status amdg_batch_store(amdg_batch* b, int solve);
 /* Device pointer of the concatenated state and the element offsets (n+1 entries, may be NULL). */
 amdg_status amdg_batch_coefficients_device(amdg_batch* b, double** device_ptr, int64_t* elem_offsets);
+/* Tile of the stage kernel: amdg_batch_create times one stage with CTAs of 128, 256 and 512
+ * threads (threads / (k+1)^(dim-1) elements per CTA; dim <= 3, 256 only above) for each
+ * precision and keeps the fastest (batches under 100,000 DOF keep 256).  tile[2] = chosen CTA
+ * size (FP64, mixed); stage_ms[2][3] = measured stage times per candidate, 0 where not timed. */
+amdg_status amdg_batch_tuning(const amdg_batch* b, int* tile, float* stage_ms);
+/* Override the tile of one precision (AMDG_ERR_ARG if the dimension does not offer it). */
+amdg_status amdg_batch_set_tile(amdg_batch* b, amdg_precision prec, int threads);
 
 /* Work counters since creation: RK-stage DOF updates (3 x DOF per SSP-RK3
  * step) and right-hand-side evaluations (including adaptive predictors).  No

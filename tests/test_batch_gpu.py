@@ -73,3 +73,33 @@ def test_batch_mixed_and_l2_error(ctx):
             g.close()
     for i in range(len(work)):
         assert abs(errs[(amdg.MIXED, i)] - errs[(amdg.FP64, i)]) <= 1e-3 * errs[(amdg.FP64, i)]
+
+
+def test_batch_tiles_agree_and_autotuner_picks_one(ctx):
+    """Every CTA size sums each output in the same order, so all tiles give bitwise the same
+    steps; a batch over 100,000 DOF is timed with every tile and keeps the fastest."""
+    work = O.batched_workload(8, seed=11)
+    grids = _grids(ctx, work, 6, 1e-4)
+    dts = [0.1 / (sum(abs(v) for v in w["velocity"]) * 64) for w in work]
+    results = {}
+    for prec in (amdg.FP64, amdg.MIXED):
+        for th in (128, 256, 512):
+            batch = amdg.Batch(ctx, grids, [w["velocity"] for w in work])
+            assert batch.dof > 100000
+            tile, ms = batch.tuning()
+            row = ms[0 if prec == amdg.FP64 else 1]
+            assert all(t > 0 for t in row)
+            assert tile[0 if prec == amdg.FP64 else 1] == (128, 256, 512)[int(np.argmin(row))]
+            batch.set_tile(prec, th)
+            batch.set_dt(dts)
+            batch.rk3_steps(2, prec, use_graph=True)
+            ctx.synchronize()
+            batch.store(3)
+            results[(prec, th)] = grids[3].coefficients().copy()
+            batch.close()
+            for g, w in zip(grids, work):  # restore the initial state for the next batch
+                g.init_separable(O.gaussian_bump_terms(w["centers"], w["widths"], w["amplitudes"]))
+        assert np.array_equal(results[(prec, 128)], results[(prec, 256)])
+        assert np.array_equal(results[(prec, 512)], results[(prec, 256)])
+    for g in grids:
+        g.close()
