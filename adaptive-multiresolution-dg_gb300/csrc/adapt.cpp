@@ -122,11 +122,10 @@ std::vector<uint64_t> refine_keys(const HostGrid& g, const double* norms, double
             }
         work.swap(next);
     }
-    std::vector<uint64_t> keys;
-    keys.reserve(g.key.size() + fresh.size());
-    keys.insert(keys.end(), g.key.begin(), g.key.end());
-    keys.insert(keys.end(), fresh.begin(), fresh.end());
-    std::sort(keys.begin(), keys.end());
+    // the existing keys are ascending: sort the new ones and merge
+    std::sort(fresh.begin(), fresh.end());
+    std::vector<uint64_t> keys(g.key.size() + fresh.size());
+    std::merge(g.key.begin(), g.key.end(), fresh.begin(), fresh.end(), keys.begin());
     return keys;
 }
 
@@ -196,7 +195,7 @@ void parent_table(const HostGrid& g, std::vector<int32_t>* pg) {
 }
 
 void grid_from_keys(int dim, int nmax, int k, std::vector<uint64_t> keys, HostGrid* g) {
-    std::sort(keys.begin(), keys.end());
+    if (!std::is_sorted(keys.begin(), keys.end())) std::sort(keys.begin(), keys.end());
     keys.erase(std::unique(keys.begin(), keys.end()), keys.end());
     g->dim = dim;
     g->nmax = nmax;

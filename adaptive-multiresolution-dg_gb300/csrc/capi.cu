@@ -119,10 +119,15 @@ amdg_status grid_set_keys(amdg_grid* g, std::vector<uint64_t> keys) {
     ng.sparse = g->host.sparse;
     grid_from_keys(g->host.dim, g->host.nmax, g->host.k, std::move(keys), &ng);
     if (ng.num_elements > (int64_t(1) << 31) - 1) return fail(AMDG_ERR_CAPACITY, "more than 2^31-1 elements");
+    // old index of every new element (-1: new), by a merge of the two ascending key lists
     std::vector<int32_t> map(ng.num_elements);
-    for (int64_t e = 0; e < ng.num_elements; ++e) {
-        auto it = std::lower_bound(g->host.key.begin(), g->host.key.end(), ng.key[e]);
-        map[e] = (it != g->host.key.end() && *it == ng.key[e]) ? int32_t(it - g->host.key.begin()) : -1;
+    {
+        const std::vector<uint64_t>& ok = g->host.key;
+        size_t j = 0;
+        for (int64_t e = 0; e < ng.num_elements; ++e) {
+            while (j < ok.size() && ok[j] < ng.key[e]) ++j;
+            map[e] = (j < ok.size() && ok[j] == ng.key[e]) ? int32_t(j) : -1;
+        }
     }
     cudaStream_t st = stream_of(g->ctx);
     const int64_t E = ng.num_elements;

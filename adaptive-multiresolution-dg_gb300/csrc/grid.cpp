@@ -200,17 +200,23 @@ static void fibres_along(const HostGrid& g, int t, std::vector<int32_t>* perm, s
 
 namespace {
 
-// One fibre along t: members perm[s0 .. s0 + n) sorted by 1D order, and cum[o] = the number of
-// members whose 1D order is below o (o = 0 .. 2^nmax), so the members with orders in [lo, hi]
-// are perm[s0 + cum[lo] .. s0 + cum[hi + 1]).
+// One fibre along t: members perm[s0 .. s1) sorted by 1D order.  A long fibre also keeps
+// cum[o] = the number of members whose 1D order is below o (o = 0 .. 2^nmax), so the members
+// with orders in [lo, hi] are perm[s0 + cum[lo] .. s0 + cum[hi + 1]); a short one is scanned.
+constexpr int64_t kScanFibre = 48;
 struct Fibre {
     const HostGrid& g;
     const int32_t* perm;
+    const int64_t* lo;  // 1D support [lo[o], hi[o]) of order o, in units of 2^-nmax
+    const int64_t* hi;
     int t;
-    int64_t s0;
+    int64_t s0, s1;
+    bool indexed;
     std::vector<int32_t>& cum;
-    Fibre(const HostGrid& g_, const int32_t* perm_, int t_, int64_t s0_, int64_t s1, std::vector<int32_t>& cum_)
-        : g(g_), perm(perm_), t(t_), s0(s0_), cum(cum_) {
+    Fibre(const HostGrid& g_, const int32_t* perm_, const int64_t* lo_, const int64_t* hi_, int t_, int64_t s0_,
+          int64_t s1_, std::vector<int32_t>& cum_)
+        : g(g_), perm(perm_), lo(lo_), hi(hi_), t(t_), s0(s0_), s1(s1_), indexed(s1_ - s0_ > kScanFibre), cum(cum_) {
+        if (!indexed) return;
         const int n1 = 1 << g.nmax;
         cum.assign(size_t(n1) + 1, 0);
         for (int64_t j = s0; j < s1; ++j) ++cum[size_t(ord(j)) + 1];
@@ -232,8 +238,18 @@ template <class V, class F>
 void fibre_neighbours(const Fibre& fb, int64_t i, V&& vol, F&& flx) {
     const int nmax = fb.g.nmax;
     const int64_t one = int64_t(1) << nmax;
-    int64_t a0, b0;
-    support_units(fb.ord(i), nmax, &a0, &b0);
+    const int oi = fb.ord(i);
+    const int64_t a0 = fb.lo[oi], b0 = fb.hi[oi];
+    if (!fb.indexed) {  // short fibre: test every member
+        for (int64_t j = fb.s0; j < fb.s1; ++j) {
+            const int o = fb.ord(j);
+            const int64_t a2 = fb.lo[o], b2 = fb.hi[o];
+            const bool v = !((a0 >= b2) || (b0 <= a2));
+            if (v) vol(fb.perm[j], o);
+            if (v || flux_related(a0, b0, a2, b2, one)) flx(fb.perm[j], o);
+        }
+        return;
+    }
     for (int l = 0; l <= nmax && l <= 1; ++l) {
         fb.range(l, l, vol);
         fb.range(l, l, flx);
@@ -256,7 +272,11 @@ void fibre_neighbours(const Fibre& fb, int64_t i, V&& vol, F&& flx) {
 void build_transform_topology(const HostGrid& g, TransformTopology* out) {
     const int dim = g.dim, nmax = g.nmax, n1 = 1 << nmax;
     std::vector<int32_t> lev(n1);
-    for (int o = 0; o < n1; ++o) lev[o] = level_of_order(o);
+    std::vector<int64_t> slo(n1), shi(n1);
+    for (int o = 0; o < n1; ++o) {
+        lev[o] = level_of_order(o);
+        support_units(o, nmax, &slo[o], &shi[o]);
+    }
     const int64_t E = g.num_elements;
     std::vector<std::vector<int32_t>> perm(dim);
     std::vector<std::vector<int64_t>> start(dim);
@@ -266,12 +286,12 @@ void build_transform_topology(const HostGrid& g, TransformTopology* out) {
     std::vector<int32_t> vcnt(size_t(E) * dim), fcnt(size_t(E) * dim);
     for (int t = 0; t < dim; ++t) {
         const int64_t nf = int64_t(start[t].size()) - 1;
-#pragma omp parallel if (E >= 4096)
+#pragma omp parallel if (E >= 8192)
         {
             std::vector<int32_t> cum;
 #pragma omp for schedule(dynamic, 8)
             for (int64_t f = 0; f < nf; ++f) {
-                const Fibre fb(g, perm[t].data(), t, start[t][f], start[t][f + 1], cum);
+                const Fibre fb(g, perm[t].data(), slo.data(), shi.data(), t, start[t][f], start[t][f + 1], cum);
                 for (int64_t i = start[t][f]; i < start[t][f + 1]; ++i) {
                     int32_t nv = 0, nfx = 0;
                     fibre_neighbours(fb, i, [&](int32_t, int) { ++nv; }, [&](int32_t, int) { ++nfx; });
@@ -294,12 +314,12 @@ void build_transform_topology(const HostGrid& g, TransformTopology* out) {
     out->flx_split.assign(size_t(E) * dim, 0);
     for (int t = 0; t < dim; ++t) {
         const int64_t nf = int64_t(start[t].size()) - 1;
-#pragma omp parallel if (E >= 4096)
+#pragma omp parallel if (E >= 8192)
         {
             std::vector<int32_t> cum;
 #pragma omp for schedule(dynamic, 8)
             for (int64_t f = 0; f < nf; ++f) {
-                const Fibre fb(g, perm[t].data(), t, start[t][f], start[t][f + 1], cum);
+                const Fibre fb(g, perm[t].data(), slo.data(), shi.data(), t, start[t][f], start[t][f + 1], cum);
                 for (int64_t i = start[t][f]; i < start[t][f + 1]; ++i) {
                     const size_t r = size_t(perm[t][i]) * dim + t;
                     const int own = lev[fb.ord(i)];

@@ -440,12 +440,12 @@ def bench_burgers_adaptive(ctx, stream, args):
 def bench_wave_adaptive(ctx, stream, args):
     """2D wave equation u_tt = div(c^2 grad u), c = 1 + 0.5 sin(2 pi x) sin(2 pi y), Gaussian bump
     exp(-200 |x - (0.3, 0.4)|^2) at rest, adaptive (refine 1e-5, coarsen 1e-6, max level 9, start
-    level 3), IPDG sigma = 10, RK4ODE2nd, CFL 0.1, to T = 0.5: the plain FP64 path (EulerODE2nd
-    predictor, refine, RK4, coarsen) against mixed precision with the learned refine/coarsen
-    classifier, trained on the plain criterion's decisions in 20 seeded runs (bump centre in
-    [0.25, 0.75]^2, width parameter in [100, 300]).  No exact solution: each final solution is
-    compared, on a 128^2 cell-centre mesh, with a plain FP64 run at refine 1e-6 / coarsen 1e-7 and
-    max level 10."""
+    level 3), IPDG sigma = 10, RK4ODE2nd, CFL 0.1, to T = --wave-time: the plain FP64 path
+    (EulerODE2nd predictor, refine, RK4, coarsen) against mixed precision with the learned
+    refine/coarsen classifier, trained on the plain criterion's decisions in 20 seeded runs (bump
+    centre in [0.25, 0.75]^2, width parameter in [100, 300]).  No exact solution: each final
+    solution is compared, on a 128^2 cell-centre mesh, with a plain FP64 run at max level 10 and
+    the same thresholds."""
     import torch
 
     import amdg
@@ -475,14 +475,27 @@ def bench_wave_adaptive(ctx, stream, args):
         op.close()
         g.close()
     x, y = np.concatenate(feats), np.concatenate(labs)
+    collected = int(len(y))
+    # the grids fill up, so the runs give millions of samples: keep every sample of the rare
+    # classes (refine, coarsen) up to half the cap and fill the rest with "keep" samples
+    cap = args.wave_train_samples
+    if len(y) > cap:
+        pick = np.random.default_rng(3)
+        rare = np.flatnonzero(y != 1)
+        if len(rare) > cap // 2:
+            rare = pick.choice(rare, cap // 2, replace=False)
+        keep = pick.choice(np.flatnonzero(y == 1), cap - len(rare), replace=False)
+        idx = np.sort(np.concatenate([rare, keep]))
+        x, y = x[idx], y[idx]
     collect_s = time.perf_counter() - t0
-    dx, dy = torch.from_numpy(x).cuda(), torch.from_numpy(y).cuda()
+    dx, dy = torch.from_numpy(np.ascontiguousarray(x)).cuda(), torch.from_numpy(np.ascontiguousarray(y)).cuda()
     torch.cuda.synchronize()
     mlp = amdg.MLP(ctx, F, 64, 3, 3, seed=21)
     t0 = time.perf_counter()
     loss = mlp.train_device(dx.data_ptr(), dy.data_ptr(), len(y), epochs=args.learn_epochs, batch=256, lr=2e-3,
                             seed=22)
-    out["training"] = {"runs": args.wave_learn_runs, "steps_per_run": args.wave_learn_steps, "samples": int(len(y)),
+    out["training"] = {"runs": args.wave_learn_runs, "steps_per_run": args.wave_learn_steps,
+                       "samples_collected": collected, "samples": int(len(y)),
                        "class_counts": [int((y == i).sum()) for i in range(3)], "epochs": args.learn_epochs,
                        "final_loss": loss, "collect_s": collect_s, "train_s": time.perf_counter() - t0}
     mesh = (np.arange(128) + 0.5) / 128
@@ -526,8 +539,11 @@ def bench_wave_adaptive(ctx, stream, args):
         g.close()
         return res
 
-    ref = run(False, amdg.FP64, T, eps / 10, eta / 10, 10)["_mesh_values"]
-    out["reference_run"] = "plain FP64, refine 1e-6, coarsen 1e-7, max level 10"
+    ref_run = run(False, amdg.FP64, T, eps, eta, 10)
+    ref = ref_run.pop("_mesh_values")
+    out["reference_run"] = {"what": "plain FP64, refine 1e-5, coarsen 1e-6, max level 10",
+                            "wall_s": ref_run["wall_s"], "steps": ref_run["steps"],
+                            "elements_final": ref_run["elements_final"]}
     for name, learned, prec in (("plain_fp64", False, amdg.FP64), ("mixed_learned", True, amdg.MIXED),
                                 ("mixed_plain", False, amdg.MIXED)):
         run(learned, prec, 4 * CFL / (speed * dim * 128))  # warm-up: a few steps
@@ -583,8 +599,12 @@ def bench_batched(ctx, stream, args):
         e.record(stream)
         torch.cuda.synchronize()
         sec = s.elapsed_time(e) / 1e3
+        tile, tile_ms = batch.tuning()
+        pi = 0 if prec == amdg.FP64 else 1
         out[name] = {"value": 3.0 * batch.dof * args.steps / sec, "ms_per_step": sec / args.steps * 1e3,
-                     "dof": batch.dof, "launches_per_step": 3}
+                     "dof": batch.dof, "launches_per_step": 3,
+                     "autotuned_tile": {"cta_threads": tile[pi],
+                                        "stage_ms_by_cta_threads": dict(zip(("128", "256", "512"), tile_ms[pi]))}}
         errs = []
         nsteps = args.warmup + args.steps
         for i in range(0, len(work), max(1, len(work) // 16)):
@@ -603,6 +623,50 @@ def bench_batched(ctx, stream, args):
     for g in grids:
         g.close()
     return out
+
+
+def profile_wave_rhs():
+    """Profiling case of the wave right-hand side (not a bench line): the 2D adaptive wave grid
+    after 40 plain adaptive steps (max level 9, refine 1e-5, coarsen 1e-6; about 20,000
+    elements), RHS times in FP64 and mixed, then one FP64 and one mixed right-hand side between
+    cudaProfilerStart / cudaProfilerStop, for ncu --profile-from-start off."""
+    import torch
+
+    import amdg
+    import amdg_oracle as O
+    torch.cuda.set_device(0)
+    ctx = amdg.Context(0)
+    stream = torch.cuda.Stream()
+    torch.cuda.set_stream(stream)
+    ctx.set_stream(stream.cuda_stream)
+    g = amdg.Grid(ctx, 2, 9, 2, level_init=3)
+    g.init_separable_adaptive(O.wave_ic_terms(2), 1e-5)
+    op = amdg.WaveOperator(g, 10.0)
+    for _ in range(40):
+        op.adaptive_step(CFL, 1.0, 1e-5, 1e-6)
+    ctx.synchronize()
+    du = torch.from_numpy(g.coefficients().reshape(-1).copy()).cuda()
+    out = torch.zeros_like(du)
+    torch.cuda.synchronize()
+    for prec in (amdg.FP64, amdg.MIXED):
+        op.rhs_device(du.data_ptr(), out.data_ptr(), prec)
+    ctx.synchronize()
+    s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    for prec, name in ((amdg.FP64, "fp64"), (amdg.MIXED, "mixed")):
+        s.record(stream)
+        for _ in range(20):
+            op.rhs_device(du.data_ptr(), out.data_ptr(), prec)
+        e.record(stream)
+        torch.cuda.synchronize()
+        print(json.dumps({"elements": g.num_elements, "dof": g.dof, f"rhs_{name}_ms": s.elapsed_time(e) / 20}),
+              flush=True)
+    torch.cuda.cudart().cudaProfilerStart()
+    op.rhs_device(du.data_ptr(), out.data_ptr(), amdg.FP64)
+    op.rhs_device(du.data_ptr(), out.data_ptr(), amdg.MIXED)
+    ctx.synchronize()
+    torch.cuda.cudart().cudaProfilerStop()
+    op.close()
+    g.close()
 
 
 def cpu_baseline(g, u0, budget_s=15.0):
@@ -680,9 +744,15 @@ def main():
     ap.add_argument("--learn-epochs", type=int, default=30)
     ap.add_argument("--wave-learn-runs", type=int, default=20, help="plain wave runs that train its classifier (0: skip)")
     ap.add_argument("--wave-learn-steps", type=int, default=30)
-    ap.add_argument("--wave-time", type=float, default=0.5)
+    ap.add_argument("--wave-train-samples", type=int, default=300000, help="training samples kept (stratified)")
+    ap.add_argument("--profile", choices=["none", "wave_rhs"], default="none",
+                    help="wave_rhs: run the wave right-hand-side profiling case instead of the bench")
+    ap.add_argument("--wave-time", type=float, default=0.05,
+                    help="final time of the 2D wave runs (the config's 0.5 takes ~5000 steps on a filling grid)")
     args = ap.parse_args()
-    if args.impl == "reference":
+    if args.profile == "wave_rhs":
+        profile_wave_rhs()
+    elif args.impl == "reference":
         run_reference(args)
     else:
         run_ours(args)
