@@ -58,8 +58,21 @@ void build_oper1d(const Basis1D& b, Oper1D* out, bool want_u_v);
 // n-point Gauss-Legendre nodes and weights on [-1, 1] (n <= 16)
 void gauss_legendre(int n, double* x, double* w);
 
+// A separable factor given point by point or in bulk.
+struct Fn1d {
+    amdg_fn1d f = nullptr;
+    amdg_fn1d_batch fb = nullptr;
+    void* user = nullptr;
+    void eval(const double* x, int64_t n, int d, int term, double* out) const {
+        if (fb) {
+            fb(x, n, d, term, out, user);
+            return;
+        }
+        for (int64_t i = 0; i < n; ++i) out[i] = f(x[i], d, term, user);
+    }
+};
 // 1D projection of f(., d, term) onto every basis function (Basis::product_function).
-void project_1d(const Basis1D& b, amdg_fn1d f, void* user, int d, int term, double* out);
+void project_1d(const Basis1D& b, const Fn1d& f, int d, int term, double* out);
 
 // ---- Lagrange interpolation path (hierarchical Lagrange of degree 3 or 4) ----
 constexpr int kMaxLagrPoints = 5;  // points per element and dimension (degree 4)

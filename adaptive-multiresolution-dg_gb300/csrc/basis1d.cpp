@@ -216,9 +216,9 @@ void build_oper1d(const Basis1D& b, Oper1D* out, bool want_u_v) {
     }
 }
 
-void project_1d(const Basis1D& b, amdg_fn1d f, void* user, int d, int term, double* out) {
+void project_1d(const Basis1D& b, const Fn1d& f, int d, int term, double* out) {
     const GaussRule& g = gauss10();
-    const int nb = b.num_basis(), np = b.k + 1, nq = g.n;
+    const int nb = b.num_basis(), np = b.k + 1, nq = g.n, n1 = nb / np;
     auto qpt = [&](int q, double a, double c) { return a + (g.x[q] + 1.0) * 0.5 * (c - a); };
     // Gauss sum over [a, c] of basis r times f, with f given at the rule's points
     auto panel = [&](int r, const double* fv, double a, double c) {
@@ -226,26 +226,34 @@ void project_1d(const Basis1D& b, amdg_fn1d f, void* user, int d, int term, doub
         for (int q = 0; q < nq; ++q) s += g.w[q] * (b.eval(r, 0, qpt(q, a, c), 0) * fv[q]);
         return s * (c - a) / 2.0;
     };
-    // f is evaluated once per quadrature point: the 16 uniform panels are shared
-    // by every coarse order, the two half-supports by the k+1 functions of an order
-    std::vector<double> fc(size_t(16) * nq), ff(size_t(2) * nq);
+    // f is evaluated once per quadrature point, all points in one call: the 16
+    // uniform panels shared by every coarse order, then the two half-supports of
+    // every finer order (shared by its k+1 functions)
+    std::vector<double> x, v;
     for (int i = 0; i < 16; ++i)
-        for (int q = 0; q < nq; ++q) fc[size_t(i) * nq + q] = f(qpt(q, i / 16.0, (i + 1) / 16.0), d, term, user);
-    for (int o = 0; o < nb / np; ++o) {
+        for (int q = 0; q < nq; ++q) x.push_back(qpt(q, i / 16.0, (i + 1) / 16.0));
+    for (int o = 0; o < n1; ++o) {
+        if (level_of_order(o) <= 4) continue;
+        const double a = supp_lo(o), c = supp_hi(o), m = 0.5 * (a + c);
+        for (int q = 0; q < nq; ++q) x.push_back(qpt(q, a, m));
+        for (int q = 0; q < nq; ++q) x.push_back(qpt(q, m, c));
+    }
+    v.resize(x.size());
+    f.eval(x.data(), int64_t(x.size()), d, term, v.data());
+    const double* fc = v.data();
+    const double* ff = v.data() + size_t(16) * nq;
+    for (int o = 0; o < n1; ++o) {
         if (level_of_order(o) <= 4) {
             // coarse levels: 16 uniform panels over [0,1] (Basis.cpp:38-59)
             for (int p = 0; p < np; ++p) {
                 double s = 0.0;
-                for (int i = 0; i < 16; ++i) s += panel(o * np + p, &fc[size_t(i) * nq], i / 16.0, (i + 1) / 16.0);
+                for (int i = 0; i < 16; ++i) s += panel(o * np + p, fc + size_t(i) * nq, i / 16.0, (i + 1) / 16.0);
                 out[o * np + p] = s;
             }
         } else {
             const double a = supp_lo(o), c = supp_hi(o), m = 0.5 * (a + c);
-            for (int q = 0; q < nq; ++q) {
-                ff[q] = f(qpt(q, a, m), d, term, user);
-                ff[nq + q] = f(qpt(q, m, c), d, term, user);
-            }
-            for (int p = 0; p < np; ++p) out[o * np + p] = panel(o * np + p, ff.data(), a, m) + panel(o * np + p, ff.data() + nq, m, c);
+            for (int p = 0; p < np; ++p) out[o * np + p] = panel(o * np + p, ff, a, m) + panel(o * np + p, ff + nq, m, c);
+            ff += size_t(2) * nq;
         }
     }
 }

@@ -77,12 +77,12 @@ amdg_status set_device(const amdg_context* ctx) {
 }
 
 // 1D separable projections of nterms terms: [term][d][nb1]
-amdg_status project_terms(const amdg_grid* g, int nterms, amdg_fn1d f, void* user, std::vector<double>* out) {
+amdg_status project_terms(const amdg_grid* g, int nterms, const Fn1d& f, std::vector<double>* out) {
     Basis1D b{g->host.k, g->host.nmax};
     const int nb1 = b.num_basis(), dim = g->host.dim;
     out->assign(size_t(nterms) * dim * nb1, 0.0);
     for (int t = 0; t < nterms; ++t)
-        for (int d = 0; d < dim; ++d) project_1d(b, f, user, d, t, out->data() + (size_t(t) * dim + d) * nb1);
+        for (int d = 0; d < dim; ++d) project_1d(b, f, d, t, out->data() + (size_t(t) * dim + d) * nb1);
     for (double v : *out)
         if (!std::isfinite(v)) return fail(AMDG_ERR_NONFINITE, "separable projection produced a non-finite value");
     return AMDG_OK;
@@ -685,12 +685,12 @@ amdg_status amdg_grid_coefficients_device(amdg_grid* g, double** device_ptr) {
     return AMDG_OK;
 }
 
-amdg_status amdg_grid_init_separable(amdg_grid* g, int nterms, amdg_fn1d f, void* user) {
-    AMDG_REQUIRE(g && f && nterms > 0, AMDG_ERR_ARG, "bad arguments");
+static amdg_status init_separable(amdg_grid* g, int nterms, const Fn1d& f) {
+    AMDG_REQUIRE(g && (f.f || f.fb) && nterms > 0, AMDG_ERR_ARG, "bad arguments");
     amdg_status s = set_device(g->ctx);
     if (s != AMDG_OK) return s;
     std::vector<double> coef;
-    if ((s = project_terms(g, nterms, f, user, &coef)) != AMDG_OK) return s;
+    if ((s = project_terms(g, nterms, f, &coef)) != AMDG_OK) return s;
     cudaStream_t st = stream_of(g->ctx);
     double* d_coef = nullptr;
     if ((s = upload(&d_coef, coef, st)) != AMDG_OK) return s;
@@ -704,12 +704,20 @@ amdg_status amdg_grid_init_separable(amdg_grid* g, int nterms, amdg_fn1d f, void
     return AMDG_OK;
 }
 
-amdg_status amdg_grid_init_separable_adaptive(amdg_grid* g, int nterms, amdg_fn1d f, void* user, double eps) {
-    AMDG_REQUIRE(g && f && nterms > 0, AMDG_ERR_ARG, "bad arguments");
+amdg_status amdg_grid_init_separable(amdg_grid* g, int nterms, amdg_fn1d f, void* user) {
+    return init_separable(g, nterms, Fn1d{f, nullptr, user});
+}
+
+amdg_status amdg_grid_init_separable_batch(amdg_grid* g, int nterms, amdg_fn1d_batch f, void* user) {
+    return init_separable(g, nterms, Fn1d{nullptr, f, user});
+}
+
+static amdg_status init_separable_adaptive(amdg_grid* g, int nterms, const Fn1d& f, double eps) {
+    AMDG_REQUIRE(g && (f.f || f.fb) && nterms > 0, AMDG_ERR_ARG, "bad arguments");
     amdg_status s = set_device(g->ctx);
     if (s != AMDG_OK) return s;
     std::vector<double> coef;
-    if ((s = project_terms(g, nterms, f, user, &coef)) != AMDG_OK) return s;
+    if ((s = project_terms(g, nterms, f, &coef)) != AMDG_OK) return s;
     // refine every leaf whose projected block exceeds eps, fill holes, repeat
     // until nothing changes (DGAdapt::refine_init_separable_scalar_sum)
     // norms depend only on the element, so each is computed once; the element
@@ -744,6 +752,15 @@ amdg_status amdg_grid_init_separable_adaptive(amdg_grid* g, int nterms, amdg_fn1
     cudaFree(d_coef);
     if (e != cudaSuccess) return fail(AMDG_ERR_CUDA, std::string("init_separable: ") + cudaGetErrorString(e));
     return AMDG_OK;
+}
+
+amdg_status amdg_grid_init_separable_adaptive(amdg_grid* g, int nterms, amdg_fn1d f, void* user, double eps) {
+    return init_separable_adaptive(g, nterms, Fn1d{f, nullptr, user}, eps);
+}
+
+amdg_status amdg_grid_init_separable_adaptive_batch(amdg_grid* g, int nterms, amdg_fn1d_batch f, void* user,
+                                                    double eps) {
+    return init_separable_adaptive(g, nterms, Fn1d{nullptr, f, user}, eps);
 }
 
 amdg_status amdg_grid_refine(amdg_grid* g, const double* d_indicator, double eps, int64_t* num_elements) {
@@ -827,11 +844,11 @@ amdg_status amdg_grid_l2_error_separable(const amdg_grid* g, amdg_fn1d f, void* 
     return amdg_grid_l2_error_separable_sum(g, 1, f, user, l2_norm_exact, out);
 }
 
-amdg_status amdg_grid_l2_error_separable_sum(const amdg_grid* g, int nterms, amdg_fn1d f, void* user,
-                                             double l2_norm_exact, double* out) {
-    AMDG_REQUIRE(g && f && out && nterms > 0, AMDG_ERR_ARG, "bad arguments");
+static amdg_status l2_error_separable_sum(const amdg_grid* g, int nterms, const Fn1d& f, double l2_norm_exact,
+                                          double* out) {
+    AMDG_REQUIRE(g && (f.f || f.fb) && out && nterms > 0, AMDG_ERR_ARG, "bad arguments");
     std::vector<double> coef;
-    amdg_status s = project_terms(g, nterms, f, user, &coef);
+    amdg_status s = project_terms(g, nterms, f, &coef);
     if (s != AMDG_OK) return s;
     cudaStream_t st = stream_of(g->ctx);
     double* d_coef = nullptr;
@@ -843,6 +860,16 @@ amdg_status amdg_grid_l2_error_separable_sum(const amdg_grid* g, int nterms, amd
     const double err2 = l2_norm_exact * l2_norm_exact + r;
     *out = std::sqrt(err2 > 0.0 ? err2 : 0.0);
     return AMDG_OK;
+}
+
+amdg_status amdg_grid_l2_error_separable_sum(const amdg_grid* g, int nterms, amdg_fn1d f, void* user,
+                                             double l2_norm_exact, double* out) {
+    return l2_error_separable_sum(g, nterms, Fn1d{f, nullptr, user}, l2_norm_exact, out);
+}
+
+amdg_status amdg_grid_l2_error_separable_sum_batch(const amdg_grid* g, int nterms, amdg_fn1d_batch f, void* user,
+                                                   double l2_norm_exact, double* out) {
+    return l2_error_separable_sum(g, nterms, Fn1d{nullptr, f, user}, l2_norm_exact, out);
 }
 
 // ---- linear operator ---------------------------------------------------------

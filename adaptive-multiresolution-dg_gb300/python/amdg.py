@@ -23,6 +23,7 @@ STATUS = {0: "ok", 1: "invalid argument", 2: "capacity exceeded", 3: "non-finite
           5: "CUDA error", 6: "invalid state", 7: "out of memory", 8: "I/O error", 9: "bad checkpoint"}
 
 FN1D = C.CFUNCTYPE(C.c_double, C.c_double, C.c_int, C.c_int, C.c_void_p)
+FN1D_BATCH = C.CFUNCTYPE(None, C.POINTER(C.c_double), C.c_int64, C.c_int, C.c_int, C.POINTER(C.c_double), C.c_void_p)
 
 
 class AmdgError(RuntimeError):
@@ -92,6 +93,9 @@ def load():
         "amdg_mlp_train": ([vp, vp, vp, i64, i32, i32, C.c_float, C.c_uint64, C.POINTER(dbl)], i32),
         "amdg_grid_create_ex": ([vp, i32, i32, i32, i32, i32, pp], i32),
         "amdg_grid_init_separable_adaptive": ([vp, i32, FN1D, vp, dbl], i32),
+        "amdg_grid_init_separable_batch": ([vp, i32, FN1D_BATCH, vp], i32),
+        "amdg_grid_init_separable_adaptive_batch": ([vp, i32, FN1D_BATCH, vp, dbl], i32),
+        "amdg_grid_l2_error_separable_sum_batch": ([vp, i32, FN1D_BATCH, vp, dbl, C.POINTER(dbl)], i32),
         "amdg_grid_refine": ([vp, vp, dbl, C.POINTER(i64)], i32),
         "amdg_grid_coarsen": ([vp, dbl, C.POINTER(i64)], i32),
         "amdg_grid_version": ([vp, C.POINTER(i64)], i32),
@@ -176,6 +180,14 @@ def _fn1d(funcs):
     def cb(x, d, term, _user):
         return float(funcs[term](x, d))
     return FN1D(cb)
+
+
+def _fn1d_batch(funcs):
+    """Callback for factors that take a numpy array of points: one call per dimension and term."""
+    def cb(x, n, d, term, out, _user):
+        xs = np.ctypeslib.as_array(x, shape=(n,))
+        np.ctypeslib.as_array(out, shape=(n,))[:] = funcs[term](xs, d)
+    return FN1D_BATCH(cb)
 
 
 class Context:
@@ -265,9 +277,16 @@ class Grid:
         """IO::output_element_level_support: "level xl xr " per dimension, one element per line."""
         _ck(load().amdg_grid_write_level_support(self._h, os.fsencode(path)), "grid_write_level_support")
 
-    def init_separable_adaptive(self, funcs, eps: float):
-        cb = _fn1d(funcs)
-        _ck(load().amdg_grid_init_separable_adaptive(self._h, len(funcs), cb, None, eps), "grid_init_separable_adaptive")
+    def init_separable_adaptive(self, funcs, eps: float, vectorized: bool = False):
+        """vectorized: the factors take a numpy array of points (one callback per dimension and term)."""
+        if vectorized:
+            cb = _fn1d_batch(funcs)
+            _ck(load().amdg_grid_init_separable_adaptive_batch(self._h, len(funcs), cb, None, eps),
+                "grid_init_separable_adaptive_batch")
+        else:
+            cb = _fn1d(funcs)
+            _ck(load().amdg_grid_init_separable_adaptive(self._h, len(funcs), cb, None, eps),
+                "grid_init_separable_adaptive")
         self._refresh()
 
     def refine(self, eps: float, d_indicator: int | None = None):
@@ -316,20 +335,29 @@ class Grid:
         _ck(load().amdg_grid_coefficients_device(self._h, C.byref(p)), "grid_coefficients_device")
         return p.value
 
-    def init_separable(self, funcs):
-        cb = _fn1d(funcs)
-        _ck(load().amdg_grid_init_separable(self._h, len(funcs), cb, None), "grid_init_separable")
+    def init_separable(self, funcs, vectorized: bool = False):
+        if vectorized:
+            cb = _fn1d_batch(funcs)
+            _ck(load().amdg_grid_init_separable_batch(self._h, len(funcs), cb, None), "grid_init_separable_batch")
+        else:
+            cb = _fn1d(funcs)
+            _ck(load().amdg_grid_init_separable(self._h, len(funcs), cb, None), "grid_init_separable")
 
     def l2_norm_sq(self) -> float:
         r = C.c_double()
         _ck(load().amdg_grid_l2_norm(self._h, C.byref(r)), "grid_l2_norm")
         return r.value
 
-    def l2_error_separable_sum(self, funcs, l2_norm_exact: float) -> float:
-        cb = _fn1d(funcs)
+    def l2_error_separable_sum(self, funcs, l2_norm_exact: float, vectorized: bool = False) -> float:
         r = C.c_double()
-        _ck(load().amdg_grid_l2_error_separable_sum(self._h, len(funcs), cb, None, l2_norm_exact, C.byref(r)),
-            "grid_l2_error_separable_sum")
+        if vectorized:
+            cb = _fn1d_batch(funcs)
+            _ck(load().amdg_grid_l2_error_separable_sum_batch(self._h, len(funcs), cb, None, l2_norm_exact,
+                                                              C.byref(r)), "grid_l2_error_separable_sum_batch")
+        else:
+            cb = _fn1d(funcs)
+            _ck(load().amdg_grid_l2_error_separable_sum(self._h, len(funcs), cb, None, l2_norm_exact, C.byref(r)),
+                "grid_l2_error_separable_sum")
         return r.value
 
     def set_velocity(self, v: np.ndarray):

@@ -577,7 +577,8 @@ def bench_batched(ctx, stream, args):
     grids = []
     for w in work:
         g = amdg.Grid(ctx, 3, 8, 2, level_init=2)
-        g.init_separable_adaptive(O.gaussian_bump_terms(w["centers"], w["widths"], w["amplitudes"]), args.batch_eps)
+        g.init_separable_adaptive(O.gaussian_bump_terms(w["centers"], w["widths"], w["amplitudes"], vectorized=True),
+                                  args.batch_eps, vectorized=True)
         grids.append(g)
     init_s = time.perf_counter() - t0
     sizes = [g.num_elements for g in grids]
@@ -611,15 +612,16 @@ def bench_batched(ctx, stream, args):
             w = work[i]
             batch.store(i)
             shift = [v * dts[i] * nsteps for v in w["velocity"]]
-            exact = O.gaussian_bump_terms(w["centers"], w["widths"], w["amplitudes"], shift=shift)
+            exact = O.gaussian_bump_terms(w["centers"], w["widths"], w["amplitudes"], shift=shift, vectorized=True)
             norm = O.gaussian_bump_norm(w["centers"], w["widths"], w["amplitudes"])
-            errs.append(grids[i].l2_error_separable_sum(exact, norm) / norm)
+            errs.append(grids[i].l2_error_separable_sum(exact, norm, vectorized=True) / norm)
         out[name]["rel_l2_error_sampled"] = {"median": float(np.median(errs)), "max": float(np.max(errs)),
                                              "solves_sampled": len(errs)}
         batch.close()
         # restore the initial coefficients for the next precision
         for g, w in zip(grids, work):
-            g.init_separable(O.gaussian_bump_terms(w["centers"], w["widths"], w["amplitudes"]))
+            g.init_separable(O.gaussian_bump_terms(w["centers"], w["widths"], w["amplitudes"], vectorized=True),
+                             vectorized=True)
     for g in grids:
         g.close()
     return out

@@ -64,6 +64,9 @@ typedef struct amdg_wave_op amdg_wave_op;
 /* Separable 1D factor g_d(x) of term `term` (the std::function<double(double,int)>
  * the reference takes, DGAdapt.h:17-38). */
 typedef double (*amdg_fn1d)(double x, int d, int term, void* user);
+/* The same factor at n points at once: out[i] = g_d(x[i]) for term `term` (one call per
+ * dimension and term, for callers whose functions are cheap to evaluate in bulk). */
+typedef void (*amdg_fn1d_batch)(const double* x, int64_t n, int d, int term, double* out, void* user);
 
 /* ---- library / context ------------------------------------------------- */
 int amdg_abi_version(void);
@@ -144,6 +147,13 @@ amdg_status amdg_grid_init_separable(amdg_grid* g, int nterms, amdg_fn1d f, void
  * 850-894): every leaf whose projected block has norm > eps gets its children,
  * holes are filled, until nothing changes; then the coefficients are set. */
 amdg_status amdg_grid_init_separable_adaptive(amdg_grid* g, int nterms, amdg_fn1d f, void* user, double eps);
+/* amdg_grid_init_separable / _adaptive / amdg_grid_l2_error_separable_sum with the factors given
+ * in bulk (same points, same arithmetic). */
+amdg_status amdg_grid_init_separable_batch(amdg_grid* g, int nterms, amdg_fn1d_batch f, void* user);
+amdg_status amdg_grid_init_separable_adaptive_batch(amdg_grid* g, int nterms, amdg_fn1d_batch f, void* user,
+                                                    double eps);
+amdg_status amdg_grid_l2_error_separable_sum_batch(const amdg_grid* g, int nterms, amdg_fn1d_batch f, void* user,
+                                                   double l2_norm_exact, double* out);
 /* DGAdapt::refine (DGAdapt.cpp:371-404): one pass -- leaves whose indicator
  * (the 2-norm of the element block of d_indicator, or of the grid's own
  * coefficients when NULL; DGAdapt::indicator_norm :1018-1030) exceeds eps get

@@ -550,17 +550,22 @@ def wave_adaptive_run(dim, n_init, nmax, eps, eta, sigma, cfl, speed, steps, k=2
 # Batched-serving workload: sums of periodic Gaussian bumps (separable terms)
 # ---------------------------------------------------------------------------
 
-def gaussian_bump_terms(centers, widths, amplitudes, shift=None):
+def gaussian_bump_terms(centers, widths, amplitudes, shift=None, vectorized=False):
     """Separable terms of sum_g a_g prod_d G(x_d; c_gd, w_g), G(x) = sum_{m=-1,0,1} exp(-((x - c + m)/w)^2);
-    shift (dim,) translates every centre (periodic)."""
+    shift (dim,) translates every centre (periodic).  vectorized: the factors take numpy arrays."""
     terms = []
     dim = len(centers[0])
     for c, w, a in zip(centers, widths, amplitudes):
         cc = [(c[d] + (shift[d] if shift is not None else 0.0)) % 1.0 for d in range(dim)]
 
-        def f(x, d, cc=cc, w=w, a=a):
-            v = sum(math.exp(-((x - cc[d] + m) / w) ** 2) for m in (-1.0, 0.0, 1.0))
-            return a * v if d == 0 else v
+        if vectorized:
+            def f(x, d, cc=cc, w=w, a=a):
+                v = sum(np.exp(-((x - cc[d] + m) / w) ** 2) for m in (-1.0, 0.0, 1.0))
+                return a * v if d == 0 else v
+        else:
+            def f(x, d, cc=cc, w=w, a=a):
+                v = sum(math.exp(-((x - cc[d] + m) / w) ** 2) for m in (-1.0, 0.0, 1.0))
+                return a * v if d == 0 else v
 
         terms.append(f)
     return terms

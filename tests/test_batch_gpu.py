@@ -103,3 +103,27 @@ def test_batch_tiles_agree_and_autotuner_picks_one(ctx):
         assert np.array_equal(results[(prec, 512)], results[(prec, 256)])
     for g in grids:
         g.close()
+
+
+def test_bulk_factor_callbacks_match_pointwise(ctx):
+    """The bulk-callback entry points evaluate the same points in the same order: the adaptive
+    initialisation gives the same element set and coefficients as the pointwise one (numpy's and
+    the C library's exp may differ in the last bit, hence 1e-13), and the split L2 errors agree."""
+    work = O.batched_workload(2, seed=5)
+    for w in work:
+        a = amdg.Grid(ctx, 3, 5, 2, level_init=2)
+        b = amdg.Grid(ctx, 3, 5, 2, level_init=2)
+        a.init_separable_adaptive(O.gaussian_bump_terms(w["centers"], w["widths"], w["amplitudes"]), 1e-3)
+        b.init_separable_adaptive(O.gaussian_bump_terms(w["centers"], w["widths"], w["amplitudes"], vectorized=True),
+                                  1e-3, vectorized=True)
+        for x, y in zip(a.elements(), b.elements()):
+            assert np.array_equal(x, y)
+        ua, ub = a.coefficients(), b.coefficients()
+        assert np.abs(ua - ub).max() <= 1e-13 * np.abs(ua).max()
+        norm = O.gaussian_bump_norm(w["centers"], w["widths"], w["amplitudes"])
+        ea = a.l2_error_separable_sum(O.gaussian_bump_terms(w["centers"], w["widths"], w["amplitudes"]), norm)
+        eb = b.l2_error_separable_sum(O.gaussian_bump_terms(w["centers"], w["widths"], w["amplitudes"],
+                                                            vectorized=True), norm, vectorized=True)
+        assert abs(ea - eb) <= 1e-9 * norm
+        a.close()
+        b.close()
