@@ -270,9 +270,13 @@ amdg_status check_copy_waits(amdg_linear_op* op) {
     return fail(AMDG_ERR_TIMEOUT, "linear stage: a bulk copy did not complete within its wait limit; results are invalid");
 }
 
-amdg_status rk3_steps_device(amdg_linear_op* op, double dt, int nsteps, amdg_precision prec) {
+// nsteps SSP-RK3 steps of the state `u` (the grid's own coefficients when null); check:
+// read the bulk-copy error flag back at the end (synchronises the stream)
+amdg_status rk3_steps_device(amdg_linear_op* op, double dt, int nsteps, amdg_precision prec, double* u = nullptr,
+                             bool check = true) {
     amdg_grid* g = op->grid;
     cudaStream_t st = stream_of(g->ctx);
+    if (!u) u = g->d_u;
     LinearLaunch L = linear_launch(op, prec);
     if (prec == AMDG_PREC_MIXED) {
         // the stage vectors live as FP32 (hi, lo) pairs for the whole call:
@@ -280,7 +284,7 @@ amdg_status rk3_steps_device(amdg_linear_op* op, double dt, int nsteps, amdg_pre
         float* hi[3] = {op->d_shadow, op->d_shadow + op->capacity, op->d_shadow + 2 * op->capacity};
         float* lo[3] = {op->d_lo, op->d_lo + op->capacity, op->d_lo + 2 * op->capacity};
         if (nsteps == 0) return AMDG_OK;
-        AMDG_CK(launch_split(g->d_u, hi[0], lo[0], g->dof, st));
+        AMDG_CK(launch_split(u, hi[0], lo[0], g->dof, st));
         g->ctx->launches++;
         const int in_i[3] = {0, 1, 2}, out_i[3] = {1, 2, 0};
         for (int s = 0; s < nsteps; ++s) {
@@ -301,17 +305,17 @@ amdg_status rk3_steps_device(amdg_linear_op* op, double dt, int nsteps, amdg_pre
                 g->ctx->launches++;
             }
         }
-        AMDG_CK(launch_merge(hi[0], lo[0], g->d_u, g->dof, st));
+        AMDG_CK(launch_merge(hi[0], lo[0], u, g->dof, st));
         g->ctx->launches++;
-        return L.variant == 2 ? check_copy_waits(op) : AMDG_OK;
+        return L.variant == 2 && check ? check_copy_waits(op) : AMDG_OK;
     }
     for (int s = 0; s < nsteps; ++s) {
         // u1 = u + dt L(u); u2 = 3/4 u + 1/4 (u1 + dt L(u1)); u = 1/3 u + 2/3 (u2 + dt L(u2))
-        double* in[3] = {g->d_u, op->d_u1, op->d_u2};
-        double* outp[3] = {op->d_u1, op->d_u2, g->d_u};
+        double* in[3] = {u, op->d_u1, op->d_u2};
+        double* outp[3] = {op->d_u1, op->d_u2, u};
         for (int stage = 0; stage < 3; ++stage) {
             L.us = in[stage];
-            L.un = g->d_u;
+            L.un = u;
             L.out = outp[stage];
             AMDG_CK(launch_linear(L, false, rk3_stage_coef(stage, dt), st));
             g->ctx->launches++;
@@ -910,6 +914,12 @@ amdg_status amdg_linear_destroy(amdg_linear_op* op) {
     cudaFree(op->d_err);
     cudaFree(op->d_shadow);
     cudaFree(op->d_lo);
+    cudaFree(op->d_io[0]);
+    cudaFree(op->d_io[1]);
+    for (void* e : op->io_event)
+        if (e) cudaEventDestroy(static_cast<cudaEvent_t>(e));
+    for (void* c : op->io_stream)
+        if (c) cudaStreamDestroy(static_cast<cudaStream_t>(c));
     delete op;
     return AMDG_OK;
 }
@@ -987,6 +997,74 @@ amdg_status amdg_rk3ssp_steps_host(amdg_linear_op* op, double dt, int nsteps, do
     AMDG_CK(cudaMemcpyAsync(host_u, g->d_u, bytes, cudaMemcpyDeviceToHost, st));
     AMDG_CK(cudaStreamSynchronize(st));
     return AMDG_OK;
+}
+
+amdg_status amdg_rk3ssp_serve_host(amdg_linear_op* op, double dt, int nsteps, amdg_precision prec, int nreq,
+                                   const double* const* host_in, double* const* host_out) {
+    AMDG_REQUIRE(op && nsteps >= 0 && nreq >= 0 && std::isfinite(dt) && (nreq == 0 || (host_in && host_out)),
+                 AMDG_ERR_ARG, "bad arguments");
+    AMDG_REQUIRE(prec == AMDG_PREC_FP64 || prec == AMDG_PREC_MIXED, AMDG_ERR_ARG, "bad precision");
+    for (int r = 0; r < nreq; ++r) AMDG_REQUIRE(host_in[r] && host_out[r], AMDG_ERR_ARG, "null request buffer");
+    amdg_grid* g = op->grid;
+    amdg_status s = set_device(g->ctx);
+    if (s != AMDG_OK) return s;
+    if ((s = linear_sync(op)) != AMDG_OK) return s;
+    const size_t bytes = size_t(g->dof) * sizeof(double);
+    if (!op->d_io[0] || op->io_capacity < g->dof) {
+        cudaFree(op->d_io[0]);
+        cudaFree(op->d_io[1]);
+        op->d_io[0] = op->d_io[1] = nullptr;
+        op->io_capacity = 0;
+        if ((s = dev_alloc(&op->d_io[0], size_t(g->dof))) != AMDG_OK ||
+            (s = dev_alloc(&op->d_io[1], size_t(g->dof))) != AMDG_OK)
+            return s;
+        op->io_capacity = g->dof;
+    }
+    if (!op->io_stream[0]) {
+        for (int i = 0; i < 2; ++i) {
+            cudaStream_t c = nullptr;
+            AMDG_CK(cudaStreamCreateWithFlags(&c, cudaStreamNonBlocking));
+            op->io_stream[i] = c;
+        }
+        for (int i = 0; i < 6; ++i) {
+            cudaEvent_t e = nullptr;
+            AMDG_CK(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+            op->io_event[i] = e;
+        }
+    }
+    cudaStream_t st = stream_of(g->ctx);
+    cudaStream_t in_st = static_cast<cudaStream_t>(op->io_stream[0]);
+    cudaStream_t out_st = static_cast<cudaStream_t>(op->io_stream[1]);
+    // per buffer b: copied in, stepped, copied out
+    cudaEvent_t in_done[2] = {static_cast<cudaEvent_t>(op->io_event[0]), static_cast<cudaEvent_t>(op->io_event[1])};
+    cudaEvent_t stepped[2] = {static_cast<cudaEvent_t>(op->io_event[2]), static_cast<cudaEvent_t>(op->io_event[3])};
+    cudaEvent_t out_done[2] = {static_cast<cudaEvent_t>(op->io_event[4]), static_cast<cudaEvent_t>(op->io_event[5])};
+    // earlier work on the context stream (the grid's state, the operator's tables) comes first
+    AMDG_CK(cudaEventRecord(stepped[0], st));
+    AMDG_CK(cudaStreamWaitEvent(in_st, stepped[0], 0));
+    auto copy_in = [&](int r) -> amdg_status {
+        const int b = r & 1;
+        if (r >= 2) AMDG_CK(cudaStreamWaitEvent(in_st, out_done[b], 0));  // buffer b's previous result is out
+        AMDG_CK(cudaMemcpyAsync(op->d_io[b], host_in[r], bytes, cudaMemcpyHostToDevice, in_st));
+        AMDG_CK(cudaEventRecord(in_done[b], in_st));
+        return AMDG_OK;
+    };
+    // request r + 1 is copied in while request r is stepped and request r - 1 copied out
+    if (nreq > 0 && (s = copy_in(0)) != AMDG_OK) return s;
+    for (int r = 0; r < nreq; ++r) {
+        const int b = r & 1;
+        if (r + 1 < nreq && (s = copy_in(r + 1)) != AMDG_OK) return s;
+        AMDG_CK(cudaStreamWaitEvent(st, in_done[b], 0));
+        if ((s = rk3_steps_device(op, dt, nsteps, prec, op->d_io[b], false)) != AMDG_OK) return s;
+        AMDG_CK(cudaEventRecord(stepped[b], st));
+        AMDG_CK(cudaStreamWaitEvent(out_st, stepped[b], 0));
+        AMDG_CK(cudaMemcpyAsync(host_out[r], op->d_io[b], bytes, cudaMemcpyDeviceToHost, out_st));
+        AMDG_CK(cudaEventRecord(out_done[b], out_st));
+    }
+    AMDG_CK(cudaStreamSynchronize(out_st));
+    AMDG_CK(cudaStreamSynchronize(in_st));
+    AMDG_CK(cudaStreamSynchronize(st));
+    return linear_launch(op, prec).variant == 2 ? check_copy_waits(op) : AMDG_OK;
 }
 
 amdg_status amdg_rk3_stage_update(amdg_context* ctx, int stage, double dt, const double* d_un, double* d_u,

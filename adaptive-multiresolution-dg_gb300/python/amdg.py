@@ -76,6 +76,7 @@ def load():
         "amdg_linear_set_variant": ([vp, i32, i32], i32),
         "amdg_rk3ssp_steps": ([vp, dbl, i32, i32], i32),
         "amdg_rk3ssp_steps_host": ([vp, dbl, i32, vp, i32], i32),
+        "amdg_rk3ssp_serve_host": ([vp, dbl, i32, i32, i32, vp, vp], i32),
         "amdg_rk3_stage_update": ([vp, i32, dbl, vp, vp, vp, i64], i32),
         "amdg_rk3ssp_steps_noalloc": ([vp, vp, dbl, i32, i32], i32),
         "amdg_burgers_create": ([vp, vp, pp], i32),
@@ -434,6 +435,17 @@ class LinearOperator:
     def rk3_steps_host(self, u: np.ndarray, dt: float, nsteps: int, prec: int = FP64):
         assert u.dtype == np.float64 and u.flags.c_contiguous and u.size == self.grid.dof
         _ck(load().amdg_rk3ssp_steps_host(self._h, dt, nsteps, _ptr(u), prec), "rk3ssp_steps_host")
+
+    def serve_host(self, inputs, outputs, dt: float, nsteps: int, prec: int = FP64):
+        """Independent requests: inputs[r] (host, dof doubles) stepped into outputs[r], copies of
+        neighbouring requests overlapped with the steps (pin the buffers for overlap)."""
+        assert len(inputs) == len(outputs)
+        for a in list(inputs) + list(outputs):
+            assert a.dtype == np.float64 and a.flags.c_contiguous and a.size == self.grid.dof
+        n = len(inputs)
+        pin = (C.c_void_p * n)(*[a.ctypes.data for a in inputs])
+        pout = (C.c_void_p * n)(*[a.ctypes.data for a in outputs])
+        _ck(load().amdg_rk3ssp_serve_host(self._h, dt, nsteps, prec, n, pin, pout), "rk3ssp_serve_host")
 
     def close(self):
         if self._h:

@@ -231,6 +231,13 @@ amdg_status amdg_rk3ssp_steps(amdg_linear_op* op, double dt, int nsteps, amdg_pr
  * when it keeps Element::ucoe_alpt on the host (ODESolver::init/final,
  * ODESolver.cpp:25-60). */
 amdg_status amdg_rk3ssp_steps_host(amdg_linear_op* op, double dt, int nsteps, double* host_u, amdg_precision prec);
+/* Serving form of amdg_rk3ssp_steps_host, no reference counterpart: nreq independent requests
+ * on the operator's grid, request r stepped from host_in[r] (dof doubles) into host_out[r]
+ * (host_out[r] may equal host_in[r]).  Request r + 1 is copied in and request r - 1 copied out
+ * while request r is stepped (two device states, one copy stream per direction); pinned host
+ * buffers let the copies overlap.  The grid's own coefficients are left unchanged. */
+amdg_status amdg_rk3ssp_serve_host(amdg_linear_op* op, double dt, int nsteps, amdg_precision prec, int nreq,
+                                   const double* const* host_in, double* const* host_out);
 
 /* Allocation-free variant of amdg_rk3ssp_steps, with no counterpart in the
  * reference: for callers that cannot call cudaMalloc (code running during CUDA

@@ -217,3 +217,29 @@ def test_kernel_variants_agree_on_mixed_steps(ctx):
         op.set_variant(amdg.FP64, 2)
     op.close()
     g.close()
+
+
+@pytest.mark.parametrize("prec", [amdg.FP64, amdg.MIXED])
+def test_serve_host_matches_device_steps(ctx, prec):
+    """Pipelined host requests: every result bitwise equal to the same steps on the device state,
+    the grid's own state untouched, and an in-place request (output = input) allowed."""
+    g = amdg.Grid(ctx, 4, 6, 2)
+    op = amdg.LinearOperator(g, [1.0, -0.5, 0.25, 0.75])
+    rng = np.random.default_rng(9)
+    base = rng.standard_normal(g.dof)
+    g.set_coefficients(base)
+    inputs = [rng.standard_normal(g.dof) for _ in range(5)]
+    outputs = [np.zeros(g.dof) for _ in range(4)]
+    inplace = inputs[4].copy()
+    dt = 1e-3
+    op.serve_host(inputs[:4] + [inplace], outputs + [inplace], dt, 2, prec)
+    assert np.array_equal(g.coefficients(), base)
+    for r in range(5):
+        g.set_coefficients(inputs[r])
+        op.rk3_steps(dt, 2, prec)
+        ctx.synchronize()
+        want = g.coefficients()
+        got = outputs[r] if r < 4 else inplace
+        assert np.array_equal(got, want), f"request {r}"
+    op.close()
+    g.close()
