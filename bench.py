@@ -211,7 +211,7 @@ def run_ours(args):
     g.set_coefficients(u0)
     op.rk3_steps(dt, 1, amdg.MIXED)
     ctx.synchronize()
-    serve_ok = bool(np.array_equal(outs[(args.steps - 1) % 2], g.coefficients()))
+    serve_ok = bool(np.array_equal(outs[(args.steps - 1) % 2], g.coefficients().reshape(-1)))
     host = ins[0]
     op.rk3_steps_host(host, dt, 1, amdg.MIXED)  # warm-up
     host[:] = u0
