@@ -256,6 +256,7 @@ LinearLaunch linear_launch(const amdg_linear_op* op, amdg_precision prec = AMDG_
     L.blocks64p = op->d_blocks64p;
     L.blocks32p = op->d_blocks32p;
     L.err = op->d_err;
+    L.tma_cfg = op->tma_cfg;
     return L;
 }
 
@@ -342,29 +343,41 @@ amdg_status autotune_linear(amdg_linear_op* op) {
     for (int p = 0; p < 2; ++p) {
         float best = 1e30f;
         for (int v = 0; v < (p == 1 && tma ? 3 : 2); ++v) {
-            LinearLaunch L = linear_launch(op);
-            L.variant = v;
-            const StageCoef rk{1, 0.0, 1.0, 0.0};
-            L.us = g->d_u;
-            L.un = g->d_u;
-            L.out = op->d_u1;
-            if (p == 1) {  // the mixed stage as rk3_steps_device runs it
-                L.us_shadow = op->d_shadow;
-                L.df = df_stage(rk);
-                L.df.us_hi = L.df.un_hi = op->d_shadow;
-                L.df.us_lo = L.df.un_lo = op->d_lo;
-                L.df.out_hi = op->d_shadow + op->capacity;
-                L.df.out_lo = op->d_lo + op->capacity;
+            // the bulk-copy variant: time each of its configurations, keep the fastest
+            const int ncfg = v == 2 ? kTmaConfigs : 1;
+            float best_cfg = 1e30f;
+            for (int cfg = 0; cfg < ncfg; ++cfg) {
+                if (v == 2 && !linear_tma_supported(dim, np, cfg)) continue;
+                LinearLaunch L = linear_launch(op);
+                L.variant = v;
+                L.tma_cfg = cfg;
+                const StageCoef rk{1, 0.0, 1.0, 0.0};
+                L.us = g->d_u;
+                L.un = g->d_u;
+                L.out = op->d_u1;
+                if (p == 1) {  // the mixed stage as rk3_steps_device runs it
+                    L.us_shadow = op->d_shadow;
+                    L.df = df_stage(rk);
+                    L.df.us_hi = L.df.un_hi = op->d_shadow;
+                    L.df.us_lo = L.df.un_lo = op->d_lo;
+                    L.df.out_hi = op->d_shadow + op->capacity;
+                    L.df.out_lo = op->d_lo + op->capacity;
+                }
+                AMDG_CK(launch_linear(L, p == 1, rk, st));  // warm-up
+                AMDG_CK(cudaEventRecord(a, st));
+                for (int r = 0; r < 3; ++r) AMDG_CK(launch_linear(L, p == 1, rk, st));
+                AMDG_CK(cudaEventRecord(b, st));
+                AMDG_CK(cudaEventSynchronize(b));
+                float ms = 0;
+                AMDG_CK(cudaEventElapsedTime(&ms, a, b));
+                if (v == 2) op->tma_ms[cfg] = ms / 3;
+                if (ms < best_cfg) {
+                    best_cfg = ms;
+                    if (v == 2) op->tma_cfg = cfg;
+                }
             }
-            AMDG_CK(launch_linear(L, p == 1, rk, st));  // warm-up
-            AMDG_CK(cudaEventRecord(a, st));
-            for (int r = 0; r < 3; ++r) AMDG_CK(launch_linear(L, p == 1, rk, st));
-            AMDG_CK(cudaEventRecord(b, st));
-            AMDG_CK(cudaEventSynchronize(b));
-            float ms = 0;
-            AMDG_CK(cudaEventElapsedTime(&ms, a, b));
-            op->variant_ms[p][v] = ms / 3;
-            if (ms < best) { best = ms; op->variant[p] = v; }
+            op->variant_ms[p][v] = best_cfg / 3;
+            if (best_cfg < best) { best = best_cfg; op->variant[p] = v; }
         }
     }
     cudaEventDestroy(a);
@@ -941,6 +954,22 @@ amdg_status amdg_linear_set_variant(amdg_linear_op* op, amdg_precision prec, int
                      (variant == 2 && prec == AMDG_PREC_MIXED && linear_tma_supported(dim, np)),
                  AMDG_ERR_ARG, "unsupported kernel variant");
     op->variant[prec == AMDG_PREC_MIXED ? 1 : 0] = variant;
+    return AMDG_OK;
+}
+
+amdg_status amdg_linear_copy_config(const amdg_linear_op* op, int* config, float* stage_ms) {
+    AMDG_REQUIRE(op, AMDG_ERR_ARG, "op is null");
+    if (config) *config = op->tma_cfg;
+    if (stage_ms)
+        for (int c = 0; c < kTmaConfigs; ++c) stage_ms[c] = op->tma_ms[c];
+    return AMDG_OK;
+}
+
+amdg_status amdg_linear_set_copy_config(amdg_linear_op* op, int config) {
+    AMDG_REQUIRE(op, AMDG_ERR_ARG, "op is null");
+    const int dim = op->grid->host.dim, np = op->grid->host.k + 1;
+    AMDG_REQUIRE(linear_tma_supported(dim, np, config), AMDG_ERR_ARG, "unsupported bulk-copy configuration");
+    op->tma_cfg = config;
     return AMDG_OK;
 }
 

@@ -250,8 +250,13 @@ static cudaError_t launch_col_t(const LinearLaunch& L, const T* blocks, const X*
 // leading floats.  Every wait is bounded (kSpinLimit polls) and agreed on by
 // the whole warp; on a timeout the kernel sets *err, waits (bounded) for its
 // copies still in flight and returns without writing.
-constexpr int kRing = 3;
+// Configurations (LinearLaunch::tma_cfg, picked by the autotuner): RING slots,
+// and whether the 1D operator block rides in the slot as a second bulk copy
+// (LDG false) or is read by every lane from the L1-resident table, issued
+// before the wait on the slot (LDG true, one bulk copy per neighbour).
 constexpr uint32_t kSpinLimit = 1u << 22;
+constexpr int kTmaRing[3] = {3, 3, 6};
+constexpr bool kTmaLdg[3] = {false, true, true};
 
 __device__ __forceinline__ uint32_t smem_u32(const void* p) { return uint32_t(__cvta_generic_to_shared(p)); }
 
@@ -289,7 +294,7 @@ __device__ __forceinline__ void bulk_copy_g2s(void* dst, const void* src, uint32
                  : "memory");
 }
 
-template <int D, int NP>
+template <int D, int NP, int kRing, bool LDG>
 __global__ void __launch_bounds__(32) linear_tma_kernel(const float* __restrict__ xs, const int32_t* __restrict__ row_ptr,
                                                         const int2* __restrict__ pairs, const float* __restrict__ blocks,
                                                         int nblocks, int64_t num_elements, DFState df, int* err) {
@@ -298,11 +303,12 @@ __global__ void __launch_bounds__(32) linear_tma_kernel(const float* __restrict_
     constexpr int CPT = (C + 31) / 32;  // columns per lane
     constexpr int BS = (NP * NP + 3) / 4 * 4;
     constexpr int DATA = (B + 3) / 4 * 4 + 4;  // floats: an aligned superset of any block
-    constexpr int SLOT = DATA + BS;            // then the 1D operator block
+    constexpr int SLOT = DATA + (LDG ? 0 : BS);  // then (copied) the 1D operator block
     __shared__ __align__(128) float ring[kRing * SLOT];
     __shared__ float y[B];
     __shared__ __align__(8) uint64_t full[kRing];
     __shared__ int lead[kRing];                // floats before the block in its slot
+    __shared__ int bidx[kRing];                // LDG: the slot's 1D operator block in the table
     const int lane = threadIdx.x;
     const int64_t e = blockIdx.x;
     if (e >= num_elements) return;
@@ -324,9 +330,15 @@ __global__ void __launch_bounds__(32) linear_tma_kernel(const float* __restrict_
         float* dst = ring + (kk % kRing) * SLOT;
         lead[kk % kRing] = int((a - a0) / 4);
         uint64_t* fb = &full[kk % kRing];
-        mbar_expect_tx(fb, bytes + uint32_t(BS * sizeof(float)));
-        bulk_copy_g2s(dst, reinterpret_cast<const void*>(a0), bytes, fb);
-        bulk_copy_g2s(dst + DATA, blocks + (size_t(idim) * nblocks + pr.y) * BS, uint32_t(BS * sizeof(float)), fb);
+        if constexpr (LDG) {
+            bidx[kk % kRing] = idim * nblocks + pr.y;
+            mbar_expect_tx(fb, bytes);
+            bulk_copy_g2s(dst, reinterpret_cast<const void*>(a0), bytes, fb);
+        } else {
+            mbar_expect_tx(fb, bytes + uint32_t(BS * sizeof(float)));
+            bulk_copy_g2s(dst, reinterpret_cast<const void*>(a0), bytes, fb);
+            bulk_copy_g2s(dst + DATA, blocks + (size_t(idim) * nblocks + pr.y) * BS, uint32_t(BS * sizeof(float)), fb);
+        }
         ++issued;
     };
     if (lane == 0)
@@ -352,6 +364,15 @@ __global__ void __launch_bounds__(32) linear_tma_kernel(const float* __restrict_
             for (int q = 0; q < NP; ++q) acc[j][q] = 0.f;
         const int kend = __ldg(row_ptr + e * D + t + 1) - beg;
         for (; k < kend; ++k) {
+            float m[BS];
+            if constexpr (LDG) {  // the operator block's loads are in flight during the wait
+                const float4* g4 = reinterpret_cast<const float4*>(blocks + size_t(bidx[slot]) * BS);
+#pragma unroll
+                for (int jj = 0; jj < BS / 4; ++jj) {
+                    const float4 v = __ldg(g4 + jj);
+                    m[4 * jj] = v.x; m[4 * jj + 1] = v.y; m[4 * jj + 2] = v.z; m[4 * jj + 3] = v.w;
+                }
+            }
             const bool ok = mbar_wait_bounded(&full[slot], (parity >> slot) & 1u, kSpinLimit);
             if (__any_sync(0xffffffffu, !ok)) {
                 failed = true;
@@ -359,12 +380,13 @@ __global__ void __launch_bounds__(32) linear_tma_kernel(const float* __restrict_
             }
             parity ^= 1u << slot;
             const float* x = ring + slot * SLOT + lead[slot];
-            const float4* m4 = reinterpret_cast<const float4*>(ring + slot * SLOT + DATA);
-            float m[BS];
+            if constexpr (!LDG) {
+                const float4* m4 = reinterpret_cast<const float4*>(ring + slot * SLOT + DATA);
 #pragma unroll
-            for (int jj = 0; jj < BS / 4; ++jj) {
-                const float4 v = m4[jj];
-                m[4 * jj] = v.x; m[4 * jj + 1] = v.y; m[4 * jj + 2] = v.z; m[4 * jj + 3] = v.w;
+                for (int jj = 0; jj < BS / 4; ++jj) {
+                    const float4 v = m4[jj];
+                    m[4 * jj] = v.x; m[4 * jj + 1] = v.y; m[4 * jj + 2] = v.z; m[4 * jj + 3] = v.w;
+                }
             }
 #pragma unroll
             for (int j = 0; j < CPT; ++j) {
@@ -409,24 +431,36 @@ __global__ void __launch_bounds__(32) linear_tma_kernel(const float* __restrict_
     for (int i = lane; i < B; i += 32) df_stage_update(df, e * B + i, y[i]);
 }
 
-template <int D, int NP>
-static cudaError_t launch_tma_t(const LinearLaunch& L, cudaStream_t st) {
+// the ring, the accumulator and the mbarriers must fit the static shared-memory limit (48 KB)
+constexpr bool tma_fits(int B, int np, int ring, bool ldg) {
+    return B / np <= 256 && size_t(ring * ((B + 3) / 4 * 4 + 4 + (ldg ? 0 : 16)) + B) * sizeof(float) + 512 <= 48 * 1024;
+}
+
+template <int D, int NP, int CFG>
+static cudaError_t launch_tma_cfg(const LinearLaunch& L, cudaStream_t st) {
     constexpr int B = IPow<NP, D>::v;
-    if constexpr (B / NP > 256) {
+    if constexpr (!tma_fits(B, NP, kTmaRing[CFG], kTmaLdg[CFG])) {
         return cudaErrorInvalidValue;
     } else {
         if (L.num_elements == 0) return cudaSuccess;
-        linear_tma_kernel<D, NP><<<unsigned(L.num_elements), 32, 0, st>>>(L.us_shadow, L.row_ptr, L.pairs, L.blocks32p,
-                                                                          L.num_blocks, L.num_elements, L.df, L.err);
+        linear_tma_kernel<D, NP, kTmaRing[CFG], kTmaLdg[CFG]><<<unsigned(L.num_elements), 32, 0, st>>>(
+            L.us_shadow, L.row_ptr, L.pairs, L.blocks32p, L.num_blocks, L.num_elements, L.df, L.err);
         return cudaGetLastError();
     }
 }
 
-bool linear_tma_supported(int dim, int np) {
+template <int D, int NP>
+static cudaError_t launch_tma_t(const LinearLaunch& L, cudaStream_t st) {
+    if (L.tma_cfg == 1) return launch_tma_cfg<D, NP, 1>(L, st);
+    if (L.tma_cfg == 2) return launch_tma_cfg<D, NP, 2>(L, st);
+    return launch_tma_cfg<D, NP, 0>(L, st);
+}
+
+bool linear_tma_supported(int dim, int np, int cfg) {
     int B = 1;
     for (int d = 0; d < dim; ++d) B *= np;
-    // the ring, the accumulator and the mbarriers must fit the static shared-memory limit (48 KB)
-    return B / np <= 256 && size_t(kRing * ((B + 3) / 4 * 4 + 4 + 16) + B) * sizeof(float) + 256 <= 48 * 1024;
+    if (cfg < 0 || cfg >= kTmaConfigs) return false;
+    return tma_fits(B, np, kTmaRing[cfg], kTmaLdg[cfg]);
 }
 
 bool linear_col_supported(int dim, int np) {

@@ -53,6 +53,7 @@ struct LinearLaunch {
     const float* blocks32p;
     DFState df;              // zero-initialised: FP64 epilogue
     int* err;                // variant 2: set to 1 when a copy wait gives up (device flag)
+    int tma_cfg;             // variant 2: ring depth / operator-block source (kernels.cu, kTmaRing, kTmaLdg)
 };
 
 // Batched solves: concatenated element tables, per-element solve index.
@@ -87,7 +88,8 @@ constexpr int kReduceBlocks = 1216;  // 8 CTAs per SM on 152 SMs
 cudaError_t launch_linear(const LinearLaunch& L, bool mixed, StageCoef rk, cudaStream_t st);
 // Variant 2 needs the FP32 stage state with 16-byte aligned array bases and
 // at least 16 bytes readable past the last coefficient.
-bool linear_tma_supported(int dim, int np);
+constexpr int kTmaConfigs = 3;
+bool linear_tma_supported(int dim, int np, int cfg = 0);
 bool linear_col_supported(int dim, int np);
 // FP64 vector <-> FP32 (hi, lo) pairs
 cudaError_t launch_split(const double* in, float* hi, float* lo, int64_t n, cudaStream_t st);

@@ -74,6 +74,8 @@ def load():
         "amdg_linear_apply": ([vp, vp, vp, i32], i32),
         "amdg_linear_tuning": ([vp, vp, vp], i32),
         "amdg_linear_set_variant": ([vp, i32, i32], i32),
+        "amdg_linear_copy_config": ([vp, vp, vp], i32),
+        "amdg_linear_set_copy_config": ([vp, i32], i32),
         "amdg_rk3ssp_steps": ([vp, dbl, i32, i32], i32),
         "amdg_rk3ssp_steps_host": ([vp, dbl, i32, vp, i32], i32),
         "amdg_rk3ssp_serve_host": ([vp, dbl, i32, i32, i32, vp, vp], i32),
@@ -421,6 +423,16 @@ class LinearOperator:
 
     def set_variant(self, prec: int, variant: int):
         _ck(load().amdg_linear_set_variant(self._h, prec, variant), "linear_set_variant")
+
+    def copy_config(self):
+        """(configuration of the bulk-copy variant, stage ms per configuration)."""
+        c = C.c_int()
+        ms = np.zeros(3, np.float32)
+        _ck(load().amdg_linear_copy_config(self._h, C.byref(c), _ptr(ms)), "linear_copy_config")
+        return c.value, ms.tolist()
+
+    def set_copy_config(self, config: int):
+        _ck(load().amdg_linear_set_copy_config(self._h, config), "linear_set_copy_config")
 
     def apply_device(self, d_u: int, d_rhs: int, prec: int = FP64):
         _ck(load().amdg_linear_apply(self._h, C.c_void_p(d_u), C.c_void_p(d_rhs), prec), "linear_apply")

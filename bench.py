@@ -273,6 +273,10 @@ def run_ours(args):
         "gpu_launches": launches32,
         "autotune": {"variants": {"fp64": op.tuning()[0][0], "mixed": op.tuning()[0][1]},
                      "stage_ms": {"fp64": op.tuning()[1][0], "mixed": op.tuning()[1][1]},
+                     "bulk_copy_config": {"chosen": op.copy_config()[0],
+                                          "stage_ms_by_config": op.copy_config()[1],
+                                          "configs": ["3 slots, operator block copied", "3 slots, operator block "
+                                                      "from the L1 table", "6 slots, operator block from the table"]},
                      "legend": "variant 0 = thread per output, 1 = column variant, "
                                "2 = column variant fed by bulk asynchronous copies (mixed only)"},
         "clocks": clocks,
