@@ -97,6 +97,17 @@ def dist_env():
     return rank, world, local
 
 
+def max_over_ranks(value: float, world: int, device: str = "cuda") -> float:
+    """The largest of every rank's value (a timed region is as long as its slowest replica)."""
+    if world <= 1:
+        return value
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([value], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
 def dt_for():
     dx = 1.0 / (1 << NMAX)
     return CFL * dx / sum(abs(c) for c in COEF)
@@ -165,11 +176,7 @@ def run_ours(args):
         e.record(stream)
         barrier()
         launches = ctx.launch_count() - l0
-        sec = s.elapsed_time(e) / 1e3
-        if world > 1:
-            t = torch.tensor([sec], device="cuda")
-            torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-            sec = float(t.item())
+        sec = max_over_ranks(s.elapsed_time(e) / 1e3, world)
         err = exact_l2(g, args.steps * dt)
         return sec, launches, err
 
