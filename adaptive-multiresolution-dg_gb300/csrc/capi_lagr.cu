@@ -822,10 +822,16 @@ amdg_status amdg_burgers_features(amdg_burgers_op* op, const double* d_u, float*
     return AMDG_OK;
 }
 
+// The learned adaptive step over a horizon of `horizon` time steps on one pre-adapted grid
+// (horizon 1: one step).  With t_left > 0 no step goes past t_left: the horizon is cut to
+// ceil(t_left / dt) steps and the last one shortened to land on it.  *t_advanced: the time
+// stepped; *steps_out: the steps taken.
 static amdg_status learned_step_any(amdg_burgers_op* op, amdg_mlp* mlp, double cfl, double wave_speed, double eps,
-                                    double eta, double tau, amdg_precision prec, double* dt_out, int64_t* stats) {
-    AMDG_REQUIRE(op && mlp && std::isfinite(cfl) && cfl > 0 && std::isfinite(wave_speed) && wave_speed > 0, AMDG_ERR_ARG,
-                 "bad arguments");
+                                    double eta, double tau, amdg_precision prec, int horizon, double t_left,
+                                    double* t_advanced, int* steps_out, int64_t* stats) {
+    AMDG_REQUIRE(op && mlp && std::isfinite(cfl) && cfl > 0 && std::isfinite(wave_speed) && wave_speed > 0 &&
+                     horizon >= 1 && std::isfinite(t_left) && t_left >= 0,
+                 AMDG_ERR_ARG, "bad arguments");
     AMDG_REQUIRE(prec == AMDG_PREC_FP64 || prec == AMDG_PREC_MIXED, AMDG_ERR_ARG, "bad precision");
     AMDG_CK(cudaSetDevice(op->device));
     if (amdg_status rs = burgers_sync(op); rs != AMDG_OK) return rs;
@@ -885,8 +891,23 @@ static amdg_status learned_step_any(amdg_burgers_op* op, amdg_mlp* mlp, double c
         std::vector<uint64_t> keys = refine_keys(g->host, norms.data(), eps, nullptr, force.data());
         if (int64_t(keys.size()) != g->host.num_elements && (s = grid_set_keys(g, std::move(keys))) != AMDG_OK) return s;
     }
-    // 3. one time step, no predictor step
-    if ((s = one_step(op, dt, prec)) != AMDG_OK) return s;
+    // 3. the horizon's time steps on this grid, no predictor: n - 1 steps of dt (replayed as a
+    //    CUDA graph when n - 1 > 1), the last one of dt_last
+    int n = horizon;
+    double dt_last = dt;
+    if (t_left > 0) {
+        const int need = std::max(1, int(std::ceil(t_left / dt - 1e-9)));
+        if (need <= n) {
+            n = need;
+            dt_last = t_left - (n - 1) * dt;
+        }
+    }
+    if (n > 1) {
+        if (op->kind == 0) s = amdg_burgers_rk3_steps(op, dt, n - 1, prec);
+        else s = wave_rk4(op, dt, n - 1, prec);
+        if (s != AMDG_OK) return s;
+    }
+    if ((s = one_step(op, dt_last, prec)) != AMDG_OK) return s;
     // 4. coarsening (amdg_grid_coarsen), then the surplus criterion judges the
     //    result: leaves still above eps are missed refinements, refined at the
     //    start of the next step
@@ -906,7 +927,8 @@ static amdg_status learned_step_any(amdg_burgers_op* op, amdg_mlp* mlp, double c
             if (it != g->host.key.end() && *it == kv.first && leaf[it - g->host.key.begin()]) op->missed_keys.push_back(kv.first);
         }
     }
-    if (dt_out) *dt_out = dt;
+    if (t_advanced) *t_advanced = (n - 1) * dt + dt_last;
+    if (steps_out) *steps_out = n;
     if (stats) {
         stats[0] = n_net;
         stats[1] = n_unsure;
@@ -919,7 +941,13 @@ static amdg_status learned_step_any(amdg_burgers_op* op, amdg_mlp* mlp, double c
 amdg_status amdg_burgers_adaptive_step_learned(amdg_burgers_op* op, amdg_mlp* mlp, double cfl, double wave_speed,
                                                double eps, double eta, double tau, amdg_precision prec, double* dt_out,
                                                int64_t* stats) {
-    return learned_step_any(op, mlp, cfl, wave_speed, eps, eta, tau, prec, dt_out, stats);
+    return learned_step_any(op, mlp, cfl, wave_speed, eps, eta, tau, prec, 1, 0.0, dt_out, nullptr, stats);
+}
+
+amdg_status amdg_burgers_adaptive_steps_learned(amdg_burgers_op* op, amdg_mlp* mlp, double cfl, double wave_speed,
+                                                double eps, double eta, double tau, amdg_precision prec, int horizon,
+                                                double t_left, double* t_advanced, int* steps, int64_t* stats) {
+    return learned_step_any(op, mlp, cfl, wave_speed, eps, eta, tau, prec, horizon, t_left, t_advanced, steps, stats);
 }
 
 amdg_status amdg_burgers_counters(const amdg_burgers_op* op, int64_t* stage_dof_updates, int64_t* rhs_evaluations) {
@@ -1026,7 +1054,15 @@ amdg_status amdg_wave_features(amdg_wave_op* w, const double* d_u, float* d_feat
 amdg_status amdg_wave_adaptive_step_learned(amdg_wave_op* w, amdg_mlp* mlp, double cfl, double wave_speed, double eps,
                                             double eta, double tau, amdg_precision prec, double* dt_out, int64_t* stats) {
     AMDG_REQUIRE(w, AMDG_ERR_ARG, "null operator");
-    return learned_step_any(w->lagr, mlp, cfl, wave_speed, eps, eta, tau, prec, dt_out, stats);
+    return learned_step_any(w->lagr, mlp, cfl, wave_speed, eps, eta, tau, prec, 1, 0.0, dt_out, nullptr, stats);
+}
+
+amdg_status amdg_wave_adaptive_steps_learned(amdg_wave_op* w, amdg_mlp* mlp, double cfl, double wave_speed,
+                                             double eps, double eta, double tau, amdg_precision prec, int horizon,
+                                             double t_left, double* t_advanced, int* steps, int64_t* stats) {
+    AMDG_REQUIRE(w, AMDG_ERR_ARG, "null operator");
+    return learned_step_any(w->lagr, mlp, cfl, wave_speed, eps, eta, tau, prec, horizon, t_left, t_advanced, steps,
+                            stats);
 }
 
 amdg_status amdg_wave_counters(const amdg_wave_op* w, int64_t* stage_dof_updates, int64_t* rhs_evaluations) {

@@ -86,6 +86,7 @@ def load():
         "amdg_burgers_adaptive_step_ex": ([vp, dbl, dbl, dbl, dbl, i32, C.POINTER(dbl), vp], i32),
         "amdg_burgers_features": ([vp, vp, vp], i32),
         "amdg_burgers_adaptive_step_learned": ([vp, vp, dbl, dbl, dbl, dbl, dbl, i32, C.POINTER(dbl), vp], i32),
+        "amdg_burgers_adaptive_steps_learned": ([vp, vp, dbl, dbl, dbl, dbl, dbl, i32, i32, dbl, vp, vp, vp], i32),
         "amdg_mlp_create": ([vp, i32, i32, i32, i32, C.c_uint64, pp], i32),
         "amdg_mlp_destroy": ([vp], i32),
         "amdg_mlp_num_params": ([vp, C.POINTER(i64)], i32),
@@ -119,6 +120,7 @@ def load():
         "amdg_wave_adaptive_step_ex": ([vp, dbl, dbl, dbl, dbl, i32, C.POINTER(dbl), vp], i32),
         "amdg_wave_features": ([vp, vp, vp], i32),
         "amdg_wave_adaptive_step_learned": ([vp, vp, dbl, dbl, dbl, dbl, dbl, i32, C.POINTER(dbl), vp], i32),
+        "amdg_wave_adaptive_steps_learned": ([vp, vp, dbl, dbl, dbl, dbl, dbl, i32, i32, dbl, vp, vp, vp], i32),
         "amdg_context_profile": ([vp, i32], i32),
         "amdg_context_profile_read": ([vp, vp, vp], i32),
         "amdg_burgers_counters": ([vp, C.POINTER(i64), C.POINTER(i64)], i32),
@@ -516,6 +518,17 @@ class BurgersOperator:
         self.grid._refresh()
         return dt.value, stats
 
+    def adaptive_steps_learned(self, mlp, cfl: float, wave_speed: float, eps: float, eta: float, tau: float,
+                               horizon: int, t_left: float = 0.0, prec: int = FP64):
+        """(time advanced, steps taken, stats) of one learned pre-adaptation and `horizon` steps."""
+        stats = np.zeros(4, np.int64)
+        ta, n = C.c_double(), C.c_int()
+        _ck(load().amdg_burgers_adaptive_steps_learned(self._h, mlp.handle, cfl, wave_speed, eps, eta, tau, prec,
+                                                       horizon, t_left, C.byref(ta), C.byref(n), _ptr(stats)),
+            "burgers_adaptive_steps_learned")
+        self.grid._refresh()
+        return ta.value, n.value, stats
+
     def counters(self):
         """(RK-stage DOF updates, right-hand-side evaluations) since creation."""
         a, b = C.c_int64(), C.c_int64()
@@ -593,6 +606,16 @@ class WaveOperator:
                                                    C.byref(dt), _ptr(stats)), "wave_adaptive_step_learned")
         self.grid._refresh()
         return dt.value, stats
+
+    def adaptive_steps_learned(self, mlp, cfl: float, wave_speed: float, eps: float, eta: float, tau: float,
+                               horizon: int, t_left: float = 0.0, prec: int = FP64):
+        stats = np.zeros(4, np.int64)
+        ta, n = C.c_double(), C.c_int()
+        _ck(load().amdg_wave_adaptive_steps_learned(self._h, mlp.handle, cfl, wave_speed, eps, eta, tau, prec,
+                                                    horizon, t_left, C.byref(ta), C.byref(n), _ptr(stats)),
+            "wave_adaptive_steps_learned")
+        self.grid._refresh()
+        return ta.value, n.value, stats
 
     def close(self):
         if self._h:

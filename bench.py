@@ -97,6 +97,29 @@ def dist_env():
     return rank, world, local
 
 
+def element_keys(g) -> np.ndarray:
+    """Packed 1D orders of the grid's elements (nmax bits per dimension), one int64 per element."""
+    lv, sp = g.elements()
+    o = np.where(lv == 0, 0, (1 << np.maximum(lv - 1, 0)) + (sp - 1) // 2).astype(np.int64)
+    key = np.zeros(len(o), np.int64)
+    for d in range(o.shape[1]):
+        key = (key << g.nmax) | o[:, d]
+    return key
+
+
+def horizon_labels(keys_steps, dec_steps, horizon):
+    """Classifier labels for a learned step over `horizon` steps: 0 (refine) where the plain
+    criterion refines the element at this step or one of the next horizon - 1, else 2 (coarsen)
+    where it removes the element at this step, else 1 (keep)."""
+    out = []
+    for s in range(len(keys_steps)):
+        refined = np.concatenate([keys_steps[j][dec_steps[j] == 1]
+                                  for j in range(s, min(len(keys_steps), s + horizon))])
+        lab = np.where(np.isin(keys_steps[s], refined), 0, np.where(dec_steps[s] == 2, 2, 1))
+        out.append(lab.astype(np.int32))
+    return out
+
+
 def max_over_ranks(value: float, world: int, device: str = "cuda") -> float:
     """The largest of every rank's value (a timed region is as long as its slowest replica)."""
     if world <= 1:
@@ -382,20 +405,24 @@ def bench_burgers_adaptive(ctx, stream, args):
     # training data from plain FP64 runs of other waves
     t0 = time.perf_counter()
     rng = np.random.default_rng(1)
+    H = args.learn_horizon
     feats, labs = [], []
     for _ in range(args.learn_runs):
         a, b, c = rng.uniform(0.4, 0.6), rng.uniform(0.15, 0.3), rng.uniform(0.0, 1.0)
         g = amdg.Grid(ctx, dim, nmax, 2, level_init=level_init)
         g.init_separable_adaptive(wave_ic_terms(dim, a, b, c), eps)
         op = amdg.BurgersOperator(g, 1.1 * (a + b))
+        keys_steps, dec_steps = [], []
         for _s in range(args.learn_steps):
             buf = torch.empty(g.num_elements * F, dtype=torch.float32, device="cuda")
             torch.cuda.synchronize()
             op.features_device(g.device_ptr(), buf.data_ptr())
             ctx.synchronize()
             feats.append(buf.cpu().numpy().reshape(-1, F))
+            keys_steps.append(element_keys(g))
             _dt, dec = op.adaptive_step_ex(CFL, a + b, eps, eta)
-            labs.append(np.where(dec == 1, 0, np.where(dec == 2, 2, 1)).astype(np.int32))
+            dec_steps.append(np.asarray(dec))
+        labs.extend(horizon_labels(keys_steps, dec_steps, H))
         op.close()
         g.close()
     x, y = np.concatenate(feats), np.concatenate(labs)
@@ -407,13 +434,14 @@ def bench_burgers_adaptive(ctx, stream, args):
     loss = mlp.train_device(dx.data_ptr(), dy.data_ptr(), len(y), epochs=args.learn_epochs, batch=256, lr=2e-3,
                             seed=12)
     train_s = time.perf_counter() - t0
-    out["training"] = {"runs": args.learn_runs, "steps_per_run": args.learn_steps, "samples": int(len(y)),
+    out["training"] = {"runs": args.learn_runs, "steps_per_run": args.learn_steps, "horizon": H,
+                       "samples": int(len(y)),
                        "class_counts": [int((y == i).sum()) for i in range(3)], "epochs": args.learn_epochs,
                        "final_loss": loss, "collect_s": collect_s, "train_s": train_s}
 
     mesh = (np.arange(48) + 0.5) / 48
 
-    def run(learned, prec, t_end):
+    def run(learned, prec, t_end, horizon=1):
         g = amdg.Grid(ctx, dim, nmax, 2, level_init=level_init)
         g.init_separable_adaptive(O.burgers_ic_terms(dim), eps)
         op = amdg.BurgersOperator(g, 1.1 * umax)
@@ -422,14 +450,16 @@ def bench_burgers_adaptive(ctx, stream, args):
         ctx.profile(True)
         t0 = time.perf_counter()
         while t < t_end - 1e-12:
+            if learned:  # one pre-adaptation, then `horizon` steps (the last one landing on t_end)
+                dt, n, st = op.adaptive_steps_learned(mlp, CFL, umax, eps, eta, tau, horizon, t_end - t, prec)
+                cls += st[:3]
+                t += dt
+                steps += n
+                continue
             lv = g.max_mesh_level()
             dt_full = CFL / sum(umax * 2.0 ** int(m) for m in lv)
             cfl = CFL if t + dt_full <= t_end else CFL * (t_end - t) / dt_full
-            if learned:
-                dt, st = op.adaptive_step_learned(mlp, cfl, umax, eps, eta, tau, prec)
-                cls += st[:3]
-            else:
-                dt = op.adaptive_step(cfl, umax, eps, eta, prec)
+            dt = op.adaptive_step(cfl, umax, eps, eta, prec)
             t += dt
             steps += 1
         ctx.synchronize()
@@ -454,12 +484,14 @@ def bench_burgers_adaptive(ctx, stream, args):
         g.close()
         return res
 
-    for name, learned, prec in (("plain_fp64", False, amdg.FP64), ("mixed_learned", True, amdg.MIXED),
-                                ("mixed_plain", False, amdg.MIXED)):
-        run(learned, prec, 4 * CFL / (umax * dim * 32))  # warm-up: a few steps
-        out[name] = run(learned, prec, T)
+    arms = (("plain_fp64", False, amdg.FP64, 1), ("mixed_learned", True, amdg.MIXED, H),
+            ("mixed_learned_h1", True, amdg.MIXED, 1), ("mixed_plain", False, amdg.MIXED, 1))
+    for name, learned, prec, horizon in arms:
+        run(learned, prec, 4 * CFL / (umax * dim * 32), horizon)  # warm-up: a few steps
+        out[name] = run(learned, prec, T, horizon)
+        out[name]["horizon"] = horizon
     ref = out["plain_fp64"].pop("_mesh_values")
-    for name in ("mixed_learned", "mixed_plain"):
+    for name in ("mixed_learned", "mixed_learned_h1", "mixed_plain"):
         v = out[name].pop("_mesh_values")
         out[name]["rel_l2_diff_vs_plain_fp64"] = float(np.linalg.norm(v - ref) / np.linalg.norm(ref))
         out[name]["l2_error_ratio_vs_plain_fp64"] = (out[name]["error_vs_exact_l1_l2_linf"][1] /
@@ -775,6 +807,8 @@ def main():
     ap.add_argument("--batch-eps", type=float, default=1e-5)
     ap.add_argument("--learn-runs", type=int, default=4, help="plain runs whose decisions train the classifier (0: skip)")
     ap.add_argument("--learn-steps", type=int, default=12)
+    ap.add_argument("--learn-horizon", type=int, default=4,
+                    help="time steps per learned pre-adaptation in the 3D Burgers runs")
     ap.add_argument("--learn-epochs", type=int, default=30)
     ap.add_argument("--wave-learn-runs", type=int, default=20, help="plain wave runs that train its classifier (0: skip)")
     ap.add_argument("--wave-learn-steps", type=int, default=30)

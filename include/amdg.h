@@ -393,6 +393,9 @@ amdg_status amdg_wave_adaptive_step_ex(amdg_wave_op* op, double cfl, double wave
 amdg_status amdg_wave_features(amdg_wave_op* op, const double* d_u, float* d_features);
 amdg_status amdg_wave_adaptive_step_learned(amdg_wave_op* op, amdg_mlp* mlp, double cfl, double wave_speed, double eps,
                                             double eta, double tau, amdg_precision prec, double* dt_out, int64_t* stats);
+amdg_status amdg_wave_adaptive_steps_learned(amdg_wave_op* op, amdg_mlp* mlp, double cfl, double wave_speed,
+                                             double eps, double eta, double tau, amdg_precision prec, int horizon,
+                                             double t_left, double* t_advanced, int* steps, int64_t* stats);
 /* As amdg_burgers_counters (4 x DOF per RK4ODE2nd step). */
 amdg_status amdg_wave_counters(const amdg_wave_op* op, int64_t* stage_dof_updates, int64_t* rhs_evaluations);
 
@@ -432,6 +435,15 @@ amdg_status amdg_burgers_features(amdg_burgers_op* op, const double* d_u, float*
 amdg_status amdg_burgers_adaptive_step_learned(amdg_burgers_op* op, amdg_mlp* mlp, double cfl, double wave_speed,
                                                double eps, double eta, double tau, amdg_precision prec, double* dt_out,
                                                int64_t* stats);
+/* The learned step over a horizon: the classifier (trained on the plain criterion's refinements
+ * within the next `horizon` steps) pre-adapts the grid once, then `horizon` SSP-RK3 steps of one dt
+ * run on that grid (a CUDA graph replays them), then coarsening and the criterion's check for
+ * missed refinements as above.  With t_left > 0 no step passes t_left: the horizon is cut and its
+ * last step shortened to land on it.  *t_advanced = the time stepped, *steps = the steps taken
+ * (either may be NULL). */
+amdg_status amdg_burgers_adaptive_steps_learned(amdg_burgers_op* op, amdg_mlp* mlp, double cfl, double wave_speed,
+                                                double eps, double eta, double tau, amdg_precision prec, int horizon,
+                                                double t_left, double* t_advanced, int* steps, int64_t* stats);
 
 #ifdef __cplusplus
 }

@@ -198,3 +198,46 @@ def test_learned_wave_steps_follow_the_plain_criterion(ctx):
     b = np.array([u_learn[pl[k]] for k in common])
     assert np.linalg.norm(a - b) <= 1e-3 * np.linalg.norm(a)
     mlp.close()
+
+
+def test_learned_horizon_steps_land_on_the_end_time(ctx):
+    """Learned pre-adaptation over a horizon of 4 steps: the time advanced is 4 dt per call except
+    the last, which stops exactly at the end time; the right-hand sides are 3 per step (no
+    predictor); the final solution stays close to the plain run's on the common elements."""
+    dim, nmax, eps, eta = 2, 7, 1e-4, 1e-5
+    x, y = _collect(ctx, dim, nmax, eps, eta, steps=6, seeds=range(4))
+    dx, dy = torch.from_numpy(x).cuda(), torch.from_numpy(y).cuda()
+    torch.cuda.synchronize()
+    mlp = amdg.MLP(ctx, x.shape[1], 64, 3, 3, seed=13)
+    mlp.train_device(dx.data_ptr(), dy.data_ptr(), x.shape[0], epochs=30, batch=256, lr=2e-3, seed=14)
+    t_end = 0.01
+
+    def run(horizon):
+        g = amdg.Grid(ctx, dim, nmax, 2, level_init=3)
+        g.init_separable_adaptive(O.burgers_ic_terms(dim), eps)
+        op = amdg.BurgersOperator(g, 1.1 * 0.75)
+        t, steps, calls = 0.0, 0, 0
+        while t < t_end - 1e-14:
+            dt, n, _st = op.adaptive_steps_learned(mlp, 0.1, 0.75, eps, eta, 0.8, horizon, t_end - t)
+            assert 1 <= n <= horizon and dt > 0
+            t += dt
+            steps += n
+            calls += 1
+        ctx.synchronize()
+        lv, sp = g.elements()
+        res = (t, steps, calls, O.arrays_to_keys(lv, sp), g.coefficients().copy(), op.counters())
+        op.close()
+        g.close()
+        return res
+
+    t1, s1, c1, k1, u1, w1 = run(1)
+    t4, s4, c4, k4, u4, w4 = run(4)
+    assert abs(t1 - t_end) < 1e-14 and abs(t4 - t_end) < 1e-14
+    assert c1 == s1 and c4 < s4 and w4[1] == 3 * s4
+    common = sorted(set(k1) & set(k4))
+    p1 = {k: i for i, k in enumerate(k1)}
+    p4 = {k: i for i, k in enumerate(k4)}
+    a = np.array([u1[p1[k]] for k in common])
+    b = np.array([u4[p4[k]] for k in common])
+    assert np.linalg.norm(a - b) <= 1e-3 * np.linalg.norm(a)
+    mlp.close()
