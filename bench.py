@@ -516,6 +516,7 @@ def bench_wave_adaptive(ctx, stream, args):
     import amdg_oracle as O
     dim, nmax, level_init, eps, eta, sigma, T, tau, speed = 2, 9, 3, 1e-5, 1e-6, 10.0, args.wave_time, 0.8, 1.0
     F = 2 * 9 * (1 + 2 * dim)  # features of u and of u_t
+    H = args.wave_learn_horizon
     out = {"workload": f"2D wave u_tt = div(c^2 grad u), c = 1 + 0.5 sin(2 pi x) sin(2 pi y), Gaussian bump at "
                        f"rest, adaptive (refine 1e-5, coarsen 1e-6, max level 9, start level 3), Alpert k=2, "
                        f"Lagrange degree 4 (msh_case 2 nodes), IPDG sigma 10, RK4ODE2nd, CFL 0.1, to T = {T}"}
@@ -528,14 +529,17 @@ def bench_wave_adaptive(ctx, stream, args):
         g = amdg.Grid(ctx, dim, nmax, 2, level_init=level_init)
         g.init_separable_adaptive(O.wave_ic_terms(dim, centre, width), eps)
         op = amdg.WaveOperator(g, sigma)
+        keys_steps, dec_steps = [], []
         for _s in range(args.wave_learn_steps):
             buf = torch.empty(g.num_elements * F, dtype=torch.float32, device="cuda")
             torch.cuda.synchronize()
             op.features_device(g.device_ptr(), buf.data_ptr())
             ctx.synchronize()
             feats.append(buf.cpu().numpy().reshape(-1, F))
+            keys_steps.append(element_keys(g))
             _dt, dec = op.adaptive_step_ex(CFL, speed, eps, eta)
-            labs.append(np.where(dec == 1, 0, np.where(dec == 2, 2, 1)).astype(np.int32))
+            dec_steps.append(np.asarray(dec))
+        labs.extend(horizon_labels(keys_steps, dec_steps, args.wave_learn_horizon))
         op.close()
         g.close()
     x, y = np.concatenate(feats), np.concatenate(labs)
@@ -558,7 +562,7 @@ def bench_wave_adaptive(ctx, stream, args):
     t0 = time.perf_counter()
     loss = mlp.train_device(dx.data_ptr(), dy.data_ptr(), len(y), epochs=args.learn_epochs, batch=256, lr=2e-3,
                             seed=22)
-    out["training"] = {"runs": args.wave_learn_runs, "steps_per_run": args.wave_learn_steps,
+    out["training"] = {"runs": args.wave_learn_runs, "steps_per_run": args.wave_learn_steps, "horizon": H,
                        "samples_collected": collected, "samples": int(len(y)),
                        "class_counts": [int((y == i).sum()) for i in range(3)], "epochs": args.learn_epochs,
                        "final_loss": loss, "collect_s": collect_s, "train_s": time.perf_counter() - t0}
@@ -573,14 +577,16 @@ def bench_wave_adaptive(ctx, stream, args):
         ctx.profile(True)
         t0 = time.perf_counter()
         while t < t_end - 1e-12:
+            if learned:  # one pre-adaptation, then H steps (the last one landing on t_end)
+                dt, n, st = op.adaptive_steps_learned(mlp, CFL, speed, e, et, tau, H, t_end - t, prec)
+                cls += st[:3]
+                t += dt
+                steps += n
+                continue
             lv = g.max_mesh_level()
             dt_full = CFL / sum(speed * 2.0 ** int(m) for m in lv)
             cfl = CFL if t + dt_full <= t_end else CFL * (t_end - t) / dt_full
-            if learned:
-                dt, st = op.adaptive_step_learned(mlp, cfl, speed, e, et, tau, prec)
-                cls += st[:3]
-            else:
-                dt = op.adaptive_step(cfl, speed, e, et, prec)
+            dt = op.adaptive_step(cfl, speed, e, et, prec)
             t += dt
             steps += 1
         ctx.synchronize()
@@ -612,6 +618,7 @@ def bench_wave_adaptive(ctx, stream, args):
                                 ("mixed_plain", False, amdg.MIXED)):
         run(learned, prec, 4 * CFL / (speed * dim * 128))  # warm-up: a few steps
         out[name] = run(learned, prec, T)
+        out[name]["horizon"] = H if learned else 1
         v = out[name].pop("_mesh_values")
         out[name]["rel_l2_diff_vs_reference_run"] = float(np.linalg.norm(v - ref) / np.linalg.norm(ref))
         out[name]["_v"] = v
@@ -813,6 +820,7 @@ def main():
     ap.add_argument("--wave-learn-runs", type=int, default=20, help="plain wave runs that train its classifier (0: skip)")
     ap.add_argument("--wave-learn-steps", type=int, default=30)
     ap.add_argument("--wave-train-samples", type=int, default=300000, help="training samples kept (stratified)")
+    ap.add_argument("--wave-learn-horizon", type=int, default=4, help="time steps per learned pre-adaptation (wave)")
     ap.add_argument("--profile", choices=["none", "wave_rhs"], default="none",
                     help="wave_rhs: run the wave right-hand-side profiling case instead of the bench")
     ap.add_argument("--wave-time", type=float, default=0.05,
