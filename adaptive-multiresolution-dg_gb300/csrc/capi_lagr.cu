@@ -903,8 +903,8 @@ static amdg_status learned_step_any(amdg_burgers_op* op, amdg_mlp* mlp, double c
         }
     }
     if (n > 1) {
-        if (op->kind == 0) s = amdg_burgers_rk3_steps(op, dt, n - 1, prec);
-        else s = wave_rk4(op, dt, n - 1, prec);
+        if (op->kind == 0) s = amdg_burgers_rk3_steps(op, dt, n - 1, prec);  // syncs the operator itself
+        else if ((s = burgers_sync(op)) == AMDG_OK) s = wave_rk4(op, dt, n - 1, prec);
         if (s != AMDG_OK) return s;
     }
     if ((s = one_step(op, dt_last, prec)) != AMDG_OK) return s;
@@ -1007,6 +1007,7 @@ static amdg_status ensure_velocity(amdg_grid* g) {
 static amdg_status wave_rk4(amdg_burgers_op* op, double dt, int nsteps, amdg_precision prec) {
     amdg_grid* g = op->grid;
     cudaStream_t st = stream_of(op);
+    if (amdg_status s = burgers_sync(op); s != AMDG_OK) return s;  // buffers sized for the current grid
     PhaseTimer timer(g->ctx, AMDG_PHASE_RK3);
     if (amdg_status s = ensure_velocity(g); s != AMDG_OK) return s;
     const size_t bytes = size_t(g->dof) * sizeof(double);

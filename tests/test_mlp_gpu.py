@@ -191,6 +191,19 @@ def test_learned_wave_steps_follow_the_plain_criterion(ctx):
     k_plain, u_plain, w_plain = run(False)
     k_learn, u_learn, w_learn = run(True)
     assert w_plain[1] == 40 and w_learn[1] == 40
+    # the horizon form: one pre-adaptation, then 3 RK4 steps on a grid it has just grown
+    g = amdg.Grid(ctx, dim, nmax, 2, level_init=3)
+    g.init_separable_adaptive(O.wave_ic_terms(dim), eps)
+    op = amdg.WaveOperator(g, sigma)
+    t, steps = 0.0, 0
+    while steps < 9:
+        dt, n, _st = op.adaptive_steps_learned(mlp, 0.1, 1.0, eps, eta, 0.8, 3)
+        t += dt
+        steps += n
+    ctx.synchronize()
+    assert steps == 9 and op.counters()[1] == 4 * 9
+    op.close()
+    g.close()
     common = sorted(set(k_plain) & set(k_learn))
     pp = {k: i for i, k in enumerate(k_plain)}
     pl = {k: i for i, k in enumerate(k_learn)}
