@@ -568,7 +568,7 @@ def bench_wave_adaptive(ctx, stream, args):
                        "final_loss": loss, "collect_s": collect_s, "train_s": time.perf_counter() - t0}
     mesh = (np.arange(128) + 0.5) / 128
 
-    def run(learned, prec, t_end, e=eps, et=eta, nm=nmax):
+    def run(learned, prec, t_end, e=eps, et=eta, nm=nmax, horizon=H):
         g = amdg.Grid(ctx, dim, nm, 2, level_init=level_init)
         g.init_separable_adaptive(O.wave_ic_terms(dim), e)
         op = amdg.WaveOperator(g, sigma)
@@ -577,8 +577,8 @@ def bench_wave_adaptive(ctx, stream, args):
         ctx.profile(True)
         t0 = time.perf_counter()
         while t < t_end - 1e-12:
-            if learned:  # one pre-adaptation, then H steps (the last one landing on t_end)
-                dt, n, st = op.adaptive_steps_learned(mlp, CFL, speed, e, et, tau, H, t_end - t, prec)
+            if learned:  # one pre-adaptation, then `horizon` steps (the last one landing on t_end)
+                dt, n, st = op.adaptive_steps_learned(mlp, CFL, speed, e, et, tau, horizon, t_end - t, prec)
                 cls += st[:3]
                 t += dt
                 steps += n
@@ -614,16 +614,19 @@ def bench_wave_adaptive(ctx, stream, args):
     out["reference_run"] = {"what": "plain FP64, refine 1e-5, coarsen 1e-6, max level 10",
                             "wall_s": ref_run["wall_s"], "steps": ref_run["steps"],
                             "elements_final": ref_run["elements_final"]}
-    for name, learned, prec in (("plain_fp64", False, amdg.FP64), ("mixed_learned", True, amdg.MIXED),
-                                ("mixed_plain", False, amdg.MIXED)):
-        run(learned, prec, 4 * CFL / (speed * dim * 128))  # warm-up: a few steps
-        out[name] = run(learned, prec, T)
-        out[name]["horizon"] = H if learned else 1
+    # the learned arm at the trained horizon ("mixed_learned") and at shorter ones
+    arms = [("plain_fp64", False, amdg.FP64, 1), ("mixed_learned", True, amdg.MIXED, H)]
+    arms += [(f"mixed_learned_h{h}", True, amdg.MIXED, h) for h in (1, 2) if h < H]
+    arms += [("mixed_plain", False, amdg.MIXED, 1)]
+    for name, learned, prec, horizon in arms:
+        run(learned, prec, 4 * CFL / (speed * dim * 128), horizon=horizon)  # warm-up: a few steps
+        out[name] = run(learned, prec, T, horizon=horizon)
+        out[name]["horizon"] = horizon
         v = out[name].pop("_mesh_values")
         out[name]["rel_l2_diff_vs_reference_run"] = float(np.linalg.norm(v - ref) / np.linalg.norm(ref))
         out[name]["_v"] = v
     base = out["plain_fp64"].pop("_v")
-    for name in ("mixed_learned", "mixed_plain"):
+    for name in [a[0] for a in arms[1:]]:
         v = out[name].pop("_v")
         out[name]["rel_l2_diff_vs_plain_fp64"] = float(np.linalg.norm(v - base) / np.linalg.norm(base))
         out[name]["error_ratio_vs_plain_fp64"] = (out[name]["rel_l2_diff_vs_reference_run"] /
