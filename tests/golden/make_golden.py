@@ -100,6 +100,7 @@ WAVE_CASES = [
 # (name, dim, N_init, NMAX, eps, eta, sigma, cfl, steps): the adaptive wave loop
 WAVE_ADAPT_CASES = [
     ("wave_adapt2d", 2, 3, 5, 1e-5, 1e-6, 10.0, 0.1, 4),
+    ("wave_adapt3d", 3, 2, 4, 1e-3, 1e-4, 20.0, 0.05, 2),
 ]
 
 
