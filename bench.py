@@ -484,14 +484,15 @@ def bench_burgers_adaptive(ctx, stream, args):
         g.close()
         return res
 
-    arms = (("plain_fp64", False, amdg.FP64, 1), ("mixed_learned", True, amdg.MIXED, H),
-            ("mixed_learned_h1", True, amdg.MIXED, 1), ("mixed_plain", False, amdg.MIXED, 1))
+    arms = [("plain_fp64", False, amdg.FP64, 1), ("mixed_learned", True, amdg.MIXED, H)]
+    arms += [(f"mixed_learned_h{h}", True, amdg.MIXED, h) for h in (1, 8) if h != H]
+    arms += [("mixed_plain", False, amdg.MIXED, 1)]
     for name, learned, prec, horizon in arms:
         run(learned, prec, 4 * CFL / (umax * dim * 32), horizon)  # warm-up: a few steps
         out[name] = run(learned, prec, T, horizon)
         out[name]["horizon"] = horizon
     ref = out["plain_fp64"].pop("_mesh_values")
-    for name in ("mixed_learned", "mixed_learned_h1", "mixed_plain"):
+    for name in [a[0] for a in arms[1:]]:
         v = out[name].pop("_mesh_values")
         out[name]["rel_l2_diff_vs_plain_fp64"] = float(np.linalg.norm(v - ref) / np.linalg.norm(ref))
         out[name]["l2_error_ratio_vs_plain_fp64"] = (out[name]["error_vs_exact_l1_l2_linf"][1] /
