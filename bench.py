@@ -36,7 +36,7 @@ COEF = [1.0] * DIM
 CFL = 0.1
 # DRAM bytes of one mixed stage launch of the 6D N=8 workload, per kernel variant, from ncu
 # (dram__bytes_read.sum + dram__bytes_write.sum; variant 0 was not captured)
-NCU_TRAFFIC_BYTES = {1: (720.902 + 241.610) * 1e6, 2: (441.883 + 238.190) * 1e6}
+NCU_TRAFFIC_BYTES = {1: (720.902 + 241.610) * 1e6, 2: (442.000 + 237.598) * 1e6}
 METRIC = "DOF-stage updates/s at matched L2 error: plain FP64 vs mixed+learned-adapt"
 WORKLOAD = "6D linear advection, sparse grid N=8, Alpert k=2, SSP-RK3 (34,455,456 DOF)"
 
@@ -288,8 +288,8 @@ def run_ours(args):
                      "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum of one launch of this "
                                        "workload's stage kernel (bytes)", "peak_kind": pk_kind,
                      "kernel": {0: "linear_apply_kernel<6,3,float,float>", 1: "linear_col_kernel<6,3,float,float>",
-                                2: "linear_tma_kernel<6,3>"}[op.tuning()[0][1]]
-                               + " (fused RK3 stage, FP32-pair stage state)",
+                                2: "linear_tma_kernel<6,3,%d,%d>" % ((3, 0), (3, 1), (6, 1))[op.copy_config()[0]]}[
+                                    op.tuning()[0][1]] + " (fused RK3 stage, FP32-pair stage state)",
                      "kernel_ms": k32 * 1e3,
                      "algorithmic_bytes_per_launch": bytes_per_launch,
                      "fp32_tflops": flops / k32 / 1e12},
