@@ -957,6 +957,8 @@ amdg_status amdg_linear_set_variant(amdg_linear_op* op, amdg_precision prec, int
     return AMDG_OK;
 }
 
+static_assert(sizeof(amdg_linear_op::tma_ms) / sizeof(float) == kTmaConfigs, "one timing per configuration");
+
 amdg_status amdg_linear_copy_config(const amdg_linear_op* op, int* config, float* stage_ms) {
     AMDG_REQUIRE(op, AMDG_ERR_ARG, "op is null");
     if (config) *config = op->tma_cfg;

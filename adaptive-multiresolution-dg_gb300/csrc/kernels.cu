@@ -255,8 +255,8 @@ static cudaError_t launch_col_t(const LinearLaunch& L, const T* blocks, const X*
 // (LDG false) or is read by every lane from the L1-resident table, issued
 // before the wait on the slot (LDG true, one bulk copy per neighbour).
 constexpr uint32_t kSpinLimit = 1u << 22;
-constexpr int kTmaRing[3] = {3, 3, 6};
-constexpr bool kTmaLdg[3] = {false, true, true};
+constexpr int kTmaRing[kTmaConfigs] = {3, 3, 6, 2, 4};
+constexpr bool kTmaLdg[kTmaConfigs] = {false, true, true, true, true};
 
 __device__ __forceinline__ uint32_t smem_u32(const void* p) { return uint32_t(__cvta_generic_to_shared(p)); }
 
@@ -451,9 +451,13 @@ static cudaError_t launch_tma_cfg(const LinearLaunch& L, cudaStream_t st) {
 
 template <int D, int NP>
 static cudaError_t launch_tma_t(const LinearLaunch& L, cudaStream_t st) {
-    if (L.tma_cfg == 1) return launch_tma_cfg<D, NP, 1>(L, st);
-    if (L.tma_cfg == 2) return launch_tma_cfg<D, NP, 2>(L, st);
-    return launch_tma_cfg<D, NP, 0>(L, st);
+    switch (L.tma_cfg) {
+        case 1: return launch_tma_cfg<D, NP, 1>(L, st);
+        case 2: return launch_tma_cfg<D, NP, 2>(L, st);
+        case 3: return launch_tma_cfg<D, NP, 3>(L, st);
+        case 4: return launch_tma_cfg<D, NP, 4>(L, st);
+        default: return launch_tma_cfg<D, NP, 0>(L, st);
+    }
 }
 
 bool linear_tma_supported(int dim, int np, int cfg) {
