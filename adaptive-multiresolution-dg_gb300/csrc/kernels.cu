@@ -255,8 +255,8 @@ static cudaError_t launch_col_t(const LinearLaunch& L, const T* blocks, const X*
 // (LDG false) or is read by every lane from the L1-resident table, issued
 // before the wait on the slot (LDG true, one bulk copy per neighbour).
 constexpr uint32_t kSpinLimit = 1u << 22;
-constexpr int kTmaRing[kTmaConfigs] = {3, 3, 6, 2, 4};
-constexpr bool kTmaLdg[kTmaConfigs] = {false, true, true, true, true};
+constexpr int kTmaRing[kTmaConfigs] = {3, 3, 6, 2, 4, 1};
+constexpr bool kTmaLdg[kTmaConfigs] = {false, true, true, true, true, true};
 
 __device__ __forceinline__ uint32_t smem_u32(const void* p) { return uint32_t(__cvta_generic_to_shared(p)); }
 
@@ -456,6 +456,7 @@ static cudaError_t launch_tma_t(const LinearLaunch& L, cudaStream_t st) {
         case 2: return launch_tma_cfg<D, NP, 2>(L, st);
         case 3: return launch_tma_cfg<D, NP, 3>(L, st);
         case 4: return launch_tma_cfg<D, NP, 4>(L, st);
+        case 5: return launch_tma_cfg<D, NP, 5>(L, st);
         default: return launch_tma_cfg<D, NP, 0>(L, st);
     }
 }
