@@ -297,7 +297,7 @@ struct amdg_linear_op {
     int variant[2] = {0, 0};         // kernel variant per precision, picked by the autotuner
     float variant_ms[2][3] = {{0, 0, 0}, {0, 0, 0}};  // measured stage time [precision][variant]
     int tma_cfg = 0;                 // configuration of the bulk-copy variant (ring depth, operator-block source)
-    float tma_ms[6] = {0, 0, 0, 0, 0, 0};  // its measured stage time per configuration (kTmaConfigs)
+    float tma_ms[8] = {0, 0, 0, 0, 0, 0, 0, 0};  // its measured stage time per configuration (kTmaConfigs)
     // request pipeline of amdg_rk3ssp_serve_host: two device states, copy-in / copy-out streams,
     // events (in_done[2], stepped[2], out_done[2]); created on first use
     double* d_io[2] = {nullptr, nullptr};

@@ -255,8 +255,11 @@ static cudaError_t launch_col_t(const LinearLaunch& L, const T* blocks, const X*
 // (LDG false) or is read by every lane from the L1-resident table, issued
 // before the wait on the slot (LDG true, one bulk copy per neighbour).
 constexpr uint32_t kSpinLimit = 1u << 22;
-constexpr int kTmaRing[kTmaConfigs] = {3, 3, 6, 2, 4, 1};
-constexpr bool kTmaLdg[kTmaConfigs] = {false, true, true, true, true, true};
+// ... and WARPS elements per CTA (independent warps, each with its own slots and accumulator),
+// which lifts the limit of resident CTAs per SM when a warp's share of shared memory is small.
+constexpr int kTmaRing[kTmaConfigs] = {3, 3, 6, 2, 4, 1, 1, 1};
+constexpr bool kTmaLdg[kTmaConfigs] = {false, true, true, true, true, true, true, true};
+constexpr int kTmaWarps[kTmaConfigs] = {1, 1, 1, 1, 1, 1, 2, 4};
 
 __device__ __forceinline__ uint32_t smem_u32(const void* p) { return uint32_t(__cvta_generic_to_shared(p)); }
 
@@ -294,23 +297,32 @@ __device__ __forceinline__ void bulk_copy_g2s(void* dst, const void* src, uint32
                  : "memory");
 }
 
-template <int D, int NP, int kRing, bool LDG>
-__global__ void __launch_bounds__(32) linear_tma_kernel(const float* __restrict__ xs, const int32_t* __restrict__ row_ptr,
-                                                        const int2* __restrict__ pairs, const float* __restrict__ blocks,
-                                                        int nblocks, int64_t num_elements, DFState df, int* err) {
+template <int D, int NP, int kRing, bool LDG, int WPC>
+__global__ void __launch_bounds__(32 * WPC) linear_tma_kernel(const float* __restrict__ xs,
+                                                              const int32_t* __restrict__ row_ptr,
+                                                              const int2* __restrict__ pairs,
+                                                              const float* __restrict__ blocks, int nblocks,
+                                                              int64_t num_elements, DFState df, int* err) {
     constexpr int B = IPow<NP, D>::v;
     constexpr int C = B / NP;
     constexpr int CPT = (C + 31) / 32;  // columns per lane
     constexpr int BS = (NP * NP + 3) / 4 * 4;
     constexpr int DATA = (B + 3) / 4 * 4 + 4;  // floats: an aligned superset of any block
     constexpr int SLOT = DATA + (LDG ? 0 : BS);  // then (copied) the 1D operator block
-    __shared__ __align__(128) float ring[kRing * SLOT];
-    __shared__ float y[B];
-    __shared__ __align__(8) uint64_t full[kRing];
-    __shared__ int lead[kRing];                // floats before the block in its slot
-    __shared__ int bidx[kRing];                // LDG: the slot's 1D operator block in the table
-    const int lane = threadIdx.x;
-    const int64_t e = blockIdx.x;
+    __shared__ __align__(128) float ring_all[WPC * kRing * SLOT];
+    __shared__ float y_all[WPC * B];
+    __shared__ __align__(8) uint64_t full_all[WPC * kRing];
+    __shared__ int lead_all[WPC * kRing];  // floats before the block in its slot
+    __shared__ int bidx_all[WPC * kRing];  // LDG: the slot's 1D operator block in the table
+    // warp w of the CTA owns element blockIdx.x * WPC + w and its own share of every array
+    // (SLOT is a multiple of 4 floats, so every warp's slots stay 16-byte aligned)
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    float* ring = ring_all + warp * kRing * SLOT;
+    float* y = y_all + warp * B;
+    uint64_t* full = full_all + warp * kRing;
+    int* lead = lead_all + warp * kRing;
+    int* bidx = bidx_all + warp * kRing;
+    const int64_t e = int64_t(blockIdx.x) * WPC + warp;
     if (e >= num_elements) return;
     for (int i = lane; i < B; i += 32) y[i] = 0.f;
     const int beg = __ldg(row_ptr + e * D), n = __ldg(row_ptr + e * D + D) - beg;
@@ -431,19 +443,23 @@ __global__ void __launch_bounds__(32) linear_tma_kernel(const float* __restrict_
     for (int i = lane; i < B; i += 32) df_stage_update(df, e * B + i, y[i]);
 }
 
-// the ring, the accumulator and the mbarriers must fit the static shared-memory limit (48 KB)
-constexpr bool tma_fits(int B, int np, int ring, bool ldg) {
-    return B / np <= 256 && size_t(ring * ((B + 3) / 4 * 4 + 4 + (ldg ? 0 : 16)) + B) * sizeof(float) + 512 <= 48 * 1024;
+// the rings, the accumulators and the mbarriers must fit the static shared-memory limit (48 KB)
+constexpr bool tma_fits(int B, int np, int ring, bool ldg, int warps) {
+    return B / np <= 256 &&
+           size_t(warps) * (size_t(ring * ((B + 3) / 4 * 4 + 4 + (ldg ? 0 : 16)) + B) * sizeof(float) + 512) <=
+               48 * 1024;
 }
 
 template <int D, int NP, int CFG>
 static cudaError_t launch_tma_cfg(const LinearLaunch& L, cudaStream_t st) {
     constexpr int B = IPow<NP, D>::v;
-    if constexpr (!tma_fits(B, NP, kTmaRing[CFG], kTmaLdg[CFG])) {
+    constexpr int W = kTmaWarps[CFG];
+    if constexpr (!tma_fits(B, NP, kTmaRing[CFG], kTmaLdg[CFG], W)) {
         return cudaErrorInvalidValue;
     } else {
         if (L.num_elements == 0) return cudaSuccess;
-        linear_tma_kernel<D, NP, kTmaRing[CFG], kTmaLdg[CFG]><<<unsigned(L.num_elements), 32, 0, st>>>(
+        const int64_t grid = (L.num_elements + W - 1) / W;
+        linear_tma_kernel<D, NP, kTmaRing[CFG], kTmaLdg[CFG], W><<<unsigned(grid), 32 * W, 0, st>>>(
             L.us_shadow, L.row_ptr, L.pairs, L.blocks32p, L.num_blocks, L.num_elements, L.df, L.err);
         return cudaGetLastError();
     }
@@ -457,6 +473,8 @@ static cudaError_t launch_tma_t(const LinearLaunch& L, cudaStream_t st) {
         case 3: return launch_tma_cfg<D, NP, 3>(L, st);
         case 4: return launch_tma_cfg<D, NP, 4>(L, st);
         case 5: return launch_tma_cfg<D, NP, 5>(L, st);
+        case 6: return launch_tma_cfg<D, NP, 6>(L, st);
+        case 7: return launch_tma_cfg<D, NP, 7>(L, st);
         default: return launch_tma_cfg<D, NP, 0>(L, st);
     }
 }
@@ -465,7 +483,7 @@ bool linear_tma_supported(int dim, int np, int cfg) {
     int B = 1;
     for (int d = 0; d < dim; ++d) B *= np;
     if (cfg < 0 || cfg >= kTmaConfigs) return false;
-    return tma_fits(B, np, kTmaRing[cfg], kTmaLdg[cfg]);
+    return tma_fits(B, np, kTmaRing[cfg], kTmaLdg[cfg], kTmaWarps[cfg]);
 }
 
 bool linear_col_supported(int dim, int np) {

@@ -88,7 +88,7 @@ constexpr int kReduceBlocks = 1216;  // 8 CTAs per SM on 152 SMs
 cudaError_t launch_linear(const LinearLaunch& L, bool mixed, StageCoef rk, cudaStream_t st);
 // Variant 2 needs the FP32 stage state with 16-byte aligned array bases and
 // at least 16 bytes readable past the last coefficient.
-constexpr int kTmaConfigs = 6;
+constexpr int kTmaConfigs = 8;
 bool linear_tma_supported(int dim, int np, int cfg = 0);
 bool linear_col_supported(int dim, int np);
 // FP64 vector <-> FP32 (hi, lo) pairs

@@ -429,7 +429,7 @@ class LinearOperator:
     def copy_config(self):
         """(configuration of the bulk-copy variant, stage ms per configuration)."""
         c = C.c_int()
-        ms = np.zeros(6, np.float32)
+        ms = np.zeros(8, np.float32)
         _ck(load().amdg_linear_copy_config(self._h, C.byref(c), _ptr(ms)), "linear_copy_config")
         return c.value, ms.tolist()
 

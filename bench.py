@@ -288,8 +288,9 @@ def run_ours(args):
                      "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum of one launch of this "
                                        "workload's stage kernel (bytes)", "peak_kind": pk_kind,
                      "kernel": {0: "linear_apply_kernel<6,3,float,float>", 1: "linear_col_kernel<6,3,float,float>",
-                                2: "linear_tma_kernel<6,3,%d,%d>" % ((3, 0), (3, 1), (6, 1), (2, 1), (4, 1),
-                                                                      (1, 1))[op.copy_config()[0]]}[
+                                2: "linear_tma_kernel<6,3,%d,%d,%d>" % ((3, 0, 1), (3, 1, 1), (6, 1, 1), (2, 1, 1), (4, 1, 1),
+                                                                         (1, 1, 1), (1, 1, 2),
+                                                                         (1, 1, 4))[op.copy_config()[0]]}[
                                     op.tuning()[0][1]] + " (fused RK3 stage, FP32-pair stage state)",
                      "kernel_ms": k32 * 1e3,
                      "algorithmic_bytes_per_launch": bytes_per_launch,
@@ -308,7 +309,9 @@ def run_ours(args):
                                           "stage_ms_by_config": op.copy_config()[1],
                                           "configs": ["3 slots, operator block copied", "3 slots, operator block "
                                                       "from the L1 table", "6 slots, table", "2 slots, table",
-                                                      "4 slots, table", "1 slot, table"]},
+                                                      "4 slots, table", "1 slot, table",
+                                                      "1 slot, table, 2 elements per CTA",
+                                                      "1 slot, table, 4 elements per CTA"]},
                      "legend": "variant 0 = thread per output, 1 = column variant, "
                                "2 = column variant fed by bulk asynchronous copies (mixed only)"},
         "clocks": clocks,

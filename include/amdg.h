@@ -222,9 +222,9 @@ amdg_status amdg_linear_tuning(const amdg_linear_op* op, int* variants, float* s
 amdg_status amdg_linear_set_variant(amdg_linear_op* op, amdg_precision prec, int variant);
 /* Configuration of the bulk-copy variant (variant 2), picked by the same autotuner: 0 = 3-slot
  * ring with the 1D operator block copied into the slot, 1 = 3 slots with the operator block read
- * from the (L1-resident) table, 2 / 3 / 4 / 5 = 6 / 2 / 4 / 1 slots with the table read.
- * stage_ms[6]: measured stage time per configuration (0 where not timed).  All configurations sum
- * in the same order. */
+ * from the (L1-resident) table, 2 / 3 / 4 / 5 = 6 / 2 / 4 / 1 slots with the table read, 6 / 7 =
+ * 1 slot with 2 / 4 elements (warps) per CTA.  stage_ms[8]: measured stage time per configuration
+ * (0 where not timed).  All configurations sum in the same order. */
 amdg_status amdg_linear_copy_config(const amdg_linear_op* op, int* config, float* stage_ms);
 amdg_status amdg_linear_set_copy_config(amdg_linear_op* op, int config);
 /* BilinearForm::multi (BilinearForm.h:23): d_rhs = L d_u, device pointers of

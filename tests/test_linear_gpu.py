@@ -215,14 +215,14 @@ def test_kernel_variants_agree_on_mixed_steps(ctx):
     assert np.abs(out[0] - out[1]).max() <= 1e-6 * ref
     # the bulk-copy variant's configurations (ring depth, operator-block source) agree bitwise
     op.set_variant(amdg.MIXED, 2)
-    for cfg in (0, 1, 2, 3, 4, 5):
+    for cfg in range(8):
         g.set_coefficients(u0)
         op.set_copy_config(cfg)
         op.rk3_steps(1e-3, 2, amdg.MIXED)
         ctx.synchronize()
         assert np.array_equal(g.coefficients(), out[2]), f"copy configuration {cfg}"
     with pytest.raises(amdg.AmdgError):
-        op.set_copy_config(6)
+        op.set_copy_config(8)
     with pytest.raises(amdg.AmdgError):
         op.set_variant(amdg.FP64, 2)
     op.close()
