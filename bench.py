@@ -36,7 +36,7 @@ COEF = [1.0] * DIM
 CFL = 0.1
 # DRAM bytes of one mixed stage launch of the 6D N=8 workload, per kernel variant, from ncu
 # (dram__bytes_read.sum + dram__bytes_write.sum; variant 0 was not captured)
-NCU_TRAFFIC_BYTES = {1: (720.902 + 241.610) * 1e6, 2: (442.000 + 237.598) * 1e6}
+NCU_TRAFFIC_BYTES = {1: (720.902 + 241.610) * 1e6, 2: (441.076 + 236.082) * 1e6}
 METRIC = "DOF-stage updates/s at matched L2 error: plain FP64 vs mixed+learned-adapt"
 WORKLOAD = "6D linear advection, sparse grid N=8, Alpert k=2, SSP-RK3 (34,455,456 DOF)"
 
