@@ -298,12 +298,12 @@ struct amdg_linear_op {
     float variant_ms[2][3] = {{0, 0, 0}, {0, 0, 0}};  // measured stage time [precision][variant]
     int tma_cfg = 0;                 // configuration of the bulk-copy variant (ring depth, operator-block source)
     float tma_ms[8] = {0, 0, 0, 0, 0, 0, 0, 0};  // its measured stage time per configuration (kTmaConfigs)
-    // request pipeline of amdg_rk3ssp_serve_host: two device states, copy-in / copy-out streams,
-    // events (in_done[2], stepped[2], out_done[2]); created on first use
-    double* d_io[2] = {nullptr, nullptr};
+    // request pipeline of amdg_rk3ssp_serve_host: three device states, copy-in / copy-out
+    // streams, events (in_done[3], stepped[3], out_done[3]); created on first use
+    double* d_io[3] = {nullptr, nullptr, nullptr};
     int64_t io_capacity = 0;
     void* io_stream[2] = {nullptr, nullptr};
-    void* io_event[6] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
+    void* io_event[9] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
 };
 
 struct amdg_burgers_op {

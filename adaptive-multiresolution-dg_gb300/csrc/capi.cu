@@ -927,8 +927,7 @@ amdg_status amdg_linear_destroy(amdg_linear_op* op) {
     cudaFree(op->d_err);
     cudaFree(op->d_shadow);
     cudaFree(op->d_lo);
-    cudaFree(op->d_io[0]);
-    cudaFree(op->d_io[1]);
+    for (double* p : op->d_io) cudaFree(p);
     for (void* e : op->io_event)
         if (e) cudaEventDestroy(static_cast<cudaEvent_t>(e));
     for (void* c : op->io_stream)
@@ -1041,14 +1040,15 @@ amdg_status amdg_rk3ssp_serve_host(amdg_linear_op* op, double dt, int nsteps, am
     if (s != AMDG_OK) return s;
     if ((s = linear_sync(op)) != AMDG_OK) return s;
     const size_t bytes = size_t(g->dof) * sizeof(double);
+    constexpr int NB = 3;  // device states: request r is copied in while r - 1 steps and r - 2 is copied out
     if (!op->d_io[0] || op->io_capacity < g->dof) {
-        cudaFree(op->d_io[0]);
-        cudaFree(op->d_io[1]);
-        op->d_io[0] = op->d_io[1] = nullptr;
+        for (int b = 0; b < NB; ++b) {
+            cudaFree(op->d_io[b]);
+            op->d_io[b] = nullptr;
+        }
         op->io_capacity = 0;
-        if ((s = dev_alloc(&op->d_io[0], size_t(g->dof))) != AMDG_OK ||
-            (s = dev_alloc(&op->d_io[1], size_t(g->dof))) != AMDG_OK)
-            return s;
+        for (int b = 0; b < NB; ++b)
+            if ((s = dev_alloc(&op->d_io[b], size_t(g->dof))) != AMDG_OK) return s;
         op->io_capacity = g->dof;
     }
     if (!op->io_stream[0]) {
@@ -1057,7 +1057,7 @@ amdg_status amdg_rk3ssp_serve_host(amdg_linear_op* op, double dt, int nsteps, am
             AMDG_CK(cudaStreamCreateWithFlags(&c, cudaStreamNonBlocking));
             op->io_stream[i] = c;
         }
-        for (int i = 0; i < 6; ++i) {
+        for (int i = 0; i < 3 * NB; ++i) {
             cudaEvent_t e = nullptr;
             AMDG_CK(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
             op->io_event[i] = e;
@@ -1067,15 +1067,18 @@ amdg_status amdg_rk3ssp_serve_host(amdg_linear_op* op, double dt, int nsteps, am
     cudaStream_t in_st = static_cast<cudaStream_t>(op->io_stream[0]);
     cudaStream_t out_st = static_cast<cudaStream_t>(op->io_stream[1]);
     // per buffer b: copied in, stepped, copied out
-    cudaEvent_t in_done[2] = {static_cast<cudaEvent_t>(op->io_event[0]), static_cast<cudaEvent_t>(op->io_event[1])};
-    cudaEvent_t stepped[2] = {static_cast<cudaEvent_t>(op->io_event[2]), static_cast<cudaEvent_t>(op->io_event[3])};
-    cudaEvent_t out_done[2] = {static_cast<cudaEvent_t>(op->io_event[4]), static_cast<cudaEvent_t>(op->io_event[5])};
+    cudaEvent_t in_done[NB], stepped[NB], out_done[NB];
+    for (int b = 0; b < NB; ++b) {
+        in_done[b] = static_cast<cudaEvent_t>(op->io_event[b]);
+        stepped[b] = static_cast<cudaEvent_t>(op->io_event[NB + b]);
+        out_done[b] = static_cast<cudaEvent_t>(op->io_event[2 * NB + b]);
+    }
     // earlier work on the context stream (the grid's state, the operator's tables) comes first
     AMDG_CK(cudaEventRecord(stepped[0], st));
     AMDG_CK(cudaStreamWaitEvent(in_st, stepped[0], 0));
     auto copy_in = [&](int r) -> amdg_status {
-        const int b = r & 1;
-        if (r >= 2) AMDG_CK(cudaStreamWaitEvent(in_st, out_done[b], 0));  // buffer b's previous result is out
+        const int b = r % NB;
+        if (r >= NB) AMDG_CK(cudaStreamWaitEvent(in_st, out_done[b], 0));  // buffer b's previous result is out
         AMDG_CK(cudaMemcpyAsync(op->d_io[b], host_in[r], bytes, cudaMemcpyHostToDevice, in_st));
         AMDG_CK(cudaEventRecord(in_done[b], in_st));
         return AMDG_OK;
@@ -1083,7 +1086,7 @@ amdg_status amdg_rk3ssp_serve_host(amdg_linear_op* op, double dt, int nsteps, am
     // request r + 1 is copied in while request r is stepped and request r - 1 copied out
     if (nreq > 0 && (s = copy_in(0)) != AMDG_OK) return s;
     for (int r = 0; r < nreq; ++r) {
-        const int b = r & 1;
+        const int b = r % NB;
         if (r + 1 < nreq && (s = copy_in(r + 1)) != AMDG_OK) return s;
         AMDG_CK(cudaStreamWaitEvent(st, in_done[b], 0));
         if ((s = rk3_steps_device(op, dt, nsteps, prec, op->d_io[b], false)) != AMDG_OK) return s;

@@ -241,8 +241,9 @@ amdg_status amdg_rk3ssp_steps_host(amdg_linear_op* op, double dt, int nsteps, do
 /* Serving form of amdg_rk3ssp_steps_host, no reference counterpart: nreq independent requests
  * on the operator's grid, request r stepped from host_in[r] (dof doubles) into host_out[r]
  * (host_out[r] may equal host_in[r]).  Request r + 1 is copied in and request r - 1 copied out
- * while request r is stepped (two device states, one copy stream per direction); pinned host
- * buffers let the copies overlap.  The grid's own coefficients are left unchanged. */
+ * while request r is stepped (three device states, one copy stream per direction); pinned host
+ * buffers let the copies overlap.  Requests are independent: an output buffer must not be the
+ * input of a later request of the same call.  The grid's own coefficients are left unchanged. */
 amdg_status amdg_rk3ssp_serve_host(amdg_linear_op* op, double dt, int nsteps, amdg_precision prec, int nreq,
                                    const double* const* host_in, double* const* host_out);
 
