@@ -322,6 +322,7 @@ struct amdg_burgers_op {
     double *d_a2p = nullptr, *d_lv = nullptr, *d_lvx = nullptr, *d_lflx = nullptr, *d_ajump = nullptr;
     float *f_a2p = nullptr, *f_lv = nullptr, *f_lvx = nullptr, *f_lflx = nullptr, *f_ajump = nullptr;
     double *d_a2pd = nullptr, *d_ljv = nullptr, *d_pts = nullptr;  // wave: derivative and jump tables, point coordinates
+    void *df_a2p = nullptr, *df_a2pd = nullptr;  // double-float (float2 hi, lo) copies for the mixed point values
     float *f_a2pd = nullptr, *f_ljv = nullptr;
     void* w_fields = nullptr;        // wave: (dim+1) coefficient-weighted point fields and their surpluses, 2 (dim+1) x E x p1^dim doubles
     double *d_v1 = nullptr, *d_su = nullptr, *d_sv = nullptr;  // wave: RK4ODE2nd stage v and running sums

@@ -11,6 +11,7 @@
 #include <cstring>
 #include <new>
 #include <string>
+#include <type_traits>
 #include <vector>
 
 #include "amdg.h"
@@ -75,6 +76,24 @@ Mats<double> mats64(const amdg_burgers_op* op) {
 }
 Mats<float> mats32(const amdg_burgers_op* op) {
     return {{op->f_a2p, op->f_lv, op->f_lvx, op->f_lflx, op->f_ajump, op->f_a2pd, op->f_ljv}};
+}
+// double-float tables: only those of the point values
+Mats<float2> mats_df(const amdg_burgers_op* op) {
+    return {{static_cast<const float2*>(op->df_a2p), nullptr, nullptr, nullptr, nullptr,
+             static_cast<const float2*>(op->df_a2pd), nullptr}};
+}
+
+// a table as double-float pairs (hi = float(v), lo = float(v - hi))
+amdg_status upload_df(void** p, const std::vector<double>& host) {
+    std::vector<float2> h(host.size());
+    for (size_t i = 0; i < host.size(); ++i) {
+        const float hi = float(host[i]);
+        h[i] = make_float2(hi, float(host[i] - double(hi)));
+    }
+    float2* d = nullptr;
+    amdg_status s = upload_vec(&d, h);
+    *p = d;
+    return s;
 }
 
 int ipow(int b, int e) {
@@ -249,6 +268,29 @@ amdg_status eval_point_values(amdg_burgers_op* op, const Mats<T>& m, const T* u,
     return AMDG_OK;
 }
 
+// u_h at the interpolation points in double-float arithmetic (the mixed mode): the sweeps on the
+// FP32 pipe with about 48-bit precision, the slices summed in FP64 into up, or, when fp is
+// given, f(u) = u^2/2 at the points into fp
+amdg_status eval_point_values_df(amdg_burgers_op* op, const double* u, double* up, double* fp, cudaStream_t st) {
+    const int np = op->grid->host.k + 1;
+    const int64_t n = op->grid->host.num_elements * op->points;
+    float2* udf = static_cast<float2*>(op->w_u);
+    AMDG_CK(launch_to_df(u, udf, op->grid->dof, st));
+    op->grid->ctx->launches++;
+    float2* slots = static_cast<float2*>(op->w_slots);
+    const float2* src[1] = {udf};
+    for (int c0 = 0; c0 < op->n_pv_terms; c0 += op->chunk) {
+        const int cnt = std::min(op->chunk, op->n_pv_terms - c0);
+        if (amdg_status r = run_terms<float2>(op, mats_df(op), c0, cnt, np, op->p1, src, 1, nullptr, slots, st);
+            r != AMDG_OK)
+            return r;
+        const bool last = c0 + cnt == op->n_pv_terms;
+        AMDG_CK(launch_reduce_points_df(slots, cnt, n, c0 == 0 ? 1 : 0, up, last ? fp : nullptr, st));
+        op->grid->ctx->launches++;
+    }
+    return AMDG_OK;
+}
+
 // interpolation coefficients from values at the points: dim surplus passes
 // (w_a / w_b as ping-pong buffers), the last one into `out` (type To)
 template <typename T, typename To>
@@ -327,28 +369,46 @@ amdg_status eval_wave_fields(amdg_burgers_op* op, const double* u, To** fucoe, c
     const int dim = g->host.dim, np = g->host.k + 1;
     const int64_t E = g->host.num_elements, n = E * op->points;
     const int G = int(op->sched_dims.size());  // terms per point field
-    double* slots = static_cast<double*>(op->w_slots);
     double* fields = static_cast<double*>(op->w_fields);
     const size_t stride = size_t(op->capacity) * op->points;
-    const double* src[1] = {u};
+    // the mixed mode (FP32 coefficients out) computes the point values in double-float
+    constexpr bool df = std::is_same<To, float>::value;
+    using Tp = typename std::conditional<df, float2, double>::type;
+    Tp* slots = static_cast<Tp*>(op->w_slots);
+    const Tp* src[1];
+    if constexpr (df) {
+        AMDG_CK(launch_to_df(u, static_cast<float2*>(op->w_u), g->dof, st));
+        op->grid->ctx->launches++;
+        src[0] = static_cast<const float2*>(op->w_u);
+    } else {
+        src[0] = u;
+    }
+    const Mats<Tp> m = [&] {
+        if constexpr (df) return mats_df(op);
+        else return mats64(op);
+    }();
     for (int f = 0; f <= dim; ++f) {
         double* kp = fields + size_t(f) * stride;  // K times the point values of field f
         double* acc = static_cast<double*>(op->w_up);
         for (int c0 = 0; c0 < G; c0 += op->chunk) {
             const int cnt = std::min(op->chunk, G - c0);
-            if (amdg_status r = run_terms<double>(op, mats64(op), f * G + c0, cnt, np, op->p1, src, 1, nullptr, slots, st);
+            if (amdg_status r = run_terms<Tp>(op, m, f * G + c0, cnt, np, op->p1, src, 1, nullptr, slots, st);
                 r != AMDG_OK)
                 return r;
+            auto fold = [&](int first) -> cudaError_t {  // the slices into acc, in FP64
+                if constexpr (df) return launch_reduce_points_df(slots, cnt, n, first, acc, nullptr, st);
+                else return launch_reduce_points<double>(slots, cnt, n, first, acc, nullptr, st);
+            };
             if (c0 + cnt == G) {
                 if (c0 > 0) {  // earlier chunks were summed into acc: fold them in as one more slice
-                    AMDG_CK(launch_reduce_points<double>(slots, cnt, n, 0, acc, nullptr, st));
+                    AMDG_CK(fold(0));
                     AMDG_CK(launch_reduce_points_coef(acc, 1, E, dim, op->p1, g->d_order, op->d_pts, op->amp, kp, st));
                     op->grid->ctx->launches++;
                 } else {
                     AMDG_CK(launch_reduce_points_coef(slots, cnt, E, dim, op->p1, g->d_order, op->d_pts, op->amp, kp, st));
                 }
             } else {
-                AMDG_CK(launch_reduce_points<double>(slots, cnt, n, c0 == 0 ? 1 : 0, acc, nullptr, st));
+                AMDG_CK(fold(c0 == 0 ? 1 : 0));
             }
             op->grid->ctx->launches++;
         }
@@ -384,7 +444,9 @@ amdg_status eval_rhs(amdg_burgers_op* op, const double* u, double* rhs, amdg_pre
         return eval_back_transforms<float>(op, mats32(op), fc, dim + 1, u32, rhs, so, st);
     }
     double* fp = static_cast<double*>(op->w_a);
-    amdg_status r = eval_point_values<double>(op, mats64(op), u, static_cast<double*>(op->w_up), fp, st);
+    amdg_status r = prec == AMDG_PREC_FP64
+                        ? eval_point_values<double>(op, mats64(op), u, static_cast<double*>(op->w_up), fp, st)
+                        : eval_point_values_df(op, u, static_cast<double*>(op->w_up), fp, st);
     if (r != AMDG_OK) return r;
     if (prec == AMDG_PREC_FP64) {
         double* fu = static_cast<double*>(op->w_fu);
@@ -572,6 +634,7 @@ static amdg_status lagr_create(amdg_grid* g, int kind, const double* alpha, doub
         (kind == 1 && ((s = upload_both(&op->d_a2pd, &op->f_a2pd, t.a2pd)) != AMDG_OK ||
                        (s = upload_both(&op->d_ljv, &op->f_ljv, t.ljv)) != AMDG_OK ||
                        (s = upload_vec(&op->d_pts, t.pts)) != AMDG_OK)) ||
+        (s = upload_df(&op->df_a2p, t.a2p)) != AMDG_OK || (kind == 1 && (s = upload_df(&op->df_a2pd, t.a2pd)) != AMDG_OK) ||
         (s = upload_vec(&op->d_anc_point, t.anc_point)) != AMDG_OK || (s = upload_vec(&op->d_anc_rank, t.anc_rank)) != AMDG_OK ||
         (s = upload_vec(&op->d_terms, op->terms)) != AMDG_OK || (s = burgers_sync(op)) != AMDG_OK) {
         amdg_burgers_destroy(op);
@@ -598,7 +661,7 @@ amdg_status amdg_burgers_destroy(amdg_burgers_op* op) {
                     op->d_u1, op->d_u2, op->d_rhs64, op->d_pred, op->d_vol_split, op->d_flx_split,
                     op->d_pg,
                     op->d_feat, op->d_prob, op->d_a2pd, op->d_ljv, op->d_pts, op->f_a2pd, op->f_ljv,
-                    op->w_fields, op->d_v1, op->d_su, op->d_sv};
+                    op->w_fields, op->d_v1, op->d_su, op->d_sv, op->df_a2p, op->df_a2pd};
     for (void* p : ptrs) cudaFree(p);
     delete op;
     return AMDG_OK;

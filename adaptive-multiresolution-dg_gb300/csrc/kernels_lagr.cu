@@ -22,6 +22,53 @@
 
 namespace amdg {
 
+// ---- double-float arithmetic (float2 = hi + lo, |lo| <= ulp(hi)/2, about 48 bits) -------------
+// The error-free transformations two-sum (Knuth) and the FMA-based exact product, combined as in
+// the double-double algorithms of Hida, Li and Bailey ("accurate" addition): the point-value
+// sweeps of the mixed mode run on the FP32 pipe with near-FP64 accuracy.
+__device__ __forceinline__ float2 df_two_sum(float a, float b) {
+    const float s = a + b;
+    const float bb = s - a;
+    return make_float2(s, (a - (s - bb)) + (b - bb));
+}
+__device__ __forceinline__ float2 df_quick_two_sum(float a, float b) {
+    const float s = a + b;
+    return make_float2(s, b - (s - a));
+}
+__device__ __forceinline__ float2 df_add(float2 a, float2 b) {
+    float2 s = df_two_sum(a.x, b.x);
+    const float2 t = df_two_sum(a.y, b.y);
+    s.y += t.x;
+    s = df_quick_two_sum(s.x, s.y);
+    s.y += t.y;
+    return df_quick_two_sum(s.x, s.y);
+}
+__device__ __forceinline__ float2 df_mul(float2 a, float2 b) {
+    const float p = a.x * b.x;
+    float e = fmaf(a.x, b.x, -p);
+    e = fmaf(a.x, b.y, e);
+    e = fmaf(a.y, b.x, e);
+    return df_quick_two_sum(p, e);
+}
+
+// the sweep's arithmetic for T = double, float or float2 (double-float)
+__device__ __forceinline__ double madd(double x, double m, double acc) { return fma(x, m, acc); }
+__device__ __forceinline__ float madd(float x, float m, float acc) { return fmaf(x, m, acc); }
+__device__ __forceinline__ float2 madd(float2 x, float2 m, float2 acc) { return df_add(df_mul(x, m), acc); }
+__device__ __forceinline__ double scale(double a, double c) { return a * c; }
+__device__ __forceinline__ float scale(float a, float c) { return a * c; }
+__device__ __forceinline__ float2 scale(float2 a, float2 c) { return df_mul(a, c); }
+template <typename T>
+__device__ __forceinline__ T from_double(double v) { return T(v); }
+template <>
+__device__ __forceinline__ float2 from_double<float2>(double v) {
+    const float hi = float(v);
+    return make_float2(hi, float(v - double(hi)));
+}
+__device__ __forceinline__ double to_double(double v) { return v; }
+__device__ __forceinline__ double to_double(float v) { return double(v); }
+__device__ __forceinline__ double to_double(float2 v) { return double(v.x) + double(v.y); }
+
 // acc + sum over four neighbours j (in order) and k < NF of x[j][k*stride] * m[j][k*ncols],
 // all operands loaded before the first multiply-add
 template <int NF, typename T>
@@ -37,7 +84,7 @@ __device__ __forceinline__ T fibre_quad(const T* const* x, const T* const* m, in
 #pragma unroll
     for (int j = 0; j < 4; ++j)
 #pragma unroll
-        for (int k = 0; k < NF; ++k) acc = fma(xv[j][k], mv[j][k], acc);
+        for (int k = 0; k < NF; ++k) acc = madd(xv[j][k], mv[j][k], acc);
     return acc;
 }
 
@@ -63,7 +110,7 @@ __global__ void __launch_bounds__(256) sweep_kernel(SweepArgs<T> a) {
         M = a.mats[D.mat[a.sweep]];
         n_from = a.n_in;
         n_to = a.n_out;
-        coef = a.sweep == 0 ? T(D.coef) : T(1);
+        coef = from_double<T>(a.sweep == 0 ? D.coef : 1.0);
         in = a.sweep == 0 ? a.src[D.src] : a.in + int64_t(slot) * a.in_slice;
         // block shape: n_out along the dimensions already transformed, n_in elsewhere
         int done_after = 0;
@@ -76,7 +123,7 @@ __global__ void __launch_bounds__(256) sweep_kernel(SweepArgs<T> a) {
         flx = 1;
         M = a.mats[kMatAJump];
         n_from = n_to = a.np;
-        coef = T(D.coef);
+        coef = from_double<T>(D.coef);
         in = a.pen_in;
         for (int d = 0; d < a.dim - 1 - t; ++d) stride *= a.np;
         for (int d = 0; d < a.dim; ++d) in_block *= a.np;
@@ -96,7 +143,7 @@ __global__ void __launch_bounds__(256) sweep_kernel(SweepArgs<T> a) {
     const T* mcol = M + size_t(oe) * n_to + qt;
     const int in_off = outer * n_from * stride + inner;
     const size_t mstep = size_t(n_from) * ncols;
-    T acc = T(0);
+    T acc = from_double<T>(0.0);
     // four neighbours per pass: their (element, order) pairs and operands are
     // independent loads issued together; the sum keeps the neighbour order
     int i = beg;
@@ -117,16 +164,16 @@ __global__ void __launch_bounds__(256) sweep_kernel(SweepArgs<T> a) {
         else {
 #pragma unroll
             for (int j = 0; j < 4; ++j)
-                for (int k = 0; k < n_from; ++k) acc = fma(__ldg(x[j] + k * stride), __ldg(m[j] + size_t(k) * ncols), acc);
+                for (int k = 0; k < n_from; ++k) acc = madd(__ldg(x[j] + k * stride), __ldg(m[j] + size_t(k) * ncols), acc);
         }
     }
     for (; i < end; ++i) {
         const int2 nb = __ldg(nbr + i);
         const T* x = in + int64_t(nb.x) * in_block + in_off;
         const T* m = mcol + size_t(nb.y) * mstep;
-        for (int k = 0; k < n_from; ++k) acc = fma(__ldg(x + k * stride), __ldg(m + size_t(k) * ncols), acc);
+        for (int k = 0; k < n_from; ++k) acc = madd(__ldg(x + k * stride), __ldg(m + size_t(k) * ncols), acc);
     }
-    a.out[int64_t(slot) * per + r] = acc * coef;
+    a.out[int64_t(slot) * per + r] = scale(acc, coef);
 }
 
 template <typename T>
@@ -139,6 +186,7 @@ cudaError_t launch_sweep(const SweepArgs<T>& a, cudaStream_t st) {
 
 template cudaError_t launch_sweep<double>(const SweepArgs<double>&, cudaStream_t);
 template cudaError_t launch_sweep<float>(const SweepArgs<float>&, cudaStream_t);
+template cudaError_t launch_sweep<float2>(const SweepArgs<float2>&, cudaStream_t);
 
 template <typename T>
 __global__ void reduce_points_kernel(const T* __restrict__ buf, int count, int64_t n, int first, T* acc, T* fp) {
@@ -148,6 +196,24 @@ __global__ void reduce_points_kernel(const T* __restrict__ buf, int count, int64
     for (int s = 0; s < count; ++s) v += buf[int64_t(s) * n + i];
     if (fp) fp[i] = v * v * T(0.5);  // u^2/2
     else acc[i] = v;
+}
+
+// double-float slices summed in FP64 (each slice rounded to double first)
+__global__ void reduce_points_df_kernel(const float2* __restrict__ buf, int count, int64_t n, int first, double* acc,
+                                        double* fp) {
+    const int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    double v = first ? 0.0 : acc[i];
+    for (int s = 0; s < count; ++s) v += to_double(buf[int64_t(s) * n + i]);
+    if (fp) fp[i] = v * v * 0.5;  // u^2/2
+    else acc[i] = v;
+}
+
+cudaError_t launch_reduce_points_df(const float2* buf, int count, int64_t n, int first, double* acc, double* fp,
+                                    cudaStream_t st) {
+    if (n == 0) return cudaSuccess;
+    reduce_points_df_kernel<<<unsigned((n + 255) / 256), 256, 0, st>>>(buf, count, n, first, acc, fp);
+    return cudaGetLastError();
 }
 
 template <typename T>
@@ -234,7 +300,8 @@ cudaError_t launch_convert(const Ti* in, To* out, int64_t n, cudaStream_t st) {
 template cudaError_t launch_convert<double, float>(const double*, float*, int64_t, cudaStream_t);
 template cudaError_t launch_convert<float, double>(const float*, double*, int64_t, cudaStream_t);
 
-__global__ void reduce_points_coef_kernel(const double* __restrict__ buf, int count, int64_t E, int dim, int p1,
+template <typename Tin>
+__global__ void reduce_points_coef_kernel(const Tin* __restrict__ buf, int count, int64_t E, int dim, int p1,
                                           const int32_t* __restrict__ order, const double* __restrict__ pts, double amp,
                                           double* __restrict__ out) {
     int P = 1;
@@ -243,7 +310,7 @@ __global__ void reduce_points_coef_kernel(const double* __restrict__ buf, int co
     const int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
     if (i >= n) return;
     double v = 0.0;
-    for (int s = 0; s < count; ++s) v += buf[int64_t(s) * n + i];
+    for (int s = 0; s < count; ++s) v += to_double(buf[int64_t(s) * n + i]);
     const int64_t e = i / P;
     int r = int(i - e * P);
     // the coefficient function of the registered wave problem, at this point
@@ -259,12 +326,30 @@ __global__ void reduce_points_coef_kernel(const double* __restrict__ buf, int co
     out[i] = (c * c) * v;
 }
 
-cudaError_t launch_reduce_points_coef(const double* buf, int count, int64_t E, int dim, int p1, const int32_t* order,
+template <typename Tin>
+cudaError_t launch_reduce_points_coef(const Tin* buf, int count, int64_t E, int dim, int p1, const int32_t* order,
                                       const double* pts, double amp, double* out, cudaStream_t st) {
     int64_t n = E;
     for (int d = 0; d < dim; ++d) n *= p1;
     if (n == 0) return cudaSuccess;
-    reduce_points_coef_kernel<<<unsigned((n + 255) / 256), 256, 0, st>>>(buf, count, E, dim, p1, order, pts, amp, out);
+    reduce_points_coef_kernel<Tin><<<unsigned((n + 255) / 256), 256, 0, st>>>(buf, count, E, dim, p1, order, pts, amp,
+                                                                               out);
+    return cudaGetLastError();
+}
+
+template cudaError_t launch_reduce_points_coef<double>(const double*, int, int64_t, int, int, const int32_t*,
+                                                       const double*, double, double*, cudaStream_t);
+template cudaError_t launch_reduce_points_coef<float2>(const float2*, int, int64_t, int, int, const int32_t*,
+                                                       const double*, double, double*, cudaStream_t);
+
+__global__ void to_df_kernel(const double* __restrict__ in, float2* __restrict__ out, int64_t n) {
+    const int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (i < n) out[i] = from_double<float2>(in[i]);
+}
+
+cudaError_t launch_to_df(const double* in, float2* out, int64_t n, cudaStream_t st) {
+    if (n == 0) return cudaSuccess;
+    to_df_kernel<<<unsigned((n + 255) / 256), 256, 0, st>>>(in, out, n);
     return cudaGetLastError();
 }
 

@@ -43,11 +43,19 @@ cudaError_t launch_sweep(const SweepArgs<T>& a, cudaStream_t st);
 template <typename T>
 cudaError_t launch_reduce_points(const T* buf, int count, int64_t n, int first, T* acc, T* fp, cudaStream_t st);
 
-// Diffusion coefficient at the points: out = K(x) * sum_s buf[s] (in order), K = (1 + amp
+// The same from double-float slices (float2 = hi + lo), summed in FP64.
+cudaError_t launch_reduce_points_df(const float2* buf, int count, int64_t n, int first, double* acc, double* fp,
+                                    cudaStream_t st);
+
+// Diffusion coefficient at the points: out = K(x) * sum_s buf[s] (in order, in FP64), K = (1 + amp
 // prod_d sin(2 pi x_d))^2 at the point's coordinates (pts[order * p1 + p_d] per dimension,
-// p1 points per dimension).
-cudaError_t launch_reduce_points_coef(const double* buf, int count, int64_t E, int dim, int p1, const int32_t* order,
+// p1 points per dimension); buf double or double-float (float2).
+template <typename Tin>
+cudaError_t launch_reduce_points_coef(const Tin* buf, int count, int64_t E, int dim, int p1, const int32_t* order,
                                       const double* pts, double amp, double* out, cudaStream_t st);
+
+// double -> double-float (hi = float(v), lo = float(v - hi))
+cudaError_t launch_to_df(const double* in, float2* out, int64_t n, cudaStream_t st);
 
 // One RK4ODE2nd stage (ODESolver.cpp:579-615) given the right-hand side at (us, vs):
 // ku = dt vs, kv = dt rhs; stages 0-2 update (us, vs) from (un, vn) and the running sums
