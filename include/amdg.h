@@ -31,7 +31,7 @@
 extern "C" {
 #endif
 
-#define AMDG_ABI_VERSION 2
+#define AMDG_ABI_VERSION 3
 
 typedef enum amdg_status {
     AMDG_OK = 0,
