@@ -98,11 +98,12 @@ public:
     static inline int VEC_NUM = 1;
     static inline std::vector<int> ind_var_vec{0};
 
+    // the grid starts with the elements of levels up to level_init (sum of levels for a sparse grid)
     DGSolution(bool sparse, int level_init, int NMAX, AllBasis<AlptBasis>& all_bas, AllBasis<LagrBasis>&,
                AllBasis<HermBasis>&, Hash&)
         : nmax_(NMAX) {
-        if (level_init != NMAX) throw Error(AMDG_ERR_ARG, "DGSolution: level_init must equal NMAX");
-        check(amdg_grid_create(Runtime::context(), DIM, NMAX, all_bas.PMAX, sparse ? 1 : 0, &grid_), "amdg_grid_create");
+        check(amdg_grid_create_ex(Runtime::context(), DIM, level_init, NMAX, all_bas.PMAX, sparse ? 1 : 0, &grid_),
+              "amdg_grid_create_ex");
     }
     DGSolution(const DGSolution&) = delete;
     DGSolution& operator=(const DGSolution&) = delete;
@@ -142,6 +143,20 @@ public:
         check(amdg_grid_get_coefficients(grid_, u.data(), int64_t(u.size())), "amdg_grid_get_coefficients");
         return u;
     }
+    // Element::ucoe_ut of every element (second-order-in-time problems)
+    std::vector<double> ucoe_ut() const {
+        std::vector<double> v(size_basis_alpt());
+        check(amdg_grid_get_velocity(grid_, v.data(), int64_t(v.size())), "amdg_grid_get_velocity");
+        return v;
+    }
+    void copy_ucoe_to_ucoe_ut() {
+        const std::vector<double> u = coefficients();
+        check(amdg_grid_set_velocity(grid_, u.data(), int64_t(u.size())), "amdg_grid_set_velocity");
+    }
+    void set_ucoe_alpt_zero() {
+        const std::vector<double> z(size_basis_alpt(), 0.0);
+        check(amdg_grid_set_coefficients(grid_, z.data(), int64_t(z.size())), "amdg_grid_set_coefficients");
+    }
     amdg_grid* handle() const { return grid_; }
 
 protected:
@@ -157,10 +172,15 @@ public:
             bool /*is_find_ptr_general*/ = false)
         : DGSolution(sparse, level_init, NMAX, a, l, h, hash), eps_(eps), eta_(eta) {}
     void init_separable_scalar(std::function<double(double, int)> f) { init_separable_scalar_sum({f}); }
+    // projection with adaptive refinement from the starting level (DGAdapt.cpp:120-147); drivers
+    // that pass refine_eps = 1e10 get no refinement
     void init_separable_scalar_sum(std::vector<std::function<double(double, int)>> fns) {
         detail::SepFns sf{&fns};
-        check(amdg_grid_init_separable(grid_, int(fns.size()), detail::sep_trampoline, &sf), "amdg_grid_init_separable");
+        check(amdg_grid_init_separable_adaptive(grid_, int(fns.size()), detail::sep_trampoline, &sf, eps_),
+              "amdg_grid_init_separable_adaptive");
     }
+    void refine() { check(amdg_grid_refine(grid_, nullptr, eps_, nullptr), "amdg_grid_refine"); }
+    void coarsen() { check(amdg_grid_coarsen(grid_, eta_, nullptr), "amdg_grid_coarsen"); }
     double refine_eps() const { return eps_; }
     double coarsen_eta() const { return eta_; }
 
@@ -221,6 +241,33 @@ public:
 
 private:
     amdg_burgers_op* op_ = nullptr;
+};
+
+// ---- variable-coefficient wave equation (example/03_wave_06_var_coeff_adapt.cpp) ----
+// DiffusionRHS with the Lagrange-interpolated K grad u and K u, the IPDG penalty -sigma/dx [u][v]
+// and RK4ODE2nd, K = (1 + a prod_d sin(2 pi x_d))^2: the library registers the coefficient
+// function (a device function cannot be a host std::function).  adaptive_step runs the loop body
+// of the example (EulerODE2nd predictor, refine, four RK4ODE2nd stages, coarsen).
+class WaveLagrRHS {
+public:
+    WaveLagrRHS(DGSolution& dg, double sigma_ipdg, double amplitude = 0.5) {
+        check(amdg_wave_create(dg.handle(), sigma_ipdg, amplitude, &op_), "amdg_wave_create");
+    }
+    WaveLagrRHS(const WaveLagrRHS&) = delete;
+    ~WaveLagrRHS() { amdg_wave_destroy(op_); }
+    void rk4_step(double dt, amdg_precision prec = AMDG_PREC_FP64) {
+        check(amdg_wave_rk4_steps(op_, dt, 1, prec), "amdg_wave_rk4_steps");
+    }
+    // one adaptive step; returns the dt taken (cfl / sum_d wave_speed 2^maxlevel_d)
+    double adaptive_step(double cfl, double wave_speed, double eps, double eta, amdg_precision prec = AMDG_PREC_FP64) {
+        double dt = 0;
+        check(amdg_wave_adaptive_step(op_, cfl, wave_speed, eps, eta, prec, &dt), "amdg_wave_adaptive_step");
+        return dt;
+    }
+    amdg_wave_op* handle() const { return op_; }
+
+private:
+    amdg_wave_op* op_ = nullptr;
 };
 
 inline void synchronize() { check(amdg_context_synchronize(Runtime::context()), "amdg_context_synchronize"); }

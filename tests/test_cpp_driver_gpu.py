@@ -35,3 +35,23 @@ def test_cpp_driver_matches_oracle():
     ref = math.sqrt(max(0.0, 0.5 + n2 - 2.0 * cross))
     assert abs(err - ref) <= 1e-6 * ref
     assert ref < 1e-3
+
+
+def test_cpp_wave_driver_matches_oracle():
+    """The adaptive wave driver written against the C++ mirror (like
+    example/03_wave_06_var_coeff_adapt.cpp) ends on the oracle's element set and coefficients."""
+    exe = os.path.join(os.path.dirname(amdg.LIB_PATH), "wave_var_coeff_adapt")
+    assert os.path.exists(exe), "example driver not built"
+    n_init, nmax, steps, eps, eta = 3, 5, 4, 1e-5, 1e-6
+    out = subprocess.run([exe, str(n_init), str(nmax), str(steps), repr(eps), repr(eta)], capture_output=True,
+                         text=True, timeout=300, check=True).stdout
+    fields = dict(line.split(":", 1) for line in out.splitlines() if ":" in line)
+    head = out.splitlines()[0].split()
+    elements, t = int(head[5]), float(head[3])
+    hist = O.wave_adaptive_run(2, n_init, nmax, eps, eta, 10.0, 0.1, 1.0, steps)
+    keys, u, v, _dt = hist[-1]
+    assert elements == len(keys)
+    assert abs(t - sum(h[3] for h in hist[1:])) <= 1e-15
+    su, sut = float(np.sum(u * u)), float(np.sum(v * v))
+    assert abs(float(fields["sum of squares u"]) - su) <= 1e-12 * su
+    assert abs(float(fields["sum of squares u_t"]) - sut) <= 1e-11 * sut
