@@ -397,4 +397,8 @@ struct amdg_batch {
     int64_t launches_per_graph = 0;
     int tile[2] = {256, 256};             // CTA size of the stage kernel per precision (FP64, mixed)
     float tile_ms[2][3] = {{0}};          // autotuner: one stage per candidate of kBatchTiles (0: not timed)
+    // amdg_batch_adapt scratch (grow-only): parent table, classifier features and probabilities
+    int32_t* d_pg = nullptr;
+    float *d_feat = nullptr, *d_prob = nullptr;
+    int64_t scratch_elems = 0;
 };

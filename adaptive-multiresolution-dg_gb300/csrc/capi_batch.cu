@@ -15,6 +15,7 @@
 #include "amdg.h"
 #include "amdg_internal.hpp"
 #include "kernels.cuh"
+#include "kernels_mlp.cuh"
 
 using namespace amdg;
 
@@ -85,6 +86,50 @@ amdg_status batch_step(amdg_batch* b, amdg_precision prec, cudaStream_t st) {
             AMDG_CK(launch_batch<double, double>(L, st));
         }
     }
+    return AMDG_OK;
+}
+
+// The concatenated element tables, neighbour lists and state of the batch's grids (as they are
+// now), replacing any earlier ones; captured step graphs are dropped.
+amdg_status batch_build(amdg_batch* b) {
+    const int n = b->nsolves;
+    std::vector<const HostGrid*> hg(n);
+    for (int i = 0; i < n; ++i) hg[i] = &b->grids[i]->host;
+    Basis1D basis{b->k, b->nmax};
+    Oper1D op;
+    build_oper1d(basis, &op, false);
+    BatchTopology topo;
+    build_batch_topology(hg, op, &topo);
+    for (int p = 0; p < 2; ++p)
+        if (b->graph_exec[p]) {
+            cudaGraphExecDestroy(static_cast<cudaGraphExec_t>(b->graph_exec[p]));
+            b->graph_exec[p] = nullptr;
+        }
+    void* old[] = {b->d_row_ptr, b->d_src, b->d_blk, b->d_solve, b->d_blocks64, b->d_blocks32,
+                   b->d_u, b->d_u1, b->d_u2, b->d_shadow};
+    for (void* p : old) cudaFree(p);
+    b->d_row_ptr = b->d_src = nullptr;
+    b->d_blk = b->d_solve = nullptr;
+    b->d_blocks64 = b->d_u = b->d_u1 = b->d_u2 = nullptr;
+    b->d_blocks32 = b->d_shadow = nullptr;
+    b->elem_offset = topo.elem_offset;
+    b->num_elements = topo.elem_offset[n];
+    b->dof = b->num_elements * b->block;
+    b->pairs = int64_t(topo.src.size());
+    b->num_blocks = topo.num_blocks;
+    std::vector<float> b32(topo.blocks.begin(), topo.blocks.end());
+    amdg_status s;
+    if ((s = put(&b->d_row_ptr, topo.row_ptr)) != AMDG_OK || (s = put(&b->d_src, topo.src)) != AMDG_OK ||
+        (s = put(&b->d_blk, topo.blk)) != AMDG_OK || (s = put(&b->d_solve, topo.solve_of)) != AMDG_OK ||
+        (s = put(&b->d_blocks64, topo.blocks)) != AMDG_OK || (s = put(&b->d_blocks32, b32)) != AMDG_OK ||
+        (s = alloc(&b->d_u, size_t(b->dof))) != AMDG_OK || (s = alloc(&b->d_u1, size_t(b->dof))) != AMDG_OK ||
+        (s = alloc(&b->d_u2, size_t(b->dof))) != AMDG_OK || (s = alloc(&b->d_shadow, size_t(b->dof) * 3)) != AMDG_OK)
+        return s;
+    cudaStream_t st = stream_of(b);
+    for (int i = 0; i < n; ++i)
+        AMDG_CK(cudaMemcpyAsync(b->d_u + b->elem_offset[i] * b->block, b->grids[i]->d_u,
+                                size_t(b->grids[i]->dof) * sizeof(double), cudaMemcpyDeviceToDevice, st));
+    AMDG_CK(cudaStreamSynchronize(st));
     return AMDG_OK;
 }
 
@@ -171,45 +216,16 @@ amdg_status amdg_batch_create(amdg_context* ctx, int n, amdg_grid* const* grids,
     b->dim = dim; b->nmax = nmax; b->k = k; b->nsolves = n;
     b->block = grids[0]->block;
     b->grids.assign(grids, grids + n);
-    Basis1D basis{k, nmax};
-    Oper1D op;
-    build_oper1d(basis, &op, false);
-    BatchTopology topo;
-    build_batch_topology(hg, op, &topo);
-    b->elem_offset = topo.elem_offset;
-    b->num_elements = topo.elem_offset[n];
-    b->dof = b->num_elements * b->block;
-    b->pairs = int64_t(topo.src.size());
-    b->num_blocks = topo.num_blocks;
     std::vector<double> c64(coef, coef + size_t(n) * dim);
     std::vector<float> c32(c64.begin(), c64.end());
-    std::vector<float> b32(topo.blocks.begin(), topo.blocks.end());
     std::vector<double> dt(n, 0.0);
     amdg_status s;
-    if ((s = put(&b->d_row_ptr, topo.row_ptr)) != AMDG_OK || (s = put(&b->d_src, topo.src)) != AMDG_OK ||
-        (s = put(&b->d_blk, topo.blk)) != AMDG_OK || (s = put(&b->d_solve, topo.solve_of)) != AMDG_OK ||
-        (s = put(&b->d_blocks64, topo.blocks)) != AMDG_OK || (s = put(&b->d_blocks32, b32)) != AMDG_OK ||
-        (s = put(&b->d_coef64, c64)) != AMDG_OK || (s = put(&b->d_coef32, c32)) != AMDG_OK ||
-        (s = put(&b->d_dt, dt)) != AMDG_OK || (s = alloc(&b->d_u, size_t(b->dof))) != AMDG_OK ||
-        (s = alloc(&b->d_u1, size_t(b->dof))) != AMDG_OK || (s = alloc(&b->d_u2, size_t(b->dof))) != AMDG_OK ||
-        (s = alloc(&b->d_shadow, size_t(b->dof) * 3)) != AMDG_OK) {
+    if ((s = put(&b->d_coef64, c64)) != AMDG_OK || (s = put(&b->d_coef32, c32)) != AMDG_OK ||
+        (s = put(&b->d_dt, dt)) != AMDG_OK || (s = batch_build(b)) != AMDG_OK) {
         amdg_batch_destroy(b);
         return s;
     }
     cudaStream_t st = stream_of(b);
-    for (int i = 0; i < n; ++i) {
-        cudaError_t e = cudaMemcpyAsync(b->d_u + b->elem_offset[i] * b->block, grids[i]->d_u,
-                                        size_t(grids[i]->dof) * sizeof(double), cudaMemcpyDeviceToDevice, st);
-        if (e != cudaSuccess) {
-            amdg_batch_destroy(b);
-            return fail(AMDG_ERR_CUDA, std::string("batch gather: ") + cudaGetErrorString(e));
-        }
-    }
-    cudaError_t e = cudaStreamSynchronize(st);
-    if (e != cudaSuccess) {
-        amdg_batch_destroy(b);
-        return fail(AMDG_ERR_CUDA, std::string("batch create: ") + cudaGetErrorString(e));
-    }
     if ((s = autotune_batch(b, st)) != AMDG_OK) {
         amdg_batch_destroy(b);
         return s;
@@ -250,7 +266,7 @@ amdg_status amdg_batch_destroy(amdg_batch* b) {
     for (int p = 0; p < 2; ++p)
         if (b->graph_exec[p]) cudaGraphExecDestroy(static_cast<cudaGraphExec_t>(b->graph_exec[p]));
     void* ptrs[] = {b->d_row_ptr, b->d_src, b->d_blk, b->d_solve, b->d_blocks64, b->d_blocks32, b->d_coef64,
-                    b->d_coef32, b->d_dt, b->d_u, b->d_u1, b->d_u2, b->d_shadow};
+                    b->d_coef32, b->d_dt, b->d_u, b->d_u1, b->d_u2, b->d_shadow, b->d_pg, b->d_feat, b->d_prob};
     for (void* p : ptrs) cudaFree(p);
     delete b;
     return AMDG_OK;
@@ -322,6 +338,79 @@ amdg_status amdg_batch_store(amdg_batch* b, int solve) {
     AMDG_CK(cudaMemcpyAsync(g->d_u, b->d_u + b->elem_offset[solve] * b->block, size_t(g->dof) * sizeof(double),
                             cudaMemcpyDeviceToDevice, stream_of(b)));
     AMDG_CK(cudaStreamSynchronize(stream_of(b)));
+    return AMDG_OK;
+}
+
+amdg_status amdg_batch_adapt(amdg_batch* b, amdg_mlp* mlp, double eps, double eta, double tau, int64_t* stats) {
+    AMDG_REQUIRE(b && std::isfinite(eps) && std::isfinite(eta) && std::isfinite(tau), AMDG_ERR_ARG, "bad arguments");
+    AMDG_CK(cudaSetDevice(b->device));
+    cudaStream_t st = stream_of(b);
+    const int F = b->block * (1 + 2 * b->dim);
+    if (mlp) {
+        int n_in = 0, n_out = 0;
+        mlp_shape(mlp, &n_in, &n_out);
+        AMDG_REQUIRE(n_in == F && n_out == 3, AMDG_ERR_ARG,
+                     "classifier must take " + std::to_string(F) + " features and give 3 classes");
+    }
+    int64_t n_net = 0, n_unsure = 0;
+    amdg_status s;
+    for (int i = 0; i < b->nsolves; ++i) {
+        // the solve's state back into its grid
+        if ((s = amdg_batch_store(b, i)) != AMDG_OK) return s;
+        amdg_grid* g = b->grids[i];
+        const int64_t E = g->host.num_elements;
+        std::vector<double> norms;
+        if ((s = grid_norms(g, g->d_u, &norms)) != AMDG_OK) return s;
+        std::vector<uint8_t> force;
+        if (mlp) {
+            // classifier on the current coefficients; the criterion decides where it is unsure
+            if (E > b->scratch_elems) {
+                cudaFree(b->d_pg);
+                cudaFree(b->d_feat);
+                cudaFree(b->d_prob);
+                b->d_pg = nullptr;
+                b->d_feat = b->d_prob = nullptr;
+                b->scratch_elems = 0;
+                const int64_t cap = E + E / 4;
+                if ((s = alloc(&b->d_pg, size_t(cap) * b->dim * 2)) != AMDG_OK ||
+                    (s = alloc(&b->d_feat, size_t(cap) * F)) != AMDG_OK || (s = alloc(&b->d_prob, size_t(cap) * 3)) != AMDG_OK)
+                    return s;
+                b->scratch_elems = cap;
+            }
+            std::vector<int32_t> pg;
+            parent_table(g->host, &pg);
+            AMDG_CK(cudaMemcpyAsync(b->d_pg, pg.data(), pg.size() * sizeof(int32_t), cudaMemcpyHostToDevice, st));
+            AMDG_CK(launch_element_features(g->d_u, nullptr, b->d_pg, E, b->dim, b->block, b->d_feat, st));
+            b->ctx->launches++;
+            if ((s = amdg_mlp_predict(mlp, b->d_feat, E, b->d_prob)) != AMDG_OK) return s;
+            std::vector<float> prob(size_t(E) * 3);
+            AMDG_CK(cudaMemcpyAsync(prob.data(), b->d_prob, prob.size() * sizeof(float), cudaMemcpyDeviceToHost, st));
+            AMDG_CK(cudaStreamSynchronize(st));  // pg and prob are host vectors of this iteration
+            force.assign(E, 0);
+            for (int64_t e = 0; e < E; ++e) {
+                const float* p = &prob[size_t(e) * 3];
+                int arg = 0;  // classes: 0 refine, 1 keep, 2 coarsen
+                for (int q = 1; q < 3; ++q)
+                    if (p[q] > p[arg]) arg = q;
+                if (p[arg] < float(tau)) {
+                    ++n_unsure;
+                    force[e] = norms[e] > eps ? 1 : 0;
+                } else if (arg == 0) {
+                    force[e] = 1;
+                    ++n_net;
+                }
+            }
+        }
+        std::vector<uint64_t> keys = refine_keys(g->host, norms.data(), eps, nullptr, mlp ? force.data() : nullptr);
+        if (int64_t(keys.size()) != E && (s = grid_set_keys(g, std::move(keys))) != AMDG_OK) return s;
+        if ((s = grid_coarsen(g, eta, nullptr, nullptr)) != AMDG_OK) return s;
+    }
+    if ((s = batch_build(b)) != AMDG_OK) return s;
+    if (stats) {
+        stats[0] = n_net;
+        stats[1] = n_unsure;
+        stats[2] = b->num_elements;
+    }
     return AMDG_OK;
 }
 

@@ -133,6 +133,7 @@ def load():
         "amdg_batch_store": ([vp, i32], i32),
         "amdg_batch_coefficients_device": ([vp, pp, vp], i32),
         "amdg_batch_tuning": ([vp, vp, vp], i32),
+        "amdg_batch_adapt": ([vp, vp, dbl, dbl, dbl, vp], i32),
         "amdg_batch_set_tile": ([vp, i32, i32], i32),
         "amdg_burgers_destroy": ([vp], i32),
         "amdg_burgers_rhs": ([vp, vp, vp, i32], i32),
@@ -651,6 +652,19 @@ class Batch:
 
     def store(self, solve: int):
         _ck(load().amdg_batch_store(self._h, solve), "batch_store")
+
+    def adapt(self, eps: float, eta: float, mlp=None, tau: float = 0.8):
+        """Refine (criterion, or classifier + criterion) and coarsen every solve's grid, then rebuild
+        the batch; returns [refined by the classifier, uncertain, elements after]."""
+        stats = np.zeros(3, np.int64)
+        _ck(load().amdg_batch_adapt(self._h, mlp.handle if mlp is not None else None, eps, eta, tau, _ptr(stats)),
+            "batch_adapt")
+        ne, dof, pairs = C.c_int64(), C.c_int64(), C.c_int64()
+        _ck(load().amdg_batch_size(self._h, C.byref(ne), C.byref(dof), C.byref(pairs)), "batch_size")
+        self.num_elements, self.dof, self.pairs = ne.value, dof.value, pairs.value
+        for g in self.grids:
+            g._refresh()
+        return stats
 
     def tuning(self):
         """(CTA size per precision [FP64, mixed], stage ms per candidate [2][128, 256, 512 threads])."""

@@ -318,6 +318,15 @@ amdg_status amdg_batch_rk3_steps(amdg_batch* b, int nsteps, amdg_precision prec,
 amdg_status amdg_batch_store(amdg_batch* b, int solve);
 /* Device pointer of the concatenated state and the element offsets (n+1 entries, may be NULL). */
 amdg_status amdg_batch_coefficients_device(amdg_batch* b, double** device_ptr, int64_t* elem_offsets);
+/* Adaptivity inside the batch (no reference counterpart for the batching): every solve's state
+ * is written back to its grid, the grid is refined -- on the surplus criterion (leaves with block
+ * norm > eps get their children, DGAdapt::refine), or, with a classifier, on its "refine" class
+ * where its largest class probability is at least tau and on the criterion elsewhere (as
+ * amdg_burgers_adaptive_step_learned) -- then coarsened on the criterion (norm < eta), and the
+ * batch is rebuilt on the new element sets (neighbour lists, state; step graphs re-captured).
+ * The solves' time steps are kept: set them again if the finest levels changed.  stats (may be
+ * NULL): [refined by the classifier, uncertain, elements after]. */
+amdg_status amdg_batch_adapt(amdg_batch* b, amdg_mlp* mlp, double eps, double eta, double tau, int64_t* stats);
 /* Tile of the stage kernel: amdg_batch_create times one stage with CTAs of 128, 256 and 512
  * threads (threads / (k+1)^(dim-1) elements per CTA; dim <= 3, 256 only above) for each
  * precision and keeps the fastest (batches under 100,000 DOF keep 256).  tile[2] = chosen CTA

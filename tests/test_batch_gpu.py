@@ -127,3 +127,69 @@ def test_bulk_factor_callbacks_match_pointwise(ctx):
         assert abs(ea - eb) <= 1e-9 * norm
         a.close()
         b.close()
+
+
+def test_batch_adapt_matches_per_grid_adaptivity(ctx):
+    """amdg_batch_adapt with the surplus criterion refines and coarsens every solve's grid as
+    amdg_grid_refine + amdg_grid_coarsen do on its own, and the rebuilt batch still steps every
+    solve as the single-grid operator does; a classifier that is never sure (tau above 1) falls
+    back to the criterion everywhere and gives the same grids."""
+    work = O.batched_workload(4, seed=13)
+    eps, eta = 3e-4, 3e-5
+    dts = [0.1 / (sum(abs(v) for v in w["velocity"]) * 32) for w in work]
+
+    def fresh():
+        return _grids(ctx, work, 5, 1e-3)
+
+    ga, gb, gc = fresh(), fresh(), fresh()
+    batch = amdg.Batch(ctx, ga, [w["velocity"] for w in work])
+    batch.set_dt(dts)
+    batch.rk3_steps(2, amdg.FP64, use_graph=True)
+    for i in range(len(work)):  # the same two steps on the reference copies
+        batch.store(i)
+    u_after = [g.coefficients().copy() for g in ga]
+    for g, u in zip(gb, u_after):
+        g.set_coefficients(u)
+    for g, u in zip(gc, u_after):
+        g.set_coefficients(u)
+    stats = batch.adapt(eps, eta)
+    assert stats[2] == batch.num_elements
+    for g in gb:
+        g.refine(eps)
+        g.coarsen(eta)
+    for a, b in zip(ga, gb):
+        for x, y in zip(a.elements(), b.elements()):
+            assert np.array_equal(x, y)
+        assert np.array_equal(a.coefficients(), b.coefficients())
+    assert batch.num_elements == sum(g.num_elements for g in gb)
+    # the rebuilt batch steps each solve as the single-grid operator
+    batch.set_dt(dts)
+    batch.rk3_steps(2, amdg.FP64, use_graph=True)
+    for i, (g, w) in enumerate(zip(gb, work)):
+        batch.store(i)
+        op = amdg.LinearOperator(g, w["velocity"])
+        op.rk3_steps(dts[i], 2, amdg.FP64)
+        ctx.synchronize()
+        want = g.coefficients()
+        assert np.abs(ga[i].coefficients() - want).max() <= 1e-12 * np.abs(want).max()
+        op.close()
+    batch.close()
+    # a classifier that is never sure: the criterion decides everywhere
+    F = 27 * (1 + 2 * 3)
+    mlp = amdg.MLP(ctx, F, 64, 3, 3, seed=5)
+    batch2 = amdg.Batch(ctx, gc, [w["velocity"] for w in work])
+    st = batch2.adapt(eps, eta, mlp=mlp, tau=1.5)
+    assert st[0] == 0 and st[1] > 0
+    gd = fresh()
+    for g, u in zip(gd, u_after):
+        g.set_coefficients(u)
+    for g in gd:
+        g.refine(eps)
+        g.coarsen(eta)
+    for a, b in zip(gc, gd):
+        for x, y in zip(a.elements(), b.elements()):
+            assert np.array_equal(x, y)
+    batch2.close()
+    mlp.close()
+    for g in ga + gb + gc + gd:
+        g.close()
