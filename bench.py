@@ -704,6 +704,141 @@ def bench_batched(ctx, stream, args):
                              vectorized=True)
     for g in grids:
         g.close()
+    if args.batch_adapt_every > 0:
+        out["adaptive"] = bench_batched_adaptive(ctx, stream, args, work[:args.batch_adapt_solves])
+    return out
+
+
+def grid_features(g) -> np.ndarray:
+    """Classifier inputs of every element as the feature kernel computes them: log10(|c| + 1e-20)/20 + 1
+    of the element's coefficients, then of its parent and grandparent in each dimension (0 where
+    absent)."""
+    keys = element_keys(g)
+    B, dim, mask = g.block, g.dim, (1 << g.nmax) - 1
+    mag = (np.log10(np.abs(g.coefficients().reshape(len(keys), B)) + 1e-20) / 20.0 + 1.0).astype(np.float32)
+    srt = np.argsort(keys, kind="stable")
+    F = np.zeros((len(keys), B * (1 + 2 * dim)), np.float32)
+    F[:, :B] = mag
+    for d in range(dim):
+        shift = g.nmax * (dim - 1 - d)
+        k = keys.copy()
+        alive = np.ones(len(keys), bool)
+        for gen in range(2):
+            o = (k >> shift) & mask
+            alive &= o > 0
+            k = (k & ~(mask << shift)) | (np.where(o == 1, 0, o // 2) << shift)
+            pos = np.minimum(np.searchsorted(keys[srt], k), len(keys) - 1)
+            hit = alive & (keys[srt][pos] == k)
+            slot = 1 + 2 * d + gen
+            F[hit, slot * B:(slot + 1) * B] = mag[srt[pos[hit]]]
+    return F
+
+
+def adapt_labels(g, keys_before) -> np.ndarray:
+    """Labels of the elements present before an adaptation: 0 where one of their children appeared,
+    else 2 where they were removed, else 1."""
+    after = element_keys(g)
+    fresh = np.setdiff1d(after, keys_before)
+    dim, mask = g.dim, (1 << g.nmax) - 1
+    refined = np.zeros(len(keys_before), bool)
+    for d in range(dim):
+        shift = g.nmax * (dim - 1 - d)
+        o = (keys_before >> shift) & mask
+        base = keys_before & ~(mask << shift)
+        lev = np.where(o == 0, 0, np.floor(np.log2(np.maximum(o, 1))).astype(np.int64) + 1)
+        refined |= (o == 0) & np.isin(base | (1 << shift), fresh)
+        for c in (0, 1):
+            refined |= (o > 0) & (lev < g.nmax) & np.isin(base | ((2 * o + c) << shift), fresh)
+    return np.where(refined, 0, np.where(np.isin(keys_before, after), 1, 2)).astype(np.int32)
+
+
+def bench_batched_adaptive(ctx, stream, args, work):
+    """The batched solves with adaptivity inside the batch: every A steps each solve's grid is refined
+    (surplus criterion, or the classifier with the criterion where it is unsure) and coarsened, and
+    the batch rebuilt.  The classifier is trained on the criterion's decisions in a separate seeded
+    batch.  Throughput counts the adaptation's time; errors against the exact translated bumps."""
+    import torch
+
+    import amdg
+    import amdg_oracle as O
+    A, eps, eta, tau = args.batch_adapt_every, args.batch_eps, args.batch_eps / 10, 0.8
+    nsteps = 2 * A
+
+    def make(ws):
+        gs = []
+        for w in ws:
+            g = amdg.Grid(ctx, 3, 8, 2, level_init=2)
+            g.init_separable_adaptive(O.gaussian_bump_terms(w["centers"], w["widths"], w["amplitudes"],
+                                                            vectorized=True), eps, vectorized=True)
+            gs.append(g)
+        return gs
+
+    def dts_of(gs, ws):
+        return [CFL / sum(abs(v) * 2.0 ** int(m) for v, m in zip(w["velocity"], g.max_mesh_level()))
+                for g, w in zip(gs, ws)]
+
+    # training data: the criterion's decisions on another seeded set of solves
+    t0 = time.perf_counter()
+    train = O.batched_workload(min(32, len(work)), seed=1)
+    gs = make(train)
+    batch = amdg.Batch(ctx, gs, [w["velocity"] for w in train])
+    feats, labs = [], []
+    for _ in range(3):
+        batch.set_dt(dts_of(gs, train))
+        batch.rk3_steps(A, amdg.MIXED, use_graph=True)
+        for i in range(len(train)):
+            batch.store(i)
+        before = [element_keys(g) for g in gs]
+        feats += [grid_features(g) for g in gs]
+        batch.adapt(eps, eta)
+        labs += [adapt_labels(g, k) for g, k in zip(gs, before)]
+    batch.close()
+    for g in gs:
+        g.close()
+    x, y = np.concatenate(feats), np.concatenate(labs)
+    dx, dy = torch.from_numpy(x).cuda(), torch.from_numpy(y).cuda()
+    torch.cuda.synchronize()
+    mlp = amdg.MLP(ctx, x.shape[1], 64, 3, 3, seed=31)
+    loss = mlp.train_device(dx.data_ptr(), dy.data_ptr(), len(y), epochs=args.learn_epochs, batch=256, lr=2e-3,
+                            seed=32)
+    out = {"solves": len(work), "adapt_every_steps": A, "steps": nsteps, "refine_eps": eps, "coarsen_eta": eta, "tau": tau,
+           "training": {"solves": len(train), "samples": int(len(y)),
+                        "class_counts": [int((y == i).sum()) for i in range(3)], "final_loss": loss,
+                        "s": time.perf_counter() - t0}}
+    for name, learned in (("criterion", False), ("learned", True)):
+        gs = make(work)
+        batch = amdg.Batch(ctx, gs, [w["velocity"] for w in work])
+        elapsed = np.zeros(len(work))
+        dof_stages = 0.0
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        stats = np.zeros(2, np.int64)
+        for _ in range(nsteps // A):
+            dts = dts_of(gs, work)
+            batch.set_dt(dts)
+            batch.rk3_steps(A, amdg.MIXED, use_graph=True)
+            dof_stages += 3.0 * batch.dof * A
+            elapsed += np.asarray(dts) * A
+            st = batch.adapt(eps, eta, mlp if learned else None, tau)
+            stats += st[:2]
+        torch.cuda.synchronize()
+        wall = time.perf_counter() - t0
+        errs = []
+        for i in range(0, len(work), max(1, len(work) // 16)):
+            w = work[i]
+            batch.store(i)
+            shift = [v * elapsed[i] for v in w["velocity"]]
+            exact = O.gaussian_bump_terms(w["centers"], w["widths"], w["amplitudes"], shift=shift, vectorized=True)
+            norm = O.gaussian_bump_norm(w["centers"], w["widths"], w["amplitudes"])
+            errs.append(gs[i].l2_error_separable_sum(exact, norm, vectorized=True) / norm)
+        out[name] = {"value": dof_stages / wall, "wall_s": wall, "elements_final": batch.num_elements,
+                     "rel_l2_error_sampled": {"median": float(np.median(errs)), "max": float(np.max(errs))}}
+        if learned:
+            out[name]["classifier"] = {"net_refine": int(stats[0]), "unsure": int(stats[1])}
+        batch.close()
+        for g in gs:
+            g.close()
+    mlp.close()
     return out
 
 
@@ -821,6 +956,9 @@ def main():
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--batch-solves", type=int, default=256)
     ap.add_argument("--batch-eps", type=float, default=1e-5)
+    ap.add_argument("--batch-adapt-every", type=int, default=5,
+                    help="steps between adaptations of the batched solves' grids (0: skip that run)")
+    ap.add_argument("--batch-adapt-solves", type=int, default=64, help="solves in the adaptive batched run")
     ap.add_argument("--learn-runs", type=int, default=4, help="plain runs whose decisions train the classifier (0: skip)")
     ap.add_argument("--learn-steps", type=int, default=12)
     ap.add_argument("--learn-horizon", type=int, default=4,
