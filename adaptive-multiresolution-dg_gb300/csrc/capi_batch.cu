@@ -401,9 +401,22 @@ amdg_status amdg_batch_adapt(amdg_batch* b, amdg_mlp* mlp, double eps, double et
                 }
             }
         }
-        std::vector<uint64_t> keys = refine_keys(g->host, norms.data(), eps, nullptr, mlp ? force.data() : nullptr);
-        if (int64_t(keys.size()) != E && (s = grid_set_keys(g, std::move(keys))) != AMDG_OK) return s;
-        if ((s = grid_coarsen(g, eta, nullptr, nullptr)) != AMDG_OK) return s;
+        // the chosen elements by key (ascending, as the grid's keys are), then coarsen, then refine
+        // those of them that the coarsening kept
+        std::vector<uint64_t> chosen;
+        for (int64_t e = 0; e < E; ++e)
+            if (mlp ? force[e] != 0 : norms[e] > eps) chosen.push_back(g->host.key[e]);
+        std::vector<uint64_t> kept = coarsen_keys(g->host, norms.data(), eta);
+        if (int64_t(kept.size()) != E && (s = grid_set_keys(g, std::move(kept))) != AMDG_OK) return s;
+        const int64_t Ec = g->host.num_elements;
+        std::vector<uint8_t> pick(Ec, 0);
+        size_t c = 0;
+        for (int64_t e = 0; e < Ec && c < chosen.size(); ++e) {
+            while (c < chosen.size() && chosen[c] < g->host.key[e]) ++c;
+            if (c < chosen.size() && chosen[c] == g->host.key[e]) pick[e] = 1;
+        }
+        std::vector<uint64_t> keys = refine_keys(g->host, nullptr, eps, nullptr, pick.data());
+        if (int64_t(keys.size()) != Ec && (s = grid_set_keys(g, std::move(keys))) != AMDG_OK) return s;
     }
     if ((s = batch_build(b)) != AMDG_OK) return s;
     if (stats) {

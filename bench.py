@@ -734,35 +734,26 @@ def grid_features(g) -> np.ndarray:
     return F
 
 
-def adapt_labels(g, keys_before) -> np.ndarray:
-    """Labels of the elements present before an adaptation: 0 where one of their children appeared,
-    else 2 where they were removed, else 1."""
-    after = element_keys(g)
-    fresh = np.setdiff1d(after, keys_before)
-    dim, mask = g.dim, (1 << g.nmax) - 1
-    refined = np.zeros(len(keys_before), bool)
-    for d in range(dim):
-        shift = g.nmax * (dim - 1 - d)
-        o = (keys_before >> shift) & mask
-        base = keys_before & ~(mask << shift)
-        lev = np.where(o == 0, 0, np.floor(np.log2(np.maximum(o, 1))).astype(np.int64) + 1)
-        refined |= (o == 0) & np.isin(base | (1 << shift), fresh)
-        for c in (0, 1):
-            refined |= (o > 0) & (lev < g.nmax) & np.isin(base | ((2 * o + c) << shift), fresh)
-    return np.where(refined, 0, np.where(np.isin(keys_before, after), 1, 2)).astype(np.int32)
+def refine_labels(g, eps) -> np.ndarray:
+    """The criterion's choice for every element: 0 (refine) where its block norm exceeds eps, else
+    1 (keep).  Coarsening stays on the criterion and refinement only touches leaves, so these
+    are the decisions the classifier stands in for."""
+    u = g.coefficients().reshape(g.num_elements, g.block)
+    return np.where(np.sqrt(np.sum(u * u, axis=1)) > eps, 0, 1).astype(np.int32)
 
 
 def bench_batched_adaptive(ctx, stream, args, work):
     """The batched solves with adaptivity inside the batch: every A steps each solve's grid is refined
     (surplus criterion, or the classifier with the criterion where it is unsure) and coarsened, and
-    the batch rebuilt.  The classifier is trained on the criterion's decisions in a separate seeded
-    batch.  Throughput counts the adaptation's time; errors against the exact translated bumps."""
+    the batch rebuilt; "static" keeps the initial grids.  The classifier is trained on the
+    criterion's decisions in a separate seeded batch.  Throughput counts the adaptation's time;
+    errors against the exact translated bumps."""
     import torch
 
     import amdg
     import amdg_oracle as O
     A, eps, eta, tau = args.batch_adapt_every, args.batch_eps, args.batch_eps / 10, 0.8
-    nsteps = 2 * A
+    nsteps = args.batch_adapt_rounds * A
 
     def make(ws):
         gs = []
@@ -783,15 +774,14 @@ def bench_batched_adaptive(ctx, stream, args, work):
     gs = make(train)
     batch = amdg.Batch(ctx, gs, [w["velocity"] for w in train])
     feats, labs = [], []
-    for _ in range(3):
+    for _ in range(max(2, args.batch_adapt_rounds - 2)):
         batch.set_dt(dts_of(gs, train))
         batch.rk3_steps(A, amdg.MIXED, use_graph=True)
         for i in range(len(train)):
             batch.store(i)
-        before = [element_keys(g) for g in gs]
         feats += [grid_features(g) for g in gs]
+        labs += [refine_labels(g, eps) for g in gs]
         batch.adapt(eps, eta)
-        labs += [adapt_labels(g, k) for g, k in zip(gs, before)]
     batch.close()
     for g in gs:
         g.close()
@@ -805,7 +795,7 @@ def bench_batched_adaptive(ctx, stream, args, work):
            "training": {"solves": len(train), "samples": int(len(y)),
                         "class_counts": [int((y == i).sum()) for i in range(3)], "final_loss": loss,
                         "s": time.perf_counter() - t0}}
-    for name, learned in (("criterion", False), ("learned", True)):
+    for name, learned in (("static", None), ("criterion", False), ("learned", True)):
         gs = make(work)
         batch = amdg.Batch(ctx, gs, [w["velocity"] for w in work])
         elapsed = np.zeros(len(work))
@@ -813,14 +803,20 @@ def bench_batched_adaptive(ctx, stream, args, work):
         torch.cuda.synchronize()
         t0 = time.perf_counter()
         stats = np.zeros(2, np.int64)
+        sizes, adapt_s = [batch.num_elements], 0.0
         for _ in range(nsteps // A):
             dts = dts_of(gs, work)
             batch.set_dt(dts)
             batch.rk3_steps(A, amdg.MIXED, use_graph=True)
             dof_stages += 3.0 * batch.dof * A
             elapsed += np.asarray(dts) * A
+            if learned is None:
+                continue
+            t1 = time.perf_counter()
             st = batch.adapt(eps, eta, mlp if learned else None, tau)
+            adapt_s += time.perf_counter() - t1
             stats += st[:2]
+            sizes.append(int(st[2]))
         torch.cuda.synchronize()
         wall = time.perf_counter() - t0
         errs = []
@@ -831,7 +827,7 @@ def bench_batched_adaptive(ctx, stream, args, work):
             exact = O.gaussian_bump_terms(w["centers"], w["widths"], w["amplitudes"], shift=shift, vectorized=True)
             norm = O.gaussian_bump_norm(w["centers"], w["widths"], w["amplitudes"])
             errs.append(gs[i].l2_error_separable_sum(exact, norm, vectorized=True) / norm)
-        out[name] = {"value": dof_stages / wall, "wall_s": wall, "elements_final": batch.num_elements,
+        out[name] = {"value": dof_stages / wall, "wall_s": wall, "adapt_s": adapt_s, "elements_by_adaptation": sizes,
                      "rel_l2_error_sampled": {"median": float(np.median(errs)), "max": float(np.max(errs))}}
         if learned:
             out[name]["classifier"] = {"net_refine": int(stats[0]), "unsure": int(stats[1])}
@@ -956,9 +952,10 @@ def main():
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--batch-solves", type=int, default=256)
     ap.add_argument("--batch-eps", type=float, default=1e-5)
-    ap.add_argument("--batch-adapt-every", type=int, default=5,
+    ap.add_argument("--batch-adapt-every", type=int, default=20,
                     help="steps between adaptations of the batched solves' grids (0: skip that run)")
     ap.add_argument("--batch-adapt-solves", type=int, default=64, help="solves in the adaptive batched run")
+    ap.add_argument("--batch-adapt-rounds", type=int, default=10, help="adaptations in the adaptive batched run")
     ap.add_argument("--learn-runs", type=int, default=4, help="plain runs whose decisions train the classifier (0: skip)")
     ap.add_argument("--learn-steps", type=int, default=12)
     ap.add_argument("--learn-horizon", type=int, default=4,

@@ -318,14 +318,18 @@ amdg_status amdg_batch_rk3_steps(amdg_batch* b, int nsteps, amdg_precision prec,
 amdg_status amdg_batch_store(amdg_batch* b, int solve);
 /* Device pointer of the concatenated state and the element offsets (n+1 entries, may be NULL). */
 amdg_status amdg_batch_coefficients_device(amdg_batch* b, double** device_ptr, int64_t* elem_offsets);
-/* Adaptivity inside the batch (no reference counterpart for the batching): every solve's state
- * is written back to its grid, the grid is refined -- on the surplus criterion (leaves with block
- * norm > eps get their children, DGAdapt::refine), or, with a classifier, on its "refine" class
- * where its largest class probability is at least tau and on the criterion elsewhere (as
- * amdg_burgers_adaptive_step_learned) -- then coarsened on the criterion (norm < eta), and the
- * batch is rebuilt on the new element sets (neighbour lists, state; step graphs re-captured).
- * The solves' time steps are kept: set them again if the finest levels changed.  stats (may be
- * NULL): [refined by the classifier, uncertain, elements after]. */
+/* Adaptivity inside the batch (no reference counterpart for the batching), the part of the
+ * reference's refine -> step -> coarsen loop that falls between two steps: every solve's state is
+ * written back to its grid; the elements to refine are chosen on the current state -- by the
+ * surplus criterion (leaves with block norm > eps, DGAdapt::refine), or, with a classifier, by
+ * its "refine" class where its largest class probability is at least tau and by the criterion
+ * elsewhere (as amdg_burgers_adaptive_step_learned); the grid is coarsened on the criterion
+ * (leaves with norm < eta, DGAdapt::coarsen), then the chosen elements still present get their
+ * children (zero coefficients: the next steps give them values, and the next call's coarsening
+ * removes those that stay small); and the batch is rebuilt on the new element sets (neighbour
+ * lists, state; step graphs re-captured).  The solves' time steps are kept: set them again if
+ * the finest levels changed.  stats (may be NULL): [refined by the classifier, uncertain,
+ * elements after]. */
 amdg_status amdg_batch_adapt(amdg_batch* b, amdg_mlp* mlp, double eps, double eta, double tau, int64_t* stats);
 /* Tile of the stage kernel: amdg_batch_create times one stage with CTAs of 128, 256 and 512
  * threads (threads / (k+1)^(dim-1) elements per CTA; dim <= 3, 256 only above) for each

@@ -20,6 +20,12 @@ def _grids(ctx, work, nmax, eps):
     return grids
 
 
+def _keys(g):
+    """One int per element: its per-dimension (level, support index) pairs packed together."""
+    lv, sp = g.elements()
+    return (lv.astype(np.int64) * 1024 + sp).dot(1 << (20 * np.arange(lv.shape[1], dtype=np.int64)))
+
+
 @pytest.mark.parametrize("use_graph", [False, True])
 def test_batch_matches_individual_solves(ctx, use_graph):
     work = O.batched_workload(5, seed=3)
@@ -130,10 +136,11 @@ def test_bulk_factor_callbacks_match_pointwise(ctx):
 
 
 def test_batch_adapt_matches_per_grid_adaptivity(ctx):
-    """amdg_batch_adapt with the surplus criterion refines and coarsens every solve's grid as
-    amdg_grid_refine + amdg_grid_coarsen do on its own, and the rebuilt batch still steps every
-    solve as the single-grid operator does; a classifier that is never sure (tau above 1) falls
-    back to the criterion everywhere and gives the same grids."""
+    """amdg_batch_adapt with the surplus criterion coarsens and refines every solve's grid as
+    amdg_grid_coarsen + amdg_grid_refine do on its own (the between-steps part of the reference's
+    refine -> step -> coarsen loop: the new children survive the call), and the rebuilt batch
+    still steps every solve as the single-grid operator does; a classifier that is never sure
+    (tau above 1) falls back to the criterion everywhere and gives the same grids."""
     work = O.batched_workload(4, seed=13)
     eps, eta = 3e-4, 3e-5
     dts = [0.1 / (sum(abs(v) for v in w["velocity"]) * 32) for w in work]
@@ -152,11 +159,28 @@ def test_batch_adapt_matches_per_grid_adaptivity(ctx):
         g.set_coefficients(u)
     for g, u in zip(gc, u_after):
         g.set_coefficients(u)
+    keys_before = [_keys(g) for g in ga]
     stats = batch.adapt(eps, eta)
     assert stats[2] == batch.num_elements
+    # new children start at zero; coarsened leaves whose parent is refined come straight back,
+    # also at zero (as in the reference loop, where the next refine re-adds what coarsen removed);
+    # every other element keeps its coefficients
+    fresh_total = zeroed_total = 0
+    for g, kb, ub in zip(ga, keys_before, u_after):
+        ka, ua = _keys(g), g.coefficients()
+        new = ~np.isin(ka, kb)
+        fresh_total += int(new.sum())
+        assert not ua[new].any()
+        srt = np.argsort(kb)
+        pos = srt[np.searchsorted(kb[srt], ka[~new])]
+        same = np.all(ua[~new] == ub[pos], axis=1)
+        zero = ~ua[~new].any(axis=1)
+        assert np.all(same | zero)
+        zeroed_total += int((zero & ~same).sum())
+    assert fresh_total > 0 and zeroed_total > 0
     for g in gb:
-        g.refine(eps)
         g.coarsen(eta)
+        g.refine(eps)
     for a, b in zip(ga, gb):
         for x, y in zip(a.elements(), b.elements()):
             assert np.array_equal(x, y)
@@ -184,8 +208,8 @@ def test_batch_adapt_matches_per_grid_adaptivity(ctx):
     for g, u in zip(gd, u_after):
         g.set_coefficients(u)
     for g in gd:
-        g.refine(eps)
         g.coarsen(eta)
+        g.refine(eps)
     for a, b in zip(gc, gd):
         for x, y in zip(a.elements(), b.elements()):
             assert np.array_equal(x, y)
