@@ -145,7 +145,15 @@ void build_key_index(HostGrid* g);
 void build_grid(int dim, int nmax, int sparse, HostGrid* g, int level_init = -1);
 int64_t find_element(const HostGrid& g, const int32_t* orders);  // binary search, -1 if absent
 
-// Batched independent grids sharing nmax, k and dim.
+// Batched independent grids sharing nmax, k and dim.  The 1D part depends on k and nmax only
+// and is built once per batch; the element part on every element set.
+struct BatchTables {
+    std::vector<std::vector<int>> rel1d;  // 1D order -> related 1D orders (nonzero block)
+    std::vector<int> blk_base;            // 1D order -> first block index of its row
+    std::vector<double> blocks;           // [2][num_blocks][k+1][k+1]
+    int num_blocks = 0;
+};
+void build_batch_tables(const Oper1D& op, int nmax, int np, BatchTables* out);
 struct BatchTopology {
     std::vector<int64_t> row_ptr, src;   // CSR over (global element, dimension)
     std::vector<int32_t> blk;
@@ -154,7 +162,8 @@ struct BatchTopology {
     std::vector<int64_t> elem_offset;    // solves + 1
     int num_blocks = 0;
 };
-void build_batch_topology(const std::vector<const HostGrid*>& grids, const Oper1D& op, BatchTopology* out);
+// rows of every solve built in parallel, then concatenated in solve order
+void build_batch_topology(const std::vector<const HostGrid*>& grids, const BatchTables& t, BatchTopology* out);
 
 // Adaptivity on packed keys (one refine pass with hole filling; repeated coarsening).
 // refined (optional): per element, 1 where the element was refined; force (optional): refine
@@ -370,8 +379,10 @@ struct amdg_wave_op {
 };
 
 namespace amdg {
-// replace a grid's element set (coefficients carried over, new elements zero; bumps the version)
-amdg_status grid_set_keys(amdg_grid* g, std::vector<uint64_t> keys);
+// replace a grid's element set (coefficients carried over, new elements zero; bumps the version);
+// with `carry`, only old elements e with (*carry)[e] != 0 keep their coefficients (the others
+// start at zero if they are in the new set)
+amdg_status grid_set_keys(amdg_grid* g, std::vector<uint64_t> keys, const std::vector<uint8_t>* carry = nullptr);
 // indicator norms of a device coefficient vector on the grid's element set, plus those of a
 // second vector when d_u2 is given (the wave problem's u_t) (synchronises)
 amdg_status grid_norms(amdg_grid* g, const double* d_u, std::vector<double>* norms, const double* d_u2 = nullptr);
@@ -384,6 +395,7 @@ struct amdg_batch {
     int device = 0;
     int dim = 0, nmax = 0, k = 0, block = 0, nsolves = 0;
     std::vector<amdg_grid*> grids;
+    amdg::BatchTables tables;  // built on the first rebuild
     std::vector<int64_t> elem_offset;
     int64_t num_elements = 0, dof = 0, pairs = 0;
     int num_blocks = 0;

@@ -113,7 +113,7 @@ namespace amdg {
 
 // Replace the grid's element set by `keys` (sorted, unique), carrying the
 // coefficients of surviving elements over and zeroing new ones.
-amdg_status grid_set_keys(amdg_grid* g, std::vector<uint64_t> keys) {
+amdg_status grid_set_keys(amdg_grid* g, std::vector<uint64_t> keys, const std::vector<uint8_t>* carry) {
     PhaseTimer timer(g->ctx, AMDG_PHASE_SET_KEYS);
     HostGrid ng;
     ng.sparse = g->host.sparse;
@@ -126,7 +126,7 @@ amdg_status grid_set_keys(amdg_grid* g, std::vector<uint64_t> keys) {
         size_t j = 0;
         for (int64_t e = 0; e < ng.num_elements; ++e) {
             while (j < ok.size() && ok[j] < ng.key[e]) ++j;
-            map[e] = (j < ok.size() && ok[j] == ng.key[e]) ? int32_t(j) : -1;
+            map[e] = (j < ok.size() && ok[j] == ng.key[e] && (!carry || (*carry)[j])) ? int32_t(j) : -1;
         }
     }
     cudaStream_t st = stream_of(g->ctx);

@@ -6,6 +6,7 @@
 // A step's launches can be captured once into a CUDA graph and replayed.
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cmath>
 #include <cstring>
 #include <new>
@@ -95,11 +96,14 @@ amdg_status batch_build(amdg_batch* b) {
     const int n = b->nsolves;
     std::vector<const HostGrid*> hg(n);
     for (int i = 0; i < n; ++i) hg[i] = &b->grids[i]->host;
-    Basis1D basis{b->k, b->nmax};
-    Oper1D op;
-    build_oper1d(basis, &op, false);
+    if (b->tables.rel1d.empty()) {
+        Basis1D basis{b->k, b->nmax};
+        Oper1D op;
+        build_oper1d(basis, &op, false);
+        build_batch_tables(op, b->nmax, b->k + 1, &b->tables);
+    }
     BatchTopology topo;
-    build_batch_topology(hg, op, &topo);
+    build_batch_topology(hg, b->tables, &topo);
     for (int p = 0; p < 2; ++p)
         if (b->graph_exec[p]) {
             cudaGraphExecDestroy(static_cast<cudaGraphExec_t>(b->graph_exec[p]));
@@ -364,6 +368,7 @@ amdg_status amdg_batch_adapt(amdg_batch* b, amdg_mlp* mlp, double eps, double et
         std::vector<uint8_t> force;
         if (mlp) {
             // classifier on the current coefficients; the criterion decides where it is unsure
+            PhaseTimer timer(b->ctx, AMDG_PHASE_CLASSIFIER);
             if (E > b->scratch_elems) {
                 cudaFree(b->d_pg);
                 cudaFree(b->d_feat);
@@ -401,24 +406,34 @@ amdg_status amdg_batch_adapt(amdg_batch* b, amdg_mlp* mlp, double eps, double et
                 }
             }
         }
-        // the chosen elements by key (ascending, as the grid's keys are), then coarsen, then refine
-        // those of them that the coarsening kept
-        std::vector<uint64_t> chosen;
-        for (int64_t e = 0; e < E; ++e)
-            if (mlp ? force[e] != 0 : norms[e] > eps) chosen.push_back(g->host.key[e]);
-        std::vector<uint64_t> kept = coarsen_keys(g->host, norms.data(), eta);
-        if (int64_t(kept.size()) != E && (s = grid_set_keys(g, std::move(kept))) != AMDG_OK) return s;
-        const int64_t Ec = g->host.num_elements;
-        std::vector<uint8_t> pick(Ec, 0);
-        size_t c = 0;
-        for (int64_t e = 0; e < Ec && c < chosen.size(); ++e) {
-            while (c < chosen.size() && chosen[c] < g->host.key[e]) ++c;
-            if (c < chosen.size() && chosen[c] == g->host.key[e]) pick[e] = 1;
+        // coarsen, then refine the chosen elements that the coarsening kept, both on the host key
+        // sets; one element-set replacement in which the coarsened elements that the refinement
+        // adds back start at zero, as after a separate coarsen and refine
+        std::vector<uint64_t> keys;
+        std::vector<uint8_t> carry;
+        {
+            PhaseTimer timer(b->ctx, AMDG_PHASE_ADAPT_HOST);
+            const std::vector<uint64_t>& old = g->host.key;  // ascending
+            HostGrid kept;
+            kept.sparse = g->host.sparse;
+            grid_from_keys(b->dim, b->nmax, b->k, coarsen_keys(g->host, norms.data(), eta), &kept);
+            carry.assign(E, 0);
+            std::vector<uint8_t> pick(kept.num_elements, 0);
+            for (int64_t e = 0, j = 0; e < kept.num_elements; ++e) {
+                while (old[j] < kept.key[e]) ++j;  // kept is a subset of old
+                carry[j] = 1;
+                pick[e] = mlp ? force[j] : (norms[j] > eps ? 1 : 0);
+            }
+            keys = refine_keys(kept, nullptr, eps, nullptr, pick.data());
         }
-        std::vector<uint64_t> keys = refine_keys(g->host, nullptr, eps, nullptr, pick.data());
-        if (int64_t(keys.size()) != Ec && (s = grid_set_keys(g, std::move(keys))) != AMDG_OK) return s;
+        if ((int64_t(keys.size()) != E || !std::all_of(carry.begin(), carry.end(), [](uint8_t c) { return c != 0; })) &&
+            (s = grid_set_keys(g, std::move(keys), &carry)) != AMDG_OK)
+            return s;
     }
-    if ((s = batch_build(b)) != AMDG_OK) return s;
+    {
+        PhaseTimer timer(b->ctx, AMDG_PHASE_TOPOLOGY);
+        if ((s = batch_build(b)) != AMDG_OK) return s;
+    }
     if (stats) {
         stats[0] = n_net;
         stats[1] = n_unsure;

@@ -377,14 +377,14 @@ bool build_surplus_ancestors(const HostGrid& g, const LagrTables& t, std::vector
 
 namespace amdg {
 
-void build_batch_topology(const std::vector<const HostGrid*>& grids, const Oper1D& op, BatchTopology* out) {
-    const int dim = grids[0]->dim, nmax = grids[0]->nmax, np = grids[0]->k + 1, n1 = 1 << nmax;
+void build_batch_tables(const Oper1D& op, int nmax, int np, BatchTables* out) {
+    const int n1 = 1 << nmax;
     const int64_t one = int64_t(1) << nmax;
     const int nb = op.nb;
     // shared 1D blocks, one table per upwind side: u_vx on intersecting supports
     // plus ulft_vjp (c >= 0) or urgt_vjp (c < 0), entries below 1e-13 dropped;
     // a pair is listed when either side is nonzero
-    std::vector<std::vector<int>> rel1d(n1);
+    out->rel1d.assign(n1, {});
     std::vector<double> t0, t1;
     for (int o = 0; o < n1; ++o) {
         int64_t a, b;
@@ -409,7 +409,7 @@ void build_batch_topology(const std::vector<const HostGrid*>& grids, const Oper1
                     }
             }
             if (!any) continue;
-            rel1d[o].push_back(oc);
+            out->rel1d[o].push_back(oc);
             t0.insert(t0.end(), blk[0], blk[0] + np * np);
             t1.insert(t1.end(), blk[1], blk[1] + np * np);
         }
@@ -417,39 +417,59 @@ void build_batch_topology(const std::vector<const HostGrid*>& grids, const Oper1
     out->num_blocks = int(t0.size() / (np * np));
     out->blocks = t0;
     out->blocks.insert(out->blocks.end(), t1.begin(), t1.end());
-    std::vector<int> blk_base(n1 + 1, 0);
-    for (int o = 0; o < n1; ++o) blk_base[o + 1] = blk_base[o] + int(rel1d[o].size());
-    int64_t total = 0;
-    for (const HostGrid* g : grids) total += g->num_elements;
-    out->row_ptr.assign(size_t(total) * dim + 1, 0);
-    out->src.clear();
-    out->blk.clear();
-    out->solve_of.assign(total, 0);
-    out->elem_offset.assign(grids.size() + 1, 0);
-    std::vector<int32_t> o2(dim);
-    int64_t base = 0;
-    for (size_t sv = 0; sv < grids.size(); ++sv) {
+    out->blk_base.assign(n1 + 1, 0);
+    for (int o = 0; o < n1; ++o) out->blk_base[o + 1] = out->blk_base[o] + int(out->rel1d[o].size());
+}
+
+void build_batch_topology(const std::vector<const HostGrid*>& grids, const BatchTables& t, BatchTopology* out) {
+    const int dim = grids[0]->dim;
+    const int64_t n = int64_t(grids.size());
+    out->num_blocks = t.num_blocks;
+    out->blocks = t.blocks;
+    out->elem_offset.assign(n + 1, 0);
+    for (int64_t sv = 0; sv < n; ++sv) out->elem_offset[sv + 1] = out->elem_offset[sv] + grids[sv]->num_elements;
+    const int64_t total = out->elem_offset[n];
+    // per solve: row ends relative to the solve's first pair, sources relative to its first element
+    std::vector<std::vector<int64_t>> rows(n);
+    std::vector<std::vector<int32_t>> src(n), blk(n);
+#pragma omp parallel for schedule(dynamic, 1) if (total >= 16384)
+    for (int64_t sv = 0; sv < n; ++sv) {
         const HostGrid& g = *grids[sv];
-        out->elem_offset[sv] = base;
+        std::vector<int32_t> o2(dim);
+        rows[sv].resize(size_t(g.num_elements) * dim);
         for (int64_t e = 0; e < g.num_elements; ++e) {
-            out->solve_of[base + e] = int32_t(sv);
             const int32_t* oe = &g.order[size_t(e) * dim];
-            for (int t = 0; t < dim; ++t) {
+            for (int d = 0; d < dim; ++d) {
                 std::copy(oe, oe + dim, o2.begin());
-                const int o = oe[t];
-                for (size_t i = 0; i < rel1d[o].size(); ++i) {
-                    o2[t] = rel1d[o][i];
+                const int o = oe[d];
+                const std::vector<int>& rel = t.rel1d[o];
+                for (size_t i = 0; i < rel.size(); ++i) {
+                    o2[d] = rel[i];
                     const int64_t s = find_element(g, o2.data());
                     if (s < 0) continue;
-                    out->src.push_back(base + s);
-                    out->blk.push_back(blk_base[o] + int32_t(i));
+                    src[sv].push_back(int32_t(s));
+                    blk[sv].push_back(t.blk_base[o] + int32_t(i));
                 }
-                out->row_ptr[size_t(base + e) * dim + t + 1] = int64_t(out->src.size());
+                rows[sv][size_t(e) * dim + d] = int64_t(src[sv].size());
             }
         }
-        base += g.num_elements;
     }
-    out->elem_offset[grids.size()] = base;
+    std::vector<int64_t> pair_offset(n + 1, 0);
+    for (int64_t sv = 0; sv < n; ++sv) pair_offset[sv + 1] = pair_offset[sv] + int64_t(src[sv].size());
+    out->row_ptr.assign(size_t(total) * dim + 1, 0);
+    out->src.resize(pair_offset[n]);
+    out->blk.resize(pair_offset[n]);
+    out->solve_of.resize(total);
+#pragma omp parallel for schedule(dynamic, 1) if (total >= 16384)
+    for (int64_t sv = 0; sv < n; ++sv) {
+        const int64_t e0 = out->elem_offset[sv], p0 = pair_offset[sv];
+        for (size_t r = 0; r < rows[sv].size(); ++r) out->row_ptr[size_t(e0) * dim + r + 1] = p0 + rows[sv][r];
+        for (size_t i = 0; i < src[sv].size(); ++i) {
+            out->src[p0 + i] = e0 + src[sv][i];
+            out->blk[p0 + i] = blk[sv][i];
+        }
+        std::fill(out->solve_of.begin() + e0, out->solve_of.begin() + e0 + grids[sv]->num_elements, int32_t(sv));
+    }
 }
 
 }  // namespace amdg

@@ -804,6 +804,7 @@ def bench_batched_adaptive(ctx, stream, args, work):
         t0 = time.perf_counter()
         stats = np.zeros(2, np.int64)
         sizes, adapt_s = [batch.num_elements], 0.0
+        ctx.profile(True)
         for _ in range(nsteps // A):
             dts = dts_of(gs, work)
             batch.set_dt(dts)
@@ -819,6 +820,8 @@ def bench_batched_adaptive(ctx, stream, args, work):
             sizes.append(int(st[2]))
         torch.cuda.synchronize()
         wall = time.perf_counter() - t0
+        prof = ctx.profile_read()
+        ctx.profile(False)
         errs = []
         for i in range(0, len(work), max(1, len(work) // 16)):
             w = work[i]
@@ -828,6 +831,7 @@ def bench_batched_adaptive(ctx, stream, args, work):
             norm = O.gaussian_bump_norm(w["centers"], w["widths"], w["amplitudes"])
             errs.append(gs[i].l2_error_separable_sum(exact, norm, vectorized=True) / norm)
         out[name] = {"value": dof_stages / wall, "wall_s": wall, "adapt_s": adapt_s, "elements_by_adaptation": sizes,
+                     "host_phase_ms": {k: round(v[0] * 1e3, 3) for k, v in prof.items() if v[1]},
                      "rel_l2_error_sampled": {"median": float(np.median(errs)), "max": float(np.max(errs))}}
         if learned:
             out[name]["classifier"] = {"net_refine": int(stats[0]), "unsure": int(stats[1])}
