@@ -194,6 +194,48 @@ void parent_table(const HostGrid& g, std::vector<int32_t>* pg) {
         }
 }
 
+void batch_parent_table(const std::vector<const HostGrid*>& grids, const std::vector<int64_t>& offset,
+                        std::vector<int32_t>* pg) {
+    const int64_t n = int64_t(grids.size());
+    const int dim = n ? grids[0]->dim : 0;
+    pg->assign(n ? size_t(offset[n]) * dim * 2 : 0, -1);
+#pragma omp parallel for schedule(dynamic, 1) if (n > 1 && offset[n] >= 16384)
+    for (int64_t i = 0; i < n; ++i) {
+        std::vector<int32_t> local;
+        parent_table(*grids[i], &local);
+        int32_t* out = pg->data() + size_t(offset[i]) * dim * 2;
+        for (size_t j = 0; j < local.size(); ++j) out[j] = local[j] < 0 ? -1 : int32_t(offset[i] + local[j]);
+    }
+}
+
+void adapt_keys_between_steps(const HostGrid& g, const double* norms, const uint8_t* force, double eps, double eta,
+                              std::vector<uint64_t>* keys, std::vector<uint8_t>* carry) {
+    const int64_t E = g.num_elements;
+    HostGrid kept;
+    kept.sparse = g.sparse;
+    grid_from_keys(g.dim, g.nmax, g.k, coarsen_keys(g, norms, eta), &kept);
+    carry->assign(E, 0);
+    std::vector<uint8_t> pick(kept.num_elements, 0);
+    for (int64_t e = 0, j = 0; e < kept.num_elements; ++e) {
+        while (g.key[j] < kept.key[e]) ++j;  // kept is a subset of the ascending old keys
+        (*carry)[j] = 1;
+        pick[e] = force ? force[j] : (norms[j] > eps ? 1 : 0);
+    }
+    *keys = refine_keys(kept, nullptr, eps, nullptr, pick.data());
+}
+
+void batch_adapt_keys(const std::vector<const HostGrid*>& grids, const std::vector<int64_t>& offset,
+                      const double* norms, const uint8_t* force, double eps, double eta,
+                      std::vector<std::vector<uint64_t>>* keys, std::vector<std::vector<uint8_t>>* carry) {
+    const int64_t n = int64_t(grids.size());
+    keys->assign(n, {});
+    carry->assign(n, {});
+#pragma omp parallel for schedule(dynamic, 1) if (n > 1 && offset[n] >= 16384)
+    for (int64_t i = 0; i < n; ++i)
+        adapt_keys_between_steps(*grids[i], norms + offset[i], force ? force + offset[i] : nullptr, eps, eta,
+                                 &(*keys)[i], &(*carry)[i]);
+}
+
 void grid_from_keys(int dim, int nmax, int k, std::vector<uint64_t> keys, HostGrid* g) {
     if (!std::is_sorted(keys.begin(), keys.end())) std::sort(keys.begin(), keys.end());
     keys.erase(std::unique(keys.begin(), keys.end()), keys.end());

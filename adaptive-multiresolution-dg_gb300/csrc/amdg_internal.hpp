@@ -173,6 +173,20 @@ std::vector<uint64_t> refine_keys(const HostGrid& g, const double* norms, double
 void leaf_flags(const HostGrid& g, std::vector<uint8_t>* leaf);
 // [e][d][2]: parent and grandparent in dimension d, -1 when absent
 void parent_table(const HostGrid& g, std::vector<int32_t>* pg);
+// parent tables of several grids whose elements are concatenated (offsets: grids + 1), with
+// indices into the concatenation
+void batch_parent_table(const std::vector<const HostGrid*>& grids, const std::vector<int64_t>& offset,
+                        std::vector<int32_t>* pg);
+// the adaptation between two steps on the host key set: coarsen (norm < eta), then give the
+// chosen elements (force, or norm > eps without it) that the coarsening kept their children;
+// carry[e] = 0 for the old elements that the coarsening removed (they start at zero if the
+// refinement adds them back).  norms and force are per old element.
+void adapt_keys_between_steps(const HostGrid& g, const double* norms, const uint8_t* force, double eps, double eta,
+                              std::vector<uint64_t>* keys, std::vector<uint8_t>* carry);
+// the same for several grids in parallel (norms and force over the concatenation)
+void batch_adapt_keys(const std::vector<const HostGrid*>& grids, const std::vector<int64_t>& offset,
+                      const double* norms, const uint8_t* force, double eps, double eta,
+                      std::vector<std::vector<uint64_t>>* keys, std::vector<std::vector<uint8_t>>* carry);
 // input and output widths of a classifier (capi_mlp.cu)
 void mlp_shape(const amdg_mlp* m, int* n_in, int* n_out);
 std::vector<uint64_t> coarsen_keys(const HostGrid& g, const double* norms, double eta);
@@ -409,8 +423,10 @@ struct amdg_batch {
     int64_t launches_per_graph = 0;
     int tile[2] = {256, 256};             // CTA size of the stage kernel per precision (FP64, mixed)
     float tile_ms[2][3] = {{0}};          // autotuner: one stage per candidate of kBatchTiles (0: not timed)
-    // amdg_batch_adapt scratch (grow-only): parent table, classifier features and probabilities
+    // amdg_batch_adapt scratch over all elements (grow-only): norms, parent table, classifier
+    // features and probabilities
+    double* d_norms = nullptr;
     int32_t* d_pg = nullptr;
     float *d_feat = nullptr, *d_prob = nullptr;
-    int64_t scratch_elems = 0;
+    int64_t scratch_elems = 0, norms_elems = 0;
 };

@@ -270,7 +270,7 @@ amdg_status amdg_batch_destroy(amdg_batch* b) {
     for (int p = 0; p < 2; ++p)
         if (b->graph_exec[p]) cudaGraphExecDestroy(static_cast<cudaGraphExec_t>(b->graph_exec[p]));
     void* ptrs[] = {b->d_row_ptr, b->d_src, b->d_blk, b->d_solve, b->d_blocks64, b->d_blocks32, b->d_coef64,
-                    b->d_coef32, b->d_dt, b->d_u, b->d_u1, b->d_u2, b->d_shadow, b->d_pg, b->d_feat, b->d_prob};
+                    b->d_coef32, b->d_dt, b->d_u, b->d_u1, b->d_u2, b->d_shadow, b->d_pg, b->d_feat, b->d_prob, b->d_norms};
     for (void* p : ptrs) cudaFree(p);
     delete b;
     return AMDG_OK;
@@ -356,79 +356,98 @@ amdg_status amdg_batch_adapt(amdg_batch* b, amdg_mlp* mlp, double eps, double et
         AMDG_REQUIRE(n_in == F && n_out == 3, AMDG_ERR_ARG,
                      "classifier must take " + std::to_string(F) + " features and give 3 classes");
     }
-    int64_t n_net = 0, n_unsure = 0;
+    const int n = b->nsolves;
+    const int64_t T = b->num_elements;
+    std::vector<const HostGrid*> hg(n);
+    for (int i = 0; i < n; ++i) {
+        hg[i] = &b->grids[i]->host;
+        AMDG_REQUIRE(hg[i]->num_elements == b->elem_offset[i + 1] - b->elem_offset[i], AMDG_ERR_STATE,
+                     "a grid changed since the batch was built");
+    }
     amdg_status s;
-    for (int i = 0; i < b->nsolves; ++i) {
-        // the solve's state back into its grid
-        if ((s = amdg_batch_store(b, i)) != AMDG_OK) return s;
+    AMDG_CK(cudaStreamSynchronize(st));  // steps still in flight finish outside the phase timers
+    // element norms of the whole batch state: one launch, one read
+    std::vector<double> norms(T);
+    {
+        PhaseTimer timer(b->ctx, AMDG_PHASE_NORMS);
+        if (T > b->norms_elems) {
+            cudaFree(b->d_norms);
+            b->d_norms = nullptr;
+            b->norms_elems = 0;
+            if ((s = alloc(&b->d_norms, size_t(T + T / 4))) != AMDG_OK) return s;
+            b->norms_elems = T + T / 4;
+        }
+        AMDG_CK(launch_element_norms(b->d_u, b->block, T, b->d_norms, st));
+        b->ctx->launches++;
+        if (T > 0) AMDG_CK(cudaMemcpyAsync(norms.data(), b->d_norms, size_t(T) * sizeof(double), cudaMemcpyDeviceToHost, st));
+        AMDG_CK(cudaStreamSynchronize(st));
+        for (double v : norms) AMDG_REQUIRE(std::isfinite(v), AMDG_ERR_NONFINITE, "element indicator is not finite");
+    }
+    // classifier over the whole batch state (parent indices into the concatenation); the
+    // criterion decides where it is unsure
+    int64_t n_net = 0, n_unsure = 0;
+    std::vector<uint8_t> force;
+    if (mlp) {
+        PhaseTimer timer(b->ctx, AMDG_PHASE_CLASSIFIER);
+        AMDG_REQUIRE(T < (int64_t(1) << 31), AMDG_ERR_CAPACITY, "more than 2^31-1 elements in the batch");
+        if (T > b->scratch_elems) {
+            cudaFree(b->d_pg);
+            cudaFree(b->d_feat);
+            cudaFree(b->d_prob);
+            b->d_pg = nullptr;
+            b->d_feat = b->d_prob = nullptr;
+            b->scratch_elems = 0;
+            const int64_t cap = T + T / 4;
+            if ((s = alloc(&b->d_pg, size_t(cap) * b->dim * 2)) != AMDG_OK ||
+                (s = alloc(&b->d_feat, size_t(cap) * F)) != AMDG_OK || (s = alloc(&b->d_prob, size_t(cap) * 3)) != AMDG_OK)
+                return s;
+            b->scratch_elems = cap;
+        }
+        std::vector<int32_t> pg;
+        batch_parent_table(hg, b->elem_offset, &pg);
+        AMDG_CK(cudaMemcpyAsync(b->d_pg, pg.data(), pg.size() * sizeof(int32_t), cudaMemcpyHostToDevice, st));
+        AMDG_CK(launch_element_features(b->d_u, nullptr, b->d_pg, T, b->dim, b->block, b->d_feat, st));
+        b->ctx->launches++;
+        if ((s = amdg_mlp_predict(mlp, b->d_feat, T, b->d_prob)) != AMDG_OK) return s;
+        std::vector<float> prob(size_t(T) * 3);
+        AMDG_CK(cudaMemcpyAsync(prob.data(), b->d_prob, prob.size() * sizeof(float), cudaMemcpyDeviceToHost, st));
+        AMDG_CK(cudaStreamSynchronize(st));  // pg and prob are host vectors of this scope
+        force.assign(T, 0);
+        for (int64_t e = 0; e < T; ++e) {
+            const float* p = &prob[size_t(e) * 3];
+            int arg = 0;  // classes: 0 refine, 1 keep, 2 coarsen
+            for (int q = 1; q < 3; ++q)
+                if (p[q] > p[arg]) arg = q;
+            if (p[arg] < float(tau)) {
+                ++n_unsure;
+                force[e] = norms[e] > eps ? 1 : 0;
+            } else if (arg == 0) {
+                force[e] = 1;
+                ++n_net;
+            }
+        }
+    }
+    // every solve's state back into its grid
+    for (int i = 0; i < n; ++i) {
         amdg_grid* g = b->grids[i];
-        const int64_t E = g->host.num_elements;
-        std::vector<double> norms;
-        if ((s = grid_norms(g, g->d_u, &norms)) != AMDG_OK) return s;
-        std::vector<uint8_t> force;
-        if (mlp) {
-            // classifier on the current coefficients; the criterion decides where it is unsure
-            PhaseTimer timer(b->ctx, AMDG_PHASE_CLASSIFIER);
-            if (E > b->scratch_elems) {
-                cudaFree(b->d_pg);
-                cudaFree(b->d_feat);
-                cudaFree(b->d_prob);
-                b->d_pg = nullptr;
-                b->d_feat = b->d_prob = nullptr;
-                b->scratch_elems = 0;
-                const int64_t cap = E + E / 4;
-                if ((s = alloc(&b->d_pg, size_t(cap) * b->dim * 2)) != AMDG_OK ||
-                    (s = alloc(&b->d_feat, size_t(cap) * F)) != AMDG_OK || (s = alloc(&b->d_prob, size_t(cap) * 3)) != AMDG_OK)
-                    return s;
-                b->scratch_elems = cap;
-            }
-            std::vector<int32_t> pg;
-            parent_table(g->host, &pg);
-            AMDG_CK(cudaMemcpyAsync(b->d_pg, pg.data(), pg.size() * sizeof(int32_t), cudaMemcpyHostToDevice, st));
-            AMDG_CK(launch_element_features(g->d_u, nullptr, b->d_pg, E, b->dim, b->block, b->d_feat, st));
-            b->ctx->launches++;
-            if ((s = amdg_mlp_predict(mlp, b->d_feat, E, b->d_prob)) != AMDG_OK) return s;
-            std::vector<float> prob(size_t(E) * 3);
-            AMDG_CK(cudaMemcpyAsync(prob.data(), b->d_prob, prob.size() * sizeof(float), cudaMemcpyDeviceToHost, st));
-            AMDG_CK(cudaStreamSynchronize(st));  // pg and prob are host vectors of this iteration
-            force.assign(E, 0);
-            for (int64_t e = 0; e < E; ++e) {
-                const float* p = &prob[size_t(e) * 3];
-                int arg = 0;  // classes: 0 refine, 1 keep, 2 coarsen
-                for (int q = 1; q < 3; ++q)
-                    if (p[q] > p[arg]) arg = q;
-                if (p[arg] < float(tau)) {
-                    ++n_unsure;
-                    force[e] = norms[e] > eps ? 1 : 0;
-                } else if (arg == 0) {
-                    force[e] = 1;
-                    ++n_net;
-                }
-            }
-        }
-        // coarsen, then refine the chosen elements that the coarsening kept, both on the host key
-        // sets; one element-set replacement in which the coarsened elements that the refinement
-        // adds back start at zero, as after a separate coarsen and refine
-        std::vector<uint64_t> keys;
-        std::vector<uint8_t> carry;
-        {
-            PhaseTimer timer(b->ctx, AMDG_PHASE_ADAPT_HOST);
-            const std::vector<uint64_t>& old = g->host.key;  // ascending
-            HostGrid kept;
-            kept.sparse = g->host.sparse;
-            grid_from_keys(b->dim, b->nmax, b->k, coarsen_keys(g->host, norms.data(), eta), &kept);
-            carry.assign(E, 0);
-            std::vector<uint8_t> pick(kept.num_elements, 0);
-            for (int64_t e = 0, j = 0; e < kept.num_elements; ++e) {
-                while (old[j] < kept.key[e]) ++j;  // kept is a subset of old
-                carry[j] = 1;
-                pick[e] = mlp ? force[j] : (norms[j] > eps ? 1 : 0);
-            }
-            keys = refine_keys(kept, nullptr, eps, nullptr, pick.data());
-        }
-        if ((int64_t(keys.size()) != E || !std::all_of(carry.begin(), carry.end(), [](uint8_t c) { return c != 0; })) &&
-            (s = grid_set_keys(g, std::move(keys), &carry)) != AMDG_OK)
-            return s;
+        AMDG_CK(cudaMemcpyAsync(g->d_u, b->d_u + b->elem_offset[i] * b->block, size_t(g->dof) * sizeof(double),
+                                cudaMemcpyDeviceToDevice, st));
+    }
+    AMDG_CK(cudaStreamSynchronize(st));
+    // coarsen, then refine the chosen elements that the coarsening kept, on the host key sets of
+    // all solves in parallel; then one element-set replacement per changed solve, in which the
+    // coarsened elements that the refinement adds back start at zero (as after a separate
+    // coarsen and refine)
+    std::vector<std::vector<uint64_t>> keys;
+    std::vector<std::vector<uint8_t>> carry;
+    {
+        PhaseTimer timer(b->ctx, AMDG_PHASE_ADAPT_HOST);
+        batch_adapt_keys(hg, b->elem_offset, norms.data(), mlp ? force.data() : nullptr, eps, eta, &keys, &carry);
+    }
+    for (int i = 0; i < n; ++i) {
+        const bool same = int64_t(keys[i].size()) == hg[i]->num_elements &&
+                          std::all_of(carry[i].begin(), carry[i].end(), [](uint8_t c) { return c != 0; });
+        if (!same && (s = grid_set_keys(b->grids[i], std::move(keys[i]), &carry[i])) != AMDG_OK) return s;
     }
     {
         PhaseTimer timer(b->ctx, AMDG_PHASE_TOPOLOGY);
