@@ -1224,6 +1224,33 @@ int amdg_oracle_lagr_point_values_fast(int dim, int N, int k, int64_t E, const i
     return rc;
 }
 
+/* Lagrange interpolation coefficients to Alpert coefficients: the partial sums of the transform
+ * schedule with u_v (Lagrange x Alpert) along every dimension, summed into zeroed coefficients
+ * (FastLagrInit::eval_ucoe_Alpt_Lagr, FastMultiplyLU.cpp:1617-1620, and
+ * FastInitial::transform_ucoeintp_to_ucoealpt, FastMultiplyLU.cpp:1418-1436) */
+int amdg_oracle_lagr_to_alpert_fast(int dim, int N, int k, int64_t E, const int32_t* level, const int32_t* suppt,
+                                    const double* coe, double* out) {
+    const int np = k + 1, n1 = 1 << N, nr = n1 * LS->p1, nc = n1 * np;
+    fast_ctx c;
+    if (fast_ctx_init(&c, dim, N, E, level, suppt)) return -2;
+    double* Lv = (double*)malloc((size_t)nr * nc * sizeof(double));
+    double* Lvx = (double*)malloc((size_t)nr * nc * sizeof(double));
+    double* Lf = (double*)malloc((size_t)nr * nc * sizeof(double));
+    if (!Lv || !Lvx || !Lf) return -2;
+    amdg_oracle_oper1d_lagr(N, k, Lv, Lvx, Lf);
+    memset(out, 0, (size_t)E * ipow(np, dim) * sizeof(double));
+    const double* M[16];
+    int flx[16];
+    for (int s = 0; s < dim; ++s) {
+        M[s] = Lv;
+        flx[s] = 0;
+    }
+    const int rc = fast_partial_sums(&c, coe, LS->p1, np, M, flx, 1.0, out);
+    free(Lv); free(Lvx); free(Lf);
+    fast_ctx_free(&c);
+    return rc;
+}
+
 /* Burgers RHS by the reference's fast transforms (HyperbolicLagrRHS::rhs_vol_scalar,
  * rhs_flx_intp_scalar, HyperbolicAlptRHS::rhs_flx_penalty_scalar) */
 int amdg_oracle_burgers_rhs_fast(int dim, int N, int k, int64_t E, const int32_t* level, const int32_t* suppt,

@@ -86,6 +86,10 @@ int amdg_oracle_lagr_point_values(int dim, int N, int k, int64_t E, const int32_
 /* Hierarchical surplus of point values (E x 4^dim). */
 int amdg_oracle_lagr_surplus(int dim, int N, int64_t E, const int32_t* level, const int32_t* suppt, const double* fp,
                              double* out);
+/* Alpert coefficients (E x (k+1)^dim) of the Lagrange interpolant with coefficients coe
+ * (E x p1^dim) by the fast transforms with u_v (Lagrange x Alpert) in every dimension. */
+int amdg_oracle_lagr_to_alpert_fast(int dim, int N, int k, int64_t E, const int32_t* level, const int32_t* suppt,
+                                    const double* coe, double* out);
 /* Burgers right-hand side from flux interpolation coefficients (dim x E x 4^dim) and u. */
 int amdg_oracle_burgers_rhs(int dim, int N, int k, int64_t E, const int32_t* level, const int32_t* suppt,
                             const double* fucoe, const double* u, double alpha, double* rhs);

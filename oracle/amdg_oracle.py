@@ -63,6 +63,7 @@ def lib():
         L.amdg_oracle_oper1d_lagr.argtypes = [C.c_int, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p]
         L.amdg_oracle_lagr_point_values.argtypes = [C.c_int, C.c_int, C.c_int, C.c_int64, i32p, i32p, f64p, f64p]
         L.amdg_oracle_lagr_surplus.argtypes = [C.c_int, C.c_int, C.c_int64, i32p, i32p, f64p, f64p]
+        L.amdg_oracle_lagr_to_alpert_fast.argtypes = [C.c_int, C.c_int, C.c_int, C.c_int64, i32p, i32p, f64p, f64p]
         L.amdg_oracle_burgers_rhs.argtypes = [C.c_int, C.c_int, C.c_int, C.c_int64, i32p, i32p, f64p, f64p, C.c_double,
                                               f64p]
         L.amdg_oracle_lagr_point_values_fast.argtypes = [C.c_int, C.c_int, C.c_int, C.c_int64, i32p, i32p, f64p, f64p]
@@ -306,6 +307,77 @@ def lagr_surplus(dim, N, level, suppt, fp, degree=BURGERS_LAGR_DEGREE):
     out = np.zeros_like(fp)
     _check(lib().amdg_oracle_lagr_surplus(dim, N, level.shape[0], level, suppt, np.ascontiguousarray(fp), out))
     return out
+
+
+def lagr_to_alpert_fast(dim, N, k, level, suppt, coe, degree=BURGERS_LAGR_DEGREE):
+    lagr_degree(degree)
+    out = np.zeros((level.shape[0], (k + 1) ** dim))
+    _check(lib().amdg_oracle_lagr_to_alpert_fast(dim, N, k, level.shape[0], level, suppt, np.ascontiguousarray(coe), out))
+    return out
+
+
+def lagr_points_1d(N, degree):
+    """Interpolation point coordinates of every 1D element order (2^N x (degree + 1))."""
+    lagr_degree(degree)
+    P1 = degree + 1
+    out = np.zeros((1 << N, P1))
+    for o in range(1 << N):
+        lev, sp = _elem_of_order(o)
+        for p in range(P1):
+            out[o, p] = lib().amdg_oracle_lagr_point(lev, sp, p)
+    return out
+
+
+def lagr_mass_diag_1d(N, degree):
+    """Integral of the square of every 1D Lagrange interpolation basis function over its support
+    (the diagonal of OperatorMatrix1D<LagrBasis, LagrBasis>::u_v), 10-point Gauss on each half."""
+    lagr_degree(degree)
+    P1 = degree + 1
+    x, w = gauss_legendre(10)
+    out = np.zeros((1 << N, P1))
+    for o in range(1 << N):
+        lev, sp = _elem_of_order(o)
+        h = 1.0 if lev <= 1 else 2.0 ** (1 - lev)
+        lo = 0.0 if lev <= 1 else (sp - 1) / 2 * h
+        for p in range(P1):
+            s = 0.0
+            for a, b in ((lo, lo + h / 2), (lo + h / 2, lo + h)):
+                for xi, wi in zip(x, w):
+                    xx = 0.5 * (a + b) + 0.5 * (b - a) * xi
+                    s += 0.5 * (b - a) * wi * lib().amdg_oracle_lagr_val(lev, sp, p, xx, 0) ** 2
+            out[o, p] = s
+    return out
+
+
+def init_adaptive_intp(dim, n_init, nmax, k, func, eps, degree):
+    """DGAdaptIntp::init_adaptive_intp (DGAdaptIntp.cpp:35-46, 184-235, 236-270): interpolate
+    func (x: (n, dim) array -> (n,) values) at the Lagrange points of the sparse grid of level
+    n_init, take the hierarchical surplus, refine every leaf whose indicator
+    sqrt(sum_points prod_d M_d * surplus^2) (M the 1D Lagrange mass diagonal) exceeds eps, fill
+    holes, repeat until nothing changes; then the Alpert coefficients by the fast transforms.
+    Returns (keys, u, rounds)."""
+    P1 = degree + 1
+    pts1d = lagr_points_1d(nmax, degree)
+    diag1d = lagr_mass_diag_1d(nmax, degree)
+    pidx = np.indices((P1,) * dim).reshape(dim, -1).T  # point q -> (p_0, ..., p_{dim-1})
+    lv, sp = grid(dim, n_init)
+    keys = arrays_to_keys(lv, sp)
+    rounds = 0
+    while True:
+        lv, sp = keys_to_arrays(keys, dim)
+        o = np.where(lv == 0, 0, (1 << np.maximum(lv - 1, 0)) + (sp - 1) // 2)
+        x = np.stack([pts1d[o[:, d][:, None], pidx[None, :, d]] for d in range(dim)], axis=-1)
+        fp = np.asarray(func(x.reshape(-1, dim)), dtype=np.float64).reshape(len(keys), -1)
+        coe = lagr_surplus(dim, nmax, lv, sp, fp, degree)
+        wgt = np.ones((len(keys), P1 ** dim))
+        for d in range(dim):
+            wgt = wgt * diag1d[o[:, d][:, None], pidx[None, :, d]]
+        norms = np.sqrt(np.sum(wgt * coe * coe, axis=1))
+        new = refine_keys(keys, norms, eps, nmax)
+        if len(new) == len(keys):
+            return keys, lagr_to_alpert_fast(dim, nmax, k, lv, sp, coe, degree), rounds
+        keys = new
+        rounds += 1
 
 
 def lagr_point_values_fast(dim, N, k, level, suppt, u, degree=BURGERS_LAGR_DEGREE):

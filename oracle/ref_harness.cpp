@@ -41,6 +41,10 @@
 //     source); dumps u and u_t after the adaptive initialisation and after every step.
 //   ref_harness matrices <N> <k>
 //     dumps the 1D operator matrices u_v, u_vx, ulft_vjp, urgt_vjp.
+//   ref_harness intp_init <dim> <N_init> <NMAX> <eps> <degree> <width>
+//     DGAdaptIntp::init_adaptive_intp (k = 2, Lagrange degree 3 with msh_case 1 or 4 with
+//     msh_case 2) of exp(-width |x - (0.3, 0.4, 0.5)|^2); dumps the element set and the Alpert
+//     coefficients (u_init).
 //
 // Output (text, %.17g): blocks "BEGIN <name> <rows> <cols>" ... "END".
 // Element blocks have one row per element: level[dim] suppt[dim] coeff[(k+1)^dim]
@@ -49,6 +53,7 @@
 #include "AlptBasis.h"
 #include "BilinearForm.h"
 #include "DGAdapt.h"
+#include "DGAdaptIntp.h"
 #include "DGSolution.h"
 #include "Element.h"
 #include "ExactSolution.h"
@@ -664,6 +669,38 @@ int run_matrices(int argc, char** argv) {
     return 0;
 }
 
+int run_intp_init(int argc, char** argv) {
+    if (argc < 8) { std::fprintf(stderr, "intp_init: bad args\n"); return 2; }
+    const int dim = std::atoi(argv[2]);
+    const int N_init = std::atoi(argv[3]);
+    const int NMAX = std::atoi(argv[4]);
+    const double eps = std::atof(argv[5]);
+    const int degree = std::atoi(argv[6]);
+    const double width = std::atof(argv[7]);
+    const int k = 2;
+    set_statics(dim, k, degree);
+    Hash hash;
+    LagrBasis::set_interp_msh01();
+    HermBasis::set_interp_msh01();
+    AllBasis<AlptBasis> all_bas_alpt(NMAX);
+    AllBasis<LagrBasis> all_bas_lagr(NMAX);
+    AllBasis<HermBasis> all_bas_herm(NMAX);
+    OperatorMatrix1D<LagrBasis, LagrBasis> oper_ll(all_bas_lagr, all_bas_lagr, "period");
+    OperatorMatrix1D<HermBasis, HermBasis> oper_hh(all_bas_herm, all_bas_herm, "period");
+    DGAdaptIntp dg(true, N_init, NMAX, all_bas_alpt, all_bas_lagr, all_bas_herm, hash, eps, eps / 10, true, false,
+                   oper_ll, oper_hh);
+    const double centre[3] = {0.3, 0.4, 0.5};
+    auto f = [=](std::vector<double> x, int) {
+        double r2 = 0.0;
+        for (int d = 0; d < dim; ++d) r2 += (x[d] - centre[d]) * (x[d] - centre[d]);
+        return std::exp(-width * r2);
+    };
+    dg.init_adaptive_intp(f);
+    std::printf("META dim=%d N=%d k=%d sparse=1 elements=%zu dof=%d\n", dim, NMAX, k, dg.dg.size(), dg.get_dof());
+    dump_elements("u_init", dg, 0);
+    return 0;
+}
+
 }  // namespace
 
 int main(int argc, char** argv) {
@@ -675,6 +712,7 @@ int main(int argc, char** argv) {
     if (mode == "burgers_adapt") return run_burgers_adapt(argc, argv);
     if (mode == "wave") return run_wave(argc, argv);
     if (mode == "wave_adapt") return run_wave_adapt(argc, argv);
+    if (mode == "intp_init") return run_intp_init(argc, argv);
     std::fprintf(stderr, "unknown mode %s\n", mode.c_str());
     return 2;
 }

@@ -103,10 +103,35 @@ WAVE_ADAPT_CASES = [
     ("wave_adapt3d", 3, 2, 4, 1e-3, 1e-4, 20.0, 0.05, 2),
 ]
 
+# (name, dim, N_init, NMAX, eps, Lagrange degree, width): the adaptive-interpolation initialisation
+# of exp(-width |x - (0.3, 0.4, 0.5)|^2)
+INTP_CASES = [
+    ("intp_init2d_m3", 2, 3, 6, 1e-4, 3, 100.0),
+    ("intp_init2d_m4", 2, 3, 6, 1e-4, 4, 100.0),
+    ("intp_init3d_m3", 3, 2, 5, 1e-3, 3, 50.0),
+]
+
+
+def intp_cases(manifest):
+    for name, dim, n0, nmax, eps, degree, width in INTP_CASES:
+        r = run(["intp_init", dim, n0, nmax, repr(eps), degree, repr(width)])
+        lv, sp, u = split_elements(r["u_init"], dim)
+        np.savez_compressed(os.path.join(HERE, name + ".npz"), level=lv, suppt=sp, u=u)
+        manifest[name] = dict(kind="intp_init", dim=dim, n_init=n0, nmax=nmax, k=2, eps=eps, lagr_degree=degree,
+                              width=width, centre=[0.3, 0.4, 0.5][:dim], elements=int(r["meta"]["elements"]))
+        print(name, r["meta"])
+
 
 def main():
     if not os.path.exists(HARNESS):
         sys.exit("build the reference first: make -C oracle ref")
+    if sys.argv[1:] == ["intp"]:  # only the interpolation-init cases, merged into the manifest
+        path = os.path.join(HERE, "manifest.json")
+        manifest = json.load(open(path))
+        intp_cases(manifest)
+        with open(path, "w") as f:
+            json.dump(manifest, f, indent=1)
+        return
     manifest = {}
     for name, dim, N, k, ic, engine, steps, dt, c in LINEAR_CASES:
         r = run(["linear", dim, N, k, 1, ic, engine, steps, repr(dt)] + [repr(x) for x in c])
@@ -168,6 +193,7 @@ def main():
         manifest[name] = dict(kind="wave_adapt", dim=dim, n_init=n0, nmax=nmax, eps=eps, eta=eta, sigma=sigma,
                               cfl=cfl, steps=steps, lagr_degree=4)
         print(name, r["meta"])
+    intp_cases(manifest)
     for N, k in [(4, 2), (3, 1), (3, 3)]:
         r = run(["matrices", N, k])
         name = f"oper1d_n{N}_k{k}"

@@ -262,3 +262,30 @@ def test_wave_operator_matches_reference(name):
                       m["steps"])
     assert rel_err(u, z["uT"]) < 1e-13
     assert rel_err(v, z["vT"]) < 1e-12
+
+
+INTP = [n for n, m in sorted(manifest().items()) if m["kind"] == "intp_init"]
+
+
+def gaussian_bump(m):
+    """exp(-width |x - centre|^2) on an (n, dim) array of points, as the reference run evaluates it."""
+    c, w = np.asarray(m["centre"]), m["width"]
+    return lambda x: np.exp(-w * np.sum((x - c) ** 2, axis=1))
+
+
+@pytest.mark.parametrize("name", INTP)
+def test_adaptive_interpolation_init_matches_reference(name):
+    """DGAdaptIntp::init_adaptive_intp: the adaptive Lagrange interpolation (surplus indicator
+    with the Lagrange mass diagonal, refine and fill holes until nothing changes) gives the
+    reference's element set bit-exact, and the fast Lagrange-to-Alpert transform its
+    coefficients to 1e-12 of their largest entry."""
+    m = manifest()[name]
+    z = golden(name)
+    keys, u, rounds = O.init_adaptive_intp(m["dim"], m["n_init"], m["nmax"], m["k"], gaussian_bump(m), m["eps"],
+                                           m["lagr_degree"])
+    assert rounds > 0
+    ref_keys = O.arrays_to_keys(z["level"], z["suppt"])
+    assert sorted(ref_keys) == sorted(keys)
+    pos = {kk: j for j, kk in enumerate(ref_keys)}
+    perm = [pos[kk] for kk in keys]
+    assert rel_err(u, z["u"][perm]) < 1e-12
