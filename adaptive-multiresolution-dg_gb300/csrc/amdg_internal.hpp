@@ -113,6 +113,9 @@ struct LagrTables {
 // basis function `order` (1D element order * p1 + p) at x, one-sided for sgn = -1 / 1
 double lagr_eval(const LagrSpec& s, int order, double x, int sgn);
 double lagr_point(const LagrSpec& s, int o, int p);
+// integral of the square of every 1D Lagrange basis function (order * p1 + p) over its support,
+// 10-point Gauss on each half (the diagonal of the Lagrange x Lagrange u_v)
+void lagr_mass_diag(const LagrSpec& S, int nmax, std::vector<double>* out);
 // all tables for Lagrange degree `degree` (3 or 4)
 void build_lagr_tables(const Basis1D& alpt, int degree, LagrTables* t, bool diffusion = false);
 // anc_order/anc_point/anc_rank only (t->spec and t->p1 set from `degree`)

@@ -155,6 +155,12 @@ void build_terms(amdg_burgers_op* op) {
     const int dim = op->grid->host.dim;
     op->terms.clear();
     int mat[kMaxDim], flx[kMaxDim];
+    if (op->kind == 2) {  // interpolation init: u_v (Lagrange x Alpert) in every dimension
+        op->n_pv_terms = 0;
+        for (int t = 0; t < dim; ++t) { mat[t] = kMatLV; flx[t] = 0; }
+        push_psums(op, mat, flx, 1.0, 0);
+        return;
+    }
     if (op->kind == 0) {
         for (int t = 0; t < dim; ++t) { mat[t] = kMatA2P; flx[t] = 0; }
         push_psums(op, mat, flx, 1.0, 0);
@@ -601,7 +607,8 @@ StageCoef stage_coef(int stage, double dt) {
 extern "C" {
 
 // a Lagrange-path operator of the given kind on g (tables, terms, neighbour lists)
-static amdg_status lagr_create(amdg_grid* g, int kind, const double* alpha, double sigma, amdg_burgers_op** out) {
+static amdg_status lagr_create(amdg_grid* g, int kind, const double* alpha, double sigma, amdg_burgers_op** out,
+                               int lagr_degree = 0) {
     *out = nullptr;
     AMDG_REQUIRE(g->host.k == 2, AMDG_ERR_ARG, "the Lagrange path is built for Alpert degree k = 2");
     AMDG_CK(cudaSetDevice(g->device));
@@ -614,8 +621,9 @@ static amdg_status lagr_create(amdg_grid* g, int kind, const double* alpha, doub
     op->device = g->device;
     if (alpha) op->alpha.assign(alpha, alpha + dim);
     else op->alpha.assign(dim, 0.0);
-    // Lagrange degree as the examples set it: 3 for Burgers, 4 for the wave equation
-    const int degree = kind == 1 ? 4 : 3;
+    // Lagrange degree as the examples set it: 3 for Burgers, 4 for the wave equation; the
+    // interpolation init takes the caller's
+    const int degree = kind == 1 ? 4 : (kind == 2 ? lagr_degree : 3);
     op->p1 = degree + 1;
     op->points = 1;
     for (int d = 0; d < dim; ++d) op->points *= op->p1;
@@ -1132,6 +1140,83 @@ amdg_status amdg_wave_adaptive_steps_learned(amdg_wave_op* w, amdg_mlp* mlp, dou
 amdg_status amdg_wave_counters(const amdg_wave_op* w, int64_t* stage_dof_updates, int64_t* rhs_evaluations) {
     AMDG_REQUIRE(w, AMDG_ERR_ARG, "null operator");
     return amdg_burgers_counters(w->lagr, stage_dof_updates, rhs_evaluations);
+}
+
+// The adaptive interpolation of f (DGAdaptIntp::init_adaptive_intp): point values from f on the
+// host, surpluses on the device, the indicator and refinement on the host, until the element set
+// stops changing; then the Alpert coefficients from the last surpluses by the mass term.
+static amdg_status init_adaptive_intp(amdg_burgers_op* op, amdg_fn_points f, void* user, double eps, int* rounds_out) {
+    amdg_grid* g = op->grid;
+    const int dim = g->host.dim, P1 = op->p1, P = op->points;
+    const LagrSpec& S = *lagr_spec(P1 - 1);
+    const int n1 = 1 << g->host.nmax;
+    std::vector<double> x1(size_t(n1) * P1), m1;
+    for (int o = 0; o < n1; ++o)
+        for (int p = 0; p < P1; ++p) x1[size_t(o) * P1 + p] = lagr_point(S, o, p);
+    lagr_mass_diag(S, g->host.nmax, &m1);
+    int stride[kMaxDim];
+    for (int d = 0; d < dim; ++d) stride[d] = ipow(P1, dim - 1 - d);
+    cudaStream_t st = stream_of(op);
+    std::vector<double> x, vals, coe, norms;
+    int rounds = 0;
+    amdg_status s;
+    for (;;) {
+        if ((s = burgers_sync(op)) != AMDG_OK) return s;
+        const int64_t E = g->host.num_elements, n = E * P;
+        x.resize(size_t(n) * dim);
+        vals.assign(n, 0.0);
+        for (int64_t e = 0; e < E; ++e) {
+            const int32_t* oe = &g->host.order[size_t(e) * dim];
+            for (int q = 0; q < P; ++q)
+                for (int d = 0; d < dim; ++d)
+                    x[(size_t(e) * P + q) * dim + d] = x1[size_t(oe[d]) * P1 + (q / stride[d]) % P1];
+        }
+        f(x.data(), n, dim, vals.data(), user);
+        for (double v : vals) AMDG_REQUIRE(std::isfinite(v), AMDG_ERR_NONFINITE, "the function is not finite at a point");
+        double* d_up = static_cast<double*>(op->w_up);
+        double* d_coe = static_cast<double*>(op->w_fu);
+        AMDG_CK(cudaMemcpyAsync(d_up, vals.data(), size_t(n) * sizeof(double), cudaMemcpyHostToDevice, st));
+        if ((s = eval_surplus<double, double>(op, d_up, d_coe, st)) != AMDG_OK) return s;
+        coe.resize(n);
+        AMDG_CK(cudaMemcpyAsync(coe.data(), d_coe, size_t(n) * sizeof(double), cudaMemcpyDeviceToHost, st));
+        AMDG_CK(cudaStreamSynchronize(st));
+        // DGAdaptIntp::indicator_norm_intp_Lag: sum over the points of prod_d M_d * surplus^2
+        norms.assign(E, 0.0);
+        for (int64_t e = 0; e < E; ++e) {
+            const int32_t* oe = &g->host.order[size_t(e) * dim];
+            double sum = 0.0;
+            for (int q = 0; q < P; ++q) {
+                double w = 1.0;
+                for (int d = 0; d < dim; ++d) w *= m1[size_t(oe[d]) * P1 + (q / stride[d]) % P1];
+                const double c = coe[size_t(e) * P + q];
+                sum += w * (c * c);
+            }
+            norms[e] = std::sqrt(sum);
+        }
+        std::vector<uint64_t> keys = refine_keys(g->host, norms.data(), eps);
+        if (int64_t(keys.size()) == E) break;
+        if ((s = grid_set_keys(g, std::move(keys))) != AMDG_OK) return s;
+        ++rounds;
+    }
+    const double* src[1] = {static_cast<const double*>(op->w_fu)};
+    if ((s = eval_term_range<double>(op, mats64(op), 0, int(op->terms.size()), src, 1, nullptr, g->d_u, StageOut{}, st)) !=
+        AMDG_OK)
+        return s;
+    AMDG_CK(cudaStreamSynchronize(st));
+    if (rounds_out) *rounds_out = rounds;
+    return AMDG_OK;
+}
+
+amdg_status amdg_grid_init_adaptive_intp(amdg_grid* g, int lagr_degree, amdg_fn_points f, void* user, double eps,
+                                         int* rounds) {
+    AMDG_REQUIRE(g && f && std::isfinite(eps) && eps >= 0.0, AMDG_ERR_ARG, "bad arguments");
+    AMDG_REQUIRE(lagr_degree == 3 || lagr_degree == 4, AMDG_ERR_ARG, "Lagrange degree must be 3 or 4");
+    amdg_burgers_op* op = nullptr;
+    amdg_status s = lagr_create(g, 2, nullptr, 0.0, &op, lagr_degree);
+    if (s != AMDG_OK) return s;
+    s = init_adaptive_intp(op, f, user, eps, rounds);
+    amdg_burgers_destroy(op);
+    return s;
 }
 
 }  // extern "C"

@@ -163,6 +163,23 @@ void build_lagr_ancestors(const Basis1D& alpt, int degree, LagrTables* t) {
     }
 }
 
+void lagr_mass_diag(const LagrSpec& S, int nmax, std::vector<double>* out) {
+    static const GL10 g;
+    const int n1 = 1 << nmax, P1 = S.p1;
+    out->assign(size_t(n1) * P1, 0.0);
+    for (int o = 0; o < n1; ++o) {
+        const double a = supp_lo(o), b = supp_hi(o), m = 0.5 * (a + b);
+        for (int p = 0; p < P1; ++p) {
+            const int r = o * P1 + p;
+            auto sq = [&](double x) {
+                const double v = lagr_eval(S, r, x, 0);
+                return v * v;
+            };
+            (*out)[r] = g.integrate(sq, a, m) + g.integrate(sq, m, b);
+        }
+    }
+}
+
 void build_lagr_tables(const Basis1D& alpt, int degree, LagrTables* t, bool diffusion) {
     static const GL10 g;
     const LagrSpec& S = *lagr_spec(degree);

@@ -24,6 +24,7 @@ STATUS = {0: "ok", 1: "invalid argument", 2: "capacity exceeded", 3: "non-finite
 
 FN1D = C.CFUNCTYPE(C.c_double, C.c_double, C.c_int, C.c_int, C.c_void_p)
 FN1D_BATCH = C.CFUNCTYPE(None, C.POINTER(C.c_double), C.c_int64, C.c_int, C.c_int, C.POINTER(C.c_double), C.c_void_p)
+FN_POINTS = C.CFUNCTYPE(None, C.POINTER(C.c_double), C.c_int64, C.c_int, C.POINTER(C.c_double), C.c_void_p)
 
 
 class AmdgError(RuntimeError):
@@ -100,6 +101,7 @@ def load():
         "amdg_grid_init_separable_batch": ([vp, i32, FN1D_BATCH, vp], i32),
         "amdg_grid_init_separable_adaptive_batch": ([vp, i32, FN1D_BATCH, vp, dbl], i32),
         "amdg_grid_l2_error_separable_sum_batch": ([vp, i32, FN1D_BATCH, vp, dbl, C.POINTER(dbl)], i32),
+        "amdg_grid_init_adaptive_intp": ([vp, i32, FN_POINTS, vp, dbl, C.POINTER(i32)], i32),
         "amdg_grid_refine": ([vp, vp, dbl, C.POINTER(i64)], i32),
         "amdg_grid_coarsen": ([vp, dbl, C.POINTER(i64)], i32),
         "amdg_grid_version": ([vp, C.POINTER(i64)], i32),
@@ -294,6 +296,21 @@ class Grid:
             _ck(load().amdg_grid_init_separable_adaptive(self._h, len(funcs), cb, None, eps),
                 "grid_init_separable_adaptive")
         self._refresh()
+
+    def init_adaptive_intp(self, func, eps: float, degree: int = 3) -> int:
+        """DGAdaptIntp::init_adaptive_intp: adaptive Lagrange interpolation (degree 3 or 4) of
+        func, which maps an (n, dim) array of points to n values, from the current element set;
+        returns the refinement rounds."""
+        def cb(x, n, dim, out, _user):
+            xs = np.ctypeslib.as_array(x, shape=(n, dim))
+            np.ctypeslib.as_array(out, shape=(n,))[:] = func(xs)
+
+        fn = FN_POINTS(cb)
+        rounds = C.c_int()
+        _ck(load().amdg_grid_init_adaptive_intp(self._h, degree, fn, None, eps, C.byref(rounds)),
+            "grid_init_adaptive_intp")
+        self._refresh()
+        return rounds.value
 
     def refine(self, eps: float, d_indicator: int | None = None):
         n = C.c_int64()

@@ -67,6 +67,10 @@ typedef double (*amdg_fn1d)(double x, int d, int term, void* user);
 /* The same factor at n points at once: out[i] = g_d(x[i]) for term `term` (one call per
  * dimension and term, for callers whose functions are cheap to evaluate in bulk). */
 typedef void (*amdg_fn1d_batch)(const double* x, int64_t n, int d, int term, double* out, void* user);
+/* A function of the point at n points at once: out[i] = f(x[i*dim], ..., x[i*dim + dim - 1]) (the
+ * std::function<double(std::vector<double>, int)> of DGAdaptIntp::init_adaptive_intp,
+ * DGAdaptIntp.h:33-50, for one unknown). */
+typedef void (*amdg_fn_points)(const double* x, int64_t n, int dim, double* out, void* user);
 
 /* ---- library / context ------------------------------------------------- */
 int amdg_abi_version(void);
@@ -154,6 +158,18 @@ amdg_status amdg_grid_init_separable_adaptive_batch(amdg_grid* g, int nterms, am
                                                     double eps);
 amdg_status amdg_grid_l2_error_separable_sum_batch(const amdg_grid* g, int nterms, amdg_fn1d_batch f, void* user,
                                                    double l2_norm_exact, double* out);
+/* DGAdaptIntp::init_adaptive_intp (DGAdaptIntp.cpp:35-46, 184-270; FastLagrInit,
+ * FastMultiplyLU.cpp:1617-1620): starting from the grid's element set (the sparse grid of the
+ * initial level), f is interpolated at the Lagrange points (degree 3 with the msh_case 1 nodes,
+ * or 4 with msh_case 2) and turned into hierarchical surpluses on the device; every leaf whose
+ * indicator sqrt(sum_points prod_d M_d * surplus^2) exceeds eps (M the 1D Lagrange mass diagonal,
+ * DGAdaptIntp::indicator_norm_intp_Lag) gets its children, holes are filled, and this repeats
+ * until nothing changes.  The grid's coefficients are then the Alpert coefficients of the
+ * interpolant, by the fast transforms with u_v (Lagrange x Alpert) in every dimension.  f is
+ * called once per round on all points of the current element set.  k must be 2.  rounds (may
+ * be NULL): refinement rounds that changed the element set. */
+amdg_status amdg_grid_init_adaptive_intp(amdg_grid* g, int lagr_degree, amdg_fn_points f, void* user, double eps,
+                                         int* rounds);
 /* DGAdapt::refine (DGAdapt.cpp:371-404): one pass -- leaves whose indicator
  * (the 2-norm of the element block of d_indicator, or of the grid's own
  * coefficients when NULL; DGAdapt::indicator_norm :1018-1030) exceeds eps get
