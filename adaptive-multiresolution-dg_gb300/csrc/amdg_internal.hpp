@@ -75,7 +75,7 @@ struct Fn1d {
 void project_1d(const Basis1D& b, const Fn1d& f, int d, int term, double* out);
 
 // ---- Lagrange interpolation path (hierarchical Lagrange of degree 3 or 4) ----
-constexpr int kMaxLagrPoints = 5;  // points per element and dimension (degree 4)
+constexpr int kMaxLagrPoints = 6;  // points per element and dimension (degree 5)
 
 // Node layout of a hierarchical Lagrange basis (LagrBasis.cpp:33-155): degree 3
 // with msh_case 1 (the Burgers examples) or degree 4 with msh_case 2 (the wave

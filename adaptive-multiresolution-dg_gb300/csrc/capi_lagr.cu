@@ -1210,7 +1210,7 @@ static amdg_status init_adaptive_intp(amdg_burgers_op* op, amdg_fn_points f, voi
 amdg_status amdg_grid_init_adaptive_intp(amdg_grid* g, int lagr_degree, amdg_fn_points f, void* user, double eps,
                                          int* rounds) {
     AMDG_REQUIRE(g && f && std::isfinite(eps) && eps >= 0.0, AMDG_ERR_ARG, "bad arguments");
-    AMDG_REQUIRE(lagr_degree == 3 || lagr_degree == 4, AMDG_ERR_ARG, "Lagrange degree must be 3 or 4");
+    AMDG_REQUIRE(lagr_degree >= 3 && lagr_degree <= 5, AMDG_ERR_ARG, "Lagrange degree must be 3, 4 or 5");
     amdg_burgers_op* op = nullptr;
     amdg_status s = lagr_create(g, 2, nullptr, 0.0, &op, lagr_degree);
     if (s != AMDG_OK) return s;

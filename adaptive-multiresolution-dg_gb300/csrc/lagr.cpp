@@ -37,6 +37,17 @@ const LagrSpec kDeg4 = {5,
                         {{-1, -0.75, -0.5, -0.25, 0}, {0, 0.25, 0.5, 0.75, 1}},
                         {0, 0, 1, 1, 1},
                         {1, 3, 0, 1, 3}};
+// Degree 5, msh_case 1 (the node layout of the linear example's initial interpolation):
+// level-0 nodes {-1,-3/5,-1/5,1/5,3/5,1}, the end points 1e-13 inside the element; level-1
+// nodes {-4/5,-2/5,0} on the left half and {0,2/5,4/5} on the right half (0 just left / right
+// of it), each the quintic through the level-0 nodes mapped onto its half.
+const LagrSpec kDeg5 = {6,
+                        {-1 + kRoundOff, -0.6, -0.2, 0.2, 0.6, 1 - kRoundOff},
+                        {-0.8, -0.4, 0 - kRoundOff, 0 + kRoundOff, 0.4, 0.8},
+                        {-1, -0.6, -0.2, 0.2, 0.6, 1},
+                        {{-1, -0.8, -0.6, -0.4, -0.2, 0}, {0, 0.2, 0.4, 0.6, 0.8, 1}},
+                        {0, 0, 0, 1, 1, 1},
+                        {1, 3, 5, 0, 2, 4}};
 
 double lagrange_poly(const double* nodes, int n, int i, double x) {
     double v = 1.0;
@@ -102,6 +113,7 @@ struct GL10 {
 const LagrSpec* lagr_spec(int degree) {
     if (degree == 3) return &kDeg3;
     if (degree == 4) return &kDeg4;
+    if (degree == 5) return &kDeg5;
     return nullptr;
 }
 

@@ -184,8 +184,40 @@ public:
     double refine_eps() const { return eps_; }
     double coarsen_eta() const { return eta_; }
 
-private:
+protected:
     double eps_, eta_;
+};
+
+namespace detail {
+struct PointFn {
+    const std::function<double(std::vector<double>, int)>* f;
+};
+inline void point_trampoline(const double* x, int64_t n, int dim, double* out, void* user) {
+    const auto& f = *static_cast<PointFn*>(user)->f;
+    std::vector<double> p(dim);
+    for (int64_t i = 0; i < n; ++i) {
+        p.assign(x + i * dim, x + (i + 1) * dim);
+        out[i] = f(p, 0);
+    }
+}
+}  // namespace detail
+
+// DGAdaptIntp (DGAdaptIntp.h): initialisation by adaptive Lagrange interpolation, with the
+// degree and node layout of LagrBasis (PMAX 3 or 5 with msh_case 1, or 4 with msh_case 2)
+class DGAdaptIntp : public DGAdapt {
+public:
+    DGAdaptIntp(bool sparse, int level_init, int NMAX, AllBasis<AlptBasis>& a, AllBasis<LagrBasis>& l,
+                AllBasis<HermBasis>& h, Hash& hash, double eps, double eta, bool find_alpt, bool find_intp,
+                const OperatorMatrix1D<LagrBasis, LagrBasis>&, const OperatorMatrix1D<HermBasis, HermBasis>&)
+        : DGAdapt(sparse, level_init, NMAX, a, l, h, hash, eps, eta, find_alpt, find_intp) {}
+    void init_adaptive_intp(std::function<double(std::vector<double>, int)> f) {
+        const bool ok = ((LagrBasis::PMAX == 3 || LagrBasis::PMAX == 5) && LagrBasis::msh_case == 1) ||
+                        (LagrBasis::PMAX == 4 && LagrBasis::msh_case == 2);
+        if (!ok) throw Error(AMDG_ERR_ARG, "init_adaptive_intp: Lagrange PMAX 3 or 5 (msh_case 1) or 4 (msh_case 2) only");
+        detail::PointFn pf{&f};
+        check(amdg_grid_init_adaptive_intp(grid_, LagrBasis::PMAX, detail::point_trampoline, &pf, eps_, nullptr),
+              "amdg_grid_init_adaptive_intp");
+    }
 };
 
 // ---- linear constant-coefficient operator + explicit RK ----------------------

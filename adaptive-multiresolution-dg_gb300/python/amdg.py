@@ -298,7 +298,7 @@ class Grid:
         self._refresh()
 
     def init_adaptive_intp(self, func, eps: float, degree: int = 3) -> int:
-        """DGAdaptIntp::init_adaptive_intp: adaptive Lagrange interpolation (degree 3 or 4) of
+        """DGAdaptIntp::init_adaptive_intp: adaptive Lagrange interpolation (degree 3, 4 or 5) of
         func, which maps an (n, dim) array of points to n values, from the current element set;
         returns the refinement rounds."""
         def cb(x, n, dim, out, _user):

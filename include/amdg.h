@@ -160,8 +160,8 @@ amdg_status amdg_grid_l2_error_separable_sum_batch(const amdg_grid* g, int nterm
                                                    double l2_norm_exact, double* out);
 /* DGAdaptIntp::init_adaptive_intp (DGAdaptIntp.cpp:35-46, 184-270; FastLagrInit,
  * FastMultiplyLU.cpp:1617-1620): starting from the grid's element set (the sparse grid of the
- * initial level), f is interpolated at the Lagrange points (degree 3 with the msh_case 1 nodes,
- * or 4 with msh_case 2) and turned into hierarchical surpluses on the device; every leaf whose
+ * initial level), f is interpolated at the Lagrange points (degree 3 or 5 with the msh_case 1
+ * nodes, or 4 with msh_case 2) and turned into hierarchical surpluses on the device; every leaf whose
  * indicator sqrt(sum_points prod_d M_d * surplus^2) exceeds eps (M the 1D Lagrange mass diagonal,
  * DGAdaptIntp::indicator_norm_intp_Lag) gets its children, holes are filled, and this repeats
  * until nothing changes.  The grid's coefficients are then the Alpert coefficients of the

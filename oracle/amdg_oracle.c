@@ -652,10 +652,10 @@ double amdg_oracle_l2_error_split(int dim, int N, int k, int64_t E, const int32_
  *    degree-4 polynomial on the nodes of its half at spacing 1/4. */
 typedef struct {
     int p1;                /* points per element and dimension: degree + 1 */
-    double pt0[5], pt1[5]; /* interpolation points of level 0 / levels >= 1 on [-1, 1] */
-    double node0[5];       /* level-0 polynomial nodes */
-    double half[2][5];     /* level-1 polynomial nodes of the left / right half */
-    int side[5], node[5];  /* level-1 function p: its half and its node there */
+    double pt0[6], pt1[6]; /* interpolation points of level 0 / levels >= 1 on [-1, 1] */
+    double node0[6];       /* level-0 polynomial nodes */
+    double half[2][6];     /* level-1 polynomial nodes of the left / right half */
+    int side[6], node[6];  /* level-1 function p: its half and its node there */
 } lagr_spec;
 
 static const lagr_spec LAGR_DEG3 = {4,
@@ -672,11 +672,23 @@ static const lagr_spec LAGR_DEG4 = {5,
                                     {{-1, -0.75, -0.5, -0.25, 0}, {0, 0.25, 0.5, 0.75, 1}},
                                     {0, 0, 1, 1, 1},
                                     {1, 3, 0, 1, 3}};
+/* degree 5, msh_case 1 (02_hyperbolic_01_scalar_const_coefficient.cpp:44-45): level-0 nodes
+ * {-1,-3/5,-1/5,1/5,3/5,1}, the end points 1e-13 inside; level-1 nodes {-4/5,-2/5,0} on the
+ * left half and {0,2/5,4/5} on the right half (0 just left / right of it), each the quintic on
+ * the nodes of its half at spacing 1/5 (the level-0 nodes mapped onto the half) */
+static const lagr_spec LAGR_DEG5 = {6,
+                                    {-1 + ROUND_OFF, -0.6, -0.2, 0.2, 0.6, 1 - ROUND_OFF},
+                                    {-0.8, -0.4, 0 - ROUND_OFF, 0 + ROUND_OFF, 0.4, 0.8},
+                                    {-1, -0.6, -0.2, 0.2, 0.6, 1},
+                                    {{-1, -0.8, -0.6, -0.4, -0.2, 0}, {0, 0.2, 0.4, 0.6, 0.8, 1}},
+                                    {0, 0, 0, 1, 1, 1},
+                                    {1, 3, 5, 0, 2, 4}};
 static const lagr_spec* LS = &LAGR_DEG3;
 
 int amdg_oracle_set_lagr_degree(int degree) {
     if (degree == 3) LS = &LAGR_DEG3;
     else if (degree == 4) LS = &LAGR_DEG4;
+    else if (degree == 5) LS = &LAGR_DEG5;
     else return -1;
     return 0;
 }
@@ -879,8 +891,8 @@ int amdg_oracle_lagr_surplus(int dim, int N, int64_t E, const int32_t* level, co
             /* the p1 coarser points inside this element's dimension-d support */
             const int P1 = LS->p1;
             const double xl = support_lo(l, j), xr = support_hi(l, j);
-            int anc_o[5], anc_q[5];
-            double anc_x[5];
+            int anc_o[6], anc_q[6];
+            double anc_x[6];
             int ic = 0;
             for (int o = 0; o < (1 << l) && ic < P1; ++o) {
                 const elem1d ea = elem_of_order(o);
@@ -897,12 +909,12 @@ int amdg_oracle_lagr_surplus(int dim, int N, int64_t E, const int32_t* level, co
             }
             /* weight: minus the level-0 Lagrange basis of the ancestor's rank among the
              * sorted ancestor positions, at this element's own node */
-            int rank[5];
+            int rank[6];
             for (int a = 0; a < P1; ++a) {
                 rank[a] = 0;
                 for (int b = 0; b < P1; ++b) if (anc_x[b] < anc_x[a]) ++rank[a];
             }
-            int64_t anc_e[5];
+            int64_t anc_e[6];
             int missing = ic != P1;
             for (int a = 0; a < P1 && !missing; ++a) {
                 int o[16];

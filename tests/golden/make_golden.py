@@ -109,6 +109,8 @@ INTP_CASES = [
     ("intp_init2d_m3", 2, 3, 6, 1e-4, 3, 100.0),
     ("intp_init2d_m4", 2, 3, 6, 1e-4, 4, 100.0),
     ("intp_init3d_m3", 3, 2, 5, 1e-3, 3, 50.0),
+    ("intp_init2d_m5", 2, 3, 6, 1e-5, 5, 100.0),
+    ("intp_init3d_m5", 3, 2, 5, 1e-4, 5, 50.0),
 ]
 
 

@@ -50,7 +50,7 @@ def test_init_adaptive_intp_matches_oracle(ctx, dim, n_init, nmax, eps, degree, 
 def test_init_adaptive_intp_rejects_bad_input(ctx):
     g = amdg.Grid(ctx, 2, 5, 2, level_init=2)
     with pytest.raises(RuntimeError):
-        g.init_adaptive_intp(bump((0.5, 0.5), 10.0), 1e-4, degree=5)
+        g.init_adaptive_intp(bump((0.5, 0.5), 10.0), 1e-4, degree=6)
     with pytest.raises(RuntimeError):
         g.init_adaptive_intp(lambda x: np.full(len(x), np.nan), 1e-4)
     g.close()
