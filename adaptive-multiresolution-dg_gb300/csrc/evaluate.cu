@@ -299,6 +299,22 @@ amdg_status prepare(const amdg_grid* g, const std::vector<double>& x1d, EvalTabl
     return AMDG_OK;
 }
 
+// out[i] = a_block(ia[i]) . b_block(ib[i]) (ia / ib NULL: the index i itself), one warp per pair
+__global__ void __launch_bounds__(kEvalThreads) block_dot_kernel(const double* __restrict__ a, const double* __restrict__ b,
+                                                               const int32_t* __restrict__ ia,
+                                                               const int32_t* __restrict__ ib, int64_t n, int B,
+                                                               double* __restrict__ out) {
+    const int lane = threadIdx.x & 31;
+    const int64_t warps = int64_t(gridDim.x) * (blockDim.x >> 5);
+    for (int64_t i = int64_t(blockIdx.x) * (blockDim.x >> 5) + (threadIdx.x >> 5); i < n; i += warps) {
+        const int64_t ea = ia ? ia[i] : i, eb = ib ? ib[i] : i;
+        double s = 0.0;
+        for (int q = lane; q < B; q += 32) s = fma(a[ea * B + q], b[eb * B + q], s);
+        for (int off = 16; off > 0; off >>= 1) s += __shfl_down_sync(0xffffffffu, s, off);
+        if (lane == 0) out[i] = s;
+    }
+}
+
 unsigned eval_blocks(int64_t total) {
     int dev = 0, sms = 152;
     if (cudaGetDevice(&dev) == cudaSuccess) cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
@@ -390,6 +406,50 @@ amdg_status amdg_grid_error_burgers(const amdg_grid* g, double a, double b, doub
     err[0] = l1 * scale;
     err[1] = std::sqrt(l2 * scale);
     err[2] = mx;
+    return AMDG_OK;
+}
+
+amdg_status amdg_grid_l2_error_split_grid(const amdg_grid* g, const amdg_grid* exact, double* out) {
+    AMDG_REQUIRE(g && exact && out, AMDG_ERR_ARG, "null argument");
+    const HostGrid& h = g->host;
+    const HostGrid& he = exact->host;
+    AMDG_REQUIRE(h.dim == he.dim && h.nmax == he.nmax && h.k == he.k && g->device == exact->device, AMDG_ERR_ARG,
+                 "the grids differ in dimension, finest level, degree or device");
+    AMDG_CK(cudaSetDevice(g->device));
+    cudaStream_t st = static_cast<cudaStream_t>(g->ctx->stream);
+    if (exact->ctx != g->ctx) AMDG_CK(cudaStreamSynchronize(static_cast<cudaStream_t>(exact->ctx->stream)));
+    // shared elements by a merge of the two ascending key lists
+    std::vector<int32_t> ia, ib;
+    for (int64_t i = 0, j = 0; i < h.num_elements && j < he.num_elements;) {
+        if (h.key[i] < he.key[j]) ++i;
+        else if (he.key[j] < h.key[i]) ++j;
+        else {
+            ia.push_back(int32_t(i++));
+            ib.push_back(int32_t(j++));
+        }
+    }
+    const int64_t E = h.num_elements, Ee = he.num_elements, n = int64_t(ia.size());
+    EvalTables T;
+    const int32_t *d_ia = nullptr, *d_ib = nullptr;
+    const double* d_dot0 = nullptr;
+    std::vector<double> dots(size_t(E + Ee + n), 0.0);
+    amdg_status s;
+    if ((s = T.put(ia, &d_ia)) != AMDG_OK || (s = T.put(ib, &d_ib)) != AMDG_OK || (s = T.put(dots, &d_dot0)) != AMDG_OK)
+        return s;
+    double* d_dot = const_cast<double*>(d_dot0);
+    const int B = g->block;
+    if (Ee > 0) block_dot_kernel<<<eval_blocks(Ee * 32), kEvalThreads, 0, st>>>(exact->d_u, exact->d_u, nullptr, nullptr, Ee, B, d_dot);
+    if (E > 0) block_dot_kernel<<<eval_blocks(E * 32), kEvalThreads, 0, st>>>(g->d_u, g->d_u, nullptr, nullptr, E, B, d_dot + Ee);
+    if (n > 0) block_dot_kernel<<<eval_blocks(n * 32), kEvalThreads, 0, st>>>(g->d_u, exact->d_u, d_ia, d_ib, n, B, d_dot + Ee + E);
+    AMDG_CK(cudaGetLastError());
+    g->ctx->launches += 3;
+    AMDG_CK(cudaMemcpyAsync(dots.data(), d_dot, dots.size() * sizeof(double), cudaMemcpyDeviceToHost, st));
+    AMDG_CK(cudaStreamSynchronize(st));
+    // the reference's order: |u_exact|^2, then |u|^2, then the shared products
+    double err2 = 0.0;
+    for (int64_t i = 0; i < Ee + E; ++i) err2 += dots[i];
+    for (int64_t i = 0; i < n; ++i) err2 -= 2.0 * dots[Ee + E + i];
+    *out = err2 < 0.0 ? err2 : std::sqrt(err2);
     return AMDG_OK;
 }
 

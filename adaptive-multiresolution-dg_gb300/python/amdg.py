@@ -102,6 +102,7 @@ def load():
         "amdg_grid_init_separable_adaptive_batch": ([vp, i32, FN1D_BATCH, vp, dbl], i32),
         "amdg_grid_l2_error_separable_sum_batch": ([vp, i32, FN1D_BATCH, vp, dbl, C.POINTER(dbl)], i32),
         "amdg_grid_init_adaptive_intp": ([vp, i32, FN_POINTS, vp, dbl, C.POINTER(i32)], i32),
+        "amdg_grid_l2_error_split_grid": ([vp, vp, C.POINTER(dbl)], i32),
         "amdg_grid_refine": ([vp, vp, dbl, C.POINTER(i64)], i32),
         "amdg_grid_coarsen": ([vp, dbl, C.POINTER(i64)], i32),
         "amdg_grid_version": ([vp, C.POINTER(i64)], i32),
@@ -311,6 +312,12 @@ class Grid:
             "grid_init_adaptive_intp")
         self._refresh()
         return rounds.value
+
+    def l2_error_split_grid(self, exact) -> float:
+        """DGAdaptIntp::get_L2_error_split_adaptive_intp_scalar against the solution on `exact`."""
+        out = C.c_double()
+        _ck(load().amdg_grid_l2_error_split_grid(self._h, exact.handle, C.byref(out)), "grid_l2_error_split_grid")
+        return out.value
 
     def refine(self, eps: float, d_indicator: int | None = None):
         n = C.c_int64()

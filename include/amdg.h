@@ -170,6 +170,12 @@ amdg_status amdg_grid_l2_error_separable_sum_batch(const amdg_grid* g, int nterm
  * be NULL): refinement rounds that changed the element set. */
 amdg_status amdg_grid_init_adaptive_intp(amdg_grid* g, int lagr_degree, amdg_fn_points f, void* user, double eps,
                                          int* rounds);
+/* DGAdaptIntp::get_L2_error_split_adaptive_intp_scalar (DGAdaptIntp.cpp:57-102): the L2 distance
+ * between the solutions on g and on `exact` (same dimension, finest level and degree), from the
+ * orthonormality of the Alpert basis: err^2 = |u_exact|^2 + |u|^2 - 2 * (sum over the elements
+ * both grids hold of u . u_exact).  The block products run on the device.  *out = sqrt(err^2),
+ * or err^2 itself when it is negative, as the reference returns it. */
+amdg_status amdg_grid_l2_error_split_grid(const amdg_grid* g, const amdg_grid* exact, double* out);
 /* DGAdapt::refine (DGAdapt.cpp:371-404): one pass -- leaves whose indicator
  * (the 2-norm of the element block of d_indicator, or of the grid's own
  * coefficients when NULL; DGAdapt::indicator_norm :1018-1030) exceeds eps get

@@ -380,6 +380,19 @@ def init_adaptive_intp(dim, n_init, nmax, k, func, eps, degree):
         rounds += 1
 
 
+def l2_error_split_grids(keys, u, keys_exact, u_exact):
+    """DGAdaptIntp::get_L2_error_split_adaptive_intp_scalar (DGAdaptIntp.cpp:57-102): with the
+    orthonormal Alpert basis, err^2 = |u_exact|^2 + |u|^2 - 2 sum over the shared elements of
+    u . u_exact; a negative err^2 is returned as it is, else its square root."""
+    err2 = float(np.sum(np.asarray(u_exact) ** 2)) + float(np.sum(np.asarray(u) ** 2))
+    pos = {k: i for i, k in enumerate(keys_exact)}
+    for i, k in enumerate(keys):
+        j = pos.get(k)
+        if j is not None:
+            err2 -= 2.0 * float(np.dot(u[i], u_exact[j]))
+    return err2 if err2 < 0 else math.sqrt(err2)
+
+
 def lagr_point_values_fast(dim, N, k, level, suppt, u, degree=BURGERS_LAGR_DEGREE):
     lagr_degree(degree)
     up = np.zeros((level.shape[0], (degree + 1) ** dim))

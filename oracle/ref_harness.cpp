@@ -45,6 +45,10 @@
 //     DGAdaptIntp::init_adaptive_intp (k = 2, Lagrange degree 3 with msh_case 1 or 4 with
 //     msh_case 2) of exp(-width |x - (0.3, 0.4, 0.5)|^2); dumps the element set and the Alpert
 //     coefficients (u_init).
+//   ref_harness intp_error <dim> <N_init> <NMAX> <eps_a> <eps_b> <degree> <width>
+//     two such initialisations (refine eps_a and eps_b) and
+//     DGAdaptIntp::get_L2_error_split_adaptive_intp_scalar of the first against the second
+//     (dumps u_a, u_b and the 1 x 1 block err).
 //
 // Output (text, %.17g): blocks "BEGIN <name> <rows> <cols>" ... "END".
 // Element blocks have one row per element: level[dim] suppt[dim] coeff[(k+1)^dim]
@@ -701,6 +705,43 @@ int run_intp_init(int argc, char** argv) {
     return 0;
 }
 
+int run_intp_error(int argc, char** argv) {
+    if (argc < 9) { std::fprintf(stderr, "intp_error: bad args\n"); return 2; }
+    const int dim = std::atoi(argv[2]);
+    const int N_init = std::atoi(argv[3]);
+    const int NMAX = std::atoi(argv[4]);
+    const double eps_a = std::atof(argv[5]);
+    const double eps_b = std::atof(argv[6]);
+    const int degree = std::atoi(argv[7]);
+    const double width = std::atof(argv[8]);
+    set_statics(dim, 2, degree);
+    Hash hash;
+    LagrBasis::set_interp_msh01();
+    HermBasis::set_interp_msh01();
+    AllBasis<AlptBasis> all_bas_alpt(NMAX);
+    AllBasis<LagrBasis> all_bas_lagr(NMAX);
+    AllBasis<HermBasis> all_bas_herm(NMAX);
+    OperatorMatrix1D<LagrBasis, LagrBasis> oper_ll(all_bas_lagr, all_bas_lagr, "period");
+    OperatorMatrix1D<HermBasis, HermBasis> oper_hh(all_bas_herm, all_bas_herm, "period");
+    const double centre[3] = {0.3, 0.4, 0.5};
+    auto f = [=](std::vector<double> x, int) {
+        double r2 = 0.0;
+        for (int d = 0; d < dim; ++d) r2 += (x[d] - centre[d]) * (x[d] - centre[d]);
+        return std::exp(-width * r2);
+    };
+    DGAdaptIntp a(true, N_init, NMAX, all_bas_alpt, all_bas_lagr, all_bas_herm, hash, eps_a, eps_a / 10, true, false,
+                  oper_ll, oper_hh);
+    a.init_adaptive_intp(f);
+    DGAdaptIntp b(true, N_init, NMAX, all_bas_alpt, all_bas_lagr, all_bas_herm, hash, eps_b, eps_b / 10, true, false,
+                  oper_ll, oper_hh);
+    b.init_adaptive_intp(f);
+    const double err = a.get_L2_error_split_adaptive_intp_scalar(b);
+    dump_elements("u_a", a, 0);
+    dump_elements("u_b", b, 0);
+    std::printf("BEGIN err 1 1\n%.17g\nEND\n", err);
+    return 0;
+}
+
 }  // namespace
 
 int main(int argc, char** argv) {
@@ -713,6 +754,7 @@ int main(int argc, char** argv) {
     if (mode == "wave") return run_wave(argc, argv);
     if (mode == "wave_adapt") return run_wave_adapt(argc, argv);
     if (mode == "intp_init") return run_intp_init(argc, argv);
+    if (mode == "intp_error") return run_intp_error(argc, argv);
     std::fprintf(stderr, "unknown mode %s\n", mode.c_str());
     return 2;
 }

@@ -114,7 +114,25 @@ INTP_CASES = [
 ]
 
 
+# (name, dim, N_init, NMAX, eps_a, eps_b, Lagrange degree, width): the split L2 error of one
+# adaptive interpolation against a finer one
+INTP_ERROR_CASES = [
+    ("intp_error2d", 2, 3, 7, 1e-3, 1e-6, 3, 100.0),
+    ("intp_error3d", 3, 2, 6, 1e-3, 1e-5, 4, 50.0),
+]
+
+
 def intp_cases(manifest):
+    for name, dim, n0, nmax, ea, eb, degree, width in INTP_ERROR_CASES:
+        r = run(["intp_error", dim, n0, nmax, repr(ea), repr(eb), degree, repr(width)])
+        la, sa, ua = split_elements(r["u_a"], dim)
+        lb, sb, ub = split_elements(r["u_b"], dim)
+        np.savez_compressed(os.path.join(HERE, name + ".npz"), level_a=la, suppt_a=sa, u_a=ua, level_b=lb,
+                            suppt_b=sb, u_b=ub, err=r["err"].reshape(-1))
+        manifest[name] = dict(kind="intp_error", dim=dim, n_init=n0, nmax=nmax, k=2, eps_a=ea, eps_b=eb,
+                              lagr_degree=degree, width=width, centre=[0.3, 0.4, 0.5][:dim],
+                              err=float(r["err"].reshape(-1)[0]))
+        print(name, float(r["err"].reshape(-1)[0]), len(ua), len(ub))
     for name, dim, n0, nmax, eps, degree, width in INTP_CASES:
         r = run(["intp_init", dim, n0, nmax, repr(eps), degree, repr(width)])
         lv, sp, u = split_elements(r["u_init"], dim)

@@ -54,3 +54,29 @@ def test_init_adaptive_intp_rejects_bad_input(ctx):
     with pytest.raises(RuntimeError):
         g.init_adaptive_intp(lambda x: np.full(len(x), np.nan), 1e-4)
     g.close()
+
+
+INTP_ERR = [n for n, m in sorted(manifest().items()) if m["kind"] == "intp_error"]
+
+
+@pytest.mark.parametrize("name", INTP_ERR)
+def test_interpolated_split_error_matches_reference(ctx, name):
+    """DGAdaptIntp::get_L2_error_split_adaptive_intp_scalar of a coarse adaptive interpolation
+    against a finer one: to 1e-9 of the reference's value (err^2 is a difference of sums of
+    squares); the distance of a solution to itself is at roundoff level."""
+    m = manifest()[name]
+    f = bump(m["centre"], m["width"])
+    grids = []
+    for eps in (m["eps_a"], m["eps_b"]):
+        g = amdg.Grid(ctx, m["dim"], m["nmax"], m["k"], level_init=m["n_init"])
+        g.init_adaptive_intp(f, eps, m["lagr_degree"])
+        grids.append(g)
+    a, b = grids
+    err = a.l2_error_split_grid(b)
+    assert abs(err - m["err"]) <= 1e-9 * m["err"]
+    assert abs(a.l2_error_split_grid(a)) < 1e-6
+    other = amdg.Grid(ctx, m["dim"], m["nmax"] - 1, m["k"])
+    with pytest.raises(RuntimeError):
+        a.l2_error_split_grid(other)
+    for g in (a, b, other):
+        g.close()

@@ -289,3 +289,22 @@ def test_adaptive_interpolation_init_matches_reference(name):
     pos = {kk: j for j, kk in enumerate(ref_keys)}
     perm = [pos[kk] for kk in keys]
     assert rel_err(u, z["u"][perm]) < 1e-12
+
+
+INTP_ERR = [n for n, m in sorted(manifest().items()) if m["kind"] == "intp_error"]
+
+
+@pytest.mark.parametrize("name", INTP_ERR)
+def test_interpolated_split_error_matches_reference(name):
+    """DGAdaptIntp::get_L2_error_split_adaptive_intp_scalar of a coarse adaptive interpolation
+    against a finer one: both element sets bit-exact, the error to 1e-9 relative (err^2 is a
+    difference of sums of squares, so the error's own accuracy is that of the cancellation)."""
+    m = manifest()[name]
+    z = golden(name)
+    f = gaussian_bump(m)
+    ka, ua, _ = O.init_adaptive_intp(m["dim"], m["n_init"], m["nmax"], m["k"], f, m["eps_a"], m["lagr_degree"])
+    kb, ub, _ = O.init_adaptive_intp(m["dim"], m["n_init"], m["nmax"], m["k"], f, m["eps_b"], m["lagr_degree"])
+    assert sorted(ka) == sorted(O.arrays_to_keys(z["level_a"], z["suppt_a"]))
+    assert sorted(kb) == sorted(O.arrays_to_keys(z["level_b"], z["suppt_b"]))
+    err = O.l2_error_split_grids(ka, ua, kb, ub)
+    assert abs(err - m["err"]) <= 1e-9 * m["err"]
