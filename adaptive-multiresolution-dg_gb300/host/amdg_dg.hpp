@@ -218,6 +218,13 @@ public:
         check(amdg_grid_init_adaptive_intp(grid_, LagrBasis::PMAX, detail::point_trampoline, &pf, eps_, nullptr),
               "amdg_grid_init_adaptive_intp");
     }
+    // L2 distance to the solution held by `exact_solu` (the reference's name for the argument;
+    // its drivers pass the numerical solution to the interpolated exact one)
+    double get_L2_error_split_adaptive_intp_scalar(DGSolution& exact_solu) const {
+        double err = 0.0;
+        check(amdg_grid_l2_error_split_grid(grid_, exact_solu.handle(), &err), "amdg_grid_l2_error_split_grid");
+        return err;
+    }
 };
 
 // ---- linear constant-coefficient operator + explicit RK ----------------------

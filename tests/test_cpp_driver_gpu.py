@@ -55,3 +55,29 @@ def test_cpp_wave_driver_matches_oracle():
     su, sut = float(np.sum(u * u)), float(np.sum(v * v))
     assert abs(float(fields["sum of squares u"]) - su) <= 1e-12 * su
     assert abs(float(fields["sum of squares u_t"]) - sut) <= 1e-11 * sut
+
+
+def test_cpp_intp_driver_matches_oracle():
+    """The linear driver with the reference's own initialisation (adaptive Lagrange interpolation
+    of degree 5, msh_case 1, of cos(2 pi (x + y))) and error (split L2 distance to the exact
+    solution interpolated with refine 1e-6): the oracle's element counts and error."""
+    exe = os.path.join(os.path.dirname(amdg.LIB_PATH), "hyperbolic_const_coefficient_intp")
+    assert os.path.exists(exe), "example driver not built"
+    N, T, dim = 5, 0.05, 2
+    out = subprocess.run([exe, str(N), str(T)], capture_output=True, text=True, timeout=300, check=True).stdout
+    fields = dict(line.split(":", 1) for line in out.splitlines() if ":" in line)
+    err = float(fields["L2 error at final time"])
+    head = out.splitlines()[0].split()
+    elements, steps, dt, elements_ext = int(head[1]), int(head[5]), float(head[7]), int(head[9])
+
+    def f(shift):
+        return lambda x: np.cos(2 * np.pi * (np.sum(x, axis=1) - shift))
+
+    keys, u0, _ = O.init_adaptive_intp(dim, N, N, 2, f(0.0), 1e10, 5)
+    lv, sp = O.keys_to_arrays(keys, dim)
+    uT = O.linear_rk3(dim, N, 2, lv, sp, [1.0, 1.0], u0, dt, steps)
+    keys_ext, u_ext, _ = O.init_adaptive_intp(dim, N, N, 2, f(dim * T), 1e-6, 5)
+    ref = O.l2_error_split_grids(keys_ext, u_ext, keys, uT)
+    assert (elements, elements_ext) == (len(keys), len(keys_ext))
+    assert abs(err - ref) <= 1e-7 * ref
+    assert 0 < ref < 1e-2
