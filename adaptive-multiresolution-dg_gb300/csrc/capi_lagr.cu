@@ -900,7 +900,7 @@ amdg_status amdg_burgers_features(amdg_burgers_op* op, const double* d_u, float*
 static amdg_status learned_step_any(amdg_burgers_op* op, amdg_mlp* mlp, double cfl, double wave_speed, double eps,
                                     double eta, double tau, amdg_precision prec, int horizon, double t_left,
                                     double* t_advanced, int* steps_out, int64_t* stats) {
-    AMDG_REQUIRE(op && mlp && std::isfinite(cfl) && cfl > 0 && std::isfinite(wave_speed) && wave_speed > 0 &&
+    AMDG_REQUIRE(op && std::isfinite(cfl) && cfl > 0 && std::isfinite(wave_speed) && wave_speed > 0 &&
                      horizon >= 1 && std::isfinite(t_left) && t_left >= 0,
                  AMDG_ERR_ARG, "bad arguments");
     AMDG_REQUIRE(prec == AMDG_PREC_FP64 || prec == AMDG_PREC_MIXED, AMDG_ERR_ARG, "bad precision");
@@ -913,14 +913,17 @@ static amdg_status learned_step_any(amdg_burgers_op* op, amdg_mlp* mlp, double c
     const int64_t E = g->host.num_elements;
     // the wave classifier also reads u_t (the indicator of prob "wave" adds ||u_t||)
     const int F = g->block * (1 + 2 * g->host.dim) * (op->kind == 1 ? 2 : 1);
-    int n_in = 0, n_out = 0;
-    mlp_shape(mlp, &n_in, &n_out);
-    AMDG_REQUIRE(n_in == F && n_out == 3, AMDG_ERR_ARG,
-                 "classifier must take " + std::to_string(F) + " features and give 3 classes");
-    // 1. the network's refine/keep/coarsen probabilities from the current coefficients
+    if (mlp) {
+        int n_in = 0, n_out = 0;
+        mlp_shape(mlp, &n_in, &n_out);
+        AMDG_REQUIRE(n_in == F && n_out == 3, AMDG_ERR_ARG,
+                     "classifier must take " + std::to_string(F) + " features and give 3 classes");
+    }
+    // 1. the network's refine/keep/coarsen probabilities from the current coefficients (without
+    //    a network every element counts as unsure: the criterion decides everywhere)
     amdg_status s = AMDG_OK;
-    std::vector<float> prob(size_t(E) * 3);
-    {
+    std::vector<float> prob(size_t(E) * 3, 0.0f);
+    if (mlp) {
         PhaseTimer tc(g->ctx, AMDG_PHASE_CLASSIFIER);
         if ((s = ensure_features(op, E, F)) != AMDG_OK) return s;
         if (op->kind == 1 && (s = ensure_velocity(g)) != AMDG_OK) return s;

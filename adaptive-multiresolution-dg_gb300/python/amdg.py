@@ -355,9 +355,11 @@ class Grid:
         u = np.ascontiguousarray(u, np.float64).reshape(-1)
         _ck(load().amdg_grid_set_coefficients(self._h, _ptr(u), u.size), "grid_set_coefficients")
 
-    def coefficients(self) -> np.ndarray:
-        u = np.zeros(self.dof)
-        _ck(load().amdg_grid_get_coefficients(self._h, _ptr(u), u.size), "grid_get_coefficients")
+    def coefficients(self, out: np.ndarray | None = None) -> np.ndarray:
+        """The coefficients as (num_elements, block); into `out` (dof float64 entries, e.g. pinned
+        host memory) when given."""
+        u = np.zeros(self.dof) if out is None else out.reshape(-1)[:self.dof]
+        _ck(load().amdg_grid_get_coefficients(self._h, _ptr(u), self.dof), "grid_get_coefficients")
         return u.reshape(self.num_elements, self.block)
 
     def device_ptr(self) -> int:
@@ -538,7 +540,7 @@ class BurgersOperator:
                               prec: int = FP64):
         stats = np.zeros(4, np.int64)
         dt = C.c_double()
-        _ck(load().amdg_burgers_adaptive_step_learned(self._h, mlp.handle, cfl, wave_speed, eps, eta, tau, prec,
+        _ck(load().amdg_burgers_adaptive_step_learned(self._h, mlp.handle if mlp is not None else None, cfl, wave_speed, eps, eta, tau, prec,
                                                       C.byref(dt), _ptr(stats)), "burgers_adaptive_step_learned")
         self.grid._refresh()
         return dt.value, stats
@@ -548,7 +550,7 @@ class BurgersOperator:
         """(time advanced, steps taken, stats) of one learned pre-adaptation and `horizon` steps."""
         stats = np.zeros(4, np.int64)
         ta, n = C.c_double(), C.c_int()
-        _ck(load().amdg_burgers_adaptive_steps_learned(self._h, mlp.handle, cfl, wave_speed, eps, eta, tau, prec,
+        _ck(load().amdg_burgers_adaptive_steps_learned(self._h, mlp.handle if mlp is not None else None, cfl, wave_speed, eps, eta, tau, prec,
                                                        horizon, t_left, C.byref(ta), C.byref(n), _ptr(stats)),
             "burgers_adaptive_steps_learned")
         self.grid._refresh()
@@ -627,7 +629,7 @@ class WaveOperator:
                               prec: int = FP64):
         stats = np.zeros(4, np.int64)
         dt = C.c_double()
-        _ck(load().amdg_wave_adaptive_step_learned(self._h, mlp.handle, cfl, wave_speed, eps, eta, tau, prec,
+        _ck(load().amdg_wave_adaptive_step_learned(self._h, mlp.handle if mlp is not None else None, cfl, wave_speed, eps, eta, tau, prec,
                                                    C.byref(dt), _ptr(stats)), "wave_adaptive_step_learned")
         self.grid._refresh()
         return dt.value, stats
@@ -636,7 +638,7 @@ class WaveOperator:
                                horizon: int, t_left: float = 0.0, prec: int = FP64):
         stats = np.zeros(4, np.int64)
         ta, n = C.c_double(), C.c_int()
-        _ck(load().amdg_wave_adaptive_steps_learned(self._h, mlp.handle, cfl, wave_speed, eps, eta, tau, prec,
+        _ck(load().amdg_wave_adaptive_steps_learned(self._h, mlp.handle if mlp is not None else None, cfl, wave_speed, eps, eta, tau, prec,
                                                     horizon, t_left, C.byref(ta), C.byref(n), _ptr(stats)),
             "wave_adaptive_steps_learned")
         self.grid._refresh()

@@ -475,7 +475,9 @@ amdg_status amdg_burgers_adaptive_step_learned(amdg_burgers_op* op, amdg_mlp* ml
 /* The learned step over a horizon: the classifier (trained on the plain criterion's refinements
  * within the next `horizon` steps) pre-adapts the grid once, then `horizon` SSP-RK3 steps of one dt
  * run on that grid (a CUDA graph replays them), then coarsening and the criterion's check for
- * missed refinements as above.  With t_left > 0 no step passes t_left: the horizon is cut and its
+ * missed refinements as above.  mlp may be NULL: the surplus criterion on the current coefficients
+ * then pre-adapts the grid alone (the same horizon without a network, the ablation of the
+ * classifier).  With t_left > 0 no step passes t_left: the horizon is cut and its
  * last step shortened to land on it.  *t_advanced = the time stepped, *steps = the steps taken
  * (either may be NULL). */
 amdg_status amdg_burgers_adaptive_steps_learned(amdg_burgers_op* op, amdg_mlp* mlp, double cfl, double wave_speed,

@@ -30,7 +30,15 @@
 //     dt = cfl / sum_d umax 2^maxlevel_d, copy_ucoe_to_predict, ForwardEuler
 //     predictor, refine, copy_predict_to_ucoe, three RK3SSP stages, coarsen.
 //     Dumps the element set and coefficients after init (u_init) and after
-//     every step (u_step<i>), with the step sizes.
+//     every step (u_step<i>), with the step sizes and the largest level sum of
+//     any element (Hash::hash_key overflows int32 in 3D once it reaches 23,
+//     Hash.cpp:55-114; such a step is flagged "HASH_OVERFLOW").
+//   ref_harness burgers_adapt ... <steps> time [t_end]
+//     the same loop without dumps: wall time of every time step (the evolution
+//     loop only, initialisation excluded) with the DOF the step's RK stages
+//     advanced (get_dof after refine), "TSTEP <i> <seconds> <dof> <elements>";
+//     with t_end the last step is shortened to land on it, as
+//     02_hyperbolic_05_burgers_adapt.cpp does (dt = min(dt, final_time - t)).
 //   ref_harness wave <dim> <N> <sigma> <steps> <dt> [a]
 //     u_tt = div(K grad u), K = (1 + a prod_d sin(2 pi x_d))^2 (a = 0.5 by default), u0 = Gaussian
 //     bump, u_t(0) = 0:
@@ -70,6 +78,7 @@
 #include "OperatorMatrix1D.h"
 #include "Timer.h"
 
+#include <algorithm>
 #include <chrono>
 #include <cmath>
 #include <cstdio>
@@ -378,6 +387,8 @@ int run_burgers_adapt(int argc, char** argv) {
     const double cfl = std::atof(argv[8]);
     const double umax = std::atof(argv[9]);
     const int steps = std::atoi(argv[10]);
+    const bool timing = argc > 11 && std::string(argv[11]) == "time";
+    const double t_end = argc > 12 ? std::atof(argv[12]) : 0.0;
     const int k = 2;
     set_statics(dim, k);
     Hash hash;
@@ -404,7 +415,7 @@ int run_burgers_adapt(int argc, char** argv) {
     }
     dg.init_separable_scalar_sum(funcs);
     std::printf("META dim=%d N=%d k=%d sparse=1 elements=%zu dof=%d\n", dim, NMAX, k, dg.dg.size(), dg.get_dof());
-    dump_elements("u_init", dg, 0);
+    if (!timing) dump_elements("u_init", dg, 0);
 
     auto flux = [](std::vector<double> u, int, int) -> double { return FluxFunction::burgers_flux_scalar(u[0]); };
     std::vector<std::vector<bool>> is_intp(1, std::vector<bool>(dim, true));
@@ -413,10 +424,13 @@ int run_burgers_adapt(int argc, char** argv) {
     const std::vector<double> lxf(dim, alpha);
     double t = 0.0;
     for (int step = 0; step < steps; ++step) {
+        if (t_end > 0.0 && t >= t_end) break;
+        const auto t0 = std::chrono::steady_clock::now();
         const std::vector<int> max_mesh = dg.max_mesh_level_vec();
         double sum_c_dx = 0.;
         for (int d = 0; d < dim; ++d) sum_c_dx += umax * std::pow(2., max_mesh[d]);
-        const double dt = cfl / sum_c_dx;
+        double dt = cfl / sum_c_dx;
+        if (t_end > 0.0) dt = std::min(dt, t_end - t);
         // LagrInterpolation and FastLagrIntp hold per-grid data: rebuild after adaptation
         auto rhs_eval = [&]() {
             LagrInterpolation interp(dg);
@@ -439,6 +453,7 @@ int run_burgers_adapt(int argc, char** argv) {
         }
         dg.refine();
         dg.copy_predict_to_ucoe();
+        const int stage_dof = dg.get_dof();
         {
             RK3SSP ode(dg, dt);
             ode.init();
@@ -452,7 +467,20 @@ int run_burgers_adapt(int argc, char** argv) {
         }
         dg.coarsen();
         t += dt;
-        std::printf("STEP %d dt=%.17g elements=%zu\n", step, dt, dg.dg.size());
+        if (timing) {
+            const double sec = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+            std::printf("TSTEP %d %.9g %d %zu\n", step, sec, stage_dof, dg.dg.size());
+            std::fflush(stdout);
+            continue;
+        }
+        int maxsum = 0;
+        for (auto& it : dg.dg) {
+            int s = 0;
+            for (int d = 0; d < dim; ++d) s += it.second.level[d];
+            maxsum = std::max(maxsum, s);
+        }
+        std::printf("STEP %d dt=%.17g elements=%zu maxlevsum=%d%s\n", step, dt, dg.dg.size(), maxsum,
+                    (dim == 3 && maxsum >= 23) ? " HASH_OVERFLOW" : "");
         char nm[32];
         std::snprintf(nm, sizeof nm, "u_step%d", step);
         dump_elements(nm, dg, 0);

@@ -89,6 +89,34 @@ BURGERS_ADAPT_CASES = [
 ]
 
 
+# (name, dim, n_init, nmax, eps, eta, alpha, cfl, umax, steps, snapshot steps): the adaptive Burgers
+# time loop at full length -- the 3D configuration of the benchmark (start level 3, max level 8,
+# refine 1e-5, coarsen 1e-6, LxF alpha 0.825, CFL 0.1, 36 steps of 1/720 to T = 0.05).  The element
+# set and three checksums of the coefficients are kept after every step, the coefficients themselves
+# after the snapshot steps (0 = after the adaptive initialisation).
+BURGERS_ADAPT_LONG_CASES = [
+    ("burgers_adapt3d_config3", 3, 3, 8, 1e-5, 1e-6, 0.825, 0.1, 0.75, 36, [0, 1, 2, 9, 18, 27, 36]),
+]
+
+
+def checksum_weights(level: np.ndarray, suppt: np.ndarray, nb: int) -> np.ndarray:
+    """Weights of the position-dependent checksum sum_e,i w(e, i) u[e, i]: a function of the
+    element's level and support index and of the coefficient index only, so it does not depend on
+    the order in which a run lists its elements."""
+    dim = level.shape[1]
+    h = np.zeros(len(level), np.int64)
+    for d in range(dim):
+        h = h * 131 + level[:, d].astype(np.int64) * 17 + suppt[:, d].astype(np.int64) * 5 + d
+    w = (h[:, None] * 7 + np.arange(nb)[None, :] * 31) % 97
+    return 0.5 + w / 97.0
+
+
+def checksums(level: np.ndarray, suppt: np.ndarray, u: np.ndarray) -> np.ndarray:
+    """[sum of squares, max |u|, weighted sum, sum of |weight * u|] of a coefficient field."""
+    w = checksum_weights(level, suppt, u.shape[1])
+    return np.array([float((u * u).sum()), float(np.abs(u).max()), float((w * u).sum()), float(np.abs(w * u).sum())])
+
+
 # (name, dim, N, sigma, steps, dt): wave equation with interpolated K grad u, IPDG, RK4ODE2nd
 WAVE_CASES = [
     ("wave2d_n4", 2, 4, 10.0, 2, 0.001),
@@ -142,13 +170,41 @@ def intp_cases(manifest):
         print(name, r["meta"])
 
 
+def burgers_adapt_long(manifest):
+    for name, dim, n0, nmax, eps, eta, alpha, cfl, umax, steps, snaps in BURGERS_ADAPT_LONG_CASES:
+        res = subprocess.run([HARNESS, "burgers_adapt"] + [str(a) for a in (dim, n0, nmax, repr(eps), repr(eta),
+                                                                             repr(alpha), repr(cfl), repr(umax), steps)],
+                             check=True, capture_output=True, text=True)
+        r = parse_harness(res.stdout)
+        assert "HASH_OVERFLOW" not in res.stdout, "the reference's int32 element hash overflowed"
+        maxlevsum = max(int(ln.split("maxlevsum=")[1].split()[0]) for ln in res.stdout.splitlines()
+                        if ln.startswith("STEP"))
+        dts = [float(ln.split("dt=")[1].split()[0]) for ln in res.stdout.splitlines() if ln.startswith("STEP")]
+        arrs = {"dt": np.array(dts)}
+        sums = []
+        for i, key in enumerate(["u_init"] + [f"u_step{s}" for s in range(steps)]):
+            lv, sp, u = split_elements(r[key], dim)
+            arrs[f"level_{i}"], arrs[f"suppt_{i}"] = lv.astype(np.int16), sp.astype(np.int16)
+            sums.append(checksums(lv, sp, u))
+            if i in snaps:
+                arrs[f"u_{i}"] = u
+        arrs["checksums"] = np.array(sums)
+        np.savez_compressed(os.path.join(HERE, name + ".npz"), **arrs)
+        manifest[name] = dict(kind="burgers_adapt_long", dim=dim, n_init=n0, nmax=nmax, eps=eps, eta=eta,
+                              alpha=alpha, cfl=cfl, umax=umax, steps=steps, snapshots=snaps,
+                              max_level_sum=maxlevsum, t_end=float(np.sum(dts)),
+                              elements=[int(len(arrs[f"level_{i}"])) for i in range(steps + 1)])
+        print(name, r["meta"], "max level sum", maxlevsum)
+
+
 def main():
     if not os.path.exists(HARNESS):
         sys.exit("build the reference first: make -C oracle ref")
-    if sys.argv[1:] == ["intp"]:  # only the interpolation-init cases, merged into the manifest
+    only = {"intp": intp_cases, "burgers_adapt_long": burgers_adapt_long}
+    if len(sys.argv) == 2 and sys.argv[1] in only:  # one group of cases, merged into the manifest
         path = os.path.join(HERE, "manifest.json")
         manifest = json.load(open(path))
-        intp_cases(manifest)
+        only[sys.argv[1]](manifest)
         with open(path, "w") as f:
             json.dump(manifest, f, indent=1)
         return
@@ -189,6 +245,7 @@ def main():
         manifest[name] = dict(kind="burgers_adapt", dim=dim, n_init=n0, nmax=nmax, eps=eps, eta=eta, alpha=alpha,
                               cfl=cfl, umax=umax, steps=steps)
         print(name, r["meta"])
+    burgers_adapt_long(manifest)
     for name, dim, N, sigma, steps, dt in WAVE_CASES:
         r = run(["wave", dim, N, repr(sigma), steps, repr(dt)])
         lv, sp, u0 = split_elements(r["u0"], dim)

@@ -41,6 +41,44 @@ def test_adaptive_burgers_matches_reference(ctx, name):
     g.close()
 
 
+LONG = [n for n, m in manifest().items() if m["kind"] == "burgers_adapt_long"]
+
+
+@pytest.mark.parametrize("name", LONG)
+def test_adaptive_burgers_full_run_matches_reference(ctx, name):
+    """The benchmark's 3D configuration over its whole length (36 steps to T = 0.05): after the
+    adaptive initialisation and after every step the element set equals the reference's; the
+    coefficients agree to 1e-12 relative at the snapshot steps, and every step's checksums (sum of
+    squares, max |u|, a position-weighted sum) agree to 1e-12 relative."""
+    from golden.make_golden import checksums
+    m = manifest()[name]
+    z = golden(name)
+    dim = m["dim"]
+    g = amdg.Grid(ctx, dim, m["nmax"], 2, level_init=m["n_init"])
+    g.init_separable_adaptive(O.burgers_ic_terms(dim), m["eps"])
+    op = amdg.BurgersOperator(g, m["alpha"])
+    for i in range(m["steps"] + 1):
+        if i > 0:
+            dt = op.adaptive_step(m["cfl"], m["umax"], m["eps"], m["eta"], amdg.FP64)
+            assert dt == z["dt"][i - 1]
+            ctx.synchronize()
+        lv, sp = g.elements()
+        keys = O.arrays_to_keys(lv, sp)
+        ref_keys = O.arrays_to_keys(z[f"level_{i}"], z[f"suppt_{i}"])
+        assert set(keys) == set(ref_keys), f"element set differs at step {i}"
+        u = g.coefficients().reshape(len(keys), -1)
+        cs, ref_cs = checksums(lv, sp, u), z["checksums"][i]
+        assert abs(cs[0] - ref_cs[0]) <= 1e-12 * ref_cs[0], f"sum of squares differs at step {i}"
+        assert abs(cs[1] - ref_cs[1]) <= 1e-12 * ref_cs[1], f"max |u| differs at step {i}"
+        assert abs(cs[2] - ref_cs[2]) <= 1e-12 * ref_cs[3], f"weighted sum differs at step {i}"
+        if f"u_{i}" in z:
+            pos = {k: j for j, k in enumerate(ref_keys)}
+            perm = np.array([pos[k] for k in keys])
+            assert rel_err(u, z[f"u_{i}"][perm]) < 1e-12, f"coefficients differ at step {i}"
+    op.close()
+    g.close()
+
+
 def test_refine_coarsen_round_trip_and_version(ctx):
     g = amdg.Grid(ctx, 2, 6, 2, level_init=3)
     g.init_separable(O.burgers_ic_terms(2))

@@ -159,6 +159,32 @@ def test_adaptive_burgers_matches_reference(name):
         assert rel_err(u, z[f"u_{i}"][perm]) < 1e-12
 
 
+LONG = [n for n, m in manifest().items() if m["kind"] == "burgers_adapt_long"]
+
+
+@pytest.mark.parametrize("name", LONG)
+def test_adaptive_burgers_long_fixture_first_steps(name):
+    """The oracle against the first two steps of the full-length 3D adaptive Burgers fixture
+    (the whole run is checked on the GPU)."""
+    from golden.make_golden import checksums
+    m = manifest()[name]
+    z = golden(name)
+    dim = m["dim"]
+    hist = O.burgers_adaptive_run(dim, m["n_init"], m["nmax"], m["eps"], m["eta"], m["alpha"], m["cfl"], m["umax"], 2)
+    for i, (keys, u, dt) in enumerate(hist):
+        ref_keys = O.arrays_to_keys(z[f"level_{i}"], z[f"suppt_{i}"])
+        assert set(keys) == set(ref_keys)
+        if dt is not None:
+            assert dt == z["dt"][i - 1]
+        lv, sp = O.keys_to_arrays(keys, dim)
+        cs, ref_cs = checksums(lv, sp, u), z["checksums"][i]
+        assert abs(cs[0] - ref_cs[0]) <= 1e-12 * ref_cs[0]
+        assert abs(cs[2] - ref_cs[2]) <= 1e-12 * ref_cs[3]
+        pos = {k: j for j, k in enumerate(ref_keys)}
+        perm = np.array([pos[k] for k in keys])
+        assert rel_err(u, z[f"u_{i}"][perm]) < 1e-12
+
+
 def test_fast_transforms_equal_direct_sums_on_sparse_grids():
     """On a sparse grid the reference's L/U partial sums equal the direct sums
     over element pairs (an independent check of both formulations)."""
