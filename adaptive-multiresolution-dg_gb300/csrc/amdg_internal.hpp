@@ -249,6 +249,7 @@ struct amdg_context {
     void* stream = nullptr;        // cudaStream_t in use
     void* own_stream = nullptr;    // stream created by the context
     int64_t launches = 0;
+    int adapt_mode = 0;            // AMDG_ADAPT_DEVICE or AMDG_ADAPT_HOST (amdg_context_set_adapt_mode)
     // host phase profile (amdg_context_profile): wall seconds and calls per phase
     bool profile = false;
     double phase_sec[AMDG_PHASE_COUNT] = {0};
@@ -270,8 +271,45 @@ private:
 };
 }  // namespace amdg
 
+namespace amdg {
+// Device side of the element set (adapt_device.cu): the sorted packed keys, an open-addressing
+// key -> element hash, and the grow-only work arrays of the device refine / coarsen.  Plain
+// pointers so host translation units can hold it.
+struct GridDevice {
+    uint64_t* key = nullptr;         // sorted packed keys of the current element set
+    uint64_t* key_alt = nullptr;     // the next element set is assembled here, then swapped in
+    int64_t key_cap = 0;
+    unsigned long long* hkey = nullptr;  // hash slots (all bits set: empty)
+    int32_t* hval = nullptr;         // element index of the slot's key (-1: a key added by refinement)
+    int64_t hcap = 0;                // slots (a power of two)
+    int hbits = 0;
+    int64_t hash_version = -1;       // element set the hash holds
+    uint64_t* newk = nullptr;        // keys added by a refinement
+    int64_t new_cap = 0;
+    uint8_t* flag = nullptr;         // per element: refined / removed / forced
+    uint8_t* force = nullptr;
+    int32_t* pos = nullptr;          // exclusive scan of the kept elements (coarsen)
+    int64_t flag_cap = 0;
+    uint64_t* missed = nullptr;      // learned steps: leaves the criterion found above eps
+    int64_t missed_cap = 0, n_missed = 0;
+    void* stats = nullptr;           // device AdaptStats
+    void* host_stats = nullptr;      // pinned host copy
+    void* temp = nullptr;            // sort / scan scratch
+    size_t temp_bytes = 0;
+};
+}  // namespace amdg
+
 struct amdg_grid {
     int64_t version = 0;             // bumped whenever the element set changes
+    // element-set statistics kept with every change: largest level and sum of levels per
+    // dimension, largest level sum of an element (time step, coarsening passes, list bounds)
+    int lev_max[amdg::kMaxDim] = {0};
+    int64_t lev_sum[amdg::kMaxDim] = {0};
+    int levsum_max = 0;
+    // the device holds the element set (dev.key); after a device-side refine / coarsen the host
+    // mirror `host` keeps only num_elements current until grid_ensure_host refreshes it
+    bool host_stale = false;
+    amdg::GridDevice dev;
     int64_t capacity = 0;            // elements the device arrays can hold
     amdg_context* ctx = nullptr;
     int device = 0;                  // kept so destroy never dereferences ctx
@@ -292,6 +330,13 @@ struct amdg_grid {
     int64_t map_capacity = 0;
     double* d_norms = nullptr;
     int64_t norms_capacity = 0;
+    // Element::ucoe_alpt_predict, remapped with u (new elements zero); Element::rhs, zeroed
+    // when the element set changes
+    double* d_pred = nullptr;
+    double* d_pred_spare = nullptr;
+    int64_t pred_capacity = 0, pred_spare_capacity = 0;
+    double* d_rhs = nullptr;
+    int64_t rhs_capacity = 0, rhs_version = -1;
     // second field v = u_t of second-order-in-time problems (Element::ucoe_ut), remapped with u
     double* d_v = nullptr;           // v_capacity elements, null until set
     double* d_v_spare = nullptr;
@@ -363,6 +408,9 @@ struct amdg_burgers_op {
     std::vector<amdg::PartialSum> terms;
     amdg::PartialSum* d_terms = nullptr;
     int n_pv_terms = 0;
+    int grp_first[3] = {0, 0, 0}, grp_count[3] = {0, 0, 0};  // Burgers: volume, interface, penalty terms
+    int64_t interp_version = -1;     // element set of the flux coefficients amdg_lagr_interpolate kept
+    int interp_prec = -1;            // ... and their arithmetic
     int chunk = 1;  // terms per launch
     // work buffers sized for FP64: E x p1^dim doubles each, the sweep buffers and
     // term slices chunk times that
@@ -371,6 +419,10 @@ struct amdg_burgers_op {
     double *d_u1 = nullptr, *d_u2 = nullptr, *d_rhs64 = nullptr, *d_pred = nullptr;
     std::vector<double> host_norms;
     // one SSP-RK3 step captured as a CUDA graph, valid for (grid version, precision, dt)
+    int32_t* d_anc_order = nullptr;  // device copy of anc_order (the device-built ancestors)
+    int32_t* d_topo_cnt = nullptr;   // per (element, dimension) list lengths of the device build
+    unsigned long long* d_cls = nullptr;  // learned step: [refined by the network, unsure] (device)
+    unsigned long long* h_cls = nullptr;  // pinned host copy
     int32_t* d_pg = nullptr;         // [e][d][2] parent / grandparent (learned adaptivity features)
     float *d_feat = nullptr, *d_prob = nullptr;  // classifier features / probabilities
     int64_t feat_cap = 0;                        // elements the two hold
@@ -405,6 +457,57 @@ amdg_status grid_set_keys(amdg_grid* g, std::vector<uint64_t> keys, const std::v
 amdg_status grid_norms(amdg_grid* g, const double* d_u, std::vector<double>* norms, const double* d_u2 = nullptr);
 // coarsen the grid on the indicator ||u|| (+ ||u2|| when d_u2 is given)
 amdg_status grid_coarsen(amdg_grid* g, double eta, const double* d_u2, int64_t* num_elements);
+
+// ---- device-side element-set changes (adapt_device.cu) ------------------------
+// refresh the host mirror (keys, orders, key index) after device-side changes
+amdg_status grid_ensure_host(const amdg_grid* g);
+// lev_max / lev_sum / levsum_max of the host element set
+void grid_host_level_stats(amdg_grid* g);
+// upload the host element set's keys (after a host-side change)
+amdg_status grid_upload_keys(amdg_grid* g);
+// the key -> element hash of the current element set (rebuilt when the set changed)
+amdg_status grid_hash(amdg_grid* g);
+// element indicators into g->d_norms: ||u_e|| (+ ||u2_e|| when d_u2 is given), summed as
+// DGAdapt::indicator_norm does; a non-finite indicator is reported by the next refine / coarsen
+amdg_status grid_device_norms(amdg_grid* g, const double* d_u, const double* d_u2);
+// DGAdapt::refine on the device: leaves with indicator > eps (g->d_norms), or those flagged in
+// d_force (device, one byte per element) when given, get all their children, holes are filled;
+// new elements start at zero.  refined (host, may be null): per old element, 1 if refined.
+// *added: elements added.  One stream synchronisation (the new element count).
+amdg_status grid_device_refine(amdg_grid* g, double eps, const uint8_t* d_force, int8_t* refined, int64_t* added);
+// DGAdapt::coarsen on the device on the indicators in g->d_norms.  With missed_eps > 0 the leaves
+// of the coarsened set whose indicator exceeds it are recorded as missed refinements
+// (g->dev.missed).  One stream synchronisation.
+amdg_status grid_device_coarsen(amdg_grid* g, double eta, double missed_eps, int64_t* removed);
+// 1 in d_force (device) for every element whose key is a recorded missed refinement
+amdg_status grid_mark_missed(amdg_grid* g, uint8_t* d_force);
+// the learned pre-adaptation flags into the grid's force buffer (*d_force): the classifier's
+// refine class where confident (d_prob: E x 3, may be null), the criterion on g->d_norms elsewhere;
+// d_counts[0] += refined by the classifier, d_counts[1] += unsure (device counters)
+amdg_status grid_learned_flags(amdg_grid* g, const float* d_prob, double tau, double eps, uint8_t** d_force,
+                               unsigned long long* d_counts);
+// device flag the neighbour-list kernels set (reported by the next refine / coarsen or check)
+int* grid_topology_error_flag(amdg_grid* g);
+// synchronise and report a neighbour-list or ancestor error of the last device build
+amdg_status grid_check_topology(amdg_grid* g);
+// the element-set change of a remap: grow the spare arrays for E_new elements and move u (and v)
+// through g->d_map (new -> old, -1 new element); bumps the version
+amdg_status grid_apply_remap(amdg_grid* g, int64_t E_new);
+// device neighbour lists of the fast transforms and surplus ancestors for the current element set
+struct DeviceTopoOut {
+    int32_t *vol_ptr, *vol_nbr, *vol_split, *flx_ptr, *flx_nbr, *flx_split, *anc;
+    int64_t vol_cap, flx_cap;        // pairs the nbr arrays hold
+    const int32_t* anc_order;        // device [n1][p1]
+    int p1;
+    int* err;                        // device flag: a surplus ancestor is missing / a list overflowed
+};
+// bounds on the number of (element, neighbour) pairs of the vol and flx lists over all dimensions
+void transform_topology_bounds(const amdg_grid* g, int64_t* vol_pairs, int64_t* flx_pairs);
+amdg_status device_transform_topology(amdg_grid* g, const DeviceTopoOut& out, int32_t* d_cnt, void* stream);
+// [e][d][2] parent / grandparent table on the device
+amdg_status device_parent_table(amdg_grid* g, int32_t* d_pg, void* stream);
+// the grid's Element::rhs vector (dof entries, zero after every element-set change)
+amdg_status grid_rhs(amdg_grid* g, double** d_rhs);
 }  // namespace amdg
 
 struct amdg_batch {

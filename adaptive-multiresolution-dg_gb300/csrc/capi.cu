@@ -115,6 +115,7 @@ namespace amdg {
 // coefficients of surviving elements over and zeroing new ones.
 amdg_status grid_set_keys(amdg_grid* g, std::vector<uint64_t> keys, const std::vector<uint8_t>* carry) {
     PhaseTimer timer(g->ctx, AMDG_PHASE_SET_KEYS);
+    if (amdg_status s = grid_ensure_host(g); s != AMDG_OK) return s;
     HostGrid ng;
     ng.sparse = g->host.sparse;
     grid_from_keys(g->host.dim, g->host.nmax, g->host.k, std::move(keys), &ng);
@@ -133,14 +134,6 @@ amdg_status grid_set_keys(amdg_grid* g, std::vector<uint64_t> keys, const std::v
     const int64_t E = ng.num_elements;
     const int64_t grown = E + E / 4 + 16;
     amdg_status s;
-    // remap into the spare coefficient array, then swap it in; buffers grow by a quarter
-    if (E > g->spare_capacity) {
-        cudaFree(g->d_u_spare);
-        g->d_u_spare = nullptr;
-        g->spare_capacity = 0;
-        if ((s = dev_alloc(&g->d_u_spare, size_t(grown) * g->block)) != AMDG_OK) return s;
-        g->spare_capacity = grown;
-    }
     if (E > g->map_capacity) {
         cudaFree(g->d_map);
         g->d_map = nullptr;
@@ -156,29 +149,12 @@ amdg_status grid_set_keys(amdg_grid* g, std::vector<uint64_t> keys, const std::v
         g->order_capacity = grown;
     }
     if (E > 0) AMDG_CK(cudaMemcpyAsync(g->d_map, map.data(), size_t(E) * sizeof(int32_t), cudaMemcpyHostToDevice, st));
-    AMDG_CK(launch_remap(g->d_u, g->d_map, g->block, E, g->d_u_spare, st));
-    g->ctx->launches++;
-    if (g->d_v) {  // the velocity field follows the element set (into its own spare, then swapped)
-        if (E > g->v_spare_capacity) {
-            cudaFree(g->d_v_spare);
-            g->d_v_spare = nullptr;
-            g->v_spare_capacity = 0;
-            if ((s = dev_alloc(&g->d_v_spare, size_t(grown) * g->block)) != AMDG_OK) return s;
-            g->v_spare_capacity = grown;
-        }
-        AMDG_CK(launch_remap(g->d_v, g->d_map, g->block, E, g->d_v_spare, st));
-        g->ctx->launches++;
-        std::swap(g->d_v, g->d_v_spare);
-        std::swap(g->v_capacity, g->v_spare_capacity);
-    }
-    std::swap(g->d_u, g->d_u_spare);
-    std::swap(g->capacity, g->spare_capacity);
+    // u (and u_t, the prediction) through the map into spare arrays, swapped in; new elements zero
+    if ((s = grid_apply_remap(g, E)) != AMDG_OK) return s;
     AMDG_CK(cudaMemcpyAsync(g->d_order, ng.order.data(), ng.order.size() * sizeof(int32_t), cudaMemcpyHostToDevice, st));
     AMDG_CK(cudaStreamSynchronize(st));  // the host map and orders are released on return
     g->host = std::move(ng);
-    g->dof = g->host.num_elements * g->block;
-    g->version++;
-    return AMDG_OK;
+    return grid_upload_keys(g);
 }
 
 // indicator norms of a device coefficient vector on the grid's current element set
@@ -215,6 +191,14 @@ amdg_status grid_norms(amdg_grid* g, const double* d_u, std::vector<double>* nor
 amdg_status grid_coarsen(amdg_grid* g, double eta, const double* d_u2, int64_t* num_elements) {
     amdg_status s = set_device(g->ctx);
     if (s != AMDG_OK) return s;
+    if (g->ctx->adapt_mode == AMDG_ADAPT_DEVICE) {
+        PhaseTimer timer(g->ctx, AMDG_PHASE_ADAPT_DEVICE);
+        if ((s = grid_device_norms(g, g->d_u, d_u2)) != AMDG_OK || (s = grid_device_coarsen(g, eta, 0.0, nullptr)) != AMDG_OK)
+            return s;
+        if (num_elements) *num_elements = g->host.num_elements;
+        return AMDG_OK;
+    }
+    if ((s = grid_ensure_host(g)) != AMDG_OK) return s;
     std::vector<double> norms;
     if ((s = grid_norms(g, g->d_u, &norms, d_u2)) != AMDG_OK) return s;
     std::vector<uint64_t> keys;
@@ -394,6 +378,7 @@ amdg_status linear_sync(amdg_linear_op* op) {
     Oper1D op1d;
     build_oper1d(b, &op1d, false);
     LinearTopology topo;
+    if (amdg_status s = grid_ensure_host(g); s != AMDG_OK) return s;
     build_linear_topology(g->host, op1d, op->coef.data(), &topo);
     cudaFree(op->d_row_ptr); cudaFree(op->d_src); cudaFree(op->d_blk); cudaFree(op->d_blocks64); cudaFree(op->d_blocks32);
     cudaFree(op->d_pairs); cudaFree(op->d_blocks64p); cudaFree(op->d_blocks32p);
@@ -526,6 +511,12 @@ amdg_status amdg_context_launch_count(amdg_context* ctx, int64_t* count) {
     return AMDG_OK;
 }
 
+amdg_status amdg_context_set_adapt_mode(amdg_context* ctx, int mode) {
+    AMDG_REQUIRE(ctx && (mode == AMDG_ADAPT_DEVICE || mode == AMDG_ADAPT_HOST), AMDG_ERR_ARG, "bad adapt mode");
+    ctx->adapt_mode = mode;
+    return AMDG_OK;
+}
+
 amdg_status amdg_context_profile(amdg_context* ctx, int enable) {
     AMDG_REQUIRE(ctx, AMDG_ERR_ARG, "null context");
     ctx->profile = enable != 0;
@@ -613,6 +604,10 @@ amdg_status amdg_grid_create_ex(amdg_context* ctx, int dim, int level_init, int 
         return s;
     }
     g->scratch_bytes = size_t(reduce_partials_needed()) * sizeof(double);
+    if ((s = grid_upload_keys(g)) != AMDG_OK) {
+        amdg_grid_destroy(g);
+        return s;
+    }
     cudaError_t e = cudaMemsetAsync(g->d_u, 0, size_t(g->dof) * sizeof(double), st);
     if (e == cudaSuccess) e = cudaStreamSynchronize(st);
     if (e != cudaSuccess) {
@@ -639,6 +634,19 @@ amdg_status amdg_grid_destroy(amdg_grid* g) {
     cudaFree(g->d_norms);
     cudaFree(g->d_v);
     cudaFree(g->d_v_spare);
+    GridDevice& d = g->dev;
+    cudaFree(d.key);
+    cudaFree(d.key_alt);
+    cudaFree(d.hkey);
+    cudaFree(d.hval);
+    cudaFree(d.newk);
+    cudaFree(d.flag);
+    cudaFree(d.force);
+    cudaFree(d.pos);
+    cudaFree(d.missed);
+    cudaFree(d.stats);
+    cudaFreeHost(d.host_stats);
+    cudaFree(d.temp);
     delete g;
     return AMDG_OK;
 }
@@ -652,6 +660,7 @@ amdg_status amdg_grid_size(const amdg_grid* g, int64_t* num_elements, int64_t* d
 
 amdg_status amdg_grid_elements(const amdg_grid* g, int32_t* level, int32_t* suppt) {
     AMDG_REQUIRE(g && level && suppt, AMDG_ERR_ARG, "null argument");
+    if (amdg_status s = grid_ensure_host(g); s != AMDG_OK) return s;
     const size_t n = g->host.order.size();
     for (size_t i = 0; i < n; ++i) {
         int lv, j;
@@ -664,13 +673,7 @@ amdg_status amdg_grid_elements(const amdg_grid* g, int32_t* level, int32_t* supp
 
 amdg_status amdg_grid_max_mesh_level(const amdg_grid* g, int32_t* levels) {
     AMDG_REQUIRE(g && levels, AMDG_ERR_ARG, "null argument");
-    const int dim = g->host.dim;
-    for (int d = 0; d < dim; ++d) levels[d] = 0;
-    for (int64_t e = 0; e < g->host.num_elements; ++e)
-        for (int d = 0; d < dim; ++d) {
-            const int lv = level_of_order(g->host.order[size_t(e) * dim + d]);
-            if (lv > levels[d]) levels[d] = lv;
-        }
+    for (int d = 0; d < g->host.dim; ++d) levels[d] = g->lev_max[d];
     return AMDG_OK;
 }
 
@@ -739,6 +742,7 @@ static amdg_status init_separable_adaptive(amdg_grid* g, int nterms, const Fn1d&
     // until nothing changes (DGAdapt::refine_init_separable_scalar_sum)
     // norms depend only on the element, so each is computed once; the element
     // set is refined on the host and the device arrays are rebuilt once at the end
+    if ((s = grid_ensure_host(g)) != AMDG_OK) return s;
     HostGrid work = g->host;
     std::unordered_map<uint64_t, double> cache;
     for (;;) {
@@ -784,6 +788,15 @@ amdg_status amdg_grid_refine(amdg_grid* g, const double* d_indicator, double eps
     AMDG_REQUIRE(g, AMDG_ERR_ARG, "grid is null");
     amdg_status s = set_device(g->ctx);
     if (s != AMDG_OK) return s;
+    if (g->ctx->adapt_mode == AMDG_ADAPT_DEVICE) {
+        PhaseTimer timer(g->ctx, AMDG_PHASE_ADAPT_DEVICE);
+        if ((s = grid_device_norms(g, d_indicator ? d_indicator : g->d_u, nullptr)) != AMDG_OK ||
+            (s = grid_device_refine(g, eps, nullptr, nullptr, nullptr)) != AMDG_OK)
+            return s;
+        if (num_elements) *num_elements = g->host.num_elements;
+        return AMDG_OK;
+    }
+    if ((s = grid_ensure_host(g)) != AMDG_OK) return s;
     std::vector<double> norms;
     if ((s = grid_norms(g, d_indicator ? d_indicator : g->d_u, &norms)) != AMDG_OK) return s;
     std::vector<uint64_t> keys;

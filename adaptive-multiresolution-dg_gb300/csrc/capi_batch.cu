@@ -95,7 +95,10 @@ amdg_status batch_step(amdg_batch* b, amdg_precision prec, cudaStream_t st) {
 amdg_status batch_build(amdg_batch* b) {
     const int n = b->nsolves;
     std::vector<const HostGrid*> hg(n);
-    for (int i = 0; i < n; ++i) hg[i] = &b->grids[i]->host;
+    for (int i = 0; i < n; ++i) {
+        if (amdg_status s = grid_ensure_host(b->grids[i]); s != AMDG_OK) return s;
+        hg[i] = &b->grids[i]->host;
+    }
     if (b->tables.rel1d.empty()) {
         Basis1D basis{b->k, b->nmax};
         Oper1D op;
@@ -209,6 +212,7 @@ amdg_status amdg_batch_create(amdg_context* ctx, int n, amdg_grid* const* grids,
         AMDG_REQUIRE(grids[i] && grids[i]->ctx == ctx, AMDG_ERR_ARG, "every grid must belong to the context");
         AMDG_REQUIRE(grids[i]->host.dim == dim && grids[i]->host.nmax == nmax && grids[i]->host.k == k, AMDG_ERR_ARG,
                      "grids must share dim, nmax and k");
+        if (amdg_status s = grid_ensure_host(grids[i]); s != AMDG_OK) return s;
         hg[i] = &grids[i]->host;
     }
     for (int i = 0; i < n * dim; ++i) AMDG_REQUIRE(std::isfinite(coef[i]), AMDG_ERR_ARG, "non-finite velocity");
@@ -360,6 +364,7 @@ amdg_status amdg_batch_adapt(amdg_batch* b, amdg_mlp* mlp, double eps, double et
     const int64_t T = b->num_elements;
     std::vector<const HostGrid*> hg(n);
     for (int i = 0; i < n; ++i) {
+        if (amdg_status s = grid_ensure_host(b->grids[i]); s != AMDG_OK) return s;
         hg[i] = &b->grids[i]->host;
         AMDG_REQUIRE(hg[i]->num_elements == b->elem_offset[i + 1] - b->elem_offset[i], AMDG_ERR_STATE,
                      "a grid changed since the batch was built");

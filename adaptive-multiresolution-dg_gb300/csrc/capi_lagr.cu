@@ -136,12 +136,13 @@ void push_penalty(amdg_burgers_op* op, int d, double coef) {
 // Burgers:
 //  - point values: the 2^(dim-1) partial sums of the schedule with the
 //    Alpert-at-Lagrange-point matrix in every dimension (FastLagrIntp::eval_up_Lagr);
-//  - right-hand side, in the order the reference adds them: for each dimension
-//    d the volume partial sums (u_vx in d, u_v elsewhere, vol sets), the
+//  - right-hand side, in the order the reference adds them: the volume partial
+//    sums (u_vx in d, u_v elsewhere, vol sets) for every dimension d, then the
 //    interface partial sums (0.5 (ulft+urgt)_vjp in d on the flx sets, u_v
-//    elsewhere) (HyperbolicLagrRHS::rhs_vol_scalar / rhs_flx_intp_scalar,
-//    FastMultiplyLU.cpp:1125-1189), then the LxF penalty -alpha_d/2 ujp_vjp
-//    along d (HyperbolicAlptRHS::rhs_flx_penalty_scalar, :1269-1276).
+//    elsewhere) for every d (HyperbolicLagrRHS::rhs_vol_scalar /
+//    rhs_flx_intp_scalar, FastMultiplyLU.cpp:1125-1189), then the LxF penalty
+//    -alpha_d/2 ujp_vjp along every d (HyperbolicAlptRHS::rhs_flx_penalty_scalar,
+//    :1269-1276).
 // Wave (03_wave_06_var_coeff_adapt.cpp:154-245):
 //  - point values: group d < dim is u_{x_d} (the Alpert derivative at the
 //    points along d, FastLagrIntp::eval_der_up_Lagr), group dim is u;
@@ -165,15 +166,22 @@ void build_terms(amdg_burgers_op* op) {
         for (int t = 0; t < dim; ++t) { mat[t] = kMatA2P; flx[t] = 0; }
         push_psums(op, mat, flx, 1.0, 0);
         op->n_pv_terms = int(op->terms.size());
-        for (int d = 0; d < dim; ++d) {
-            for (int term = 0; term < 2; ++term) {
+        // the three groups in the order the reference's driver calls them: rhs_vol_scalar (every
+        // d), rhs_flx_intp_scalar (every d), rhs_flx_penalty_scalar (every d)
+        for (int term = 0; term < 3; ++term) {
+            op->grp_first[term] = int(op->terms.size());
+            for (int d = 0; d < dim; ++d) {
+                if (term == 2) {
+                    push_penalty(op, d, -op->alpha[d] / 2.0);
+                    continue;
+                }
                 for (int t = 0; t < dim; ++t) {
                     mat[t] = (t == d) ? (term == 0 ? kMatLVX : kMatLFLX) : kMatLV;
                     flx[t] = (term == 1 && t == d) ? 1 : 0;
                 }
                 push_psums(op, mat, flx, term == 0 ? 1.0 : 0.5, 0);
             }
-            push_penalty(op, d, -op->alpha[d] / 2.0);
+            op->grp_count[term] = int(op->terms.size()) - op->grp_first[term];
         }
         return;
     }
@@ -200,7 +208,7 @@ void build_terms(amdg_burgers_op* op) {
 // IPDG coefficient -sigma/dx, dx = 2^-(finest level of the grid) (BilinearForm.cpp:922-923)
 double wave_penalty_coef(const amdg_burgers_op* op) {
     int maxl = 0;
-    for (int32_t o : op->grid->host.order) maxl = std::max(maxl, level_of_order(o));
+    for (int d = 0; d < op->grid->host.dim; ++d) maxl = std::max(maxl, op->grid->lev_max[d]);
     return -op->sigma / (1.0 / std::pow(2.0, maxl));
 }
 
@@ -336,14 +344,15 @@ amdg_status eval_surplus(amdg_burgers_op* op, const T* in, To* out, cudaStream_t
 // stage update
 template <typename T>
 amdg_status eval_term_range(amdg_burgers_op* op, const Mats<T>& m, int first, int total, const T* const* src, int nsrc,
-                            const T* u, double* rhs, StageOut so, cudaStream_t st) {
+                            const T* u, double* rhs, StageOut so, cudaStream_t st, bool accumulate = false) {
     const int np = op->grid->host.k + 1;
     T* slots = static_cast<T*>(op->w_slots);
     for (int c0 = 0; c0 < total; c0 += op->chunk) {
         const int cnt = std::min(op->chunk, total - c0);
         if (amdg_status r = run_terms<T>(op, m, first + c0, cnt, op->p1, np, src, nsrc, u, slots, st); r != AMDG_OK)
             return r;
-        AMDG_CK(launch_reduce_rhs<T>(slots, cnt, op->grid->dof, c0 == 0 ? 1 : 0, c0 + cnt == total ? 1 : 0, rhs, so, st));
+        AMDG_CK(launch_reduce_rhs<T>(slots, cnt, op->grid->dof, (c0 == 0 && !accumulate) ? 1 : 0,
+                                     c0 + cnt == total ? 1 : 0, rhs, so, st));
         op->grid->ctx->launches++;
     }
     return AMDG_OK;
@@ -488,6 +497,58 @@ amdg_status upload_grow(amdg_burgers_op* op, T** p, const std::vector<T>& host, 
     return AMDG_OK;
 }
 
+// Grow-only device array of the operator with room for `bytes` (contents not kept).
+template <typename T>
+amdg_status reserve_grow(amdg_burgers_op* op, T** p, size_t bytes) {
+    size_t& cap = op->dev_cap[static_cast<const void*>(p)];
+    if (bytes <= cap && *p) return AMDG_OK;
+    cudaFree(*p);
+    *p = nullptr;
+    cap = 0;
+    const size_t want = bytes + bytes / 4 + 64;
+    if (cudaMalloc(reinterpret_cast<void**>(p), want) != cudaSuccess) {
+        *p = nullptr;
+        return fail(AMDG_ERR_NOMEM, "cudaMalloc failed (neighbour lists)");
+    }
+    cap = want;
+    return AMDG_OK;
+}
+
+// The neighbour lists and surplus ancestors built on the device from the grid's keys
+// (csrc/adapt_device.cu), into arrays sized by the bounds of the element set's level sums.
+amdg_status device_topology(amdg_burgers_op* op, cudaStream_t st) {
+    amdg_grid* g = op->grid;
+    const int64_t rows = g->host.num_elements * g->host.dim;
+    int64_t vb = 0, fb = 0;
+    transform_topology_bounds(g, &vb, &fb);
+    AMDG_REQUIRE(vb < (int64_t(1) << 31) && fb < (int64_t(1) << 31), AMDG_ERR_CAPACITY, "neighbour lists exceed 2^31 pairs");
+    amdg_status s;
+    if ((s = reserve_grow(op, &op->d_vol_ptr, size_t(rows + 1) * sizeof(int32_t))) != AMDG_OK ||
+        (s = reserve_grow(op, &op->d_flx_ptr, size_t(rows + 1) * sizeof(int32_t))) != AMDG_OK ||
+        (s = reserve_grow(op, &op->d_vol_split, size_t(rows + 1) * sizeof(int32_t))) != AMDG_OK ||
+        (s = reserve_grow(op, &op->d_flx_split, size_t(rows + 1) * sizeof(int32_t))) != AMDG_OK ||
+        (s = reserve_grow(op, &op->d_topo_cnt, size_t(2 * (rows + 1)) * sizeof(int32_t))) != AMDG_OK ||
+        (s = reserve_grow(op, &op->d_vol_nbr, size_t(2 * vb) * sizeof(int32_t))) != AMDG_OK ||
+        (s = reserve_grow(op, &op->d_flx_nbr, size_t(2 * fb) * sizeof(int32_t))) != AMDG_OK ||
+        (s = reserve_grow(op, &op->d_anc, size_t(rows) * op->p1 * sizeof(int32_t))) != AMDG_OK)
+        return s;
+    if (!op->d_anc_order) {
+        std::vector<int32_t> ao = op->anc_order;
+        if ((s = upload_vec(&op->d_anc_order, ao)) != AMDG_OK) return s;
+    }
+    int* err = grid_topology_error_flag(g);
+    AMDG_REQUIRE(err, AMDG_ERR_NOMEM, "device adaptivity statistics");
+    const size_t vcap = op->dev_cap[static_cast<const void*>(&op->d_vol_nbr)] / (2 * sizeof(int32_t));
+    const size_t fcap = op->dev_cap[static_cast<const void*>(&op->d_flx_nbr)] / (2 * sizeof(int32_t));
+    DeviceTopoOut out{op->d_vol_ptr, op->d_vol_nbr, op->d_vol_split, op->d_flx_ptr, op->d_flx_nbr, op->d_flx_split,
+                      op->d_anc, int64_t(vcap), int64_t(fcap), op->d_anc_order, op->p1, err};
+    if ((s = device_transform_topology(g, out, op->d_topo_cnt, st)) != AMDG_OK) return s;
+    // a set that came from the host may have holes: report them now (sets the device refine and
+    // coarsen produce are hole-free; their build errors surface at the next element-set change)
+    if (!g->host_stale) return grid_check_topology(g);
+    return AMDG_OK;
+}
+
 // (Re)build the neighbour lists and surplus ancestors for the grid's current
 // element set; device arrays and work buffers only grow.
 amdg_status burgers_sync(amdg_burgers_op* op) {
@@ -505,19 +566,27 @@ amdg_status burgers_sync(amdg_burgers_op* op) {
         t.anc_order = op->anc_order;
         t.p1 = op->p1;
     }
-    TransformTopology topo;
-    build_transform_topology(g->host, &topo);
-    std::vector<int32_t> anc;
-    if (!build_surplus_ancestors(g->host, t, &anc)) return fail(AMDG_ERR_STATE, "element set has a hole: a surplus ancestor is missing");
     amdg_status s;
-    if ((s = upload_grow(op, &op->d_vol_ptr, topo.vol_ptr, st)) != AMDG_OK ||
-        (s = upload_grow(op, &op->d_vol_nbr, topo.vol_nbr, st)) != AMDG_OK ||
-        (s = upload_grow(op, &op->d_flx_ptr, topo.flx_ptr, st)) != AMDG_OK ||
-        (s = upload_grow(op, &op->d_flx_nbr, topo.flx_nbr, st)) != AMDG_OK ||
-        (s = upload_grow(op, &op->d_anc, anc, st)) != AMDG_OK ||
-        (s = upload_grow(op, &op->d_vol_split, topo.vol_split, st)) != AMDG_OK ||
-        (s = upload_grow(op, &op->d_flx_split, topo.flx_split, st)) != AMDG_OK)
-        return s;
+    if (g->ctx->adapt_mode == AMDG_ADAPT_DEVICE) {
+        if ((s = device_topology(op, st)) != AMDG_OK) return s;
+    } else {
+        if ((s = grid_ensure_host(g)) != AMDG_OK) return s;
+        TransformTopology topo;
+        build_transform_topology(g->host, &topo);
+        std::vector<int32_t> anc;
+        if (!build_surplus_ancestors(g->host, t, &anc))
+            return fail(AMDG_ERR_STATE, "element set has a hole: a surplus ancestor is missing");
+        if ((s = upload_grow(op, &op->d_vol_ptr, topo.vol_ptr, st)) != AMDG_OK ||
+            (s = upload_grow(op, &op->d_vol_nbr, topo.vol_nbr, st)) != AMDG_OK ||
+            (s = upload_grow(op, &op->d_flx_ptr, topo.flx_ptr, st)) != AMDG_OK ||
+            (s = upload_grow(op, &op->d_flx_nbr, topo.flx_nbr, st)) != AMDG_OK ||
+            (s = upload_grow(op, &op->d_anc, anc, st)) != AMDG_OK ||
+            (s = upload_grow(op, &op->d_vol_split, topo.vol_split, st)) != AMDG_OK ||
+            (s = upload_grow(op, &op->d_flx_split, topo.flx_split, st)) != AMDG_OK)
+            return s;
+        // the host vectors above are released on return: wait for their copies
+        AMDG_CK(cudaStreamSynchronize(st));
+    }
     const int64_t E = g->host.num_elements;
     if (E > op->capacity) {
         const int64_t cap = E + E / 2 + 16;
@@ -555,12 +624,12 @@ amdg_status burgers_sync(amdg_burgers_op* op) {
         bool changed = false;
         for (PartialSum& p : op->terms)
             if (p.kind == 1 && p.coef != c) { p.coef = c; changed = true; }
-        if (changed)
+        if (changed) {  // only when the finest level changed
             AMDG_CK(cudaMemcpyAsync(op->d_terms, op->terms.data(), op->terms.size() * sizeof(PartialSum),
                                     cudaMemcpyHostToDevice, st));
+            AMDG_CK(cudaStreamSynchronize(st));
+        }
     }
-    // the host vectors above are released on return: wait for their copies
-    AMDG_CK(cudaStreamSynchronize(st));
     op->built_version = g->version;
     return AMDG_OK;
 }
@@ -572,10 +641,18 @@ amdg_status ensure_features(amdg_burgers_op* op, int64_t E, int F) {
     amdg_grid* g = op->grid;
     amdg_status s;
     if (op->pg_version != g->version) {
-        std::vector<int32_t> pg;
-        parent_table(g->host, &pg);
-        if ((s = upload_grow(op, &op->d_pg, pg, stream_of(op))) != AMDG_OK) return s;
-        AMDG_CK(cudaStreamSynchronize(stream_of(op)));  // pg is released on return
+        if (g->ctx->adapt_mode == AMDG_ADAPT_DEVICE) {
+            if ((s = reserve_grow(op, &op->d_pg, size_t(g->host.num_elements) * g->host.dim * 2 * sizeof(int32_t))) !=
+                    AMDG_OK ||
+                (s = device_parent_table(g, op->d_pg, stream_of(op))) != AMDG_OK)
+                return s;
+        } else {
+            if ((s = grid_ensure_host(g)) != AMDG_OK) return s;
+            std::vector<int32_t> pg;
+            parent_table(g->host, &pg);
+            if ((s = upload_grow(op, &op->d_pg, pg, stream_of(op))) != AMDG_OK) return s;
+            AMDG_CK(cudaStreamSynchronize(stream_of(op)));  // pg is released on return
+        }
         op->pg_version = g->version;
     }
     if (E > op->feat_cap) {
@@ -669,8 +746,10 @@ amdg_status amdg_burgers_destroy(amdg_burgers_op* op) {
                     op->d_u1, op->d_u2, op->d_rhs64, op->d_pred, op->d_vol_split, op->d_flx_split,
                     op->d_pg,
                     op->d_feat, op->d_prob, op->d_a2pd, op->d_ljv, op->d_pts, op->f_a2pd, op->f_ljv,
-                    op->w_fields, op->d_v1, op->d_su, op->d_sv, op->df_a2p, op->df_a2pd};
+                    op->w_fields, op->d_v1, op->d_su, op->d_sv, op->df_a2p, op->df_a2pd,
+                    op->d_anc_order, op->d_topo_cnt, op->d_cls};
     for (void* p : ptrs) cudaFree(p);
+    cudaFreeHost(op->h_cls);
     delete op;
     return AMDG_OK;
 }
@@ -682,6 +761,123 @@ amdg_status amdg_burgers_rhs(amdg_burgers_op* op, const double* d_u, double* d_r
     if (amdg_status rs = burgers_sync(op); rs != AMDG_OK) return rs;
     op->rhs_evaluations++;
     return eval_rhs(op, d_u, d_rhs, prec);
+}
+
+amdg_status amdg_burgers_work(amdg_burgers_op* op, double* flops, double* transform_pairs) {
+    AMDG_REQUIRE(op, AMDG_ERR_ARG, "null argument");
+    AMDG_CK(cudaSetDevice(op->device));
+    if (amdg_status rs = burgers_sync(op); rs != AMDG_OK) return rs;
+    amdg_grid* g = op->grid;
+    const int dim = g->host.dim, np = g->host.k + 1, p1 = op->p1;
+    const int64_t E = g->host.num_elements, rows = E * dim;
+    // neighbour counts per (dimension, vol/flx, L/full/U) summed over the elements
+    std::vector<int32_t> ptr[2], split[2];
+    const int32_t* dp[2] = {op->d_vol_ptr, op->d_flx_ptr};
+    const int32_t* ds[2] = {op->d_vol_split, op->d_flx_split};
+    for (int f = 0; f < 2; ++f) {
+        ptr[f].resize(size_t(rows + 1));
+        split[f].resize(size_t(std::max<int64_t>(rows, 1)));
+        AMDG_CK(cudaMemcpy(ptr[f].data(), dp[f], size_t(rows + 1) * sizeof(int32_t), cudaMemcpyDeviceToHost));
+        if (rows) AMDG_CK(cudaMemcpy(split[f].data(), ds[f], size_t(rows) * sizeof(int32_t), cudaMemcpyDeviceToHost));
+    }
+    double cnt[kMaxDim][2][3] = {};
+    for (int64_t r = 0; r < rows; ++r)
+        for (int f = 0; f < 2; ++f) {
+            const int t = int(r % dim);
+            cnt[t][f][0] += ptr[f][r + 1] - split[f][r];  // "L": finer neighbours
+            cnt[t][f][1] += ptr[f][r + 1] - ptr[f][r];
+            cnt[t][f][2] += split[f][r] - ptr[f][r];      // "U": coarser or equal
+        }
+    double fl = 0.0, pairs = 0.0;
+    for (size_t i = 0; i < op->terms.size(); ++i) {
+        const PartialSum& D = op->terms[i];
+        const bool pv = int(i) < op->n_pv_terms;
+        if (D.kind == 1) {  // the penalty: one full transform along dims[0] on the flx sets
+            const double c = cnt[D.dims[0]][1][1];
+            fl += 2.0 * np * ipow(np, dim) * c;
+            pairs += c;
+            continue;
+        }
+        const int n_in = pv ? np : p1, n_out = pv ? p1 : np;
+        for (int j = 0; j < dim; ++j) {
+            const double c = cnt[D.dims[j]][D.flx[j]][D.lu[j]];
+            fl += 2.0 * n_in * ipow(n_out, j + 1) * ipow(n_in, dim - j - 1) * c;
+            pairs += c;
+        }
+    }
+    // hierarchical surplus passes (one field for Burgers, dim + 1 for the wave operator)
+    fl += 2.0 * dim * double(E) * op->points * p1 * (op->kind == 1 ? dim + 1 : 1);
+    if (flops) *flops = fl;
+    if (transform_pairs) *transform_pairs = pairs;
+    return AMDG_OK;
+}
+
+amdg_status amdg_lagr_interpolate(amdg_burgers_op* op, amdg_precision prec) {
+    AMDG_REQUIRE(op && op->kind == 0, AMDG_ERR_ARG, "a Burgers operator is required");
+    AMDG_REQUIRE(prec == AMDG_PREC_FP64 || prec == AMDG_PREC_MIXED, AMDG_ERR_ARG, "bad precision");
+    AMDG_CK(cudaSetDevice(op->device));
+    if (amdg_status rs = burgers_sync(op); rs != AMDG_OK) return rs;
+    amdg_grid* g = op->grid;
+    cudaStream_t st = stream_of(op);
+    // point values (FP64, or double-float in mixed mode), the flux u^2/2 at the points, and its
+    // surpluses: FP64, or the FP32 coefficients the mixed back transforms read
+    double* fp = static_cast<double*>(op->w_a);
+    amdg_status r = prec == AMDG_PREC_FP64
+                        ? eval_point_values<double>(op, mats64(op), g->d_u, static_cast<double*>(op->w_up), fp, st)
+                        : eval_point_values_df(op, g->d_u, static_cast<double*>(op->w_up), fp, st);
+    if (r != AMDG_OK) return r;
+    r = prec == AMDG_PREC_FP64 ? eval_surplus<double, double>(op, fp, static_cast<double*>(op->w_fu), st)
+                               : eval_surplus<double, float>(op, fp, static_cast<float*>(op->w_fu), st);
+    if (r != AMDG_OK) return r;
+    op->interp_version = g->version;
+    op->interp_prec = prec;
+    return AMDG_OK;
+}
+
+amdg_status amdg_lagr_rhs_add(amdg_burgers_op* op, int group, const double* alpha, amdg_precision prec) {
+    AMDG_REQUIRE(op && op->kind == 0, AMDG_ERR_ARG, "a Burgers operator is required");
+    AMDG_REQUIRE(group >= AMDG_LAGR_RHS_VOL && group <= AMDG_LAGR_RHS_PENALTY, AMDG_ERR_ARG, "unknown term group");
+    AMDG_REQUIRE(prec == AMDG_PREC_FP64 || prec == AMDG_PREC_MIXED, AMDG_ERR_ARG, "bad precision");
+    AMDG_CK(cudaSetDevice(op->device));
+    if (amdg_status rs = burgers_sync(op); rs != AMDG_OK) return rs;
+    amdg_grid* g = op->grid;
+    cudaStream_t st = stream_of(op);
+    const int dim = g->host.dim;
+    if (group != AMDG_LAGR_RHS_PENALTY)
+        AMDG_REQUIRE(op->interp_version == g->version && op->interp_prec == int(prec), AMDG_ERR_STATE,
+                     "no flux interpolation of this element set and precision: call amdg_lagr_interpolate first");
+    if (group == AMDG_LAGR_RHS_PENALTY && alpha) {  // the LxF constants of this call
+        bool changed = false;
+        for (int d = 0; d < dim; ++d) {
+            AMDG_REQUIRE(std::isfinite(alpha[d]), AMDG_ERR_ARG, "non-finite alpha");
+            PartialSum& p = op->terms[size_t(op->grp_first[2] + d)];
+            if (p.coef != -alpha[d] / 2.0) {
+                p.coef = -alpha[d] / 2.0;
+                op->alpha[d] = alpha[d];
+                changed = true;
+            }
+        }
+        if (changed) {
+            AMDG_CK(cudaMemcpyAsync(op->d_terms, op->terms.data(), op->terms.size() * sizeof(PartialSum),
+                                    cudaMemcpyHostToDevice, st));
+            AMDG_CK(cudaStreamSynchronize(st));  // op->terms may change again before the copy runs
+            op->graph_version = -1;              // a captured step holds the old constants
+        }
+    }
+    double* rhs = nullptr;
+    if (amdg_status s = grid_rhs(g, &rhs); s != AMDG_OK) return s;
+    const int first = op->grp_first[group], count = op->grp_count[group];
+    if (prec == AMDG_PREC_FP64) {
+        const double* src[1] = {static_cast<const double*>(op->w_fu)};
+        return eval_term_range<double>(op, mats64(op), first, count, src, 1, g->d_u, rhs, StageOut{}, st, true);
+    }
+    float* u32 = static_cast<float*>(op->w_u);
+    if (group == AMDG_LAGR_RHS_PENALTY) {
+        AMDG_CK(launch_convert<double, float>(g->d_u, u32, g->dof, st));
+        g->ctx->launches++;
+    }
+    const float* src[1] = {static_cast<const float*>(op->w_fu)};
+    return eval_term_range<float>(op, mats32(op), first, count, src, 1, u32, rhs, StageOut{}, st, true);
 }
 
 amdg_status amdg_burgers_point_values(amdg_burgers_op* op, const double* d_u, double* d_up, amdg_precision prec) {
@@ -795,12 +991,8 @@ amdg_status amdg_burgers_rk3_steps(amdg_burgers_op* op, double dt, int nsteps, a
 
 static double adaptive_dt(const amdg_grid* g, double cfl, double wave_speed) {
     // dt = cfl / sum_d c_d 2^maxlevel_d  (02_hyperbolic_05_burgers_adapt.cpp:239-247)
-    std::vector<int> lv(g->host.dim, 0);
-    for (int64_t e = 0; e < g->host.num_elements; ++e)
-        for (int d = 0; d < g->host.dim; ++d)
-            lv[d] = std::max(lv[d], level_of_order(g->host.order[size_t(e) * g->host.dim + d]));
     double sum_c_dx = 0.0;
-    for (int d = 0; d < g->host.dim; ++d) sum_c_dx += wave_speed * std::pow(2.0, lv[d]);
+    for (int d = 0; d < g->host.dim; ++d) sum_c_dx += wave_speed * std::pow(2.0, g->lev_max[d]);
     return cfl / sum_c_dx;
 }
 
@@ -833,8 +1025,13 @@ static amdg_status adaptive_step_any(amdg_burgers_op* op, double cfl, double wav
     PhaseTimer timer(g->ctx, AMDG_PHASE_ADAPT_STEP);
     cudaStream_t st = stream_of(op);
     const double dt = adaptive_dt(g, cfl, wave_speed);
-    const std::vector<uint64_t> old_keys = g->host.key;
+    const bool on_device = g->ctx->adapt_mode == AMDG_ADAPT_DEVICE;
     amdg_status s;
+    std::vector<uint64_t> old_keys;
+    if (decisions || !on_device) {
+        if ((s = grid_ensure_host(g)) != AMDG_OK) return s;
+        old_keys = g->host.key;
+    }
     if (op->kind == 0) {
         op->rhs_evaluations++;
         // forward Euler into the prediction buffer (ForwardEuler::step_stage)
@@ -851,6 +1048,24 @@ static amdg_status adaptive_step_any(amdg_burgers_op* op, double cfl, double wav
     // refine on the predicted coefficients (and, for the wave, the predicted u_t: the
     // indicator of prob "wave" is ||u|| + ||u_t||); new elements start from zero
     // (DGAdapt::refine, copy_predict_to_ucoe)
+    if (on_device) {
+        {
+            PhaseTimer ta(g->ctx, AMDG_PHASE_ADAPT_DEVICE);
+            std::vector<int8_t> refined(decisions ? size_t(g->host.num_elements) : 0);
+            if ((s = grid_device_norms(g, op->d_pred, op->kind == 1 ? op->d_su : nullptr)) != AMDG_OK ||
+                (s = grid_device_refine(g, eps, nullptr, decisions ? refined.data() : nullptr, nullptr)) != AMDG_OK)
+                return s;
+            if (decisions) std::copy(refined.begin(), refined.end(), decisions);
+        }
+        if ((s = one_step(op, dt, prec)) != AMDG_OK) return s;
+        if ((s = grid_coarsen(g, eta, op->kind == 1 ? g->d_v : nullptr, nullptr)) != AMDG_OK) return s;
+        if (decisions) {
+            if ((s = grid_ensure_host(g)) != AMDG_OK) return s;
+            mark_removed(old_keys, g->host, decisions);
+        }
+        if (dt_out) *dt_out = dt;
+        return AMDG_OK;
+    }
     std::vector<double> norms;
     if ((s = grid_norms(g, op->d_pred, &norms, op->kind == 1 ? op->d_su : nullptr)) != AMDG_OK) return s;
     std::vector<uint8_t> refined;
@@ -893,6 +1108,80 @@ amdg_status amdg_burgers_features(amdg_burgers_op* op, const double* d_u, float*
     return AMDG_OK;
 }
 
+// The horizon's time steps on the current grid, no predictor: n - 1 steps of dt (replayed as a CUDA
+// graph when n - 1 > 1), the last one of dt_last (n = horizon, or fewer to land on t_left).
+static amdg_status horizon_steps(amdg_burgers_op* op, double dt, amdg_precision prec, int horizon, double t_left,
+                                 double* t_advanced, int* steps_out) {
+    int n = horizon;
+    double dt_last = dt;
+    if (t_left > 0) {
+        const int need = std::max(1, int(std::ceil(t_left / dt - 1e-9)));
+        if (need <= n) {
+            n = need;
+            dt_last = t_left - (n - 1) * dt;
+        }
+    }
+    amdg_status s;
+    if (n > 1) {
+        if (op->kind == 0) s = amdg_burgers_rk3_steps(op, dt, n - 1, prec);  // syncs the operator itself
+        else if ((s = burgers_sync(op)) == AMDG_OK) s = wave_rk4(op, dt, n - 1, prec);
+        if (s != AMDG_OK) return s;
+    }
+    if ((s = one_step(op, dt_last, prec)) != AMDG_OK) return s;
+    if (t_advanced) *t_advanced = (n - 1) * dt + dt_last;
+    if (steps_out) *steps_out = n;
+    return AMDG_OK;
+}
+
+// The learned step with the element-set changes on the device: the classifier's probabilities
+// (already in op->d_prob when mlp is given), the criterion's indicators and the missed
+// refinements of the previous step decide the refined leaves without leaving the device; the
+// coarsening records this step's missed refinements there too.
+static amdg_status learned_step_device(amdg_burgers_op* op, amdg_mlp* mlp, double dt, double eps, double eta,
+                                       double tau, amdg_precision prec, int horizon, double t_left, double* t_advanced,
+                                       int* steps_out, int64_t* stats) {
+    amdg_grid* g = op->grid;
+    cudaStream_t st = stream_of(op);
+    amdg_status s;
+    if (!op->d_cls) {
+        void *d = nullptr, *h = nullptr;
+        if (cudaMalloc(&d, 2 * sizeof(unsigned long long)) != cudaSuccess ||
+            cudaMallocHost(&h, 2 * sizeof(unsigned long long)) != cudaSuccess) {
+            cudaFree(d);
+            return fail(AMDG_ERR_NOMEM, "classifier counters");
+        }
+        op->d_cls = static_cast<unsigned long long*>(d);
+        op->h_cls = static_cast<unsigned long long*>(h);
+    }
+    {
+        PhaseTimer ta(g->ctx, AMDG_PHASE_ADAPT_DEVICE);
+        uint8_t* d_force = nullptr;
+        AMDG_CK(cudaMemsetAsync(op->d_cls, 0, 2 * sizeof(unsigned long long), st));
+        if ((s = grid_device_norms(g, g->d_u, op->kind == 1 ? g->d_v : nullptr)) != AMDG_OK ||
+            (s = grid_learned_flags(g, mlp ? op->d_prob : nullptr, tau, eps, &d_force, op->d_cls)) != AMDG_OK ||
+            (s = grid_mark_missed(g, d_force)) != AMDG_OK)
+            return s;
+        // read back with the refinement's synchronisation
+        AMDG_CK(cudaMemcpyAsync(op->h_cls, op->d_cls, 2 * sizeof(unsigned long long), cudaMemcpyDeviceToHost, st));
+        if ((s = grid_device_refine(g, eps, d_force, nullptr, nullptr)) != AMDG_OK) return s;
+    }
+    const int64_t n_net = int64_t(op->h_cls[0]), n_unsure = int64_t(op->h_cls[1]);
+    if ((s = horizon_steps(op, dt, prec, horizon, t_left, t_advanced, steps_out)) != AMDG_OK) return s;
+    {
+        PhaseTimer ta(g->ctx, AMDG_PHASE_ADAPT_DEVICE);
+        if ((s = grid_device_norms(g, g->d_u, op->kind == 1 ? g->d_v : nullptr)) != AMDG_OK ||
+            (s = grid_device_coarsen(g, eta, eps, nullptr)) != AMDG_OK)
+            return s;
+    }
+    if (stats) {
+        stats[0] = n_net;
+        stats[1] = n_unsure;
+        stats[2] = g->dev.n_missed;
+        stats[3] = g->host.num_elements;
+    }
+    return AMDG_OK;
+}
+
 // The learned adaptive step over a horizon of `horizon` time steps on one pre-adapted grid
 // (horizon 1: one step).  With t_left > 0 no step goes past t_left: the horizon is cut to
 // ceil(t_left / dt) steps and the last one shortened to land on it.  *t_advanced: the time
@@ -931,10 +1220,14 @@ static amdg_status learned_step_any(amdg_burgers_op* op, amdg_mlp* mlp, double c
                                         op->d_feat, st));
         g->ctx->launches++;
         if ((s = amdg_mlp_predict(mlp, op->d_feat, E, op->d_prob)) != AMDG_OK) return s;
-        AMDG_CK(cudaMemcpyAsync(prob.data(), op->d_prob, prob.size() * sizeof(float), cudaMemcpyDeviceToHost, st));
+        if (g->ctx->adapt_mode != AMDG_ADAPT_DEVICE)
+            AMDG_CK(cudaMemcpyAsync(prob.data(), op->d_prob, prob.size() * sizeof(float), cudaMemcpyDeviceToHost, st));
     }
     if (op->kind == 1 && (s = ensure_velocity(g)) != AMDG_OK) return s;
     const double* d_ut = op->kind == 1 ? g->d_v : nullptr;  // the wave indicator adds ||u_t||
+    if (g->ctx->adapt_mode == AMDG_ADAPT_DEVICE)
+        return learned_step_device(op, mlp, dt, eps, eta, tau, prec, horizon, t_left, t_advanced, steps_out, stats);
+    if ((s = grid_ensure_host(g)) != AMDG_OK) return s;
     std::vector<double> norms;
     if ((s = grid_norms(g, g->d_u, &norms, d_ut)) != AMDG_OK) return s;  // synchronises the stream
     // 2. pre-adapt: leaves the network marks "refine" (class 0) get children;
@@ -1214,6 +1507,7 @@ amdg_status amdg_grid_init_adaptive_intp(amdg_grid* g, int lagr_degree, amdg_fn_
                                          int* rounds) {
     AMDG_REQUIRE(g && f && std::isfinite(eps) && eps >= 0.0, AMDG_ERR_ARG, "bad arguments");
     AMDG_REQUIRE(lagr_degree >= 3 && lagr_degree <= 5, AMDG_ERR_ARG, "Lagrange degree must be 3, 4 or 5");
+    if (amdg_status s = grid_ensure_host(g); s != AMDG_OK) return s;
     amdg_burgers_op* op = nullptr;
     amdg_status s = lagr_create(g, 2, nullptr, 0.0, &op, lagr_degree);
     if (s != AMDG_OK) return s;

@@ -99,7 +99,9 @@ amdg_status amdg_grid_save(const amdg_grid* g, const char* path, double time) {
     if (!g || !path) return fail(AMDG_ERR_ARG, "null argument");
     if (cudaSetDevice(g->device) != cudaSuccess) return fail(AMDG_ERR_CUDA, "cudaSetDevice failed");
     std::vector<double> u, v;
-    amdg_status s = copy_from_device(g, g->d_u, &u);
+    amdg_status s = grid_ensure_host(g);
+    if (s != AMDG_OK) return s;
+    s = copy_from_device(g, g->d_u, &u);
     if (s != AMDG_OK) return s;
     const int32_t flags = g->d_v ? 1 : 0;
     if (flags && (s = copy_from_device(g, g->d_v, &v)) != AMDG_OK) return s;
@@ -201,6 +203,7 @@ amdg_status amdg_grid_write_level_support(const amdg_grid* g, const char* path) 
     File out;
     out.f = std::fopen(path, "w");
     if (!out.f) return fail(AMDG_ERR_IO, std::string("cannot open ") + path + " for writing");
+    if (amdg_status s = grid_ensure_host(g); s != AMDG_OK) return s;
     const int dim = g->host.dim;
     bool ok = true;
     for (int64_t e = 0; e < g->host.num_elements && ok; ++e) {

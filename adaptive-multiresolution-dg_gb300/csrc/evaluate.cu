@@ -230,6 +230,7 @@ struct EvalTables {
 
 // element hash, level vectors and 1D tables for the coordinates x1d
 amdg_status prepare(const amdg_grid* g, const std::vector<double>& x1d, EvalTables* T, EvalArgs* A) {
+    if (amdg_status s = grid_ensure_host(g); s != AMDG_OK) return s;
     const HostGrid& h = g->host;
     const int dim = h.dim, np = h.k + 1, nmax = h.nmax;
     const int64_t E = h.num_elements;
@@ -354,6 +355,7 @@ amdg_status amdg_grid_error_burgers(const amdg_grid* g, double a, double b, doub
     AMDG_REQUIRE(gauss_points >= 1 && gauss_points <= 10, AMDG_ERR_ARG, "gauss_points must be in 1..10");
     AMDG_REQUIRE(std::isfinite(a) && std::isfinite(b) && std::isfinite(c) && std::isfinite(t) && t >= 0, AMDG_ERR_ARG,
                  "bad exact-solution parameters");
+    if (amdg_status s = grid_ensure_host(g); s != AMDG_OK) return s;
     const HostGrid& h = g->host;
     int qlev = 0;
     for (int32_t o : h.order) qlev = std::max(qlev, level_of_order(o));
@@ -411,6 +413,8 @@ amdg_status amdg_grid_error_burgers(const amdg_grid* g, double a, double b, doub
 
 amdg_status amdg_grid_l2_error_split_grid(const amdg_grid* g, const amdg_grid* exact, double* out) {
     AMDG_REQUIRE(g && exact && out, AMDG_ERR_ARG, "null argument");
+    if (amdg_status s = grid_ensure_host(g); s != AMDG_OK) return s;
+    if (amdg_status s = grid_ensure_host(exact); s != AMDG_OK) return s;
     const HostGrid& h = g->host;
     const HostGrid& he = exact->host;
     AMDG_REQUIRE(h.dim == he.dim && h.nmax == he.nmax && h.k == he.k && g->device == exact->device, AMDG_ERR_ARG,

@@ -176,11 +176,100 @@ __global__ void __launch_bounds__(256) sweep_kernel(SweepArgs<T> a) {
     a.out[int64_t(slot) * per + r] = scale(acc, coef);
 }
 
+// The same sweep with one thread per (term, element, column): a column is one line of the
+// output block along the transformed dimension (its n_to entries), so every input value the
+// thread loads serves all n_to outputs, and the threads of an element walk the same neighbour
+// list (broadcast loads of the pairs and of the 1D matrix rows).  Each output is summed in the
+// order of sweep_kernel (neighbours in list order, k ascending): the results are identical.
+template <typename T, int NTO>
+__global__ void __launch_bounds__(256) sweep_col_kernel(SweepArgs<T> a) {
+    const int cols = a.out_block / NTO;
+    const int64_t per = a.num_elements * cols;
+    const int64_t gid = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (gid >= per * a.count) return;
+    const int slot = int(gid / per);
+    const int64_t r = gid - int64_t(slot) * per;
+    const int64_t e = r / cols;
+    const int c = int(r - e * cols);
+    const PartialSum& D = a.desc[a.first + slot];
+    if (D.kind == 1 && a.sweep + 1 < a.dim) return;  // a penalty term is a single (last) sweep
+    int t, lu, flx, n_from, stride = 1, in_block = 1;
+    const T* M;
+    const T* in;
+    T coef;
+    if (D.kind == 0) {
+        t = D.dims[a.sweep];
+        lu = D.lu[a.sweep];
+        flx = D.flx[a.sweep];
+        M = a.mats[D.mat[a.sweep]];
+        n_from = a.n_in;
+        coef = from_double<T>(a.sweep == 0 ? D.coef : 1.0);
+        in = a.sweep == 0 ? a.src[D.src] : a.in + int64_t(slot) * a.in_slice;
+        int done_after = 0;
+        for (int j = 0; j < a.sweep; ++j) done_after += D.dims[j] > t ? 1 : 0;
+        for (int d = 0; d < a.dim - 1 - t; ++d) stride *= d < done_after ? a.n_out : a.n_in;
+        for (int d = 0; d < a.dim; ++d) in_block *= d < a.sweep ? a.n_out : a.n_in;
+    } else {
+        t = D.dims[0];
+        lu = 1;
+        flx = 1;
+        M = a.mats[kMatAJump];
+        n_from = a.np;
+        coef = from_double<T>(D.coef);
+        in = a.pen_in;
+        for (int d = 0; d < a.dim - 1 - t; ++d) stride *= a.np;
+        for (int d = 0; d < a.dim; ++d) in_block *= a.np;
+    }
+    const int inner = c % stride;
+    const int outer = c / stride;
+    const int64_t et = e * a.dim + t;
+    const int32_t* ptr = flx ? a.flx_ptr : a.vol_ptr;
+    const int32_t* split = flx ? a.flx_split : a.vol_split;
+    const int2* nbr = flx ? a.flx_nbr : a.vol_nbr;
+    const int oe = __ldg(a.order + et);
+    const int beg = lu == 0 ? __ldg(split + et) : __ldg(ptr + et);
+    const int end = lu == 2 ? __ldg(split + et) : __ldg(ptr + et + 1);
+    const int ncols = a.n1 * NTO;
+    const T* mcol = M + size_t(oe) * NTO;
+    const int in_off = outer * n_from * stride + inner;
+    const size_t mstep = size_t(n_from) * ncols;
+    T acc[NTO];
+#pragma unroll
+    for (int q = 0; q < NTO; ++q) acc[q] = from_double<T>(0.0);
+    for (int i = beg; i < end; ++i) {
+        const int2 nb = __ldg(nbr + i);
+        const T* x = in + int64_t(nb.x) * in_block + in_off;
+        const T* m = mcol + size_t(nb.y) * mstep;
+        for (int k = 0; k < n_from; ++k) {
+            const T xv = __ldg(x + k * stride);
+            T mv[NTO];
+#pragma unroll
+            for (int q = 0; q < NTO; ++q) mv[q] = __ldg(m + size_t(k) * ncols + q);
+#pragma unroll
+            for (int q = 0; q < NTO; ++q) acc[q] = madd(xv, mv[q], acc[q]);
+        }
+    }
+    T* o = a.out + int64_t(slot) * a.num_elements * a.out_block + e * a.out_block + int64_t(outer) * stride * NTO + inner;
+#pragma unroll
+    for (int q = 0; q < NTO; ++q) o[int64_t(q) * stride] = scale(acc[q], coef);
+}
+
 template <typename T>
 cudaError_t launch_sweep(const SweepArgs<T>& a, cudaStream_t st) {
     const int64_t total = a.num_elements * a.out_block * a.count;
     if (total == 0) return cudaSuccess;
-    sweep_kernel<T><<<unsigned((total + 255) / 256), 256, 0, st>>>(a);
+    // every term of the range writes n_out entries per column (the penalty terms of a right-hand
+    // side have n_out = np too)
+    const int nto = a.n_out;
+    const int64_t cols = total / nto;
+    const unsigned blocks = unsigned((cols + 255) / 256);
+    switch (a.out_block % nto == 0 ? nto : 0) {
+        case 3: sweep_col_kernel<T, 3><<<blocks, 256, 0, st>>>(a); break;
+        case 4: sweep_col_kernel<T, 4><<<blocks, 256, 0, st>>>(a); break;
+        case 5: sweep_col_kernel<T, 5><<<blocks, 256, 0, st>>>(a); break;
+        case 6: sweep_col_kernel<T, 6><<<blocks, 256, 0, st>>>(a); break;
+        default: sweep_kernel<T><<<unsigned((total + 255) / 256), 256, 0, st>>>(a); break;
+    }
     return cudaGetLastError();
 }
 

@@ -10,9 +10,16 @@
 // prints and calls exit(1)).
 //
 // Mirrors: DGSolution/DGAdapt (DGAdapt.h:10-91, DGSolution.h:21-214),
-// HyperbolicAlpt (BilinearForm.h:137-152), RK3SSP/ForwardEuler (ODESolver.h:93-205),
+// HyperbolicAlpt (BilinearForm.h:137-152), RK3SSP/ForwardEuler (ODESolver.h:5-205),
 // LagrInterpolation + FastLagrIntp + HyperbolicLagrRHS + HyperbolicAlptRHS
-// (Interpolation.h:36-97, FastMultiplyLU.h:194-205, 575-629).
+// (Interpolation.h:36-129, FastMultiplyLU.h:194-205, 575-629), FluxFunction
+// (Interplation.cpp:5070-5073).
+//
+// A host std::function cannot run on the device: LagrInterpolation recognises the
+// fluxes the library registers by evaluating the given function at a few states
+// (u^2/2, the Burgers flux of FluxFunction::burgers_flux_scalar) and throws
+// AMDG_ERR_ARG for any other.  Arithmetic: amdg_gpu::precision (FP64 by default;
+// AMDG_PREC_MIXED runs the back transforms in FP32).
 #pragma once
 
 #include <cmath>
@@ -34,6 +41,10 @@ struct Error : std::runtime_error {
 inline void check(amdg_status s, const char* where) {
     if (s != AMDG_OK) throw Error(s, where);
 }
+
+// arithmetic of the Lagrange-path classes below (a process-wide setting, like the reference's
+// static configuration)
+inline amdg_precision precision = AMDG_PREC_FP64;
 
 // ---- static configuration, as set by the reference drivers ----------------
 struct AlptBasis { static inline int PMAX = 2; };
@@ -107,7 +118,10 @@ public:
     }
     DGSolution(const DGSolution&) = delete;
     DGSolution& operator=(const DGSolution&) = delete;
-    virtual ~DGSolution() { amdg_grid_destroy(grid_); }
+    virtual ~DGSolution() {
+        release_lagr();
+        amdg_grid_destroy(grid_);
+    }
 
     int size_elem() const { int64_t e = 0; check(amdg_grid_size(grid_, &e, nullptr), "amdg_grid_size"); return int(e); }
     int size_basis_alpt() const { int64_t d = 0; check(amdg_grid_size(grid_, nullptr, &d), "amdg_grid_size"); return int(d); }
@@ -137,6 +151,13 @@ public:
               "amdg_grid_l2_error_separable");
         return err;
     }
+    // level and support index of every element (size_elem() x DIM each, Element::level / suppt)
+    void elements(std::vector<int>& level, std::vector<int>& suppt) const {
+        std::vector<int32_t> lv(size_t(size_elem()) * DIM), sp(lv.size());
+        check(amdg_grid_elements(grid_, lv.data(), sp.data()), "amdg_grid_elements");
+        level.assign(lv.begin(), lv.end());
+        suppt.assign(sp.begin(), sp.end());
+    }
     // coefficients of all elements, element blocks in the library's element order
     std::vector<double> coefficients() const {
         std::vector<double> u(size_basis_alpt());
@@ -159,8 +180,32 @@ public:
     }
     amdg_grid* handle() const { return grid_; }
 
+    // Element::rhs / ucoe_alpt_predict of every element (DGSolution.h:153, 171-174)
+    void set_rhs_zero() { check(amdg_grid_set_rhs_zero(grid_), "amdg_grid_set_rhs_zero"); }
+    void copy_ucoe_to_predict() { check(amdg_grid_copy_ucoe_to_predict(grid_), "amdg_grid_copy_ucoe_to_predict"); }
+    void copy_predict_to_ucoe() { check(amdg_grid_copy_predict_to_ucoe(grid_), "amdg_grid_copy_predict_to_ucoe"); }
+    std::vector<double> rhs() const {
+        std::vector<double> r(size_basis_alpt());
+        check(amdg_grid_get_rhs(grid_, r.data(), int64_t(r.size())), "amdg_grid_get_rhs");
+        return r;
+    }
+    // the device operator behind the Lagrange-path classes of this solution (one per grid, as the
+    // reference keeps the interpolation data in the elements)
+    amdg_burgers_op* lagr_op() {
+        if (!lagr_) {
+            const std::vector<double> zero(DIM, 0.0);
+            check(amdg_burgers_create(grid_, zero.data(), &lagr_), "amdg_burgers_create");
+        }
+        return lagr_;
+    }
+
 protected:
+    void release_lagr() {
+        amdg_burgers_destroy(lagr_);
+        lagr_ = nullptr;
+    }
     amdg_grid* grid_ = nullptr;
+    amdg_burgers_op* lagr_ = nullptr;
     int nmax_;
 };
 
@@ -246,19 +291,131 @@ private:
     amdg_linear_op* op_ = nullptr;
 };
 
-class RK3SSP {
+// ExplicitRK on a DGSolution (ODESolver.h:5-38, 93): init() keeps the coefficients at t_n,
+// set_rhs_zero / add_rhs_to_eigenvec act on the solver's own rhs vector, step_stage updates the
+// solution, final() zeroes the solver's rhs.
+class ExplicitRK {
 public:
-    RK3SSP(HyperbolicAlpt& op, double dt, amdg_precision prec = AMDG_PREC_FP64) : op_(op), dt_(dt), prec_(prec) {}
-    const int num_stage = 3;
-    // the state stays on the device between init() and final()
-    void init() {}
-    void step_rk() { check(amdg_rk3ssp_steps(op_.handle(), dt_, 1, prec_), "amdg_rk3ssp_steps"); }
-    void final() {}
+    ExplicitRK(DGSolution& dg, double dt, int scheme, int stages) : dg_(dg), dt_(dt), scheme_(scheme), num_stage(stages) {}
+    ExplicitRK(const ExplicitRK&) = delete;
+    virtual ~ExplicitRK() { amdg_ode_destroy(ode_); }
+    void init() {
+        amdg_ode_destroy(ode_);
+        ode_ = nullptr;
+        check(amdg_ode_create(dg_.handle(), scheme_, dt_, &ode_), "amdg_ode_create");
+    }
+    void set_rhs_zero() { check(amdg_ode_set_rhs_zero(need()), "amdg_ode_set_rhs_zero"); }
+    void add_rhs_to_eigenvec() { check(amdg_ode_add_rhs_to_eigenvec(need()), "amdg_ode_add_rhs_to_eigenvec"); }
+    void step_stage(int stage) { check(amdg_ode_step_stage(need(), stage), "amdg_ode_step_stage"); }
+    void final() { check(amdg_ode_final(need()), "amdg_ode_final"); }
 
 private:
-    HyperbolicAlpt& op_;
+    amdg_ode* need() {
+        if (!ode_) throw Error(AMDG_ERR_STATE, "ExplicitRK: init() first");
+        return ode_;
+    }
+    DGSolution& dg_;
     double dt_;
-    amdg_precision prec_;
+    int scheme_;
+    amdg_ode* ode_ = nullptr;
+
+public:
+    const int num_stage;
+};
+
+class ForwardEuler : public ExplicitRK {
+public:
+    ForwardEuler(DGSolution& dg, double dt) : ExplicitRK(dg, dt, AMDG_ODE_FORWARD_EULER, 1) {}
+};
+
+class RK3SSP : public ExplicitRK {
+public:
+    // on a DGSolution, stage by stage (ODESolver.h:183-198)
+    RK3SSP(DGSolution& dg, double dt) : ExplicitRK(dg, dt, AMDG_ODE_RK3SSP, 3), op_(nullptr) {}
+    // on an assembled linear operator: whole steps (RK3SSP::step_rk, ODESolver.cpp:261-271)
+    RK3SSP(HyperbolicAlpt& op, double dt, amdg_precision prec = AMDG_PREC_FP64)
+        : ExplicitRK(op.solution(), dt, AMDG_ODE_RK3SSP, 3), op_(&op), dt_(dt), prec_(prec) {}
+    void init() {
+        if (!op_) ExplicitRK::init();  // the linear form keeps its state on the device
+    }
+    void step_rk() {
+        if (!op_) throw Error(AMDG_ERR_STATE, "RK3SSP::step_rk needs the operator form");
+        check(amdg_rk3ssp_steps(op_->handle(), dt_, 1, prec_), "amdg_rk3ssp_steps");
+    }
+    void final() {
+        if (!op_) ExplicitRK::final();
+    }
+
+private:
+    HyperbolicAlpt* op_;
+    double dt_ = 0.0;
+    amdg_precision prec_ = AMDG_PREC_FP64;
+};
+
+// ---- Lagrange interpolation of the nonlinear flux, term by term --------------------
+struct FluxFunction {
+    static double burgers_flux_scalar(const double u) { return u * u * 0.5; }
+};
+
+// FastLagrIntp(dg, Lag_pt_Alpt_1D, Lag_pt_Alpt_1D_d1) (FastMultiplyLU.h:194-205): the tables
+// live in the device operator; the object only carries the solution.
+class FastLagrIntp {
+public:
+    FastLagrIntp(DGSolution& dg, const std::vector<std::vector<double>>&, const std::vector<std::vector<double>>&)
+        : dg_(dg) {}
+    DGSolution& solution() const { return dg_; }
+
+private:
+    DGSolution& dg_;
+};
+
+// LagrInterpolation (Interpolation.h:36-129)
+class LagrInterpolation {
+public:
+    explicit LagrInterpolation(DGSolution& dg) : dg_(dg) {}
+    // the 1D tables the reference exposes for FastLagrIntp (built on the device instead)
+    std::vector<std::vector<double>> Lag_pt_Alpt_1D, Lag_pt_Alpt_1D_d1;
+    // LagrInterpolation::nonlinear_Lagr_fast (Interplation.cpp:4033-4047): flux coefficients of
+    // the current solution, kept for the HyperbolicLagrRHS calls that follow
+    void nonlinear_Lagr_fast(std::function<double(std::vector<double>, int, int)> func,
+                             const std::vector<std::vector<bool>>& /*is_intp: the flux is the same in every dimension*/,
+                             FastLagrIntp& /*fast*/) {
+        for (double u : {0.375, -1.3125, 2.25})
+            for (int d = 0; d < DGSolution::DIM; ++d)
+                if (func(std::vector<double>{u}, 0, d) != FluxFunction::burgers_flux_scalar(u))
+                    throw Error(AMDG_ERR_ARG, "LagrInterpolation::nonlinear_Lagr_fast: only the Burgers flux u^2/2 is registered");
+        check(amdg_lagr_interpolate(dg_.lagr_op(), precision), "amdg_lagr_interpolate");
+    }
+
+private:
+    DGSolution& dg_;
+};
+
+// HyperbolicLagrRHS (FastMultiplyLU.h:575-586): adds into Element::rhs
+class HyperbolicLagrRHS {
+public:
+    HyperbolicLagrRHS(DGSolution& dg, const OperatorMatrix1D<LagrBasis, AlptBasis>&) : dg_(dg) {}
+    void rhs_vol_scalar() { check(amdg_lagr_rhs_add(dg_.lagr_op(), AMDG_LAGR_RHS_VOL, nullptr, precision), "rhs_vol_scalar"); }
+    void rhs_flx_intp_scalar() {
+        check(amdg_lagr_rhs_add(dg_.lagr_op(), AMDG_LAGR_RHS_FLX, nullptr, precision), "rhs_flx_intp_scalar");
+    }
+
+private:
+    DGSolution& dg_;
+};
+
+// HyperbolicAlptRHS (FastMultiplyLU.h:623-629): the LxF penalty, added into Element::rhs
+class HyperbolicAlptRHS {
+public:
+    HyperbolicAlptRHS(DGSolution& dg, const OperatorMatrix1D<AlptBasis, AlptBasis>&) : dg_(dg) {}
+    void rhs_flx_penalty_scalar(const std::vector<double>& lax_alpha) {
+        if (int(lax_alpha.size()) != DGSolution::DIM) throw Error(AMDG_ERR_ARG, "rhs_flx_penalty_scalar: one alpha per dimension");
+        check(amdg_lagr_rhs_add(dg_.lagr_op(), AMDG_LAGR_RHS_PENALTY, lax_alpha.data(), precision),
+              "rhs_flx_penalty_scalar");
+    }
+
+private:
+    DGSolution& dg_;
 };
 
 // ---- nonlinear flux (Burgers) through Lagrange interpolation ------------------

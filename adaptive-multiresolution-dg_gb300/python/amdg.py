@@ -125,6 +125,22 @@ def load():
         "amdg_wave_adaptive_step_learned": ([vp, vp, dbl, dbl, dbl, dbl, dbl, i32, C.POINTER(dbl), vp], i32),
         "amdg_wave_adaptive_steps_learned": ([vp, vp, dbl, dbl, dbl, dbl, dbl, i32, i32, dbl, vp, vp, vp], i32),
         "amdg_context_profile": ([vp, i32], i32),
+        "amdg_context_set_adapt_mode": ([vp, i32], i32),
+        "amdg_grid_set_rhs_zero": ([vp], i32),
+        "amdg_grid_rhs_device": ([vp, pp], i32),
+        "amdg_grid_get_rhs": ([vp, vp, i64], i32),
+        "amdg_grid_copy_ucoe_to_predict": ([vp], i32),
+        "amdg_grid_copy_predict_to_ucoe": ([vp], i32),
+        "amdg_vector_axpy": ([vp, dbl, vp, vp, i64], i32),
+        "amdg_ode_create": ([vp, i32, dbl, pp], i32),
+        "amdg_ode_destroy": ([vp], i32),
+        "amdg_ode_set_rhs_zero": ([vp], i32),
+        "amdg_ode_add_rhs_to_eigenvec": ([vp], i32),
+        "amdg_ode_step_stage": ([vp, i32], i32),
+        "amdg_ode_final": ([vp], i32),
+        "amdg_lagr_interpolate": ([vp, i32], i32),
+        "amdg_burgers_work": ([vp, C.POINTER(dbl), C.POINTER(dbl)], i32),
+        "amdg_lagr_rhs_add": ([vp, i32, vp, i32], i32),
         "amdg_context_profile_read": ([vp, vp, vp], i32),
         "amdg_burgers_counters": ([vp, C.POINTER(i64), C.POINTER(i64)], i32),
         "amdg_grid_error_burgers": ([vp, dbl, dbl, dbl, dbl, i32, vp], i32),
@@ -219,7 +235,13 @@ class Context:
         _ck(load().amdg_context_launch_count(self._h, C.byref(n)), "context_launch_count")
         return n.value
 
-    PHASES = ("topology", "set_keys", "norms", "adapt_host", "rhs", "rk3", "classifier", "adapt_step")
+    PHASES = ("topology", "set_keys", "norms", "adapt_host", "rhs", "rk3", "classifier", "adapt_step", "adapt_device")
+    ADAPT_DEVICE, ADAPT_HOST = 0, 1
+
+    def set_adapt_mode(self, mode: int):
+        """ADAPT_DEVICE (default): element-set changes and neighbour lists on the device;
+        ADAPT_HOST: on the host key set."""
+        _ck(load().amdg_context_set_adapt_mode(self._h, mode), "context_set_adapt_mode")
 
     def profile(self, enable: bool = True):
         """Start (and reset) or stop the host phase profile."""
@@ -366,6 +388,27 @@ class Grid:
         p = C.c_void_p()
         _ck(load().amdg_grid_coefficients_device(self._h, C.byref(p)), "grid_coefficients_device")
         return p.value
+
+    def set_rhs_zero(self):
+        """DGSolution::set_rhs_zero: the grid's Element::rhs vector = 0."""
+        _ck(load().amdg_grid_set_rhs_zero(self._h), "grid_set_rhs_zero")
+
+    def rhs_device_ptr(self) -> int:
+        p = C.c_void_p()
+        _ck(load().amdg_grid_rhs_device(self._h, C.byref(p)), "grid_rhs_device")
+        return p.value
+
+    def rhs(self) -> np.ndarray:
+        """The grid's Element::rhs vector, as (num_elements, block)."""
+        out = np.zeros(self.dof)
+        _ck(load().amdg_grid_get_rhs(self._h, _ptr(out), self.dof), "grid_get_rhs")
+        return out.reshape(self.num_elements, self.block)
+
+    def copy_ucoe_to_predict(self):
+        _ck(load().amdg_grid_copy_ucoe_to_predict(self._h), "grid_copy_ucoe_to_predict")
+
+    def copy_predict_to_ucoe(self):
+        _ck(load().amdg_grid_copy_predict_to_ucoe(self._h), "grid_copy_predict_to_ucoe")
 
     def init_separable(self, funcs, vectorized: bool = False):
         if vectorized:
@@ -514,6 +557,24 @@ class BurgersOperator:
     def rhs_device(self, d_u: int, d_rhs: int, prec: int = FP64):
         _ck(load().amdg_burgers_rhs(self._h, C.c_void_p(d_u), C.c_void_p(d_rhs), prec), "burgers_rhs")
 
+    RHS_VOL, RHS_FLX, RHS_PENALTY = 0, 1, 2
+
+    def work(self):
+        """(flops, neighbour pairs) of one right-hand side on the current element set."""
+        f, p = C.c_double(), C.c_double()
+        _ck(load().amdg_burgers_work(self._h, C.byref(f), C.byref(p)), "burgers_work")
+        return f.value, p.value
+
+    def interpolate(self, prec: int = FP64):
+        """LagrInterpolation::nonlinear_Lagr_fast for u^2/2 on the grid's coefficients."""
+        _ck(load().amdg_lagr_interpolate(self._h, prec), "lagr_interpolate")
+
+    def rhs_add(self, group: int, alpha=None, prec: int = FP64):
+        """Add one term group (RHS_VOL / RHS_FLX / RHS_PENALTY) into the grid's Element::rhs."""
+        a = None if alpha is None else np.ascontiguousarray(
+            np.broadcast_to(np.asarray(alpha, np.float64), (self.grid.dim,)))
+        _ck(load().amdg_lagr_rhs_add(self._h, group, None if a is None else _ptr(a), prec), "lagr_rhs_add")
+
     def point_values_device(self, d_u: int, d_up: int, prec: int = FP64):
         _ck(load().amdg_burgers_point_values(self._h, C.c_void_p(d_u), C.c_void_p(d_up), prec), "burgers_point_values")
 
@@ -647,6 +708,38 @@ class WaveOperator:
     def close(self):
         if self._h:
             load().amdg_wave_destroy(self._h)
+            self._h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class ODE:
+    """ForwardEuler / RK3SSP (ODESolver) on a grid's device state, stage by stage."""
+    FORWARD_EULER, RK3SSP = 0, 1
+
+    def __init__(self, grid: Grid, scheme: int, dt: float):
+        self._h = C.c_void_p()
+        _ck(load().amdg_ode_create(grid.handle, scheme, dt, C.byref(self._h)), "ode_create")
+
+    def set_rhs_zero(self):
+        _ck(load().amdg_ode_set_rhs_zero(self._h), "ode_set_rhs_zero")
+
+    def add_rhs_to_eigenvec(self):
+        _ck(load().amdg_ode_add_rhs_to_eigenvec(self._h), "ode_add_rhs_to_eigenvec")
+
+    def step_stage(self, stage: int):
+        _ck(load().amdg_ode_step_stage(self._h, stage), "ode_step_stage")
+
+    def final(self):
+        _ck(load().amdg_ode_final(self._h), "ode_final")
+
+    def close(self):
+        if self._h:
+            load().amdg_ode_destroy(self._h)
             self._h = C.c_void_p()
 
     def __del__(self):

@@ -31,7 +31,7 @@
 extern "C" {
 #endif
 
-#define AMDG_ABI_VERSION 3
+#define AMDG_ABI_VERSION 4
 
 typedef enum amdg_status {
     AMDG_OK = 0,
@@ -101,10 +101,20 @@ enum {
     AMDG_PHASE_RK3 = 5,        /* Burgers SSP-RK3 steps enqueued (graph capture included) */
     AMDG_PHASE_CLASSIFIER = 6, /* learned refine/coarsen: features, network, probabilities read back */
     AMDG_PHASE_ADAPT_STEP = 7, /* whole adaptive steps (plain or learned) */
-    AMDG_PHASE_COUNT = 8
+    AMDG_PHASE_ADAPT_DEVICE = 8, /* refine / coarsen on the device, including the one wait for the new element count */
+    AMDG_PHASE_COUNT = 9
 };
 /* enable != 0 starts (and resets) the profile, 0 stops it. */
 amdg_status amdg_context_profile(amdg_context* ctx, int enable);
+
+/* Where the element set changes of this context's grids run (no reference counterpart; the
+ * reference's DGAdapt::refine / coarsen and DGSolution::find_ptr_* are host code):
+ * AMDG_ADAPT_DEVICE (default) -- refine, coarsen, hole filling and the fast transforms' neighbour
+ * lists and surplus ancestors are computed on the device from the sorted element keys, with one
+ * stream synchronisation per change (the new element count); AMDG_ADAPT_HOST -- the same on
+ * the host key set, uploaded after every change.  Both give the same element sets and lists. */
+enum { AMDG_ADAPT_DEVICE = 0, AMDG_ADAPT_HOST = 1 };
+amdg_status amdg_context_set_adapt_mode(amdg_context* ctx, int mode);
 /* seconds[AMDG_PHASE_COUNT] and calls[AMDG_PHASE_COUNT] (either may be NULL). */
 amdg_status amdg_context_profile_read(const amdg_context* ctx, double* seconds, int64_t* calls);
 
@@ -280,6 +290,39 @@ amdg_status amdg_rk3ssp_serve_host(amdg_linear_op* op, double dt, int nsteps, am
  * capture. */
 amdg_status amdg_rk3ssp_steps_noalloc(amdg_linear_op* op, double* d_u, double dt, int nsteps, amdg_precision prec);
 
+/* ---- the reference driver's per-element vectors and explicit integrators ----
+ * (no separate reference entry points: these are the Element members and ODESolver calls a
+ * driver's stage loop uses, e.g. example/07_vlasov_maxwell_adapt.cpp:278-320) */
+/* DGSolution::set_rhs_zero (DGSolution.h:153): Element::rhs of every element = 0.  The grid's rhs
+ * vector (dof doubles) is what the *_rhs_add calls accumulate into; it restarts at zero whenever
+ * the element set changes. */
+amdg_status amdg_grid_set_rhs_zero(amdg_grid* g);
+amdg_status amdg_grid_rhs_device(amdg_grid* g, double** device_ptr);
+/* Element::rhs of every element into host memory (n = dof doubles). */
+amdg_status amdg_grid_get_rhs(amdg_grid* g, double* host, int64_t n);
+/* DGSolution::copy_ucoe_to_predict / copy_predict_to_ucoe (DGSolution.h:171-174): the prediction
+ * vector follows refine / coarsen like the coefficients (new elements zero, as the reference's
+ * new Element objects are). */
+amdg_status amdg_grid_copy_ucoe_to_predict(amdg_grid* g);
+amdg_status amdg_grid_copy_predict_to_ucoe(amdg_grid* g);
+/* y += a x on device vectors of n doubles (Eigen's vector update). */
+amdg_status amdg_vector_axpy(amdg_context* ctx, double a, const double* d_x, double* d_y, int64_t n);
+
+/* ODESolver (ODESolver.h:5-38) for ForwardEuler (ODESolver.h:115-127, ODESolver.cpp:209-213) and
+ * RK3SSP (ODESolver.h:183-198, ODESolver.cpp:285-301) on a grid's device state: create = the
+ * constructor + ExplicitRK::init() (ODESolver.h:93: the coefficients at t_n are kept, the
+ * solver's rhs is zero); set_rhs_zero / add_rhs_to_eigenvec (:38, :24) act on the solver's rhs
+ * vector (add: += the grid's Element::rhs); step_stage(stage) updates the grid's coefficients;
+ * final() (:17) zeroes the solver's rhs (the state already is the grid's).  The element set must not change between create and step_stage. */
+typedef struct amdg_ode amdg_ode;
+enum { AMDG_ODE_FORWARD_EULER = 0, AMDG_ODE_RK3SSP = 1 };
+amdg_status amdg_ode_create(amdg_grid* g, int scheme, double dt, amdg_ode** out);
+amdg_status amdg_ode_destroy(amdg_ode* ode);
+amdg_status amdg_ode_set_rhs_zero(amdg_ode* ode);
+amdg_status amdg_ode_add_rhs_to_eigenvec(amdg_ode* ode);
+amdg_status amdg_ode_step_stage(amdg_ode* ode, int stage);
+amdg_status amdg_ode_final(amdg_ode* ode);
+
 /* ---- stage updates for an externally computed right-hand side ----------- */
 /* RK3SSP::step_stage / ForwardEuler::step_stage (ODESolver.cpp:209-213,
  * 285-301) on device vectors of n doubles: stage 0 u = un + dt*rhs,
@@ -319,6 +362,23 @@ amdg_status amdg_burgers_flux_coefficients(amdg_burgers_op* op, const double* d_
  * re-evaluated per stage (RK3SSP::step_stage, ODESolver.cpp:285-301, in the
  * stage loop of example/07_vlasov_maxwell_adapt.cpp:278-320). */
 amdg_status amdg_burgers_rk3_steps(amdg_burgers_op* op, double dt, int nsteps, amdg_precision prec);
+/* The right-hand side call by call, as a reference driver composes it:
+ * LagrInterpolation::nonlinear_Lagr_fast (Interplation.cpp:4033-4047) for the registered flux
+ * u^2/2 -- point values of the grid's coefficients, the flux there and its hierarchical surpluses,
+ * kept in the operator -- then each group added into the grid's rhs (amdg_grid_rhs_device):
+ * AMDG_LAGR_RHS_VOL = HyperbolicLagrRHS::rhs_vol_scalar, AMDG_LAGR_RHS_FLX = rhs_flx_intp_scalar
+ * (FastMultiplyLU.cpp:1125-1189; both need the interpolation of the current element set and
+ * precision), AMDG_LAGR_RHS_PENALTY = HyperbolicAlptRHS::rhs_flx_penalty_scalar(alpha)
+ * (:1269-1276) on the grid's coefficients; alpha (dim entries) replaces the operator's LxF
+ * constants, NULL keeps them.  vol + flx + penalty added in that order equal amdg_burgers_rhs. */
+enum { AMDG_LAGR_RHS_VOL = 0, AMDG_LAGR_RHS_FLX = 1, AMDG_LAGR_RHS_PENALTY = 2 };
+/* Algorithmic work of one right-hand side on the current element set (no reference counterpart):
+ * the multiply-adds of every 1D transform sweep of every term (2 flops each, from the neighbour
+ * lists' L / full / U counts) plus the surplus passes, and the (element, neighbour) pairs the
+ * sweeps visit.  Reads the lists back (synchronises): for measurement, not for the step loop. */
+amdg_status amdg_burgers_work(amdg_burgers_op* op, double* flops, double* transform_pairs);
+amdg_status amdg_lagr_interpolate(amdg_burgers_op* op, amdg_precision prec);
+amdg_status amdg_lagr_rhs_add(amdg_burgers_op* op, int group, const double* alpha, amdg_precision prec);
 
 /* ---- batched independent linear solves ------------------------------------ */
 /* Many independent constant-coefficient solves (one HyperbolicAlpt + RK3SSP

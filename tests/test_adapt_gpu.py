@@ -107,8 +107,10 @@ def test_refine_coarsen_round_trip_and_version(ctx):
 
 def test_host_phase_profile_counts_adaptive_work(ctx):
     """Two plain adaptive steps: every step evaluates four right-hand sides
-    (predictor and three stages), reads norms twice, and rebuilds the neighbour
-    lists whenever the element set changed; the profile stops when disabled."""
+    (predictor and three stages), changes the element set twice on the device
+    (refine and coarsen, no norms read back to the host), and rebuilds the
+    neighbour lists whenever the element set changed; the profile stops when
+    disabled."""
     g = amdg.Grid(ctx, 2, 6, 2, level_init=3)
     g.init_separable_adaptive(O.burgers_ic_terms(2), 1e-4)
     op = amdg.BurgersOperator(g, 0.825)
@@ -121,7 +123,8 @@ def test_host_phase_profile_counts_adaptive_work(ctx):
     assert prof["adapt_step"][1] == 2
     assert prof["rhs"][1] == 8
     assert prof["rk3"][1] == 2
-    assert prof["norms"][1] == 4
+    assert prof["adapt_device"][1] == 4
+    assert prof["norms"][1] == 0 and prof["adapt_host"][1] == 0
     assert prof["topology"][1] >= 1
     assert all(v[0] >= 0.0 for v in prof.values())
     assert prof["adapt_step"][0] >= prof["rk3"][0]

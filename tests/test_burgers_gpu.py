@@ -91,3 +91,31 @@ def test_burgers_rhs_deterministic_and_hole_detection(ctx):
     assert np.array_equal(a, b)
     op.close()
     g.close()
+
+
+@pytest.mark.parametrize("prec", [amdg.FP64, amdg.MIXED])
+def test_rhs_term_groups_add_up_to_the_fused_rhs(ctx, prec):
+    """LagrInterpolation + rhs_vol_scalar + rhs_flx_intp_scalar + rhs_flx_penalty_scalar called one
+    by one into the grid's rhs equal the fused right-hand side bitwise (same terms, same order)."""
+    dim, N = 3, 4
+    g = amdg.Grid(ctx, dim, N, 2)
+    g.init_separable(O.burgers_ic_terms(dim))
+    op = amdg.BurgersOperator(g, 0.825)
+    du = torch.from_numpy(g.coefficients().reshape(-1).copy()).cuda()
+    fused = torch.zeros_like(du)
+    torch.cuda.synchronize()
+    op.rhs_device(du.data_ptr(), fused.data_ptr(), prec)
+    op.interpolate(prec)
+    g.set_rhs_zero()
+    for group in (op.RHS_VOL, op.RHS_FLX, op.RHS_PENALTY):
+        op.rhs_add(group, 0.825 if group == op.RHS_PENALTY else None, prec=prec)
+    assert np.array_equal(g.rhs().reshape(-1), fused.cpu().numpy())
+    # the penalty constant of the call replaces the operator's
+    g.set_rhs_zero()
+    op.rhs_add(op.RHS_PENALTY, 1.5, prec=prec)
+    pen15 = g.rhs().copy()
+    g.set_rhs_zero()
+    op.rhs_add(op.RHS_PENALTY, 0.75, prec=prec)
+    assert np.allclose(pen15, 2.0 * g.rhs(), rtol=1e-12, atol=0)
+    op.close()
+    g.close()

@@ -81,3 +81,30 @@ def test_cpp_intp_driver_matches_oracle():
     assert (elements, elements_ext) == (len(keys), len(keys_ext))
     assert abs(err - ref) <= 1e-7 * ref
     assert 0 < ref < 1e-2
+
+
+def _read_elements(path, dim):
+    rows = np.loadtxt(path, ndmin=2)
+    return rows[:, :dim].astype(int), rows[:, dim:2 * dim].astype(int), rows[:, 2 * dim:]
+
+
+@pytest.mark.parametrize("name", ["burgers_adapt3d", "burgers_adapt3d_config3"])
+def test_cpp_burgers_driver_matches_reference(tmp_path, name):
+    """The adaptive Burgers driver written call for call like the reference's loop (LagrInterpolation,
+    HyperbolicLagrRHS, HyperbolicAlptRHS, ForwardEuler predictor, refine, RK3SSP stages, coarsen)
+    ends on the reference's element set, coefficients to 1e-12 of their largest entry."""
+    from helpers import golden, manifest, rel_err
+    exe = os.path.join(os.path.dirname(amdg.LIB_PATH), "burgers_adapt")
+    assert os.path.exists(exe), "example driver not built"
+    m = manifest()[name]
+    z = golden(name)
+    out_file = str(tmp_path / "u.txt")
+    args = [m["dim"], m["n_init"], m["nmax"], m["steps"], repr(m["eps"]), repr(m["eta"]), repr(m["alpha"]), out_file]
+    subprocess.run([exe] + [str(a) for a in args], capture_output=True, text=True, timeout=600, check=True)
+    lv, sp, u = _read_elements(out_file, m["dim"])
+    s = m["steps"]
+    keys = O.arrays_to_keys(lv, sp)
+    ref_keys = O.arrays_to_keys(z[f"level_{s}"], z[f"suppt_{s}"])
+    assert set(keys) == set(ref_keys)
+    pos = {k: j for j, k in enumerate(ref_keys)}
+    assert rel_err(u, z[f"u_{s}"][[pos[k] for k in keys]]) < 1e-12
