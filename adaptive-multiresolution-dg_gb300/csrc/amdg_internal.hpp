@@ -237,7 +237,20 @@ struct PartialSum {
     int8_t src;    // input of the first sweep (index into the launch's sources)
     int32_t kind;
     double coef;
+    // as a node of a launch's sweep tree: the slice of the previous sweep this node reads (sweeps
+    // after the first), and coef is the scale this sweep applies
+    int32_t parent;
 };
+// The sweeps of a range of terms as a tree: terms whose first j sweeps coincide (same source,
+// dimensions, L/U tags, matrices and neighbour sets, power-of-two coefficients moved to their last
+// sweep) share those sweeps.  Nodes of sweep j at nodes[offset[j] .. offset[j] + count[j]); the last
+// sweep has one node per term, in term order.
+struct SweepTree {
+    int offset[kMaxDim] = {0}, count[kMaxDim] = {0};
+};
+// nodes of the tree of terms [first, first + count) of `terms`, appended to `nodes`
+SweepTree build_sweep_tree(const std::vector<PartialSum>& terms, int first, int count, int dim,
+                           std::vector<PartialSum>* nodes);
 // surplus ancestors: [e][d][ic] element index, ic < t.p1 (-1 for level 0 in d); false if a hole is found
 bool build_surplus_ancestors(const HostGrid& g, const LagrTables& t, std::vector<int32_t>* anc);
 
@@ -409,9 +422,16 @@ struct amdg_burgers_op {
     amdg::PartialSum* d_terms = nullptr;
     int n_pv_terms = 0;
     int grp_first[3] = {0, 0, 0}, grp_count[3] = {0, 0, 0};  // Burgers: volume, interface, penalty terms
+    // sweep trees of the term ranges launched so far, keyed by (first, count), their nodes on the
+    // host and (uploaded whenever a tree is added or a coefficient changes) on the device
+    std::vector<std::pair<std::pair<int, int>, amdg::SweepTree>> trees;
+    std::vector<amdg::PartialSum> nodes;
+    amdg::PartialSum* d_nodes = nullptr;
+    size_t nodes_cap = 0;
     int64_t interp_version = -1;     // element set of the flux coefficients amdg_lagr_interpolate kept
     int interp_prec = -1;            // ... and their arithmetic
     int chunk = 1;  // terms per launch
+    int sweep_variant = 0;  // transform sweep kernel: 0 thread per output entry, 1 thread per column
     // work buffers sized for FP64: E x p1^dim doubles each, the sweep buffers and
     // term slices chunk times that
     void *w_up = nullptr, *w_fu = nullptr, *w_a = nullptr, *w_b = nullptr, *w_u = nullptr;

@@ -212,6 +212,72 @@ double wave_penalty_coef(const amdg_burgers_op* op) {
     return -op->sigma / (1.0 / std::pow(2.0, maxl));
 }
 
+// The nodes of every sweep tree on the device (grown when a tree is added; a step captured as a
+// graph refers to the buffer, so growing it drops the graph).
+amdg_status upload_nodes(amdg_burgers_op* op, cudaStream_t st) {
+    const size_t bytes = op->nodes.size() * sizeof(PartialSum);
+    if (bytes > op->nodes_cap) {
+        AMDG_CK(cudaStreamSynchronize(st));
+        cudaFree(op->d_nodes);
+        op->d_nodes = nullptr;
+        op->nodes_cap = 0;
+        const size_t want = 2 * bytes + 1024;
+        if (cudaMalloc(reinterpret_cast<void**>(&op->d_nodes), want) != cudaSuccess)
+            return fail(AMDG_ERR_NOMEM, "cudaMalloc failed (sweep trees)");
+        op->nodes_cap = want;
+        op->graph_version = -1;
+    }
+    if (bytes) AMDG_CK(cudaMemcpyAsync(op->d_nodes, op->nodes.data(), bytes, cudaMemcpyHostToDevice, st));
+    AMDG_CK(cudaStreamSynchronize(st));  // op->nodes may change again before the copy would run
+    return AMDG_OK;
+}
+
+// after a change of term coefficients: the nodes of every tree again (the same structure: only
+// the penalty's coefficient changes, and the penalty is never shared)
+amdg_status refresh_nodes(amdg_burgers_op* op, cudaStream_t st) {
+    op->nodes.clear();
+    for (auto& kv : op->trees)
+        kv.second = build_sweep_tree(op->terms, kv.first.first, kv.first.second, op->grid->host.dim, &op->nodes);
+    return upload_nodes(op, st);
+}
+
+// the sweep tree of terms [first, first + count), built and uploaded on first use
+amdg_status sweep_tree(amdg_burgers_op* op, int first, int count, SweepTree* out, cudaStream_t st) {
+    for (const auto& kv : op->trees)
+        if (kv.first.first == first && kv.first.second == count) {
+            *out = kv.second;
+            return AMDG_OK;
+        }
+    cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+    AMDG_CK(cudaStreamIsCapturing(st, &cap));
+    AMDG_REQUIRE(cap == cudaStreamCaptureStatusNone, AMDG_ERR_STATE, "sweep tree built during stream capture");
+    op->trees.push_back({{first, count}, build_sweep_tree(op->terms, first, count, op->grid->host.dim, &op->nodes)});
+    *out = op->trees.back().second;
+    return upload_nodes(op, st);
+}
+
+// the trees of every term range the right-hand side launches with the current chunk size, so a
+// step captured as a graph finds them all
+amdg_status prepare_trees(amdg_burgers_op* op, cudaStream_t st) {
+    SweepTree t;
+    auto chunks = [&](int first, int total) -> amdg_status {
+        for (int c0 = 0; c0 < total; c0 += op->chunk)
+            if (amdg_status s = sweep_tree(op, first + c0, std::min(op->chunk, total - c0), &t, st); s != AMDG_OK) return s;
+        return AMDG_OK;
+    };
+    const int nterms = int(op->terms.size()), dim = op->grid->host.dim;
+    amdg_status s;
+    if (op->kind == 1) {
+        const int G = int(op->sched_dims.size());
+        for (int f = 0; f <= dim; ++f)
+            if ((s = chunks(f * G, G)) != AMDG_OK) return s;
+        if ((s = chunks(nterms - dim, dim)) != AMDG_OK) return s;
+    } else if ((s = chunks(0, op->n_pv_terms)) != AMDG_OK) {
+        return s;
+    }
+    return chunks(op->n_pv_terms, nterms - op->n_pv_terms);
+}
+
 template <typename T>
 SweepArgs<T> sweep_args(const amdg_burgers_op* op, const Mats<T>& m) {
     const amdg_grid* g = op->grid;
@@ -221,6 +287,7 @@ SweepArgs<T> sweep_args(const amdg_burgers_op* op, const Mats<T>& m) {
     a.n1 = op->n1;
     a.num_elements = g->host.num_elements;
     a.desc = op->d_terms;
+    a.variant = op->sweep_variant;
     for (int i = 0; i < kNumLagrMats; ++i) a.mats[i] = m.m[i];
     a.vol_ptr = op->d_vol_ptr;
     a.vol_split = op->d_vol_split;
@@ -242,9 +309,10 @@ amdg_status run_terms(amdg_burgers_op* op, const Mats<T>& m, int first, int coun
     const int64_t E = op->grid->host.num_elements;
     T* ping = static_cast<T*>(op->w_s0);
     T* pong = static_cast<T*>(op->w_s1);
+    SweepTree tree;
+    if (amdg_status s = sweep_tree(op, first, count, &tree, st); s != AMDG_OK) return s;
     SweepArgs<T> a = sweep_args<T>(op, m);
-    a.first = first;
-    a.count = count;
+    a.first = 0;
     a.n_in = n_in;
     a.n_out = n_out;
     a.pen_in = pen_in;
@@ -257,6 +325,8 @@ amdg_status run_terms(amdg_burgers_op* op, const Mats<T>& m, int first, int coun
         a.in_slice = j == 0 ? 0 : E * ipow(n_out, j) * ipow(n_in, dim - j);
         a.out_block = ipow(n_out, j + 1) * ipow(n_in, dim - j - 1);
         a.out = last ? slots : (j % 2 == 0 ? ping : pong);
+        a.desc = op->d_nodes + tree.offset[j];
+        a.count = tree.count[j];
         AMDG_CK(launch_sweep<T>(a, st));
         op->grid->ctx->launches++;
         cur = a.out;
@@ -624,12 +694,9 @@ amdg_status burgers_sync(amdg_burgers_op* op) {
         bool changed = false;
         for (PartialSum& p : op->terms)
             if (p.kind == 1 && p.coef != c) { p.coef = c; changed = true; }
-        if (changed) {  // only when the finest level changed
-            AMDG_CK(cudaMemcpyAsync(op->d_terms, op->terms.data(), op->terms.size() * sizeof(PartialSum),
-                                    cudaMemcpyHostToDevice, st));
-            AMDG_CK(cudaStreamSynchronize(st));
-        }
+        if (changed && (s = refresh_nodes(op, st)) != AMDG_OK) return s;  // only when the finest level changed
     }
+    if ((s = prepare_trees(op, st)) != AMDG_OK) return s;
     op->built_version = g->version;
     return AMDG_OK;
 }
@@ -747,7 +814,7 @@ amdg_status amdg_burgers_destroy(amdg_burgers_op* op) {
                     op->d_pg,
                     op->d_feat, op->d_prob, op->d_a2pd, op->d_ljv, op->d_pts, op->f_a2pd, op->f_ljv,
                     op->w_fields, op->d_v1, op->d_su, op->d_sv, op->df_a2p, op->df_a2pd,
-                    op->d_anc_order, op->d_topo_cnt, op->d_cls};
+                    op->d_anc_order, op->d_topo_cnt, op->d_cls, op->d_nodes};
     for (void* p : ptrs) cudaFree(p);
     cudaFreeHost(op->h_cls);
     delete op;
@@ -788,27 +855,50 @@ amdg_status amdg_burgers_work(amdg_burgers_op* op, double* flops, double* transf
             cnt[t][f][1] += ptr[f][r + 1] - ptr[f][r];
             cnt[t][f][2] += split[f][r] - ptr[f][r];      // "U": coarser or equal
         }
+    // the sweeps one right-hand side runs: the nodes of the sweep trees of its term ranges
     double fl = 0.0, pairs = 0.0;
-    for (size_t i = 0; i < op->terms.size(); ++i) {
-        const PartialSum& D = op->terms[i];
-        const bool pv = int(i) < op->n_pv_terms;
-        if (D.kind == 1) {  // the penalty: one full transform along dims[0] on the flx sets
-            const double c = cnt[D.dims[0]][1][1];
-            fl += 2.0 * np * ipow(np, dim) * c;
-            pairs += c;
-            continue;
-        }
+    std::vector<std::pair<int, int>> ranges;
+    auto chunks = [&](int first, int total) {
+        for (int c0 = 0; c0 < total; c0 += op->chunk) ranges.push_back({first + c0, std::min(op->chunk, total - c0)});
+    };
+    const int nterms = int(op->terms.size());
+    if (op->kind == 1) {
+        const int G = int(op->sched_dims.size());
+        for (int f = 0; f <= dim; ++f) chunks(f * G, G);
+    } else {
+        chunks(0, op->n_pv_terms);
+    }
+    chunks(op->n_pv_terms, nterms - op->n_pv_terms);
+    for (const auto& r : ranges) {
+        SweepTree tree;
+        if (amdg_status s = sweep_tree(op, r.first, r.second, &tree, stream_of(op)); s != AMDG_OK) return s;
+        const bool pv = r.first < op->n_pv_terms;
         const int n_in = pv ? np : p1, n_out = pv ? p1 : np;
-        for (int j = 0; j < dim; ++j) {
-            const double c = cnt[D.dims[j]][D.flx[j]][D.lu[j]];
-            fl += 2.0 * n_in * ipow(n_out, j + 1) * ipow(n_in, dim - j - 1) * c;
-            pairs += c;
-        }
+        for (int j = 0; j < dim; ++j)
+            for (int k = 0; k < tree.count[j]; ++k) {
+                const PartialSum& D = op->nodes[size_t(tree.offset[j] + k)];
+                if (D.kind == 1) {  // the penalty: one full transform along dims[0] on the flx sets
+                    const double c = cnt[D.dims[0]][1][1];
+                    fl += 2.0 * np * ipow(np, dim) * c;
+                    pairs += c;
+                    continue;
+                }
+                const double c = cnt[D.dims[j]][D.flx[j]][D.lu[j]];
+                fl += 2.0 * n_in * ipow(n_out, j + 1) * ipow(n_in, dim - j - 1) * c;
+                pairs += c;
+            }
     }
     // hierarchical surplus passes (one field for Burgers, dim + 1 for the wave operator)
     fl += 2.0 * dim * double(E) * op->points * p1 * (op->kind == 1 ? dim + 1 : 1);
     if (flops) *flops = fl;
     if (transform_pairs) *transform_pairs = pairs;
+    return AMDG_OK;
+}
+
+amdg_status amdg_burgers_set_sweep_variant(amdg_burgers_op* op, int variant) {
+    AMDG_REQUIRE(op && (variant == 0 || variant == 1), AMDG_ERR_ARG, "variant must be 0 or 1");
+    op->sweep_variant = variant;
+    op->graph_version = -1;  // a captured step launched the other kernel
     return AMDG_OK;
 }
 
@@ -857,12 +947,8 @@ amdg_status amdg_lagr_rhs_add(amdg_burgers_op* op, int group, const double* alph
                 changed = true;
             }
         }
-        if (changed) {
-            AMDG_CK(cudaMemcpyAsync(op->d_terms, op->terms.data(), op->terms.size() * sizeof(PartialSum),
-                                    cudaMemcpyHostToDevice, st));
-            AMDG_CK(cudaStreamSynchronize(st));  // op->terms may change again before the copy runs
-            op->graph_version = -1;              // a captured step holds the old constants
-        }
+        if (changed)
+            if (amdg_status s = refresh_nodes(op, st); s != AMDG_OK) return s;
     }
     double* rhs = nullptr;
     if (amdg_status s = grid_rhs(g, &rhs); s != AMDG_OK) return s;

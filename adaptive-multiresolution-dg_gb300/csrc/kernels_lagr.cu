@@ -110,8 +110,8 @@ __global__ void __launch_bounds__(256) sweep_kernel(SweepArgs<T> a) {
         M = a.mats[D.mat[a.sweep]];
         n_from = a.n_in;
         n_to = a.n_out;
-        coef = from_double<T>(a.sweep == 0 ? D.coef : 1.0);
-        in = a.sweep == 0 ? a.src[D.src] : a.in + int64_t(slot) * a.in_slice;
+        coef = from_double<T>(D.coef);
+        in = a.sweep == 0 ? a.src[D.src] : a.in + int64_t(D.parent) * a.in_slice;
         // block shape: n_out along the dimensions already transformed, n_in elsewhere
         int done_after = 0;
         for (int j = 0; j < a.sweep; ++j) done_after += D.dims[j] > t ? 1 : 0;
@@ -203,8 +203,8 @@ __global__ void __launch_bounds__(256) sweep_col_kernel(SweepArgs<T> a) {
         flx = D.flx[a.sweep];
         M = a.mats[D.mat[a.sweep]];
         n_from = a.n_in;
-        coef = from_double<T>(a.sweep == 0 ? D.coef : 1.0);
-        in = a.sweep == 0 ? a.src[D.src] : a.in + int64_t(slot) * a.in_slice;
+        coef = from_double<T>(D.coef);
+        in = a.sweep == 0 ? a.src[D.src] : a.in + int64_t(D.parent) * a.in_slice;
         int done_after = 0;
         for (int j = 0; j < a.sweep; ++j) done_after += D.dims[j] > t ? 1 : 0;
         for (int d = 0; d < a.dim - 1 - t; ++d) stride *= d < done_after ? a.n_out : a.n_in;
@@ -263,7 +263,7 @@ cudaError_t launch_sweep(const SweepArgs<T>& a, cudaStream_t st) {
     const int nto = a.n_out;
     const int64_t cols = total / nto;
     const unsigned blocks = unsigned((cols + 255) / 256);
-    switch (a.out_block % nto == 0 ? nto : 0) {
+    switch (a.variant == 1 && a.out_block % nto == 0 ? nto : 0) {
         case 3: sweep_col_kernel<T, 3><<<blocks, 256, 0, st>>>(a); break;
         case 4: sweep_col_kernel<T, 4><<<blocks, 256, 0, st>>>(a); break;
         case 5: sweep_col_kernel<T, 5><<<blocks, 256, 0, st>>>(a); break;

@@ -10,28 +10,29 @@
 
 namespace amdg {
 
-// One sweep over a range of terms: thread per (term, element, output entry).
-// Sweep j of a kind-0 term reads its block shape from the dimensions already
-// transformed (n_out there, n_in elsewhere); sweep 0 reads the shared input,
-// later sweeps the term's own slice of `in`.  Kind-1 terms (only in the last
-// sweep) read pen_in with np entries per dimension.  Output: the term's slice
-// of `out`, overwritten (out[slot][e][idx]).
+// One sweep over the nodes of a sweep tree (desc[first .. first + count)): thread per (node,
+// element, output entry or column).  A kind-0 node of sweep j reads its block shape from the
+// dimensions already transformed (n_out there, n_in elsewhere); in sweep 0 it reads its source,
+// later its parent's slice of `in`, and it scales by its coef.  Kind-1 nodes (penalty terms,
+// only in the last sweep) read pen_in with np entries per dimension.  Output: the node's slice of
+// `out`, overwritten (out[slot][e][idx]).
 template <typename T>
 struct SweepArgs {
     int dim, sweep, n_in, n_out, np, n1;
     int64_t num_elements;
-    int first, count;              // terms [first, first + count) of desc
+    int first, count;              // nodes [first, first + count) of desc
     const PartialSum* desc;
     const T* mats[kNumLagrMats];   // [n1 * rows per element][n1 * cols per element]
     const int32_t *vol_ptr, *vol_split, *flx_ptr, *flx_split;
     const int2 *vol_nbr, *flx_nbr; // (element, 1D order along t)
     const int32_t* order;          // [element][dim]
-    const T* src[kMaxTermSources]; // sweep 0: term t reads src[t.src]
-    const T* in;                   // later sweeps: term slot s reads in + s * in_slice
+    const T* src[kMaxTermSources]; // sweep 0: node n reads src[n.src]
+    const T* in;                   // later sweeps: node n reads in + n.parent * in_slice
     int64_t in_slice;
     const T* pen_in;               // Alpert coefficients for kind-1 terms
     T* out;
     int out_block;                 // output entries per element (uniform over the range)
+    int variant;                   // 0: thread per output entry; 1: thread per column (sweep_col_kernel)
 };
 
 template <typename T>

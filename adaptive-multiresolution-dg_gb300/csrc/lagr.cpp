@@ -311,6 +311,55 @@ void build_lagr_tables(const Basis1D& alpt, int degree, LagrTables* t, bool diff
         for (int r = 0; r < P1; ++r) t->weight[p0 * P1 + r] = -lagr_mother(S, (S.pt1[p0] + 1.0) / 2.0, 0, r);
 }
 
+SweepTree build_sweep_tree(const std::vector<PartialSum>& terms, int first, int count, int dim,
+                           std::vector<PartialSum>* nodes) {
+    // A coefficient of a power of two commutes exactly with the linear sweeps (every rounding is
+    // scale-invariant), so such a term may apply it in its last sweep and share earlier ones.
+    auto pow2 = [](double c) {
+        int e = 0;
+        return c != 0.0 && std::frexp(std::fabs(c), &e) == 0.5;
+    };
+    SweepTree tree;
+    std::vector<std::vector<PartialSum>> level(dim);
+    std::vector<int> at(count, -1);  // node of each term at the current sweep
+    for (int j = 0; j + 1 < dim; ++j) {
+        for (int i = 0; i < count; ++i) {
+            const PartialSum& t = terms[size_t(first + i)];
+            if (t.kind != 0) continue;  // the penalty is a single (last) sweep
+            const bool share = pow2(t.coef);
+            PartialSum n = t;
+            n.parent = j == 0 ? -1 : at[i];
+            n.coef = (j == 0 && !share) ? t.coef : 1.0;
+            int found = -1;
+            for (size_t k = 0; share && k < level[j].size() && found < 0; ++k) {
+                const PartialSum& o = level[j][k];
+                bool same = o.parent == n.parent && o.coef == 1.0 && o.kind == 0 && (j > 0 || o.src == n.src);
+                for (int q = 0; same && q <= j; ++q)
+                    same = o.dims[q] == n.dims[q] && o.lu[q] == n.lu[q] && o.mat[q] == n.mat[q] && o.flx[q] == n.flx[q];
+                if (same) found = int(k);
+            }
+            if (found < 0) {  // a new node (an unshared term's nodes are never matched: their
+                found = int(level[j].size());  // first one carries a coefficient other than 1)
+                level[j].push_back(n);
+            }
+            at[i] = found;
+        }
+    }
+    for (int i = 0; i < count; ++i) {  // the last sweep: one node per term, in term order
+        const PartialSum& t = terms[size_t(first + i)];
+        PartialSum n = t;
+        n.parent = (t.kind != 0 || dim == 1) ? -1 : at[i];
+        n.coef = (t.kind != 0 || dim == 1 || pow2(t.coef)) ? t.coef : 1.0;
+        level[dim - 1].push_back(n);
+    }
+    for (int j = 0; j < dim; ++j) {
+        tree.offset[j] = int(nodes->size());
+        tree.count[j] = int(level[j].size());
+        nodes->insert(nodes->end(), level[j].begin(), level[j].end());
+    }
+    return tree;
+}
+
 void transform_schedule(int dim, std::vector<std::vector<int>>* dim_order, std::vector<std::vector<int>>* lu) {
     // 2^(dim-1) partial sums; sum s: dimension d gets tag 2*bit_d(s) for d < dim-1
     // and tag 1 for the last, then dimensions are ordered by tag

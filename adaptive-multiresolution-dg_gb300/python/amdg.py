@@ -140,6 +140,7 @@ def load():
         "amdg_ode_final": ([vp], i32),
         "amdg_lagr_interpolate": ([vp, i32], i32),
         "amdg_burgers_work": ([vp, C.POINTER(dbl), C.POINTER(dbl)], i32),
+        "amdg_burgers_set_sweep_variant": ([vp, i32], i32),
         "amdg_lagr_rhs_add": ([vp, i32, vp, i32], i32),
         "amdg_context_profile_read": ([vp, vp, vp], i32),
         "amdg_burgers_counters": ([vp, C.POINTER(i64), C.POINTER(i64)], i32),
@@ -558,6 +559,9 @@ class BurgersOperator:
         _ck(load().amdg_burgers_rhs(self._h, C.c_void_p(d_u), C.c_void_p(d_rhs), prec), "burgers_rhs")
 
     RHS_VOL, RHS_FLX, RHS_PENALTY = 0, 1, 2
+
+    def set_sweep_variant(self, variant: int):
+        _ck(load().amdg_burgers_set_sweep_variant(self._h, variant), "burgers_set_sweep_variant")
 
     def work(self):
         """(flops, neighbour pairs) of one right-hand side on the current element set."""

@@ -314,7 +314,8 @@ def run_ours(args):
     e2e_sec = max_over_ranks(sum(r["sec"] for r in e2e), world)
     # dominant work: one FP64 right-hand side on the final grid (CUDA events), against the
     # per-DOF-stage traffic of the Lagrange path (233 B: state, point values, surplus passes)
-    rhs_sec, rhs_dof, rhs_E = config3_rhs_timing(cfg, amdg.FP64)
+    rhs_sec, rhs_dof, rhs_E, rhs_flops = config3_rhs_timing(cfg, amdg.FP64)
+    rhs32_sec, _, _, _ = config3_rhs_timing(cfg, amdg.MIXED)
     pk, pk_kind = peaks()
     fp64_peak = fp64_peak_tflops(torch)
     ach = 233.0 * rhs_dof / rhs_sec / 1e9
@@ -344,8 +345,11 @@ def run_ours(args):
                      "kernel": "one FP64 right-hand side (point values, surplus passes, transforms, reduction) "
                                f"on the final grid ({rhs_E} elements, {rhs_dof} DOF)",
                      "kernel_ms": rhs_sec * 1e3, "algorithmic_bytes_per_launch": 233.0 * rhs_dof,
-                     "note": "L2-resident working set: the FP64 pipe (measured peak "
-                             f"{fp64_peak:.2f} TFLOP/s) binds, not HBM"},
+                     "algorithmic_flops": rhs_flops, "fp64_tflops": rhs_flops / rhs_sec / 1e12,
+                     "fp64_peak_tflops_measured": fp64_peak, "fp64_frac": rhs_flops / rhs_sec / 1e12 / fp64_peak,
+                     "mixed_rhs_ms": rhs32_sec * 1e3,
+                     "note": "L2-resident working set: the FP64 pipe binds, not HBM (fp64_frac against the "
+                             "measured float64 GEMM rate)"},
         "e2e": {"value": units / e2e_sec, "unit": "DOF-stage updates/s",
                 "h2d_bytes_per_step": 8 * 22464, "d2h_bytes_per_step": 8 * e2e[-1]["dof_final"],
                 "call": "amdg_grid_set_coefficients from pinned host memory, 36 amdg_burgers_adaptive_step calls, "
@@ -457,13 +461,15 @@ class Config3:
         g.init_separable_adaptive(O.burgers_ic_terms(c["dim"]), c["eps"])
         return g, amdg.BurgersOperator(g, c["alpha"])
 
-    def run(self, prec, mlp=None, horizon=0, keep=False, host_io=None, t_end=None):
+    def run(self, prec, mlp=None, horizon=0, keep=False, host_io=None, t_end=None, eps=None):
         """horizon 0: the plain adaptive step; horizon >= 1: one pre-adaptation (classifier `mlp`, or
         the criterion alone when mlp is None) then `horizon` steps.  host_io = (pinned input,
         pinned output): the state is copied in from host memory at the start of the timed region
         and out at its end (the end-to-end form)."""
-        torch, ctx, c = self.torch, self.ctx, CONFIG3
-        g, op = self.make()
+        torch, ctx, c = self.torch, self.ctx, dict(CONFIG3)
+        g, op = self.make()  # the initial grid is the workload's (refine 1e-5)
+        if eps is not None:  # the adaptivity of the run itself
+            c["eps"], c["eta"] = eps, eps / 10.0
         t_end = c["T"] if t_end is None else t_end
         if host_io is not None:
             host_io[0][:g.dof] = g.coefficients().reshape(-1)
@@ -533,15 +539,16 @@ def config3_rhs_timing(cfg, prec, reps=20):
     ev1.synchronize()
     sec = ev0.elapsed_time(ev1) / 1e3 / reps
     dof, E = g.dof, g.num_elements
+    flops, pairs = op.work()
     op.close()
     g.close()
-    return sec, dof, E
+    return sec, dof, E, flops
 
 
-def train_config3_classifier(cfg, args, horizon):
-    """The classifier of the learned arm, trained on the decisions of plain FP64 runs of other seeded
-    waves a + b sin(2 pi (x+y+z+c)) (horizon labels: refine where the criterion refines the element
-    within the next `horizon` steps)."""
+def train_config3_classifier(cfg, args, horizon, eps):
+    """The classifier of a learned arm, trained on the decisions of plain FP64 runs (refine eps,
+    coarsen eps/10) of other seeded waves a + b sin(2 pi (x+y+z+c)) (horizon labels: refine where
+    the criterion refines the element within the next `horizon` steps)."""
     import torch
 
     import amdg
@@ -565,7 +572,7 @@ def train_config3_classifier(cfg, args, horizon):
             ctx.synchronize()
             feats.append(buf.cpu().numpy().reshape(-1, F))
             keys_steps.append(element_keys(g))
-            _dt, dec = op.adaptive_step_ex(c["cfl"], a + b, c["eps"], c["eta"])
+            _dt, dec = op.adaptive_step_ex(c["cfl"], a + b, eps, eps / 10.0)
             dec_steps.append(np.asarray(dec))
         labs.extend(horizon_labels(keys_steps, dec_steps, horizon))
         op.close()
@@ -578,28 +585,27 @@ def train_config3_classifier(cfg, args, horizon):
     t0 = time.perf_counter()
     loss = mlp.train_device(dx.data_ptr(), dy.data_ptr(), len(y), epochs=args.learn_epochs, batch=256, lr=2e-3,
                             seed=12)
-    info = {"runs": args.learn_runs, "steps_per_run": args.learn_steps, "horizon": horizon, "samples": int(len(y)),
-            "class_counts": [int((y == i).sum()) for i in range(3)], "epochs": args.learn_epochs,
-            "final_loss": loss, "collect_s": collect_s, "train_s": time.perf_counter() - t0}
+    info = {"runs": args.learn_runs, "steps_per_run": args.learn_steps, "horizon": horizon, "refine_eps": eps,
+            "samples": int(len(y)), "class_counts": [int((y == i).sum()) for i in range(3)],
+            "epochs": args.learn_epochs, "final_loss": loss, "collect_s": collect_s,
+            "train_s": time.perf_counter() - t0}
     return mlp, info
 
 
 def bench_config3_arms(cfg, args, plain):
     """The metric itself: wall time to T of mixed precision with learned adaptivity against the plain
-    FP64 path, at matched error (final L2 error against the exact solution within 10 % of the plain
-    path's), beside mixed precision without the network (plain loop, and the criterion alone
-    pre-adapting over the same horizon: what the network itself gains)."""
+    FP64 path at matched error (final L2 error against the exact solution within 10 % of the plain
+    path's).  Arms with a pre-adaptation over a horizon (classifier, or the surplus criterion alone:
+    what the network itself gains) run at refine thresholds eps = s x 1e-5 (coarsen eps/10), the
+    classifier trained at the same eps; a learned arm counts for the metric only at matched error."""
     import amdg
-    H = args.learn_horizon
-    mlp, training = train_config3_classifier(cfg, args, H)
-    out = {"training": training, "plain_fp64": plain}
-    arms = [("mixed_plain", amdg.MIXED, None, 0)]
-    for h in sorted({H, 8}):
-        arms += [(f"mixed_learned_h{h}", amdg.MIXED, mlp, h), (f"mixed_criterion_h{h}", amdg.MIXED, None, h)]
-    arms += [("fp64_learned_h%d" % H, amdg.FP64, mlp, H)]
-    for name, prec, net, h in arms:
-        cfg.run(prec, mlp=net, horizon=h, t_end=4 * CONFIG3["cfl"] / (CONFIG3["umax"] * 3 * 32))  # warm-up
-        runs = [cfg.run(prec, mlp=net, horizon=h, keep=(i == 0)) for i in range(args.arm_runs)]
+    out = {"plain_fp64": plain}
+    ref_err = plain["error_vs_exact_l1_l2_linf"][1]
+
+    def measure(prec, net, h, eps):
+        t_short = 4 * CONFIG3["cfl"] / (CONFIG3["umax"] * 3 * 32)
+        cfg.run(prec, mlp=net, horizon=h, t_end=t_short, eps=eps)  # warm-up
+        runs = [cfg.run(prec, mlp=net, horizon=h, keep=(i == 0), eps=eps) for i in range(args.arm_runs)]
         r = runs[0]
         g, op = r.pop("_grid"), r.pop("_op")
         op.close()
@@ -608,15 +614,31 @@ def bench_config3_arms(cfg, args, plain):
         r["sec"] = secs[len(secs) // 2]
         r["sec_runs"] = secs
         r["value"] = r["stage_dof_updates"] / r["sec"]
-        r["horizon"] = h
-        r["error_ratio_vs_plain_fp64"] = r["error_vs_exact_l1_l2_linf"][1] / plain["error_vs_exact_l1_l2_linf"][1]
+        r["horizon"], r["refine_eps"] = h, eps
+        r["error_ratio_vs_plain_fp64"] = r["error_vs_exact_l1_l2_linf"][1] / ref_err
         r["wall_speedup_vs_plain_fp64"] = plain["sec"] / r["sec"]
         r["dof_stage_speedup_vs_plain_fp64"] = r["value"] / plain["value"]
         r["matched_error"] = bool(0.9 <= r["error_ratio_vs_plain_fp64"] <= 1.1)
-        out[name] = r
-    mlp.close()
+        return r
+
+    out["mixed_plain"] = measure(amdg.MIXED, None, 0, None)
+    trainings = []
+    for h in args.arm_horizons:
+        for scale in args.eps_scales:
+            eps = 1e-5 * scale
+            mlp, info = train_config3_classifier(cfg, args, h, eps)
+            trainings.append(info)
+            out[f"mixed_learned_h{h}_s{scale:g}"] = measure(amdg.MIXED, mlp, h, eps)
+            out[f"mixed_criterion_h{h}_s{scale:g}"] = measure(amdg.MIXED, None, h, eps)
+            mlp.close()
+    out["training"] = trainings
     learned = [k for k in out if k.startswith("mixed_learned") and out[k]["matched_error"]]
     best = max(learned, key=lambda k: out[k]["wall_speedup_vs_plain_fp64"]) if learned else None
+    gain = {}
+    for k in out:
+        if k.startswith("mixed_learned"):
+            crit = k.replace("learned", "criterion")
+            gain[k] = out[crit]["sec"] / out[k]["sec"]
     out["metric"] = {
         "definition": "wall time to T = 0.05 of the plain FP64 path over that of mixed precision + learned "
                       "adaptivity, counting only arms whose final L2 error vs exact is within 10 % of the plain "
@@ -624,8 +646,8 @@ def bench_config3_arms(cfg, args, plain):
         "best_matched_arm": best,
         "wall_speedup": out[best]["wall_speedup_vs_plain_fp64"] if best else None,
         "dof_stage_speedup": out[best]["dof_stage_speedup_vs_plain_fp64"] if best else None,
-        "network_gain_vs_criterion_same_horizon": {
-            f"h{h}": out[f"mixed_criterion_h{h}"]["sec"] / out[f"mixed_learned_h{h}"]["sec"] for h in sorted({H, 8})},
+        "error_ratio": out[best]["error_ratio_vs_plain_fp64"] if best else None,
+        "network_gain_vs_criterion_same_horizon_and_eps": gain,
     }
     return out
 
@@ -1033,6 +1055,73 @@ def profile_wave_rhs():
     g.close()
 
 
+def profile_config3():
+    """Profiling case (not a bench line): one plain FP64 and one mixed run of the 3D adaptive Burgers
+    workload after a warm-up run each, between cudaProfilerStart / cudaProfilerStop, for
+    ncu --profile-from-start off."""
+    import torch
+
+    import amdg
+    torch.cuda.set_device(0)
+    ctx = amdg.Context(0)
+    stream = torch.cuda.Stream()
+    torch.cuda.set_stream(stream)
+    ctx.set_stream(stream.cuda_stream)
+    cfg = Config3(ctx, stream)
+    for prec in (amdg.FP64, amdg.MIXED):
+        cfg.run(prec)
+    torch.cuda.synchronize()
+    torch.cuda.cudart().cudaProfilerStart()
+    for prec in (amdg.FP64, amdg.MIXED):
+        r = cfg.run(prec)
+        print(json.dumps({"prec": int(prec), "ms": r["sec"] * 1e3, "launches": r["launches"]}), flush=True)
+    torch.cuda.cudart().cudaProfilerStop()
+
+
+def profile_rhs3d():
+    """Profiling case (not a bench line): the 3D Burgers right-hand side on the sparse grid N=8
+    (4096 elements), FP64 and mixed, with each transform-sweep kernel variant; times by CUDA
+    events, then one right-hand side per (variant, precision) between cudaProfilerStart / Stop."""
+    import torch
+
+    import amdg
+    import amdg_oracle as O
+    torch.cuda.set_device(0)
+    ctx = amdg.Context(0)
+    stream = torch.cuda.Stream()
+    torch.cuda.set_stream(stream)
+    ctx.set_stream(stream.cuda_stream)
+    g = amdg.Grid(ctx, 3, 8, 2)
+    g.init_separable(O.burgers_ic_terms(3))
+    op = amdg.BurgersOperator(g, 0.825)
+    du = torch.from_numpy(g.coefficients().reshape(-1).copy()).cuda()
+    out = torch.zeros_like(du)
+    torch.cuda.synchronize()
+    flops, _ = op.work()
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    for variant in (0, 1):
+        op.set_sweep_variant(variant)
+        for prec in (amdg.FP64, amdg.MIXED):
+            op.rhs_device(du.data_ptr(), out.data_ptr(), prec)
+            ev0.record(stream)
+            for _ in range(10):
+                op.rhs_device(du.data_ptr(), out.data_ptr(), prec)
+            ev1.record(stream)
+            ev1.synchronize()
+            ms = ev0.elapsed_time(ev1) / 10
+            print(json.dumps({"variant": variant, "prec": int(prec), "rhs_ms": ms, "elements": g.num_elements,
+                              "flops": flops, "tflops": flops / ms / 1e9}), flush=True)
+    torch.cuda.cudart().cudaProfilerStart()
+    for variant in (0, 1):
+        op.set_sweep_variant(variant)
+        for prec in (amdg.FP64, amdg.MIXED):
+            op.rhs_device(du.data_ptr(), out.data_ptr(), prec)
+    torch.cuda.synchronize()
+    torch.cuda.cudart().cudaProfilerStop()
+    op.close()
+    g.close()
+
+
 def cpu_baseline(g, u0, budget_s=15.0):
     """Oracle (port of the reference algorithm) on the host cores: one RHS
     evaluation over a bounded, contiguous sample of elements of the same grid,
@@ -1169,6 +1258,10 @@ def main():
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--cpu-steps", type=int, default=4, help="time steps of the reference loop in cpu_baseline")
     ap.add_argument("--arm-runs", type=int, default=3, help="timed runs per arm of the 3D adaptive Burgers metric")
+    ap.add_argument("--arm-horizons", type=int, nargs="+", default=[4, 8],
+                    help="horizons of the pre-adapted arms of the 3D adaptive Burgers metric")
+    ap.add_argument("--eps-scales", type=float, nargs="+", default=[1, 4, 8, 16],
+                    help="refine thresholds of the pre-adapted arms, in units of 1e-5")
     ap.add_argument("--batch-solves", type=int, default=256)
     ap.add_argument("--batch-eps", type=float, default=1e-5)
     ap.add_argument("--batch-adapt-every", type=int, default=20,
@@ -1184,13 +1277,17 @@ def main():
     ap.add_argument("--wave-learn-steps", type=int, default=30)
     ap.add_argument("--wave-train-samples", type=int, default=300000, help="training samples kept (stratified)")
     ap.add_argument("--wave-learn-horizon", type=int, default=2, help="time steps per learned pre-adaptation (wave)")
-    ap.add_argument("--profile", choices=["none", "wave_rhs"], default="none",
+    ap.add_argument("--profile", choices=["none", "wave_rhs", "config3", "rhs3d"], default="none",
                     help="wave_rhs: run the wave right-hand-side profiling case instead of the bench")
     ap.add_argument("--wave-time", type=float, default=0.05,
                     help="final time of the 2D wave runs (the config's 0.5 takes ~5000 steps on a filling grid)")
     args = ap.parse_args()
     if args.profile == "wave_rhs":
         profile_wave_rhs()
+    elif args.profile == "config3":
+        profile_config3()
+    elif args.profile == "rhs3d":
+        profile_rhs3d()
     elif args.impl == "reference":
         run_reference(args)
     else:

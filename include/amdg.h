@@ -373,10 +373,14 @@ amdg_status amdg_burgers_rk3_steps(amdg_burgers_op* op, double dt, int nsteps, a
  * constants, NULL keeps them.  vol + flx + penalty added in that order equal amdg_burgers_rhs. */
 enum { AMDG_LAGR_RHS_VOL = 0, AMDG_LAGR_RHS_FLX = 1, AMDG_LAGR_RHS_PENALTY = 2 };
 /* Algorithmic work of one right-hand side on the current element set (no reference counterpart):
- * the multiply-adds of every 1D transform sweep of every term (2 flops each, from the neighbour
- * lists' L / full / U counts) plus the surplus passes, and the (element, neighbour) pairs the
- * sweeps visit.  Reads the lists back (synchronises): for measurement, not for the step loop. */
+ * the multiply-adds of every 1D transform sweep the right-hand side runs (2 flops each, from the
+ * neighbour lists' L / full / U counts; terms whose first sweeps coincide share them) plus the
+ * surplus passes, and the (element, neighbour) pairs the sweeps visit.  Reads the lists back (synchronises): for measurement, not for the step loop. */
 amdg_status amdg_burgers_work(amdg_burgers_op* op, double* flops, double* transform_pairs);
+/* Kernel of the transform sweeps (no reference counterpart): 0 (default) one thread per output
+ * entry; 1 one thread per column of the transformed dimension, all its entries from one load of
+ * each input value.  Both sum every output in the same order (identical results). */
+amdg_status amdg_burgers_set_sweep_variant(amdg_burgers_op* op, int variant);
 amdg_status amdg_lagr_interpolate(amdg_burgers_op* op, amdg_precision prec);
 amdg_status amdg_lagr_rhs_add(amdg_burgers_op* op, int group, const double* alpha, amdg_precision prec);
 
