@@ -30,6 +30,7 @@
 
 #include "amdg_internal.hpp"
 #include "kernels.cuh"
+#include "device_alloc.cuh"
 
 using namespace amdg;
 
@@ -67,7 +68,7 @@ amdg_status grow(T** p, int64_t* cap, int64_t need, int64_t want) {
     cudaFree(*p);
     *p = nullptr;
     *cap = 0;
-    if (cudaMalloc(reinterpret_cast<void**>(p), size_t(want) * sizeof(T)) != cudaSuccess) {
+    if (amdg::device_malloc(reinterpret_cast<void**>(p), size_t(want) * sizeof(T)) != cudaSuccess) {
         *p = nullptr;
         return fail(AMDG_ERR_NOMEM, "cudaMalloc failed (device adaptivity buffers)");
     }
@@ -81,7 +82,7 @@ amdg_status grow_temp(GridDevice& d, size_t bytes) {
     d.temp = nullptr;
     d.temp_bytes = 0;
     const size_t want = bytes + bytes / 2 + 4096;
-    if (cudaMalloc(&d.temp, want) != cudaSuccess) {
+    if (amdg::device_malloc(&d.temp, want) != cudaSuccess) {
         d.temp = nullptr;
         return fail(AMDG_ERR_NOMEM, "cudaMalloc failed (sort / scan scratch)");
     }
@@ -90,14 +91,14 @@ amdg_status grow_temp(GridDevice& d, size_t bytes) {
 }
 
 amdg_status ensure_stats(GridDevice& d) {
-    if (d.stats) return AMDG_OK;
-    if (cudaMalloc(&d.stats, sizeof(AdaptStats)) != cudaSuccess) {
-        d.stats = nullptr;
-        return fail(AMDG_ERR_NOMEM, "cudaMalloc failed (adaptivity statistics)");
-    }
-    if (cudaMallocHost(&d.host_stats, sizeof(AdaptStats)) != cudaSuccess) {
+    if (d.stats && d.host_stats) return AMDG_OK;
+    if (!d.host_stats && cudaMallocHost(&d.host_stats, sizeof(AdaptStats)) != cudaSuccess) {
         d.host_stats = nullptr;
         return fail(AMDG_ERR_NOMEM, "cudaMallocHost failed (adaptivity statistics)");
+    }
+    if (!d.stats && amdg::device_malloc(&d.stats, sizeof(AdaptStats)) != cudaSuccess) {
+        d.stats = nullptr;
+        return fail(AMDG_ERR_NOMEM, "cudaMalloc failed (adaptivity statistics)");
     }
     // every field starts at zero (the error flags are only ever set, and cleared when reported)
     if (cudaMemset(d.stats, 0, sizeof(AdaptStats)) != cudaSuccess)
@@ -676,8 +677,8 @@ amdg_status ensure_flags(amdg_grid* g, int64_t E) {
     d.pos = nullptr;
     d.flag_cap = 0;
     const int64_t want = E + E / 2 + 64;
-    if (cudaMalloc(&d.flag, size_t(want)) != cudaSuccess || cudaMalloc(&d.force, size_t(want)) != cudaSuccess ||
-        cudaMalloc(&d.pos, size_t(want) * sizeof(int32_t)) != cudaSuccess)
+    if (amdg::device_malloc(&d.flag, size_t(want)) != cudaSuccess || amdg::device_malloc(&d.force, size_t(want)) != cudaSuccess ||
+        amdg::device_malloc(&d.pos, size_t(want) * sizeof(int32_t)) != cudaSuccess)
         return fail(AMDG_ERR_NOMEM, "cudaMalloc failed (adaptivity flags)");
     d.flag_cap = want;
     return AMDG_OK;
@@ -713,8 +714,8 @@ static amdg_status ensure_keys(amdg_grid* g, int64_t E, bool preserve) {
     if (E <= d.key_cap && d.key && d.key_alt) return AMDG_OK;
     const int64_t want = std::max<int64_t>(E + E / 4 + 16, d.key_cap);
     uint64_t *k = nullptr, *a = nullptr;
-    if (cudaMalloc(&k, size_t(want) * sizeof(uint64_t)) != cudaSuccess ||
-        cudaMalloc(&a, size_t(want) * sizeof(uint64_t)) != cudaSuccess) {
+    if (amdg::device_malloc(&k, size_t(want) * sizeof(uint64_t)) != cudaSuccess ||
+        amdg::device_malloc(&a, size_t(want) * sizeof(uint64_t)) != cudaSuccess) {
         cudaFree(k);
         return fail(AMDG_ERR_NOMEM, "cudaMalloc failed (element keys)");
     }
@@ -773,8 +774,8 @@ amdg_status grid_hash(amdg_grid* g) {
         int bits = 6;
         while ((int64_t(1) << bits) < need + need / 2) ++bits;
         const int64_t cap = int64_t(1) << bits;
-        if (cudaMalloc(&d.hkey, size_t(cap) * sizeof(unsigned long long)) != cudaSuccess ||
-            cudaMalloc(&d.hval, size_t(cap) * sizeof(int32_t)) != cudaSuccess)
+        if (amdg::device_malloc(&d.hkey, size_t(cap) * sizeof(unsigned long long)) != cudaSuccess ||
+            amdg::device_malloc(&d.hval, size_t(cap) * sizeof(int32_t)) != cudaSuccess)
             return fail(AMDG_ERR_NOMEM, "cudaMalloc failed (element hash)");
         d.hcap = cap;
         d.hbits = bits;
@@ -799,7 +800,7 @@ amdg_status grid_device_norms(amdg_grid* g, const double* d_u, const double* d_u
         g->d_norms = nullptr;
         g->norms_capacity = 0;
         const int64_t cap = E + E / 4 + 16;
-        if (cudaMalloc(reinterpret_cast<void**>(&g->d_norms), size_t(cap) * sizeof(double)) != cudaSuccess)
+        if (amdg::device_malloc(reinterpret_cast<void**>(&g->d_norms), size_t(cap) * sizeof(double)) != cudaSuccess)
             return fail(AMDG_ERR_NOMEM, "cudaMalloc failed (indicators)");
         g->norms_capacity = cap;
     }
@@ -814,31 +815,37 @@ amdg_status grid_device_norms(amdg_grid* g, const double* d_u, const double* d_u
     return AMDG_OK;
 }
 
-amdg_status grid_apply_remap(amdg_grid* g, int64_t E) {
-    cudaStream_t st = stream_of(g);
+amdg_status grid_reserve_remap(amdg_grid* g, int64_t E) {
     const int64_t grown = E + E / 4 + 16;
     auto regrow = [&](double** p, int64_t* cap) -> amdg_status {
         if (E <= *cap) return AMDG_OK;
         cudaFree(*p);
         *p = nullptr;
         *cap = 0;
-        if (cudaMalloc(reinterpret_cast<void**>(p), size_t(grown) * g->block * sizeof(double)) != cudaSuccess)
+        if (amdg::device_malloc(reinterpret_cast<void**>(p), size_t(grown) * g->block * sizeof(double)) != cudaSuccess)
             return fail(AMDG_ERR_NOMEM, "cudaMalloc failed (coefficient remap)");
         *cap = grown;
         return AMDG_OK;
     };
-    if (amdg_status s = regrow(&g->d_u_spare, &g->spare_capacity); s != AMDG_OK) return s;
+    amdg_status s;
+    if ((s = regrow(&g->d_u_spare, &g->spare_capacity)) != AMDG_OK) return s;
+    if (g->d_v && (s = regrow(&g->d_v_spare, &g->v_spare_capacity)) != AMDG_OK) return s;
+    if (g->d_pred && (s = regrow(&g->d_pred_spare, &g->pred_spare_capacity)) != AMDG_OK) return s;
+    return AMDG_OK;
+}
+
+amdg_status grid_apply_remap(amdg_grid* g, int64_t E) {
+    cudaStream_t st = stream_of(g);
+    if (amdg_status s = grid_reserve_remap(g, E); s != AMDG_OK) return s;
     AMDG_CK(launch_remap(g->d_u, g->d_map, g->block, E, g->d_u_spare, st));
     g->ctx->launches++;
     if (g->d_v) {
-        if (amdg_status s = regrow(&g->d_v_spare, &g->v_spare_capacity); s != AMDG_OK) return s;
         AMDG_CK(launch_remap(g->d_v, g->d_map, g->block, E, g->d_v_spare, st));
         g->ctx->launches++;
         std::swap(g->d_v, g->d_v_spare);
         std::swap(g->v_capacity, g->v_spare_capacity);
     }
     if (g->d_pred) {
-        if (amdg_status s = regrow(&g->d_pred_spare, &g->pred_spare_capacity); s != AMDG_OK) return s;
         AMDG_CK(launch_remap(g->d_pred, g->d_map, g->block, E, g->d_pred_spare, st));
         g->ctx->launches++;
         std::swap(g->d_pred, g->d_pred_spare);
@@ -859,16 +866,20 @@ static amdg_status ensure_set_arrays(amdg_grid* g, int64_t E) {
         cudaFree(g->d_map);
         g->d_map = nullptr;
         g->map_capacity = 0;
-        if (cudaMalloc(reinterpret_cast<void**>(&g->d_map), size_t(grown) * sizeof(int32_t)) != cudaSuccess)
+        if (amdg::device_malloc(reinterpret_cast<void**>(&g->d_map), size_t(grown) * sizeof(int32_t)) != cudaSuccess)
             return fail(AMDG_ERR_NOMEM, "cudaMalloc failed (element map)");
         g->map_capacity = grown;
     }
-    if (E > g->order_capacity) {
-        cudaFree(g->d_order);
-        g->d_order = nullptr;
-        g->order_capacity = 0;
-        if (cudaMalloc(reinterpret_cast<void**>(&g->d_order), size_t(grown) * g->host.dim * sizeof(int32_t)) != cudaSuccess)
+    if (E > g->order_capacity) {  // the current set's orders move along (a failure later leaves them intact)
+        int32_t* p = nullptr;
+        if (amdg::device_malloc(&p, size_t(grown) * g->host.dim * sizeof(int32_t)) != cudaSuccess)
             return fail(AMDG_ERR_NOMEM, "cudaMalloc failed (element orders)");
+        const int64_t n = g->host.num_elements * g->host.dim;
+        cudaStream_t st = stream_of(g);
+        if (n > 0) AMDG_CK(cudaMemcpyAsync(p, g->d_order, size_t(n) * sizeof(int32_t), cudaMemcpyDeviceToDevice, st));
+        AMDG_CK(cudaStreamSynchronize(st));
+        cudaFree(g->d_order);
+        g->d_order = p;
         g->order_capacity = grown;
     }
     return AMDG_OK;
@@ -908,15 +919,18 @@ amdg_status grid_device_refine(amdg_grid* g, double eps, const uint8_t* d_force,
     if (n_new == 0) return AMDG_OK;
     const int64_t En = E + n_new;
     if (En > (int64_t(1) << 31) - 1) return fail(AMDG_ERR_CAPACITY, "more than 2^31-1 elements");
-    if ((s = ensure_keys(g, En, true)) != AMDG_OK || (s = ensure_set_arrays(g, En)) != AMDG_OK) return s;
+    // every allocation before the first change, so a failure leaves the element set as it was
+    if ((s = ensure_keys(g, En, true)) != AMDG_OK || (s = ensure_set_arrays(g, En)) != AMDG_OK ||
+        (s = grid_reserve_remap(g, En)) != AMDG_OK)
+        return s;
+    size_t temp = 0;
+    AMDG_CK(cub::DeviceRadixSort::SortKeys(nullptr, temp, d.key_alt, d.key, int(En), 0, ks.dim * ks.nmax, st));
+    if ((s = grow_temp(d, temp)) != AMDG_OK) return s;
     // old and new keys side by side in key_alt, then sorted into key (keys use dim * nmax bits);
     // the old keys are not needed again: the map comes from the old set's hash
     concat_keys_kernel<<<blocks_for(En, 256), 256, 0, st>>>(d.key, E, d.newk, n_new, d.key_alt);
     AMDG_CK(cudaGetLastError());
     const int bits = ks.dim * ks.nmax;
-    size_t temp = 0;
-    AMDG_CK(cub::DeviceRadixSort::SortKeys(nullptr, temp, d.key_alt, d.key, int(En), 0, bits, st));
-    if ((s = grow_temp(d, temp)) != AMDG_OK) return s;
     size_t tb = d.temp_bytes;
     AMDG_CK(cub::DeviceRadixSort::SortKeys(d.temp, tb, d.key_alt, d.key, int(En), 0, bits, st));
     map_from_hash_kernel<<<blocks_for(En, 256), 256, 0, st>>>(d.key, En, ks, hash_of(g), g->d_map, g->d_order);
@@ -972,7 +986,9 @@ amdg_status grid_device_coarsen(amdg_grid* g, double eta, double missed_eps, int
     if (missed_eps > 0) d.n_missed = std::min<int64_t>(hs.missed, d.missed_cap);
     if (removed_out) *removed_out = E - En;
     if (En == E) return AMDG_OK;
-    if ((s = ensure_keys(g, En, true)) != AMDG_OK || (s = ensure_set_arrays(g, En)) != AMDG_OK) return s;
+    if ((s = ensure_keys(g, En, true)) != AMDG_OK || (s = ensure_set_arrays(g, En)) != AMDG_OK ||
+        (s = grid_reserve_remap(g, En)) != AMDG_OK)
+        return s;
     compact_kernel<<<blocks_for(E, 256), 256, 0, st>>>(d.key, E, ks, d.flag, d.pos, d.key_alt, g->d_map, g->d_order);
     AMDG_CK(cudaGetLastError());
     g->ctx->launches++;

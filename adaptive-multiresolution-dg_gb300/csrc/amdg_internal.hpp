@@ -378,6 +378,7 @@ struct amdg_linear_op {
     float* d_shadow = nullptr;       // mixed mode: hi parts of u, u1, u2 (3 x capacity)
     float* d_lo = nullptr;           // mixed mode: lo parts of u, u1, u2 (3 x capacity)
     int* d_err = nullptr;            // set by a bounded copy wait that gave up (variant 2)
+    uint32_t wait_limit = 1u << 22;  // polls of a bulk-copy wait before it gives up
     int variant[2] = {0, 0};         // kernel variant per precision, picked by the autotuner
     float variant_ms[2][3] = {{0, 0, 0}, {0, 0, 0}};  // measured stage time [precision][variant]
     int tma_cfg = 0;                 // configuration of the bulk-copy variant (ring depth, operator-block source)
@@ -513,6 +514,8 @@ amdg_status grid_check_topology(amdg_grid* g);
 // the element-set change of a remap: grow the spare arrays for E_new elements and move u (and v)
 // through g->d_map (new -> old, -1 new element); bumps the version
 amdg_status grid_apply_remap(amdg_grid* g, int64_t E_new);
+// the spare arrays of that remap, allocated ahead of any change
+amdg_status grid_reserve_remap(amdg_grid* g, int64_t E_new);
 // device neighbour lists of the fast transforms and surplus ancestors for the current element set
 struct DeviceTopoOut {
     int32_t *vol_ptr, *vol_nbr, *vol_split, *flx_ptr, *flx_nbr, *flx_split, *anc;

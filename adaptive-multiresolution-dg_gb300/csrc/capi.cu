@@ -5,6 +5,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <atomic>
 #include <chrono>
 #include <cmath>
 #include <unordered_map>
@@ -16,8 +17,24 @@
 #include "amdg.h"
 #include "amdg_internal.hpp"
 #include "kernels.cuh"
+#include "device_alloc.cuh"
 
 namespace amdg {
+
+// test hook of amdg_debug_fail_device_allocations: allocations left before one fails (-1: none)
+static std::atomic<int64_t> g_fail_after{-1};
+
+cudaError_t device_malloc_raw(void** p, size_t bytes) {
+    int64_t left = g_fail_after.load();
+    while (left >= 0) {
+        if (left == 0) {
+            *p = nullptr;
+            return cudaErrorMemoryAllocation;
+        }
+        if (g_fail_after.compare_exchange_weak(left, left - 1)) break;
+    }
+    return cudaMalloc(p, bytes);
+}
 
 static thread_local std::string g_last_error;
 
@@ -52,7 +69,7 @@ template <class T>
 amdg_status dev_alloc(T** p, size_t count) {
     *p = nullptr;
     if (count == 0) return AMDG_OK;
-    cudaError_t e = cudaMalloc(reinterpret_cast<void**>(p), count * sizeof(T));
+    cudaError_t e = amdg::device_malloc(reinterpret_cast<void**>(p), count * sizeof(T));
     if (e != cudaSuccess) return fail(AMDG_ERR_NOMEM, std::string("cudaMalloc: ") + cudaGetErrorString(e));
     return AMDG_OK;
 }
@@ -134,18 +151,20 @@ amdg_status grid_set_keys(amdg_grid* g, std::vector<uint64_t> keys, const std::v
     const int64_t E = ng.num_elements;
     const int64_t grown = E + E / 4 + 16;
     amdg_status s;
+    // every allocation before the first change, so a failure leaves the element set as it was
+    if ((s = grid_reserve_remap(g, E)) != AMDG_OK) return s;
     if (E > g->map_capacity) {
-        cudaFree(g->d_map);
+        cudaFree(g->d_map);  // scratch: no contents to keep
         g->d_map = nullptr;
         g->map_capacity = 0;
         if ((s = dev_alloc(&g->d_map, size_t(grown))) != AMDG_OK) return s;
         g->map_capacity = grown;
     }
     if (E > g->order_capacity) {
+        int32_t* p = nullptr;
+        if ((s = dev_alloc(&p, size_t(grown) * g->host.dim)) != AMDG_OK) return s;
         cudaFree(g->d_order);
-        g->d_order = nullptr;
-        g->order_capacity = 0;
-        if ((s = dev_alloc(&g->d_order, size_t(grown) * g->host.dim)) != AMDG_OK) return s;
+        g->d_order = p;
         g->order_capacity = grown;
     }
     if (E > 0) AMDG_CK(cudaMemcpyAsync(g->d_map, map.data(), size_t(E) * sizeof(int32_t), cudaMemcpyHostToDevice, st));
@@ -240,6 +259,7 @@ LinearLaunch linear_launch(const amdg_linear_op* op, amdg_precision prec = AMDG_
     L.blocks64p = op->d_blocks64p;
     L.blocks32p = op->d_blocks32p;
     L.err = op->d_err;
+    L.wait_limit = op->wait_limit;
     L.tma_cfg = op->tma_cfg;
     return L;
 }
@@ -290,9 +310,12 @@ amdg_status rk3_steps_device(amdg_linear_op* op, double dt, int nsteps, amdg_pre
                 g->ctx->launches++;
             }
         }
+        // a copy wait that gave up leaves the state as it was: the merge runs only after the check
+        if (L.variant == 2 && check)
+            if (amdg_status s = check_copy_waits(op); s != AMDG_OK) return s;
         AMDG_CK(launch_merge(hi[0], lo[0], u, g->dof, st));
         g->ctx->launches++;
-        return L.variant == 2 && check ? check_copy_waits(op) : AMDG_OK;
+        return AMDG_OK;
     }
     for (int s = 0; s < nsteps; ++s) {
         // u1 = u + dt L(u); u2 = 3/4 u + 1/4 (u1 + dt L(u1)); u = 1/3 u + 2/3 (u2 + dt L(u2))
@@ -508,6 +531,12 @@ amdg_status amdg_context_synchronize(amdg_context* ctx) {
 amdg_status amdg_context_launch_count(amdg_context* ctx, int64_t* count) {
     AMDG_REQUIRE(ctx && count, AMDG_ERR_ARG, "null argument");
     *count = ctx->launches;
+    return AMDG_OK;
+}
+
+amdg_status amdg_debug_fail_device_allocations(int64_t after) {
+    AMDG_REQUIRE(after >= -1, AMDG_ERR_ARG, "after must be -1 or more");
+    g_fail_after.store(after);
     return AMDG_OK;
 }
 
@@ -984,6 +1013,12 @@ amdg_status amdg_linear_set_copy_config(amdg_linear_op* op, int config) {
     const int dim = op->grid->host.dim, np = op->grid->host.k + 1;
     AMDG_REQUIRE(linear_tma_supported(dim, np, config), AMDG_ERR_ARG, "unsupported bulk-copy configuration");
     op->tma_cfg = config;
+    return AMDG_OK;
+}
+
+amdg_status amdg_linear_set_wait_limit(amdg_linear_op* op, uint32_t polls) {
+    AMDG_REQUIRE(op, AMDG_ERR_ARG, "null argument");
+    op->wait_limit = polls;
     return AMDG_OK;
 }
 

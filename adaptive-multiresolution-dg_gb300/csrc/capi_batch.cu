@@ -17,6 +17,7 @@
 #include "amdg_internal.hpp"
 #include "kernels.cuh"
 #include "kernels_mlp.cuh"
+#include "device_alloc.cuh"
 
 using namespace amdg;
 
@@ -38,7 +39,7 @@ template <class T>
 amdg_status alloc(T** p, size_t n) {
     *p = nullptr;
     if (n == 0) return AMDG_OK;
-    cudaError_t e = cudaMalloc(reinterpret_cast<void**>(p), n * sizeof(T));
+    cudaError_t e = amdg::device_malloc(reinterpret_cast<void**>(p), n * sizeof(T));
     if (e != cudaSuccess) return fail(AMDG_ERR_NOMEM, std::string("cudaMalloc: ") + cudaGetErrorString(e));
     return AMDG_OK;
 }

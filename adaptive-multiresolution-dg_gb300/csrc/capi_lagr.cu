@@ -19,6 +19,7 @@
 #include "kernels.cuh"
 #include "kernels_lagr.cuh"
 #include "kernels_mlp.cuh"
+#include "device_alloc.cuh"
 
 using namespace amdg;
 
@@ -43,7 +44,7 @@ template <class T>
 amdg_status upload_vec(T** p, const std::vector<T>& host) {
     *p = nullptr;
     if (host.empty()) return AMDG_OK;
-    cudaError_t e = cudaMalloc(reinterpret_cast<void**>(p), host.size() * sizeof(T));
+    cudaError_t e = amdg::device_malloc(reinterpret_cast<void**>(p), host.size() * sizeof(T));
     if (e != cudaSuccess) return fail(AMDG_ERR_NOMEM, std::string("cudaMalloc: ") + cudaGetErrorString(e));
     AMDG_CK(cudaMemcpy(*p, host.data(), host.size() * sizeof(T), cudaMemcpyHostToDevice));
     return AMDG_OK;
@@ -59,7 +60,7 @@ amdg_status upload_both(double** d, float** f, const std::vector<double>& host) 
 amdg_status alloc_bytes(void** p, size_t bytes) {
     *p = nullptr;
     if (bytes == 0) return AMDG_OK;
-    cudaError_t e = cudaMalloc(p, bytes);
+    cudaError_t e = amdg::device_malloc(p, bytes);
     if (e != cudaSuccess) return fail(AMDG_ERR_NOMEM, std::string("cudaMalloc: ") + cudaGetErrorString(e));
     return AMDG_OK;
 }
@@ -222,7 +223,7 @@ amdg_status upload_nodes(amdg_burgers_op* op, cudaStream_t st) {
         op->d_nodes = nullptr;
         op->nodes_cap = 0;
         const size_t want = 2 * bytes + 1024;
-        if (cudaMalloc(reinterpret_cast<void**>(&op->d_nodes), want) != cudaSuccess)
+        if (amdg::device_malloc(reinterpret_cast<void**>(&op->d_nodes), want) != cudaSuccess)
             return fail(AMDG_ERR_NOMEM, "cudaMalloc failed (sweep trees)");
         op->nodes_cap = want;
         op->graph_version = -1;
@@ -559,7 +560,7 @@ amdg_status upload_grow(amdg_burgers_op* op, T** p, const std::vector<T>& host, 
         *p = nullptr;
         cap = 0;
         const size_t want = bytes + bytes / 4 + 256;
-        cudaError_t e = cudaMalloc(reinterpret_cast<void**>(p), want);
+        cudaError_t e = amdg::device_malloc(reinterpret_cast<void**>(p), want);
         if (e != cudaSuccess) return fail(AMDG_ERR_NOMEM, std::string("cudaMalloc: ") + cudaGetErrorString(e));
         cap = want;
     }
@@ -576,7 +577,7 @@ amdg_status reserve_grow(amdg_burgers_op* op, T** p, size_t bytes) {
     *p = nullptr;
     cap = 0;
     const size_t want = bytes + bytes / 4 + 64;
-    if (cudaMalloc(reinterpret_cast<void**>(p), want) != cudaSuccess) {
+    if (amdg::device_malloc(reinterpret_cast<void**>(p), want) != cudaSuccess) {
         *p = nullptr;
         return fail(AMDG_ERR_NOMEM, "cudaMalloc failed (neighbour lists)");
     }
@@ -1223,15 +1224,15 @@ static amdg_status horizon_steps(amdg_burgers_op* op, double dt, amdg_precision 
 // (already in op->d_prob when mlp is given), the criterion's indicators and the missed
 // refinements of the previous step decide the refined leaves without leaving the device; the
 // coarsening records this step's missed refinements there too.
-static amdg_status learned_step_device(amdg_burgers_op* op, amdg_mlp* mlp, double dt, double eps, double eta,
-                                       double tau, amdg_precision prec, int horizon, double t_left, double* t_advanced,
-                                       int* steps_out, int64_t* stats) {
+static amdg_status learned_step_device(amdg_burgers_op* op, amdg_mlp* mlp, double cfl, double wave_speed, double eps,
+                                       double eta, double tau, amdg_precision prec, int horizon, double t_left,
+                                       double* t_advanced, int* steps_out, int64_t* stats) {
     amdg_grid* g = op->grid;
     cudaStream_t st = stream_of(op);
     amdg_status s;
     if (!op->d_cls) {
         void *d = nullptr, *h = nullptr;
-        if (cudaMalloc(&d, 2 * sizeof(unsigned long long)) != cudaSuccess ||
+        if (amdg::device_malloc(&d, 2 * sizeof(unsigned long long)) != cudaSuccess ||
             cudaMallocHost(&h, 2 * sizeof(unsigned long long)) != cudaSuccess) {
             cudaFree(d);
             return fail(AMDG_ERR_NOMEM, "classifier counters");
@@ -1252,6 +1253,8 @@ static amdg_status learned_step_device(amdg_burgers_op* op, amdg_mlp* mlp, doubl
         if ((s = grid_device_refine(g, eps, d_force, nullptr, nullptr)) != AMDG_OK) return s;
     }
     const int64_t n_net = int64_t(op->h_cls[0]), n_unsure = int64_t(op->h_cls[1]);
+    // the step size of the pre-adapted grid: a refinement to finer levels shortens it
+    const double dt = adaptive_dt(g, cfl, wave_speed);
     if ((s = horizon_steps(op, dt, prec, horizon, t_left, t_advanced, steps_out)) != AMDG_OK) return s;
     {
         PhaseTimer ta(g->ctx, AMDG_PHASE_ADAPT_DEVICE);
@@ -1284,7 +1287,6 @@ static amdg_status learned_step_any(amdg_burgers_op* op, amdg_mlp* mlp, double c
     amdg_grid* g = op->grid;
     PhaseTimer timer(g->ctx, AMDG_PHASE_ADAPT_STEP);
     cudaStream_t st = stream_of(op);
-    const double dt = adaptive_dt(g, cfl, wave_speed);
     const int64_t E = g->host.num_elements;
     // the wave classifier also reads u_t (the indicator of prob "wave" adds ||u_t||)
     const int F = g->block * (1 + 2 * g->host.dim) * (op->kind == 1 ? 2 : 1);
@@ -1312,7 +1314,8 @@ static amdg_status learned_step_any(amdg_burgers_op* op, amdg_mlp* mlp, double c
     if (op->kind == 1 && (s = ensure_velocity(g)) != AMDG_OK) return s;
     const double* d_ut = op->kind == 1 ? g->d_v : nullptr;  // the wave indicator adds ||u_t||
     if (g->ctx->adapt_mode == AMDG_ADAPT_DEVICE)
-        return learned_step_device(op, mlp, dt, eps, eta, tau, prec, horizon, t_left, t_advanced, steps_out, stats);
+        return learned_step_device(op, mlp, cfl, wave_speed, eps, eta, tau, prec, horizon, t_left, t_advanced,
+                                   steps_out, stats);
     if ((s = grid_ensure_host(g)) != AMDG_OK) return s;
     std::vector<double> norms;
     if ((s = grid_norms(g, g->d_u, &norms, d_ut)) != AMDG_OK) return s;  // synchronises the stream
@@ -1344,23 +1347,11 @@ static amdg_status learned_step_any(amdg_burgers_op* op, amdg_mlp* mlp, double c
         std::vector<uint64_t> keys = refine_keys(g->host, norms.data(), eps, nullptr, force.data());
         if (int64_t(keys.size()) != g->host.num_elements && (s = grid_set_keys(g, std::move(keys))) != AMDG_OK) return s;
     }
-    // 3. the horizon's time steps on this grid, no predictor: n - 1 steps of dt (replayed as a
-    //    CUDA graph when n - 1 > 1), the last one of dt_last
-    int n = horizon;
-    double dt_last = dt;
-    if (t_left > 0) {
-        const int need = std::max(1, int(std::ceil(t_left / dt - 1e-9)));
-        if (need <= n) {
-            n = need;
-            dt_last = t_left - (n - 1) * dt;
-        }
-    }
-    if (n > 1) {
-        if (op->kind == 0) s = amdg_burgers_rk3_steps(op, dt, n - 1, prec);  // syncs the operator itself
-        else if ((s = burgers_sync(op)) == AMDG_OK) s = wave_rk4(op, dt, n - 1, prec);
-        if (s != AMDG_OK) return s;
-    }
-    if ((s = one_step(op, dt_last, prec)) != AMDG_OK) return s;
+    // 3. the horizon's time steps on this grid (step size from its finest level), no predictor
+    int n = 0;
+    double advanced = 0.0;
+    if ((s = horizon_steps(op, adaptive_dt(g, cfl, wave_speed), prec, horizon, t_left, &advanced, &n)) != AMDG_OK)
+        return s;
     // 4. coarsening (amdg_grid_coarsen), then the surplus criterion judges the
     //    result: leaves still above eps are missed refinements, refined at the
     //    start of the next step
@@ -1380,7 +1371,7 @@ static amdg_status learned_step_any(amdg_burgers_op* op, amdg_mlp* mlp, double c
             if (it != g->host.key.end() && *it == kv.first && leaf[it - g->host.key.begin()]) op->missed_keys.push_back(kv.first);
         }
     }
-    if (t_advanced) *t_advanced = (n - 1) * dt + dt_last;
+    if (t_advanced) *t_advanced = advanced;
     if (steps_out) *steps_out = n;
     if (stats) {
         stats[0] = n_net;
@@ -1449,7 +1440,10 @@ amdg_status amdg_wave_rhs(amdg_wave_op* w, const double* d_u, double* d_rhs, amd
 static amdg_status ensure_velocity(amdg_grid* g) {
     if (g->d_v) return AMDG_OK;
     const int64_t cap = std::max<int64_t>(g->capacity, 1);
-    AMDG_CK(cudaMalloc(reinterpret_cast<void**>(&g->d_v), size_t(cap) * g->block * sizeof(double)));
+    if (amdg::device_malloc(&g->d_v, size_t(cap) * g->block * sizeof(double)) != cudaSuccess) {
+        g->d_v = nullptr;
+        return fail(AMDG_ERR_NOMEM, "cudaMalloc failed (velocity field)");
+    }
     AMDG_CK(cudaMemsetAsync(g->d_v, 0, size_t(cap) * g->block * sizeof(double), static_cast<cudaStream_t>(g->ctx->stream)));
     g->v_capacity = cap;
     return AMDG_OK;

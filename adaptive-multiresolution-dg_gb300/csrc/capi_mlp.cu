@@ -15,6 +15,7 @@
 #include "amdg.h"
 #include "amdg_internal.hpp"
 #include "kernels_mlp.cuh"
+#include "device_alloc.cuh"
 
 using namespace amdg;
 
@@ -61,10 +62,10 @@ amdg_status ensure_ws(amdg_mlp* m, int64_t n) {
     }
     for (int d : m->dims) widest = std::max<int64_t>(widest, d);
     const int k = m->dims.back();
-    cudaError_t e = cudaMalloc(&m->d_act, size_t(tot) * sizeof(float));
-    if (e == cudaSuccess) e = cudaMalloc(&m->d_delta, size_t(2 * widest * n) * sizeof(float));
-    if (e == cudaSuccess) e = cudaMalloc(&m->d_loss, size_t(n) * sizeof(float));
-    if (e == cudaSuccess) e = cudaMalloc(&m->d_probs, size_t(n) * k * sizeof(float));
+    cudaError_t e = amdg::device_malloc(&m->d_act, size_t(tot) * sizeof(float));
+    if (e == cudaSuccess) e = amdg::device_malloc(&m->d_delta, size_t(2 * widest * n) * sizeof(float));
+    if (e == cudaSuccess) e = amdg::device_malloc(&m->d_loss, size_t(n) * sizeof(float));
+    if (e == cudaSuccess) e = amdg::device_malloc(&m->d_probs, size_t(n) * k * sizeof(float));
     if (e != cudaSuccess) return fail(AMDG_ERR_NOMEM, std::string("mlp workspace: ") + cudaGetErrorString(e));
     m->ws_n = n;
     return AMDG_OK;
@@ -151,10 +152,10 @@ amdg_status amdg_mlp_create(amdg_context* ctx, int n_in, int hidden, int n_hidde
         std::normal_distribution<double> nd(0.0, std::sqrt(2.0 / m->dims[l]));
         for (int64_t i = 0; i < int64_t(m->dims[l]) * m->dims[l + 1]; ++i) p[m->w_off[l] + i] = float(nd(rng));
     }
-    cudaError_t e = cudaMalloc(&m->d_params, size_t(off) * sizeof(float));
-    if (e == cudaSuccess) e = cudaMalloc(&m->d_grad, size_t(off) * sizeof(float));
-    if (e == cudaSuccess) e = cudaMalloc(&m->d_m, size_t(off) * sizeof(float));
-    if (e == cudaSuccess) e = cudaMalloc(&m->d_v, size_t(off) * sizeof(float));
+    cudaError_t e = amdg::device_malloc(&m->d_params, size_t(off) * sizeof(float));
+    if (e == cudaSuccess) e = amdg::device_malloc(&m->d_grad, size_t(off) * sizeof(float));
+    if (e == cudaSuccess) e = amdg::device_malloc(&m->d_m, size_t(off) * sizeof(float));
+    if (e == cudaSuccess) e = amdg::device_malloc(&m->d_v, size_t(off) * sizeof(float));
     if (e == cudaSuccess) e = cudaMemcpy(m->d_params, p.data(), size_t(off) * sizeof(float), cudaMemcpyHostToDevice);
     if (e == cudaSuccess) e = cudaMemset(m->d_m, 0, size_t(off) * sizeof(float));
     if (e == cudaSuccess) e = cudaMemset(m->d_v, 0, size_t(off) * sizeof(float));
@@ -240,9 +241,14 @@ amdg_status amdg_mlp_train(amdg_mlp* m, const float* d_x, const int32_t* d_label
     float* xs = nullptr;
     int32_t* ls = nullptr;
     int64_t* d_idx = nullptr;
-    AMDG_CK(cudaMalloc(&xs, size_t(n) * f * sizeof(float)));
-    AMDG_CK(cudaMalloc(&ls, size_t(n) * sizeof(int32_t)));
-    AMDG_CK(cudaMalloc(&d_idx, size_t(n) * sizeof(int64_t)));
+    if (amdg::device_malloc(&xs, size_t(n) * f * sizeof(float)) != cudaSuccess ||
+        amdg::device_malloc(&ls, size_t(n) * sizeof(int32_t)) != cudaSuccess ||
+        amdg::device_malloc(&d_idx, size_t(n) * sizeof(int64_t)) != cudaSuccess) {
+        cudaFree(xs);
+        cudaFree(ls);
+        cudaFree(d_idx);
+        return fail(AMDG_ERR_NOMEM, "cudaMalloc failed (training minibatches)");
+    }
     std::vector<int64_t> idx(n);
     std::mt19937_64 rng(seed);
     double last = 0.0;

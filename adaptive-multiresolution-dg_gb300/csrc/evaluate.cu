@@ -28,6 +28,7 @@
 
 #include "amdg.h"
 #include "amdg_internal.hpp"
+#include "device_alloc.cuh"
 
 using namespace amdg;
 
@@ -216,7 +217,7 @@ struct EvalTables {
     amdg_status put(const std::vector<T>& h, const T** out) {
         void* p = nullptr;
         const size_t bytes = std::max<size_t>(h.size(), 1) * sizeof(T);
-        cudaError_t e = cudaMalloc(&p, bytes);
+        cudaError_t e = amdg::device_malloc(&p, bytes);
         if (e != cudaSuccess) return fail(AMDG_ERR_NOMEM, std::string("cudaMalloc: ") + cudaGetErrorString(e));
         bufs.push_back(p);
         if (!h.empty()) {

@@ -302,7 +302,7 @@ __global__ void __launch_bounds__(32 * WPC) linear_tma_kernel(const float* __res
                                                               const int32_t* __restrict__ row_ptr,
                                                               const int2* __restrict__ pairs,
                                                               const float* __restrict__ blocks, int nblocks,
-                                                              int64_t num_elements, DFState df, int* err) {
+                                                              int64_t num_elements, DFState df, int* err, uint32_t wait_limit) {
     constexpr int B = IPow<NP, D>::v;
     constexpr int C = B / NP;
     constexpr int CPT = (C + 31) / 32;  // columns per lane
@@ -385,7 +385,7 @@ __global__ void __launch_bounds__(32 * WPC) linear_tma_kernel(const float* __res
                     m[4 * jj] = v.x; m[4 * jj + 1] = v.y; m[4 * jj + 2] = v.z; m[4 * jj + 3] = v.w;
                 }
             }
-            const bool ok = mbar_wait_bounded(&full[slot], (parity >> slot) & 1u, kSpinLimit);
+            const bool ok = mbar_wait_bounded(&full[slot], (parity >> slot) & 1u, wait_limit);
             if (__any_sync(0xffffffffu, !ok)) {
                 failed = true;
                 break;
@@ -460,7 +460,7 @@ static cudaError_t launch_tma_cfg(const LinearLaunch& L, cudaStream_t st) {
         if (L.num_elements == 0) return cudaSuccess;
         const int64_t grid = (L.num_elements + W - 1) / W;
         linear_tma_kernel<D, NP, kTmaRing[CFG], kTmaLdg[CFG], W><<<unsigned(grid), 32 * W, 0, st>>>(
-            L.us_shadow, L.row_ptr, L.pairs, L.blocks32p, L.num_blocks, L.num_elements, L.df, L.err);
+            L.us_shadow, L.row_ptr, L.pairs, L.blocks32p, L.num_blocks, L.num_elements, L.df, L.err, L.wait_limit);
         return cudaGetLastError();
     }
 }

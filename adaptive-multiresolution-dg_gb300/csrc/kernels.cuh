@@ -53,6 +53,7 @@ struct LinearLaunch {
     const float* blocks32p;
     DFState df;              // zero-initialised: FP64 epilogue
     int* err;                // variant 2: set to 1 when a copy wait gives up (device flag)
+    uint32_t wait_limit;     // variant 2: polls of a copy wait before it gives up (0: at once)
     int tma_cfg;             // variant 2: ring depth / operator-block source (kernels.cu, kTmaRing, kTmaLdg)
 };
 

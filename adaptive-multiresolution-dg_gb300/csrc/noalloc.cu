@@ -80,7 +80,10 @@ extern "C" amdg_status amdg_rk3ssp_steps_noalloc(amdg_linear_op* op, double* d_u
     double* u2 = scratch + kNoAllocMaxDof;
     cudaStream_t st = static_cast<cudaStream_t>(g->ctx->stream);
     LinearLaunch L{};
-    L.variant = op->variant[prec == AMDG_PREC_MIXED ? 1 : 0];  // same kernel as amdg_rk3ssp_steps
+    // the operator's kernel variant; this call has no FP32 (hi, lo) stage state, so in mixed mode
+    // the column variant reads the FP64 stage vectors and converts each value as it loads it
+    // (the bulk-copy variant needs the FP32 state and is not taken)
+    L.variant = op->variant[prec == AMDG_PREC_MIXED ? 1 : 0];
     L.dim = g->host.dim;
     L.np = g->host.k + 1;
     L.num_elements = g->host.num_elements;

@@ -13,6 +13,7 @@
 
 #include "amdg_internal.hpp"
 #include "kernels.cuh"
+#include "device_alloc.cuh"
 
 using namespace amdg;
 
@@ -55,7 +56,7 @@ __global__ void add_kernel(const double* __restrict__ x, double* __restrict__ y,
 
 amdg_status alloc_vec(double** p, int64_t n) {
     *p = nullptr;
-    if (cudaMalloc(reinterpret_cast<void**>(p), size_t(std::max<int64_t>(n, 1)) * sizeof(double)) != cudaSuccess) {
+    if (amdg::device_malloc(reinterpret_cast<void**>(p), size_t(std::max<int64_t>(n, 1)) * sizeof(double)) != cudaSuccess) {
         *p = nullptr;
         return fail(AMDG_ERR_NOMEM, "cudaMalloc failed (time integrator vectors)");
     }

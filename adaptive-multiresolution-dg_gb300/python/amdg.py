@@ -126,6 +126,8 @@ def load():
         "amdg_wave_adaptive_steps_learned": ([vp, vp, dbl, dbl, dbl, dbl, dbl, i32, i32, dbl, vp, vp, vp], i32),
         "amdg_context_profile": ([vp, i32], i32),
         "amdg_context_set_adapt_mode": ([vp, i32], i32),
+        "amdg_debug_fail_device_allocations": ([i64], i32),
+        "amdg_linear_set_wait_limit": ([vp, C.c_uint32], i32),
         "amdg_grid_set_rhs_zero": ([vp], i32),
         "amdg_grid_rhs_device": ([vp, pp], i32),
         "amdg_grid_get_rhs": ([vp, vp, i64], i32),
@@ -506,6 +508,10 @@ class LinearOperator:
 
     def set_copy_config(self, config: int):
         _ck(load().amdg_linear_set_copy_config(self._h, config), "linear_set_copy_config")
+
+    def set_wait_limit(self, polls: int):
+        """Polls of the bulk-copy variant's waits (default 2**22; 0: give up at once, for tests)."""
+        _ck(load().amdg_linear_set_wait_limit(self._h, polls), "linear_set_wait_limit")
 
     def apply_device(self, d_u: int, d_rhs: int, prec: int = FP64):
         _ck(load().amdg_linear_apply(self._h, C.c_void_p(d_u), C.c_void_p(d_rhs), prec), "linear_apply")

@@ -115,6 +115,11 @@ amdg_status amdg_context_profile(amdg_context* ctx, int enable);
  * the host key set, uploaded after every change.  Both give the same element sets and lists. */
 enum { AMDG_ADAPT_DEVICE = 0, AMDG_ADAPT_HOST = 1 };
 amdg_status amdg_context_set_adapt_mode(amdg_context* ctx, int mode);
+
+/* Test hook (no reference counterpart): after `after` more device allocations by the library,
+ * every allocation fails as if the device were out of memory (the calls report AMDG_ERR_NOMEM);
+ * -1 turns it off.  Process-wide. */
+amdg_status amdg_debug_fail_device_allocations(int64_t after);
 /* seconds[AMDG_PHASE_COUNT] and calls[AMDG_PHASE_COUNT] (either may be NULL). */
 amdg_status amdg_context_profile_read(const amdg_context* ctx, double* seconds, int64_t* calls);
 
@@ -259,6 +264,12 @@ amdg_status amdg_linear_set_variant(amdg_linear_op* op, amdg_precision prec, int
  * (0 where not timed).  All configurations sum in the same order. */
 amdg_status amdg_linear_copy_config(const amdg_linear_op* op, int* config, float* stage_ms);
 amdg_status amdg_linear_set_copy_config(amdg_linear_op* op, int config);
+/* Polls of the bulk-copy variant's bounded waits before a wait gives up (no reference
+ * counterpart; default 4194304 = 2^22).  A wait that gives up makes the kernel drain its copies in
+ * flight (with its own bound) and return without writing; the call then fails with
+ * AMDG_ERR_TIMEOUT and leaves the state as it was.  0 makes every wait give up at once, for
+ * testing that path. */
+amdg_status amdg_linear_set_wait_limit(amdg_linear_op* op, uint32_t polls);
 /* BilinearForm::multi (BilinearForm.h:23): d_rhs = L d_u, device pointers of
  * dof doubles each. */
 amdg_status amdg_linear_apply(amdg_linear_op* op, const double* d_u, double* d_rhs, amdg_precision prec);
@@ -287,7 +298,11 @@ amdg_status amdg_rk3ssp_serve_host(amdg_linear_op* op, double dt, int nsteps, am
  * every call, so the grid may hold at most 262,144 coefficients (larger grids
  * get AMDG_ERR_CAPACITY) and calls that overlap on the GPU race.  The first
  * call on a device looks up the array's address; make it before any stream
- * capture. */
+ * capture.  The address is kept until the library is unloaded: a device reset
+ * in between is not supported.  With AMDG_PREC_MIXED this call keeps its stage
+ * vectors in FP64 (the operator converts each value it loads to FP32), where
+ * amdg_rk3ssp_steps keeps them as FP32 (hi, lo) pairs: the two agree to about
+ * 1e-6 relative, not bitwise; in FP64 they agree bitwise. */
 amdg_status amdg_rk3ssp_steps_noalloc(amdg_linear_op* op, double* d_u, double dt, int nsteps, amdg_precision prec);
 
 /* ---- the reference driver's per-element vectors and explicit integrators ----
@@ -538,7 +553,8 @@ amdg_status amdg_burgers_adaptive_step_learned(amdg_burgers_op* op, amdg_mlp* ml
                                                int64_t* stats);
 /* The learned step over a horizon: the classifier (trained on the plain criterion's refinements
  * within the next `horizon` steps) pre-adapts the grid once, then `horizon` SSP-RK3 steps of one dt
- * run on that grid (a CUDA graph replays them), then coarsening and the criterion's check for
+ * (cfl / sum_d wave_speed 2^maxlevel_d of the pre-adapted grid) run on that grid (a CUDA graph
+ * replays them), then coarsening and the criterion's check for
  * missed refinements as above.  mlp may be NULL: the surplus criterion on the current coefficients
  * then pre-adapts the grid alone (the same horizon without a network, the ablation of the
  * classifier).  With t_left > 0 no step passes t_left: the horizon is cut and its
