@@ -1224,9 +1224,9 @@ static amdg_status horizon_steps(amdg_burgers_op* op, double dt, amdg_precision 
 // (already in op->d_prob when mlp is given), the criterion's indicators and the missed
 // refinements of the previous step decide the refined leaves without leaving the device; the
 // coarsening records this step's missed refinements there too.
-static amdg_status learned_step_device(amdg_burgers_op* op, amdg_mlp* mlp, double cfl, double wave_speed, double eps,
-                                       double eta, double tau, amdg_precision prec, int horizon, double t_left,
-                                       double* t_advanced, int* steps_out, int64_t* stats) {
+static amdg_status learned_step_device(amdg_burgers_op* op, amdg_mlp* mlp, double dt, double eps, double eta,
+                                       double tau, amdg_precision prec, int horizon, double t_left, double* t_advanced,
+                                       int* steps_out, int64_t* stats) {
     amdg_grid* g = op->grid;
     cudaStream_t st = stream_of(op);
     amdg_status s;
@@ -1253,8 +1253,6 @@ static amdg_status learned_step_device(amdg_burgers_op* op, amdg_mlp* mlp, doubl
         if ((s = grid_device_refine(g, eps, d_force, nullptr, nullptr)) != AMDG_OK) return s;
     }
     const int64_t n_net = int64_t(op->h_cls[0]), n_unsure = int64_t(op->h_cls[1]);
-    // the step size of the pre-adapted grid: a refinement to finer levels shortens it
-    const double dt = adaptive_dt(g, cfl, wave_speed);
     if ((s = horizon_steps(op, dt, prec, horizon, t_left, t_advanced, steps_out)) != AMDG_OK) return s;
     {
         PhaseTimer ta(g->ctx, AMDG_PHASE_ADAPT_DEVICE);
@@ -1313,9 +1311,11 @@ static amdg_status learned_step_any(amdg_burgers_op* op, amdg_mlp* mlp, double c
     }
     if (op->kind == 1 && (s = ensure_velocity(g)) != AMDG_OK) return s;
     const double* d_ut = op->kind == 1 ? g->d_v : nullptr;  // the wave indicator adds ||u_t||
+    // the step size of the element set before the pre-adaptation, as the plain step takes it before
+    // its refinement (02_hyperbolic_05_burgers_adapt.cpp:234-243)
+    const double dt = adaptive_dt(g, cfl, wave_speed);
     if (g->ctx->adapt_mode == AMDG_ADAPT_DEVICE)
-        return learned_step_device(op, mlp, cfl, wave_speed, eps, eta, tau, prec, horizon, t_left, t_advanced,
-                                   steps_out, stats);
+        return learned_step_device(op, mlp, dt, eps, eta, tau, prec, horizon, t_left, t_advanced, steps_out, stats);
     if ((s = grid_ensure_host(g)) != AMDG_OK) return s;
     std::vector<double> norms;
     if ((s = grid_norms(g, g->d_u, &norms, d_ut)) != AMDG_OK) return s;  // synchronises the stream
@@ -1347,11 +1347,10 @@ static amdg_status learned_step_any(amdg_burgers_op* op, amdg_mlp* mlp, double c
         std::vector<uint64_t> keys = refine_keys(g->host, norms.data(), eps, nullptr, force.data());
         if (int64_t(keys.size()) != g->host.num_elements && (s = grid_set_keys(g, std::move(keys))) != AMDG_OK) return s;
     }
-    // 3. the horizon's time steps on this grid (step size from its finest level), no predictor
+    // 3. the horizon's time steps on this grid, no predictor
     int n = 0;
     double advanced = 0.0;
-    if ((s = horizon_steps(op, adaptive_dt(g, cfl, wave_speed), prec, horizon, t_left, &advanced, &n)) != AMDG_OK)
-        return s;
+    if ((s = horizon_steps(op, dt, prec, horizon, t_left, &advanced, &n)) != AMDG_OK) return s;
     // 4. coarsening (amdg_grid_coarsen), then the surplus criterion judges the
     //    result: leaves still above eps are missed refinements, refined at the
     //    start of the next step

@@ -176,12 +176,39 @@ __global__ void __launch_bounds__(256) sweep_kernel(SweepArgs<T> a) {
     a.out[int64_t(slot) * per + r] = scale(acc, coef);
 }
 
-// The same sweep with one thread per (term, element, column): a column is one line of the
-// output block along the transformed dimension (its n_to entries), so every input value the
-// thread loads serves all n_to outputs, and the threads of an element walk the same neighbour
-// list (broadcast loads of the pairs and of the 1D matrix rows).  Each output is summed in the
-// order of sweep_kernel (neighbours in list order, k ascending): the results are identical.
-template <typename T, int NTO>
+// Neighbours i and i + 1 of a column: every operand of both loaded, then i's multiply-adds (k
+// ascending), then i + 1's -- the order of sweep_kernel.
+template <typename T, int NF, int NTO>
+__device__ __forceinline__ void col_pair(const T* x0, const T* m0, const T* x1, const T* m1, int stride, int ncols,
+                                         T* acc) {
+    T xa[NF], xb[NF], ma[NF][NTO], mb[NF][NTO];
+#pragma unroll
+    for (int k = 0; k < NF; ++k) {
+        xa[k] = __ldg(x0 + k * stride);
+        xb[k] = __ldg(x1 + k * stride);
+#pragma unroll
+        for (int q = 0; q < NTO; ++q) {
+            ma[k][q] = __ldg(m0 + size_t(k) * ncols + q);
+            mb[k][q] = __ldg(m1 + size_t(k) * ncols + q);
+        }
+    }
+#pragma unroll
+    for (int k = 0; k < NF; ++k)
+#pragma unroll
+        for (int q = 0; q < NTO; ++q) acc[q] = madd(xa[k], ma[k][q], acc[q]);
+#pragma unroll
+    for (int k = 0; k < NF; ++k)
+#pragma unroll
+        for (int q = 0; q < NTO; ++q) acc[q] = madd(xb[k], mb[k][q], acc[q]);
+}
+
+// The same sweep with one thread per (node, element, column): a column is one line of the output
+// block along the transformed dimension (its NTO entries), so every input value the thread loads
+// serves all NTO outputs, and the threads of an element walk the same neighbour list (broadcast
+// loads of the pairs and of the 1D matrix rows).  Kind-0 nodes transform NF values per column,
+// two neighbours per pass; kind-1 nodes (the penalty, np values) take a plain loop.  Each output is
+// summed in the order of sweep_kernel (neighbours in list order, k ascending): identical results.
+template <typename T, int NF, int NTO>
 __global__ void __launch_bounds__(256) sweep_col_kernel(SweepArgs<T> a) {
     const int cols = a.out_block / NTO;
     const int64_t per = a.num_elements * cols;
@@ -196,14 +223,12 @@ __global__ void __launch_bounds__(256) sweep_col_kernel(SweepArgs<T> a) {
     int t, lu, flx, n_from, stride = 1, in_block = 1;
     const T* M;
     const T* in;
-    T coef;
     if (D.kind == 0) {
         t = D.dims[a.sweep];
         lu = D.lu[a.sweep];
         flx = D.flx[a.sweep];
         M = a.mats[D.mat[a.sweep]];
-        n_from = a.n_in;
-        coef = from_double<T>(D.coef);
+        n_from = NF;
         in = a.sweep == 0 ? a.src[D.src] : a.in + int64_t(D.parent) * a.in_slice;
         int done_after = 0;
         for (int j = 0; j < a.sweep; ++j) done_after += D.dims[j] > t ? 1 : 0;
@@ -215,11 +240,11 @@ __global__ void __launch_bounds__(256) sweep_col_kernel(SweepArgs<T> a) {
         flx = 1;
         M = a.mats[kMatAJump];
         n_from = a.np;
-        coef = from_double<T>(D.coef);
         in = a.pen_in;
         for (int d = 0; d < a.dim - 1 - t; ++d) stride *= a.np;
         for (int d = 0; d < a.dim; ++d) in_block *= a.np;
     }
+    const T coef = from_double<T>(D.coef);
     const int inner = c % stride;
     const int outer = c / stride;
     const int64_t et = e * a.dim + t;
@@ -236,7 +261,16 @@ __global__ void __launch_bounds__(256) sweep_col_kernel(SweepArgs<T> a) {
     T acc[NTO];
 #pragma unroll
     for (int q = 0; q < NTO; ++q) acc[q] = from_double<T>(0.0);
-    for (int i = beg; i < end; ++i) {
+    int i = beg;
+    if (D.kind == 0) {
+        for (; i + 2 <= end; i += 2) {
+            const int2 nb0 = __ldg(nbr + i), nb1 = __ldg(nbr + i + 1);
+            col_pair<T, NF, NTO>(in + int64_t(nb0.x) * in_block + in_off, mcol + size_t(nb0.y) * mstep,
+                                 in + int64_t(nb1.x) * in_block + in_off, mcol + size_t(nb1.y) * mstep, stride, ncols,
+                                 acc);
+        }
+    }
+    for (; i < end; ++i) {
         const int2 nb = __ldg(nbr + i);
         const T* x = in + int64_t(nb.x) * in_block + in_off;
         const T* m = mcol + size_t(nb.y) * mstep;
@@ -263,11 +297,16 @@ cudaError_t launch_sweep(const SweepArgs<T>& a, cudaStream_t st) {
     const int nto = a.n_out;
     const int64_t cols = total / nto;
     const unsigned blocks = unsigned((cols + 255) / 256);
-    switch (a.variant == 1 && a.out_block % nto == 0 ? nto : 0) {
-        case 3: sweep_col_kernel<T, 3><<<blocks, 256, 0, st>>>(a); break;
-        case 4: sweep_col_kernel<T, 4><<<blocks, 256, 0, st>>>(a); break;
-        case 5: sweep_col_kernel<T, 5><<<blocks, 256, 0, st>>>(a); break;
-        case 6: sweep_col_kernel<T, 6><<<blocks, 256, 0, st>>>(a); break;
+    // (n_in, n_out) of the transforms the library runs: point values np -> p1, right-hand sides
+    // p1 -> np (the penalty np -> np in the same launch), the interpolation init p1 -> np
+    const int pair = (a.variant == 1 && a.out_block % nto == 0) ? a.n_in * 10 + nto : 0;
+    switch (pair) {
+        case 33: sweep_col_kernel<T, 3, 3><<<blocks, 256, 0, st>>>(a); break;
+        case 34: sweep_col_kernel<T, 3, 4><<<blocks, 256, 0, st>>>(a); break;
+        case 35: sweep_col_kernel<T, 3, 5><<<blocks, 256, 0, st>>>(a); break;
+        case 43: sweep_col_kernel<T, 4, 3><<<blocks, 256, 0, st>>>(a); break;
+        case 53: sweep_col_kernel<T, 5, 3><<<blocks, 256, 0, st>>>(a); break;
+        case 63: sweep_col_kernel<T, 6, 3><<<blocks, 256, 0, st>>>(a); break;
         default: sweep_kernel<T><<<unsigned((total + 255) / 256), 256, 0, st>>>(a); break;
     }
     return cudaGetLastError();

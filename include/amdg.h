@@ -553,7 +553,8 @@ amdg_status amdg_burgers_adaptive_step_learned(amdg_burgers_op* op, amdg_mlp* ml
                                                int64_t* stats);
 /* The learned step over a horizon: the classifier (trained on the plain criterion's refinements
  * within the next `horizon` steps) pre-adapts the grid once, then `horizon` SSP-RK3 steps of one dt
- * (cfl / sum_d wave_speed 2^maxlevel_d of the pre-adapted grid) run on that grid (a CUDA graph
+ * (cfl / sum_d wave_speed 2^maxlevel_d of the grid before the pre-adaptation, as the plain step
+ * takes it before its refinement) run on that grid (a CUDA graph
  * replays them), then coarsening and the criterion's check for
  * missed refinements as above.  mlp may be NULL: the surplus criterion on the current coefficients
  * then pre-adapts the grid alone (the same horizon without a network, the ablation of the
