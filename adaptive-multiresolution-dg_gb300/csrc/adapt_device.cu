@@ -444,135 +444,138 @@ struct TopoArgs {
     KeyHash h;
 };
 
-// Present descendants along t below root (levels >= 2), by depth-first search: absent orders
-// have no present descendants in a hole-free set.
-__device__ int count_descendants(const TopoArgs& A, uint64_t key, int t, int root) {
-    int stack[2 * kMaxLevels + 2];
-    int sp = 0, count = 0, ch[2];
-    int nc = children_of(root, A.ks.nmax, ch);
-    for (int c = 0; c < nc; ++c)
-        if (hfind(A.h, A.ks.with(key, t, ch[c])) >= 0) stack[sp++] = ch[c];
-    while (sp > 0) {
-        const int o = stack[--sp];
-        ++count;
-        nc = children_of(o, A.ks.nmax, ch);
-        for (int c = 0; c < nc; ++c)
-            if (hfind(A.h, A.ks.with(key, t, ch[c])) >= 0) stack[sp++] = ch[c];
+// The candidate 1D orders of level l for a row (element, dimension t) with 1D support [a0, b0),
+// in increasing order: levels 0 and 1 are the single order l (intersecting every support); at
+// level l >= 2 the interval across x = 1 (when it touches the support from the periodic side),
+// the intervals lo .. hi (first .. last intersect the support: vol; the ones beside them touch
+// it: flx only), and the interval across x = 0.  This is the host builder's sequence
+// (csrc/grid.cpp, fibre_neighbours), so the lists come out in the same order.
+struct LevelCands {
+    int n;                 // candidates at this level
+    int base, lo, wl;      // order of candidate i: cnt if i < wl (wrap), else base + lo + i - wl, ...
+    int vfirst, vlast;     // vol range (orders)
+    int wrap_hi_order;     // last candidate when >= 0
+};
+__device__ __forceinline__ LevelCands level_cands(int l, int nmax, int64_t a0, int64_t b0) {
+    LevelCands c;
+    if (l <= 1) {
+        c.n = 1;
+        c.base = l;
+        c.lo = 0;
+        c.wl = 0;
+        c.vfirst = c.vlast = l;
+        c.wrap_hi_order = -1;
+        return c;
     }
-    return count;
+    const LevelRange r = level_range(l, nmax, a0, b0);
+    c.wl = r.wrap_lo ? 1 : 0;
+    c.base = r.cnt;
+    c.lo = r.lo;
+    c.n = c.wl + (r.hi - r.lo + 1) + (r.wrap_hi ? 1 : 0);
+    c.vfirst = r.cnt + r.first;
+    c.vlast = r.cnt + r.last;
+    c.wrap_hi_order = r.wrap_hi ? 2 * r.cnt - 1 : -1;
+    return c;
+}
+__device__ __forceinline__ int cand_order(const LevelCands& c, int i) {
+    if (i < c.wl) return c.base;  // the interval across x = 1 (order cnt)
+    if (c.wrap_hi_order >= 0 && i == c.n - 1) return c.wrap_hi_order;
+    return c.base + c.lo + (i - c.wl);
+}
+
+// One warp per row (element, dimension): every level's candidates looked up 32 at a time, the
+// present ones counted (fill == nullptr) or written in order (ballot prefix) -- no per-thread
+// chains of dependent lookups.  Returns, on lane 0, the vol / flx counts and the counts at levels
+// up to the element's own (the split between the "U" and "L" parts).
+struct RowOut {
+    int2* vol;
+    int2* flx;
+    int64_t vmax, fmax;  // entries the row may write (fill)
+};
+__device__ __forceinline__ void row_lists(const TopoArgs& A, int64_t e, int t, const RowOut* out, int* nv_out,
+                                          int* nf_out, int* sv_out, int* sf_out) {
+    const int lane = threadIdx.x & 31;
+    const int nmax = A.ks.nmax;
+    const uint64_t key = A.keys[e];
+    const int oi = A.ks.field(key, t), own = level_of(oi);
+    int64_t a0, b0;
+    support_of(oi, nmax, &a0, &b0);
+    int nv = 0, nf = 0, sv = 0, sf = 0;
+    for (int l = 0; l <= nmax; ++l) {
+        const LevelCands c = level_cands(l, nmax, a0, b0);
+        for (int base = 0; base < c.n; base += 32) {
+            const int i = base + lane;
+            int s = -1, o = 0;
+            if (i < c.n) {
+                o = cand_order(c, i);
+                s = hfind(A.h, A.ks.with(key, t, o));
+            }
+            const bool inv = s >= 0 && o >= c.vfirst && o <= c.vlast;
+            const unsigned bf = __ballot_sync(0xffffffffu, s >= 0);
+            const unsigned bv = __ballot_sync(0xffffffffu, inv);
+            if (out) {
+                const unsigned below = (1u << lane) - 1u;
+                if (s >= 0) {
+                    const int pf = nf + __popc(bf & below);
+                    if (pf < out->fmax) out->flx[pf] = make_int2(s, o);
+                }
+                if (inv) {
+                    const int pv = nv + __popc(bv & below);
+                    if (pv < out->vmax) out->vol[pv] = make_int2(s, o);
+                }
+            }
+            nf += __popc(bf);
+            nv += __popc(bv);
+        }
+        if (l <= own) {
+            sv = nv;
+            sf = nf;
+        }
+    }
+    *nv_out = nv;
+    *nf_out = nf;
+    *sv_out = sv;
+    *sf_out = sf;
 }
 
 __global__ void topo_count_kernel(TopoArgs A, int32_t* __restrict__ vcnt, int32_t* __restrict__ fcnt) {
-    const int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
-    const int dim = A.ks.dim, nmax = A.ks.nmax;
-    if (i >= A.E * dim) {
-        if (i == A.E * dim) vcnt[i] = fcnt[i] = 0;
+    const int64_t row = (int64_t(blockIdx.x) * blockDim.x + threadIdx.x) >> 5;
+    const int dim = A.ks.dim;
+    if (row > A.E * dim) return;  // whole warps: the row test is uniform
+    if (row == A.E * dim) {
+        if ((threadIdx.x & 31) == 0) vcnt[row] = fcnt[row] = 0;
         return;
     }
-    const int64_t e = i / dim;
-    const int t = int(i - e * dim);
-    const uint64_t key = A.keys[e];
-    const int oi = A.ks.field(key, t), own = level_of(oi);
-    int64_t a0, b0;
-    support_of(oi, nmax, &a0, &b0);
-    int nv = 0, nf = 0;
-    auto present = [&](int o) { return hfind(A.h, A.ks.with(key, t, o)) >= 0; };
-    for (int l = 0; l <= nmax; ++l) {
-        if (l <= 1) {
-            if (present(l)) { ++nv; ++nf; }
-            continue;
-        }
-        const LevelRange r = level_range(l, nmax, a0, b0);
-        if (l <= own) {
-            if (r.wrap_lo && present(r.cnt)) ++nf;
-            for (int j = r.lo; j <= r.hi; ++j)
-                if (present(r.cnt + j)) {
-                    ++nf;
-                    if (j >= r.first && j <= r.last) ++nv;
-                }
-            if (r.wrap_hi && present(2 * r.cnt - 1)) ++nf;
-        } else {
-            if (r.wrap_lo && present(r.cnt)) ++nf;
-            if (r.lo < r.first && present(r.cnt + r.lo)) ++nf;
-            if (r.hi > r.last && present(r.cnt + r.hi)) ++nf;
-            if (r.wrap_hi && present(2 * r.cnt - 1)) ++nf;
-        }
+    const int64_t e = row / dim;
+    int nv, nf, sv, sf;
+    row_lists(A, e, int(row - e * dim), nullptr, &nv, &nf, &sv, &sf);
+    if ((threadIdx.x & 31) == 0) {
+        vcnt[row] = nv;
+        fcnt[row] = nf;
     }
-    const int desc = count_descendants(A, key, t, own <= 1 ? 1 : oi);
-    vcnt[i] = nv + desc;
-    fcnt[i] = nf + desc;
 }
 
-// The lists in increasing 1D order, level by level: levels up to the element's own from the
-// candidate ranges, finer levels from the children of the previous level's members (the vol list
-// itself is the queue), with the flx-only neighbours at the range ends.
 __global__ void topo_fill_kernel(TopoArgs A, const int32_t* __restrict__ vol_ptr, const int32_t* __restrict__ flx_ptr,
                                  int2* __restrict__ vol_nbr, int2* __restrict__ flx_nbr, int32_t* __restrict__ vol_split,
                                  int32_t* __restrict__ flx_split, int64_t vol_cap, int64_t flx_cap, int* err) {
-    const int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
-    const int dim = A.ks.dim, nmax = A.ks.nmax;
-    if (i >= A.E * dim) return;
-    const int64_t e = i / dim;
-    const int t = int(i - e * dim);
-    const uint64_t key = A.keys[e];
-    const int oi = A.ks.field(key, t), own = level_of(oi);
-    int64_t a0, b0;
-    support_of(oi, nmax, &a0, &b0);
-    const int64_t v0 = vol_ptr[i], f0 = flx_ptr[i];
-    const int64_t vmax = vol_ptr[i + 1] - v0, fmax = flx_ptr[i + 1] - f0;
-    if (vol_ptr[i + 1] > vol_cap || flx_ptr[i + 1] > flx_cap) {
-        atomicOr(err, 1);
+    const int64_t row = (int64_t(blockIdx.x) * blockDim.x + threadIdx.x) >> 5;
+    const int dim = A.ks.dim;
+    if (row >= A.E * dim) return;
+    const int64_t v0 = vol_ptr[row], f0 = flx_ptr[row];
+    const int64_t v1 = vol_ptr[row + 1], f1 = flx_ptr[row + 1];
+    if (v1 > vol_cap || f1 > flx_cap) {  // lists beyond the arrays: write nothing
+        if ((threadIdx.x & 31) == 0) atomicOr(err, 1);
         return;
     }
-    int2* vp = vol_nbr + v0;
-    int2* fp = flx_nbr + f0;
-    int64_t nv = 0, nf = 0, sv = 0, sf = 0, pbeg = 0, pend = 0;
-    bool over = false;
-    auto find = [&](int o) { return hfind(A.h, A.ks.with(key, t, o)); };
-    auto put_f = [&](int32_t s, int o) {
-        if (nf < fmax) fp[nf] = make_int2(s, o);
-        else over = true;
-        ++nf;
-    };
-    auto put_v = [&](int32_t s, int o) {
-        if (nv < vmax) vp[nv] = make_int2(s, o);
-        else over = true;
-        ++nv;
-    };
-    for (int l = 0; l <= nmax; ++l) {
-        const int64_t lstart = nv;
-        if (l <= 1) {
-            const int32_t s = find(l);
-            if (s >= 0) { put_v(s, l); put_f(s, l); }
-        } else {
-            const LevelRange r = level_range(l, nmax, a0, b0);
-            int32_t s;
-            if (r.wrap_lo && (s = find(r.cnt)) >= 0) put_f(s, r.cnt);
-            if (l <= own) {
-                for (int j = r.lo; j <= r.hi; ++j)
-                    if ((s = find(r.cnt + j)) >= 0) {
-                        if (j >= r.first && j <= r.last) put_v(s, r.cnt + j);
-                        put_f(s, r.cnt + j);
-                    }
-            } else {
-                if (r.lo < r.first && (s = find(r.cnt + r.lo)) >= 0) put_f(s, r.cnt + r.lo);
-                for (int64_t j = pbeg; j < pend && !over; ++j) {
-                    const int p = vp[j].y;
-                    for (int c = 2 * p; c <= 2 * p + 1; ++c)
-                        if ((s = find(c)) >= 0) { put_v(s, c); put_f(s, c); }
-                }
-                if (r.hi > r.last && (s = find(r.cnt + r.hi)) >= 0) put_f(s, r.cnt + r.hi);
-            }
-            if (r.wrap_hi && (s = find(2 * r.cnt - 1)) >= 0) put_f(s, 2 * r.cnt - 1);
-        }
-        if (l <= own) { sv = nv; sf = nf; }
-        pbeg = lstart;
-        pend = nv;
-        if (over) break;
+    const RowOut out{vol_nbr + v0, flx_nbr + f0, v1 - v0, f1 - f0};
+    const int64_t e = row / dim;
+    int nv, nf, sv, sf;
+    row_lists(A, e, int(row - e * dim), &out, &nv, &nf, &sv, &sf);
+    if ((threadIdx.x & 31) == 0) {
+        if (nv != v1 - v0 || nf != f1 - f0) atomicOr(err, 1);
+        vol_split[row] = int32_t(v0 + sv);
+        flx_split[row] = int32_t(f0 + sf);
     }
-    if (over || nv != vmax || nf != fmax) atomicOr(err, 1);
-    vol_split[i] = int32_t(v0 + sv);
-    flx_split[i] = int32_t(f0 + sf);
 }
 
 // surplus ancestors anc[e][d][ic]: the element owning surplus point ic of e along d
@@ -1058,7 +1061,7 @@ amdg_status device_transform_topology(amdg_grid* g, const DeviceTopoOut& out, in
     // counts of the vol rows in d_cnt[0 .. rows], of the flx rows in d_cnt[rows + 1 ..]
     int32_t* vcnt = d_cnt;
     int32_t* fcnt = d_cnt + rows + 1;
-    topo_count_kernel<<<blocks_for(rows + 1, 128), 128, 0, st>>>(A, vcnt, fcnt);
+    topo_count_kernel<<<blocks_for(32 * (rows + 1), 256), 256, 0, st>>>(A, vcnt, fcnt);
     AMDG_CK(cudaGetLastError());
     size_t temp = 0;
     AMDG_CK(cub::DeviceScan::ExclusiveSum(nullptr, temp, vcnt, out.vol_ptr, int(rows + 1), st));
@@ -1067,7 +1070,7 @@ amdg_status device_transform_topology(amdg_grid* g, const DeviceTopoOut& out, in
     AMDG_CK(cub::DeviceScan::ExclusiveSum(g->dev.temp, tb, vcnt, out.vol_ptr, int(rows + 1), st));
     tb = g->dev.temp_bytes;
     AMDG_CK(cub::DeviceScan::ExclusiveSum(g->dev.temp, tb, fcnt, out.flx_ptr, int(rows + 1), st));
-    topo_fill_kernel<<<blocks_for(rows, 128), 128, 0, st>>>(
+    topo_fill_kernel<<<blocks_for(32 * rows, 256), 256, 0, st>>>(
         A, out.vol_ptr, out.flx_ptr, reinterpret_cast<int2*>(out.vol_nbr), reinterpret_cast<int2*>(out.flx_nbr),
         out.vol_split, out.flx_split, out.vol_cap, out.flx_cap, out.err);
     AMDG_CK(cudaGetLastError());
