@@ -7,7 +7,8 @@
 // Usage:
 //   ref_harness linear <dim> <N> <k> <sparse 0|1> <ic> <engine> <steps> <dt> <c_0> ... <c_{dim-1}>
 //     ic     : sin_sum  -> u0 = sin(2 pi sum x_d)  (init_separable_scalar_sum, as in
-//                          example/02_hyperbolic_01_scalar_const_coefficient.cpp)
+//                          example/02_hyperbolic_01_scalar_const_coefficient.cpp); the final
+//                          L1/L2/Linf errors against the translated solution ("NORMERR")
 //              sin_prod -> u0 = prod_d sin(2 pi x_d) (init_separable_scalar)
 //     engine : assembled -> HyperbolicAlpt::assemble_matrix_scalar + RK3SSP::step_rk
 //              matfree   -> FastRHS::transform_ucoe_alpt_to_rhs per dim with
@@ -268,6 +269,21 @@ int run_linear(int argc, char** argv) {
         auto f = [=](double x, int d) { return std::sin(2 * PI * (x - c[d] * T)); };
         const double err = dg.get_L2_error_split_separable_scalar(f, std::pow(0.5, 0.5 * dim));
         std::printf("L2ERR %.17g\n", err);
+    } else if (ic == "sin_sum") {
+        // exact solution sin(2 pi sum_d (x_d - c_d t)): DGSolution::get_error_no_separable_scalar
+        // (DGSolution.cpp:326-335) with 1 and 2 Gauss points
+        const double T = steps * dt;
+        double shift = 0.0;
+        for (int d = 0; d < dim; ++d) shift += c[d] * T;
+        auto f = [=](std::vector<double> x) {
+            double s = -shift;
+            for (double xd : x) s += xd;
+            return std::sin(2 * PI * s);
+        };
+        for (int gp = 1; gp <= 2; ++gp) {
+            std::vector<double> err = dg.get_error_no_separable_scalar(f, gp);
+            std::printf("NORMERR %d %.17g %.17g %.17g\n", gp, err[0], err[1], err[2]);
+        }
     }
     std::printf("TIME evolve_s=%.9g dof_stage=%.17g\n", t_evolve, 3.0 * steps * dg.get_dof());
     return 0;

@@ -117,6 +117,59 @@ def checksums(level: np.ndarray, suppt: np.ndarray, u: np.ndarray) -> np.ndarray
     return np.array([float((u * u).sum()), float(np.abs(u).max()), float((w * u).sum()), float(np.abs(w * u).sum())])
 
 
+# (name, dim, N, k, ic, engine, steps, dt, c): the linear advection case at its full length -- 2D,
+# full sparse grid N = 7, CFL 0.1 (dt = 1/2561), 2561 SSP-RK3 steps to T = 1; initial and final
+# coefficients and the final L1/L2/Linf errors against the exact translated solution (1 and 2
+# Gauss points)
+LINEAR_LONG_CASES = [
+    ("lin2d_n7_config1_T1", 2, 7, 2, "sin_sum", "assembled", 2561, 1.0 / 2561.0, [1.0, 1.0]),
+]
+
+
+def linear_long(manifest):
+    for name, dim, N, k, ic, engine, steps, dt, c in LINEAR_LONG_CASES:
+        r = run(["linear", dim, N, k, 1, ic, engine, steps, repr(dt)] + [repr(x) for x in c])
+        lv, sp, u0 = split_elements(r["u0"], dim)
+        lv3, sp3, uT = split_elements(r["uT"], dim)
+        assert (lv == lv3).all() and (sp == sp3).all()
+        np.savez_compressed(os.path.join(HERE, name + ".npz"), level=lv, suppt=sp, u0=u0, uT=uT,
+                            **{f"normerr_g{gp}": np.array(err) for gp, err in r["normerr"].items()})
+        manifest[name] = dict(kind="linear_long", dim=dim, N=N, k=k, ic=ic, engine=engine, steps=steps, dt=dt, c=c,
+                              elements=int(r["meta"]["elements"]), normerr_g2=r["normerr"][2])
+        print(name, r["meta"], r["normerr"])
+
+
+# (name, dim, N_init, NMAX, eps, eta, sigma, cfl, steps, snapshot steps): the adaptive wave loop
+# over 24 steps at max level 7 (refine 1e-5, coarsen 1e-6, start level 3): the element set and the
+# checksums of u and u_t after every step, u and u_t themselves at the snapshot steps
+WAVE_ADAPT_LONG_CASES = [
+    ("wave_adapt2d_n7_long", 2, 3, 7, 1e-5, 1e-6, 10.0, 0.1, 24, [0, 1, 12, 24]),
+]
+
+
+def wave_adapt_long(manifest):
+    for name, dim, n0, nmax, eps, eta, sigma, cfl, steps, snaps in WAVE_ADAPT_LONG_CASES:
+        res = subprocess.run([HARNESS, "wave_adapt"] + [str(a) for a in (dim, n0, nmax, repr(eps), repr(eta),
+                                                                          repr(sigma), repr(cfl), steps)],
+                             check=True, capture_output=True, text=True)
+        r = parse_harness(res.stdout)
+        arrs, sums, elements = {}, [], []
+        for i, tag in enumerate(["init"] + [f"step{s}" for s in range(steps)]):
+            lv, sp, u = split_elements(r["u_" + tag], dim)
+            lv2, sp2, ut = split_elements(r["ut_" + tag], dim)
+            assert (lv == lv2).all() and (sp == sp2).all()
+            arrs[f"level_{i}"], arrs[f"suppt_{i}"] = lv.astype(np.int16), sp.astype(np.int16)
+            sums.append(np.concatenate([checksums(lv, sp, u), checksums(lv, sp, ut)]))
+            elements.append(int(len(lv)))
+            if i in snaps:
+                arrs[f"u_{i}"], arrs[f"ut_{i}"] = u, ut
+        arrs["checksums"] = np.array(sums)
+        np.savez_compressed(os.path.join(HERE, name + ".npz"), **arrs)
+        manifest[name] = dict(kind="wave_adapt_long", dim=dim, n_init=n0, nmax=nmax, eps=eps, eta=eta, sigma=sigma,
+                              cfl=cfl, steps=steps, lagr_degree=4, snapshots=snaps, elements=elements)
+        print(name, r["meta"], elements[-1])
+
+
 # (name, dim, N, sigma, steps, dt): wave equation with interpolated K grad u, IPDG, RK4ODE2nd
 WAVE_CASES = [
     ("wave2d_n4", 2, 4, 10.0, 2, 0.001),
@@ -200,7 +253,8 @@ def burgers_adapt_long(manifest):
 def main():
     if not os.path.exists(HARNESS):
         sys.exit("build the reference first: make -C oracle ref")
-    only = {"intp": intp_cases, "burgers_adapt_long": burgers_adapt_long}
+    only = {"intp": intp_cases, "burgers_adapt_long": burgers_adapt_long, "linear_long": linear_long,
+            "wave_adapt_long": wave_adapt_long}
     if len(sys.argv) == 2 and sys.argv[1] in only:  # one group of cases, merged into the manifest
         path = os.path.join(HERE, "manifest.json")
         manifest = json.load(open(path))
@@ -246,6 +300,7 @@ def main():
                               cfl=cfl, umax=umax, steps=steps)
         print(name, r["meta"])
     burgers_adapt_long(manifest)
+    linear_long(manifest)
     for name, dim, N, sigma, steps, dt in WAVE_CASES:
         r = run(["wave", dim, N, repr(sigma), steps, repr(dt)])
         lv, sp, u0 = split_elements(r["u0"], dim)
@@ -270,6 +325,7 @@ def main():
         manifest[name] = dict(kind="wave_adapt", dim=dim, n_init=n0, nmax=nmax, eps=eps, eta=eta, sigma=sigma,
                               cfl=cfl, steps=steps, lagr_degree=4)
         print(name, r["meta"])
+    wave_adapt_long(manifest)
     intp_cases(manifest)
     for N, k in [(4, 2), (3, 1), (3, 3)]:
         r = run(["matrices", N, k])

@@ -1,6 +1,7 @@
 """Batched independent solves (one launch per RK stage for all grids) against
-the same solves stepped one by one with the single-grid operator.  The batch
-multiplies the velocity after the 1D contraction instead of into the 1D
+the oracle's SSP-RK3 per solve (its own grid, velocity and time step) and
+against the same solves stepped one by one with the single-grid operator.  The
+batch multiplies the velocity after the 1D contraction instead of into the 1D
 blocks, so the FP64 results agree to 1e-12 relative, not bitwise."""
 import numpy as np
 import pytest
@@ -49,6 +50,31 @@ def test_batch_matches_individual_solves(ctx, use_graph):
         want = g.coefficients()
         assert np.abs(got - want).max() <= 1e-12 * np.abs(want).max(), f"solve {i}"
         op.close()
+    batch.close()
+    for g in grids:
+        g.close()
+
+
+@pytest.mark.parametrize("prec,tol", [(amdg.FP64, 1e-12), (amdg.MIXED, 1e-6)])
+def test_batch_matches_oracle_per_solve(ctx, prec, tol):
+    """Every solve of the batch against the oracle's SSP-RK3 (the reference's linear operator
+    restated on the CPU) at that solve's own velocity and time step, on its own adaptive grid:
+    FP64 to 1e-12 and mixed to 1e-6 relative (max norm over the solve's field)."""
+    work = O.batched_workload(6, seed=11)
+    grids = _grids(ctx, work, 5, 1e-3)
+    u0 = [g.coefficients().copy() for g in grids]
+    dts = [0.1 / (sum(abs(v) for v in w["velocity"]) * 32) for w in work]
+    batch = amdg.Batch(ctx, grids, [w["velocity"] for w in work])
+    batch.set_dt(dts)
+    nsteps = 3
+    batch.rk3_steps(nsteps, prec, use_graph=True)
+    ctx.synchronize()
+    for i, (g, w) in enumerate(zip(grids, work)):
+        batch.store(i)
+        got = g.coefficients()
+        lv, sp = g.elements()
+        want = O.linear_rk3(3, g.nmax, 2, lv, sp, w["velocity"], u0[i], dts[i], nsteps)
+        assert np.abs(got - want).max() <= tol * np.abs(want).max(), f"solve {i}"
     batch.close()
     for g in grids:
         g.close()

@@ -61,6 +61,39 @@ def test_linear_matches_reference(ctx, name):
     g.close()
 
 
+LONG = [n for n, m in manifest().items() if m["kind"] == "linear_long"]
+
+
+@pytest.mark.parametrize("name", LONG)
+def test_linear_full_length_matches_reference(ctx, name):
+    """The 2D linear advection case over its whole length (full sparse grid N = 7, 2561 SSP-RK3
+    steps of 1/2561 to T = 1) against the reference run: FP64 coefficients to 1e-12 relative, the
+    L1/L2/Linf errors against the exact translated solution (2 Gauss points) to 1e-9 relative; the
+    mixed path's coefficients to 1e-6 and its L2 error within 1 % of the reference's."""
+    m = manifest()[name]
+    z = golden(name)
+    dim, N, k = m["dim"], m["N"], m["k"]
+    g = amdg.Grid(ctx, dim, N, k)
+    lv, sp = g.elements()
+    perm = align(z["level"], z["suppt"], lv, sp)
+    g.init_separable(ic_terms(m["ic"], dim))
+    u0 = g.coefficients().copy()
+    assert rel_err(u0, z["u0"][perm]) < 1e-13
+    op = amdg.LinearOperator(g, m["c"])
+    T = m["steps"] * m["dt"]
+    shift = -sum(m["c"]) * T
+    for prec, tol, etol in ((amdg.FP64, TOL64, 1e-9), (amdg.MIXED, TOL_MIXED_STEP, 1e-2)):
+        g.set_coefficients(u0)
+        op.rk3_steps(m["dt"], m["steps"], prec)
+        ctx.synchronize()
+        assert rel_err(g.coefficients(), z["uT"][perm]) < tol
+        err = g.error_burgers(0.0, a=0.0, b=1.0, c=shift, gauss_points=2)
+        ref = z["normerr_g2"]
+        assert np.all(np.abs(err - ref) <= etol * np.abs(ref)), (prec, err, ref)
+    op.close()
+    g.close()
+
+
 @pytest.mark.parametrize("dim,N,k,c", [(1, 6, 2, [1.0]), (2, 5, 2, [0.0, 1.0]), (3, 5, 3, [-1.0, 0.5, 2.0]),
                                        (5, 4, 1, [1.0, -1.0, 1.0, -1.0, 1.0]), (2, 4, 2, [1.0, 1.0])])
 def test_random_state_matches_oracle(ctx, dim, N, k, c):

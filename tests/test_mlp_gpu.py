@@ -84,7 +84,7 @@ def _collect(ctx, dim, nmax, eps, eta, steps, seeds):
     return np.concatenate(feats), np.concatenate(labs)
 
 
-def test_learned_adaptivity_gains_over_the_plain_criterion(ctx):
+def test_learned_step_skips_the_predictor_and_tracks_the_plain_run(ctx):
     dim, nmax, eps, eta = 2, 7, 1e-4, 1e-5
     x, y = _collect(ctx, dim, nmax, eps, eta, steps=6, seeds=range(6))
     assert (y == 0).sum() > 0, "training data must contain refinements"
@@ -253,4 +253,93 @@ def test_learned_horizon_steps_land_on_the_end_time(ctx):
     a = np.array([u1[p1[k]] for k in common])
     b = np.array([u4[p4[k]] for k in common])
     assert np.linalg.norm(a - b) <= 1e-3 * np.linalg.norm(a)
+    mlp.close()
+
+
+def _collect_horizon(ctx, dim, nmax, eps, eta, steps, seeds, horizon):
+    """Features and horizon labels from plain adaptive Burgers runs of seeded waves a + b sin(2 pi
+    (sum x + c)): 0 (refine) where the criterion refines the element at this step or one of the next
+    horizon - 1, else 2 where it removes the element at this step, else 1."""
+    feats, labs = [], []
+    for seed in seeds:
+        rng = np.random.default_rng(seed)
+        a, b = rng.uniform(0.4, 0.6), rng.uniform(0.15, 0.3)
+        terms = [lambda x, d, a=a: a if d == 0 else 1.0]
+        for f in O.sin_sum_terms(dim, shift=rng.uniform(0.0, 1.0)):
+            terms.append(lambda x, d, f=f, b=b: (b if d == 0 else 1.0) * f(x, d))
+        g = amdg.Grid(ctx, dim, nmax, 2, level_init=3)
+        g.init_separable_adaptive(terms, eps)
+        op = amdg.BurgersOperator(g, 1.1 * (a + b))
+        F = g.block * (1 + 2 * dim)
+        keys, decs = [], []
+        for _ in range(steps):
+            buf = torch.zeros(g.num_elements * F, dtype=torch.float32, device="cuda")
+            torch.cuda.synchronize()
+            op.features_device(g.device_ptr(), buf.data_ptr())
+            ctx.synchronize()
+            feats.append(buf.cpu().numpy().reshape(g.num_elements, F))
+            lv, sp = g.elements()
+            keys.append(np.array(O.arrays_to_keys(lv, sp)))
+            _dt, dec = op.adaptive_step_ex(0.1, a + b, eps, eta)
+            decs.append(np.asarray(dec))
+        for s in range(steps):
+            refined = np.concatenate([keys[j][decs[j] == 1] for j in range(s, min(steps, s + horizon))])
+            labs.append(np.where(np.isin(keys[s], refined), 0, np.where(decs[s] == 2, 2, 1)).astype(np.int32))
+        op.close()
+        g.close()
+    return np.concatenate(feats), np.concatenate(labs)
+
+
+def test_network_against_criterion_only_pre_adaptation(ctx):
+    """The network's own contribution: pre-adaptation over a horizon of 4 steps by the trained
+    classifier (criterion where it is unsure) against pre-adaptation by the surplus criterion alone,
+    same horizon, same thresholds, same mixed precision, 3D Burgers to t = 0.02.  The network
+    refines ahead of the moving front (elements the criterion will refine within the horizon), so
+    it ends on more elements with a smaller error against the exact solution; the plain FP64 run is
+    the yardstick.  Wall times are printed, not asserted: on this workload the extra elements cost
+    more than the network saves, and the criterion-only arm is the faster one."""
+    dim, nmax, eps, eta, horizon, t_end = 3, 6, 2e-5, 2e-6, 4, 0.02
+    x, y = _collect_horizon(ctx, dim, nmax, eps, eta, steps=10, seeds=range(3), horizon=horizon)
+    assert (y == 0).sum() > 0
+    dx, dy = torch.from_numpy(x).cuda(), torch.from_numpy(y).cuda()
+    torch.cuda.synchronize()
+    mlp = amdg.MLP(ctx, x.shape[1], 64, 3, 3, seed=17)
+    mlp.train_device(dx.data_ptr(), dy.data_ptr(), x.shape[0], epochs=30, batch=256, lr=2e-3, seed=18)
+
+    def run(net, h, prec):
+        g = amdg.Grid(ctx, dim, nmax, 2, level_init=3)
+        g.init_separable_adaptive(O.burgers_ic_terms(dim), 1e-5)
+        op = amdg.BurgersOperator(g, 0.825)
+        t, cls = 0.0, np.zeros(3, np.int64)
+        ctx.synchronize()
+        t0 = time.perf_counter()
+        while t < t_end - 1e-14:
+            if h == 0:
+                lv = g.max_mesh_level()
+                dt_full = 0.1 / sum(0.75 * 2.0 ** int(m) for m in lv)
+                cfl = 0.1 if t + dt_full <= t_end else 0.1 * (t_end - t) / dt_full
+                t += op.adaptive_step(cfl, 0.75, eps, eta, prec)
+            else:
+                dt, _n, st = op.adaptive_steps_learned(net, 0.1, 0.75, eps, eta, 0.6 if net else 2.0, h, t_end - t,
+                                                       prec)
+                t += dt
+                cls += st[:3]
+        ctx.synchronize()
+        sec = time.perf_counter() - t0
+        err = g.error_burgers(t, gauss_points=2)[1]
+        res = dict(sec=sec, err=err, elements=g.num_elements, net_refine=int(cls[0]), missed=int(cls[2]),
+                   work=op.counters())
+        op.close()
+        g.close()
+        return res
+
+    plain = run(None, 0, amdg.FP64)
+    crit = run(None, horizon, amdg.MIXED)
+    net = run(mlp, horizon, amdg.MIXED)
+    print(f"plain {plain}\ncriterion-only {crit}\nnetwork {net}")
+    assert crit["net_refine"] == 0 and net["net_refine"] > 0
+    assert net["elements"] >= crit["elements"]
+    assert net["err"] <= crit["err"] * 1.001
+    # both pre-adapted arms stay within a factor 2 of the plain run's error
+    assert crit["err"] <= 2.0 * plain["err"] and net["err"] <= 2.0 * plain["err"]
     mlp.close()

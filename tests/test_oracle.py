@@ -40,6 +40,28 @@ def test_linear_matches_reference(name):
     assert rel_err(uT, z["uT"][perm]) < 1e-12
 
 
+@pytest.mark.parametrize("name", [n for n, m in manifest().items() if m["kind"] == "linear_long"])
+def test_linear_long_fixture_matches_oracle(name):
+    """The full-length linear fixture (T = 1): the oracle's projection gives its initial
+    coefficients, and the oracle's quadrature of its final coefficients against the exact translated
+    solution sin(2 pi (sum x - sum c T)) gives the reference's L1/L2/Linf errors (1 and 2 Gauss
+    points).  The run itself is compared with the GPU path (the oracle's SSP-RK3 would take over
+    a minute for 2561 steps)."""
+    m = manifest()[name]
+    z = golden(name)
+    dim, N, k = m["dim"], m["N"], m["k"]
+    lv, sp = O.grid(dim, N)
+    perm = align(z["level"], z["suppt"], lv, sp)
+    coef = O.project_separable(N, k, dim, ic_terms(m["ic"], dim))
+    u0 = O.init_separable(dim, N, k, lv, sp, coef)
+    assert rel_err(u0, z["u0"][perm]) < 1e-13
+    T = m["steps"] * m["dt"]
+    for gp in (1, 2):
+        err = O.error_burgers(dim, N, k, z["level"], z["suppt"], z["uT"], gp, a=0.0, b=1.0, c=-sum(m["c"]) * T)
+        ref = z[f"normerr_g{gp}"]
+        assert np.all(np.abs(err - ref) <= 1e-10 * ref), (gp, err, ref)
+
+
 def test_l2_error_matches_reference():
     name = "lin3d_n4_sinprod"
     m = manifest()[name]

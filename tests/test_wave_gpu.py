@@ -128,3 +128,44 @@ def test_adaptive_wave_matches_reference(ctx, name):
             assert np.abs(g.velocity() - v_ref).max() <= 1e-12 * np.abs(v_ref).max()
     op.close()
     g.close()
+
+
+WAVE_LONG = [n for n, m in manifest().items() if m["kind"] == "wave_adapt_long"]
+
+
+@pytest.mark.parametrize("name", WAVE_LONG)
+def test_adaptive_wave_long_run_matches_reference(ctx, name):
+    """The adaptive wave loop at max level 7 over 24 steps against the reference run: element sets
+    bit-exact after the initialisation and every step; every step's checksums of u and u_t (sum of
+    squares, max, position-weighted sum) to 1e-12 relative; u and u_t at the snapshot steps to
+    1e-12 of their largest entry."""
+    from golden.make_golden import checksums
+    m = manifest()[name]
+    z = golden(name)
+    dim = m["dim"]
+    g = amdg.Grid(ctx, dim, m["nmax"], 2, level_init=m["n_init"])
+    g.init_separable_adaptive(O.wave_ic_terms(dim), m["eps"])
+    op = amdg.WaveOperator(g, m["sigma"])
+    for i in range(m["steps"] + 1):
+        if i > 0:
+            op.adaptive_step(m["cfl"], 1.0, m["eps"], m["eta"])
+        lv, sp = g.elements()
+        mine = O.arrays_to_keys(lv, sp)
+        ref = O.arrays_to_keys(z[f"level_{i}"], z[f"suppt_{i}"])
+        assert sorted(mine) == sorted(ref), f"element set differs after step {i}"
+        u, v = g.coefficients(), g.velocity()
+        cs = np.concatenate([checksums(lv, sp, u), checksums(lv, sp, v)])
+        rc = z["checksums"][i]
+        for j, what in ((0, "u sum of squares"), (1, "u max"), (4, "u_t sum of squares"), (5, "u_t max")):
+            assert abs(cs[j] - rc[j]) <= 1e-12 * max(rc[j], 1e-300) + 1e-300, f"{what} differs after step {i}"
+        for j, jn, what in ((2, 3, "u weighted sum"), (6, 7, "u_t weighted sum")):
+            assert abs(cs[j] - rc[j]) <= 1e-12 * max(rc[jn], 1e-300), f"{what} differs after step {i}"
+        if f"u_{i}" in z:
+            pos = {k: j for j, k in enumerate(ref)}
+            perm = np.array([pos[k] for k in mine])
+            u_ref, v_ref = z[f"u_{i}"][perm], z[f"ut_{i}"][perm]
+            assert np.abs(u - u_ref).max() <= 1e-12 * np.abs(u_ref).max()
+            if i > 0:
+                assert np.abs(v - v_ref).max() <= 1e-12 * np.abs(v_ref).max()
+    op.close()
+    g.close()
