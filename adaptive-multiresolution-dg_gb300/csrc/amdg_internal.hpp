@@ -380,7 +380,7 @@ struct amdg_linear_op {
     int* d_err = nullptr;            // set by a bounded copy wait that gave up (variant 2)
     uint32_t wait_limit = 1u << 22;  // polls of a bulk-copy wait before it gives up
     int variant[2] = {0, 0};         // kernel variant per precision, picked by the autotuner
-    float variant_ms[2][3] = {{0, 0, 0}, {0, 0, 0}};  // measured stage time [precision][variant]
+    float variant_ms[2][4] = {{0, 0, 0, 0}, {0, 0, 0, 0}};  // measured stage time [precision][variant]
     int tma_cfg = 0;                 // configuration of the bulk-copy variant (ring depth, operator-block source)
     float tma_ms[8] = {0, 0, 0, 0, 0, 0, 0, 0};  // its measured stage time per configuration (kTmaConfigs)
     // request pipeline of amdg_rk3ssp_serve_host: three device states, copy-in / copy-out

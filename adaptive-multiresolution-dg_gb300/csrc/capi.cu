@@ -311,7 +311,7 @@ amdg_status rk3_steps_device(amdg_linear_op* op, double dt, int nsteps, amdg_pre
             }
         }
         // a copy wait that gave up leaves the state as it was: the merge runs only after the check
-        if (L.variant == 2 && check)
+        if (L.variant >= 2 && check)
             if (amdg_status s = check_copy_waits(op); s != AMDG_OK) return s;
         AMDG_CK(launch_merge(hi[0], lo[0], u, g->dof, st));
         g->ctx->launches++;
@@ -340,6 +340,7 @@ amdg_status autotune_linear(amdg_linear_op* op) {
     const int dim = g->host.dim, np = g->host.k + 1;
     const bool col = linear_col_supported(dim, np);
     const bool tma = linear_tma_supported(dim, np);
+    const bool mma = linear_mma_supported(dim, np);
     for (int p = 0; p < 2; ++p) op->variant[p] = col ? 1 : 0;
     if (!col || g->dof < 200000) return AMDG_OK;
     cudaStream_t st = stream_of(g->ctx);
@@ -349,7 +350,8 @@ amdg_status autotune_linear(amdg_linear_op* op) {
     AMDG_CK(launch_split(g->d_u, op->d_shadow, op->d_lo, g->dof, st));
     for (int p = 0; p < 2; ++p) {
         float best = 1e30f;
-        for (int v = 0; v < (p == 1 && tma ? 3 : 2); ++v) {
+        for (int v = 0; v < (p == 1 && tma ? 4 : 2); ++v) {
+            if (v == 3 && !mma) continue;
             // the bulk-copy variant: time each of its configurations, keep the fastest
             const int ncfg = v == 2 ? kTmaConfigs : 1;
             float best_cfg = 1e30f;
@@ -982,8 +984,8 @@ amdg_status amdg_linear_tuning(const amdg_linear_op* op, int* variants, float* s
     AMDG_REQUIRE(op, AMDG_ERR_ARG, "op is null");
     for (int p = 0; p < 2; ++p) {
         if (variants) variants[p] = op->variant[p];
-        for (int v = 0; v < 3; ++v)
-            if (stage_ms) stage_ms[p * 3 + v] = op->variant_ms[p][v];
+        for (int v = 0; v < 4; ++v)
+            if (stage_ms) stage_ms[p * 4 + v] = op->variant_ms[p][v];
     }
     return AMDG_OK;
 }
@@ -992,7 +994,8 @@ amdg_status amdg_linear_set_variant(amdg_linear_op* op, amdg_precision prec, int
     AMDG_REQUIRE(op && (prec == AMDG_PREC_FP64 || prec == AMDG_PREC_MIXED), AMDG_ERR_ARG, "bad arguments");
     const int dim = op->grid->host.dim, np = op->grid->host.k + 1;
     AMDG_REQUIRE(variant == 0 || (variant == 1 && linear_col_supported(dim, np)) ||
-                     (variant == 2 && prec == AMDG_PREC_MIXED && linear_tma_supported(dim, np)),
+                     (variant == 2 && prec == AMDG_PREC_MIXED && linear_tma_supported(dim, np)) ||
+                     (variant == 3 && prec == AMDG_PREC_MIXED && linear_mma_supported(dim, np)),
                  AMDG_ERR_ARG, "unsupported kernel variant");
     op->variant[prec == AMDG_PREC_MIXED ? 1 : 0] = variant;
     return AMDG_OK;
@@ -1146,7 +1149,7 @@ amdg_status amdg_rk3ssp_serve_host(amdg_linear_op* op, double dt, int nsteps, am
     AMDG_CK(cudaStreamSynchronize(out_st));
     AMDG_CK(cudaStreamSynchronize(in_st));
     AMDG_CK(cudaStreamSynchronize(st));
-    return linear_launch(op, prec).variant == 2 ? check_copy_waits(op) : AMDG_OK;
+    return linear_launch(op, prec).variant >= 2 ? check_copy_waits(op) : AMDG_OK;
 }
 
 amdg_status amdg_rk3_stage_update(amdg_context* ctx, int stage, double dt, const double* d_un, double* d_u,

@@ -465,6 +465,207 @@ static cudaError_t launch_tma_cfg(const LinearLaunch& L, cudaStream_t st) {
     }
 }
 
+// ---- tensor-core variant: the bulk-copy ring feeding 3xTF32 mma.sync ------------
+// The same data movement as linear_tma_kernel (one warp per element, its neighbour blocks streamed
+// into a ring of shared-memory slots by bulk copies, bounded mbarrier waits), with the per-dimension
+// contraction Y[c][q] += sum_{s, p} X_s[c][p] M_s[p][q] on the tensor pipe: the columns c of the
+// block are the MMA's M (16-row tiles), the output index q its N (NP of 8 used), and (neighbour, p)
+// its K (8 / NP neighbours per k8 step, the rest zero).  Each FP32 operand is split into a TF32
+// high part and a TF32 remainder, and the three products lo*hi + hi*lo + hi*hi accumulate in FP32
+// (3xTF32, about FP32 accuracy).  Fragment layouts of mma.m16n8k8 (tf32, row.col): lane = 4 g + t;
+// A (16 x 8): a0 (g, t), a1 (g + 8, t), a2 (g, t + 4), a3 (g + 8, t + 4); B (8 x 8): b0 (t, g),
+// b1 (t + 4, g); D (16 x 8): d0 (g, 2t), d1 (g, 2t + 1), d2 (g + 8, 2t), d3 (g + 8, 2t + 1).
+constexpr int kMmaRing = 4;
+
+__device__ __forceinline__ uint32_t to_tf32(float x) {
+    uint32_t r;
+    asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(r) : "f"(x));
+    return r;
+}
+
+// x = hi + lo with hi = tf32(x) and lo = tf32(x - hi) (the difference is exact in FP32)
+__device__ __forceinline__ void split_tf32(float x, uint32_t& hi, uint32_t& lo) {
+    hi = to_tf32(x);
+    lo = to_tf32(x - __uint_as_float(hi));
+}
+
+__device__ __forceinline__ void mma_tf32(float (&d)[4], uint32_t a0, uint32_t a1, uint32_t a2, uint32_t a3,
+                                         uint32_t b0, uint32_t b1) {
+    asm volatile(
+        "mma.sync.aligned.m16n8k8.row.col.f32.tf32.tf32.f32 {%0, %1, %2, %3}, {%4, %5, %6, %7}, {%8, %9}, "
+        "{%0, %1, %2, %3};"
+        : "+f"(d[0]), "+f"(d[1]), "+f"(d[2]), "+f"(d[3])
+        : "r"(a0), "r"(a1), "r"(a2), "r"(a3), "r"(b0), "r"(b1));
+}
+
+template <int D, int NP>
+__global__ void __launch_bounds__(32) linear_mma_kernel(const float* __restrict__ xs, const int32_t* __restrict__ row_ptr,
+                                                        const int2* __restrict__ pairs, const float* __restrict__ blocks,
+                                                        int nblocks, int64_t num_elements, DFState df, int* err,
+                                                        uint32_t wait_limit) {
+    constexpr int B = IPow<NP, D>::v;
+    constexpr int C = B / NP;
+    constexpr int MT = (C + 15) / 16;          // 16-row tiles of columns
+    constexpr int NB = 8 / NP;                 // neighbours per k8 step
+    constexpr int BS = (NP * NP + 3) / 4 * 4;
+    constexpr int DATA = (B + 3) / 4 * 4 + 4;  // floats: an aligned superset of any block
+    static_assert(NB <= kMmaRing, "a k8 step's neighbours must fit the ring");
+    __shared__ __align__(128) float ring[kMmaRing * DATA];
+    __shared__ float y[B];
+    __shared__ __align__(8) uint64_t full[kMmaRing];
+    __shared__ int lead[kMmaRing];
+    __shared__ int bidx[kMmaRing];
+    const int lane = threadIdx.x;
+    const int64_t e = blockIdx.x;
+    if (e >= num_elements) return;
+    for (int i = lane; i < B; i += 32) y[i] = 0.f;
+    const int beg = __ldg(row_ptr + e * D), n = __ldg(row_ptr + e * D + D) - beg;
+    if (lane == 0) {
+        for (int b = 0; b < kMmaRing; ++b) mbar_init(&full[b], 1);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    __syncwarp();
+    int issued = 0, idim = 0;
+    auto issue = [&]() {  // next neighbour into slot issued % kMmaRing (lane 0)
+        const int kk = issued;
+        while (kk >= __ldg(row_ptr + e * D + idim + 1) - beg) ++idim;
+        const int2 pr = __ldg(pairs + beg + kk);
+        const uintptr_t a = reinterpret_cast<uintptr_t>(xs + int64_t(pr.x) * B);
+        const uintptr_t a0 = a & ~uintptr_t(15);
+        const uint32_t bytes = uint32_t(((a + uintptr_t(B) * 4 + 15) & ~uintptr_t(15)) - a0);
+        const int sl = kk % kMmaRing;
+        lead[sl] = int((a - a0) / 4);
+        bidx[sl] = idim * nblocks + pr.y;
+        mbar_expect_tx(&full[sl], bytes);
+        bulk_copy_g2s(ring + sl * DATA, reinterpret_cast<const void*>(a0), bytes, &full[sl]);
+        ++issued;
+    };
+    if (lane == 0)
+        while (issued < n && issued < kMmaRing) issue();
+    __syncwarp();
+    const int g = lane >> 2, t4 = lane & 3;
+    // this lane's two k-columns of A (and rows of B): kc = t4 and t4 + 4 -> neighbour j, index p
+    const int j0 = t4 / NP, p0 = t4 % NP, j1 = (t4 + 4) / NP, p1 = (t4 + 4) % NP;
+    bool failed = false;
+    int k = 0, slot = 0;
+    uint32_t parity = 0;
+    for (int t = 0; t < D && !failed; ++t) {
+        int stride = 1;
+#pragma unroll
+        for (int s2 = t + 1; s2 < D; ++s2) stride *= NP;
+        // offsets of the lane's rows g and g + 8 of every tile (columns c; -1 past the last column)
+        int rb[MT][2];
+#pragma unroll
+        for (int mt = 0; mt < MT; ++mt)
+#pragma unroll
+            for (int h = 0; h < 2; ++h) {
+                const int c = 16 * mt + g + 8 * h;
+                rb[mt][h] = c < C ? (c / stride) * stride * NP + c % stride : -1;
+            }
+        float acc[MT][4];
+#pragma unroll
+        for (int mt = 0; mt < MT; ++mt)
+#pragma unroll
+            for (int r = 0; r < 4; ++r) acc[mt][r] = 0.f;
+        const int kend = __ldg(row_ptr + e * D + t + 1) - beg;
+        while (k < kend) {
+            const int nv = min(NB, kend - k);
+            bool ok = true;
+            for (int j = 0; j < nv; ++j) {
+                const int sl = (slot + j) % kMmaRing;
+                ok = ok && mbar_wait_bounded(&full[sl], (parity >> sl) & 1u, wait_limit);
+            }
+            if (__any_sync(0xffffffffu, !ok)) {
+                failed = true;
+                break;
+            }
+            for (int j = 0; j < nv; ++j) parity ^= 1u << ((slot + j) % kMmaRing);
+            const bool u0 = j0 < nv, u1 = j1 < nv;
+            const int s0 = (slot + j0) % kMmaRing, s1 = (slot + j1) % kMmaRing;
+            // B: this lane's entries M_j[p][q = g] of the step's neighbours (zero outside)
+            float bv0 = 0.f, bv1 = 0.f;
+            if (g < NP) {
+                if (u0) bv0 = __ldg(blocks + size_t(bidx[s0]) * BS + p0 * NP + g);
+                if (u1) bv1 = __ldg(blocks + size_t(bidx[s1]) * BS + p1 * NP + g);
+            }
+            uint32_t bh0, bl0, bh1, bl1;
+            split_tf32(bv0, bh0, bl0);
+            split_tf32(bv1, bh1, bl1);
+            const float* x0 = ring + s0 * DATA + lead[s0] + p0 * stride;
+            const float* x1 = ring + s1 * DATA + lead[s1] + p1 * stride;
+#pragma unroll
+            for (int mt = 0; mt < MT; ++mt) {
+                const float a0 = (u0 && rb[mt][0] >= 0) ? x0[rb[mt][0]] : 0.f;
+                const float a1 = (u0 && rb[mt][1] >= 0) ? x0[rb[mt][1]] : 0.f;
+                const float a2 = (u1 && rb[mt][0] >= 0) ? x1[rb[mt][0]] : 0.f;
+                const float a3 = (u1 && rb[mt][1] >= 0) ? x1[rb[mt][1]] : 0.f;
+                uint32_t ah0, al0, ah1, al1, ah2, al2, ah3, al3;
+                split_tf32(a0, ah0, al0);
+                split_tf32(a1, ah1, al1);
+                split_tf32(a2, ah2, al2);
+                split_tf32(a3, ah3, al3);
+                mma_tf32(acc[mt], al0, al1, al2, al3, bh0, bh1);
+                mma_tf32(acc[mt], ah0, ah1, ah2, ah3, bl0, bl1);
+                mma_tf32(acc[mt], ah0, ah1, ah2, ah3, bh0, bh1);
+            }
+            __syncwarp();  // the warp has read the step's slots
+            if (lane == 0) {
+                asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+                for (int j = 0; j < nv && issued < n; ++j) issue();
+            }
+            __syncwarp();  // lead[] / bidx[] of the refilled slots are written before any lane reads them
+            k += nv;
+            slot = (slot + nv) % kMmaRing;
+        }
+        if (failed) break;
+        // D fragment (rows g, g + 8; columns q = 2 t4, 2 t4 + 1) into the element's accumulator
+#pragma unroll
+        for (int mt = 0; mt < MT; ++mt)
+#pragma unroll
+            for (int h = 0; h < 2; ++h)
+                if (rb[mt][h] >= 0) {
+                    if (2 * t4 < NP) y[rb[mt][h] + 2 * t4 * stride] += acc[mt][2 * h];
+                    if (2 * t4 + 1 < NP) y[rb[mt][h] + (2 * t4 + 1) * stride] += acc[mt][2 * h + 1];
+                }
+        __syncwarp();
+    }
+    if (failed) {
+        if (lane == 0) {
+            atomicExch(err, 1);
+            for (int k2 = k; k2 < issued; ++k2) {
+                const int s2 = k2 % kMmaRing;
+                mbar_wait_bounded(&full[s2], (parity >> s2) & 1u, 1u << 16);
+                parity ^= 1u << s2;
+            }
+        }
+        return;
+    }
+    for (int i = lane; i < B; i += 32) df_stage_update(df, e * B + i, y[i]);
+}
+
+constexpr bool mma_fits(int B, int np) {
+    return B / np <= 256 && 8 / np >= 1 && size_t(kMmaRing * ((B + 3) / 4 * 4 + 4) + B) * sizeof(float) + 256 <= 48 * 1024;
+}
+
+template <int D, int NP>
+static cudaError_t launch_mma_t(const LinearLaunch& L, cudaStream_t st) {
+    constexpr int B = IPow<NP, D>::v;
+    if constexpr (!mma_fits(B, NP)) {
+        return cudaErrorInvalidValue;
+    } else {
+        if (L.num_elements == 0) return cudaSuccess;
+        linear_mma_kernel<D, NP><<<unsigned(L.num_elements), 32, 0, st>>>(
+            L.us_shadow, L.row_ptr, L.pairs, L.blocks32p, L.num_blocks, L.num_elements, L.df, L.err, L.wait_limit);
+        return cudaGetLastError();
+    }
+}
+
+bool linear_mma_supported(int dim, int np) {
+    int B = 1;
+    for (int d = 0; d < dim; ++d) B *= np;
+    return np >= 2 && np <= 4 && mma_fits(B, np);
+}
+
 template <int D, int NP>
 static cudaError_t launch_tma_t(const LinearLaunch& L, cudaStream_t st) {
     switch (L.tma_cfg) {
@@ -507,13 +708,19 @@ static cudaError_t launch_linear_t(const LinearLaunch& L, const T* blocks, const
 template <typename T, typename X>
 static cudaError_t dispatch_linear(const LinearLaunch& L, const T* blocks, const X* xs, StageCoef rk, cudaStream_t st) {
     // variant 2 runs on the FP32-pair stage state only (float shadow input, FP32-pair output)
-    bool tma = false;
-    if constexpr (std::is_same<T, float>::value && std::is_same<X, float>::value)
-        tma = L.variant == 2 && L.df.out_hi && L.err && L.us_shadow;
+    // variant 3 (tensor cores) likewise
+    bool tma = false, mma = false;
+    if constexpr (std::is_same<T, float>::value && std::is_same<X, float>::value) {
+        const bool df_state = L.df.out_hi && L.err && L.us_shadow;
+        tma = L.variant == 2 && df_state;
+        mma = L.variant == 3 && df_state;
+    }
 #define AMDG_CASE(D, NP)                                                                \
     if (L.dim == D && L.np == NP) {                                                       \
-        if constexpr (std::is_same<T, float>::value && std::is_same<X, float>::value)     \
+        if constexpr (std::is_same<T, float>::value && std::is_same<X, float>::value) {   \
             if (tma) return launch_tma_t<D, NP>(L, st);                                   \
+            if (mma) return launch_mma_t<D, NP>(L, st);                                   \
+        }                                                                                 \
         return L.variant >= 1 ? launch_col_t<D, NP, T, X>(L, blocks, xs, rk, st)          \
                               : launch_linear_t<D, NP, T, X>(L, blocks, xs, rk, st);      \
     }

@@ -35,7 +35,8 @@ struct LinearLaunch {
     int dim, np;
     int variant;             // 0: thread per output coefficient; 1: column variant (linear_col_supported);
                              // 2: column variant fed by bulk asynchronous copies (linear_tma_supported;
-                             //    FP32-pair stage state only, else as 1)
+                             //    FP32-pair stage state only, else as 1); 3: the bulk-copy ring with the
+                             //    contraction as 3xTF32 on the tensor pipe (linear_mma_supported; same state)
     int64_t num_elements;
     int num_blocks;
     const double* us;        // input coefficients of the stage
@@ -52,8 +53,8 @@ struct LinearLaunch {
     const double* blocks64p;  // column variant: blocks padded to a multiple of 4 entries
     const float* blocks32p;
     DFState df;              // zero-initialised: FP64 epilogue
-    int* err;                // variant 2: set to 1 when a copy wait gives up (device flag)
-    uint32_t wait_limit;     // variant 2: polls of a copy wait before it gives up (0: at once)
+    int* err;                // variants 2, 3: set to 1 when a copy wait gives up (device flag)
+    uint32_t wait_limit;     // variants 2, 3: polls of a copy wait before it gives up (0: at once)
     int tma_cfg;             // variant 2: ring depth / operator-block source (kernels.cu, kTmaRing, kTmaLdg)
 };
 
@@ -92,6 +93,7 @@ cudaError_t launch_linear(const LinearLaunch& L, bool mixed, StageCoef rk, cudaS
 constexpr int kTmaConfigs = 8;
 bool linear_tma_supported(int dim, int np, int cfg = 0);
 bool linear_col_supported(int dim, int np);
+bool linear_mma_supported(int dim, int np);
 // FP64 vector <-> FP32 (hi, lo) pairs
 cudaError_t launch_split(const double* in, float* hi, float* lo, int64_t n, cudaStream_t st);
 cudaError_t launch_merge(const float* hi, const float* lo, double* out, int64_t n, cudaStream_t st);

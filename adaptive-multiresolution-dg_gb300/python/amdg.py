@@ -490,11 +490,11 @@ class LinearOperator:
         self.pairs, self.flops_per_apply = pairs.value, flops.value
 
     def tuning(self):
-        """(variants[fp64, mixed], stage_ms[[fp64 v0, v1, v2], [mixed v0, v1, v2]]) chosen by the autotuner."""
+        """(variants[fp64, mixed], stage_ms[[fp64 v0 .. v3], [mixed v0 .. v3]]) chosen by the autotuner."""
         v = np.zeros(2, np.int32)
-        ms = np.zeros(6, np.float32)
+        ms = np.zeros(8, np.float32)
         _ck(load().amdg_linear_tuning(self._h, _ptr(v), _ptr(ms)), "linear_tuning")
-        return v.tolist(), ms.reshape(2, 3).tolist()
+        return v.tolist(), ms.reshape(2, 4).tolist()
 
     def set_variant(self, prec: int, variant: int):
         _ck(load().amdg_linear_set_variant(self._h, prec, variant), "linear_set_variant")

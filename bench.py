@@ -211,6 +211,12 @@ def bench_linear6d(ctx, stream, args, world):
     sec32, launches32, err32 = timed_device(amdg.MIXED)
     k64 = timed_kernel(amdg.FP64)
     k32 = timed_kernel(amdg.MIXED)
+    # the tensor-core variant (3xTF32 mma.sync on the bulk-copy ring) forced, beside the autotuner's pick
+    chosen = op.tuning()[0][1]
+    op.set_variant(amdg.MIXED, 3)
+    k_mma = timed_kernel(amdg.MIXED)
+    sec_mma, _, err_mma = timed_device(amdg.MIXED)
+    op.set_variant(amdg.MIXED, chosen)
     # end to end: every step is a request whose state comes from pinned host memory and whose
     # result goes back to it; amdg_rk3ssp_serve_host overlaps the copies of neighbouring requests
     ins = [torch.empty(dof, dtype=torch.float64, pin_memory=True).numpy() for _ in range(2)]
@@ -254,6 +260,10 @@ def bench_linear6d(ctx, stream, args, world):
                       "h2d_bytes_per_step": 8 * dof, "d2h_bytes_per_step": 8 * dof,
                       "call": "amdg_rk3ssp_serve_host (mixed), one RK3 step per request, pinned host buffers",
                       "result_matches_device_step": serve_ok},
+        "tensor_core_variant": {"kernel": "linear_mma_kernel<6,3> (3xTF32 mma.sync m16n8k8, FP32 accumulation)",
+                                "kernel_ms": k_mma * 1e3, "hbm_frac": bytes_per_launch / k_mma / 1e9 / pk["hbm_gbs"],
+                                "ms_per_step": sec_mma / args.steps * 1e3, "l2_error_vs_exact": err_mma,
+                                "speed_vs_chosen_variant": k32 / k_mma},
         "autotune": {"variants": {"fp64": op.tuning()[0][0], "mixed": op.tuning()[0][1]},
                      "stage_ms": {"fp64": op.tuning()[1][0], "mixed": op.tuning()[1][1]},
                      "bulk_copy_config": {"chosen": op.copy_config()[0],
@@ -1111,6 +1121,43 @@ def profile_config3():
     torch.cuda.cudart().cudaProfilerStop()
 
 
+def profile_linear6d():
+    """Profiling case (not a bench line): one mixed SSP-RK3 step of the 6D N=8 linear workload with
+    the tensor-core variant (3 launches of linear_mma_kernel), then one with the bulk-copy FMA
+    variant, between cudaProfilerStart / cudaProfilerStop; stage times by CUDA events first."""
+    import torch
+
+    import amdg
+    torch.cuda.set_device(0)
+    ctx = amdg.Context(0)
+    stream = torch.cuda.Stream()
+    torch.cuda.set_stream(stream)
+    ctx.set_stream(stream.cuda_stream)
+    g = amdg.Grid(ctx, DIM, NMAX, K)
+    g.init_separable([lambda x, d: math.sin(2 * math.pi * x)])
+    op = amdg.LinearOperator(g, COEF)
+    dt = dt_for()
+    op.rk3_steps(dt, 1, amdg.MIXED)
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    for v in (3, 2):
+        op.set_variant(amdg.MIXED, v)
+        op.rk3_steps(dt, 1, amdg.MIXED)
+        ev0.record(stream)
+        op.rk3_steps(dt, 4, amdg.MIXED)
+        ev1.record(stream)
+        ev1.synchronize()
+        print(json.dumps({"variant": v, "stage_ms": ev0.elapsed_time(ev1) / 12, "dof": g.dof}), flush=True)
+    torch.cuda.synchronize()
+    torch.cuda.cudart().cudaProfilerStart()
+    for v in (3, 2):
+        op.set_variant(amdg.MIXED, v)
+        op.rk3_steps(dt, 1, amdg.MIXED)
+    torch.cuda.synchronize()
+    torch.cuda.cudart().cudaProfilerStop()
+    op.close()
+    g.close()
+
+
 def profile_rhs3d():
     """Profiling case (not a bench line): the 3D Burgers right-hand side on the sparse grid N=8
     (4096 elements), FP64 and mixed, with each transform-sweep kernel variant; times by CUDA
@@ -1312,7 +1359,7 @@ def main():
     ap.add_argument("--wave-learn-steps", type=int, default=30)
     ap.add_argument("--wave-train-samples", type=int, default=300000, help="training samples kept (stratified)")
     ap.add_argument("--wave-learn-horizon", type=int, default=2, help="time steps per learned pre-adaptation (wave)")
-    ap.add_argument("--profile", choices=["none", "wave_rhs", "config3", "rhs3d"], default="none",
+    ap.add_argument("--profile", choices=["none", "wave_rhs", "config3", "rhs3d", "linear6d"], default="none",
                     help="wave_rhs: run the wave right-hand-side profiling case instead of the bench")
     ap.add_argument("--wave-time", type=float, default=0.05,
                     help="final time of the 2D wave runs (the config's 0.5 takes ~5000 steps on a filling grid)")
@@ -1321,6 +1368,8 @@ def main():
         profile_wave_rhs()
     elif args.profile == "config3":
         profile_config3()
+    elif args.profile == "linear6d":
+        profile_linear6d()
     elif args.profile == "rhs3d":
         profile_rhs3d()
     elif args.impl == "reference":

@@ -31,7 +31,7 @@
 extern "C" {
 #endif
 
-#define AMDG_ABI_VERSION 4
+#define AMDG_ABI_VERSION 5
 
 typedef enum amdg_status {
     AMDG_OK = 0,
@@ -251,9 +251,12 @@ amdg_status amdg_linear_stats(const amdg_linear_op* op, int64_t* pairs, double* 
 /* Kernel variant per precision (variants[0] FP64, variants[1] mixed; 0 = one
  * thread per output coefficient, 1 = column variant, 2 = column variant whose
  * neighbour blocks arrive in shared memory by bulk asynchronous copies, mixed
- * only), chosen when the operator is built by timing the candidates on its
- * grid, and the measured stage times stage_ms[precision*3 + variant] (0 where
- * not timed).  No reference counterpart.  Either pointer may be NULL. */
+ * only, 3 = the same bulk-copy ring with the per-dimension contraction
+ * (FastMultiplyLU::transform_1D, FastMultiplyLU.cpp:436-512) on the tensor pipe
+ * as 3xTF32 mma.sync with FP32 accumulation, mixed only), chosen when the
+ * operator is built by timing the candidates on its grid, and the measured stage
+ * times stage_ms[precision*4 + variant] (0 where not timed).  No reference
+ * counterpart.  Either pointer may be NULL. */
 amdg_status amdg_linear_tuning(const amdg_linear_op* op, int* variants, float* stage_ms);
 /* Override the autotuner's choice (kept until the grid changes). */
 amdg_status amdg_linear_set_variant(amdg_linear_op* op, amdg_precision prec, int variant);

@@ -262,6 +262,60 @@ def test_kernel_variants_agree_on_mixed_steps(ctx):
     g.close()
 
 
+@pytest.mark.parametrize("dim,N,k,c", [(3, 6, 2, [1.0, -0.5, 0.25]), (4, 6, 2, [1.0, -0.5, 0.25, 0.75]),
+                                       (2, 7, 1, [0.7, -1.3]), (3, 5, 3, [-1.0, 0.5, 2.0])])
+def test_tensor_core_variant_matches_oracle(ctx, dim, N, k, c):
+    """Variant 3 (the bulk-copy ring with the contraction as 3xTF32 mma.sync, FP32 accumulation)
+    against the oracle: two mixed SSP-RK3 steps of a random state to 1e-6 relative, and to 1e-6 of
+    the FP32 column variant, whose sums run in another order (k = 1, 2, 3: 4, 2 and 2 neighbours
+    per k8 step)."""
+    g = amdg.Grid(ctx, dim, N, k)
+    lv, sp = g.elements()
+    rng = np.random.default_rng(dim * 10 + N)
+    u0 = rng.standard_normal((g.num_elements, g.block))
+    op = amdg.LinearOperator(g, c)
+    dt = 1e-3
+    ref = O.linear_rk3(dim, N, k, lv, sp, c, u0, dt, 2)
+    g.set_coefficients(u0)
+    op.rk3_steps(dt, 1, amdg.MIXED)  # builds the operator
+    out = {}
+    for v in (1, 3):
+        op.set_variant(amdg.MIXED, v)
+        g.set_coefficients(u0)
+        op.rk3_steps(dt, 2, amdg.MIXED)
+        ctx.synchronize()
+        out[v] = g.coefficients().copy()
+    assert rel_err(out[3], ref) < TOL_MIXED_STEP
+    assert rel_err(out[3], out[1]) < TOL_MIXED_STEP
+    op.close()
+    g.close()
+
+
+def test_tensor_core_variant_timeout_leaves_the_state(ctx):
+    """The tensor-core variant's bounded waits: with a wait limit of 0 the step fails with
+    AMDG_ERR_TIMEOUT and leaves the coefficients bitwise unchanged; with the limit restored it
+    steps."""
+    g = amdg.Grid(ctx, 3, 6, 2)
+    g.init_separable(O.sin_sum_terms(3))
+    u0 = g.coefficients().copy()
+    op = amdg.LinearOperator(g, [1.0, -0.5, 0.25])
+    op.set_variant(amdg.MIXED, 3)
+    op.set_wait_limit(0)
+    with pytest.raises(amdg.AmdgError) as ei:
+        op.rk3_steps(1e-3, 1, amdg.MIXED)
+    assert ei.value.status == 4
+    ctx.synchronize()
+    assert np.array_equal(g.coefficients(), u0)
+    op.set_wait_limit(1 << 22)
+    op.rk3_steps(1e-3, 1, amdg.MIXED)
+    ctx.synchronize()
+    assert not np.array_equal(g.coefficients(), u0)
+    with pytest.raises(amdg.AmdgError):
+        op.set_variant(amdg.FP64, 3)
+    op.close()
+    g.close()
+
+
 @pytest.mark.parametrize("prec", [amdg.FP64, amdg.MIXED])
 def test_serve_host_matches_device_steps(ctx, prec):
     """Pipelined host requests: every result bitwise equal to the same steps on the device state,
