@@ -432,7 +432,8 @@ struct amdg_burgers_op {
     int64_t interp_version = -1;     // element set of the flux coefficients amdg_lagr_interpolate kept
     int interp_prec = -1;            // ... and their arithmetic
     int chunk = 1;  // terms per launch
-    int sweep_variant = 0;  // transform sweep kernel: 0 thread per output entry, 1 thread per column
+    int sweep_variant = -1;  // transform sweep kernel: -1 by precision, 0 thread per output entry, 1 thread per
+                             // column, 2 / 3 / 4 warp per (node, element) with 1 / 2 / 4 elements per warp
     // work buffers sized for FP64: E x p1^dim doubles each, the sweep buffers and
     // term slices chunk times that
     void *w_up = nullptr, *w_fu = nullptr, *w_a = nullptr, *w_b = nullptr, *w_u = nullptr;

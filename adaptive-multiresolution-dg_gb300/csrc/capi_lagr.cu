@@ -84,6 +84,22 @@ Mats<float2> mats_df(const amdg_burgers_op* op) {
              static_cast<const float2*>(op->df_a2pd), nullptr}};
 }
 
+// [n1 nf][n1 nt] row-major -> blocked by order pair: [o_from][o_to][nf][nt] (an empty table stays
+// empty); false when the size does not match
+bool reblock_table(std::vector<double>* m, int n1, int nf, int nt) {
+    if (m->empty()) return true;
+    const size_t ncols = size_t(n1) * nt;
+    if (m->size() != size_t(n1) * nf * ncols) return false;
+    std::vector<double> out(m->size());
+    size_t w = 0;
+    for (int os = 0; os < n1; ++os)
+        for (int oe = 0; oe < n1; ++oe)
+            for (int p = 0; p < nf; ++p)
+                for (int q = 0; q < nt; ++q) out[w++] = (*m)[(size_t(os) * nf + p) * ncols + size_t(oe) * nt + q];
+    m->swap(out);
+    return true;
+}
+
 // a table as double-float pairs (hi = float(v), lo = float(v - hi))
 amdg_status upload_df(void** p, const std::vector<double>& host) {
     std::vector<float2> h(host.size());
@@ -288,7 +304,9 @@ SweepArgs<T> sweep_args(const amdg_burgers_op* op, const Mats<T>& m) {
     a.n1 = op->n1;
     a.num_elements = g->host.num_elements;
     a.desc = op->d_terms;
-    a.variant = op->sweep_variant;
+    // default kernels: thread per output entry for the FP64 sweeps (FP64-pipe work per warp kept
+    // whole), warp per (node, element) for the FP32 and double-float ones (fewer issued instructions)
+    a.variant = op->sweep_variant >= 0 ? op->sweep_variant : (std::is_same<T, double>::value ? 0 : 2);
     for (int i = 0; i < kNumLagrMats; ++i) a.mats[i] = m.m[i];
     a.vol_ptr = op->d_vol_ptr;
     a.vol_split = op->d_vol_split;
@@ -776,6 +794,15 @@ static amdg_status lagr_create(amdg_grid* g, int kind, const double* alpha, doub
     Basis1D b{g->host.k, g->host.nmax};
     LagrTables t;
     build_lagr_tables(b, degree, &t, kind == 1);
+    // the sweeps read the tables blocked by 1D order pair (the rows and columns of one pair contiguous)
+    const int np = g->host.k + 1;
+    if (!reblock_table(&t.a2p, op->n1, np, op->p1) || !reblock_table(&t.lv, op->n1, op->p1, np) ||
+        !reblock_table(&t.lvx, op->n1, op->p1, np) || !reblock_table(&t.lflx, op->n1, op->p1, np) ||
+        !reblock_table(&t.ajump, op->n1, np, np) || !reblock_table(&t.a2pd, op->n1, np, op->p1) ||
+        !reblock_table(&t.ljv, op->n1, op->p1, np)) {
+        delete op;
+        return fail(AMDG_ERR_ARG, "Lagrange table of unexpected size");
+    }
     std::memcpy(op->weight, t.weight, sizeof(op->weight));
     transform_schedule(dim, &op->sched_dims, &op->sched_lu);
     build_terms(op);
@@ -897,7 +924,7 @@ amdg_status amdg_burgers_work(amdg_burgers_op* op, double* flops, double* transf
 }
 
 amdg_status amdg_burgers_set_sweep_variant(amdg_burgers_op* op, int variant) {
-    AMDG_REQUIRE(op && (variant == 0 || variant == 1), AMDG_ERR_ARG, "variant must be 0 or 1");
+    AMDG_REQUIRE(op && variant >= -1 && variant <= 4, AMDG_ERR_ARG, "variant must be -1 .. 4");
     op->sweep_variant = variant;
     op->graph_version = -1;  // a captured step launched the other kernel
     return AMDG_OK;
@@ -1423,6 +1450,11 @@ amdg_status amdg_wave_destroy(amdg_wave_op* w) {
     amdg_burgers_destroy(w->lagr);
     delete w;
     return AMDG_OK;
+}
+
+amdg_status amdg_wave_set_sweep_variant(amdg_wave_op* w, int variant) {
+    AMDG_REQUIRE(w, AMDG_ERR_ARG, "null argument");
+    return amdg_burgers_set_sweep_variant(w->lagr, variant);
 }
 
 amdg_status amdg_wave_rhs(amdg_wave_op* w, const double* d_u, double* d_rhs, amdg_precision prec) {

@@ -17,6 +17,7 @@
 #include <cuda_runtime.h>
 
 #include <cstdint>
+#include <type_traits>
 
 #include "kernels_lagr.cuh"
 
@@ -88,15 +89,25 @@ __device__ __forceinline__ T fibre_quad(const T* const* x, const T* const* m, in
     return acc;
 }
 
-template <typename T>
+// NODE_ROWS: the node is blockIdx.y and the thread's (element, entry) its index in the node's
+// E x out_block outputs (32-bit index arithmetic); else one 1D grid over all nodes' outputs
+template <typename T, bool NODE_ROWS>
 __global__ void __launch_bounds__(256) sweep_kernel(SweepArgs<T> a) {
     const int64_t per = a.num_elements * a.out_block;
-    const int64_t gid = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
-    if (gid >= per * a.count) return;
-    const int slot = int(gid / per);
-    const int64_t r = gid - int64_t(slot) * per;
-    const int64_t e = r / a.out_block;
-    const int idx = int(r - e * a.out_block);
+    int slot;
+    int64_t r;
+    if constexpr (NODE_ROWS) {
+        slot = blockIdx.y;
+        r = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+        if (r >= per) return;
+    } else {
+        const int64_t gid = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+        if (gid >= per * a.count) return;
+        slot = int(gid / per);
+        r = gid - int64_t(slot) * per;
+    }
+    const int e = int(r / a.out_block);
+    const int idx = int(r - int64_t(e) * a.out_block);
     const PartialSum& D = a.desc[a.first + slot];
     if (D.kind == 1 && a.sweep + 1 < a.dim) return;  // a penalty term is a single (last) sweep
     int t, lu, flx, n_from, n_to, stride = 1, in_block = 1;
@@ -131,7 +142,7 @@ __global__ void __launch_bounds__(256) sweep_kernel(SweepArgs<T> a) {
     const int inner = idx % stride;
     const int qt = (idx / stride) % n_to;
     const int outer = idx / (stride * n_to);
-    const int64_t et = e * a.dim + t;
+    const int64_t et = int64_t(e) * a.dim + t;
     const int32_t* ptr = flx ? a.flx_ptr : a.vol_ptr;
     const int32_t* split = flx ? a.flx_split : a.vol_split;
     const int2* nbr = flx ? a.flx_nbr : a.vol_nbr;
@@ -139,10 +150,12 @@ __global__ void __launch_bounds__(256) sweep_kernel(SweepArgs<T> a) {
     // "L": neighbours finer than e in dimension t; "U": coarser or equal; neighbours are level-sorted
     const int beg = lu == 0 ? __ldg(split + et) : __ldg(ptr + et);
     const int end = lu == 2 ? __ldg(split + et) : __ldg(ptr + et + 1);
-    const int ncols = a.n1 * n_to;
-    const T* mcol = M + size_t(oe) * n_to + qt;
+    // the 1D table is blocked by order pair: block (o_s, o_e) holds M[o_s n_from + k][o_e n_to + q]
+    // at (k, q), n_from x n_to contiguous
+    const int ncols = n_to;
+    const T* mcol = M + size_t(oe) * (n_from * n_to) + qt;
     const int in_off = outer * n_from * stride + inner;
-    const size_t mstep = size_t(n_from) * ncols;
+    const size_t mstep = size_t(a.n1) * (n_from * n_to);
     T acc = from_double<T>(0.0);
     // four neighbours per pass: their (element, order) pairs and operands are
     // independent loads issued together; the sum keeps the neighbour order
@@ -254,10 +267,10 @@ __global__ void __launch_bounds__(256) sweep_col_kernel(SweepArgs<T> a) {
     const int oe = __ldg(a.order + et);
     const int beg = lu == 0 ? __ldg(split + et) : __ldg(ptr + et);
     const int end = lu == 2 ? __ldg(split + et) : __ldg(ptr + et + 1);
-    const int ncols = a.n1 * NTO;
-    const T* mcol = M + size_t(oe) * NTO;
+    const int ncols = NTO;  // blocked 1D table: k-rows of a block are NTO apart
+    const T* mcol = M + size_t(oe) * (n_from * NTO);
     const int in_off = outer * n_from * stride + inner;
-    const size_t mstep = size_t(n_from) * ncols;
+    const size_t mstep = size_t(a.n1) * (n_from * NTO);
     T acc[NTO];
 #pragma unroll
     for (int q = 0; q < NTO; ++q) acc[q] = from_double<T>(0.0);
@@ -288,6 +301,179 @@ __global__ void __launch_bounds__(256) sweep_col_kernel(SweepArgs<T> a) {
     for (int q = 0; q < NTO; ++q) o[int64_t(q) * stride] = scale(acc[q], coef);
 }
 
+// ---- warp per (node, element) -----------------------------------------------------------------
+// The lanes of a warp split as (column c, phase ph): lane = ph * cols + c for cols columns of the
+// output block (lines along the transformed dimension, NT outputs each) and P = 32 / cols phases;
+// lane (c, ph) walks neighbours beg + ph, beg + ph + P, ... of the element's list, and per neighbour
+// loads its column's NF inputs and the NF x NT block of the 1D table for the (neighbour, element)
+// order pair (contiguous in the blocked table, so vector loads), then does the NF x NT
+// multiply-adds.  The phases' partial sums are added by shuffles (fixed order), and the phase-0
+// lanes write.  Every lane of a warp serves the same element, so the neighbour list and the table
+// block are broadcast loads and the warp follows one trip count.  Kind-1 nodes (the penalty, np
+// inputs per column) take the same path with NF = np.  Sums run in another order than
+// sweep_kernel's: results agree to rounding, not bitwise.
+
+// the n entries of a table block (16-byte aligned when n * sizeof(T) is a multiple of 16)
+template <typename T, int N>
+__device__ __forceinline__ void load_block(const T* p, T (&v)[N]) {
+    if constexpr ((N * sizeof(T)) % 16 == 0) {
+        constexpr int V = N * sizeof(T) / 16;
+        const float4* p4 = reinterpret_cast<const float4*>(p);
+        float4 w[V];
+#pragma unroll
+        for (int i = 0; i < V; ++i) w[i] = __ldg(p4 + i);
+        const T* wt = reinterpret_cast<const T*>(w);
+#pragma unroll
+        for (int i = 0; i < N; ++i) v[i] = wt[i];
+    } else {
+#pragma unroll
+        for (int i = 0; i < N; ++i) v[i] = __ldg(p + i);
+    }
+}
+
+__device__ __forceinline__ double shfl_from(double v, int src) { return __shfl_sync(0xffffffffu, v, src); }
+__device__ __forceinline__ float shfl_from(float v, int src) { return __shfl_sync(0xffffffffu, v, src); }
+__device__ __forceinline__ float2 shfl_from(float2 v, int src) {
+    return make_float2(__shfl_sync(0xffffffffu, v.x, src), __shfl_sync(0xffffffffu, v.y, src));
+}
+__device__ __forceinline__ double add_t(double a, double b) { return a + b; }
+__device__ __forceinline__ float add_t(float a, float b) { return a + b; }
+__device__ __forceinline__ float2 add_t(float2 a, float2 b) { return df_add(a, b); }
+
+// one lane's share of a column: neighbours i = first, first + P, ... < end, two per pass
+template <typename T, int NF, int NT>
+__device__ __forceinline__ void warp_column(const int2* __restrict__ nbr, int first, int end, int P, const T* in,
+                                            int64_t in_block, int in_off, int stride, const T* M, size_t mrow, int oe,
+                                            T (&acc)[NT]) {
+    constexpr int BS = NF * NT;
+    int i = first;
+    for (; i + P < end; i += 2 * P) {
+        const int2 n0 = __ldg(nbr + i), n1 = __ldg(nbr + i + P);
+        const T* x0 = in + int64_t(n0.x) * in_block + in_off;
+        const T* x1 = in + int64_t(n1.x) * in_block + in_off;
+        T xa[NF], xb[NF], ma[BS], mb[BS];
+#pragma unroll
+        for (int p = 0; p < NF; ++p) {
+            xa[p] = __ldg(x0 + p * stride);
+            xb[p] = __ldg(x1 + p * stride);
+        }
+        load_block<T, BS>(M + (size_t(n0.y) * mrow + oe) * BS, ma);
+        load_block<T, BS>(M + (size_t(n1.y) * mrow + oe) * BS, mb);
+#pragma unroll
+        for (int p = 0; p < NF; ++p)
+#pragma unroll
+            for (int q = 0; q < NT; ++q) acc[q] = madd(xa[p], ma[p * NT + q], acc[q]);
+#pragma unroll
+        for (int p = 0; p < NF; ++p)
+#pragma unroll
+            for (int q = 0; q < NT; ++q) acc[q] = madd(xb[p], mb[p * NT + q], acc[q]);
+    }
+    if (i < end) {
+        const int2 n0 = __ldg(nbr + i);
+        const T* x0 = in + int64_t(n0.x) * in_block + in_off;
+        T xa[NF], ma[BS];
+#pragma unroll
+        for (int p = 0; p < NF; ++p) xa[p] = __ldg(x0 + p * stride);
+        load_block<T, BS>(M + (size_t(n0.y) * mrow + oe) * BS, ma);
+#pragma unroll
+        for (int p = 0; p < NF; ++p)
+#pragma unroll
+            for (int q = 0; q < NT; ++q) acc[q] = madd(xa[p], ma[p * NT + q], acc[q]);
+    }
+}
+
+// node blockIdx.y; warp w of CTA x serves elements x * 8 + w, then every gridDim.x * 8-th after it
+template <typename T, int NF, int NT>
+__global__ void __launch_bounds__(256) sweep_warp_kernel(SweepArgs<T> a) {
+    const int slot = blockIdx.y;
+    const PartialSum& D = a.desc[a.first + slot];
+    if (D.kind == 1 && a.sweep + 1 < a.dim) return;  // a penalty term is a single (last) sweep
+    const int lane = threadIdx.x & 31;
+    int t, lu, flx, stride = 1, in_block = 1, nf = NF;
+    const T* M;
+    const T* in;
+    if (D.kind == 0) {
+        t = D.dims[a.sweep];
+        lu = D.lu[a.sweep];
+        flx = D.flx[a.sweep];
+        M = a.mats[D.mat[a.sweep]];
+        in = a.sweep == 0 ? a.src[D.src] : a.in + int64_t(D.parent) * a.in_slice;
+        int done_after = 0;
+        for (int j = 0; j < a.sweep; ++j) done_after += D.dims[j] > t ? 1 : 0;
+        for (int d = 0; d < a.dim - 1 - t; ++d) stride *= d < done_after ? a.n_out : a.n_in;
+        for (int d = 0; d < a.dim; ++d) in_block *= d < a.sweep ? a.n_out : a.n_in;
+    } else {
+        t = D.dims[0];
+        lu = 1;
+        flx = 1;
+        nf = a.np;
+        M = a.mats[kMatAJump];
+        in = a.pen_in;
+        for (int d = 0; d < a.dim - 1 - t; ++d) stride *= a.np;
+        for (int d = 0; d < a.dim; ++d) in_block *= a.np;
+    }
+    const T coef = from_double<T>(D.coef);
+    const int cols = a.out_block / NT;
+    const int P = cols >= 32 ? 1 : 32 / cols;
+    const int ph = P > 1 ? lane / cols : 0;
+    const int32_t* ptr = flx ? a.flx_ptr : a.vol_ptr;
+    const int32_t* split = flx ? a.flx_split : a.vol_split;
+    const int2* nbr = flx ? a.flx_nbr : a.vol_nbr;
+    const int E = int(a.num_elements);
+    T* outs = a.out + int64_t(slot) * E * a.out_block;
+    const size_t mrow = size_t(a.n1);
+    for (int e = blockIdx.x * 8 + (threadIdx.x >> 5); e < E; e += gridDim.x * 8) {
+        const int et = e * a.dim + t;
+        const int oe = __ldg(a.order + et);
+        const int beg = lu == 0 ? __ldg(split + et) : __ldg(ptr + et);
+        const int end = lu == 2 ? __ldg(split + et) : __ldg(ptr + et + 1);
+        T* oute = outs + int64_t(e) * a.out_block;
+        // columns c = lane % cols (phase lane / cols), or c0 + lane when cols > 32
+        for (int c0 = 0; c0 < cols; c0 += (P > 1 ? cols : 32)) {
+            const int c = P > 1 ? lane % cols : c0 + lane;
+            const bool active = P > 1 ? ph < P : c < cols;
+            const int inner = c % stride, outer = c / stride;
+            T acc[NT];
+#pragma unroll
+            for (int q = 0; q < NT; ++q) acc[q] = from_double<T>(0.0);
+            if (active) {
+                if (nf == NF) {
+                    warp_column<T, NF, NT>(nbr, beg + ph, end, P, in, in_block, outer * NF * stride + inner, stride, M,
+                                           mrow, oe, acc);
+                } else if constexpr (NT == 3) {
+                    warp_column<T, 3, 3>(nbr, beg + ph, end, P, in, in_block, outer * 3 * stride + inner, stride, M,
+                                         mrow, oe, acc);
+                }
+            }
+            // phase sums into the phase-0 lanes: lane l adds lane l + off for off = cols, 2 cols, 4 cols, ...
+            if (P > 1) {
+                for (int off = cols; off < P * cols; off *= 2) {
+                    const int src = lane + off;
+#pragma unroll
+                    for (int q = 0; q < NT; ++q) {
+                        const T v = shfl_from(acc[q], src & 31);
+                        if (src < 32 && src < P * cols) acc[q] = add_t(acc[q], v);
+                    }
+                }
+            }
+            if (active && ph == 0) {
+                T* o = oute + outer * stride * NT + inner;
+#pragma unroll
+                for (int q = 0; q < NT; ++q) o[q * stride] = scale(acc[q], coef);
+            }
+        }
+    }
+}
+
+// epw elements per warp (one CTA of 8 warps per 8 epw elements and node)
+template <typename T, int NF, int NT>
+static void launch_warp(const SweepArgs<T>& a, int epw, cudaStream_t st) {
+    const int64_t per_cta = 8 * epw;
+    const int64_t gx = (a.num_elements + per_cta - 1) / per_cta;
+    const dim3 grid(unsigned(gx > 0 ? gx : 1), unsigned(a.count));
+    sweep_warp_kernel<T, NF, NT><<<grid, 256, 0, st>>>(a);
+}
+
 template <typename T>
 cudaError_t launch_sweep(const SweepArgs<T>& a, cudaStream_t st) {
     const int64_t total = a.num_elements * a.out_block * a.count;
@@ -299,6 +485,19 @@ cudaError_t launch_sweep(const SweepArgs<T>& a, cudaStream_t st) {
     const unsigned blocks = unsigned((cols + 255) / 256);
     // (n_in, n_out) of the transforms the library runs: point values np -> p1, right-hand sides
     // p1 -> np (the penalty np -> np in the same launch), the interpolation init p1 -> np
+    if (a.variant >= 2 && a.out_block % nto == 0) {
+        const int epw = a.variant == 2 ? 1 : (a.variant == 3 ? 2 : 4);
+        switch (a.n_in * 10 + nto) {
+            case 33: launch_warp<T, 3, 3>(a, epw, st); return cudaGetLastError();
+            case 34: launch_warp<T, 3, 4>(a, epw, st); return cudaGetLastError();
+            case 35: launch_warp<T, 3, 5>(a, epw, st); return cudaGetLastError();
+            case 36: launch_warp<T, 3, 6>(a, epw, st); return cudaGetLastError();
+            case 43: launch_warp<T, 4, 3>(a, epw, st); return cudaGetLastError();
+            case 53: launch_warp<T, 5, 3>(a, epw, st); return cudaGetLastError();
+            case 63: launch_warp<T, 6, 3>(a, epw, st); return cudaGetLastError();
+            default: break;
+        }
+    }
     const int pair = (a.variant == 1 && a.out_block % nto == 0) ? a.n_in * 10 + nto : 0;
     switch (pair) {
         case 33: sweep_col_kernel<T, 3, 3><<<blocks, 256, 0, st>>>(a); break;
@@ -307,7 +506,16 @@ cudaError_t launch_sweep(const SweepArgs<T>& a, cudaStream_t st) {
         case 43: sweep_col_kernel<T, 4, 3><<<blocks, 256, 0, st>>>(a); break;
         case 53: sweep_col_kernel<T, 5, 3><<<blocks, 256, 0, st>>>(a); break;
         case 63: sweep_col_kernel<T, 6, 3><<<blocks, 256, 0, st>>>(a); break;
-        default: sweep_kernel<T><<<unsigned((total + 255) / 256), 256, 0, st>>>(a); break;
+        default:
+            // measured: the node-row grid is the faster one for the FP32 and double-float sweeps, the
+            // flat grid for the FP64 ones
+            if constexpr (std::is_same<T, double>::value) {
+                sweep_kernel<T, false><<<unsigned((total + 255) / 256), 256, 0, st>>>(a);
+            } else {
+                const dim3 grid(unsigned((a.num_elements * a.out_block + 255) / 256), unsigned(a.count));
+                sweep_kernel<T, true><<<grid, 256, 0, st>>>(a);
+            }
+            break;
     }
     return cudaGetLastError();
 }

@@ -22,7 +22,7 @@ struct SweepArgs {
     int64_t num_elements;
     int first, count;              // nodes [first, first + count) of desc
     const PartialSum* desc;
-    const T* mats[kNumLagrMats];   // [n1 * rows per element][n1 * cols per element]
+    const T* mats[kNumLagrMats];   // blocked by order pair: [o_from][o_to][rows per element][cols per element]
     const int32_t *vol_ptr, *vol_split, *flx_ptr, *flx_split;
     const int2 *vol_nbr, *flx_nbr; // (element, 1D order along t)
     const int32_t* order;          // [element][dim]
@@ -32,7 +32,8 @@ struct SweepArgs {
     const T* pen_in;               // Alpert coefficients for kind-1 terms
     T* out;
     int out_block;                 // output entries per element (uniform over the range)
-    int variant;                   // 0: thread per output entry; 1: thread per column (sweep_col_kernel)
+    int variant;                   // 0: thread per output entry; 1: thread per column (sweep_col_kernel);
+                                   // 2: warp per (node, element), lanes over (column, neighbour phase)
 };
 
 template <typename T>

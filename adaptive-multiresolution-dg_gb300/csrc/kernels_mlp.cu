@@ -1,8 +1,8 @@
 // Per-element refine/keep/coarsen classifier: a small fully connected network
 // (ReLU hidden layers, softmax output) with hand-written forward, backward
-// and Adam kernels, and the feature gather from the DG coefficients.  Sizes
-// are small (tens of thousands of samples, 64-wide layers), so every kernel
-// is a plain one-thread-per-output loop with deterministic reductions.
+// and Adam kernels, and the feature gather from the DG coefficients.  The
+// dense layers (forward, input and weight gradients) run as one shared-memory
+// tiled product kernel; every reduction has a fixed order (deterministic).
 #include <cuda_runtime.h>
 
 #include <cstdint>
@@ -11,18 +11,106 @@
 
 namespace amdg {
 
-// y[n][j] = act(b[j] + sum_i W[j][i] x[n][i])
-__global__ void dense_forward_kernel(const float* __restrict__ x, const float* __restrict__ W, const float* __restrict__ b,
-                                     float* __restrict__ y, int64_t n, int in, int out, int relu) {
-    const int64_t gid = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
-    if (gid >= n * out) return;
-    const int64_t s = gid / out;
-    const int j = int(gid - s * out);
-    const float* xs = x + s * in;
-    const float* w = W + int64_t(j) * in;
-    float acc = b[j];
-    for (int i = 0; i < in; ++i) acc = fmaf(w[i], xs[i], acc);
-    y[gid] = (relu && acc < 0.f) ? 0.f : acc;
+#define AMDG_CK_CUDA(x)                          \
+    do {                                         \
+        const cudaError_t e_ = (x);              \
+        if (e_ != cudaSuccess) return e_;        \
+    } while (0)
+
+// ---- dense layers as one tiled product kernel ------------------------------------------------
+// C[m][n] = (bias ? bias[n] : 0) + sum_k A(m, k) B(k, n), A and B given by element strides, so
+// the forward pass (x W^T), the input gradient (dy W) and the weight gradient (dy^T x) are the same
+// kernel.  A CTA of 256 threads owns a 32 x 64 tile of C and walks k in chunks of 32 staged in
+// shared memory; each thread keeps a 2 x 4 register tile.  Every output sums k in ascending order
+// from its bias (one rounding per multiply-add), the order of a plain loop over k.
+constexpr int kTM = 32, kTN = 64, kTK = 32;
+
+struct DenseArgs {
+    const float* A;
+    int64_t sam, sak;  // A(m, k) = A[m * sam + k * sak]
+    const float* B;
+    int64_t sbk, sbn;  // B(k, n) = B[k * sbk + n * sbn]
+    float* C;          // C[m * N + n]
+    const float* bias; // [N] or null
+    const float* mask; // C[m][n] = 0 where mask[m * N + n] <= 0 (null: no mask)
+    int relu;
+    int64_t M;
+    int N, K;
+};
+
+__global__ void __launch_bounds__(256) dense_tile_kernel(DenseArgs a) {
+    __shared__ float As[kTK][kTM + 1];
+    __shared__ __align__(16) float Bs[kTK][kTN];
+    const int tid = threadIdx.x;
+    const int ty = tid / 16, tx = tid % 16;  // rows 2 ty, 2 ty + 1; columns 4 tx .. 4 tx + 3
+    const int64_t m0 = int64_t(blockIdx.x) * kTM;
+    const int n0 = blockIdx.y * kTN;
+    float acc[2][4];
+#pragma unroll
+    for (int r = 0; r < 2; ++r)
+#pragma unroll
+        for (int c = 0; c < 4; ++c) {
+            const int n = n0 + 4 * tx + c;
+            acc[r][c] = (a.bias && n < a.N) ? a.bias[n] : 0.f;
+        }
+    for (int k0 = 0; k0 < a.K; k0 += kTK) {
+        for (int i = tid; i < kTK * kTM; i += 256) {  // A tile, k-major in shared memory
+            const int kk = i / kTM, mm = i % kTM;
+            const int64_t m = m0 + mm;
+            const int k = k0 + kk;
+            As[kk][mm] = (m < a.M && k < a.K) ? a.A[m * a.sam + int64_t(k) * a.sak] : 0.f;
+        }
+        for (int i = tid; i < kTK * kTN; i += 256) {
+            const int kk = i / kTN, nn = i % kTN;
+            const int n = n0 + nn, k = k0 + kk;
+            Bs[kk][nn] = (n < a.N && k < a.K) ? a.B[int64_t(k) * a.sbk + int64_t(n) * a.sbn] : 0.f;
+        }
+        __syncthreads();
+        const int kn = min(kTK, a.K - k0);
+        for (int kk = 0; kk < kn; ++kk) {
+            const float x0 = As[kk][2 * ty], x1 = As[kk][2 * ty + 1];
+            const float4 w = *reinterpret_cast<const float4*>(&Bs[kk][4 * tx]);
+            acc[0][0] = fmaf(x0, w.x, acc[0][0]);
+            acc[0][1] = fmaf(x0, w.y, acc[0][1]);
+            acc[0][2] = fmaf(x0, w.z, acc[0][2]);
+            acc[0][3] = fmaf(x0, w.w, acc[0][3]);
+            acc[1][0] = fmaf(x1, w.x, acc[1][0]);
+            acc[1][1] = fmaf(x1, w.y, acc[1][1]);
+            acc[1][2] = fmaf(x1, w.z, acc[1][2]);
+            acc[1][3] = fmaf(x1, w.w, acc[1][3]);
+        }
+        __syncthreads();
+    }
+#pragma unroll
+    for (int r = 0; r < 2; ++r) {
+        const int64_t m = m0 + 2 * ty + r;
+        if (m >= a.M) continue;
+#pragma unroll
+        for (int c = 0; c < 4; ++c) {
+            const int n = n0 + 4 * tx + c;
+            if (n >= a.N) continue;
+            float v = acc[r][c];
+            if (a.relu && v < 0.f) v = 0.f;
+            if (a.mask && !(a.mask[m * a.N + n] > 0.f)) v = 0.f;
+            a.C[m * a.N + n] = v;
+        }
+    }
+}
+
+static cudaError_t launch_dense_tile(const DenseArgs& a, cudaStream_t st) {
+    if (a.M == 0 || a.N == 0) return cudaSuccess;
+    const dim3 grid(unsigned((a.M + kTM - 1) / kTM), unsigned((a.N + kTN - 1) / kTN));
+    dense_tile_kernel<<<grid, 256, 0, st>>>(a);
+    return cudaGetLastError();
+}
+
+// db[j] = sum_n dy[n][j] (samples in order)
+__global__ void bias_grad_kernel(const float* __restrict__ dy, float* __restrict__ db, int64_t n, int out) {
+    const int j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= out) return;
+    float acc = 0.f;
+    for (int64_t s = 0; s < n; ++s) acc += dy[s * out + j];
+    db[j] = acc;
 }
 
 // softmax of logits; when labels are given also the per-sample cross entropy and
@@ -42,37 +130,6 @@ __global__ void softmax_xent_kernel(const float* __restrict__ logits, const int3
         if (labels) dlogits[s * k + j] = (p - (labels[s] == j ? 1.f : 0.f)) / float(n);
     }
     if (labels) loss[s] = -(z[labels[s]] - m - logf(sum));
-}
-
-// dx[n][i] = (sum_j W[j][i] dy[n][j]) * (x[n][i] > 0 when relu_mask)
-__global__ void dense_backward_input_kernel(const float* __restrict__ dy, const float* __restrict__ W,
-                                            const float* __restrict__ xact, float* __restrict__ dx, int64_t n, int in,
-                                            int out, int relu_mask) {
-    const int64_t gid = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
-    if (gid >= n * in) return;
-    const int64_t s = gid / in;
-    const int i = int(gid - s * in);
-    float acc = 0.f;
-    for (int j = 0; j < out; ++j) acc = fmaf(W[int64_t(j) * in + i], dy[s * out + j], acc);
-    if (relu_mask && !(xact[gid] > 0.f)) acc = 0.f;
-    dx[gid] = acc;
-}
-
-// dW[j][i] = sum_n dy[n][j] x[n][i]; db[j] = sum_n dy[n][j]  (thread per weight, samples in order)
-__global__ void dense_backward_weight_kernel(const float* __restrict__ dy, const float* __restrict__ x, float* __restrict__ dW,
-                                             float* __restrict__ db, int64_t n, int in, int out) {
-    const int64_t gid = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
-    if (gid >= int64_t(out) * (in + 1)) return;
-    const int j = int(gid / (in + 1));
-    const int i = int(gid - int64_t(j) * (in + 1));
-    float acc = 0.f;
-    if (i < in) {
-        for (int64_t s = 0; s < n; ++s) acc = fmaf(dy[s * out + j], x[s * in + i], acc);
-        dW[int64_t(j) * in + i] = acc;
-    } else {
-        for (int64_t s = 0; s < n; ++s) acc += dy[s * out + j];
-        db[j] = acc;
-    }
 }
 
 __global__ void adam_kernel(float* __restrict__ p, const float* __restrict__ g, float* __restrict__ m, float* __restrict__ v,
@@ -120,9 +177,9 @@ static unsigned blocks_for(int64_t n) { return unsigned((n + 255) / 256); }
 
 cudaError_t launch_dense_forward(const float* x, const float* W, const float* b, float* y, int64_t n, int in, int out,
                                  bool relu, cudaStream_t st) {
-    if (n == 0) return cudaSuccess;
-    dense_forward_kernel<<<blocks_for(n * out), 256, 0, st>>>(x, W, b, y, n, in, out, relu ? 1 : 0);
-    return cudaGetLastError();
+    // y = x W^T + b: A(s, i) = x[s in + i], B(i, j) = W[j in + i]
+    DenseArgs a{x, in, 1, W, 1, in, y, b, nullptr, relu ? 1 : 0, n, out, in};
+    return launch_dense_tile(a, st);
 }
 
 cudaError_t launch_softmax_xent(const float* logits, const int32_t* labels, int64_t n, int k, float* probs, float* dlogits,
@@ -135,11 +192,15 @@ cudaError_t launch_softmax_xent(const float* logits, const int32_t* labels, int6
 cudaError_t launch_dense_backward(const float* dy, const float* x, const float* W, float* dx, float* dW, float* db,
                                   int64_t n, int in, int out, bool relu_mask_input, cudaStream_t st) {
     if (n == 0) return cudaSuccess;
-    dense_backward_weight_kernel<<<blocks_for(int64_t(out) * (in + 1)), 256, 0, st>>>(dy, x, dW, db, n, in, out);
-    cudaError_t e = cudaGetLastError();
-    if (e != cudaSuccess || !dx) return e;
-    dense_backward_input_kernel<<<blocks_for(n * in), 256, 0, st>>>(dy, W, x, dx, n, in, out, relu_mask_input ? 1 : 0);
-    return cudaGetLastError();
+    // dW = dy^T x: A(j, s) = dy[s out + j], B(s, i) = x[s in + i]
+    DenseArgs gw{dy, 1, out, x, in, 1, dW, nullptr, nullptr, 0, out, in, int(n)};
+    AMDG_CK_CUDA(launch_dense_tile(gw, st));
+    bias_grad_kernel<<<unsigned((out + 127) / 128), 128, 0, st>>>(dy, db, n, out);
+    AMDG_CK_CUDA(cudaGetLastError());
+    if (!dx) return cudaSuccess;
+    // dx = (dy W) * (x > 0): A(s, j) = dy[s out + j], B(j, i) = W[j in + i]
+    DenseArgs gi{dy, out, 1, W, in, 1, dx, nullptr, relu_mask_input ? x : nullptr, 0, n, in, out};
+    return launch_dense_tile(gi, st);
 }
 
 cudaError_t launch_adam(float* p, const float* g, float* m, float* v, int64_t n, float lr, float b1, float b2, float eps,

@@ -143,6 +143,7 @@ def load():
         "amdg_lagr_interpolate": ([vp, i32], i32),
         "amdg_burgers_work": ([vp, C.POINTER(dbl), C.POINTER(dbl)], i32),
         "amdg_burgers_set_sweep_variant": ([vp, i32], i32),
+        "amdg_wave_set_sweep_variant": ([vp, i32], i32),
         "amdg_lagr_rhs_add": ([vp, i32, vp, i32], i32),
         "amdg_context_profile_read": ([vp, vp, vp], i32),
         "amdg_burgers_counters": ([vp, C.POINTER(i64), C.POINTER(i64)], i32),
@@ -663,6 +664,9 @@ class WaveOperator:
 
     def rhs_device(self, d_u: int, d_rhs: int, prec: int = FP64):
         _ck(load().amdg_wave_rhs(self._h, C.c_void_p(d_u), C.c_void_p(d_rhs), prec), "wave_rhs")
+
+    def set_sweep_variant(self, variant: int):
+        _ck(load().amdg_wave_set_sweep_variant(self._h, variant), "wave_set_sweep_variant")
 
     def rk4_steps(self, dt: float, nsteps: int, prec: int = FP64):
         _ck(load().amdg_wave_rk4_steps(self._h, dt, nsteps, prec), "wave_rk4_steps")

@@ -1160,8 +1160,9 @@ def profile_linear6d():
 
 def profile_rhs3d():
     """Profiling case (not a bench line): the 3D Burgers right-hand side on the sparse grid N=8
-    (4096 elements), FP64 and mixed, with each transform-sweep kernel variant; times by CUDA
-    events, then one right-hand side per (variant, precision) between cudaProfilerStart / Stop."""
+    (4096 elements), FP64 and mixed, with each transform-sweep kernel variant (0 thread per output,
+    1 thread per column, 2 warp per term and element); times by CUDA events, then one right-hand
+    side per (variant, precision) between cudaProfilerStart / Stop."""
     import torch
 
     import amdg
@@ -1179,7 +1180,7 @@ def profile_rhs3d():
     torch.cuda.synchronize()
     flops, _ = op.work()
     ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    for variant in (0, 1):
+    for variant in (0, 1, 2, 3, 4):
         op.set_sweep_variant(variant)
         for prec in (amdg.FP64, amdg.MIXED):
             op.rhs_device(du.data_ptr(), out.data_ptr(), prec)
@@ -1192,7 +1193,7 @@ def profile_rhs3d():
             print(json.dumps({"variant": variant, "prec": int(prec), "rhs_ms": ms, "elements": g.num_elements,
                               "flops": flops, "tflops": flops / ms / 1e9}), flush=True)
     torch.cuda.cudart().cudaProfilerStart()
-    for variant in (0, 1):
+    for variant in (0, 1, 2, 3, 4):
         op.set_sweep_variant(variant)
         for prec in (amdg.FP64, amdg.MIXED):
             op.rhs_device(du.data_ptr(), out.data_ptr(), prec)

@@ -395,9 +395,13 @@ enum { AMDG_LAGR_RHS_VOL = 0, AMDG_LAGR_RHS_FLX = 1, AMDG_LAGR_RHS_PENALTY = 2 }
  * neighbour lists' L / full / U counts; terms whose first sweeps coincide share them) plus the
  * surplus passes, and the (element, neighbour) pairs the sweeps visit.  Reads the lists back (synchronises): for measurement, not for the step loop. */
 amdg_status amdg_burgers_work(amdg_burgers_op* op, double* flops, double* transform_pairs);
-/* Kernel of the transform sweeps (no reference counterpart): 0 (default) one thread per output
- * entry; 1 one thread per column of the transformed dimension, all its entries from one load of
- * each input value.  Both sum every output in the same order (identical results). */
+/* Kernel of the transform sweeps (no reference counterpart): 0 one thread per output entry; 1 one
+ * thread per column of the transformed dimension, all its entries from one load of each input
+ * value; 2 / 3 / 4 one warp per (term, element), its lanes over (column, neighbour phase), the
+ * phases' partial sums added by shuffles, each warp serving 1 / 2 / 4 elements; -1 (default) 0 for
+ * the FP64 sweeps and 2 for the FP32 and double-float sweeps of the mixed mode.  0 and 1 sum every
+ * output in the same order (identical results); 2-4 sum in another fixed order (deterministic,
+ * equal to rounding). */
 amdg_status amdg_burgers_set_sweep_variant(amdg_burgers_op* op, int variant);
 amdg_status amdg_lagr_interpolate(amdg_burgers_op* op, amdg_precision prec);
 amdg_status amdg_lagr_rhs_add(amdg_burgers_op* op, int group, const double* alpha, amdg_precision prec);
@@ -493,6 +497,8 @@ amdg_status amdg_wave_create(amdg_grid* g, double sigma, double amplitude, amdg_
 amdg_status amdg_wave_destroy(amdg_wave_op* op);
 /* d_rhs = L(d_u) (device arrays, dof entries). */
 amdg_status amdg_wave_rhs(amdg_wave_op* op, const double* d_u, double* d_rhs, amdg_precision prec);
+/* amdg_burgers_set_sweep_variant for the wave operator's transform sweeps. */
+amdg_status amdg_wave_set_sweep_variant(amdg_wave_op* op, int variant);
 /* nsteps RK4ODE2nd steps of u' = v, v' = L u on the grid's (u, v)
  * (RK4ODE2nd::step_stage, ODESolver.cpp:579-615). */
 amdg_status amdg_wave_rk4_steps(amdg_wave_op* op, double dt, int nsteps, amdg_precision prec);

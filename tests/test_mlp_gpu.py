@@ -279,7 +279,8 @@ def _collect_horizon(ctx, dim, nmax, eps, eta, steps, seeds, horizon):
             ctx.synchronize()
             feats.append(buf.cpu().numpy().reshape(g.num_elements, F))
             lv, sp = g.elements()
-            keys.append(np.array(O.arrays_to_keys(lv, sp)))
+            o = np.where(lv == 0, 0, (1 << np.maximum(lv - 1, 0)) + (sp - 1) // 2).astype(np.int64)
+            keys.append(sum(o[:, d] << (nmax * d) for d in range(dim)))
             _dt, dec = op.adaptive_step_ex(0.1, a + b, eps, eta)
             decs.append(np.asarray(dec))
         for s in range(steps):
