@@ -548,11 +548,22 @@ struct amdg_batch {
     double *d_blocks64 = nullptr, *d_coef64 = nullptr, *d_dt = nullptr;
     float *d_blocks32 = nullptr, *d_coef32 = nullptr;
     double *d_u = nullptr, *d_u1 = nullptr, *d_u2 = nullptr;
-    float* d_shadow = nullptr;           // 3 x dof
+    // mixed-mode stage state: three FP32 high and three FP32 low arrays at stride sstride (16-byte
+    // aligned bases, 16 bytes of slack); the column kernel uses the high arrays as FP32 shadows
+    float* d_shadow = nullptr;            // 3 x sstride
+    float* d_lo = nullptr;                // 3 x sstride
+    int64_t sstride = 0;
+    int32_t* d_pairs = nullptr;           // (src, blk) interleaved per neighbour pair (bulk-copy ring kernel)
+    float* d_blocks32p = nullptr;         // [2][num_blocks][(np^2 + 3) / 4 * 4]
+    float* d_dt32 = nullptr;              // [solve]
+    int* d_err = nullptr;                 // bulk-copy wait gave up (device flag)
     void* graph_exec[2] = {nullptr, nullptr};  // cudaGraphExec_t per precision
     int64_t launches_per_graph = 0;
-    int tile[2] = {256, 256};             // CTA size of the stage kernel per precision (FP64, mixed)
-    float tile_ms[2][3] = {{0}};          // autotuner: one stage per candidate of kBatchTiles (0: not timed)
+    // stage kernel per precision (FP64, mixed): candidate c < kBatchTileCount is the column
+    // kernel with kBatchTiles[c] threads, c >= kBatchTileCount the bulk-copy ring configuration
+    // c - kBatchTileCount (mixed only); picked by the autotuner
+    int kernel[2] = {2, 2};
+    float kernel_ms[2][16] = {{0}};       // autotuner: one stage per candidate (0: not timed)
     // amdg_batch_adapt scratch over all elements (grow-only): norms, parent table, classifier
     // features and probabilities
     double* d_norms = nullptr;

@@ -62,17 +62,54 @@ StageCoef coef_of(int stage) {
     }
 }
 
-// one SSP-RK3 step of every solve: three fused launches
+bool ring_kernel(const amdg_batch* b, int pi) { return pi == 1 && b->kernel[1] >= kBatchTileCount; }
+
+// the stage-state arrays of the mixed mode: high and low parts of slot i
+float* hi_of(amdg_batch* b, int i) { return b->d_shadow + i * b->sstride; }
+float* lo_of(amdg_batch* b, int i) { return b->d_lo + i * b->sstride; }
+
+// one launch of the bulk-copy ring kernel: stage `stage` of the FP32-pair state, slot in -> out
+amdg_status ring_stage(amdg_batch* b, int cfg, int stage, int in, int out, cudaStream_t st) {
+    const StageCoef c = coef_of(stage);
+    BatchRingLaunch L{};
+    L.dim = b->dim; L.np = b->k + 1; L.cfg = cfg;
+    L.num_elements = b->num_elements; L.num_blocks = b->num_blocks;
+    L.row_ptr = b->d_row_ptr; L.pairs = reinterpret_cast<const int2*>(b->d_pairs); L.blocks = b->d_blocks32p;
+    L.coef = b->d_coef32; L.dt = b->d_dt32; L.solve_of = b->d_solve;
+    L.xs = hi_of(b, in);
+    L.df = df_stage(c);
+    L.df.us_hi = hi_of(b, in); L.df.us_lo = lo_of(b, in);
+    L.df.un_hi = hi_of(b, 0); L.df.un_lo = lo_of(b, 0);
+    L.df.out_hi = hi_of(b, out); L.df.out_lo = lo_of(b, out);
+    L.err = b->d_err;
+    L.wait_limit = 1u << 22;
+    AMDG_CK(launch_batch_ring(L, st));
+    return AMDG_OK;
+}
+
+// one SSP-RK3 step of every solve: three fused launches.  The ring kernel steps the FP32-pair
+// state (slots 0 -> 1 -> 2 -> 0, split from and merged into d_u by amdg_batch_rk3_steps); the
+// column kernel steps the FP64 state with FP32 shadows of the stage inputs (mixed) or in FP64.
 amdg_status batch_step(amdg_batch* b, amdg_precision prec, cudaStream_t st) {
+    const int pi = prec == AMDG_PREC_MIXED ? 1 : 0;
+    if (ring_kernel(b, pi)) {
+        const int in_i[3] = {0, 1, 2}, out_i[3] = {1, 2, 0};
+        for (int stage = 0; stage < 3; ++stage)
+            if (amdg_status r = ring_stage(b, b->kernel[1] - kBatchTileCount, stage, in_i[stage], out_i[stage], st);
+                r != AMDG_OK)
+                return r;
+        return AMDG_OK;
+    }
     double* in[3] = {b->d_u, b->d_u1, b->d_u2};
     double* out[3] = {b->d_u1, b->d_u2, b->d_u};
-    float* sh[3] = {b->d_shadow, b->d_shadow + b->dof, b->d_shadow + 2 * b->dof};
+    float* sh[3] = {hi_of(b, 0), hi_of(b, 1), hi_of(b, 2)};
     const int sout[3] = {1, 2, 0};
+    const int threads = kBatchTiles[b->kernel[pi]];
     for (int stage = 0; stage < 3; ++stage) {
         const StageCoef c = coef_of(stage);
         if (prec == AMDG_PREC_MIXED) {
             BatchLaunch<float, float> L{};
-            L.dim = b->dim; L.np = b->k + 1; L.mode = 1; L.a = c.a; L.b = c.b; L.threads = b->tile[1];
+            L.dim = b->dim; L.np = b->k + 1; L.mode = 1; L.a = c.a; L.b = c.b; L.threads = threads;
             L.num_elements = b->num_elements; L.num_blocks = b->num_blocks;
             L.us = in[stage]; L.xs = sh[stage]; L.un = b->d_u; L.out = out[stage]; L.shadow_out = sh[sout[stage]];
             L.row_ptr = b->d_row_ptr; L.src = b->d_src; L.blk = b->d_blk; L.blocks = b->d_blocks32;
@@ -80,7 +117,7 @@ amdg_status batch_step(amdg_batch* b, amdg_precision prec, cudaStream_t st) {
             AMDG_CK(launch_batch<float, float>(L, st));
         } else {
             BatchLaunch<double, double> L{};
-            L.dim = b->dim; L.np = b->k + 1; L.mode = 1; L.a = c.a; L.b = c.b; L.threads = b->tile[0];
+            L.dim = b->dim; L.np = b->k + 1; L.mode = 1; L.a = c.a; L.b = c.b; L.threads = threads;
             L.num_elements = b->num_elements; L.num_blocks = b->num_blocks;
             L.us = in[stage]; L.xs = in[stage]; L.un = b->d_u; L.out = out[stage]; L.shadow_out = nullptr;
             L.row_ptr = b->d_row_ptr; L.src = b->d_src; L.blk = b->d_blk; L.blocks = b->d_blocks64;
@@ -89,6 +126,16 @@ amdg_status batch_step(amdg_batch* b, amdg_precision prec, cudaStream_t st) {
         }
     }
     return AMDG_OK;
+}
+
+// a bulk-copy wait of the ring kernel gave up: report it and clear the flag (synchronises)
+amdg_status check_ring_waits(amdg_batch* b, cudaStream_t st) {
+    int h = 0;
+    AMDG_CK(cudaMemcpyAsync(&h, b->d_err, sizeof(int), cudaMemcpyDeviceToHost, st));
+    AMDG_CK(cudaStreamSynchronize(st));
+    if (h == 0) return AMDG_OK;
+    AMDG_CK(cudaMemsetAsync(b->d_err, 0, sizeof(int), st));
+    return fail(AMDG_ERR_TIMEOUT, "batch stage: a bulk copy did not complete within its wait limit; results are invalid");
 }
 
 // The concatenated element tables, neighbour lists and state of the batch's grids (as they are
@@ -114,24 +161,40 @@ amdg_status batch_build(amdg_batch* b) {
             b->graph_exec[p] = nullptr;
         }
     void* old[] = {b->d_row_ptr, b->d_src, b->d_blk, b->d_solve, b->d_blocks64, b->d_blocks32,
-                   b->d_u, b->d_u1, b->d_u2, b->d_shadow};
+                   b->d_u, b->d_u1, b->d_u2, b->d_shadow, b->d_lo, b->d_pairs, b->d_blocks32p};
     for (void* p : old) cudaFree(p);
     b->d_row_ptr = b->d_src = nullptr;
     b->d_blk = b->d_solve = nullptr;
     b->d_blocks64 = b->d_u = b->d_u1 = b->d_u2 = nullptr;
-    b->d_blocks32 = b->d_shadow = nullptr;
+    b->d_blocks32 = b->d_shadow = b->d_lo = b->d_blocks32p = nullptr;
+    b->d_pairs = nullptr;
     b->elem_offset = topo.elem_offset;
     b->num_elements = topo.elem_offset[n];
     b->dof = b->num_elements * b->block;
     b->pairs = int64_t(topo.src.size());
     b->num_blocks = topo.num_blocks;
     std::vector<float> b32(topo.blocks.begin(), topo.blocks.end());
+    // the ring kernel's tables padded to 16-byte blocks and its interleaved (src, blk) pairs
+    const int np = b->k + 1, bs = (np * np + 3) / 4 * 4;
+    std::vector<float> b32p(size_t(2) * b->num_blocks * bs, 0.f);
+    for (int64_t j = 0; j < int64_t(2) * b->num_blocks; ++j)
+        for (int i = 0; i < np * np; ++i) b32p[size_t(j) * bs + i] = b32[size_t(j) * np * np + i];
+    AMDG_REQUIRE(b->num_elements < (int64_t(1) << 31), AMDG_ERR_CAPACITY, "more than 2^31-1 elements in the batch");
+    std::vector<int32_t> pairs(2 * topo.src.size());
+    for (size_t i = 0; i < topo.src.size(); ++i) {
+        pairs[2 * i] = int32_t(topo.src[i]);
+        pairs[2 * i + 1] = topo.blk[i];
+    }
+    b->sstride = (b->dof + 3) / 4 * 4 + 4;
     amdg_status s;
     if ((s = put(&b->d_row_ptr, topo.row_ptr)) != AMDG_OK || (s = put(&b->d_src, topo.src)) != AMDG_OK ||
         (s = put(&b->d_blk, topo.blk)) != AMDG_OK || (s = put(&b->d_solve, topo.solve_of)) != AMDG_OK ||
         (s = put(&b->d_blocks64, topo.blocks)) != AMDG_OK || (s = put(&b->d_blocks32, b32)) != AMDG_OK ||
+        (s = put(&b->d_blocks32p, b32p)) != AMDG_OK || (s = put(&b->d_pairs, pairs)) != AMDG_OK ||
         (s = alloc(&b->d_u, size_t(b->dof))) != AMDG_OK || (s = alloc(&b->d_u1, size_t(b->dof))) != AMDG_OK ||
-        (s = alloc(&b->d_u2, size_t(b->dof))) != AMDG_OK || (s = alloc(&b->d_shadow, size_t(b->dof) * 3)) != AMDG_OK)
+        (s = alloc(&b->d_u2, size_t(b->dof))) != AMDG_OK ||
+        (s = alloc(&b->d_shadow, size_t(b->sstride) * 3)) != AMDG_OK ||
+        (s = alloc(&b->d_lo, size_t(b->sstride) * 3)) != AMDG_OK)
         return s;
     cudaStream_t st = stream_of(b);
     for (int i = 0; i < n; ++i)
@@ -141,37 +204,44 @@ amdg_status batch_build(amdg_batch* b) {
     return AMDG_OK;
 }
 
-// Autotuner of the stage kernel's tile: for each precision, time one stage
-// (the first RK stage from the current state into the scratch vectors, best of
-// three after a warm-up) with every CTA size the dimension supports and keep
-// the fastest.  Batches under 100,000 DOF keep 256 threads.
+// Autotuner of the stage kernel: for each precision, time one stage (the first RK stage from the
+// current state into the scratch vectors, best of three after a warm-up) with every candidate the
+// dimension supports -- the column kernel at each CTA size of kBatchTiles and, mixed only, the
+// bulk-copy ring kernel in each configuration -- and keep the fastest.  Batches under 100,000 DOF
+// keep the column kernel with 256 threads.
 amdg_status autotune_batch(amdg_batch* b, cudaStream_t st) {
     if (b->dof < 100000) return AMDG_OK;
     cudaEvent_t e0, e1;
     AMDG_CK(cudaEventCreate(&e0));
     AMDG_CK(cudaEventCreate(&e1));
     amdg_status status = AMDG_OK;
-    AMDG_CK(launch_to_float(b->d_u, b->d_shadow, b->dof, st));
+    AMDG_CK(launch_split(b->d_u, hi_of(b, 0), lo_of(b, 0), b->dof, st));
     const StageCoef c = coef_of(0);
     for (int pi = 0; pi < 2 && status == AMDG_OK; ++pi) {
         float best = 0.f;
-        for (int ci = 0; ci < 3; ++ci) {
-            const int th = kBatchTiles[ci];
-            if (!batch_tile_supported(b->dim, b->k + 1, th)) continue;
+        const int ncand = kBatchTileCount + (pi == 1 ? kBatchRingConfigs : 0);
+        for (int ci = 0; ci < ncand; ++ci) {
+            const bool ring = ci >= kBatchTileCount;
+            if (ring ? !batch_ring_supported(b->dim, b->k + 1, ci - kBatchTileCount)
+                     : !batch_tile_supported(b->dim, b->k + 1, kBatchTiles[ci]))
+                continue;
             float t_min = 0.f;
             for (int rep = 0; rep < 4 && status == AMDG_OK; ++rep) {
                 cudaError_t e = cudaEventRecord(e0, st);
-                if (pi == 1) {
+                if (ring) {
+                    if (e == cudaSuccess && ring_stage(b, ci - kBatchTileCount, 0, 0, 1, st) != AMDG_OK)
+                        e = cudaErrorLaunchFailure;
+                } else if (pi == 1) {
                     BatchLaunch<float, float> L{};
-                    L.dim = b->dim; L.np = b->k + 1; L.mode = 1; L.a = c.a; L.b = c.b; L.threads = th;
+                    L.dim = b->dim; L.np = b->k + 1; L.mode = 1; L.a = c.a; L.b = c.b; L.threads = kBatchTiles[ci];
                     L.num_elements = b->num_elements; L.num_blocks = b->num_blocks;
-                    L.us = b->d_u; L.xs = b->d_shadow; L.un = b->d_u; L.out = b->d_u1; L.shadow_out = b->d_shadow + b->dof;
+                    L.us = b->d_u; L.xs = hi_of(b, 0); L.un = b->d_u; L.out = b->d_u1; L.shadow_out = hi_of(b, 1);
                     L.row_ptr = b->d_row_ptr; L.src = b->d_src; L.blk = b->d_blk; L.blocks = b->d_blocks32;
                     L.coef = b->d_coef32; L.dt = b->d_dt; L.solve_of = b->d_solve;
                     if (e == cudaSuccess) e = launch_batch<float, float>(L, st);
                 } else {
                     BatchLaunch<double, double> L{};
-                    L.dim = b->dim; L.np = b->k + 1; L.mode = 1; L.a = c.a; L.b = c.b; L.threads = th;
+                    L.dim = b->dim; L.np = b->k + 1; L.mode = 1; L.a = c.a; L.b = c.b; L.threads = kBatchTiles[ci];
                     L.num_elements = b->num_elements; L.num_blocks = b->num_blocks;
                     L.us = b->d_u; L.xs = b->d_u; L.un = b->d_u; L.out = b->d_u1; L.shadow_out = nullptr;
                     L.row_ptr = b->d_row_ptr; L.src = b->d_src; L.blk = b->d_blk; L.blocks = b->d_blocks64;
@@ -188,15 +258,16 @@ amdg_status autotune_batch(amdg_batch* b, cudaStream_t st) {
                 }
                 if (rep > 0 && (t_min == 0.f || ms < t_min)) t_min = ms;  // rep 0 warms up
             }
-            b->tile_ms[pi][ci] = t_min;
+            b->kernel_ms[pi][ci] = t_min;
             if (status == AMDG_OK && (best == 0.f || t_min < best)) {
                 best = t_min;
-                b->tile[pi] = th;
+                b->kernel[pi] = ci;
             }
         }
     }
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
+    if (status == AMDG_OK) status = check_ring_waits(b, st);
     return status;
 }
 
@@ -228,9 +299,12 @@ amdg_status amdg_batch_create(amdg_context* ctx, int n, amdg_grid* const* grids,
     std::vector<double> c64(coef, coef + size_t(n) * dim);
     std::vector<float> c32(c64.begin(), c64.end());
     std::vector<double> dt(n, 0.0);
+    std::vector<float> dt32(n, 0.f);
+    std::vector<int> err0(1, 0);
     amdg_status s;
     if ((s = put(&b->d_coef64, c64)) != AMDG_OK || (s = put(&b->d_coef32, c32)) != AMDG_OK ||
-        (s = put(&b->d_dt, dt)) != AMDG_OK || (s = batch_build(b)) != AMDG_OK) {
+        (s = put(&b->d_dt, dt)) != AMDG_OK || (s = put(&b->d_dt32, dt32)) != AMDG_OK ||
+        (s = put(&b->d_err, err0)) != AMDG_OK || (s = batch_build(b)) != AMDG_OK) {
         amdg_batch_destroy(b);
         return s;
     }
@@ -243,30 +317,41 @@ amdg_status amdg_batch_create(amdg_context* ctx, int n, amdg_grid* const* grids,
     return AMDG_OK;
 }
 
-amdg_status amdg_batch_tuning(const amdg_batch* b, int* tile, float* stage_ms) {
+amdg_status amdg_batch_tuning(const amdg_batch* b, int* kernel, float* stage_ms) {
     AMDG_REQUIRE(b, AMDG_ERR_ARG, "batch is null");
-    if (tile) {
-        tile[0] = b->tile[0];
-        tile[1] = b->tile[1];
+    if (kernel) {
+        kernel[0] = b->kernel[0];
+        kernel[1] = b->kernel[1];
     }
     if (stage_ms)
         for (int p = 0; p < 2; ++p)
-            for (int c = 0; c < 3; ++c) stage_ms[p * 3 + c] = b->tile_ms[p][c];
+            for (int c = 0; c < AMDG_BATCH_KERNELS; ++c) stage_ms[p * AMDG_BATCH_KERNELS + c] = b->kernel_ms[p][c];
+    return AMDG_OK;
+}
+
+amdg_status amdg_batch_set_kernel(amdg_batch* b, amdg_precision prec, int kernel) {
+    AMDG_REQUIRE(b, AMDG_ERR_ARG, "batch is null");
+    AMDG_REQUIRE(prec == AMDG_PREC_FP64 || prec == AMDG_PREC_MIXED, AMDG_ERR_ARG, "bad precision");
+    const bool ok = kernel >= 0 && kernel < AMDG_BATCH_KERNELS &&
+                    (kernel < kBatchTileCount ? batch_tile_supported(b->dim, b->k + 1, kBatchTiles[kernel])
+                                              : prec == AMDG_PREC_MIXED &&
+                                                    batch_ring_supported(b->dim, b->k + 1, kernel - kBatchTileCount));
+    AMDG_REQUIRE(ok, AMDG_ERR_ARG, "unsupported stage kernel for this dimension and precision");
+    const int pi = prec == AMDG_PREC_MIXED ? 1 : 0;
+    if (b->kernel[pi] != kernel && b->graph_exec[pi]) {
+        AMDG_CK(cudaSetDevice(b->device));
+        cudaGraphExecDestroy(static_cast<cudaGraphExec_t>(b->graph_exec[pi]));
+        b->graph_exec[pi] = nullptr;
+    }
+    b->kernel[pi] = kernel;
     return AMDG_OK;
 }
 
 amdg_status amdg_batch_set_tile(amdg_batch* b, amdg_precision prec, int threads) {
     AMDG_REQUIRE(b, AMDG_ERR_ARG, "batch is null");
-    AMDG_REQUIRE(prec == AMDG_PREC_FP64 || prec == AMDG_PREC_MIXED, AMDG_ERR_ARG, "bad precision");
-    AMDG_REQUIRE(batch_tile_supported(b->dim, b->k + 1, threads), AMDG_ERR_ARG, "unsupported CTA size for this dimension");
-    const int pi = prec == AMDG_PREC_MIXED ? 1 : 0;
-    if (b->tile[pi] != threads && b->graph_exec[pi]) {
-        AMDG_CK(cudaSetDevice(b->device));
-        cudaGraphExecDestroy(static_cast<cudaGraphExec_t>(b->graph_exec[pi]));
-        b->graph_exec[pi] = nullptr;
-    }
-    b->tile[pi] = threads;
-    return AMDG_OK;
+    for (int c = 0; c < kBatchTileCount; ++c)
+        if (kBatchTiles[c] == threads) return amdg_batch_set_kernel(b, prec, c);
+    return fail(AMDG_ERR_ARG, "unsupported CTA size");
 }
 
 amdg_status amdg_batch_destroy(amdg_batch* b) {
@@ -275,7 +360,8 @@ amdg_status amdg_batch_destroy(amdg_batch* b) {
     for (int p = 0; p < 2; ++p)
         if (b->graph_exec[p]) cudaGraphExecDestroy(static_cast<cudaGraphExec_t>(b->graph_exec[p]));
     void* ptrs[] = {b->d_row_ptr, b->d_src, b->d_blk, b->d_solve, b->d_blocks64, b->d_blocks32, b->d_coef64,
-                    b->d_coef32, b->d_dt, b->d_u, b->d_u1, b->d_u2, b->d_shadow, b->d_pg, b->d_feat, b->d_prob, b->d_norms};
+                    b->d_coef32, b->d_dt, b->d_u, b->d_u1, b->d_u2, b->d_shadow, b->d_lo, b->d_pairs,
+                    b->d_blocks32p, b->d_dt32, b->d_err, b->d_pg, b->d_feat, b->d_prob, b->d_norms};
     for (void* p : ptrs) cudaFree(p);
     delete b;
     return AMDG_OK;
@@ -293,7 +379,10 @@ amdg_status amdg_batch_set_dt(amdg_batch* b, const double* dt) {
     AMDG_REQUIRE(b && dt, AMDG_ERR_ARG, "null argument");
     for (int i = 0; i < b->nsolves; ++i) AMDG_REQUIRE(std::isfinite(dt[i]), AMDG_ERR_ARG, "non-finite dt");
     AMDG_CK(cudaSetDevice(b->device));
+    std::vector<float> dt32(dt, dt + b->nsolves);
     AMDG_CK(cudaMemcpyAsync(b->d_dt, dt, size_t(b->nsolves) * sizeof(double), cudaMemcpyHostToDevice, stream_of(b)));
+    AMDG_CK(cudaMemcpyAsync(b->d_dt32, dt32.data(), size_t(b->nsolves) * sizeof(float), cudaMemcpyHostToDevice,
+                            stream_of(b)));
     AMDG_CK(cudaStreamSynchronize(stream_of(b)));
     return AMDG_OK;
 }
@@ -305,17 +394,29 @@ amdg_status amdg_batch_rk3_steps(amdg_batch* b, int nsteps, amdg_precision prec,
     cudaStream_t st = stream_of(b);
     const int pi = prec == AMDG_PREC_MIXED ? 1 : 0;
     if (nsteps == 0) return AMDG_OK;
-    if (prec == AMDG_PREC_MIXED) {
-        AMDG_CK(launch_to_float(b->d_u, b->d_shadow, b->dof, st));
+    const bool ring = ring_kernel(b, pi);
+    if (ring) {  // the FP32-pair state for the whole call: split once here, merged once at the end
+        AMDG_CK(launch_split(b->d_u, hi_of(b, 0), lo_of(b, 0), b->dof, st));
+        b->ctx->launches++;
+    } else if (prec == AMDG_PREC_MIXED) {
+        AMDG_CK(launch_to_float(b->d_u, hi_of(b, 0), b->dof, st));
         b->ctx->launches++;
     }
+    // after the steps: the ring kernel's wait check, then the merge (a wait that gave up leaves d_u)
+    auto finish = [&]() -> amdg_status {
+        if (!ring) return AMDG_OK;
+        if (amdg_status r = check_ring_waits(b, st); r != AMDG_OK) return r;
+        AMDG_CK(launch_merge(hi_of(b, 0), lo_of(b, 0), b->d_u, b->dof, st));
+        b->ctx->launches++;
+        return AMDG_OK;
+    };
     if (!use_graph) {
         for (int s = 0; s < nsteps; ++s) {
             amdg_status r = batch_step(b, prec, st);
             if (r != AMDG_OK) return r;
             b->ctx->launches += 3;
         }
-        return AMDG_OK;
+        return finish();
     }
     if (!b->graph_exec[pi]) {
         // capture one step (three launches) once; pointers and the dt array are fixed
@@ -335,7 +436,7 @@ amdg_status amdg_batch_rk3_steps(amdg_batch* b, int nsteps, amdg_precision prec,
         AMDG_CK(cudaGraphLaunch(static_cast<cudaGraphExec_t>(b->graph_exec[pi]), st));
         b->ctx->launches += 3;
     }
-    return AMDG_OK;
+    return finish();
 }
 
 amdg_status amdg_batch_store(amdg_batch* b, int solve) {

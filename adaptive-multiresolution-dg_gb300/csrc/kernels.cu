@@ -666,6 +666,192 @@ bool linear_mma_supported(int dim, int np) {
     return np >= 2 && np <= 4 && mma_fits(B, np);
 }
 
+// ---- batched solves on the bulk-copy ring with the FP32-pair stage state ------------------------
+// linear_tma_kernel for a batch of independent solves: element e belongs to solve s = solve_of[e],
+// whose velocity c_s,t scales dimension t's contraction after the sum over neighbours (the 1D blocks
+// u_vx + upwind flux come from the table of the flux side sign(c_s,t)) and whose step dt_s enters
+// the double-float stage update.  Same ring, bounded waits and drain as linear_tma_kernel.
+template <int D, int NP, int kRing, int WPC>
+__global__ void __launch_bounds__(32 * WPC) batch_ring_kernel(BatchRingLaunch L) {
+    constexpr int B = IPow<NP, D>::v;
+    constexpr int C = B / NP;
+    constexpr int CPT = (C + 31) / 32;
+    constexpr int BS = (NP * NP + 3) / 4 * 4;
+    constexpr int DATA = (B + 3) / 4 * 4 + 4;
+    __shared__ __align__(128) float ring_all[WPC * kRing * DATA];
+    __shared__ float y_all[WPC * B];
+    __shared__ __align__(8) uint64_t full_all[WPC * kRing];
+    __shared__ int lead_all[WPC * kRing];
+    __shared__ int bidx_all[WPC * kRing];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    float* ring = ring_all + warp * kRing * DATA;
+    float* y = y_all + warp * B;
+    uint64_t* full = full_all + warp * kRing;
+    int* lead = lead_all + warp * kRing;
+    int* bidx = bidx_all + warp * kRing;
+    const int64_t e = int64_t(blockIdx.x) * WPC + warp;
+    if (e >= L.num_elements) return;
+    const int solve = __ldg(L.solve_of + e);
+    for (int i = lane; i < B; i += 32) y[i] = 0.f;
+    const int64_t beg = __ldg(L.row_ptr + e * D);
+    const int n = int(__ldg(L.row_ptr + e * D + D) - beg);
+    if (lane == 0) {
+        for (int b = 0; b < kRing; ++b) mbar_init(&full[b], 1);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    __syncwarp();
+    int issued = 0, idim = 0;
+    auto issue = [&]() {  // next neighbour into slot issued % kRing (lane 0)
+        const int kk = issued;
+        while (kk >= int(__ldg(L.row_ptr + e * D + idim + 1) - beg)) ++idim;
+        const int2 pr = __ldg(L.pairs + beg + kk);
+        const uintptr_t a = reinterpret_cast<uintptr_t>(L.xs + int64_t(pr.x) * B);
+        const uintptr_t a0 = a & ~uintptr_t(15);
+        const uint32_t bytes = uint32_t(((a + uintptr_t(B) * 4 + 15) & ~uintptr_t(15)) - a0);
+        const int sl = kk % kRing;
+        lead[sl] = int((a - a0) / 4);
+        const int side = __ldg(L.coef + solve * D + idim) >= 0.f ? 0 : 1;
+        bidx[sl] = side * L.num_blocks + pr.y;
+        mbar_expect_tx(&full[sl], bytes);
+        bulk_copy_g2s(ring + sl * DATA, reinterpret_cast<const void*>(a0), bytes, &full[sl]);
+        ++issued;
+    };
+    if (lane == 0)
+        while (issued < n && issued < kRing) issue();
+    __syncwarp();
+    bool failed = false;
+    int k = 0, slot = 0;
+    uint32_t parity = 0;
+    for (int t = 0; t < D && !failed; ++t) {
+        int stride = 1;
+#pragma unroll
+        for (int s2 = t + 1; s2 < D; ++s2) stride *= NP;
+        int base[CPT];
+#pragma unroll
+        for (int j = 0; j < CPT; ++j) {
+            const int c = lane + 32 * j;
+            base[j] = (c / stride) * stride * NP + c % stride;
+        }
+        float acc[CPT][NP];
+#pragma unroll
+        for (int j = 0; j < CPT; ++j)
+#pragma unroll
+            for (int q = 0; q < NP; ++q) acc[j][q] = 0.f;
+        const int kend = int(__ldg(L.row_ptr + e * D + t + 1) - beg);
+        for (; k < kend; ++k) {
+            float m[BS];
+            {
+                const float4* g4 = reinterpret_cast<const float4*>(L.blocks + size_t(bidx[slot]) * BS);
+#pragma unroll
+                for (int jj = 0; jj < BS / 4; ++jj) {
+                    const float4 v = __ldg(g4 + jj);
+                    m[4 * jj] = v.x; m[4 * jj + 1] = v.y; m[4 * jj + 2] = v.z; m[4 * jj + 3] = v.w;
+                }
+            }
+            const bool ok = mbar_wait_bounded(&full[slot], (parity >> slot) & 1u, L.wait_limit);
+            if (__any_sync(0xffffffffu, !ok)) {
+                failed = true;
+                break;
+            }
+            parity ^= 1u << slot;
+            const float* x = ring + slot * DATA + lead[slot];
+#pragma unroll
+            for (int j = 0; j < CPT; ++j) {
+                if (C % 32 == 0 || lane + 32 * j < C) {
+                    float xv[NP];
+#pragma unroll
+                    for (int p = 0; p < NP; ++p) xv[p] = x[base[j] + p * stride];
+#pragma unroll
+                    for (int p = 0; p < NP; ++p)
+#pragma unroll
+                        for (int q = 0; q < NP; ++q) acc[j][q] = fmaf(m[p * NP + q], xv[p], acc[j][q]);
+                }
+            }
+            __syncwarp();
+            if (lane == 0 && issued < n) {
+                asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+                issue();
+            }
+            __syncwarp();
+            slot = slot + 1 == kRing ? 0 : slot + 1;
+        }
+        if (failed) break;
+        const float ct = __ldg(L.coef + solve * D + t);
+#pragma unroll
+        for (int j = 0; j < CPT; ++j)
+            if (C % 32 == 0 || lane + 32 * j < C)
+#pragma unroll
+                for (int q = 0; q < NP; ++q) y[base[j] + q * stride] += ct * acc[j][q];
+        __syncwarp();
+    }
+    if (failed) {
+        if (lane == 0) {
+            atomicExch(L.err, 1);
+            for (int k2 = k; k2 < issued; ++k2) {
+                const int s2 = k2 % kRing;
+                mbar_wait_bounded(&full[s2], (parity >> s2) & 1u, 1u << 16);
+                parity ^= 1u << s2;
+            }
+        }
+        return;
+    }
+    DFState df = L.df;
+    df.dt = __ldg(L.dt + solve);
+    for (int i = lane; i < B; i += 32) df_stage_update(df, e * B + i, y[i]);
+}
+
+constexpr bool batch_ring_fits(int B, int np, int ring, int warps) {
+    return B / np <= 256 && size_t(warps) * (size_t(ring * ((B + 3) / 4 * 4 + 4)) + B) * sizeof(float) + 512 <= 48 * 1024;
+}
+
+template <int D, int NP, int R, int W>
+static cudaError_t launch_batch_ring_cfg(const BatchRingLaunch& L, cudaStream_t st) {
+    constexpr int B = IPow<NP, D>::v;
+    if constexpr (!batch_ring_fits(B, NP, R, W)) {
+        return cudaErrorInvalidValue;
+    } else {
+        if (L.num_elements == 0) return cudaSuccess;
+        batch_ring_kernel<D, NP, R, W><<<unsigned((L.num_elements + W - 1) / W), 32 * W, 0, st>>>(L);
+        return cudaGetLastError();
+    }
+}
+
+template <int D, int NP>
+static cudaError_t launch_batch_ring_t(const BatchRingLaunch& L, cudaStream_t st) {
+    switch (L.cfg) {
+        case 0: return launch_batch_ring_cfg<D, NP, 1, 1>(L, st);
+        case 1: return launch_batch_ring_cfg<D, NP, 1, 2>(L, st);
+        case 2: return launch_batch_ring_cfg<D, NP, 1, 4>(L, st);
+        case 3: return launch_batch_ring_cfg<D, NP, 2, 1>(L, st);
+        case 4: return launch_batch_ring_cfg<D, NP, 2, 2>(L, st);
+        case 5: return launch_batch_ring_cfg<D, NP, 2, 4>(L, st);
+        default: return cudaErrorInvalidValue;
+    }
+}
+
+constexpr int kBatchRingShape[kBatchRingConfigs][2] = {{1, 1}, {1, 2}, {1, 4}, {2, 1}, {2, 2}, {2, 4}};
+
+bool batch_ring_supported(int dim, int np, int cfg) {
+    if (cfg < 0 || cfg >= kBatchRingConfigs || np < 2 || np > 4 || dim < 1 || dim > 6) return false;
+    int B = 1;
+    for (int d = 0; d < dim; ++d) B *= np;
+    return batch_ring_fits(B, np, kBatchRingShape[cfg][0], kBatchRingShape[cfg][1]);
+}
+
+cudaError_t launch_batch_ring(const BatchRingLaunch& L, cudaStream_t st) {
+    if (!batch_ring_supported(L.dim, L.np, L.cfg)) return cudaErrorInvalidValue;
+#define AMDG_RCASE(D, NP) \
+    if (L.dim == D && L.np == NP) return launch_batch_ring_t<D, NP>(L, st);
+    AMDG_RCASE(1, 2) AMDG_RCASE(1, 3) AMDG_RCASE(1, 4)
+    AMDG_RCASE(2, 2) AMDG_RCASE(2, 3) AMDG_RCASE(2, 4)
+    AMDG_RCASE(3, 2) AMDG_RCASE(3, 3) AMDG_RCASE(3, 4)
+    AMDG_RCASE(4, 2) AMDG_RCASE(4, 3) AMDG_RCASE(4, 4)
+    AMDG_RCASE(5, 2) AMDG_RCASE(5, 3) AMDG_RCASE(5, 4)
+    AMDG_RCASE(6, 2) AMDG_RCASE(6, 3)
+#undef AMDG_RCASE
+    return cudaErrorInvalidValue;
+}
+
 template <int D, int NP>
 static cudaError_t launch_tma_t(const LinearLaunch& L, cudaStream_t st) {
     switch (L.tma_cfg) {

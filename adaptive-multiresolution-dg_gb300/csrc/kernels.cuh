@@ -81,9 +81,33 @@ struct BatchLaunch {
 };
 template <typename T, typename X>
 cudaError_t launch_batch(const BatchLaunch<T, X>& L, cudaStream_t st);
-// CTA sizes launch_batch offers for a dimension (all of them fit at least one element)
-constexpr int kBatchTiles[3] = {128, 256, 512};
+// CTA sizes launch_batch offers (those of at least (k+1)^(dim-1) threads fit at least one element)
+constexpr int kBatchTileCount = 5;
+constexpr int kBatchTiles[kBatchTileCount] = {64, 128, 256, 512, 1024};
 bool batch_tile_supported(int dim, int np, int threads);
+
+// Batched solves on the bulk-copy ring (kernels.cu, batch_ring_kernel): the stage input's FP32
+// high parts (xs) stream into shared memory by bulk copies, the stage vectors are FP32 (hi, lo)
+// pairs (df; df.dt unused: dt[solve] per element), one warp per element.  Configurations cfg:
+// (ring slots, elements per CTA) = (1, 1), (1, 2), (1, 4), (2, 1), (2, 2), (2, 4).
+constexpr int kBatchRingConfigs = 6;
+struct BatchRingLaunch {
+    int dim, np, cfg;
+    int64_t num_elements;
+    int num_blocks;
+    const int64_t* row_ptr;  // CSR over (element, dimension)
+    const int2* pairs;       // (src, blk)
+    const float* blocks;     // [2][num_blocks][(np^2 + 3) / 4 * 4]: the two flux sides, padded
+    const float* coef;       // [solve][dim]
+    const float* dt;         // [solve]
+    const int32_t* solve_of; // [element]
+    const float* xs;         // stage input, high parts (16-byte aligned base, 16 bytes of slack)
+    DFState df;
+    int* err;
+    uint32_t wait_limit;
+};
+bool batch_ring_supported(int dim, int np, int cfg);
+cudaError_t launch_batch_ring(const BatchRingLaunch& L, cudaStream_t st);
 
 constexpr int kReduceBlocks = 1216;  // 8 CTAs per SM on 152 SMs
 

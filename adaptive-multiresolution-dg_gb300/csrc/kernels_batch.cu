@@ -5,8 +5,8 @@
 // (u_vx + upwind flux, one table per flux side), and the solve's dt enters
 // the fused SSP-RK3 epilogue.  Column layout as linear_col_kernel; the CTA
 // size TH (the tile: TH / np^(dim-1) elements per CTA) is a template
-// parameter the batch's autotuner picks (128, 256 or 512 threads for
-// dim <= 3, 256 above).
+// parameter the batch's autotuner picks (64 to 1024 threads for dim <= 3,
+// 256 above), beside the bulk-copy ring kernel of kernels.cu.
 #include <cuda_runtime.h>
 
 #include <cstdint>
@@ -87,7 +87,7 @@ bool batch_tile_supported(int dim, int np, int threads) {
     int c = 1;
     for (int d = 1; d < dim; ++d) c *= np;
     if (threads < c) return false;
-    if (dim <= 3) return threads == 128 || threads == 256 || threads == 512;
+    if (dim <= 3) return threads == 64 || threads == 128 || threads == 256 || threads == 512 || threads == 1024;
     return threads == 256;
 }
 
@@ -108,8 +108,10 @@ cudaError_t launch_batch(const BatchLaunch<T, X>& L, cudaStream_t st) {
     if (!batch_tile_supported(L.dim, L.np, th)) return cudaErrorInvalidValue;
 #define AMDG_BCASE3(D, NP)                                                            \
     if (L.dim == D && L.np == NP) {                                                    \
+        if (th == 64) return launch_batch_tile<D, NP, 64, T, X>(L, st);                \
         if (th == 128) return launch_batch_tile<D, NP, 128, T, X>(L, st);              \
         if (th == 512) return launch_batch_tile<D, NP, 512, T, X>(L, st);              \
+        if (th == 1024) return launch_batch_tile<D, NP, 1024, T, X>(L, st);            \
         return launch_batch_tile<D, NP, 256, T, X>(L, st);                             \
     }
 #define AMDG_BCASE1(D, NP) \

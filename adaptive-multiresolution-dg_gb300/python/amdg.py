@@ -157,6 +157,7 @@ def load():
         "amdg_batch_coefficients_device": ([vp, pp, vp], i32),
         "amdg_batch_tuning": ([vp, vp, vp], i32),
         "amdg_batch_adapt": ([vp, vp, dbl, dbl, dbl, vp], i32),
+        "amdg_batch_set_kernel": ([vp, i32, i32], i32),
         "amdg_batch_set_tile": ([vp, i32, i32], i32),
         "amdg_burgers_destroy": ([vp], i32),
         "amdg_burgers_rhs": ([vp, vp, vp, i32], i32),
@@ -799,12 +800,28 @@ class Batch:
             g._refresh()
         return stats
 
+    # stage-kernel candidates: the column kernel at these CTA sizes, then the bulk-copy ring kernel
+    # (mixed only) in these (ring slots, elements per CTA) configurations
+    TILES = (64, 128, 256, 512, 1024)
+    RING_CONFIGS = ((1, 1), (1, 2), (1, 4), (2, 1), (2, 2), (2, 4))
+    KERNELS = len(TILES) + len(RING_CONFIGS)
+
+    @classmethod
+    def kernel_name(cls, c: int) -> str:
+        if c < len(cls.TILES):
+            return f"column {cls.TILES[c]} threads"
+        r, w = cls.RING_CONFIGS[c - len(cls.TILES)]
+        return f"bulk-copy ring {r} slot{'s' if r > 1 else ''}, {w} element{'s' if w > 1 else ''} per CTA"
+
     def tuning(self):
-        """(CTA size per precision [FP64, mixed], stage ms per candidate [2][128, 256, 512 threads])."""
-        tile = np.zeros(2, np.int32)
-        ms = np.zeros(6, np.float32)
-        _ck(load().amdg_batch_tuning(self._h, _ptr(tile), _ptr(ms)), "batch_tuning")
-        return tile.tolist(), ms.reshape(2, 3).tolist()
+        """(stage-kernel candidate per precision [FP64, mixed], stage ms per candidate [2][KERNELS])."""
+        k = np.zeros(2, np.int32)
+        ms = np.zeros(2 * self.KERNELS, np.float32)
+        _ck(load().amdg_batch_tuning(self._h, _ptr(k), _ptr(ms)), "batch_tuning")
+        return k.tolist(), ms.reshape(2, self.KERNELS).tolist()
+
+    def set_kernel(self, prec: int, kernel: int):
+        _ck(load().amdg_batch_set_kernel(self._h, prec, kernel), "batch_set_kernel")
 
     def set_tile(self, prec: int, threads: int):
         _ck(load().amdg_batch_set_tile(self._h, prec, threads), "batch_set_tile")

@@ -370,6 +370,9 @@ def run_ours(args):
     }
     if args.learn_runs > 0:
         line["burgers3d_adaptive"] = bench_config3_arms(cfg, args, plain)
+        m = line["burgers3d_adaptive"]["metric"]
+        line["metric_at_matched_error"] = {k: v for k, v in m.items()
+                                           if k != "network_gain_vs_criterion_same_horizon_and_eps"}
     lin = bench_linear6d(ctx, stream, args, world)
     lin_cpu = lin.pop("_cpu")
     line["linear6d"] = lin
@@ -841,12 +844,16 @@ def bench_batched(ctx, stream, args):
     import amdg
     import amdg_oracle as O
     work = O.batched_workload(args.batch_solves, seed=0)
+    # each solve's refine threshold log-uniform in [batch_eps_min, batch_eps_max] (seeded): grid sizes
+    # from about 10^3 to 10^5 elements
+    lo, hi = math.log(args.batch_eps_min), math.log(args.batch_eps_max)
+    eps_of = np.exp(np.random.default_rng(7).uniform(lo, hi, len(work)))
     t0 = time.perf_counter()
     grids = []
-    for w in work:
+    for w, eps in zip(work, eps_of):
         g = amdg.Grid(ctx, 3, 8, 2, level_init=2)
         g.init_separable_adaptive(O.gaussian_bump_terms(w["centers"], w["widths"], w["amplitudes"], vectorized=True),
-                                  args.batch_eps, vectorized=True)
+                                  float(eps), vectorized=True)
         grids.append(g)
     init_s = time.perf_counter() - t0
     sizes = [g.num_elements for g in grids]
@@ -854,9 +861,10 @@ def bench_batched(ctx, stream, args):
     for g, w in zip(grids, work):
         lv = g.max_mesh_level()
         dts.append(CFL / sum(abs(v) * 2.0 ** int(m) for v, m in zip(w["velocity"], lv)))
-    out = {"workload": f"{len(work)} independent 3D linear advection solves, adaptive N<=8, k=2, seed 0",
+    out = {"workload": f"{len(work)} independent 3D linear advection solves, adaptive N<=8, k=2, seed 0, "
+                       f"refine threshold per solve log-uniform in [{args.batch_eps_min:g}, {args.batch_eps_max:g}]",
            "solves": len(work), "elements_min": min(sizes), "elements_max": max(sizes),
-           "elements_total": sum(sizes), "init_s": init_s, "eps": args.batch_eps}
+           "elements_median": int(np.median(sizes)), "elements_total": sum(sizes), "init_s": init_s}
     for name, prec in (("fp64", amdg.FP64), ("mixed", amdg.MIXED)):
         batch = amdg.Batch(ctx, grids, [w["velocity"] for w in work])
         batch.set_dt(dts)
@@ -868,12 +876,19 @@ def bench_batched(ctx, stream, args):
         e.record(stream)
         torch.cuda.synchronize()
         sec = s.elapsed_time(e) / 1e3
-        tile, tile_ms = batch.tuning()
+        kernel, kernel_ms = batch.tuning()
         pi = 0 if prec == amdg.FP64 else 1
+        stage_s = kernel_ms[pi][kernel[pi]] / 1e3
+        # algorithmic bytes of one stage: 24 B per DOF (stage input, u^n, output) + 8 B per pair + 8 B per row
+        stage_bytes = 24.0 * batch.dof + 8.0 * batch.pairs + 8.0 * (batch.num_elements * 3 + 1)
+        pk, pk_kind = peaks()
         out[name] = {"value": 3.0 * batch.dof * args.steps / sec, "ms_per_step": sec / args.steps * 1e3,
                      "dof": batch.dof, "launches_per_step": 3,
-                     "autotuned_tile": {"cta_threads": tile[pi],
-                                        "stage_ms_by_cta_threads": dict(zip(("128", "256", "512"), tile_ms[pi]))}}
+                     "stage_kernel": amdg.Batch.kernel_name(kernel[pi]),
+                     "stage_ms_by_kernel": {amdg.Batch.kernel_name(c): t for c, t in enumerate(kernel_ms[pi]) if t > 0},
+                     "roofline": {"bound": "hbm", "achieved": stage_bytes / stage_s / 1e9, "peak": pk["hbm_gbs"],
+                                  "unit": "GB/s", "frac": stage_bytes / stage_s / 1e9 / pk["hbm_gbs"],
+                                  "peak_kind": pk_kind, "algorithmic_bytes_per_stage": stage_bytes}}
         errs = []
         nsteps = args.warmup + args.steps
         for i in range(0, len(work), max(1, len(work) // 16)):
@@ -1346,7 +1361,9 @@ def main():
     ap.add_argument("--eps-bisect", type=int, default=3,
                     help="bisection steps on the refine threshold of a horizon whose scales matched no error")
     ap.add_argument("--batch-solves", type=int, default=256)
-    ap.add_argument("--batch-eps", type=float, default=1e-5)
+    ap.add_argument("--batch-eps", type=float, default=1e-5, help="refine threshold of the adaptive batch")
+    ap.add_argument("--batch-eps-min", type=float, default=1e-8, help="smallest per-solve refine threshold")
+    ap.add_argument("--batch-eps-max", type=float, default=1e-5, help="largest per-solve refine threshold")
     ap.add_argument("--batch-adapt-every", type=int, default=20,
                     help="steps between adaptations of the batched solves' grids (0: skip that run)")
     ap.add_argument("--batch-adapt-solves", type=int, default=64, help="solves in the adaptive batched run")

@@ -439,12 +439,21 @@ amdg_status amdg_batch_coefficients_device(amdg_batch* b, double** device_ptr, i
  * the finest levels changed.  stats (may be NULL): [refined by the classifier, uncertain,
  * elements after]. */
 amdg_status amdg_batch_adapt(amdg_batch* b, amdg_mlp* mlp, double eps, double eta, double tau, int64_t* stats);
-/* Tile of the stage kernel: amdg_batch_create times one stage with CTAs of 128, 256 and 512
- * threads (threads / (k+1)^(dim-1) elements per CTA; dim <= 3, 256 only above) for each
- * precision and keeps the fastest (batches under 100,000 DOF keep 256).  tile[2] = chosen CTA
- * size (FP64, mixed); stage_ms[2][3] = measured stage times per candidate, 0 where not timed. */
-amdg_status amdg_batch_tuning(const amdg_batch* b, int* tile, float* stage_ms);
-/* Override the tile of one precision (AMDG_ERR_ARG if the dimension does not offer it). */
+/* Stage kernel of the batch: amdg_batch_create times one stage with every candidate and keeps
+ * the fastest per precision (batches under 100,000 DOF keep candidate 2).  Candidates 0-4: the
+ * column kernel with CTAs of 64, 128, 256, 512 and 1024 threads (threads / (k+1)^(dim-1) elements
+ * per CTA; dim <= 3, 256 only above).  Candidates 5-10, mixed only: one warp per element with the
+ * neighbour blocks streamed into shared memory by bulk asynchronous copies and the stage vectors
+ * kept as FP32 (hi, lo) pairs for the whole amdg_batch_rk3_steps call, in (ring slots, elements
+ * per CTA) = (1, 1), (1, 2), (1, 4), (2, 1), (2, 2), (2, 4); its waits are bounded, and a wait
+ * that gives up fails the call with AMDG_ERR_TIMEOUT and leaves the state as it was.
+ * kernel[2] = chosen candidate (FP64, mixed); stage_ms[2][AMDG_BATCH_KERNELS] = measured stage
+ * times per candidate, 0 where not timed. */
+#define AMDG_BATCH_KERNELS 11
+amdg_status amdg_batch_tuning(const amdg_batch* b, int* kernel, float* stage_ms);
+/* Override the stage kernel of one precision (AMDG_ERR_ARG where it is not offered). */
+amdg_status amdg_batch_set_kernel(amdg_batch* b, amdg_precision prec, int kernel);
+/* The column kernel with the given CTA size (candidates 0-4). */
 amdg_status amdg_batch_set_tile(amdg_batch* b, amdg_precision prec, int threads);
 
 /* Work counters since creation: RK-stage DOF updates (3 x DOF per SSP-RK3

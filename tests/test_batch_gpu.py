@@ -107,32 +107,72 @@ def test_batch_mixed_and_l2_error(ctx):
         assert abs(errs[(amdg.MIXED, i)] - errs[(amdg.FP64, i)]) <= 1e-3 * errs[(amdg.FP64, i)]
 
 
-def test_batch_tiles_agree_and_autotuner_picks_one(ctx):
-    """Every CTA size sums each output in the same order, so all tiles give bitwise the same
-    steps; a batch over 100,000 DOF is timed with every tile and keeps the fastest."""
+def test_batch_kernels_agree_and_autotuner_picks_one(ctx):
+    """Every CTA size of the column kernel sums each output in the same order (bitwise the same
+    steps); the bulk-copy ring configurations agree bitwise among themselves and, their stage
+    vectors being FP32 pairs instead of FP64, with the mixed column kernel to 1e-6.  A batch over
+    100,000 DOF is timed with every candidate and keeps the fastest."""
     work = O.batched_workload(8, seed=11)
     grids = _grids(ctx, work, 6, 1e-4)
     dts = [0.1 / (sum(abs(v) for v in w["velocity"]) * 64) for w in work]
+    K = amdg.Batch.KERNELS
     results = {}
     for prec in (amdg.FP64, amdg.MIXED):
-        for th in (128, 256, 512):
+        pi = 0 if prec == amdg.FP64 else 1
+        cands = range(K) if prec == amdg.MIXED else range(len(amdg.Batch.TILES))
+        for c in cands:
             batch = amdg.Batch(ctx, grids, [w["velocity"] for w in work])
             assert batch.dof > 100000
-            tile, ms = batch.tuning()
-            row = ms[0 if prec == amdg.FP64 else 1]
-            assert all(t > 0 for t in row)
-            assert tile[0 if prec == amdg.FP64 else 1] == (128, 256, 512)[int(np.argmin(row))]
-            batch.set_tile(prec, th)
+            kernel, ms = batch.tuning()
+            row = ms[pi]
+            timed = [i for i in range(K) if row[i] > 0]
+            assert set(timed) == set(cands)
+            assert kernel[pi] == min(timed, key=lambda i: row[i])
+            batch.set_kernel(prec, c)
             batch.set_dt(dts)
             batch.rk3_steps(2, prec, use_graph=True)
             ctx.synchronize()
             batch.store(3)
-            results[(prec, th)] = grids[3].coefficients().copy()
+            results[(prec, c)] = grids[3].coefficients().copy()
             batch.close()
             for g, w in zip(grids, work):  # restore the initial state for the next batch
                 g.init_separable(O.gaussian_bump_terms(w["centers"], w["widths"], w["amplitudes"]))
-        assert np.array_equal(results[(prec, 128)], results[(prec, 256)])
-        assert np.array_equal(results[(prec, 512)], results[(prec, 256)])
+        for c in range(1, len(amdg.Batch.TILES)):
+            assert np.array_equal(results[(prec, c)], results[(prec, 0)])
+    ring0 = len(amdg.Batch.TILES)
+    for c in range(ring0 + 1, K):
+        assert np.array_equal(results[(amdg.MIXED, c)], results[(amdg.MIXED, ring0)])
+    ref = results[(amdg.MIXED, 2)]
+    assert np.abs(results[(amdg.MIXED, ring0)] - ref).max() <= 1e-6 * np.abs(ref).max()
+    with pytest.raises(amdg.AmdgError):
+        batch = amdg.Batch(ctx, grids, [w["velocity"] for w in work])
+        try:
+            batch.set_kernel(amdg.FP64, ring0)
+        finally:
+            batch.close()
+    for g in grids:
+        g.close()
+
+
+@pytest.mark.parametrize("seed", [3, 8])
+def test_batch_ring_kernel_matches_oracle(ctx, seed):
+    """The bulk-copy ring kernel (FP32 contraction, FP32-pair stage state) against the oracle's
+    SSP-RK3 per solve, each at its own velocity and step: 1e-6 relative after 3 steps."""
+    work = O.batched_workload(5, seed=seed)
+    grids = _grids(ctx, work, 5, 1e-3)
+    u0 = [g.coefficients().copy() for g in grids]
+    dts = [0.1 / (sum(abs(v) for v in w["velocity"]) * 32) for w in work]
+    batch = amdg.Batch(ctx, grids, [w["velocity"] for w in work])
+    batch.set_kernel(amdg.MIXED, len(amdg.Batch.TILES))
+    batch.set_dt(dts)
+    batch.rk3_steps(3, amdg.MIXED, use_graph=False)
+    ctx.synchronize()
+    for i, (g, w) in enumerate(zip(grids, work)):
+        batch.store(i)
+        lv, sp = g.elements()
+        want = O.linear_rk3(3, g.nmax, 2, lv, sp, w["velocity"], u0[i], dts[i], 3)
+        assert np.abs(g.coefficients() - want).max() <= 1e-6 * np.abs(want).max(), f"solve {i}"
+    batch.close()
     for g in grids:
         g.close()
 

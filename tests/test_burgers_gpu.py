@@ -146,10 +146,12 @@ def test_sweep_variants_agree_bitwise(ctx, prec):
         g.close()
 
 
-@pytest.mark.parametrize("prec,tol", [(amdg.FP64, 1e-12), (amdg.MIXED, 1e-6)])
+@pytest.mark.parametrize("prec,tol", [(amdg.FP64, 1e-12), (amdg.MIXED, 1e-4)])
 def test_warp_sweep_variant_matches(ctx, prec, tol):
     """The warp-per-(term, element) sweep kernel sums in another fixed order: its right-hand sides
-    equal the thread-per-output kernel's to rounding (relative to the field's max), are
+    equal the thread-per-output kernel's to rounding (relative to the field's max; mixed: FP32
+    back transforms of a right-hand side that is a difference of large flux terms, the 1e-4 of the
+    mixed right-hand-side bar), are
     deterministic run to run, and in FP64 match the oracle to 5e-12 on the 3D sparse grid N = 6 and
     the 2D wave grid (degree-4 points, 5 -> 3 and 3 -> 5 transforms)."""
     cases = [("burgers", 3, 6, False), ("burgers", 2, 7, True), ("wave", 2, 6, False)]

@@ -296,8 +296,8 @@ def test_network_against_criterion_only_pre_adaptation(ctx):
     classifier (criterion where it is unsure) against pre-adaptation by the surplus criterion alone,
     same horizon, same thresholds, same mixed precision, 3D Burgers to t = 0.02.  The network
     refines ahead of the moving front (elements the criterion will refine within the horizon), so
-    it ends on more elements with a smaller error against the exact solution; the plain FP64 run is
-    the yardstick.  Wall times are printed, not asserted: on this workload the extra elements cost
+    its steps carry more DOF and it ends with a smaller error against the exact solution; the plain
+    FP64 run is the yardstick.  Wall times are printed, not asserted: on this workload the extra elements cost
     more than the network saves, and the criterion-only arm is the faster one."""
     dim, nmax, eps, eta, horizon, t_end = 3, 6, 2e-5, 2e-6, 4, 0.02
     x, y = _collect_horizon(ctx, dim, nmax, eps, eta, steps=10, seeds=range(3), horizon=horizon)
@@ -339,7 +339,7 @@ def test_network_against_criterion_only_pre_adaptation(ctx):
     net = run(mlp, horizon, amdg.MIXED)
     print(f"plain {plain}\ncriterion-only {crit}\nnetwork {net}")
     assert crit["net_refine"] == 0 and net["net_refine"] > 0
-    assert net["elements"] >= crit["elements"]
+    assert net["work"][0] >= crit["work"][0]  # RK-stage DOF updates over the run
     assert net["err"] <= crit["err"] * 1.001
     # both pre-adapted arms stay within a factor 2 of the plain run's error
     assert crit["err"] <= 2.0 * plain["err"] and net["err"] <= 2.0 * plain["err"]
