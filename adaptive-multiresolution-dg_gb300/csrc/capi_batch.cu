@@ -62,7 +62,14 @@ StageCoef coef_of(int stage) {
     }
 }
 
-bool ring_kernel(const amdg_batch* b, int pi) { return pi == 1 && b->kernel[1] >= kBatchTileCount; }
+// mixed-mode candidates: [kBatchTileCount, 2 kBatchTileCount) the column kernel on the FP32-pair
+// state, from 2 kBatchTileCount the bulk-copy ring kernel (on the same state)
+constexpr int kRingFirst = 2 * kBatchTileCount;
+bool df_state(const amdg_batch* b, int pi) { return pi == 1 && b->kernel[1] >= kBatchTileCount; }
+bool ring_kernel(const amdg_batch* b, int pi) { return pi == 1 && b->kernel[1] >= kRingFirst; }
+
+// one launch of the column kernel on the FP32-pair state: stage `stage`, slot in -> out
+amdg_status df_col_stage(amdg_batch* b, int threads, int stage, int in, int out, cudaStream_t st);
 
 // the stage-state arrays of the mixed mode: high and low parts of slot i
 float* hi_of(amdg_batch* b, int i) { return b->d_shadow + i * b->sstride; }
@@ -87,17 +94,37 @@ amdg_status ring_stage(amdg_batch* b, int cfg, int stage, int in, int out, cudaS
     return AMDG_OK;
 }
 
+amdg_status df_col_stage(amdg_batch* b, int threads, int stage, int in, int out, cudaStream_t st) {
+    const StageCoef c = coef_of(stage);
+    BatchLaunch<float, float> L{};
+    L.dim = b->dim; L.np = b->k + 1; L.mode = 1; L.a = c.a; L.b = c.b; L.threads = threads;
+    L.num_elements = b->num_elements; L.num_blocks = b->num_blocks;
+    L.xs = hi_of(b, in);
+    L.row_ptr = b->d_row_ptr; L.src = b->d_src; L.blk = b->d_blk; L.blocks = b->d_blocks32;
+    L.coef = b->d_coef32; L.dt = b->d_dt; L.solve_of = b->d_solve;
+    L.df = df_stage(c);
+    L.df.us_hi = hi_of(b, in); L.df.us_lo = lo_of(b, in);
+    L.df.un_hi = hi_of(b, 0); L.df.un_lo = lo_of(b, 0);
+    L.df.out_hi = hi_of(b, out); L.df.out_lo = lo_of(b, out);
+    L.dt32 = b->d_dt32;
+    AMDG_CK(launch_batch<float, float>(L, st));
+    return AMDG_OK;
+}
+
 // one SSP-RK3 step of every solve: three fused launches.  The ring kernel steps the FP32-pair
 // state (slots 0 -> 1 -> 2 -> 0, split from and merged into d_u by amdg_batch_rk3_steps); the
 // column kernel steps the FP64 state with FP32 shadows of the stage inputs (mixed) or in FP64.
 amdg_status batch_step(amdg_batch* b, amdg_precision prec, cudaStream_t st) {
     const int pi = prec == AMDG_PREC_MIXED ? 1 : 0;
-    if (ring_kernel(b, pi)) {
+    if (df_state(b, pi)) {
         const int in_i[3] = {0, 1, 2}, out_i[3] = {1, 2, 0};
-        for (int stage = 0; stage < 3; ++stage)
-            if (amdg_status r = ring_stage(b, b->kernel[1] - kBatchTileCount, stage, in_i[stage], out_i[stage], st);
-                r != AMDG_OK)
-                return r;
+        for (int stage = 0; stage < 3; ++stage) {
+            amdg_status r = ring_kernel(b, pi)
+                                ? ring_stage(b, b->kernel[1] - kRingFirst, stage, in_i[stage], out_i[stage], st)
+                                : df_col_stage(b, kBatchTiles[b->kernel[1] - kBatchTileCount], stage, in_i[stage],
+                                               out_i[stage], st);
+            if (r != AMDG_OK) return r;
+        }
         return AMDG_OK;
     }
     double* in[3] = {b->d_u, b->d_u1, b->d_u2};
@@ -219,21 +246,24 @@ amdg_status autotune_batch(amdg_batch* b, cudaStream_t st) {
     const StageCoef c = coef_of(0);
     for (int pi = 0; pi < 2 && status == AMDG_OK; ++pi) {
         float best = 0.f;
-        const int ncand = kBatchTileCount + (pi == 1 ? kBatchRingConfigs : 0);
+        const int ncand = pi == 1 ? kRingFirst + kBatchRingConfigs : kBatchTileCount;
         for (int ci = 0; ci < ncand; ++ci) {
-            const bool ring = ci >= kBatchTileCount;
-            if (ring ? !batch_ring_supported(b->dim, b->k + 1, ci - kBatchTileCount)
-                     : !batch_tile_supported(b->dim, b->k + 1, kBatchTiles[ci]))
+            const bool ring = ci >= kRingFirst, dfcol = ci >= kBatchTileCount && !ring;
+            const int tile = ring ? 0 : kBatchTiles[ci % kBatchTileCount];
+            if (ring ? !batch_ring_supported(b->dim, b->k + 1, ci - kRingFirst)
+                     : !batch_tile_supported(b->dim, b->k + 1, tile))
                 continue;
             float t_min = 0.f;
             for (int rep = 0; rep < 4 && status == AMDG_OK; ++rep) {
                 cudaError_t e = cudaEventRecord(e0, st);
                 if (ring) {
-                    if (e == cudaSuccess && ring_stage(b, ci - kBatchTileCount, 0, 0, 1, st) != AMDG_OK)
+                    if (e == cudaSuccess && ring_stage(b, ci - kRingFirst, 0, 0, 1, st) != AMDG_OK)
                         e = cudaErrorLaunchFailure;
+                } else if (dfcol) {
+                    if (e == cudaSuccess && df_col_stage(b, tile, 0, 0, 1, st) != AMDG_OK) e = cudaErrorLaunchFailure;
                 } else if (pi == 1) {
                     BatchLaunch<float, float> L{};
-                    L.dim = b->dim; L.np = b->k + 1; L.mode = 1; L.a = c.a; L.b = c.b; L.threads = kBatchTiles[ci];
+                    L.dim = b->dim; L.np = b->k + 1; L.mode = 1; L.a = c.a; L.b = c.b; L.threads = tile;
                     L.num_elements = b->num_elements; L.num_blocks = b->num_blocks;
                     L.us = b->d_u; L.xs = hi_of(b, 0); L.un = b->d_u; L.out = b->d_u1; L.shadow_out = hi_of(b, 1);
                     L.row_ptr = b->d_row_ptr; L.src = b->d_src; L.blk = b->d_blk; L.blocks = b->d_blocks32;
@@ -241,7 +271,7 @@ amdg_status autotune_batch(amdg_batch* b, cudaStream_t st) {
                     if (e == cudaSuccess) e = launch_batch<float, float>(L, st);
                 } else {
                     BatchLaunch<double, double> L{};
-                    L.dim = b->dim; L.np = b->k + 1; L.mode = 1; L.a = c.a; L.b = c.b; L.threads = kBatchTiles[ci];
+                    L.dim = b->dim; L.np = b->k + 1; L.mode = 1; L.a = c.a; L.b = c.b; L.threads = tile;
                     L.num_elements = b->num_elements; L.num_blocks = b->num_blocks;
                     L.us = b->d_u; L.xs = b->d_u; L.un = b->d_u; L.out = b->d_u1; L.shadow_out = nullptr;
                     L.row_ptr = b->d_row_ptr; L.src = b->d_src; L.blk = b->d_blk; L.blocks = b->d_blocks64;
@@ -332,10 +362,10 @@ amdg_status amdg_batch_tuning(const amdg_batch* b, int* kernel, float* stage_ms)
 amdg_status amdg_batch_set_kernel(amdg_batch* b, amdg_precision prec, int kernel) {
     AMDG_REQUIRE(b, AMDG_ERR_ARG, "batch is null");
     AMDG_REQUIRE(prec == AMDG_PREC_FP64 || prec == AMDG_PREC_MIXED, AMDG_ERR_ARG, "bad precision");
-    const bool ok = kernel >= 0 && kernel < AMDG_BATCH_KERNELS &&
-                    (kernel < kBatchTileCount ? batch_tile_supported(b->dim, b->k + 1, kBatchTiles[kernel])
-                                              : prec == AMDG_PREC_MIXED &&
-                                                    batch_ring_supported(b->dim, b->k + 1, kernel - kBatchTileCount));
+    bool ok = kernel >= 0 && kernel < AMDG_BATCH_KERNELS && (kernel < kBatchTileCount || prec == AMDG_PREC_MIXED);
+    if (ok)
+        ok = kernel < kRingFirst ? batch_tile_supported(b->dim, b->k + 1, kBatchTiles[kernel % kBatchTileCount])
+                                 : batch_ring_supported(b->dim, b->k + 1, kernel - kRingFirst);
     AMDG_REQUIRE(ok, AMDG_ERR_ARG, "unsupported stage kernel for this dimension and precision");
     const int pi = prec == AMDG_PREC_MIXED ? 1 : 0;
     if (b->kernel[pi] != kernel && b->graph_exec[pi]) {
@@ -394,8 +424,8 @@ amdg_status amdg_batch_rk3_steps(amdg_batch* b, int nsteps, amdg_precision prec,
     cudaStream_t st = stream_of(b);
     const int pi = prec == AMDG_PREC_MIXED ? 1 : 0;
     if (nsteps == 0) return AMDG_OK;
-    const bool ring = ring_kernel(b, pi);
-    if (ring) {  // the FP32-pair state for the whole call: split once here, merged once at the end
+    const bool ring = ring_kernel(b, pi), pairs_state = df_state(b, pi);
+    if (pairs_state) {  // the FP32-pair state for the whole call: split once here, merged once at the end
         AMDG_CK(launch_split(b->d_u, hi_of(b, 0), lo_of(b, 0), b->dof, st));
         b->ctx->launches++;
     } else if (prec == AMDG_PREC_MIXED) {
@@ -404,8 +434,9 @@ amdg_status amdg_batch_rk3_steps(amdg_batch* b, int nsteps, amdg_precision prec,
     }
     // after the steps: the ring kernel's wait check, then the merge (a wait that gave up leaves d_u)
     auto finish = [&]() -> amdg_status {
-        if (!ring) return AMDG_OK;
-        if (amdg_status r = check_ring_waits(b, st); r != AMDG_OK) return r;
+        if (!pairs_state) return AMDG_OK;
+        if (ring)
+            if (amdg_status r = check_ring_waits(b, st); r != AMDG_OK) return r;
         AMDG_CK(launch_merge(hi_of(b, 0), lo_of(b, 0), b->d_u, b->dof, st));
         b->ctx->launches++;
         return AMDG_OK;

@@ -78,6 +78,10 @@ struct BatchLaunch {
     const T* coef;           // [solve][dim] velocities
     const double* dt;        // [solve] step sizes
     const int32_t* solve_of; // [element]
+    // T = float only: with df.out_hi set the stage vectors are FP32 (hi, lo) pairs (df, the step of
+    // solve s is dt32[s]) and us / un / out / shadow_out are unused
+    DFState df;
+    const float* dt32;
 };
 template <typename T, typename X>
 cudaError_t launch_batch(const BatchLaunch<T, X>& L, cudaStream_t st);

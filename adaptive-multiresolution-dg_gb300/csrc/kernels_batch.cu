@@ -10,8 +10,10 @@
 #include <cuda_runtime.h>
 
 #include <cstdint>
+#include <type_traits>
 
 #include "kernels.cuh"
+#include "df_arith.cuh"
 
 namespace amdg {
 
@@ -76,6 +78,14 @@ __global__ void __launch_bounds__(TH) batch_col_kernel(BatchLaunch<T, X> L) {
         const int64_t gid = first + i;
         if (gid >= total) break;
         const int sv = __ldg(L.solve_of + gid / B);
+        if constexpr (std::is_same<T, float>::value) {
+            if (L.df.out_hi) {  // FP32-pair stage state: the double-float update with the solve's step
+                DFState df = L.df;
+                df.dt = __ldg(L.dt32 + sv);
+                df_stage_update(df, gid, float(y[i]));
+                continue;
+            }
+        }
         const double rhs = double(y[i]);
         const double v = L.mode == 0 ? rhs : batch_combine(L.a, L.un[gid], L.b, L.us[gid], L.dt[sv], rhs);
         L.out[gid] = v;

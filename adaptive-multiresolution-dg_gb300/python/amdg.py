@@ -804,13 +804,17 @@ class Batch:
     # (mixed only) in these (ring slots, elements per CTA) configurations
     TILES = (64, 128, 256, 512, 1024)
     RING_CONFIGS = ((1, 1), (1, 2), (1, 4), (2, 1), (2, 2), (2, 4))
-    KERNELS = len(TILES) + len(RING_CONFIGS)
+    DF_COLUMN_FIRST = len(TILES)       # the column kernel on the FP32-pair state (mixed)
+    RING_FIRST = 2 * len(TILES)        # the bulk-copy ring kernel (mixed)
+    KERNELS = 2 * len(TILES) + len(RING_CONFIGS)
 
     @classmethod
     def kernel_name(cls, c: int) -> str:
-        if c < len(cls.TILES):
+        if c < cls.DF_COLUMN_FIRST:
             return f"column {cls.TILES[c]} threads"
-        r, w = cls.RING_CONFIGS[c - len(cls.TILES)]
+        if c < cls.RING_FIRST:
+            return f"column {cls.TILES[c - cls.DF_COLUMN_FIRST]} threads, FP32-pair state"
+        r, w = cls.RING_CONFIGS[c - cls.RING_FIRST]
         return f"bulk-copy ring {r} slot{'s' if r > 1 else ''}, {w} element{'s' if w > 1 else ''} per CTA"
 
     def tuning(self):

@@ -442,14 +442,16 @@ amdg_status amdg_batch_adapt(amdg_batch* b, amdg_mlp* mlp, double eps, double et
 /* Stage kernel of the batch: amdg_batch_create times one stage with every candidate and keeps
  * the fastest per precision (batches under 100,000 DOF keep candidate 2).  Candidates 0-4: the
  * column kernel with CTAs of 64, 128, 256, 512 and 1024 threads (threads / (k+1)^(dim-1) elements
- * per CTA; dim <= 3, 256 only above).  Candidates 5-10, mixed only: one warp per element with the
- * neighbour blocks streamed into shared memory by bulk asynchronous copies and the stage vectors
- * kept as FP32 (hi, lo) pairs for the whole amdg_batch_rk3_steps call, in (ring slots, elements
- * per CTA) = (1, 1), (1, 2), (1, 4), (2, 1), (2, 2), (2, 4); its waits are bounded, and a wait
- * that gives up fails the call with AMDG_ERR_TIMEOUT and leaves the state as it was.
- * kernel[2] = chosen candidate (FP64, mixed); stage_ms[2][AMDG_BATCH_KERNELS] = measured stage
- * times per candidate, 0 where not timed. */
-#define AMDG_BATCH_KERNELS 11
+ * per CTA; dim <= 3, 256 only above) on the FP64 state (mixed: FP32 contraction, FP32 shadows of
+ * the stage inputs).  Mixed only: candidates 5-9, the same column kernel with the stage vectors
+ * kept as FP32 (hi, lo) pairs for the whole amdg_batch_rk3_steps call (split once, merged once,
+ * a double-float stage update); candidates 10-15, one warp per element with the neighbour blocks
+ * streamed into shared memory by bulk asynchronous copies, on the same FP32-pair state, in (ring
+ * slots, elements per CTA) = (1, 1), (1, 2), (1, 4), (2, 1), (2, 2), (2, 4) -- its waits are
+ * bounded, and a wait that gives up fails the call with AMDG_ERR_TIMEOUT and leaves the state as it
+ * was.  kernel[2] = chosen candidate (FP64, mixed); stage_ms[2][AMDG_BATCH_KERNELS] = measured
+ * stage times per candidate, 0 where not timed. */
+#define AMDG_BATCH_KERNELS 16
 amdg_status amdg_batch_tuning(const amdg_batch* b, int* kernel, float* stage_ms);
 /* Override the stage kernel of one precision (AMDG_ERR_ARG where it is not offered). */
 amdg_status amdg_batch_set_kernel(amdg_batch* b, amdg_precision prec, int kernel);

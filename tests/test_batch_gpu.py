@@ -109,9 +109,10 @@ def test_batch_mixed_and_l2_error(ctx):
 
 def test_batch_kernels_agree_and_autotuner_picks_one(ctx):
     """Every CTA size of the column kernel sums each output in the same order (bitwise the same
-    steps); the bulk-copy ring configurations agree bitwise among themselves and, their stage
-    vectors being FP32 pairs instead of FP64, with the mixed column kernel to 1e-6.  A batch over
-    100,000 DOF is timed with every candidate and keeps the fastest."""
+    steps); on the FP32-pair stage state the column tiles and the bulk-copy ring configurations
+    agree bitwise with each other and, their stage vectors being FP32 pairs instead of FP64, with
+    the mixed column kernel on the FP64 state to 1e-6.  A batch over 100,000 DOF is timed with every
+    candidate and keeps the fastest."""
     work = O.batched_workload(8, seed=11)
     grids = _grids(ctx, work, 6, 1e-4)
     dts = [0.1 / (sum(abs(v) for v in w["velocity"]) * 64) for w in work]
@@ -139,11 +140,12 @@ def test_batch_kernels_agree_and_autotuner_picks_one(ctx):
                 g.init_separable(O.gaussian_bump_terms(w["centers"], w["widths"], w["amplitudes"]))
         for c in range(1, len(amdg.Batch.TILES)):
             assert np.array_equal(results[(prec, c)], results[(prec, 0)])
-    ring0 = len(amdg.Batch.TILES)
-    for c in range(ring0 + 1, K):
-        assert np.array_equal(results[(amdg.MIXED, c)], results[(amdg.MIXED, ring0)])
+    ring0, df0 = amdg.Batch.RING_FIRST, amdg.Batch.DF_COLUMN_FIRST
+    # FP32-pair state: the column tiles and the ring configurations sum in the same order
+    for c in range(df0 + 1, K):
+        assert np.array_equal(results[(amdg.MIXED, c)], results[(amdg.MIXED, df0)]), amdg.Batch.kernel_name(c)
     ref = results[(amdg.MIXED, 2)]
-    assert np.abs(results[(amdg.MIXED, ring0)] - ref).max() <= 1e-6 * np.abs(ref).max()
+    assert np.abs(results[(amdg.MIXED, df0)] - ref).max() <= 1e-6 * np.abs(ref).max()
     with pytest.raises(amdg.AmdgError):
         batch = amdg.Batch(ctx, grids, [w["velocity"] for w in work])
         try:
@@ -154,16 +156,17 @@ def test_batch_kernels_agree_and_autotuner_picks_one(ctx):
         g.close()
 
 
-@pytest.mark.parametrize("seed", [3, 8])
-def test_batch_ring_kernel_matches_oracle(ctx, seed):
-    """The bulk-copy ring kernel (FP32 contraction, FP32-pair stage state) against the oracle's
-    SSP-RK3 per solve, each at its own velocity and step: 1e-6 relative after 3 steps."""
+@pytest.mark.parametrize("seed,which", [(3, "ring"), (8, "ring"), (3, "column")])
+def test_batch_ring_kernel_matches_oracle(ctx, seed, which):
+    """The FP32-pair stage state (FP32 contraction) with the bulk-copy ring kernel or the column
+    kernel against the oracle's SSP-RK3 per solve, each at its own velocity and step: 1e-6
+    relative after 3 steps."""
     work = O.batched_workload(5, seed=seed)
     grids = _grids(ctx, work, 5, 1e-3)
     u0 = [g.coefficients().copy() for g in grids]
     dts = [0.1 / (sum(abs(v) for v in w["velocity"]) * 32) for w in work]
     batch = amdg.Batch(ctx, grids, [w["velocity"] for w in work])
-    batch.set_kernel(amdg.MIXED, len(amdg.Batch.TILES))
+    batch.set_kernel(amdg.MIXED, amdg.Batch.RING_FIRST if which == "ring" else amdg.Batch.DF_COLUMN_FIRST + 2)
     batch.set_dt(dts)
     batch.rk3_steps(3, amdg.MIXED, use_graph=False)
     ctx.synchronize()
