@@ -834,6 +834,7 @@ amdg_status grid_reserve_remap(amdg_grid* g, int64_t E) {
     if ((s = regrow(&g->d_u_spare, &g->spare_capacity)) != AMDG_OK) return s;
     if (g->d_v && (s = regrow(&g->d_v_spare, &g->v_spare_capacity)) != AMDG_OK) return s;
     if (g->d_pred && (s = regrow(&g->d_pred_spare, &g->pred_spare_capacity)) != AMDG_OK) return s;
+    if (g->d_pred_v && (s = regrow(&g->d_pred_v_spare, &g->pred_v_spare_capacity)) != AMDG_OK) return s;
     return AMDG_OK;
 }
 
@@ -853,6 +854,12 @@ amdg_status grid_apply_remap(amdg_grid* g, int64_t E) {
         g->ctx->launches++;
         std::swap(g->d_pred, g->d_pred_spare);
         std::swap(g->pred_capacity, g->pred_spare_capacity);
+    }
+    if (g->d_pred_v) {
+        AMDG_CK(launch_remap(g->d_pred_v, g->d_map, g->block, E, g->d_pred_v_spare, st));
+        g->ctx->launches++;
+        std::swap(g->d_pred_v, g->d_pred_v_spare);
+        std::swap(g->pred_v_capacity, g->pred_v_spare_capacity);
     }
     std::swap(g->d_u, g->d_u_spare);
     std::swap(g->capacity, g->spare_capacity);

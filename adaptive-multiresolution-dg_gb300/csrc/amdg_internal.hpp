@@ -354,6 +354,25 @@ struct amdg_grid {
     double* d_v = nullptr;           // v_capacity elements, null until set
     double* d_v_spare = nullptr;
     int64_t v_capacity = 0, v_spare_capacity = 0;
+    // Element::ucoe_ut_predict, remapped with u like d_pred
+    double* d_pred_v = nullptr;
+    double* d_pred_v_spare = nullptr;
+    int64_t pred_v_capacity = 0, pred_v_spare_capacity = 0;
+    int indicator = 0;               // AMDG_INDICATOR_U / AMDG_INDICATOR_U_UT for amdg_grid_refine / _coarsen
+};
+
+// ODESolver on a grid (ode.cu): the state at t_n (u, and u_t for the second-order schemes), the
+// solver's rhs vector and the RK4ODE2nd running sums of the stage increments
+struct amdg_ode {
+    amdg_grid* grid = nullptr;
+    int device = 0;
+    int scheme = 0;        // AMDG_ODE_*
+    double dt = 0.0;
+    int64_t version = -1;  // element set of init()
+    int64_t n = 0;         // dof
+    double* d_un = nullptr;
+    double* d_rhs = nullptr;
+    double *d_vn = nullptr, *d_su = nullptr, *d_sv = nullptr;  // second-order schemes
 };
 
 struct amdg_linear_op {
@@ -431,6 +450,9 @@ struct amdg_burgers_op {
     size_t nodes_cap = 0;
     int64_t interp_version = -1;     // element set of the flux coefficients amdg_lagr_interpolate kept
     int interp_prec = -1;            // ... and their arithmetic
+    // wave: element set and arithmetic of the K grad u [0] and K u [1] interpolations amdg_wave_interpolate kept
+    int64_t wave_interp_version[2] = {-1, -1};
+    int wave_interp_prec[2] = {-1, -1};
     int chunk = 1;  // terms per launch
     int sweep_variant = -1;  // transform sweep kernel: -1 by precision, 0 thread per output entry, 1 thread per
                              // column, 2 / 3 / 4 warp per (node, element) with 1 / 2 / 4 elements per warp
@@ -532,6 +554,8 @@ amdg_status device_transform_topology(amdg_grid* g, const DeviceTopoOut& out, in
 amdg_status device_parent_table(amdg_grid* g, int32_t* d_pg, void* stream);
 // the grid's Element::rhs vector (dof entries, zero after every element-set change)
 amdg_status grid_rhs(amdg_grid* g, double** d_rhs);
+// the grid's velocity field (u_t), created as zero when absent
+amdg_status grid_ensure_velocity(amdg_grid* g);
 }  // namespace amdg
 
 struct amdg_batch {

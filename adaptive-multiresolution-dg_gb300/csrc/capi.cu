@@ -665,6 +665,11 @@ amdg_status amdg_grid_destroy(amdg_grid* g) {
     cudaFree(g->d_norms);
     cudaFree(g->d_v);
     cudaFree(g->d_v_spare);
+    cudaFree(g->d_pred);
+    cudaFree(g->d_pred_spare);
+    cudaFree(g->d_pred_v);
+    cudaFree(g->d_pred_v_spare);
+    cudaFree(g->d_rhs);
     GridDevice& d = g->dev;
     cudaFree(d.key);
     cudaFree(d.key_alt);
@@ -819,9 +824,12 @@ amdg_status amdg_grid_refine(amdg_grid* g, const double* d_indicator, double eps
     AMDG_REQUIRE(g, AMDG_ERR_ARG, "grid is null");
     amdg_status s = set_device(g->ctx);
     if (s != AMDG_OK) return s;
+    const double* u2 = g->indicator == AMDG_INDICATOR_U_UT ? g->d_v : nullptr;
+    AMDG_REQUIRE(g->indicator != AMDG_INDICATOR_U_UT || u2, AMDG_ERR_STATE,
+                 "the u + u_t indicator needs the grid's velocity field");
     if (g->ctx->adapt_mode == AMDG_ADAPT_DEVICE) {
         PhaseTimer timer(g->ctx, AMDG_PHASE_ADAPT_DEVICE);
-        if ((s = grid_device_norms(g, d_indicator ? d_indicator : g->d_u, nullptr)) != AMDG_OK ||
+        if ((s = grid_device_norms(g, d_indicator ? d_indicator : g->d_u, u2)) != AMDG_OK ||
             (s = grid_device_refine(g, eps, nullptr, nullptr, nullptr)) != AMDG_OK)
             return s;
         if (num_elements) *num_elements = g->host.num_elements;
@@ -829,7 +837,7 @@ amdg_status amdg_grid_refine(amdg_grid* g, const double* d_indicator, double eps
     }
     if ((s = grid_ensure_host(g)) != AMDG_OK) return s;
     std::vector<double> norms;
-    if ((s = grid_norms(g, d_indicator ? d_indicator : g->d_u, &norms)) != AMDG_OK) return s;
+    if ((s = grid_norms(g, d_indicator ? d_indicator : g->d_u, &norms, u2)) != AMDG_OK) return s;
     std::vector<uint64_t> keys;
     {
         PhaseTimer timer(g->ctx, AMDG_PHASE_ADAPT_HOST);
@@ -842,7 +850,16 @@ amdg_status amdg_grid_refine(amdg_grid* g, const double* d_indicator, double eps
 
 amdg_status amdg_grid_coarsen(amdg_grid* g, double eta, int64_t* num_elements) {
     AMDG_REQUIRE(g, AMDG_ERR_ARG, "grid is null");
-    return amdg::grid_coarsen(g, eta, nullptr, num_elements);
+    const double* u2 = g->indicator == AMDG_INDICATOR_U_UT ? g->d_v : nullptr;
+    AMDG_REQUIRE(g->indicator != AMDG_INDICATOR_U_UT || u2, AMDG_ERR_STATE,
+                 "the u + u_t indicator needs the grid's velocity field");
+    return amdg::grid_coarsen(g, eta, u2, num_elements);
+}
+
+amdg_status amdg_grid_set_indicator(amdg_grid* g, int mode) {
+    AMDG_REQUIRE(g && (mode == AMDG_INDICATOR_U || mode == AMDG_INDICATOR_U_UT), AMDG_ERR_ARG, "bad arguments");
+    g->indicator = mode;
+    return AMDG_OK;
 }
 
 amdg_status amdg_grid_set_velocity(amdg_grid* g, const double* host, int64_t n) {

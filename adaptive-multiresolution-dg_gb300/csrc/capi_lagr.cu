@@ -304,9 +304,10 @@ SweepArgs<T> sweep_args(const amdg_burgers_op* op, const Mats<T>& m) {
     a.n1 = op->n1;
     a.num_elements = g->host.num_elements;
     a.desc = op->d_terms;
-    // default kernels: thread per output entry for the FP64 sweeps (FP64-pipe work per warp kept
-    // whole), warp per (node, element) for the FP32 and double-float ones (fewer issued instructions)
-    a.variant = op->sweep_variant >= 0 ? op->sweep_variant : (std::is_same<T, double>::value ? 0 : 2);
+    // default kernels (measured on the config-3 runs): warp per (node, element) for the FP32 sweeps
+    // (fewer issued instructions), thread per output entry for the FP64 ones (FP64-pipe work per
+    // warp kept whole) and the double-float ones (their arithmetic, not the issue overhead, binds)
+    a.variant = op->sweep_variant >= 0 ? op->sweep_variant : (std::is_same<T, float>::value ? 2 : 0);
     for (int i = 0; i < kNumLagrMats; ++i) a.mats[i] = m.m[i];
     a.vol_ptr = op->d_vol_ptr;
     a.vol_split = op->d_vol_split;
@@ -468,7 +469,8 @@ amdg_status eval_wave_penalty(amdg_burgers_op* op, const double* u, double* rhs,
 // wave: K u_{x_d} (d < dim) and K u at the points, then their interpolation
 // coefficients (type To) into fields dim+1 .. 2 dim+1 of w_fields
 template <typename To>
-amdg_status eval_wave_fields(amdg_burgers_op* op, const double* u, To** fucoe, cudaStream_t st) {
+amdg_status eval_wave_fields(amdg_burgers_op* op, const double* u, To** fucoe, cudaStream_t st, int f_first = 0,
+                             int f_last = -1) {
     amdg_grid* g = op->grid;
     const int dim = g->host.dim, np = g->host.k + 1;
     const int64_t E = g->host.num_elements, n = E * op->points;
@@ -491,7 +493,7 @@ amdg_status eval_wave_fields(amdg_burgers_op* op, const double* u, To** fucoe, c
         if constexpr (df) return mats_df(op);
         else return mats64(op);
     }();
-    for (int f = 0; f <= dim; ++f) {
+    for (int f = f_first; f <= (f_last < 0 ? dim : f_last); ++f) {
         double* kp = fields + size_t(f) * stride;  // K times the point values of field f
         double* acc = static_cast<double*>(op->w_up);
         for (int c0 = 0; c0 < G; c0 += op->chunk) {
@@ -519,6 +521,16 @@ amdg_status eval_wave_fields(amdg_burgers_op* op, const double* u, To** fucoe, c
         if (amdg_status r = eval_surplus<double, To>(op, kp, fucoe[f], st); r != AMDG_OK) return r;
     }
     return AMDG_OK;
+}
+
+// the coefficient arrays of the wave's point fields (K du/dx_d for d < dim, K u): FP64, or the FP32
+// ones of the mixed back transforms, in the second half of w_fields
+template <typename To>
+void wave_field_coefs(amdg_burgers_op* op, To** fc) {
+    const int dim = op->grid->host.dim;
+    const size_t stride = size_t(op->capacity) * op->points;
+    double* fields = static_cast<double*>(op->w_fields);
+    for (int f = 0; f <= dim; ++f) fc[f] = reinterpret_cast<To*>(fields + size_t(dim + 1 + f) * stride);
 }
 
 // rhs (FP64, dof entries) of the FP64 state u, or the stage update `so` with it.
@@ -1153,7 +1165,7 @@ static amdg_status adaptive_step_any(amdg_burgers_op* op, double cfl, double wav
         if ((s = eval_rhs(op, g->d_u, op->d_rhs64, prec, so)) != AMDG_OK) return s;
     } else {
         // EulerODE2nd::step_rk_source on copies of (u, v): u + dt v, v + dt (IPDG u)
-        if ((s = ensure_velocity(g)) != AMDG_OK) return s;
+        if ((s = grid_ensure_velocity(g)) != AMDG_OK) return s;
         if ((s = eval_wave_penalty(op, g->d_u, op->d_rhs64, st)) != AMDG_OK) return s;
         AMDG_CK(launch_rk4_2nd_stage(-1, dt, op->d_rhs64, g->d_u, g->d_v, op->d_pred, op->d_su, nullptr, nullptr, g->dof,
                                      st));
@@ -1215,7 +1227,7 @@ amdg_status amdg_burgers_features(amdg_burgers_op* op, const double* d_u, float*
     amdg_grid* g = op->grid;
     if (amdg_status s = ensure_features(op, 0, 0); s != AMDG_OK) return s;
     if (op->kind == 1)
-        if (amdg_status s = ensure_velocity(g); s != AMDG_OK) return s;
+        if (amdg_status s = grid_ensure_velocity(g); s != AMDG_OK) return s;
     AMDG_CK(launch_element_features(d_u, op->kind == 1 ? g->d_v : nullptr, op->d_pg, g->host.num_elements, g->host.dim,
                                     g->block, d_features, stream_of(op)));
     g->ctx->launches++;
@@ -1328,7 +1340,7 @@ static amdg_status learned_step_any(amdg_burgers_op* op, amdg_mlp* mlp, double c
     if (mlp) {
         PhaseTimer tc(g->ctx, AMDG_PHASE_CLASSIFIER);
         if ((s = ensure_features(op, E, F)) != AMDG_OK) return s;
-        if (op->kind == 1 && (s = ensure_velocity(g)) != AMDG_OK) return s;
+        if (op->kind == 1 && (s = grid_ensure_velocity(g)) != AMDG_OK) return s;
         AMDG_CK(launch_element_features(g->d_u, op->kind == 1 ? g->d_v : nullptr, op->d_pg, E, g->host.dim, g->block,
                                         op->d_feat, st));
         g->ctx->launches++;
@@ -1336,7 +1348,7 @@ static amdg_status learned_step_any(amdg_burgers_op* op, amdg_mlp* mlp, double c
         if (g->ctx->adapt_mode != AMDG_ADAPT_DEVICE)
             AMDG_CK(cudaMemcpyAsync(prob.data(), op->d_prob, prob.size() * sizeof(float), cudaMemcpyDeviceToHost, st));
     }
-    if (op->kind == 1 && (s = ensure_velocity(g)) != AMDG_OK) return s;
+    if (op->kind == 1 && (s = grid_ensure_velocity(g)) != AMDG_OK) return s;
     const double* d_ut = op->kind == 1 ? g->d_v : nullptr;  // the wave indicator adds ||u_t||
     // the step size of the element set before the pre-adaptation, as the plain step takes it before
     // its refinement (02_hyperbolic_05_burgers_adapt.cpp:234-243)
@@ -1452,6 +1464,98 @@ amdg_status amdg_wave_destroy(amdg_wave_op* w) {
     return AMDG_OK;
 }
 
+amdg_status amdg_wave_set_sigma(amdg_wave_op* w, double sigma) {
+    AMDG_REQUIRE(w && std::isfinite(sigma), AMDG_ERR_ARG, "bad arguments");
+    amdg_burgers_op* op = w->lagr;
+    if (op->sigma == sigma) return AMDG_OK;
+    AMDG_CK(cudaSetDevice(op->device));
+    op->sigma = sigma;
+    op->graph_version = -1;
+    if (op->built_version != op->grid->version) return AMDG_OK;  // the next sync sets the coefficient
+    const double c = wave_penalty_coef(op);
+    for (PartialSum& p : op->terms)
+        if (p.kind == 1) p.coef = c;
+    return refresh_nodes(op, stream_of(op));
+}
+
+amdg_status amdg_wave_interpolate(amdg_wave_op* w, int which, amdg_precision prec) {
+    AMDG_REQUIRE(w && (which == AMDG_WAVE_INTERP_GRADU || which == AMDG_WAVE_INTERP_U), AMDG_ERR_ARG, "bad arguments");
+    AMDG_REQUIRE(prec == AMDG_PREC_FP64 || prec == AMDG_PREC_MIXED, AMDG_ERR_ARG, "bad precision");
+    amdg_burgers_op* op = w->lagr;
+    AMDG_CK(cudaSetDevice(op->device));
+    if (amdg_status rs = burgers_sync(op); rs != AMDG_OK) return rs;
+    amdg_grid* g = op->grid;
+    const int dim = g->host.dim;
+    const int f0 = which == AMDG_WAVE_INTERP_GRADU ? 0 : dim, f1 = which == AMDG_WAVE_INTERP_GRADU ? dim - 1 : dim;
+    cudaStream_t st = stream_of(op);
+    amdg_status r;
+    if (prec == AMDG_PREC_FP64) {
+        double* fc[kMaxTermSources];
+        wave_field_coefs(op, fc);
+        r = eval_wave_fields<double>(op, g->d_u, fc, st, f0, f1);
+    } else {
+        float* fc[kMaxTermSources];
+        wave_field_coefs(op, fc);
+        r = eval_wave_fields<float>(op, g->d_u, fc, st, f0, f1);
+    }
+    if (r != AMDG_OK) return r;
+    op->wave_interp_version[which] = g->version;
+    op->wave_interp_prec[which] = int(prec);
+    return AMDG_OK;
+}
+
+amdg_status amdg_wave_rhs_add(amdg_wave_op* w, int group, amdg_precision prec) {
+    AMDG_REQUIRE(w && group >= AMDG_WAVE_RHS_FLX_GRADU && group <= AMDG_WAVE_RHS_IPDG, AMDG_ERR_ARG, "bad arguments");
+    AMDG_REQUIRE(prec == AMDG_PREC_FP64 || prec == AMDG_PREC_MIXED, AMDG_ERR_ARG, "bad precision");
+    amdg_burgers_op* op = w->lagr;
+    AMDG_CK(cudaSetDevice(op->device));
+    if (amdg_status rs = burgers_sync(op); rs != AMDG_OK) return rs;
+    amdg_grid* g = op->grid;
+    const int dim = g->host.dim;
+    if (group != AMDG_WAVE_RHS_IPDG) {
+        const int need = group == AMDG_WAVE_RHS_FLX_U ? AMDG_WAVE_INTERP_U : AMDG_WAVE_INTERP_GRADU;
+        AMDG_REQUIRE(op->wave_interp_version[need] == g->version && op->wave_interp_prec[need] == int(prec),
+                     AMDG_ERR_STATE, "no interpolation of this element set and precision: call amdg_wave_interpolate first");
+    }
+    // the terms in build_terms order: point values ((dim + 1) fields x G), then per group dim x G
+    // right-hand-side terms, then the dim IPDG terms
+    const int G = int(op->sched_dims.size());
+    const int first = group == AMDG_WAVE_RHS_IPDG ? int(op->terms.size()) - dim : op->n_pv_terms + group * dim * G;
+    const int count = group == AMDG_WAVE_RHS_IPDG ? dim : dim * G;
+    double* rhs = nullptr;
+    if (amdg_status s = grid_rhs(g, &rhs); s != AMDG_OK) return s;
+    cudaStream_t st = stream_of(op);
+    if (prec == AMDG_PREC_FP64) {
+        double* fc[kMaxTermSources];
+        wave_field_coefs(op, fc);
+        const double* src[kMaxTermSources];
+        for (int f = 0; f <= dim; ++f) src[f] = fc[f];
+        return eval_term_range<double>(op, mats64(op), first, count, src, dim + 1, g->d_u, rhs, StageOut{}, st, true);
+    }
+    float* fc[kMaxTermSources];
+    wave_field_coefs(op, fc);
+    const float* src[kMaxTermSources];
+    for (int f = 0; f <= dim; ++f) src[f] = fc[f];
+    float* u32 = static_cast<float*>(op->w_u);
+    if (group == AMDG_WAVE_RHS_IPDG) {
+        AMDG_CK(launch_convert<double, float>(g->d_u, u32, g->dof, st));
+        g->ctx->launches++;
+    }
+    return eval_term_range<float>(op, mats32(op), first, count, src, dim + 1, u32, rhs, StageOut{}, st, true);
+}
+
+amdg_status amdg_ode_add_wave_penalty(amdg_ode* o, amdg_wave_op* w) {
+    AMDG_REQUIRE(o && w && o->grid == w->lagr->grid, AMDG_ERR_ARG, "the integrator and the operator must share the grid");
+    AMDG_REQUIRE(o->grid->version == o->version, AMDG_ERR_STATE, "the element set changed since the integrator was created");
+    amdg_burgers_op* op = w->lagr;
+    AMDG_CK(cudaSetDevice(op->device));
+    if (amdg_status rs = burgers_sync(op); rs != AMDG_OK) return rs;
+    const int dim = op->grid->host.dim;
+    const double* src[1] = {op->grid->d_u};
+    return eval_term_range<double>(op, mats64(op), int(op->terms.size()) - dim, dim, src, 1, op->grid->d_u, o->d_rhs,
+                                   StageOut{}, stream_of(op), true);
+}
+
 amdg_status amdg_wave_set_sweep_variant(amdg_wave_op* w, int variant) {
     AMDG_REQUIRE(w, AMDG_ERR_ARG, "null argument");
     return amdg_burgers_set_sweep_variant(w->lagr, variant);
@@ -1467,19 +1571,6 @@ amdg_status amdg_wave_rhs(amdg_wave_op* w, const double* d_u, double* d_rhs, amd
     return eval_rhs(op, d_u, d_rhs, prec);
 }
 
-// the grid's velocity field, created as zero when absent
-static amdg_status ensure_velocity(amdg_grid* g) {
-    if (g->d_v) return AMDG_OK;
-    const int64_t cap = std::max<int64_t>(g->capacity, 1);
-    if (amdg::device_malloc(&g->d_v, size_t(cap) * g->block * sizeof(double)) != cudaSuccess) {
-        g->d_v = nullptr;
-        return fail(AMDG_ERR_NOMEM, "cudaMalloc failed (velocity field)");
-    }
-    AMDG_CK(cudaMemsetAsync(g->d_v, 0, size_t(cap) * g->block * sizeof(double), static_cast<cudaStream_t>(g->ctx->stream)));
-    g->v_capacity = cap;
-    return AMDG_OK;
-}
-
 // nsteps RK4ODE2nd steps of (u, v) (RK4ODE2nd::step_stage, ODESolver.cpp:579-615), the
 // right-hand side re-evaluated at every stage
 static amdg_status wave_rk4(amdg_burgers_op* op, double dt, int nsteps, amdg_precision prec) {
@@ -1487,7 +1578,7 @@ static amdg_status wave_rk4(amdg_burgers_op* op, double dt, int nsteps, amdg_pre
     cudaStream_t st = stream_of(op);
     if (amdg_status s = burgers_sync(op); s != AMDG_OK) return s;  // buffers sized for the current grid
     PhaseTimer timer(g->ctx, AMDG_PHASE_RK3);
-    if (amdg_status s = ensure_velocity(g); s != AMDG_OK) return s;
+    if (amdg_status s = grid_ensure_velocity(g); s != AMDG_OK) return s;
     const size_t bytes = size_t(g->dof) * sizeof(double);
     for (int step = 0; step < nsteps; ++step) {
         AMDG_CK(cudaMemcpyAsync(op->d_u1, g->d_u, bytes, cudaMemcpyDeviceToDevice, st));

@@ -7,12 +7,14 @@
 // 223-476) runs call for call on the device.
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cmath>
 #include <new>
 #include <string>
 
 #include "amdg_internal.hpp"
 #include "kernels.cuh"
+#include "kernels_lagr.cuh"
 #include "device_alloc.cuh"
 
 using namespace amdg;
@@ -27,17 +29,6 @@ using namespace amdg;
     do {                              \
         if (!(cond)) return fail(code, msg); \
     } while (0)
-
-struct amdg_ode {
-    amdg_grid* grid = nullptr;
-    int device = 0;
-    int scheme = 0;        // AMDG_ODE_FORWARD_EULER / AMDG_ODE_RK3SSP
-    double dt = 0.0;
-    int64_t version = -1;  // element set of init()
-    int64_t n = 0;         // dof
-    double* d_un = nullptr;
-    double* d_rhs = nullptr;
-};
 
 namespace {
 
@@ -66,6 +57,18 @@ amdg_status alloc_vec(double** p, int64_t n) {
 }  // namespace
 
 namespace amdg {
+
+amdg_status grid_ensure_velocity(amdg_grid* g) {
+    if (g->d_v) return AMDG_OK;
+    const int64_t cap = std::max<int64_t>(g->capacity, 1);
+    if (amdg::device_malloc(&g->d_v, size_t(cap) * g->block * sizeof(double)) != cudaSuccess) {
+        g->d_v = nullptr;
+        return fail(AMDG_ERR_NOMEM, "cudaMalloc failed (velocity field)");
+    }
+    AMDG_CK(cudaMemsetAsync(g->d_v, 0, size_t(cap) * g->block * sizeof(double), stream_of(g)));
+    g->v_capacity = cap;
+    return AMDG_OK;
+}
 
 amdg_status grid_rhs(amdg_grid* g, double** d_rhs) {
     const int64_t E = g->host.num_elements;
@@ -143,6 +146,36 @@ amdg_status amdg_grid_copy_predict_to_ucoe(amdg_grid* g) {
     return AMDG_OK;
 }
 
+amdg_status amdg_grid_copy_ucoe_ut_to_predict(amdg_grid* g) {
+    AMDG_REQUIRE(g, AMDG_ERR_ARG, "grid is null");
+    AMDG_CK(cudaSetDevice(g->device));
+    if (amdg_status s = grid_ensure_velocity(g); s != AMDG_OK) return s;
+    const int64_t E = g->host.num_elements;
+    if (!g->d_pred_v || E > g->pred_v_capacity) {
+        cudaFree(g->d_pred_v);
+        g->d_pred_v = nullptr;
+        g->pred_v_capacity = 0;
+        const int64_t cap = E + E / 4 + 16;
+        if (amdg_status s = alloc_vec(&g->d_pred_v, cap * g->block); s != AMDG_OK) return s;
+        g->pred_v_capacity = cap;
+    }
+    if (g->dof)
+        AMDG_CK(cudaMemcpyAsync(g->d_pred_v, g->d_v, size_t(g->dof) * sizeof(double), cudaMemcpyDeviceToDevice,
+                                stream_of(g)));
+    return AMDG_OK;
+}
+
+amdg_status amdg_grid_copy_predict_to_ucoe_ut(amdg_grid* g) {
+    AMDG_REQUIRE(g, AMDG_ERR_ARG, "grid is null");
+    AMDG_REQUIRE(g->d_pred_v, AMDG_ERR_STATE, "no prediction: call amdg_grid_copy_ucoe_ut_to_predict first");
+    AMDG_CK(cudaSetDevice(g->device));
+    if (amdg_status s = grid_ensure_velocity(g); s != AMDG_OK) return s;
+    if (g->dof)
+        AMDG_CK(cudaMemcpyAsync(g->d_v, g->d_pred_v, size_t(g->dof) * sizeof(double), cudaMemcpyDeviceToDevice,
+                                stream_of(g)));
+    return AMDG_OK;
+}
+
 amdg_status amdg_vector_axpy(amdg_context* ctx, double a, const double* d_x, double* d_y, int64_t n) {
     AMDG_REQUIRE(ctx && n >= 0 && (n == 0 || (d_x && d_y)), AMDG_ERR_ARG, "bad arguments");
     if (n == 0) return AMDG_OK;
@@ -156,7 +189,7 @@ amdg_status amdg_vector_axpy(amdg_context* ctx, double a, const double* d_x, dou
 amdg_status amdg_ode_create(amdg_grid* g, int scheme, double dt, amdg_ode** out) {
     AMDG_REQUIRE(g && out, AMDG_ERR_ARG, "null argument");
     *out = nullptr;
-    AMDG_REQUIRE(scheme == AMDG_ODE_FORWARD_EULER || scheme == AMDG_ODE_RK3SSP, AMDG_ERR_ARG, "unknown scheme");
+    AMDG_REQUIRE(scheme >= AMDG_ODE_FORWARD_EULER && scheme <= AMDG_ODE_RK4ODE2ND, AMDG_ERR_ARG, "unknown scheme");
     AMDG_REQUIRE(std::isfinite(dt), AMDG_ERR_ARG, "dt must be finite");
     AMDG_CK(cudaSetDevice(g->device));
     amdg_ode* o = new (std::nothrow) amdg_ode;
@@ -167,16 +200,20 @@ amdg_status amdg_ode_create(amdg_grid* g, int scheme, double dt, amdg_ode** out)
     o->dt = dt;
     o->n = g->dof;
     o->version = g->version;
+    const bool second = scheme == AMDG_ODE_EULER_ODE2ND || scheme == AMDG_ODE_RK4ODE2ND;
     amdg_status s;
-    if ((s = alloc_vec(&o->d_un, o->n)) != AMDG_OK || (s = alloc_vec(&o->d_rhs, o->n)) != AMDG_OK) {
+    if ((s = alloc_vec(&o->d_un, o->n)) != AMDG_OK || (s = alloc_vec(&o->d_rhs, o->n)) != AMDG_OK ||
+        (second && ((s = grid_ensure_velocity(g)) != AMDG_OK || (s = alloc_vec(&o->d_vn, o->n)) != AMDG_OK ||
+                    (s = alloc_vec(&o->d_su, o->n)) != AMDG_OK || (s = alloc_vec(&o->d_sv, o->n)) != AMDG_OK))) {
         amdg_ode_destroy(o);
         return s;
     }
     cudaStream_t st = stream_of(g);
-    // ODESolver::init: the coefficients at t_n; the solver's right-hand side starts at zero
-    cudaError_t e = o->n ? cudaMemcpyAsync(o->d_un, g->d_u, size_t(o->n) * sizeof(double), cudaMemcpyDeviceToDevice, st)
-                         : cudaSuccess;
-    if (e == cudaSuccess && o->n) e = cudaMemsetAsync(o->d_rhs, 0, size_t(o->n) * sizeof(double), st);
+    // ODESolver::init: the coefficients (and u_t) at t_n; the solver's right-hand side starts at zero
+    const size_t bytes = size_t(o->n) * sizeof(double);
+    cudaError_t e = o->n ? cudaMemcpyAsync(o->d_un, g->d_u, bytes, cudaMemcpyDeviceToDevice, st) : cudaSuccess;
+    if (e == cudaSuccess && o->n) e = cudaMemsetAsync(o->d_rhs, 0, bytes, st);
+    if (e == cudaSuccess && o->n && second) e = cudaMemcpyAsync(o->d_vn, g->d_v, bytes, cudaMemcpyDeviceToDevice, st);
     if (e != cudaSuccess) {
         amdg_ode_destroy(o);
         return fail(AMDG_ERR_CUDA, std::string("amdg_ode_create: ") + cudaGetErrorString(e));
@@ -190,6 +227,9 @@ amdg_status amdg_ode_destroy(amdg_ode* o) {
     cudaSetDevice(o->device);
     cudaFree(o->d_un);
     cudaFree(o->d_rhs);
+    cudaFree(o->d_vn);
+    cudaFree(o->d_su);
+    cudaFree(o->d_sv);
     delete o;
     return AMDG_OK;
 }
@@ -219,9 +259,25 @@ amdg_status amdg_ode_step_stage(amdg_ode* o, int stage) {
     AMDG_REQUIRE(o, AMDG_ERR_ARG, "null argument");
     amdg_grid* g = o->grid;
     AMDG_REQUIRE(g->version == o->version, AMDG_ERR_STATE, "the element set changed since the integrator was created");
-    const int nstage = o->scheme == AMDG_ODE_RK3SSP ? 3 : 1;
+    const int nstage = o->scheme == AMDG_ODE_RK3SSP ? 3 : (o->scheme == AMDG_ODE_RK4ODE2ND ? 4 : 1);
     AMDG_REQUIRE(stage >= 0 && stage < nstage, AMDG_ERR_ARG, "stage out of range");
     AMDG_CK(cudaSetDevice(o->device));
+    if (o->scheme == AMDG_ODE_EULER_ODE2ND || o->scheme == AMDG_ODE_RK4ODE2ND) {
+        // the stage state goes into the grid's (u, u_t); the RK4ODE2nd step's end (stage 3) is
+        // computed into the t_n copies, then copied to the grid
+        AMDG_REQUIRE(g->d_v, AMDG_ERR_STATE, "the grid has no velocity field");
+        cudaStream_t st = stream_of(g);
+        const int kstage = o->scheme == AMDG_ODE_EULER_ODE2ND ? -1 : stage;
+        AMDG_CK(launch_rk4_2nd_stage(kstage, o->dt, o->d_rhs, o->d_un, o->d_vn, g->d_u, g->d_v, o->d_su, o->d_sv, o->n,
+                                     st));
+        g->ctx->launches++;
+        if (kstage == 3 && o->n) {
+            const size_t bytes = size_t(o->n) * sizeof(double);
+            AMDG_CK(cudaMemcpyAsync(g->d_u, o->d_un, bytes, cudaMemcpyDeviceToDevice, st));
+            AMDG_CK(cudaMemcpyAsync(g->d_v, o->d_vn, bytes, cudaMemcpyDeviceToDevice, st));
+        }
+        return AMDG_OK;
+    }
     // ForwardEuler::step_stage (ODESolver.cpp:209-213) and RK3SSP::step_stage (:285-301):
     // u = un + dt rhs; u = 3/4 un + 1/4 (u + dt rhs); u = 1/3 un + 2/3 (u + dt rhs)
     StageCoef rk{1, 0.0, 1.0, o->dt};

@@ -108,6 +108,8 @@ public:
     static inline int DIM = 1;
     static inline int VEC_NUM = 1;
     static inline std::vector<int> ind_var_vec{0};
+    // "wave": the refine / coarsen indicator adds the norm of u_t (DGAdapt.cpp:1018-1030)
+    static inline std::string prob;
 
     // the grid starts with the elements of levels up to level_init (sum of levels for a sparse grid)
     DGSolution(bool sparse, int level_init, int NMAX, AllBasis<AlptBasis>& all_bas, AllBasis<LagrBasis>&,
@@ -174,6 +176,10 @@ public:
         const std::vector<double> u = coefficients();
         check(amdg_grid_set_velocity(grid_, u.data(), int64_t(u.size())), "amdg_grid_set_velocity");
     }
+    void set_ucoe_ut_zero() {
+        const std::vector<double> z(size_basis_alpt(), 0.0);
+        check(amdg_grid_set_velocity(grid_, z.data(), int64_t(z.size())), "amdg_grid_set_velocity");
+    }
     void set_ucoe_alpt_zero() {
         const std::vector<double> z(size_basis_alpt(), 0.0);
         check(amdg_grid_set_coefficients(grid_, z.data(), int64_t(z.size())), "amdg_grid_set_coefficients");
@@ -184,6 +190,14 @@ public:
     void set_rhs_zero() { check(amdg_grid_set_rhs_zero(grid_), "amdg_grid_set_rhs_zero"); }
     void copy_ucoe_to_predict() { check(amdg_grid_copy_ucoe_to_predict(grid_), "amdg_grid_copy_ucoe_to_predict"); }
     void copy_predict_to_ucoe() { check(amdg_grid_copy_predict_to_ucoe(grid_), "amdg_grid_copy_predict_to_ucoe"); }
+    void copy_ucoe_ut_to_predict() {
+        check(amdg_grid_copy_ucoe_ut_to_predict(grid_), "amdg_grid_copy_ucoe_ut_to_predict");
+    }
+    void copy_predict_to_ucoe_ut() {
+        check(amdg_grid_copy_predict_to_ucoe_ut(grid_), "amdg_grid_copy_predict_to_ucoe_ut");
+    }
+    // Element::source: the registered problems have no source term; drivers' source assembly drops out
+    void set_source_zero() {}
     std::vector<double> rhs() const {
         std::vector<double> r(size_basis_alpt());
         check(amdg_grid_get_rhs(grid_, r.data(), int64_t(r.size())), "amdg_grid_get_rhs");
@@ -198,14 +212,33 @@ public:
         }
         return lagr_;
     }
+    // ... and behind the wave-path classes (the registered K = (1 + a prod_d sin 2 pi x_d)^2, IPDG
+    // parameter from the last DiffusionAlpt built on this solution)
+    amdg_wave_op* wave_op() {
+        if (!wave_) check(amdg_wave_create(grid_, wave_sigma_, 0.5, &wave_), "amdg_wave_create");
+        return wave_;
+    }
+    void set_wave_sigma(double sigma) {
+        wave_sigma_ = sigma;
+        if (wave_) check(amdg_wave_set_sigma(wave_, sigma), "amdg_wave_set_sigma");
+    }
+    // the refine / coarsen indicator for DGSolution::prob
+    void apply_indicator() {
+        check(amdg_grid_set_indicator(grid_, prob == "wave" ? AMDG_INDICATOR_U_UT : AMDG_INDICATOR_U),
+              "amdg_grid_set_indicator");
+    }
 
 protected:
     void release_lagr() {
         amdg_burgers_destroy(lagr_);
         lagr_ = nullptr;
+        amdg_wave_destroy(wave_);
+        wave_ = nullptr;
     }
     amdg_grid* grid_ = nullptr;
     amdg_burgers_op* lagr_ = nullptr;
+    amdg_wave_op* wave_ = nullptr;
+    double wave_sigma_ = 0.0;
     int nmax_;
 };
 
@@ -224,8 +257,14 @@ public:
         check(amdg_grid_init_separable_adaptive(grid_, int(fns.size()), detail::sep_trampoline, &sf, eps_),
               "amdg_grid_init_separable_adaptive");
     }
-    void refine() { check(amdg_grid_refine(grid_, nullptr, eps_, nullptr), "amdg_grid_refine"); }
-    void coarsen() { check(amdg_grid_coarsen(grid_, eta_, nullptr), "amdg_grid_coarsen"); }
+    void refine() {
+        apply_indicator();
+        check(amdg_grid_refine(grid_, nullptr, eps_, nullptr), "amdg_grid_refine");
+    }
+    void coarsen() {
+        apply_indicator();
+        check(amdg_grid_coarsen(grid_, eta_, nullptr), "amdg_grid_coarsen");
+    }
     double refine_eps() const { return eps_; }
     double coarsen_eta() const { return eta_; }
 
@@ -369,6 +408,26 @@ private:
     DGSolution& dg_;
 };
 
+namespace detail {
+// the registered coefficient of the wave operator, K = (1 + a prod_d sin(2 pi x_d))^2, a = 0.5
+inline double wave_coefficient(const std::vector<double>& x) {
+    double prod = 1.0;
+    for (double xd : x) prod *= std::sin(2.0 * 3.14159265358979323846 * xd);
+    const double c = 1.0 + 0.5 * prod;
+    return c * c;
+}
+inline void require_wave_coefficient(const std::function<double(std::vector<double>, int)>& coe, const char* where) {
+    const std::vector<std::vector<double>> xs{{0.125, 0.3, 0.7}, {0.61, 0.2, 0.45}, {0.9, 0.35, 0.15}};
+    for (const auto& x3 : xs) {
+        const std::vector<double> x(x3.begin(), x3.begin() + DGSolution::DIM);
+        for (int d = 0; d < DGSolution::DIM; ++d)
+            if (std::abs(coe(x, d) - wave_coefficient(x)) > 1e-12 * wave_coefficient(x))
+                throw Error(AMDG_ERR_ARG, std::string(where) +
+                                              ": only the coefficient (1 + 0.5 prod_d sin(2 pi x_d))^2 is registered");
+    }
+}
+}  // namespace detail
+
 // LagrInterpolation (Interpolation.h:36-129)
 class LagrInterpolation {
 public:
@@ -385,6 +444,19 @@ public:
                 if (func(std::vector<double>{u}, 0, d) != FluxFunction::burgers_flux_scalar(u))
                     throw Error(AMDG_ERR_ARG, "LagrInterpolation::nonlinear_Lagr_fast: only the Burgers flux u^2/2 is registered");
         check(amdg_lagr_interpolate(dg_.lagr_op(), precision), "amdg_lagr_interpolate");
+    }
+    // LagrInterpolation::var_coeff_gradu_Lagr_fast / var_coeff_u_Lagr_fast (Interpolation.h:40-47):
+    // K du/dx_d (every d) or K u of the current solution at the interpolation points and their
+    // interpolation coefficients, kept for the DiffusionRHS calls that follow
+    void var_coeff_gradu_Lagr_fast(std::function<double(std::vector<double>, int)> coe,
+                                   const std::vector<std::vector<bool>>& /*is_intp*/, FastLagrIntp& /*fast*/) {
+        detail::require_wave_coefficient(coe, "LagrInterpolation::var_coeff_gradu_Lagr_fast");
+        check(amdg_wave_interpolate(dg_.wave_op(), AMDG_WAVE_INTERP_GRADU, precision), "amdg_wave_interpolate");
+    }
+    void var_coeff_u_Lagr_fast(std::function<double(std::vector<double>, int)> coe,
+                               const std::vector<std::vector<bool>>& /*is_intp*/, FastLagrIntp& /*fast*/) {
+        detail::require_wave_coefficient(coe, "LagrInterpolation::var_coeff_u_Lagr_fast");
+        check(amdg_wave_interpolate(dg_.wave_op(), AMDG_WAVE_INTERP_U, precision), "amdg_wave_interpolate");
     }
 
 private:
@@ -416,6 +488,92 @@ public:
 
 private:
     DGSolution& dg_;
+};
+
+// ---- variable-coefficient wave equation, term by term (03_wave_06_var_coeff_adapt.cpp) -------
+// DiffusionAlpt(dg, oper, sigma) + assemble_matrix_flx_ujp_vjp (BilinearForm.h): the IPDG term
+// -sigma/dx [u][v]; on the device it is the operator's last term group, applied to the current u.
+class DiffusionAlpt {
+public:
+    DiffusionAlpt(DGSolution& dg, OperatorMatrix1D<AlptBasis, AlptBasis>&, double sigma) : dg_(dg) {
+        dg_.set_wave_sigma(sigma);
+    }
+    void assemble_matrix_flx_ujp_vjp() {}
+    DGSolution& solution() const { return dg_; }
+
+private:
+    DGSolution& dg_;
+};
+
+
+// DiffusionRHS (FastMultiplyLU.h:655-676): the interface and volume terms of div(K grad u), added
+// into Element::rhs from the interpolations of K grad u and K u
+class DiffusionRHS {
+public:
+    DiffusionRHS(DGSolution& dg, OperatorMatrix1D<LagrBasis, AlptBasis>&) : dg_(dg) {}
+    void rhs_flx_gradu() { add(AMDG_WAVE_RHS_FLX_GRADU, "DiffusionRHS::rhs_flx_gradu"); }
+    void rhs_vol() { add(AMDG_WAVE_RHS_VOL, "DiffusionRHS::rhs_vol"); }
+    void rhs_flx_u() { add(AMDG_WAVE_RHS_FLX_U, "DiffusionRHS::rhs_flx_u"); }
+
+private:
+    void add(int group, const char* where) { check(amdg_wave_rhs_add(dg_.wave_op(), group, precision), where); }
+    DGSolution& dg_;
+};
+
+// The second-order-in-time integrators on (u, u_t) (ODESolver.h:257-371): init keeps the state at
+// t_n; rhs_to_eigenvec takes Element::rhs as the solver's rhs, add_rhs_matrix adds the IPDG term of
+// the current u; step_stage writes the stage state into the solution; final zeroes the solver's rhs.
+class RKODE2nd {
+public:
+    RKODE2nd(DiffusionAlpt& op, double dt, int scheme, int stages)
+        : op_(op), dg_(op.solution()), dt_(dt), scheme_(scheme), num_stage(stages) {}
+    RKODE2nd(const RKODE2nd&) = delete;
+    virtual ~RKODE2nd() { amdg_ode_destroy(ode_); }
+    void init() {
+        amdg_ode_destroy(ode_);
+        ode_ = nullptr;
+        check(amdg_ode_create(dg_.handle(), scheme_, dt_, &ode_), "amdg_ode_create");
+    }
+    void rhs_to_eigenvec() {
+        check(amdg_ode_set_rhs_zero(need()), "amdg_ode_set_rhs_zero");
+        check(amdg_ode_add_rhs_to_eigenvec(need()), "amdg_ode_add_rhs_to_eigenvec");
+    }
+    void add_rhs_matrix(DiffusionAlpt& op) {
+        check(amdg_ode_add_wave_penalty(need(), op.solution().wave_op()), "RKODE2nd::add_rhs_matrix");
+    }
+    void step_stage(int stage) { check(amdg_ode_step_stage(need(), stage), "amdg_ode_step_stage"); }
+    void final() { check(amdg_ode_final(need()), "amdg_ode_final"); }
+
+protected:
+    amdg_ode* need() {
+        if (!ode_) throw Error(AMDG_ERR_STATE, "RKODE2nd: init() first");
+        return ode_;
+    }
+    DiffusionAlpt& op_;
+    DGSolution& dg_;
+    double dt_;
+    int scheme_;
+    amdg_ode* ode_ = nullptr;
+
+public:
+    const int num_stage;
+};
+
+class EulerODE2nd : public RKODE2nd {
+public:
+    EulerODE2nd(DiffusionAlpt& op, double dt) : RKODE2nd(op, dt, AMDG_ODE_EULER_ODE2ND, 1) {}
+    // EulerODE2nd::step_rk (ODESolver.cpp:394-399): the rhs is recomputed as the operator matrix
+    // (the IPDG term) times u, whatever was assembled before
+    void step_rk() {
+        check(amdg_ode_set_rhs_zero(need()), "amdg_ode_set_rhs_zero");
+        add_rhs_matrix(op_);
+        step_stage(0);
+    }
+};
+
+class RK4ODE2nd : public RKODE2nd {
+public:
+    RK4ODE2nd(DiffusionAlpt& op, double dt) : RKODE2nd(op, dt, AMDG_ODE_RK4ODE2ND, 4) {}
 };
 
 // ---- nonlinear flux (Burgers) through Lagrange interpolation ------------------

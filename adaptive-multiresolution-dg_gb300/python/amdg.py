@@ -133,6 +133,13 @@ def load():
         "amdg_grid_get_rhs": ([vp, vp, i64], i32),
         "amdg_grid_copy_ucoe_to_predict": ([vp], i32),
         "amdg_grid_copy_predict_to_ucoe": ([vp], i32),
+        "amdg_grid_copy_ucoe_ut_to_predict": ([vp], i32),
+        "amdg_grid_copy_predict_to_ucoe_ut": ([vp], i32),
+        "amdg_grid_set_indicator": ([vp, i32], i32),
+        "amdg_wave_set_sigma": ([vp, dbl], i32),
+        "amdg_wave_interpolate": ([vp, i32, i32], i32),
+        "amdg_wave_rhs_add": ([vp, i32, i32], i32),
+        "amdg_ode_add_wave_penalty": ([vp, vp], i32),
         "amdg_vector_axpy": ([vp, dbl, vp, vp, i64], i32),
         "amdg_ode_create": ([vp, i32, dbl, pp], i32),
         "amdg_ode_destroy": ([vp], i32),
@@ -415,6 +422,17 @@ class Grid:
     def copy_predict_to_ucoe(self):
         _ck(load().amdg_grid_copy_predict_to_ucoe(self._h), "grid_copy_predict_to_ucoe")
 
+    INDICATOR_U, INDICATOR_U_UT = 0, 1
+
+    def set_indicator(self, mode: int):
+        _ck(load().amdg_grid_set_indicator(self._h, mode), "grid_set_indicator")
+
+    def copy_ucoe_ut_to_predict(self):
+        _ck(load().amdg_grid_copy_ucoe_ut_to_predict(self._h), "grid_copy_ucoe_ut_to_predict")
+
+    def copy_predict_to_ucoe_ut(self):
+        _ck(load().amdg_grid_copy_predict_to_ucoe_ut(self._h), "grid_copy_predict_to_ucoe_ut")
+
     def init_separable(self, funcs, vectorized: bool = False):
         if vectorized:
             cb = _fn1d_batch(funcs)
@@ -669,6 +687,20 @@ class WaveOperator:
     def set_sweep_variant(self, variant: int):
         _ck(load().amdg_wave_set_sweep_variant(self._h, variant), "wave_set_sweep_variant")
 
+    INTERP_GRADU, INTERP_U = 0, 1
+    RHS_FLX_GRADU, RHS_VOL, RHS_FLX_U, RHS_IPDG = 0, 1, 2, 3
+
+    def set_sigma(self, sigma: float):
+        _ck(load().amdg_wave_set_sigma(self._h, sigma), "wave_set_sigma")
+
+    def interpolate(self, which: int, prec: int = FP64):
+        """LagrInterpolation::var_coeff_gradu_Lagr_fast (INTERP_GRADU) / var_coeff_u_Lagr_fast (INTERP_U)."""
+        _ck(load().amdg_wave_interpolate(self._h, which, prec), "wave_interpolate")
+
+    def rhs_add(self, group: int, prec: int = FP64):
+        """DiffusionRHS::rhs_flx_gradu / rhs_vol / rhs_flx_u or the IPDG term, added into the grid's rhs."""
+        _ck(load().amdg_wave_rhs_add(self._h, group, prec), "wave_rhs_add")
+
     def rk4_steps(self, dt: float, nsteps: int, prec: int = FP64):
         _ck(load().amdg_wave_rk4_steps(self._h, dt, nsteps, prec), "wave_rk4_steps")
 
@@ -733,8 +765,8 @@ class WaveOperator:
 
 
 class ODE:
-    """ForwardEuler / RK3SSP (ODESolver) on a grid's device state, stage by stage."""
-    FORWARD_EULER, RK3SSP = 0, 1
+    """ForwardEuler / RK3SSP / EulerODE2nd / RK4ODE2nd (ODESolver) on a grid's device state, stage by stage."""
+    FORWARD_EULER, RK3SSP, EULER_ODE2ND, RK4ODE2ND = 0, 1, 2, 3
 
     def __init__(self, grid: Grid, scheme: int, dt: float):
         self._h = C.c_void_p()
@@ -751,6 +783,10 @@ class ODE:
 
     def final(self):
         _ck(load().amdg_ode_final(self._h), "ode_final")
+
+    def add_wave_penalty(self, op):
+        """RKODE2nd::add_rhs_matrix: the solver's rhs += the IPDG term of the grid's current u."""
+        _ck(load().amdg_ode_add_wave_penalty(self._h, op._h), "ode_add_wave_penalty")
 
     def close(self):
         if self._h:

@@ -1136,6 +1136,46 @@ def profile_config3():
     torch.cuda.cudart().cudaProfilerStop()
 
 
+def profile_batch():
+    """Profiling case (not a bench line): 64 of the batched solves (per-solve refine thresholds
+    log-uniform in [1e-8, 1e-5], adaptive N<=8), one mixed SSP-RK3 step with the autotuner's stage
+    kernel between cudaProfilerStart / cudaProfilerStop, stage times per candidate first."""
+    import torch
+
+    import amdg
+    import amdg_oracle as O
+    torch.cuda.set_device(0)
+    ctx = amdg.Context(0)
+    stream = torch.cuda.Stream()
+    torch.cuda.set_stream(stream)
+    ctx.set_stream(stream.cuda_stream)
+    work = O.batched_workload(64, seed=0)
+    eps_of = np.exp(np.random.default_rng(7).uniform(math.log(1e-8), math.log(1e-5), len(work)))
+    grids = []
+    for w, eps in zip(work, eps_of):
+        g = amdg.Grid(ctx, 3, 8, 2, level_init=2)
+        g.init_separable_adaptive(O.gaussian_bump_terms(w["centers"], w["widths"], w["amplitudes"], vectorized=True),
+                                  float(eps), vectorized=True)
+        grids.append(g)
+    dts = [CFL / sum(abs(v) * 2.0 ** int(m) for v, m in zip(w["velocity"], g.max_mesh_level()))
+           for g, w in zip(grids, work)]
+    batch = amdg.Batch(ctx, grids, [w["velocity"] for w in work])
+    batch.set_dt(dts)
+    kernel, ms = batch.tuning()
+    print(json.dumps({"elements": batch.num_elements, "dof": batch.dof, "pairs": batch.pairs,
+                      "mixed_kernel": amdg.Batch.kernel_name(kernel[1]),
+                      "stage_ms": {amdg.Batch.kernel_name(c): t for c, t in enumerate(ms[1]) if t > 0}}), flush=True)
+    batch.rk3_steps(1, amdg.MIXED, use_graph=False)
+    torch.cuda.synchronize()
+    torch.cuda.cudart().cudaProfilerStart()
+    batch.rk3_steps(1, amdg.MIXED, use_graph=False)
+    torch.cuda.synchronize()
+    torch.cuda.cudart().cudaProfilerStop()
+    batch.close()
+    for g in grids:
+        g.close()
+
+
 def profile_linear6d():
     """Profiling case (not a bench line): one mixed SSP-RK3 step of the 6D N=8 linear workload with
     the tensor-core variant (3 launches of linear_mma_kernel), then one with the bulk-copy FMA
@@ -1377,7 +1417,7 @@ def main():
     ap.add_argument("--wave-learn-steps", type=int, default=30)
     ap.add_argument("--wave-train-samples", type=int, default=300000, help="training samples kept (stratified)")
     ap.add_argument("--wave-learn-horizon", type=int, default=2, help="time steps per learned pre-adaptation (wave)")
-    ap.add_argument("--profile", choices=["none", "wave_rhs", "config3", "rhs3d", "linear6d"], default="none",
+    ap.add_argument("--profile", choices=["none", "wave_rhs", "config3", "rhs3d", "linear6d", "batch"], default="none",
                     help="wave_rhs: run the wave right-hand-side profiling case instead of the bench")
     ap.add_argument("--wave-time", type=float, default=0.05,
                     help="final time of the 2D wave runs (the config's 0.5 takes ~5000 steps on a filling grid)")
@@ -1388,6 +1428,8 @@ def main():
         profile_config3()
     elif args.profile == "linear6d":
         profile_linear6d()
+    elif args.profile == "batch":
+        profile_batch()
     elif args.profile == "rhs3d":
         profile_rhs3d()
     elif args.impl == "reference":

@@ -323,6 +323,15 @@ amdg_status amdg_grid_get_rhs(amdg_grid* g, double* host, int64_t n);
  * new Element objects are). */
 amdg_status amdg_grid_copy_ucoe_to_predict(amdg_grid* g);
 amdg_status amdg_grid_copy_predict_to_ucoe(amdg_grid* g);
+/* DGSolution::copy_ucoe_ut_to_predict / copy_predict_to_ucoe_ut: the same for u_t (the grid's
+ * velocity field, created as zero when absent). */
+amdg_status amdg_grid_copy_ucoe_ut_to_predict(amdg_grid* g);
+amdg_status amdg_grid_copy_predict_to_ucoe_ut(amdg_grid* g);
+/* Element indicator of amdg_grid_refine / amdg_grid_coarsen: AMDG_INDICATOR_U (default) the block
+ * norm of u; AMDG_INDICATOR_U_UT that plus the block norm of u_t, as DGAdapt::indicator_norm
+ * computes it when DGSolution::prob is "wave" (DGAdapt.cpp:1018-1030). */
+enum { AMDG_INDICATOR_U = 0, AMDG_INDICATOR_U_UT = 1 };
+amdg_status amdg_grid_set_indicator(amdg_grid* g, int mode);
 /* y += a x on device vectors of n doubles (Eigen's vector update). */
 amdg_status amdg_vector_axpy(amdg_context* ctx, double a, const double* d_x, double* d_y, int64_t n);
 
@@ -332,8 +341,14 @@ amdg_status amdg_vector_axpy(amdg_context* ctx, double a, const double* d_x, dou
  * solver's rhs is zero); set_rhs_zero / add_rhs_to_eigenvec (:38, :24) act on the solver's rhs
  * vector (add: += the grid's Element::rhs); step_stage(stage) updates the grid's coefficients;
  * final() (:17) zeroes the solver's rhs (the state already is the grid's).  The element set must not change between create and step_stage. */
+/* Second-order-in-time schemes on (u, u_t) (RKODE2nd, ODESolver.h:257-283): AMDG_ODE_EULER_ODE2ND
+ * (EulerODE2nd::step_stage, ODESolver.cpp:409-414: u += dt u_t, u_t += dt rhs) and
+ * AMDG_ODE_RK4ODE2ND (RK4ODE2nd::step_stage, ODESolver.cpp:579-615: the stage state from (u, u_t)
+ * at t_n and the stage increments, the step's end at stage 3); create keeps u and u_t at t_n
+ * (the grid's velocity field, created as zero when absent), step_stage writes the grid's u and
+ * u_t. */
 typedef struct amdg_ode amdg_ode;
-enum { AMDG_ODE_FORWARD_EULER = 0, AMDG_ODE_RK3SSP = 1 };
+enum { AMDG_ODE_FORWARD_EULER = 0, AMDG_ODE_RK3SSP = 1, AMDG_ODE_EULER_ODE2ND = 2, AMDG_ODE_RK4ODE2ND = 3 };
 amdg_status amdg_ode_create(amdg_grid* g, int scheme, double dt, amdg_ode** out);
 amdg_status amdg_ode_destroy(amdg_ode* ode);
 amdg_status amdg_ode_set_rhs_zero(amdg_ode* ode);
@@ -398,8 +413,8 @@ amdg_status amdg_burgers_work(amdg_burgers_op* op, double* flops, double* transf
 /* Kernel of the transform sweeps (no reference counterpart): 0 one thread per output entry; 1 one
  * thread per column of the transformed dimension, all its entries from one load of each input
  * value; 2 / 3 / 4 one warp per (term, element), its lanes over (column, neighbour phase), the
- * phases' partial sums added by shuffles, each warp serving 1 / 2 / 4 elements; -1 (default) 0 for
- * the FP64 sweeps and 2 for the FP32 and double-float sweeps of the mixed mode.  0 and 1 sum every
+ * phases' partial sums added by shuffles, each warp serving 1 / 2 / 4 elements; -1 (default) 2 for
+ * the FP32 sweeps of the mixed mode and 0 for the FP64 and double-float sweeps.  0 and 1 sum every
  * output in the same order (identical results); 2-4 sum in another fixed order (deterministic,
  * equal to rounding). */
 amdg_status amdg_burgers_set_sweep_variant(amdg_burgers_op* op, int variant);
@@ -508,6 +523,24 @@ amdg_status amdg_wave_create(amdg_grid* g, double sigma, double amplitude, amdg_
 amdg_status amdg_wave_destroy(amdg_wave_op* op);
 /* d_rhs = L(d_u) (device arrays, dof entries). */
 amdg_status amdg_wave_rhs(amdg_wave_op* op, const double* d_u, double* d_rhs, amdg_precision prec);
+/* The wave right-hand side term by term, as the reference's driver composes it
+ * (03_wave_06_var_coeff_adapt.cpp:258-276): amdg_wave_interpolate interpolates K du/dx_d for every
+ * d (AMDG_WAVE_INTERP_GRADU: LagrInterpolation::var_coeff_gradu_Lagr_fast) or K u
+ * (AMDG_WAVE_INTERP_U: var_coeff_u_Lagr_fast) of the grid's current u; amdg_wave_rhs_add adds a
+ * term group into the grid's rhs vector (Element::rhs): AMDG_WAVE_RHS_FLX_GRADU
+ * (DiffusionRHS::rhs_flx_gradu) and AMDG_WAVE_RHS_VOL (rhs_vol) read the K grad u interpolation,
+ * AMDG_WAVE_RHS_FLX_U (rhs_flx_u) the K u one, AMDG_WAVE_RHS_IPDG the IPDG term -sigma/dx [u][v]
+ * of the current u (DiffusionAlpt::assemble_matrix_flx_ujp_vjp times u).  AMDG_ERR_STATE when the
+ * interpolation a group reads is missing for this element set and precision. */
+/* The IPDG parameter sigma of the operator (DiffusionAlpt's, BilinearForm.cpp:922-923). */
+amdg_status amdg_wave_set_sigma(amdg_wave_op* op, double sigma);
+enum { AMDG_WAVE_INTERP_GRADU = 0, AMDG_WAVE_INTERP_U = 1 };
+amdg_status amdg_wave_interpolate(amdg_wave_op* op, int which, amdg_precision prec);
+enum { AMDG_WAVE_RHS_FLX_GRADU = 0, AMDG_WAVE_RHS_VOL = 1, AMDG_WAVE_RHS_FLX_U = 2, AMDG_WAVE_RHS_IPDG = 3 };
+amdg_status amdg_wave_rhs_add(amdg_wave_op* op, int group, amdg_precision prec);
+/* RKODE2nd::add_rhs_matrix (the solver's rhs += the IPDG term of the grid's current u, FP64), and
+ * the rhs of EulerODE2nd::step_rk (the solver's rhs = that term alone, ODESolver.cpp:394-399). */
+amdg_status amdg_ode_add_wave_penalty(amdg_ode* ode, amdg_wave_op* op);
 /* amdg_burgers_set_sweep_variant for the wave operator's transform sweeps. */
 amdg_status amdg_wave_set_sweep_variant(amdg_wave_op* op, int variant);
 /* nsteps RK4ODE2nd steps of u' = v, v' = L u on the grid's (u, v)

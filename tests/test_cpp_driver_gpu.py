@@ -38,8 +38,9 @@ def test_cpp_driver_matches_oracle():
 
 
 def test_cpp_wave_driver_matches_oracle():
-    """The adaptive wave driver written against the C++ mirror (like
-    example/03_wave_06_var_coeff_adapt.cpp) ends on the oracle's element set and coefficients."""
+    """The adaptive wave driver written against the C++ mirror statement by statement like
+    example/03_wave_06_var_coeff_adapt.cpp (LagrInterpolation, DiffusionRHS, DiffusionAlpt,
+    EulerODE2nd, RK4ODE2nd) ends on the oracle's element set and coefficients."""
     exe = os.path.join(os.path.dirname(amdg.LIB_PATH), "wave_var_coeff_adapt")
     assert os.path.exists(exe), "example driver not built"
     n_init, nmax, steps, eps, eta = 3, 5, 4, 1e-5, 1e-6
@@ -55,6 +56,25 @@ def test_cpp_wave_driver_matches_oracle():
     su, sut = float(np.sum(u * u)), float(np.sum(v * v))
     assert abs(float(fields["sum of squares u"]) - su) <= 1e-12 * su
     assert abs(float(fields["sum of squares u_t"]) - sut) <= 1e-11 * sut
+
+
+def test_cpp_wave_driver_matches_reference_long_run():
+    """The same driver (term by term: EulerODE2nd predictor, refine, RK4ODE2nd stages of
+    LagrInterpolation::var_coeff_* + DiffusionRHS + the IPDG matrix term, coarsen) over the
+    reference's 24-step max-level-7 run: the final element count and the sums of squares of u and
+    u_t equal the reference run's to 1e-12 / 1e-11 relative."""
+    from helpers import golden, manifest
+    exe = os.path.join(os.path.dirname(amdg.LIB_PATH), "wave_var_coeff_adapt")
+    m = manifest()["wave_adapt2d_n7_long"]
+    z = golden("wave_adapt2d_n7_long")
+    out = subprocess.run([exe, str(m["n_init"]), str(m["nmax"]), str(m["steps"]), repr(m["eps"]), repr(m["eta"])],
+                         capture_output=True, text=True, timeout=600, check=True).stdout
+    fields = dict(line.split(":", 1) for line in out.splitlines() if ":" in line)
+    head = out.splitlines()[0].split()
+    assert int(head[5]) == m["elements"][-1]
+    cs = z["checksums"][-1]
+    assert abs(float(fields["sum of squares u"]) - cs[0]) <= 1e-12 * cs[0]
+    assert abs(float(fields["sum of squares u_t"]) - cs[4]) <= 1e-11 * cs[4]
 
 
 def test_cpp_intp_driver_matches_oracle():

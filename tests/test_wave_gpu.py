@@ -170,3 +170,92 @@ def test_adaptive_wave_long_run_matches_reference(ctx, name):
                 assert np.abs(v - v_ref).max() <= 1e-11 * np.abs(v_ref).max()
     op.close()
     g.close()
+
+
+@pytest.mark.parametrize("prec", [amdg.FP64, amdg.MIXED])
+def test_wave_terms_compose_the_fused_rhs(ctx, prec):
+    """The right-hand side composed term by term as the reference's driver does (K grad u
+    interpolation, DiffusionRHS::rhs_flx_gradu, rhs_vol, K u interpolation, rhs_flx_u, the IPDG
+    term) into the grid's rhs vector equals the fused amdg_wave_rhs bitwise (same terms, same
+    order); a group read before its interpolation is refused."""
+    g = amdg.Grid(ctx, 2, 6, 2, level_init=3)
+    g.init_separable_adaptive(O.wave_ic_terms(2), 1e-5)
+    op = amdg.WaveOperator(g, 10.0)
+    u = g.coefficients().copy()
+    du = _on_device(u)
+    out = torch.zeros_like(du)
+    torch.cuda.synchronize()
+    op.rhs_device(du.data_ptr(), out.data_ptr(), prec)
+    ctx.synchronize()
+    fused = out.cpu().numpy().reshape(u.shape)
+    g.set_rhs_zero()
+    with pytest.raises(amdg.AmdgError) as ei:
+        op.rhs_add(op.RHS_FLX_U, prec)
+    assert ei.value.status == 6
+    op.interpolate(op.INTERP_GRADU, prec)
+    op.rhs_add(op.RHS_FLX_GRADU, prec)
+    op.rhs_add(op.RHS_VOL, prec)
+    op.interpolate(op.INTERP_U, prec)
+    op.rhs_add(op.RHS_FLX_U, prec)
+    op.rhs_add(op.RHS_IPDG, prec)
+    ctx.synchronize()
+    assert np.array_equal(g.rhs(), fused)
+    op.close()
+    g.close()
+
+
+def test_wave_rk4ode2nd_stages_match_the_fused_step(ctx):
+    """RK4ODE2nd stage by stage (the integrator object, rhs_to_eigenvec + add_rhs_matrix per
+    stage) equals amdg_wave_rk4_steps bitwise; EulerODE2nd's step_rk (rhs = the IPDG term alone)
+    gives u + dt u_t and u_t + dt IPDG(u)."""
+    g = amdg.Grid(ctx, 2, 5, 2)
+    g.init_separable(O.wave_ic_terms(2))
+    u0 = g.coefficients().copy()
+    rng = np.random.default_rng(2)
+    v0 = 1e-3 * rng.standard_normal(u0.shape)
+    op = amdg.WaveOperator(g, 10.0)
+    dt = 1e-4
+    g.set_coefficients(u0)
+    g.set_velocity(v0)
+    op.rk4_steps(dt, 1)
+    ctx.synchronize()
+    want_u, want_v = g.coefficients().copy(), g.velocity().copy()
+    g.set_coefficients(u0)
+    g.set_velocity(v0)
+    ode = amdg.ODE(g, amdg.ODE.RK4ODE2ND, dt)
+    for stage in range(4):
+        g.set_rhs_zero()
+        op.interpolate(op.INTERP_GRADU)
+        op.rhs_add(op.RHS_FLX_GRADU)
+        op.rhs_add(op.RHS_VOL)
+        op.interpolate(op.INTERP_U)
+        op.rhs_add(op.RHS_FLX_U)
+        ode.set_rhs_zero()
+        ode.add_rhs_to_eigenvec()
+        ode.add_wave_penalty(op)
+        ode.step_stage(stage)
+        ode.final()
+    ctx.synchronize()
+    assert np.array_equal(g.coefficients(), want_u)
+    assert np.array_equal(g.velocity(), want_v)
+    ode.close()
+    # EulerODE2nd: u + dt v, v + dt IPDG(u)
+    g.set_coefficients(u0)
+    g.set_velocity(v0)
+    pen = torch.zeros(g.dof, dtype=torch.float64, device="cuda")
+    g.set_rhs_zero()
+    op.rhs_add(op.RHS_IPDG)
+    ctx.synchronize()
+    ipdg = g.rhs().copy()
+    ode = amdg.ODE(g, amdg.ODE.EULER_ODE2ND, dt)
+    ode.set_rhs_zero()
+    ode.add_wave_penalty(op)
+    ode.step_stage(0)
+    ode.final()
+    ctx.synchronize()
+    assert np.array_equal(g.coefficients(), u0 + dt * v0)
+    assert np.array_equal(g.velocity(), v0 + dt * ipdg)
+    del pen
+    ode.close()
+    op.close()
+    g.close()
