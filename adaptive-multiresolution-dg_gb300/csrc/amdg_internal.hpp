@@ -579,6 +579,7 @@ struct amdg_batch {
     int64_t sstride = 0;
     int32_t* d_pairs = nullptr;           // (src, blk) interleaved per neighbour pair (bulk-copy ring kernel)
     float* d_blocks32p = nullptr;         // [2][num_blocks][(np^2 + 3) / 4 * 4]
+    double* d_blocks64p = nullptr;        // the same in FP64
     float* d_dt32 = nullptr;              // [solve]
     int* d_err = nullptr;                 // bulk-copy wait gave up (device flag)
     void* graph_exec[2] = {nullptr, nullptr};  // cudaGraphExec_t per precision

@@ -101,6 +101,7 @@ amdg_status df_col_stage(amdg_batch* b, int threads, int stage, int in, int out,
     L.num_elements = b->num_elements; L.num_blocks = b->num_blocks;
     L.xs = hi_of(b, in);
     L.row_ptr = b->d_row_ptr; L.src = b->d_src; L.blk = b->d_blk; L.blocks = b->d_blocks32;
+    L.pairs = reinterpret_cast<const int2*>(b->d_pairs); L.blocks_p = b->d_blocks32p;
     L.coef = b->d_coef32; L.dt = b->d_dt; L.solve_of = b->d_solve;
     L.df = df_stage(c);
     L.df.us_hi = hi_of(b, in); L.df.us_lo = lo_of(b, in);
@@ -140,6 +141,7 @@ amdg_status batch_step(amdg_batch* b, amdg_precision prec, cudaStream_t st) {
             L.num_elements = b->num_elements; L.num_blocks = b->num_blocks;
             L.us = in[stage]; L.xs = sh[stage]; L.un = b->d_u; L.out = out[stage]; L.shadow_out = sh[sout[stage]];
             L.row_ptr = b->d_row_ptr; L.src = b->d_src; L.blk = b->d_blk; L.blocks = b->d_blocks32;
+            L.pairs = reinterpret_cast<const int2*>(b->d_pairs); L.blocks_p = b->d_blocks32p;
             L.coef = b->d_coef32; L.dt = b->d_dt; L.solve_of = b->d_solve;
             AMDG_CK(launch_batch<float, float>(L, st));
         } else {
@@ -148,6 +150,7 @@ amdg_status batch_step(amdg_batch* b, amdg_precision prec, cudaStream_t st) {
             L.num_elements = b->num_elements; L.num_blocks = b->num_blocks;
             L.us = in[stage]; L.xs = in[stage]; L.un = b->d_u; L.out = out[stage]; L.shadow_out = nullptr;
             L.row_ptr = b->d_row_ptr; L.src = b->d_src; L.blk = b->d_blk; L.blocks = b->d_blocks64;
+            L.pairs = reinterpret_cast<const int2*>(b->d_pairs); L.blocks_p = b->d_blocks64p;
             L.coef = b->d_coef64; L.dt = b->d_dt; L.solve_of = b->d_solve;
             AMDG_CK(launch_batch<double, double>(L, st));
         }
@@ -188,12 +191,13 @@ amdg_status batch_build(amdg_batch* b) {
             b->graph_exec[p] = nullptr;
         }
     void* old[] = {b->d_row_ptr, b->d_src, b->d_blk, b->d_solve, b->d_blocks64, b->d_blocks32,
-                   b->d_u, b->d_u1, b->d_u2, b->d_shadow, b->d_lo, b->d_pairs, b->d_blocks32p};
+                   b->d_u, b->d_u1, b->d_u2, b->d_shadow, b->d_lo, b->d_pairs, b->d_blocks32p, b->d_blocks64p};
     for (void* p : old) cudaFree(p);
     b->d_row_ptr = b->d_src = nullptr;
     b->d_blk = b->d_solve = nullptr;
     b->d_blocks64 = b->d_u = b->d_u1 = b->d_u2 = nullptr;
     b->d_blocks32 = b->d_shadow = b->d_lo = b->d_blocks32p = nullptr;
+    b->d_blocks64p = nullptr;
     b->d_pairs = nullptr;
     b->elem_offset = topo.elem_offset;
     b->num_elements = topo.elem_offset[n];
@@ -204,8 +208,12 @@ amdg_status batch_build(amdg_batch* b) {
     // the ring kernel's tables padded to 16-byte blocks and its interleaved (src, blk) pairs
     const int np = b->k + 1, bs = (np * np + 3) / 4 * 4;
     std::vector<float> b32p(size_t(2) * b->num_blocks * bs, 0.f);
+    std::vector<double> b64p(size_t(2) * b->num_blocks * bs, 0.0);
     for (int64_t j = 0; j < int64_t(2) * b->num_blocks; ++j)
-        for (int i = 0; i < np * np; ++i) b32p[size_t(j) * bs + i] = b32[size_t(j) * np * np + i];
+        for (int i = 0; i < np * np; ++i) {
+            b32p[size_t(j) * bs + i] = b32[size_t(j) * np * np + i];
+            b64p[size_t(j) * bs + i] = topo.blocks[size_t(j) * np * np + i];
+        }
     AMDG_REQUIRE(b->num_elements < (int64_t(1) << 31), AMDG_ERR_CAPACITY, "more than 2^31-1 elements in the batch");
     std::vector<int32_t> pairs(2 * topo.src.size());
     for (size_t i = 0; i < topo.src.size(); ++i) {
@@ -217,7 +225,8 @@ amdg_status batch_build(amdg_batch* b) {
     if ((s = put(&b->d_row_ptr, topo.row_ptr)) != AMDG_OK || (s = put(&b->d_src, topo.src)) != AMDG_OK ||
         (s = put(&b->d_blk, topo.blk)) != AMDG_OK || (s = put(&b->d_solve, topo.solve_of)) != AMDG_OK ||
         (s = put(&b->d_blocks64, topo.blocks)) != AMDG_OK || (s = put(&b->d_blocks32, b32)) != AMDG_OK ||
-        (s = put(&b->d_blocks32p, b32p)) != AMDG_OK || (s = put(&b->d_pairs, pairs)) != AMDG_OK ||
+        (s = put(&b->d_blocks32p, b32p)) != AMDG_OK || (s = put(&b->d_blocks64p, b64p)) != AMDG_OK ||
+        (s = put(&b->d_pairs, pairs)) != AMDG_OK ||
         (s = alloc(&b->d_u, size_t(b->dof))) != AMDG_OK || (s = alloc(&b->d_u1, size_t(b->dof))) != AMDG_OK ||
         (s = alloc(&b->d_u2, size_t(b->dof))) != AMDG_OK ||
         (s = alloc(&b->d_shadow, size_t(b->sstride) * 3)) != AMDG_OK ||
@@ -267,6 +276,7 @@ amdg_status autotune_batch(amdg_batch* b, cudaStream_t st) {
                     L.num_elements = b->num_elements; L.num_blocks = b->num_blocks;
                     L.us = b->d_u; L.xs = hi_of(b, 0); L.un = b->d_u; L.out = b->d_u1; L.shadow_out = hi_of(b, 1);
                     L.row_ptr = b->d_row_ptr; L.src = b->d_src; L.blk = b->d_blk; L.blocks = b->d_blocks32;
+                    L.pairs = reinterpret_cast<const int2*>(b->d_pairs); L.blocks_p = b->d_blocks32p;
                     L.coef = b->d_coef32; L.dt = b->d_dt; L.solve_of = b->d_solve;
                     if (e == cudaSuccess) e = launch_batch<float, float>(L, st);
                 } else {
@@ -275,6 +285,7 @@ amdg_status autotune_batch(amdg_batch* b, cudaStream_t st) {
                     L.num_elements = b->num_elements; L.num_blocks = b->num_blocks;
                     L.us = b->d_u; L.xs = b->d_u; L.un = b->d_u; L.out = b->d_u1; L.shadow_out = nullptr;
                     L.row_ptr = b->d_row_ptr; L.src = b->d_src; L.blk = b->d_blk; L.blocks = b->d_blocks64;
+                    L.pairs = reinterpret_cast<const int2*>(b->d_pairs); L.blocks_p = b->d_blocks64p;
                     L.coef = b->d_coef64; L.dt = b->d_dt; L.solve_of = b->d_solve;
                     if (e == cudaSuccess) e = launch_batch<double, double>(L, st);
                 }
@@ -391,7 +402,7 @@ amdg_status amdg_batch_destroy(amdg_batch* b) {
         if (b->graph_exec[p]) cudaGraphExecDestroy(static_cast<cudaGraphExec_t>(b->graph_exec[p]));
     void* ptrs[] = {b->d_row_ptr, b->d_src, b->d_blk, b->d_solve, b->d_blocks64, b->d_blocks32, b->d_coef64,
                     b->d_coef32, b->d_dt, b->d_u, b->d_u1, b->d_u2, b->d_shadow, b->d_lo, b->d_pairs,
-                    b->d_blocks32p, b->d_dt32, b->d_err, b->d_pg, b->d_feat, b->d_prob, b->d_norms};
+                    b->d_blocks32p, b->d_blocks64p, b->d_dt32, b->d_err, b->d_pg, b->d_feat, b->d_prob, b->d_norms};
     for (void* p : ptrs) cudaFree(p);
     delete b;
     return AMDG_OK;

@@ -82,6 +82,10 @@ struct BatchLaunch {
     // solve s is dt32[s]) and us / un / out / shadow_out are unused
     DFState df;
     const float* dt32;
+    // when both are set: (src, blk) as int32 pairs and the table padded to (np^2 + 3) / 4 * 4
+    // entries per block (vector loads)
+    const int2* pairs;
+    const T* blocks_p;
 };
 template <typename T, typename X>
 cudaError_t launch_batch(const BatchLaunch<T, X>& L, cudaStream_t st);

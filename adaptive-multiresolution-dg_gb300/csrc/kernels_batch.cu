@@ -26,6 +26,19 @@ __device__ __forceinline__ double batch_combine(double a, double un, double b, d
     return __dadd_rn(__dmul_rn(a, un), __dmul_rn(b, __dadd_rn(us, __dmul_rn(dt, rhs))));
 }
 
+// the BS entries of a padded 1D block (BS a multiple of 4: 16-byte loads)
+template <typename T, int BS>
+__device__ __forceinline__ void load_padded_block(const T* p, T (&v)[BS]) {
+    constexpr int V = BS * int(sizeof(T)) / 16;
+    const float4* p4 = reinterpret_cast<const float4*>(p);
+    float4 w[V];
+#pragma unroll
+    for (int i = 0; i < V; ++i) w[i] = __ldg(p4 + i);
+    const T* wt = reinterpret_cast<const T*>(w);
+#pragma unroll
+    for (int i = 0; i < BS; ++i) v[i] = wt[i];
+}
+
 template <int D, int NP, int TH, typename T, typename X>
 __global__ void __launch_bounds__(TH) batch_col_kernel(BatchLaunch<T, X> L) {
     constexpr int B = BPow<NP, D>::v;
@@ -54,17 +67,36 @@ __global__ void __launch_bounds__(TH) batch_col_kernel(BatchLaunch<T, X> L) {
             for (int q = 0; q < NP; ++q) acc[q] = T(0);
             const int64_t beg = __ldg(L.row_ptr + e * D + t);
             const int64_t end = __ldg(L.row_ptr + e * D + t + 1);
-            for (int64_t i = beg; i < end; ++i) {
-                const int64_t sidx = __ldg(L.src + i);
-                const T* m = table + __ldg(L.blk + i) * NP * NP;
-                const X* x = L.xs + sidx * B + base;
-                T xv[NP];
+            if (L.pairs && L.blocks_p) {
+                // (src, blk) as one 8-byte load, the 1D block as 16-byte loads of the padded table
+                constexpr int BS = (NP * NP + 3) / 4 * 4;
+                const T* tab = L.blocks_p + (ct >= T(0) ? 0 : size_t(L.num_blocks) * BS);
+                for (int64_t i = beg; i < end; ++i) {
+                    const int2 pr = __ldg(L.pairs + i);
+                    T mv[BS];
+                    load_padded_block<T, BS>(tab + size_t(pr.y) * BS, mv);
+                    const X* x = L.xs + int64_t(pr.x) * B + base;
+                    T xv[NP];
 #pragma unroll
-                for (int p = 0; p < NP; ++p) xv[p] = T(__ldg(x + p * stride));
+                    for (int p = 0; p < NP; ++p) xv[p] = T(__ldg(x + p * stride));
 #pragma unroll
-                for (int p = 0; p < NP; ++p)
+                    for (int p = 0; p < NP; ++p)
 #pragma unroll
-                    for (int q = 0; q < NP; ++q) acc[q] = fma(__ldg(m + p * NP + q), xv[p], acc[q]);
+                        for (int q = 0; q < NP; ++q) acc[q] = fma(mv[p * NP + q], xv[p], acc[q]);
+                }
+            } else {
+                for (int64_t i = beg; i < end; ++i) {
+                    const int64_t sidx = __ldg(L.src + i);
+                    const T* m = table + __ldg(L.blk + i) * NP * NP;
+                    const X* x = L.xs + sidx * B + base;
+                    T xv[NP];
+#pragma unroll
+                    for (int p = 0; p < NP; ++p) xv[p] = T(__ldg(x + p * stride));
+#pragma unroll
+                    for (int p = 0; p < NP; ++p)
+#pragma unroll
+                        for (int q = 0; q < NP; ++q) acc[q] = fma(__ldg(m + p * NP + q), xv[p], acc[q]);
+                }
             }
             T* yb = y + g * B + base;
 #pragma unroll

@@ -507,9 +507,9 @@ cudaError_t launch_sweep(const SweepArgs<T>& a, cudaStream_t st) {
         case 53: sweep_col_kernel<T, 5, 3><<<blocks, 256, 0, st>>>(a); break;
         case 63: sweep_col_kernel<T, 6, 3><<<blocks, 256, 0, st>>>(a); break;
         default:
-            // measured: the node-row grid is the faster one for the FP32 and double-float sweeps, the
-            // flat grid for the FP64 ones
-            if constexpr (std::is_same<T, double>::value) {
+            // measured: the node-row grid is the faster one for the FP32 sweeps, the flat grid for
+            // the FP64 and double-float ones
+            if constexpr (!std::is_same<T, float>::value) {
                 sweep_kernel<T, false><<<unsigned((total + 255) / 256), 256, 0, st>>>(a);
             } else {
                 const dim3 grid(unsigned((a.num_elements * a.out_block + 255) / 256), unsigned(a.count));

@@ -24,6 +24,9 @@
 //     coefficients of the flux in dimension d), rhs0 and uT; then DGSolution::val
 //     and the exact solution at 48 fixed points ("vals") and the L1/L2/Linf errors
 //     of get_error_no_separable_scalar with 1 and 2 Gauss points ("NORMERR").
+//   ref_harness burgers_herm <N> <alpha> <steps> <dt>
+//     the 2D version with the flux interpolated by cubic Hermite interpolation
+//     (HermInterpolation::nonlinear_Herm_2D_fast, HyperbolicSameFluxHermRHS), see run_burgers_herm.
 //   ref_harness burgers_adapt <dim> <N_init> <NMAX> <eps> <eta> <alpha> <cfl> <umax> <steps>
 //     adaptive version of the above, following the time loop of
 //     example/02_hyperbolic_05_burgers_adapt.cpp:223-476 with the Lagrange
@@ -389,6 +392,78 @@ int run_burgers(int argc, char** argv) {
         std::vector<double> err = dg.get_error_no_separable_scalar(exact, gp);
         std::printf("NORMERR %d %.17g %.17g %.17g\n", gp, err[0], err[1], err[2]);
     }
+    return 0;
+}
+
+// 2D Burgers with the flux interpolated by cubic Hermite interpolation (HermBasis::PMAX = 3,
+// msh_case 1), as example/02_hyperbolic_05_burgers_adapt.cpp:192-263 composes it:
+// HermInterpolation::nonlinear_Herm_2D_fast (flux, its first and second derivative; interpolation
+// in x only, the flux being the same in every direction), HyperbolicSameFluxHermRHS::rhs_vol_scalar
+// and rhs_flx_intp_scalar, HyperbolicAlptRHS::rhs_flx_penalty_scalar(alpha); RK3SSP step_stage on
+// the sparse grid of level N.  Dumps u0, up0 (u and its x / y / xy derivatives at the Hermite
+// points), fu0 (the flux's Hermite coefficients), rhs0 and uT.
+int run_burgers_herm(int argc, char** argv) {
+    if (argc < 6) { std::fprintf(stderr, "burgers_herm: bad args\n"); return 2; }
+    const int dim = 2;
+    const int N = std::atoi(argv[2]);
+    const double alpha = std::atof(argv[3]);
+    const int steps = std::atoi(argv[4]);
+    const double dt = std::atof(argv[5]);
+    const int k = 2;
+    set_statics(dim, k);
+    Hash hash;
+    LagrBasis::set_interp_msh01();
+    HermBasis::set_interp_msh01();
+    AllBasis<AlptBasis> all_bas_alpt(N);
+    AllBasis<LagrBasis> all_bas_lagr(N);
+    AllBasis<HermBasis> all_bas_herm(N);
+    OperatorMatrix1D<AlptBasis, AlptBasis> oper_alpt(all_bas_alpt, all_bas_alpt, "period");
+    OperatorMatrix1D<HermBasis, AlptBasis> oper_herm(all_bas_herm, all_bas_alpt, "period");
+    DGAdapt dg(true, N, N, all_bas_alpt, all_bas_lagr, all_bas_herm, hash, 1e10, -1, true, false);
+    const double PI = Const::PI;
+    std::vector<std::function<double(double, int)>> funcs;
+    funcs.push_back([](double, int d) { return d == 0 ? 0.5 : 1.0; });
+    funcs.push_back([=](double x, int d) { return d == 0 ? 0.25 * std::sin(2 * PI * x) : std::cos(2 * PI * x); });
+    funcs.push_back([=](double x, int d) { return d == 0 ? 0.25 * std::cos(2 * PI * x) : std::sin(2 * PI * x); });
+    dg.init_separable_scalar_sum(funcs);
+    std::printf("META dim=%d N=%d k=%d sparse=1 elements=%zu dof=%d\n", dim, N, k, dg.dg.size(), dg.get_dof());
+    dump_elements("u0", dg, 0);
+    auto flux = [](std::vector<double> u, int, int) -> double { return FluxFunction::burgers_flux_scalar(u[0]); };
+    auto flux_d1 = [](std::vector<double> u, int, int, int) -> double {
+        return FluxFunction::burgers_flux_1st_derivative_scalar(u[0]);
+    };
+    auto flux_d2 = [](std::vector<double> u, int, int, int, int) -> double {
+        return FluxFunction::burgers_flux_2nd_derivative_scalar(u[0]);
+    };
+    std::vector<std::vector<bool>> is_intp_herm{std::vector<bool>{true, false}};
+    HermInterpolation interp(dg);
+    FastHermIntp fast_herm(dg, interp.Her_pt_Alpt_1D);
+    HyperbolicSameFluxHermRHS rhs_herm(dg, oper_herm);
+    HyperbolicAlptRHS rhs_alpt(dg, oper_alpt);
+    const std::vector<double> lxf(dim, alpha);
+    auto rhs_eval = [&]() {
+        interp.nonlinear_Herm_2D_fast(flux, flux_d1, flux_d2, is_intp_herm, fast_herm);
+        dg.set_rhs_zero();
+        rhs_herm.rhs_vol_scalar();
+        rhs_herm.rhs_flx_intp_scalar();
+        rhs_alpt.rhs_flx_penalty_scalar(lxf);
+    };
+    rhs_eval();
+    dump_elements_vec("up0", dg, [](const Element& e) -> const VecMultiD<double>& { return e.up_intp[0]; });
+    dump_elements_vec("fu0", dg, [](const Element& e) -> const VecMultiD<double>& { return e.fucoe_intp[0][0]; });
+    dump_elements("rhs0", dg, 1);
+    for (int s = 0; s < steps; ++s) {
+        RK3SSP ode(dg, dt);
+        ode.init();
+        for (int stage = 0; stage < 3; ++stage) {
+            rhs_eval();
+            ode.set_rhs_zero();
+            ode.add_rhs_to_eigenvec();
+            ode.step_stage(stage);
+            ode.final();
+        }
+    }
+    dump_elements("uT", dg, 0);
     return 0;
 }
 
@@ -794,6 +869,7 @@ int main(int argc, char** argv) {
     if (mode == "linear") return run_linear(argc, argv);
     if (mode == "matrices") return run_matrices(argc, argv);
     if (mode == "burgers") return run_burgers(argc, argv);
+    if (mode == "burgers_herm") return run_burgers_herm(argc, argv);
     if (mode == "burgers_adapt") return run_burgers_adapt(argc, argv);
     if (mode == "wave") return run_wave(argc, argv);
     if (mode == "wave_adapt") return run_wave_adapt(argc, argv);
