@@ -735,9 +735,11 @@ double amdg_oracle_lagr_point(int level, int suppt, int p) {
     return a + (b - a) * (LS->pt1[p] + 1.0) / 2.0;
 }
 
-/* generic 1D basis evaluation: type 0 = Alpert (degree k), 1 = Lagrange (the chosen degree) */
+/* generic 1D basis evaluation: type 0 = Alpert (degree k), 1 = Lagrange (the chosen degree),
+ * 2 = cubic Hermite */
 static double basis_val(int type, int k, int n, int j, int p, int deriv, double x, int sgn) {
     if (type == 0) return amdg_oracle_alpert_val(k, n, j, p, deriv, x, sgn);
+    if (type == 2) return amdg_oracle_herm_val(n, j, p, deriv, x, sgn);
     return amdg_oracle_lagr_val(n, j, p, x, sgn);
 }
 
@@ -1600,4 +1602,336 @@ int amdg_oracle_wave_penalty(int dim, int N, int k, int64_t E, const int32_t* le
     free(ul); free(ur);
     fast_ctx_free(&c);
     return 0;
+}
+
+/* ------------------------------------------------------------------------ */
+/* Cubic Hermite interpolation of the flux (HermBasis with PMAX 3 and        */
+/* msh_case 1, HermInterpolation::nonlinear_Herm_2D_fast,                    */
+/* Interplation.cpp:4609-4621; the 2D Burgers driver                         */
+/* example/02_hyperbolic_05_burgers_adapt.cpp).  A 1D element carries four   */
+/* degrees of freedom pp: point pp % 2 and derivative order pp / 2           */
+/* (HermBasis::deg_pt_deri_1d, HermBasis.cpp).                               */
+/* ------------------------------------------------------------------------ */
+
+/* Mother functions on [0, 1] and their first derivatives (HermBasis::phi_P1_L1 and its
+ * derivative).  Level 0 interpolates value and slope at x = 0 (point 0) and x = 1 (point 1);
+ * level 1 at the midpoint, the point-0 pair supported on [0, 1/2] and the point-1 pair on
+ * [1/2, 1], both vanishing with their slope at the far end. */
+static double herm_mother(double x, int msh, int pp, int deriv) {
+    if (x < 0.0 || x > 1.0) return 0.0;
+    const int pt = pp % 2, l = pp / 2;
+    if (msh == 0) {
+        if (pt == 0) {
+            if (l == 0) return deriv ? 6.0 * x * (x - 1.0) : (x - 1.0) * (x - 1.0) * (1.0 + 2.0 * x);
+            return deriv ? (1.0 - x) * (1.0 - 3.0 * x) : (1.0 - x) * (1.0 - x) * x;
+        }
+        if (l == 0) return deriv ? 6.0 * x * (1.0 - x) : x * x * (3.0 - 2.0 * x);
+        return deriv ? x * (3.0 * x - 2.0) : (x - 1.0) * x * x;
+    }
+    if (pt == 0) {
+        if (x > 0.5) return 0.0;
+        if (l == 0) return deriv ? 24.0 * x * (1.0 - 2.0 * x) : 4.0 * x * x * (3.0 - 4.0 * x);
+        return deriv ? 4.0 * x * (3.0 * x - 1.0) : 2.0 * x * x * (2.0 * x - 1.0);
+    }
+    if (x < 0.5) return 0.0;
+    if (l == 0) return deriv ? 24.0 * (x - 1.0) * (2.0 * x - 1.0) : 4.0 * (x - 1.0) * (x - 1.0) * (4.0 * x - 1.0);
+    return deriv ? 4.0 * (x - 1.0) * (3.0 * x - 2.0) : 2.0 * (x - 1.0) * (x - 1.0) * (2.0 * x - 1.0);
+}
+
+/* HermBasis::val (HermBasis.cpp): levels >= 2 are the level-1 pair mapped onto the support, a
+ * slope dof scaled by the support width (2^-(n-1) per derivative order of the dof, 2^(n-1) per
+ * derivative taken); the one-sided limits of Basis::val. */
+double amdg_oracle_herm_val(int level, int suppt, int p, int deriv, double x, int sgn) {
+    double xl = x;
+    if (sgn == -1) {
+        if (fabs(x) <= ROUND_OFF) return 0.0;
+        xl -= ROUND_OFF;
+    } else if (sgn == 1) {
+        if (fabs(x - 1.0) <= ROUND_OFF) return 0.0;
+        xl += ROUND_OFF;
+    }
+    if (level <= 1) return herm_mother(xl, level, p, deriv);
+    const double xt = pow(2.0, level - 1) * xl - (suppt - 1) / 2;
+    return herm_mother(xt, 1, p, deriv) * pow(2.0, -(level - 1) * (p / 2 - deriv));
+}
+
+/* interpolation point of dof p of 1D element (n, j) (HermBasis::set_interp_msh01 and the
+ * HermBasis constructor): level 0 the two end points moved 1e-13 inside, in [-1, 1] coordinates
+ * mapped by (x + 1) / 2; level >= 1 the two sides of the midpoint */
+double amdg_oracle_herm_point(int level, int suppt, int p) {
+    if (level == 0) return ((p % 2 == 0 ? (-1.0 + ROUND_OFF) : (1.0 - ROUND_OFF)) + 1.0) / 2.0;
+    const double m = ((p % 2 == 0 ? (0.0 - ROUND_OFF) : (0.0 + ROUND_OFF)) + 1.0) / 2.0;
+    const double a = support_lo(level, suppt), b = support_hi(level, suppt);
+    return a + (b - a) * m;
+}
+
+/* Hermite (rows, 2^N x 4) x Alpert (cols, 2^N x (k+1)) 1D matrices of
+ * OperatorMatrix1D<HermBasis, AlptBasis> (OperatorMatrix1D.h:166-199): u_v, u_vx and
+ * (ulft_vjp + urgt_vjp) */
+int amdg_oracle_oper1d_herm(int N, int k, double* u_v, double* u_vx, double* uave2_vjp) {
+    const int nr = (1 << N) * 4, nc = (1 << N) * (k + 1);
+#pragma omp parallel for schedule(dynamic)
+    for (int r = 0; r < nr; ++r) {
+        const elem1d u = elem_of_order(r / 4);
+        const int pu = r % 4;
+        for (int c = 0; c < nc; ++c) {
+            const elem1d v = elem_of_order(c / (k + 1));
+            const int pv = c % (k + 1);
+            const size_t idx = (size_t)r * nc + c;
+            if (u_v) u_v[idx] = gproduct_volume(2, 0, k, u, pu, v, pv, 0, 0);
+            if (u_vx) u_vx[idx] = gproduct_volume(2, 0, k, u, pu, v, pv, 0, 1);
+            if (uave2_vjp) {
+                const double l = gproduct_edge(2, 0, k, u, pu, v, pv, -1, 1) - gproduct_edge(2, 0, k, u, pu, v, pv, -1, -1);
+                const double rr = gproduct_edge(2, 0, k, u, pu, v, pv, 1, 1) - gproduct_edge(2, 0, k, u, pu, v, pv, 1, -1);
+                uave2_vjp[idx] = l + rr;
+            }
+        }
+    }
+    return 0;
+}
+
+/* Alpert basis at the Hermite points, rows = Alpert basis, cols = Hermite dof: the value for a
+ * value dof, the first derivative for a slope dof, zero where the point lies outside the
+ * support (HermInterpolation::eval_Her_pt_at_Alpt_1D, Interplation.cpp:1886-1975, transposed as
+ * FastHermIntp's alpt_basis_herm_pt, FastMultiplyLU.cpp:1316-1331) */
+static double* alpt_at_herm_points(int N, int k) {
+    const int np = k + 1, n1 = 1 << N, na = n1 * np, nh = n1 * 4;
+    double* m = (double*)calloc((size_t)na * nh, sizeof(double));
+    if (!m) return NULL;
+    for (int c = 0; c < nh; ++c) {
+        const elem1d eh = elem_of_order(c / 4);
+        const double x = amdg_oracle_herm_point(eh.n, eh.j, c % 4);
+        for (int r = 0; r < na; ++r) {
+            const elem1d ea = elem_of_order(r / np);
+            if (x < support_lo(ea.n, ea.j) || x > support_hi(ea.n, ea.j)) continue;
+            m[(size_t)r * nh + c] = amdg_oracle_alpert_val(k, ea.n, ea.j, r % np, (c % 4) / 2, x, 0);
+        }
+    }
+    return m;
+}
+
+/* u_h and its derivatives at the Hermite points of every element, summed directly over all
+ * elements whose support holds the point: up[e][p], 4^dim per element, entry p the mixed
+ * derivative of u_h given by the slope dofs of p (FastHermIntp::eval_up_Herm's quantity) */
+int amdg_oracle_herm_point_values(int dim, int N, int k, int64_t E, const int32_t* level, const int32_t* suppt,
+                                  const double* u, double* up) {
+    ehash h;
+    if (ehash_build(&h, dim, N, E, level, suppt)) return -2;
+    const int np = k + 1, B = ipow(np, dim), P = ipow(4, dim);
+#pragma omp parallel for schedule(dynamic, 8)
+    for (int64_t e = 0; e < E; ++e) {
+        for (int p = 0; p < P; ++p) {
+            double x[16];
+            int pd[16], rem = p;
+            for (int d = dim - 1; d >= 0; --d) { pd[d] = rem % 4; rem /= 4; }
+            for (int d = 0; d < dim; ++d) x[d] = amdg_oracle_herm_point(level[e * dim + d], suppt[e * dim + d], pd[d]);
+            double val = 0.0;
+            int lv[16] = {0};
+            for (;;) {
+                int o[16];
+                for (int d = 0; d < dim; ++d) o[d] = order_containing(lv[d], x[d]);
+                const int64_t s = ehash_find(&h, pack_key(o, dim, N));
+                if (s >= 0) {
+                    double phi[16][4];
+                    for (int d = 0; d < dim; ++d) {
+                        const elem1d ed = elem_of_order(o[d]);
+                        for (int q = 0; q < np; ++q) phi[d][q] = amdg_oracle_alpert_val(k, ed.n, ed.j, q, pd[d] / 2, x[d], 0);
+                    }
+                    for (int q = 0; q < B; ++q) {
+                        int r2 = q, qd[16];
+                        double w = 1.0;
+                        for (int d = dim - 1; d >= 0; --d) { qd[d] = r2 % np; r2 /= np; }
+                        for (int d = 0; d < dim; ++d) w *= phi[d][qd[d]];
+                        val += w * u[s * B + q];
+                    }
+                }
+                int d = dim - 1;
+                while (d >= 0) {
+                    if (++lv[d] <= N) break;
+                    lv[d] = 0;
+                    --d;
+                }
+                if (d < 0) break;
+            }
+            up[e * P + p] = val;
+        }
+    }
+    ehash_free(&h);
+    return 0;
+}
+
+/* the same quantity by the reference's fast transforms (FastHermIntp::eval_up_Herm ->
+ * transform_ucoealpt_to_upintp, FastMultiplyLU.cpp:1333-1336) */
+int amdg_oracle_herm_point_values_fast(int dim, int N, int k, int64_t E, const int32_t* level, const int32_t* suppt,
+                                       const double* u, double* up) {
+    fast_ctx c;
+    if (fast_ctx_init(&c, dim, N, E, level, suppt)) return -2;
+    double* a2h = alpt_at_herm_points(N, k);
+    if (!a2h) return -2;
+    const double* M[16];
+    int flx[16];
+    for (int d = 0; d < dim; ++d) { M[d] = a2h; flx[d] = 0; }
+    memset(up, 0, (size_t)E * ipow(4, dim) * sizeof(double));
+    const int rc = fast_partial_sums(&c, u, k + 1, 4, M, flx, 1.0, up);
+    free(a2h);
+    fast_ctx_free(&c);
+    return rc;
+}
+
+/* The Burgers flux f = u^2/2 and its derivatives at the 2D Hermite points, from u_h and its
+ * derivatives there (HermInterpolation::eval_fp_Her_2D, Interplation.cpp:2045-2300, with
+ * f' = u and f'' = 1, FluxFunction::burgers_flux_*, Interplation.cpp:5070-5083): f for a value
+ * dof pair, f' u_x or f' u_y for one slope dof, f'' u_x u_y + f' u_xy for two; the same operation
+ * order. */
+int amdg_oracle_herm_flux_burgers2d(int64_t E, const double* up, double* fp) {
+    for (int64_t e = 0; e < E; ++e) {
+        const double* v = up + e * 16;
+        double* f = fp + e * 16;
+        for (int p0 = 0; p0 < 4; ++p0)
+            for (int p1 = 0; p1 < 4; ++p1) {
+                const int kx = p0 / 2, ky = p1 / 2, i = p0 * 4 + p1;
+                if (!kx && !ky) {
+                    f[i] = v[i] * v[i] * 0.5;
+                } else if (kx && !ky) {
+                    f[i] = 0.0 + v[(p0 - 2) * 4 + p1] * v[i];
+                } else if (!kx && ky) {
+                    f[i] = 0.0 + v[p0 * 4 + p1 - 2] * v[i];
+                } else {
+                    const double uu = v[(p0 - 2) * 4 + p1 - 2], ux = v[p0 * 4 + p1 - 2], uy = v[(p0 - 2) * 4 + p1];
+                    double a = 0.0;
+                    a += 1.0 * ux * uy;
+                    a += uu * v[i];
+                    f[i] = a;
+                }
+            }
+    }
+    return 0;
+}
+
+/* Hierarchical Hermite surplus, dimension by dimension (HermInterpolation::eval_fp_to_coe_D_Her,
+ * Interplation.cpp:3651-3849, weights of set_pts_wts_1d_ada_Her, :3166-3316): in pass d every
+ * element with level_d = l > 0 subtracts the cubic Hermite interpolant through the four coarser
+ * dofs inside its dimension-d support (the two end points, value and slope each): ancestor ic
+ * (found in the order of coarser levels, elements, dofs) is numbered ic0 = 0, 2 at the smaller
+ * position and 1, 3 at the larger one, and dof p0 = (point, order l1) of the element adds
+ * -2^((l-1)(l1 - l2)) H0_ic0^(l1)(x_p0) times the ancestor's value, l2 = ic0 / 2, H0 the level-0
+ * Hermite functions on [0, 1] and x_p0 the dof's point in the element's [0, 1] coordinates. */
+int amdg_oracle_herm_surplus(int dim, int N, int64_t E, const int32_t* level, const int32_t* suppt, const double* fp,
+                             double* out) {
+    ehash h;
+    if (ehash_build(&h, dim, N, E, level, suppt)) return -2;
+    const int P = ipow(4, dim);
+    double* cur = (double*)malloc((size_t)E * P * sizeof(double));
+    double* nxt = (double*)malloc((size_t)E * P * sizeof(double));
+    if (!cur || !nxt) return -2;
+    memcpy(cur, fp, (size_t)E * P * sizeof(double));
+    for (int d = 0; d < dim; ++d) {
+        int stride = 1;
+        for (int s = d + 1; s < dim; ++s) stride *= 4;
+#pragma omp parallel for schedule(dynamic, 8)
+        for (int64_t e = 0; e < E; ++e) {
+            const int l = level[e * dim + d], j = suppt[e * dim + d];
+            if (l == 0) {
+                memcpy(nxt + e * P, cur + e * P, P * sizeof(double));
+                continue;
+            }
+            const double xl = support_lo(l, j), xr = support_hi(l, j);
+            int anc_o[4], anc_q[4], ic = 0;
+            double anc_x[4];
+            for (int o = 0; o < (1 << l) && ic < 4; ++o) {
+                const elem1d ea = elem_of_order(o);
+                if (ea.n >= l) break;
+                for (int q = 0; q < 4; ++q) {
+                    const double pos = amdg_oracle_herm_point(ea.n, ea.j, q);
+                    if (pos > xl && pos < xr && ic < 4) {
+                        anc_o[ic] = o;
+                        anc_q[ic] = q;
+                        anc_x[ic] = pos;
+                        ++ic;
+                    }
+                }
+            }
+            if (ic != 4) continue;
+            double pl = anc_x[0];
+            for (int a = 1; a < 4; ++a) pl = anc_x[a] < pl ? anc_x[a] : pl;
+            int ic0[4], nl = 0, nr = 1;
+            for (int a = 0; a < 4; ++a) {
+                if (fabs(anc_x[a] - pl) < 1.0e-14) { ic0[a] = nl; nl += 2; }
+                else { ic0[a] = nr; nr += 2; }
+            }
+            int64_t anc_e[4];
+            int missing = 0;
+            for (int a = 0; a < 4 && !missing; ++a) {
+                int o[16];
+                for (int s = 0; s < dim; ++s) o[s] = order_of_elem(level[e * dim + s], suppt[e * dim + s]);
+                o[d] = anc_o[a];
+                anc_e[a] = ehash_find(&h, pack_key(o, dim, N));
+                missing |= anc_e[a] < 0;
+            }
+            if (missing) continue;
+            double wt[4][4];
+            for (int p0 = 0; p0 < 4; ++p0) {
+                const int l1 = p0 / 2;
+                const double xt = ((p0 % 2 == 0 ? (0.0 - ROUND_OFF) : (0.0 + ROUND_OFF)) + 1.0) / 2.0;
+                for (int a = 0; a < 4; ++a) {
+                    const int l2 = ic0[a] / 2;
+                    wt[p0][a] = -1.0 * pow(2.0, (l - 1) * (l1 - l2)) * herm_mother(xt, 0, ic0[a], l1);
+                }
+            }
+            for (int p = 0; p < P; ++p) {
+                const int pd = (p / stride) % 4, base = p - pd * stride;
+                double c = cur[e * P + p];
+                for (int a = 0; a < 4; ++a) c += wt[pd][a] * cur[anc_e[a] * P + base + anc_q[a] * stride];
+                nxt[e * P + p] = c;
+            }
+        }
+        double* t = cur; cur = nxt; nxt = t;
+    }
+    memcpy(out, cur, (size_t)E * P * sizeof(double));
+    free(cur); free(nxt);
+    ehash_free(&h);
+    return 0;
+}
+
+/* Burgers right-hand side from the Hermite coefficients of the flux (E x 4^dim, the same flux
+ * in every dimension) by the fast transforms, in the reference's order:
+ * HyperbolicSameFluxHermRHS::rhs_vol_scalar (u_vx along d, u_v elsewhere, every d), then
+ * rhs_flx_intp_scalar (1/2 (ulft + urgt)_vjp along d on the flux sets, every d)
+ * (FastMultiplyLU.cpp:970-1016), then the LxF penalty -alpha/2 ujp_vjp along every d (the
+ * driver's assembled HyperbolicAlpt::assemble_matrix_flx_scalar(d, -1, alpha/2) and
+ * (d, 1, -alpha/2), BilinearForm.cpp:759-769) */
+int amdg_oracle_burgers_herm_rhs_fast(int dim, int N, int k, int64_t E, const int32_t* level, const int32_t* suppt,
+                                      const double* fucoe, const double* u, double alpha, double* rhs) {
+    const int np = k + 1, n1 = 1 << N, nr = n1 * 4, nc = n1 * np;
+    fast_ctx c;
+    if (fast_ctx_init(&c, dim, N, E, level, suppt)) return -2;
+    double* Hv = (double*)malloc((size_t)nr * nc * sizeof(double));
+    double* Hvx = (double*)malloc((size_t)nr * nc * sizeof(double));
+    double* Hf = (double*)malloc((size_t)nr * nc * sizeof(double));
+    double* ul = (double*)malloc((size_t)nc * nc * sizeof(double));
+    double* ur = (double*)malloc((size_t)nc * nc * sizeof(double));
+    if (!Hv || !Hvx || !Hf || !ul || !ur) return -2;
+    amdg_oracle_oper1d_herm(N, k, Hv, Hvx, Hf);
+    amdg_oracle_oper1d(N, k, NULL, NULL, ul, ur);
+    for (size_t i = 0; i < (size_t)nc * nc; ++i) ur[i] = ur[i] - ul[i]; /* ujp_vjp */
+    memset(rhs, 0, (size_t)E * ipow(np, dim) * sizeof(double));
+    int rc = 0;
+    for (int term = 0; term < 2 && !rc; ++term)
+        for (int d = 0; d < dim && !rc; ++d) {
+            const double* M[16];
+            int flx[16];
+            for (int s = 0; s < dim; ++s) {
+                M[s] = (s == d) ? (term == 0 ? Hvx : Hf) : Hv;
+                flx[s] = (term == 1 && s == d);
+            }
+            rc = fast_partial_sums(&c, fucoe, 4, np, M, flx, term == 0 ? 1.0 : 0.5, rhs);
+        }
+    for (int d = 0; d < dim && !rc; ++d) {
+        int from[16];
+        for (int s = 0; s < dim; ++s) from[s] = np;
+        fast_transform_1d(&c, u, from, rhs, from, d, ur, nc, 1, 1, -alpha / 2.0, 1);
+    }
+    free(Hv); free(Hvx); free(Hf); free(ul); free(ur);
+    fast_ctx_free(&c);
+    return rc;
 }

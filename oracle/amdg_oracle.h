@@ -129,6 +129,26 @@ int amdg_oracle_wave_rhs_fast(int dim, int N, int k, int64_t E, const int32_t* l
 int amdg_oracle_wave_penalty(int dim, int N, int k, int64_t E, const int32_t* level, const int32_t* suppt,
                              const double* u, double sigma, double* rhs);
 
+/* ---- cubic Hermite interpolation of the flux (2D Burgers, 02_hyperbolic_05_burgers_adapt.cpp) ---- */
+/* dof p of a 1D Hermite element: point p % 2, derivative order p / 2 */
+double amdg_oracle_herm_val(int level, int suppt, int p, int deriv, double x, int sgn);
+double amdg_oracle_herm_point(int level, int suppt, int p);
+/* Hermite (2^N*4 rows) x Alpert (2^N*(k+1) cols): u_v, u_vx, ulft_vjp + urgt_vjp (any may be NULL) */
+int amdg_oracle_oper1d_herm(int N, int k, double* u_v, double* u_vx, double* uave2_vjp);
+/* u_h and its derivatives at the Hermite points, E x 4^dim: direct sums and fast transforms */
+int amdg_oracle_herm_point_values(int dim, int N, int k, int64_t E, const int32_t* level, const int32_t* suppt,
+                                  const double* u, double* up);
+int amdg_oracle_herm_point_values_fast(int dim, int N, int k, int64_t E, const int32_t* level, const int32_t* suppt,
+                                       const double* u, double* up);
+/* f = u^2/2 and its derivatives at the 2D Hermite points from up (E x 16) */
+int amdg_oracle_herm_flux_burgers2d(int64_t E, const double* up, double* fp);
+/* hierarchical Hermite surplus of point data fp (E x 4^dim) */
+int amdg_oracle_herm_surplus(int dim, int N, int64_t E, const int32_t* level, const int32_t* suppt, const double* fp,
+                             double* out);
+/* Burgers right-hand side from the flux's Hermite coefficients (fast transforms) plus the LxF penalty */
+int amdg_oracle_burgers_herm_rhs_fast(int dim, int N, int k, int64_t E, const int32_t* level, const int32_t* suppt,
+                                      const double* fucoe, const double* u, double alpha, double* rhs);
+
 #ifdef __cplusplus
 }
 #endif

@@ -82,6 +82,17 @@ def lib():
         L.amdg_oracle_wave_penalty.argtypes = [C.c_int, C.c_int, C.c_int, C.c_int64, i32p, i32p, f64p, C.c_double, f64p]
         L.amdg_oracle_wave_coef.restype = C.c_double
         L.amdg_oracle_wave_coef.argtypes = [C.c_int, f64p, C.c_double]
+        L.amdg_oracle_herm_val.restype = C.c_double
+        L.amdg_oracle_herm_val.argtypes = [C.c_int, C.c_int, C.c_int, C.c_int, C.c_double, C.c_int]
+        L.amdg_oracle_herm_point.restype = C.c_double
+        L.amdg_oracle_herm_point.argtypes = [C.c_int, C.c_int, C.c_int]
+        L.amdg_oracle_oper1d_herm.argtypes = [C.c_int, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p]
+        for fn in ("amdg_oracle_herm_point_values", "amdg_oracle_herm_point_values_fast"):
+            getattr(L, fn).argtypes = [C.c_int, C.c_int, C.c_int, C.c_int64, i32p, i32p, f64p, f64p]
+        L.amdg_oracle_herm_flux_burgers2d.argtypes = [C.c_int64, f64p, f64p]
+        L.amdg_oracle_herm_surplus.argtypes = [C.c_int, C.c_int, C.c_int64, i32p, i32p, f64p, f64p]
+        L.amdg_oracle_burgers_herm_rhs_fast.argtypes = [C.c_int, C.c_int, C.c_int, C.c_int64, i32p, i32p, f64p, f64p,
+                                                        C.c_double, f64p]
         _lib = L
     return _lib
 
@@ -733,3 +744,102 @@ def mlp_loss_grad(params, dims, x, labels):
 
 def mlp_loss(params, dims, x, labels):
     return mlp_loss_grad(params, dims, x, labels)[0]
+
+
+# ---------------------------------------------------------------------------
+# Cubic Hermite interpolation of the flux (2D Burgers driver
+# example/02_hyperbolic_05_burgers_adapt.cpp): HermInterpolation::nonlinear_Herm_2D_fast
+# (Interplation.cpp:4609-4621) + HyperbolicSameFluxHermRHS (FastMultiplyLU.cpp:970-1016) + the
+# assembled LxF matrix
+# ---------------------------------------------------------------------------
+
+def oper1d_herm(N, k):
+    """Hermite x Alpert 1D matrices (u_v, u_vx, ulft_vjp + urgt_vjp), (2^N 4) x (2^N (k+1))."""
+    shape = ((1 << N) * 4, (1 << N) * (k + 1))
+    mats = [np.zeros(shape) for _ in range(3)]
+    _check(lib().amdg_oracle_oper1d_herm(N, k, *[m.ctypes.data for m in mats]))
+    return mats
+
+
+def herm_points_1d(N):
+    """Hermite dof point coordinates of every 1D element order (2^N x 4)."""
+    out = np.zeros((1 << N, 4))
+    for o in range(1 << N):
+        lev, sp = _elem_of_order(o)
+        for p in range(4):
+            out[o, p] = lib().amdg_oracle_herm_point(lev, sp, p)
+    return out
+
+
+def herm_point_values(dim, N, k, level, suppt, u, direct=False):
+    level = np.ascontiguousarray(level, np.int32)
+    suppt = np.ascontiguousarray(suppt, np.int32)
+    up = np.zeros((level.shape[0], 4 ** dim))
+    fn = lib().amdg_oracle_herm_point_values if direct else lib().amdg_oracle_herm_point_values_fast
+    _check(fn(dim, N, k, level.shape[0], level, suppt, np.ascontiguousarray(u), up))
+    return up
+
+
+def herm_flux_burgers2d(up):
+    fp = np.zeros_like(up)
+    _check(lib().amdg_oracle_herm_flux_burgers2d(up.shape[0], np.ascontiguousarray(up), fp))
+    return fp
+
+
+def herm_surplus(dim, N, level, suppt, fp):
+    level = np.ascontiguousarray(level, np.int32)
+    suppt = np.ascontiguousarray(suppt, np.int32)
+    out = np.zeros_like(fp)
+    _check(lib().amdg_oracle_herm_surplus(dim, N, level.shape[0], level, suppt, np.ascontiguousarray(fp), out))
+    return out
+
+
+def burgers_herm_rhs(N, k, level, suppt, u, alpha, direct=False):
+    """2D Burgers right-hand side with the Hermite-interpolated flux: point values and slopes ->
+    f, f' u_x, f' u_y, f'' u_x u_y + f' u_xy -> Hermite surplus -> volume, interface and LxF
+    penalty terms.  Returns (rhs, up, fu)."""
+    level = np.ascontiguousarray(level, np.int32)
+    suppt = np.ascontiguousarray(suppt, np.int32)
+    up = herm_point_values(2, N, k, level, suppt, u, direct)
+    fu = herm_surplus(2, N, level, suppt, herm_flux_burgers2d(up))
+    rhs = np.zeros_like(u)
+    _check(lib().amdg_oracle_burgers_herm_rhs_fast(2, N, k, level.shape[0], level, suppt, fu,
+                                                   np.ascontiguousarray(u), float(alpha), rhs))
+    return rhs, up, fu
+
+
+def burgers_herm_rk3(N, k, level, suppt, u, alpha, dt, steps):
+    un = np.array(u, np.float64, copy=True)
+    for _ in range(steps):
+        cur = un.copy()
+        for stage in range(3):
+            rhs = burgers_herm_rhs(N, k, level, suppt, cur, alpha)[0]
+            if stage == 0:
+                cur = un + dt * rhs
+            elif stage == 1:
+                cur = 3. / 4. * un + 1. / 4. * (cur + dt * rhs)
+            else:
+                cur = 1. / 3. * un + 2. / 3. * (cur + dt * rhs)
+        un = cur
+    return un
+
+
+def burgers_herm_adaptive_run(n_init, nmax, eps, eta, alpha, cfl, steps, k=2):
+    """The adaptive loop of 02_hyperbolic_05_burgers_adapt.cpp (no artificial viscosity):
+    u0 = sin(2 pi (x+y)), dt = cfl / sum_d 2^maxlevel_d, predictor, refine, SSP-RK3, coarsen."""
+    keys, u = init_adaptive_separable(2, n_init, nmax, k, sin_sum_terms(2), eps)
+    history = [(list(keys), u.copy(), None)]
+    for _ in range(steps):
+        lv, sp = keys_to_arrays(keys, 2)
+        dt = cfl / sum(2.0 ** int(m) for m in lv.max(axis=0))
+        pred = u + dt * burgers_herm_rhs(nmax, k, lv, sp, u, alpha)[0]
+        new_keys = refine_keys(keys, element_norms(pred), eps, nmax)
+        u = remap(keys, u, new_keys)
+        keys = new_keys
+        lv, sp = keys_to_arrays(keys, 2)
+        u = burgers_herm_rk3(nmax, k, lv, sp, u, alpha, dt, 1)
+        new_keys = coarsen_keys(keys, element_norms(u), eta)
+        u = remap(keys, u, new_keys)
+        keys = new_keys
+        history.append((list(keys), u.copy(), dt))
+    return history

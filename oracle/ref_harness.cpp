@@ -27,6 +27,9 @@
 //   ref_harness burgers_herm <N> <alpha> <steps> <dt>
 //     the 2D version with the flux interpolated by cubic Hermite interpolation
 //     (HermInterpolation::nonlinear_Herm_2D_fast, HyperbolicSameFluxHermRHS), see run_burgers_herm.
+//   ref_harness burgers_herm_adapt <N_init> <NMAX> <eps> <eta> <alpha> <cfl> <steps> [time [t_end]]
+//     the 2D adaptive Burgers loop of example/02_hyperbolic_05_burgers_adapt.cpp as that driver
+//     runs it (Hermite flux interpolation, assembled LxF matrix), see run_burgers_herm_adapt.
 //   ref_harness burgers_adapt <dim> <N_init> <NMAX> <eps> <eta> <alpha> <cfl> <umax> <steps>
 //     adaptive version of the above, following the time loop of
 //     example/02_hyperbolic_05_burgers_adapt.cpp:223-476 with the Lagrange
@@ -467,6 +470,122 @@ int run_burgers_herm(int argc, char** argv) {
     return 0;
 }
 
+// The time loop of example/02_hyperbolic_05_burgers_adapt.cpp:223-476 as that driver runs it
+// without artificial viscosity: 2D, u0 = sin(2 pi (x+y)) by init_separable_scalar_sum, cubic
+// Hermite interpolation of the flux (HermInterpolation::nonlinear_Herm_2D_fast, built once before
+// the loop, as the driver does), HyperbolicSameFluxHermRHS volume and interface terms, the LxF
+// penalty as the assembled HyperbolicAlpt matrix (assemble_matrix_flx_scalar(d, -1, alpha/2) and
+// (d, 1, -alpha/2)) added by add_rhs_matrix, dt = cfl / sum_d 2^maxlevel_d (wave speed 1),
+// predictor, refine, SSP-RK3, coarsen.  Dumps u after init and after every step; with "time" the
+// step wall times instead (as burgers_adapt).
+int run_burgers_herm_adapt(int argc, char** argv) {
+    if (argc < 9) { std::fprintf(stderr, "burgers_herm_adapt: bad args\n"); return 2; }
+    const int dim = 2;
+    const int N_init = std::atoi(argv[2]);
+    const int NMAX = std::atoi(argv[3]);
+    const double eps = std::atof(argv[4]);
+    const double eta = std::atof(argv[5]);
+    const double alpha = std::atof(argv[6]);
+    const double cfl = std::atof(argv[7]);
+    const int steps = std::atoi(argv[8]);
+    const bool timing = argc > 9 && std::string(argv[9]) == "time";
+    const double t_end = argc > 10 ? std::atof(argv[10]) : 0.0;
+    const int k = 2;
+    set_statics(dim, k);
+    Hash hash;
+    LagrBasis::set_interp_msh01();
+    HermBasis::set_interp_msh01();
+    AllBasis<AlptBasis> all_bas_alpt(NMAX);
+    AllBasis<LagrBasis> all_bas_lagr(NMAX);
+    AllBasis<HermBasis> all_bas_herm(NMAX);
+    OperatorMatrix1D<AlptBasis, AlptBasis> oper_alpt(all_bas_alpt, all_bas_alpt, "period");
+    OperatorMatrix1D<HermBasis, AlptBasis> oper_herm(all_bas_herm, all_bas_alpt, "period");
+    DGAdapt dg(true, N_init, NMAX, all_bas_alpt, all_bas_lagr, all_bas_herm, hash, eps, eta, true, true);
+    const double PI = Const::PI;
+    std::vector<std::function<double(double, int)>> funcs;
+    funcs.push_back([=](double x, int d) { return d == 0 ? std::sin(2. * PI * x) : std::cos(2. * PI * x); });
+    funcs.push_back([=](double x, int d) { return d == 0 ? std::cos(2. * PI * x) : std::sin(2. * PI * x); });
+    dg.init_separable_scalar_sum(funcs);
+    std::printf("META dim=%d N=%d k=%d sparse=1 elements=%zu dof=%d\n", dim, NMAX, k, dg.dg.size(), dg.get_dof());
+    if (!timing) dump_elements("u_init", dg, 0);
+    auto flux = [](std::vector<double> u, int, int) -> double { return FluxFunction::burgers_flux_scalar(u[0]); };
+    auto flux_d1 = [](std::vector<double> u, int, int, int) -> double {
+        return FluxFunction::burgers_flux_1st_derivative_scalar(u[0]);
+    };
+    auto flux_d2 = [](std::vector<double> u, int, int, int, int) -> double {
+        return FluxFunction::burgers_flux_2nd_derivative_scalar(u[0]);
+    };
+    HyperbolicSameFluxHermRHS rhs_herm(dg, oper_herm);
+    HermInterpolation interp(dg);
+    std::vector<std::vector<bool>> is_intp_herm{std::vector<bool>{true, false}};
+    FastHermIntp fast_herm(dg, interp.Her_pt_Alpt_1D);
+    auto assemble = [&](HyperbolicAlpt& lin) {
+        for (int d = 0; d < dim; ++d) {
+            lin.assemble_matrix_flx_scalar(d, -1, alpha / 2);
+            lin.assemble_matrix_flx_scalar(d, 1, -alpha / 2);
+        }
+    };
+    auto herm_rhs = [&]() {
+        interp.nonlinear_Herm_2D_fast(flux, flux_d1, flux_d2, is_intp_herm, fast_herm);
+        dg.set_rhs_zero();
+        rhs_herm.rhs_vol_scalar();
+        rhs_herm.rhs_flx_intp_scalar();
+    };
+    double t = 0.0;
+    for (int step = 0; step < steps; ++step) {
+        if (t_end > 0.0 && t >= t_end) break;
+        const auto t0 = std::chrono::steady_clock::now();
+        const std::vector<int> max_mesh = dg.max_mesh_level_vec();
+        double sum_c_dx = 0.;
+        for (int d = 0; d < dim; ++d) sum_c_dx += 1.0 * std::pow(2., max_mesh[d]);
+        double dt = cfl / sum_c_dx;
+        if (t_end > 0.0) dt = std::min(dt, t_end - t);
+        {
+            dg.copy_ucoe_to_predict();
+            HyperbolicAlpt linear(dg, oper_alpt);
+            assemble(linear);
+            ForwardEuler ode(linear, dt);
+            ode.init();
+            herm_rhs();
+            ode.set_rhs_zero();
+            ode.add_rhs_to_eigenvec();
+            ode.add_rhs_matrix(linear);
+            ode.step_stage(0);
+            ode.final();
+        }
+        dg.refine();
+        const int stage_dof = dg.get_dof();
+        dg.copy_predict_to_ucoe();
+        {
+            HyperbolicAlpt linear(dg, oper_alpt);
+            assemble(linear);
+            RK3SSP ode(linear, dt);
+            ode.init();
+            for (int stage = 0; stage < ode.num_stage; ++stage) {
+                herm_rhs();
+                ode.set_rhs_zero();
+                ode.add_rhs_to_eigenvec();
+                ode.add_rhs_matrix(linear);
+                ode.step_stage(stage);
+                ode.final();
+            }
+        }
+        dg.coarsen();
+        t += dt;
+        if (timing) {
+            const double sec = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+            std::printf("TSTEP %d %.9g %d %zu\n", step, sec, stage_dof, dg.dg.size());
+            std::fflush(stdout);
+            continue;
+        }
+        std::printf("STEP %d dt=%.17g elements=%zu\n", step, dt, dg.dg.size());
+        char nm[32];
+        std::snprintf(nm, sizeof nm, "u_step%d", step);
+        dump_elements(nm, dg, 0);
+    }
+    return 0;
+}
+
 int run_burgers_adapt(int argc, char** argv) {
     if (argc < 11) { std::fprintf(stderr, "burgers_adapt: bad args\n"); return 2; }
     const int dim = std::atoi(argv[2]);
@@ -871,6 +990,7 @@ int main(int argc, char** argv) {
     if (mode == "burgers") return run_burgers(argc, argv);
     if (mode == "burgers_herm") return run_burgers_herm(argc, argv);
     if (mode == "burgers_adapt") return run_burgers_adapt(argc, argv);
+    if (mode == "burgers_herm_adapt") return run_burgers_herm_adapt(argc, argv);
     if (mode == "wave") return run_wave(argc, argv);
     if (mode == "wave_adapt") return run_wave_adapt(argc, argv);
     if (mode == "intp_init") return run_intp_init(argc, argv);

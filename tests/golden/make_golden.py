@@ -250,11 +250,63 @@ def burgers_adapt_long(manifest):
         print(name, r["meta"], "max level sum", maxlevsum)
 
 
+# (name, N, alpha, steps, dt): 2D Burgers on the full sparse grid with the flux interpolated by
+# cubic Hermite interpolation (HermInterpolation::nonlinear_Herm_2D_fast,
+# HyperbolicSameFluxHermRHS, LxF penalty), SSP-RK3; u0 = 0.5 + 0.25 sin(2 pi (x+y))
+HERM_CASES = [
+    ("burgers_herm2d_n4", 4, 1.2, 2, 0.002),
+    ("burgers_herm2d_n6", 6, 1.2, 1, 0.0005),
+]
+
+# (name, N_init, NMAX, eps, eta, alpha, cfl, steps, snapshot steps): the adaptive loop of
+# example/02_hyperbolic_05_burgers_adapt.cpp (u0 = sin(2 pi (x+y)), Hermite flux, assembled LxF
+# matrix, CFL 0.2 with wave speed 1): element sets and checksums after every step, coefficients at
+# the snapshot steps (all of them when None)
+HERM_ADAPT_CASES = [
+    ("burgers_herm_adapt2d", 3, 6, 1e-4, 1e-5, 1.2, 0.2, 6, None),
+    ("burgers_herm_adapt2d_n8_T003", 3, 8, 1e-5, 1e-6, 1.2, 0.2, 34, [0, 1, 2, 17, 34]),
+]
+
+
+def herm_cases(manifest):
+    for name, N, alpha, steps, dt in HERM_CASES:
+        r = run(["burgers_herm", N, repr(alpha), steps, repr(dt)])
+        lv, sp, u0 = split_elements(r["u0"], 2)
+        arrs = {"level": lv, "suppt": sp, "u0": u0}
+        for key in ("up0", "fu0", "rhs0", "uT"):
+            lv2, sp2, v = split_elements(r[key], 2)
+            assert (lv == lv2).all() and (sp == sp2).all()
+            arrs[key] = v
+        np.savez_compressed(os.path.join(HERE, name + ".npz"), **arrs)
+        manifest[name] = dict(kind="burgers_herm", dim=2, N=N, k=2, herm_degree=3, alpha=alpha, steps=steps, dt=dt,
+                              elements=int(r["meta"]["elements"]))
+        print(name, r["meta"])
+    for name, n0, nmax, eps, eta, alpha, cfl, steps, snaps in HERM_ADAPT_CASES:
+        res = subprocess.run([HARNESS, "burgers_herm_adapt"] + [str(a) for a in (n0, nmax, repr(eps), repr(eta),
+                                                                                  repr(alpha), repr(cfl), steps)],
+                             check=True, capture_output=True, text=True)
+        r = parse_harness(res.stdout)
+        dts = [float(ln.split("dt=")[1].split()[0]) for ln in res.stdout.splitlines() if ln.startswith("STEP")]
+        arrs, sums = {"dt": np.array(dts)}, []
+        for i, key in enumerate(["u_init"] + [f"u_step{s}" for s in range(steps)]):
+            lv, sp, u = split_elements(r[key], 2)
+            arrs[f"level_{i}"], arrs[f"suppt_{i}"] = lv.astype(np.int16), sp.astype(np.int16)
+            sums.append(checksums(lv, sp, u))
+            if snaps is None or i in snaps:
+                arrs[f"u_{i}"] = u
+        arrs["checksums"] = np.array(sums)
+        np.savez_compressed(os.path.join(HERE, name + ".npz"), **arrs)
+        manifest[name] = dict(kind="burgers_herm_adapt", dim=2, n_init=n0, nmax=nmax, eps=eps, eta=eta, alpha=alpha,
+                              cfl=cfl, steps=steps, snapshots=snaps, t_end=float(np.sum(dts)),
+                              elements=[int(len(arrs[f"level_{i}"])) for i in range(steps + 1)])
+        print(name, r["meta"], len(arrs[f"level_{steps}"]))
+
+
 def main():
     if not os.path.exists(HARNESS):
         sys.exit("build the reference first: make -C oracle ref")
     only = {"intp": intp_cases, "burgers_adapt_long": burgers_adapt_long, "linear_long": linear_long,
-            "wave_adapt_long": wave_adapt_long}
+            "wave_adapt_long": wave_adapt_long, "herm": herm_cases}
     if len(sys.argv) == 2 and sys.argv[1] in only:  # one group of cases, merged into the manifest
         path = os.path.join(HERE, "manifest.json")
         manifest = json.load(open(path))
@@ -300,6 +352,7 @@ def main():
                               cfl=cfl, umax=umax, steps=steps)
         print(name, r["meta"])
     burgers_adapt_long(manifest)
+    herm_cases(manifest)
     linear_long(manifest)
     for name, dim, N, sigma, steps, dt in WAVE_CASES:
         r = run(["wave", dim, N, repr(sigma), steps, repr(dt)])

@@ -356,3 +356,68 @@ def test_interpolated_split_error_matches_reference(name):
     assert sorted(kb) == sorted(O.arrays_to_keys(z["level_b"], z["suppt_b"]))
     err = O.l2_error_split_grids(ka, ua, kb, ub)
     assert abs(err - m["err"]) <= 1e-9 * m["err"]
+
+
+HERM = [n for n, m in manifest().items() if m["kind"] == "burgers_herm"]
+
+
+@pytest.mark.parametrize("name", HERM)
+def test_burgers_hermite_path_matches_reference(name):
+    """Cubic Hermite interpolation of the 2D Burgers flux (HermInterpolation::nonlinear_Herm_2D_fast,
+    HyperbolicSameFluxHermRHS): u_h and its slopes at the Hermite points (direct sums and fast
+    transforms), the flux's Hermite coefficients, the right-hand side and SSP-RK3 steps against the
+    reference."""
+    m = manifest()[name]
+    z = golden(name)
+    N, k = m["N"], m["k"]
+    lv, sp = O.grid(2, N)
+    perm = align(z["level"], z["suppt"], lv, sp)
+    coef = O.project_separable(N, k, 2, O.burgers_ic_terms(2))
+    u0 = O.init_separable(2, N, k, lv, sp, coef)
+    assert rel_err(u0, z["u0"][perm]) < 1e-13
+    u0 = np.ascontiguousarray(z["u0"][perm])
+    assert rel_err(O.herm_point_values(2, N, k, lv, sp, u0, direct=True), z["up0"][perm]) < 1e-13
+    rhs, up, fu = O.burgers_herm_rhs(N, k, lv, sp, u0, m["alpha"])
+    assert rel_err(up, z["up0"][perm]) < 1e-13
+    assert rel_err(fu, z["fu0"][perm]) < 1e-12
+    assert rel_err(rhs, z["rhs0"][perm]) < 5e-12
+    uT = O.burgers_herm_rk3(N, k, lv, sp, u0, m["alpha"], m["dt"], m["steps"])
+    assert rel_err(uT, z["uT"][perm]) < 1e-12
+
+
+def test_hermite_basis_interpolates_its_dofs():
+    """Each Hermite function has value (or slope) 1 at its own dof and 0 at the element's other
+    dofs; the points sit 1e-13 off the nodes (relative to the element size)."""
+    for n, j in [(0, 1), (1, 1), (2, 1), (2, 3), (3, 5)]:
+        h = 1.0 if n <= 1 else 2.0 ** (1 - n)
+        for p in range(4):
+            for q in range(4):
+                x = O.lib().amdg_oracle_herm_point(n, j, q)
+                v = O.lib().amdg_oracle_herm_val(n, j, p, q // 2, x, 0)
+                assert abs(v - (1.0 if p == q else 0.0)) < 1e-11 / h, (n, j, p, q)
+
+
+HERM_ADAPT = [n for n, m in manifest().items() if m["kind"] == "burgers_herm_adapt"]
+
+
+@pytest.mark.parametrize("name", HERM_ADAPT)
+def test_adaptive_burgers_hermite_matches_reference(name):
+    """The adaptive loop of 02_hyperbolic_05_burgers_adapt.cpp (Hermite flux): element sets
+    bit-exact and coefficients to 1e-12 after the adaptive init and every step; the long
+    fixture's first two steps only (the whole run is checked on the GPU)."""
+    from golden.make_golden import checksums
+    m = manifest()[name]
+    z = golden(name)
+    steps = m["steps"] if m["snapshots"] is None else 2
+    hist = O.burgers_herm_adaptive_run(m["n_init"], m["nmax"], m["eps"], m["eta"], m["alpha"], m["cfl"], steps)
+    for i, (keys, u, dt) in enumerate(hist):
+        ref_keys = O.arrays_to_keys(z[f"level_{i}"], z[f"suppt_{i}"])
+        assert set(ref_keys) == set(keys), f"element set differs after step {i}"
+        if dt is not None:
+            assert dt == z["dt"][i - 1]
+        lv, sp = O.keys_to_arrays(keys, 2)
+        cs, ref_cs = checksums(lv, sp, u), z["checksums"][i]
+        assert abs(cs[2] - ref_cs[2]) <= 1e-12 * ref_cs[3]
+        pos = {kk: jj for jj, kk in enumerate(ref_keys)}
+        perm = np.array([pos[kk] for kk in keys])
+        assert rel_err(u, z[f"u_{i}"][perm]) < 1e-12
