@@ -109,6 +109,7 @@ struct LagrTables {
     std::vector<int32_t> anc_point;  // [n_elem1d][p1]: its point index
     std::vector<int32_t> anc_rank;   // [n_elem1d][p1]: rank of its position among the p1
     double weight[kMaxLagrPoints * kMaxLagrPoints] = {0};  // [p0][rank]
+    bool herm = false;  // Hermite weights: scaled per element level (build_herm_tables)
 };
 // basis function `order` (1D element order * p1 + p) at x, one-sided for sgn = -1 / 1
 double lagr_eval(const LagrSpec& s, int order, double x, int sgn);
@@ -120,6 +121,17 @@ void lagr_mass_diag(const LagrSpec& S, int nmax, std::vector<double>* out);
 void build_lagr_tables(const Basis1D& alpt, int degree, LagrTables* t, bool diffusion = false);
 // anc_order/anc_point/anc_rank only (t->spec and t->p1 set from `degree`)
 void build_lagr_ancestors(const Basis1D& alpt, int degree, LagrTables* t);
+// interpolation basis (S: Lagrange; nullptr: cubic Hermite) x Alpert products lv, lvx, lflx
+void build_interp_products(const Basis1D& alpt, const LagrSpec* S, int P1, LagrTables* t);
+// Cubic Hermite interpolation (HermBasis with PMAX 3, msh_case 1): dof p of a 1D element is
+// point p % 2 and derivative order p / 2.  Basis function `order` (1D order * 4 + p), or its
+// derivative, at x (one-sided for sgn = -1 / 1), the point of dof p of 1D element o, and the
+// tables of the Hermite path (a2p: Alpert values or slopes at the Hermite points; the Hermite x
+// Alpert products; ancestors with anc_rank = the ancestor's dof number ic0 and weight[p0][ic0]
+// the level-1 weights, scaled by 2^((level - 1)(p0 / 2 - ic0 / 2)) per element level)
+double herm_eval(int order, int deriv, double x, int sgn);
+double herm_point(int o, int p);
+void build_herm_tables(const Basis1D& alpt, LagrTables* t);
 // dimension orders and L(0)/full(1)/U(2) tags of the 2^(dim-1) partial sums
 void transform_schedule(int dim, std::vector<std::vector<int>>* dim_order, std::vector<std::vector<int>>* lu);
 

@@ -596,7 +596,13 @@ amdg_status amdg_batch_adapt(amdg_batch* b, amdg_mlp* mlp, double eps, double et
     for (int i = 0; i < n; ++i) {
         const bool same = int64_t(keys[i].size()) == hg[i]->num_elements &&
                           std::all_of(carry[i].begin(), carry[i].end(), [](uint8_t c) { return c != 0; });
-        if (!same && (s = grid_set_keys(b->grids[i], std::move(keys[i]), &carry[i])) != AMDG_OK) return s;
+        if (!same && (s = grid_set_keys(b->grids[i], std::move(keys[i]), &carry[i])) != AMDG_OK) {
+            // solves before i already have their new element sets: rebuild the batch on the sets the
+            // grids now hold, so it stays usable, and report the failure
+            const std::string msg = amdg_last_error();
+            if (batch_build(b) != AMDG_OK) return s;
+            return fail(s, msg);
+        }
     }
     {
         PhaseTimer timer(b->ctx, AMDG_PHASE_TOPOLOGY);

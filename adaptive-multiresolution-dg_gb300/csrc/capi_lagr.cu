@@ -119,6 +119,10 @@ int ipow(int b, int e) {
     return p;
 }
 
+// the Burgers operators: flux u^2/2 interpolated by Lagrange (kind 0) or cubic Hermite (kind 3)
+// interpolation; both step by SSP-RK3 with the same right-hand-side terms
+bool burgers_like(const amdg_burgers_op* op) { return op->kind == 0 || op->kind == 3; }
+
 // partial sums of the schedule with the given matrix and vol/flx choice per
 // dimension, reading input `src`, appended to op->terms
 void push_psums(amdg_burgers_op* op, const int* mat, const int* flx, double coef, int src) {
@@ -179,7 +183,7 @@ void build_terms(amdg_burgers_op* op) {
         push_psums(op, mat, flx, 1.0, 0);
         return;
     }
-    if (op->kind == 0) {
+    if (burgers_like(op)) {
         for (int t = 0; t < dim; ++t) { mat[t] = kMatA2P; flx[t] = 0; }
         push_psums(op, mat, flx, 1.0, 0);
         op->n_pv_terms = int(op->terms.size());
@@ -360,13 +364,18 @@ template <typename T>
 amdg_status eval_point_values(amdg_burgers_op* op, const Mats<T>& m, const T* u, T* up, T* fp, cudaStream_t st) {
     const int np = op->grid->host.k + 1;
     const int64_t n = op->grid->host.num_elements * op->points;
+    const bool herm = op->kind == 3;  // the Hermite flux needs the slopes too: applied after the sum
     T* slots = static_cast<T*>(op->w_slots);
     const T* src[1] = {u};
     for (int c0 = 0; c0 < op->n_pv_terms; c0 += op->chunk) {
         const int cnt = std::min(op->chunk, op->n_pv_terms - c0);
         if (amdg_status r = run_terms<T>(op, m, c0, cnt, np, op->p1, src, 1, nullptr, slots, st); r != AMDG_OK) return r;
         const bool last = c0 + cnt == op->n_pv_terms;
-        AMDG_CK(launch_reduce_points<T>(slots, cnt, n, c0 == 0 ? 1 : 0, up, last ? fp : nullptr, st));
+        AMDG_CK(launch_reduce_points<T>(slots, cnt, n, c0 == 0 ? 1 : 0, up, (last && !herm) ? fp : nullptr, st));
+        op->grid->ctx->launches++;
+    }
+    if (herm && fp) {
+        AMDG_CK(launch_herm_flux_burgers2d<T>(up, fp, op->grid->host.num_elements, st));
         op->grid->ctx->launches++;
     }
     return AMDG_OK;
@@ -389,7 +398,11 @@ amdg_status eval_point_values_df(amdg_burgers_op* op, const double* u, double* u
             r != AMDG_OK)
             return r;
         const bool last = c0 + cnt == op->n_pv_terms;
-        AMDG_CK(launch_reduce_points_df(slots, cnt, n, c0 == 0 ? 1 : 0, up, last ? fp : nullptr, st));
+        AMDG_CK(launch_reduce_points_df(slots, cnt, n, c0 == 0 ? 1 : 0, up, (last && op->kind != 3) ? fp : nullptr, st));
+        op->grid->ctx->launches++;
+    }
+    if (op->kind == 3 && fp) {  // the Hermite flux from the FP64 sums of values and slopes
+        AMDG_CK(launch_herm_flux_burgers2d<double>(up, fp, op->grid->host.num_elements, st));
         op->grid->ctx->launches++;
     }
     return AMDG_OK;
@@ -413,6 +426,7 @@ amdg_status eval_surplus(amdg_burgers_op* op, const T* in, To* out, cudaStream_t
     a.anc_point = op->d_anc_point;
     a.anc_rank = op->d_anc_rank;
     for (int i = 0; i < kMaxLagrPoints * kMaxLagrPoints; ++i) a.weight[i] = op->weight[i];
+    a.herm = op->kind == 3;
     const T* cur = in;
     for (int d = 0; d < dim; ++d) {
         a.d = d;
@@ -798,14 +812,16 @@ static amdg_status lagr_create(amdg_grid* g, int kind, const double* alpha, doub
     else op->alpha.assign(dim, 0.0);
     // Lagrange degree as the examples set it: 3 for Burgers, 4 for the wave equation; the
     // interpolation init takes the caller's
-    const int degree = kind == 1 ? 4 : (kind == 2 ? lagr_degree : 3);
+    const int degree = kind == 1 ? 4 : (kind == 2 ? lagr_degree : 3);  // kind 3: cubic Hermite
     op->p1 = degree + 1;
     op->points = 1;
     for (int d = 0; d < dim; ++d) op->points *= op->p1;
     op->n1 = 1 << g->host.nmax;
     Basis1D b{g->host.k, g->host.nmax};
     LagrTables t;
-    build_lagr_tables(b, degree, &t, kind == 1);
+    if (kind == 3) build_herm_tables(b, &t);
+    else build_lagr_tables(b, degree, &t, kind == 1);
+    op->anc_order = t.anc_order;
     // the sweeps read the tables blocked by 1D order pair (the rows and columns of one pair contiguous)
     const int np = g->host.k + 1;
     if (!reblock_table(&t.a2p, op->n1, np, op->p1) || !reblock_table(&t.lv, op->n1, op->p1, np) ||
@@ -840,6 +856,13 @@ amdg_status amdg_burgers_create(amdg_grid* g, const double* alpha, amdg_burgers_
     AMDG_REQUIRE(g && alpha && out, AMDG_ERR_ARG, "null argument");
     for (int d = 0; d < g->host.dim; ++d) AMDG_REQUIRE(std::isfinite(alpha[d]), AMDG_ERR_ARG, "non-finite alpha");
     return lagr_create(g, 0, alpha, 0.0, out);
+}
+
+amdg_status amdg_burgers_create_herm(amdg_grid* g, const double* alpha, amdg_burgers_op** out) {
+    AMDG_REQUIRE(g && alpha && out, AMDG_ERR_ARG, "null argument");
+    AMDG_REQUIRE(g->host.dim == 2, AMDG_ERR_ARG, "the Hermite flux interpolation is two-dimensional (nonlinear_Herm_2D_fast)");
+    for (int d = 0; d < g->host.dim; ++d) AMDG_REQUIRE(std::isfinite(alpha[d]), AMDG_ERR_ARG, "non-finite alpha");
+    return lagr_create(g, 3, alpha, 0.0, out);
 }
 
 amdg_status amdg_burgers_destroy(amdg_burgers_op* op) {
@@ -943,7 +966,7 @@ amdg_status amdg_burgers_set_sweep_variant(amdg_burgers_op* op, int variant) {
 }
 
 amdg_status amdg_lagr_interpolate(amdg_burgers_op* op, amdg_precision prec) {
-    AMDG_REQUIRE(op && op->kind == 0, AMDG_ERR_ARG, "a Burgers operator is required");
+    AMDG_REQUIRE(op && burgers_like(op), AMDG_ERR_ARG, "a Burgers operator is required");
     AMDG_REQUIRE(prec == AMDG_PREC_FP64 || prec == AMDG_PREC_MIXED, AMDG_ERR_ARG, "bad precision");
     AMDG_CK(cudaSetDevice(op->device));
     if (amdg_status rs = burgers_sync(op); rs != AMDG_OK) return rs;
@@ -965,7 +988,7 @@ amdg_status amdg_lagr_interpolate(amdg_burgers_op* op, amdg_precision prec) {
 }
 
 amdg_status amdg_lagr_rhs_add(amdg_burgers_op* op, int group, const double* alpha, amdg_precision prec) {
-    AMDG_REQUIRE(op && op->kind == 0, AMDG_ERR_ARG, "a Burgers operator is required");
+    AMDG_REQUIRE(op && burgers_like(op), AMDG_ERR_ARG, "a Burgers operator is required");
     AMDG_REQUIRE(group >= AMDG_LAGR_RHS_VOL && group <= AMDG_LAGR_RHS_PENALTY, AMDG_ERR_ARG, "unknown term group");
     AMDG_REQUIRE(prec == AMDG_PREC_FP64 || prec == AMDG_PREC_MIXED, AMDG_ERR_ARG, "bad precision");
     AMDG_CK(cudaSetDevice(op->device));
@@ -1133,7 +1156,7 @@ static amdg_status ensure_velocity(amdg_grid* g);
 
 // one time step of the operator's scheme: SSP-RK3 (Burgers) or RK4ODE2nd (wave)
 static amdg_status one_step(amdg_burgers_op* op, double dt, amdg_precision prec) {
-    if (op->kind == 0) return amdg_burgers_rk3_steps(op, dt, 1, prec);
+    if (burgers_like(op)) return amdg_burgers_rk3_steps(op, dt, 1, prec);
     if (amdg_status s = burgers_sync(op); s != AMDG_OK) return s;
     return wave_rk4(op, dt, 1, prec);
 }
@@ -1158,7 +1181,7 @@ static amdg_status adaptive_step_any(amdg_burgers_op* op, double cfl, double wav
         if ((s = grid_ensure_host(g)) != AMDG_OK) return s;
         old_keys = g->host.key;
     }
-    if (op->kind == 0) {
+    if (burgers_like(op)) {
         op->rhs_evaluations++;
         // forward Euler into the prediction buffer (ForwardEuler::step_stage)
         const StageOut so{1, stage_coef(0, dt), g->d_u, g->d_u, op->d_pred};
@@ -1249,7 +1272,7 @@ static amdg_status horizon_steps(amdg_burgers_op* op, double dt, amdg_precision 
     }
     amdg_status s;
     if (n > 1) {
-        if (op->kind == 0) s = amdg_burgers_rk3_steps(op, dt, n - 1, prec);  // syncs the operator itself
+        if (burgers_like(op)) s = amdg_burgers_rk3_steps(op, dt, n - 1, prec);  // syncs the operator itself
         else if ((s = burgers_sync(op)) == AMDG_OK) s = wave_rk4(op, dt, n - 1, prec);
         if (s != AMDG_OK) return s;
     }

@@ -213,6 +213,16 @@ struct EvalTables {
     ~EvalTables() {
         for (void* p : bufs) cudaFree(p);
     }
+    // an uninitialised device array of n elements
+    template <class T>
+    amdg_status alloc(size_t n, T** out) {
+        void* p = nullptr;
+        cudaError_t e = amdg::device_malloc(&p, std::max<size_t>(n, 1) * sizeof(T));
+        if (e != cudaSuccess) return fail(AMDG_ERR_NOMEM, std::string("cudaMalloc: ") + cudaGetErrorString(e));
+        bufs.push_back(p);
+        *out = static_cast<T*>(p);
+        return AMDG_OK;
+    }
     template <class T>
     amdg_status put(const std::vector<T>& h, const T** out) {
         void* p = nullptr;
@@ -436,12 +446,11 @@ amdg_status amdg_grid_l2_error_split_grid(const amdg_grid* g, const amdg_grid* e
     const int64_t E = h.num_elements, Ee = he.num_elements, n = int64_t(ia.size());
     EvalTables T;
     const int32_t *d_ia = nullptr, *d_ib = nullptr;
-    const double* d_dot0 = nullptr;
-    std::vector<double> dots(size_t(E + Ee + n), 0.0);
+    double* d_dot = nullptr;  // every entry written by the block products below
+    std::vector<double> dots(size_t(E + Ee + n));
     amdg_status s;
-    if ((s = T.put(ia, &d_ia)) != AMDG_OK || (s = T.put(ib, &d_ib)) != AMDG_OK || (s = T.put(dots, &d_dot0)) != AMDG_OK)
+    if ((s = T.put(ia, &d_ia)) != AMDG_OK || (s = T.put(ib, &d_ib)) != AMDG_OK || (s = T.alloc(dots.size(), &d_dot)) != AMDG_OK)
         return s;
-    double* d_dot = const_cast<double*>(d_dot0);
     const int B = g->block;
     if (Ee > 0) block_dot_kernel<<<eval_blocks(Ee * 32), kEvalThreads, 0, st>>>(exact->d_u, exact->d_u, nullptr, nullptr, Ee, B, d_dot);
     if (E > 0) block_dot_kernel<<<eval_blocks(E * 32), kEvalThreads, 0, st>>>(g->d_u, g->d_u, nullptr, nullptr, E, B, d_dot + Ee);

@@ -598,11 +598,14 @@ __global__ void __launch_bounds__(256) surplus_pass_kernel(SurplusArgs<Ti> a, co
         const int pd = (p / a.stride) % P1;
         const int base = p - pd * a.stride;
         const int32_t* anc = a.anc + (e * a.dim + a.d) * P1;
+        // Hermite: the level-1 weights scaled to the element's level (a power of two, exact)
+        const int lscale = a.herm ? (31 - __clz(od)) : 0;
         for (int ic = 0; ic < P1; ++ic) {
             const int s = __ldg(anc + ic);
             const int q = __ldg(a.anc_point + od * P1 + ic);
             const int r = __ldg(a.anc_rank + od * P1 + ic);
-            c = fma(Ti(a.weight[pd * P1 + r]), in[int64_t(s) * a.points + base + q * a.stride], c);
+            const double w = a.herm ? ldexp(a.weight[pd * P1 + r], lscale * (pd / 2 - r / 2)) : a.weight[pd * P1 + r];
+            c = fma(Ti(w), in[int64_t(s) * a.points + base + q * a.stride], c);
         }
     }
     out[gid] = To(c);
@@ -632,6 +635,41 @@ cudaError_t launch_convert(const Ti* in, To* out, int64_t n, cudaStream_t st) {
     convert_kernel<Ti, To><<<unsigned((n + 255) / 256), 256, 0, st>>>(in, out, n);
     return cudaGetLastError();
 }
+
+__device__ __forceinline__ double mul_rn(double a, double b) { return __dmul_rn(a, b); }
+__device__ __forceinline__ float mul_rn(float a, float b) { return __fmul_rn(a, b); }
+__device__ __forceinline__ double add_rn(double a, double b) { return __dadd_rn(a, b); }
+__device__ __forceinline__ float add_rn(float a, float b) { return __fadd_rn(a, b); }
+
+// one thread per (element, point pair (q0, q1)): the four dofs of the pair, in the operation
+// order of HermInterpolation::eval_fp_Her_2D (Interplation.cpp:2045-2300) with f' = u, f'' = 1
+template <typename T>
+__global__ void herm_flux_burgers2d_kernel(const T* __restrict__ up, T* __restrict__ fp, int64_t n) {
+    const int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const int64_t e = i >> 2;
+    const int q0 = int(i & 3) >> 1, q1 = int(i & 1);
+    const T* v = up + e * 16;
+    T* f = fp + e * 16;
+    // entry (p0, p1) at p0 * 4 + p1; p = q (value) or q + 2 (slope)
+    const int i00 = q0 * 4 + q1, i10 = (q0 + 2) * 4 + q1, i01 = q0 * 4 + q1 + 2, i11 = (q0 + 2) * 4 + q1 + 2;
+    const T u = v[i00], ux = v[i10], uy = v[i01], uxy = v[i11];
+    f[i00] = u * u * T(0.5);
+    f[i10] = u * ux;
+    f[i01] = u * uy;
+    f[i11] = add_rn(mul_rn(ux, uy), mul_rn(u, uxy));  // both products rounded, as the reference
+}
+
+template <typename T>
+cudaError_t launch_herm_flux_burgers2d(const T* up, T* fp, int64_t num_elements, cudaStream_t st) {
+    const int64_t n = num_elements * 4;
+    if (n == 0) return cudaSuccess;
+    herm_flux_burgers2d_kernel<T><<<unsigned((n + 255) / 256), 256, 0, st>>>(up, fp, n);
+    return cudaGetLastError();
+}
+
+template cudaError_t launch_herm_flux_burgers2d<double>(const double*, double*, int64_t, cudaStream_t);
+template cudaError_t launch_herm_flux_burgers2d<float>(const float*, float*, int64_t, cudaStream_t);
 
 template cudaError_t launch_convert<double, float>(const double*, float*, int64_t, cudaStream_t);
 template cudaError_t launch_convert<float, double>(const float*, double*, int64_t, cudaStream_t);

@@ -89,6 +89,7 @@ struct SurplusArgs {
     const int32_t* anc_point;    // [1D order][p1]
     const int32_t* anc_rank;     // [1D order][p1]
     double weight[kMaxLagrPoints * kMaxLagrPoints];  // [p0][rank]
+    int herm;  // Hermite surplus: weight[p0][r] scaled by 2^((level_d - 1)(p0 / 2 - r / 2))
 };
 // one surplus pass, input and output types may differ (the last pass of the
 // mixed mode writes the FP32 coefficients of the back transforms)
@@ -96,5 +97,9 @@ template <typename Ti, typename To>
 cudaError_t launch_surplus_pass(const SurplusArgs<Ti>& a, const Ti* in, To* out, cudaStream_t st);
 template <typename Ti, typename To>
 cudaError_t launch_convert(const Ti* in, To* out, int64_t n, cudaStream_t st);
+// The Burgers flux f = u^2/2 and its derivatives at the 2D cubic Hermite points (16 per
+// element) from u_h and its derivatives there: f, f' u_x, f' u_y, f'' u_x u_y + f' u_xy
+template <typename T>
+cudaError_t launch_herm_flux_burgers2d(const T* up, T* fp, int64_t num_elements, cudaStream_t st);
 
 }  // namespace amdg

@@ -192,6 +192,60 @@ void lagr_mass_diag(const LagrSpec& S, int nmax, std::vector<double>* out) {
     }
 }
 
+// Interpolation basis (rows, 1D order * p1 + p) x Alpert basis (columns) products of
+// OperatorMatrix1D<Interp, AlptBasis> (OperatorMatrix1D.h:166-199): u_v and u_vx by 10-point
+// Gauss on the two halves of the finer support, ulft_vjp + urgt_vjp from the one-sided values at
+// the Alpert function's discontinuities.  S selects the Lagrange basis; nullptr the cubic Hermite
+// basis (herm_eval).
+void build_interp_products(const Basis1D& alpt, const LagrSpec* S, int P1, LagrTables* t) {
+    static const GL10 g;
+    const int n1 = alpt.num_elem(), na = alpt.num_basis(), np = alpt.k + 1, nl = n1 * P1;
+    auto ieval = [S](int r, double x, int sgn) { return S ? lagr_eval(*S, r, x, sgn) : herm_eval(r, 0, x, sgn); };
+    t->lv.assign(size_t(nl) * na, 0.0);
+    t->lvx.assign(size_t(nl) * na, 0.0);
+    t->lflx.assign(size_t(nl) * na, 0.0);
+#pragma omp parallel for schedule(dynamic)
+    for (int r = 0; r < nl; ++r) {
+        const int ou = r / P1;
+        const int lu = level_of_order(ou);
+        const double ua = supp_lo(ou), ub = supp_hi(ou);
+        for (int c = 0; c < na; ++c) {
+            const int ov = c / np;
+            const double va = supp_lo(ov), vb = supp_hi(ov);
+            const size_t idx = size_t(r) * na + c;
+            if (!(va >= ub || vb <= ua)) {
+                double xl = ua, xr = ub;
+                if (lu <= level_of_order(ov)) { xl = va; xr = vb; }
+                const double xm = 0.5 * (xl + xr);
+                auto fv = [&](double x) { return ieval(r, x, 0) * alpt.eval(c, 0, x, 0); };
+                auto fvx = [&](double x) { return ieval(r, x, 0) * alpt.eval(c, 1, x, 0); };
+                t->lv[idx] = g.integrate(fv, xl, xm) + g.integrate(fv, xm, xr);
+                t->lvx[idx] = g.integrate(fvx, xl, xm) + g.integrate(fvx, xm, xr);
+            }
+            const double pts[3] = {va, 0.5 * (va + vb), vb};
+            const int npts = level_of_order(ov) <= 1 ? 2 : 3;
+            auto edge = [&](int su, int sv) {
+                double s = 0.0;
+                for (int i = 0; i < npts; ++i) {
+                    const double x = pts[i];
+                    double fu = ieval(r, x, su), fw = alpt.eval(c, 0, x, sv);
+                    if (std::fabs(x) < kRoundOff) {
+                        if (su == -1) fu = ieval(r, 1.0, su);
+                        if (sv == -1) fw = alpt.eval(c, 0, 1.0, sv);
+                    } else if (std::fabs(x - 1.0) < kRoundOff) {
+                        if (su == 1) fu = ieval(r, 0.0, su);
+                        if (sv == 1) fw = alpt.eval(c, 0, 0.0, sv);
+                    }
+                    s += fu * fw;
+                }
+                return s;
+            };
+            // (ulft_vjp + urgt_vjp), HyperbolicLagrRHS::rhs_flx_intp_scalar (FastMultiplyLU.cpp:1166)
+            t->lflx[idx] = (edge(-1, 1) - edge(-1, -1)) + (edge(1, 1) - edge(1, -1));
+        }
+    }
+}
+
 void build_lagr_tables(const Basis1D& alpt, int degree, LagrTables* t, bool diffusion) {
     static const GL10 g;
     const LagrSpec& S = *lagr_spec(degree);
@@ -211,50 +265,7 @@ void build_lagr_tables(const Basis1D& alpt, int degree, LagrTables* t, bool diff
             t->a2p[size_t(r) * nl + c] = alpt.eval(r, 0, x, 0);
         }
     }
-    // Lagrange (row) x Alpert (col) products
-    t->lv.assign(size_t(nl) * na, 0.0);
-    t->lvx.assign(size_t(nl) * na, 0.0);
-    t->lflx.assign(size_t(nl) * na, 0.0);
-#pragma omp parallel for schedule(dynamic)
-    for (int r = 0; r < nl; ++r) {
-        const int ou = r / P1;
-        const int lu = level_of_order(ou);
-        const double ua = supp_lo(ou), ub = supp_hi(ou);
-        for (int c = 0; c < na; ++c) {
-            const int ov = c / np;
-            const double va = supp_lo(ov), vb = supp_hi(ov);
-            const size_t idx = size_t(r) * na + c;
-            if (!(va >= ub || vb <= ua)) {
-                double xl = ua, xr = ub;
-                if (lu <= level_of_order(ov)) { xl = va; xr = vb; }
-                const double xm = 0.5 * (xl + xr);
-                auto fv = [&](double x) { return lagr_eval(S, r, x, 0) * alpt.eval(c, 0, x, 0); };
-                auto fvx = [&](double x) { return lagr_eval(S, r, x, 0) * alpt.eval(c, 1, x, 0); };
-                t->lv[idx] = g.integrate(fv, xl, xm) + g.integrate(fv, xm, xr);
-                t->lvx[idx] = g.integrate(fvx, xl, xm) + g.integrate(fvx, xm, xr);
-            }
-            const double pts[3] = {va, 0.5 * (va + vb), vb};
-            const int npts = level_of_order(ov) <= 1 ? 2 : 3;
-            auto edge = [&](int su, int sv) {
-                double s = 0.0;
-                for (int i = 0; i < npts; ++i) {
-                    const double x = pts[i];
-                    double fu = lagr_eval(S, r, x, su), fw = alpt.eval(c, 0, x, sv);
-                    if (std::fabs(x) < kRoundOff) {
-                        if (su == -1) fu = lagr_eval(S, r, 1.0, su);
-                        if (sv == -1) fw = alpt.eval(c, 0, 1.0, sv);
-                    } else if (std::fabs(x - 1.0) < kRoundOff) {
-                        if (su == 1) fu = lagr_eval(S, r, 0.0, su);
-                        if (sv == 1) fw = alpt.eval(c, 0, 0.0, sv);
-                    }
-                    s += fu * fw;
-                }
-                return s;
-            };
-            // (ulft_vjp + urgt_vjp), HyperbolicLagrRHS::rhs_flx_intp_scalar (FastMultiplyLU.cpp:1166)
-            t->lflx[idx] = (edge(-1, 1) - edge(-1, -1)) + (edge(1, 1) - edge(1, -1));
-        }
-    }
+    build_interp_products(alpt, &S, P1, t);
     if (diffusion) {
         // Alpert derivative at the Lagrange points (Lag_pt_Alpt_1D_d1, Interplation.cpp:16-101)
         // and the point coordinates

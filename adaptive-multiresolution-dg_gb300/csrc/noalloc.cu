@@ -3,11 +3,10 @@
 //
 // The stage vectors u1 and u2 live in one file-scope device array of fixed
 // size instead of in memory allocated by amdg_linear_create.  Callers that
-// cannot call cudaMalloc -- code running while a stream is being captured into
-// a CUDA graph (cudaMalloc is not a stream operation and is not allowed in
-// capture), host callbacks launched with cudaLaunchHostFunc (which may not
-// call CUDA at all), or processes whose device memory is fully handed to
-// another allocator -- can step a small grid with this entry point.
+// cannot call cudaMalloc -- host callbacks launched with cudaLaunchHostFunc
+// (which may not call CUDA at all), processes whose device memory is fully
+// handed to another allocator, loops that must not allocate -- can step a
+// small grid with this entry point.
 //
 // Limits and sharing:
 //   * at most kNoAllocMaxDof coefficients (2 x 262,144 doubles = 4 MiB of

@@ -212,6 +212,16 @@ public:
         }
         return lagr_;
     }
+    // ... and behind the Hermite-path classes (HermInterpolation, HyperbolicSameFluxHermRHS; 2D)
+    amdg_burgers_op* herm_op() {
+        if (!herm_) {
+            const std::vector<double> zero(DIM, 0.0);
+            check(amdg_burgers_create_herm(grid_, zero.data(), &herm_), "amdg_burgers_create_herm");
+        }
+        return herm_;
+    }
+    // the operator an LxF penalty is added through (either Burgers operator computes it alike)
+    amdg_burgers_op* penalty_op() { return herm_ ? herm_ : lagr_op(); }
     // ... and behind the wave-path classes (the registered K = (1 + a prod_d sin 2 pi x_d)^2, IPDG
     // parameter from the last DiffusionAlpt built on this solution)
     amdg_wave_op* wave_op() {
@@ -232,11 +242,14 @@ protected:
     void release_lagr() {
         amdg_burgers_destroy(lagr_);
         lagr_ = nullptr;
+        amdg_burgers_destroy(herm_);
+        herm_ = nullptr;
         amdg_wave_destroy(wave_);
         wave_ = nullptr;
     }
     amdg_grid* grid_ = nullptr;
     amdg_burgers_op* lagr_ = nullptr;
+    amdg_burgers_op* herm_ = nullptr;
     amdg_wave_op* wave_ = nullptr;
     double wave_sigma_ = 0.0;
     int nmax_;
@@ -322,12 +335,33 @@ public:
         op_ = nullptr;
         check(amdg_linear_create(dg_.handle(), coef.data(), &op_), "amdg_linear_create");
     }
+    // assemble_matrix_flx_scalar(dim, sign, coef) (BilinearForm.cpp:759-769): coef times ulft_vjp
+    // (sign -1) or urgt_vjp (sign 1) along dim.  The terms are recorded; the pair
+    // (d, -1, alpha_d / 2) + (d, 1, -alpha_d / 2) for every d is the global Lax-Friedrichs penalty
+    // -alpha_d / 2 [u][v], which add_rhs_matrix applies on the device (lxf_alpha)
+    void assemble_matrix_flx_scalar(int dim, int sign, double coefficient) {
+        if (dim < 0 || dim >= DGSolution::DIM || (sign != -1 && sign != 1))
+            throw Error(AMDG_ERR_ARG, "assemble_matrix_flx_scalar: bad dimension or sign");
+        if (flx_.empty()) flx_.assign(size_t(2 * DGSolution::DIM), 0.0);
+        flx_[size_t(2 * dim + (sign == 1 ? 1 : 0))] += coefficient;
+    }
+    std::vector<double> lxf_alpha() const {
+        std::vector<double> alpha(DGSolution::DIM);
+        for (int d = 0; d < DGSolution::DIM && !flx_.empty(); ++d) {
+            alpha[size_t(d)] = 2.0 * flx_[size_t(2 * d)];
+            if (flx_[size_t(2 * d + 1)] != -flx_[size_t(2 * d)])
+                throw Error(AMDG_ERR_ARG, "HyperbolicAlpt: only Lax-Friedrichs pairs (d, -1, a/2), (d, 1, -a/2) are supported");
+        }
+        if (flx_.empty()) throw Error(AMDG_ERR_ARG, "HyperbolicAlpt: no flux terms assembled");
+        return alpha;
+    }
     amdg_linear_op* handle() const { return op_; }
     DGSolution& solution() const { return dg_; }
 
 private:
     DGSolution& dg_;
     amdg_linear_op* op_ = nullptr;
+    std::vector<double> flx_;  // [dim][sign -1, +1] coefficients of assemble_matrix_flx_scalar
 };
 
 // ExplicitRK on a DGSolution (ODESolver.h:5-38, 93): init() keeps the coefficients at t_n,
@@ -347,6 +381,16 @@ public:
     void add_rhs_to_eigenvec() { check(amdg_ode_add_rhs_to_eigenvec(need()), "amdg_ode_add_rhs_to_eigenvec"); }
     void step_stage(int stage) { check(amdg_ode_step_stage(need(), stage), "amdg_ode_step_stage"); }
     void final() { check(amdg_ode_final(need()), "amdg_ode_final"); }
+    // ODESolver::add_rhs_matrix (ODESolver.h:30): the solver's rhs += the operator's matrix times
+    // the current solution, for the Lax-Friedrichs matrix a driver assembles with
+    // assemble_matrix_flx_scalar.  The penalty is computed into Element::rhs (zeroed first, so it
+    // holds the penalty alone afterwards) and added to the solver's rhs.
+    void add_rhs_matrix(const HyperbolicAlpt& lin) {
+        const std::vector<double> alpha = lin.lxf_alpha();
+        dg_.set_rhs_zero();
+        check(amdg_lagr_rhs_add(dg_.penalty_op(), AMDG_LAGR_RHS_PENALTY, alpha.data(), precision), "add_rhs_matrix");
+        check(amdg_ode_add_rhs_to_eigenvec(need()), "amdg_ode_add_rhs_to_eigenvec");
+    }
 
 private:
     amdg_ode* need() {
@@ -365,15 +409,20 @@ public:
 class ForwardEuler : public ExplicitRK {
 public:
     ForwardEuler(DGSolution& dg, double dt) : ExplicitRK(dg, dt, AMDG_ODE_FORWARD_EULER, 1) {}
+    // on a flux-assembled linear form (the Lax-Friedrichs matrix): stage by stage, the matrix
+    // added by add_rhs_matrix
+    ForwardEuler(HyperbolicAlpt& lin, double dt) : ExplicitRK(lin.solution(), dt, AMDG_ODE_FORWARD_EULER, 1) {}
 };
 
 class RK3SSP : public ExplicitRK {
 public:
     // on a DGSolution, stage by stage (ODESolver.h:183-198)
     RK3SSP(DGSolution& dg, double dt) : ExplicitRK(dg, dt, AMDG_ODE_RK3SSP, 3), op_(nullptr) {}
-    // on an assembled linear operator: whole steps (RK3SSP::step_rk, ODESolver.cpp:261-271)
+    // on an assembled linear operator: whole steps (RK3SSP::step_rk, ODESolver.cpp:261-271); on a
+    // linear form with only flux terms assembled (the Lax-Friedrichs matrix of the Burgers
+    // drivers), stage by stage with add_rhs_matrix
     RK3SSP(HyperbolicAlpt& op, double dt, amdg_precision prec = AMDG_PREC_FP64)
-        : ExplicitRK(op.solution(), dt, AMDG_ODE_RK3SSP, 3), op_(&op), dt_(dt), prec_(prec) {}
+        : ExplicitRK(op.solution(), dt, AMDG_ODE_RK3SSP, 3), op_(op.handle() ? &op : nullptr), dt_(dt), prec_(prec) {}
     void init() {
         if (!op_) ExplicitRK::init();  // the linear form keeps its state on the device
     }
@@ -394,6 +443,8 @@ private:
 // ---- Lagrange interpolation of the nonlinear flux, term by term --------------------
 struct FluxFunction {
     static double burgers_flux_scalar(const double u) { return u * u * 0.5; }
+    static double burgers_flux_1st_derivative_scalar(const double u) { return u; }
+    static double burgers_flux_2nd_derivative_scalar(const double) { return 1.; }
 };
 
 // FastLagrIntp(dg, Lag_pt_Alpt_1D, Lag_pt_Alpt_1D_d1) (FastMultiplyLU.h:194-205): the tables
@@ -484,6 +535,59 @@ public:
         if (int(lax_alpha.size()) != DGSolution::DIM) throw Error(AMDG_ERR_ARG, "rhs_flx_penalty_scalar: one alpha per dimension");
         check(amdg_lagr_rhs_add(dg_.lagr_op(), AMDG_LAGR_RHS_PENALTY, lax_alpha.data(), precision),
               "rhs_flx_penalty_scalar");
+    }
+
+private:
+    DGSolution& dg_;
+};
+
+// ---- cubic Hermite interpolation of the flux, term by term (02_hyperbolic_05_burgers_adapt.cpp) ----
+// FastHermIntp(dg, Her_pt_Alpt_1D) (FastMultiplyLU.h:224-235): the table lives in the device operator
+class FastHermIntp {
+public:
+    FastHermIntp(DGSolution& dg, const std::vector<std::vector<double>>&) : dg_(dg) {}
+    DGSolution& solution() const { return dg_; }
+
+private:
+    DGSolution& dg_;
+};
+
+// HermInterpolation (Interpolation.h:251-311), HermBasis PMAX 3 with msh_case 1, 2D
+class HermInterpolation {
+public:
+    explicit HermInterpolation(DGSolution& dg) : dg_(dg) {}
+    std::vector<std::vector<double>> Her_pt_Alpt_1D;  // built on the device instead
+    // HermInterpolation::nonlinear_Herm_2D_fast (Interplation.cpp:4609-4621): u_h and its slopes at
+    // the Hermite points, f, f' u_x, f' u_y, f'' u_x u_y + f' u_xy there and their Hermite
+    // surpluses, kept for the HyperbolicSameFluxHermRHS calls that follow.  The registered flux is
+    // Burgers' (f = u^2/2, f' = u, f'' = 1); other functions are refused.
+    void nonlinear_Herm_2D_fast(std::function<double(std::vector<double>, int, int)> func,
+                                std::function<double(std::vector<double>, int, int, int)> func_d1,
+                                std::function<double(std::vector<double>, int, int, int, int)> func_d2,
+                                const std::vector<std::vector<bool>>& /*is_intp: the same flux in x and y*/,
+                                FastHermIntp& /*fast*/) {
+        if (DGSolution::DIM != 2 || HermBasis::PMAX != 3)
+            throw Error(AMDG_ERR_ARG, "HermInterpolation::nonlinear_Herm_2D_fast: 2D with HermBasis::PMAX = 3");
+        for (double u : {0.375, -1.3125, 2.25})
+            for (int d = 0; d < DGSolution::DIM; ++d)
+                if (func(std::vector<double>{u}, 0, d) != FluxFunction::burgers_flux_scalar(u) ||
+                    func_d1(std::vector<double>{u}, 0, d, 0) != FluxFunction::burgers_flux_1st_derivative_scalar(u) ||
+                    func_d2(std::vector<double>{u}, 0, d, 0, 0) != FluxFunction::burgers_flux_2nd_derivative_scalar(u))
+                    throw Error(AMDG_ERR_ARG, "HermInterpolation::nonlinear_Herm_2D_fast: only the Burgers flux is registered");
+        check(amdg_lagr_interpolate(dg_.herm_op(), precision), "amdg_lagr_interpolate (Hermite)");
+    }
+
+private:
+    DGSolution& dg_;
+};
+
+// HyperbolicSameFluxHermRHS (FastMultiplyLU.h:477-499): adds into Element::rhs
+class HyperbolicSameFluxHermRHS {
+public:
+    HyperbolicSameFluxHermRHS(DGSolution& dg, const OperatorMatrix1D<HermBasis, AlptBasis>&) : dg_(dg) {}
+    void rhs_vol_scalar() { check(amdg_lagr_rhs_add(dg_.herm_op(), AMDG_LAGR_RHS_VOL, nullptr, precision), "rhs_vol_scalar"); }
+    void rhs_flx_intp_scalar() {
+        check(amdg_lagr_rhs_add(dg_.herm_op(), AMDG_LAGR_RHS_FLX, nullptr, precision), "rhs_flx_intp_scalar");
     }
 
 private:

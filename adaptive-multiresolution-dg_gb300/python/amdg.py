@@ -83,6 +83,7 @@ def load():
         "amdg_rk3_stage_update": ([vp, i32, dbl, vp, vp, vp, i64], i32),
         "amdg_rk3ssp_steps_noalloc": ([vp, vp, dbl, i32, i32], i32),
         "amdg_burgers_create": ([vp, vp, pp], i32),
+        "amdg_burgers_create_herm": ([vp, vp, pp], i32),
         "amdg_burgers_adaptive_step": ([vp, dbl, dbl, dbl, dbl, i32, C.POINTER(dbl)], i32),
         "amdg_burgers_adaptive_step_ex": ([vp, dbl, dbl, dbl, dbl, i32, C.POINTER(dbl), vp], i32),
         "amdg_burgers_features": ([vp, vp, vp], i32),
@@ -574,11 +575,14 @@ class BurgersOperator:
     """LagrInterpolation + HyperbolicLagrRHS + HyperbolicAlptRHS for the Burgers
     flux u^2/2 with global Lax-Friedrichs penalty alpha, on the device."""
 
-    def __init__(self, grid: Grid, alpha):
+    def __init__(self, grid: Grid, alpha, hermite: bool = False):
+        """hermite=True: the flux interpolated by cubic Hermite interpolation (2D;
+        HermInterpolation + HyperbolicSameFluxHermRHS, amdg_burgers_create_herm)."""
         self.grid = grid
         a = np.ascontiguousarray(np.broadcast_to(np.asarray(alpha, np.float64), (grid.dim,)))
         self._h = C.c_void_p()
-        _ck(load().amdg_burgers_create(grid.handle, _ptr(a), C.byref(self._h)), "burgers_create")
+        fn = load().amdg_burgers_create_herm if hermite else load().amdg_burgers_create
+        _ck(fn(grid.handle, _ptr(a), C.byref(self._h)), "burgers_create_herm" if hermite else "burgers_create")
         self.points = 4 ** grid.dim
 
     def rhs_device(self, d_u: int, d_rhs: int, prec: int = FP64):

@@ -381,6 +381,8 @@ def run_ours(args):
         line["batched"] = bench_batched(ctx, stream, args)
     if args.wave_learn_runs > 0:
         line["wave2d_adaptive"] = bench_wave_adaptive(ctx, stream, args)
+    if args.herm_runs > 0:
+        line["burgers2d_hermite_adaptive"] = bench_herm_adaptive(ctx, stream, args)
     if rank == 0 and world == 1:
         line["cpu_baseline"] = cpu_baseline_config3(args)
         line["linear6d"]["cpu_baseline"] = cpu_baseline(*lin_cpu[:2], budget_s=args.cpu_seconds)
@@ -436,6 +438,87 @@ def bench_burgers(ctx, stream, args):
     del ref
     op.close()
     g.close()
+    return out
+
+
+HERM2D = {"n_init": 3, "nmax": 8, "eps": 1e-5, "eta": 1e-6, "alpha": 1.2, "cfl": 0.2, "T": 0.03}
+
+
+def ref_herm_steps(nsteps: int, threads: int):
+    """The reference's adaptive 2D Hermite Burgers loop (02_hyperbolic_05_burgers_adapt.cpp), timing
+    mode: per time step the wall seconds and the DOF its RK stages advanced."""
+    c = HERM2D
+    cmd = [REF_HARNESS, "burgers_herm_adapt", str(c["n_init"]), str(c["nmax"]), repr(c["eps"]), repr(c["eta"]),
+           repr(c["alpha"]), repr(c["cfl"]), str(nsteps), "time", repr(c["T"])]
+    env = dict(os.environ, OMP_NUM_THREADS=str(threads))
+    res = subprocess.run(cmd, env=env, capture_output=True, text=True, check=True)
+    return [(float(f[2]), int(f[3])) for f in (ln.split() for ln in res.stdout.splitlines()) if f and f[0] == "TSTEP"]
+
+
+def bench_herm_adaptive(ctx, stream, args):
+    """2D adaptive Burgers with the flux interpolated by cubic Hermite interpolation: the loop of
+    example/02_hyperbolic_05_burgers_adapt.cpp without artificial viscosity (u0 = sin(2 pi (x+y)),
+    start level 3, max level 8, refine 1e-5, coarsen 1e-6, LxF 1.2, CFL 0.2 with wave speed 1,
+    to T = 0.03, 34 steps).  DOF-stage updates/s of whole runs (CUDA events, initialisation
+    excluded) in FP64 and mixed precision, beside the reference's own loop on the host cores."""
+    import torch
+
+    import amdg
+    import amdg_oracle as O
+    c = HERM2D
+    flush = torch.empty(512 << 20, dtype=torch.uint8, device="cuda")
+
+    def one(prec):
+        g = amdg.Grid(ctx, 2, c["nmax"], 2, level_init=c["n_init"])
+        g.init_separable_adaptive(O.sin_sum_terms(2), c["eps"])
+        op = amdg.BurgersOperator(g, c["alpha"], hermite=True)
+        ctx.synchronize()
+        flush.fill_(1)
+        torch.cuda.synchronize()
+        sd0, _ = op.counters()
+        ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        ev0.record(stream)
+        t, steps = 0.0, 0
+        while t < c["T"] - 1e-12:
+            lv = g.max_mesh_level()
+            dt_full = c["cfl"] / sum(2.0 ** int(m) for m in lv)
+            cfl = c["cfl"] if t + dt_full <= c["T"] else c["cfl"] * (c["T"] - t) / dt_full
+            t += op.adaptive_step(cfl, 1.0, c["eps"], c["eta"], prec)
+            steps += 1
+        ev1.record(stream)
+        ev1.synchronize()
+        sd1, _ = op.counters()
+        res = {"sec": ev0.elapsed_time(ev1) / 1e3, "stage_dof_updates": sd1 - sd0, "steps": steps,
+               "elements_final": g.num_elements, "u": g.coefficients().reshape(-1).copy()}
+        op.close()
+        g.close()
+        return res
+
+    out = {"workload": "2D adaptive Burgers, cubic Hermite flux interpolation (HermInterpolation + "
+                       "HyperbolicSameFluxHermRHS), u0 = sin(2 pi (x+y)), start level 3, max level 8, refine 1e-5, "
+                       "coarsen 1e-6, LxF alpha 1.2, CFL 0.2, to T = 0.03"}
+    finals = {}
+    for name, prec in (("fp64", amdg.FP64), ("mixed", amdg.MIXED)):
+        for _ in range(max(1, args.warmup)):
+            one(prec)
+        runs = [one(prec) for _ in range(args.herm_runs)]
+        sec = sum(r["sec"] for r in runs)
+        out[name] = {"value": sum(r["stage_dof_updates"] for r in runs) / sec, "ms_per_run": sec / len(runs) * 1e3,
+                     "steps": runs[-1]["steps"], "elements_final": runs[-1]["elements_final"]}
+        finals[name] = runs[-1]["u"]
+    if finals["fp64"].shape == finals["mixed"].shape:
+        out["mixed_vs_fp64_rel_l2"] = float(np.linalg.norm(finals["mixed"] - finals["fp64"]) /
+                                            np.linalg.norm(finals["fp64"]))
+    out["mixed_speedup_vs_fp64"] = out["mixed"]["value"] / out["fp64"]["value"]
+    if ensure_ref_harness():
+        cores = os.cpu_count() or 1
+        steps = ref_herm_steps(args.cpu_steps + 2, cores)
+        sec = sum(x[0] for x in steps)
+        ref = sum(3.0 * x[1] for x in steps) / sec
+        out["reference_cpu"] = {"value": ref, "unit": "DOF-stage updates/s", "cores": cores, "kind": "reference",
+                                "sample": f"the first {len(steps)} time steps of the same run (AdaM-DG built from its "
+                                          f"sources on this host, {cores} OpenMP threads), {sec:.1f} s"}
+        out["fp64_vs_reference_cpu"] = out["fp64"]["value"] / ref
     return out
 
 
@@ -1413,6 +1496,7 @@ def main():
     ap.add_argument("--learn-horizon", type=int, default=4,
                     help="time steps per learned pre-adaptation in the 3D Burgers runs")
     ap.add_argument("--learn-epochs", type=int, default=30)
+    ap.add_argument("--herm-runs", type=int, default=3, help="timed runs of the 2D Hermite Burgers line (0: skip)")
     ap.add_argument("--wave-learn-runs", type=int, default=20, help="plain wave runs that train its classifier (0: skip)")
     ap.add_argument("--wave-learn-steps", type=int, default=30)
     ap.add_argument("--wave-train-samples", type=int, default=300000, help="training samples kept (stratified)")

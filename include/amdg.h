@@ -294,9 +294,9 @@ amdg_status amdg_rk3ssp_serve_host(amdg_linear_op* op, double dt, int nsteps, am
                                    const double* const* host_in, double* const* host_out);
 
 /* Allocation-free variant of amdg_rk3ssp_steps, with no counterpart in the
- * reference: for callers that cannot call cudaMalloc (code running during CUDA
- * stream capture, host callbacks, processes whose device memory belongs to
- * another allocator).  d_u is the caller's device state (dof doubles, input
+ * reference: for callers that cannot call cudaMalloc (host callbacks, which may
+ * not call CUDA, processes whose device memory belongs to another allocator,
+ * loops that must not allocate).  d_u is the caller's device state (dof doubles, input
  * and output).  The stage vectors live in a fixed 4 MiB device array shared by
  * every call, so the grid may hold at most 262,144 coefficients (larger grids
  * get AMDG_ERR_CAPACITY) and calls that overlap on the GPU race.  The first
@@ -374,6 +374,22 @@ amdg_status amdg_rk3_stage_update(amdg_context* ctx, int stage, double dt, const
  * must be free of holes (every element's parents present, DGAdapt::check_hole);
  * otherwise AMDG_ERR_STATE. */
 amdg_status amdg_burgers_create(amdg_grid* g, const double* alpha, amdg_burgers_op** out);
+/* The same operator with the flux interpolated by cubic Hermite interpolation (HermBasis with
+ * PMAX 3, msh_case 1: value and slope at two points per 1D element), 2D only, as
+ * example/02_hyperbolic_05_burgers_adapt.cpp runs Burgers: replaces the set-up of
+ * HermInterpolation(dg) + FastHermIntp(dg, Her_pt_Alpt_1D) + HyperbolicSameFluxHermRHS(dg,
+ * oper_matx_herm) (Interpolation.h:251-283, FastMultiplyLU.h:224-235, 477-498) for the registered
+ * flux u^2/2 with f' = u, f'' = 1.  Every amdg_burgers_* and amdg_lagr_* call below takes it:
+ * point values are then u_h and its slopes at the Hermite points (4^2 per element,
+ * Element::up_intp), flux coefficients the Hermite coefficients of the flux
+ * (HermInterpolation::eval_fp_to_coe_D_Her, Interplation.cpp:3651-3849), amdg_lagr_interpolate
+ * is HermInterpolation::nonlinear_Herm_2D_fast (Interplation.cpp:4609-4621) and the
+ * AMDG_LAGR_RHS_VOL / _FLX groups are HyperbolicSameFluxHermRHS::rhs_vol_scalar /
+ * rhs_flx_intp_scalar (FastMultiplyLU.cpp:970-1016).  The LxF penalty group is the driver's
+ * assembled HyperbolicAlpt::assemble_matrix_flx_scalar(d, -1, alpha/2) + (d, 1, -alpha/2)
+ * (BilinearForm.cpp:759-769), equal to rhs_flx_penalty_scalar(alpha) up to rounding.
+ * AMDG_ERR_ARG unless the grid is 2D. */
+amdg_status amdg_burgers_create_herm(amdg_grid* g, const double* alpha, amdg_burgers_op** out);
 amdg_status amdg_burgers_destroy(amdg_burgers_op* op);
 /* One right-hand-side evaluation, d_rhs = R(d_u) (device vectors of dof doubles).
  * Point values and the hierarchical surplus run in FP64 in both modes; with

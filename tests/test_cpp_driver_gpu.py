@@ -128,3 +128,28 @@ def test_cpp_burgers_driver_matches_reference(tmp_path, name):
     assert set(keys) == set(ref_keys)
     pos = {k: j for j, k in enumerate(ref_keys)}
     assert rel_err(u, z[f"u_{s}"][[pos[k] for k in keys]]) < 1e-12
+
+
+@pytest.mark.parametrize("name", ["burgers_herm_adapt2d", "burgers_herm_adapt2d_n8_T003"])
+def test_cpp_hermite_burgers_driver_matches_reference(tmp_path, name):
+    """example/02_hyperbolic_05_burgers_adapt.cpp rewritten against amdg_dg.hpp statement by
+    statement (HermInterpolation, FastHermIntp, HyperbolicSameFluxHermRHS, the Lax-Friedrichs
+    matrix assembled by HyperbolicAlpt::assemble_matrix_flx_scalar and added by add_rhs_matrix,
+    ForwardEuler predictor, refine, RK3SSP stages, coarsen) ends on the reference's element set,
+    coefficients to 1e-12 of their largest entry."""
+    from helpers import golden, manifest, rel_err
+    exe = os.path.join(os.path.dirname(amdg.LIB_PATH), "burgers_herm_adapt")
+    assert os.path.exists(exe), "example driver not built"
+    m = manifest()[name]
+    z = golden(name)
+    s = m["steps"]
+    out_file = str(tmp_path / "u.txt")
+    args = [m["n_init"], m["nmax"], 1.0, repr(m["eps"]), repr(m["eta"]), s, out_file]
+    res = subprocess.run([exe] + [str(a) for a in args], capture_output=True, text=True, timeout=600, check=True)
+    assert res.stdout.startswith(f"steps {s} ")
+    lv, sp, u = _read_elements(out_file, 2)
+    keys = O.arrays_to_keys(lv, sp)
+    ref_keys = O.arrays_to_keys(z[f"level_{s}"], z[f"suppt_{s}"])
+    assert set(keys) == set(ref_keys)
+    pos = {k: j for j, k in enumerate(ref_keys)}
+    assert rel_err(u, z[f"u_{s}"][[pos[k] for k in keys]]) < 1e-12

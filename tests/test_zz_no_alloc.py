@@ -1,8 +1,8 @@
 """The allocation-free RK3 entry point (amdg_rk3ssp_steps_noalloc).
 
-Some callers of this library cannot allocate device memory -- code that runs
-while a stream is captured into a CUDA graph, host callbacks, processes whose
-device memory belongs to another allocator -- so the library offers one RK3
+Some callers of this library cannot allocate device memory -- host callbacks,
+processes whose device memory belongs to another allocator, loops that must
+not allocate -- so the library offers one RK3
 stepping call whose stage vectors sit in a fixed device array instead of in
 cudaMalloc'ed memory.  This file checks it through the C-ABI against the
 allocating entry point (amdg_rk3ssp_steps) on two calls in a row, with the
