@@ -594,13 +594,15 @@ struct amdg_batch {
     double* d_blocks64p = nullptr;        // the same in FP64
     float* d_dt32 = nullptr;              // [solve]
     int* d_err = nullptr;                 // bulk-copy wait gave up (device flag)
+    unsigned long long* d_queue = nullptr;  // [3] chunk counters of the warp kernel's queue schedule, one per stage
+    int sms = 0;                          // multiprocessors of the device (persistent grids)
     void* graph_exec[2] = {nullptr, nullptr};  // cudaGraphExec_t per precision
     int64_t launches_per_graph = 0;
-    // stage kernel per precision (FP64, mixed): candidate c < kBatchTileCount is the column
-    // kernel with kBatchTiles[c] threads, c >= kBatchTileCount the bulk-copy ring configuration
-    // c - kBatchTileCount (mixed only); picked by the autotuner
+    // stage kernel per precision (FP64, mixed), candidates as amdg_batch_tuning numbers them (the
+    // column kernel at each CTA size, on the FP64 state or, mixed, on the FP32-pair state, the
+    // bulk-copy ring and the warp-per-element kernel configurations); picked by the autotuner
     int kernel[2] = {2, 2};
-    float kernel_ms[2][16] = {{0}};       // autotuner: one stage per candidate (0: not timed)
+    float kernel_ms[2][AMDG_BATCH_KERNELS] = {{0}};  // autotuner: one stage per candidate (0: not timed)
     // amdg_batch_adapt scratch over all elements (grow-only): norms, parent table, classifier
     // features and probabilities
     double* d_norms = nullptr;

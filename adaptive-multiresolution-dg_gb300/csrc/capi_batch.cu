@@ -65,11 +65,24 @@ StageCoef coef_of(int stage) {
 // mixed-mode candidates: [kBatchTileCount, 2 kBatchTileCount) the column kernel on the FP32-pair
 // state, from 2 kBatchTileCount the bulk-copy ring kernel (on the same state)
 constexpr int kRingFirst = 2 * kBatchTileCount;
+// then the column kernel on the same state with a persistent grid, (CTA size, schedule) per
+// configuration (schedule 1: static tile order, 2: tiles from a device counter), then the
+// warp-per-element kernel
+constexpr int kPersistFirst = kRingFirst + kBatchRingConfigs;
+constexpr int kPersistConfigs = 3;
+constexpr int kPersist[kPersistConfigs][2] = {{64, 1}, {128, 1}, {64, 2}};
+constexpr int kWarpFirst = kPersistFirst + kPersistConfigs;
+static_assert(kWarpFirst + kBatchWarpConfigs == AMDG_BATCH_KERNELS, "candidate numbering");
 bool df_state(const amdg_batch* b, int pi) { return pi == 1 && b->kernel[1] >= kBatchTileCount; }
-bool ring_kernel(const amdg_batch* b, int pi) { return pi == 1 && b->kernel[1] >= kRingFirst; }
+bool ring_kernel(const amdg_batch* b, int pi) { return pi == 1 && b->kernel[1] >= kRingFirst && b->kernel[1] < kPersistFirst; }
+bool persist_kernel(const amdg_batch* b, int pi) {
+    return pi == 1 && b->kernel[1] >= kPersistFirst && b->kernel[1] < kWarpFirst;
+}
+bool warp_kernel(const amdg_batch* b, int pi) { return pi == 1 && b->kernel[1] >= kWarpFirst; }
 
-// one launch of the column kernel on the FP32-pair state: stage `stage`, slot in -> out
-amdg_status df_col_stage(amdg_batch* b, int threads, int stage, int in, int out, cudaStream_t st);
+// one launch of the column kernel on the FP32-pair state: stage `stage`, slot in -> out; schedule
+// 1 / 2 persistent (the counter schedule takes its tiles from counter `stage`, zeroed by the caller)
+amdg_status df_col_stage(amdg_batch* b, int threads, int stage, int in, int out, cudaStream_t st, int schedule = 0);
 
 // the stage-state arrays of the mixed mode: high and low parts of slot i
 float* hi_of(amdg_batch* b, int i) { return b->d_shadow + i * b->sstride; }
@@ -94,7 +107,24 @@ amdg_status ring_stage(amdg_batch* b, int cfg, int stage, int in, int out, cudaS
     return AMDG_OK;
 }
 
-amdg_status df_col_stage(amdg_batch* b, int threads, int stage, int in, int out, cudaStream_t st) {
+// one launch of the warp-per-element kernel: stage `stage` of the FP32-pair state, slot in -> out
+amdg_status warp_stage(amdg_batch* b, int cfg, int stage, int in, int out, cudaStream_t st) {
+    const StageCoef c = coef_of(stage);
+    BatchWarpLaunch L{};
+    L.dim = b->dim; L.np = b->k + 1; L.cfg = cfg;
+    L.num_elements = b->num_elements; L.num_blocks = b->num_blocks;
+    L.row_ptr = b->d_row_ptr; L.pairs = reinterpret_cast<const int2*>(b->d_pairs); L.blocks = b->d_blocks32p;
+    L.coef = b->d_coef32; L.dt = b->d_dt32; L.solve_of = b->d_solve;
+    L.xs = hi_of(b, in);
+    L.df = df_stage(c);
+    L.df.us_hi = hi_of(b, in); L.df.us_lo = lo_of(b, in);
+    L.df.un_hi = hi_of(b, 0); L.df.un_lo = lo_of(b, 0);
+    L.df.out_hi = hi_of(b, out); L.df.out_lo = lo_of(b, out);
+    AMDG_CK(launch_batch_warp(L, st));
+    return AMDG_OK;
+}
+
+amdg_status df_col_stage(amdg_batch* b, int threads, int stage, int in, int out, cudaStream_t st, int schedule) {
     const StageCoef c = coef_of(stage);
     BatchLaunch<float, float> L{};
     L.dim = b->dim; L.np = b->k + 1; L.mode = 1; L.a = c.a; L.b = c.b; L.threads = threads;
@@ -108,6 +138,9 @@ amdg_status df_col_stage(amdg_batch* b, int threads, int stage, int in, int out,
     L.df.un_hi = hi_of(b, 0); L.df.un_lo = lo_of(b, 0);
     L.df.out_hi = hi_of(b, out); L.df.out_lo = lo_of(b, out);
     L.dt32 = b->d_dt32;
+    L.schedule = schedule;
+    L.queue = b->d_queue + stage;
+    L.sms = b->sms;
     AMDG_CK(launch_batch<float, float>(L, st));
     return AMDG_OK;
 }
@@ -119,8 +152,15 @@ amdg_status batch_step(amdg_batch* b, amdg_precision prec, cudaStream_t st) {
     const int pi = prec == AMDG_PREC_MIXED ? 1 : 0;
     if (df_state(b, pi)) {
         const int in_i[3] = {0, 1, 2}, out_i[3] = {1, 2, 0};
+        const int pc = b->kernel[1] - kPersistFirst;
+        if (persist_kernel(b, pi) && kPersist[pc][1] == 2)
+            AMDG_CK(cudaMemsetAsync(b->d_queue, 0, 3 * sizeof(unsigned long long), st));
         for (int stage = 0; stage < 3; ++stage) {
-            amdg_status r = ring_kernel(b, pi)
+            amdg_status r = warp_kernel(b, pi)
+                                ? warp_stage(b, b->kernel[1] - kWarpFirst, stage, in_i[stage], out_i[stage], st)
+                            : persist_kernel(b, pi)
+                                ? df_col_stage(b, kPersist[pc][0], stage, in_i[stage], out_i[stage], st, kPersist[pc][1])
+                            : ring_kernel(b, pi)
                                 ? ring_stage(b, b->kernel[1] - kRingFirst, stage, in_i[stage], out_i[stage], st)
                                 : df_col_stage(b, kBatchTiles[b->kernel[1] - kBatchTileCount], stage, in_i[stage],
                                                out_i[stage], st);
@@ -255,17 +295,29 @@ amdg_status autotune_batch(amdg_batch* b, cudaStream_t st) {
     const StageCoef c = coef_of(0);
     for (int pi = 0; pi < 2 && status == AMDG_OK; ++pi) {
         float best = 0.f;
-        const int ncand = pi == 1 ? kRingFirst + kBatchRingConfigs : kBatchTileCount;
+        const int ncand = pi == 1 ? AMDG_BATCH_KERNELS : kBatchTileCount;
         for (int ci = 0; ci < ncand; ++ci) {
-            const bool ring = ci >= kRingFirst, dfcol = ci >= kBatchTileCount && !ring;
-            const int tile = ring ? 0 : kBatchTiles[ci % kBatchTileCount];
-            if (ring ? !batch_ring_supported(b->dim, b->k + 1, ci - kRingFirst)
-                     : !batch_tile_supported(b->dim, b->k + 1, tile))
+            const bool warp = ci >= kWarpFirst, persist = ci >= kPersistFirst && !warp;
+            const bool ring = ci >= kRingFirst && ci < kPersistFirst;
+            const bool dfcol = ci >= kBatchTileCount && ci < kRingFirst;
+            const int tile = persist ? kPersist[ci - kPersistFirst][0] : (ring || warp) ? 0 : kBatchTiles[ci % kBatchTileCount];
+            if (warp ? !batch_warp_supported(b->dim, b->k + 1, ci - kWarpFirst)
+                : ring ? !batch_ring_supported(b->dim, b->k + 1, ci - kRingFirst)
+                       : !batch_tile_supported(b->dim, b->k + 1, tile))
                 continue;
             float t_min = 0.f;
             for (int rep = 0; rep < 4 && status == AMDG_OK; ++rep) {
                 cudaError_t e = cudaEventRecord(e0, st);
-                if (ring) {
+                if (warp) {
+                    if (e == cudaSuccess && warp_stage(b, ci - kWarpFirst, 0, 0, 1, st) != AMDG_OK)
+                        e = cudaErrorLaunchFailure;
+                } else if (persist) {
+                    const int sched = kPersist[ci - kPersistFirst][1];
+                    if (e == cudaSuccess && sched == 2)
+                        e = cudaMemsetAsync(b->d_queue, 0, 3 * sizeof(unsigned long long), st);
+                    if (e == cudaSuccess && df_col_stage(b, tile, 0, 0, 1, st, sched) != AMDG_OK)
+                        e = cudaErrorLaunchFailure;
+                } else if (ring) {
                     if (e == cudaSuccess && ring_stage(b, ci - kRingFirst, 0, 0, 1, st) != AMDG_OK)
                         e = cudaErrorLaunchFailure;
                 } else if (dfcol) {
@@ -342,12 +394,19 @@ amdg_status amdg_batch_create(amdg_context* ctx, int n, amdg_grid* const* grids,
     std::vector<double> dt(n, 0.0);
     std::vector<float> dt32(n, 0.f);
     std::vector<int> err0(1, 0);
+    std::vector<unsigned long long> queue0(3, 0);
+    if (cudaDeviceGetAttribute(&b->sms, cudaDevAttrMultiProcessorCount, b->device) != cudaSuccess) b->sms = 0;
     amdg_status s;
     if ((s = put(&b->d_coef64, c64)) != AMDG_OK || (s = put(&b->d_coef32, c32)) != AMDG_OK ||
         (s = put(&b->d_dt, dt)) != AMDG_OK || (s = put(&b->d_dt32, dt32)) != AMDG_OK ||
-        (s = put(&b->d_err, err0)) != AMDG_OK || (s = batch_build(b)) != AMDG_OK) {
+        (s = put(&b->d_err, err0)) != AMDG_OK || (s = put(&b->d_queue, queue0)) != AMDG_OK ||
+        (s = batch_build(b)) != AMDG_OK) {
         amdg_batch_destroy(b);
         return s;
+    }
+    if (cudaError_t e = batch_prepare_persistent(dim, k + 1); e != cudaSuccess) {
+        amdg_batch_destroy(b);
+        return fail(AMDG_ERR_CUDA, std::string("persistent batch kernel occupancy: ") + cudaGetErrorString(e));
     }
     cudaStream_t st = stream_of(b);
     if ((s = autotune_batch(b, st)) != AMDG_OK) {
@@ -375,8 +434,10 @@ amdg_status amdg_batch_set_kernel(amdg_batch* b, amdg_precision prec, int kernel
     AMDG_REQUIRE(prec == AMDG_PREC_FP64 || prec == AMDG_PREC_MIXED, AMDG_ERR_ARG, "bad precision");
     bool ok = kernel >= 0 && kernel < AMDG_BATCH_KERNELS && (kernel < kBatchTileCount || prec == AMDG_PREC_MIXED);
     if (ok)
-        ok = kernel < kRingFirst ? batch_tile_supported(b->dim, b->k + 1, kBatchTiles[kernel % kBatchTileCount])
-                                 : batch_ring_supported(b->dim, b->k + 1, kernel - kRingFirst);
+        ok = kernel < kRingFirst     ? batch_tile_supported(b->dim, b->k + 1, kBatchTiles[kernel % kBatchTileCount])
+             : kernel < kPersistFirst ? batch_ring_supported(b->dim, b->k + 1, kernel - kRingFirst)
+             : kernel < kWarpFirst    ? batch_tile_supported(b->dim, b->k + 1, kPersist[kernel - kPersistFirst][0])
+                                      : batch_warp_supported(b->dim, b->k + 1, kernel - kWarpFirst);
     AMDG_REQUIRE(ok, AMDG_ERR_ARG, "unsupported stage kernel for this dimension and precision");
     const int pi = prec == AMDG_PREC_MIXED ? 1 : 0;
     if (b->kernel[pi] != kernel && b->graph_exec[pi]) {
@@ -402,7 +463,7 @@ amdg_status amdg_batch_destroy(amdg_batch* b) {
         if (b->graph_exec[p]) cudaGraphExecDestroy(static_cast<cudaGraphExec_t>(b->graph_exec[p]));
     void* ptrs[] = {b->d_row_ptr, b->d_src, b->d_blk, b->d_solve, b->d_blocks64, b->d_blocks32, b->d_coef64,
                     b->d_coef32, b->d_dt, b->d_u, b->d_u1, b->d_u2, b->d_shadow, b->d_lo, b->d_pairs,
-                    b->d_blocks32p, b->d_blocks64p, b->d_dt32, b->d_err, b->d_pg, b->d_feat, b->d_prob, b->d_norms};
+                    b->d_blocks32p, b->d_blocks64p, b->d_dt32, b->d_err, b->d_queue, b->d_pg, b->d_feat, b->d_prob, b->d_norms};
     for (void* p : ptrs) cudaFree(p);
     delete b;
     return AMDG_OK;

@@ -86,6 +86,11 @@ struct BatchLaunch {
     // entries per block (vector loads)
     const int2* pairs;
     const T* blocks_p;
+    // FP32-pair state only: 0 one CTA per tile; 1 persistent (grid of resident CTAs, static tile
+    // order); 2 persistent, tiles taken from the counter `queue` (zero before the launch)
+    int schedule;
+    unsigned long long* queue;
+    int sms;  // multiprocessors of the device (persistent grids)
 };
 template <typename T, typename X>
 cudaError_t launch_batch(const BatchLaunch<T, X>& L, cudaStream_t st);
@@ -93,6 +98,8 @@ cudaError_t launch_batch(const BatchLaunch<T, X>& L, cudaStream_t st);
 constexpr int kBatchTileCount = 5;
 constexpr int kBatchTiles[kBatchTileCount] = {64, 128, 256, 512, 1024};
 bool batch_tile_supported(int dim, int np, int threads);
+// the occupancy queries of the persistent schedules, run before any stream capture
+cudaError_t batch_prepare_persistent(int dim, int np);
 
 // Batched solves on the bulk-copy ring (kernels.cu, batch_ring_kernel): the stage input's FP32
 // high parts (xs) stream into shared memory by bulk copies, the stage vectors are FP32 (hi, lo)
@@ -116,6 +123,28 @@ struct BatchRingLaunch {
 };
 bool batch_ring_supported(int dim, int np, int cfg);
 cudaError_t launch_batch_ring(const BatchRingLaunch& L, cudaStream_t st);
+
+// Batched solves, one warp per element (kernels_batch.cu, batch_warp_kernel): lane i holds
+// coefficient i of the element block (blocks of at most 32 coefficients), each neighbour block is
+// one coalesced load of its FP32 high parts, the 1D block one load of its np^2 entries, and the
+// contraction along a dimension gathers the np values of a lane's fibre by warp shuffles; one CTA
+// of 8 warps per 8 elements.  FP32 (hi, lo) stage state as BatchRingLaunch.
+constexpr int kBatchWarpConfigs = 1;
+struct BatchWarpLaunch {
+    int dim, np, cfg;
+    int64_t num_elements;
+    int num_blocks;
+    const int64_t* row_ptr;
+    const int2* pairs;
+    const float* blocks;     // padded as BatchRingLaunch
+    const float* coef;
+    const float* dt;
+    const int32_t* solve_of;
+    const float* xs;
+    DFState df;
+};
+bool batch_warp_supported(int dim, int np, int cfg);
+cudaError_t launch_batch_warp(const BatchWarpLaunch& L, cudaStream_t st);
 
 constexpr int kReduceBlocks = 1216;  // 8 CTAs per SM on 152 SMs
 

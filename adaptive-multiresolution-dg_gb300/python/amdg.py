@@ -841,12 +841,17 @@ class Batch:
         return stats
 
     # stage-kernel candidates: the column kernel at these CTA sizes, then the bulk-copy ring kernel
-    # (mixed only) in these (ring slots, elements per CTA) configurations
+    # (mixed only) in these (ring slots, elements per CTA) configurations, then the warp-per-element
+    # kernel (mixed only) in these (warps per CTA, schedule) configurations
     TILES = (64, 128, 256, 512, 1024)
     RING_CONFIGS = ((1, 1), (1, 2), (1, 4), (2, 1), (2, 2), (2, 4))
+    PERSIST_CONFIGS = ((64, "static tile order"), (128, "static tile order"), (64, "tiles from a counter"))
+    WARP_CONFIGS = ((8, "one CTA per 8 elements"),)
     DF_COLUMN_FIRST = len(TILES)       # the column kernel on the FP32-pair state (mixed)
     RING_FIRST = 2 * len(TILES)        # the bulk-copy ring kernel (mixed)
-    KERNELS = 2 * len(TILES) + len(RING_CONFIGS)
+    PERSIST_FIRST = RING_FIRST + len(RING_CONFIGS)  # the column kernel, persistent (mixed)
+    WARP_FIRST = PERSIST_FIRST + len(PERSIST_CONFIGS)  # the warp-per-element kernel (mixed)
+    KERNELS = WARP_FIRST + len(WARP_CONFIGS)
 
     @classmethod
     def kernel_name(cls, c: int) -> str:
@@ -854,8 +859,14 @@ class Batch:
             return f"column {cls.TILES[c]} threads"
         if c < cls.RING_FIRST:
             return f"column {cls.TILES[c - cls.DF_COLUMN_FIRST]} threads, FP32-pair state"
-        r, w = cls.RING_CONFIGS[c - cls.RING_FIRST]
-        return f"bulk-copy ring {r} slot{'s' if r > 1 else ''}, {w} element{'s' if w > 1 else ''} per CTA"
+        if c < cls.PERSIST_FIRST:
+            r, w = cls.RING_CONFIGS[c - cls.RING_FIRST]
+            return f"bulk-copy ring {r} slot{'s' if r > 1 else ''}, {w} element{'s' if w > 1 else ''} per CTA"
+        if c < cls.WARP_FIRST:
+            t, sched = cls.PERSIST_CONFIGS[c - cls.PERSIST_FIRST]
+            return f"column {t} threads, FP32-pair state, persistent, {sched}"
+        w, sched = cls.WARP_CONFIGS[c - cls.WARP_FIRST]
+        return f"warp per element, {w} warps per CTA, {sched}"
 
     def tuning(self):
         """(stage-kernel candidate per precision [FP64, mixed], stage ms per candidate [2][KERNELS])."""

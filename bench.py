@@ -888,12 +888,14 @@ def bench_wave_adaptive(ctx, stream, args):
         g.close()
         return res
 
-    ref_run = run(False, amdg.FP64, T, eps, eta, 10)
-    ref = ref_run.pop("_mesh_values")
-    out["fp64_level10_run"] = {"what": "plain FP64 on this GPU (not the reference code), refine 1e-5, coarsen 1e-6, "
-                                       "max level 10",
-                               "wall_s": ref_run["wall_s"], "steps": ref_run["steps"],
-                               "elements_final": ref_run["elements_final"]}
+    ref = None
+    if not args.wave_no_level10:
+        ref_run = run(False, amdg.FP64, T, eps, eta, 10)
+        ref = ref_run.pop("_mesh_values")
+        out["fp64_level10_run"] = {"what": "plain FP64 on this GPU (not the reference code), refine 1e-5, coarsen "
+                                           "1e-6, max level 10",
+                                   "wall_s": ref_run["wall_s"], "steps": ref_run["steps"],
+                                   "elements_final": ref_run["elements_final"]}
     # the learned arm at the trained horizon ("mixed_learned") and at horizons 1 and 4
     arms = [("plain_fp64", False, amdg.FP64, 1), ("mixed_learned", True, amdg.MIXED, H)]
     arms += [(f"mixed_learned_h{h}", True, amdg.MIXED, h) for h in (1, 4) if h != H]
@@ -903,14 +905,16 @@ def bench_wave_adaptive(ctx, stream, args):
         out[name] = run(learned, prec, T, horizon=horizon)
         out[name]["horizon"] = horizon
         v = out[name].pop("_mesh_values")
-        out[name]["rel_l2_diff_vs_fp64_level10_run"] = float(np.linalg.norm(v - ref) / np.linalg.norm(ref))
+        if ref is not None:
+            out[name]["rel_l2_diff_vs_fp64_level10_run"] = float(np.linalg.norm(v - ref) / np.linalg.norm(ref))
         out[name]["_v"] = v
     base = out["plain_fp64"].pop("_v")
     for name in [a[0] for a in arms[1:]]:
         v = out[name].pop("_v")
         out[name]["rel_l2_diff_vs_plain_fp64"] = float(np.linalg.norm(v - base) / np.linalg.norm(base))
-        out[name]["error_ratio_vs_plain_fp64"] = (out[name]["rel_l2_diff_vs_fp64_level10_run"] /
-                                                 out["plain_fp64"]["rel_l2_diff_vs_fp64_level10_run"])
+        if ref is not None:
+            out[name]["error_ratio_vs_plain_fp64"] = (out[name]["rel_l2_diff_vs_fp64_level10_run"] /
+                                                     out["plain_fp64"]["rel_l2_diff_vs_fp64_level10_run"])
         out[name]["speedup_vs_plain_fp64"] = out["plain_fp64"]["wall_s"] / out[name]["wall_s"]
     mlp.close()
     return out
@@ -1219,6 +1223,51 @@ def profile_config3():
     torch.cuda.cudart().cudaProfilerStop()
 
 
+def profile_herm():
+    """Profiling case (not a bench line): one plain FP64 and one mixed run of the 2D adaptive
+    Hermite Burgers workload (max level 8 to T = 0.03) after a warm-up run each, between
+    cudaProfilerStart / cudaProfilerStop, for ncu --profile-from-start off."""
+    import torch
+
+    import amdg
+    torch.cuda.set_device(0)
+    ctx = amdg.Context(0)
+    stream = torch.cuda.Stream()
+    torch.cuda.set_stream(stream)
+    ctx.set_stream(stream.cuda_stream)
+    import amdg_oracle as O
+    c = HERM2D
+
+    def one(prec):
+        g = amdg.Grid(ctx, 2, c["nmax"], 2, level_init=c["n_init"])
+        g.init_separable_adaptive(O.sin_sum_terms(2), c["eps"])
+        op = amdg.BurgersOperator(g, c["alpha"], hermite=True)
+        ctx.synchronize()
+        l0 = ctx.launch_count()
+        ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        ev0.record(stream)
+        t = 0.0
+        while t < c["T"] - 1e-12:
+            dt_full = c["cfl"] / sum(2.0 ** int(m) for m in g.max_mesh_level())
+            cfl = c["cfl"] if t + dt_full <= c["T"] else c["cfl"] * (c["T"] - t) / dt_full
+            t += op.adaptive_step(cfl, 1.0, c["eps"], c["eta"], prec)
+        ev1.record(stream)
+        ev1.synchronize()
+        res = {"prec": int(prec), "ms": ev0.elapsed_time(ev1), "launches": ctx.launch_count() - l0,
+               "elements_final": g.num_elements}
+        op.close()
+        g.close()
+        return res
+
+    for prec in (amdg.FP64, amdg.MIXED):
+        one(prec)
+    torch.cuda.synchronize()
+    torch.cuda.cudart().cudaProfilerStart()
+    for prec in (amdg.FP64, amdg.MIXED):
+        print(json.dumps(one(prec)), flush=True)
+    torch.cuda.cudart().cudaProfilerStop()
+
+
 def profile_batch():
     """Profiling case (not a bench line): 64 of the batched solves (per-solve refine thresholds
     log-uniform in [1e-8, 1e-5], adaptive N<=8), one mixed SSP-RK3 step with the autotuner's stage
@@ -1501,8 +1550,13 @@ def main():
     ap.add_argument("--wave-learn-steps", type=int, default=30)
     ap.add_argument("--wave-train-samples", type=int, default=300000, help="training samples kept (stratified)")
     ap.add_argument("--wave-learn-horizon", type=int, default=2, help="time steps per learned pre-adaptation (wave)")
-    ap.add_argument("--profile", choices=["none", "wave_rhs", "config3", "rhs3d", "linear6d", "batch"], default="none",
+    ap.add_argument("--profile", choices=["none", "wave_rhs", "config3", "rhs3d", "linear6d", "batch", "herm"],
+                    default="none",
                     help="wave_rhs: run the wave right-hand-side profiling case instead of the bench")
+    ap.add_argument("--wave-only", action="store_true",
+                    help="run only the 2D adaptive wave line (for a run to the config's T = 0.5) and print it")
+    ap.add_argument("--wave-no-level10", action="store_true",
+                    help="skip the max-level-10 FP64 run the wave arms' errors are measured against")
     ap.add_argument("--wave-time", type=float, default=0.05,
                     help="final time of the 2D wave runs (the config's 0.5 takes ~5000 steps on a filling grid)")
     args = ap.parse_args()
@@ -1514,8 +1568,20 @@ def main():
         profile_linear6d()
     elif args.profile == "batch":
         profile_batch()
+    elif args.profile == "herm":
+        profile_herm()
     elif args.profile == "rhs3d":
         profile_rhs3d()
+    elif args.wave_only:
+        import torch
+
+        import amdg
+        torch.cuda.set_device(0)
+        ctx = amdg.Context(0)
+        stream = torch.cuda.Stream()
+        torch.cuda.set_stream(stream)
+        ctx.set_stream(stream.cuda_stream)
+        print(json.dumps({"wave2d_adaptive": bench_wave_adaptive(ctx, stream, args)}), flush=True)
     elif args.impl == "reference":
         run_reference(args)
     else:

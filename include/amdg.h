@@ -31,7 +31,7 @@
 extern "C" {
 #endif
 
-#define AMDG_ABI_VERSION 5
+#define AMDG_ABI_VERSION 6
 
 typedef enum amdg_status {
     AMDG_OK = 0,
@@ -468,7 +468,9 @@ amdg_status amdg_batch_coefficients_device(amdg_batch* b, double** device_ptr, i
  * removes those that stay small); and the batch is rebuilt on the new element sets (neighbour
  * lists, state; step graphs re-captured).  The solves' time steps are kept: set them again if
  * the finest levels changed.  stats (may be NULL): [refined by the classifier, uncertain,
- * elements after]. */
+ * elements after].  When replacing a solve's element set fails (AMDG_ERR_NOMEM), the solves
+ * before it keep their new sets and the batch is rebuilt on the sets the grids hold, so it stays
+ * usable. */
 amdg_status amdg_batch_adapt(amdg_batch* b, amdg_mlp* mlp, double eps, double eta, double tau, int64_t* stats);
 /* Stage kernel of the batch: amdg_batch_create times one stage with every candidate and keeps
  * the fastest per precision (batches under 100,000 DOF keep candidate 2).  Candidates 0-4: the
@@ -480,9 +482,15 @@ amdg_status amdg_batch_adapt(amdg_batch* b, amdg_mlp* mlp, double eps, double et
  * streamed into shared memory by bulk asynchronous copies, on the same FP32-pair state, in (ring
  * slots, elements per CTA) = (1, 1), (1, 2), (1, 4), (2, 1), (2, 2), (2, 4) -- its waits are
  * bounded, and a wait that gives up fails the call with AMDG_ERR_TIMEOUT and leaves the state as it
- * was.  kernel[2] = chosen candidate (FP64, mixed); stage_ms[2][AMDG_BATCH_KERNELS] = measured
- * stage times per candidate, 0 where not timed. */
-#define AMDG_BATCH_KERNELS 16
+ * was; candidates 16-18, the column kernel on the FP32-pair state as one persistent launch (a grid
+ * of the CTAs that fit on the device at once, each taking tile after tile) in (CTA threads,
+ * schedule) = (64, static tile order), (128, static), (64, tiles taken from a device counter);
+ * candidate 19 (blocks of at most 32 coefficients), one warp per element with a lane per
+ * coefficient, each neighbour block one coalesced load and the 1D contraction by warp shuffles.
+ * Every FP32-pair candidate sums in the same order (identical results).  kernel[2] = chosen
+ * candidate (FP64, mixed); stage_ms[2][AMDG_BATCH_KERNELS] = measured stage times per candidate, 0
+ * where not timed. */
+#define AMDG_BATCH_KERNELS 20
 amdg_status amdg_batch_tuning(const amdg_batch* b, int* kernel, float* stage_ms);
 /* Override the stage kernel of one precision (AMDG_ERR_ARG where it is not offered). */
 amdg_status amdg_batch_set_kernel(amdg_batch* b, amdg_precision prec, int kernel);

@@ -20,7 +20,7 @@ def test_library_exports_every_declared_symbol():
 
 
 def test_abi_version():
-    assert amdg.load().amdg_abi_version() == 5
+    assert amdg.load().amdg_abi_version() == 6
 
 
 @pytest.mark.parametrize("name", [n for n, m in manifest().items() if m["kind"] == "oper1d"])
