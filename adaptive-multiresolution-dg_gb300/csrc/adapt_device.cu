@@ -385,6 +385,92 @@ __global__ void coarsen_stats_kernel(const uint64_t* __restrict__ keys, int64_t 
     }
 }
 
+// The whole coarsening of a small element set in one CTA: the level-sum passes (finest first,
+// separated by barriers), the keep flags and their exclusive scan (a block scan over
+// kSmallCoarsenItems elements per thread), and the statistics of the kept set -- the same flags,
+// positions and statistics as coarsen_pass_kernel + keep_flags_kernel + the device scan +
+// coarsen_stats_kernel, without their launches.
+constexpr int kSmallCoarsenThreads = 1024, kSmallCoarsenItems = 8;
+constexpr int64_t kSmallCoarsenMax = int64_t(kSmallCoarsenThreads) * kSmallCoarsenItems;
+__global__ void __launch_bounds__(kSmallCoarsenThreads)
+    coarsen_small_kernel(const uint64_t* __restrict__ keys, int64_t E, KeyShape ks, const double* __restrict__ norms,
+                         double eta, int levsum_max, KeyHash h, uint8_t* __restrict__ removed,
+                         int32_t* __restrict__ pos, double missed_eps, uint64_t* __restrict__ missed,
+                         int64_t missed_cap, AdaptStats* st) {
+    const int tid = threadIdx.x;
+    for (int64_t e = tid; e < E; e += kSmallCoarsenThreads) removed[e] = 0;
+    __syncthreads();
+    for (int L = levsum_max; L >= 1; --L) {
+        for (int64_t e = tid; e < E; e += kSmallCoarsenThreads) {
+            const uint64_t key = keys[e];
+            int sum = 0, mx = 0;
+            for (int d = 0; d < ks.dim; ++d) {
+                const int l = level_of(ks.field(key, d));
+                sum += l;
+                mx = l > mx ? l : mx;
+            }
+            if (sum != L || mx == 0 || !(norms[e] < eta)) continue;
+            bool keep_it = false;
+            int ch[2];
+            for (int d = 0; d < ks.dim && !keep_it; ++d) {
+                const int nc = children_of(ks.field(key, d), ks.nmax, ch);
+                for (int c = 0; c < nc; ++c) {
+                    const int32_t i = hfind(h, ks.with(key, d, ch[c]));
+                    if (i >= 0 && !removed[i]) keep_it = true;
+                }
+            }
+            if (!keep_it) removed[e] = 1;
+        }
+        __syncthreads();  // pass L - 1 reads the flags of pass L
+    }
+    using Scan = cub::BlockScan<int, kSmallCoarsenThreads>;
+    __shared__ typename Scan::TempStorage scan_tmp;
+    int v[kSmallCoarsenItems];
+#pragma unroll
+    for (int i = 0; i < kSmallCoarsenItems; ++i) {
+        const int64_t e = int64_t(tid) * kSmallCoarsenItems + i;
+        v[i] = (e < E && !removed[e]) ? 1 : 0;
+    }
+    int total = 0;
+    Scan(scan_tmp).ExclusiveSum(v, v, total);
+#pragma unroll
+    for (int i = 0; i < kSmallCoarsenItems; ++i) {
+        const int64_t e = int64_t(tid) * kSmallCoarsenItems + i;
+        if (e < E) pos[e] = v[i];
+    }
+    if (tid == 0) {
+        pos[E] = total;
+        st->count = (unsigned long long)total;
+    }
+    for (int64_t e = tid; e < E; e += kSmallCoarsenThreads) {
+        if (removed[e]) continue;
+        const uint64_t key = keys[e];
+        int sum = 0;
+        for (int d = 0; d < ks.dim; ++d) {
+            const int l = level_of(ks.field(key, d));
+            sum += l;
+            atomicAdd(&st->lev_sum[d], (unsigned long long)l);
+            atomicMax(&st->lev_max[d], l);
+        }
+        atomicMax(&st->levsum_max, sum);
+        if (missed_eps > 0.0 && norms[e] > missed_eps) {
+            int existing = 0, tot = 0, ch[2];
+            for (int d = 0; d < ks.dim; ++d) {
+                const int nc = children_of(ks.field(key, d), ks.nmax, ch);
+                tot += nc;
+                for (int c = 0; c < nc; ++c) {
+                    const int32_t i = hfind(h, ks.with(key, d, ch[c]));
+                    existing += (i >= 0 && !removed[i]) ? 1 : 0;
+                }
+            }
+            if (existing < tot) {
+                const long long j = (long long)atomicAdd(&st->missed, 1ull);
+                if (j < missed_cap) missed[j] = key;
+            }
+        }
+    }
+}
+
 __global__ void compact_kernel(const uint64_t* __restrict__ keys, int64_t E, KeyShape ks, const uint8_t* __restrict__ removed,
                                const int32_t* __restrict__ pos, uint64_t* __restrict__ out_keys,
                                int32_t* __restrict__ map, int32_t* __restrict__ order) {
@@ -971,24 +1057,33 @@ amdg_status grid_device_coarsen(amdg_grid* g, double eta, double missed_eps, int
         if (removed_out) *removed_out = 0;
         return AMDG_OK;
     }
-    AMDG_CK(cudaMemsetAsync(d.flag, 0, size_t(E), st));
-    for (int L = g->levsum_max; L >= 1; --L) {
-        coarsen_pass_kernel<<<blocks_for(E, 128), 128, 0, st>>>(d.key, E, ks, g->d_norms, eta, L, hash_of(g), d.flag);
+    if (E <= kSmallCoarsenMax) {  // one CTA does it all
+        coarsen_small_kernel<<<1, kSmallCoarsenThreads, 0, st>>>(d.key, E, ks, g->d_norms, eta, g->levsum_max,
+                                                                  hash_of(g), d.flag, d.pos, missed_eps, d.missed,
+                                                                  d.missed_cap, dst);
         AMDG_CK(cudaGetLastError());
         g->ctx->launches++;
+    } else {
+        AMDG_CK(cudaMemsetAsync(d.flag, 0, size_t(E), st));
+        for (int L = g->levsum_max; L >= 1; --L) {
+            coarsen_pass_kernel<<<blocks_for(E, 128), 128, 0, st>>>(d.key, E, ks, g->d_norms, eta, L, hash_of(g),
+                                                                    d.flag);
+            AMDG_CK(cudaGetLastError());
+            g->ctx->launches++;
+        }
+        // kept positions: exclusive scan of keep flags (E + 1 entries, the last one 0 -> total)
+        keep_flags_kernel<<<blocks_for(E + 1, 256), 256, 0, st>>>(d.flag, E, d.pos);
+        AMDG_CK(cudaGetLastError());
+        size_t temp = 0;
+        AMDG_CK(cub::DeviceScan::ExclusiveSum(nullptr, temp, d.pos, d.pos, int(E + 1), st));
+        if ((s = grow_temp(d, temp)) != AMDG_OK) return s;
+        size_t tb = d.temp_bytes;
+        AMDG_CK(cub::DeviceScan::ExclusiveSum(d.temp, tb, d.pos, d.pos, int(E + 1), st));
+        coarsen_stats_kernel<<<blocks_for(E, 128), 128, 0, st>>>(d.key, E, ks, d.flag, d.pos, g->d_norms, missed_eps,
+                                                                 hash_of(g), d.missed, d.missed_cap, dst);
+        AMDG_CK(cudaGetLastError());
+        g->ctx->launches += 3;
     }
-    // kept positions: exclusive scan of keep flags (E + 1 entries, the last one 0 -> total)
-    keep_flags_kernel<<<blocks_for(E + 1, 256), 256, 0, st>>>(d.flag, E, d.pos);
-    AMDG_CK(cudaGetLastError());
-    size_t temp = 0;
-    AMDG_CK(cub::DeviceScan::ExclusiveSum(nullptr, temp, d.pos, d.pos, int(E + 1), st));
-    if ((s = grow_temp(d, temp)) != AMDG_OK) return s;
-    size_t tb = d.temp_bytes;
-    AMDG_CK(cub::DeviceScan::ExclusiveSum(d.temp, tb, d.pos, d.pos, int(E + 1), st));
-    coarsen_stats_kernel<<<blocks_for(E, 128), 128, 0, st>>>(d.key, E, ks, d.flag, d.pos, g->d_norms, missed_eps,
-                                                             hash_of(g), d.missed, d.missed_cap, dst);
-    AMDG_CK(cudaGetLastError());
-    g->ctx->launches += 3;
     AdaptStats hs;
     if ((s = read_stats(g, &hs)) != AMDG_OK) return s;
     if (hs.nonfinite) return fail(AMDG_ERR_NONFINITE, "element indicator is not finite");
@@ -1058,6 +1153,33 @@ void transform_topology_bounds(const amdg_grid* g, int64_t* vol_pairs, int64_t* 
     *flx_pairs = v + 4 * int64_t(std::max(g->host.nmax - 1, 0)) * E * g->host.dim;
 }
 
+// Exclusive scans of the vol and flx row counts (n entries each) in one CTA, for small element
+// sets: the results of the two device-wide scans without their launches.
+__global__ void __launch_bounds__(kSmallCoarsenThreads)
+    scan_pair_small_kernel(const int32_t* __restrict__ a, const int32_t* __restrict__ b, int64_t n,
+                           int32_t* __restrict__ sa, int32_t* __restrict__ sb) {
+    using Scan = cub::BlockScan<int, kSmallCoarsenThreads>;
+    __shared__ typename Scan::TempStorage tmp;
+    const int tid = threadIdx.x;
+    for (int which = 0; which < 2; ++which) {
+        const int32_t* in = which ? b : a;
+        int32_t* out = which ? sb : sa;
+        int v[kSmallCoarsenItems];
+#pragma unroll
+        for (int i = 0; i < kSmallCoarsenItems; ++i) {
+            const int64_t r = int64_t(tid) * kSmallCoarsenItems + i;
+            v[i] = r < n ? in[r] : 0;
+        }
+        Scan(tmp).ExclusiveSum(v, v);
+#pragma unroll
+        for (int i = 0; i < kSmallCoarsenItems; ++i) {
+            const int64_t r = int64_t(tid) * kSmallCoarsenItems + i;
+            if (r < n) out[r] = v[i];
+        }
+        __syncthreads();  // the temp storage is reused
+    }
+}
+
 amdg_status device_transform_topology(amdg_grid* g, const DeviceTopoOut& out, int32_t* d_cnt, void* stream) {
     cudaStream_t st = static_cast<cudaStream_t>(stream);
     if (amdg_status s = grid_hash(g); s != AMDG_OK) return s;
@@ -1070,13 +1192,18 @@ amdg_status device_transform_topology(amdg_grid* g, const DeviceTopoOut& out, in
     int32_t* fcnt = d_cnt + rows + 1;
     topo_count_kernel<<<blocks_for(32 * (rows + 1), 256), 256, 0, st>>>(A, vcnt, fcnt);
     AMDG_CK(cudaGetLastError());
-    size_t temp = 0;
-    AMDG_CK(cub::DeviceScan::ExclusiveSum(nullptr, temp, vcnt, out.vol_ptr, int(rows + 1), st));
-    if (amdg_status s = grow_temp(g->dev, temp); s != AMDG_OK) return s;
-    size_t tb = g->dev.temp_bytes;
-    AMDG_CK(cub::DeviceScan::ExclusiveSum(g->dev.temp, tb, vcnt, out.vol_ptr, int(rows + 1), st));
-    tb = g->dev.temp_bytes;
-    AMDG_CK(cub::DeviceScan::ExclusiveSum(g->dev.temp, tb, fcnt, out.flx_ptr, int(rows + 1), st));
+    if (rows + 1 <= kSmallCoarsenMax) {
+        scan_pair_small_kernel<<<1, kSmallCoarsenThreads, 0, st>>>(vcnt, fcnt, rows + 1, out.vol_ptr, out.flx_ptr);
+        AMDG_CK(cudaGetLastError());
+    } else {
+        size_t temp = 0;
+        AMDG_CK(cub::DeviceScan::ExclusiveSum(nullptr, temp, vcnt, out.vol_ptr, int(rows + 1), st));
+        if (amdg_status s = grow_temp(g->dev, temp); s != AMDG_OK) return s;
+        size_t tb = g->dev.temp_bytes;
+        AMDG_CK(cub::DeviceScan::ExclusiveSum(g->dev.temp, tb, vcnt, out.vol_ptr, int(rows + 1), st));
+        tb = g->dev.temp_bytes;
+        AMDG_CK(cub::DeviceScan::ExclusiveSum(g->dev.temp, tb, fcnt, out.flx_ptr, int(rows + 1), st));
+    }
     topo_fill_kernel<<<blocks_for(32 * rows, 256), 256, 0, st>>>(
         A, out.vol_ptr, out.flx_ptr, reinterpret_cast<int2*>(out.vol_nbr), reinterpret_cast<int2*>(out.flx_nbr),
         out.vol_split, out.flx_split, out.vol_cap, out.flx_cap, out.err);
