@@ -342,7 +342,9 @@ amdg_status autotune_linear(amdg_linear_op* op) {
     const bool tma = linear_tma_supported(dim, np);
     const bool mma = linear_mma_supported(dim, np);
     for (int p = 0; p < 2; ++p) op->variant[p] = col ? 1 : 0;
-    if (!col || g->dof < 200000) return AMDG_OK;
+    if (!col) return AMDG_OK;
+    // small grids time the two CUDA-core variants only (thread per output, column)
+    const bool small = g->dof < 200000;
     cudaStream_t st = stream_of(g->ctx);
     cudaEvent_t a, b;
     AMDG_CK(cudaEventCreate(&a));
@@ -350,7 +352,7 @@ amdg_status autotune_linear(amdg_linear_op* op) {
     AMDG_CK(launch_split(g->d_u, op->d_shadow, op->d_lo, g->dof, st));
     for (int p = 0; p < 2; ++p) {
         float best = 1e30f;
-        for (int v = 0; v < (p == 1 && tma ? 4 : 2); ++v) {
+        for (int v = 0; v < (p == 1 && tma && !small ? 4 : 2); ++v) {
             if (v == 3 && !mma) continue;
             // the bulk-copy variant: time each of its configurations, keep the fastest
             const int ncfg = v == 2 ? kTmaConfigs : 1;

@@ -54,7 +54,30 @@ __global__ void __launch_bounds__(256) linear_apply_kernel(const double* __restr
         const int beg = __ldg(row_ptr + e * D + t);
         const int end = __ldg(row_ptr + e * D + t + 1);
         const T* bt = blocks + size_t(t) * nblocks * NP * NP + qt;
-        for (int i = beg; i < end; ++i) {
+        // four neighbours per pass: their indices, block entries and values are independent loads
+        // issued together; the multiply-adds keep the neighbour order
+        int i = beg;
+        for (; i + 4 <= end; i += 4) {
+            int sv[4], bv[4];
+#pragma unroll
+            for (int j = 0; j < 4; ++j) {
+                sv[j] = __ldg(src + i + j);
+                bv[j] = __ldg(blk + i + j);
+            }
+            T mv[4][NP], xv[4][NP];
+#pragma unroll
+            for (int j = 0; j < 4; ++j)
+#pragma unroll
+                for (int p = 0; p < NP; ++p) {
+                    mv[j][p] = __ldg(bt + bv[j] * NP * NP + p * NP);
+                    xv[j][p] = T(__ldg(xs + int64_t(sv[j]) * B + base + p * stride));
+                }
+#pragma unroll
+            for (int j = 0; j < 4; ++j)
+#pragma unroll
+                for (int p = 0; p < NP; ++p) acc = fma(mv[j][p], xv[j][p], acc);
+        }
+        for (; i < end; ++i) {
             const int s = __ldg(src + i);
             const T* m = bt + __ldg(blk + i) * NP * NP;
             const X* x = xs + int64_t(s) * B + base;
@@ -847,7 +870,16 @@ static cudaError_t launch_linear_t(const LinearLaunch& L, const T* blocks, const
     constexpr int B = IPow<NP, D>::v;
     const int64_t total = L.num_elements * B;
     if (total == 0) return cudaSuccess;
-    const int threads = 256;
+    // small grids: smaller CTAs until there are two per multiprocessor (a grid of a few thousand
+    // coefficients otherwise runs on a few SMs, bound by their FP64 pipes)
+    static int sms = 0;
+    if (sms == 0) {
+        int dev = 0;
+        if (cudaGetDevice(&dev) != cudaSuccess || cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)
+            sms = 152;
+    }
+    int threads = 256;
+    while (threads > 32 && (total + threads - 1) / threads < 2 * int64_t(sms)) threads /= 2;
     const int64_t grid = (total + threads - 1) / threads;
     linear_apply_kernel<D, NP, T, X><<<unsigned(grid), threads, 0, st>>>(L.us, xs, L.un, L.out, L.shadow_out, L.row_ptr,
                                                                         L.src, L.blk, blocks, L.num_blocks, total, rk, L.df);

@@ -273,6 +273,76 @@ def bench_linear6d(ctx, stream, args, world):
     return out
 
 
+def bench_linear_small(ctx, stream, args):
+    """Config 1 at its stated length (2D linear advection, c = (1, 1), u0 = sin(2 pi (x+y)),
+    sparse N = 7, 576 elements, 2561 SSP-RK3 steps of 1/2561 to T = 1) and the 4D part of config 2
+    (4D N = 8, 850,176 DOF, c = 1, u0 = prod sin(2 pi x_d), to T = 0.1): whole runs timed with CUDA
+    events in FP64 and mixed precision, L2 error against the exact translated solution (split
+    formula), and for config 1 the reference's own assembled-matrix loop on the host (one thread:
+    the Eigen SpMV path has no OpenMP)."""
+    import torch
+
+    import amdg
+    import amdg_oracle as O
+    out = {}
+
+    def run(g, op, u0, dt, steps, prec):
+        g.set_coefficients(u0)
+        op.rk3_steps(dt, min(steps, 20), prec)  # warm-up
+        g.set_coefficients(u0)
+        torch.cuda.synchronize()
+        s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        s.record(stream)
+        op.rk3_steps(dt, steps, prec)
+        e.record(stream)
+        e.synchronize()
+        return s.elapsed_time(e) / 1e3
+
+    # config 1
+    g = amdg.Grid(ctx, 2, 7, 2)
+    g.init_separable(O.sin_sum_terms(2))
+    u0 = g.coefficients().reshape(-1).copy()
+    op = amdg.LinearOperator(g, [1.0, 1.0])
+    steps, dt = 2561, 1.0 / 2561
+    c1 = {"workload": "2D linear advection, sparse grid N=7 (576 elements, 5,184 DOF), k=2, upwind, SSP-RK3, "
+                      "2561 steps to T = 1"}
+    for name, prec in (("fp64", amdg.FP64), ("mixed", amdg.MIXED)):
+        sec = run(g, op, u0, dt, steps, prec)
+        err = g.l2_error_separable_sum([lambda x, d, f=f: f(x - 1.0, d) for f in O.sin_sum_terms(2)], 0.5 ** 0.5)
+        c1[name] = {"value": 3.0 * g.dof * steps / sec, "ms_per_run": sec * 1e3, "l2_error_vs_exact_T1": err}
+    op.close()
+    g.close()
+    if ensure_ref_harness():
+        res = subprocess.run([REF_HARNESS, "linear", "2", "7", "2", "1", "sin_sum", "assembled", str(steps), repr(dt),
+                              "1.0", "1.0"], capture_output=True, text=True, check=True,
+                             env=dict(os.environ, OMP_NUM_THREADS="1"))
+        f = [ln.split() for ln in res.stdout.splitlines() if ln.startswith("TIME")][0]
+        kv = dict(x.split("=") for x in f[1:])
+        ref = float(kv["dof_stage"]) / float(kv["evolve_s"])
+        c1["reference_cpu"] = {"value": ref, "unit": "DOF-stage updates/s", "cores": 1, "kind": "reference",
+                               "sample": f"the whole run (AdaM-DG's assembled HyperbolicAlpt + RK3SSP::step_rk, "
+                                         f"{float(kv['evolve_s']):.2f} s of evolution)"}
+        c1["fp64_vs_reference_cpu"] = c1["fp64"]["value"] / ref
+    out["linear2d_config1_T1"] = c1
+    # the 4D part of config 2
+    g = amdg.Grid(ctx, 4, 8, 2)
+    g.init_separable([lambda x, d: math.sin(2 * math.pi * x)])
+    u0 = g.coefficients().reshape(-1).copy()
+    op = amdg.LinearOperator(g, [1.0] * 4)
+    dt = CFL * (1.0 / 256) / 4.0
+    steps = int(round(0.1 / dt))
+    c2 = {"workload": f"4D linear advection, sparse grid N=8 (10,496 elements, 850,176 DOF), k=2, SSP-RK3, "
+                      f"{steps} steps to T = 0.1"}
+    for name, prec in (("fp64", amdg.FP64), ("mixed", amdg.MIXED)):
+        sec = run(g, op, u0, dt, steps, prec)
+        err = g.l2_error_separable(lambda x, d, t=steps * dt: math.sin(2 * math.pi * (x - t)), 0.5 ** 2)
+        c2[name] = {"value": 3.0 * g.dof * steps / sec, "ms_per_step": sec / steps * 1e3, "l2_error_vs_exact": err}
+    op.close()
+    g.close()
+    out["linear4d_n8_T01"] = c2
+    return out
+
+
 def run_ours(args):
     import torch
 
@@ -373,6 +443,7 @@ def run_ours(args):
         m = line["burgers3d_adaptive"]["metric"]
         line["metric_at_matched_error"] = {k: v for k, v in m.items()
                                            if k != "network_gain_vs_criterion_same_horizon_and_eps"}
+    line.update(bench_linear_small(ctx, stream, args))
     lin = bench_linear6d(ctx, stream, args, world)
     lin_cpu = lin.pop("_cpu")
     line["linear6d"] = lin
@@ -898,7 +969,8 @@ def bench_wave_adaptive(ctx, stream, args):
                                    "elements_final": ref_run["elements_final"]}
     # the learned arm at the trained horizon ("mixed_learned") and at horizons 1 and 4
     arms = [("plain_fp64", False, amdg.FP64, 1), ("mixed_learned", True, amdg.MIXED, H)]
-    arms += [(f"mixed_learned_h{h}", True, amdg.MIXED, h) for h in (1, 4) if h != H]
+    if not args.wave_main_arms:
+        arms += [(f"mixed_learned_h{h}", True, amdg.MIXED, h) for h in (1, 4) if h != H]
     arms += [("mixed_plain", False, amdg.MIXED, 1)]
     for name, learned, prec, horizon in arms:
         run(learned, prec, 4 * CFL / (speed * dim * 128), horizon=horizon)  # warm-up: a few steps
@@ -1555,6 +1627,8 @@ def main():
                     help="wave_rhs: run the wave right-hand-side profiling case instead of the bench")
     ap.add_argument("--wave-only", action="store_true",
                     help="run only the 2D adaptive wave line (for a run to the config's T = 0.5) and print it")
+    ap.add_argument("--wave-main-arms", action="store_true",
+                    help="wave line: plain FP64, mixed + learned at the trained horizon and mixed plain only")
     ap.add_argument("--wave-no-level10", action="store_true",
                     help="skip the max-level-10 FP64 run the wave arms' errors are measured against")
     ap.add_argument("--wave-time", type=float, default=0.05,
