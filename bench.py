@@ -38,6 +38,9 @@ CFL = 0.1
 # DRAM bytes of one mixed stage launch of the 6D N=8 workload, per kernel variant, from ncu
 # (dram__bytes_read.sum + dram__bytes_write.sum; variant 0 was not captured)
 NCU_TRAFFIC_BYTES = {1: (720.902 + 241.610) * 1e6, 2: (441.076 + 236.082) * 1e6}
+# DRAM bytes of one FP64 right-hand side of the 3D adaptive Burgers workload on its final grid
+# (1,004 elements), summed over its 11 kernels, ncu with a cold L2 before every kernel
+NCU_TRAFFIC_RHS_CONFIG3 = 24.704512e6
 METRIC = "DOF-stage updates/s at matched L2 error: plain FP64 vs mixed+learned-adapt"
 WORKLOAD = "6D linear advection, sparse grid N=8, Alpert k=2, SSP-RK3 (34,455,456 DOF)"
 
@@ -421,7 +424,11 @@ def run_ours(args):
                    "parallelism": "replicas" if world > 1 else "single GPU"},
         "l2_error_vs_exact_l1_l2_linf": plain["error_vs_exact_l1_l2_linf"],
         "roofline": {"bound": "hbm", "achieved": ach, "peak": pk["hbm_gbs"], "unit": "GB/s",
-                     "frac": ach / pk["hbm_gbs"], "traffic": None, "peak_kind": pk_kind,
+                     "frac": ach / pk["hbm_gbs"], "traffic": NCU_TRAFFIC_RHS_CONFIG3, "peak_kind": pk_kind,
+                     "traffic_note": "dram__bytes_read.sum + dram__bytes_write.sum summed over the 11 kernels of one "
+                                     "FP64 right-hand side on this grid, ncu with its default cache flush before "
+                                     "every kernel (cold L2); in the run the working set stays in L2 "
+                                     "(profiles/rhs_burgers3d_config3.md)",
                      "kernel": "one FP64 right-hand side (point values, surplus passes, transforms, reduction) "
                                f"on the final grid ({rhs_E} elements, {rhs_dof} DOF)",
                      "kernel_ms": rhs_sec * 1e3, "algorithmic_bytes_per_launch": 233.0 * rhs_dof,
@@ -1340,6 +1347,37 @@ def profile_herm():
     torch.cuda.cudart().cudaProfilerStop()
 
 
+def profile_rhs_config3():
+    """Profiling case (not a bench line): one FP64 and one mixed right-hand side on the final grid of
+    a plain 3D adaptive Burgers run (1,004 elements), each after a warm-up evaluation, between
+    cudaProfilerStart / cudaProfilerStop (the dozen kernels of each, for DRAM traffic per RHS)."""
+    import torch
+
+    import amdg
+    torch.cuda.set_device(0)
+    ctx = amdg.Context(0)
+    stream = torch.cuda.Stream()
+    torch.cuda.set_stream(stream)
+    ctx.set_stream(stream.cuda_stream)
+    cfg = Config3(ctx, stream)
+    r = cfg.run(amdg.FP64, keep=True)
+    g, op = r["_grid"], r["_op"]
+    du = torch.from_numpy(g.coefficients().reshape(-1).copy()).cuda()
+    out = torch.zeros_like(du)
+    for prec in (amdg.FP64, amdg.MIXED):
+        op.rhs_device(du.data_ptr(), out.data_ptr(), prec)
+    torch.cuda.synchronize()
+    l0 = ctx.launch_count()
+    torch.cuda.cudart().cudaProfilerStart()
+    for prec in (amdg.FP64, amdg.MIXED):
+        op.rhs_device(du.data_ptr(), out.data_ptr(), prec)
+    torch.cuda.synchronize()
+    torch.cuda.cudart().cudaProfilerStop()
+    print(json.dumps({"elements": g.num_elements, "dof": g.dof, "launches": ctx.launch_count() - l0}), flush=True)
+    op.close()
+    g.close()
+
+
 def profile_batch():
     """Profiling case (not a bench line): 64 of the batched solves (per-solve refine thresholds
     log-uniform in [1e-8, 1e-5], adaptive N<=8), one mixed SSP-RK3 step with the autotuner's stage
@@ -1622,7 +1660,8 @@ def main():
     ap.add_argument("--wave-learn-steps", type=int, default=30)
     ap.add_argument("--wave-train-samples", type=int, default=300000, help="training samples kept (stratified)")
     ap.add_argument("--wave-learn-horizon", type=int, default=2, help="time steps per learned pre-adaptation (wave)")
-    ap.add_argument("--profile", choices=["none", "wave_rhs", "config3", "rhs3d", "linear6d", "batch", "herm"],
+    ap.add_argument("--profile", choices=["none", "wave_rhs", "config3", "rhs3d", "linear6d", "batch", "herm",
+                                          "rhs_config3"],
                     default="none",
                     help="wave_rhs: run the wave right-hand-side profiling case instead of the bench")
     ap.add_argument("--wave-only", action="store_true",
@@ -1644,6 +1683,8 @@ def main():
         profile_batch()
     elif args.profile == "herm":
         profile_herm()
+    elif args.profile == "rhs_config3":
+        profile_rhs_config3()
     elif args.profile == "rhs3d":
         profile_rhs3d()
     elif args.wave_only:
