@@ -106,6 +106,10 @@ int main(int argc, char* argv[]) {
         return FluxFunction::burgers_flux_2nd_derivative_scalar(u[0]);
     };
 
+    // third and fourth derivatives of the physical flux (used by the PMAX 5 variant)
+    auto func_flux_d3 = [&](std::vector<double> u, int i, int d, int i1, int i2, int i3) -> double { return 0.; };
+    auto func_flux_d4 = [&](std::vector<double> u, int i, int d, int i1, int i2, int i3, int i4) -> double { return 0.; };
+
     // Hermite interpolation for the nonlinear physical flux
     HyperbolicSameFluxHermRHS fast_rhs_herm(dg_solu, oper_matx_herm);
     HermInterpolation interp_herm(dg_solu);
@@ -151,7 +155,12 @@ int main(int argc, char* argv[]) {
             odeSolver.init();
 
             // Hermite interpolation
-            interp_herm.nonlinear_Herm_2D_fast(func_flux, func_flux_d1, func_flux_d2, is_intp_herm, fast_herm_intp);
+            if (HermBasis::PMAX == 3) {
+                interp_herm.nonlinear_Herm_2D_fast(func_flux, func_flux_d1, func_flux_d2, is_intp_herm, fast_herm_intp);
+            } else if (HermBasis::PMAX == 5) {
+                interp_herm.nonlinear_Herm_2D_PMAX5_scalar_fast(func_flux, func_flux_d1, func_flux_d2, func_flux_d3,
+                                                                func_flux_d4, is_intp_herm, fast_herm_intp);
+            }
 
             // calculate rhs
             dg_solu.set_rhs_zero();
@@ -188,7 +197,12 @@ int main(int argc, char* argv[]) {
 
         for (int stage = 0; stage < odeSolver.num_stage; ++stage) {
             // Hermite interpolation
-            interp_herm.nonlinear_Herm_2D_fast(func_flux, func_flux_d1, func_flux_d2, is_intp_herm, fast_herm_intp);
+            if (HermBasis::PMAX == 3) {
+                interp_herm.nonlinear_Herm_2D_fast(func_flux, func_flux_d1, func_flux_d2, is_intp_herm, fast_herm_intp);
+            } else if (HermBasis::PMAX == 5) {
+                interp_herm.nonlinear_Herm_2D_PMAX5_scalar_fast(func_flux, func_flux_d1, func_flux_d2, func_flux_d3,
+                                                                func_flux_d4, is_intp_herm, fast_herm_intp);
+            }
 
             // calculate rhs and update Element::ucoe_alpt
             dg_solu.set_rhs_zero();

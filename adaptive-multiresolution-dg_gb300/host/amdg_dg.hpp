@@ -576,6 +576,17 @@ public:
                     throw Error(AMDG_ERR_ARG, "HermInterpolation::nonlinear_Herm_2D_fast: only the Burgers flux is registered");
         check(amdg_lagr_interpolate(dg_.herm_op(), precision), "amdg_lagr_interpolate (Hermite)");
     }
+    // HermInterpolation::nonlinear_Herm_2D_PMAX5_scalar_fast (Interplation.cpp:5001-5017), the quintic
+    // Hermite variant a driver selects with HermBasis::PMAX = 5: declared so such drivers compile
+    // unchanged; not built on the device, so it reports AMDG_ERR_ARG
+    void nonlinear_Herm_2D_PMAX5_scalar_fast(std::function<double(std::vector<double>, int, int)>,
+                                             std::function<double(std::vector<double>, int, int, int)>,
+                                             std::function<double(std::vector<double>, int, int, int, int)>,
+                                             std::function<double(std::vector<double>, int, int, int, int, int)>,
+                                             std::function<double(std::vector<double>, int, int, int, int, int, int)>,
+                                             const std::vector<std::vector<bool>>&, FastHermIntp&) {
+        throw Error(AMDG_ERR_ARG, "HermInterpolation::nonlinear_Herm_2D_PMAX5_scalar_fast: only HermBasis::PMAX = 3 is built");
+    }
 
 private:
     DGSolution& dg_;
