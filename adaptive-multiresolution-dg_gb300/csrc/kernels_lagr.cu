@@ -91,8 +91,11 @@ __device__ __forceinline__ T fibre_quad(const T* const* x, const T* const* m, in
 
 // NODE_ROWS: the node is blockIdx.y and the thread's (element, entry) its index in the node's
 // E x out_block outputs (32-bit index arithmetic); else one 1D grid over all nodes' outputs
+// At most 64 registers (four CTAs of 256 per multiprocessor): without the bound the FP64 and
+// double-float forms took 80 / 74 registers and three CTAs, and the config-3 right-hand side ran
+// 4 % slower; a bound of five CTAs spills.
 template <typename T, bool NODE_ROWS>
-__global__ void __launch_bounds__(256) sweep_kernel(SweepArgs<T> a) {
+__global__ void __launch_bounds__(256, 4) sweep_kernel(SweepArgs<T> a) {
     const int64_t per = a.num_elements * a.out_block;
     int slot;
     int64_t r;
