@@ -91,11 +91,28 @@ __device__ __forceinline__ T fibre_quad(const T* const* x, const T* const* m, in
 
 // NODE_ROWS: the node is blockIdx.y and the thread's (element, entry) its index in the node's
 // E x out_block outputs (32-bit index arithmetic); else one 1D grid over all nodes' outputs
+constexpr int kSweepThreads = 128;
+
+// CTA size of the element-wise kernels: 256 threads, halved (down to 64) until the grid has two
+// CTAs per multiprocessor -- on the ~1,000-element grids of the adaptive runs a 256-thread grid
+// leaves multiprocessors idle
+inline int ew_threads(int64_t n) {
+    static int sms = 0;
+    if (sms == 0) {
+        int dev = 0;
+        if (cudaGetDevice(&dev) != cudaSuccess || cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)
+            sms = 152;
+    }
+    int t = 256;
+    while (t > 64 && (n + t - 1) / t < 2 * int64_t(sms)) t /= 2;
+    return t;
+}
+#define AMDG_EW_GRID(n) unsigned(((n) + ew_threads(n) - 1) / ew_threads(n)), ew_threads(n)
 // At most 64 registers (four CTAs of 256 per multiprocessor): without the bound the FP64 and
 // double-float forms took 80 / 74 registers and three CTAs, and the config-3 right-hand side ran
 // 4 % slower; a bound of five CTAs spills.
 template <typename T, bool NODE_ROWS>
-__global__ void __launch_bounds__(256, 4) sweep_kernel(SweepArgs<T> a) {
+__global__ void __launch_bounds__(kSweepThreads, 1024 / kSweepThreads) sweep_kernel(SweepArgs<T> a) {
     const int64_t per = a.num_elements * a.out_block;
     int slot;
     int64_t r;
@@ -513,10 +530,11 @@ cudaError_t launch_sweep(const SweepArgs<T>& a, cudaStream_t st) {
             // measured: the node-row grid is the faster one for the FP32 sweeps, the flat grid for
             // the FP64 and double-float ones
             if constexpr (!std::is_same<T, float>::value) {
-                sweep_kernel<T, false><<<unsigned((total + 255) / 256), 256, 0, st>>>(a);
+                sweep_kernel<T, false><<<unsigned((total + kSweepThreads - 1) / kSweepThreads), kSweepThreads, 0, st>>>(a);
             } else {
-                const dim3 grid(unsigned((a.num_elements * a.out_block + 255) / 256), unsigned(a.count));
-                sweep_kernel<T, true><<<grid, 256, 0, st>>>(a);
+                const dim3 grid(unsigned((a.num_elements * a.out_block + kSweepThreads - 1) / kSweepThreads),
+                                unsigned(a.count));
+                sweep_kernel<T, true><<<grid, kSweepThreads, 0, st>>>(a);
             }
             break;
     }
@@ -551,14 +569,14 @@ __global__ void reduce_points_df_kernel(const float2* __restrict__ buf, int coun
 cudaError_t launch_reduce_points_df(const float2* buf, int count, int64_t n, int first, double* acc, double* fp,
                                     cudaStream_t st) {
     if (n == 0) return cudaSuccess;
-    reduce_points_df_kernel<<<unsigned((n + 255) / 256), 256, 0, st>>>(buf, count, n, first, acc, fp);
+    reduce_points_df_kernel<<<AMDG_EW_GRID(n), 0, st>>>(buf, count, n, first, acc, fp);
     return cudaGetLastError();
 }
 
 template <typename T>
 cudaError_t launch_reduce_points(const T* buf, int count, int64_t n, int first, T* acc, T* fp, cudaStream_t st) {
     if (n == 0) return cudaSuccess;
-    reduce_points_kernel<T><<<unsigned((n + 255) / 256), 256, 0, st>>>(buf, count, n, first, acc, fp);
+    reduce_points_kernel<T><<<AMDG_EW_GRID(n), 0, st>>>(buf, count, n, first, acc, fp);
     return cudaGetLastError();
 }
 
@@ -580,7 +598,7 @@ template <typename T>
 cudaError_t launch_reduce_rhs(const T* buf, int count, int64_t n, int first, int last, double* acc, StageOut so,
                               cudaStream_t st) {
     if (n == 0) return cudaSuccess;
-    reduce_rhs_kernel<T><<<unsigned((n + 255) / 256), 256, 0, st>>>(buf, count, n, first, last, acc, so);
+    reduce_rhs_kernel<T><<<AMDG_EW_GRID(n), 0, st>>>(buf, count, n, first, last, acc, so);
     return cudaGetLastError();
 }
 
@@ -618,7 +636,7 @@ template <typename Ti, typename To>
 cudaError_t launch_surplus_pass(const SurplusArgs<Ti>& a, const Ti* in, To* out, cudaStream_t st) {
     const int64_t total = a.num_elements * a.points;
     if (total == 0) return cudaSuccess;
-    surplus_pass_kernel<Ti, To><<<unsigned((total + 255) / 256), 256, 0, st>>>(a, in, out);
+    surplus_pass_kernel<Ti, To><<<AMDG_EW_GRID(total), 0, st>>>(a, in, out);
     return cudaGetLastError();
 }
 
@@ -635,7 +653,7 @@ __global__ void convert_kernel(const Ti* __restrict__ in, To* __restrict__ out, 
 template <typename Ti, typename To>
 cudaError_t launch_convert(const Ti* in, To* out, int64_t n, cudaStream_t st) {
     if (n == 0) return cudaSuccess;
-    convert_kernel<Ti, To><<<unsigned((n + 255) / 256), 256, 0, st>>>(in, out, n);
+    convert_kernel<Ti, To><<<AMDG_EW_GRID(n), 0, st>>>(in, out, n);
     return cudaGetLastError();
 }
 
@@ -667,7 +685,7 @@ template <typename T>
 cudaError_t launch_herm_flux_burgers2d(const T* up, T* fp, int64_t num_elements, cudaStream_t st) {
     const int64_t n = num_elements * 4;
     if (n == 0) return cudaSuccess;
-    herm_flux_burgers2d_kernel<T><<<unsigned((n + 255) / 256), 256, 0, st>>>(up, fp, n);
+    herm_flux_burgers2d_kernel<T><<<AMDG_EW_GRID(n), 0, st>>>(up, fp, n);
     return cudaGetLastError();
 }
 
@@ -709,7 +727,7 @@ cudaError_t launch_reduce_points_coef(const Tin* buf, int count, int64_t E, int 
     int64_t n = E;
     for (int d = 0; d < dim; ++d) n *= p1;
     if (n == 0) return cudaSuccess;
-    reduce_points_coef_kernel<Tin><<<unsigned((n + 255) / 256), 256, 0, st>>>(buf, count, E, dim, p1, order, pts, amp,
+    reduce_points_coef_kernel<Tin><<<AMDG_EW_GRID(n), 0, st>>>(buf, count, E, dim, p1, order, pts, amp,
                                                                                out);
     return cudaGetLastError();
 }
@@ -726,7 +744,7 @@ __global__ void to_df_kernel(const double* __restrict__ in, float2* __restrict__
 
 cudaError_t launch_to_df(const double* in, float2* out, int64_t n, cudaStream_t st) {
     if (n == 0) return cudaSuccess;
-    to_df_kernel<<<unsigned((n + 255) / 256), 256, 0, st>>>(in, out, n);
+    to_df_kernel<<<AMDG_EW_GRID(n), 0, st>>>(in, out, n);
     return cudaGetLastError();
 }
 
@@ -765,7 +783,7 @@ __global__ void rk4_2nd_stage_kernel(int stage, double dt, const double* __restr
 cudaError_t launch_rk4_2nd_stage(int stage, double dt, const double* rhs, double* un, double* vn, double* us, double* vs,
                                  double* su, double* sv, int64_t n, cudaStream_t st) {
     if (n == 0) return cudaSuccess;
-    rk4_2nd_stage_kernel<<<unsigned((n + 255) / 256), 256, 0, st>>>(stage, dt, rhs, un, vn, us, vs, su, sv, n);
+    rk4_2nd_stage_kernel<<<AMDG_EW_GRID(n), 0, st>>>(stage, dt, rhs, un, vn, us, vs, su, sv, n);
     return cudaGetLastError();
 }
 
