@@ -89,8 +89,11 @@ __device__ __forceinline__ T fibre_quad(const T* const* x, const T* const* m, in
     return acc;
 }
 
-// NODE_ROWS: the node is blockIdx.y and the thread's (element, entry) its index in the node's
-// E x out_block outputs (32-bit index arithmetic); else one 1D grid over all nodes' outputs
+// CTAs of 128 threads, at most 64 registers (eight CTAs per multiprocessor).  Measured on the
+// 3D adaptive Burgers runs (~1,000 elements): without the register bound the FP64 and
+// double-float forms took 80 / 74 registers, three CTAs of 256 fitted, and the FP64 run took 7 %
+// longer; 256-thread CTAs under the same bound another 4 % (coarser tails); 64-thread CTAs gained
+// nothing more.  A bound of 48 registers spills.
 constexpr int kSweepThreads = 128;
 
 // CTA size of the element-wise kernels: 256 threads, halved (down to 64) until the grid has two
@@ -108,9 +111,9 @@ inline int ew_threads(int64_t n) {
     return t;
 }
 #define AMDG_EW_GRID(n) unsigned(((n) + ew_threads(n) - 1) / ew_threads(n)), ew_threads(n)
-// At most 64 registers (four CTAs of 256 per multiprocessor): without the bound the FP64 and
-// double-float forms took 80 / 74 registers and three CTAs, and the config-3 right-hand side ran
-// 4 % slower; a bound of five CTAs spills.
+
+// NODE_ROWS: the node is blockIdx.y and the thread's (element, entry) its index in the node's
+// E x out_block outputs (32-bit index arithmetic); else one 1D grid over all nodes' outputs
 template <typename T, bool NODE_ROWS>
 __global__ void __launch_bounds__(kSweepThreads, 1024 / kSweepThreads) sweep_kernel(SweepArgs<T> a) {
     const int64_t per = a.num_elements * a.out_block;
