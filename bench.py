@@ -1636,7 +1636,7 @@ def main():
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--cpu-steps", type=int, default=4, help="time steps of the reference loop in cpu_baseline")
     ap.add_argument("--arm-runs", type=int, default=3, help="timed runs per arm of the 3D adaptive Burgers metric")
-    ap.add_argument("--arm-horizons", type=int, nargs="+", default=[4, 8],
+    ap.add_argument("--arm-horizons", type=int, nargs="+", default=[8, 12],
                     help="horizons of the pre-adapted arms of the 3D adaptive Burgers metric")
     ap.add_argument("--eps-scales", type=float, nargs="+", default=[1.5, 2, 2.25, 2.5],
                     help="refine thresholds of the pre-adapted arms, in units of 1e-5")
