@@ -1638,6 +1638,9 @@ def main():
     ap.add_argument("--arm-runs", type=int, default=3, help="timed runs per arm of the 3D adaptive Burgers metric")
     ap.add_argument("--arm-horizons", type=int, nargs="+", default=[8, 12],
                     help="horizons of the pre-adapted arms of the 3D adaptive Burgers metric")
+    ap.add_argument("--arm-tau", type=float, default=CONFIG3["tau"],
+                    help="probability at or above which the classifier's refine decision replaces the criterion's "
+                         "in the learned arms of the 3D adaptive Burgers metric")
     ap.add_argument("--eps-scales", type=float, nargs="+", default=[1.5, 2, 2.25, 2.5],
                     help="refine thresholds of the pre-adapted arms, in units of 1e-5")
     ap.add_argument("--eps-bisect", type=int, default=3,
@@ -1673,6 +1676,7 @@ def main():
     ap.add_argument("--wave-time", type=float, default=0.05,
                     help="final time of the 2D wave runs (the config's 0.5 takes ~5000 steps on a filling grid)")
     args = ap.parse_args()
+    CONFIG3["tau"] = args.arm_tau
     if args.profile == "wave_rhs":
         profile_wave_rhs()
     elif args.profile == "config3":
